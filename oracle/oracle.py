@@ -1,0 +1,182 @@
+"""ctypes access to the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Loads ``oracle/liboracle{8,10}.so`` (the C restatement in xin_oracle.c) and,
+where it was built, ``oracle/_ref/libxinref{8,10}.so`` (the reference's open C
+compiled in place, see oracle/Makefile).  Both expose the same logical calls,
+so a test can run one case through either and compare.  Used only by tests/,
+__graft_entry__.smoke() and bench.py's CPU legs, never by the product.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+i32, u32, u64, ip = C.c_int32, C.c_uint32, C.c_uint64, C.c_ssize_t
+vp = C.c_void_p
+
+
+def build(ref: bool = False) -> None:
+    """Compile the oracle (and, with ref=True and the reference tree present, oracle/_ref)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def ref_available(bitdepth: int = 8) -> bool:
+    return os.path.exists(os.path.join(HERE, "_ref", f"libxinref{bitdepth}.so"))
+
+
+def ptr(a: np.ndarray, off: int = 0) -> int:
+    """Address of element ``off`` (flat index, may be negative) of a C-contiguous array."""
+    return a.ctypes.data + off * a.itemsize
+
+
+class orc_me_io(C.Structure):
+    _fields_ = [("best_mvx", i32), ("best_mvy", i32), ("best_cost", u32), ("best_sad", u32)]
+
+
+class orc_qparams(C.Structure):
+    _fields_ = [("qmult", i32), ("qadd", i32), ("qshift", i32), ("iqmult", i32), ("iqadd", i32), ("iqshift", i32)]
+
+
+class orc_frame_desc(C.Structure):
+    _fields_ = [("width", i32), ("height", i32), ("ctu", i32),
+                ("in_", vp * 3), ("in_stride", ip * 2),
+                ("ref", vp * 3), ("ref_stride", ip * 2),
+                ("search_range", i32), ("sad_lambda", u32), ("qp", i32), ("uv_qp", i32), ("intra_frame", i32)]
+
+
+class orc_cu_out(C.Structure):
+    _fields_ = [("mvx", i32), ("mvy", i32), ("cost", u32), ("int_cost", u32), ("nz", u64 * 3), ("ssd", u64 * 3)]
+
+
+# logical name -> (oracle symbol, reference symbol or None, argtypes)
+_INTERP8 = [vp, ip, vp, ip, i32, u32, u32, u32]
+_SIGS = {
+    "interp_copy": ("orc_interp_copy", "Xin266InterpCopy", _INTERP8),
+    "interp_copy_s16": ("orc_interp_copy_s16", "Xin266InterpCopyU8S16", _INTERP8),
+    "luma_hor": ("orc_luma_hor", "Xin266LumaInterpHor", _INTERP8),
+    "luma_vet": ("orc_luma_vet", "Xin266LumaInterpVet", _INTERP8),
+    "luma_hv": ("orc_luma_hv", "Xin266LumaInterpHorVet", _INTERP8),
+    "luma_hor_s16": ("orc_luma_hor_s16", "Xin266LumaInterpHorU8S16", _INTERP8),
+    "luma_vet_s16": ("orc_luma_vet_s16", "Xin266LumaInterpVetU8S16", _INTERP8),
+    "luma_hv_s16": ("orc_luma_hv_s16", "Xin266LumaInterpHorVetU8S16", _INTERP8),
+    "luma_vet_s16_pix": ("orc_luma_vet_s16_pix", "Xin266LumaInterpVetS16U8", _INTERP8),
+    "luma_vet_s16_s16": ("orc_luma_vet_s16_s16", "Xin266LumaInterpVetS16S16", _INTERP8),
+    "chroma_hor": ("orc_chroma_hor", "Xin266ChromaInterpHor", _INTERP8),
+    "chroma_vet": ("orc_chroma_vet", "Xin266ChromaInterpVet", _INTERP8),
+    "chroma_hv": ("orc_chroma_hv", "Xin266ChromaInterpHorVet", _INTERP8),
+    "chroma_hor_s16": ("orc_chroma_hor_s16", "Xin266ChromaInterpHorU8S16", _INTERP8),
+    "chroma_vet_s16": ("orc_chroma_vet_s16", "Xin266ChromaInterpVetU8S16", _INTERP8),
+    "chroma_hv_s16": ("orc_chroma_hv_s16", "Xin266ChromaInterpHorVetU8S16", _INTERP8),
+    "chroma_vet_s16_pix": ("orc_chroma_vet_s16_pix", "Xin266ChromaInterpVetS16U8", _INTERP8),
+    "chroma_vet_s16_s16": ("orc_chroma_vet_s16_s16", "Xin266ChromaInterpVetS16S16", _INTERP8),
+    "interp_avg": ("orc_interp_avg", "Xin266InterpAvgS16U8", [vp, ip, vp, ip, vp, ip, u32, u32]),
+    "interp_weight": ("orc_interp_weight", "Xin266InterpWeightS16U8", [vp, ip, vp, ip, vp, ip, u32, u32, i32, i32]),
+    "quant_inv_quant": ("orc_quant_inv_quant", "Xin266QuantInvQuant",
+                        [vp, vp, vp, ip, u32, u32, u32, u32, i32, i32, i32, i32, i32, i32, vp]),
+    "pre_rdoq": ("orc_pre_rdoq", "Xin266PreRdoq", [vp, vp, vp, ip, u32, u32, u32, u32, i32, vp, vp]),
+    "iskip_wxh": ("orc_iskip_wxh", "Xin266ISkipWxH", [vp, ip, vp, ip, u32, u32]),
+    "fdct_wxh": ("orc_fdct_wxh", "ref_fdct_wxh", [vp, ip, vp, ip, u32, u32, u32, u32, i32, i32]),
+    "idct_wxh": ("orc_idct_wxh", "ref_idct_wxh", [vp, ip, vp, ip, u32, u32, i32, u32, u32, i32]),
+    "sub_fdct_wxh": ("orc_sub_fdct_wxh", "ref_sub_fdct_wxh", [vp, ip, vp, ip, vp, ip, u32, u32, i32, i32, i32, i32]),
+    "idct_add": ("orc_idct_add", "ref_idct_add", [vp, ip, vp, ip, vp, ip, i32, u32, u32, u32, u32, i32]),
+    # oracle-only
+    "sad": ("orc_sad", None, [vp, ip, vp, ip, u32, u32, vp]),
+    "sad_xn": ("orc_sad_xn", None, [vp, ip, vp, C.c_int, ip, u32, u32, vp]),
+    "avg_sad": ("orc_avg_sad", None, [vp, ip, vp, vp, ip, u32, u32, vp]),
+    "avg_sad_xn": ("orc_avg_sad_xn", None, [vp, ip, vp, vp, C.c_int, ip, u32, u32, vp]),
+    "satd": ("orc_satd", None, [vp, ip, vp, ip, u32, u32, vp]),
+    "avg_satd": ("orc_avg_satd", None, [vp, ip, vp, vp, ip, u32, u32, vp]),
+    "weight_sad": ("orc_weight_sad", None, [vp, ip, vp, vp, ip, u32, u32, i32, i32, vp]),
+    "weight_satd": ("orc_weight_satd", None, [vp, ip, vp, vp, ip, u32, u32, i32, i32, vp]),
+    "hada8x8": ("orc_hada8x8", None, [vp, ip, vp]),
+    "var": ("orc_var", None, [vp, ip, vp, ip, u32, u32, vp]),
+    "avg_var": ("orc_avg_var", None, [vp, ip, vp, vp, ip, u32, u32, vp]),
+    "fdct1d": ("orc_fdct1d", None, [C.c_int, C.c_int, vp, ip, vp, ip, i32, i32]),
+    "idct1d": ("orc_idct1d", None, [C.c_int, C.c_int, vp, ip, vp, ip, i32, i32, i32]),
+    "fdct2_wxh": ("orc_fdct2_wxh", None, [vp, ip, vp, ip, u32, u32, i32, i32]),
+    "idct2_wxh": ("orc_idct2_wxh", None, [vp, ip, vp, ip, u32, u32, i32, i32]),
+    "fskip_wxh": ("orc_fskip_wxh", None, [vp, ip, vp, ip, u32, u32]),
+    "block_sub": ("orc_block_sub", None, [vp, ip, vp, ip, vp, ip, u32, u32]),
+    "block_add": ("orc_block_add", None, [vp, ip, vp, ip, vp, ip, u32, u32]),
+    "luma_interpolation": ("orc_luma_interpolation", None, [vp, ip, vp, ip, i32, u32, u32, u32]),
+    "luma_inter_pred": ("orc_luma_inter_pred", None, [vp, ip, vp, ip, i32, i32, i32, i32, i32, i32, i32, i32, u32, u32, u32]),
+    "chroma_motion_comp": ("orc_chroma_motion_comp", None, [vp, ip, vp, ip, i32, i32, i32, i32, i32, i32, i32, i32, u32, u32]),
+    "quant_params": ("orc_quant_params", None, [i32, u32, u32, u32, C.c_int, C.c_int, C.POINTER(orc_qparams)]),
+    "transform_tu": ("orc_transform_tu", None, [vp, ip, vp, ip, vp, vp, vp, ip, u32, u32, u32, u32, i32, C.c_int, C.c_int,
+                                                C.c_int, C.c_int, vp]),
+    "mvd_bits": ("orc_mvd_bits", None, [i32]),
+    "mv_window": ("orc_mv_window", None, [i32] * 7 + [C.POINTER(i32)] * 4),
+    "me_full": ("orc_me_full", None, [vp, ip, vp, ip, u32, u32, i32, i32, i32, u32, i32, i32, i32, i32, C.POINTER(orc_me_io)]),
+    "full_subpel_me": ("orc_full_subpel_me", None, [vp, ip, vp, ip, u32, u32, i32, i32, u32, i32, i32, i32, i32,
+                                                    C.POINTER(orc_me_io)]),
+    "cu_hotpath": ("orc_cu_hotpath", None, [C.POINTER(orc_frame_desc), i32, i32, i32, vp * 3, ip * 2, vp * 3, ip * 2,
+                                            C.POINTER(orc_cu_out)]),
+    "tr_matrix": ("orc_tr_matrix", None, [C.c_int, C.c_int]),
+}
+_REF_ONLY = {
+    "idct2_wxh_tmp": ("Xin266IDct2WxH", [vp, ip, vp, ip, u32, u32, vp, i32, i32]),
+    "full_subpel_me_io": ("ref_full_subpel_me", [vp, ip, vp, ip, u32, u32, i32, i32, u32, i32, i32, i32, i32, vp]),
+    "transform_tu_ref": ("ref_transform_tu", [vp, ip, vp, ip, vp, vp, vp, ip, u32, u32, u32, u32, i32, i32, u32, i32, i32,
+                                              i32, vp, vp]),
+}
+
+
+class _Lib:
+    def __init__(self, path: str, which: int, bitdepth: int):
+        self.path = path
+        self.lib = C.CDLL(path, mode=C.RTLD_LOCAL)
+        self.bitdepth = bitdepth
+        self.pix = np.uint8 if bitdepth == 8 else np.uint16
+        self.coef = np.int16 if bitdepth == 8 else np.int32
+        self.max_pix = (1 << bitdepth) - 1
+        for name, spec in _SIGS.items():
+            sym = spec[which]
+            if sym is None:
+                continue
+            f = getattr(self.lib, sym)
+            f.argtypes = spec[2]
+            f.restype = None
+            setattr(self, name, f)
+        if which == 0:
+            self.mvd_bits.restype = u32
+            self.tr_matrix.restype = C.POINTER(C.c_int16)
+        else:
+            for name, (sym, args) in _REF_ONLY.items():
+                f = getattr(self.lib, sym)
+                f.argtypes = args
+                f.restype = None
+                setattr(self, name, f)
+
+    def matrix(self, tr_type: int, n: int) -> np.ndarray:
+        p = self.tr_matrix(tr_type, n)
+        return np.ctypeslib.as_array(p, shape=(n * n,)).reshape(n, n).copy()
+
+
+_CACHE: dict = {}
+
+
+def oracle(bitdepth: int = 8) -> _Lib:
+    """The C restatement (checker), built on demand."""
+    key = ("orc", bitdepth)
+    if key not in _CACHE:
+        path = os.path.join(HERE, f"liboracle{bitdepth}.so")
+        if not os.path.exists(path):
+            build()
+        _CACHE[key] = _Lib(path, 0, bitdepth)
+    return _CACHE[key]
+
+
+def reference(bitdepth: int = 8) -> _Lib:
+    """The reference's open C compiled in place (only where oracle/_ref was built)."""
+    key = ("ref", bitdepth)
+    if key not in _CACHE:
+        path = os.path.join(HERE, "_ref", f"libxinref{bitdepth}.so")
+        _CACHE[key] = _Lib(path, 1, bitdepth)
+    return _CACHE[key]

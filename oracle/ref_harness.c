@@ -1,0 +1,165 @@
+/*
+ * ref_harness.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Flat C entry points around the reference's open drivers, which take the
+ * encoder's section / sequence / CU structures.  Each harness fills the few
+ * fields the driver reads (everything else zero) and calls it unmodified:
+ *   Xin266FDctWxH       h266_encoder/source/h266_forward_trans.c:45
+ *   Xin266IDctWxH       h266_encoder/source/h266_inverse_trans.c:117
+ *   Xin266SubFDctWxH    h266_encoder/source/h266_sub_dct.c:47
+ *   Xin266IDctAdd       h266_encoder/source/h266_idct_add.c:45
+ *   Xin266FullSubPelMe  h266_encoder/source/h266_sub_pel_refine.c:81
+ *   Xin266Transform     h266_encoder/source/h266_trans_quant.c:61
+ * The quant parameter table of Xin266ConstructQuantParam (static in
+ * h266_encoder_create.c:1677) is rebuilt here from the same formula.
+ */
+#include "xin_typedef.h"
+#include "string.h"
+#include "basic_macro.h"
+#include "h266_constant.h"
+#include "xin_video_common.h"
+#include "h26x_definition.h"
+#include "h266_definition.h"
+#include "h266_picture_struct.h"
+#include "h266_intra_pred_context.h"
+#include "h266_pred_unit_struct.h"
+#include "h266_seq_struct.h"
+#include "h266_trans_unit_struct.h"
+#include "h26x_me_struct.h"
+#include "h266_cabac_struct.h"
+#include "h266_md_buffer_struct.h"
+#include "h266_coding_unit_struct.h"
+#include "h266_alf_struct.h"
+#include "h266_section_struct.h"
+#include "h26x_trans_context.h"
+#include "h266_func_struct.h"
+#include "h266_motion_est.h"
+#include "h266_forward_trans.h"
+#include "h266_inverse_trans.h"
+#include "h266_sub_dct.h"
+#include "h266_idct_add.h"
+#include "h266_trans_recon.h"
+
+void shim_fill_table(xin_func_struct *fs);
+extern const UINT32 calcLog2[256];
+void Xin266Transform(xin_sec_struct *secSet, xin_cu_struct *cu, xin_fast_md_buf *fastBuf, UINT32 mtsIdx, UINT32 planeIdx);
+
+typedef struct harness {
+    xin_sec_struct  sec;
+    xin_seq_struct  seq;
+    xin_pic_struct  pic;
+    xin_func_struct fs;
+    xin_me_struct   me;
+    xin_ref_picture pw;
+    COEFF           temp[4 * 128 * 128];
+    xin_quant_param qp0[128], qp1[128];
+} harness;
+
+static harness *harness_new(int enable_mts)
+{
+    harness *h = (harness *)calloc(1, sizeof(harness));
+    shim_fill_table(&h->fs);
+    h->sec.seqSet = &h->seq;
+    h->sec.picSet = &h->pic;
+    h->sec.funcSet = &h->fs;
+    h->sec.meSet = &h->me;
+    h->sec.tempBuffer = (UINT8 *)h->temp;
+    h->pic.pictureWrite = &h->pw;
+    h->seq.config.internalBitDepth = XIN_INTERNAL_BIT_DEPTH;
+    h->seq.config.enableMts = enable_mts;
+    for (UINT32 qp = 0; qp < 128; qp++) {
+        static const UINT32 qm[2][6] = { { 26214, 23302, 20560, 18396, 16384, 14564 }, { 18396, 16384, 14564, 13107, 11651, 10280 } };
+        static const UINT32 iqm[2][6] = { { 40, 45, 51, 57, 64, 72 }, { 57, 64, 72, 80, 90, 102 } };
+        UINT32 rem = qp % 6, per = qp / 6;
+        h->qp0[qp].qMult = (SINT32)qm[0][rem]; h->qp0[qp].iqMult = (SINT32)(iqm[0][rem] << per);
+        h->qp1[qp].qMult = (SINT32)qm[1][rem]; h->qp1[qp].iqMult = (SINT32)(iqm[1][rem] << per);
+        h->qp0[qp].qShift = h->qp1[qp].qShift = (SINT32)(14 + (15 - XIN_INTERNAL_BIT_DEPTH) + per);
+        h->qp0[qp].iqShift = h->qp1[qp].iqShift = 6 - (15 - XIN_INTERNAL_BIT_DEPTH);
+    }
+    h->seq.quantParam[0] = h->qp0;
+    h->seq.quantParam[1] = h->qp1;
+    return h;
+}
+
+void ref_fdct_wxh(COEFF *in, intptr_t is, COEFF *out, intptr_t os, UINT32 comp, UINT32 w, UINT32 h,
+                  UINT32 mts, BOOL is_intra, BOOL enable_mts)
+{
+    harness *hs = harness_new(enable_mts);
+    Xin266FDctWxH(&hs->sec, in, is, out, os, comp, w, h, mts, is_intra);
+    free(hs);
+}
+
+void ref_idct_wxh(COEFF *in, intptr_t is, COEFF *out, intptr_t os, UINT32 w, UINT32 h,
+                  BOOL is_intra, UINT32 comp, UINT32 mts, BOOL enable_mts)
+{
+    harness *hs = harness_new(enable_mts);
+    Xin266IDctWxH(&hs->sec, in, is, out, os, w, h, is_intra, comp, mts);
+    free(hs);
+}
+
+void ref_sub_fdct_wxh(PIXEL *in, intptr_t is, PIXEL *pred, intptr_t ps, COEFF *out, intptr_t os,
+                      UINT32 comp, UINT32 mts, SINT32 w, SINT32 h, BOOL is_intra, BOOL enable_mts)
+{
+    harness *hs = harness_new(enable_mts);
+    Xin266SubFDctWxH(&hs->sec, in, is, pred, ps, out, os, comp, mts, w, h, is_intra);
+    free(hs);
+}
+
+void ref_idct_add(COEFF *in, intptr_t is, PIXEL *pred, intptr_t ps, PIXEL *out, intptr_t os,
+                  BOOL is_intra, UINT32 comp, UINT32 mts, UINT32 w, UINT32 h, BOOL enable_mts)
+{
+    harness *hs = harness_new(enable_mts);
+    Xin266IDctAdd(&hs->sec, in, is, pred, ps, out, os, is_intra, comp, mts, w, h);
+    free(hs);
+}
+
+/* mv and cost in/out: io[0]=mvx, io[1]=mvy (quarter-pel), io[2]=cost */
+void ref_full_subpel_me(PIXEL *in, intptr_t is, PIXEL *ref_at_pu, intptr_t rs, UINT32 w, UINT32 h,
+                        SINT32 mvpx, SINT32 mvpy, UINT32 lambda,
+                        SINT32 min_mvx, SINT32 min_mvy, SINT32 max_mvx, SINT32 max_mvy, SINT32 *io)
+{
+    harness *hs = harness_new(0);
+    xin_me_struct *me = &hs->me;
+    me->input = in; me->inputStride = is; me->ref = ref_at_pu; me->refStride = rs;
+    me->width = w; me->height = h; me->sadLambda = lambda;
+    me->predMv.mv.mvX = (SINT16)mvpx; me->predMv.mv.mvY = (SINT16)mvpy;
+    me->bestMv.mv.mvX = (SINT16)io[0]; me->bestMv.mv.mvY = (SINT16)io[1]; me->bestCost = (UINT32)io[2];
+    me->minMv.mv.mvX = (SINT16)min_mvx; me->minMv.mv.mvY = (SINT16)min_mvy;
+    me->maxMv.mv.mvX = (SINT16)max_mvx; me->maxMv.mv.mvY = (SINT16)max_mvy;
+    Xin266FullSubPelMe(&hs->sec, 0, 0);
+    io[0] = me->bestMv.mv.mvX; io[1] = me->bestMv.mv.mvY; io[2] = (SINT32)me->bestCost;
+    free(hs);
+}
+
+/* One CU with one TU of w x h (TU = CU) at the origin of the given planes.
+ * Returns t, q, r with stride cs and the non-zero CG map. */
+void ref_transform_tu(PIXEL *in, intptr_t is, PIXEL *pred, intptr_t ps, COEFF *t, COEFF *q, COEFF *r, intptr_t cs,
+                      UINT32 w, UINT32 h, UINT32 plane, UINT32 mts, SINT32 qp, BOOL rdoq, UINT32 rdoq_thr,
+                      BOOL intra_frame, BOOL is_intra, BOOL enable_mts, xin_scan_pos *scan_cg, UINT64 *nz)
+{
+    harness *hs = harness_new(enable_mts);
+    xin_cu_struct cu; xin_tu_struct tu; xin_fast_md_buf fast; xin_full_md_buf full;
+    UINT32 comp = plane != 0, lw = calcLog2[w], lh = calcLog2[h];
+    memset(&cu, 0, sizeof cu); memset(&tu, 0, sizeof tu); memset(&fast, 0, sizeof fast); memset(&full, 0, sizeof full);
+    hs->seq.config.enableRdoq = rdoq;
+    hs->seq.config.rdoqThrVal = rdoq_thr;
+    hs->pw.frameType = intra_frame ? XIN_I_FRAME : XIN_P_FRAME;
+    hs->sec.qp = qp; hs->sec.uvQp = qp;
+    hs->sec.inputYStride = is; hs->sec.inputUvStride = is;
+    hs->sec.reshapeCu[plane] = in;
+    cu.lgTuWidth[comp] = (UINT8)lw; cu.lgTuHeight[comp] = (UINT8)lh;
+    cu.tu[0] = &tu;
+    tu.lgWidth[comp] = (UINT8)lw; tu.lgHeight[comp] = (UINT8)lh;
+    tu.lgCGWidth[comp] = 2; tu.lgCGHeight[comp] = 2;
+    tu.scanOrderCG[comp] = scan_cg;
+    fast.fullBuf = &full;
+    fast.type = is_intra ? XIN_INTRA_MODE : 0;
+    fast.predBuf[plane] = pred;
+    fast.lumaStride = ps; fast.chromaStride = ps;
+    full.coeffStride[comp] = cs;
+    full.tuNum = 1;
+    full.tCoefBuf[mts][plane] = t; full.qCoefBuf[mts][plane] = q; full.rCoefBuf[mts][plane] = r;
+    Xin266Transform(&hs->sec, &cu, &fast, mts, plane);
+    *nz = full.nzCGMapRs[mts][0][plane];
+    free(hs);
+}

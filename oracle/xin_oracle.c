@@ -1,0 +1,907 @@
+/*
+ * xin_oracle.c -- CPU oracle (checker) for the xin26x VVC encoder pixel hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
+ * CPU legs of bench.py to check the CUDA library.  The product never links it.
+ * See xin_oracle.h for the parity status legend ("pinned (open C)",
+ * "pinned (H.266)", "unpinned").  Reference citations are path:line inside the
+ * xin26x source tree.
+ */
+#include "xin_oracle.h"
+#include <stdlib.h>
+#include <string.h>
+
+#define CLIP3(lo, hi, v) ((v) < (lo) ? (lo) : ((v) > (hi) ? (hi) : (v)))
+#define IABS(v) ((v) < 0 ? -(v) : (v))
+
+int orc_bitdepth(void) { return ORC_BITDEPTH; }
+
+static inline opix clip_pix(int32_t v) { return (opix)CLIP3(0, ORC_MAX_PIX, v); }
+static inline int32_t clip16(int32_t v) { return CLIP3(-32768, 32767, v); }
+static inline uint32_t lg2u(uint32_t v) { uint32_t l = 0; while ((1u << l) < v) l++; return l; }
+
+/* ======================================================================
+ * Distortion.  The reference ships these only as a closed binary
+ * (declarations h26x_core/include/h26x_compute_dist.h:27-1096).
+ * ====================================================================== */
+
+/* SAD: sum |in - ref| over w x h.  Unpinned but unambiguous (Xin26xComputeSad,
+ * h26x_compute_dist.h:27). */
+void orc_sad(const opix *in, intptr_t is, const opix *ref, intptr_t rs, uint32_t w, uint32_t h, uint32_t *sad)
+{
+    uint32_t s = 0;
+    for (uint32_t y = 0; y < h; y++, in += is, ref += rs)
+        for (uint32_t x = 0; x < w; x++) s += (uint32_t)IABS((int32_t)in[x] - (int32_t)ref[x]);
+    *sad = s;
+}
+
+/* n SADs of one input against n references (Xin26xComputeSadx8/x5/x3,
+ * h26x_compute_dist.h:400,482,625).  Unpinned, unambiguous. */
+void orc_sad_xn(const opix *in, intptr_t is, const opix *const *ref, int n, intptr_t rs, uint32_t w, uint32_t h, uint32_t *sad)
+{
+    for (int i = 0; i < n; i++) orc_sad(in, is, ref[i], rs, w, h, sad + i);
+}
+
+/* bi-prediction average (a + b + 1) >> 1, the H.266 default-weight rounding.
+ * Used by Xin26xComputeAvgSad/AvgSatd/AvgVar (h26x_compute_dist.h:153,880,1008).
+ * Unpinned (closed). */
+static inline int32_t avg2(int32_t a, int32_t b) { return (a + b + 1) >> 1; }
+
+void orc_avg_sad(const opix *in, intptr_t is, const opix *a, const opix *b, intptr_t rs, uint32_t w, uint32_t h, uint32_t *sad)
+{
+    uint32_t s = 0;
+    for (uint32_t y = 0; y < h; y++, in += is, a += rs, b += rs)
+        for (uint32_t x = 0; x < w; x++) s += (uint32_t)IABS((int32_t)in[x] - avg2(a[x], b[x]));
+    *sad = s;
+}
+
+void orc_avg_sad_xn(const opix *in, intptr_t is, const opix *const *a, const opix *const *b, int n, intptr_t rs, uint32_t w, uint32_t h, uint32_t *sad)
+{
+    for (int i = 0; i < n; i++) orc_avg_sad(in, is, a[i], b[i], rs, w, h, sad + i);
+}
+
+/* BCW blend of two pixel predictions, weights in units of 1/8
+ * (XIN_BCW_LOG_WGT_BASE = 3, h266_core/include/h266_constant.h:24):
+ * clip((wa*a + wb*b + 4) >> 3).  Unpinned (closed Xin26xComputeWeightSad/Satd,
+ * h26x_compute_dist.h:1048,1060). */
+static inline int32_t wblend(int32_t a, int32_t b, int32_t wa, int32_t wb)
+{
+    return CLIP3(0, ORC_MAX_PIX, (wa * a + wb * b + 4) >> 3);
+}
+
+void orc_weight_sad(const opix *in, intptr_t is, const opix *a, const opix *b, intptr_t rs, uint32_t w, uint32_t h, int32_t wa, int32_t wb, uint32_t *sad)
+{
+    uint32_t s = 0;
+    for (uint32_t y = 0; y < h; y++, in += is, a += rs, b += rs)
+        for (uint32_t x = 0; x < w; x++) s += (uint32_t)IABS((int32_t)in[x] - wblend(a[x], b[x], wa, wb));
+    *sad = s;
+}
+
+/* Walsh-Hadamard SATD of a difference block.  Published method: HM's
+ * TComRdCost::xCalcHADs4x4 / xCalcHADs8x8 -- sum of |H D H^T| over 4x4 tiles
+ * normalised (S + 1) >> 1, over 8x8 tiles normalised (S + 2) >> 2; 8x8 tiles
+ * when both sides are multiples of 8, else 4x4 tiles.  The sum of absolute
+ * values does not depend on the butterfly order.  Unpinned (closed
+ * Xin26xComputeSatd, h26x_compute_dist.h:806-936). */
+static uint32_t had4(const int32_t *d, int ds)
+{
+    int32_t m[16], t[16];
+    for (int r = 0; r < 4; r++) {
+        const int32_t *p = d + r * ds;
+        int32_t s01 = p[0] + p[1], d01 = p[0] - p[1], s23 = p[2] + p[3], d23 = p[2] - p[3];
+        t[r * 4 + 0] = s01 + s23; t[r * 4 + 1] = s01 - s23; t[r * 4 + 2] = d01 + d23; t[r * 4 + 3] = d01 - d23;
+    }
+    for (int c = 0; c < 4; c++) {
+        int32_t s01 = t[c] + t[4 + c], d01 = t[c] - t[4 + c], s23 = t[8 + c] + t[12 + c], d23 = t[8 + c] - t[12 + c];
+        m[c] = s01 + s23; m[4 + c] = s01 - s23; m[8 + c] = d01 + d23; m[12 + c] = d01 - d23;
+    }
+    uint32_t s = 0;
+    for (int i = 0; i < 16; i++) s += (uint32_t)IABS(m[i]);
+    return s;
+}
+
+static uint32_t had8(const int32_t *d, int ds)
+{
+    int32_t t[64];
+    for (int r = 0; r < 8; r++) {
+        const int32_t *p = d + r * ds;
+        int32_t a[8], b[8];
+        for (int i = 0; i < 4; i++) { a[i] = p[i] + p[i + 4]; a[i + 4] = p[i] - p[i + 4]; }
+        for (int g = 0; g < 8; g += 4) { b[g] = a[g] + a[g + 2]; b[g + 1] = a[g + 1] + a[g + 3]; b[g + 2] = a[g] - a[g + 2]; b[g + 3] = a[g + 1] - a[g + 3]; }
+        for (int i = 0; i < 8; i += 2) { t[r * 8 + i] = b[i] + b[i + 1]; t[r * 8 + i + 1] = b[i] - b[i + 1]; }
+    }
+    uint32_t s = 0;
+    for (int c = 0; c < 8; c++) {
+        int32_t a[8], b[8];
+        for (int i = 0; i < 4; i++) { a[i] = t[i * 8 + c] + t[(i + 4) * 8 + c]; a[i + 4] = t[i * 8 + c] - t[(i + 4) * 8 + c]; }
+        for (int g = 0; g < 8; g += 4) { b[g] = a[g] + a[g + 2]; b[g + 1] = a[g + 1] + a[g + 3]; b[g + 2] = a[g] - a[g + 2]; b[g + 3] = a[g + 1] - a[g + 3]; }
+        for (int i = 0; i < 8; i += 2) s += (uint32_t)IABS(b[i] + b[i + 1]) + (uint32_t)IABS(b[i] - b[i + 1]);
+    }
+    return s;
+}
+
+static uint32_t satd_of_diff(const int32_t *d, int ds, uint32_t w, uint32_t h)
+{
+    uint32_t s = 0;
+    if ((w % 8) == 0 && (h % 8) == 0) {
+        for (uint32_t y = 0; y < h; y += 8)
+            for (uint32_t x = 0; x < w; x += 8) s += (had8(d + y * ds + x, ds) + 2) >> 2;
+    } else {
+        for (uint32_t y = 0; y < h; y += 4)
+            for (uint32_t x = 0; x < w; x += 4) s += (had4(d + y * ds + x, ds) + 1) >> 1;
+    }
+    return s;
+}
+
+void orc_satd(const opix *in, intptr_t is, const opix *ref, intptr_t rs, uint32_t w, uint32_t h, uint32_t *satd)
+{
+    int32_t *d = (int32_t *)malloc(sizeof(int32_t) * w * h);
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) d[y * w + x] = (int32_t)in[y * is + x] - (int32_t)ref[y * rs + x];
+    *satd = satd_of_diff(d, (int)w, w, h);
+    free(d);
+}
+
+void orc_avg_satd(const opix *in, intptr_t is, const opix *a, const opix *b, intptr_t rs, uint32_t w, uint32_t h, uint32_t *satd)
+{
+    int32_t *d = (int32_t *)malloc(sizeof(int32_t) * w * h);
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) d[y * w + x] = (int32_t)in[y * is + x] - avg2(a[y * rs + x], b[y * rs + x]);
+    *satd = satd_of_diff(d, (int)w, w, h);
+    free(d);
+}
+
+void orc_weight_satd(const opix *in, intptr_t is, const opix *a, const opix *b, intptr_t rs, uint32_t w, uint32_t h, int32_t wa, int32_t wb, uint32_t *satd)
+{
+    int32_t *d = (int32_t *)malloc(sizeof(int32_t) * w * h);
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) d[y * w + x] = (int32_t)in[y * is + x] - wblend(a[y * rs + x], b[y * rs + x], wa, wb);
+    *satd = satd_of_diff(d, (int)w, w, h);
+    free(d);
+}
+
+/* Hadamard activity of one 8x8 pixel block (no prediction), normalised like
+ * the 8x8 SATD.  Unpinned (closed Xin26xComputeHada8x8, h26x_compute_dist.h:937). */
+void orc_hada8x8(const opix *in, intptr_t is, uint32_t *satd)
+{
+    int32_t d[64];
+    for (int y = 0; y < 8; y++) for (int x = 0; x < 8; x++) d[y * 8 + x] = in[y * is + x];
+    *satd = (had8(d, 8) + 2) >> 2;
+}
+
+/* Variance of the difference in - pred: sum(d^2) - (sum d)^2 / (w*h), the
+ * division done as a shift by log2(w*h) on the magnitude.  Unpinned (closed
+ * Xin26xComputeVar/AvgVar, h26x_compute_dist.h:972,1008). */
+static uint32_t var_of(int64_t s, int64_t s2, uint32_t w, uint32_t h)
+{
+    uint32_t lg = lg2u(w * h);
+    int64_t mean2 = (s * s) >> lg;
+    return (uint32_t)(s2 - mean2);
+}
+
+void orc_var(const opix *in, intptr_t is, const opix *ref, intptr_t rs, uint32_t w, uint32_t h, uint32_t *var)
+{
+    int64_t s = 0, s2 = 0;
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) { int32_t d = (int32_t)in[y * is + x] - (int32_t)ref[y * rs + x]; s += d; s2 += (int64_t)d * d; }
+    *var = var_of(s, s2, w, h);
+}
+
+void orc_avg_var(const opix *in, intptr_t is, const opix *a, const opix *b, intptr_t rs, uint32_t w, uint32_t h, uint32_t *var)
+{
+    int64_t s = 0, s2 = 0;
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) { int32_t d = (int32_t)in[y * is + x] - avg2(a[y * rs + x], b[y * rs + x]); s += d; s2 += (int64_t)d * d; }
+    *var = var_of(s, s2, w, h);
+}
+
+/* ======================================================================
+ * Interpolation.  Pinned (open C): h266_core/source/h266_luma_mc.c and
+ * h266_chroma_mc.c.  Filter taps are the H.266 normative tables; only the
+ * first half of each table is written, the second half is the mirror image
+ * (phase P = reverse of phase N - P), which is how the standard's tables are
+ * built.
+ * ====================================================================== */
+#define IF_SHIFT 6                                   /* INTERP_SHIFT, h266_inter_pred_context.h:31 */
+#define IF_PREC 14                                   /* INTERP_PRECISION, :37 */
+#define IF_OFF14 (1 << (IF_PREC - 1))                /* INTERP_PREC_OFFSET, :38 */
+#define IF_HEAD (IF_PREC - ORC_BITDEPTH > 2 ? IF_PREC - ORC_BITDEPTH : 2)  /* max(2, 14 - bd) */
+
+static const int8_t luma_half[9][8] = {             /* H.266 luma 1/16 phases 0..8 */
+    { 0, 0, 0, 64, 0, 0, 0, 0 }, { 0, 1, -3, 63, 4, -2, 1, 0 }, { -1, 2, -5, 62, 8, -3, 1, 0 },
+    { -1, 3, -8, 60, 13, -4, 1, 0 }, { -1, 4, -10, 58, 17, -5, 1, 0 }, { -1, 4, -11, 52, 26, -8, 3, -1 },
+    { -1, 3, -9, 47, 31, -10, 4, -1 }, { -1, 4, -11, 45, 34, -10, 4, -1 }, { -1, 4, -11, 40, 40, -11, 4, -1 } };
+static const int8_t luma4x4_half[9][8] = {          /* H.266 affine 4x4 luma phases 0..8 */
+    { 0, 0, 0, 64, 0, 0, 0, 0 }, { 0, 1, -3, 63, 4, -2, 1, 0 }, { 0, 1, -5, 62, 8, -3, 1, 0 },
+    { 0, 2, -8, 60, 13, -4, 1, 0 }, { 0, 3, -10, 58, 17, -5, 1, 0 }, { 0, 3, -11, 52, 26, -8, 2, 0 },
+    { 0, 2, -9, 47, 31, -10, 3, 0 }, { 0, 3, -11, 45, 34, -10, 3, 0 }, { 0, 3, -11, 40, 40, -11, 3, 0 } };
+static const int8_t luma_alt_hpel[8] = { 0, 3, 9, 20, 20, 9, 3, 0 };  /* H.266 alternative half-pel */
+static const int8_t chroma_half[17][4] = {          /* H.266 chroma 1/32 phases 0..16 */
+    { 0, 64, 0, 0 }, { -1, 63, 2, 0 }, { -2, 62, 4, 0 }, { -2, 60, 7, -1 }, { -2, 58, 10, -2 },
+    { -3, 57, 12, -2 }, { -4, 56, 14, -2 }, { -4, 55, 15, -2 }, { -4, 54, 16, -2 }, { -5, 53, 18, -2 },
+    { -6, 52, 20, -2 }, { -6, 49, 24, -3 }, { -6, 46, 28, -4 }, { -5, 44, 29, -4 }, { -4, 42, 30, -4 },
+    { -4, 39, 33, -4 }, { -4, 36, 36, -4 } };
+
+/* fills taps[8] for a 1/16 luma phase and filterIndex (0 default, 1 alt half-pel, 2 affine 4x4),
+ * following the selection at h266_luma_mc.c:117-128 */
+static void luma_taps(int phase, uint32_t fi, int32_t *taps)
+{
+    if (fi == 1 && phase == 8) { for (int i = 0; i < 8; i++) taps[i] = luma_alt_hpel[i]; return; }
+    const int8_t (*tab)[8] = (fi == 2) ? luma4x4_half : luma_half;
+    if (phase <= 8) for (int i = 0; i < 8; i++) taps[i] = tab[phase][i];
+    else for (int i = 0; i < 8; i++) taps[i] = tab[16 - phase][7 - i];
+}
+
+static void chroma_taps(int phase, int32_t *taps)
+{
+    if (phase <= 16) for (int i = 0; i < 4; i++) taps[i] = chroma_half[phase][i];
+    else for (int i = 0; i < 4; i++) taps[i] = chroma_half[32 - phase][3 - i];
+}
+
+/* generic separable FIR pass: NT taps, input element type selected by the caller */
+#define FIR_ROW(SRC, STEP, T, NT) ({ int32_t _s = 0; for (int _k = 0; _k < (NT); _k++) _s += (int32_t)(SRC)[_k * (STEP)] * (T)[_k]; _s; })
+
+/* Copy (Xin266InterpCopy, h266_luma_mc.c:72) */
+void orc_interp_copy(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{
+    (void)frac; (void)fi;
+    for (uint32_t y = 0; y < h; y++, src += ss, dst += ds) memcpy(dst, src, w * sizeof(opix));
+}
+
+/* Copy to the 14-bit intermediate: (p << max(2,14-bd)) - 8192 (Xin266InterpCopyU8S16, h266_luma_mc.c:430) */
+void orc_interp_copy_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{
+    (void)frac; (void)fi;
+    for (uint32_t y = 0; y < h; y++, src += ss, dst += ds)
+        for (uint32_t x = 0; x < w; x++) dst[x] = (int16_t)(((int32_t)src[x] << IF_HEAD) - IF_OFF14);
+}
+
+/* One-pass filter to pixels: clip((sum + 32) >> 6).  NT = 8 (luma) or 4 (chroma);
+ * dir 0 = horizontal, 1 = vertical.  Xin266LumaInterpHor/Vet (h266_luma_mc.c:100,157),
+ * Xin266ChromaInterpHor/Vet (h266_chroma_mc.c:62,99). */
+static void fir_pix(const opix *src, intptr_t ss, opix *dst, intptr_t ds, const int32_t *t, int nt, int dir, uint32_t w, uint32_t h)
+{
+    intptr_t step = dir ? ss : 1;
+    src -= (nt / 2 - 1) * step;
+    for (uint32_t y = 0; y < h; y++, src += ss, dst += ds)
+        for (uint32_t x = 0; x < w; x++) dst[x] = clip_pix((FIR_ROW(src + x, step, t, nt) + (1 << (IF_SHIFT - 1))) >> IF_SHIFT);
+}
+
+/* One-pass filter from pixels to the 14-bit intermediate: (sum - (8192 << s)) >> s,
+ * s = 6 - max(2, 14 - bd).  Xin266LumaInterpHorU8S16 / VetU8S16 (h266_luma_mc.c:216,465). */
+static void fir_pix_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, const int32_t *t, int nt, int dir, uint32_t w, uint32_t h)
+{
+    intptr_t step = dir ? ss : 1;
+    int32_t shift = IF_SHIFT - IF_HEAD, offset = -IF_OFF14 * (1 << shift);
+    src -= (nt / 2 - 1) * step;
+    for (uint32_t y = 0; y < h; y++, src += ss, dst += ds)
+        for (uint32_t x = 0; x < w; x++) dst[x] = (int16_t)((FIR_ROW(src + x, step, t, nt) + offset) >> shift);
+}
+
+/* Vertical pass from the intermediate to pixels: clip((sum + (1 << (s-1)) + (8192 << 6)) >> s),
+ * s = 6 + max(2, 14 - bd).  Xin266LumaInterpVetS16U8 (h266_luma_mc.c:275). */
+static void fir_s16_pix(const int16_t *src, intptr_t ss, opix *dst, intptr_t ds, const int32_t *t, int nt, uint32_t w, uint32_t h)
+{
+    int32_t shift = IF_SHIFT + IF_HEAD, offset = (1 << (shift - 1)) + (IF_OFF14 << IF_SHIFT);
+    src -= (nt / 2 - 1) * ss;
+    for (uint32_t y = 0; y < h; y++, src += ss, dst += ds)
+        for (uint32_t x = 0; x < w; x++) dst[x] = clip_pix((FIR_ROW(src + x, ss, t, nt) + offset) >> shift);
+}
+
+/* Vertical pass intermediate -> intermediate: sum >> 6.  Xin266LumaInterpVetS16S16 (h266_luma_mc.c:338). */
+static void fir_s16_s16(const int16_t *src, intptr_t ss, int16_t *dst, intptr_t ds, const int32_t *t, int nt, uint32_t w, uint32_t h)
+{
+    src -= (nt / 2 - 1) * ss;
+    for (uint32_t y = 0; y < h; y++, src += ss, dst += ds)
+        for (uint32_t x = 0; x < w; x++) dst[x] = (int16_t)(FIR_ROW(src + x, ss, t, nt) >> IF_SHIFT);
+}
+
+/* Two-pass HV: horizontal to the intermediate over h + nt - 1 rows, then vertical.
+ * Xin266LumaInterpHorVet (h266_luma_mc.c:394), HorVetU8S16 (:525). */
+static void fir_hv(const opix *src, intptr_t ss, void *dst, intptr_t ds, const int32_t *th, const int32_t *tv, int nt,
+                   uint32_t w, uint32_t h, int to_s16)
+{
+    int16_t *tmp = (int16_t *)malloc(sizeof(int16_t) * w * (h + nt - 1));
+    fir_pix_s16(src - (nt / 2 - 1) * ss, ss, tmp, w, th, nt, 0, w, h + nt - 1);
+    if (to_s16) fir_s16_s16(tmp + (nt / 2 - 1) * w, w, (int16_t *)dst, ds, tv, nt, w, h);
+    else fir_s16_pix(tmp + (nt / 2 - 1) * w, w, (opix *)dst, ds, tv, nt, w, h);
+    free(tmp);
+}
+
+/* luma: horizontal phase = frac & 15 (h266_luma_mc.c:116), vertical phase = frac >> 4 (:173) */
+void orc_luma_hor(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ int32_t t[8]; luma_taps(frac & 15, fi, t); fir_pix(src, ss, dst, ds, t, 8, 0, w, h); }
+void orc_luma_vet(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ int32_t t[8]; luma_taps(frac >> 4, fi, t); fir_pix(src, ss, dst, ds, t, 8, 1, w, h); }
+void orc_luma_hv(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ int32_t th[8], tv[8]; luma_taps(frac & 15, fi, th); luma_taps(frac >> 4, fi, tv); fir_hv(src, ss, dst, ds, th, tv, 8, w, h, 0); }
+void orc_luma_hor_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ int32_t t[8]; luma_taps(frac & 15, fi, t); fir_pix_s16(src, ss, dst, ds, t, 8, 0, w, h); }
+void orc_luma_vet_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ int32_t t[8]; luma_taps(frac >> 4, fi, t); fir_pix_s16(src, ss, dst, ds, t, 8, 1, w, h); }
+void orc_luma_hv_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ int32_t th[8], tv[8]; luma_taps(frac & 15, fi, th); luma_taps(frac >> 4, fi, tv); fir_hv(src, ss, dst, ds, th, tv, 8, w, h, 1); }
+void orc_luma_vet_s16_pix(const int16_t *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ int32_t t[8]; luma_taps(frac >> 4, fi, t); fir_s16_pix(src, ss, dst, ds, t, 8, w, h); }
+void orc_luma_vet_s16_s16(const int16_t *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ int32_t t[8]; luma_taps(frac >> 4, fi, t); fir_s16_s16(src, ss, dst, ds, t, 8, w, h); }
+
+/* chroma: horizontal phase = frac & 31 (h266_chroma_mc.c:72), vertical phase = frac >> 5 (:109) */
+void orc_chroma_hor(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ (void)fi; int32_t t[4]; chroma_taps(frac & 31, t); fir_pix(src, ss, dst, ds, t, 4, 0, w, h); }
+void orc_chroma_vet(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ (void)fi; int32_t t[4]; chroma_taps(frac >> 5, t); fir_pix(src, ss, dst, ds, t, 4, 1, w, h); }
+void orc_chroma_hv(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ (void)fi; int32_t th[4], tv[4]; chroma_taps(frac & 31, th); chroma_taps(frac >> 5, tv); fir_hv(src, ss, dst, ds, th, tv, 4, w, h, 0); }
+void orc_chroma_hor_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ (void)fi; int32_t t[4]; chroma_taps(frac & 31, t); fir_pix_s16(src, ss, dst, ds, t, 4, 0, w, h); }
+void orc_chroma_vet_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ (void)fi; int32_t t[4]; chroma_taps(frac >> 5, t); fir_pix_s16(src, ss, dst, ds, t, 4, 1, w, h); }
+void orc_chroma_hv_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ (void)fi; int32_t th[4], tv[4]; chroma_taps(frac & 31, th); chroma_taps(frac >> 5, tv); fir_hv(src, ss, dst, ds, th, tv, 4, w, h, 1); }
+void orc_chroma_vet_s16_pix(const int16_t *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ (void)fi; int32_t t[4]; chroma_taps(frac >> 5, t); fir_s16_pix(src, ss, dst, ds, t, 4, w, h); }
+void orc_chroma_vet_s16_s16(const int16_t *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi)
+{ (void)fi; int32_t t[4]; chroma_taps(frac >> 5, t); fir_s16_s16(src, ss, dst, ds, t, 4, w, h); }
+
+/* bi average of two intermediates: clip((a + b + (1 << (s-1)) + 2*8192) >> s), s = max(2,14-bd) + 1
+ * (Xin266InterpAvgS16U8, h266_luma_mc.c:561) */
+void orc_interp_avg(const int16_t *a, intptr_t as, const int16_t *b, intptr_t bs, opix *dst, intptr_t ds, uint32_t w, uint32_t h)
+{
+    int32_t shift = IF_HEAD + 1, offset = (1 << (shift - 1)) + 2 * IF_OFF14;
+    for (uint32_t y = 0; y < h; y++, a += as, b += bs, dst += ds)
+        for (uint32_t x = 0; x < w; x++) dst[x] = clip_pix(((int32_t)a[x] + b[x] + offset) >> shift);
+}
+
+/* BCW blend of two intermediates: clip((a*wa + b*wb + (1 << (s-1)) + (8192 << 3)) >> s),
+ * s = max(2,14-bd) + 3 (Xin266InterpWeightS16U8, h266_luma_mc.c:595) */
+void orc_interp_weight(const int16_t *a, intptr_t as, const int16_t *b, intptr_t bs, opix *dst, intptr_t ds, uint32_t w, uint32_t h, int32_t wa, int32_t wb)
+{
+    int32_t shift = IF_HEAD + 3, offset = (1 << (shift - 1)) + (IF_OFF14 << 3);
+    for (uint32_t y = 0; y < h; y++, a += as, b += bs, dst += ds)
+        for (uint32_t x = 0; x < w; x++) dst[x] = clip_pix(((int32_t)a[x] * wa + (int32_t)b[x] * wb + offset) >> shift);
+}
+
+/* Table dispatch pfXinLumaInterp[!!fx][!!fy][lgW] (h266_encoder/source/h266_inter_prediction.c:143-169).
+ * The 8-argument form is the one h266_sub_pel_refine.c calls through the header
+ * h266_encoder/include/h266_inter_prediction.h:43; the filter index is the
+ * caller's (0 in that call path). */
+void orc_luma_interpolation(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t lgw, uint32_t h, uint32_t fi)
+{
+    int fx = frac & 15, fy = (frac >> 4) & 15;
+    uint32_t w = 1u << lgw;
+    if (!fx && !fy) orc_interp_copy(src, ss, dst, ds, frac, w, h, fi);
+    else if (fx && !fy) orc_luma_hor(src, ss, dst, ds, frac, w, h, fi);
+    else if (!fx && fy) orc_luma_vet(src, ss, dst, ds, frac, w, h, fi);
+    else orc_luma_hv(src, ss, dst, ds, frac, w, h, fi);
+}
+
+/* h266_inter_prediction.c:171 Xin266ChromaInterpolation (frac = fy << 5 | fx) */
+void orc_chroma_interpolation(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t lgw, uint32_t h)
+{
+    uint32_t w = 1u << lgw;
+    if (!frac) orc_interp_copy(src, ss, dst, ds, frac, w, h, 0);
+    else if (!(frac & (31 << 5))) orc_chroma_hor(src, ss, dst, ds, frac, w, h, 0);
+    else if (!(frac & 31)) orc_chroma_vet(src, ss, dst, ds, frac, w, h, 0);
+    else orc_chroma_hv(src, ss, dst, ds, frac, w, h, 0);
+}
+
+/* Xin266LumaInterPred (h266_inter_prediction.c:302-351): clamp the 1/16-pel MV to the
+ * CU's window, split into integer offset and phase, dispatch. */
+void orc_luma_inter_pred(const opix *ref_origin, intptr_t rs, opix *pred, intptr_t ps, int32_t mvx16, int32_t mvy16,
+                         int32_t cu_x, int32_t cu_y, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
+                         uint32_t w, uint32_t h, uint32_t fi)
+{
+    int32_t mvx = CLIP3(min_mvx * 16, max_mvx * 16, mvx16), mvy = CLIP3(min_mvy * 16, max_mvy * 16, mvy16);
+    int32_t ox = cu_x * 16 + mvx, oy = cu_y * 16 + mvy;
+    int32_t frac = ((oy & 15) << 4) + (ox & 15);
+    orc_luma_interpolation(ref_origin + (intptr_t)(oy >> 4) * rs + (ox >> 4), rs, pred, ps, frac, lg2u(w), h, fi);
+}
+
+/* Uni-prediction branch of Xin266ChromaMotionComp (h266_inter_prediction.c:784-818):
+ * chroma phase is the 1/32 remainder (mask 31) of the luma 1/16 position. */
+void orc_chroma_motion_comp(const opix *ref_origin, intptr_t rs, opix *pred, intptr_t ps, int32_t mvx16, int32_t mvy16,
+                            int32_t cu_x, int32_t cu_y, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
+                            uint32_t w, uint32_t h)
+{
+    int32_t mvx = CLIP3(min_mvx * 16, max_mvx * 16, mvx16), mvy = CLIP3(min_mvy * 16, max_mvy * 16, mvy16);
+    int32_t ox = cu_x * 16 + mvx, oy = cu_y * 16 + mvy;
+    int32_t fx = ox & 31, fy = oy & 31, frac = (fy << 5) + fx;
+    const opix *src = ref_origin + (intptr_t)(oy >> 5) * rs + (ox >> 5);
+    uint32_t cw = w >> 1, ch = h >> 1;
+    if (!fx && !fy) orc_interp_copy(src, rs, pred, ps, frac, cw, ch, 0);
+    else if (fx && !fy) orc_chroma_hor(src, rs, pred, ps, frac, cw, ch, 0);
+    else if (!fx && fy) orc_chroma_vet(src, rs, pred, ps, frac, cw, ch, 0);
+    else orc_chroma_hv(src, rs, pred, ps, frac, cw, ch, 0);
+}
+
+/* ======================================================================
+ * Transforms.
+ * Matrices: H.266 clause 8.7.4.5 transMatrix (DCT-II up to 64 points) and the
+ * DST-VII / DCT-VIII matrices for 4..32 points.  They are generated here from
+ * the standard's unique coefficient magnitudes and the trigonometric sign /
+ * index structure of each transform:
+ *   DCT-II : T64[k][n] = g(k*(2n+1) mod 256), g(m) ~ 64*sqrt(2)*cos(m*pi/128),
+ *            row 0 = 64, and the N-point matrix is rows 0, 64/N, 2*64/N ... of T64.
+ *   DST-VII: T[k][n] = a((2k+1)(n+1)), a(m) ~ sin(m*pi/(2N+1)) with period 2(2N+1).
+ *   DCT-VIII: T[k][n] = (-1)^k * DST-VII[k][N-1-n].
+ * The 1-D routines (closed in the reference, h26x_core/include/h26x_forward_1d_trans.h,
+ * h26x_inverse_1d_trans.h) follow the reference's call contract read from the open
+ * 2-D wrappers h266_encoder/source/h266_forward_trans.c:100-151 and
+ * h266_inverse_trans.c:52-88,184-229:
+ *   forward: line i of input (stride is) -> out[k*os + i]   (transposing)
+ *   inverse: column j: coefficients in[k*is + j] -> out[j*os + n] (transposing);
+ *            the last skip_line lines are not transformed and come out zero.
+ * Rounding (x + 2^(s-1)) >> s.  Forward outputs saturate to 16 bits (unpinned);
+ * inverse outputs clip to 16 bits after each stage (H.266 8.7.4.1 intermediate clip).
+ * ====================================================================== */
+static const uint8_t dct2_c64[65] = {
+    /* m = 0..64 : magnitude for angle m*pi/128 (m = 0 only reached by row 0) */
+    64, 91, 90, 90, 90, 90, 90, 90, 89, 88, 88, 87, 87, 86, 85, 84,
+    83, 83, 82, 81, 80, 79, 78, 77, 75, 73, 73, 71, 70, 69, 67, 65,
+    64, 62, 61, 59, 57, 56, 54, 52, 50, 48, 46, 44, 43, 41, 38, 37,
+    36, 33, 31, 28, 25, 24, 22, 20, 18, 15, 13, 11, 9, 7, 4, 2, 0 };
+static const uint8_t dst7_a4[4]  = { 29, 55, 74, 84 };
+static const uint8_t dst7_a8[8]  = { 17, 32, 46, 60, 71, 78, 85, 86 };
+static const uint8_t dst7_a16[16] = { 8, 17, 25, 33, 40, 48, 55, 62, 68, 73, 77, 81, 85, 87, 88, 88 };
+static const uint8_t dst7_a32[32] = { 4, 9, 13, 17, 21, 26, 30, 34, 38, 42, 46, 50, 53, 56, 60, 63,
+                                      66, 68, 72, 74, 77, 78, 80, 82, 84, 85, 86, 88, 88, 89, 90, 90 };
+
+static int16_t mat_dct2[7][64 * 64];   /* index lg 1..6 */
+static int16_t mat_dst7[6][32 * 32];   /* index lg 2..5 */
+static int16_t mat_dct8[6][32 * 32];
+static int mats_ready = 0;
+
+static int dct2_g(int m)
+{
+    m &= 255;
+    if (m <= 64) return dct2_c64[m];
+    if (m <= 128) return -dct2_c64[128 - m];
+    if (m <= 192) return -dct2_c64[m - 128];
+    return dct2_c64[256 - m];
+}
+
+static void build_mats(void)
+{
+    if (mats_ready) return;
+    for (int lg = 1; lg <= 6; lg++) {
+        int n = 1 << lg, step = 64 / n;
+        for (int k = 0; k < n; k++)
+            for (int i = 0; i < n; i++) {
+                int kk = k * step;
+                mat_dct2[lg][k * n + i] = (int16_t)(kk == 0 ? 64 : dct2_g(kk * (2 * i + 1)));
+            }
+    }
+    for (int lg = 2; lg <= 5; lg++) {
+        int n = 1 << lg, period = 2 * (2 * n + 1);
+        const uint8_t *a = lg == 2 ? dst7_a4 : lg == 3 ? dst7_a8 : lg == 4 ? dst7_a16 : dst7_a32;
+        for (int k = 0; k < n; k++)
+            for (int i = 0; i < n; i++) {
+                int m = ((2 * k + 1) * (i + 1)) % period, v;
+                int half = 2 * n + 1;
+                if (m == 0 || m == half) v = 0;
+                else if (m < half) v = a[(m <= n ? m : half - m) - 1];
+                else { int mm = m - half; v = -a[(mm <= n ? mm : half - mm) - 1]; }
+                mat_dst7[lg][k * n + i] = (int16_t)v;
+            }
+        for (int k = 0; k < n; k++)
+            for (int i = 0; i < n; i++)
+                mat_dct8[lg][k * n + i] = (int16_t)((k & 1 ? -1 : 1) * mat_dst7[lg][k * n + (n - 1 - i)]);
+    }
+    mats_ready = 1;
+}
+
+/* type: 0 DCT2, 1 DCT8, 2 DST7 (XIN_DCT2/DCT8/DST7, h26x_core/include/h26x_trans_context.h:33-40) */
+const int16_t *orc_tr_matrix(int type, int n)
+{
+    build_mats();
+    int lg = (int)lg2u((uint32_t)n);
+    if (type == 0 && lg >= 1 && lg <= 6) return mat_dct2[lg];
+    if (type == 1 && lg >= 2 && lg <= 5) return mat_dct8[lg];
+    if (type == 2 && lg >= 2 && lg <= 5) return mat_dst7[lg];
+    return NULL;
+}
+
+static inline int32_t rshift_rnd(int32_t v, int32_t s) { return s > 0 ? (v + (1 << (s - 1))) >> s : v; }
+
+void orc_fdct1d(int type, int lg, const ocoef *in, intptr_t is, ocoef *out, intptr_t os, int32_t line, int32_t shift)
+{
+    int n = 1 << lg;
+    const int16_t *m = orc_tr_matrix(type, n);
+    for (int i = 0; i < line; i++)
+        for (int k = 0; k < n; k++) {
+            int32_t s = 0;
+            for (int j = 0; j < n; j++) s += (int32_t)m[k * n + j] * (int32_t)in[i * is + j];
+            out[k * os + i] = (ocoef)clip16(rshift_rnd(s, shift));
+        }
+}
+
+void orc_idct1d(int type, int lg, const ocoef *in, intptr_t is, ocoef *out, intptr_t os, int32_t line, int32_t skip_line, int32_t shift)
+{
+    int n = 1 << lg;
+    const int16_t *m = orc_tr_matrix(type, n);
+    for (int j = 0; j < line; j++)
+        for (int x = 0; x < n; x++) {
+            int32_t s = 0;
+            if (j < line - skip_line)
+                for (int k = 0; k < n; k++) s += (int32_t)m[k * n + x] * (int32_t)in[k * is + j];
+            out[j * os + x] = (ocoef)(j < line - skip_line ? clip16(rshift_rnd(s, shift)) : 0);
+        }
+}
+
+/* Xin26xFDct2WxH (closed, h26x_core/include/h26x_forward_2d_trans.h): rows then columns
+ * through a transposed temporary, the same composition Xin266FDctWxH uses for the
+ * separable types (h266_forward_trans.c:112-128).  Unpinned. */
+void orc_fdct2_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t w, uint32_t h, int32_t s1, int32_t s2)
+{
+    ocoef *tmp = (ocoef *)malloc(sizeof(ocoef) * w * h);
+    orc_fdct1d(0, (int)lg2u(w), in, is, tmp, h, (int32_t)h, s1);
+    orc_fdct1d(0, (int)lg2u(h), tmp, h, out, os, (int32_t)w, s2);
+    free(tmp);
+}
+
+/* Xin266IDct2WxH (open, h266_inverse_trans.c:52-88): columns first with the zero-out
+ * skip of lines beyond 32, then rows. */
+void orc_idct2_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t w, uint32_t h, int32_t s1, int32_t s2)
+{
+    ocoef *tmp = (ocoef *)malloc(sizeof(ocoef) * w * h);
+    int32_t skip = w > 32 ? (int32_t)w - 32 : 0;
+    orc_idct1d(0, (int)lg2u(h), in, is, tmp, h, (int32_t)w, skip, s1);
+    orc_idct1d(0, (int)lg2u(w), tmp, h, out, os, (int32_t)h, 0, s2);
+    free(tmp);
+}
+
+/* Forward transform skip: r << (15 - bd - (lgW + lgH)/2) (H.266 transform-skip scaling,
+ * mirror of the open inverse Xin266ISkipWxH).  Unpinned (closed Xin26xFSkipWxH). */
+void orc_fskip_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t w, uint32_t h)
+{
+    int32_t sh = 15 - ORC_BITDEPTH - (int32_t)((lg2u(w) + lg2u(h)) >> 1);
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) {
+            int32_t v = in[y * is + x];
+            out[y * os + x] = (ocoef)clip16(sh >= 0 ? v * (1 << sh) : rshift_rnd(v, -sh));
+        }
+}
+
+/* Xin266ISkipWxH (open, h266_inverse_trans.c:91-115): v >> (15 - 8 - (lgW+lgH)/2), truncated to 16 bits. */
+void orc_iskip_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t w, uint32_t h)
+{
+    int32_t sh = 15 - 8 - (int32_t)((lg2u(w) + lg2u(h)) >> 1);
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) out[y * os + x] = (ocoef)(int16_t)((int32_t)in[y * is + x] >> sh);
+}
+
+/* MTS index -> (horizontal, vertical) type; XIN_MTS_* order at
+ * h26x_core/include/h26x_trans_context.h:42-51 (1 = transform skip, coded as 4). */
+static const int8_t mts_tx[6][2] = { { 0, 0 }, { 4, 4 }, { 2, 2 }, { 1, 2 }, { 2, 1 }, { 1, 1 } };
+
+/* Xin266FDctWxH (open, h266_forward_trans.c:45-151) */
+void orc_fdct_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t comp, uint32_t w, uint32_t h,
+                  uint32_t mts, int is_intra, int enable_mts)
+{
+    int hor = mts_tx[mts][0], ver = mts_tx[mts][1];
+    int lgw = (int)lg2u(w), lgh = (int)lg2u(h);
+    int32_t s1 = lgw + ORC_BITDEPTH + 6 - 15, s2 = lgh + 6;
+    if (is_intra && comp == 0 && enable_mts && mts == 0) {
+        if (w >= 4 && w <= 16) hor = 2;
+        if (h >= 4 && h <= 16) ver = 2;
+    }
+    if (lgw > 0 && lgh > 0 && hor == 0 && ver == 0) { orc_fdct2_wxh(in, is, out, os, w, h, s1, s2); return; }
+    if (hor == 4) { orc_fskip_wxh(in, is, out, os, w, h); return; }
+    if (lgw > 0 && lgh > 0) {
+        ocoef *tmp = (ocoef *)malloc(sizeof(ocoef) * w * h);
+        orc_fdct1d(hor, lgw, in, is, tmp, h, (int32_t)h, s1);
+        orc_fdct1d(ver, lgh, tmp, h, out, os, (int32_t)w, s2);
+        free(tmp);
+    } else if (lgw > 0) orc_fdct1d(hor, lgw, in, is, out, os, (int32_t)h, s1);
+    else orc_fdct1d(ver, lgh, in, is, out, os, (int32_t)w, s2);
+}
+
+/* Xin266IDctWxH (open, h266_inverse_trans.c:117-229).  The two degenerate 1-D branches
+ * write into the reference's scratch buffer and leave the output untouched; here the
+ * same result goes to the scratch and the output is left untouched too. */
+void orc_idct_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t w, uint32_t h,
+                  int is_intra, uint32_t comp, uint32_t mts, int enable_mts)
+{
+    int hor = mts_tx[mts][0], ver = mts_tx[mts][1];
+    int lgw = (int)lg2u(w), lgh = (int)lg2u(h);
+    int32_t s1 = 6 + 1, s2 = 6 + 15 - 1 - ORC_BITDEPTH;
+    int32_t skip = (hor != 0 && w == 32) ? 16 : (w > 32 ? (int32_t)w - 32 : 0);
+    if (is_intra && comp == 0 && enable_mts && mts == 0) {
+        if (w >= 4 && w <= 16) hor = 2;
+        if (h >= 4 && h <= 16) ver = 2;
+    }
+    if (lgw > 0 && lgh > 0 && hor == 0 && ver == 0) { orc_idct2_wxh(in, is, out, os, w, h, s1, s2); return; }
+    if (hor == 4) { orc_iskip_wxh(in, is, out, os, w, h); return; }
+    if (lgw > 0 && lgh > 0) {
+        ocoef *tmp = (ocoef *)malloc(sizeof(ocoef) * w * h);
+        orc_idct1d(ver, lgh, in, is, tmp, h, (int32_t)w, skip, s1);
+        orc_idct1d(hor, lgw, tmp, h, out, os, (int32_t)h, 0, s2);
+        free(tmp);
+    }
+}
+
+/* residual = input - prediction (closed Xin26xBlockSubForDct, h26x_core/include/h26x_block_utility.h).
+ * Unpinned, unambiguous. */
+void orc_block_sub(const opix *in, intptr_t is, const opix *pred, intptr_t ps, ocoef *diff, intptr_t ds, uint32_t w, uint32_t h)
+{
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) diff[y * ds + x] = (ocoef)((int32_t)in[y * is + x] - (int32_t)pred[y * ps + x]);
+}
+
+/* recon = clip(pred + residual) (closed Xin26xBlockRecon via pfXinBlockAddForDct,
+ * h266_idct_add.c:94).  Unpinned, unambiguous. */
+void orc_block_add(const ocoef *res, intptr_t rs, const opix *pred, intptr_t ps, opix *rec, intptr_t os, uint32_t w, uint32_t h)
+{
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) rec[y * os + x] = clip_pix((int32_t)pred[y * ps + x] + (int32_t)res[y * rs + x]);
+}
+
+/* Xin266SubFDctWxH (open, h266_sub_dct.c:47-107), LMCS chroma scaling off */
+void orc_sub_fdct_wxh(const opix *in, intptr_t is, const opix *pred, intptr_t ps, ocoef *out, intptr_t os,
+                      uint32_t comp, uint32_t mts, int32_t w, int32_t h, int is_intra, int enable_mts)
+{
+    ocoef *res = (ocoef *)malloc(sizeof(ocoef) * (size_t)(w * h));
+    orc_block_sub(in, is, pred, ps, res, w, (uint32_t)w, (uint32_t)h);
+    orc_fdct_wxh(res, w, out, os, comp, (uint32_t)w, (uint32_t)h, mts, is_intra, enable_mts);
+    free(res);
+}
+
+/* Xin266IDctAdd (open, h266_idct_add.c:45-105), LMCS chroma scaling off */
+void orc_idct_add(const ocoef *in, intptr_t is, const opix *pred, intptr_t ps, opix *out, intptr_t os,
+                  int is_intra, uint32_t comp, uint32_t mts, uint32_t w, uint32_t h, int enable_mts)
+{
+    ocoef *buf = (ocoef *)calloc(64 * 64, sizeof(ocoef));
+    orc_idct_wxh(in, is, buf, 64, w, h, is_intra, comp, mts, enable_mts);
+    orc_block_add(buf, 64, pred, ps, out, os, w, h);
+    free(buf);
+}
+
+/* ======================================================================
+ * Quantisation.  Pinned (open C).
+ * ====================================================================== */
+
+/* Xin266QuantInvQuant + Xin266QIQCodingGroup (h266_quant_inv_quant.c:27-139):
+ * coding groups visited from the last (bottom-right) to the first in raster order;
+ * bit 0 of the map is CG 0 (raster), i.e. bit b <-> CG b. */
+void orc_quant_inv_quant(ocoef *q, const ocoef *t, ocoef *r, intptr_t stride, uint32_t w, uint32_t h,
+                         uint32_t cgw, uint32_t cgh, int32_t qmult, int32_t qadd, int32_t qshift,
+                         int32_t iqmult, int32_t iqadd, int32_t iqshift, uint64_t *nz)
+{
+    uint32_t wcg = w / cgw, hcg = h / cgh;
+    uint64_t map = 0;
+    for (int by = (int)hcg - 1; by >= 0; by--)
+        for (int bx = (int)wcg - 1; bx >= 0; bx--) {
+            int any = 0;
+            for (uint32_t y = 0; y < cgh; y++)
+                for (uint32_t x = 0; x < cgw; x++) {
+                    intptr_t p = (intptr_t)(by * (int)cgh + (int)y) * stride + bx * (int)cgw + (int)x;
+                    int32_t tv = t[p], a = IABS(tv);
+                    int32_t qv = (int32_t)(((int64_t)a * qmult + qadd) >> qshift);
+                    qv = CLIP3(-32768, 32767, tv < 0 ? -qv : qv);
+                    q[p] = (ocoef)qv;
+                    int32_t rv = (int32_t)(((int64_t)qv * iqmult + iqadd) >> iqshift);
+                    r[p] = (ocoef)CLIP3(-32768, 32767, rv);
+                    any |= qv != 0;
+                }
+            map = (map << 1) | (uint64_t)any;
+        }
+    *nz = map;
+}
+
+/* Xin266PreRdoq (h266_quant_inv_quant.c:208-288): walking the CG scan backwards,
+ * zero each non-zero CG whose |t| are all <= thr, stop at the first that is not. */
+void orc_pre_rdoq(const ocoef *t, ocoef *r, ocoef *q, intptr_t stride, uint32_t w, uint32_t h,
+                  uint32_t cgw, uint32_t cgh, int32_t thr, const orc_scan_pos *scan_cg, uint64_t *nz)
+{
+    int32_t nblk = (int32_t)(w * h / (cgw * cgh)), wcg = (int32_t)(w / cgw);
+    uint64_t map = *nz;
+    for (int32_t i = nblk - 1; i >= 1; i--) {
+        uint32_t pos = scan_cg[i].posIdx;
+        if (!(map & ((uint64_t)1 << pos))) continue;
+        int32_t by = (int32_t)pos / wcg, bx = (int32_t)pos - by * wcg;
+        int big = 0;
+        for (uint32_t y = 0; y < cgh; y++)
+            for (uint32_t x = 0; x < 4; x++) {
+                int32_t v = t[(by * (int32_t)cgh + (int32_t)y) * stride + bx * (int32_t)cgw + (int32_t)x];
+                big |= IABS(v) > thr;
+            }
+        if (big) break;
+        for (uint32_t y = 0; y < 4; y++)
+            for (uint32_t x = 0; x < cgw; x++) {
+                intptr_t p = (intptr_t)(by * (int32_t)cgh + (int32_t)y) * stride + bx * (int32_t)cgw + (int32_t)x;
+                r[p] = 0; q[p] = 0;
+            }
+        map &= ~((uint64_t)1 << pos);
+    }
+    *nz = map;
+}
+
+/* Quant parameters of one TU.  qMult/iqMult tables and shift bases from
+ * Xin266ConstructQuantParam (h266_encoder_create.c:94-105,1677-1707); the per-TU
+ * adjustment, qAdd and iqAdd from Xin266Transform (h266_trans_quant.c:107-120).
+ * qp is the slice QP; the 10-bit build adds XIN_QP_SHIFT = 12 like :101. */
+void orc_quant_params(int32_t qp, uint32_t lgw, uint32_t lgh, uint32_t mts, int rdoq, int intra_frame, orc_qparams *p)
+{
+    static const int32_t qm[2][6] = { { 26214, 23302, 20560, 18396, 16384, 14564 }, { 18396, 16384, 14564, 13107, 11651, 10280 } };
+    static const int32_t iqm[2][6] = { { 40, 45, 51, 57, 64, 72 }, { 57, 64, 72, 80, 90, 102 } };
+    if (ORC_BITDEPTH == 10) qp += 12;
+    uint32_t lgt = lgw + lgh;
+    int adj = (int)(lgt & 1) && mts != 1;
+    int32_t lgs = (int32_t)(lgt >> 1);
+    int32_t per = qp / 6, rem = qp % 6;
+    p->qmult = qm[adj][rem];
+    p->iqmult = iqm[adj][rem] << per;
+    p->qshift = 14 + (15 - ORC_BITDEPTH) + per - lgs - adj;
+    p->iqshift = 6 - (15 - ORC_BITDEPTH) + lgs + adj;
+    p->qadd = (rdoq && mts != 1) ? (1 << (p->qshift - 1)) : ((intra_frame ? 171 : 85) << (p->qshift - 9));
+    p->iqadd = (mts != 1) ? (1 << (p->iqshift - 1)) : (1 << ((p->iqshift - lgs) + (15 - ORC_BITDEPTH) - 1));
+}
+
+/* One TU of Xin266Transform without dependent quantisation and without the
+ * pre-RDOQ pass (h266_trans_quant.c:131-220): residual + forward transform into t,
+ * zero-out of r beyond 32, quant/dequant over the low min(w,32) x min(h,32) part
+ * with 4x4 coding groups.  Output strides are cs. */
+void orc_transform_tu(const opix *in, intptr_t is, const opix *pred, intptr_t ps,
+                      ocoef *t, ocoef *q, ocoef *r, intptr_t cs, uint32_t w, uint32_t h, uint32_t comp,
+                      uint32_t mts, int32_t qp, int rdoq, int intra_frame, int is_intra, int enable_mts, uint64_t *nz)
+{
+    orc_qparams p;
+    orc_quant_params(qp, lg2u(w), lg2u(h), mts, rdoq, intra_frame, &p);
+    orc_sub_fdct_wxh(in, is, pred, ps, t, cs, comp, mts, (int32_t)w, (int32_t)h, is_intra, enable_mts);
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++)
+            if (x >= 32 || y >= 32) { r[y * cs + x] = 0; q[y * cs + x] = 0; }
+    orc_quant_inv_quant(q, t, r, cs, w < 32 ? w : 32, h < 32 ? h : 32, 4, 4, p.qmult, p.qadd, p.qshift,
+                        p.iqmult, p.iqadd, p.iqshift, nz);
+}
+
+/* ======================================================================
+ * Motion estimation.
+ * ====================================================================== */
+
+/* Signed Exp-Golomb code length of v: 2*floor(log2(u+1)) + 1 with u = 2v-1 (v > 0)
+ * or -2v (v <= 0).  Stands in for the closed table ExpGolombBits
+ * (h26x_core/include/h26x_common_data.h:23) read through
+ * CALC_MVD_BIT (common/include/h26x_definition.h:176).  Unpinned. */
+uint32_t orc_mvd_bits(int32_t v)
+{
+    uint32_t u = v > 0 ? (uint32_t)(2 * v - 1) : (uint32_t)(-2 * v), l = 0;
+    u += 1;
+    while (u > 1) { u >>= 1; l++; }
+    return 2 * l + 1;
+}
+
+void orc_exp_golomb_table(uint32_t *tab)
+{
+    for (int32_t i = 0; i < 32767; i++) tab[i] = orc_mvd_bits(i - 16383);
+}
+
+static inline uint32_t mv_cost(int32_t mvx, int32_t mvy, int32_t mvpx, int32_t mvpy, uint32_t lambda)
+{
+    return (orc_mvd_bits(mvx - mvpx) + orc_mvd_bits(mvy - mvpy)) * lambda;
+}
+
+/* Per-CU integer MV window from the reference-plane padding (ctu + 16 on each side):
+ * h266_encoder/source/h266_enc_init.c:1462-1465. */
+void orc_mv_window(int32_t frame_w, int32_t frame_h, int32_t ctu, int32_t cu_x, int32_t cu_y, int32_t cu_w, int32_t cu_h,
+                   int32_t *min_mvx, int32_t *min_mvy, int32_t *max_mvx, int32_t *max_mvy)
+{
+    *min_mvx = (int16_t)(-cu_x - ctu - (16 - 8));
+    *min_mvy = (int16_t)(-cu_y - ctu - (16 - 8));
+    *max_mvx = (int16_t)(frame_w + (ctu - cu_w + 16 - 8) - cu_x);
+    *max_mvy = (int16_t)(frame_h + (ctu - cu_h + 16 - 8) - cu_y);
+}
+
+/* Exhaustive integer search (stands in for the closed Xin26xMotionEstFull,
+ * h26x_core/include/h26x_motion_est.h:23-36): every integer MV in
+ * [c - range, c + range]^2 intersected with [min, max], c = predictor >> 2, visited
+ * in raster order (y outer, x inner) with a strict '<' on
+ * cost = (SAD << 8) + (bits(mvd_x) + bits(mvd_y)) * lambda, mvd in quarter-pel,
+ * the cost form of the open sub-pel search (h266_sub_pel_refine.c:155-156).
+ * The search starts from io->best_cost (the caller's running best).  Unpinned
+ * (the closed drivers' search order is not visible). */
+void orc_me_full(const opix *in, intptr_t is, const opix *ref_at_pu, intptr_t rs, uint32_t w, uint32_t h,
+                 int32_t mvpx, int32_t mvpy, int32_t range, uint32_t lambda,
+                 int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy, orc_me_io *io)
+{
+    int32_t cx = mvpx >> 2, cy = mvpy >> 2;
+    int32_t x0 = cx - range > min_mvx ? cx - range : min_mvx, x1 = cx + range < max_mvx ? cx + range : max_mvx;
+    int32_t y0 = cy - range > min_mvy ? cy - range : min_mvy, y1 = cy + range < max_mvy ? cy + range : max_mvy;
+    uint32_t best = io->best_cost, bsad = io->best_sad;
+    int32_t bx = io->best_mvx, by = io->best_mvy;
+    for (int32_t y = y0; y <= y1; y++)
+        for (int32_t x = x0; x <= x1; x++) {
+            uint32_t sad;
+            orc_sad(in, is, ref_at_pu + (intptr_t)y * rs + x, rs, w, h, &sad);
+            uint32_t c = (sad << 8) + mv_cost(x * 4, y * 4, mvpx, mvpy, lambda);
+            if (c < best) { best = c; bsad = sad; bx = x * 4; by = y * 4; }
+        }
+    io->best_cost = best; io->best_sad = bsad; io->best_mvx = bx; io->best_mvy = by;
+}
+
+/* Xin266FullSubPelMe (open, h266_sub_pel_refine.c:81-212): 8 half-pel then 8
+ * quarter-pel neighbours in the fixed order of :47-55, luma interpolation with the
+ * default filter into a W x H block, SAD, strict '<'.  Returns unchanged when the
+ * integer part of the start MV is outside the window (:117-120). */
+void orc_full_subpel_me(const opix *in, intptr_t is, const opix *ref_at_pu, intptr_t rs, uint32_t w, uint32_t h,
+                        int32_t mvpx, int32_t mvpy, uint32_t lambda,
+                        int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy, orc_me_io *io)
+{
+    static const int8_t off[8][2] = { { -1, 0 }, { 1, 0 }, { 0, -1 }, { 0, 1 }, { -1, -1 }, { 1, -1 }, { -1, 1 }, { 1, 1 } };
+    int32_t mvx = io->best_mvx, mvy = io->best_mvy;
+    if (!((mvx >> 2) >= min_mvx && (mvy >> 2) >= min_mvy && (mvx >> 2) <= max_mvx && (mvy >> 2) <= max_mvy)) return;
+    opix *pred = (opix *)malloc(sizeof(opix) * w * h);
+    uint32_t best = io->best_cost;
+    int32_t bx = mvx, by = mvy;
+    for (int step = 2; step >= 1; step--) {
+        int32_t cxm = bx, cym = by;
+        for (int p = 0; p < 8; p++) {
+            int32_t tx = cxm + off[p][0] * step, ty = cym + off[p][1] * step;
+            int32_t frac = (((ty << 2) & 15) << 4) + ((tx << 2) & 15);
+            uint32_t sad;
+            orc_luma_interpolation(ref_at_pu + (intptr_t)((ty << 2) >> 4) * rs + ((tx << 2) >> 4), rs, pred, w, frac, lg2u(w), h, 0);
+            orc_sad(in, is, pred, w, w, h, &sad);
+            uint32_t c = (sad << 8) + mv_cost(tx, ty, mvpx, mvpy, lambda);
+            if (c < best) { best = c; bx = tx; by = ty; }
+        }
+    }
+    free(pred);
+    io->best_cost = best; io->best_mvx = bx; io->best_mvy = by;
+}
+
+/* ======================================================================
+ * Frame hot path of one CU (the checker of the batched GPU frame stages):
+ *   window (h266_enc_init.c:1462) -> exhaustive integer search around MVP 0
+ *   -> Xin266FullSubPelMe -> Xin266LumaInterPred / uni Xin266ChromaMotionComp
+ *   -> per plane Xin266Transform TU (DCT2, TU = CU, 4x4 CGs, no RDOQ)
+ *   -> Xin266IDctAdd recon; SSD(recon, input) per plane.
+ * The integer search starts from cost UINT32_MAX at MV (0,0).
+ * ====================================================================== */
+void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size,
+                    ocoef *q[3], intptr_t q_stride[2], opix *rec[3], intptr_t rec_stride[2], orc_cu_out *out)
+{
+    int32_t mnx, mny, mxx, mxy;
+    orc_mv_window(f->width, f->height, f->ctu, cu_x, cu_y, size, size, &mnx, &mny, &mxx, &mxy);
+    const opix *in_y = f->in[0] + (intptr_t)cu_y * f->in_stride[0] + cu_x;
+    const opix *ref_y = f->ref[0] + (intptr_t)cu_y * f->ref_stride[0] + cu_x;
+    orc_me_io io = { 0, 0, 0xFFFFFFFFu, 0 };
+    orc_me_full(in_y, f->in_stride[0], ref_y, f->ref_stride[0], (uint32_t)size, (uint32_t)size, 0, 0,
+                f->search_range, f->sad_lambda, mnx, mny, mxx, mxy, &io);
+    out->int_cost = io.best_cost;
+    orc_full_subpel_me(in_y, f->in_stride[0], ref_y, f->ref_stride[0], (uint32_t)size, (uint32_t)size, 0, 0,
+                       f->sad_lambda, mnx, mny, mxx, mxy, &io);
+    out->mvx = io.best_mvx; out->mvy = io.best_mvy; out->cost = io.best_cost;
+
+    int32_t cs = size >> 1;
+    opix *pred = (opix *)malloc(sizeof(opix) * (size_t)(size * size));
+    ocoef *t = (ocoef *)malloc(sizeof(ocoef) * (size_t)(size * size));
+    ocoef *qb = (ocoef *)malloc(sizeof(ocoef) * (size_t)(size * size));
+    ocoef *r = (ocoef *)malloc(sizeof(ocoef) * (size_t)(size * size));
+    for (int pl = 0; pl < 3; pl++) {
+        int32_t bs = pl ? cs : size, px = pl ? cu_x >> 1 : cu_x, py = pl ? cu_y >> 1 : cu_y;
+        intptr_t istr = f->in_stride[pl ? 1 : 0], qstr = q_stride[pl ? 1 : 0], rstr = rec_stride[pl ? 1 : 0];
+        if (pl == 0)
+            orc_luma_inter_pred(f->ref[0], f->ref_stride[0], pred, bs, io.best_mvx * 4, io.best_mvy * 4, cu_x, cu_y,
+                                mnx, mny, mxx, mxy, (uint32_t)size, (uint32_t)size, 0);
+        else
+            orc_chroma_motion_comp(f->ref[pl], f->ref_stride[1], pred, bs, io.best_mvx * 4, io.best_mvy * 4, cu_x, cu_y,
+                                   mnx, mny, mxx, mxy, (uint32_t)size, (uint32_t)size);
+        const opix *src = f->in[pl] + (intptr_t)py * istr + px;
+        ocoef *qo = q[pl] + (intptr_t)py * qstr + px;
+        opix *ro = rec[pl] + (intptr_t)py * rstr + px;
+        orc_transform_tu(src, istr, pred, bs, t, qb, r, bs, (uint32_t)bs, (uint32_t)bs,
+                         pl ? 1u : 0u, 0, pl ? f->uv_qp : f->qp, 0, f->intra_frame, 0, 0, &out->nz[pl]);
+        for (int32_t y = 0; y < bs; y++)
+            for (int32_t x = 0; x < bs; x++) qo[y * qstr + x] = qb[y * bs + x];
+        orc_idct_add(r, bs, pred, bs, ro, rstr, 0, pl ? 1u : 0u, 0, (uint32_t)bs, (uint32_t)bs, 0);
+        uint64_t ssd = 0;
+        for (int32_t y = 0; y < bs; y++)
+            for (int32_t x = 0; x < bs; x++) {
+                int64_t d = (int64_t)src[y * istr + x] - (int64_t)ro[y * rstr + x];
+                ssd += (uint64_t)(d * d);
+            }
+        out->ssd[pl] = ssd;
+    }
+    free(pred); free(t); free(qb); free(r);
+}

@@ -1,0 +1,169 @@
+/*
+ * xin_oracle.h -- CPU oracle for the xin26x VVC encoder pixel hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference's
+ * hot-path arithmetic, used by tests/, __graft_entry__.smoke() and the
+ * cpu_baseline / reference legs of bench.py as the checker.  Nothing in the
+ * product (xin26x_gb300/, libxingpu.so) links, loads or calls it.
+ *
+ * Build: compiled twice, once per bit depth, like the reference's compile-time
+ * switch ENABLE_10BIT_ENCODER (video_api/video_common/include/xin_typedef.h:72-96):
+ *   -DORC_BITDEPTH=8  -> opix = uint8_t,  ocoef = int16_t  (liboracle8.so)
+ *   -DORC_BITDEPTH=10 -> opix = uint16_t, ocoef = int32_t  (liboracle10.so)
+ *
+ * Parity status per function is stated in its comment:
+ *   "pinned (open C)"  -- the reference implementation is open C; the oracle
+ *                         restates it and tests/test_oracle_vs_ref.py checks it
+ *                         against that C compiled in place (oracle/_ref) and
+ *                         against the committed golden fixtures.
+ *   "pinned (H.266)"   -- normative arithmetic of the H.266 standard.
+ *   "unpinned"         -- the reference ships only a closed binary for it;
+ *                         restated from the signature, the open call sites and
+ *                         a published method that is named in the comment.
+ */
+#ifndef XIN_ORACLE_H
+#define XIN_ORACLE_H
+
+#include <stdint.h>
+
+#ifndef ORC_BITDEPTH
+#define ORC_BITDEPTH 8
+#endif
+
+#if ORC_BITDEPTH == 10
+typedef uint16_t opix;
+typedef int32_t  ocoef;
+#else
+typedef uint8_t  opix;
+typedef int16_t  ocoef;
+#endif
+
+#define ORC_MAX_PIX ((1 << ORC_BITDEPTH) - 1)
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* scan position triple, same layout as xin_scan_pos
+ * (h266_encoder/include/h266_trans_unit_struct.h:23-28) */
+typedef struct orc_scan_pos { uint32_t posX, posY, posIdx; } orc_scan_pos;
+
+int  orc_bitdepth(void);
+
+/* ---- distortion (closed in the reference: h26x_core/include/h26x_compute_dist.h) */
+void orc_sad(const opix *in, intptr_t is, const opix *ref, intptr_t rs, uint32_t w, uint32_t h, uint32_t *sad);
+void orc_sad_xn(const opix *in, intptr_t is, const opix *const *ref, int n, intptr_t rs, uint32_t w, uint32_t h, uint32_t *sad);
+void orc_avg_sad(const opix *in, intptr_t is, const opix *a, const opix *b, intptr_t rs, uint32_t w, uint32_t h, uint32_t *sad);
+void orc_avg_sad_xn(const opix *in, intptr_t is, const opix *const *a, const opix *const *b, int n, intptr_t rs, uint32_t w, uint32_t h, uint32_t *sad);
+void orc_satd(const opix *in, intptr_t is, const opix *ref, intptr_t rs, uint32_t w, uint32_t h, uint32_t *satd);
+void orc_avg_satd(const opix *in, intptr_t is, const opix *a, const opix *b, intptr_t rs, uint32_t w, uint32_t h, uint32_t *satd);
+void orc_weight_sad(const opix *in, intptr_t is, const opix *a, const opix *b, intptr_t rs, uint32_t w, uint32_t h, int32_t wa, int32_t wb, uint32_t *sad);
+void orc_weight_satd(const opix *in, intptr_t is, const opix *a, const opix *b, intptr_t rs, uint32_t w, uint32_t h, int32_t wa, int32_t wb, uint32_t *satd);
+void orc_hada8x8(const opix *in, intptr_t is, uint32_t *satd);
+void orc_var(const opix *in, intptr_t is, const opix *ref, intptr_t rs, uint32_t w, uint32_t h, uint32_t *var);
+void orc_avg_var(const opix *in, intptr_t is, const opix *a, const opix *b, intptr_t rs, uint32_t w, uint32_t h, uint32_t *var);
+
+/* ---- interpolation (open in the reference: h266_core/source/h266_luma_mc.c, h266_chroma_mc.c) */
+void orc_interp_copy(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_interp_copy_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_luma_hor(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_luma_vet(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_luma_hv(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_luma_hor_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_luma_vet_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_luma_hv_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_luma_vet_s16_pix(const int16_t *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_luma_vet_s16_s16(const int16_t *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_chroma_hor(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_chroma_vet(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_chroma_hv(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_chroma_hor_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_chroma_vet_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_chroma_hv_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_chroma_vet_s16_pix(const int16_t *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_chroma_vet_s16_s16(const int16_t *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
+void orc_interp_avg(const int16_t *a, intptr_t as, const int16_t *b, intptr_t bs, opix *dst, intptr_t ds, uint32_t w, uint32_t h);
+void orc_interp_weight(const int16_t *a, intptr_t as, const int16_t *b, intptr_t bs, opix *dst, intptr_t ds, uint32_t w, uint32_t h, int32_t wa, int32_t wb);
+
+/* call-site dispatch (h266_encoder/source/h266_inter_prediction.c) */
+void orc_luma_interpolation(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t lgw, uint32_t h, uint32_t fi);
+void orc_chroma_interpolation(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t lgw, uint32_t h);
+void orc_luma_inter_pred(const opix *ref_origin, intptr_t rs, opix *pred, intptr_t ps, int32_t mvx16, int32_t mvy16,
+                         int32_t cu_x, int32_t cu_y, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
+                         uint32_t w, uint32_t h, uint32_t fi);
+void orc_chroma_motion_comp(const opix *ref_origin, intptr_t rs, opix *pred, intptr_t ps, int32_t mvx16, int32_t mvy16,
+                            int32_t cu_x, int32_t cu_y, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
+                            uint32_t w, uint32_t h);
+
+/* ---- transforms (1-D closed, 2-D wrappers open) */
+const int16_t *orc_tr_matrix(int type, int n);   /* [n][n] row = basis function k */
+void orc_fdct1d(int type, int lg, const ocoef *in, intptr_t is, ocoef *out, intptr_t os, int32_t line, int32_t shift);
+void orc_idct1d(int type, int lg, const ocoef *in, intptr_t is, ocoef *out, intptr_t os, int32_t line, int32_t skip_line, int32_t shift);
+void orc_fdct2_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t w, uint32_t h, int32_t s1, int32_t s2);
+void orc_idct2_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t w, uint32_t h, int32_t s1, int32_t s2);
+void orc_fskip_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t w, uint32_t h);
+void orc_iskip_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t w, uint32_t h);
+void orc_fdct_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t comp, uint32_t w, uint32_t h,
+                  uint32_t mts, int is_intra, int enable_mts);
+void orc_idct_wxh(const ocoef *in, intptr_t is, ocoef *out, intptr_t os, uint32_t w, uint32_t h,
+                  int is_intra, uint32_t comp, uint32_t mts, int enable_mts);
+void orc_block_sub(const opix *in, intptr_t is, const opix *pred, intptr_t ps, ocoef *diff, intptr_t ds, uint32_t w, uint32_t h);
+void orc_block_add(const ocoef *res, intptr_t rs, const opix *pred, intptr_t ps, opix *rec, intptr_t os, uint32_t w, uint32_t h);
+void orc_sub_fdct_wxh(const opix *in, intptr_t is, const opix *pred, intptr_t ps, ocoef *out, intptr_t os,
+                      uint32_t comp, uint32_t mts, int32_t w, int32_t h, int is_intra, int enable_mts);
+void orc_idct_add(const ocoef *in, intptr_t is, const opix *pred, intptr_t ps, opix *out, intptr_t os,
+                  int is_intra, uint32_t comp, uint32_t mts, uint32_t w, uint32_t h, int enable_mts);
+
+/* ---- quant (open: h266_encoder/source/h266_quant_inv_quant.c, h266_trans_quant.c) */
+void orc_quant_inv_quant(ocoef *q, const ocoef *t, ocoef *r, intptr_t stride, uint32_t w, uint32_t h,
+                         uint32_t cgw, uint32_t cgh, int32_t qmult, int32_t qadd, int32_t qshift,
+                         int32_t iqmult, int32_t iqadd, int32_t iqshift, uint64_t *nz);
+void orc_pre_rdoq(const ocoef *t, ocoef *r, ocoef *q, intptr_t stride, uint32_t w, uint32_t h,
+                  uint32_t cgw, uint32_t cgh, int32_t thr, const orc_scan_pos *scan_cg, uint64_t *nz);
+typedef struct orc_qparams { int32_t qmult, qadd, qshift, iqmult, iqadd, iqshift; } orc_qparams;
+void orc_quant_params(int32_t qp, uint32_t lgw, uint32_t lgh, uint32_t mts, int rdoq, int intra_frame, orc_qparams *p);
+void orc_transform_tu(const opix *in, intptr_t is, const opix *pred, intptr_t ps,
+                      ocoef *t, ocoef *q, ocoef *r, intptr_t cs, uint32_t w, uint32_t h, uint32_t comp,
+                      uint32_t mts, int32_t qp, int rdoq, int intra_frame, int is_intra, int enable_mts, uint64_t *nz);
+
+/* ---- motion estimation */
+uint32_t orc_mvd_bits(int32_t v);
+void orc_exp_golomb_table(uint32_t *tab32767);
+typedef struct orc_me_io {
+    int32_t  best_mvx, best_mvy;      /* quarter-pel, in/out */
+    uint32_t best_cost;               /* in/out */
+    uint32_t best_sad;                /* out (integer search only) */
+} orc_me_io;
+void orc_mv_window(int32_t frame_w, int32_t frame_h, int32_t ctu, int32_t cu_x, int32_t cu_y, int32_t cu_w, int32_t cu_h,
+                   int32_t *min_mvx, int32_t *min_mvy, int32_t *max_mvx, int32_t *max_mvy);
+void orc_me_full(const opix *in, intptr_t is, const opix *ref_at_pu, intptr_t rs, uint32_t w, uint32_t h,
+                 int32_t mvpx, int32_t mvpy, int32_t range, uint32_t lambda,
+                 int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy, orc_me_io *io);
+void orc_full_subpel_me(const opix *in, intptr_t is, const opix *ref_at_pu, intptr_t rs, uint32_t w, uint32_t h,
+                        int32_t mvpx, int32_t mvpy, uint32_t lambda,
+                        int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy, orc_me_io *io);
+
+/* ---- frame hot path: one CU through ME + MC + TQ + recon (the batched GPU frame stage's checker) */
+typedef struct orc_frame_desc {
+    int32_t width, height, ctu;            /* luma size, CTU size (padding = ctu + 16) */
+    const opix *in[3];  intptr_t in_stride[2];    /* current picture planes, [0]=Y stride, [1]=UV stride */
+    const opix *ref[3]; intptr_t ref_stride[2];   /* padded reference planes, pointers at picture (0,0) */
+    int32_t search_range;
+    uint32_t sad_lambda;
+    int32_t qp, uv_qp;
+    int32_t intra_frame;                   /* 0 for P/B: qAdd = 85 << (qShift - 9) */
+} orc_frame_desc;
+typedef struct orc_cu_out {
+    int32_t mvx, mvy;                      /* quarter-pel */
+    uint32_t cost;                         /* after sub-pel */
+    uint32_t int_cost;                     /* after integer search */
+    uint64_t nz[3];
+    uint64_t ssd[3];                       /* recon vs input per plane */
+} orc_cu_out;
+void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size,
+                    ocoef *q[3], intptr_t q_stride[2], opix *rec[3], intptr_t rec_stride[2], orc_cu_out *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,110 @@
+"""Generate the golden fixtures in tests/golden/ from the reference's own C.
+
+Runs in the container that has the xin26x source tree: it builds
+oracle/_ref/libxinref{8,10}.so (the reference's open hot-path C compiled in
+place, oracle/Makefile target ``ref``) and records seeded inputs with that
+library's outputs.  tests/test_oracle_golden.py replays the inputs through
+the oracle anywhere (no reference tree needed) and requires identical output.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from oracle import oracle as O  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def scan_cg(wcg, hcg):
+    out, x, y, n = [], 0, 0, 0
+    while n < wcg * hcg:
+        while y >= 0:
+            if x < wcg and y < hcg:
+                out.append((x, y, y * wcg + x))
+                n += 1
+            y -= 1
+            x += 1
+        y, x = x, 0
+    return np.array(out, np.uint32)
+
+
+def make(bd):
+    O.build(ref=True)
+    r = O.reference(bd)
+    o = O.oracle(bd)
+    rng = np.random.default_rng(20260 + bd)
+    g = {}
+    # interpolation: one 16x8 block per (function, filter index, phase subset)
+    src = rng.integers(0, r.max_pix + 1, size=(4 + 16, 8 + 16)).astype(r.pix)
+    s16 = rng.integers(-8192, 8192, size=(4 + 16, 8 + 16)).astype(np.int16)
+    g["interp_src"] = src
+    g["interp_s16"] = s16
+    for name in ["luma_hor", "luma_vet", "luma_hv", "luma_hor_s16", "luma_vet_s16", "luma_hv_s16", "luma_vet_s16_pix",
+                 "luma_vet_s16_s16", "chroma_hor", "chroma_vet", "chroma_hv", "chroma_hor_s16", "chroma_vet_s16",
+                 "chroma_hv_s16", "chroma_vet_s16_pix", "chroma_vet_s16_s16"]:
+        chroma = name.startswith("chroma")
+        ins = s16 if name.endswith(("s16_pix", "s16_s16")) else src
+        outt = np.int16 if name.endswith("s16") else r.pix
+        fracs = list(range(0, 1024, 29)) if chroma else list(range(0, 256, 3)) + [8, 128, 136]
+        res = []
+        for fi in ((0,) if chroma else (0, 1, 2)):
+            for frac in fracs:
+                b = np.zeros((4, 8), outt)
+                getattr(r, name)(O.ptr(ins, 8 * ins.shape[1] + 8), ins.shape[1], O.ptr(b), 8, frac, 8, 4, fi)
+                res.append(b)
+        g[f"interp_{name}"] = np.stack(res)
+    # quantiser
+    t = np.clip(rng.laplace(0, 400, size=(16, 16)), -32768, 32767).astype(r.coef)
+    g["quant_t"] = t
+    qo, ro, nzo = [], [], []
+    for qp in range(0, 52):
+        p = O.orc_qparams()
+        o.quant_params(qp, 4, 4, 0, qp & 1, qp & 2, p)
+        q = np.zeros((16, 16), r.coef); rr = np.zeros((16, 16), r.coef); nz = np.zeros(1, np.uint64)
+        r.quant_inv_quant(O.ptr(q), O.ptr(t), O.ptr(rr), 16, 16, 16, 4, 4, p.qmult, p.qadd, p.qshift, p.iqmult, p.iqadd,
+                          p.iqshift, O.ptr(nz))
+        qo.append(q); ro.append(rr); nzo.append(nz[0])
+    g["quant_q"], g["quant_r"], g["quant_nz"] = np.stack(qo), np.stack(ro), np.array(nzo, np.uint64)
+    # transforms through the reference's 2-D wrappers (all MTS types, 4..32 and DCT2 64)
+    cases = [(w, h, m) for (w, h) in [(4, 4), (8, 8), (16, 16), (32, 32), (4, 16), (32, 8)] for m in range(6)]
+    cases += [(64, 64, 0), (64, 16, 0), (8, 64, 0)]
+    fres, ires, fin, iin = [], [], [], []
+    lim = (1 << bd) - 1
+    for (w, h, m) in cases:
+        x = rng.integers(-lim, lim + 1, size=(64, 64)).astype(r.coef)
+        c = np.clip(rng.laplace(0, 300, size=(64, 64)), -32768, 32767).astype(r.coef)
+        c[32:, :] = 0
+        c[:, 32:] = 0
+        a = np.zeros((64, 64), r.coef)
+        b = np.zeros((64, 64), r.coef)
+        r.fdct_wxh(O.ptr(x), 64, O.ptr(a), 64, 0, w, h, m, 0, 1)
+        r.idct_wxh(O.ptr(c), 64, O.ptr(b), 64, w, h, 0, 0, m, 1)
+        for lst, arr in ((fin, x), (iin, c), (fres, a), (ires, b)):
+            lst.append(arr[:h, :w].ravel())
+    g["tr_cases"] = np.array(cases, np.int32)
+    g["tr_fin"], g["tr_fout"], g["tr_iin"], g["tr_iout"] = map(np.concatenate, (fin, fres, iin, ires))
+    # sub-pel search
+    pad = 24
+    refp = rng.integers(0, r.max_pix + 1, size=(16 + 2 * pad, 16 + 2 * pad)).astype(r.pix)
+    inp = refp[pad + 1:pad + 17, pad + 2:pad + 18].copy()
+    g["subpel_ref"], g["subpel_in"] = refp, inp
+    sp = []
+    for mvx in range(-6, 7, 3):
+        for mvy in range(-6, 7, 3):
+            io = np.array([mvx, mvy, 0x7FFFFFF0], np.int32)
+            r.full_subpel_me_io(O.ptr(inp), 16, O.ptr(refp, pad * refp.shape[1] + pad), refp.shape[1], 16, 16, 1, -1, 57,
+                                -10, -10, 10, 10, O.ptr(io))
+            sp.append([mvx, mvy, io[0], io[1], io[2]])
+    g["subpel_io"] = np.array(sp, np.int64)
+    np.savez_compressed(os.path.join(OUT, f"ref_golden_{bd}bit.npz"), **g)
+    print("wrote", os.path.join(OUT, f"ref_golden_{bd}bit.npz"))
+
+
+if __name__ == "__main__":
+    for bd in (8, 10):
+        make(bd)
