@@ -1,0 +1,430 @@
+"""Benchmark: 1080p VVC hot path (ME + TQ) on one GB300, batched frame form.
+
+A step is one picture of the 1920x1080 8-bit 4:2:0 single-stream workload
+through the whole hot path: exhaustive +-64 integer search for every CU of the
+64/32/16/8 quadtree levels, full sub-pel search, luma + chroma motion
+compensation, DCT2 / quant / dequant / inverse DCT2 / reconstruction of every
+CU (the reference previous picture resident on the GPU, low-delay P).
+
+  value   Mpixel/s with the pictures already in HBM (device-resident stream),
+          device time of K steps measured with CUDA events, L2 flushed between
+          steps (a 512 MB write outside the timed events)
+  e2e     the same through the public C ABI with host buffers: picture H2D and
+          CU results + coefficient planes D2H inside the timed region
+  roofline  of the dominant kernel (integer search): absolute differences per
+          second against this GPU's measured vabsdiff4+dp4a throughput
+  cpu_baseline  the oracle (C restatement of the reference path) on a sample of
+          CTUs on the host cores
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H = 1920, 1080
+SEARCH = 64
+LEVELS = (64, 32, 16, 8)
+QPS = (27, 32, 37)
+LAMBDA = {27: 45, 32: 64, 37: 91}      # sad lambda per QP (fixed table for the synthetic run)
+NFRAMES = 30
+SEED = 1080
+
+
+def workload_config():
+    return {"workload": "1080p single stream, 8-bit 4:2:0, low-delay P with the previous picture as reference, "
+                        "exhaustive +-64 integer search + full sub-pel search, CU levels 64/32/16/8, DCT2 TU=CU, "
+                        "QP 27/32/37 cycling, 30 synthetic pictures (seeded texture + 4 moving rectangles)",
+            "width": W, "height": H, "search_range": SEARCH, "levels": list(LEVELS), "frames": NFRAMES,
+            "l2": "flushed between steps (512 MB write outside the timed events)"}
+
+
+def make_frames(n=NFRAMES):
+    from xin26x_gb300 import synth
+    return synth.sequence(W, H, n, seed=SEED, objects=4)
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU legs
+def cpu_sample(frames, seconds_target=15.0, threads=1):
+    """Time the oracle's per-CU hot path on a sample of CTUs (all four levels of each
+    CTU) and return Mpixel/s of luma, extrapolated per CTU area."""
+    from oracle import oracle as O
+    from tests import oracle_frame
+    from xin26x_gb300.frame import CU_DTYPE  # noqa: F401
+
+    cur, ref = frames[1], frames[0]
+    o = O.oracle(8)
+    ctus = [(x, y) for y in range(0, H - 63, 64) for x in range(0, W - 63, 64)]
+    rng = np.random.default_rng(5)
+    order = rng.permutation(len(ctus))
+    levels = []
+    first = 0
+    for s in LEVELS:
+        levels.append((s, first, W // s, H // s))
+        first += (W // s) * (H // s)
+
+    def cus_of_ctu(cx, cy):
+        out = []
+        for (s, f, nx, ny) in levels:
+            for yy in range(cy, cy + 64, s):
+                for xx in range(cx, cx + 64, s):
+                    out.append(f + (yy // s) * nx + xx // s)
+        return out
+
+    done = 0
+    t0 = time.perf_counter()
+    lock = threading.Lock()
+    idx = [0]
+
+    def worker():
+        nonlocal done
+        while True:
+            with lock:
+                if time.perf_counter() - t0 > seconds_target or idx[0] >= len(order):
+                    return
+                k = order[idx[0]]
+                idx[0] += 1
+            cx, cy = ctus[k]
+            oracle_frame.run(cur, ref, levels, search_range=SEARCH, qp=32, uv_qp=32, sad_lambda=LAMBDA[32],
+                             cus=cus_of_ctu(cx, cy))
+            with lock:
+                done += 1
+
+    ths = [threading.Thread(target=worker) for _ in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    el = time.perf_counter() - t0
+    mpx = done * 64 * 64 / el / 1e6
+    del o
+    return mpx, done, el
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    frames = make_frames(2)
+    cores = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, n, el = cpu_sample(frames, seconds_target=4.0 if i >= args.warmup else 1.0, threads=cores)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.mean(vals))
+    line = {"metric": "1080p VVC ME+TQ Mpixel/s", "value": value, "unit": "Mpixel/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": workload_config(),
+            "cpu_baseline": {"value": value, "unit": "Mpixel/s", "cores": cores, "kind": "port",
+                             "sample": "each step: as many 64x64 CTUs (all four CU levels, +-64 exhaustive search) as "
+                                       "finish in ~4 s on all host threads, oracle C restatement"},
+            "e2e": {"value": value, "unit": "Mpixel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU legs
+def run_gpu(args):
+    import torch  # device memory for the resident pictures and the L2 flush buffer
+    from xin26x_gb300 import _lib
+    from xin26x_gb300.frame import FrameStream
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    lib = _lib.load(8)
+    assert lib.xin_gpu_init(local) == 0
+    frames = make_frames()
+    npix = W * H
+
+    # resident pictures for the device-timed leg
+    dev = []
+    for (y, u, v) in frames:
+        dev.append(tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in (y, u, v)))
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    cfg = _lib.xin_gpu_stream_cfg(W, H, 64, SEARCH, sum(LEVELS), 0, 1, 1)
+    h = C.c_void_p()
+    assert lib.xin_gpu_stream_open(C.byref(cfg), C.byref(h)) == 0, lib.xin_gpu_last_error()
+
+    def submit_dev(k):
+        pic = _lib.xin_gpu_picture()
+        y, u, v = dev[k % len(dev)]
+        for i, t in enumerate((y, u, v)):
+            pic.plane[i] = t.data_ptr()
+            pic.stride[i] = t.shape[1]
+        qp = QPS[k % 3]
+        pic.qp, pic.uv_qp, pic.sad_lambda = qp, qp, LAMBDA[qp]
+        assert lib.xin_gpu_frame_submit(h, C.byref(pic)) == 0, lib.xin_gpu_last_error()
+
+    res = _lib.xin_gpu_results()
+    submit_dev(0)
+    lib.xin_gpu_frame_wait(h, C.byref(res), -1)
+    for k in range(1, args.warmup + 1):
+        submit_dev(k)
+        lib.xin_gpu_frame_wait(h, C.byref(res), -1)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler()
+    clocks.start()
+    launches0 = lib.xin_gpu_kernel_launches()
+    step_ms, stage = [], np.zeros(4)
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.fill_(k & 255)                       # evict L2 (outside the timed events)
+        torch.cuda.synchronize()
+        submit_dev(args.warmup + 1 + k)
+        assert lib.xin_gpu_frame_wait(h, C.byref(res), -1) == 0
+        step_ms.append(res.gpu_ms)
+        st = (C.c_float * 4)()
+        lib.xin_gpu_stream_stage_ms(h, st)
+        stage += np.array(list(st))
+    torch.cuda.synchronize()
+    launches = lib.xin_gpu_kernel_launches() - launches0
+    clk = clocks.stop()
+    total_ms = float(np.sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = npix * args.steps * world / (total_ms * 1e-3) / 1e6
+    stage /= args.steps
+
+    # roofline of the integer search kernel
+    peak = C.c_double()
+    lib.xin_gpu_measure_sad_peak(C.byref(peak))
+    algo = (W // 8) * (H // 8) * (2 * SEARCH + 1) ** 2 * 64      # abs differences per launch (8x8 SADs)
+    me_ms = stage[1]
+    achieved = algo / (me_ms * 1e-3)
+    lib.xin_gpu_stream_close(h)
+
+    # e2e through the public API with host buffers
+    e2e_fs = FrameStream(W, H, search_range=SEARCH, levels=LEVELS, out_q=True, out_rec=False, use_graph=True)
+    cu_bytes = e2e_fs.ncus * 64
+    q_bytes = sum((W * H if p == 0 else W * H // 4) * len(LEVELS) * 2 for p in range(3))
+    e2e_fs.submit(*frames[0], qp=32, uv_qp=32, sad_lambda=LAMBDA[32])
+    e2e_fs.wait()
+    lat = []
+    for k in range(1, args.warmup + 1):
+        e2e_fs.submit(*frames[k], qp=QPS[k % 3], uv_qp=QPS[k % 3], sad_lambda=LAMBDA[QPS[k % 3]])
+        e2e_fs.wait(copy=False)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        f = frames[(args.warmup + 1 + k) % len(frames)]
+        qp = QPS[k % 3]
+        ts = time.perf_counter()
+        e2e_fs.submit(*f, qp=qp, uv_qp=qp, sad_lambda=LAMBDA[qp])
+        e2e_fs.wait(copy=False)
+        lat.append((time.perf_counter() - ts) * 1e3)
+    e2e_s = time.perf_counter() - t0
+    e2e_fs.close()
+    e2e_val = npix * args.steps * world / e2e_s / 1e6
+
+    # plain per-call form on a sample of CUs (one synchronous launch per reference call)
+    percall = percall_sample(lib, frames)
+
+    out = None
+    if rank == 0:
+        cpu = None
+        if world == 1:
+            v, n, el = cpu_sample(frames[:2], seconds_target=12.0, threads=1)
+            cpu = {"value": v, "unit": "Mpixel/s", "cores": 1, "kind": "port",
+                   "sample": f"{n} random 64x64 CTUs (all four CU levels, +-64 exhaustive search), oracle C restatement, "
+                             f"1 thread, {el:.1f} s"}
+        out = {"metric": "1080p VVC ME+TQ Mpixel/s", "value": value, "unit": "Mpixel/s", "n_gpus": world,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+               "data": "synthetic (seeded texture + 4 moving rectangles, 1920x1080 4:2:0)",
+               "config": workload_config(),
+               "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_mc_tq": stage[2], "copies": stage[3]},
+               "roofline": {"bound": "int", "kernel": "k_me_tiles", "achieved": achieved / 1e12, "peak": peak.value / 1e12,
+                            "unit": "Tabsdiff/s", "frac": achieved / peak.value, "traffic": None,
+                            "peak_source": "xin_gpu_measure_sad_peak: vabsdiff4+dp4a register loop on this GPU, this run",
+                            "algorithmic": f"(W/8)(H/8)(2R+1)^2*64 = {algo:.4g} abs differences per launch"},
+               "e2e": {"value": e2e_val, "unit": "Mpixel/s", "h2d_bytes_per_step": W * H * 3 // 2,
+                       "d2h_bytes_per_step": cu_bytes + q_bytes,
+                       "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}},
+               "percall": percall,
+               "gpu_launches": int(launches),
+               "clocks": clk,
+               "cpu_baseline": cpu}
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def quant_params(qp, lg):
+    """Square-TU DCT2 quant parameters, 8-bit, P picture, no RDOQ (h266_trans_quant.c:107-120)."""
+    qm = (26214, 23302, 20560, 18396, 16384, 14564)[qp % 6]
+    iqm = (40, 45, 51, 57, 64, 72)[qp % 6] << (qp // 6)
+    qs = 14 + 7 + qp // 6 - lg
+    iqs = 6 - 7 + lg
+    return qm, 85 << (qs - 9), qs, iqm, 1 << (iqs - 1), iqs
+
+
+def percall_sample(lib, frames, seconds=6.0):
+    """Plain per-call GPU form: the same CU hot path as ~20 synchronous per-call
+    launches per CU (integer search, sub-pel search, luma and chroma MC, per plane
+    residual, DCT2, quant, inverse DCT2, reconstruction) on a sample of CUs;
+    Mpixel/s extrapolated per CU area."""
+    from xin26x_gb300 import _lib
+    from xin26x_gb300.synth import pad_plane
+    cur, ref = frames[1], frames[0]
+    pad = 80
+    refp = [pad_plane(ref[0], pad), pad_plane(ref[1], pad // 2), pad_plane(ref[2], pad // 2)]
+    rng = np.random.default_rng(3)
+    me = _lib.xin_gpu_me_struct()
+    pix = 0
+    ncu = 0
+    calls = 0
+    t0 = time.perf_counter()
+    P = lambda a, off=0: a.ctypes.data + off * a.itemsize  # noqa: E731
+    while time.perf_counter() - t0 < seconds:
+        s = int(rng.choice(LEVELS, p=[0.1, 0.2, 0.3, 0.4]))
+        cx = int(rng.integers(0, W // s)) * s
+        cy = int(rng.integers(0, H // s)) * s
+        inp = np.ascontiguousarray(cur[0][cy:cy + s, cx:cx + s])
+        me.width = me.height = s
+        me.input, me.inputStride = inp.ctypes.data, s
+        me.ref, me.refStride = P(refp[0], (pad + cy) * refp[0].shape[1] + pad + cx), refp[0].shape[1]
+        me.searchWidth = me.searchHeight = SEARCH
+        me.predMv.mvX = me.predMv.mvY = 0
+        me.bestMv.mvX = me.bestMv.mvY = 0
+        me.bestCost = 0xFFFFFFFF
+        me.minMv.mvX, me.minMv.mvY = -cx - 72, -cy - 72
+        me.maxMv.mvX, me.maxMv.mvY = W + 72 - s - cx, H + 72 - s - cy
+        me.sadLambda = LAMBDA[32]
+        lib.XinGpuMotionEstFull(C.byref(me))
+        lib.XinGpuFullSubPelMe(C.byref(me))
+        calls += 2
+        mvx, mvy = me.bestMv.mvX * 4, me.bestMv.mvY * 4
+        pred = np.zeros((s, s), np.uint8)
+        ox, oy = cx * 16 + mvx, cy * 16 + mvy
+        frac = ((oy & 15) << 4) | (ox & 15)
+        src = P(refp[0], (pad + (oy >> 4)) * refp[0].shape[1] + pad + (ox >> 4))
+        fn = [lib.XinGpuInterpCopy, lib.XinGpuLumaInterpHor, lib.XinGpuLumaInterpVet, lib.XinGpuLumaInterpHorVet][
+            (1 if frac & 15 else 0) + (2 if frac >> 4 else 0)]
+        fn(src, refp[0].shape[1], pred.ctypes.data, s, frac, s, s, 0)
+        calls += 1
+        coef = np.zeros((s, s), np.int16)
+        t = np.zeros((s, s), np.int16)
+        q = np.zeros((s, s), np.int16)
+        r = np.zeros((s, s), np.int16)
+        rec = np.zeros((s, s), np.uint8)
+        nz = np.zeros(1, np.uint64)
+        for p in range(3):
+            bs = s if p == 0 else s // 2
+            if p:
+                pc = np.zeros((bs, bs), np.uint8)
+                cfx, cfy = (cx * 16 + mvx) & 31, (cy * 16 + mvy) & 31
+                csrc = P(refp[p], (pad // 2 + ((cy * 16 + mvy) >> 5)) * refp[p].shape[1] + pad // 2 + ((cx * 16 + mvx) >> 5))
+                lib.XinGpuChromaInterpHorVet(csrc, refp[p].shape[1], pc.ctypes.data, bs, (cfy << 5) | cfx, bs, bs, 0)
+                pr, org = pc, np.ascontiguousarray(cur[p][cy // 2:cy // 2 + bs, cx // 2:cx // 2 + bs])
+                calls += 1
+            else:
+                pr, org = pred, inp
+            lg = bs.bit_length() - 1
+            lib.XinGpuBlockSubForDct(org.ctypes.data, bs, pr.ctypes.data, bs, coef.ctypes.data, bs, bs, bs)
+            lib.XinGpuFDct2WxH(coef.ctypes.data, bs, t.ctypes.data, bs, bs, bs, None, lg - 1, lg + 6)
+            k = min(bs, 32)
+            qm, qa, qs, iqm, iqa, iqs = quant_params(32, lg)
+            lib.XinGpuQuantInvQuant(q.ctypes.data, t.ctypes.data, r.ctypes.data, bs, k, k, 4, 4, qm, qa, qs, iqm, iqa, iqs,
+                                    nz.ctypes.data)
+            lib.XinGpuIDct2WxH(r.ctypes.data, bs, coef.ctypes.data, bs, bs, bs, None, 7, 12)
+            lib.XinGpuBlockAddForDct(coef.ctypes.data, bs, pr.ctypes.data, bs, rec.ctypes.data, bs, bs, bs)
+            calls += 5
+        _lib.check(lib, "per-call sample")
+        pix += s * s
+        ncu += 1
+    el = time.perf_counter() - t0
+    return {"value": pix / el / 1e6, "unit": "Mpixel/s", "cus": ncu, "calls": calls, "seconds": el,
+            "sample": "random CUs of the four levels (10/20/30/40 % of 64/32/16/8), ~20 synchronous C-ABI calls each"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,292 @@
+/*
+ * xingpu.h -- C ABI of libxingpu: the xin26x VVC encoder pixel hot path on a
+ * GB300 GPU (sm_103a).
+ *
+ * Three layers, all plain C with host pointers and sizes:
+ *
+ *  1. Per-call functions ("plain per-call GPU form").  Each has exactly the
+ *     signature of the reference function-pointer type it replaces, so it can
+ *     be stored in the reference's tables xin_func_struct
+ *     (h266_encoder/include/h266_func_struct.h:719-799) and xin_me_func
+ *     (h26x_core/include/h26x_me_func_struct.h:174-191).  Arguments are host
+ *     pointers; every call copies its inputs to the GPU, runs one kernel, copies
+ *     the outputs back and synchronises.  The reference types return void and
+ *     have no error channel, so failures are reported through
+ *     xin_gpu_last_status() / xin_gpu_last_error() (per calling thread) and the
+ *     outputs are left untouched.  Calls are re-entrant: each host thread gets
+ *     its own CUDA stream and staging buffers.
+ *
+ *  2. Motion-estimation drivers taking the reference's xin_me_struct
+ *     (h26x_core/include/h26x_me_struct.h:60-131, mirrored in xingpu_me.h).
+ *
+ *  3. The batched frame form: a stream handle keeps reference pictures, padded
+ *     planes, quarter-pel planes and outputs resident on the GPU and runs the
+ *     whole hot path of a picture (integer search, sub-pel search, motion
+ *     compensation, transform, quantisation, reconstruction for every CU of
+ *     every quadtree level) as a few launches captured in a CUDA graph.
+ *
+ * PIXEL / COEFF follow the reference's compile switch ENABLE_10BIT_ENCODER
+ * (video_api/video_common/include/xin_typedef.h:72-96): libxingpu8.so is the
+ * 8-bit build, libxingpu10.so the 10-bit build.
+ *
+ * Status codes mirror XIN_SUCCESS / XIN_FAIL (xin_typedef.h:36-37): 0 is
+ * success, negative values are errors.
+ */
+#ifndef XINGPU_H
+#define XINGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifdef ENABLE_10BIT_ENCODER
+typedef uint16_t XG_PIXEL;
+typedef int32_t  XG_COEFF;
+#else
+typedef uint8_t  XG_PIXEL;
+typedef int16_t  XG_COEFF;
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define XIN_GPU_OK            0
+#define XIN_GPU_FAIL         -1   /* generic failure (XIN_FAIL) */
+#define XIN_GPU_ERR_ARG      -2   /* invalid argument (size, stride, pointer) */
+#define XIN_GPU_ERR_CUDA     -3   /* CUDA runtime error; message in xin_gpu_last_error() */
+#define XIN_GPU_ERR_NOMEM    -4   /* device or pinned allocation failed */
+#define XIN_GPU_ERR_TIMEOUT  -5   /* wait limit reached */
+#define XIN_GPU_ERR_STATE    -6   /* call not valid in the current state */
+#define XIN_GPU_ERR_ADMIT    -7   /* serving: not enough device memory to admit */
+
+int         xin_gpu_init(int device);          /* select the CUDA device; idempotent */
+int         xin_gpu_bitdepth(void);            /* 8 or 10: the build of this library */
+int         xin_gpu_last_status(void);         /* status of this thread's last call */
+const char *xin_gpu_last_error(void);          /* message of this thread's last failure */
+void        xin_gpu_clear_error(void);
+uint64_t    xin_gpu_kernel_launches(void);     /* kernels launched by this library so far */
+
+/* ------------------------------------------------------ distortion (a2-a6)
+ * replaces Xin26xComputeSad / Sadx8 / Sadx5 / Sadx3 / AvgSad / AvgSadx8 /
+ * Satd / AvgSatd / WeightSad / WeightSatd / Var / AvgVar / ComputeHada8x8
+ * (h26x_core/include/h26x_compute_dist.h:27-1096); typedefs XinComputeDist,
+ * XinComputeAvgDist, XinComputeWeightDist, XinComputeSadx8/x5/x3,
+ * XinComputeAvgSadx8, XinComputeHada8x8 (h266_func_struct.h:56-128,459). */
+void XinGpuComputeSad(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *pred, intptr_t predStride,
+                      uint32_t width, uint32_t height, uint32_t *sad);
+void XinGpuComputeSatd(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *pred, intptr_t predStride,
+                       uint32_t width, uint32_t height, uint32_t *satd);
+void XinGpuComputeAvgSad(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *refA, XG_PIXEL *refB, intptr_t refStride,
+                         uint32_t width, uint32_t height, uint32_t *sad);
+void XinGpuComputeAvgSatd(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *refA, XG_PIXEL *refB, intptr_t refStride,
+                          uint32_t width, uint32_t height, uint32_t *satd);
+void XinGpuComputeWeightSad(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *refA, XG_PIXEL *refB, intptr_t refStride,
+                            uint32_t width, uint32_t height, int32_t weightA, int32_t weightB, uint32_t *sad);
+void XinGpuComputeWeightSatd(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *refA, XG_PIXEL *refB, intptr_t refStride,
+                             uint32_t width, uint32_t height, int32_t weightA, int32_t weightB, uint32_t *satd);
+void XinGpuComputeSadx8(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *ref[8], intptr_t refStride,
+                        uint32_t width, uint32_t height, uint32_t *sad);
+void XinGpuComputeSadx5(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *ref0, XG_PIXEL *ref1, XG_PIXEL *ref2,
+                        XG_PIXEL *ref3, XG_PIXEL *ref4, intptr_t refStride, uint32_t width, uint32_t height, uint32_t *sad);
+void XinGpuComputeSadx3(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *ref0, XG_PIXEL *ref1, XG_PIXEL *ref2,
+                        intptr_t refStride, uint32_t width, uint32_t height, uint32_t *sad);
+void XinGpuComputeAvgSadx8(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *refA[8], XG_PIXEL *refB[8],
+                           intptr_t refStride, uint32_t width, uint32_t height, uint32_t *sad);
+void XinGpuComputeVar(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *pred, intptr_t predStride,
+                      uint32_t width, uint32_t height, uint32_t *var);
+void XinGpuComputeAvgVar(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *predA, XG_PIXEL *predB, intptr_t predStride,
+                         uint32_t width, uint32_t height, uint32_t *var);
+void XinGpuComputeHada8x8(XG_PIXEL *input, intptr_t inputStride, uint32_t *satd);
+
+/* ----------------------------------------------- interpolation (a10-a12)
+ * replaces Xin266InterpCopy, Xin266LumaInterpHor/Vet/HorVet and the U8S16 /
+ * S16U8 / S16S16 stages (h266_core/source/h266_luma_mc.c:72-630),
+ * Xin266ChromaInterp* (h266_core/source/h266_chroma_mc.c:62-386),
+ * Xin266InterpAvgS16U8 / Xin266InterpWeightS16U8 (h266_luma_mc.c:561,595);
+ * typedefs XinMotionInterp, XinMotionInterpS16, XinMotionInterpAvg,
+ * XinMotionInterpWeight (h266_func_struct.h:130-179).  Luma frac = fy << 4 | fx
+ * (1/16 pel), chroma frac = fy << 5 | fx (1/32 pel); filterIndex 0 default,
+ * 1 alternative half-pel, 2 affine 4x4. */
+#define XG_INTERP_ARGS(SRC_T, DST_T) const SRC_T *src, intptr_t srcStride, DST_T *dst, intptr_t dstStride, \
+                                     int32_t frac, uint32_t width, uint32_t height, uint32_t filterIndex
+void XinGpuInterpCopy(XG_INTERP_ARGS(XG_PIXEL, XG_PIXEL));
+void XinGpuInterpCopyU8S16(XG_INTERP_ARGS(XG_PIXEL, int16_t));
+void XinGpuLumaInterpHor(XG_INTERP_ARGS(XG_PIXEL, XG_PIXEL));
+void XinGpuLumaInterpVet(XG_INTERP_ARGS(XG_PIXEL, XG_PIXEL));
+void XinGpuLumaInterpHorVet(XG_INTERP_ARGS(XG_PIXEL, XG_PIXEL));
+void XinGpuLumaInterpHorU8S16(XG_INTERP_ARGS(XG_PIXEL, int16_t));
+void XinGpuLumaInterpVetU8S16(XG_INTERP_ARGS(XG_PIXEL, int16_t));
+void XinGpuLumaInterpHorVetU8S16(XG_INTERP_ARGS(XG_PIXEL, int16_t));
+void XinGpuLumaInterpVetS16U8(XG_INTERP_ARGS(int16_t, XG_PIXEL));
+void XinGpuLumaInterpVetS16S16(XG_INTERP_ARGS(int16_t, int16_t));
+void XinGpuChromaInterpHor(XG_INTERP_ARGS(XG_PIXEL, XG_PIXEL));
+void XinGpuChromaInterpVet(XG_INTERP_ARGS(XG_PIXEL, XG_PIXEL));
+void XinGpuChromaInterpHorVet(XG_INTERP_ARGS(XG_PIXEL, XG_PIXEL));
+void XinGpuChromaInterpHorU8S16(XG_INTERP_ARGS(XG_PIXEL, int16_t));
+void XinGpuChromaInterpVetU8S16(XG_INTERP_ARGS(XG_PIXEL, int16_t));
+void XinGpuChromaInterpHorVetU8S16(XG_INTERP_ARGS(XG_PIXEL, int16_t));
+void XinGpuChromaInterpVetS16U8(XG_INTERP_ARGS(int16_t, XG_PIXEL));
+void XinGpuChromaInterpVetS16S16(XG_INTERP_ARGS(int16_t, int16_t));
+void XinGpuInterpAvgS16U8(const int16_t *src0, intptr_t src0Stride, const int16_t *src1, intptr_t src1Stride,
+                          XG_PIXEL *dst, intptr_t dstStride, uint32_t width, uint32_t height);
+void XinGpuInterpWeightS16U8(const int16_t *src0, intptr_t src0Stride, const int16_t *src1, intptr_t src1Stride,
+                             XG_PIXEL *dst, intptr_t dstStride, uint32_t width, uint32_t height,
+                             int32_t weightA, int32_t weightB);
+
+/* ------------------------------------------------------- transforms (a14-a19)
+ * 1-D forward: replaces Xin26xFDct2P2..P64, Xin26xFDst7P4..P32, Xin26xFDct8P4..P32
+ * (h26x_core/include/h26x_forward_1d_trans.h), typedef XinFor1dDct
+ * (h266_func_struct.h:198).  1-D inverse: replaces Xin26xIDct2P2..P64,
+ * Xin26xIDst7P4..P32, Xin26xIDct8P4..P32 (h26x_core/include/h26x_inverse_1d_trans.h),
+ * typedef XinInv1dDct (h266_func_struct.h:280). */
+#define XG_FDCT1D(NAME) void NAME(XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, intptr_t outputStride, \
+                                  int32_t line, int32_t shift)
+#define XG_IDCT1D(NAME) void NAME(XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, intptr_t outputStride, \
+                                  int32_t line, int32_t skipLine, int32_t shift)
+XG_FDCT1D(XinGpuFDct2P2); XG_FDCT1D(XinGpuFDct2P4); XG_FDCT1D(XinGpuFDct2P8); XG_FDCT1D(XinGpuFDct2P16);
+XG_FDCT1D(XinGpuFDct2P32); XG_FDCT1D(XinGpuFDct2P64);
+XG_FDCT1D(XinGpuFDst7P4); XG_FDCT1D(XinGpuFDst7P8); XG_FDCT1D(XinGpuFDst7P16); XG_FDCT1D(XinGpuFDst7P32);
+XG_FDCT1D(XinGpuFDct8P4); XG_FDCT1D(XinGpuFDct8P8); XG_FDCT1D(XinGpuFDct8P16); XG_FDCT1D(XinGpuFDct8P32);
+XG_IDCT1D(XinGpuIDct2P2); XG_IDCT1D(XinGpuIDct2P4); XG_IDCT1D(XinGpuIDct2P8); XG_IDCT1D(XinGpuIDct2P16);
+XG_IDCT1D(XinGpuIDct2P32); XG_IDCT1D(XinGpuIDct2P64);
+XG_IDCT1D(XinGpuIDst7P4); XG_IDCT1D(XinGpuIDst7P8); XG_IDCT1D(XinGpuIDst7P16); XG_IDCT1D(XinGpuIDst7P32);
+XG_IDCT1D(XinGpuIDct8P4); XG_IDCT1D(XinGpuIDct8P8); XG_IDCT1D(XinGpuIDct8P16); XG_IDCT1D(XinGpuIDct8P32);
+
+/* 2-D DCT2: replaces Xin26xFDct2WxH (XinFor2dDct2, h266_func_struct.h:206) and
+ * Xin266IDct2WxH (XinInv2dDct2, :269; h266_encoder/source/h266_inverse_trans.c:52).
+ * tempBuf is accepted for signature compatibility and not used. */
+void XinGpuFDct2WxH(XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, intptr_t outputStride,
+                    uint32_t width, uint32_t height, XG_COEFF *tempBuf, int32_t shift1st, int32_t shift2nd);
+void XinGpuIDct2WxH(XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, intptr_t outputStride,
+                    uint32_t width, uint32_t height, XG_COEFF *tempBuf, int32_t shift1st, int32_t shift2nd);
+/* transform skip: replaces Xin26xFSkipWxH (XinFor2dSkip, :217) and Xin266ISkipWxH
+ * (XinInv2dSkip, :635; h266_inverse_trans.c:91) */
+void XinGpuFSkipWxH(XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, intptr_t outputStride,
+                    uint32_t width, uint32_t height, XG_COEFF *tempBuf);
+void XinGpuISkipWxH(XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, intptr_t outputStride,
+                    uint32_t width, uint32_t height);
+/* residual / reconstruction: replaces Xin26xBlockSubForDct (XinBlockSubForDct, :520) and
+ * Xin26xBlockRecon (XinBlockAddForDct, :530) */
+void XinGpuBlockSubForDct(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *recon, intptr_t reconStride,
+                          XG_COEFF *diff, intptr_t diffStride, uint32_t width, uint32_t height);
+void XinGpuBlockAddForDct(XG_COEFF *input, intptr_t inputStride, XG_PIXEL *pred, intptr_t predStride,
+                          XG_PIXEL *recon, intptr_t reconStride, uint32_t width, uint32_t height);
+
+/* ----------------------------------------------------------- quant (a16-a17)
+ * replaces Xin266QuantInvQuant (XinQuantInvQuant, h266_func_struct.h:181;
+ * h266_encoder/source/h266_quant_inv_quant.c:80) and Xin266PreRdoq (XinPreRdoq,
+ * :622; h266_quant_inv_quant.c:208).  xin_gpu_scan_pos has the layout of
+ * xin_scan_pos (h266_encoder/include/h266_trans_unit_struct.h:23-28). */
+typedef struct xin_gpu_scan_pos { uint32_t posX, posY, posIdx; } xin_gpu_scan_pos;
+void XinGpuQuantInvQuant(XG_COEFF *qCoeff, XG_COEFF *tCoeff, XG_COEFF *rCoeff, intptr_t coeffStride,
+                         uint32_t width, uint32_t height, uint32_t cGWidth, uint32_t cGHeight,
+                         int32_t qMult, int32_t qAdd, int32_t qShift, int32_t iqMult, int32_t iqAdd, int32_t iqShift,
+                         uint64_t *nzCGBitMapRs);
+void XinGpuPreRdoq(XG_COEFF *tCoeff, XG_COEFF *rCoeff, XG_COEFF *qCoeff, intptr_t coeffStride,
+                   uint32_t width, uint32_t height, uint32_t cGWidth, uint32_t cGHeight, int32_t rdoqThrVal,
+                   xin_gpu_scan_pos *scanOrderCG, uint64_t *nzCGBitMapRs);
+
+/* ------------------------------------------------------- motion search (a7-a8)
+ * xin_me_struct is the reference's ME state (h26x_core/include/h26x_me_struct.h:60-131);
+ * xingpu_me.h mirrors its layout.  Pass a pointer to the reference's struct.
+ *
+ * XinGpuMotionEstFull: stands in for Xin26xMotionEstFull (h26x_motion_est.h:23-36):
+ *   exhaustive integer search of every MV within searchWidth x searchHeight of
+ *   predMv >> 2, clipped to [minMv, maxMv], raster order, strict '<' on
+ *   (SAD << 8) + (bits(mvd_x) + bits(mvd_y)) * sadLambda; starts from bestMv /
+ *   bestCost; writes bestMv (quarter-pel), bestCost, bestSad.
+ * XinGpuFullSubPelMe: the search of Xin266FullSubPelMe
+ *   (h266_encoder/source/h266_sub_pel_refine.c:81), reading its inputs from the
+ *   ME state instead of the section state. */
+struct xin_me_struct;
+void XinGpuMotionEstFull(struct xin_me_struct *meSet);
+void XinGpuFullSubPelMe(struct xin_me_struct *meSet);
+
+/* ------------------------------------------------------------- frame form
+ * One stream = one sequence.  Pictures are submitted in coding order; each
+ * picture after the first uses the previously submitted picture as its
+ * reference (low-delay P, one reference), which stays resident on the GPU
+ * together with its padded planes and its 15 quarter-pel luma planes.
+ *
+ * For every quadtree level in level_mask (bit s set = s x s CUs, s in
+ * {8,16,32,64}) and every s x s CU that lies inside the picture, in raster
+ * order per level, the frame pipeline computes:
+ *   window  [minMv, maxMv] from the padding (h266_encoder/source/h266_enc_init.c:1462)
+ *   integer exhaustive search around MV 0 (as XinGpuMotionEstFull, predictor 0)
+ *   Xin266FullSubPelMe refinement
+ *   luma MC (Xin266LumaInterPred) and chroma MC (uni branch of Xin266ChromaMotionComp)
+ *   per plane: residual, DCT2 (TU = CU), quant/dequant with 4x4 CGs (no RDOQ,
+ *   qAdd = 85 << (qShift - 9) for P), inverse DCT2, reconstruction, SSD
+ * Outputs per CU: mv (quarter-pel), cost after sub-pel, integer cost,
+ * non-zero-CG map and SSD per plane; per level and plane: quantised
+ * coefficient plane and reconstructed plane (picture layout). */
+typedef struct xin_gpu_stream xin_gpu_stream;
+
+#define XIN_GPU_OUT_Q     1u   /* copy the quantised coefficient planes back */
+#define XIN_GPU_OUT_REC   2u   /* copy the reconstructed planes back */
+
+typedef struct xin_gpu_stream_cfg {
+    int32_t  width, height;      /* luma size, even */
+    int32_t  ctu_size;           /* 64 or 128: reference padding = ctu_size + 16 */
+    int32_t  search_range;       /* integer search radius, 1..256 */
+    uint32_t level_mask;         /* bit s (8,16,32,64) set = evaluate s x s CUs */
+    uint32_t out_flags;          /* XIN_GPU_OUT_* */
+    int32_t  use_graph;          /* 1: capture the per-picture launches in a CUDA graph */
+    int32_t  device_io;          /* 1: picture planes are device pointers and results stay on the
+                                    device (xin_gpu_stream_device_results); for callers whose
+                                    pictures already live in GPU memory */
+} xin_gpu_stream_cfg;
+
+typedef struct xin_gpu_picture {
+    const XG_PIXEL *plane[3];    /* host Y, U, V */
+    intptr_t stride[3];          /* elements */
+    int32_t  qp, uv_qp;          /* slice QPs */
+    uint32_t sad_lambda;
+} xin_gpu_picture;
+
+typedef struct xin_gpu_cu_result {
+    int32_t  mvx, mvy;           /* quarter-pel */
+    uint32_t cost;               /* after sub-pel */
+    uint32_t int_cost;           /* after the integer search */
+    uint64_t nz[3];
+    uint64_t ssd[3];
+} xin_gpu_cu_result;
+
+typedef struct xin_gpu_results {
+    xin_gpu_cu_result *cu;       /* [xin_gpu_stream_num_cus()], levels from 64 down to 8 */
+    XG_COEFF *q[3];              /* [levels][plane height][plane width] when XIN_GPU_OUT_Q */
+    XG_PIXEL *rec[3];            /* same layout when XIN_GPU_OUT_REC */
+    float    gpu_ms;             /* device time of the picture's launches */
+} xin_gpu_results;
+
+int  xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream **out);
+int  xin_gpu_stream_close(xin_gpu_stream *s);
+int  xin_gpu_stream_num_cus(const xin_gpu_stream *s);             /* CUs per picture over all levels */
+int  xin_gpu_stream_level_info(const xin_gpu_stream *s, int level, int32_t *size, int32_t *first_cu,
+                               int32_t *cus_x, int32_t *cus_y);      /* level 0 = largest size */
+int  xin_gpu_stream_num_levels(const xin_gpu_stream *s);
+/* Upload a picture and queue its hot path (asynchronous).  The first picture of
+ * a stream only becomes the reference (no CU results). */
+int  xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic);
+/* Wait for the last submitted picture (bounded by timeout_ms; < 0 waits without
+ * limit) and copy its results into the caller's buffers.  Members of res left
+ * NULL receive views of the stream's pinned result buffers instead, valid until
+ * the next frame_submit. */
+int  xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32_t timeout_ms);
+/* Device time of the stages of the last completed picture:
+ * ms[0] upload + padding + quarter-pel planes, ms[1] integer search,
+ * ms[2] sub-pel search + MC + transform/quant + reconstruction, ms[3] result copies. */
+int  xin_gpu_stream_stage_ms(const xin_gpu_stream *s, float ms[4]);
+/* Device pointers of the result arrays (same layouts as xin_gpu_results). */
+int  xin_gpu_stream_device_results(const xin_gpu_stream *s, void **cu, void *q[3], void *rec[3]);
+
+/* Measured throughput of this GPU's packed 8-bit SAD instruction pair
+ * (vabsdiff4 + dp4a) on register-resident data, in absolute differences per
+ * second: the ceiling of the integer search kernel, used as its roofline. */
+int  xin_gpu_measure_sad_peak(double *absdiff_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

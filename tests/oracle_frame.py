@@ -1,0 +1,52 @@
+"""Oracle of the batched frame form: runs oracle/xin_oracle.c's per-CU hot path
+(orc_cu_hotpath) over every CU of every level, in the library's output order.
+Test infrastructure only."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from oracle import oracle as O
+from xin26x_gb300.frame import CU_DTYPE
+from xin26x_gb300.synth import pad_plane
+
+
+def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=64, bitdepth=8, cus=None):
+    """cur, ref: (Y, U, V) planes.  levels: [(size, first, cus_x, cus_y)] as the stream reports.
+    cus: optional list of global CU indices to evaluate (others left zero).
+    Returns (cu records, q planes [levels,h,w] x3, rec planes x3)."""
+    o = O.oracle(bitdepth)
+    h, w = cur[0].shape
+    pad = ctu + 16
+    refp = [pad_plane(ref[0], pad), pad_plane(ref[1], pad // 2), pad_plane(ref[2], pad // 2)]
+    curc = [np.ascontiguousarray(p) for p in cur]
+    f = O.orc_frame_desc()
+    f.width, f.height, f.ctu = w, h, ctu
+    for i in range(3):
+        f.in_[i] = curc[i].ctypes.data
+        pp = pad if i == 0 else pad // 2
+        f.ref[i] = refp[i].ctypes.data + (pp * refp[i].shape[1] + pp) * refp[i].itemsize
+    f.in_stride[0], f.in_stride[1] = w, w // 2
+    f.ref_stride[0], f.ref_stride[1] = refp[0].shape[1], refp[1].shape[1]
+    f.search_range, f.sad_lambda, f.qp, f.uv_qp, f.intra_frame = search_range, sad_lambda, qp, uv_qp, 0
+    ncu = sum(cx * cy for (_, _, cx, cy) in levels)
+    recs = np.zeros(ncu, CU_DTYPE)
+    nl = len(levels)
+    q = [np.zeros((nl, h, w), o.coef), np.zeros((nl, h // 2, w // 2), o.coef), np.zeros((nl, h // 2, w // 2), o.coef)]
+    rec = [np.zeros((nl, h, w), o.pix), np.zeros((nl, h // 2, w // 2), o.pix), np.zeros((nl, h // 2, w // 2), o.pix)]
+    want = None if cus is None else set(int(c) for c in cus)
+    for li, (size, first, cx, cy) in enumerate(levels):
+        qptr = (C.c_void_p * 3)(*[q[p][li].ctypes.data for p in range(3)])
+        rptr = (C.c_void_p * 3)(*[rec[p][li].ctypes.data for p in range(3)])
+        qs = (C.c_ssize_t * 2)(w, w // 2)
+        for j in range(cx * cy):
+            if want is not None and first + j not in want:
+                continue
+            out = O.orc_cu_out()
+            o.cu_hotpath(C.byref(f), (j % cx) * size, (j // cx) * size, size, qptr, qs, rptr, qs, C.byref(out))
+            r = recs[first + j]
+            r["mvx"], r["mvy"], r["cost"], r["int_cost"] = out.mvx, out.mvy, out.cost, out.int_cost
+            r["nz"] = list(out.nz)
+            r["ssd"] = list(out.ssd)
+    return recs, q, rec

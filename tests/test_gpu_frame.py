@@ -1,0 +1,89 @@
+"""Batched frame form (xin_gpu_stream_* through the C ABI, host buffers) against
+the oracle's per-CU hot path: every CU of every level -- integer search,
+sub-pel search, costs, non-zero maps, SSDs, coefficient planes and
+reconstructed planes -- bit-exact on seeded synthetic pictures."""
+import numpy as np
+import pytest
+
+from xin26x_gb300 import synth
+from xin26x_gb300.frame import FrameStream
+from tests import oracle_frame
+
+pytestmark = pytest.mark.gpu
+
+
+def _compare(out, ref, levels, label):
+    recs, q, rec = ref
+    cu = out["cu"]
+    for name in ("mvx", "mvy", "int_cost", "cost"):
+        bad = np.nonzero(cu[name] != recs[name])[0]
+        assert bad.size == 0, (label, name, bad[:5], cu[bad[:5]], recs[bad[:5]])
+    assert np.array_equal(cu["nz"], recs["nz"]), label
+    assert np.array_equal(cu["ssd"], recs["ssd"]), label
+    for p in range(3):
+        for li, (size, first, cx, cy) in enumerate(levels):
+            s = size if p == 0 else size // 2
+            hh, ww = cy * s, cx * s          # the area the level's CUs cover
+            assert np.array_equal(out["q"][p][li, :hh, :ww], q[p][li, :hh, :ww]), (label, "q", p, size)
+            assert np.array_equal(out["rec"][p][li, :hh, :ww], rec[p][li, :hh, :ww]), (label, "rec", p, size)
+
+
+@pytest.mark.parametrize("bd", (8, 10))
+@pytest.mark.parametrize("w,h,R,ctu", [(192, 128, 16, 64), (208, 120, 24, 64), (256, 136, 8, 128)])
+def test_frame_pipeline_matches_oracle(bd, w, h, R, ctu):
+    seq = synth.sequence(w, h, 3, seed=w + h + R, bitdepth=bd, objects=1)
+    fs = FrameStream(w, h, ctu=ctu, search_range=R, out_q=True, out_rec=True, bitdepth=bd)
+    try:
+        fs.submit(*seq[0], qp=32, uv_qp=32, sad_lambda=70)
+        fs.wait()
+        for k in (1, 2):
+            qp = 27 + 5 * k
+            fs.submit(*seq[k], qp=qp, uv_qp=qp + 1, sad_lambda=40 + 30 * k)
+            out = fs.wait()
+            ref = oracle_frame.run(seq[k], seq[k - 1], fs.levels, ctu=ctu, search_range=R, qp=qp, uv_qp=qp + 1,
+                                   sad_lambda=40 + 30 * k, bitdepth=bd)
+            _compare(out, ref, fs.levels, (bd, w, h, R, k))
+    finally:
+        fs.close()
+
+
+def test_frame_graph_and_direct_paths_agree():
+    w, h = 192, 128
+    seq = synth.sequence(w, h, 4, seed=3, objects=2)
+    outs = []
+    for graph in (True, False):
+        fs = FrameStream(w, h, search_range=32, out_q=True, out_rec=True, use_graph=graph)
+        res = []
+        for k in range(4):
+            fs.submit(*seq[k], qp=30 + k, uv_qp=31, sad_lambda=55)
+            r = fs.wait()
+            if k:
+                res.append(r)
+        fs.close()
+        outs.append(res)
+    for a, b in zip(*outs):
+        assert np.array_equal(a["cu"], b["cu"])
+        for p in range(3):
+            assert np.array_equal(a["q"][p], b["q"][p]) and np.array_equal(a["rec"][p], b["rec"][p])
+
+
+def test_frame_full_search_range_64():
+    """The benchmark's search range on a 416x240 picture (every level), checked on a CU sample."""
+    w, h, R = 416, 240, 64
+    seq = synth.sequence(w, h, 2, seed=11)
+    fs = FrameStream(w, h, search_range=R, out_q=True, out_rec=True)
+    fs.submit(*seq[0], qp=32, uv_qp=32, sad_lambda=64)
+    fs.wait()
+    fs.submit(*seq[1], qp=32, uv_qp=32, sad_lambda=64)
+    out = fs.wait()
+    rng = np.random.default_rng(0)
+    sample = []
+    for (size, first, cx, cy) in fs.levels:
+        n = cx * cy
+        sample += list(first + rng.choice(n, size=min(n, 12), replace=False))
+    recs, q, rec = oracle_frame.run(seq[1], seq[0], fs.levels, search_range=R, qp=32, uv_qp=32, sad_lambda=64, cus=sample)
+    fs.close()
+    for i in sample:
+        for name in ("mvx", "mvy", "int_cost", "cost"):
+            assert out["cu"][name][i] == recs[name][i], (i, name)
+        assert np.array_equal(out["cu"]["nz"][i], recs["nz"][i]) and np.array_equal(out["cu"]["ssd"][i], recs["ssd"][i])

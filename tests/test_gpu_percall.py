@@ -1,0 +1,321 @@
+"""Per-call GPU form (libxingpu XinGpu* entry points, host pointers through the
+C ABI) against the CPU oracle: bit-exact on seeded inputs, every size class,
+every interpolation phase family, every transform type and size."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+BDS = (8, 10)
+
+
+@pytest.fixture(scope="module", params=BDS)
+def libs(request):
+    from xin26x_gb300 import _lib
+    bd = request.param
+    g = _lib.load(bd)
+    assert g.xin_gpu_init(0) == 0, g.xin_gpu_last_error()
+    assert g.xin_gpu_bitdepth() == bd
+    return g, O.oracle(bd), bd
+
+
+def P(a, off=0):
+    return O.ptr(a, off)
+
+
+def _ok(g, what=""):
+    assert g.xin_gpu_last_status() == 0, (what, g.xin_gpu_last_error())
+
+
+SIZES = [(4, 4), (8, 8), (16, 16), (32, 32), (64, 64), (128, 128), (8, 4), (4, 16), (32, 8), (64, 16), (16, 128)]
+
+
+def test_distortion_family(libs):
+    g, o, bd = libs
+    rng = np.random.default_rng(1)
+    mx = (1 << bd) - 1
+    for w, h in SIZES:
+        stride = w + 7
+        inp = rng.integers(0, mx + 1, size=(h, stride)).astype(o.pix)
+        refs = [rng.integers(0, mx + 1, size=(h, stride + 3)).astype(o.pix) for _ in range(16)]
+        rs = stride + 3
+        a, b = np.zeros(8, np.uint32), np.zeros(8, np.uint32)
+        g.XinGpuComputeSad(P(inp), stride, P(refs[0]), rs, w, h, P(a)); _ok(g)
+        o.sad(P(inp), stride, P(refs[0]), rs, w, h, P(b))
+        assert a[0] == b[0], (w, h)
+        g.XinGpuComputeAvgSad(P(inp), stride, P(refs[0]), P(refs[1]), rs, w, h, P(a)); _ok(g)
+        o.avg_sad(P(inp), stride, P(refs[0]), P(refs[1]), rs, w, h, P(b))
+        assert a[0] == b[0]
+        for wa in (-2, 3, 5, 10):
+            g.XinGpuComputeWeightSad(P(inp), stride, P(refs[0]), P(refs[1]), rs, w, h, wa, 8 - wa, P(a)); _ok(g)
+            o.weight_sad(P(inp), stride, P(refs[0]), P(refs[1]), rs, w, h, wa, 8 - wa, P(b))
+            assert a[0] == b[0]
+        ptrs = (C.c_void_p * 8)(*[refs[i].ctypes.data for i in range(8)])
+        ptrsb = (C.c_void_p * 8)(*[refs[8 + i].ctypes.data for i in range(8)])
+        g.XinGpuComputeSadx8(P(inp), stride, ptrs, rs, w, h, P(a)); _ok(g)
+        o.sad_xn(P(inp), stride, ptrs, 8, rs, w, h, P(b))
+        assert np.array_equal(a, b)
+        g.XinGpuComputeSadx5(P(inp), stride, *[refs[i].ctypes.data for i in range(5)], rs, w, h, P(a)); _ok(g)
+        o.sad_xn(P(inp), stride, ptrs, 5, rs, w, h, P(b))
+        assert np.array_equal(a[:5], b[:5])
+        g.XinGpuComputeSadx3(P(inp), stride, *[refs[i].ctypes.data for i in range(3)], rs, w, h, P(a)); _ok(g)
+        o.sad_xn(P(inp), stride, ptrs, 3, rs, w, h, P(b))
+        assert np.array_equal(a[:3], b[:3])
+        g.XinGpuComputeAvgSadx8(P(inp), stride, ptrs, ptrsb, rs, w, h, P(a)); _ok(g)
+        o.avg_sad_xn(P(inp), stride, ptrs, ptrsb, 8, rs, w, h, P(b))
+        assert np.array_equal(a, b)
+        g.XinGpuComputeVar(P(inp), stride, P(refs[2]), rs, w, h, P(a)); _ok(g)
+        o.var(P(inp), stride, P(refs[2]), rs, w, h, P(b))
+        assert a[0] == b[0]
+        g.XinGpuComputeAvgVar(P(inp), stride, P(refs[2]), P(refs[3]), rs, w, h, P(a)); _ok(g)
+        o.avg_var(P(inp), stride, P(refs[2]), P(refs[3]), rs, w, h, P(b))
+        assert a[0] == b[0]
+        g.XinGpuComputeSatd(P(inp), stride, P(refs[4]), rs, w, h, P(a)); _ok(g)
+        o.satd(P(inp), stride, P(refs[4]), rs, w, h, P(b))
+        assert a[0] == b[0], (w, h)
+        g.XinGpuComputeAvgSatd(P(inp), stride, P(refs[4]), P(refs[5]), rs, w, h, P(a)); _ok(g)
+        o.avg_satd(P(inp), stride, P(refs[4]), P(refs[5]), rs, w, h, P(b))
+        assert a[0] == b[0]
+        g.XinGpuComputeWeightSatd(P(inp), stride, P(refs[4]), P(refs[5]), rs, w, h, 3, 5, P(a)); _ok(g)
+        o.weight_satd(P(inp), stride, P(refs[4]), P(refs[5]), rs, w, h, 3, 5, P(b))
+        assert a[0] == b[0]
+    blk = rng.integers(0, mx + 1, size=(8, 11)).astype(o.pix)
+    g.XinGpuComputeHada8x8(P(blk), 11, P(a)); _ok(g)
+    o.hada8x8(P(blk), 11, P(b))
+    assert a[0] == b[0]
+
+
+INTERP = [  # (gpu name, oracle name, taps, src s16, dst s16)
+    ("InterpCopy", "interp_copy", 8, False, False), ("InterpCopyU8S16", "interp_copy_s16", 8, False, True),
+    ("LumaInterpHor", "luma_hor", 8, False, False), ("LumaInterpVet", "luma_vet", 8, False, False),
+    ("LumaInterpHorVet", "luma_hv", 8, False, False), ("LumaInterpHorU8S16", "luma_hor_s16", 8, False, True),
+    ("LumaInterpVetU8S16", "luma_vet_s16", 8, False, True), ("LumaInterpHorVetU8S16", "luma_hv_s16", 8, False, True),
+    ("LumaInterpVetS16U8", "luma_vet_s16_pix", 8, True, False), ("LumaInterpVetS16S16", "luma_vet_s16_s16", 8, True, True),
+    ("ChromaInterpHor", "chroma_hor", 4, False, False), ("ChromaInterpVet", "chroma_vet", 4, False, False),
+    ("ChromaInterpHorVet", "chroma_hv", 4, False, False), ("ChromaInterpHorU8S16", "chroma_hor_s16", 4, False, True),
+    ("ChromaInterpVetU8S16", "chroma_vet_s16", 4, False, True), ("ChromaInterpHorVetU8S16", "chroma_hv_s16", 4, False, True),
+    ("ChromaInterpVetS16U8", "chroma_vet_s16_pix", 4, True, False), ("ChromaInterpVetS16S16", "chroma_vet_s16_s16", 4, True, True),
+]
+
+
+@pytest.mark.parametrize("spec", INTERP, ids=[s[0] for s in INTERP])
+def test_interpolation(libs, spec):
+    g, o, bd = libs
+    gname, oname, nt, s16, d16 = spec
+    rng = np.random.default_rng(hash(gname) & 0xFFFF)
+    mx = (1 << bd) - 1
+    sizes = [(1, 1), (2, 4), (4, 4), (8, 8), (16, 16), (32, 32), (64, 64), (8, 2)]
+    if nt == 8:
+        sizes.append((128, 128))
+    for w, h in sizes:
+        m = 8
+        if s16:
+            src = rng.integers(-8192, 8192, size=(h + 2 * m, w + 2 * m + 5)).astype(np.int16)
+        else:
+            src = rng.integers(0, mx + 1, size=(h + 2 * m, w + 2 * m + 5)).astype(o.pix)
+        sp = src.shape[1]
+        off = m * sp + m
+        dt = np.int16 if d16 else o.pix
+        fracs = range(0, 256, 5) if nt == 8 else range(0, 1024, 19)
+        for fi in ((0, 1, 2) if nt == 8 else (0,)):
+            for frac in fracs:
+                a = np.zeros((h, w + 3), dt)
+                b = np.zeros((h, w + 3), dt)
+                getattr(g, "XinGpu" + gname)(P(src, off), sp, P(a), w + 3, frac, w, h, fi)
+                _ok(g, gname)
+                getattr(o, oname)(P(src, off), sp, P(b), w + 3, frac, w, h, fi)
+                assert np.array_equal(a, b), (gname, w, h, fi, frac)
+
+
+def test_interp_avg_weight(libs):
+    g, o, bd = libs
+    rng = np.random.default_rng(3)
+    for w, h in [(2, 2), (4, 8), (16, 16), (64, 64), (128, 128)]:
+        a = rng.integers(-8192, 8192, size=(h, w + 1)).astype(np.int16)
+        b = rng.integers(-8192, 8192, size=(h, w + 2)).astype(np.int16)
+        x = np.zeros((h, w), o.pix)
+        y = np.zeros((h, w), o.pix)
+        g.XinGpuInterpAvgS16U8(P(a), w + 1, P(b), w + 2, P(x), w, w, h); _ok(g)
+        o.interp_avg(P(a), w + 1, P(b), w + 2, P(y), w, w, h)
+        assert np.array_equal(x, y)
+        for wa in (-2, 3, 4, 5, 10):
+            g.XinGpuInterpWeightS16U8(P(a), w + 1, P(b), w + 2, P(x), w, w, h, wa, 8 - wa); _ok(g)
+            o.interp_weight(P(a), w + 1, P(b), w + 2, P(y), w, w, h, wa, 8 - wa)
+            assert np.array_equal(x, y)
+
+
+ONE_D = [("Dct2", 0, (2, 4, 8, 16, 32, 64)), ("Dst7", 2, (4, 8, 16, 32)), ("Dct8", 1, (4, 8, 16, 32))]
+
+
+def test_1d_transforms(libs):
+    g, o, bd = libs
+    rng = np.random.default_rng(5)
+    lim = (1 << bd) - 1
+    for name, ty, sizes in ONE_D:
+        for n in sizes:
+            lg = n.bit_length() - 1
+            for line in (1, 4, 16, 64):
+                x = rng.integers(-lim, lim + 1, size=(line, n + 2)).astype(o.coef)
+                a = np.zeros((n, line + 1), o.coef)
+                b = np.zeros((n, line + 1), o.coef)
+                shift = lg + bd + 6 - 15
+                getattr(g, f"XinGpuF{name}P{n}")(P(x), n + 2, P(a), line + 1, line, shift); _ok(g)
+                o.fdct1d(ty, lg, P(x), n + 2, P(b), line + 1, line, shift)
+                assert np.array_equal(a, b), ("F", name, n, line)
+                c = np.clip(rng.laplace(0, 500, size=(n, line + 2)), -32768, 32767).astype(o.coef)
+                for skip in {0, line // 2}:
+                    for shift in (7, 20 - bd):
+                        a = np.zeros((line, n + 1), o.coef)
+                        b = np.zeros((line, n + 1), o.coef)
+                        getattr(g, f"XinGpuI{name}P{n}")(P(c), line + 2, P(a), n + 1, line, skip, shift); _ok(g)
+                        o.idct1d(ty, lg, P(c), line + 2, P(b), n + 1, line, skip, shift)
+                        assert np.array_equal(a, b), ("I", name, n, line, skip)
+
+
+def test_2d_dct2_skip_sub_add(libs):
+    g, o, bd = libs
+    rng = np.random.default_rng(7)
+    lim = (1 << bd) - 1
+    for w in (2, 4, 8, 16, 32, 64):
+        for h in (2, 4, 8, 16, 32, 64):
+            lw, lh = w.bit_length() - 1, h.bit_length() - 1
+            x = rng.integers(-lim, lim + 1, size=(h, w + 1)).astype(o.coef)
+            a = np.zeros((h, w + 2), o.coef)
+            b = np.zeros((h, w + 2), o.coef)
+            s1, s2 = lw + bd + 6 - 15, lh + 6
+            g.XinGpuFDct2WxH(P(x), w + 1, P(a), w + 2, w, h, None, s1, s2); _ok(g)
+            o.fdct2_wxh(P(x), w + 1, P(b), w + 2, w, h, s1, s2)
+            assert np.array_equal(a, b), ("FDct2WxH", w, h)
+            c = np.clip(rng.laplace(0, 300, size=(h, w + 1)), -32768, 32767).astype(o.coef)
+            g.XinGpuIDct2WxH(P(c), w + 1, P(a), w + 2, w, h, None, 7, 20 - bd); _ok(g)
+            o.idct2_wxh(P(c), w + 1, P(b), w + 2, w, h, 7, 20 - bd)
+            assert np.array_equal(a, b), ("IDct2WxH", w, h)
+            g.XinGpuFSkipWxH(P(x), w + 1, P(a), w + 2, w, h, None); _ok(g)
+            o.fskip_wxh(P(x), w + 1, P(b), w + 2, w, h)
+            assert np.array_equal(a, b)
+            g.XinGpuISkipWxH(P(c), w + 1, P(a), w + 2, w, h); _ok(g)
+            o.iskip_wxh(P(c), w + 1, P(b), w + 2, w, h)
+            assert np.array_equal(a, b)
+            inp = rng.integers(0, lim + 1, size=(h, w + 3)).astype(o.pix)
+            prd = rng.integers(0, lim + 1, size=(h, w + 4)).astype(o.pix)
+            g.XinGpuBlockSubForDct(P(inp), w + 3, P(prd), w + 4, P(a), w + 2, w, h); _ok(g)
+            o.block_sub(P(inp), w + 3, P(prd), w + 4, P(b), w + 2, w, h)
+            assert np.array_equal(a, b)
+            r1 = np.zeros((h, w + 1), o.pix)
+            r2 = np.zeros((h, w + 1), o.pix)
+            g.XinGpuBlockAddForDct(P(c), w + 1, P(prd), w + 4, P(r1), w + 1, w, h); _ok(g)
+            o.block_add(P(c), w + 1, P(prd), w + 4, P(r2), w + 1, w, h)
+            assert np.array_equal(r1, r2)
+
+
+def _scan_cg(wcg, hcg):
+    out, x, y, n = [], 0, 0, 0
+    while n < wcg * hcg:
+        while y >= 0:
+            if x < wcg and y < hcg:
+                out.append((x, y, y * wcg + x))
+                n += 1
+            y -= 1
+            x += 1
+        y, x = x, 0
+    return np.array(out, np.uint32)
+
+
+def test_quant_and_prerdoq(libs):
+    g, o, bd = libs
+    rng = np.random.default_rng(9)
+    for qp in range(0, 64, 5):
+        for lgw, lgh in [(2, 2), (3, 3), (4, 4), (5, 5), (2, 5), (5, 3)]:
+            w, h = 1 << lgw, 1 << lgh
+            p = O.orc_qparams()
+            o.quant_params(qp, lgw, lgh, qp % 2, qp % 3 == 0, qp % 4 == 0, p)
+            t = np.clip(rng.laplace(0, 400, size=(h, w + 2)), -32768, 32767).astype(o.coef)
+            outs = []
+            for which in (0, 1):
+                q = np.full((h, w + 2), 5, o.coef)
+                r = np.full((h, w + 2), 5, o.coef)
+                nz = np.zeros(1, np.uint64)
+                f = g.XinGpuQuantInvQuant if which == 0 else o.quant_inv_quant
+                f(P(q), P(t), P(r), w + 2, w, h, 4, 4, p.qmult, p.qadd, p.qshift, p.iqmult, p.iqadd, p.iqshift, P(nz))
+                if which == 0:
+                    _ok(g)
+                outs.append((q, r, nz))
+            for x, y in zip(*outs):
+                assert np.array_equal(x, y), (qp, w, h)
+    for lgw, lgh in [(2, 2), (3, 3), (4, 4), (5, 5), (3, 5)]:
+        w, h = 1 << lgw, 1 << lgh
+        scan = _scan_cg(w // 4, h // 4)
+        for thr in (0, 8, 40, 200):
+            t = np.clip(rng.laplace(0, 30, size=(h, w)), -32768, 32767).astype(o.coef)
+            q0 = rng.integers(-3, 4, size=(h, w)).astype(o.coef)
+            nblk = (w // 4) * (h // 4)
+            nz0 = np.array([int(rng.integers(0, 1 << 62)) & ((1 << nblk) - 1)], np.uint64)
+            outs = []
+            for which in (0, 1):
+                q, r, nz = q0.copy(), q0.copy() * 3, nz0.copy()
+                f = g.XinGpuPreRdoq if which == 0 else o.pre_rdoq
+                f(P(t), P(r), P(q), w, w, h, 4, 4, thr, P(scan), P(nz))
+                if which == 0:
+                    _ok(g)
+                outs.append((q, r, nz))
+            for x, y in zip(*outs):
+                assert np.array_equal(x, y), (w, h, thr)
+
+
+def _me_state(g_lib, inp, refp, pad, w, h, rng_range, mvp, lam, start, window):
+    from xin26x_gb300 import _lib
+    me = _lib.xin_gpu_me_struct()
+    me.width, me.height = w, h
+    me.input, me.inputStride = inp.ctypes.data, inp.shape[1]
+    me.ref, me.refStride = refp.ctypes.data + (pad * refp.shape[1] + pad) * refp.itemsize, refp.shape[1]
+    me.searchWidth = me.searchHeight = rng_range
+    me.predMv.mvX, me.predMv.mvY = mvp
+    me.bestMv.mvX, me.bestMv.mvY = start[:2]
+    me.bestCost = start[2]
+    me.bestSad = 12345
+    me.minMv.mvX, me.minMv.mvY, me.maxMv.mvX, me.maxMv.mvY = window
+    me.sadLambda = lam
+    return me
+
+
+def test_motion_search_drivers(libs):
+    g, o, bd = libs
+    rng = np.random.default_rng(11)
+    mx = (1 << bd) - 1
+    for w, h in [(8, 8), (16, 16), (32, 32), (64, 64), (16, 8), (8, 32)]:
+        pad = 48
+        base = rng.integers(0, mx + 1, size=(h + 2 * pad, w + 2 * pad)).astype(np.int32)
+        refp = ((base + np.roll(base, 1, 0) + np.roll(base, 1, 1)) // 3).astype(o.pix)
+        inp = np.ascontiguousarray(refp[pad + 5:pad + 5 + h, pad - 3:pad - 3 + w])
+        for R, mvp, win in [(8, (0, 0), (-20, -20, 20, 20)), (12, (5, -7), (-9, -30, 4, 30)), (6, (-13, 2), (-40, -40, 40, 40))]:
+            lam = int(rng.integers(0, 300))
+            me = _me_state(g, inp, refp, pad, w, h, R, mvp, lam, (0, 0, 0xFFFFFFFF), win)
+            g.XinGpuMotionEstFull(C.byref(me)); _ok(g, "MotionEstFull")
+            io = O.orc_me_io(0, 0, 0xFFFFFFFF, 12345)
+            o.me_full(P(inp), w, P(refp, pad * refp.shape[1] + pad), refp.shape[1], w, h, mvp[0], mvp[1], R, lam,
+                      win[0], win[1], win[2], win[3], io)
+            assert (me.bestMv.mvX, me.bestMv.mvY, me.bestCost, me.bestSad) == (io.best_mvx, io.best_mvy, io.best_cost, io.best_sad)
+            g.XinGpuFullSubPelMe(C.byref(me)); _ok(g, "FullSubPelMe")
+            o.full_subpel_me(P(inp), w, P(refp, pad * refp.shape[1] + pad), refp.shape[1], w, h, mvp[0], mvp[1], lam,
+                             win[0], win[1], win[2], win[3], io)
+            assert (me.bestMv.mvX, me.bestMv.mvY, me.bestCost) == (io.best_mvx, io.best_mvy, io.best_cost)
+        # an incoming best that no candidate beats is kept
+        me = _me_state(g, inp, refp, pad, w, h, 4, (0, 0), 10, (8, 4, 0), (-20, -20, 20, 20))
+        g.XinGpuMotionEstFull(C.byref(me)); _ok(g)
+        assert (me.bestMv.mvX, me.bestMv.mvY, me.bestCost, me.bestSad) == (8, 4, 0, 12345)
+
+
+def test_invalid_arguments_report_errors(libs):
+    g, o, bd = libs
+    a = np.zeros(64, o.pix)
+    out = np.array([7], np.uint32)
+    g.XinGpuComputeSad(P(a), 8, P(a), 8, 0, 8, P(out))
+    assert g.xin_gpu_last_status() == -2 and out[0] == 7
+    g.XinGpuComputeSatd(P(a), 8, P(a), 8, 6, 6, P(out))
+    assert g.xin_gpu_last_status() == -2
+    g.XinGpuComputeSad(P(a), 8, P(a), 8, 8, 8, P(out))
+    assert g.xin_gpu_last_status() == 0 and out[0] == 0

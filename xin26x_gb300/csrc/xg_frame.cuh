@@ -1,0 +1,453 @@
+/*
+ * xg_frame.cuh -- host side of the batched frame form (xin_gpu_stream_*,
+ * xin_gpu_frame_*): device-resident picture slots, quarter-pel planes and
+ * outputs; the per-picture launches captured once per slot into a CUDA graph.
+ */
+#include "xg_frame_kernels.cuh"
+
+#include <chrono>
+#include <new>
+#include <string.h>
+#include <thread>
+
+static const int XG_LEVEL_SIZE[4] = { 64, 32, 16, 8 };
+
+struct xin_gpu_stream {
+    xin_gpu_stream_cfg cfg;
+    int pad, pitch, cpad, cpitch, rows, crows;
+    int lev_on[4], lev_first[4], lev_cx[4], lev_cy[4];
+    int nlev, ncus;
+    size_t plane_elems, cplane_elems;
+    xg_pix *slot_base[2][3];
+    XgPlane slot[2][3];
+    xg_pix *qpel_base[2];
+    XgQpel qpel[2];
+    unsigned long long *keys;
+    xin_gpu_cu_result *dres;
+    xg_coef *dq[3];
+    xg_pix *drec[3];
+    XgPicParams *dpp;
+    /* pinned host staging */
+    xg_pix *h_in[3];
+    XgPicParams *h_pp;
+    xin_gpu_cu_result *h_res;
+    xg_coef *h_q[3];
+    xg_pix *h_rec[3];
+    cudaStream_t st;
+    cudaEvent_t ev0, ev1;
+    cudaEvent_t evs[5];    /* stage boundaries, recorded inside the picture's launches */
+    cudaGraphExec_t gexec[2];
+    int me_bands, me_band_rows, me_row_words, me_copy_words;
+    size_t me_smem;
+    int nsub;
+    int inflight;          /* a picture with results is queued */
+    int graph_launches[2]; /* kernels inside each captured graph */
+};
+
+static void xg_quant_params(int qp, int lg, int intra_frame, XgQuant *q)
+{
+    /* qMult / iqMult tables and shifts of Xin266ConstructQuantParam (h266_encoder_create.c:94-105,1677-1707),
+     * per-TU adjustment and rounding of Xin266Transform (h266_trans_quant.c:107-120), square TU, DCT2, no RDOQ */
+    static const int qm[6] = { 26214, 23302, 20560, 18396, 16384, 14564 };
+    static const int iqm[6] = { 40, 45, 51, 57, 64, 72 };
+    if (XG_BITDEPTH == 10) qp += 12;
+    int per = qp / 6, rem = qp % 6;
+    q->qmult = qm[rem];
+    q->iqmult = iqm[rem] << per;
+    q->qshift = 14 + (15 - XG_BITDEPTH) + per - lg;
+    q->iqshift = 6 - (15 - XG_BITDEPTH) + lg;
+    q->qadd = (intra_frame ? 171 : 85) << (q->qshift - 9);
+    q->iqadd = 1 << (q->iqshift - 1);
+}
+
+static int xg_stream_free(xin_gpu_stream *s)
+{
+    if (!s) return XIN_GPU_OK;
+    cudaStreamSynchronize(s->st);
+    for (int i = 0; i < 2; i++) if (s->gexec[i]) cudaGraphExecDestroy(s->gexec[i]);
+    for (int i = 0; i < 2; i++) { for (int p = 0; p < 3; p++) cudaFree(s->slot_base[i][p]); cudaFree(s->qpel_base[i]); }
+    cudaFree(s->keys); cudaFree(s->dres); cudaFree(s->dpp);
+    for (int p = 0; p < 3; p++) { cudaFree(s->dq[p]); cudaFree(s->drec[p]); cudaFreeHost(s->h_in[p]); cudaFreeHost(s->h_q[p]); cudaFreeHost(s->h_rec[p]); }
+    cudaFreeHost(s->h_pp); cudaFreeHost(s->h_res);
+    for (int i = 0; i < 5; i++) if (s->evs[i]) cudaEventDestroy(s->evs[i]);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->st) cudaStreamDestroy(s->st);
+    delete s;
+    return XIN_GPU_OK;
+}
+
+extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream **out)
+{
+    xin_gpu_clear_error();
+    if (!cfg || !out) { xg_set_error(XIN_GPU_ERR_ARG, "stream_open: null argument"); return XIN_GPU_ERR_ARG; }
+    *out = nullptr;
+    if (xg_ensure_init()) return XIN_GPU_ERR_CUDA;
+    const xin_gpu_stream_cfg &c = *cfg;
+    if (c.width < 16 || c.height < 16 || (c.width & 1) || (c.height & 1) || c.width > 8192 || c.height > 8192 ||
+        (c.ctu_size != 64 && c.ctu_size != 128) || c.search_range < 1 || c.search_range > 256 ||
+        !(c.level_mask & (8u | 16u | 32u | 64u))) {
+        xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range or level mask");
+        return XIN_GPU_ERR_ARG;
+    }
+    xin_gpu_stream *s = new (std::nothrow) xin_gpu_stream();
+    if (!s) { xg_set_error(XIN_GPU_ERR_NOMEM, "stream_open: host allocation"); return XIN_GPU_ERR_NOMEM; }
+    s->cfg = c;
+    /* margin: the reference pads ctu + 16; the tile search also reads R + 64 + 8 around full tiles */
+    int pad = c.ctu_size + 16 > c.search_range + 72 ? c.ctu_size + 16 : c.search_range + 72;
+    pad = (pad + 31) & ~31;
+    s->pad = pad;
+    s->pitch = ((c.width + 2 * pad) + 127) & ~127;
+    s->rows = c.height + 2 * pad;
+    s->cpad = pad / 2;
+    s->cpitch = ((c.width / 2 + 2 * s->cpad) + 127) & ~127;
+    s->crows = c.height / 2 + 2 * s->cpad;
+    s->plane_elems = (size_t)s->pitch * s->rows;
+    s->cplane_elems = (size_t)s->cpitch * s->crows;
+    int first = 0;
+    for (int L = 0; L < 4; L++) {
+        int sz = XG_LEVEL_SIZE[L];
+        s->lev_on[L] = (c.level_mask & (uint32_t)sz) != 0;
+        s->lev_cx[L] = c.width / sz;
+        s->lev_cy[L] = c.height / sz;
+        s->lev_first[L] = first;
+        if (s->lev_on[L]) { first += s->lev_cx[L] * s->lev_cy[L]; s->nlev++; }
+    }
+    s->ncus = first;
+
+    cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
+    for (int i = 0; i < 5 && e == cudaSuccess; i++) e = cudaEventCreate(&s->evs[i]);
+    size_t ysz = s->plane_elems * sizeof(xg_pix), csz = s->cplane_elems * sizeof(xg_pix);
+    size_t lq = (size_t)c.width * c.height, lc = lq / 4;
+    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+        for (int p = 0; p < 3 && e == cudaSuccess; p++) e = cudaMalloc(&s->slot_base[i][p], p ? csz : ysz);
+        if (e == cudaSuccess) e = cudaMalloc(&s->qpel_base[i], 16 * ysz);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&s->keys, sizeof(unsigned long long) * (s->ncus > 0 ? s->ncus : 1));
+    if (e == cudaSuccess) e = cudaMalloc(&s->dres, sizeof(xin_gpu_cu_result) * s->ncus);
+    if (e == cudaSuccess) e = cudaMalloc(&s->dpp, sizeof(XgPicParams));
+    for (int p = 0; p < 3 && e == cudaSuccess; p++) {
+        size_t n = (p ? lc : lq) * s->nlev;
+        e = cudaMalloc(&s->dq[p], n * sizeof(xg_coef));
+        if (e == cudaSuccess) e = cudaMalloc(&s->drec[p], n * sizeof(xg_pix));
+        if (c.device_io) continue;
+        if (e == cudaSuccess) e = cudaMallocHost(&s->h_in[p], (p ? lc : lq) * sizeof(xg_pix));
+        if (e == cudaSuccess && (c.out_flags & XIN_GPU_OUT_Q)) e = cudaMallocHost(&s->h_q[p], n * sizeof(xg_coef));
+        if (e == cudaSuccess && (c.out_flags & XIN_GPU_OUT_REC)) e = cudaMallocHost(&s->h_rec[p], n * sizeof(xg_pix));
+    }
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_pp, sizeof(XgPicParams));
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_res, sizeof(xin_gpu_cu_result) * s->ncus);
+    if (e != cudaSuccess) {
+        int st = (e == cudaErrorMemoryAllocation) ? XIN_GPU_ERR_NOMEM : XIN_GPU_ERR_CUDA;
+        xg_set_error(st, "stream_open: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+        xg_stream_free(s);
+        return st;
+    }
+    for (int i = 0; i < 2; i++) {
+        for (int p = 0; p < 3; p++) {
+            XgPlane &pl = s->slot[i][p];
+            int pd = p ? s->cpad : s->pad, pt = p ? s->cpitch : s->pitch;
+            pl.data = s->slot_base[i][p] + (size_t)pd * pt + pd;
+            pl.pitch = pt;
+            pl.w = p ? c.width / 2 : c.width;
+            pl.h = p ? c.height / 2 : c.height;
+            pl.pad = pd;
+        }
+        XgQpel &q = s->qpel[i];
+        for (int k = 0; k < 16; k++) q.plane[k] = s->qpel_base[i] + (size_t)k * s->plane_elems + (size_t)pad * s->pitch + pad;
+        q.plane[0] = s->slot[i][0].data;
+        q.pitch = s->pitch; q.w = c.width; q.h = c.height; q.pad = pad;
+    }
+    /* integer-search band geometry: enough CTAs for the GPU, shared memory under 200 KB */
+    int R = c.search_range, ndy = 2 * R + 1;
+    int tiles = ((c.width + 63) / 64) * ((c.height + 63) / 64);
+    int bands = (4 * 152 + tiles - 1) / tiles;
+    if (bands < 1) bands = 1;
+    if (bands > ndy) bands = ndy;
+    s->me_row_words = (67 + 2 * R) / 4 + 1;
+    for (;;) {
+        s->me_band_rows = (ndy + bands - 1) / bands;
+        int rows = 64 + s->me_band_rows - 1;
+        int cw = rows * s->me_row_words;
+        cw += (8 - cw % 32 + 32) % 32;          /* copy stride = 8 (mod 32) words: conflict-free lanes */
+        s->me_copy_words = cw;
+        s->me_smem = sizeof(uint32_t) * (4 * (size_t)cw + (2 * R + 1) + s->me_band_rows + 16 * XG_ME_GROUP);
+        if (s->me_smem <= 200 * 1024 || s->me_band_rows == 1) break;
+        bands++;
+    }
+    s->me_bands = (ndy + s->me_band_rows - 1) / s->me_band_rows;
+#if XG_BITDEPTH == 8
+    if (xg_cuda_check(cudaFuncSetAttribute(k_me_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->me_smem),
+                      "me smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
+#endif
+    *out = s;
+    return XIN_GPU_OK;
+}
+
+extern "C" int xin_gpu_stream_close(xin_gpu_stream *s) { return xg_stream_free(s); }
+extern "C" int xin_gpu_stream_num_cus(const xin_gpu_stream *s) { return s ? s->ncus : 0; }
+extern "C" int xin_gpu_stream_num_levels(const xin_gpu_stream *s) { return s ? s->nlev : 0; }
+extern "C" int xin_gpu_stream_level_info(const xin_gpu_stream *s, int level, int32_t *size, int32_t *first_cu, int32_t *cus_x,
+                                         int32_t *cus_y)
+{
+    if (!s) return XIN_GPU_ERR_ARG;
+    int k = 0;
+    for (int L = 0; L < 4; L++) {
+        if (!s->lev_on[L]) continue;
+        if (k++ != level) continue;
+        if (size) *size = XG_LEVEL_SIZE[L];
+        if (first_cu) *first_cu = s->lev_first[L];
+        if (cus_x) *cus_x = s->lev_cx[L];
+        if (cus_y) *cus_y = s->lev_cy[L];
+        return XIN_GPU_OK;
+    }
+    return XIN_GPU_ERR_ARG;
+}
+
+/* the launches of one picture in slot `cur` against the reference in 1 - cur */
+static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me)
+{
+    const xin_gpu_stream_cfg &c = s->cfg;
+    cudaStream_t st = s->st;
+    size_t lq = (size_t)c.width * c.height, lc = lq / 4;
+    int nl = 0;
+    /* upload and pad the current picture; it becomes the next picture's reference */
+    cudaEventRecord(s->evs[0], st);
+    cudaMemcpyAsync(s->dpp, s->h_pp, sizeof(XgPicParams), cudaMemcpyHostToDevice, st);
+    if (c.device_io) {
+        k_copy_in<<<152 * 4, 256, 0, st>>>(s->slot[cur][0], s->slot[cur][1], s->slot[cur][2], s->dpp);
+        nl++;
+    }
+    for (int p = 0; p < 3; p++) {
+        XgPlane &pl = s->slot[cur][p];
+        if (!c.device_io)
+            cudaMemcpy2DAsync(pl.data, (size_t)pl.pitch * sizeof(xg_pix), s->h_in[p], (size_t)pl.w * sizeof(xg_pix),
+                              (size_t)pl.w * sizeof(xg_pix), pl.h, cudaMemcpyHostToDevice, st);
+        k_pad<<<152 * 4, 256, 0, st>>>(pl);
+        nl++;
+    }
+    {
+        dim3 blk(32, 8), grd((c.width + 2 * s->pad - 8 + 31) / 32, (c.height + 2 * s->pad - 8 + 7) / 8, 15);
+        k_qpel_planes<<<grd, blk, 0, st>>>(s->slot[cur][0], s->qpel[cur]);
+        nl++;
+    }
+    cudaEventRecord(s->evs[1], st);
+    if (with_me) {
+        int ref = 1 - cur;
+        cudaMemsetAsync(s->keys, 0xff, sizeof(unsigned long long) * s->ncus, st);
+        XgMeParams mp;
+        mp.cur = s->slot[cur][0];
+        mp.ref = s->slot[ref][0];
+        mp.W = c.width; mp.H = c.height; mp.ctu = c.ctu_size; mp.R = c.search_range;
+        mp.band_rows = s->me_band_rows; mp.row_words = s->me_row_words; mp.copy_words = s->me_copy_words;
+        for (int L = 0; L < 4; L++) {
+            mp.keys[L] = s->lev_on[L] ? s->keys + s->lev_first[L] : nullptr;
+            mp.cus_x[L] = s->lev_cx[L];
+        }
+#if XG_BITDEPTH == 8
+        dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, s->me_bands);
+        k_me_tiles<<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, s->dpp);
+        nl++;
+#else
+        for (int L = 0; L < 4; L++) {
+            if (!s->lev_on[L]) continue;
+            dim3 grd(s->lev_cx[L] * s->lev_cy[L], 8);
+            k_me_generic<<<grd, 128, 0, st>>>(mp, s->dpp, L, XG_LEVEL_SIZE[L], s->lev_cx[L]);
+            nl++;
+        }
+#endif
+        cudaEventRecord(s->evs[2], st);
+        int li = 0;
+        for (int L = 0; L < 4; L++) {
+            if (!s->lev_on[L]) continue;
+            XgTailParams tp;
+            for (int p = 0; p < 3; p++) { tp.cur[p] = s->slot[cur][p]; tp.ref[p] = s->slot[ref][p]; }
+            tp.qpel = s->qpel[ref];
+            tp.W = c.width; tp.H = c.height; tp.ctu = c.ctu_size; tp.R = c.search_range;
+            tp.keys = s->keys + s->lev_first[L];
+            tp.cus_x = s->lev_cx[L]; tp.first_cu = s->lev_first[L]; tp.size = XG_LEVEL_SIZE[L]; tp.level = L;
+            for (int p = 0; p < 3; p++) {
+                tp.q[p] = s->dq[p] + (p ? lc : lq) * li;
+                tp.rec[p] = s->drec[p] + (p ? lc : lq) * li;
+            }
+            tp.res = s->dres;
+            int n = s->lev_cx[L] * s->lev_cy[L];
+            if (n > 0) {
+                switch (XG_LEVEL_SIZE[L]) {
+                case 64: k_cu_tail<64, 256><<<n, 256, 0, st>>>(tp, s->dpp); break;
+                case 32: k_cu_tail<32, 256><<<n, 256, 0, st>>>(tp, s->dpp); break;
+                case 16: k_cu_tail<16, 128><<<n, 128, 0, st>>>(tp, s->dpp); break;
+                default: k_cu_tail<8, 64><<<n, 64, 0, st>>>(tp, s->dpp); break;
+                }
+                nl++;
+            }
+            li++;
+        }
+        cudaEventRecord(s->evs[3], st);
+        if (!c.device_io) {
+            cudaMemcpyAsync(s->h_res, s->dres, sizeof(xin_gpu_cu_result) * s->ncus, cudaMemcpyDeviceToHost, st);
+            for (int p = 0; p < 3; p++) {
+                size_t n = (p ? lc : lq) * s->nlev;
+                if (c.out_flags & XIN_GPU_OUT_Q) cudaMemcpyAsync(s->h_q[p], s->dq[p], n * sizeof(xg_coef), cudaMemcpyDeviceToHost, st);
+                if (c.out_flags & XIN_GPU_OUT_REC) cudaMemcpyAsync(s->h_rec[p], s->drec[p], n * sizeof(xg_pix), cudaMemcpyDeviceToHost, st);
+            }
+        }
+    } else {
+        cudaEventRecord(s->evs[2], st);
+        cudaEventRecord(s->evs[3], st);
+    }
+    cudaEventRecord(s->evs[4], st);
+    return nl;
+}
+
+extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic)
+{
+    xin_gpu_clear_error();
+    if (!s || !pic) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: null argument"); return XIN_GPU_ERR_ARG; }
+    if (s->inflight) { xg_set_error(XIN_GPU_ERR_STATE, "frame_submit: previous picture not collected by frame_wait"); return XIN_GPU_ERR_STATE; }
+    const xin_gpu_stream_cfg &c = s->cfg;
+    if (pic->qp < 0 || pic->qp > 63 || pic->uv_qp < 0 || pic->uv_qp > 63) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: QP out of range"); return XIN_GPU_ERR_ARG; }
+    XgPicParams pp;
+    memset(&pp, 0, sizeof pp);
+    for (int p = 0; p < 3; p++) {
+        int w = p ? c.width / 2 : c.width, h = p ? c.height / 2 : c.height;
+        if (!pic->plane[p] || pic->stride[p] < w) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: bad plane"); return XIN_GPU_ERR_ARG; }
+        if (c.device_io) {
+            pp.src[p] = (const xg_pix *)pic->plane[p];
+            pp.src_stride[p] = pic->stride[p];
+            continue;
+        }
+        for (int y = 0; y < h; y++)
+            memcpy(s->h_in[p] + (size_t)y * w, pic->plane[p] + (size_t)y * pic->stride[p], (size_t)w * sizeof(xg_pix));
+    }
+    pp.lambda = pic->sad_lambda;
+    for (int L = 0; L < 4; L++) {
+        int lg = XG_LEVEL_SIZE[L] == 64 ? 6 : XG_LEVEL_SIZE[L] == 32 ? 5 : XG_LEVEL_SIZE[L] == 16 ? 4 : 3;
+        xg_quant_params(pic->qp, lg, 0, &pp.quant[L][0]);
+        xg_quant_params(pic->uv_qp, lg - 1, 0, &pp.quant[L][1]);
+        pp.quant[L][2] = pp.quant[L][1];
+    }
+    *s->h_pp = pp;
+    int cur = s->nsub & 1;
+    bool with_me = s->nsub > 0;
+    cudaEventRecord(s->ev0, s->st);
+    if (with_me && c.use_graph) {
+        if (!s->gexec[cur]) {
+            cudaGraph_t g;
+            if (xg_cuda_check(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal), "begin capture")) return XIN_GPU_ERR_CUDA;
+            s->graph_launches[cur] = xg_enqueue_picture(s, cur, true);
+            if (xg_cuda_check(cudaStreamEndCapture(s->st, &g), "end capture")) return XIN_GPU_ERR_CUDA;
+            cudaError_t e = cudaGraphInstantiate(&s->gexec[cur], g, 0);
+            cudaGraphDestroy(g);
+            if (xg_cuda_check(e, "graph instantiate")) return XIN_GPU_ERR_CUDA;
+        }
+        if (xg_cuda_check(cudaGraphLaunch(s->gexec[cur], s->st), "graph launch")) return XIN_GPU_ERR_CUDA;
+        xg_count_launch((uint64_t)s->graph_launches[cur]);
+    } else {
+        xg_count_launch((uint64_t)xg_enqueue_picture(s, cur, with_me));
+    }
+    cudaEventRecord(s->ev1, s->st);
+    if (xg_cuda_check(cudaGetLastError(), "frame_submit")) return XIN_GPU_ERR_CUDA;
+    s->nsub++;
+    s->inflight = with_me;
+    return XIN_GPU_OK;
+}
+
+extern "C" int xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32_t timeout_ms)
+{
+    xin_gpu_clear_error();
+    if (!s) { xg_set_error(XIN_GPU_ERR_ARG, "frame_wait: null stream"); return XIN_GPU_ERR_ARG; }
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaEventQuery(s->ev1);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) return xg_cuda_check(e, "frame_wait");
+        double el = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_ms >= 0 && el > timeout_ms) { xg_set_error(XIN_GPU_ERR_TIMEOUT, "frame_wait: timed out after %d ms", timeout_ms); return XIN_GPU_ERR_TIMEOUT; }
+        std::this_thread::yield();
+    }
+    if (!s->inflight) {
+        if (res) { res->gpu_ms = 0; }
+        return XIN_GPU_OK;
+    }
+    s->inflight = 0;
+    if (!res) return XIN_GPU_OK;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, s->evs[0], s->evs[4]);
+    res->gpu_ms = ms;
+    const xin_gpu_stream_cfg &c = s->cfg;
+    if (c.device_io) return XIN_GPU_OK;
+    size_t lq = (size_t)c.width * c.height, lc = lq / 4;
+    /* caller buffers are filled; NULL members receive views of the stream's pinned
+     * buffers, valid until the next frame_submit */
+    if (res->cu) memcpy(res->cu, s->h_res, sizeof(xin_gpu_cu_result) * s->ncus);
+    else res->cu = s->h_res;
+    for (int p = 0; p < 3; p++) {
+        size_t n = (p ? lc : lq) * s->nlev;
+        if (c.out_flags & XIN_GPU_OUT_Q) {
+            if (res->q[p]) memcpy(res->q[p], s->h_q[p], n * sizeof(xg_coef));
+            else res->q[p] = s->h_q[p];
+        }
+        if (c.out_flags & XIN_GPU_OUT_REC) {
+            if (res->rec[p]) memcpy(res->rec[p], s->h_rec[p], n * sizeof(xg_pix));
+            else res->rec[p] = s->h_rec[p];
+        }
+    }
+    return XIN_GPU_OK;
+}
+
+extern "C" int xin_gpu_stream_stage_ms(const xin_gpu_stream *s, float ms[4])
+{
+    if (!s || !ms) return XIN_GPU_ERR_ARG;
+    for (int i = 0; i < 4; i++) {
+        ms[i] = 0;
+        if (cudaEventElapsedTime(&ms[i], s->evs[i], s->evs[i + 1]) != cudaSuccess) { cudaGetLastError(); return XIN_GPU_ERR_STATE; }
+    }
+    return XIN_GPU_OK;
+}
+
+extern "C" int xin_gpu_stream_device_results(const xin_gpu_stream *s, void **cu, void *q[3], void *rec[3])
+{
+    if (!s) return XIN_GPU_ERR_ARG;
+    if (cu) *cu = s->dres;
+    for (int p = 0; p < 3; p++) {
+        if (q) q[p] = s->dq[p];
+        if (rec) rec[p] = s->drec[p];
+    }
+    return XIN_GPU_OK;
+}
+
+extern "C" int xin_gpu_measure_sad_peak(double *absdiff_per_s)
+{
+    xin_gpu_clear_error();
+    if (!absdiff_per_s) return XIN_GPU_ERR_ARG;
+    XgThread *t = xg_thread();
+    if (!t) return XIN_GPU_ERR_CUDA;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 16, threads = 256, iters = 4096;
+    uint32_t *in = (uint32_t *)xg_dalloc(t, 4096), *out = (uint32_t *)xg_dalloc(t, (size_t)blocks * threads * 4);
+    if (!in || !out) return XIN_GPU_ERR_NOMEM;
+    cudaMemsetAsync(in, 0x5a, 4096, t->stream);
+    cudaEvent_t a, b;
+    cudaEventCreate(&a); cudaEventCreate(&b);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        cudaEventRecord(a, t->stream);
+        k_sad_peak<<<blocks, threads, 0, t->stream>>>(in, out, iters);
+        cudaEventRecord(b, t->stream);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (rep && ms < best) best = ms;
+    }
+    xg_count_launch(4);
+    cudaEventDestroy(a); cudaEventDestroy(b);
+    if (xg_cuda_check(cudaGetLastError(), "sad peak")) return XIN_GPU_ERR_CUDA;
+    *absdiff_per_s = (double)blocks * threads * iters * 8 * 4 / (best * 1e-3);
+    return XIN_GPU_OK;
+}
