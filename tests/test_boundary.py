@@ -71,3 +71,62 @@ def test_me_mirror_matches_reference_layout():
     ref = _offsets_c(_probe("xin_me_struct", ["xin_typedef.h", "xin_video_common.h", "h26x_me_struct.h"]), incs)
     mine = _offsets_c(_probe("xin_gpu_me_struct", ["xingpu_me.h"]), [os.path.join(ROOT, "include")])
     assert ref == mine
+
+
+_FUNC_MEMBERS = ["pfXinComputeSad", "pfXinComputeSatd", "pfXinComputeDist", "pfXinComputeAvgSad", "pfXinComputeAvgDist",
+                 "pfXinComputeWeightDist", "pfXinComputeSadx8", "pfXinComputeAvgSadx8", "pfXinLumaInterp",
+                 "pfXinChromaInterp", "pfXinLumaInterpS16", "pfXinChromaInterpS16", "pfXinInterpAvg", "pfXinInterpWeight",
+                 "pfXinQuantInvQuant", "pfXinFor2dDct2", "pfXinFor2dSkip", "pfXinInv2dSkip", "pfXinFor1dDct",
+                 "pfXinInv2dDct2", "pfXinInv1dDct", "pfXinBlockSubForDct", "pfXinBlockAddForDct", "pfXinComputeHada8x8",
+                 "pfXinPreRdoq", "pfXinFilterIntraNB"]
+
+
+def _func_probe(struct, headers):
+    inc = "".join(f'#include "{h}"\n' for h in headers)
+    body = "".join(f'printf("{f} %zu\\n", offsetof({struct}, {f}));\n' for f in _FUNC_MEMBERS)
+    return f"#include <stdio.h>\n#include <stddef.h>\n#include <stdint.h>\n{inc}int main(void){{\n{body}printf(\"sizeof %zu\\n\", sizeof({struct}));return 0;}}\n"
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "h266_encoder")), reason="reference tree absent")
+def test_func_table_mirror_matches_reference_layout():
+    hdrs = ["xin_typedef.h", "basic_macro.h", "h26x_definition.h", "h266_definition.h", "h266_constant.h",
+            "xin_video_common.h", "h266_picture_struct.h", "h266_intra_pred_context.h", "h266_pred_unit_struct.h",
+            "h266_seq_struct.h", "h266_trans_unit_struct.h", "h26x_me_struct.h", "h266_cabac_struct.h",
+            "h266_md_buffer_struct.h", "h266_coding_unit_struct.h", "h266_alf_struct.h", "h266_section_struct.h",
+            "h26x_trans_context.h", "h266_func_struct.h"]
+    incs = [os.path.join(REF, p) for p in ("common/include", "video_api/video_common/include", "video_api/video_encoder/include",
+                                           "h26x_core/include", "h266_core/include", "h266_encoder/include")]
+    ref = _offsets_c(_func_probe("xin_func_struct", hdrs), incs)
+    mine = _offsets_c(_func_probe("xin_gpu_func_struct", ["xingpu_install.h"]), [os.path.join(ROOT, "include")])
+    assert ref == mine
+
+
+@pytest.mark.parametrize("bd", (8, 10))
+def test_installer_fills_tables_without_gpu(bd):
+    path = _lib.lib_path(bd)
+    if not os.path.exists(path):
+        pytest.skip("libxingpu not built")
+    lib = C.CDLL(path)
+    lib.xin_gpu_install.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32]
+    # offsets from the mirror header, via a probe program
+    offs = _offsets_c(_func_probe("xin_gpu_func_struct", ["xingpu_install.h"]), [os.path.join(ROOT, "include")])
+    size = offs["sizeof"]
+    fs = (C.c_void_p * (size // 8))()
+    satd_slot = offs["pfXinComputeSatd"] // 8 + 3
+    dist_slot = offs["pfXinComputeDist"] // 8 + 3
+    fs[satd_slot] = fs[dist_slot] = 0x1234        # preset selected SATD for width 8
+    me = _lib.xin_gpu_me_struct()
+    assert lib.xin_gpu_install(C.addressof(fs), C.addressof(me), 15) == 0
+    addr = lambda n: C.cast(getattr(lib, n), C.c_void_p).value  # noqa: E731
+    assert fs[offs["pfXinComputeSad"] // 8] == addr("XinGpuComputeSad")
+    assert fs[dist_slot] == addr("XinGpuComputeSatd")
+    assert fs[offs["pfXinComputeDist"] // 8 + 4] == addr("XinGpuComputeSad")
+    assert fs[offs["pfXinLumaInterp"] // 8 + 16 + 3] == addr("XinGpuLumaInterpHor")       # [1][0][3]
+    assert fs[offs["pfXinFor1dDct"] // 8 + 2 * 8 + 4] == addr("XinGpuFDst7P16")          # [DST7][16]
+    assert fs[offs["pfXinInv1dDct"] // 8 + 6] == addr("XinGpuIDct2P64")
+    assert fs[offs["pfXinFor1dDct"] // 8 + 1 * 8 + 6] is None                             # no 64-point DCT8
+    assert fs[offs["pfXinQuantInvQuant"] // 8 + 5] == addr("XinGpuQuantInvQuant")
+    assert fs[offs["pfXinPreRdoq"] // 8] == addr("XinGpuPreRdoq")
+    assert fs[offs["pfXinFilterIntraNB"] // 8] is None                                    # off the hot path
+    assert me.funcSet[0] == addr("XinGpuComputeSad")
+    assert lib.xin_gpu_install(None, None, 15) == -2

@@ -12,6 +12,7 @@ import re
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 HEADER = os.path.join(ROOT, "include", "xingpu.h")
+HEADERS = [os.path.join(ROOT, "include", f) for f in ("xingpu.h", "xingpu_me.h", "xingpu_install.h")]
 
 i32, u32, u64, ip, vp = C.c_int32, C.c_uint32, C.c_uint64, C.c_ssize_t, C.c_void_p
 
@@ -101,6 +102,7 @@ SIGNATURES = {
     "xin_gpu_stream_stage_ms": ([vp, C.POINTER(C.c_float)], C.c_int),
     "xin_gpu_stream_device_results": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)], C.c_int),
     "xin_gpu_measure_sad_peak": ([C.POINTER(C.c_double)], C.c_int),
+    "xin_gpu_install": ([vp, vp, u32], C.c_int),
 }
 for _n in ["InterpCopy", "InterpCopyU8S16", "LumaInterpHor", "LumaInterpVet", "LumaInterpHorVet", "LumaInterpHorU8S16",
            "LumaInterpVetU8S16", "LumaInterpHorVetU8S16", "LumaInterpVetS16U8", "LumaInterpVetS16S16",
@@ -113,9 +115,9 @@ for _t, _sizes in (("Dct2", (2, 4, 8, 16, 32, 64)), ("Dst7", (4, 8, 16, 32)), ("
         SIGNATURES[f"XinGpuI{_t}P{_n}"] = (_I1, None)
 
 
-def header_functions(path: str = HEADER) -> list:
-    """Every function name include/xingpu.h declares (after macro expansion of the 1-D families)."""
-    txt = re.sub(r"/\*.*?\*/", " ", open(path).read(), flags=re.S)
+def header_functions(paths=None) -> list:
+    """Every function name the include/*.h headers declare (after macro expansion of the 1-D families)."""
+    txt = " ".join(re.sub(r"/\*.*?\*/", " ", open(p).read(), flags=re.S) for p in (paths or HEADERS))
     names = set(re.findall(r"\b(?:void|int|const char \*|uint64_t)\s*\**\s*(\w+)\s*\(", txt))
     names |= set(re.findall(r"XG_[FI]DCT1D\((\w+)\)", txt))
     return sorted(n for n in names if n not in ("XG_FDCT1D", "XG_IDCT1D") and not n.startswith("NAME"))

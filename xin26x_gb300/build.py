@@ -18,7 +18,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 def _sources():
     return [os.path.join(CSRC, f) for f in sorted(os.listdir(CSRC))] + [os.path.join(ROOT, "include", "xingpu.h"),
-                                                                       os.path.join(ROOT, "include", "xingpu_me.h")]
+                                                                       os.path.join(ROOT, "include", "xingpu_me.h"),
+                                                                       os.path.join(ROOT, "include", "xingpu_install.h")]
 
 
 def _stale(out: str) -> bool:

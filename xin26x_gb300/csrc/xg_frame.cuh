@@ -37,7 +37,7 @@ struct xin_gpu_stream {
     cudaEvent_t ev0, ev1;
     cudaEvent_t evs[5];    /* stage boundaries, recorded inside the picture's launches */
     cudaGraphExec_t gexec[2];
-    int me_bands, me_band_rows, me_row_words, me_copy_words;
+    int me_bands, me_band_rows, me_row_words;
     size_t me_smem;
     int nsub;
     int inflight;          /* a picture with results is queued */
@@ -167,14 +167,15 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     int bands = (4 * 152 + tiles - 1) / tiles;
     if (bands < 1) bands = 1;
     if (bands > ndy) bands = ndy;
-    s->me_row_words = (67 + 2 * R) / 4 + 1;
+    {
+        /* word positions per band row: nx + 60; pitch congruent to nx (mod 32) */
+        int nx = 2 * R + 1, relw = nx + 60;
+        s->me_row_words = relw + (((nx - relw) % 32) + 32) % 32;
+    }
     for (;;) {
         s->me_band_rows = (ndy + bands - 1) / bands;
         int rows = 64 + s->me_band_rows - 1;
-        int cw = rows * s->me_row_words;
-        cw += (8 - cw % 32 + 32) % 32;          /* copy stride = 8 (mod 32) words: conflict-free lanes */
-        s->me_copy_words = cw;
-        s->me_smem = sizeof(uint32_t) * (4 * (size_t)cw + (2 * R + 1) + s->me_band_rows + 16 * XG_ME_GROUP);
+        s->me_smem = sizeof(uint32_t) * ((size_t)rows * s->me_row_words + (2 * R + 1) + s->me_band_rows + 16 * XG_ME_GROUP);
         if (s->me_smem <= 200 * 1024 || s->me_band_rows == 1) break;
         bands++;
     }
@@ -207,15 +208,23 @@ extern "C" int xin_gpu_stream_level_info(const xin_gpu_stream *s, int level, int
     return XIN_GPU_ERR_ARG;
 }
 
+/* stage-boundary event: inside a stream capture it must be an external record
+ * node to be recorded when the graph runs; outside a capture a plain record */
+static void xg_stage_event(cudaEvent_t e, cudaStream_t st, bool capturing)
+{
+    if (capturing) cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+    else cudaEventRecord(e, st);
+}
+
 /* the launches of one picture in slot `cur` against the reference in 1 - cur */
-static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me)
+static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool capturing)
 {
     const xin_gpu_stream_cfg &c = s->cfg;
     cudaStream_t st = s->st;
     size_t lq = (size_t)c.width * c.height, lc = lq / 4;
     int nl = 0;
     /* upload and pad the current picture; it becomes the next picture's reference */
-    cudaEventRecord(s->evs[0], st);
+    xg_stage_event(s->evs[0], st, capturing);
     cudaMemcpyAsync(s->dpp, s->h_pp, sizeof(XgPicParams), cudaMemcpyHostToDevice, st);
     if (c.device_io) {
         k_copy_in<<<152 * 4, 256, 0, st>>>(s->slot[cur][0], s->slot[cur][1], s->slot[cur][2], s->dpp);
@@ -234,7 +243,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me)
         k_qpel_planes<<<grd, blk, 0, st>>>(s->slot[cur][0], s->qpel[cur]);
         nl++;
     }
-    cudaEventRecord(s->evs[1], st);
+    xg_stage_event(s->evs[1], st, capturing);
     if (with_me) {
         int ref = 1 - cur;
         cudaMemsetAsync(s->keys, 0xff, sizeof(unsigned long long) * s->ncus, st);
@@ -242,7 +251,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me)
         mp.cur = s->slot[cur][0];
         mp.ref = s->slot[ref][0];
         mp.W = c.width; mp.H = c.height; mp.ctu = c.ctu_size; mp.R = c.search_range;
-        mp.band_rows = s->me_band_rows; mp.row_words = s->me_row_words; mp.copy_words = s->me_copy_words;
+        mp.band_rows = s->me_band_rows; mp.row_words = s->me_row_words;
         for (int L = 0; L < 4; L++) {
             mp.keys[L] = s->lev_on[L] ? s->keys + s->lev_first[L] : nullptr;
             mp.cus_x[L] = s->lev_cx[L];
@@ -259,7 +268,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me)
             nl++;
         }
 #endif
-        cudaEventRecord(s->evs[2], st);
+        xg_stage_event(s->evs[2], st, capturing);
         int li = 0;
         for (int L = 0; L < 4; L++) {
             if (!s->lev_on[L]) continue;
@@ -286,7 +295,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me)
             }
             li++;
         }
-        cudaEventRecord(s->evs[3], st);
+        xg_stage_event(s->evs[3], st, capturing);
         if (!c.device_io) {
             cudaMemcpyAsync(s->h_res, s->dres, sizeof(xin_gpu_cu_result) * s->ncus, cudaMemcpyDeviceToHost, st);
             for (int p = 0; p < 3; p++) {
@@ -296,16 +305,17 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me)
             }
         }
     } else {
-        cudaEventRecord(s->evs[2], st);
-        cudaEventRecord(s->evs[3], st);
+        xg_stage_event(s->evs[2], st, capturing);
+        xg_stage_event(s->evs[3], st, capturing);
     }
-    cudaEventRecord(s->evs[4], st);
+    xg_stage_event(s->evs[4], st, capturing);
     return nl;
 }
 
 extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic)
 {
     xin_gpu_clear_error();
+    (void)cudaGetLastError();   /* errors of earlier, unrelated calls are not this picture's */
     if (!s || !pic) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: null argument"); return XIN_GPU_ERR_ARG; }
     if (s->inflight) { xg_set_error(XIN_GPU_ERR_STATE, "frame_submit: previous picture not collected by frame_wait"); return XIN_GPU_ERR_STATE; }
     const xin_gpu_stream_cfg &c = s->cfg;
@@ -338,7 +348,7 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
         if (!s->gexec[cur]) {
             cudaGraph_t g;
             if (xg_cuda_check(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal), "begin capture")) return XIN_GPU_ERR_CUDA;
-            s->graph_launches[cur] = xg_enqueue_picture(s, cur, true);
+            s->graph_launches[cur] = xg_enqueue_picture(s, cur, true, true);
             if (xg_cuda_check(cudaStreamEndCapture(s->st, &g), "end capture")) return XIN_GPU_ERR_CUDA;
             cudaError_t e = cudaGraphInstantiate(&s->gexec[cur], g, 0);
             cudaGraphDestroy(g);
@@ -347,7 +357,7 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
         if (xg_cuda_check(cudaGraphLaunch(s->gexec[cur], s->st), "graph launch")) return XIN_GPU_ERR_CUDA;
         xg_count_launch((uint64_t)s->graph_launches[cur]);
     } else {
-        xg_count_launch((uint64_t)xg_enqueue_picture(s, cur, with_me));
+        xg_count_launch((uint64_t)xg_enqueue_picture(s, cur, with_me, false));
     }
     cudaEventRecord(s->ev1, s->st);
     if (xg_cuda_check(cudaGetLastError(), "frame_submit")) return XIN_GPU_ERR_CUDA;
@@ -376,7 +386,7 @@ extern "C" int xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32
     s->inflight = 0;
     if (!res) return XIN_GPU_OK;
     float ms = 0;
-    cudaEventElapsedTime(&ms, s->evs[0], s->evs[4]);
+    if (cudaEventElapsedTime(&ms, s->evs[0], s->evs[4]) != cudaSuccess) { cudaGetLastError(); ms = -1.0f; }
     res->gpu_ms = ms;
     const xin_gpu_stream_cfg &c = s->cfg;
     if (c.device_io) return XIN_GPU_OK;

@@ -61,9 +61,12 @@ __global__ void k_qpel_planes(XgPlane ref, XgQpel qp)
  * Grid: (tiles_x, tiles_y, bands).  A CTA takes one 64x64 tile and one band of
  * candidate rows; warp w owns the 16x16 sub-block (w & 3, w >> 2), lane l the
  * l-th candidate of each group of 32 consecutive candidates (raster order of
- * the band).  The reference band sits in shared memory as four byte-shifted
- * copies so that every 4-pixel group of every candidate is one aligned 32-bit
- * word; |a - b| of four pixels is vabsdiff4 and the byte sum dp4a.
+ * the band).  The reference band sits in shared memory as one 32-bit word per
+ * pixel position, word (r, x) holding pixels x .. x+3 of band row r, so the
+ * four pixels at any candidate offset are one aligned word; the row pitch is
+ * congruent to the candidate-row length modulo 32, so the 32 consecutive
+ * candidates of a warp read 32 consecutive banks.  |a - b| of four pixels and
+ * their sum is one vabsdiff4 with add-reduction.
  * Per candidate a warp has the SADs of its four 8x8 blocks and of its 16x16
  * block in registers (running minimum per lane); the 16x16 SADs of 128
  * candidates at a time go to shared memory, from which the 32x32 and 64x64
@@ -128,8 +131,7 @@ struct XgMeParams {
     XgPlane cur, ref;
     int W, H, ctu, R;
     int band_rows;                      /* candidate rows per band */
-    int row_words;                      /* words per reference row per copy */
-    int copy_words;                     /* words per copy (row_words * rows, padded) */
+    int row_words;                      /* words per band row (pitch of the word array) */
     unsigned long long *keys[4];        /* level 0..3 = 64, 32, 16, 8 (NULL = level off) */
     int cus_x[4];                       /* CUs per row of each level */
 };
@@ -143,9 +145,12 @@ __device__ __forceinline__ void xg_cu_window(const XgMeParams &p, int cx, int cy
     y1 = min(p.R, (int)(int16_t)(p.H + (p.ctu - s + 8) - cy));
 }
 
+/* acc + sum over the four bytes of |a - b|: one vabsdiff4 with add-reduction */
 __device__ __forceinline__ uint32_t xg_sad4(uint32_t a, uint32_t b, uint32_t acc)
 {
-    return __dp4a(__vabsdiffu4(a, b), 0x01010101u, acc);
+    uint32_t d;
+    asm("vabsdiff4.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(acc));
+    return d;
 }
 
 #if XG_BITDEPTH == 8
@@ -160,19 +165,18 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     const int ncand = nx * ndy;
     const int rows = XG_ME_TILE + ndy - 1;
 
-    uint32_t *copies = sm;                                   /* [4][copy_words] */
-    uint32_t *mvcx = sm + 4 * p.copy_words;                  /* [nx] */
+    const int relw = nx + 60;                                /* word positions read per band row */
+    uint32_t *refw = sm;                                     /* [rows][row_words] */
+    uint32_t *mvcx = sm + (XG_ME_TILE + p.band_rows - 1) * p.row_words;   /* [nx] */
     uint32_t *mvcy = mvcx + nx;                              /* [band_rows] */
     uint32_t *s16 = mvcy + p.band_rows;                      /* [16][XG_ME_GROUP] */
 
-    /* ---- stage the reference band: pixel (X0 + 4j + s, Y0 + r) -> copies[s][r * row_words + j] */
+    /* ---- stage the reference band: pixels (X0 + x .. X0 + x + 3, Y0 + r) -> refw[r * row_words + x] */
     const int X0 = tx0 - p.R, Y0 = ty0 + dyb0;
-    for (int i = threadIdx.x; i < 4 * rows * p.row_words; i += blockDim.x) {
-        int s = i / (rows * p.row_words), rem = i % (rows * p.row_words);
-        int r = rem / p.row_words, j = rem % p.row_words;
-        const xg_pix *src = p.ref.data + (intptr_t)(Y0 + r) * p.ref.pitch + X0 + 4 * j + s;
-        uint32_t v = (uint32_t)src[0] | ((uint32_t)src[1] << 8) | ((uint32_t)src[2] << 16) | ((uint32_t)src[3] << 24);
-        copies[s * p.copy_words + r * p.row_words + j] = v;
+    for (int i = threadIdx.x; i < rows * relw; i += blockDim.x) {
+        int r = i / relw, x = i - r * relw;
+        const xg_pix *src = p.ref.data + (intptr_t)(Y0 + r) * p.ref.pitch + X0 + x;
+        refw[r * p.row_words + x] = (uint32_t)src[0] | ((uint32_t)src[1] << 8) | ((uint32_t)src[2] << 16) | ((uint32_t)src[3] << 24);
     }
     const uint32_t lambda = pp->lambda;
     for (int i = threadIdx.x; i < nx; i += blockDim.x) mvcx[i] = xg_mvd_bits(4 * (i - p.R)) * lambda;
@@ -220,20 +224,19 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
             bool valid = ci < ncand;
             int cc = valid ? ci : ncand - 1;
             int row = cc / nx, col = cc - row * nx;        /* dy = dyb0 + row, dx = col - R */
-            int rel = bx + col;                             /* x of the block's first pixel relative to X0 */
-            const uint32_t *base = copies + (rel & 3) * p.copy_words + (by + row) * p.row_words + (rel >> 2);
+            const uint32_t *base = refw + (by + row) * p.row_words + bx + col;   /* block origin at this candidate */
             uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
             for (int r = 0; r < 8; r++) {
                 const uint32_t *q = base + r * p.row_words;
-                a0 = xg_sad4(cur[r][0], q[0], a0); a0 = xg_sad4(cur[r][1], q[1], a0);
-                a1 = xg_sad4(cur[r][2], q[2], a1); a1 = xg_sad4(cur[r][3], q[3], a1);
+                a0 = xg_sad4(cur[r][0], q[0], a0); a0 = xg_sad4(cur[r][1], q[4], a0);
+                a1 = xg_sad4(cur[r][2], q[8], a1); a1 = xg_sad4(cur[r][3], q[12], a1);
             }
 #pragma unroll
             for (int r = 8; r < 16; r++) {
                 const uint32_t *q = base + r * p.row_words;
-                a2 = xg_sad4(cur[r][0], q[0], a2); a2 = xg_sad4(cur[r][1], q[1], a2);
-                a3 = xg_sad4(cur[r][2], q[2], a3); a3 = xg_sad4(cur[r][3], q[3], a3);
+                a2 = xg_sad4(cur[r][0], q[0], a2); a2 = xg_sad4(cur[r][1], q[4], a2);
+                a3 = xg_sad4(cur[r][2], q[8], a3); a3 = xg_sad4(cur[r][3], q[12], a3);
             }
             uint32_t sum16 = a0 + a1 + a2 + a3;
             uint32_t mvc = mvcx[col] + mvcy[row];

@@ -242,6 +242,7 @@ __global__ void k_prerdoq(const xg_coef *t, xg_coef *r, xg_coef *q, int w, int h
 #define XG_BEGIN(T)                     \
     XgThread *T = xg_thread();          \
     if (!T) return;                     \
+    (void)cudaGetLastError();           \
     xin_gpu_clear_error();
 #define XG_TRY(expr) do { if (!(expr)) return; } while (0)
 #define XG_ARG(cond, msg) do { if (!(cond)) { xg_set_error(XIN_GPU_ERR_ARG, "%s", msg); return; } } while (0)

@@ -11,3 +11,4 @@
 #include "xg_percall.cuh"
 #include "xg_me_percall.cuh"
 #include "xg_frame.cuh"
+#include "xg_install.cuh"
