@@ -160,6 +160,20 @@ void XinGpuFDct2WxH(XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, int
                     uint32_t width, uint32_t height, XG_COEFF *tempBuf, int32_t shift1st, int32_t shift2nd);
 void XinGpuIDct2WxH(XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, intptr_t outputStride,
                     uint32_t width, uint32_t height, XG_COEFF *tempBuf, int32_t shift1st, int32_t shift2nd);
+/* Allocation-free variant of XinGpuFDct2WxH; no counterpart in the reference.
+ * For callers that cannot call cudaMalloc (a real-time host thread, where
+ * cudaMalloc may synchronise the device; code recording a CUDA graph; a fixed
+ * memory budget): input and output are device pointers, the work is queued on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) and the call returns
+ * without waiting.  The intermediate between the two 1-D passes lives in a
+ * file-scope device array of 64 x 64 coefficients (held by every GPU that loads
+ * the library until exit); larger blocks are rejected with XIN_GPU_ERR_ARG.
+ * The first call on a device looks up that array's device address; make that
+ * first call before any stream capture.  All calls share the array, so calls
+ * that overlap on the GPU race; serialise them.  The current device must be the
+ * one given to xin_gpu_init (XIN_GPU_ERR_STATE otherwise). */
+int  xin_gpu_fdct2_wxh_noalloc(const XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, intptr_t outputStride,
+                               uint32_t width, uint32_t height, int32_t shift1st, int32_t shift2nd, void *stream);
 /* transform skip: replaces Xin26xFSkipWxH (XinFor2dSkip, :217) and Xin266ISkipWxH
  * (XinInv2dSkip, :635; h266_inverse_trans.c:91) */
 void XinGpuFSkipWxH(XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, intptr_t outputStride,

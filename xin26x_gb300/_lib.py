@@ -103,6 +103,7 @@ SIGNATURES = {
     "xin_gpu_stream_device_results": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)], C.c_int),
     "xin_gpu_measure_sad_peak": ([C.POINTER(C.c_double)], C.c_int),
     "xin_gpu_install": ([vp, vp, u32], C.c_int),
+    "xin_gpu_fdct2_wxh_noalloc": ([vp, ip, vp, ip, u32, u32, i32, i32, vp], C.c_int),
 }
 for _n in ["InterpCopy", "InterpCopyU8S16", "LumaInterpHor", "LumaInterpVet", "LumaInterpHorVet", "LumaInterpHorU8S16",
            "LumaInterpVetU8S16", "LumaInterpHorVetU8S16", "LumaInterpVetS16U8", "LumaInterpVetS16S16",

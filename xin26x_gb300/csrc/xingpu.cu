@@ -12,3 +12,4 @@
 #include "xg_me_percall.cuh"
 #include "xg_frame.cuh"
 #include "xg_install.cuh"
+#include "xg_noalloc.cuh"
