@@ -37,7 +37,7 @@ struct xin_gpu_stream {
     cudaEvent_t ev0, ev1;
     cudaEvent_t evs[5];    /* stage boundaries, recorded inside the picture's launches */
     cudaGraphExec_t gexec[2];
-    int me_bands, me_band_rows, me_row_words;
+    int me_bands, me_band_rows, me_band_rows_alloc, me_row_words;
     size_t me_smem;
     int nsub;
     int inflight;          /* a picture with results is queued */
@@ -174,8 +174,10 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     }
     for (;;) {
         s->me_band_rows = (ndy + bands - 1) / bands;
-        int rows = 64 + s->me_band_rows - 1;
-        s->me_smem = sizeof(uint32_t) * ((size_t)rows * s->me_row_words + (2 * R + 1) + s->me_band_rows + 16 * XG_ME_GROUP);
+        int rows_rounded = (s->me_band_rows + 2) / 3 * 3;     /* candidate rows rounded up to the per-lane chunk */
+        s->me_band_rows_alloc = 64 + rows_rounded - 1;
+        s->me_smem = sizeof(uint32_t) * ((size_t)s->me_band_rows_alloc * s->me_row_words + (2 * R + 1) + s->me_band_rows_alloc +
+                                         16 * 96);
         if (s->me_smem <= 200 * 1024 || s->me_band_rows == 1) break;
         bands++;
     }
@@ -239,8 +241,8 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         nl++;
     }
     {
-        dim3 blk(32, 8), grd((c.width + 2 * s->pad - 8 + 31) / 32, (c.height + 2 * s->pad - 8 + 7) / 8, 15);
-        k_qpel_planes<<<grd, blk, 0, st>>>(s->slot[cur][0], s->qpel[cur]);
+        dim3 grd((c.width + 2 * s->pad - 8 + XG_QP_TW - 1) / XG_QP_TW, (c.height + 2 * s->pad - 8 + XG_QP_TH - 1) / XG_QP_TH);
+        k_qpel_planes<<<grd, 256, 0, st>>>(s->slot[cur][0], s->qpel[cur]);
         nl++;
     }
     xg_stage_event(s->evs[1], st, capturing);
@@ -251,7 +253,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         mp.cur = s->slot[cur][0];
         mp.ref = s->slot[ref][0];
         mp.W = c.width; mp.H = c.height; mp.ctu = c.ctu_size; mp.R = c.search_range;
-        mp.band_rows = s->me_band_rows; mp.row_words = s->me_row_words;
+        mp.band_rows = s->me_band_rows; mp.band_rows_alloc = s->me_band_rows_alloc; mp.row_words = s->me_row_words;
         for (int L = 0; L < 4; L++) {
             mp.keys[L] = s->lev_on[L] ? s->keys + s->lev_first[L] : nullptr;
             mp.cus_x[L] = s->lev_cx[L];

@@ -41,20 +41,54 @@ __global__ void k_pad(XgPlane p)
  * for the padded area shrunk by the filter reach (3 before, 4 after). */
 struct XgQpel { xg_pix *plane[16]; int pitch, w, h, pad; };
 
-__global__ void k_qpel_planes(XgPlane ref, XgQpel qp)
+/* A CTA covers a 64 x 16 block of positions for all 15 planes: the reference
+ * tile with the filter reach is staged in shared memory, the horizontal
+ * first-stage values of the three horizontal phases are computed once per row
+ * and shared by the three vertical phases, so every output costs one 8-tap sum. */
+#define XG_QP_TW 64
+#define XG_QP_TH 16
+__global__ void __launch_bounds__(256) k_qpel_planes(XgPlane ref, XgQpel qp)
 {
-    int q = blockIdx.z + 1;
-    int fx = (q & 3) * 4, fy = (q >> 2) * 4;
-    int x = blockIdx.x * blockDim.x + threadIdx.x - (qp.pad - 4);
-    int y = blockIdx.y * blockDim.y + threadIdx.y - (qp.pad - 4);
-    if (x >= qp.w + qp.pad - 4 || y >= qp.h + qp.pad - 4) return;
-    const xg_pix *p = ref.data + (intptr_t)y * ref.pitch + x;
-    const int8_t *th = c_luma_taps[0][fx], *tv = c_luma_taps[0][fy];
-    int v;
-    if (fx && !fy) v = xg_if_pix<8>(p, 1, th);
-    else if (!fx && fy) v = xg_if_pix<8>(p, ref.pitch, tv);
-    else v = xg_if_hv<8, false>(p, ref.pitch, th, tv);
-    qp.plane[q][(intptr_t)y * qp.pitch + x] = (xg_pix)v;
+    __shared__ xg_pix tile[XG_QP_TH + 7][XG_QP_TW + 8];
+    __shared__ int16_t hs[3][XG_QP_TH + 7][XG_QP_TW];
+    const int lo = -(qp.pad - 4);                            /* first output position (x and y) */
+    const int xe = qp.w + qp.pad - 4, ye = qp.h + qp.pad - 4; /* one past the last */
+    const int x0 = lo + (int)blockIdx.x * XG_QP_TW, y0 = lo + (int)blockIdx.y * XG_QP_TH;
+    /* stage rows y0-3 .. y0+TH+3 and columns x0-3 .. x0+TW+4, inside the padded allocation */
+    for (int i = threadIdx.x; i < (XG_QP_TH + 7) * (XG_QP_TW + 7); i += blockDim.x) {
+        int r = i / (XG_QP_TW + 7), c = i % (XG_QP_TW + 7);
+        int gy = y0 - 3 + r, gx = x0 - 3 + c;
+        bool in = gy >= -ref.pad && gy < ref.h + ref.pad && gx >= -ref.pad && gx < ref.w + ref.pad;
+        tile[r][c] = in ? ref.data[(intptr_t)gy * ref.pitch + gx] : (xg_pix)0;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * (XG_QP_TH + 7) * XG_QP_TW; i += blockDim.x) {
+        int f = i / ((XG_QP_TH + 7) * XG_QP_TW), rem = i % ((XG_QP_TH + 7) * XG_QP_TW);
+        int r = rem / XG_QP_TW, c = rem % XG_QP_TW;
+        hs[f][r][c] = xg_if_to_s16<8>(&tile[r][c + 3], 1, c_luma_taps[0][4 * (f + 1)]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 15 * XG_QP_TH * XG_QP_TW; i += blockDim.x) {
+        int q = 1 + i / (XG_QP_TH * XG_QP_TW), rem = i % (XG_QP_TH * XG_QP_TW);
+        int oy = rem / XG_QP_TW, ox = rem % XG_QP_TW;
+        int gx = x0 + ox, gy = y0 + oy;
+        if (gx >= xe || gy >= ye) continue;
+        int fx = (q & 3) * 4, fy = (q >> 2) * 4;
+        int v;
+        if (!fy) {
+            v = xg_if_pix<8>(&tile[oy + 3][ox + 3], 1, c_luma_taps[0][fx]);
+        } else if (!fx) {
+            v = xg_if_pix<8>(&tile[oy + 3][ox + 3], XG_QP_TW + 8, c_luma_taps[0][fy]);
+        } else {
+            const int8_t *tv = c_luma_taps[0][fy];
+            const int f = (fx >> 2) - 1;
+            int sum = 0;
+#pragma unroll
+            for (int k = 0; k < 8; k++) sum += (int)hs[f][oy + k][ox] * (int)tv[k];
+            v = xg_s16_to_pix(sum);
+        }
+        qp.plane[q][(intptr_t)gy * qp.pitch + gx] = (xg_pix)v;
+    }
 }
 
 /* -------------------------------------------------------------- k_me_tiles
@@ -77,7 +111,6 @@ __global__ void k_qpel_planes(XgPlane ref, XgQpel qp)
  * (predictor 0).  8-bit pixels only (10-bit uses k_me_tiles_generic). */
 #define XG_ME_TILE 64
 #define XG_ME_THREADS 512
-#define XG_ME_GROUP 128                 /* candidates per shared-memory phase */
 
 /* per-picture values, read from device memory so one captured graph serves
  * every picture of a stream */
@@ -131,6 +164,7 @@ struct XgMeParams {
     XgPlane cur, ref;
     int W, H, ctu, R;
     int band_rows;                      /* candidate rows per band */
+    int band_rows_alloc;                /* staged band rows: 64 + band_rows rounded up to XG_ME_D, minus 1 */
     int row_words;                      /* words per band row (pitch of the word array) */
     unsigned long long *keys[4];        /* level 0..3 = 64, 32, 16, 8 (NULL = level off) */
     int cus_x[4];                       /* CUs per row of each level */
@@ -154,22 +188,28 @@ __device__ __forceinline__ uint32_t xg_sad4(uint32_t a, uint32_t b, uint32_t acc
 }
 
 #if XG_BITDEPTH == 8
+#define XG_ME_D 3                         /* candidate rows per lane and pass */
+#define XG_ME_SLOTS (32 * XG_ME_D)        /* candidates per warp and pass */
 __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, const XgPicParams *pp)
 {
     extern __shared__ uint32_t sm[];
+    __shared__ int swin[16][5][4];        /* per warp: windows of its four 8x8 CUs and its 16x16 CU */
+    __shared__ int swin32[4][4], swin64[4];
+    __shared__ int sinterior[16];
     const int tx0 = blockIdx.x * XG_ME_TILE, ty0 = blockIdx.y * XG_ME_TILE;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nx = 2 * p.R + 1;
     const int dyb0 = -p.R + (int)blockIdx.z * p.band_rows;
     const int ndy = min(p.band_rows, p.R - dyb0 + 1);
-    const int ncand = nx * ndy;
-    const int rows = XG_ME_TILE + ndy - 1;
+    const int nch = (ndy + XG_ME_D - 1) / XG_ME_D;          /* chunks of XG_ME_D candidate rows */
+    const int nv = nch * nx;                                 /* (chunk, column) slots, one per lane and pass */
+    const int rows = XG_ME_TILE + nch * XG_ME_D - 1;         /* band rows staged */
 
     const int relw = nx + 60;                                /* word positions read per band row */
     uint32_t *refw = sm;                                     /* [rows][row_words] */
-    uint32_t *mvcx = sm + (XG_ME_TILE + p.band_rows - 1) * p.row_words;   /* [nx] */
-    uint32_t *mvcy = mvcx + nx;                              /* [band_rows] */
-    uint32_t *s16 = mvcy + p.band_rows;                      /* [16][XG_ME_GROUP] */
+    uint32_t *mvcx = sm + (size_t)p.band_rows_alloc * p.row_words;   /* [nx] */
+    uint32_t *mvcy = mvcx + nx;                              /* [band_rows rounded to XG_ME_D] */
+    uint32_t *s16 = mvcy + p.band_rows_alloc;                /* [16][XG_ME_SLOTS] */
 
     /* ---- stage the reference band: pixels (X0 + x .. X0 + x + 3, Y0 + r) -> refw[r * row_words + x] */
     const int X0 = tx0 - p.R, Y0 = ty0 + dyb0;
@@ -180,7 +220,7 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     }
     const uint32_t lambda = pp->lambda;
     for (int i = threadIdx.x; i < nx; i += blockDim.x) mvcx[i] = xg_mvd_bits(4 * (i - p.R)) * lambda;
-    for (int i = threadIdx.x; i < ndy; i += blockDim.x) mvcy[i] = xg_mvd_bits(4 * (dyb0 + i)) * lambda;
+    for (int i = threadIdx.x; i < nch * XG_ME_D; i += blockDim.x) mvcy[i] = xg_mvd_bits(4 * (dyb0 + i)) * lambda;
 
     /* ---- this warp's 16x16 block of the current picture in registers */
     const int bx = (warp & 3) * 16, by = (warp >> 2) * 16;
@@ -193,8 +233,7 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
             cur[r][k] = (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16) | ((uint32_t)c[3] << 24);
         }
 
-    /* ---- per-lane running bests of the four 8x8 CUs and the 16x16 CU */
-    int win[5][4];
+    /* ---- windows and liveness of this warp's CUs; a band inside every window needs no per-candidate check */
     bool live[5];
     uint32_t best[5], bidx[5];
 #pragma unroll
@@ -202,75 +241,106 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
         int s = c < 4 ? 8 : 16;
         int cx = tx0 + bx + (c < 4 ? (c & 1) * 8 : 0), cy = ty0 + by + (c < 4 ? (c >> 1) * 8 : 0);
         live[c] = p.keys[c < 4 ? 3 : 2] && cx + s <= p.W && cy + s <= p.H;
-        xg_cu_window(p, cx, cy, s, win[c][0], win[c][1], win[c][2], win[c][3]);
+        if (lane == 0) xg_cu_window(p, cx, cy, s, swin[warp][c][0], swin[warp][c][1], swin[warp][c][2], swin[warp][c][3]);
         best[c] = 0xFFFFFFFFu; bidx[c] = 0xFFFFFFFFu;
     }
-    /* 32x32 and 64x64 bookkeeping: thread t < 512 handles (cu32 = t >> 7, slot t & 127); t < 128 also the 64x64 */
-    const int c32 = threadIdx.x >> 7, slot = threadIdx.x & 127;
+    if (threadIdx.x < 4) {
+        int c32x = tx0 + (threadIdx.x & 1) * 32, c32y = ty0 + (threadIdx.x >> 1) * 32;
+        xg_cu_window(p, c32x, c32y, 32, swin32[threadIdx.x][0], swin32[threadIdx.x][1], swin32[threadIdx.x][2], swin32[threadIdx.x][3]);
+    }
+    if (threadIdx.x == 0) xg_cu_window(p, tx0, ty0, 64, swin64[0], swin64[1], swin64[2], swin64[3]);
+    __syncwarp();
+    if (lane == 0) {
+        bool in = true;
+        for (int c = 0; c < 5; c++)
+            in = in && swin[warp][c][0] <= -p.R && swin[warp][c][1] >= p.R && swin[warp][c][2] <= dyb0 && swin[warp][c][3] >= dyb0 + ndy - 1;
+        sinterior[warp] = in;
+    }
+    /* 32x32 and 64x64 bookkeeping: thread t < 4 * XG_ME_SLOTS handles (cu32 = t / XG_ME_SLOTS, slot);
+     * t < XG_ME_SLOTS also the 64x64 */
+    const int c32 = threadIdx.x / XG_ME_SLOTS, slot = threadIdx.x % XG_ME_SLOTS;
     const int c32x = tx0 + (c32 & 1) * 32, c32y = ty0 + (c32 >> 1) * 32;
-    const bool live32 = p.keys[1] && c32x + 32 <= p.W && c32y + 32 <= p.H;
-    const bool live64 = threadIdx.x < 128 && p.keys[0] && tx0 + 64 <= p.W && ty0 + 64 <= p.H;
-    int w32[4], w64[4];
-    xg_cu_window(p, c32x, c32y, 32, w32[0], w32[1], w32[2], w32[3]);
-    xg_cu_window(p, tx0, ty0, 64, w64[0], w64[1], w64[2], w64[3]);
+    const bool live32 = c32 < 4 && p.keys[1] && c32x + 32 <= p.W && c32y + 32 <= p.H;
+    const bool live64 = threadIdx.x < XG_ME_SLOTS && p.keys[0] && tx0 + 64 <= p.W && ty0 + 64 <= p.H;
     uint32_t best32 = 0xFFFFFFFFu, bidx32 = 0xFFFFFFFFu, best64 = 0xFFFFFFFFu, bidx64 = 0xFFFFFFFFu;
     __syncthreads();
+    const bool interior = sinterior[warp];
 
-    const int ngroups = (ncand + XG_ME_GROUP - 1) / XG_ME_GROUP;
-    for (int g = 0; g < ngroups; g++) {
-#pragma unroll 1
-        for (int ch = 0; ch < XG_ME_GROUP / 32; ch++) {
-            int ci = g * XG_ME_GROUP + ch * 32 + lane;
-            bool valid = ci < ncand;
-            int cc = valid ? ci : ncand - 1;
-            int row = cc / nx, col = cc - row * nx;        /* dy = dyb0 + row, dx = col - R */
-            const uint32_t *base = refw + (by + row) * p.row_words + bx + col;   /* block origin at this candidate */
-            uint32_t a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    const int npass = (nv + 31) / 32;
+    for (int pz = 0; pz < npass; pz++) {
+        {
+            const int v = pz * 32 + lane;
+            const bool vvalid = v < nv;
+            const int vv = vvalid ? v : nv - 1;
+            const int chunk = vv / nx, col = vv - chunk * nx;
+            const int row0 = chunk * XG_ME_D;
+            const uint32_t *base = refw + (by + row0) * p.row_words + bx + col;
+            uint32_t acc[XG_ME_D][4];
 #pragma unroll
-            for (int r = 0; r < 8; r++) {
-                const uint32_t *q = base + r * p.row_words;
-                a0 = xg_sad4(cur[r][0], q[0], a0); a0 = xg_sad4(cur[r][1], q[4], a0);
-                a1 = xg_sad4(cur[r][2], q[8], a1); a1 = xg_sad4(cur[r][3], q[12], a1);
-            }
+            for (int d = 0; d < XG_ME_D; d++)
 #pragma unroll
-            for (int r = 8; r < 16; r++) {
-                const uint32_t *q = base + r * p.row_words;
-                a2 = xg_sad4(cur[r][0], q[0], a2); a2 = xg_sad4(cur[r][1], q[4], a2);
-                a3 = xg_sad4(cur[r][2], q[8], a3); a3 = xg_sad4(cur[r][3], q[12], a3);
-            }
-            uint32_t sum16 = a0 + a1 + a2 + a3;
-            uint32_t mvc = mvcx[col] + mvcy[row];
-            int dx = col - p.R, dy = dyb0 + row;
-            uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
-            uint32_t sads[5] = { a0, a1, a2, a3, sum16 };
+                for (int b = 0; b < 4; b++) acc[d][b] = 0;
+            /* reference row t of the block feeds current row t - d of candidate row d */
 #pragma unroll
-            for (int c = 0; c < 5; c++) {
-                uint32_t cost = (sads[c] << XG_COST_FRACTION) + mvc;
-                bool ok = valid && live[c] && dx >= win[c][0] && dx <= win[c][1] && dy >= win[c][2] && dy <= win[c][3];
-                if (ok && cost < best[c]) { best[c] = cost; bidx[c] = gidx; }
+            for (int t = 0; t < 16 + XG_ME_D - 1; t++) {
+                const uint32_t *q = base + t * p.row_words;
+                const uint32_t w0 = q[0], w1 = q[4], w2 = q[8], w3 = q[12];
+#pragma unroll
+                for (int d = 0; d < XG_ME_D; d++) {
+                    const int r = t - d;
+                    if (r >= 0 && r < 16) {
+                        const int b = r < 8 ? 0 : 2;
+                        acc[d][b] = xg_sad4(cur[r][0], w0, acc[d][b]);
+                        acc[d][b] = xg_sad4(cur[r][1], w1, acc[d][b]);
+                        acc[d][b + 1] = xg_sad4(cur[r][2], w2, acc[d][b + 1]);
+                        acc[d][b + 1] = xg_sad4(cur[r][3], w3, acc[d][b + 1]);
+                    }
+                }
             }
-            s16[warp * XG_ME_GROUP + ch * 32 + lane] = sum16;
+            const int dx = col - p.R;
+#pragma unroll
+            for (int d = 0; d < XG_ME_D; d++) {
+                const int row = row0 + d, dy = dyb0 + row;
+                const bool valid = vvalid && row < ndy;
+                const uint32_t sum16 = acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
+                const uint32_t mvc = mvcx[col] + mvcy[row];
+                const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
+                const uint32_t sads[5] = { acc[d][0], acc[d][1], acc[d][2], acc[d][3], sum16 };
+#pragma unroll
+                for (int c = 0; c < 5; c++) {
+                    const uint32_t cost = (sads[c] << XG_COST_FRACTION) + mvc;
+                    bool ok = valid && live[c];
+                    if (!interior)
+                        ok = ok && dx >= swin[warp][c][0] && dx <= swin[warp][c][1] && dy >= swin[warp][c][2] && dy <= swin[warp][c][3];
+                    /* a lane's candidates are not visited in raster order: compare (cost, raster index) */
+                    if (ok && (cost < best[c] || (cost == best[c] && gidx < bidx[c]))) { best[c] = cost; bidx[c] = gidx; }
+                }
+                s16[warp * XG_ME_SLOTS + d * 32 + lane] = sum16;
+            }
         }
         __syncthreads();
-        {
-            int ci = g * XG_ME_GROUP + slot;
-            if (ci < ncand) {
-                int row = ci / nx, col = ci - row * nx;
-                int dx = col - p.R, dy = dyb0 + row;
-                uint32_t mvc = mvcx[col] + mvcy[row];
-                uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
+        if (c32 < 4) {
+            const int d = slot / 32, v = pz * 32 + (slot & 31);
+            const int vv = v < nv ? v : nv - 1;
+            const int chunk = vv / nx, col = vv - chunk * nx, row = chunk * XG_ME_D + d;
+            if (v < nv && row < ndy) {
+                const int dx = col - p.R, dy = dyb0 + row;
+                const uint32_t mvc = mvcx[col] + mvcy[row];
+                const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
                 /* warps of the 32x32 quadrant c32: (2*(c32&1) + {0,1}) + 4*(2*(c32>>1) + {0,1}) */
-                int w0 = (c32 & 1) * 2 + (c32 >> 1) * 8;
-                uint32_t s32 = s16[w0 * XG_ME_GROUP + slot] + s16[(w0 + 1) * XG_ME_GROUP + slot] +
-                               s16[(w0 + 4) * XG_ME_GROUP + slot] + s16[(w0 + 5) * XG_ME_GROUP + slot];
-                uint32_t cost = (s32 << XG_COST_FRACTION) + mvc;
-                if (live32 && dx >= w32[0] && dx <= w32[1] && dy >= w32[2] && dy <= w32[3] && cost < best32) { best32 = cost; bidx32 = gidx; }
+                const int w0 = (c32 & 1) * 2 + (c32 >> 1) * 8;
+                const uint32_t s32 = s16[w0 * XG_ME_SLOTS + slot] + s16[(w0 + 1) * XG_ME_SLOTS + slot] +
+                                     s16[(w0 + 4) * XG_ME_SLOTS + slot] + s16[(w0 + 5) * XG_ME_SLOTS + slot];
+                const uint32_t cost = (s32 << XG_COST_FRACTION) + mvc;
+                if (live32 && dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3] &&
+                    (cost < best32 || (cost == best32 && gidx < bidx32))) { best32 = cost; bidx32 = gidx; }
                 if (live64) {
                     uint32_t s64 = 0;
 #pragma unroll
-                    for (int w = 0; w < 16; w++) s64 += s16[w * XG_ME_GROUP + slot];
-                    uint32_t c64 = (s64 << XG_COST_FRACTION) + mvc;
-                    if (dx >= w64[0] && dx <= w64[1] && dy >= w64[2] && dy <= w64[3] && c64 < best64) { best64 = c64; bidx64 = gidx; }
+                    for (int w = 0; w < 16; w++) s64 += s16[w * XG_ME_SLOTS + slot];
+                    const uint32_t c64 = (s64 << XG_COST_FRACTION) + mvc;
+                    if (dx >= swin64[0] && dx <= swin64[1] && dy >= swin64[2] && dy <= swin64[3] &&
+                        (c64 < best64 || (c64 == best64 && gidx < bidx64))) { best64 = c64; bidx64 = gidx; }
                 }
             }
         }
@@ -350,80 +420,111 @@ struct XgTailParams {
     xin_gpu_cu_result *res;           /* all CUs */
 };
 
-/* forward 2-D DCT2 of an n x n residual in shared memory, keeping the outputs
- * below 32 in each direction (the rest is zeroed out downstream), then quant /
- * dequant with 4x4 coding groups over the low min(n, 32) square */
-template <int N, int NT>
-__device__ void xg_tq_block(const int *res, int *coef, int *rr, const XgQuant &qz, int s1, int s2, unsigned long long *nz,
-                            xg_coef *qout, int qpitch, int16_t *tmp)
+/* C(i, j) = sum_l A(i, l) * B(j, l) over shared-memory operands with
+ * A(i, l) = A[i * asi + l * asl] and B(j, l) = B[j * bsj + l * bsl].  Each
+ * thread owns a TI x TJ tile of outputs, consecutive threads consecutive j
+ * tiles, so B is read along its contiguous dimension and A is broadcast;
+ * epi(i, j, acc) consumes every output. */
+__host__ __device__ constexpr int xg_tile_j(int ni, int nj, int nt) { return (ni * nj >= 8 * nt && nj >= 64) ? 4 : ((ni * nj >= 2 * nt && nj >= 32) ? 2 : 1); }
+__host__ __device__ constexpr int xg_tile_i(int ni, int nj, int nt)
 {
-    constexpr int LG = N == 4 ? 2 : N == 8 ? 3 : N == 16 ? 4 : N == 32 ? 5 : 6;
-    constexpr int K = N > 32 ? 32 : N;
-    const int16_t *m = xg_mat(0, LG);
-    /* pass 1 (rows): tmp[k * N + i] = row i, frequency k */
-    for (int o = threadIdx.x; o < K * N; o += NT) {
-        int k = o / N, i = o % N;
-        int s = 0;
+    return (ni * nj / (nt * xg_tile_j(ni, nj, nt)) >= 4) ? 4 : ((ni * nj / (nt * xg_tile_j(ni, nj, nt)) >= 2) ? 2 : 1);
+}
+
+template <int NI, int NJ, int NL, int NT, typename TA, typename TB, typename F>
+__device__ __forceinline__ void xg_mm(const TA *A, int asi, int asl, const TB *B, int bsj, int bsl, F epi)
+{
+    constexpr int TJ = xg_tile_j(NI, NJ, NT), TI = xg_tile_i(NI, NJ, NT);
+    constexpr int tj = NJ / TJ, tiles = (NI / TI) * tj;
+    for (int t = threadIdx.x; t < tiles; t += NT) {
+        const int i0 = (t / tj) * TI, j0 = (t % tj) * TJ;
+        int acc[TI][TJ];
+#pragma unroll
+        for (int a = 0; a < TI; a++)
+#pragma unroll
+            for (int b = 0; b < TJ; b++) acc[a][b] = 0;
+        const TA *pa = A + i0 * asi;
+        const TB *pb = B + j0 * bsj;
 #pragma unroll 8
-        for (int j = 0; j < N; j++) s += (int)m[k * N + j] * res[i * N + j];
-        tmp[k * N + i] = (int16_t)xg_clip16(xg_rshift_rnd(s, s1));
-    }
-    __syncthreads();
-    /* pass 2 (columns): coef[kv * K + kh] */
-    for (int o = threadIdx.x; o < K * K; o += NT) {
-        int kv = o / K, kh = o % K;
-        int s = 0;
-#pragma unroll 8
-        for (int i = 0; i < N; i++) s += (int)m[kv * N + i] * (int)tmp[kh * N + i];
-        int t = xg_clip16(xg_rshift_rnd(s, s2));
-        int a = abs(t);
-        int qv = (int)(((long long)a * qz.qmult + qz.qadd) >> qz.qshift);
-        qv = xg_clip16(t < 0 ? -qv : qv);
-        int rv = xg_clip16((int)(((long long)qv * qz.iqmult + qz.iqadd) >> qz.iqshift));
-        coef[o] = qv;
-        rr[o] = rv;
-        if (qv) atomicOr(nz, 1ull << ((kv >> 2) * (K >> 2) + (kh >> 2)));
-    }
-    __syncthreads();
-    for (int o = threadIdx.x; o < N * N; o += NT) {
-        int y = o / N, x = o % N;
-        qout[(intptr_t)y * qpitch + x] = (xg_coef)((y < K && x < K) ? coef[y * K + x] : 0);
+        for (int l = 0; l < NL; l++) {
+            int av[TI], bv[TJ];
+#pragma unroll
+            for (int a = 0; a < TI; a++) av[a] = pa[a * asi + l * asl];
+#pragma unroll
+            for (int b = 0; b < TJ; b++) bv[b] = pb[b * bsj + l * bsl];
+#pragma unroll
+            for (int a = 0; a < TI; a++)
+#pragma unroll
+                for (int b = 0; b < TJ; b++) acc[a][b] += av[a] * bv[b];
+        }
+#pragma unroll
+        for (int a = 0; a < TI; a++)
+#pragma unroll
+            for (int b = 0; b < TJ; b++) epi(i0 + a, j0 + b, acc[a][b]);
     }
 }
 
-/* inverse 2-D DCT2 of the dequantised K x K low part (zero elsewhere), columns
- * first with lines >= 32 skipped (Xin266IDct2WxH), then rows; adds the
- * prediction, clips, writes the reconstruction and accumulates the SSD */
+/* Shared-memory work area of one N x N transform block (K = min(N, 32) kept frequencies). */
+template <int N>
+struct XgTqSmem {
+    static constexpr int K = N > 32 ? 32 : N;
+    int16_t mat[K * N];          /* DCT2 rows k < K (row = basis function) */
+    int16_t resT[N * N];         /* residual, transposed: resT[x * N + y] */
+    int16_t t1T[N * K];          /* first forward pass, t1T[i * K + k] (row i, frequency k) */
+    int16_t rr[K * K];           /* dequantised coefficients rr[kv * K + kh] */
+    xg_coef qs[K * K];           /* quantised coefficients */
+    int16_t t2[K * N];           /* first inverse pass t2[j * N + x] */
+};
+
+/* forward DCT2 (rows, then columns), keeping frequencies below 32 (the rest is
+ * zeroed out), quant / dequant over the low min(N, 32) square with 4x4 coding
+ * groups (Xin266QuantInvQuant, h266_quant_inv_quant.c:27-139), coefficient plane
+ * written with zeros beyond 32 */
 template <int N, int NT>
-__device__ void xg_itq_block(const int *rr, const xg_pix *pred, const xg_pix *org, int opitch, xg_pix *rec, int rpitch,
-                             int16_t *tmp, unsigned long long *ssd)
+__device__ void xg_tq(XgTqSmem<N> &sm, const XgQuant &qz, int s1, int s2, unsigned long long *nz, xg_coef *qout, int qpitch)
 {
-    constexpr int LG = N == 4 ? 2 : N == 8 ? 3 : N == 16 ? 4 : N == 32 ? 5 : 6;
-    constexpr int K = N > 32 ? 32 : N;
-    const int16_t *m = xg_mat(0, LG);
-    const int s2 = 6 + 15 - 1 - XG_BITDEPTH;
-    /* pass 1: column j < K (lines j >= 32 are zero): tmp[j * N + x] */
-    for (int o = threadIdx.x; o < K * N; o += NT) {
-        int j = o / N, x = o % N;
-        int s = 0;
-#pragma unroll 8
-        for (int k = 0; k < K; k++) s += (int)m[k * N + x] * rr[k * K + j];
-        tmp[j * N + x] = (int16_t)xg_clip16(xg_rshift_rnd(s, 7));
-    }
+    constexpr int K = XgTqSmem<N>::K;
+    xg_mm<K, N, N, NT>(sm.mat, N, 1, sm.resT, 1, N, [&](int k, int i, int acc) {
+        sm.t1T[i * K + k] = (int16_t)xg_clip16(xg_rshift_rnd(acc, s1));
+    });
     __syncthreads();
-    unsigned long long acc = 0;
+    xg_mm<K, K, N, NT>(sm.mat, N, 1, sm.t1T, 1, K, [&](int kv, int kh, int acc) {
+        int t = xg_clip16(xg_rshift_rnd(acc, s2));
+        int a = abs(t);
+        int qv = (int)(((long long)a * qz.qmult + qz.qadd) >> qz.qshift);
+        qv = xg_clip16(t < 0 ? -qv : qv);
+        sm.qs[kv * K + kh] = (xg_coef)qv;
+        sm.rr[kv * K + kh] = (int16_t)xg_clip16((int)(((long long)qv * qz.iqmult + qz.iqadd) >> qz.iqshift));
+        if (qv) atomicOr(nz, 1ull << ((kv >> 2) * (K >> 2) + (kh >> 2)));
+    });
+    __syncthreads();
     for (int o = threadIdx.x; o < N * N; o += NT) {
         int y = o / N, x = o % N;
-        int s = 0;
-#pragma unroll 8
-        for (int j = 0; j < K; j++) s += (int)m[j * N + x] * (int)tmp[j * N + y];
-        int resid = xg_clip16(xg_rshift_rnd(s, s2));
-        int v = xg_clip_pix((int)pred[o] + resid);
+        qout[(intptr_t)y * qpitch + x] = (y < K && x < K) ? sm.qs[y * K + x] : (xg_coef)0;
+    }
+}
+
+/* inverse DCT2 of the dequantised low K x K part (zero elsewhere): columns
+ * first, lines >= 32 skipped (Xin266IDct2WxH), then rows; adds the prediction,
+ * clips, writes the reconstruction and accumulates the SSD */
+template <int N, int NT>
+__device__ void xg_itq(XgTqSmem<N> &sm, const xg_pix *pred, const xg_pix *org, int opitch, xg_pix *rec, int rpitch,
+                       unsigned long long *ssd)
+{
+    constexpr int K = XgTqSmem<N>::K;
+    const int s2 = 6 + 15 - 1 - XG_BITDEPTH;
+    xg_mm<K, N, K, NT>(sm.rr, 1, K, sm.mat, 1, N, [&](int j, int x, int acc) {
+        sm.t2[j * N + x] = (int16_t)xg_clip16(xg_rshift_rnd(acc, 7));
+    });
+    __syncthreads();
+    unsigned long long part = 0;
+    xg_mm<N, N, K, NT>(sm.t2, 1, N, sm.mat, 1, N, [&](int y, int x, int acc) {
+        int v = xg_clip_pix((int)pred[y * N + x] + xg_clip16(xg_rshift_rnd(acc, s2)));
         rec[(intptr_t)y * rpitch + x] = (xg_pix)v;
         int d = (int)org[(intptr_t)y * opitch + x] - v;
-        acc += (unsigned long long)(d * d);
-    }
-    atomicAdd(ssd, acc);
+        part += (unsigned long long)(d * d);
+    });
+    atomicAdd(ssd, part);
     __syncthreads();
 }
 
@@ -432,10 +533,8 @@ template <int S, int NT>
 __global__ void __launch_bounds__(NT) k_cu_tail(XgTailParams p, const XgPicParams *pp)
 {
     constexpr int C = S / 2;
-    __shared__ int res[S * S];
-    __shared__ int coef[(S > 32 ? 32 : S) * (S > 32 ? 32 : S)];
-    __shared__ int rr[(S > 32 ? 32 : S) * (S > 32 ? 32 : S)];
-    __shared__ int16_t tmp[S * S];
+    __shared__ XgTqSmem<S> tl;
+    __shared__ XgTqSmem<C> tc;
     __shared__ xg_pix pred[S * S];
     __shared__ uint32_t part[8][NT / 32];
     __shared__ int bmv[3];
@@ -449,6 +548,12 @@ __global__ void __launch_bounds__(NT) k_cu_tail(XgTailParams p, const XgPicParam
     const int gidx = (int)(uint32_t)key;
     const int imx = gidx % nx - p.R, imy = gidx / nx - p.R;
     if (threadIdx.x < 3) { nz[threadIdx.x] = 0; ssd[threadIdx.x] = 0; }
+    {   /* DCT2 matrices of the luma (S) and chroma (S/2) blocks, rows k < 32 */
+        constexpr int lgs = S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : 6;
+        const int16_t *ml = xg_mat(0, lgs), *mc = xg_mat(0, lgs - 1);
+        for (int i = threadIdx.x; i < XgTqSmem<S>::K * S; i += NT) tl.mat[i] = ml[i];
+        for (int i = threadIdx.x; i < XgTqSmem<C>::K * C; i += NT) tc.mat[i] = mc[i];
+    }
     if (threadIdx.x == 0) { bmv[0] = 4 * imx; bmv[1] = 4 * imy; bmv[2] = (int)(uint32_t)(key >> 32); }
 
     /* window (h266_enc_init.c:1462) */
@@ -516,11 +621,13 @@ __global__ void __launch_bounds__(NT) k_cu_tail(XgTailParams p, const XgPicParam
 
     /* ---- luma TQ + reconstruction */
     const int lgS = S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : 6;
-    for (int i = threadIdx.x; i < S * S; i += NT) res[i] = (int)org[(intptr_t)(i / S) * p.cur[0].pitch + i % S] - (int)pred[i];
+    for (int i = threadIdx.x; i < S * S; i += NT) {
+        int y = i / S, x = i % S;
+        tl.resT[x * S + y] = (int16_t)((int)org[(intptr_t)y * p.cur[0].pitch + x] - (int)pred[i]);
+    }
     __syncthreads();
-    xg_tq_block<S, NT>(res, coef, rr, pp->quant[p.level][0], lgS + XG_BITDEPTH + 6 - 15, lgS + 6, &nz[0],
-                       p.q[0] + (intptr_t)cy * p.W + cx, p.W, tmp);
-    xg_itq_block<S, NT>(rr, pred, org, p.cur[0].pitch, p.rec[0] + (intptr_t)cy * p.W + cx, p.W, tmp, &ssd[0]);
+    xg_tq<S, NT>(tl, pp->quant[p.level][0], lgS + XG_BITDEPTH + 6 - 15, lgS + 6, &nz[0], p.q[0] + (intptr_t)cy * p.W + cx, p.W);
+    xg_itq<S, NT>(tl, pred, org, p.cur[0].pitch, p.rec[0] + (intptr_t)cy * p.W + cx, p.W, &ssd[0]);
 
     /* ---- chroma: uni branch of Xin266ChromaMotionComp (1/32 phase, mask 31), TQ, reconstruction */
     {
@@ -545,12 +652,14 @@ __global__ void __launch_bounds__(NT) k_cu_tail(XgTailParams p, const XgPicParam
             }
             __syncthreads();
             const xg_pix *corg = p.cur[pl].data + (intptr_t)(cy >> 1) * p.cur[pl].pitch + (cx >> 1);
-            for (int i = threadIdx.x; i < C * C; i += NT) res[i] = (int)corg[(intptr_t)(i / C) * p.cur[pl].pitch + i % C] - (int)pred[i];
+            for (int i = threadIdx.x; i < C * C; i += NT) {
+                int y = i / C, x = i % C;
+                tc.resT[x * C + y] = (int16_t)((int)corg[(intptr_t)y * p.cur[pl].pitch + x] - (int)pred[i]);
+            }
             __syncthreads();
-            xg_tq_block<C, NT>(res, coef, rr, pp->quant[p.level][pl], lgC + XG_BITDEPTH + 6 - 15, lgC + 6, &nz[pl],
-                               p.q[pl] + (intptr_t)(cy >> 1) * W2 + (cx >> 1), W2, tmp);
-            xg_itq_block<C, NT>(rr, pred, corg, p.cur[pl].pitch, p.rec[pl] + (intptr_t)(cy >> 1) * W2 + (cx >> 1), W2, tmp,
-                                &ssd[pl]);
+            xg_tq<C, NT>(tc, pp->quant[p.level][pl], lgC + XG_BITDEPTH + 6 - 15, lgC + 6, &nz[pl],
+                         p.q[pl] + (intptr_t)(cy >> 1) * W2 + (cx >> 1), W2);
+            xg_itq<C, NT>(tc, pred, corg, p.cur[pl].pitch, p.rec[pl] + (intptr_t)(cy >> 1) * W2 + (cx >> 1), W2, &ssd[pl]);
         }
     }
     __syncthreads();
