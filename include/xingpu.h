@@ -201,6 +201,37 @@ void XinGpuPreRdoq(XG_COEFF *tCoeff, XG_COEFF *rCoeff, XG_COEFF *qCoeff, intptr_
                    uint32_t width, uint32_t height, uint32_t cGWidth, uint32_t cGHeight, int32_t rdoqThrVal,
                    xin_gpu_scan_pos *scanOrderCG, uint64_t *nzCGBitMapRs);
 
+/* ------------------------------------------------ batched transform / quant
+ * Many residual blocks of mixed sizes and transform types in one call: per
+ * block the TU arithmetic of Xin266Transform (h266_encoder/source/h266_trans_quant.c:61;
+ * forward DCT2 / DST7 / DCT8 / skip by MTS index with the implicit-MTS rule of
+ * h266_forward_trans.c:75-86, zero-out beyond 32, quant / dequant with 4x4
+ * coding groups, no dependent quantisation or pre-RDOQ) followed by
+ * Xin266IDctWxH (h266_inverse_trans.c:117).  Block b reads resid[offset ..
+ * offset + w*h) (row-major, stride w) and writes q, r (dequantised) and
+ * resid_out (inverse-transformed r) at the same offsets, nz[b] = non-zero-CG map.
+ * tile: -1 autotune the thread-group size per block-size class (timed on the
+ * first call for each class, then cached), 0 fixed heuristic, or 32/64/128/256. */
+typedef struct xin_gpu_tq_block {
+    uint32_t offset;            /* element offset of the block in every array */
+    uint8_t  log2w, log2h;      /* 2..6 (skip, DST7 / DCT8: 2..5) */
+    uint8_t  mts;               /* 0 DCT2, 1 transform skip, 2 DST7/DST7, 3 DCT8/DST7, 4 DST7/DCT8, 5 DCT8/DCT8 */
+    uint8_t  flags;             /* XIN_GPU_TQ_* */
+    int32_t  qp;                /* slice QP 0..63 (the 10-bit build adds 12 internally) */
+} xin_gpu_tq_block;
+#define XIN_GPU_TQ_INTRA_CU     1u   /* intra CU: implicit MTS for luma DCT2 when MTS is enabled */
+#define XIN_GPU_TQ_CHROMA       2u
+#define XIN_GPU_TQ_RDOQ_ROUND   4u   /* qAdd = 1 << (qShift - 1) (RDOQ enabled) */
+#define XIN_GPU_TQ_INTRA_PIC    8u   /* qAdd = 171 << (qShift - 9) instead of 85 << (qShift - 9) */
+#define XIN_GPU_TQ_MTS_ENABLED 16u
+int  xin_gpu_tq_batch(const xin_gpu_tq_block *blocks, int32_t nblocks, const XG_COEFF *resid, XG_COEFF *q, XG_COEFF *r,
+                      XG_COEFF *resid_out, uint64_t *nz, size_t ncoeffs, int32_t tile);
+/* the same on device arrays (blocks stay a host array); tiles_used (optional,
+ * 49 entries indexed log2w * 7 + log2h) reports the group size of each class */
+int  xin_gpu_tq_batch_device(const xin_gpu_tq_block *blocks, int32_t nblocks, const XG_COEFF *resid, XG_COEFF *q,
+                             XG_COEFF *r, XG_COEFF *resid_out, uint64_t *nz, size_t ncoeffs, int32_t tile, void *stream,
+                             int32_t *tiles_used);
+
 /* ------------------------------------------------------- motion search (a7-a8)
  * xin_me_struct is the reference's ME state (h26x_core/include/h26x_me_struct.h:60-131);
  * xingpu_me.h mirrors its layout.  Pass a pointer to the reference's struct.

@@ -111,6 +111,8 @@ _SIGS = {
     "quant_params": ("orc_quant_params", None, [i32, u32, u32, u32, C.c_int, C.c_int, C.POINTER(orc_qparams)]),
     "transform_tu": ("orc_transform_tu", None, [vp, ip, vp, ip, vp, vp, vp, ip, u32, u32, u32, u32, i32, C.c_int, C.c_int,
                                                 C.c_int, C.c_int, vp]),
+    "tq_block": ("orc_tq_block", None, [vp, ip, u32, u32, u32, u32, i32, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        vp, vp, vp, ip, vp]),
     "mvd_bits": ("orc_mvd_bits", None, [i32]),
     "mv_window": ("orc_mv_window", None, [i32] * 7 + [C.POINTER(i32)] * 4),
     "me_full": ("orc_me_full", None, [vp, ip, vp, ip, u32, u32, i32, i32, i32, u32, i32, i32, i32, i32, C.POINTER(orc_me_io)]),

@@ -756,6 +756,30 @@ void orc_transform_tu(const opix *in, intptr_t is, const opix *pred, intptr_t ps
                         p.iqmult, p.iqadd, p.iqshift, nz);
 }
 
+void orc_tq_block(const ocoef *res, intptr_t rs, uint32_t w, uint32_t h, uint32_t comp, uint32_t mts, int32_t qp,
+                  int rdoq, int intra_frame, int is_intra, int enable_mts,
+                  ocoef *q, ocoef *r, ocoef *res_out, intptr_t os, uint64_t *nz)
+{
+    orc_qparams p;
+    ocoef *t = (ocoef *)malloc(sizeof(ocoef) * w * h);
+    orc_quant_params(qp, lg2u(w), lg2u(h), mts, rdoq, intra_frame, &p);
+    orc_fdct_wxh(res, rs, t, w, comp, w, h, mts, is_intra, enable_mts);
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) { q[y * os + x] = 0; r[y * os + x] = 0; }
+    {   /* quant over the low part with the outputs' stride */
+        ocoef *tq = (ocoef *)malloc(sizeof(ocoef) * w * h);
+        for (uint32_t i = 0; i < w * h; i++) tq[i] = t[i];
+        ocoef *qq = (ocoef *)calloc(w * h, sizeof(ocoef)), *rr = (ocoef *)calloc(w * h, sizeof(ocoef));
+        orc_quant_inv_quant(qq, tq, rr, w, w < 32 ? w : 32, h < 32 ? h : 32, 4, 4, p.qmult, p.qadd, p.qshift,
+                            p.iqmult, p.iqadd, p.iqshift, nz);
+        for (uint32_t y = 0; y < h; y++)
+            for (uint32_t x = 0; x < w; x++) { q[y * os + x] = qq[y * w + x]; r[y * os + x] = rr[y * w + x]; }
+        free(tq); free(qq); free(rr);
+    }
+    orc_idct_wxh(r, os, res_out, os, w, h, is_intra, comp, mts, enable_mts);
+    free(t);
+}
+
 /* ======================================================================
  * Motion estimation.
  * ====================================================================== */

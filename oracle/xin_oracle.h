@@ -126,6 +126,13 @@ void orc_transform_tu(const opix *in, intptr_t is, const opix *pred, intptr_t ps
                       ocoef *t, ocoef *q, ocoef *r, intptr_t cs, uint32_t w, uint32_t h, uint32_t comp,
                       uint32_t mts, int32_t qp, int rdoq, int intra_frame, int is_intra, int enable_mts, uint64_t *nz);
 
+/* one residual block through forward transform (MTS type), zero-out, quant /
+ * dequant (4x4 CGs) and inverse transform: the TU arithmetic of Xin266Transform
+ * (h266_trans_quant.c:131-220) followed by Xin266IDctWxH, on a residual input */
+void orc_tq_block(const ocoef *res, intptr_t rs, uint32_t w, uint32_t h, uint32_t comp, uint32_t mts, int32_t qp,
+                  int rdoq, int intra_frame, int is_intra, int enable_mts,
+                  ocoef *q, ocoef *r, ocoef *res_out, intptr_t os, uint64_t *nz);
+
 /* ---- motion estimation */
 uint32_t orc_mvd_bits(int32_t v);
 void orc_exp_golomb_table(uint32_t *tab32767);

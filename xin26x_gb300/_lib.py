@@ -34,6 +34,11 @@ class xin_gpu_results(C.Structure):
     _fields_ = [("cu", vp), ("q", vp * 3), ("rec", vp * 3), ("gpu_ms", C.c_float)]
 
 
+class xin_gpu_tq_block(C.Structure):
+    _fields_ = [("offset", u32), ("log2w", C.c_uint8), ("log2h", C.c_uint8), ("mts", C.c_uint8), ("flags", C.c_uint8),
+                ("qp", i32)]
+
+
 class xin_gpu_mv(C.Structure):
     _fields_ = [("mvX", C.c_int16), ("mvY", C.c_int16)]
 
@@ -104,6 +109,8 @@ SIGNATURES = {
     "xin_gpu_measure_sad_peak": ([C.POINTER(C.c_double)], C.c_int),
     "xin_gpu_install": ([vp, vp, u32], C.c_int),
     "xin_gpu_fdct2_wxh_noalloc": ([vp, ip, vp, ip, u32, u32, i32, i32, vp], C.c_int),
+    "xin_gpu_tq_batch": ([vp, i32, vp, vp, vp, vp, vp, C.c_size_t, i32], C.c_int),
+    "xin_gpu_tq_batch_device": ([vp, i32, vp, vp, vp, vp, vp, C.c_size_t, i32, vp, vp], C.c_int),
 }
 for _n in ["InterpCopy", "InterpCopyU8S16", "LumaInterpHor", "LumaInterpVet", "LumaInterpHorVet", "LumaInterpHorU8S16",
            "LumaInterpVetU8S16", "LumaInterpHorVetU8S16", "LumaInterpVetS16U8", "LumaInterpVetS16S16",
