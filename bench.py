@@ -291,6 +291,7 @@ def run_gpu(args):
 
     # plain per-call form on a sample of CUs (one synchronous launch per reference call)
     percall = percall_sample(lib, frames)
+    kbatch = kernel_batch_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup) if rank == 0 else None
 
     out = None
     if rank == 0:
@@ -314,6 +315,7 @@ def run_gpu(args):
                        "d2h_bytes_per_step": cu_bytes + q_bytes,
                        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}},
                "percall": percall,
+               "kernel_batch": kbatch,
                "gpu_launches": int(launches),
                "clocks": clk,
                "cpu_baseline": cpu}
@@ -322,6 +324,67 @@ def run_gpu(args):
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def kernel_batch_bench(torch, flush, steps, warmup, nblocks=65536, seed=65536):
+    """Batched transform / quant on a 10-bit block list: 65,536 blocks of sides
+    4..64 (biased to 8 and 16), 11-bit Laplacian residuals (scale 12), DCT2 70 %
+    / DST7-DCT8 pairs 30 % (sides <= 32), QP uniform in [22, 42].  The plan form
+    (block list resident on the device) timed with CUDA events per run, L2
+    flushed between runs; autotuned group sizes against the fixed heuristic."""
+    from xin26x_gb300 import _lib, synth
+    g = _lib.load(10)
+    assert g.xin_gpu_init(torch.cuda.current_device()) == 0
+    blocks, resid = synth.tq_blocks(nblocks, seed, bitdepth=10, kernel_bench_mix=True)
+    d_res = torch.from_numpy(resid).cuda()
+    q, r, ro = torch.empty_like(d_res), torch.empty_like(d_res), torch.empty_like(d_res)
+    nz = torch.empty(nblocks, dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream()
+    out = {"workload": f"{nblocks} blocks, 10-bit, sides 4..64, 11-bit Laplacian residuals (scale 12), DCT2 70 % / "
+                       "DST7-DCT8 pairs 30 % on sides <= 32, QP U[22,42]; forward transform + quant + dequant + "
+                       "inverse transform per block",
+           "coefficients": int(resid.size), "l2": "flushed between runs"}
+    algo = resid.size * 4 * 4 + nblocks * (8 + 12 + 4)      # resid in, q/r/resid_out out, nz, job + list entry
+    for name, tile in (("autotuned", -1), ("fixed", 0)):
+        plan = C.c_void_p()
+        assert g.xin_gpu_tq_plan_create(blocks.ctypes.data, nblocks, resid.size, tile, C.byref(plan)) == 0, \
+            g.xin_gpu_last_error()
+        run = lambda: g.xin_gpu_tq_plan_run(plan, d_res.data_ptr(), q.data_ptr(), r.data_ptr(), ro.data_ptr(),
+                                            nz.data_ptr(), stream.cuda_stream)
+        for _ in range(max(3, warmup)):
+            assert run() == 0, g.xin_gpu_last_error()
+        times = []
+        for _ in range(steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            assert run() == 0
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        tiles = (C.c_int32 * 49)()
+        g.xin_gpu_tq_plan_tiles(plan, tiles)
+        g.xin_gpu_tq_plan_destroy(plan)
+        ms = float(np.mean(times))
+        out[name] = {"ms": ms, "Mblocks_per_s": nblocks / ms / 1e3, "Gcoeff_per_s": resid.size / ms / 1e6,
+                     "tiles": {f"{1 << (c // 7)}x{1 << (c % 7)}": int(tiles[c]) for c in range(49) if tiles[c]}}
+    peaks = _measured_peaks()
+    hbm = peaks.get("hbm_gbs") if peaks else None
+    achieved = algo / (out["autotuned"]["ms"] * 1e-3) / 1e9
+    out["speedup_autotuned_vs_fixed"] = out["fixed"]["ms"] / out["autotuned"]["ms"]
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm or 6800.0, "unit": "GB/s",
+                       "frac": achieved / (hbm or 6800.0), "algorithmic_bytes": int(algo),
+                       "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "of fallback 6.8 TB/s"}
+    return out
+
+
+def _measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
 
 
 def quant_params(qp, lg):

@@ -231,6 +231,18 @@ int  xin_gpu_tq_batch(const xin_gpu_tq_block *blocks, int32_t nblocks, const XG_
 int  xin_gpu_tq_batch_device(const xin_gpu_tq_block *blocks, int32_t nblocks, const XG_COEFF *resid, XG_COEFF *q,
                              XG_COEFF *r, XG_COEFF *resid_out, uint64_t *nz, size_t ncoeffs, int32_t tile, void *stream,
                              int32_t *tiles_used);
+/* A plan keeps a validated block list, sorted by size class, on the device so
+ * that one list can run on new residuals without host work: run only enqueues
+ * launches on `stream` (device arrays).  With tile -1 the first run of a class
+ * not tuned yet times the candidates and synchronises; later runs are
+ * asynchronous.  tiles: 49 entries, 0 for classes not resolved yet. */
+typedef struct xin_gpu_tq_plan xin_gpu_tq_plan;
+int  xin_gpu_tq_plan_create(const xin_gpu_tq_block *blocks, int32_t nblocks, size_t ncoeffs, int32_t tile,
+                            xin_gpu_tq_plan **plan);
+int  xin_gpu_tq_plan_run(xin_gpu_tq_plan *plan, const XG_COEFF *resid, XG_COEFF *q, XG_COEFF *r, XG_COEFF *resid_out,
+                         uint64_t *nz, void *stream);
+int  xin_gpu_tq_plan_tiles(const xin_gpu_tq_plan *plan, int32_t *tiles);
+void xin_gpu_tq_plan_destroy(xin_gpu_tq_plan *plan);
 
 /* ------------------------------------------------------- motion search (a7-a8)
  * xin_me_struct is the reference's ME state (h26x_core/include/h26x_me_struct.h:60-131);

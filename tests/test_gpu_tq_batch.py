@@ -1,7 +1,9 @@
 """Batched transform / quant (xin_gpu_tq_batch) against the oracle's per-block TU
 path (orc_tq_block): mixed sizes 4..64, DCT2 / skip / DST7 / DCT8 MTS pairs,
 implicit MTS, QP 0..63, RDOQ and intra-picture rounding, 8- and 10-bit; every
-tile choice (fixed, autotuned, each group size) bit-exact."""
+tile choice (fixed, autotuned, each group size) bit-exact.  The 65,536-block
+kernel-bench mix is checked on a 2,000-block draw and at full size through the
+device entry point (autotuned and fixed tiles give identical outputs)."""
 import ctypes as C
 
 import numpy as np
@@ -13,33 +15,8 @@ pytestmark = pytest.mark.gpu
 
 
 def make_batch(n, bd, seed, kernel_bench_mix=False):
-    """Seeded block list.  kernel_bench_mix: sizes from {4..64}^2 with a geometric
-    tail biased to 8 and 16, residuals 11-bit Laplacian (scale 12), DCT2 70 % /
-    DST7-DCT8 MTS pairs 30 % restricted to sides <= 32, QP uniform in [22, 42]."""
-    from xin26x_gb300 import _lib
-    rng = np.random.default_rng(seed)
-    blocks = (_lib.xin_gpu_tq_block * n)()
-    off = 0
-    lg_p = np.array([0.12, 0.34, 0.30, 0.16, 0.08])
-    for i in range(n):
-        lw, lh = (int(rng.choice(5, p=lg_p)) + 2, int(rng.choice(5, p=lg_p)) + 2)
-        if kernel_bench_mix:
-            mts = 0 if rng.random() < 0.7 or lw > 5 or lh > 5 else int(rng.integers(2, 6))
-            qp = int(rng.integers(22, 43))
-            flags = 0
-        else:
-            mts = int(rng.integers(0, 6))
-            if mts >= 1 and (lw > 5 or lh > 5):
-                mts = 0
-            qp = int(rng.integers(0, 64))
-            flags = int(rng.integers(0, 32))
-        blocks[i].offset, blocks[i].log2w, blocks[i].log2h = off, lw, lh
-        blocks[i].mts, blocks[i].flags, blocks[i].qp = mts, flags, qp
-        off += 1 << (lw + lh)
-    lim = 1023 if kernel_bench_mix else (1 << bd) - 1
-    scale = 12 if kernel_bench_mix else 60
-    resid = np.clip(np.rint(rng.laplace(0, scale, size=off)), -lim, lim)
-    return blocks, resid.astype(np.int16 if bd == 8 else np.int32)
+    from xin26x_gb300 import synth
+    return synth.tq_blocks(n, seed, bitdepth=bd, kernel_bench_mix=kernel_bench_mix)
 
 
 def oracle_batch(o, blocks, resid):
@@ -47,11 +24,11 @@ def oracle_batch(o, blocks, resid):
     q, r, ro = np.zeros_like(resid), np.zeros_like(resid), np.zeros_like(resid)
     nz = np.zeros(n, np.uint64)
     for i in range(n):
-        b = blocks[i]
-        w, h, off = 1 << b.log2w, 1 << b.log2h, b.offset
-        f = b.flags
-        o.tq_block(O.ptr(resid, off), w, w, h, 1 if f & 2 else 0, b.mts, b.qp, 1 if f & 4 else 0, 1 if f & 8 else 0,
-                   1 if f & 1 else 0, 1 if f & 16 else 0, O.ptr(q, off), O.ptr(r, off), O.ptr(ro, off), w, O.ptr(nz, i))
+        lw, lh, off, f = int(blocks["log2w"][i]), int(blocks["log2h"][i]), int(blocks["offset"][i]), int(blocks["flags"][i])
+        w, h = 1 << lw, 1 << lh
+        o.tq_block(O.ptr(resid, off), w, w, h, 1 if f & 2 else 0, int(blocks["mts"][i]), int(blocks["qp"][i]),
+                   1 if f & 4 else 0, 1 if f & 8 else 0, 1 if f & 1 else 0, 1 if f & 16 else 0,
+                   O.ptr(q, off), O.ptr(r, off), O.ptr(ro, off), w, O.ptr(nz, i))
     return q, r, ro, nz
 
 
@@ -66,7 +43,7 @@ def test_tq_batch_matches_oracle_every_tile(bd):
     for tile in (0, -1, 32, 64, 128, 256, -1):
         q, r, ro = np.zeros_like(resid), np.zeros_like(resid), np.zeros_like(resid)
         nz = np.zeros(len(blocks), np.uint64)
-        st = g.xin_gpu_tq_batch(blocks, len(blocks), resid.ctypes.data, q.ctypes.data, r.ctypes.data, ro.ctypes.data,
+        st = g.xin_gpu_tq_batch(blocks.ctypes.data, len(blocks), resid.ctypes.data, q.ctypes.data, r.ctypes.data, ro.ctypes.data,
                                 nz.ctypes.data, resid.size, tile)
         assert st == 0, g.xin_gpu_last_error()
         for name, a, b in zip(("q", "r", "resid_out", "nz"), (q, r, ro, nz), want):
@@ -82,7 +59,7 @@ def test_tq_batch_kernel_bench_mix_and_errors():
     want = oracle_batch(o, blocks, resid)
     q, r, ro = np.zeros_like(resid), np.zeros_like(resid), np.zeros_like(resid)
     nz = np.zeros(len(blocks), np.uint64)
-    assert g.xin_gpu_tq_batch(blocks, len(blocks), resid.ctypes.data, q.ctypes.data, r.ctypes.data, ro.ctypes.data,
+    assert g.xin_gpu_tq_batch(blocks.ctypes.data, len(blocks), resid.ctypes.data, q.ctypes.data, r.ctypes.data, ro.ctypes.data,
                               nz.ctypes.data, resid.size, -1) == 0
     for a, b in zip((q, r, ro, nz), want):
         assert np.array_equal(a, b)
@@ -95,3 +72,48 @@ def test_tq_batch_kernel_bench_mix_and_errors():
         bad[0].offset, bad[0].log2w, bad[0].log2h, bad[0].mts = 0, 6, 4, mts
         assert g.xin_gpu_tq_batch(bad, 1, resid.ctypes.data, q.ctypes.data, r.ctypes.data, ro.ctypes.data,
                                   nz.ctypes.data, resid.size, 0) == -2
+
+
+def test_tq_batch_full_kernel_bench_autotuned_equals_fixed():
+    """65,536 blocks on device arrays: autotuned and fixed tiles bit-identical, and a
+    seeded sample of 300 blocks bit-exact against the oracle."""
+    import torch
+    from xin26x_gb300 import _lib
+    g = _lib.load(10)
+    o = O.oracle(10)
+    blocks, resid = make_batch(65536, 10, seed=65536, kernel_bench_mix=True)
+    d_res = torch.from_numpy(resid).cuda()
+    outs = []
+    stream = torch.cuda.current_stream().cuda_stream
+    for tile in (-1, 0):
+        q, r, ro = torch.zeros_like(d_res), torch.zeros_like(d_res), torch.zeros_like(d_res)
+        nz = torch.zeros(len(blocks), dtype=torch.int64, device="cuda")
+        used = (C.c_int32 * 49)()
+        if tile == 0:
+            st = g.xin_gpu_tq_batch_device(blocks.ctypes.data, len(blocks), d_res.data_ptr(), q.data_ptr(), r.data_ptr(),
+                                           ro.data_ptr(), nz.data_ptr(), resid.size, tile, stream, used)
+            assert st == 0, g.xin_gpu_last_error()
+        else:   # the plan form: tune on the first run, then two asynchronous runs over the same outputs
+            plan = C.c_void_p()
+            assert g.xin_gpu_tq_plan_create(blocks.ctypes.data, len(blocks), resid.size, tile, C.byref(plan)) == 0
+            for _ in range(3):
+                assert g.xin_gpu_tq_plan_run(plan, d_res.data_ptr(), q.data_ptr(), r.data_ptr(), ro.data_ptr(),
+                                             nz.data_ptr(), stream) == 0, g.xin_gpu_last_error()
+            assert g.xin_gpu_tq_plan_tiles(plan, used) == 0
+            g.xin_gpu_tq_plan_destroy(plan)
+            torch.cuda.synchronize()
+            assert all(u in (32, 64, 128, 256) for u, n in zip(used, np.bincount(
+                blocks["log2w"].astype(int) * 7 + blocks["log2h"], minlength=49)) if n)
+        assert all(u in (0, 32, 64, 128, 256) for u in used)
+        outs.append([t.cpu().numpy() for t in (q, r, ro, nz)])
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+    pick = np.random.default_rng(5).choice(len(blocks), 300, replace=False)
+    q, r, ro, nz = outs[0]
+    for i in pick:
+        off, n = int(blocks["offset"][i]), 1 << (int(blocks["log2w"][i]) + int(blocks["log2h"][i]))
+        sub = blocks[i:i + 1].copy()
+        sub["offset"] = 0
+        wq, wr, wro, wnz = oracle_batch(o, sub, resid[off:off + n].copy())
+        assert np.array_equal(q[off:off + n], wq) and np.array_equal(r[off:off + n], wr)
+        assert np.array_equal(ro[off:off + n], wro) and int(nz[i]) == int(wnz[0].astype(np.int64))

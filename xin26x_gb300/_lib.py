@@ -111,6 +111,10 @@ SIGNATURES = {
     "xin_gpu_fdct2_wxh_noalloc": ([vp, ip, vp, ip, u32, u32, i32, i32, vp], C.c_int),
     "xin_gpu_tq_batch": ([vp, i32, vp, vp, vp, vp, vp, C.c_size_t, i32], C.c_int),
     "xin_gpu_tq_batch_device": ([vp, i32, vp, vp, vp, vp, vp, C.c_size_t, i32, vp, vp], C.c_int),
+    "xin_gpu_tq_plan_create": ([vp, i32, C.c_size_t, i32, C.POINTER(vp)], C.c_int),
+    "xin_gpu_tq_plan_run": ([vp, vp, vp, vp, vp, vp, vp], C.c_int),
+    "xin_gpu_tq_plan_tiles": ([vp, vp], C.c_int),
+    "xin_gpu_tq_plan_destroy": ([vp], None),
 }
 for _n in ["InterpCopy", "InterpCopyU8S16", "LumaInterpHor", "LumaInterpVet", "LumaInterpHorVet", "LumaInterpHorU8S16",
            "LumaInterpVetU8S16", "LumaInterpHorVetU8S16", "LumaInterpVetS16U8", "LumaInterpVetS16S16",

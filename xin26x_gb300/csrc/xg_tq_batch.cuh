@@ -194,46 +194,68 @@ static cudaError_t xg_tq_launch_class(int G, int nblk, int w, int h, const XgTqJ
     return cudaGetLastError();
 }
 
-/* device pointers; blocks sorted per class into `list` (device) with per-class ranges */
-static int xg_tq_run(const XgTqJob *d_jobs, const uint32_t *d_list, const int cls_first[50], const int cls_n[50],
-                     const xg_coef *res, xg_coef *q, xg_coef *r, xg_coef *rout, unsigned long long *nz, int32_t tile,
-                     cudaStream_t st, int32_t *tiles_used)
+/* group size of one class: fixed, explicit, or autotuned (times every candidate
+ * on this class's blocks with the caller's arrays, then caches the winner) */
+static int xg_tq_pick(int c, int cls_first, int cls_n, const XgTqJob *d_jobs, const uint32_t *d_list, const xg_coef *res,
+                      xg_coef *q, xg_coef *r, xg_coef *rout, unsigned long long *nz, int32_t tile, cudaStream_t st, int *G)
+{
+    int lw = c / 7, lh = c % 7, w = 1 << lw, h = 1 << lh;
+    if (tile > 0) *G = tile;
+    else if (tile == 0) *G = xg_tq_fixed_group(w, h);
+    else {
+        std::lock_guard<std::mutex> lock(g_tq_tuner.mu);
+        *G = g_tq_tuner.g[lw][lh];
+        if (!*G) {
+            cudaEvent_t a, b;
+            if (xg_cuda_check(cudaEventCreate(&a), "tq autotune") || xg_cuda_check(cudaEventCreate(&b), "tq autotune"))
+                return XIN_GPU_ERR_CUDA;
+            float best = 1e30f;
+            int bestG = xg_tq_fixed_group(w, h);
+            for (int cand : { 32, 64, 128, 256 }) {
+                if ((size_t)(256 / cand) * xg_tq_group_words(w, h) * 4 > 200 * 1024) continue;
+                for (int rep = 0; rep < 3; rep++) {
+                    cudaEventRecord(a, st);
+                    cudaError_t e = xg_tq_launch_class(cand, cls_n, w, h, d_jobs, d_list + cls_first, res, q, r, rout, nz, st);
+                    cudaEventRecord(b, st);
+                    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+                    if (e != cudaSuccess) { cudaEventDestroy(a); cudaEventDestroy(b); return xg_cuda_check(e, "tq autotune"); }
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, a, b);
+                    if (rep && ms < best) { best = ms; bestG = cand; }
+                }
+            }
+            cudaEventDestroy(a); cudaEventDestroy(b);
+            g_tq_tuner.g[lw][lh] = *G = bestG;
+        }
+    }
+    if ((size_t)(256 / *G) * xg_tq_group_words(w, h) * 4 > 200 * 1024) *G = 256;
+    return XIN_GPU_OK;
+}
+
+/* a validated, sorted block list resident on the device */
+struct xin_gpu_tq_plan {
+    int device;
+    int32_t nblocks;
+    size_t ncoeffs;
+    int32_t tile;               /* as requested */
+    XgTqJob *d_jobs;
+    uint32_t *d_list;
+    int first[50], cnt[50];
+    int G[49];                  /* resolved group size per class, 0 = not resolved yet */
+};
+
+/* enqueue every class on st; resolves group sizes on first use */
+static int xg_tq_plan_enqueue(xin_gpu_tq_plan *p, const xg_coef *res, xg_coef *q, xg_coef *r, xg_coef *rout,
+                              unsigned long long *nz, cudaStream_t st)
 {
     for (int c = 0; c < 49; c++) {
-        if (!cls_n[c]) continue;
-        int lw = c / 7, lh = c % 7, w = 1 << lw, h = 1 << lh;
-        int G;
-        if (tile > 0) G = tile;
-        else if (tile == 0) G = xg_tq_fixed_group(w, h);
-        else {
-            std::lock_guard<std::mutex> lock(g_tq_tuner.mu);
-            G = g_tq_tuner.g[lw][lh];
-            if (!G) {
-                /* autotune: time every group size on this class's blocks, keep the fastest */
-                cudaEvent_t a, b;
-                cudaEventCreate(&a); cudaEventCreate(&b);
-                float best = 1e30f;
-                G = xg_tq_fixed_group(w, h);
-                for (int cand : { 32, 64, 128, 256 }) {
-                    if ((size_t)(256 / cand) * xg_tq_group_words(w, h) * 4 > 200 * 1024) continue;
-                    for (int rep = 0; rep < 3; rep++) {
-                        cudaEventRecord(a, st);
-                        cudaError_t e = xg_tq_launch_class(cand, cls_n[c], w, h, d_jobs, d_list + cls_first[c], res, q, r, rout, nz, st);
-                        cudaEventRecord(b, st);
-                        if (e != cudaSuccess) { cudaEventDestroy(a); cudaEventDestroy(b); return xg_cuda_check(e, "tq autotune"); }
-                        cudaEventSynchronize(b);
-                        float ms = 0;
-                        cudaEventElapsedTime(&ms, a, b);
-                        if (rep && ms < best) { best = ms; G = cand; }
-                    }
-                }
-                cudaEventDestroy(a); cudaEventDestroy(b);
-                g_tq_tuner.g[lw][lh] = G;
-            }
+        if (!p->cnt[c]) continue;
+        if (!p->G[c]) {
+            int s = xg_tq_pick(c, p->first[c], p->cnt[c], p->d_jobs, p->d_list, res, q, r, rout, nz, p->tile, st, &p->G[c]);
+            if (s) return s;
         }
-        if ((size_t)(256 / G) * xg_tq_group_words(w, h) * 4 > 200 * 1024) G = 256;
-        if (tiles_used) tiles_used[c] = G;
-        cudaError_t e = xg_tq_launch_class(G, cls_n[c], w, h, d_jobs, d_list + cls_first[c], res, q, r, rout, nz, st);
+        cudaError_t e = xg_tq_launch_class(p->G[c], p->cnt[c], 1 << (c / 7), 1 << (c % 7), p->d_jobs, p->d_list + p->first[c],
+                                           res, q, r, rout, nz, st);
         if (e != cudaSuccess) return xg_cuda_check(e, "tq launch");
     }
     return XIN_GPU_OK;
@@ -263,40 +285,76 @@ static int xg_tq_validate(const xin_gpu_tq_block *blocks, int32_t n, size_t ncoe
     return XIN_GPU_OK;
 }
 
-static int xg_tq_batch_impl(XgThread *t, const xin_gpu_tq_block *blocks, int32_t nblocks, const xg_coef *resid, xg_coef *q,
-                            xg_coef *r, xg_coef *resid_out, unsigned long long *nz, size_t ncoeffs, int32_t tile,
-                            cudaStream_t s, int32_t *tiles_used)
+extern "C" void xin_gpu_tq_plan_destroy(xin_gpu_tq_plan *p)
 {
+    if (!p) return;
+    cudaFree(p->d_jobs);
+    cudaFree(p->d_list);
+    delete p;
+}
+
+extern "C" int xin_gpu_tq_plan_create(const xin_gpu_tq_block *blocks, int32_t nblocks, size_t ncoeffs, int32_t tile,
+                                      xin_gpu_tq_plan **out)
+{
+    xin_gpu_clear_error();
+    if (!blocks || nblocks <= 0 || !out || (tile != -1 && tile != 0 && tile != 32 && tile != 64 && tile != 128 && tile != 256)) {
+        xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_create: bad argument (tile must be -1, 0, 32, 64, 128 or 256)");
+        return XIN_GPU_ERR_ARG;
+    }
+    *out = nullptr;
+    if (!xg_thread()) return xin_gpu_last_status();
     std::vector<XgTqJob> jobs;
     std::vector<uint32_t> list;
-    int first[50], cnt[50];
-    int st = xg_tq_validate(blocks, nblocks, ncoeffs, jobs, list, first, cnt);
-    if (st) return st;
-    XgTqJob *d_jobs = (XgTqJob *)xg_dalloc(t, jobs.size() * sizeof(XgTqJob));
-    uint32_t *d_list = (uint32_t *)xg_dalloc(t, list.size() * 4);
-    if (!d_jobs || !d_list) return xin_gpu_last_status();
-    if (xg_cuda_check(cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(XgTqJob), cudaMemcpyHostToDevice, s), "tq jobs") ||
-        xg_cuda_check(cudaMemcpyAsync(d_list, list.data(), list.size() * 4, cudaMemcpyHostToDevice, s), "tq list"))
+    xin_gpu_tq_plan *p = new xin_gpu_tq_plan();
+    int st = xg_tq_validate(blocks, nblocks, ncoeffs, jobs, list, p->first, p->cnt);
+    if (st) { delete p; return st; }
+    cudaGetDevice(&p->device);
+    p->nblocks = nblocks;
+    p->ncoeffs = ncoeffs;
+    p->tile = tile;
+    if (xg_cuda_check(cudaMalloc(&p->d_jobs, jobs.size() * sizeof(XgTqJob)), "tq plan") ||
+        xg_cuda_check(cudaMalloc(&p->d_list, list.size() * 4), "tq plan") ||
+        xg_cuda_check(cudaMemcpy(p->d_jobs, jobs.data(), jobs.size() * sizeof(XgTqJob), cudaMemcpyHostToDevice), "tq plan") ||
+        xg_cuda_check(cudaMemcpy(p->d_list, list.data(), list.size() * 4, cudaMemcpyHostToDevice), "tq plan")) {
+        xin_gpu_tq_plan_destroy(p);
         return XIN_GPU_ERR_CUDA;
-    st = xg_tq_run(d_jobs, d_list, first, cnt, resid, q, r, resid_out, nz, tile, s, tiles_used);
-    if (st) return st;
-    return xg_cuda_check(cudaStreamSynchronize(s), "tq sync");
+    }
+    *out = p;
+    return XIN_GPU_OK;
+}
+
+extern "C" int xin_gpu_tq_plan_run(xin_gpu_tq_plan *p, const XG_COEFF *resid, XG_COEFF *q, XG_COEFF *r, XG_COEFF *resid_out,
+                                   uint64_t *nz, void *stream)
+{
+    xin_gpu_clear_error();
+    if (!p || !resid || !q || !r || !resid_out || !nz) {
+        xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_run: bad argument");
+        return XIN_GPU_ERR_ARG;
+    }
+    cudaGetLastError();
+    return xg_tq_plan_enqueue(p, (const xg_coef *)resid, (xg_coef *)q, (xg_coef *)r, (xg_coef *)resid_out,
+                              (unsigned long long *)nz, (cudaStream_t)stream);
+}
+
+extern "C" int xin_gpu_tq_plan_tiles(const xin_gpu_tq_plan *p, int32_t *tiles)
+{
+    if (!p || !tiles) { xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_tiles: bad argument"); return XIN_GPU_ERR_ARG; }
+    for (int c = 0; c < 49; c++) tiles[c] = p->G[c];
+    return XIN_GPU_OK;
 }
 
 extern "C" int xin_gpu_tq_batch_device(const xin_gpu_tq_block *blocks, int32_t nblocks, const XG_COEFF *resid, XG_COEFF *q,
                                        XG_COEFF *r, XG_COEFF *resid_out, uint64_t *nz, size_t ncoeffs, int32_t tile,
                                        void *stream, int32_t *tiles_used)
 {
-    xin_gpu_clear_error();
-    if (!blocks || nblocks <= 0 || !resid || !q || !r || !resid_out || !nz ||
-        (tile > 0 && tile != 32 && tile != 64 && tile != 128 && tile != 256)) {
-        xg_set_error(XIN_GPU_ERR_ARG, "tq_batch_device: bad argument");
-        return XIN_GPU_ERR_ARG;
-    }
-    XgThread *t = xg_thread();
-    if (!t) return xin_gpu_last_status();
-    return xg_tq_batch_impl(t, blocks, nblocks, (const xg_coef *)resid, (xg_coef *)q, (xg_coef *)r, (xg_coef *)resid_out,
-                            (unsigned long long *)nz, ncoeffs, tile, (cudaStream_t)stream, tiles_used);
+    xin_gpu_tq_plan *p = nullptr;
+    int st = xin_gpu_tq_plan_create(blocks, nblocks, ncoeffs, tile, &p);
+    if (st) return st;
+    st = xin_gpu_tq_plan_run(p, resid, q, r, resid_out, nz, stream);
+    if (!st) st = xg_cuda_check(cudaStreamSynchronize((cudaStream_t)stream), "tq sync");
+    if (!st && tiles_used) xin_gpu_tq_plan_tiles(p, tiles_used);
+    xin_gpu_tq_plan_destroy(p);
+    return st;
 }
 
 extern "C" int xin_gpu_tq_batch(const xin_gpu_tq_block *blocks, int32_t nblocks, const XG_COEFF *resid, XG_COEFF *q, XG_COEFF *r,
@@ -313,18 +371,24 @@ extern "C" int xin_gpu_tq_batch(const xin_gpu_tq_block *blocks, int32_t nblocks,
     }
     XgThread *t = xg_thread();
     if (!t) return xin_gpu_last_status();
+    xin_gpu_tq_plan *p = nullptr;
+    int st = xin_gpu_tq_plan_create(blocks, nblocks, ncoeffs, tile, &p);
+    if (st) return st;
     size_t bytes = ncoeffs * sizeof(xg_coef);
     xg_coef *d_res = (xg_coef *)xg_dalloc(t, bytes), *d_q = (xg_coef *)xg_dalloc(t, bytes), *d_r = (xg_coef *)xg_dalloc(t, bytes),
             *d_o = (xg_coef *)xg_dalloc(t, bytes);
     unsigned long long *d_nz = (unsigned long long *)xg_dalloc(t, (size_t)nblocks * 8);
-    if (!d_res || !d_q || !d_r || !d_o || !d_nz) return xin_gpu_last_status();
-    if (xg_cuda_check(cudaMemcpyAsync(d_res, resid, bytes, cudaMemcpyHostToDevice, t->stream), "tq h2d")) return XIN_GPU_ERR_CUDA;
-    int st = xg_tq_batch_impl(t, blocks, nblocks, d_res, d_q, d_r, d_o, d_nz, ncoeffs, tile, t->stream, nullptr);
-    if (st) return st;
-    if (xg_cuda_check(cudaMemcpyAsync(q, d_q, bytes, cudaMemcpyDeviceToHost, t->stream), "tq d2h") ||
-        xg_cuda_check(cudaMemcpyAsync(r, d_r, bytes, cudaMemcpyDeviceToHost, t->stream), "tq d2h") ||
-        xg_cuda_check(cudaMemcpyAsync(resid_out, d_o, bytes, cudaMemcpyDeviceToHost, t->stream), "tq d2h") ||
-        xg_cuda_check(cudaMemcpyAsync(nz, d_nz, (size_t)nblocks * 8, cudaMemcpyDeviceToHost, t->stream), "tq d2h"))
-        return XIN_GPU_ERR_CUDA;
-    return xg_cuda_check(cudaStreamSynchronize(t->stream), "tq sync");
+    if (!d_res || !d_q || !d_r || !d_o || !d_nz) { xin_gpu_tq_plan_destroy(p); return xin_gpu_last_status(); }
+    st = xg_cuda_check(cudaMemcpyAsync(d_res, resid, bytes, cudaMemcpyHostToDevice, t->stream), "tq h2d");
+    if (!st) st = xin_gpu_tq_plan_run(p, (const XG_COEFF *)d_res, (XG_COEFF *)d_q, (XG_COEFF *)d_r, (XG_COEFF *)d_o,
+                                      (uint64_t *)d_nz, t->stream);
+    if (!st)
+        st = xg_cuda_check(cudaMemcpyAsync(q, d_q, bytes, cudaMemcpyDeviceToHost, t->stream), "tq d2h") ||
+             xg_cuda_check(cudaMemcpyAsync(r, d_r, bytes, cudaMemcpyDeviceToHost, t->stream), "tq d2h") ||
+             xg_cuda_check(cudaMemcpyAsync(resid_out, d_o, bytes, cudaMemcpyDeviceToHost, t->stream), "tq d2h") ||
+             xg_cuda_check(cudaMemcpyAsync(nz, d_nz, (size_t)nblocks * 8, cudaMemcpyDeviceToHost, t->stream), "tq d2h")
+                 ? XIN_GPU_ERR_CUDA : XIN_GPU_OK;
+    if (!st) st = xg_cuda_check(cudaStreamSynchronize(t->stream), "tq sync");
+    xin_gpu_tq_plan_destroy(p);
+    return st;
 }

@@ -71,3 +71,40 @@ def sequence(width: int, height: int, frames: int, seed: int, bitdepth: int = 8,
 def pad_plane(p: np.ndarray, pad: int) -> np.ndarray:
     """Edge-replicated padding (the reference-picture layout)."""
     return np.pad(p, pad, mode="edge")
+
+
+TQ_BLOCK_DTYPE = np.dtype([("offset", "<u4"), ("log2w", "u1"), ("log2h", "u1"), ("mts", "u1"), ("flags", "u1"),
+                           ("qp", "<i4")])     # xin_gpu_tq_block, 12 bytes
+
+
+def tq_blocks(n: int, seed: int, bitdepth: int = 10, kernel_bench_mix: bool = True):
+    """Seeded residual blocks for xin_gpu_tq_batch: (blocks, residuals).
+
+    Sides 4..64 drawn per axis with P(4, 8, 16, 32, 64) = (.12, .34, .30, .16, .08),
+    a geometric-like tail biased to 8 and 16.  kernel_bench_mix: residuals are
+    11-bit signed Laplacian (scale 12) clipped to +-1023, DCT2 70 % and the four
+    DST7/DCT8 pairs 30 % on blocks with both sides <= 32 (no 64-point DST7/DCT8
+    exists), QP uniform in [22, 42], no flags.  Otherwise: Laplacian scale 60
+    clipped to the bit depth, every MTS index (skip and the pairs only up to 32),
+    QP 0..63 and every flag combination."""
+    rng = np.random.default_rng(seed)
+    p = np.array([0.12, 0.34, 0.30, 0.16, 0.08])
+    b = np.zeros(n, TQ_BLOCK_DTYPE)
+    lw = rng.choice(5, size=n, p=p) + 2
+    lh = rng.choice(5, size=n, p=p) + 2
+    small = (lw <= 5) & (lh <= 5)
+    if kernel_bench_mix:
+        mts = np.where((rng.random(n) < 0.3) & small, rng.integers(2, 6, size=n), 0)
+        qp = rng.integers(22, 43, size=n)
+        flags = np.zeros(n, np.int64)
+    else:
+        mts = np.where(small, rng.integers(0, 6, size=n), 0)
+        qp = rng.integers(0, 64, size=n)
+        flags = rng.integers(0, 32, size=n)
+    area = (1 << (lw + lh)).astype(np.int64)
+    off = np.concatenate(([0], np.cumsum(area)[:-1]))
+    b["offset"], b["log2w"], b["log2h"], b["mts"], b["flags"], b["qp"] = off, lw, lh, mts, flags, qp
+    lim = 1023 if kernel_bench_mix else (1 << bitdepth) - 1
+    scale = 12 if kernel_bench_mix else 60
+    resid = np.clip(np.rint(rng.laplace(0, scale, size=int(area.sum()))), -lim, lim)
+    return b, resid.astype(np.int16 if bitdepth == 8 else np.int32)
