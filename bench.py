@@ -292,6 +292,10 @@ def run_gpu(args):
     # plain per-call form on a sample of CUs (one synchronous launch per reference call)
     percall = percall_sample(lib, frames)
     kbatch = kernel_batch_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup) if rank == 0 else None
+    serving = None
+    if rank == 0 and world == 1:
+        from xin26x_gb300 import serve_bench
+        serving = serve_bench.run(seconds=3.0, mpix_budget=900.0, max_inflight=6)
 
     out = None
     if rank == 0:
@@ -316,6 +320,7 @@ def run_gpu(args):
                        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}},
                "percall": percall,
                "kernel_batch": kbatch,
+               "serving": serving,
                "gpu_launches": int(launches),
                "clocks": clk,
                "cpu_baseline": cpu}

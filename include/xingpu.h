@@ -338,6 +338,58 @@ int  xin_gpu_stream_stage_ms(const xin_gpu_stream *s, float ms[4]);
 /* Device pointers of the result arrays (same layouts as xin_gpu_results). */
 int  xin_gpu_stream_device_results(const xin_gpu_stream *s, void **cu, void *q[3], void *rec[3]);
 
+/* Device and pinned-host bytes a stream of this configuration allocates
+ * (before the CUDA allocator's rounding); no GPU needed. */
+int  xin_gpu_stream_footprint(const xin_gpu_stream_cfg *cfg, uint64_t *device_bytes, uint64_t *host_bytes);
+
+/* ------------------------------------------------------------ serving
+ * Many live streams on one GPU.  join admits a stream only if its device
+ * footprint fits the HBM budget and, when mpix_budget > 0, the luma Mpixel/s
+ * already promised plus width*height*fps stays within it; otherwise
+ * XIN_GPU_ERR_ADMIT and nothing is allocated.  submit copies the picture and
+ * queues it (the caller's planes are free on return; cu_out must hold
+ * xin_gpu_stream_num_cus records of that configuration and stay valid until the
+ * picture is reported by poll; it may be NULL for a stream's first picture).
+ * One scheduler thread runs up to max_inflight pictures of different streams
+ * at once and starts the oldest waiting picture whenever one finishes; the
+ * pictures of one stream run in order.  A stream's results are the same as
+ * when it runs alone.  leave drains the stream's queue, then frees it. */
+typedef struct xin_gpu_server xin_gpu_server;
+typedef struct xin_gpu_server_cfg {
+    uint64_t hbm_budget;         /* device bytes for streams; 0 = 90 % of the free memory at open */
+    double   mpix_budget;        /* sustained luma Mpixel/s admission may promise; 0 = no limit */
+    uint32_t max_inflight;       /* pictures on the GPU at once; 0 = 8 */
+    uint32_t max_streams;        /* 0 = 256 */
+    uint32_t max_queue;          /* pictures a stream may have waiting; 0 = 4 */
+    uint32_t reserved;
+} xin_gpu_server_cfg;
+typedef struct xin_gpu_server_done {
+    int32_t  stream_id;
+    uint32_t frame_index;        /* per stream, from 0 */
+    uint64_t user_tag;
+    int32_t  status;             /* XIN_GPU_OK or this picture's error */
+    int32_t  has_results;        /* 0 for a stream's first picture (it only becomes the reference) */
+    float    gpu_ms;             /* device time of the picture */
+    float    reserved;
+    double   queue_ms;           /* submit -> start on the GPU */
+    double   latency_ms;         /* submit -> results in cu_out */
+} xin_gpu_server_done;
+typedef struct xin_gpu_server_stats {
+    int32_t  streams, running, queued, reserved;
+    uint64_t hbm_budget, hbm_used;
+    double   mpix_used;
+    uint64_t launched, completed;
+} xin_gpu_server_stats;
+int  xin_gpu_server_open(const xin_gpu_server_cfg *cfg, xin_gpu_server **srv);     /* cfg may be NULL */
+int  xin_gpu_server_join(xin_gpu_server *srv, const xin_gpu_stream_cfg *cfg, double fps, int32_t *stream_id);
+int  xin_gpu_server_submit(xin_gpu_server *srv, int32_t stream_id, const xin_gpu_picture *pic,
+                           xin_gpu_cu_result *cu_out, uint64_t user_tag);
+/* up to max completed pictures; waits up to timeout_ms (< 0: until one completes) */
+int  xin_gpu_server_poll(xin_gpu_server *srv, xin_gpu_server_done *out, int32_t max, int32_t timeout_ms, int32_t *n);
+int  xin_gpu_server_leave(xin_gpu_server *srv, int32_t stream_id, int32_t timeout_ms);
+int  xin_gpu_server_get_stats(xin_gpu_server *srv, xin_gpu_server_stats *stats);
+int  xin_gpu_server_close(xin_gpu_server *srv);     /* finishes queued pictures, frees every stream */
+
 /* Measured throughput of this GPU's packed 8-bit SAD instruction pair
  * (vabsdiff4 + dp4a) on register-resident data, in absolute differences per
  * second: the ceiling of the integer search kernel, used as its roofline. */

@@ -1,0 +1,153 @@
+"""Serving layer (xin_gpu_server_*): a stream's CU results through the server are
+bit-identical to the same stream run alone through xin_gpu_frame_* (itself
+checked against the oracle in test_gpu_frame.py), whether it shares the GPU with
+other streams or not; admission by device footprint and by promised Mpixel/s;
+join / leave while other streams run; argument and queue errors."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+R = 16
+
+
+def _frames(w, h, n, seed):
+    from xin26x_gb300 import synth
+    return synth.sequence(w, h, n, seed=seed, objects=2)
+
+
+def _alone(w, h, frames):
+    from xin26x_gb300.frame import FrameStream
+    fs = FrameStream(w, h, search_range=R, out_q=False, out_rec=False)
+    out = []
+    for k, f in enumerate(frames):
+        fs.submit(*f, qp=27 + 5 * (k % 3), uv_qp=27 + 5 * (k % 3), sad_lambda=64)
+        r = fs.wait()
+        if k:
+            out.append(r["cu"].copy())
+    fs.close()
+    return out
+
+
+def _serve(streams, max_inflight=4, leave_after=None):
+    """streams: list of (w, h, frames).  Pictures are submitted round-robin;
+    leave_after = (stream number, pictures) makes that stream leave early."""
+    from xin26x_gb300.server import Server
+    got = {}
+    with Server(max_inflight=max_inflight, max_queue=2) as srv:
+        sids = [srv.join(w, h, fps=30, search_range=R) for (w, h, _) in streams]
+        nxt = [0] * len(streams)
+        limit = [len(f) for (_, _, f) in streams]
+        if leave_after:
+            limit[leave_after[0]] = leave_after[1]
+        outstanding = 0
+        left = False
+        while any(nxt[i] < limit[i] for i in range(len(streams))) or outstanding:
+            for i, (w, h, fr) in enumerate(streams):
+                if nxt[i] >= limit[i]:
+                    continue
+                k = nxt[i]
+                st = srv.submit(sids[i], *fr[k], qp=27 + 5 * (k % 3), sad_lambda=64, tag=i * 1000 + k)
+                if st == 0:
+                    nxt[i] += 1
+                    outstanding += 1
+                else:
+                    assert st == -6          # queue full: collect and retry
+            if leave_after and not left and nxt[leave_after[0]] >= leave_after[1]:
+                assert srv.leave(sids[leave_after[0]], 30000) == 0
+                left = True
+            for d, cu in srv.poll(timeout_ms=20):
+                outstanding -= 1
+                assert d.status == 0
+                assert d.user_tag == sids.index(d.stream_id) * 1000 + d.frame_index
+                assert d.has_results == (d.frame_index > 0)
+                assert d.latency_ms >= d.queue_ms >= 0
+                if d.has_results:
+                    got[(sids.index(d.stream_id), d.frame_index)] = cu
+        st = srv.stats()
+        assert st["running"] == 0 and st["queued"] == 0
+    return got
+
+
+def test_server_results_equal_alone_and_mixed():
+    x = (416, 240, _frames(416, 240, 6, seed=11))
+    others = [(640, 360, _frames(640, 360, 5, seed=12)), (256, 128, _frames(256, 128, 7, seed=13)),
+              (416, 240, _frames(416, 240, 5, seed=14))]
+    want = _alone(*x)
+    alone = _serve([x], max_inflight=1)
+    mixed = _serve([x] + others, max_inflight=3)
+    for k in range(1, len(x[2])):
+        assert np.array_equal(alone[(0, k)], want[k - 1]), k
+        assert np.array_equal(mixed[(0, k)], want[k - 1]), k
+    # every other stream equals its own solo run too
+    for i, o in enumerate(others, 1):
+        w = _alone(*o)
+        for k in range(1, len(o[2])):
+            assert np.array_equal(mixed[(i, k)], w[k - 1]), (i, k)
+
+
+def test_server_leave_while_others_run():
+    x = (416, 240, _frames(416, 240, 6, seed=21))
+    y = (640, 360, _frames(640, 360, 6, seed=22))
+    want = _alone(*x)
+    got = _serve([x, y], max_inflight=2, leave_after=(1, 3))
+    for k in range(1, 6):
+        assert np.array_equal(got[(0, k)], want[k - 1])
+    assert (1, 2) in got and (1, 3) not in got
+
+
+def test_server_admission_by_footprint_and_throughput():
+    from xin26x_gb300.server import Admission, Server
+    probe = Server(hbm_budget=1)
+    fp, _ = probe.footprint(416, 240, search_range=R)
+    with pytest.raises(Admission):
+        probe.join(416, 240, search_range=R)
+    probe.close()
+    with Server(hbm_budget=2 * fp + fp // 2) as srv:
+        a = srv.join(416, 240, search_range=R)
+        srv.join(416, 240, search_range=R)
+        with pytest.raises(Admission):
+            srv.join(416, 240, search_range=R)
+        assert srv.stats()["hbm_used"] == 2 * fp
+        assert srv.leave(a, 10000) == 0
+        srv.join(416, 240, search_range=R)
+    with Server(mpix_budget=10.0) as srv:       # 416x240 at 30 fps = 3.0 Mpixel/s each
+        for _ in range(3):
+            srv.join(416, 240, fps=30, search_range=R)
+        with pytest.raises(Admission):
+            srv.join(416, 240, fps=30, search_range=R)
+        srv.join(416, 240, fps=5, search_range=R)
+
+
+def test_server_argument_and_queue_errors():
+    import ctypes as C
+    from xin26x_gb300 import _lib
+    from xin26x_gb300.server import Server
+    fr = _frames(1920, 1080, 2, seed=31)
+    with Server(max_queue=1, max_inflight=1) as srv:
+        sid = srv.join(1920, 1080, search_range=64)
+        assert srv.submit(sid + 100, *fr[0]) == -2                 # no such stream
+        assert srv.submit(sid, *fr[0], qp=64) == -2                # QP out of range
+        assert srv.submit(sid, *fr[0]) == 0
+        pic = _lib.xin_gpu_picture()
+        planes = [np.ascontiguousarray(p) for p in fr[1]]
+        for i, p in enumerate(planes):
+            pic.plane[i] = p.ctypes.data
+            pic.stride[i] = p.shape[1]
+        pic.qp = pic.uv_qp = 32
+        assert srv.lib.xin_gpu_server_submit(srv.h, sid, C.byref(pic), None, 0) == -2    # no cu_out after picture 0
+        full = 0
+        accepted = 1
+        for k in range(40):
+            st = srv.submit(sid, *fr[k % 2])
+            if st == -6:
+                full += 1
+            else:
+                assert st == 0
+                accepted += 1
+        assert full > 0
+        seen = 0
+        while seen < accepted:
+            for d, _ in srv.poll(timeout_ms=1000):
+                assert d.status == 0
+                seen += 1

@@ -1,0 +1,39 @@
+"""Host-side parts of the serving layer that need no GPU: the device-footprint
+arithmetic that admission uses, and its argument checks."""
+import ctypes as C
+
+import pytest
+
+from xin26x_gb300 import _lib
+
+
+def _fp(lib, w, h, ctu=64, r=64, mask=120, out=0, dio=0):
+    cfg = _lib.xin_gpu_stream_cfg(w, h, ctu, r, mask, out, 1, dio)
+    d, hb = C.c_uint64(), C.c_uint64()
+    st = lib.xin_gpu_stream_footprint(C.byref(cfg), C.byref(d), C.byref(hb))
+    return st, d.value, hb.value
+
+
+@pytest.mark.parametrize("bd", (8, 10))
+def test_footprint_arithmetic(bd):
+    lib = _lib.load(bd)
+    es = 1 if bd == 8 else 2          # pixel bytes
+    cs = 2 if bd == 8 else 4          # coefficient bytes
+    st, d, h = _fp(lib, 1920, 1080)
+    assert st == 0
+    # margin max(ctu + 16, R + 72) rounded to 32 -> 160; pitch rounded to 128 -> 2304 x 1400
+    ysz, csz = 2304 * 1400 * es, 1152 * 700 * es
+    ncus = 30 * 16 + 60 * 33 + 120 * 67 + 240 * 135
+    lq = 1920 * 1080
+    want = 2 * (ysz + 2 * csz) + 32 * ysz + 8 * ncus + 64 * ncus + lq * 3 // 2 * 4 * (cs + es)
+    assert want < d < want + 4096           # + the per-picture parameter block
+    assert h >= 64 * ncus + lq * 3 // 2 * es
+    # a wider search needs a wider margin; dropping levels drops their outputs
+    assert _fp(lib, 1920, 1080, r=256)[1] > d
+    assert _fp(lib, 1920, 1080, mask=64)[1] < d
+    assert _fp(lib, 1920, 1080, dio=1)[2] < h
+    for bad in ((1921, 1080), (8, 8)):
+        assert _fp(lib, *bad)[0] == -2
+    assert _fp(lib, 1920, 1080, ctu=32)[0] == -2
+    assert _fp(lib, 1920, 1080, r=300)[0] == -2
+    assert lib.xin_gpu_stream_footprint(None, None, None) == -2

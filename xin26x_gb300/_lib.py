@@ -39,6 +39,23 @@ class xin_gpu_tq_block(C.Structure):
                 ("qp", i32)]
 
 
+class xin_gpu_server_cfg(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("mpix_budget", C.c_double), ("max_inflight", u32), ("max_streams", u32),
+                ("max_queue", u32), ("reserved", u32)]
+
+
+class xin_gpu_server_done(C.Structure):
+    _fields_ = [("stream_id", i32), ("frame_index", u32), ("user_tag", C.c_uint64), ("status", i32),
+                ("has_results", i32), ("gpu_ms", C.c_float), ("reserved", C.c_float), ("queue_ms", C.c_double),
+                ("latency_ms", C.c_double)]
+
+
+class xin_gpu_server_stats(C.Structure):
+    _fields_ = [("streams", i32), ("running", i32), ("queued", i32), ("reserved", i32), ("hbm_budget", C.c_uint64),
+                ("hbm_used", C.c_uint64), ("mpix_used", C.c_double), ("launched", C.c_uint64),
+                ("completed", C.c_uint64)]
+
+
 class xin_gpu_mv(C.Structure):
     _fields_ = [("mvX", C.c_int16), ("mvY", C.c_int16)]
 
@@ -111,6 +128,14 @@ SIGNATURES = {
     "xin_gpu_fdct2_wxh_noalloc": ([vp, ip, vp, ip, u32, u32, i32, i32, vp], C.c_int),
     "xin_gpu_tq_batch": ([vp, i32, vp, vp, vp, vp, vp, C.c_size_t, i32], C.c_int),
     "xin_gpu_tq_batch_device": ([vp, i32, vp, vp, vp, vp, vp, C.c_size_t, i32, vp, vp], C.c_int),
+    "xin_gpu_stream_footprint": ([vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)], C.c_int),
+    "xin_gpu_server_open": ([vp, C.POINTER(vp)], C.c_int),
+    "xin_gpu_server_join": ([vp, vp, C.c_double, C.POINTER(i32)], C.c_int),
+    "xin_gpu_server_submit": ([vp, i32, vp, vp, C.c_uint64], C.c_int),
+    "xin_gpu_server_poll": ([vp, vp, i32, i32, C.POINTER(i32)], C.c_int),
+    "xin_gpu_server_leave": ([vp, i32, i32], C.c_int),
+    "xin_gpu_server_get_stats": ([vp, vp], C.c_int),
+    "xin_gpu_server_close": ([vp], C.c_int),
     "xin_gpu_tq_plan_create": ([vp, i32, C.c_size_t, i32, C.POINTER(vp)], C.c_int),
     "xin_gpu_tq_plan_run": ([vp, vp, vp, vp, vp, vp, vp], C.c_int),
     "xin_gpu_tq_plan_tiles": ([vp, vp], C.c_int),

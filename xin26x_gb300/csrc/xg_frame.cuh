@@ -8,6 +8,7 @@
 #include <chrono>
 #include <new>
 #include <string.h>
+#include <mutex>
 #include <thread>
 
 static const int XG_LEVEL_SIZE[4] = { 64, 32, 16, 8 };
@@ -183,8 +184,15 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     }
     s->me_bands = (ndy + s->me_band_rows - 1) / s->me_band_rows;
 #if XG_BITDEPTH == 8
-    if (xg_cuda_check(cudaFuncSetAttribute(k_me_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->me_smem),
-                      "me smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
+    /* the limit is per kernel, not per launch: set it once to the most any
+     * stream uses, so that streams of other sizes opened later (on any thread)
+     * cannot lower it under a stream already running */
+    static std::once_flag me_attr_once;
+    static cudaError_t me_attr_err = cudaSuccess;
+    std::call_once(me_attr_once, [] {
+        me_attr_err = cudaFuncSetAttribute(k_me_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
+    if (xg_cuda_check(me_attr_err, "me smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
 #endif
     *out = s;
     return XIN_GPU_OK;
@@ -322,6 +330,9 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
     if (s->inflight) { xg_set_error(XIN_GPU_ERR_STATE, "frame_submit: previous picture not collected by frame_wait"); return XIN_GPU_ERR_STATE; }
     const xin_gpu_stream_cfg &c = s->cfg;
     if (pic->qp < 0 || pic->qp > 63 || pic->uv_qp < 0 || pic->uv_qp > 63) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: QP out of range"); return XIN_GPU_ERR_ARG; }
+    /* the previous picture's copies may still read the pinned staging (its first
+     * picture is not collected by frame_wait) */
+    if (s->nsub > 0 && xg_cuda_check(cudaEventSynchronize(s->ev1), "frame_submit")) return XIN_GPU_ERR_CUDA;
     XgPicParams pp;
     memset(&pp, 0, sizeof pp);
     for (int p = 0; p < 3; p++) {

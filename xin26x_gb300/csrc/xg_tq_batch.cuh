@@ -180,15 +180,23 @@ static cudaError_t xg_tq_launch_class(int G, int nblk, int w, int h, const XgTqJ
     int sms = 152;
     int grid = std::min((nblk + ng - 1) / ng, sms * 8);
     if (grid < 1) grid = 1;
+    /* per-kernel limit set once to the largest group layout (200 KB), never
+     * lowered, so that concurrent callers with other block sizes cannot race */
+    static std::once_flag attr_once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(attr_once, [] {
+        const int lim = 200 * 1024;
+        attr_err = cudaFuncSetAttribute(k_tq_batch<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        if (attr_err == cudaSuccess) attr_err = cudaFuncSetAttribute(k_tq_batch<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        if (attr_err == cudaSuccess) attr_err = cudaFuncSetAttribute(k_tq_batch<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        if (attr_err == cudaSuccess) attr_err = cudaFuncSetAttribute(k_tq_batch<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    });
+    if (attr_err != cudaSuccess) return attr_err;
     switch (G) {
-    case 32: cudaFuncSetAttribute(k_tq_batch<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-             k_tq_batch<32><<<grid, 256, smem, st>>>(jobs, list, nblk, w, h, res, q, r, rout, nz); break;
-    case 64: cudaFuncSetAttribute(k_tq_batch<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-             k_tq_batch<64><<<grid, 256, smem, st>>>(jobs, list, nblk, w, h, res, q, r, rout, nz); break;
-    case 128: cudaFuncSetAttribute(k_tq_batch<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-              k_tq_batch<128><<<grid, 256, smem, st>>>(jobs, list, nblk, w, h, res, q, r, rout, nz); break;
-    default: cudaFuncSetAttribute(k_tq_batch<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-             k_tq_batch<256><<<grid, 256, smem, st>>>(jobs, list, nblk, w, h, res, q, r, rout, nz); break;
+    case 32: k_tq_batch<32><<<grid, 256, smem, st>>>(jobs, list, nblk, w, h, res, q, r, rout, nz); break;
+    case 64: k_tq_batch<64><<<grid, 256, smem, st>>>(jobs, list, nblk, w, h, res, q, r, rout, nz); break;
+    case 128: k_tq_batch<128><<<grid, 256, smem, st>>>(jobs, list, nblk, w, h, res, q, r, rout, nz); break;
+    default: k_tq_batch<256><<<grid, 256, smem, st>>>(jobs, list, nblk, w, h, res, q, r, rout, nz); break;
     }
     xg_count_launch(1);
     return cudaGetLastError();
