@@ -42,6 +42,7 @@ QPS = (27, 32, 37)
 LAMBDA = {27: 45, 32: 64, 37: 91}      # sad lambda per QP (fixed table for the synthetic run)
 NFRAMES = 30
 SEED = 1080
+ME_DRAM_BYTES = 5.260e6        # ncu: DRAM bytes of one k_me_tiles launch at this workload
 
 
 def workload_config():
@@ -69,10 +70,14 @@ class ClockSampler:
                 ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                 "--format=csv,noheader,nounits", "-lms", "20", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0:    # sampling runs before the timed region starts
+                time.sleep(0.01)
+            self.lines.clear()
         except Exception:
             self.proc = None
 
@@ -312,7 +317,10 @@ def run_gpu(args):
                "config": workload_config(),
                "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_mc_tq": stage[2], "copies": stage[3]},
                "roofline": {"bound": "int", "kernel": "k_me_tiles", "achieved": achieved / 1e12, "peak": peak.value / 1e12,
-                            "unit": "Tabsdiff/s", "frac": achieved / peak.value, "traffic": None,
+                            "unit": "Tabsdiff/s", "frac": achieved / peak.value, "traffic": ME_DRAM_BYTES,
+                            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_me_tiles launch "
+                                              "(ncu, 1080p, +-64, cold cache); algorithmic bytes (current + "
+                                              "reference luma) 4.15e6",
                             "peak_source": "xin_gpu_measure_sad_peak: vabsdiff4+dp4a register loop on this GPU, this run",
                             "algorithmic": f"(W/8)(H/8)(2R+1)^2*64 = {algo:.4g} abs differences per launch"},
                "e2e": {"value": e2e_val, "unit": "Mpixel/s", "h2d_bytes_per_step": W * H * 3 // 2,
