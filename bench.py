@@ -321,7 +321,7 @@ def run_gpu(args):
                             "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_me_tiles launch "
                                               "(ncu, 1080p, +-64, cold cache); algorithmic bytes (current + "
                                               "reference luma) 4.15e6",
-                            "peak_source": "xin_gpu_measure_sad_peak: vabsdiff4+dp4a register loop on this GPU, this run",
+                            "peak_source": "xin_gpu_measure_sad_peak: the faster of vabsdiff4+dp4a and vabsdiff4.add register loops on this GPU, this run",
                             "algorithmic": f"(W/8)(H/8)(2R+1)^2*64 = {algo:.4g} abs differences per launch"},
                "e2e": {"value": e2e_val, "unit": "Mpixel/s", "h2d_bytes_per_step": W * H * 3 // 2,
                        "d2h_bytes_per_step": cu_bytes + q_bytes,

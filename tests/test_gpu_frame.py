@@ -87,3 +87,28 @@ def test_frame_full_search_range_64():
         for name in ("mvx", "mvy", "int_cost", "cost"):
             assert out["cu"][name][i] == recs[name][i], (i, name)
         assert np.array_equal(out["cu"]["nz"][i], recs["nz"][i]) and np.array_equal(out["cu"]["ssd"][i], recs["ssd"][i])
+
+
+@pytest.mark.parametrize("bd,R", [(10, 64), (8, 256), (10, 256)])
+def test_frame_wide_search_sampled(bd, R):
+    """Search ranges up to the reference maximum (+-256, clamped by the picture window)
+    at both bit depths, checked on a CU sample of every level."""
+    w, h = 384, 256
+    seq = synth.sequence(w, h, 2, seed=R + bd, bitdepth=bd, objects=2)
+    fs = FrameStream(w, h, search_range=R, out_q=True, out_rec=True, bitdepth=bd)
+    fs.submit(*seq[0], qp=32, uv_qp=32, sad_lambda=64)
+    fs.wait()
+    fs.submit(*seq[1], qp=37, uv_qp=37, sad_lambda=91)
+    out = fs.wait()
+    rng = np.random.default_rng(R)
+    sample = []
+    for (size, first, cx, cy), n_pick in zip(fs.levels, (2, 3, 6, 12)):
+        n = cx * cy
+        sample += list(first + rng.choice(n, size=min(n, n_pick), replace=False))
+    recs, q, rec = oracle_frame.run(seq[1], seq[0], fs.levels, search_range=R, qp=37, uv_qp=37, sad_lambda=91,
+                                    bitdepth=bd, cus=sample)
+    fs.close()
+    for i in sample:
+        for name in ("mvx", "mvy", "int_cost", "cost"):
+            assert out["cu"][name][i] == recs[name][i], (bd, R, i, name)
+        assert np.array_equal(out["cu"]["nz"][i], recs["nz"][i]) and np.array_equal(out["cu"]["ssd"][i], recs["ssd"][i])

@@ -170,7 +170,7 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     if (bands > ndy) bands = ndy;
     {
         /* word positions per band row: nx + 60; pitch congruent to nx (mod 32) */
-        int nx = 2 * R + 1, relw = nx + 60;
+        int nx = 2 * R + 1, relw = XG_ME_RELW(nx);
         s->me_row_words = relw + (((nx - relw) % 32) + 32) % 32;
     }
     for (;;) {
@@ -178,12 +178,11 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         int rows_rounded = (s->me_band_rows + 2) / 3 * 3;     /* candidate rows rounded up to the per-lane chunk */
         s->me_band_rows_alloc = 64 + rows_rounded - 1;
         s->me_smem = sizeof(uint32_t) * ((size_t)s->me_band_rows_alloc * s->me_row_words + (2 * R + 1) + s->me_band_rows_alloc +
-                                         16 * 96);
+                                         16 * XG_ME_SLOTS + XG_ME_CUR_WORDS);
         if (s->me_smem <= 200 * 1024 || s->me_band_rows == 1) break;
         bands++;
     }
     s->me_bands = (ndy + s->me_band_rows - 1) / s->me_band_rows;
-#if XG_BITDEPTH == 8
     /* the limit is per kernel, not per launch: set it once to the most any
      * stream uses, so that streams of other sizes opened later (on any thread)
      * cannot lower it under a stream already running */
@@ -193,7 +192,6 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         me_attr_err = cudaFuncSetAttribute(k_me_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     });
     if (xg_cuda_check(me_attr_err, "me smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
-#endif
     *out = s;
     return XIN_GPU_OK;
 }
@@ -266,18 +264,9 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             mp.keys[L] = s->lev_on[L] ? s->keys + s->lev_first[L] : nullptr;
             mp.cus_x[L] = s->lev_cx[L];
         }
-#if XG_BITDEPTH == 8
         dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, s->me_bands);
         k_me_tiles<<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, s->dpp);
         nl++;
-#else
-        for (int L = 0; L < 4; L++) {
-            if (!s->lev_on[L]) continue;
-            dim3 grd(s->lev_cx[L] * s->lev_cy[L], 8);
-            k_me_generic<<<grd, 128, 0, st>>>(mp, s->dpp, L, XG_LEVEL_SIZE[L], s->lev_cx[L]);
-            nl++;
-        }
-#endif
         xg_stage_event(s->evs[2], st, capturing);
         int li = 0;
         for (int L = 0; L < 4; L++) {
@@ -458,17 +447,21 @@ extern "C" int xin_gpu_measure_sad_peak(double *absdiff_per_s)
     cudaMemsetAsync(in, 0x5a, 4096, t->stream);
     cudaEvent_t a, b;
     cudaEventCreate(&a); cudaEventCreate(&b);
+    /* both packed forms: vabsdiff4 + dp4a, and vabsdiff4 with add-reduction (the
+     * form the search kernel issues); the faster one is the ceiling */
     float best = 1e30f;
-    for (int rep = 0; rep < 4; rep++) {
-        cudaEventRecord(a, t->stream);
-        k_sad_peak<<<blocks, threads, 0, t->stream>>>(in, out, iters);
-        cudaEventRecord(b, t->stream);
-        cudaEventSynchronize(b);
-        float ms = 0;
-        cudaEventElapsedTime(&ms, a, b);
-        if (rep && ms < best) best = ms;
-    }
-    xg_count_launch(4);
+    for (int form = 0; form < 2; form++)
+        for (int rep = 0; rep < 4; rep++) {
+            cudaEventRecord(a, t->stream);
+            if (form == 0) k_sad_peak<<<blocks, threads, 0, t->stream>>>(in, out, iters);
+            else k_sad_peak_add<<<blocks, threads, 0, t->stream>>>(in, out, iters);
+            cudaEventRecord(b, t->stream);
+            cudaEventSynchronize(b);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, a, b);
+            if (rep && ms < best) best = ms;
+        }
+    xg_count_launch(8);
     cudaEventDestroy(a); cudaEventDestroy(b);
     if (xg_cuda_check(cudaGetLastError(), "sad peak")) return XIN_GPU_ERR_CUDA;
     *absdiff_per_s = (double)blocks * threads * iters * 8 * 4 / (best * 1e-3);

@@ -108,7 +108,11 @@ __global__ void __launch_bounds__(256) k_qpel_planes(XgPlane ref, XgQpel qp)
  * unsigned minimum over lanes, warps and CTAs (atomicMin) selects the smallest
  * cost and, among equal costs, the first candidate in raster order -- the
  * strict '<' raster search.  Costs: (SAD << 8) + (bits(4dx) + bits(4dy)) * lambda
- * (predictor 0).  8-bit pixels only (10-bit uses k_me_tiles_generic). */
+ * (predictor 0).
+ * 10-bit pictures: a word holds two 16-bit pixels (word (r, x) = pixels x, x+1),
+ * |a - b| of two pixels and their sum is one vabsdiff2 with add-reduction, and
+ * the current 64x64 tile sits in shared memory (read as broadcasts; each warp
+ * keeps a window of the three current rows a reference row meets). */
 #define XG_ME_TILE 64
 #define XG_ME_THREADS 512
 
@@ -160,6 +164,29 @@ __global__ void k_sad_peak(const uint32_t *in, uint32_t *out, int iters)
     out[t] = acc0 + acc1 + acc2 + acc3;
 }
 
+/* the same on the one-instruction form the search kernel uses: vabsdiff4 with
+ * add-reduction into the accumulator */
+__global__ void k_sad_peak_add(const uint32_t *in, uint32_t *out, int iters)
+{
+    uint32_t a[8], b[8];
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int i = 0; i < 8; i++) { a[i] = in[(t + i) & 1023]; b[i] = in[(t * 7 + i * 13) & 1023]; }
+    uint32_t acc[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            uint32_t d;
+            asm volatile("vabsdiff4.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a[i]), "r"(b[i]), "r"(acc[i]));
+            acc[i] = d;
+        }
+#pragma unroll
+        for (int i = 0; i < 8; i++) { uint32_t tmp = a[i]; a[i] = b[(i + 1) & 7] ^ (uint32_t)it; b[(i + 1) & 7] = tmp; }
+    }
+    uint32_t s = 0;
+    for (int i = 0; i < 8; i++) s += acc[i];
+    out[t] = s;
+}
+
 struct XgMeParams {
     XgPlane cur, ref;
     int W, H, ctu, R;
@@ -187,7 +214,18 @@ __device__ __forceinline__ uint32_t xg_sad4(uint32_t a, uint32_t b, uint32_t acc
     return d;
 }
 
-#if XG_BITDEPTH == 8
+/* acc + |a.lo - b.lo| + |a.hi - b.hi| over 16-bit halves: one vabsdiff2 with add-reduction */
+__device__ __forceinline__ uint32_t xg_sad2(uint32_t a, uint32_t b, uint32_t acc)
+{
+    uint32_t d;
+    asm("vabsdiff2.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(acc));
+    return d;
+}
+
+/* word positions per staged band row: the last word a warp reads starts at
+ * 48 + (2R) + 12 (8-bit, 4 pixels a word) or 48 + (2R) + 14 (10-bit, 2 pixels) */
+#define XG_ME_RELW(nx) ((nx) + (XG_BITDEPTH == 8 ? 60 : 62))
+#define XG_ME_CUR_WORDS (XG_BITDEPTH == 8 ? 0 : 64 * 32)     /* shared current tile (10-bit) */
 #define XG_ME_D 3                         /* candidate rows per lane and pass */
 #define XG_ME_SLOTS (32 * XG_ME_D)        /* candidates per warp and pass */
 __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, const XgPicParams *pp)
@@ -205,25 +243,33 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     const int nv = nch * nx;                                 /* (chunk, column) slots, one per lane and pass */
     const int rows = XG_ME_TILE + nch * XG_ME_D - 1;         /* band rows staged */
 
-    const int relw = nx + 60;                                /* word positions read per band row */
-    uint32_t *refw = sm;                                     /* [rows][row_words] */
-    uint32_t *mvcx = sm + (size_t)p.band_rows_alloc * p.row_words;   /* [nx] */
+    const int relw = XG_ME_RELW(nx);                         /* word positions read per band row */
+    uint32_t *refw = sm + XG_ME_CUR_WORDS;                   /* [rows][row_words] */
+    uint32_t *mvcx = refw + (size_t)p.band_rows_alloc * p.row_words; /* [nx] */
     uint32_t *mvcy = mvcx + nx;                              /* [band_rows rounded to XG_ME_D] */
     uint32_t *s16 = mvcy + p.band_rows_alloc;                /* [16][XG_ME_SLOTS] */
+#if XG_BITDEPTH != 8
+    uint32_t *scur = sm;                                     /* [64][32]: row y, pixels 2k, 2k+1 (16-byte aligned) */
+#endif
 
     /* ---- stage the reference band: pixels (X0 + x .. X0 + x + 3, Y0 + r) -> refw[r * row_words + x] */
     const int X0 = tx0 - p.R, Y0 = ty0 + dyb0;
     for (int i = threadIdx.x; i < rows * relw; i += blockDim.x) {
         int r = i / relw, x = i - r * relw;
         const xg_pix *src = p.ref.data + (intptr_t)(Y0 + r) * p.ref.pitch + X0 + x;
+#if XG_BITDEPTH == 8
         refw[r * p.row_words + x] = (uint32_t)src[0] | ((uint32_t)src[1] << 8) | ((uint32_t)src[2] << 16) | ((uint32_t)src[3] << 24);
+#else
+        refw[r * p.row_words + x] = (uint32_t)src[0] | ((uint32_t)src[1] << 16);
+#endif
     }
     const uint32_t lambda = pp->lambda;
     for (int i = threadIdx.x; i < nx; i += blockDim.x) mvcx[i] = xg_mvd_bits(4 * (i - p.R)) * lambda;
     for (int i = threadIdx.x; i < nch * XG_ME_D; i += blockDim.x) mvcy[i] = xg_mvd_bits(4 * (dyb0 + i)) * lambda;
 
-    /* ---- this warp's 16x16 block of the current picture in registers */
+    /* ---- this warp's 16x16 block of the current picture: registers (8-bit) or the shared tile (10-bit) */
     const int bx = (warp & 3) * 16, by = (warp >> 2) * 16;
+#if XG_BITDEPTH == 8
     uint32_t cur[16][4];
 #pragma unroll
     for (int r = 0; r < 16; r++)
@@ -232,6 +278,12 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
             const xg_pix *c = p.cur.data + (intptr_t)(ty0 + by + r) * p.cur.pitch + tx0 + bx + 4 * k;
             cur[r][k] = (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16) | ((uint32_t)c[3] << 24);
         }
+#else
+    for (int i = threadIdx.x; i < 64 * 32; i += blockDim.x) {
+        const xg_pix *c = p.cur.data + (intptr_t)(ty0 + (i >> 5)) * p.cur.pitch + tx0 + 2 * (i & 31);
+        scur[i] = (uint32_t)c[0] | ((uint32_t)c[1] << 16);
+    }
+#endif
 
     /* ---- windows and liveness of this warp's CUs; a band inside every window needs no per-candidate check */
     bool live[5];
@@ -281,6 +333,7 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
 #pragma unroll
                 for (int b = 0; b < 4; b++) acc[d][b] = 0;
             /* reference row t of the block feeds current row t - d of candidate row d */
+#if XG_BITDEPTH == 8
 #pragma unroll
             for (int t = 0; t < 16 + XG_ME_D - 1; t++) {
                 const uint32_t *q = base + t * p.row_words;
@@ -297,6 +350,34 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                     }
                 }
             }
+#else
+            uint32_t cw[XG_ME_D][8];          /* current rows t, t-1, t-2 (slot = row % XG_ME_D) */
+            const uint32_t *crow = scur + by * 32 + (bx >> 1);
+#pragma unroll
+            for (int t = 0; t < 16 + XG_ME_D - 1; t++) {
+                if (t < 16) {
+                    const uint4 lo = *(const uint4 *)(crow + t * 32), hi = *(const uint4 *)(crow + t * 32 + 4);
+                    uint32_t *w = cw[t % XG_ME_D];
+                    w[0] = lo.x; w[1] = lo.y; w[2] = lo.z; w[3] = lo.w; w[4] = hi.x; w[5] = hi.y; w[6] = hi.z; w[7] = hi.w;
+                }
+                const uint32_t *q = base + t * p.row_words;
+                uint32_t rw[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) rw[k] = q[2 * k];
+#pragma unroll
+                for (int d = 0; d < XG_ME_D; d++) {
+                    const int r = t - d;
+                    if (r >= 0 && r < 16) {
+                        const int b = r < 8 ? 0 : 2;
+                        const uint32_t *c = cw[r % XG_ME_D];
+#pragma unroll
+                        for (int k = 0; k < 4; k++) acc[d][b] = xg_sad2(c[k], rw[k], acc[d][b]);
+#pragma unroll
+                        for (int k = 4; k < 8; k++) acc[d][b + 1] = xg_sad2(c[k], rw[k], acc[d][b + 1]);
+                    }
+                }
+            }
+#endif
             const int dx = col - p.R;
 #pragma unroll
             for (int d = 0; d < XG_ME_D; d++) {
@@ -368,42 +449,6 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) { unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o); k = v < k ? v : k; }
         if (lane == 0 && live64 && k != ~0ull) atomicMin(p.keys[0] + (ty0 / 64) * p.cus_x[0] + tx0 / 64, k);
-    }
-}
-#endif
-
-/* generic (any bit depth) integer search: one CTA per (CU, candidate row band);
- * used for 10-bit pictures and as a cross-check of k_me_tiles */
-__global__ void k_me_generic(XgMeParams p, const XgPicParams *pp, int level, int size, int cus_x)
-{
-    __shared__ unsigned long long red[32];
-    int cu = blockIdx.x;
-    int cx = (cu % cus_x) * size, cy = (cu / cus_x) * size;
-    int x0, x1, y0, y1;
-    xg_cu_window(p, cx, cy, size, x0, x1, y0, y1);
-    int nx = 2 * p.R + 1;
-    unsigned long long k = ~0ull;
-    int dy = y0 + (int)blockIdx.y;
-    for (; dy <= y1; dy += gridDim.y) {
-        for (int dx = x0 + (int)threadIdx.x; dx <= x1; dx += blockDim.x) {
-            uint32_t sad = 0;
-            for (int y = 0; y < size; y++) {
-                const xg_pix *a = p.cur.data + (intptr_t)(cy + y) * p.cur.pitch + cx;
-                const xg_pix *b = p.ref.data + (intptr_t)(cy + y + dy) * p.ref.pitch + cx + dx;
-                for (int x = 0; x < size; x++) sad += (uint32_t)abs((int)a[x] - (int)b[x]);
-            }
-            uint32_t cost = (sad << XG_COST_FRACTION) + (xg_mvd_bits(4 * dx) + xg_mvd_bits(4 * dy)) * pp->lambda;
-            unsigned long long kk = ((unsigned long long)cost << 32) | (uint32_t)((dy + p.R) * nx + dx + p.R);
-            k = kk < k ? kk : k;
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) { unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o); k = v < k ? v : k; }
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = k;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int i = 1; i < (int)(blockDim.x >> 5); i++) k = red[i] < k ? red[i] : k;
-        if (k != ~0ull) atomicMin(p.keys[level] + cu, k);
     }
 }
 
