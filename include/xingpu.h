@@ -390,10 +390,11 @@ int  xin_gpu_server_leave(xin_gpu_server *srv, int32_t stream_id, int32_t timeou
 int  xin_gpu_server_get_stats(xin_gpu_server *srv, xin_gpu_server_stats *stats);
 int  xin_gpu_server_close(xin_gpu_server *srv);     /* finishes queued pictures, frees every stream */
 
-/* Measured throughput of this GPU's packed 8-bit SAD instructions on
- * register-resident data (the faster of vabsdiff4 + dp4a and vabsdiff4 with
- * add-reduction), in absolute differences per second: the ceiling of the
- * integer search kernel, used as its roofline. */
+/* Measured throughput of this GPU's packed SAD instructions on
+ * register-resident data, in absolute differences per second: the ceiling of
+ * the integer search kernel, used as its roofline.  8-bit library: the faster
+ * of vabsdiff4 + dp4a and vabsdiff4 with add-reduction; 10-bit library: the
+ * packed 16-bit add-then-max form its search issues. */
 int  xin_gpu_measure_sad_peak(double *absdiff_per_s);
 
 #ifdef __cplusplus

@@ -453,7 +453,8 @@ extern "C" int xin_gpu_measure_sad_peak(double *absdiff_per_s)
     for (int form = 0; form < 2; form++)
         for (int rep = 0; rep < 4; rep++) {
             cudaEventRecord(a, t->stream);
-            if (form == 0) k_sad_peak<<<blocks, threads, 0, t->stream>>>(in, out, iters);
+            if (XG_BITDEPTH != 8) k_sad_peak10<<<blocks, threads, 0, t->stream>>>(in, out, iters);
+            else if (form == 0) k_sad_peak<<<blocks, threads, 0, t->stream>>>(in, out, iters);
             else k_sad_peak_add<<<blocks, threads, 0, t->stream>>>(in, out, iters);
             cudaEventRecord(b, t->stream);
             cudaEventSynchronize(b);
@@ -464,6 +465,6 @@ extern "C" int xin_gpu_measure_sad_peak(double *absdiff_per_s)
     xg_count_launch(8);
     cudaEventDestroy(a); cudaEventDestroy(b);
     if (xg_cuda_check(cudaGetLastError(), "sad peak")) return XIN_GPU_ERR_CUDA;
-    *absdiff_per_s = (double)blocks * threads * iters * 8 * 4 / (best * 1e-3);
+    *absdiff_per_s = (double)blocks * threads * iters * 8 * (XG_BITDEPTH == 8 ? 4 : 2) / (best * 1e-3);
     return XIN_GPU_OK;
 }

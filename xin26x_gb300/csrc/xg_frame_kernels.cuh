@@ -109,10 +109,12 @@ __global__ void __launch_bounds__(256) k_qpel_planes(XgPlane ref, XgQpel qp)
  * cost and, among equal costs, the first candidate in raster order -- the
  * strict '<' raster search.  Costs: (SAD << 8) + (bits(4dx) + bits(4dy)) * lambda
  * (predictor 0).
- * 10-bit pictures: a word holds two 16-bit pixels (word (r, x) = pixels x, x+1),
- * |a - b| of two pixels and their sum is one vabsdiff2 with add-reduction, and
- * the current 64x64 tile sits in shared memory (read as broadcasts; each warp
- * keeps a window of the three current rows a reference row meets). */
+ * 10-bit pictures: a word holds two 16-bit pixels (word (r, x) = pixels x, x+1);
+ * per pixel pair |a - b| + 1024 per lane comes from one packed add-then-max on
+ * biased lanes and accumulates lane-wise (32 pairs per 8x8 quadrant fit 16 bits),
+ * the bias removed at the end; the current 64x64 tile sits in shared memory
+ * (read as broadcasts; each warp keeps a window of the three current rows a
+ * reference row meets, with their negations).  Samples must be below 1024. */
 #define XG_ME_TILE 64
 #define XG_ME_THREADS 512
 
@@ -187,6 +189,29 @@ __global__ void k_sad_peak_add(const uint32_t *in, uint32_t *out, int iters)
     out[t] = s;
 }
 
+/* 10-bit form: the biased packed add-then-max per pixel pair plus a lane-wise
+ * accumulate, what the 10-bit search kernel issues */
+__global__ void k_sad_peak10(const uint32_t *in, uint32_t *out, int iters)
+{
+    uint32_t a[8], b[8], an[8];
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int i = 0; i < 8; i++) {
+        a[i] = in[(t + i) & 1023] & 0x03ff03ffu;
+        b[i] = in[(t * 7 + i * 13) & 1023] & 0x03ff03ffu;
+        an[i] = 0x04000400u - a[i];
+    }
+    uint32_t acc[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+    for (int it = 0; it < iters; it++) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) acc[i] += __viaddmax_u16x2(a[i], 0x04000400u - b[i], b[i] + an[i]);
+#pragma unroll
+        for (int i = 0; i < 8; i++) { uint32_t tmp = b[i]; b[i] = b[(i + 1) & 7] ^ ((uint32_t)it & 0x01ff01ffu); b[(i + 1) & 7] = tmp; }
+    }
+    uint32_t s = 0;
+    for (int i = 0; i < 8; i++) s += acc[i];
+    out[t] = s;
+}
+
 struct XgMeParams {
     XgPlane cur, ref;
     int W, H, ctu, R;
@@ -214,13 +239,15 @@ __device__ __forceinline__ uint32_t xg_sad4(uint32_t a, uint32_t b, uint32_t acc
     return d;
 }
 
-/* acc + |a.lo - b.lo| + |a.hi - b.hi| over 16-bit halves: one vabsdiff2 with add-reduction */
-__device__ __forceinline__ uint32_t xg_sad2(uint32_t a, uint32_t b, uint32_t acc)
+/* |a - b| + 1024 in each 16-bit lane of two 10-bit pixel pairs, given the
+ * negations an = 1024 - a and bn = 1024 - b (lane-wise, no borrow since lanes are
+ * below 1024): max(a + bn, b + an), one packed add-then-max (__viaddmax_u16x2).
+ * Lanes stay below 2048, so 32 of them accumulate in a 16-bit lane exactly. */
+__device__ __forceinline__ uint32_t xg_absdiff2_biased(uint32_t a, uint32_t an, uint32_t b, uint32_t bn)
 {
-    uint32_t d;
-    asm("vabsdiff2.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(acc));
-    return d;
+    return __viaddmax_u16x2(a, bn, b + an);
 }
+#define XG_NEG2(x) (0x04000400u - (x))
 
 /* word positions per staged band row: the last word a warp reads starts at
  * 48 + (2R) + 12 (8-bit, 4 pixels a word) or 48 + (2R) + 14 (10-bit, 2 pixels) */
@@ -351,32 +378,39 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                 }
             }
 #else
-            uint32_t cw[XG_ME_D][8];          /* current rows t, t-1, t-2 (slot = row % XG_ME_D) */
+            uint32_t cw[XG_ME_D][8], cn[XG_ME_D][8];   /* current rows t, t-1, t-2 (slot = row % XG_ME_D), negated */
             const uint32_t *crow = scur + by * 32 + (bx >> 1);
 #pragma unroll
             for (int t = 0; t < 16 + XG_ME_D - 1; t++) {
                 if (t < 16) {
                     const uint4 lo = *(const uint4 *)(crow + t * 32), hi = *(const uint4 *)(crow + t * 32 + 4);
-                    uint32_t *w = cw[t % XG_ME_D];
+                    uint32_t *w = cw[t % XG_ME_D], *wn = cn[t % XG_ME_D];
                     w[0] = lo.x; w[1] = lo.y; w[2] = lo.z; w[3] = lo.w; w[4] = hi.x; w[5] = hi.y; w[6] = hi.z; w[7] = hi.w;
+#pragma unroll
+                    for (int k = 0; k < 8; k++) wn[k] = XG_NEG2(w[k]);
                 }
                 const uint32_t *q = base + t * p.row_words;
-                uint32_t rw[8];
+                uint32_t rw[8], rn[8];
 #pragma unroll
-                for (int k = 0; k < 8; k++) rw[k] = q[2 * k];
+                for (int k = 0; k < 8; k++) { rw[k] = q[2 * k]; rn[k] = XG_NEG2(rw[k]); }
 #pragma unroll
                 for (int d = 0; d < XG_ME_D; d++) {
                     const int r = t - d;
                     if (r >= 0 && r < 16) {
                         const int b = r < 8 ? 0 : 2;
-                        const uint32_t *c = cw[r % XG_ME_D];
+                        const uint32_t *c = cw[r % XG_ME_D], *cng = cn[r % XG_ME_D];
 #pragma unroll
-                        for (int k = 0; k < 4; k++) acc[d][b] = xg_sad2(c[k], rw[k], acc[d][b]);
-#pragma unroll
-                        for (int k = 4; k < 8; k++) acc[d][b + 1] = xg_sad2(c[k], rw[k], acc[d][b + 1]);
+                        for (int k = 0; k < 8; k += 2)
+                            acc[d][b + (k >> 2)] += xg_absdiff2_biased(c[k], cng[k], rw[k], rn[k]) +
+                                                    xg_absdiff2_biased(c[k + 1], cng[k + 1], rw[k + 1], rn[k + 1]);
                     }
                 }
             }
+            /* lanes -> SAD: both lanes summed, less the bias of 64 pixels x 1024 */
+#pragma unroll
+            for (int d = 0; d < XG_ME_D; d++)
+#pragma unroll
+                for (int b = 0; b < 4; b++) acc[d][b] = (acc[d][b] & 0xffffu) + (acc[d][b] >> 16) - 64u * 1024u;
 #endif
             const int dx = col - p.R;
 #pragma unroll
