@@ -297,6 +297,7 @@ def run_gpu(args):
     # plain per-call form on a sample of CUs (one synchronous launch per reference call)
     percall = percall_sample(lib, frames)
     kbatch = kernel_batch_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup) if rank == 0 else None
+    wide = wide_search_bench(torch, flush) if rank == 0 else None
     serving = None
     if rank == 0 and world == 1:
         from xin26x_gb300 import serve_bench
@@ -328,6 +329,7 @@ def run_gpu(args):
                        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}},
                "percall": percall,
                "kernel_batch": kbatch,
+               "wide_search_4k_10bit": wide,
                "serving": serving,
                "gpu_launches": int(launches),
                "clocks": clk,
@@ -390,6 +392,56 @@ def kernel_batch_bench(torch, flush, steps, warmup, nblocks=65536, seed=65536):
                        "frac": achieved / (hbm or 6800.0), "algorithmic_bytes": int(algo),
                        "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "of fallback 6.8 TB/s"}
     return out
+
+
+def wide_search_bench(torch, flush, pictures=3):
+    """3840x2160 10-bit 4:2:0, CTU 128, exhaustive +-256 integer search (the
+    reference's maximum picture size and a wide search), full sub-pel search and
+    TQ of CU levels 64/32/16/8; device-resident pictures, CUDA-event device time
+    per picture, L2 flushed between pictures."""
+    from xin26x_gb300 import _lib, synth
+    w, h, r = 3840, 2160, 256
+    g = _lib.load(10)
+    assert g.xin_gpu_init(torch.cuda.current_device()) == 0
+    seq = synth.sequence(w, h, pictures, seed=2160, bitdepth=10, objects=8, octaves=4)
+    dev = [tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f) for f in seq]
+    cfg = _lib.xin_gpu_stream_cfg(w, h, 128, r, 120, 0, 1, 1)
+    hs = C.c_void_p()
+    assert g.xin_gpu_stream_open(C.byref(cfg), C.byref(hs)) == 0, g.xin_gpu_last_error()
+    res = _lib.xin_gpu_results()
+    ms, stage = [], np.zeros(4)
+    for k in range(pictures):
+        flush.fill_(k & 255)
+        torch.cuda.synchronize()
+        pic = _lib.xin_gpu_picture()
+        for i, t in enumerate(dev[k]):
+            pic.plane[i] = t.data_ptr()
+            pic.stride[i] = t.shape[1]
+        pic.qp = pic.uv_qp = (27, 32, 37)[k % 3]
+        pic.sad_lambda = LAMBDA[pic.qp]
+        assert g.xin_gpu_frame_submit(hs, C.byref(pic)) == 0, g.xin_gpu_last_error()
+        assert g.xin_gpu_frame_wait(hs, C.byref(res), -1) == 0, g.xin_gpu_last_error()
+        if k:
+            st = (C.c_float * 4)()
+            g.xin_gpu_stream_stage_ms(hs, st)
+            stage += np.array(list(st))
+            ms.append(res.gpu_ms)
+    g.xin_gpu_stream_close(hs)
+    stage /= len(ms)
+    peak = C.c_double()
+    g.xin_gpu_measure_sad_peak(C.byref(peak))
+    algo = (w // 8) * (h // 8) * (2 * r + 1) ** 2 * 64
+    achieved = algo / (stage[1] * 1e-3)
+    return {"workload": "3840x2160 10-bit 4:2:0, CTU 128, exhaustive +-256 integer search + full sub-pel search, "
+                        "CU levels 64/32/16/8, DCT2 TU=CU, seeded texture (4 octaves) + 8 moving rectangles",
+            "pictures_timed": len(ms), "ms_per_picture": float(np.mean(ms)), "value": w * h / float(np.mean(ms)) / 1e3,
+            "unit": "Mpixel/s", "dtype": "u16",
+            "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_mc_tq": stage[2]},
+            "roofline": {"bound": "int", "kernel": "k_me_tiles (10-bit)", "achieved": achieved / 1e12,
+                         "peak": peak.value / 1e12, "unit": "Tabsdiff/s", "frac": achieved / peak.value,
+                         "peak_source": "xin_gpu_measure_sad_peak of the 10-bit library: packed 16-bit add-then-max "
+                                        "register loop on this GPU, this run",
+                         "algorithmic": f"(W/8)(H/8)(2R+1)^2*64 = {algo:.4g} abs differences per launch"}}
 
 
 def _measured_peaks():
