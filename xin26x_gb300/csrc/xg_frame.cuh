@@ -35,6 +35,8 @@ struct xin_gpu_stream {
     xg_coef *h_q[3];
     xg_pix *h_rec[3];
     cudaStream_t st;
+    cudaStream_t aux[3];   /* the tails of levels 2..4 run beside the first level's */
+    cudaEvent_t ev_fork, ev_join[3];
     cudaEvent_t ev0, ev1;
     cudaEvent_t evs[5];    /* stage boundaries, recorded inside the picture's launches */
     cudaGraphExec_t gexec[2];
@@ -71,6 +73,11 @@ static int xg_stream_free(xin_gpu_stream *s)
     for (int p = 0; p < 3; p++) { cudaFree(s->dq[p]); cudaFree(s->drec[p]); cudaFreeHost(s->h_in[p]); cudaFreeHost(s->h_q[p]); cudaFreeHost(s->h_rec[p]); }
     cudaFreeHost(s->h_pp); cudaFreeHost(s->h_res);
     for (int i = 0; i < 5; i++) if (s->evs[i]) cudaEventDestroy(s->evs[i]);
+    for (int i = 0; i < 3; i++) {
+        if (s->ev_join[i]) cudaEventDestroy(s->ev_join[i]);
+        if (s->aux[i]) cudaStreamDestroy(s->aux[i]);
+    }
+    if (s->ev_fork) cudaEventDestroy(s->ev_fork);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->st) cudaStreamDestroy(s->st);
@@ -120,6 +127,11 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
     for (int i = 0; i < 5 && e == cudaSuccess; i++) e = cudaEventCreate(&s->evs[i]);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+    for (int i = 0; i < 3 && e == cudaSuccess; i++) {
+        e = cudaStreamCreateWithFlags(&s->aux[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join[i], cudaEventDisableTiming);
+    }
     size_t ysz = s->plane_elems * sizeof(xg_pix), csz = s->cplane_elems * sizeof(xg_pix);
     size_t lq = (size_t)c.width * c.height, lc = lq / 4;
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
@@ -268,9 +280,17 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         k_me_tiles<<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, s->dpp);
         nl++;
         xg_stage_event(s->evs[2], st, capturing);
-        int li = 0;
+        /* the levels' tails are independent: fork them onto the auxiliary streams */
+        cudaEventRecord(s->ev_fork, st);
+        int li = 0, nfork = 0;
         for (int L = 0; L < 4; L++) {
             if (!s->lev_on[L]) continue;
+            cudaStream_t ls = st;
+            if (li > 0) {
+                ls = s->aux[li - 1];
+                cudaStreamWaitEvent(ls, s->ev_fork, 0);
+                nfork = li;
+            }
             XgTailParams tp;
             for (int p = 0; p < 3; p++) { tp.cur[p] = s->slot[cur][p]; tp.ref[p] = s->slot[ref][p]; }
             tp.qpel = s->qpel[ref];
@@ -285,14 +305,18 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             int n = s->lev_cx[L] * s->lev_cy[L];
             if (n > 0) {
                 switch (XG_LEVEL_SIZE[L]) {
-                case 64: k_cu_tail<64, 256><<<n, 256, 0, st>>>(tp, s->dpp); break;
-                case 32: k_cu_tail<32, 256><<<n, 256, 0, st>>>(tp, s->dpp); break;
-                case 16: k_cu_tail<16, 128><<<n, 128, 0, st>>>(tp, s->dpp); break;
-                default: k_cu_tail<8, 64><<<n, 64, 0, st>>>(tp, s->dpp); break;
+                case 64: k_cu_tail<64, 256><<<n, 256, 0, ls>>>(tp, s->dpp); break;
+                case 32: k_cu_tail<32, 256><<<n, 256, 0, ls>>>(tp, s->dpp); break;
+                case 16: k_cu_tail<16, 128><<<n, 128, 0, ls>>>(tp, s->dpp); break;
+                default: k_cu_tail<8, 64><<<n, 64, 0, ls>>>(tp, s->dpp); break;
                 }
                 nl++;
             }
             li++;
+        }
+        for (int i = 0; i < nfork; i++) {
+            cudaEventRecord(s->ev_join[i], s->aux[i]);
+            cudaStreamWaitEvent(st, s->ev_join[i], 0);
         }
         xg_stage_event(s->evs[3], st, capturing);
         if (!c.device_io) {
