@@ -299,7 +299,7 @@ typedef struct xin_gpu_picture {
     const XG_PIXEL *plane[3];    /* host Y, U, V */
     intptr_t stride[3];          /* elements */
     int32_t  qp, uv_qp;          /* slice QPs */
-    uint32_t sad_lambda;
+    uint32_t sad_lambda;         /* 0 .. 2^20 */
 } xin_gpu_picture;
 
 typedef struct xin_gpu_cu_result {

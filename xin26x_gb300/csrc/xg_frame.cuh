@@ -40,7 +40,7 @@ struct xin_gpu_stream {
     cudaEvent_t ev0, ev1;
     cudaEvent_t evs[5];    /* stage boundaries, recorded inside the picture's launches */
     cudaGraphExec_t gexec[2];
-    int me_bands, me_band_rows, me_band_rows_alloc, me_row_words;
+    int me_bands, me_band_rows, me_band_rows_alloc, me_row_words, me_nb;
     size_t me_smem;
     int nsub;
     int inflight;          /* a picture with results is queued */
@@ -174,24 +174,36 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         q.plane[0] = s->slot[i][0].data;
         q.pitch = s->pitch; q.w = c.width; q.h = c.height; q.pad = pad;
     }
-    /* integer-search band geometry: enough CTAs for the GPU, shared memory under 200 KB */
+    /* integer-search band geometry: enough CTAs for the GPU; shared memory within
+     * XG_ME_SMEM_MAX, taking more bands (less reuse of staged rows) or fewer
+     * buffered passes for the 32x32 / 64x64 sums (more barriers) when it does not fit */
     int R = c.search_range, ndy = 2 * R + 1;
     int tiles = ((c.width + 63) / 64) * ((c.height + 63) / 64);
     int bands = (4 * 152 + tiles - 1) / tiles;
     if (bands < 1) bands = 1;
     if (bands > ndy) bands = ndy;
     {
-        /* word positions per band row: nx + 60; pitch congruent to nx (mod 32) */
+        /* word positions per band row; pitch congruent to nx (mod 32) */
         int nx = 2 * R + 1, relw = XG_ME_RELW(nx);
         s->me_row_words = relw + (((nx - relw) % 32) + 32) % 32;
     }
     for (;;) {
         s->me_band_rows = (ndy + bands - 1) / bands;
-        int rows_rounded = (s->me_band_rows + 2) / 3 * 3;     /* candidate rows rounded up to the per-lane chunk */
+        int rows_rounded = (s->me_band_rows + XG_ME_D - 1) / XG_ME_D * XG_ME_D;   /* rounded up to the per-lane chunk */
         s->me_band_rows_alloc = 64 + rows_rounded - 1;
-        s->me_smem = sizeof(uint32_t) * ((size_t)s->me_band_rows_alloc * s->me_row_words + (2 * R + 1) + s->me_band_rows_alloc +
-                                         16 * XG_ME_SLOTS + XG_ME_CUR_WORDS);
-        if (s->me_smem <= 200 * 1024 || s->me_band_rows == 1) break;
+        size_t fixed = (size_t)s->me_band_rows_alloc * s->me_row_words + (2 * R + 1) + s->me_band_rows_alloc + XG_ME_CUR_WORDS;
+        s->me_nb = 0;
+        for (int nb = XG_ME_NB_MAX; nb >= 1 && !s->me_nb; nb /= 2)
+            if (sizeof(uint32_t) * (fixed + XG_ME_AGG_WORDS(nb)) <= XG_ME_SMEM_MAX) s->me_nb = nb;
+        if (s->me_nb) {
+            s->me_smem = sizeof(uint32_t) * (fixed + XG_ME_AGG_WORDS(s->me_nb));
+            break;
+        }
+        if (s->me_band_rows == 1) {
+            xg_set_error(XIN_GPU_ERR_ARG, "stream_open: search range %d needs more shared memory than a CTA has", R);
+            xg_stream_free(s);
+            return XIN_GPU_ERR_ARG;
+        }
         bands++;
     }
     s->me_bands = (ndy + s->me_band_rows - 1) / s->me_band_rows;
@@ -201,7 +213,7 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     static std::once_flag me_attr_once;
     static cudaError_t me_attr_err = cudaSuccess;
     std::call_once(me_attr_once, [] {
-        me_attr_err = cudaFuncSetAttribute(k_me_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        me_attr_err = cudaFuncSetAttribute(k_me_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, XG_ME_SMEM_MAX);
     });
     if (xg_cuda_check(me_attr_err, "me smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
     *out = s;
@@ -272,6 +284,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         mp.ref = s->slot[ref][0];
         mp.W = c.width; mp.H = c.height; mp.ctu = c.ctu_size; mp.R = c.search_range;
         mp.band_rows = s->me_band_rows; mp.band_rows_alloc = s->me_band_rows_alloc; mp.row_words = s->me_row_words;
+        mp.agg_passes = s->me_nb;
         for (int L = 0; L < 4; L++) {
             mp.keys[L] = s->lev_on[L] ? s->keys + s->lev_first[L] : nullptr;
             mp.cus_x[L] = s->lev_cx[L];
@@ -343,6 +356,8 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
     if (s->inflight) { xg_set_error(XIN_GPU_ERR_STATE, "frame_submit: previous picture not collected by frame_wait"); return XIN_GPU_ERR_STATE; }
     const xin_gpu_stream_cfg &c = s->cfg;
     if (pic->qp < 0 || pic->qp > 63 || pic->uv_qp < 0 || pic->uv_qp > 63) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: QP out of range"); return XIN_GPU_ERR_ARG; }
+    /* the search packs (cost << 2 | row) into 32 bits: costs must stay below 2^29 */
+    if (pic->sad_lambda > (1u << 20)) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: sad_lambda above 2^20"); return XIN_GPU_ERR_ARG; }
     /* the previous picture's copies may still read the pinned staging (its first
      * picture is not collected by frame_wait) */
     if (s->nsub > 0 && xg_cuda_check(cudaEventSynchronize(s->ev1), "frame_submit")) return XIN_GPU_ERR_CUDA;
@@ -473,22 +488,24 @@ extern "C" int xin_gpu_measure_sad_peak(double *absdiff_per_s)
     cudaEventCreate(&a); cudaEventCreate(&b);
     /* both packed forms: vabsdiff4 + dp4a, and vabsdiff4 with add-reduction (the
      * form the search kernel issues); the faster one is the ceiling */
-    float best = 1e30f;
+    double best = 0;      /* absolute differences per second */
     for (int form = 0; form < 2; form++)
         for (int rep = 0; rep < 4; rep++) {
             cudaEventRecord(a, t->stream);
-            if (XG_BITDEPTH != 8) k_sad_peak10<<<blocks, threads, 0, t->stream>>>(in, out, iters);
-            else if (form == 0) k_sad_peak<<<blocks, threads, 0, t->stream>>>(in, out, iters);
-            else k_sad_peak_add<<<blocks, threads, 0, t->stream>>>(in, out, iters);
+            int per = 0;  /* absolute differences per thread and loop trip */
+            if (XG_BITDEPTH != 8) { k_sad_peak10<<<blocks, threads, 0, t->stream>>>(in, out, iters); per = 64 * 2; }
+            else if (form == 0) { k_sad_peak<<<blocks, threads, 0, t->stream>>>(in, out, iters); per = 8 * 4; }
+            else { k_sad_peak_add<<<blocks, threads, 0, t->stream>>>(in, out, iters / 8); per = 64 * 4 / 8; }
             cudaEventRecord(b, t->stream);
             cudaEventSynchronize(b);
             float ms = 0;
             cudaEventElapsedTime(&ms, a, b);
-            if (rep && ms < best) best = ms;
+            double r = (double)blocks * threads * iters * per / (ms * 1e-3);
+            if (rep && r > best) best = r;
         }
     xg_count_launch(8);
     cudaEventDestroy(a); cudaEventDestroy(b);
     if (xg_cuda_check(cudaGetLastError(), "sad peak")) return XIN_GPU_ERR_CUDA;
-    *absdiff_per_s = (double)blocks * threads * iters * 8 * (XG_BITDEPTH == 8 ? 4 : 2) / (best * 1e-3);
+    *absdiff_per_s = best;
     return XIN_GPU_OK;
 }

@@ -93,18 +93,19 @@ __global__ void __launch_bounds__(256) k_qpel_planes(XgPlane ref, XgQpel qp)
 
 /* -------------------------------------------------------------- k_me_tiles
  * Grid: (tiles_x, tiles_y, bands).  A CTA takes one 64x64 tile and one band of
- * candidate rows; warp w owns the 16x16 sub-block (w & 3, w >> 2), lane l the
- * l-th candidate of each group of 32 consecutive candidates (raster order of
- * the band).  The reference band sits in shared memory as one 32-bit word per
+ * candidate rows; warp w owns the 16x16 sub-block (w & 3, w >> 2).  A pass of a
+ * warp covers 32 candidate columns x XG_ME_D consecutive candidate rows: lane l
+ * takes one column and the XG_ME_D rows, so every reference word it loads
+ * serves XG_ME_D current rows.  The reference band sits in shared memory as one 32-bit word per
  * pixel position, word (r, x) holding pixels x .. x+3 of band row r, so the
  * four pixels at any candidate offset are one aligned word; the row pitch is
  * congruent to the candidate-row length modulo 32, so the 32 consecutive
  * candidates of a warp read 32 consecutive banks.  |a - b| of four pixels and
  * their sum is one vabsdiff4 with add-reduction.
  * Per candidate a warp has the SADs of its four 8x8 blocks and of its 16x16
- * block in registers (running minimum per lane); the 16x16 SADs of 128
- * candidates at a time go to shared memory, from which the 32x32 and 64x64
- * SADs are summed.  Every CU keeps (cost, raster index) as one 64-bit key; the
+ * block in registers (running minimum per lane); the 16x16 SADs go to shared
+ * memory, from which the 32x32 and 64x64 SADs are summed every p.agg_passes passes.
+ * Every CU keeps (cost, raster index) as one 64-bit key; the
  * unsigned minimum over lanes, warps and CTAs (atomicMin) selects the smallest
  * cost and, among equal costs, the first candidate in raster order -- the
  * strict '<' raster search.  Costs: (SAD << 8) + (bits(4dx) + bits(4dy)) * lambda
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(256) k_qpel_planes(XgPlane ref, XgQpel qp)
  * per pixel pair |a - b| + 1024 per lane comes from one packed add-then-max on
  * biased lanes and accumulates lane-wise (32 pairs per 8x8 quadrant fit 16 bits),
  * the bias removed at the end; the current 64x64 tile sits in shared memory
- * (read as broadcasts; each warp keeps a window of the three current rows a
+ * (read as broadcasts; each warp keeps a window of the XG_ME_D current rows a
  * reference row meets, with their negations).  Samples must be below 1024. */
 #define XG_ME_TILE 64
 #define XG_ME_THREADS 512
@@ -166,8 +167,9 @@ __global__ void k_sad_peak(const uint32_t *in, uint32_t *out, int iters)
     out[t] = acc0 + acc1 + acc2 + acc3;
 }
 
-/* the same on the one-instruction form the search kernel uses: vabsdiff4 with
- * add-reduction into the accumulator */
+/* the one-instruction form the search kernel uses: vabsdiff4 with
+ * add-reduction into the accumulator; 64 per loop trip (8 accumulators x 8
+ * operands) so that loop overhead does not bound the rate */
 __global__ void k_sad_peak_add(const uint32_t *in, uint32_t *out, int iters)
 {
     uint32_t a[8], b[8];
@@ -176,13 +178,14 @@ __global__ void k_sad_peak_add(const uint32_t *in, uint32_t *out, int iters)
     uint32_t acc[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
     for (int it = 0; it < iters; it++) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-            uint32_t d;
-            asm volatile("vabsdiff4.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a[i]), "r"(b[i]), "r"(acc[i]));
-            acc[i] = d;
-        }
+        for (int i = 0; i < 8; i++)
 #pragma unroll
-        for (int i = 0; i < 8; i++) { uint32_t tmp = a[i]; a[i] = b[(i + 1) & 7] ^ (uint32_t)it; b[(i + 1) & 7] = tmp; }
+            for (int j = 0; j < 8; j++) {
+                uint32_t d;
+                asm volatile("vabsdiff4.u32.u32.u32.add %0, %1, %2, %3;" : "=r"(d) : "r"(a[i]), "r"(b[j]), "r"(acc[j]));
+                acc[j] = d;
+            }
+        a[0] ^= (uint32_t)it;
     }
     uint32_t s = 0;
     for (int i = 0; i < 8; i++) s += acc[i];
@@ -190,22 +193,27 @@ __global__ void k_sad_peak_add(const uint32_t *in, uint32_t *out, int iters)
 }
 
 /* 10-bit form: the biased packed add-then-max per pixel pair plus a lane-wise
- * accumulate, what the 10-bit search kernel issues */
+ * accumulate, what the 10-bit search kernel issues; 64 pairs per loop trip, the
+ * reference words changed every trip (lanes stay below 1024) */
 __global__ void k_sad_peak10(const uint32_t *in, uint32_t *out, int iters)
 {
-    uint32_t a[8], b[8], an[8];
+    uint32_t a[8], an[8], b[8], bn[8];
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     for (int i = 0; i < 8; i++) {
         a[i] = in[(t + i) & 1023] & 0x03ff03ffu;
         b[i] = in[(t * 7 + i * 13) & 1023] & 0x03ff03ffu;
         an[i] = 0x04000400u - a[i];
+        bn[i] = 0x04000400u - b[i];
     }
     uint32_t acc[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
     for (int it = 0; it < iters; it++) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) acc[i] += __viaddmax_u16x2(a[i], 0x04000400u - b[i], b[i] + an[i]);
+        for (int i = 0; i < 8; i++)
 #pragma unroll
-        for (int i = 0; i < 8; i++) { uint32_t tmp = b[i]; b[i] = b[(i + 1) & 7] ^ ((uint32_t)it & 0x01ff01ffu); b[(i + 1) & 7] = tmp; }
+            for (int j = 0; j < 8; j += 2)
+                acc[j] += __viaddmax_u16x2(a[i], bn[j], b[j] + an[i]) + __viaddmax_u16x2(a[i], bn[j + 1], b[j + 1] + an[i]);
+#pragma unroll
+        for (int j = 0; j < 8; j++) { b[j] ^= (uint32_t)it & 0x00ff00ffu; bn[j] = 0x04000400u - b[j]; }
     }
     uint32_t s = 0;
     for (int i = 0; i < 8; i++) s += acc[i];
@@ -218,6 +226,7 @@ struct XgMeParams {
     int band_rows;                      /* candidate rows per band */
     int band_rows_alloc;                /* staged band rows: 64 + band_rows rounded up to XG_ME_D, minus 1 */
     int row_words;                      /* words per band row (pitch of the word array) */
+    int agg_passes;                     /* passes buffered for the 32x32 / 64x64 sums, 1..XG_ME_NB_MAX */
     unsigned long long *keys[4];        /* level 0..3 = 64, 32, 16, 8 (NULL = level off) */
     int cus_x[4];                       /* CUs per row of each level */
 };
@@ -253,8 +262,11 @@ __device__ __forceinline__ uint32_t xg_absdiff2_biased(uint32_t a, uint32_t an, 
  * 48 + (2R) + 12 (8-bit, 4 pixels a word) or 48 + (2R) + 14 (10-bit, 2 pixels) */
 #define XG_ME_RELW(nx) ((nx) + (XG_BITDEPTH == 8 ? 60 : 62))
 #define XG_ME_CUR_WORDS (XG_BITDEPTH == 8 ? 0 : 64 * 32)     /* shared current tile (10-bit) */
-#define XG_ME_D 3                         /* candidate rows per lane and pass */
+#define XG_ME_D 4                         /* candidate rows per lane and pass (the key packs d in 2 bits: at most 4) */
 #define XG_ME_SLOTS (32 * XG_ME_D)        /* candidates per warp and pass */
+#define XG_ME_SMEM_MAX (216 * 1024)       /* dynamic shared memory of k_me_tiles, under the 227 KB a CTA may have */
+#define XG_ME_NB_MAX 4                    /* passes buffered between 32x32 / 64x64 updates (at most) */
+#define XG_ME_AGG_WORDS(nb) ((nb) * 20 * XG_ME_SLOTS)   /* 16x16 SADs [nb][16][SLOTS] + 32x32 SADs [nb][4][SLOTS] */
 __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, const XgPicParams *pp)
 {
     extern __shared__ uint32_t sm[];
@@ -274,7 +286,9 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     uint32_t *refw = sm + XG_ME_CUR_WORDS;                   /* [rows][row_words] */
     uint32_t *mvcx = refw + (size_t)p.band_rows_alloc * p.row_words; /* [nx] */
     uint32_t *mvcy = mvcx + nx;                              /* [band_rows rounded to XG_ME_D] */
-    uint32_t *s16 = mvcy + p.band_rows_alloc;                /* [16][XG_ME_SLOTS] */
+    const int nb = p.agg_passes;
+    uint32_t *s16 = mvcy + p.band_rows_alloc;                /* [nb][16][XG_ME_SLOTS] */
+    uint32_t *s32b = s16 + nb * 16 * XG_ME_SLOTS;            /* [nb][4][XG_ME_SLOTS] */
 #if XG_BITDEPTH != 8
     uint32_t *scur = sm;                                     /* [64][32]: row y, pixels 2k, 2k+1 (16-byte aligned) */
 #endif
@@ -378,7 +392,7 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                 }
             }
 #else
-            uint32_t cw[XG_ME_D][8], cn[XG_ME_D][8];   /* current rows t, t-1, t-2 (slot = row % XG_ME_D), negated */
+            uint32_t cw[XG_ME_D][8], cn[XG_ME_D][8];   /* current rows t .. t-XG_ME_D+1 (slot = row % XG_ME_D), negated */
             const uint32_t *crow = scur + by * 32 + (bx >> 1);
 #pragma unroll
             for (int t = 0; t < 16 + XG_ME_D - 1; t++) {
@@ -412,54 +426,85 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
 #pragma unroll
                 for (int b = 0; b < 4; b++) acc[d][b] = (acc[d][b] & 0xffffu) + (acc[d][b] >> 16) - 64u * 1024u;
 #endif
-            const int dx = col - p.R;
+            /* Per CU, the best of the lane's XG_ME_D candidates (same column, rows
+             * row0 + d: raster order = d order) as one key (cost << 2) | d, then a
+             * (cost, raster index) compare with the lane's running best.  Keys of
+             * candidates outside the band or the window are >= 0xE0000000, above any
+             * real key (costs stay below 2^26). */
+            const int dx = col - p.R, dyl = dyb0 + row0;
+            const uint32_t gidx0 = (uint32_t)((dyl + p.R) * nx + col);
+            uint32_t md[XG_ME_D];
+            uint32_t *s16w = s16 + (pz % nb) * 16 * XG_ME_SLOTS + warp * XG_ME_SLOTS + lane;
 #pragma unroll
             for (int d = 0; d < XG_ME_D; d++) {
-                const int row = row0 + d, dy = dyb0 + row;
-                const bool valid = vvalid && row < ndy;
-                const uint32_t sum16 = acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
-                const uint32_t mvc = mvcx[col] + mvcy[row];
-                const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
-                const uint32_t sads[5] = { acc[d][0], acc[d][1], acc[d][2], acc[d][3], sum16 };
+                const bool valid = vvalid && row0 + d < ndy;
+                md[d] = valid ? (((mvcx[col] + mvcy[row0 + d]) << 2) | (uint32_t)d) : 0xE0000000u;
+                s16w[d * 32] = acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
+            }
 #pragma unroll
-                for (int c = 0; c < 5; c++) {
-                    const uint32_t cost = (sads[c] << XG_COST_FRACTION) + mvc;
-                    bool ok = valid && live[c];
-                    if (!interior)
-                        ok = ok && dx >= swin[warp][c][0] && dx <= swin[warp][c][1] && dy >= swin[warp][c][2] && dy <= swin[warp][c][3];
-                    /* a lane's candidates are not visited in raster order: compare (cost, raster index) */
-                    if (ok && (cost < best[c] || (cost == best[c] && gidx < bidx[c]))) { best[c] = cost; bidx[c] = gidx; }
+            for (int c = 0; c < 5; c++) {
+                uint32_t k = 0xFFFFFFFFu;
+#pragma unroll
+                for (int d = 0; d < XG_ME_D; d++) {
+                    const uint32_t sad = c < 4 ? acc[d][c] : acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
+                    uint32_t kd = (sad << (XG_COST_FRACTION + 2)) + md[d];
+                    if (!interior) {
+                        const int dy = dyl + d;
+                        if (!(dx >= swin[warp][c][0] && dx <= swin[warp][c][1] && dy >= swin[warp][c][2] && dy <= swin[warp][c][3]))
+                            kd = 0xFFFFFFFFu;
+                    }
+                    k = min(k, kd);
                 }
-                s16[warp * XG_ME_SLOTS + d * 32 + lane] = sum16;
+                const uint32_t cost = k >> 2, gidx = gidx0 + (k & 3u) * (uint32_t)nx;
+                if (live[c] && k < 0xE0000000u && (cost < best[c] || (cost == best[c] && gidx < bidx[c]))) { best[c] = cost; bidx[c] = gidx; }
             }
         }
-        __syncthreads();
-        if (c32 < 4) {
-            const int d = slot / 32, v = pz * 32 + (slot & 31);
-            const int vv = v < nv ? v : nv - 1;
-            const int chunk = vv / nx, col = vv - chunk * nx, row = chunk * XG_ME_D + d;
-            if (v < nv && row < ndy) {
-                const int dx = col - p.R, dy = dyb0 + row;
-                const uint32_t mvc = mvcx[col] + mvcy[row];
-                const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
+        /* 32x32 and 64x64 CUs every nb passes: (1) thread (c32, slot) sums four
+         * 16x16 SADs per buffered pass; (2) thread slot sums the four 32x32 SADs */
+        const int pb = pz % nb;
+        if (pb == nb - 1 || pz == npass - 1) {
+            __syncthreads();
+            const int pz0 = pz - pb;
+            if (c32 < 4) {
+                const int d = slot / 32;
                 /* warps of the 32x32 quadrant c32: (2*(c32&1) + {0,1}) + 4*(2*(c32>>1) + {0,1}) */
                 const int w0 = (c32 & 1) * 2 + (c32 >> 1) * 8;
-                const uint32_t s32 = s16[w0 * XG_ME_SLOTS + slot] + s16[(w0 + 1) * XG_ME_SLOTS + slot] +
-                                     s16[(w0 + 4) * XG_ME_SLOTS + slot] + s16[(w0 + 5) * XG_ME_SLOTS + slot];
-                const uint32_t cost = (s32 << XG_COST_FRACTION) + mvc;
-                if (live32 && dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3] &&
-                    (cost < best32 || (cost == best32 && gidx < bidx32))) { best32 = cost; bidx32 = gidx; }
-                if (live64) {
-                    uint32_t s64 = 0;
-#pragma unroll
-                    for (int w = 0; w < 16; w++) s64 += s16[w * XG_ME_SLOTS + slot];
-                    const uint32_t c64 = (s64 << XG_COST_FRACTION) + mvc;
-                    if (dx >= swin64[0] && dx <= swin64[1] && dy >= swin64[2] && dy <= swin64[3] &&
-                        (c64 < best64 || (c64 == best64 && gidx < bidx64))) { best64 = c64; bidx64 = gidx; }
+                for (int j = 0; j <= pb; j++) {
+                    const int v = (pz0 + j) * 32 + (slot & 31);
+                    const uint32_t *r16 = s16 + j * 16 * XG_ME_SLOTS + slot;
+                    const uint32_t s32 = r16[w0 * XG_ME_SLOTS] + r16[(w0 + 1) * XG_ME_SLOTS] + r16[(w0 + 4) * XG_ME_SLOTS] +
+                                         r16[(w0 + 5) * XG_ME_SLOTS];
+                    s32b[(j * 4 + c32) * XG_ME_SLOTS + slot] = s32;
+                    const int vv = v < nv ? v : nv - 1;
+                    const int chunk = vv / nx, col = vv - chunk * nx, row = chunk * XG_ME_D + d;
+                    if (live32 && v < nv && row < ndy) {
+                        const int dx = col - p.R, dy = dyb0 + row;
+                        const uint32_t cost = (s32 << XG_COST_FRACTION) + mvcx[col] + mvcy[row];
+                        const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
+                        if (dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3] &&
+                            (cost < best32 || (cost == best32 && gidx < bidx32))) { best32 = cost; bidx32 = gidx; }
+                    }
+                }
+            }
+            __syncthreads();
+            if (live64) {
+                const int d = slot / 32;
+                for (int j = 0; j <= pb; j++) {
+                    const int v = (pz0 + j) * 32 + (slot & 31);
+                    const int vv = v < nv ? v : nv - 1;
+                    const int chunk = vv / nx, col = vv - chunk * nx, row = chunk * XG_ME_D + d;
+                    if (v < nv && row < ndy) {
+                        const uint32_t *r32 = s32b + j * 4 * XG_ME_SLOTS + slot;
+                        const uint32_t s64 = r32[0] + r32[XG_ME_SLOTS] + r32[2 * XG_ME_SLOTS] + r32[3 * XG_ME_SLOTS];
+                        const int dx = col - p.R, dy = dyb0 + row;
+                        const uint32_t c64 = (s64 << XG_COST_FRACTION) + mvcx[col] + mvcy[row];
+                        const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
+                        if (dx >= swin64[0] && dx <= swin64[1] && dy >= swin64[2] && dy <= swin64[3] &&
+                            (c64 < best64 || (c64 == best64 && gidx < bidx64))) { best64 = c64; bidx64 = gidx; }
+                    }
                 }
             }
         }
-        __syncthreads();
     }
 
     /* ---- publish: warp minimum of packed keys, then one atomicMin per CU and CTA */
