@@ -103,8 +103,11 @@ __global__ void __launch_bounds__(256) k_qpel_planes(XgPlane ref, XgQpel qp)
  * candidates of a warp read 32 consecutive banks.  |a - b| of four pixels and
  * their sum is one vabsdiff4 with add-reduction.
  * Per candidate a warp has the SADs of its four 8x8 blocks and of its 16x16
- * block in registers (running minimum per lane); the 16x16 SADs go to shared
- * memory, from which the 32x32 and 64x64 SADs are summed every p.agg_passes passes.
+ * block in registers (running minimum per lane).  After each pass the four
+ * warps of a 32x32 quadrant swap their 16x16 SADs through shared memory under a
+ * 128-thread named barrier, each warp taking one of the XG_ME_D candidate rows
+ * for the 32x32 CU; the 32x32 SADs go to a ring from which the first four warps
+ * sum the 64x64 SADs every p.agg_passes passes.
  * Every CU keeps (cost, raster index) as one 64-bit key; the
  * unsigned minimum over lanes, warps and CTAs (atomicMin) selects the smallest
  * cost and, among equal costs, the first candidate in raster order -- the
@@ -265,8 +268,10 @@ __device__ __forceinline__ uint32_t xg_absdiff2_biased(uint32_t a, uint32_t an, 
 #define XG_ME_D 4                         /* candidate rows per lane and pass (the key packs d in 2 bits: at most 4) */
 #define XG_ME_SLOTS (32 * XG_ME_D)        /* candidates per warp and pass */
 #define XG_ME_SMEM_MAX (216 * 1024)       /* dynamic shared memory of k_me_tiles, under the 227 KB a CTA may have */
-#define XG_ME_NB_MAX 4                    /* passes buffered between 32x32 / 64x64 updates (at most) */
-#define XG_ME_AGG_WORDS(nb) ((nb) * 20 * XG_ME_SLOTS)   /* 16x16 SADs [nb][16][SLOTS] + 32x32 SADs [nb][4][SLOTS] */
+#define XG_ME_NB_MAX 4                    /* passes buffered between 64x64 updates (at most) */
+/* 16x16 SADs [2][16][SLOTS] (double-buffered per pass) + 32x32 SADs [2][nb][4][SLOTS] */
+#define XG_ME_AGG_WORDS(nb) ((2 * 16 + 2 * (nb) * 4) * XG_ME_SLOTS)
+static_assert(XG_ME_D == 4, "the 32x32 exchange gives each of a quadrant's four warps one candidate row");
 __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, const XgPicParams *pp)
 {
     extern __shared__ uint32_t sm[];
@@ -287,8 +292,8 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     uint32_t *mvcx = refw + (size_t)p.band_rows_alloc * p.row_words; /* [nx] */
     uint32_t *mvcy = mvcx + nx;                              /* [band_rows rounded to XG_ME_D] */
     const int nb = p.agg_passes;
-    uint32_t *s16 = mvcy + p.band_rows_alloc;                /* [nb][16][XG_ME_SLOTS] */
-    uint32_t *s32b = s16 + nb * 16 * XG_ME_SLOTS;            /* [nb][4][XG_ME_SLOTS] */
+    uint32_t *s16 = mvcy + p.band_rows_alloc;                /* [2][16][XG_ME_SLOTS] */
+    uint32_t *s32r = s16 + 2 * 16 * XG_ME_SLOTS;             /* [2][nb][4][XG_ME_SLOTS] */
 #if XG_BITDEPTH != 8
     uint32_t *scur = sm;                                     /* [64][32]: row y, pixels 2k, 2k+1 (16-byte aligned) */
 #endif
@@ -306,7 +311,10 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     }
     const uint32_t lambda = pp->lambda;
     for (int i = threadIdx.x; i < nx; i += blockDim.x) mvcx[i] = xg_mvd_bits(4 * (i - p.R)) * lambda;
-    for (int i = threadIdx.x; i < nch * XG_ME_D; i += blockDim.x) mvcy[i] = xg_mvd_bits(4 * (dyb0 + i)) * lambda;
+    /* rows past the band (the last chunk's padding) get a sentinel that lifts
+     * their keys to >= 0xE0000000 (lambda <= 2^20 keeps real keys far below) */
+    for (int i = threadIdx.x; i < nch * XG_ME_D; i += blockDim.x)
+        mvcy[i] = i < ndy ? xg_mvd_bits(4 * (dyb0 + i)) * lambda : 0x38000000u;
 
     /* ---- this warp's 16x16 block of the current picture: registers (8-bit) or the shared tile (10-bit) */
     const int bx = (warp & 3) * 16, by = (warp >> 2) * 16;
@@ -349,12 +357,14 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
             in = in && swin[warp][c][0] <= -p.R && swin[warp][c][1] >= p.R && swin[warp][c][2] <= dyb0 && swin[warp][c][3] >= dyb0 + ndy - 1;
         sinterior[warp] = in;
     }
-    /* 32x32 and 64x64 bookkeeping: thread t < 4 * XG_ME_SLOTS handles (cu32 = t / XG_ME_SLOTS, slot);
-     * t < XG_ME_SLOTS also the 64x64 */
-    const int c32 = threadIdx.x / XG_ME_SLOTS, slot = threadIdx.x % XG_ME_SLOTS;
+    /* 32x32: this warp's quadrant c32 and its rank jq among the quadrant's four
+     * warps (it evaluates candidate row jq of each pass); 64x64: threads
+     * t < XG_ME_SLOTS, candidate slot t */
+    const int c32 = ((warp >> 1) & 1) + ((warp >> 3) << 1), jq = (warp & 1) + ((warp >> 1) & 2);
     const int c32x = tx0 + (c32 & 1) * 32, c32y = ty0 + (c32 >> 1) * 32;
-    const bool live32 = c32 < 4 && p.keys[1] && c32x + 32 <= p.W && c32y + 32 <= p.H;
+    const bool live32 = p.keys[1] && c32x + 32 <= p.W && c32y + 32 <= p.H;
     const bool live64 = threadIdx.x < XG_ME_SLOTS && p.keys[0] && tx0 + 64 <= p.W && ty0 + 64 <= p.H;
+    const int w32 = (c32 & 1) * 2 + (c32 >> 1) * 8;          /* first warp of the quadrant: w32, +1, +4, +5 */
     uint32_t best32 = 0xFFFFFFFFu, bidx32 = 0xFFFFFFFFu, best64 = 0xFFFFFFFFu, bidx64 = 0xFFFFFFFFu;
     __syncthreads();
     const bool interior = sinterior[warp];
@@ -430,15 +440,15 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
              * row0 + d: raster order = d order) as one key (cost << 2) | d, then a
              * (cost, raster index) compare with the lane's running best.  Keys of
              * candidates outside the band or the window are >= 0xE0000000, above any
-             * real key (costs stay below 2^26). */
+             * real key (costs stay below 2^27). */
             const int dx = col - p.R, dyl = dyb0 + row0;
             const uint32_t gidx0 = (uint32_t)((dyl + p.R) * nx + col);
             uint32_t md[XG_ME_D];
-            uint32_t *s16w = s16 + (pz % nb) * 16 * XG_ME_SLOTS + warp * XG_ME_SLOTS + lane;
+            uint32_t *s16w = s16 + (pz & 1) * 16 * XG_ME_SLOTS + warp * XG_ME_SLOTS + lane;
+            /* lanes past the last candidate repeat candidate nv - 1: same key, no effect */
 #pragma unroll
             for (int d = 0; d < XG_ME_D; d++) {
-                const bool valid = vvalid && row0 + d < ndy;
-                md[d] = valid ? (((mvcx[col] + mvcy[row0 + d]) << 2) | (uint32_t)d) : 0xE0000000u;
+                md[d] = ((mvcx[col] + mvcy[row0 + d]) << 2) | (uint32_t)d;
                 s16w[d * 32] = acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
             }
 #pragma unroll
@@ -459,43 +469,42 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                 if (live[c] && k < 0xE0000000u && (cost < best[c] || (cost == best[c] && gidx < bidx[c]))) { best[c] = cost; bidx[c] = gidx; }
             }
         }
-        /* 32x32 and 64x64 CUs every nb passes: (1) thread (c32, slot) sums four
-         * 16x16 SADs per buffered pass; (2) thread slot sums the four 32x32 SADs */
+        /* 32x32: the quadrant's four warps swap their 16x16 SADs (double-buffered by
+         * pass parity: a buffer is rewritten two passes later, after the next
+         * barrier, when every warp has read it) */
+        {
+            asm volatile("bar.sync %0, 128;" ::"r"(1 + c32) : "memory");
+            const int v = pz * 32 + lane;
+            const int vv = v < nv ? v : nv - 1;
+            const int chunk = vv / nx, col = vv - chunk * nx, row = chunk * XG_ME_D + jq;
+            const uint32_t *r16 = s16 + (pz & 1) * 16 * XG_ME_SLOTS + jq * 32 + lane;
+            const uint32_t s32 = r16[w32 * XG_ME_SLOTS] + r16[(w32 + 1) * XG_ME_SLOTS] + r16[(w32 + 4) * XG_ME_SLOTS] +
+                                 r16[(w32 + 5) * XG_ME_SLOTS];
+            s32r[((((pz / nb) & 1) * nb + pz % nb) * 4 + c32) * XG_ME_SLOTS + jq * 32 + lane] = s32;
+            if (live32 && v < nv && row < ndy) {
+                const int dx = col - p.R, dy = dyb0 + row;
+                const uint32_t cost = (s32 << XG_COST_FRACTION) + mvcx[col] + mvcy[row];
+                const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
+                if (dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3] &&
+                    (cost < best32 || (cost == best32 && gidx < bidx32))) { best32 = cost; bidx32 = gidx; }
+            }
+        }
+        /* 64x64 every nb passes, from the four quadrants' 32x32 SADs (the ring is
+         * double-buffered by group: a group's half is rewritten only after the
+         * next full barrier, which the reading threads reach after reading) */
         const int pb = pz % nb;
         if (pb == nb - 1 || pz == npass - 1) {
             __syncthreads();
-            const int pz0 = pz - pb;
-            if (c32 < 4) {
-                const int d = slot / 32;
-                /* warps of the 32x32 quadrant c32: (2*(c32&1) + {0,1}) + 4*(2*(c32>>1) + {0,1}) */
-                const int w0 = (c32 & 1) * 2 + (c32 >> 1) * 8;
-                for (int j = 0; j <= pb; j++) {
-                    const int v = (pz0 + j) * 32 + (slot & 31);
-                    const uint32_t *r16 = s16 + j * 16 * XG_ME_SLOTS + slot;
-                    const uint32_t s32 = r16[w0 * XG_ME_SLOTS] + r16[(w0 + 1) * XG_ME_SLOTS] + r16[(w0 + 4) * XG_ME_SLOTS] +
-                                         r16[(w0 + 5) * XG_ME_SLOTS];
-                    s32b[(j * 4 + c32) * XG_ME_SLOTS + slot] = s32;
-                    const int vv = v < nv ? v : nv - 1;
-                    const int chunk = vv / nx, col = vv - chunk * nx, row = chunk * XG_ME_D + d;
-                    if (live32 && v < nv && row < ndy) {
-                        const int dx = col - p.R, dy = dyb0 + row;
-                        const uint32_t cost = (s32 << XG_COST_FRACTION) + mvcx[col] + mvcy[row];
-                        const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
-                        if (dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3] &&
-                            (cost < best32 || (cost == best32 && gidx < bidx32))) { best32 = cost; bidx32 = gidx; }
-                    }
-                }
-            }
-            __syncthreads();
             if (live64) {
-                const int d = slot / 32;
+                const int d = threadIdx.x / 32, pz0 = pz - pb;
+                const uint32_t *r32 = s32r + ((pz / nb) & 1) * nb * 4 * XG_ME_SLOTS + threadIdx.x;
                 for (int j = 0; j <= pb; j++) {
-                    const int v = (pz0 + j) * 32 + (slot & 31);
+                    const int v = (pz0 + j) * 32 + lane;
                     const int vv = v < nv ? v : nv - 1;
                     const int chunk = vv / nx, col = vv - chunk * nx, row = chunk * XG_ME_D + d;
                     if (v < nv && row < ndy) {
-                        const uint32_t *r32 = s32b + j * 4 * XG_ME_SLOTS + slot;
-                        const uint32_t s64 = r32[0] + r32[XG_ME_SLOTS] + r32[2 * XG_ME_SLOTS] + r32[3 * XG_ME_SLOTS];
+                        const uint32_t *q32 = r32 + j * 4 * XG_ME_SLOTS;
+                        const uint32_t s64 = q32[0] + q32[XG_ME_SLOTS] + q32[2 * XG_ME_SLOTS] + q32[3 * XG_ME_SLOTS];
                         const int dx = col - p.R, dy = dyb0 + row;
                         const uint32_t c64 = (s64 << XG_COST_FRACTION) + mvcx[col] + mvcy[row];
                         const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
