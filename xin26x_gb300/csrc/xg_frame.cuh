@@ -317,11 +317,12 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             tp.res = s->dres;
             int n = s->lev_cx[L] * s->lev_cy[L];
             if (n > 0) {
+                /* 64 and 32: a CTA per CU; 16 and 8: a warp per CU, eight CUs per CTA */
                 switch (XG_LEVEL_SIZE[L]) {
-                case 64: k_cu_tail<64, 256><<<n, 256, 0, ls>>>(tp, s->dpp); break;
-                case 32: k_cu_tail<32, 256><<<n, 256, 0, ls>>>(tp, s->dpp); break;
-                case 16: k_cu_tail<16, 128><<<n, 128, 0, ls>>>(tp, s->dpp); break;
-                default: k_cu_tail<8, 64><<<n, 64, 0, ls>>>(tp, s->dpp); break;
+                case 64: k_cu_tail<64, 256, 1><<<n, 256, 0, ls>>>(tp, s->dpp, n); break;
+                case 32: k_cu_tail<32, 256, 1><<<n, 256, 0, ls>>>(tp, s->dpp, n); break;
+                case 16: k_cu_tail<16, 32, 8><<<(n + 7) / 8, 256, 0, ls>>>(tp, s->dpp, n); break;
+                default: k_cu_tail<8, 32, 8><<<(n + 7) / 8, 256, 0, ls>>>(tp, s->dpp, n); break;
                 }
                 nl++;
             }

@@ -553,11 +553,22 @@ struct XgTailParams {
     xin_gpu_cu_result *res;           /* all CUs */
 };
 
+/* synchronisation of the NT threads that work on one CU (group g of a CTA
+ * holding CPB groups): the whole CTA, a named barrier, or the warp */
+template <int NT, int CPB>
+__device__ __forceinline__ void xg_gsync(int g)
+{
+    if (NT == 32) __syncwarp();
+    else if (CPB == 1) __syncthreads();
+    else asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(NT) : "memory");
+}
+
 /* C(i, j) = sum_l A(i, l) * B(j, l) over shared-memory operands with
- * A(i, l) = A[i * asi + l * asl] and B(j, l) = B[j * bsj + l * bsl].  Each
- * thread owns a TI x TJ tile of outputs, consecutive threads consecutive j
- * tiles, so B is read along its contiguous dimension and A is broadcast;
- * epi(i, j, acc) consumes every output. */
+ * A(i, l) = A[i * asi + l * asl] and B(j, l) = B[j * bsj + l * bsl], computed by
+ * the NT threads of a group (tid = rank in the group).  Each thread owns a
+ * TI x TJ tile of outputs, consecutive threads consecutive j tiles, so B is
+ * read along its contiguous dimension and A is broadcast; epi(i, j, acc)
+ * consumes every output. */
 __host__ __device__ constexpr int xg_tile_j(int ni, int nj, int nt) { return (ni * nj >= 8 * nt && nj >= 64) ? 4 : ((ni * nj >= 2 * nt && nj >= 32) ? 2 : 1); }
 __host__ __device__ constexpr int xg_tile_i(int ni, int nj, int nt)
 {
@@ -565,11 +576,11 @@ __host__ __device__ constexpr int xg_tile_i(int ni, int nj, int nt)
 }
 
 template <int NI, int NJ, int NL, int NT, typename TA, typename TB, typename F>
-__device__ __forceinline__ void xg_mm(const TA *A, int asi, int asl, const TB *B, int bsj, int bsl, F epi)
+__device__ __forceinline__ void xg_mm(int tid, const TA *A, int asi, int asl, const TB *B, int bsj, int bsl, F epi)
 {
     constexpr int TJ = xg_tile_j(NI, NJ, NT), TI = xg_tile_i(NI, NJ, NT);
     constexpr int tj = NJ / TJ, tiles = (NI / TI) * tj;
-    for (int t = threadIdx.x; t < tiles; t += NT) {
+    for (int t = tid; t < tiles; t += NT) {
         const int i0 = (t / tj) * TI, j0 = (t % tj) * TJ;
         int acc[TI][TJ];
 #pragma unroll
@@ -605,7 +616,6 @@ struct XgTqSmem {
     int16_t resT[N * N];         /* residual, transposed: resT[x * N + y] */
     int16_t t1T[N * K];          /* first forward pass, t1T[i * K + k] (row i, frequency k) */
     int16_t rr[K * K];           /* dequantised coefficients rr[kv * K + kh] */
-    xg_coef qs[K * K];           /* quantised coefficients */
     int16_t t2[K * N];           /* first inverse pass t2[j * N + x] */
 };
 
@@ -613,98 +623,112 @@ struct XgTqSmem {
  * zeroed out), quant / dequant over the low min(N, 32) square with 4x4 coding
  * groups (Xin266QuantInvQuant, h266_quant_inv_quant.c:27-139), coefficient plane
  * written with zeros beyond 32 */
-template <int N, int NT>
-__device__ void xg_tq(XgTqSmem<N> &sm, const XgQuant &qz, int s1, int s2, unsigned long long *nz, xg_coef *qout, int qpitch)
+template <int N, int NT, int CPB>
+__device__ void xg_tq(XgTqSmem<N> &sm, const XgQuant &qz, int s1, int s2, unsigned long long *nz, xg_coef *qout, int qpitch,
+                      int tid, int g)
 {
     constexpr int K = XgTqSmem<N>::K;
-    xg_mm<K, N, N, NT>(sm.mat, N, 1, sm.resT, 1, N, [&](int k, int i, int acc) {
+    xg_mm<K, N, N, NT>(tid, sm.mat, N, 1, sm.resT, 1, N, [&](int k, int i, int acc) {
         sm.t1T[i * K + k] = (int16_t)xg_clip16(xg_rshift_rnd(acc, s1));
     });
-    __syncthreads();
-    xg_mm<K, K, N, NT>(sm.mat, N, 1, sm.t1T, 1, K, [&](int kv, int kh, int acc) {
+    xg_gsync<NT, CPB>(g);
+    xg_mm<K, K, N, NT>(tid, sm.mat, N, 1, sm.t1T, 1, K, [&](int kv, int kh, int acc) {
         int t = xg_clip16(xg_rshift_rnd(acc, s2));
         int a = abs(t);
         int qv = (int)(((long long)a * qz.qmult + qz.qadd) >> qz.qshift);
         qv = xg_clip16(t < 0 ? -qv : qv);
-        sm.qs[kv * K + kh] = (xg_coef)qv;
+        qout[(intptr_t)kv * qpitch + kh] = (xg_coef)qv;
         sm.rr[kv * K + kh] = (int16_t)xg_clip16((int)(((long long)qv * qz.iqmult + qz.iqadd) >> qz.iqshift));
         if (qv) atomicOr(nz, 1ull << ((kv >> 2) * (K >> 2) + (kh >> 2)));
     });
-    __syncthreads();
-    for (int o = threadIdx.x; o < N * N; o += NT) {
-        int y = o / N, x = o % N;
-        qout[(intptr_t)y * qpitch + x] = (y < K && x < K) ? sm.qs[y * K + x] : (xg_coef)0;
-    }
+    if (N > K)      /* the zeroed-out high frequencies */
+        for (int o = tid; o < N * N; o += NT) {
+            int y = o / N, x = o % N;
+            if (y >= K || x >= K) qout[(intptr_t)y * qpitch + x] = (xg_coef)0;
+        }
+    xg_gsync<NT, CPB>(g);
 }
 
 /* inverse DCT2 of the dequantised low K x K part (zero elsewhere): columns
  * first, lines >= 32 skipped (Xin266IDct2WxH), then rows; adds the prediction,
  * clips, writes the reconstruction and accumulates the SSD */
-template <int N, int NT>
+template <int N, int NT, int CPB>
 __device__ void xg_itq(XgTqSmem<N> &sm, const xg_pix *pred, const xg_pix *org, int opitch, xg_pix *rec, int rpitch,
-                       unsigned long long *ssd)
+                       unsigned long long *ssd, int tid, int g)
 {
     constexpr int K = XgTqSmem<N>::K;
     const int s2 = 6 + 15 - 1 - XG_BITDEPTH;
-    xg_mm<K, N, K, NT>(sm.rr, 1, K, sm.mat, 1, N, [&](int j, int x, int acc) {
+    xg_mm<K, N, K, NT>(tid, sm.rr, 1, K, sm.mat, 1, N, [&](int j, int x, int acc) {
         sm.t2[j * N + x] = (int16_t)xg_clip16(xg_rshift_rnd(acc, 7));
     });
-    __syncthreads();
+    xg_gsync<NT, CPB>(g);
     unsigned long long part = 0;
-    xg_mm<N, N, K, NT>(sm.t2, 1, N, sm.mat, 1, N, [&](int y, int x, int acc) {
+    xg_mm<N, N, K, NT>(tid, sm.t2, 1, N, sm.mat, 1, N, [&](int y, int x, int acc) {
         int v = xg_clip_pix((int)pred[y * N + x] + xg_clip16(xg_rshift_rnd(acc, s2)));
         rec[(intptr_t)y * rpitch + x] = (xg_pix)v;
         int d = (int)org[(intptr_t)y * opitch + x] - v;
         part += (unsigned long long)(d * d);
     });
     atomicAdd(ssd, part);
-    __syncthreads();
+    xg_gsync<NT, CPB>(g);
 }
 
-/* one CTA per CU of size S (luma S x S, chroma S/2 x S/2), NT threads */
+/* the shared state of one CU */
 template <int S, int NT>
-__global__ void __launch_bounds__(NT) k_cu_tail(XgTailParams p, const XgPicParams *pp)
+struct XgTailSmem {
+    XgTqSmem<S> tl;
+    XgTqSmem<S / 2> tc;
+    xg_pix pred[S * S];
+    uint32_t part[8][NT / 32];
+    int bmv[3];
+    unsigned long long nz[3], ssd[3];
+};
+
+/* CPB CUs of size S (luma S x S, chroma S/2 x S/2) per CTA, NT threads per CU
+ * (NT = 32: one warp per CU, warp-synchronous) */
+template <int S, int NT, int CPB>
+__global__ void __launch_bounds__(NT * CPB) k_cu_tail(XgTailParams p, const XgPicParams *pp, int ncu)
 {
     constexpr int C = S / 2;
-    __shared__ XgTqSmem<S> tl;
-    __shared__ XgTqSmem<C> tc;
-    __shared__ xg_pix pred[S * S];
-    __shared__ uint32_t part[8][NT / 32];
-    __shared__ int bmv[3];
-    __shared__ unsigned long long nz[3], ssd[3];
-
-    const int cu = blockIdx.x;
+    __shared__ XgTailSmem<S, NT> shm[CPB];
+    const int g = threadIdx.x / NT, tid = threadIdx.x % NT;
+    const int cu = blockIdx.x * CPB + g;
+    if (cu >= ncu) return;          /* whole groups only: no barrier is shared with a missing group */
+    XgTailSmem<S, NT> &m = shm[g];
+    XgTqSmem<S> &tl = m.tl;
+    XgTqSmem<C> &tc = m.tc;
+    xg_pix *pred = m.pred;
     const int cx = (cu % p.cus_x) * S, cy = (cu / p.cus_x) * S;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = tid & 31, warp = tid >> 5;
     const unsigned long long key = p.keys[cu];
     const int nx = 2 * p.R + 1;
     const int gidx = (int)(uint32_t)key;
     const int imx = gidx % nx - p.R, imy = gidx / nx - p.R;
-    if (threadIdx.x < 3) { nz[threadIdx.x] = 0; ssd[threadIdx.x] = 0; }
+    if (tid < 3) { m.nz[tid] = 0; m.ssd[tid] = 0; }
     {   /* DCT2 matrices of the luma (S) and chroma (S/2) blocks, rows k < 32 */
         constexpr int lgs = S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : 6;
         const int16_t *ml = xg_mat(0, lgs), *mc = xg_mat(0, lgs - 1);
-        for (int i = threadIdx.x; i < XgTqSmem<S>::K * S; i += NT) tl.mat[i] = ml[i];
-        for (int i = threadIdx.x; i < XgTqSmem<C>::K * C; i += NT) tc.mat[i] = mc[i];
+        for (int i = tid; i < XgTqSmem<S>::K * S; i += NT) tl.mat[i] = ml[i];
+        for (int i = tid; i < XgTqSmem<C>::K * C; i += NT) tc.mat[i] = mc[i];
     }
-    if (threadIdx.x == 0) { bmv[0] = 4 * imx; bmv[1] = 4 * imy; bmv[2] = (int)(uint32_t)(key >> 32); }
 
     /* window (h266_enc_init.c:1462) */
     const int mnx = (int16_t)(-cx - p.ctu - 8), mny = (int16_t)(-cy - p.ctu - 8);
     const int mxx = (int16_t)(p.W + (p.ctu - S + 8) - cx), mxy = (int16_t)(p.H + (p.ctu - S + 8) - cy);
-    __syncthreads();
 
     /* ---- Xin266FullSubPelMe on the quarter-pel planes (h266_sub_pel_refine.c:81-212) */
     const int offx[8] = { -1, 1, 0, 0, -1, 1, -1, 1 }, offy[8] = { 0, 0, -1, 1, -1, -1, 1, 1 };
     const xg_pix *org = p.cur[0].data + (intptr_t)cy * p.cur[0].pitch + cx;
+    int bx = 4 * imx, by = 4 * imy;
+    uint32_t bc = (uint32_t)(key >> 32);
     /* the search runs only when the integer start lies in the window (h266_sub_pel_refine.c:117-120) */
-    const bool start_in = (bmv[0] >> 2) >= mnx && (bmv[1] >> 2) >= mny && (bmv[0] >> 2) <= mxx && (bmv[1] >> 2) <= mxy;
+    const bool start_in = imx >= mnx && imy >= mny && imx <= mxx && imy <= mxy;
     for (int step = 2; step >= 1 && start_in; step--) {
-        const int bx0 = bmv[0], by0 = bmv[1];
+        const int bx0 = bx, by0 = by;
         uint32_t acc[8];
 #pragma unroll
         for (int c = 0; c < 8; c++) acc[c] = 0;
-        for (int i = threadIdx.x; i < S * S; i += NT) {
+        for (int i = tid; i < S * S; i += NT) {
             int x = i % S, y = i / S;
             int o = org[(intptr_t)y * p.cur[0].pitch + x];
 #pragma unroll
@@ -715,29 +739,37 @@ __global__ void __launch_bounds__(NT) k_cu_tail(XgTailParams p, const XgPicParam
                 acc[c] += (uint32_t)abs(o - v);
             }
         }
+        /* every thread ends with the eight sums (one warp) or reads them back (several) */
 #pragma unroll
         for (int c = 0; c < 8; c++) {
-            uint32_t s = acc[c];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) part[c][warp] = s;
+            for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t bc = (uint32_t)bmv[2];
-            int bx = bx0, by = by0;
-            for (int c = 0; c < 8; c++) {
-                uint32_t s = 0;
-                for (int w = 0; w < NT / 32; w++) s += part[c][w];
-                int tx = bx0 + offx[c] * step, ty = by0 + offy[c] * step;
-                uint32_t cost = (s << XG_COST_FRACTION) + (xg_mvd_bits(tx) + xg_mvd_bits(ty)) * pp->lambda;
-                if (cost < bc) { bc = cost; bx = tx; by = ty; }
+        if (NT > 32) {
+            if (lane == 0) {
+#pragma unroll
+                for (int c = 0; c < 8; c++) m.part[c][warp] = acc[c];
             }
-            bmv[0] = bx; bmv[1] = by; bmv[2] = (int)bc;
+            xg_gsync<NT, CPB>(g);
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                uint32_t t = 0;
+                for (int w = 0; w < NT / 32; w++) t += m.part[c][w];
+                acc[c] = t;
+            }
+            xg_gsync<NT, CPB>(g);
         }
-        __syncthreads();
+        /* strict '<' in the fixed candidate order (h266_sub_pel_refine.c:146-160) */
+        int nbx = bx0, nby = by0;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            int tx = bx0 + offx[c] * step, ty = by0 + offy[c] * step;
+            uint32_t cost = (acc[c] << XG_COST_FRACTION) + (xg_mvd_bits(tx) + xg_mvd_bits(ty)) * pp->lambda;
+            if (cost < bc) { bc = cost; nbx = tx; nby = ty; }
+        }
+        bx = nbx; by = nby;
     }
-    const int mvx = bmv[0], mvy = bmv[1];
+    const int mvx = bx, mvy = by;
 
     /* ---- luma MC (Xin266LumaInterPred: clamp to the window in 1/16 pel) */
     {
@@ -745,22 +777,23 @@ __global__ void __launch_bounds__(NT) k_cu_tail(XgTailParams p, const XgPicParam
         int ox = cx * 16 + m16x, oy = cy * 16 + m16y;
         int q = ((oy & 15) >> 2) * 4 + ((ox & 15) >> 2);
         const xg_pix *pl = q ? p.qpel.plane[q] : p.ref[0].data;
-        for (int i = threadIdx.x; i < S * S; i += NT) {
+        for (int i = tid; i < S * S; i += NT) {
             int x = i % S, y = i / S;
             pred[i] = pl[(intptr_t)((oy >> 4) + y) * p.qpel.pitch + (ox >> 4) + x];
         }
     }
-    __syncthreads();
+    xg_gsync<NT, CPB>(g);
 
     /* ---- luma TQ + reconstruction */
     const int lgS = S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : 6;
-    for (int i = threadIdx.x; i < S * S; i += NT) {
+    for (int i = tid; i < S * S; i += NT) {
         int y = i / S, x = i % S;
         tl.resT[x * S + y] = (int16_t)((int)org[(intptr_t)y * p.cur[0].pitch + x] - (int)pred[i]);
     }
-    __syncthreads();
-    xg_tq<S, NT>(tl, pp->quant[p.level][0], lgS + XG_BITDEPTH + 6 - 15, lgS + 6, &nz[0], p.q[0] + (intptr_t)cy * p.W + cx, p.W);
-    xg_itq<S, NT>(tl, pred, org, p.cur[0].pitch, p.rec[0] + (intptr_t)cy * p.W + cx, p.W, &ssd[0]);
+    xg_gsync<NT, CPB>(g);
+    xg_tq<S, NT, CPB>(tl, pp->quant[p.level][0], lgS + XG_BITDEPTH + 6 - 15, lgS + 6, &m.nz[0],
+                      p.q[0] + (intptr_t)cy * p.W + cx, p.W, tid, g);
+    xg_itq<S, NT, CPB>(tl, pred, org, p.cur[0].pitch, p.rec[0] + (intptr_t)cy * p.W + cx, p.W, &m.ssd[0], tid, g);
 
     /* ---- chroma: uni branch of Xin266ChromaMotionComp (1/32 phase, mask 31), TQ, reconstruction */
     {
@@ -773,32 +806,32 @@ __global__ void __launch_bounds__(NT) k_cu_tail(XgTailParams p, const XgPicParam
         for (int pl = 1; pl <= 2; pl++) {
             const XgPlane &rp = p.ref[pl];
             const xg_pix *src = rp.data + (intptr_t)(oy >> 5) * rp.pitch + (ox >> 5);
-            for (int i = threadIdx.x; i < C * C; i += NT) {
+            for (int i = tid; i < C * C; i += NT) {
                 int x = i % C, y = i / C;
-                const xg_pix *s = src + (intptr_t)y * rp.pitch + x;
+                const xg_pix *sp = src + (intptr_t)y * rp.pitch + x;
                 int v;
-                if (!fx && !fy) v = s[0];
-                else if (fx && !fy) v = xg_if_pix<4>(s, 1, th);
-                else if (!fx && fy) v = xg_if_pix<4>(s, rp.pitch, tv);
-                else v = xg_if_hv<4, false>(s, rp.pitch, th, tv);
+                if (!fx && !fy) v = sp[0];
+                else if (fx && !fy) v = xg_if_pix<4>(sp, 1, th);
+                else if (!fx && fy) v = xg_if_pix<4>(sp, rp.pitch, tv);
+                else v = xg_if_hv<4, false>(sp, rp.pitch, th, tv);
                 pred[i] = (xg_pix)v;
             }
-            __syncthreads();
+            xg_gsync<NT, CPB>(g);
             const xg_pix *corg = p.cur[pl].data + (intptr_t)(cy >> 1) * p.cur[pl].pitch + (cx >> 1);
-            for (int i = threadIdx.x; i < C * C; i += NT) {
+            for (int i = tid; i < C * C; i += NT) {
                 int y = i / C, x = i % C;
                 tc.resT[x * C + y] = (int16_t)((int)corg[(intptr_t)y * p.cur[pl].pitch + x] - (int)pred[i]);
             }
-            __syncthreads();
-            xg_tq<C, NT>(tc, pp->quant[p.level][pl], lgC + XG_BITDEPTH + 6 - 15, lgC + 6, &nz[pl],
-                         p.q[pl] + (intptr_t)(cy >> 1) * W2 + (cx >> 1), W2);
-            xg_itq<C, NT>(tc, pred, corg, p.cur[pl].pitch, p.rec[pl] + (intptr_t)(cy >> 1) * W2 + (cx >> 1), W2, &ssd[pl]);
+            xg_gsync<NT, CPB>(g);
+            xg_tq<C, NT, CPB>(tc, pp->quant[p.level][pl], lgC + XG_BITDEPTH + 6 - 15, lgC + 6, &m.nz[pl],
+                              p.q[pl] + (intptr_t)(cy >> 1) * W2 + (cx >> 1), W2, tid, g);
+            xg_itq<C, NT, CPB>(tc, pred, corg, p.cur[pl].pitch, p.rec[pl] + (intptr_t)(cy >> 1) * W2 + (cx >> 1), W2,
+                               &m.ssd[pl], tid, g);
         }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         xin_gpu_cu_result *o = p.res + p.first_cu + cu;
-        o->mvx = mvx; o->mvy = mvy; o->cost = (uint32_t)bmv[2]; o->int_cost = (uint32_t)(key >> 32);
-        for (int i = 0; i < 3; i++) { o->nz[i] = nz[i]; o->ssd[i] = ssd[i]; }
+        o->mvx = mvx; o->mvy = mvy; o->cost = bc; o->int_cost = (uint32_t)(key >> 32);
+        for (int i = 0; i < 3; i++) { o->nz[i] = m.nz[i]; o->ssd[i] = m.ssd[i]; }
     }
 }
