@@ -317,12 +317,13 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             tp.res = s->dres;
             int n = s->lev_cx[L] * s->lev_cy[L];
             if (n > 0) {
-                /* 64 and 32: a CTA per CU; 16 and 8: a warp per CU, eight CUs per CTA */
+                /* 64 and 32: a 128-thread CTA per CU; 16 and 8: a warp per CU, four CUs per
+                 * CTA (the fastest of the shapes measured on GB300 at 1080p) */
                 switch (XG_LEVEL_SIZE[L]) {
-                case 64: k_cu_tail<64, 256, 1><<<n, 256, 0, ls>>>(tp, s->dpp, n); break;
-                case 32: k_cu_tail<32, 256, 1><<<n, 256, 0, ls>>>(tp, s->dpp, n); break;
-                case 16: k_cu_tail<16, 32, 8><<<(n + 7) / 8, 256, 0, ls>>>(tp, s->dpp, n); break;
-                default: k_cu_tail<8, 32, 8><<<(n + 7) / 8, 256, 0, ls>>>(tp, s->dpp, n); break;
+                case 64: k_cu_tail<64, 128, 1><<<n, 128, 0, ls>>>(tp, s->dpp, n); break;
+                case 32: k_cu_tail<32, 128, 1><<<n, 128, 0, ls>>>(tp, s->dpp, n); break;
+                case 16: k_cu_tail<16, 32, 4><<<(n + 3) / 4, 128, 0, ls>>>(tp, s->dpp, n); break;
+                default: k_cu_tail<8, 32, 4><<<(n + 3) / 4, 128, 0, ls>>>(tp, s->dpp, n); break;
                 }
                 nl++;
             }
