@@ -36,7 +36,8 @@ struct xin_gpu_stream {
     xg_pix *h_rec[3];
     cudaStream_t st;
     cudaStream_t aux[3];   /* the tails of levels 2..4 run beside the first level's */
-    cudaEvent_t ev_fork, ev_join[3];
+    cudaStream_t auxq;     /* quarter-pel planes of the new picture, beside the search (low priority) */
+    cudaEvent_t ev_fork, ev_join[3], ev_qfork, ev_qjoin;
     cudaEvent_t ev0, ev1;
     cudaEvent_t evs[5];    /* stage boundaries, recorded inside the picture's launches */
     cudaGraphExec_t gexec[2];
@@ -78,6 +79,9 @@ static int xg_stream_free(xin_gpu_stream *s)
         if (s->aux[i]) cudaStreamDestroy(s->aux[i]);
     }
     if (s->ev_fork) cudaEventDestroy(s->ev_fork);
+    if (s->ev_qfork) cudaEventDestroy(s->ev_qfork);
+    if (s->ev_qjoin) cudaEventDestroy(s->ev_qjoin);
+    if (s->auxq) cudaStreamDestroy(s->auxq);
     if (s->ev0) cudaEventDestroy(s->ev0);
     if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->st) cudaStreamDestroy(s->st);
@@ -128,6 +132,13 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
     for (int i = 0; i < 5 && e == cudaSuccess; i++) e = cudaEventCreate(&s->evs[i]);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_qfork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_qjoin, cudaEventDisableTiming);
+    if (e == cudaSuccess) {
+        int lo = 0, hi = 0;
+        cudaDeviceGetStreamPriorityRange(&lo, &hi);    /* lo: the least urgent */
+        e = cudaStreamCreateWithPriority(&s->auxq, cudaStreamNonBlocking, lo);
+    }
     for (int i = 0; i < 3 && e == cudaSuccess; i++) {
         e = cudaStreamCreateWithFlags(&s->aux[i], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join[i], cudaEventDisableTiming);
@@ -248,6 +259,17 @@ static void xg_stage_event(cudaEvent_t e, cudaStream_t st, bool capturing)
     else cudaEventRecord(e, st);
 }
 
+/* quarter-pel planes of slot cur on the low-priority stream, after ev_qfork */
+static int xg_enqueue_qpel(xin_gpu_stream *s, int cur)
+{
+    const xin_gpu_stream_cfg &c = s->cfg;
+    cudaStreamWaitEvent(s->auxq, s->ev_qfork, 0);
+    dim3 grd((c.width + 2 * s->pad - 8 + XG_QP_TW - 1) / XG_QP_TW, (c.height + 2 * s->pad - 8 + XG_QP_TH - 1) / XG_QP_TH);
+    k_qpel_planes<<<grd, 256, 0, s->auxq>>>(s->slot[cur][0], s->qpel[cur]);
+    cudaEventRecord(s->ev_qjoin, s->auxq);
+    return 1;
+}
+
 /* the launches of one picture in slot `cur` against the reference in 1 - cur */
 static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool capturing)
 {
@@ -270,12 +292,10 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         k_pad<<<152 * 4, 256, 0, st>>>(pl);
         nl++;
     }
-    {
-        dim3 grd((c.width + 2 * s->pad - 8 + XG_QP_TW - 1) / XG_QP_TW, (c.height + 2 * s->pad - 8 + XG_QP_TH - 1) / XG_QP_TH);
-        k_qpel_planes<<<grd, 256, 0, st>>>(s->slot[cur][0], s->qpel[cur]);
-        nl++;
-    }
     xg_stage_event(s->evs[1], st, capturing);
+    /* the new picture's quarter-pel planes are read only by the next picture's
+     * tails: build them on a low-priority stream beside the search */
+    cudaEventRecord(s->ev_qfork, st);
     if (with_me) {
         int ref = 1 - cur;
         cudaMemsetAsync(s->keys, 0xff, sizeof(unsigned long long) * s->ncus, st);
@@ -292,6 +312,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, s->me_bands);
         k_me_tiles<<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, s->dpp);
         nl++;
+        nl += xg_enqueue_qpel(s, cur);
         xg_stage_event(s->evs[2], st, capturing);
         /* the levels' tails are independent: fork them onto the auxiliary streams */
         cudaEventRecord(s->ev_fork, st);
@@ -333,6 +354,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             cudaEventRecord(s->ev_join[i], s->aux[i]);
             cudaStreamWaitEvent(st, s->ev_join[i], 0);
         }
+        cudaStreamWaitEvent(st, s->ev_qjoin, 0);
         xg_stage_event(s->evs[3], st, capturing);
         if (!c.device_io) {
             cudaMemcpyAsync(s->h_res, s->dres, sizeof(xin_gpu_cu_result) * s->ncus, cudaMemcpyDeviceToHost, st);
@@ -343,6 +365,8 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             }
         }
     } else {
+        nl += xg_enqueue_qpel(s, cur);
+        cudaStreamWaitEvent(st, s->ev_qjoin, 0);
         xg_stage_event(s->evs[2], st, capturing);
         xg_stage_event(s->evs[3], st, capturing);
     }
@@ -393,7 +417,7 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
             if (xg_cuda_check(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal), "begin capture")) return XIN_GPU_ERR_CUDA;
             s->graph_launches[cur] = xg_enqueue_picture(s, cur, true, true);
             if (xg_cuda_check(cudaStreamEndCapture(s->st, &g), "end capture")) return XIN_GPU_ERR_CUDA;
-            cudaError_t e = cudaGraphInstantiate(&s->gexec[cur], g, 0);
+            cudaError_t e = cudaGraphInstantiate(&s->gexec[cur], g, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(g);
             if (xg_cuda_check(e, "graph instantiate")) return XIN_GPU_ERR_CUDA;
         }
