@@ -324,18 +324,22 @@ int  xin_gpu_stream_level_info(const xin_gpu_stream *s, int level, int32_t *size
                                int32_t *cus_x, int32_t *cus_y);      /* level 0 = largest size */
 int  xin_gpu_stream_num_levels(const xin_gpu_stream *s);
 /* Upload a picture and queue its hot path (asynchronous).  The first picture of
- * a stream only becomes the reference (no CU results). */
+ * a stream only becomes the reference (no CU results).  Up to two pictures may
+ * be in flight (the next one's upload and kernels overlap the previous one's
+ * result copies); a third submit before a frame_wait is XIN_GPU_ERR_STATE. */
 int  xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic);
-/* Wait for the last submitted picture (bounded by timeout_ms; < 0 waits without
- * limit) and copy its results into the caller's buffers.  Members of res left
- * NULL receive views of the stream's pinned result buffers instead, valid until
- * the next frame_submit. */
+/* Wait for the oldest picture in flight (bounded by timeout_ms; < 0 waits
+ * without limit) and copy its results into the caller's buffers.  Members of res
+ * left NULL receive views of the stream's pinned result buffers instead, valid
+ * until the second frame_submit after this call.  Every submitted picture is
+ * collected once, the first one included. */
 int  xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32_t timeout_ms);
-/* Device time of the stages of the last completed picture:
+/* Device time of the stages of the last collected picture:
  * ms[0] upload + padding + quarter-pel planes, ms[1] integer search,
  * ms[2] sub-pel search + MC + transform/quant + reconstruction, ms[3] result copies. */
 int  xin_gpu_stream_stage_ms(const xin_gpu_stream *s, float ms[4]);
-/* Device pointers of the result arrays (same layouts as xin_gpu_results). */
+/* Device pointers of the result arrays of the last collected picture (same
+ * layouts as xin_gpu_results), valid until the second submit after it. */
 int  xin_gpu_stream_device_results(const xin_gpu_stream *s, void **cu, void *q[3], void *rec[3]);
 
 /* Device and pinned-host bytes a stream of this configuration allocates

@@ -112,3 +112,36 @@ def test_frame_wide_search_sampled(bd, R):
         for name in ("mvx", "mvy", "int_cost", "cost"):
             assert out["cu"][name][i] == recs[name][i], (bd, R, i, name)
         assert np.array_equal(out["cu"]["nz"][i], recs["nz"][i]) and np.array_equal(out["cu"]["ssd"][i], recs["ssd"][i])
+
+
+def test_frame_two_in_flight_equals_one_at_a_time():
+    """Two pictures in flight (submit k + 1 before collecting k) give the same results
+    as submit / wait one picture at a time; a third submit and an empty wait are refused."""
+    w, h = 256, 192
+    seq = synth.sequence(w, h, 6, seed=5, objects=2)
+    ref = []
+    fs = FrameStream(w, h, search_range=24, out_q=True, out_rec=True)
+    for k in range(6):
+        fs.submit(*seq[k], qp=27 + k, uv_qp=28 + k, sad_lambda=50 + k)
+        r = fs.wait()
+        if k:
+            ref.append(r)
+    fs.close()
+    fs = FrameStream(w, h, search_range=24, out_q=True, out_rec=True)
+    got = []
+    fs.submit(*seq[0], qp=27, uv_qp=28, sad_lambda=50)
+    fs.submit(*seq[1], qp=28, uv_qp=29, sad_lambda=51)
+    with pytest.raises(RuntimeError, match=r"\(-6\)"):
+        fs.submit(*seq[2], qp=29, uv_qp=30, sad_lambda=52)
+    fs.wait()                                   # picture 0: the reference only
+    for k in range(2, 6):
+        fs.submit(*seq[k], qp=27 + k, uv_qp=28 + k, sad_lambda=50 + k)
+        got.append(fs.wait())
+    got.append(fs.wait())
+    with pytest.raises(RuntimeError, match=r"\(-6\)"):
+        fs.wait()
+    fs.close()
+    for a, b in zip(ref, got):
+        assert np.array_equal(a["cu"], b["cu"])
+        for p in range(3):
+            assert np.array_equal(a["q"][p], b["q"][p]) and np.array_equal(a["rec"][p], b["rec"][p])

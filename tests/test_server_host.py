@@ -25,9 +25,11 @@ def test_footprint_arithmetic(bd):
     ysz, csz = 2304 * 1400 * es, 1152 * 700 * es
     ncus = 30 * 16 + 60 * 33 + 120 * 67 + 240 * 135
     lq = 1920 * 1080
-    want = 2 * (ysz + 2 * csz) + 32 * ysz + 8 * ncus + 64 * ncus + lq * 3 // 2 * 4 * (cs + es)
-    assert want < d < want + 4096           # + the per-picture parameter block
-    assert h >= 64 * ncus + lq * 3 // 2 * es
+    # two slots + quarter-pel planes + keys, and two picture sets (CU records, coefficient
+    # and reconstruction planes of four levels, a parameter block each)
+    want = 2 * (ysz + 2 * csz) + 32 * ysz + 8 * ncus + 2 * (64 * ncus + lq * 3 // 2 * 4 * (cs + es))
+    assert want < d < want + 8192
+    assert h >= 2 * (64 * ncus + lq * 3 // 2 * es)
     # a wider search needs a wider margin; dropping levels drops their outputs
     assert _fp(lib, 1920, 1080, r=256)[1] > d
     assert _fp(lib, 1920, 1080, mask=64)[1] < d

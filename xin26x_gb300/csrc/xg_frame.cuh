@@ -24,27 +24,33 @@ struct xin_gpu_stream {
     xg_pix *qpel_base[2];
     XgQpel qpel[2];
     unsigned long long *keys;
-    xin_gpu_cu_result *dres;
-    xg_coef *dq[3];
-    xg_pix *drec[3];
-    XgPicParams *dpp;
-    /* pinned host staging */
-    xg_pix *h_in[3];
-    XgPicParams *h_pp;
-    xin_gpu_cu_result *h_res;
-    xg_coef *h_q[3];
-    xg_pix *h_rec[3];
+    /* what a picture in flight owns; picture k uses set k & 1 (its slot), so two
+     * pictures can be in flight: one computing while the other's copies run */
+    struct Set {
+        xin_gpu_cu_result *dres;
+        xg_coef *dq[3];
+        xg_pix *drec[3];
+        XgPicParams *dpp;
+        /* pinned host staging */
+        xg_pix *h_in[3];
+        XgPicParams *h_pp;
+        xin_gpu_cu_result *h_res;
+        xg_coef *h_q[3];
+        xg_pix *h_rec[3];
+        cudaEvent_t ev0, ev1;  /* submitted; results in host memory */
+        cudaEvent_t ev_kern;   /* kernels done (the copy stream waits on it) */
+        cudaEvent_t evs[5];    /* stage boundaries, recorded inside the picture's launches */
+    } set[2];
     cudaStream_t st;
+    cudaStream_t cst;      /* result copies (device to host) */
     cudaStream_t aux[3];   /* the tails of levels 2..4 run beside the first level's */
     cudaStream_t auxq;     /* quarter-pel planes of the new picture, beside the search (low priority) */
     cudaEvent_t ev_fork, ev_join[3], ev_qfork, ev_qjoin;
-    cudaEvent_t ev0, ev1;
-    cudaEvent_t evs[5];    /* stage boundaries, recorded inside the picture's launches */
     cudaGraphExec_t gexec[2];
     int me_bands, me_band_rows, me_band_rows_alloc, me_row_words, me_nb;
     size_t me_smem;
-    int nsub;
-    int inflight;          /* a picture with results is queued */
+    int nsub;              /* pictures submitted */
+    int ndone;             /* pictures collected by frame_wait (the oldest first) */
     int graph_launches[2]; /* kernels inside each captured graph */
 };
 
@@ -67,13 +73,21 @@ static void xg_quant_params(int qp, int lg, int intra_frame, XgQuant *q)
 static int xg_stream_free(xin_gpu_stream *s)
 {
     if (!s) return XIN_GPU_OK;
-    cudaStreamSynchronize(s->st);
+    if (s->st) cudaStreamSynchronize(s->st);
+    if (s->cst) cudaStreamSynchronize(s->cst);
     for (int i = 0; i < 2; i++) if (s->gexec[i]) cudaGraphExecDestroy(s->gexec[i]);
     for (int i = 0; i < 2; i++) { for (int p = 0; p < 3; p++) cudaFree(s->slot_base[i][p]); cudaFree(s->qpel_base[i]); }
-    cudaFree(s->keys); cudaFree(s->dres); cudaFree(s->dpp);
-    for (int p = 0; p < 3; p++) { cudaFree(s->dq[p]); cudaFree(s->drec[p]); cudaFreeHost(s->h_in[p]); cudaFreeHost(s->h_q[p]); cudaFreeHost(s->h_rec[p]); }
-    cudaFreeHost(s->h_pp); cudaFreeHost(s->h_res);
-    for (int i = 0; i < 5; i++) if (s->evs[i]) cudaEventDestroy(s->evs[i]);
+    cudaFree(s->keys);
+    for (auto &t : s->set) {
+        cudaFree(t.dres); cudaFree(t.dpp);
+        for (int p = 0; p < 3; p++) { cudaFree(t.dq[p]); cudaFree(t.drec[p]); cudaFreeHost(t.h_in[p]); cudaFreeHost(t.h_q[p]); cudaFreeHost(t.h_rec[p]); }
+        cudaFreeHost(t.h_pp); cudaFreeHost(t.h_res);
+        for (int i = 0; i < 5; i++) if (t.evs[i]) cudaEventDestroy(t.evs[i]);
+        if (t.ev0) cudaEventDestroy(t.ev0);
+        if (t.ev1) cudaEventDestroy(t.ev1);
+        if (t.ev_kern) cudaEventDestroy(t.ev_kern);
+    }
+    if (s->cst) cudaStreamDestroy(s->cst);
     for (int i = 0; i < 3; i++) {
         if (s->ev_join[i]) cudaEventDestroy(s->ev_join[i]);
         if (s->aux[i]) cudaStreamDestroy(s->aux[i]);
@@ -82,8 +96,6 @@ static int xg_stream_free(xin_gpu_stream *s)
     if (s->ev_qfork) cudaEventDestroy(s->ev_qfork);
     if (s->ev_qjoin) cudaEventDestroy(s->ev_qjoin);
     if (s->auxq) cudaStreamDestroy(s->auxq);
-    if (s->ev0) cudaEventDestroy(s->ev0);
-    if (s->ev1) cudaEventDestroy(s->ev1);
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
     return XIN_GPU_OK;
@@ -128,9 +140,13 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     s->ncus = first;
 
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
-    if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
-    for (int i = 0; i < 5 && e == cudaSuccess; i++) e = cudaEventCreate(&s->evs[i]);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking);
+    for (auto &t : s->set) {
+        if (e == cudaSuccess) e = cudaEventCreate(&t.ev0);
+        if (e == cudaSuccess) e = cudaEventCreate(&t.ev1);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.ev_kern, cudaEventDisableTiming);
+        for (int i = 0; i < 5 && e == cudaSuccess; i++) e = cudaEventCreate(&t.evs[i]);
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_qfork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_qjoin, cudaEventDisableTiming);
@@ -150,19 +166,21 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         if (e == cudaSuccess) e = cudaMalloc(&s->qpel_base[i], 16 * ysz);
     }
     if (e == cudaSuccess) e = cudaMalloc(&s->keys, sizeof(unsigned long long) * (s->ncus > 0 ? s->ncus : 1));
-    if (e == cudaSuccess) e = cudaMalloc(&s->dres, sizeof(xin_gpu_cu_result) * s->ncus);
-    if (e == cudaSuccess) e = cudaMalloc(&s->dpp, sizeof(XgPicParams));
-    for (int p = 0; p < 3 && e == cudaSuccess; p++) {
-        size_t n = (p ? lc : lq) * s->nlev;
-        e = cudaMalloc(&s->dq[p], n * sizeof(xg_coef));
-        if (e == cudaSuccess) e = cudaMalloc(&s->drec[p], n * sizeof(xg_pix));
-        if (c.device_io) continue;
-        if (e == cudaSuccess) e = cudaMallocHost(&s->h_in[p], (p ? lc : lq) * sizeof(xg_pix));
-        if (e == cudaSuccess && (c.out_flags & XIN_GPU_OUT_Q)) e = cudaMallocHost(&s->h_q[p], n * sizeof(xg_coef));
-        if (e == cudaSuccess && (c.out_flags & XIN_GPU_OUT_REC)) e = cudaMallocHost(&s->h_rec[p], n * sizeof(xg_pix));
+    for (auto &t : s->set) {
+        if (e == cudaSuccess) e = cudaMalloc(&t.dres, sizeof(xin_gpu_cu_result) * s->ncus);
+        if (e == cudaSuccess) e = cudaMalloc(&t.dpp, sizeof(XgPicParams));
+        for (int p = 0; p < 3 && e == cudaSuccess; p++) {
+            size_t n = (p ? lc : lq) * s->nlev;
+            e = cudaMalloc(&t.dq[p], n * sizeof(xg_coef));
+            if (e == cudaSuccess) e = cudaMalloc(&t.drec[p], n * sizeof(xg_pix));
+            if (c.device_io) continue;
+            if (e == cudaSuccess) e = cudaMallocHost(&t.h_in[p], (p ? lc : lq) * sizeof(xg_pix));
+            if (e == cudaSuccess && (c.out_flags & XIN_GPU_OUT_Q)) e = cudaMallocHost(&t.h_q[p], n * sizeof(xg_coef));
+            if (e == cudaSuccess && (c.out_flags & XIN_GPU_OUT_REC)) e = cudaMallocHost(&t.h_rec[p], n * sizeof(xg_pix));
+        }
+        if (e == cudaSuccess) e = cudaMallocHost(&t.h_pp, sizeof(XgPicParams));
+        if (e == cudaSuccess) e = cudaMallocHost(&t.h_res, sizeof(xin_gpu_cu_result) * s->ncus);
     }
-    if (e == cudaSuccess) e = cudaMallocHost(&s->h_pp, sizeof(XgPicParams));
-    if (e == cudaSuccess) e = cudaMallocHost(&s->h_res, sizeof(xin_gpu_cu_result) * s->ncus);
     if (e != cudaSuccess) {
         int st = (e == cudaErrorMemoryAllocation) ? XIN_GPU_ERR_NOMEM : XIN_GPU_ERR_CUDA;
         xg_set_error(st, "stream_open: %s", cudaGetErrorString(e));
@@ -259,6 +277,9 @@ static void xg_stage_event(cudaEvent_t e, cudaStream_t st, bool capturing)
     else cudaEventRecord(e, st);
 }
 
+/* completion event of the last submitted picture */
+static cudaEvent_t xg_stream_last_event(const xin_gpu_stream *s) { return s->set[(s->nsub - 1) & 1].ev1; }
+
 /* quarter-pel planes of slot cur on the low-priority stream, after ev_qfork */
 static int xg_enqueue_qpel(xin_gpu_stream *s, int cur)
 {
@@ -274,25 +295,26 @@ static int xg_enqueue_qpel(xin_gpu_stream *s, int cur)
 static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool capturing)
 {
     const xin_gpu_stream_cfg &c = s->cfg;
+    xin_gpu_stream::Set &t = s->set[cur];
     cudaStream_t st = s->st;
     size_t lq = (size_t)c.width * c.height, lc = lq / 4;
     int nl = 0;
     /* upload and pad the current picture; it becomes the next picture's reference */
-    xg_stage_event(s->evs[0], st, capturing);
-    cudaMemcpyAsync(s->dpp, s->h_pp, sizeof(XgPicParams), cudaMemcpyHostToDevice, st);
+    xg_stage_event(t.evs[0], st, capturing);
+    cudaMemcpyAsync(t.dpp, t.h_pp, sizeof(XgPicParams), cudaMemcpyHostToDevice, st);
     if (c.device_io) {
-        k_copy_in<<<152 * 4, 256, 0, st>>>(s->slot[cur][0], s->slot[cur][1], s->slot[cur][2], s->dpp);
+        k_copy_in<<<152 * 4, 256, 0, st>>>(s->slot[cur][0], s->slot[cur][1], s->slot[cur][2], t.dpp);
         nl++;
     }
     for (int p = 0; p < 3; p++) {
         XgPlane &pl = s->slot[cur][p];
         if (!c.device_io)
-            cudaMemcpy2DAsync(pl.data, (size_t)pl.pitch * sizeof(xg_pix), s->h_in[p], (size_t)pl.w * sizeof(xg_pix),
+            cudaMemcpy2DAsync(pl.data, (size_t)pl.pitch * sizeof(xg_pix), t.h_in[p], (size_t)pl.w * sizeof(xg_pix),
                               (size_t)pl.w * sizeof(xg_pix), pl.h, cudaMemcpyHostToDevice, st);
         k_pad<<<152 * 4, 256, 0, st>>>(pl);
         nl++;
     }
-    xg_stage_event(s->evs[1], st, capturing);
+    xg_stage_event(t.evs[1], st, capturing);
     /* the new picture's quarter-pel planes are read only by the next picture's
      * tails: build them on a low-priority stream beside the search */
     cudaEventRecord(s->ev_qfork, st);
@@ -310,10 +332,10 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             mp.cus_x[L] = s->lev_cx[L];
         }
         dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, s->me_bands);
-        k_me_tiles<<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, s->dpp);
+        k_me_tiles<<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, t.dpp);
         nl++;
         nl += xg_enqueue_qpel(s, cur);
-        xg_stage_event(s->evs[2], st, capturing);
+        xg_stage_event(t.evs[2], st, capturing);
         /* the levels' tails are independent: fork them onto the auxiliary streams */
         cudaEventRecord(s->ev_fork, st);
         int li = 0, nfork = 0;
@@ -332,19 +354,19 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             tp.keys = s->keys + s->lev_first[L];
             tp.cus_x = s->lev_cx[L]; tp.first_cu = s->lev_first[L]; tp.size = XG_LEVEL_SIZE[L]; tp.level = L;
             for (int p = 0; p < 3; p++) {
-                tp.q[p] = s->dq[p] + (p ? lc : lq) * li;
-                tp.rec[p] = s->drec[p] + (p ? lc : lq) * li;
+                tp.q[p] = t.dq[p] + (p ? lc : lq) * li;
+                tp.rec[p] = t.drec[p] + (p ? lc : lq) * li;
             }
-            tp.res = s->dres;
+            tp.res = t.dres;
             int n = s->lev_cx[L] * s->lev_cy[L];
             if (n > 0) {
                 /* 64 and 32: a 128-thread CTA per CU; 16 and 8: a warp per CU, four CUs per
                  * CTA (the fastest of the shapes measured on GB300 at 1080p) */
                 switch (XG_LEVEL_SIZE[L]) {
-                case 64: k_cu_tail<64, 128, 1><<<n, 128, 0, ls>>>(tp, s->dpp, n); break;
-                case 32: k_cu_tail<32, 128, 1><<<n, 128, 0, ls>>>(tp, s->dpp, n); break;
-                case 16: k_cu_tail<16, 32, 4><<<(n + 3) / 4, 128, 0, ls>>>(tp, s->dpp, n); break;
-                default: k_cu_tail<8, 32, 4><<<(n + 3) / 4, 128, 0, ls>>>(tp, s->dpp, n); break;
+                case 64: k_cu_tail<64, 128, 1><<<n, 128, 0, ls>>>(tp, t.dpp, n); break;
+                case 32: k_cu_tail<32, 128, 1><<<n, 128, 0, ls>>>(tp, t.dpp, n); break;
+                case 16: k_cu_tail<16, 32, 4><<<(n + 3) / 4, 128, 0, ls>>>(tp, t.dpp, n); break;
+                default: k_cu_tail<8, 32, 4><<<(n + 3) / 4, 128, 0, ls>>>(tp, t.dpp, n); break;
                 }
                 nl++;
             }
@@ -355,23 +377,35 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             cudaStreamWaitEvent(st, s->ev_join[i], 0);
         }
         cudaStreamWaitEvent(st, s->ev_qjoin, 0);
-        xg_stage_event(s->evs[3], st, capturing);
-        if (!c.device_io) {
-            cudaMemcpyAsync(s->h_res, s->dres, sizeof(xin_gpu_cu_result) * s->ncus, cudaMemcpyDeviceToHost, st);
-            for (int p = 0; p < 3; p++) {
-                size_t n = (p ? lc : lq) * s->nlev;
-                if (c.out_flags & XIN_GPU_OUT_Q) cudaMemcpyAsync(s->h_q[p], s->dq[p], n * sizeof(xg_coef), cudaMemcpyDeviceToHost, st);
-                if (c.out_flags & XIN_GPU_OUT_REC) cudaMemcpyAsync(s->h_rec[p], s->drec[p], n * sizeof(xg_pix), cudaMemcpyDeviceToHost, st);
-            }
-        }
+        xg_stage_event(t.evs[3], st, capturing);
     } else {
         nl += xg_enqueue_qpel(s, cur);
         cudaStreamWaitEvent(st, s->ev_qjoin, 0);
-        xg_stage_event(s->evs[2], st, capturing);
-        xg_stage_event(s->evs[3], st, capturing);
+        xg_stage_event(t.evs[2], st, capturing);
+        xg_stage_event(t.evs[3], st, capturing);
     }
-    xg_stage_event(s->evs[4], st, capturing);
     return nl;
+}
+
+/* the result copies of picture set t on the copy stream, after the picture's
+ * kernels, so that they overlap the next picture's kernels; then the picture's
+ * completion event */
+static void xg_enqueue_results(xin_gpu_stream *s, xin_gpu_stream::Set &t, bool with_me)
+{
+    const xin_gpu_stream_cfg &c = s->cfg;
+    cudaEventRecord(t.ev_kern, s->st);
+    cudaStreamWaitEvent(s->cst, t.ev_kern, 0);
+    if (with_me && !c.device_io) {
+        size_t lq = (size_t)c.width * c.height, lc = lq / 4;
+        cudaMemcpyAsync(t.h_res, t.dres, sizeof(xin_gpu_cu_result) * s->ncus, cudaMemcpyDeviceToHost, s->cst);
+        for (int p = 0; p < 3; p++) {
+            size_t n = (p ? lc : lq) * s->nlev;
+            if (c.out_flags & XIN_GPU_OUT_Q) cudaMemcpyAsync(t.h_q[p], t.dq[p], n * sizeof(xg_coef), cudaMemcpyDeviceToHost, s->cst);
+            if (c.out_flags & XIN_GPU_OUT_REC) cudaMemcpyAsync(t.h_rec[p], t.drec[p], n * sizeof(xg_pix), cudaMemcpyDeviceToHost, s->cst);
+        }
+    }
+    cudaEventRecord(t.evs[4], s->cst);
+    cudaEventRecord(t.ev1, s->cst);
 }
 
 extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic)
@@ -379,14 +413,18 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
     xin_gpu_clear_error();
     (void)cudaGetLastError();   /* errors of earlier, unrelated calls are not this picture's */
     if (!s || !pic) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: null argument"); return XIN_GPU_ERR_ARG; }
-    if (s->inflight) { xg_set_error(XIN_GPU_ERR_STATE, "frame_submit: previous picture not collected by frame_wait"); return XIN_GPU_ERR_STATE; }
+    if (s->nsub - s->ndone >= 2) {
+        xg_set_error(XIN_GPU_ERR_STATE, "frame_submit: two pictures in flight; collect one with frame_wait first");
+        return XIN_GPU_ERR_STATE;
+    }
     const xin_gpu_stream_cfg &c = s->cfg;
     if (pic->qp < 0 || pic->qp > 63 || pic->uv_qp < 0 || pic->uv_qp > 63) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: QP out of range"); return XIN_GPU_ERR_ARG; }
     /* the search packs (cost << 2 | row) into 32 bits: costs must stay below 2^29 */
     if (pic->sad_lambda > (1u << 20)) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: sad_lambda above 2^20"); return XIN_GPU_ERR_ARG; }
-    /* the previous picture's copies may still read the pinned staging (its first
-     * picture is not collected by frame_wait) */
-    if (s->nsub > 0 && xg_cuda_check(cudaEventSynchronize(s->ev1), "frame_submit")) return XIN_GPU_ERR_CUDA;
+    const int cur = s->nsub & 1;
+    xin_gpu_stream::Set &t = s->set[cur];
+    /* set cur was last used by picture nsub - 2, already collected by frame_wait
+     * (at most two in flight), so its staging is free */
     XgPicParams pp;
     memset(&pp, 0, sizeof pp);
     for (int p = 0; p < 3; p++) {
@@ -398,7 +436,7 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
             continue;
         }
         for (int y = 0; y < h; y++)
-            memcpy(s->h_in[p] + (size_t)y * w, pic->plane[p] + (size_t)y * pic->stride[p], (size_t)w * sizeof(xg_pix));
+            memcpy(t.h_in[p] + (size_t)y * w, pic->plane[p] + (size_t)y * pic->stride[p], (size_t)w * sizeof(xg_pix));
     }
     pp.lambda = pic->sad_lambda;
     for (int L = 0; L < 4; L++) {
@@ -407,10 +445,9 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
         xg_quant_params(pic->uv_qp, lg - 1, 0, &pp.quant[L][1]);
         pp.quant[L][2] = pp.quant[L][1];
     }
-    *s->h_pp = pp;
-    int cur = s->nsub & 1;
+    *t.h_pp = pp;
     bool with_me = s->nsub > 0;
-    cudaEventRecord(s->ev0, s->st);
+    cudaEventRecord(t.ev0, s->st);
     if (with_me && c.use_graph) {
         if (!s->gexec[cur]) {
             cudaGraph_t g;
@@ -426,10 +463,9 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
     } else {
         xg_count_launch((uint64_t)xg_enqueue_picture(s, cur, with_me, false));
     }
-    cudaEventRecord(s->ev1, s->st);
+    xg_enqueue_results(s, t, with_me);
     if (xg_cuda_check(cudaGetLastError(), "frame_submit")) return XIN_GPU_ERR_CUDA;
     s->nsub++;
-    s->inflight = with_me;
     return XIN_GPU_OK;
 }
 
@@ -437,40 +473,43 @@ extern "C" int xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32
 {
     xin_gpu_clear_error();
     if (!s) { xg_set_error(XIN_GPU_ERR_ARG, "frame_wait: null stream"); return XIN_GPU_ERR_ARG; }
+    if (s->ndone == s->nsub) { xg_set_error(XIN_GPU_ERR_STATE, "frame_wait: no picture in flight"); return XIN_GPU_ERR_STATE; }
+    const int k = s->ndone;                 /* the oldest picture in flight */
+    xin_gpu_stream::Set &t = s->set[k & 1];
     auto t0 = std::chrono::steady_clock::now();
     for (;;) {
-        cudaError_t e = cudaEventQuery(s->ev1);
+        cudaError_t e = cudaEventQuery(t.ev1);
         if (e == cudaSuccess) break;
         if (e != cudaErrorNotReady) return xg_cuda_check(e, "frame_wait");
         double el = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         if (timeout_ms >= 0 && el > timeout_ms) { xg_set_error(XIN_GPU_ERR_TIMEOUT, "frame_wait: timed out after %d ms", timeout_ms); return XIN_GPU_ERR_TIMEOUT; }
         std::this_thread::yield();
     }
-    if (!s->inflight) {
-        if (res) { res->gpu_ms = 0; }
+    s->ndone++;
+    if (k == 0) {                           /* the first picture only becomes the reference */
+        if (res) res->gpu_ms = 0;
         return XIN_GPU_OK;
     }
-    s->inflight = 0;
     if (!res) return XIN_GPU_OK;
     float ms = 0;
-    if (cudaEventElapsedTime(&ms, s->evs[0], s->evs[4]) != cudaSuccess) { cudaGetLastError(); ms = -1.0f; }
+    if (cudaEventElapsedTime(&ms, t.evs[0], t.evs[4]) != cudaSuccess) { cudaGetLastError(); ms = -1.0f; }
     res->gpu_ms = ms;
     const xin_gpu_stream_cfg &c = s->cfg;
     if (c.device_io) return XIN_GPU_OK;
     size_t lq = (size_t)c.width * c.height, lc = lq / 4;
-    /* caller buffers are filled; NULL members receive views of the stream's pinned
-     * buffers, valid until the next frame_submit */
-    if (res->cu) memcpy(res->cu, s->h_res, sizeof(xin_gpu_cu_result) * s->ncus);
-    else res->cu = s->h_res;
+    /* caller buffers are filled; NULL members receive views of the picture set's
+     * pinned buffers, valid until the second frame_submit after this call */
+    if (res->cu) memcpy(res->cu, t.h_res, sizeof(xin_gpu_cu_result) * s->ncus);
+    else res->cu = t.h_res;
     for (int p = 0; p < 3; p++) {
         size_t n = (p ? lc : lq) * s->nlev;
         if (c.out_flags & XIN_GPU_OUT_Q) {
-            if (res->q[p]) memcpy(res->q[p], s->h_q[p], n * sizeof(xg_coef));
-            else res->q[p] = s->h_q[p];
+            if (res->q[p]) memcpy(res->q[p], t.h_q[p], n * sizeof(xg_coef));
+            else res->q[p] = t.h_q[p];
         }
         if (c.out_flags & XIN_GPU_OUT_REC) {
-            if (res->rec[p]) memcpy(res->rec[p], s->h_rec[p], n * sizeof(xg_pix));
-            else res->rec[p] = s->h_rec[p];
+            if (res->rec[p]) memcpy(res->rec[p], t.h_rec[p], n * sizeof(xg_pix));
+            else res->rec[p] = t.h_rec[p];
         }
     }
     return XIN_GPU_OK;
@@ -479,9 +518,11 @@ extern "C" int xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32
 extern "C" int xin_gpu_stream_stage_ms(const xin_gpu_stream *s, float ms[4])
 {
     if (!s || !ms) return XIN_GPU_ERR_ARG;
+    if (s->ndone < 2) return XIN_GPU_ERR_STATE;
+    const xin_gpu_stream::Set &t = s->set[(s->ndone - 1) & 1];   /* the last collected picture */
     for (int i = 0; i < 4; i++) {
         ms[i] = 0;
-        if (cudaEventElapsedTime(&ms[i], s->evs[i], s->evs[i + 1]) != cudaSuccess) { cudaGetLastError(); return XIN_GPU_ERR_STATE; }
+        if (cudaEventElapsedTime(&ms[i], t.evs[i], t.evs[i + 1]) != cudaSuccess) { cudaGetLastError(); return XIN_GPU_ERR_STATE; }
     }
     return XIN_GPU_OK;
 }
@@ -489,10 +530,11 @@ extern "C" int xin_gpu_stream_stage_ms(const xin_gpu_stream *s, float ms[4])
 extern "C" int xin_gpu_stream_device_results(const xin_gpu_stream *s, void **cu, void *q[3], void *rec[3])
 {
     if (!s) return XIN_GPU_ERR_ARG;
-    if (cu) *cu = s->dres;
+    const xin_gpu_stream::Set &t = s->set[(s->ndone - 1) & 1];   /* the last collected picture */
+    if (cu) *cu = t.dres;
     for (int p = 0; p < 3; p++) {
-        if (q) q[p] = s->dq[p];
-        if (rec) rec[p] = s->drec[p];
+        if (q) q[p] = t.dq[p];
+        if (rec) rec[p] = t.drec[p];
     }
     return XIN_GPU_OK;
 }

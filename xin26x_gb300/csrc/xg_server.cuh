@@ -43,14 +43,17 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
             nlev++;
             ncus += (uint64_t)(c->width / XG_LEVEL_SIZE[L]) * (c->height / XG_LEVEL_SIZE[L]);
         }
-    uint64_t d = 2 * (ysz + 2 * csz) + 2 * 16 * ysz + 8 * (ncus ? ncus : 1) + sizeof(xin_gpu_cu_result) * ncus +
-                 sizeof(XgPicParams) + (lq + 2 * lc) * nlev * (sizeof(xg_coef) + sizeof(xg_pix));
+    /* two picture slots with their quarter-pel planes, the search keys, and two
+     * picture sets (results, parameters, pinned staging) */
+    uint64_t d = 2 * (ysz + 2 * csz) + 2 * 16 * ysz + 8 * (ncus ? ncus : 1) +
+                 2 * (sizeof(xin_gpu_cu_result) * ncus + sizeof(XgPicParams) + (lq + 2 * lc) * nlev * (sizeof(xg_coef) + sizeof(xg_pix)));
     uint64_t h = sizeof(XgPicParams) + sizeof(xin_gpu_cu_result) * ncus;
     if (!c->device_io) {
         h += (lq + 2 * lc) * sizeof(xg_pix);
         if (c->out_flags & XIN_GPU_OUT_Q) h += (lq + 2 * lc) * nlev * sizeof(xg_coef);
         if (c->out_flags & XIN_GPU_OUT_REC) h += (lq + 2 * lc) * nlev * sizeof(xg_pix);
     }
+    h *= 2;
     if (dev) *dev = d;
     if (host) *host = h;
     return XIN_GPU_OK;
@@ -145,7 +148,7 @@ static void xg_srv_loop(xin_gpu_server *v)
         for (auto &kv : v->streams) {
             XgSrvStream *t = kv.second;
             if (!t->running) continue;
-            cudaError_t e = cudaEventQuery(t->s->ev1);
+            cudaError_t e = cudaEventQuery(xg_stream_last_event(t->s));
             if (e != cudaErrorNotReady) fin.emplace_back(t, e);
         }
         if (!fin.empty()) {

@@ -60,8 +60,10 @@ class FrameStream:
             raise RuntimeError(f"xin_gpu_frame_submit ({st}): " + self.lib.xin_gpu_last_error().decode())
 
     def wait(self, timeout_ms: int = 60000, copy: bool = True):
-        """Results of the last submitted picture: dict with 'cu' (structured array),
-        'q' / 'rec' (lists of per-plane arrays [levels, h, w]) and 'gpu_ms'."""
+        """Results of the oldest picture in flight (at most two are): dict with 'cu'
+        (structured array), 'q' / 'rec' (lists of per-plane arrays [levels, h, w])
+        and 'gpu_ms'.  copy=False leaves the views of the stream's pinned buffers
+        unread (valid until the second submit after this call)."""
         res = _lib.xin_gpu_results()
         bufs = {}
         if copy:
