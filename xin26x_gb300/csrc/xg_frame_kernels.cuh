@@ -264,14 +264,21 @@ __device__ __forceinline__ uint32_t xg_absdiff2_biased(uint32_t a, uint32_t an, 
 /* word positions per staged band row: the last word a warp reads starts at
  * 48 + (2R) + 12 (8-bit, 4 pixels a word) or 48 + (2R) + 14 (10-bit, 2 pixels) */
 #define XG_ME_RELW(nx) ((nx) + (XG_BITDEPTH == 8 ? 60 : 62))
-#define XG_ME_CUR_WORDS (XG_BITDEPTH == 8 ? 0 : 64 * 32)     /* shared current tile (10-bit) */
-#define XG_ME_D 4                         /* candidate rows per lane and pass (the key packs d in 2 bits: at most 4) */
+#define XG_ME_CUR_WORDS (XG_BITDEPTH == 8 ? 64 * 16 : 64 * 32)   /* the current 64x64 tile in shared memory */
+/* candidate rows per lane and pass, and the key bits that hold the row: 8-bit 8
+ * rows (the register window of current rows is 4 words a row), 10-bit 4 (8
+ * words a row plus their negations) */
+#define XG_ME_D (XG_BITDEPTH == 8 ? 8 : 4)
+#define XG_ME_DB (XG_BITDEPTH == 8 ? 3 : 2)
+/* keys at or above this are not candidates (padding rows, windows) */
+#define XG_ME_KEY_INVALID 0xC0000000u
 #define XG_ME_SLOTS (32 * XG_ME_D)        /* candidates per warp and pass */
 #define XG_ME_SMEM_MAX (216 * 1024)       /* dynamic shared memory of k_me_tiles, under the 227 KB a CTA may have */
 #define XG_ME_NB_MAX 4                    /* passes buffered between 64x64 updates (at most) */
 /* 16x16 SADs [2][16][SLOTS] (double-buffered per pass) + 32x32 SADs [2][nb][4][SLOTS] */
 #define XG_ME_AGG_WORDS(nb) ((2 * 16 + 2 * (nb) * 4) * XG_ME_SLOTS)
-static_assert(XG_ME_D == 4, "the 32x32 exchange gives each of a quadrant's four warps one candidate row");
+static_assert(XG_ME_D % 4 == 0 && (1 << XG_ME_DB) == XG_ME_D,
+              "the 32x32 exchange gives each of a quadrant's four warps XG_ME_D / 4 candidate rows");
 __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, const XgPicParams *pp)
 {
     extern __shared__ uint32_t sm[];
@@ -294,9 +301,8 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     const int nb = p.agg_passes;
     uint32_t *s16 = mvcy + p.band_rows_alloc;                /* [2][16][XG_ME_SLOTS] */
     uint32_t *s32r = s16 + 2 * 16 * XG_ME_SLOTS;             /* [2][nb][4][XG_ME_SLOTS] */
-#if XG_BITDEPTH != 8
-    uint32_t *scur = sm;                                     /* [64][32]: row y, pixels 2k, 2k+1 (16-byte aligned) */
-#endif
+    /* current tile, 16-byte aligned: 8-bit [64][16] (pixels 4k .. 4k+3), 10-bit [64][32] (pixels 2k, 2k+1) */
+    uint32_t *scur = sm;
 
     /* ---- stage the reference band: pixels (X0 + x .. X0 + x + 3, Y0 + r) -> refw[r * row_words + x] */
     const int X0 = tx0 - p.R, Y0 = ty0 + dyb0;
@@ -312,21 +318,18 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     const uint32_t lambda = pp->lambda;
     for (int i = threadIdx.x; i < nx; i += blockDim.x) mvcx[i] = xg_mvd_bits(4 * (i - p.R)) * lambda;
     /* rows past the band (the last chunk's padding) get a sentinel that lifts
-     * their keys to >= 0xE0000000 (lambda <= 2^20 keeps real keys far below) */
+     * their keys to >= XG_ME_KEY_INVALID without wrapping (lambda <= 2^20 keeps
+     * real keys below 2^30) */
     for (int i = threadIdx.x; i < nch * XG_ME_D; i += blockDim.x)
-        mvcy[i] = i < ndy ? xg_mvd_bits(4 * (dyb0 + i)) * lambda : 0x38000000u;
+        mvcy[i] = i < ndy ? xg_mvd_bits(4 * (dyb0 + i)) * lambda : (XG_ME_KEY_INVALID >> XG_ME_DB);
 
-    /* ---- this warp's 16x16 block of the current picture: registers (8-bit) or the shared tile (10-bit) */
+    /* ---- the current tile in shared memory (read as broadcasts) */
     const int bx = (warp & 3) * 16, by = (warp >> 2) * 16;
 #if XG_BITDEPTH == 8
-    uint32_t cur[16][4];
-#pragma unroll
-    for (int r = 0; r < 16; r++)
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const xg_pix *c = p.cur.data + (intptr_t)(ty0 + by + r) * p.cur.pitch + tx0 + bx + 4 * k;
-            cur[r][k] = (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16) | ((uint32_t)c[3] << 24);
-        }
+    for (int i = threadIdx.x; i < 64 * 16; i += blockDim.x) {
+        const xg_pix *c = p.cur.data + (intptr_t)(ty0 + (i >> 4)) * p.cur.pitch + tx0 + 4 * (i & 15);
+        scur[i] = (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16) | ((uint32_t)c[3] << 24);
+    }
 #else
     for (int i = threadIdx.x; i < 64 * 32; i += blockDim.x) {
         const xg_pix *c = p.cur.data + (intptr_t)(ty0 + (i >> 5)) * p.cur.pitch + tx0 + 2 * (i & 31);
@@ -358,8 +361,8 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
         sinterior[warp] = in;
     }
     /* 32x32: this warp's quadrant c32 and its rank jq among the quadrant's four
-     * warps (it evaluates candidate row jq of each pass); 64x64: threads
-     * t < XG_ME_SLOTS, candidate slot t */
+     * warps (it evaluates candidate rows jq * XG_ME_D / 4 .. of each pass);
+     * 64x64: threads t < XG_ME_SLOTS, candidate slot t */
     const int c32 = ((warp >> 1) & 1) + ((warp >> 3) << 1), jq = (warp & 1) + ((warp >> 1) & 2);
     const int c32x = tx0 + (c32 & 1) * 32, c32y = ty0 + (c32 >> 1) * 32;
     const bool live32 = p.keys[1] && c32x + 32 <= p.W && c32y + 32 <= p.H;
@@ -385,8 +388,14 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                 for (int b = 0; b < 4; b++) acc[d][b] = 0;
             /* reference row t of the block feeds current row t - d of candidate row d */
 #if XG_BITDEPTH == 8
+            uint32_t cw[XG_ME_D][4];          /* current rows t .. t-XG_ME_D+1 (slot = row % XG_ME_D) */
+            const uint32_t *crow = scur + by * 16 + (bx >> 2);
 #pragma unroll
             for (int t = 0; t < 16 + XG_ME_D - 1; t++) {
+                if (t < 16) {
+                    const uint4 c4 = *(const uint4 *)(crow + t * 16);
+                    cw[t % XG_ME_D][0] = c4.x; cw[t % XG_ME_D][1] = c4.y; cw[t % XG_ME_D][2] = c4.z; cw[t % XG_ME_D][3] = c4.w;
+                }
                 const uint32_t *q = base + t * p.row_words;
                 const uint32_t w0 = q[0], w1 = q[4], w2 = q[8], w3 = q[12];
 #pragma unroll
@@ -394,10 +403,11 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                     const int r = t - d;
                     if (r >= 0 && r < 16) {
                         const int b = r < 8 ? 0 : 2;
-                        acc[d][b] = xg_sad4(cur[r][0], w0, acc[d][b]);
-                        acc[d][b] = xg_sad4(cur[r][1], w1, acc[d][b]);
-                        acc[d][b + 1] = xg_sad4(cur[r][2], w2, acc[d][b + 1]);
-                        acc[d][b + 1] = xg_sad4(cur[r][3], w3, acc[d][b + 1]);
+                        const uint32_t *c = cw[r % XG_ME_D];
+                        acc[d][b] = xg_sad4(c[0], w0, acc[d][b]);
+                        acc[d][b] = xg_sad4(c[1], w1, acc[d][b]);
+                        acc[d][b + 1] = xg_sad4(c[2], w2, acc[d][b + 1]);
+                        acc[d][b + 1] = xg_sad4(c[3], w3, acc[d][b + 1]);
                     }
                 }
             }
@@ -437,10 +447,10 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                 for (int b = 0; b < 4; b++) acc[d][b] = (acc[d][b] & 0xffffu) + (acc[d][b] >> 16) - 64u * 1024u;
 #endif
             /* Per CU, the best of the lane's XG_ME_D candidates (same column, rows
-             * row0 + d: raster order = d order) as one key (cost << 2) | d, then a
-             * (cost, raster index) compare with the lane's running best.  Keys of
-             * candidates outside the band or the window are >= 0xE0000000, above any
-             * real key (costs stay below 2^27). */
+             * row0 + d: raster order = d order) as one key (cost << XG_ME_DB) | d, then
+             * a (cost, raster index) compare with the lane's running best.  Keys of
+             * candidates outside the band or the window are >= XG_ME_KEY_INVALID,
+             * above any real key (costs stay below 2^27). */
             const int dx = col - p.R, dyl = dyb0 + row0;
             const uint32_t gidx0 = (uint32_t)((dyl + p.R) * nx + col);
             uint32_t md[XG_ME_D];
@@ -448,7 +458,7 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
             /* lanes past the last candidate repeat candidate nv - 1: same key, no effect */
 #pragma unroll
             for (int d = 0; d < XG_ME_D; d++) {
-                md[d] = ((mvcx[col] + mvcy[row0 + d]) << 2) | (uint32_t)d;
+                md[d] = ((mvcx[col] + mvcy[row0 + d]) << XG_ME_DB) | (uint32_t)d;
                 s16w[d * 32] = acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
             }
 #pragma unroll
@@ -457,7 +467,7 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
 #pragma unroll
                 for (int d = 0; d < XG_ME_D; d++) {
                     const uint32_t sad = c < 4 ? acc[d][c] : acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
-                    uint32_t kd = (sad << (XG_COST_FRACTION + 2)) + md[d];
+                    uint32_t kd = (sad << (XG_COST_FRACTION + XG_ME_DB)) + md[d];
                     if (!interior) {
                         const int dy = dyl + d;
                         if (!(dx >= swin[warp][c][0] && dx <= swin[warp][c][1] && dy >= swin[warp][c][2] && dy <= swin[warp][c][3]))
@@ -465,8 +475,8 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                     }
                     k = min(k, kd);
                 }
-                const uint32_t cost = k >> 2, gidx = gidx0 + (k & 3u) * (uint32_t)nx;
-                if (live[c] && k < 0xE0000000u && (cost < best[c] || (cost == best[c] && gidx < bidx[c]))) { best[c] = cost; bidx[c] = gidx; }
+                const uint32_t cost = k >> XG_ME_DB, gidx = gidx0 + (k & (XG_ME_D - 1)) * (uint32_t)nx;
+                if (live[c] && k < XG_ME_KEY_INVALID && (cost < best[c] || (cost == best[c] && gidx < bidx[c]))) { best[c] = cost; bidx[c] = gidx; }
             }
         }
         /* 32x32: the quadrant's four warps swap their 16x16 SADs (double-buffered by
@@ -476,17 +486,21 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
             asm volatile("bar.sync %0, 128;" ::"r"(1 + c32) : "memory");
             const int v = pz * 32 + lane;
             const int vv = v < nv ? v : nv - 1;
-            const int chunk = vv / nx, col = vv - chunk * nx, row = chunk * XG_ME_D + jq;
-            const uint32_t *r16 = s16 + (pz & 1) * 16 * XG_ME_SLOTS + jq * 32 + lane;
-            const uint32_t s32 = r16[w32 * XG_ME_SLOTS] + r16[(w32 + 1) * XG_ME_SLOTS] + r16[(w32 + 4) * XG_ME_SLOTS] +
-                                 r16[(w32 + 5) * XG_ME_SLOTS];
-            s32r[((((pz / nb) & 1) * nb + pz % nb) * 4 + c32) * XG_ME_SLOTS + jq * 32 + lane] = s32;
-            if (live32 && v < nv && row < ndy) {
-                const int dx = col - p.R, dy = dyb0 + row;
-                const uint32_t cost = (s32 << XG_COST_FRACTION) + mvcx[col] + mvcy[row];
-                const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
-                if (dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3] &&
-                    (cost < best32 || (cost == best32 && gidx < bidx32))) { best32 = cost; bidx32 = gidx; }
+            const int chunk = vv / nx, col = vv - chunk * nx;
+#pragma unroll
+            for (int e = 0; e < XG_ME_D / 4; e++) {
+                const int d = jq * (XG_ME_D / 4) + e, row = chunk * XG_ME_D + d;
+                const uint32_t *r16 = s16 + (pz & 1) * 16 * XG_ME_SLOTS + d * 32 + lane;
+                const uint32_t s32 = r16[w32 * XG_ME_SLOTS] + r16[(w32 + 1) * XG_ME_SLOTS] + r16[(w32 + 4) * XG_ME_SLOTS] +
+                                     r16[(w32 + 5) * XG_ME_SLOTS];
+                s32r[((((pz / nb) & 1) * nb + pz % nb) * 4 + c32) * XG_ME_SLOTS + d * 32 + lane] = s32;
+                if (live32 && v < nv && row < ndy) {
+                    const int dx = col - p.R, dy = dyb0 + row;
+                    const uint32_t cost = (s32 << XG_COST_FRACTION) + mvcx[col] + mvcy[row];
+                    const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
+                    if (dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3] &&
+                        (cost < best32 || (cost == best32 && gidx < bidx32))) { best32 = cost; bidx32 = gidx; }
+                }
             }
         }
         /* 64x64 every nb passes, from the four quadrants' 32x32 SADs (the ring is
