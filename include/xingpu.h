@@ -224,6 +224,10 @@ typedef struct xin_gpu_tq_block {
 #define XIN_GPU_TQ_RDOQ_ROUND   4u   /* qAdd = 1 << (qShift - 1) (RDOQ enabled) */
 #define XIN_GPU_TQ_INTRA_PIC    8u   /* qAdd = 171 << (qShift - 9) instead of 85 << (qShift - 9) */
 #define XIN_GPU_TQ_MTS_ENABLED 16u
+/* tile: the CUDA-core kernel's thread-group size (-1 autotune, 0 fixed, 32..256),
+ * or XIN_GPU_TQ_TENSOR: transform passes on the tensor cores (tcgen05, exact
+ * f16 halves, f32 accumulation), transform-skip blocks on the CUDA cores */
+#define XIN_GPU_TQ_TENSOR      (-2)
 int  xin_gpu_tq_batch(const xin_gpu_tq_block *blocks, int32_t nblocks, const XG_COEFF *resid, XG_COEFF *q, XG_COEFF *r,
                       XG_COEFF *resid_out, uint64_t *nz, size_t ncoeffs, int32_t tile);
 /* the same on device arrays (blocks stay a host array); tiles_used (optional,
@@ -242,6 +246,8 @@ int  xin_gpu_tq_plan_create(const xin_gpu_tq_block *blocks, int32_t nblocks, siz
 int  xin_gpu_tq_plan_run(xin_gpu_tq_plan *plan, const XG_COEFF *resid, XG_COEFF *q, XG_COEFF *r, XG_COEFF *resid_out,
                          uint64_t *nz, void *stream);
 int  xin_gpu_tq_plan_tiles(const xin_gpu_tq_plan *plan, int32_t *tiles);
+/* synchronises; XIN_GPU_ERR_TIMEOUT if a tensor-core wait of a run gave up */
+int  xin_gpu_tq_plan_status(xin_gpu_tq_plan *plan);
 void xin_gpu_tq_plan_destroy(xin_gpu_tq_plan *plan);
 
 /* ------------------------------------------------------- motion search (a7-a8)

@@ -40,7 +40,7 @@ def test_tq_batch_matches_oracle_every_tile(bd):
     o = O.oracle(bd)
     blocks, resid = make_batch(600, bd, seed=bd)
     want = oracle_batch(o, blocks, resid)
-    for tile in (0, -1, 32, 64, 128, 256, -1):
+    for tile in (0, -1, 32, 64, 128, 256, -1, -2):
         q, r, ro = np.zeros_like(resid), np.zeros_like(resid), np.zeros_like(resid)
         nz = np.zeros(len(blocks), np.uint64)
         st = g.xin_gpu_tq_batch(blocks.ctypes.data, len(blocks), resid.ctypes.data, q.ctypes.data, r.ctypes.data, ro.ctypes.data,
@@ -75,8 +75,8 @@ def test_tq_batch_kernel_bench_mix_and_errors():
 
 
 def test_tq_batch_full_kernel_bench_autotuned_equals_fixed():
-    """65,536 blocks on device arrays: autotuned and fixed tiles bit-identical, and a
-    seeded sample of 300 blocks bit-exact against the oracle."""
+    """65,536 blocks on device arrays: autotuned tiles, fixed tiles and the tensor-core
+    form bit-identical, and a seeded sample of 300 blocks bit-exact against the oracle."""
     import torch
     from xin26x_gb300 import _lib
     g = _lib.load(10)
@@ -85,11 +85,11 @@ def test_tq_batch_full_kernel_bench_autotuned_equals_fixed():
     d_res = torch.from_numpy(resid).cuda()
     outs = []
     stream = torch.cuda.current_stream().cuda_stream
-    for tile in (-1, 0):
+    for tile in (-1, 0, -2):
         q, r, ro = torch.zeros_like(d_res), torch.zeros_like(d_res), torch.zeros_like(d_res)
         nz = torch.zeros(len(blocks), dtype=torch.int64, device="cuda")
         used = (C.c_int32 * 49)()
-        if tile == 0:
+        if tile != -1:
             st = g.xin_gpu_tq_batch_device(blocks.ctypes.data, len(blocks), d_res.data_ptr(), q.data_ptr(), r.data_ptr(),
                                            ro.data_ptr(), nz.data_ptr(), resid.size, tile, stream, used)
             assert st == 0, g.xin_gpu_last_error()
@@ -106,8 +106,9 @@ def test_tq_batch_full_kernel_bench_autotuned_equals_fixed():
                 blocks["log2w"].astype(int) * 7 + blocks["log2h"], minlength=49)) if n)
         assert all(u in (0, 32, 64, 128, 256) for u in used)
         outs.append([t.cpu().numpy() for t in (q, r, ro, nz)])
-    for a, b in zip(*outs):
-        assert np.array_equal(a, b)
+    for other in outs[1:]:             # fixed tiles and the tensor-core form agree with the autotuned run
+        for a, b in zip(outs[0], other):
+            assert np.array_equal(a, b)
     pick = np.random.default_rng(5).choice(len(blocks), 300, replace=False)
     q, r, ro, nz = outs[0]
     for i in pick:

@@ -139,6 +139,7 @@ SIGNATURES = {
     "xin_gpu_tq_plan_create": ([vp, i32, C.c_size_t, i32, C.POINTER(vp)], C.c_int),
     "xin_gpu_tq_plan_run": ([vp, vp, vp, vp, vp, vp, vp], C.c_int),
     "xin_gpu_tq_plan_tiles": ([vp, vp], C.c_int),
+    "xin_gpu_tq_plan_status": ([vp], C.c_int),
     "xin_gpu_tq_plan_destroy": ([vp], None),
 }
 for _n in ["InterpCopy", "InterpCopyU8S16", "LumaInterpHor", "LumaInterpVet", "LumaInterpHorVet", "LumaInterpHorU8S16",

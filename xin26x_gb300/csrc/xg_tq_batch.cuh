@@ -162,6 +162,8 @@ __global__ void __launch_bounds__(256) k_tq_batch(const XgTqJob *jobs, const uin
     }
 }
 
+#include "xg_tq_tc.cuh"
+
 /* ------------------------------------------------------------------ host */
 struct XgTqTuner {
     std::mutex mu;
@@ -209,7 +211,7 @@ static int xg_tq_pick(int c, int cls_first, int cls_n, const XgTqJob *d_jobs, co
 {
     int lw = c / 7, lh = c % 7, w = 1 << lw, h = 1 << lh;
     if (tile > 0) *G = tile;
-    else if (tile == 0) *G = xg_tq_fixed_group(w, h);
+    else if (tile == 0 || tile == XIN_GPU_TQ_TENSOR) *G = xg_tq_fixed_group(w, h);
     else {
         std::lock_guard<std::mutex> lock(g_tq_tuner.mu);
         *G = g_tq_tuner.g[lw][lh];
@@ -247,15 +249,84 @@ struct xin_gpu_tq_plan {
     size_t ncoeffs;
     int32_t tile;               /* as requested */
     XgTqJob *d_jobs;
-    uint32_t *d_list;
+    uint32_t *d_list;           /* blocks on the CUDA cores, by size class */
     int first[50], cnt[50];
     int G[49];                  /* resolved group size per class, 0 = not resolved yet */
+    /* tensor-core form (tile == XIN_GPU_TQ_TENSOR): transform blocks in tiles of one
+     * size and transform pair; transform-skip blocks stay on the CUDA cores */
+    XgTcTile *d_tiles;
+    uint32_t *d_tlist;
+    int ntiles;
+    int *d_err;                 /* set by a tensor-core wait that timed out */
 };
+
+/* MTS index -> (horizontal, vertical) transform of the host (4 = skip) */
+static const int8_t h_mts_tx[6][2] = { { 0, 0 }, { 4, 4 }, { 2, 2 }, { 1, 2 }, { 2, 1 }, { 1, 1 } };
+
+/* tiles of the tensor-core form: transform blocks grouped by (size, hor, ver),
+ * each tile up to 128 / max(h, min(w, 32)) blocks of one group */
+static void xg_tq_tiles(const xin_gpu_tq_block *blocks, int32_t n, std::vector<XgTcTile> &tiles, std::vector<uint32_t> &tlist,
+                        std::vector<uint32_t> &skip)
+{
+    std::vector<std::pair<uint32_t, uint32_t>> keyed;     /* (group key, block) */
+    for (int i = 0; i < n; i++) {
+        const xin_gpu_tq_block &b = blocks[i];
+        int hor = h_mts_tx[b.mts][0], ver = h_mts_tx[b.mts][1];
+        if (hor == 4) { skip.push_back((uint32_t)i); continue; }
+        if ((b.flags & 1) && !(b.flags & 2) && (b.flags & 16) && b.mts == 0) {   /* implicit MTS */
+            if (b.log2w <= 4) hor = 2;
+            if (b.log2h <= 4) ver = 2;
+        }
+        keyed.push_back({ (uint32_t)((b.log2w * 7 + b.log2h) * 9 + hor * 3 + ver), (uint32_t)i });
+    }
+    /* largest blocks first: the longest tiles start earliest */
+    std::stable_sort(keyed.begin(), keyed.end(), [](const std::pair<uint32_t, uint32_t> &a, const std::pair<uint32_t, uint32_t> &b) {
+        return a.first > b.first;
+    });
+    tlist.resize(keyed.size());
+    for (size_t i = 0; i < keyed.size();) {
+        size_t j = i;
+        while (j < keyed.size() && keyed[j].first == keyed[i].first) j++;
+        const uint32_t key = keyed[i].first, cls = key / 9;
+        const int lw = cls / 7, lh = cls % 7, w = 1 << lw, h = 1 << lh, kw = w > 32 ? 32 : w;
+        const int per = 128 / (h > kw ? h : kw);
+        for (size_t k = i; k < j; k += per) {
+            XgTcTile t;
+            memset(&t, 0, sizeof t);
+            t.first = (uint32_t)k;
+            t.count = (uint8_t)std::min<size_t>(per, j - k);
+            t.lw = (uint8_t)lw; t.lh = (uint8_t)lh; t.hor = (uint8_t)((key % 9) / 3); t.ver = (uint8_t)(key % 3);
+            tiles.push_back(t);
+        }
+        for (size_t k = i; k < j; k++) tlist[k] = keyed[k].second;
+        i = j;
+    }
+}
 
 /* enqueue every class on st; resolves group sizes on first use */
 static int xg_tq_plan_enqueue(xin_gpu_tq_plan *p, const xg_coef *res, xg_coef *q, xg_coef *r, xg_coef *rout,
                               unsigned long long *nz, cudaStream_t st)
 {
+    if (p->ntiles) {
+        /* persistent CTAs: as many as fit at once (shared memory keeps it to at most
+         * four per SM, within the SM's 512 TMEM columns) */
+        static std::once_flag attr_once;
+        static cudaError_t attr_err = cudaSuccess;
+        static int resident = 0;
+        std::call_once(attr_once, [] {
+            attr_err = cudaFuncSetAttribute(k_tq_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, XG_TC_SMEM);
+            int per_sm = 0, dev = 0, sms = 0;
+            if (attr_err == cudaSuccess) attr_err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tq_tc, XG_TC_THREADS, XG_TC_SMEM);
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            resident = std::max(1, std::min(per_sm, 4)) * sms;
+        });
+        if (xg_cuda_check(attr_err, "tq tensor smem attribute")) return XIN_GPU_ERR_CUDA;
+        const int grid = std::min(p->ntiles, resident);
+        k_tq_tc<<<grid, XG_TC_THREADS, XG_TC_SMEM, st>>>(p->d_tiles, p->ntiles, p->d_jobs, p->d_tlist, res, q, r, rout, nz, p->d_err);
+        xg_count_launch(1);
+        if (xg_cuda_check(cudaGetLastError(), "tq tensor launch")) return XIN_GPU_ERR_CUDA;
+    }
     for (int c = 0; c < 49; c++) {
         if (!p->cnt[c]) continue;
         if (!p->G[c]) {
@@ -298,15 +369,29 @@ extern "C" void xin_gpu_tq_plan_destroy(xin_gpu_tq_plan *p)
     if (!p) return;
     cudaFree(p->d_jobs);
     cudaFree(p->d_list);
+    cudaFree(p->d_tiles);
+    cudaFree(p->d_tlist);
+    cudaFree(p->d_err);
     delete p;
+}
+
+/* XIN_GPU_ERR_TIMEOUT if a tensor-core wait of an earlier run gave up (synchronises) */
+static int xg_tq_plan_status(xin_gpu_tq_plan *p)
+{
+    if (!p->d_err) return XIN_GPU_OK;
+    int e = 0;
+    if (xg_cuda_check(cudaMemcpy(&e, p->d_err, sizeof e, cudaMemcpyDeviceToHost), "tq status")) return XIN_GPU_ERR_CUDA;
+    if (e) { xg_set_error(XIN_GPU_ERR_TIMEOUT, "tq_batch: a tensor-core wait timed out"); return XIN_GPU_ERR_TIMEOUT; }
+    return XIN_GPU_OK;
 }
 
 extern "C" int xin_gpu_tq_plan_create(const xin_gpu_tq_block *blocks, int32_t nblocks, size_t ncoeffs, int32_t tile,
                                       xin_gpu_tq_plan **out)
 {
     xin_gpu_clear_error();
-    if (!blocks || nblocks <= 0 || !out || (tile != -1 && tile != 0 && tile != 32 && tile != 64 && tile != 128 && tile != 256)) {
-        xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_create: bad argument (tile must be -1, 0, 32, 64, 128 or 256)");
+    if (!blocks || nblocks <= 0 || !out ||
+        (tile != XIN_GPU_TQ_TENSOR && tile != -1 && tile != 0 && tile != 32 && tile != 64 && tile != 128 && tile != 256)) {
+        xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_create: bad argument (tile must be -2, -1, 0, 32, 64, 128 or 256)");
         return XIN_GPU_ERR_ARG;
     }
     *out = nullptr;
@@ -320,10 +405,35 @@ extern "C" int xin_gpu_tq_plan_create(const xin_gpu_tq_block *blocks, int32_t nb
     p->nblocks = nblocks;
     p->ncoeffs = ncoeffs;
     p->tile = tile;
+    std::vector<XgTcTile> tiles;
+    std::vector<uint32_t> tlist;
+    if (tile == XIN_GPU_TQ_TENSOR) {
+        /* transform blocks go to the tensor cores; the CUDA-core classes keep the skip blocks */
+        std::vector<uint32_t> skip;
+        xg_tq_tiles(blocks, nblocks, tiles, tlist, skip);
+        for (int c = 0; c < 50; c++) { p->first[c] = 0; p->cnt[c] = 0; }
+        for (uint32_t i : skip) p->cnt[blocks[i].log2w * 7 + blocks[i].log2h]++;
+        for (int c = 1; c < 50; c++) p->first[c] = p->first[c - 1] + p->cnt[c - 1];
+        int pos[50];
+        for (int c = 0; c < 50; c++) pos[c] = p->first[c];
+        list.assign(skip.size() ? skip.size() : 1, 0);
+        for (uint32_t i : skip) list[pos[blocks[i].log2w * 7 + blocks[i].log2h]++] = i;
+        p->ntiles = (int)tiles.size();
+    }
     if (xg_cuda_check(cudaMalloc(&p->d_jobs, jobs.size() * sizeof(XgTqJob)), "tq plan") ||
         xg_cuda_check(cudaMalloc(&p->d_list, list.size() * 4), "tq plan") ||
         xg_cuda_check(cudaMemcpy(p->d_jobs, jobs.data(), jobs.size() * sizeof(XgTqJob), cudaMemcpyHostToDevice), "tq plan") ||
         xg_cuda_check(cudaMemcpy(p->d_list, list.data(), list.size() * 4, cudaMemcpyHostToDevice), "tq plan")) {
+        xin_gpu_tq_plan_destroy(p);
+        return XIN_GPU_ERR_CUDA;
+    }
+    if (p->ntiles &&
+        (xg_cuda_check(cudaMalloc(&p->d_tiles, tiles.size() * sizeof(XgTcTile)), "tq plan") ||
+         xg_cuda_check(cudaMalloc(&p->d_tlist, tlist.size() * 4), "tq plan") ||
+         xg_cuda_check(cudaMalloc(&p->d_err, sizeof(int)), "tq plan") ||
+         xg_cuda_check(cudaMemset(p->d_err, 0, sizeof(int)), "tq plan") ||
+         xg_cuda_check(cudaMemcpy(p->d_tiles, tiles.data(), tiles.size() * sizeof(XgTcTile), cudaMemcpyHostToDevice), "tq plan") ||
+         xg_cuda_check(cudaMemcpy(p->d_tlist, tlist.data(), tlist.size() * 4, cudaMemcpyHostToDevice), "tq plan"))) {
         xin_gpu_tq_plan_destroy(p);
         return XIN_GPU_ERR_CUDA;
     }
@@ -351,6 +461,13 @@ extern "C" int xin_gpu_tq_plan_tiles(const xin_gpu_tq_plan *p, int32_t *tiles)
     return XIN_GPU_OK;
 }
 
+extern "C" int xin_gpu_tq_plan_status(xin_gpu_tq_plan *p)
+{
+    xin_gpu_clear_error();
+    if (!p) { xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_status: null plan"); return XIN_GPU_ERR_ARG; }
+    return xg_tq_plan_status(p);
+}
+
 extern "C" int xin_gpu_tq_batch_device(const xin_gpu_tq_block *blocks, int32_t nblocks, const XG_COEFF *resid, XG_COEFF *q,
                                        XG_COEFF *r, XG_COEFF *resid_out, uint64_t *nz, size_t ncoeffs, int32_t tile,
                                        void *stream, int32_t *tiles_used)
@@ -360,6 +477,7 @@ extern "C" int xin_gpu_tq_batch_device(const xin_gpu_tq_block *blocks, int32_t n
     if (st) return st;
     st = xin_gpu_tq_plan_run(p, resid, q, r, resid_out, nz, stream);
     if (!st) st = xg_cuda_check(cudaStreamSynchronize((cudaStream_t)stream), "tq sync");
+    if (!st) st = xg_tq_plan_status(p);
     if (!st && tiles_used) xin_gpu_tq_plan_tiles(p, tiles_used);
     xin_gpu_tq_plan_destroy(p);
     return st;
@@ -374,7 +492,7 @@ extern "C" int xin_gpu_tq_batch(const xin_gpu_tq_block *blocks, int32_t nblocks,
         return XIN_GPU_ERR_ARG;
     }
     if (tile > 0 && tile != 32 && tile != 64 && tile != 128 && tile != 256) {
-        xg_set_error(XIN_GPU_ERR_ARG, "tq_batch: tile must be -1 (autotune), 0 (fixed), 32, 64, 128 or 256");
+        xg_set_error(XIN_GPU_ERR_ARG, "tq_batch: tile must be -2 (tensor cores), -1 (autotune), 0 (fixed), 32, 64, 128 or 256");
         return XIN_GPU_ERR_ARG;
     }
     XgThread *t = xg_thread();
@@ -397,6 +515,7 @@ extern "C" int xin_gpu_tq_batch(const xin_gpu_tq_block *blocks, int32_t nblocks,
              xg_cuda_check(cudaMemcpyAsync(nz, d_nz, (size_t)nblocks * 8, cudaMemcpyDeviceToHost, t->stream), "tq d2h")
                  ? XIN_GPU_ERR_CUDA : XIN_GPU_OK;
     if (!st) st = xg_cuda_check(cudaStreamSynchronize(t->stream), "tq sync");
+    if (!st) st = xg_tq_plan_status(p);
     xin_gpu_tq_plan_destroy(p);
     return st;
 }

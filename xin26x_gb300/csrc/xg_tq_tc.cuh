@@ -1,0 +1,288 @@
+/*
+ * xg_tq_tc.cuh -- the batched transform / quant of xg_tq_batch.cuh on the
+ * tensor cores (tcgen05, accumulators in tensor memory).
+ *
+ * Every transform pass is a product of 16-bit integer samples with the
+ * transform matrix (entries of magnitude <= 90).  The tensor cores compute it
+ * exactly in f16 x f16 -> f32: a sample x (int16) is split into x = 256 hi + lo
+ * with lo in [0, 255] and hi in [-128, 127], both exact in f16; each half's
+ * product sum is an integer below 2^24 in magnitude (64 x 255 x 90), exact in
+ * f32; hi * 256 + lo in int32 is then the integer sum the reference computes.
+ *
+ * A CTA (128 threads, one TMEM lane per thread) takes a tile of up to
+ * 128 / max(h, min(w, 32)) blocks that share size and transform types and runs
+ * the four passes in order, each as M = 128 rows x N x K MMAs (K-major
+ * operands in shared memory, no swizzle) for the high and the low halves:
+ *   F1  rows (b, i)  K = j  N = k  : t1 = clip16(rnd(sum, s1))            (Xin26xFDct*)
+ *   F2  rows (b, k)  K = i  N = kv : coefficient, quant / dequant            (Xin266QuantInvQuant)
+ *   I1  rows (b, j)  K = kv N = y  : t2 = clip16(rnd(sum, 7))              (Xin26xIDct*, columns)
+ *   I2  rows (b, y)  K = j  N = x  : out = clip16(rnd(sum, 20 - bd))       (rows, skip-line rule)
+ * The epilogue of a pass (tcgen05.ld, one row per thread) writes the next
+ * pass's A operand in shared memory.  Transform-skip blocks stay on the CUDA
+ * cores (xg_tq_batch.cuh).
+ */
+
+#include <cuda_fp16.h>
+
+#define XG_TC_THREADS 128
+#define XG_TC_KMAX 64                     /* K and N of any pass are at most 64 */
+#define XG_TC_A_BYTES (128 * XG_TC_KMAX * 2)
+#define XG_TC_B_BYTES (XG_TC_KMAX * XG_TC_KMAX * 2)
+/* dynamic shared memory: A hi, A lo, B, then small state; sized so that at most
+ * four CTAs share an SM (4 x 128 TMEM columns = the SM's 512) */
+#define XG_TC_SMEM (2 * XG_TC_A_BYTES + XG_TC_B_BYTES + 18 * 1024)
+#define XG_TC_TMEM_COLS 128               /* hi accumulator at column 0, lo at 64 */
+
+struct XgTcTile {
+    uint32_t first;                       /* index into the sorted block list */
+    uint8_t count, lw, lh, hor, ver;      /* blocks; log2 sizes; transform types (0 DCT2, 1 DCT8, 2 DST7) */
+    uint8_t pad[3];
+};
+
+/* byte offset of element (row, k) in a K-major, no-swizzle operand with kp
+ * (a multiple of 16) columns: 8-row x 16-byte core matrices, K-direction stride
+ * 128 B, row-group stride kp * 16 B */
+__device__ __forceinline__ int xg_tc_off(int row, int k, int kp) { return ((row >> 3) * (kp >> 3) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2; }
+
+__device__ __forceinline__ uint64_t xg_tc_desc(uint32_t saddr, int kp)
+{
+    uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)(128 >> 4) << 16;                       /* K-direction core-matrix stride */
+    d |= (uint64_t)(((kp >> 3) * 128) >> 4) << 32;         /* 8-row-group stride */
+    d |= (uint64_t)1 << 46;                                /* descriptor version */
+    return d;
+}
+
+/* store x (an int16 value) split into exact f16 halves */
+__device__ __forceinline__ void xg_tc_put(uint8_t *ahi, uint8_t *alo, int off, int x)
+{
+    *(__half *)(ahi + off) = __int2half_rn(x >> 8);
+    *(__half *)(alo + off) = __int2half_rn(x & 255);
+}
+
+/* D[hi|lo] (128 x np) = A[hi|lo] (128 x kp) . B (np x kp)^T, issued by one thread */
+__device__ __forceinline__ void xg_tc_mma(uint32_t tmem, uint32_t ahi, uint32_t alo, uint32_t b, int kp, int np, uint32_t mbar)
+{
+    const uint32_t idesc = (1u << 4) | ((uint32_t)(np >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+    for (int h = 0; h < 2; h++) {
+        const uint32_t a = h ? alo : ahi;
+        for (int kk = 0; kk < kp / 16; kk++) {
+            const uint64_t ad = xg_tc_desc(a + kk * 256, kp), bd = xg_tc_desc(b + kk * 256, kp);
+            const uint32_t en = kk > 0;
+            asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+                         ::"r"(tmem + (h ? 64u : 0u)), "l"(ad), "l"(bd), "r"(idesc), "r"(en) : "memory");
+        }
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+
+/* bounded wait for the commit of phase `phase`; false after about a second */
+__device__ __forceinline__ bool xg_tc_wait(uint32_t mbar, uint32_t phase)
+{
+    uint32_t done = 0;
+    for (long it = 0; it < (1L << 26) && !done; it++)
+        asm volatile("{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+                     : "=r"(done) : "r"(mbar), "r"(phase) : "memory");
+    return done != 0;
+}
+
+/* columns [c0, c0 + 8) of this thread's TMEM lane, hi and lo combined */
+__device__ __forceinline__ void xg_tc_row8(uint32_t tmem, int warp, int c0, int out[8])
+{
+    uint32_t h[8], l[8];
+    const uint32_t a = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(h[0]), "=r"(h[1]), "=r"(h[2]), "=r"(h[3]), "=r"(h[4]), "=r"(h[5]), "=r"(h[6]), "=r"(h[7]) : "r"(a));
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(l[0]), "=r"(l[1]), "=r"(l[2]), "=r"(l[3]), "=r"(l[4]), "=r"(l[5]), "=r"(l[6]), "=r"(l[7]) : "r"(a + 64));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 8; j++) out[j] = (int)__uint_as_float(h[j]) * 256 + (int)__uint_as_float(l[j]);
+}
+
+__global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, int ntiles, const XgTqJob *jobs,
+                                                        const uint32_t *list, const xg_coef *res, xg_coef *q, xg_coef *r,
+                                                        xg_coef *rout, unsigned long long *nzout, int *err)
+{
+    extern __shared__ __align__(1024) uint8_t smc[];
+    uint8_t *ahi = smc, *alo = smc + XG_TC_A_BYTES, *bm = smc + 2 * XG_TC_A_BYTES;
+    uint64_t *mbar = (uint64_t *)(bm + XG_TC_B_BYTES);
+    uint32_t *tslot = (uint32_t *)(mbar + 1);
+    unsigned long long *snz = (unsigned long long *)(mbar + 2);         /* [32] per-block non-zero maps */
+    XgTqJob *sjob = (XgTqJob *)(snz + 32);                              /* [32] */
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t s_ahi = (uint32_t)__cvta_generic_to_shared(ahi), s_alo = (uint32_t)__cvta_generic_to_shared(alo);
+    const uint32_t s_b = (uint32_t)__cvta_generic_to_shared(bm), s_mbar = (uint32_t)__cvta_generic_to_shared(mbar);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"((uint32_t)__cvta_generic_to_shared(tslot)), "r"(XG_TC_TMEM_COLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared.b64 [%0], %1;" ::"r"(s_mbar), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    uint32_t phase = 0;
+    bool ok = true;
+
+    /* one pass: operands written -> MMA -> wait; false (for the whole CTA) on a timeout */
+    auto run_pass = [&](int kp, int np) -> bool {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0) xg_tc_mma(tmem, s_ahi, s_alo, s_b, kp, np, s_mbar);
+        const bool done = xg_tc_wait(s_mbar, phase);
+        phase ^= 1;
+        const bool all = !__syncthreads_or(!done);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        return all;
+    };
+    /* B (np x kp) from an int16 matrix: B[n][k] = m[n * ms_n + k * ms_k] for n < nv, k < kv, else 0 */
+    auto load_b = [&](const int16_t *m, int ms_n, int ms_k, int nv, int kv, int np, int kp) {
+        for (int e = tid; e < np * kp; e += XG_TC_THREADS) {
+            const int n = e / kp, k = e - n * kp;
+            *(__half *)(bm + xg_tc_off(n, k, kp)) = __int2half_rn(n < nv && k < kv ? m[n * ms_n + k * ms_k] : 0);
+        }
+    };
+    auto zero_a = [&](int kp) {
+        for (int e = tid; e < 128 * kp / 8; e += XG_TC_THREADS) {
+            ((uint4 *)ahi)[e] = make_uint4(0, 0, 0, 0);
+            ((uint4 *)alo)[e] = make_uint4(0, 0, 0, 0);
+        }
+    };
+
+    for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+        const XgTcTile tl = tiles[ti];
+        const int T = tl.count, lw = tl.lw, lh = tl.lh, w = 1 << lw, h = 1 << lh;
+        const int kw = w > 32 ? 32 : w, kh = h > 32 ? 32 : h;
+        const int sline = (tl.hor != 0 && w == 32) ? 16 : (w > 32 ? w - 32 : 0), jmax = w - sline;
+        const int16_t *mh = xg_mat(tl.hor, lw), *mv = xg_mat(tl.ver, lh);
+        const int p16 = 16;
+        auto rnd16 = [&](int v) { return (v + p16 - 1) & ~(p16 - 1); };
+        if (tid < T) { sjob[tid] = jobs[list[tl.first + tid]]; snz[tid] = 0; }
+        __syncthreads();
+
+        /* ---- F1: A[(b, i)][j] = residual; B[k][j] = mh[k][j] */
+        {
+            const int kp = rnd16(w), np = rnd16(kw);
+            zero_a(kp);
+            load_b(mh, w, 1, kw, w, np, kp);
+            __syncthreads();
+            for (int e = tid; e < T * h * w; e += XG_TC_THREADS) {
+                const int b = e / (h * w), o = e - b * h * w, i = o / w, j = o - i * w;
+                xg_tc_put(ahi, alo, xg_tc_off(b * h + i, j, kp), (int16_t)res[sjob[b].off + o]);
+            }
+            if (!(ok = run_pass(kp, np))) break;
+        }
+        /* ---- F1 epilogue -> F2 operand A[(b, k)][i] = t1 (the MMA is done: A and B are free) */
+        {
+            const int kp = rnd16(h), np = rnd16(kh);
+            zero_a(kp);
+            load_b(mv, h, 1, kh, h, np, kp);
+            __syncthreads();
+            const int m = tid, b = m / h, i = m - b * h;
+            const bool valid = m < T * h;
+            const int s1 = lw + XG_BITDEPTH + 6 - 15;
+            for (int c = 0; c < rnd16(kw); c += 8) {
+                int v[8];
+                xg_tc_row8(tmem, warp, c, v);
+#pragma unroll
+                for (int j = 0; j < 8; j++)
+                    if (valid && c + j < kw) xg_tc_put(ahi, alo, xg_tc_off(b * kw + c + j, i, kp), xg_clip16(xg_rshift_rnd(v[j], s1)));
+            }
+            if (!(ok = run_pass(kp, np))) break;
+        }
+        /* ---- F2 epilogue: quant / dequant, q and r out; -> I1 operand A[(b, j)][kv] = r (the same rows) */
+        {
+            const int kp = rnd16(kh), np = rnd16(h);
+            zero_a(kp);
+            load_b(mv, 1, h, h, kh, np, kp);                 /* B[y][kv] = mv[kv][y] */
+            __syncthreads();
+            const int m = tid, b = m / kw, k = m - b * kw;     /* row (b, k): coefficients C[kv][k] */
+            const bool valid = m < T * kw;
+            const XgTqJob jb = sjob[valid ? b : 0];
+            const int s2 = lh + 6;
+            /* quant parameters (Xin266ConstructQuantParam + Xin266Transform), as in k_tq_batch */
+            const int adj = ((lw + lh) & 1), lgs = (lw + lh) >> 1;
+            const int qp = jb.qp + (XG_BITDEPTH == 10 ? 12 : 0), per = qp / 6, rem = qp % 6;
+            const int qmult = c_qmult[adj][rem], iqmult = c_iqmult[adj][rem] << per;
+            const int qshift = 14 + (15 - XG_BITDEPTH) + per - lgs - adj, iqshift = 6 - (15 - XG_BITDEPTH) + lgs + adj;
+            const int qadd = (jb.flags & 4) ? (1 << (qshift - 1)) : (((jb.flags & 8) ? 171 : 85) << (qshift - 9));
+            const int iqadd = 1 << (iqshift - 1);
+            unsigned long long nzb = 0;
+            for (int c = 0; c < rnd16(kh); c += 8) {
+                int v[8];
+                xg_tc_row8(tmem, warp, c, v);
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const int kv = c + j;
+                    if (!valid || kv >= kh) continue;
+                    const int tv = xg_clip16(xg_rshift_rnd(v[j], s2)), a = abs(tv);
+                    int qv = (int)(((long long)a * qmult + qadd) >> qshift);
+                    qv = xg_clip16(tv < 0 ? -qv : qv);
+                    const int rv = xg_clip16((int)(((long long)qv * iqmult + iqadd) >> iqshift));
+                    q[jb.off + kv * w + k] = (xg_coef)qv;
+                    r[jb.off + kv * w + k] = (xg_coef)rv;
+                    if (qv) nzb |= 1ull << ((kv >> 2) * (kw >> 2) + (k >> 2));
+                    if (k < jmax) xg_tc_put(ahi, alo, xg_tc_off(m, kv, kp), rv);
+                }
+            }
+            if (nzb) atomicOr(&snz[b], nzb);
+            if (!(ok = run_pass(kp, np))) break;
+        }
+        /* zeros of q / r beyond the kept 32 x 32 (64-wide or -high blocks), and the maps */
+        if (w > 32 || h > 32)
+            for (int bb = 0; bb < T; bb++) {
+                const uint32_t off = sjob[bb].off;
+                for (int o = tid; o < w * h; o += XG_TC_THREADS) {
+                    const int y = o / w, x = o - y * w;
+                    if (y >= kh || x >= kw) { q[off + o] = 0; r[off + o] = 0; }
+                }
+            }
+        if (tid < T) nzout[list[tl.first + tid]] = snz[tid];
+        /* ---- I1 epilogue -> I2 operand A[(b, y)][j] = t2 */
+        {
+            const int kp = rnd16(jmax), np = rnd16(w);
+            zero_a(kp);
+            load_b(mh, 1, w, w, jmax, np, kp);               /* B[x][j] = mh[j][x] */
+            __syncthreads();
+            const int m = tid, b = m / kw, j = m - b * kw;
+            const bool valid = m < T * kw && j < jmax;
+            for (int c = 0; c < rnd16(h); c += 8) {
+                int v[8];
+                xg_tc_row8(tmem, warp, c, v);
+#pragma unroll
+                for (int jj = 0; jj < 8; jj++)
+                    if (valid && c + jj < h) xg_tc_put(ahi, alo, xg_tc_off(b * h + c + jj, j, kp), xg_clip16(xg_rshift_rnd(v[jj], 7)));
+            }
+            if (!(ok = run_pass(kp, np))) break;
+        }
+        /* ---- I2 epilogue: the reconstructed residual */
+        {
+            const int m = tid, b = m / h, y = m - b * h;
+            const bool valid = m < T * h;
+            const int s2 = 6 + 15 - 1 - XG_BITDEPTH;
+            const int off = valid ? sjob[b].off + y * w : 0;
+            for (int c = 0; c < rnd16(w); c += 8) {
+                int v[8];
+                xg_tc_row8(tmem, warp, c, v);
+#pragma unroll
+                for (int x = 0; x < 8; x++)
+                    if (valid && c + x < w) rout[off + c + x] = (xg_coef)xg_clip16(xg_rshift_rnd(v[x], s2));
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+    if (!ok && tid == 0) atomicExch(err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(XG_TC_TMEM_COLS) : "memory");
+}
