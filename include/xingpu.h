@@ -228,6 +228,7 @@ typedef struct xin_gpu_tq_block {
  * or XIN_GPU_TQ_TENSOR: transform passes on the tensor cores (tcgen05, exact
  * f16 halves, f32 accumulation), transform-skip blocks on the CUDA cores */
 #define XIN_GPU_TQ_TENSOR      (-2)
+/* host arrays of ncoeffs samples; samples that no block covers are returned as zeros */
 int  xin_gpu_tq_batch(const xin_gpu_tq_block *blocks, int32_t nblocks, const XG_COEFF *resid, XG_COEFF *q, XG_COEFF *r,
                       XG_COEFF *resid_out, uint64_t *nz, size_t ncoeffs, int32_t tile);
 /* the same on device arrays (blocks stay a host array); tiles_used (optional,

@@ -118,3 +118,28 @@ def test_tq_batch_full_kernel_bench_autotuned_equals_fixed():
         wq, wr, wro, wnz = oracle_batch(o, sub, resid[off:off + n].copy())
         assert np.array_equal(q[off:off + n], wq) and np.array_equal(r[off:off + n], wr)
         assert np.array_equal(ro[off:off + n], wro) and int(nz[i]) == int(wnz[0].astype(np.int64))
+
+
+def test_tq_tensor_form_with_unaligned_offsets():
+    """Blocks at offsets that are not multiples of 8 samples (which the tensor-core
+    kernel's vector loads cannot take) go to the CUDA cores; the batch stays bit-exact."""
+    from xin26x_gb300 import _lib
+    g = _lib.load(10)
+    o = O.oracle(10)
+    blocks, packed = make_batch(300, 10, seed=77)
+    resid = np.zeros(packed.size + 3 * len(blocks), packed.dtype)
+    off = 0
+    for i in range(len(blocks)):
+        n = 1 << (int(blocks["log2w"][i]) + int(blocks["log2h"][i]))
+        src = int(blocks["offset"][i])
+        off += 3 * (i % 2)                      # every other block starts 3 samples later
+        resid[off:off + n] = packed[src:src + n]
+        blocks["offset"][i] = off
+        off += n
+    want = oracle_batch(o, blocks, resid)
+    q, r, ro = np.zeros_like(resid), np.zeros_like(resid), np.zeros_like(resid)
+    nz = np.zeros(len(blocks), np.uint64)
+    assert g.xin_gpu_tq_batch(blocks.ctypes.data, len(blocks), resid.ctypes.data, q.ctypes.data, r.ctypes.data,
+                              ro.ctypes.data, nz.ctypes.data, resid.size, -2) == 0, g.xin_gpu_last_error()
+    for name, a, b in zip(("q", "r", "resid_out", "nz"), (q, r, ro, nz), want):
+        assert np.array_equal(a, b), name

@@ -272,7 +272,9 @@ static void xg_tq_tiles(const xin_gpu_tq_block *blocks, int32_t n, std::vector<X
     for (int i = 0; i < n; i++) {
         const xin_gpu_tq_block &b = blocks[i];
         int hor = h_mts_tx[b.mts][0], ver = h_mts_tx[b.mts][1];
-        if (hor == 4) { skip.push_back((uint32_t)i); continue; }
+        /* transform skip, and blocks whose offset does not allow the tensor kernel's
+         * 8-sample vector loads, stay on the CUDA cores */
+        if (hor == 4 || (b.offset & 7)) { skip.push_back((uint32_t)i); continue; }
         if ((b.flags & 1) && !(b.flags & 2) && (b.flags & 16) && b.mts == 0) {   /* implicit MTS */
             if (b.log2w <= 4) hor = 2;
             if (b.log2h <= 4) ver = 2;
@@ -307,6 +309,10 @@ static void xg_tq_tiles(const xin_gpu_tq_block *blocks, int32_t n, std::vector<X
 static int xg_tq_plan_enqueue(xin_gpu_tq_plan *p, const xg_coef *res, xg_coef *q, xg_coef *r, xg_coef *rout,
                               unsigned long long *nz, cudaStream_t st)
 {
+    if (p->ntiles && ((uintptr_t)res & 15)) {
+        xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_run: the tensor-core form needs 16-byte aligned residuals");
+        return XIN_GPU_ERR_ARG;
+    }
     if (p->ntiles) {
         /* persistent CTAs: as many as fit at once (shared memory keeps it to at most
          * four per SM, within the SM's 512 TMEM columns) */
@@ -315,10 +321,11 @@ static int xg_tq_plan_enqueue(xin_gpu_tq_plan *p, const xg_coef *res, xg_coef *q
         static int resident = 0;
         std::call_once(attr_once, [] {
             attr_err = cudaFuncSetAttribute(k_tq_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, XG_TC_SMEM);
-            int per_sm = 0, dev = 0, sms = 0;
-            if (attr_err == cudaSuccess) attr_err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tq_tc, XG_TC_THREADS, XG_TC_SMEM);
+            int dev = 0, sms = 0, smem_sm = 0;
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+            const int per_sm = smem_sm / (XG_TC_SMEM + 1024);     /* the runtime keeps 1 KB per CTA */
             resident = std::max(1, std::min(per_sm, 4)) * sms;
         });
         if (xg_cuda_check(attr_err, "tq tensor smem attribute")) return XIN_GPU_ERR_CUDA;
@@ -506,6 +513,10 @@ extern "C" int xin_gpu_tq_batch(const xin_gpu_tq_block *blocks, int32_t nblocks,
     unsigned long long *d_nz = (unsigned long long *)xg_dalloc(t, (size_t)nblocks * 8);
     if (!d_res || !d_q || !d_r || !d_o || !d_nz) { xin_gpu_tq_plan_destroy(p); return xin_gpu_last_status(); }
     st = xg_cuda_check(cudaMemcpyAsync(d_res, resid, bytes, cudaMemcpyHostToDevice, t->stream), "tq h2d");
+    /* samples that no block covers come back as zeros, not as staging leftovers */
+    if (!st) st = xg_cuda_check(cudaMemsetAsync(d_q, 0, bytes, t->stream), "tq clear") ||
+                  xg_cuda_check(cudaMemsetAsync(d_r, 0, bytes, t->stream), "tq clear") ||
+                  xg_cuda_check(cudaMemsetAsync(d_o, 0, bytes, t->stream), "tq clear") ? XIN_GPU_ERR_CUDA : XIN_GPU_OK;
     if (!st) st = xin_gpu_tq_plan_run(p, (const XG_COEFF *)d_res, (XG_COEFF *)d_q, (XG_COEFF *)d_r, (XG_COEFF *)d_o,
                                       (uint64_t *)d_nz, t->stream);
     if (!st)

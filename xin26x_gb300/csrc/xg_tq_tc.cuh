@@ -27,10 +27,11 @@
 #define XG_TC_THREADS 128
 #define XG_TC_KMAX 64                     /* K and N of any pass are at most 64 */
 #define XG_TC_A_BYTES (128 * XG_TC_KMAX * 2)
-#define XG_TC_B_BYTES (XG_TC_KMAX * XG_TC_KMAX * 2)
-/* dynamic shared memory: A hi, A lo, B, then small state; sized so that at most
- * four CTAs share an SM (4 x 128 TMEM columns = the SM's 512) */
-#define XG_TC_SMEM (2 * XG_TC_A_BYTES + XG_TC_B_BYTES + 18 * 1024)
+#define XG_TC_B_BYTES (32 * XG_TC_KMAX * 2)    /* one pass's B: at most 32 x 64 or 64 x 32 */
+/* dynamic shared memory: A hi, A lo, the four passes' B (kept while the tile
+ * group does not change), then small state; 50 KB lets four CTAs share an SM,
+ * and no more (4 x 128 TMEM columns = the SM's 512) */
+#define XG_TC_SMEM (50 * 1024)
 #define XG_TC_TMEM_COLS 128               /* hi accumulator at column 0, lo at 64 */
 
 struct XgTcTile {
@@ -106,14 +107,15 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                                                         xg_coef *rout, unsigned long long *nzout, int *err)
 {
     extern __shared__ __align__(1024) uint8_t smc[];
-    uint8_t *ahi = smc, *alo = smc + XG_TC_A_BYTES, *bm = smc + 2 * XG_TC_A_BYTES;
-    uint64_t *mbar = (uint64_t *)(bm + XG_TC_B_BYTES);
+    uint8_t *ahi = smc, *alo = smc + XG_TC_A_BYTES, *bm = smc + 2 * XG_TC_A_BYTES;   /* bm: [4][XG_TC_B_BYTES] */
+    uint64_t *mbar = (uint64_t *)(bm + 4 * XG_TC_B_BYTES);
     uint32_t *tslot = (uint32_t *)(mbar + 1);
     unsigned long long *snz = (unsigned long long *)(mbar + 2);         /* [32] per-block non-zero maps */
     XgTqJob *sjob = (XgTqJob *)(snz + 32);                              /* [32] */
     const int tid = threadIdx.x, warp = tid >> 5;
     const uint32_t s_ahi = (uint32_t)__cvta_generic_to_shared(ahi), s_alo = (uint32_t)__cvta_generic_to_shared(alo);
     const uint32_t s_b = (uint32_t)__cvta_generic_to_shared(bm), s_mbar = (uint32_t)__cvta_generic_to_shared(mbar);
+    static_assert(2 * XG_TC_A_BYTES + 4 * XG_TC_B_BYTES + 16 + 32 * 8 + 32 * sizeof(XgTqJob) <= XG_TC_SMEM, "shared layout");
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                      ::"r"((uint32_t)__cvta_generic_to_shared(tslot)), "r"(XG_TC_TMEM_COLS) : "memory");
@@ -130,24 +132,35 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
     uint32_t phase = 0;
     bool ok = true;
 
-    /* one pass: operands written -> MMA -> wait; false (for the whole CTA) on a timeout */
-    auto run_pass = [&](int kp, int np) -> bool {
+    /* one pass: operands written -> MMA with B number bi -> wait; false (for the whole CTA) on a timeout */
+    auto run_pass = [&](int bi, int kp, int np) -> bool {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (tid == 0) xg_tc_mma(tmem, s_ahi, s_alo, s_b, kp, np, s_mbar);
+        if (tid == 0) xg_tc_mma(tmem, s_ahi, s_alo, s_b + bi * XG_TC_B_BYTES, kp, np, s_mbar);
         const bool done = xg_tc_wait(s_mbar, phase);
         phase ^= 1;
         const bool all = !__syncthreads_or(!done);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         return all;
     };
-    /* B (np x kp) from an int16 matrix: B[n][k] = m[n * ms_n + k * ms_k] for n < nv, k < kv, else 0 */
-    auto load_b = [&](const int16_t *m, int ms_n, int ms_k, int nv, int kv, int np, int kp) {
-        for (int e = tid; e < np * kp; e += XG_TC_THREADS) {
-            const int n = e / kp, k = e - n * kp;
-            *(__half *)(bm + xg_tc_off(n, k, kp)) = __int2half_rn(n < nv && k < kv ? m[n * ms_n + k * ms_k] : 0);
+    /* B number bi (np x kp) from an int16 matrix: B[n][k] = m[n * ms_n + k * ms_k] for n < nv, k < kv, else 0 */
+    auto load_b = [&](int bi, const int16_t *m, int ms_n, int ms_k, int nv, int kv, int np, int kp) {
+        uint8_t *bb = bm + bi * XG_TC_B_BYTES;
+        const int lkp = 31 - __clz(kp);                                   /* kp: 16, 32 or 64 */
+        for (int e0 = tid; e0 < np * kp; e0 += 8 * XG_TC_THREADS) {
+            int16_t v[8];                 /* eight independent loads in flight, then the stores */
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int e = e0 + u * XG_TC_THREADS, n = e >> lkp, k = e & (kp - 1);
+                v[u] = (e < np * kp && n < nv && k < kv) ? m[n * ms_n + k * ms_k] : (int16_t)0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int e = e0 + u * XG_TC_THREADS;
+                if (e < np * kp) *(__half *)(bb + xg_tc_off(e >> lkp, e & (kp - 1), kp)) = __int2half_rn(v[u]);
+            }
         }
     };
     auto zero_a = [&](int kp) {
@@ -157,7 +170,10 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
         }
     };
 
-    for (int ti = blockIdx.x; ti < ntiles && ok; ti += gridDim.x) {
+    /* a contiguous range of tiles per CTA: consecutive tiles mostly share their group's matrices */
+    const int per = (ntiles + gridDim.x - 1) / gridDim.x, t_end = min(ntiles, (int)(blockIdx.x + 1) * per);
+    int cached = -1;                      /* group (sizes and transform pair) whose B are loaded */
+    for (int ti = blockIdx.x * per; ti < t_end && ok; ti++) {
         const XgTcTile tl = tiles[ti];
         const int T = tl.count, lw = tl.lw, lh = tl.lh, w = 1 << lw, h = 1 << lh;
         const int kw = w > 32 ? 32 : w, kh = h > 32 ? 32 : h;
@@ -166,27 +182,56 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
         const int p16 = 16;
         auto rnd16 = [&](int v) { return (v + p16 - 1) & ~(p16 - 1); };
         if (tid < T) { sjob[tid] = jobs[list[tl.first + tid]]; snz[tid] = 0; }
+        const int group = ((lw * 7 + lh) * 3 + tl.hor) * 3 + tl.ver;
+        if (group != cached) {            /* the previous tile's MMAs are all done */
+            load_b(0, mh, w, 1, kw, w, rnd16(kw), rnd16(w));         /* F1: B[k][j] = mh[k][j] */
+            load_b(1, mv, h, 1, kh, h, rnd16(kh), rnd16(h));         /* F2: B[kv][i] = mv[kv][i] */
+            load_b(2, mv, 1, h, h, kh, rnd16(h), rnd16(kh));         /* I1: B[y][kv] = mv[kv][y] */
+            load_b(3, mh, 1, w, w, jmax, rnd16(w), rnd16(jmax));     /* I2: B[x][j] = mh[j][x] */
+            cached = group;
+        }
         __syncthreads();
 
         /* ---- F1: A[(b, i)][j] = residual; B[k][j] = mh[k][j] */
         {
             const int kp = rnd16(w), np = rnd16(kw);
             zero_a(kp);
-            load_b(mh, w, 1, kw, w, np, kp);
             __syncthreads();
-            for (int e = tid; e < T * h * w; e += XG_TC_THREADS) {
-                const int b = e / (h * w), o = e - b * h * w, i = o / w, j = o - i * w;
-                xg_tc_put(ahi, alo, xg_tc_off(b * h + i, j, kp), (int16_t)res[sjob[b].off + o]);
+            /* eight consecutive samples per load (16-byte aligned: the plan keeps block
+             * offsets at multiples of 8), four chunks in flight per thread */
+            const int nchunk = (T * h * w) >> 3, lbs = lw + lh;
+            for (int c0 = tid; c0 < nchunk; c0 += 4 * XG_TC_THREADS) {
+                xg_coef v[4][8];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int c = c0 + u * XG_TC_THREADS;
+                    if (c < nchunk) {
+                        const int e = c << 3, b = e >> lbs, o = e & ((1 << lbs) - 1);
+                        const uint4 *src = (const uint4 *)(res + sjob[b].off + o);
+                        *(uint4 *)v[u] = src[0];
+                        if (sizeof(xg_coef) == 4) *(uint4 *)(v[u] + 4) = src[1];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int c = c0 + u * XG_TC_THREADS;
+                    if (c >= nchunk) continue;
+                    const int e = c << 3, b = e >> lbs, o = e & ((1 << lbs) - 1);
+#pragma unroll
+                    for (int x = 0; x < 8; x++) {
+                        const int i = (o + x) >> lw, j = (o + x) & (w - 1);
+                        xg_tc_put(ahi, alo, xg_tc_off(b * h + i, j, kp), (int16_t)v[u][x]);
+                    }
+                }
             }
-            if (!(ok = run_pass(kp, np))) break;
+            if (!(ok = run_pass(0, kp, np))) break;
         }
         /* ---- F1 epilogue -> F2 operand A[(b, k)][i] = t1 (the MMA is done: A and B are free) */
         {
             const int kp = rnd16(h), np = rnd16(kh);
             zero_a(kp);
-            load_b(mv, h, 1, kh, h, np, kp);
             __syncthreads();
-            const int m = tid, b = m / h, i = m - b * h;
+            const int m = tid, b = m >> lh, i = m & (h - 1);
             const bool valid = m < T * h;
             const int s1 = lw + XG_BITDEPTH + 6 - 15;
             for (int c = 0; c < rnd16(kw); c += 8) {
@@ -196,15 +241,15 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                 for (int j = 0; j < 8; j++)
                     if (valid && c + j < kw) xg_tc_put(ahi, alo, xg_tc_off(b * kw + c + j, i, kp), xg_clip16(xg_rshift_rnd(v[j], s1)));
             }
-            if (!(ok = run_pass(kp, np))) break;
+            if (!(ok = run_pass(1, kp, np))) break;
         }
         /* ---- F2 epilogue: quant / dequant, q and r out; -> I1 operand A[(b, j)][kv] = r (the same rows) */
         {
             const int kp = rnd16(kh), np = rnd16(h);
             zero_a(kp);
-            load_b(mv, 1, h, h, kh, np, kp);                 /* B[y][kv] = mv[kv][y] */
             __syncthreads();
-            const int m = tid, b = m / kw, k = m - b * kw;     /* row (b, k): coefficients C[kv][k] */
+            const int lkw = lw > 5 ? 5 : lw;
+            const int m = tid, b = m >> lkw, k = m & (kw - 1);     /* row (b, k): coefficients C[kv][k] */
             const bool valid = m < T * kw;
             const XgTqJob jb = sjob[valid ? b : 0];
             const int s2 = lh + 6;
@@ -234,14 +279,14 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                 }
             }
             if (nzb) atomicOr(&snz[b], nzb);
-            if (!(ok = run_pass(kp, np))) break;
+            if (!(ok = run_pass(2, kp, np))) break;
         }
         /* zeros of q / r beyond the kept 32 x 32 (64-wide or -high blocks), and the maps */
         if (w > 32 || h > 32)
             for (int bb = 0; bb < T; bb++) {
                 const uint32_t off = sjob[bb].off;
                 for (int o = tid; o < w * h; o += XG_TC_THREADS) {
-                    const int y = o / w, x = o - y * w;
+                    const int y = o >> lw, x = o & (w - 1);
                     if (y >= kh || x >= kw) { q[off + o] = 0; r[off + o] = 0; }
                 }
             }
@@ -250,9 +295,9 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
         {
             const int kp = rnd16(jmax), np = rnd16(w);
             zero_a(kp);
-            load_b(mh, 1, w, w, jmax, np, kp);               /* B[x][j] = mh[j][x] */
             __syncthreads();
-            const int m = tid, b = m / kw, j = m - b * kw;
+            const int lkw = lw > 5 ? 5 : lw;
+            const int m = tid, b = m >> lkw, j = m & (kw - 1);
             const bool valid = m < T * kw && j < jmax;
             for (int c = 0; c < rnd16(h); c += 8) {
                 int v[8];
@@ -261,11 +306,11 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                 for (int jj = 0; jj < 8; jj++)
                     if (valid && c + jj < h) xg_tc_put(ahi, alo, xg_tc_off(b * h + c + jj, j, kp), xg_clip16(xg_rshift_rnd(v[jj], 7)));
             }
-            if (!(ok = run_pass(kp, np))) break;
+            if (!(ok = run_pass(3, kp, np))) break;
         }
         /* ---- I2 epilogue: the reconstructed residual */
         {
-            const int m = tid, b = m / h, y = m - b * h;
+            const int m = tid, b = m >> lh, y = m & (h - 1);
             const bool valid = m < T * h;
             const int s2 = 6 + 15 - 1 - XG_BITDEPTH;
             const int off = valid ? sjob[b].off + y * w : 0;
