@@ -309,8 +309,8 @@ static void xg_tq_tiles(const xin_gpu_tq_block *blocks, int32_t n, std::vector<X
 static int xg_tq_plan_enqueue(xin_gpu_tq_plan *p, const xg_coef *res, xg_coef *q, xg_coef *r, xg_coef *rout,
                               unsigned long long *nz, cudaStream_t st)
 {
-    if (p->ntiles && ((uintptr_t)res & 15)) {
-        xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_run: the tensor-core form needs 16-byte aligned residuals");
+    if (p->ntiles && (((uintptr_t)res | (uintptr_t)rout) & 15)) {
+        xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_run: the tensor-core form needs 16-byte aligned residual arrays");
         return XIN_GPU_ERR_ARG;
     }
     if (p->ntiles) {

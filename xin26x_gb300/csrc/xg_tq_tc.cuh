@@ -102,6 +102,40 @@ __device__ __forceinline__ void xg_tc_row8(uint32_t tmem, int warp, int c0, int 
     for (int j = 0; j < 8; j++) out[j] = (int)__uint_as_float(h[j]) * 256 + (int)__uint_as_float(l[j]);
 }
 
+/* columns [c0, c0 + 16) of this thread's TMEM lane, hi and lo combined: both
+ * loads in flight before one wait */
+__device__ __forceinline__ void xg_tc_row16(uint32_t tmem, int warp, int c0, int out[16])
+{
+    uint32_t h[16], l[16];
+    const uint32_t a = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                 : "=r"(h[0]), "=r"(h[1]), "=r"(h[2]), "=r"(h[3]), "=r"(h[4]), "=r"(h[5]), "=r"(h[6]), "=r"(h[7]),
+                   "=r"(h[8]), "=r"(h[9]), "=r"(h[10]), "=r"(h[11]), "=r"(h[12]), "=r"(h[13]), "=r"(h[14]), "=r"(h[15])
+                 : "r"(a));
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+                 : "=r"(l[0]), "=r"(l[1]), "=r"(l[2]), "=r"(l[3]), "=r"(l[4]), "=r"(l[5]), "=r"(l[6]), "=r"(l[7]),
+                   "=r"(l[8]), "=r"(l[9]), "=r"(l[10]), "=r"(l[11]), "=r"(l[12]), "=r"(l[13]), "=r"(l[14]), "=r"(l[15])
+                 : "r"(a + 64));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; j++) out[j] = (int)__uint_as_float(h[j]) * 256 + (int)__uint_as_float(l[j]);
+}
+
+/* eight int16 values as the f16 halves of one 16-byte core-matrix row each */
+__device__ __forceinline__ void xg_tc_put8(uint8_t *ahi, uint8_t *alo, int off, const int x[8])
+{
+    uint32_t hw[4], lw[4];
+#pragma unroll
+    for (int p = 0; p < 4; p++) {
+        const __half2 hh = __halves2half2(__int2half_rn(x[2 * p] >> 8), __int2half_rn(x[2 * p + 1] >> 8));
+        const __half2 ll = __halves2half2(__int2half_rn(x[2 * p] & 255), __int2half_rn(x[2 * p + 1] & 255));
+        hw[p] = *(const uint32_t *)&hh;
+        lw[p] = *(const uint32_t *)&ll;
+    }
+    *(uint4 *)(ahi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+    *(uint4 *)(alo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+}
+
 __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, int ntiles, const XgTqJob *jobs,
                                                         const uint32_t *list, const xg_coef *res, xg_coef *q, xg_coef *r,
                                                         xg_coef *rout, unsigned long long *nzout, int *err)
@@ -217,10 +251,15 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                     const int c = c0 + u * XG_TC_THREADS;
                     if (c >= nchunk) continue;
                     const int e = c << 3, b = e >> lbs, o = e & ((1 << lbs) - 1);
+                    int x8[8];
 #pragma unroll
-                    for (int x = 0; x < 8; x++) {
-                        const int i = (o + x) >> lw, j = (o + x) & (w - 1);
-                        xg_tc_put(ahi, alo, xg_tc_off(b * h + i, j, kp), (int16_t)v[u][x]);
+                    for (int x = 0; x < 8; x++) x8[x] = (int16_t)v[u][x];
+                    if (w >= 8) {         /* one core-matrix row: columns j .. j + 7 of row i */
+                        xg_tc_put8(ahi, alo, xg_tc_off(b * h + (o >> lw), o & (w - 1), kp), x8);
+                    } else {
+#pragma unroll
+                        for (int x = 0; x < 8; x++)
+                            xg_tc_put(ahi, alo, xg_tc_off(b * h + ((o + x) >> lw), (o + x) & (w - 1), kp), x8[x]);
                     }
                 }
             }
@@ -234,11 +273,11 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
             const int m = tid, b = m >> lh, i = m & (h - 1);
             const bool valid = m < T * h;
             const int s1 = lw + XG_BITDEPTH + 6 - 15;
-            for (int c = 0; c < rnd16(kw); c += 8) {
-                int v[8];
-                xg_tc_row8(tmem, warp, c, v);
+            for (int c = 0; c < rnd16(kw); c += 16) {
+                int v[16];
+                xg_tc_row16(tmem, warp, c, v);
 #pragma unroll
-                for (int j = 0; j < 8; j++)
+                for (int j = 0; j < 16; j++)
                     if (valid && c + j < kw) xg_tc_put(ahi, alo, xg_tc_off(b * kw + c + j, i, kp), xg_clip16(xg_rshift_rnd(v[j], s1)));
             }
             if (!(ok = run_pass(1, kp, np))) break;
@@ -261,12 +300,13 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
             const int qadd = (jb.flags & 4) ? (1 << (qshift - 1)) : (((jb.flags & 8) ? 171 : 85) << (qshift - 9));
             const int iqadd = 1 << (iqshift - 1);
             unsigned long long nzb = 0;
-            for (int c = 0; c < rnd16(kh); c += 8) {
-                int v[8];
-                xg_tc_row8(tmem, warp, c, v);
+            for (int c = 0; c < rnd16(kh); c += 16) {
+                int v[16], rr[16];
+                xg_tc_row16(tmem, warp, c, v);
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
+                for (int j = 0; j < 16; j++) {
                     const int kv = c + j;
+                    rr[j] = 0;                /* beyond kh: the I1 operand's zero padding */
                     if (!valid || kv >= kh) continue;
                     const int tv = xg_clip16(xg_rshift_rnd(v[j], s2)), a = abs(tv);
                     int qv = (int)(((long long)a * qmult + qadd) >> qshift);
@@ -275,7 +315,11 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                     q[jb.off + kv * w + k] = (xg_coef)qv;
                     r[jb.off + kv * w + k] = (xg_coef)rv;
                     if (qv) nzb |= 1ull << ((kv >> 2) * (kw >> 2) + (k >> 2));
-                    if (k < jmax) xg_tc_put(ahi, alo, xg_tc_off(m, kv, kp), rv);
+                    rr[j] = rv;
+                }
+                if (valid && k < jmax) {      /* row m of the I1 operand, columns c .. c + 15 */
+                    xg_tc_put8(ahi, alo, xg_tc_off(m, c, kp), rr);
+                    xg_tc_put8(ahi, alo, xg_tc_off(m, c + 8, kp), rr + 8);
                 }
             }
             if (nzb) atomicOr(&snz[b], nzb);
@@ -299,11 +343,11 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
             const int lkw = lw > 5 ? 5 : lw;
             const int m = tid, b = m >> lkw, j = m & (kw - 1);
             const bool valid = m < T * kw && j < jmax;
-            for (int c = 0; c < rnd16(h); c += 8) {
-                int v[8];
-                xg_tc_row8(tmem, warp, c, v);
+            for (int c = 0; c < rnd16(h); c += 16) {
+                int v[16];
+                xg_tc_row16(tmem, warp, c, v);
 #pragma unroll
-                for (int jj = 0; jj < 8; jj++)
+                for (int jj = 0; jj < 16; jj++)
                     if (valid && c + jj < h) xg_tc_put(ahi, alo, xg_tc_off(b * h + c + jj, j, kp), xg_clip16(xg_rshift_rnd(v[jj], 7)));
             }
             if (!(ok = run_pass(3, kp, np))) break;
@@ -314,12 +358,20 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
             const bool valid = m < T * h;
             const int s2 = 6 + 15 - 1 - XG_BITDEPTH;
             const int off = valid ? sjob[b].off + y * w : 0;
-            for (int c = 0; c < rnd16(w); c += 8) {
-                int v[8];
-                xg_tc_row8(tmem, warp, c, v);
+            for (int c = 0; c < rnd16(w); c += 16) {
+                int v[16];
+                xg_tc_row16(tmem, warp, c, v);
+                if (valid && w >= 4) {        /* four samples per store (the row starts 16-byte aligned) */
 #pragma unroll
-                for (int x = 0; x < 8; x++)
-                    if (valid && c + x < w) rout[off + c + x] = (xg_coef)xg_clip16(xg_rshift_rnd(v[x], s2));
+                    for (int x = 0; x < 16; x += 4)
+                        if (c + x < w) {
+                            xg_coef o4[4];
+#pragma unroll
+                            for (int u = 0; u < 4; u++) o4[u] = (xg_coef)xg_clip16(xg_rshift_rnd(v[x + u], s2));
+                            if (sizeof(xg_coef) == 4) *(uint4 *)(rout + off + c + x) = *(const uint4 *)o4;
+                            else *(uint2 *)(rout + off + c + x) = *(const uint2 *)o4;
+                        }
+                }
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
