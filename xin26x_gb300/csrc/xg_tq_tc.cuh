@@ -14,9 +14,9 @@
  * the four passes in order, each as M = 128 rows x N x K MMAs (K-major
  * operands in shared memory, no swizzle) for the high and the low halves:
  *   F1  rows (b, i)  K = j  N = k  : t1 = clip16(rnd(sum, s1))            (Xin26xFDct*)
- *   F2  rows (b, k)  K = i  N = kv : coefficient, quant / dequant            (Xin266QuantInvQuant)
+ *   F2  rows (b, k)  K = i  N = kv : coefficient, quant / dequant  (A MN-major) (Xin266QuantInvQuant)
  *   I1  rows (b, j)  K = kv N = y  : t2 = clip16(rnd(sum, 7))              (Xin26xIDct*, columns)
- *   I2  rows (b, y)  K = j  N = x  : out = clip16(rnd(sum, 20 - bd))       (rows, skip-line rule)
+ *   I2  rows (b, y)  K = j  N = x  : out = clip16(rnd(sum, 20 - bd)) (A MN-major) (rows, skip-line rule)
  * The epilogue of a pass (tcgen05.ld, one row per thread) writes the next
  * pass's A operand in shared memory.  Transform-skip blocks stay on the CUDA
  * cores (xg_tq_batch.cuh).
@@ -54,6 +54,20 @@ __device__ __forceinline__ uint64_t xg_tc_desc(uint32_t saddr, int kp)
     return d;
 }
 
+/* byte offset of element (m, k) in an MN-major, no-swizzle A operand (128 rows):
+ * core matrices of 8 K-rows x 8 M-elements (16 bytes), M-direction stride 128 B
+ * (the descriptor's SBO), K-direction stride 2048 B (its LBO) */
+__device__ __forceinline__ int xg_tc_mn_off(int m, int k) { return (m >> 3) * 128 + (k >> 3) * 2048 + (k & 7) * 16 + (m & 7) * 2; }
+
+__device__ __forceinline__ uint64_t xg_tc_desc_mn(uint32_t saddr)
+{
+    uint64_t d = (uint64_t)((saddr & 0x3FFFF) >> 4);
+    d |= (uint64_t)(2048 >> 4) << 16;                      /* K-direction core-matrix stride */
+    d |= (uint64_t)(128 >> 4) << 32;                       /* M-direction core-matrix stride */
+    d |= (uint64_t)1 << 46;                                /* descriptor version */
+    return d;
+}
+
 /* store x (an int16 value) split into exact f16 halves */
 __device__ __forceinline__ void xg_tc_put(uint8_t *ahi, uint8_t *alo, int off, int x)
 {
@@ -61,14 +75,17 @@ __device__ __forceinline__ void xg_tc_put(uint8_t *ahi, uint8_t *alo, int off, i
     *(__half *)(alo + off) = __int2half_rn(x & 255);
 }
 
-/* D[hi|lo] (128 x np) = A[hi|lo] (128 x kp) . B (np x kp)^T, issued by one thread */
-__device__ __forceinline__ void xg_tc_mma(uint32_t tmem, uint32_t ahi, uint32_t alo, uint32_t b, int kp, int np, uint32_t mbar)
+/* D[hi|lo] (128 x np) = A[hi|lo] (128 x kp) . B (np x kp)^T, issued by one thread;
+ * A K-major, or MN-major when a_mn (instruction-descriptor bit 15) */
+__device__ __forceinline__ void xg_tc_mma(uint32_t tmem, uint32_t ahi, uint32_t alo, uint32_t b, int kp, int np, uint32_t mbar,
+                                          bool a_mn)
 {
-    const uint32_t idesc = (1u << 4) | ((uint32_t)(np >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+    const uint32_t idesc = (1u << 4) | (a_mn ? 1u << 15 : 0u) | ((uint32_t)(np >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
     for (int h = 0; h < 2; h++) {
         const uint32_t a = h ? alo : ahi;
         for (int kk = 0; kk < kp / 16; kk++) {
-            const uint64_t ad = xg_tc_desc(a + kk * 256, kp), bd = xg_tc_desc(b + kk * 256, kp);
+            const uint64_t ad = a_mn ? xg_tc_desc_mn(a + kk * 4096) : xg_tc_desc(a + kk * 256, kp);
+            const uint64_t bd = xg_tc_desc(b + kk * 256, kp);
             const uint32_t en = kk > 0;
             asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                          "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
@@ -136,6 +153,21 @@ __device__ __forceinline__ void xg_tc_put8(uint8_t *ahi, uint8_t *alo, int off, 
     *(uint4 *)(alo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
 }
 
+/* four int16 values as f16 halves, 8 bytes each */
+__device__ __forceinline__ void xg_tc_put4(uint8_t *ahi, uint8_t *alo, int off, const int x[4])
+{
+    uint32_t hw[2], lw[2];
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+        const __half2 hh = __halves2half2(__int2half_rn(x[2 * p] >> 8), __int2half_rn(x[2 * p + 1] >> 8));
+        const __half2 ll = __halves2half2(__int2half_rn(x[2 * p] & 255), __int2half_rn(x[2 * p + 1] & 255));
+        hw[p] = *(const uint32_t *)&hh;
+        lw[p] = *(const uint32_t *)&ll;
+    }
+    *(uint2 *)(ahi + off) = make_uint2(hw[0], hw[1]);
+    *(uint2 *)(alo + off) = make_uint2(lw[0], lw[1]);
+}
+
 __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, int ntiles, const XgTqJob *jobs,
                                                         const uint32_t *list, const xg_coef *res, xg_coef *q, xg_coef *r,
                                                         xg_coef *rout, unsigned long long *nzout, int *err)
@@ -167,12 +199,12 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
     bool ok = true;
 
     /* one pass: operands written -> MMA with B number bi -> wait; false (for the whole CTA) on a timeout */
-    auto run_pass = [&](int bi, int kp, int np) -> bool {
+    auto run_pass = [&](int bi, int kp, int np, bool a_mn) -> bool {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (tid == 0) xg_tc_mma(tmem, s_ahi, s_alo, s_b + bi * XG_TC_B_BYTES, kp, np, s_mbar);
+        if (tid == 0) xg_tc_mma(tmem, s_ahi, s_alo, s_b + bi * XG_TC_B_BYTES, kp, np, s_mbar, a_mn);
         const bool done = xg_tc_wait(s_mbar, phase);
         phase ^= 1;
         const bool all = !__syncthreads_or(!done);
@@ -263,9 +295,10 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                     }
                 }
             }
-            if (!(ok = run_pass(0, kp, np))) break;
+            if (!(ok = run_pass(0, kp, np, false))) break;
         }
-        /* ---- F1 epilogue -> F2 operand A[(b, k)][i] = t1 (the MMA is done: A and B are free) */
+        /* ---- F1 epilogue -> F2 operand A[(b, k)][i] = t1, MN-major: a thread's values for
+         * consecutive k are consecutive rows (the MMA is done: A and B are free) */
         {
             const int kp = rnd16(h), np = rnd16(kh);
             zero_a(kp);
@@ -277,10 +310,17 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                 int v[16];
                 xg_tc_row16(tmem, warp, c, v);
 #pragma unroll
-                for (int j = 0; j < 16; j++)
-                    if (valid && c + j < kw) xg_tc_put(ahi, alo, xg_tc_off(b * kw + c + j, i, kp), xg_clip16(xg_rshift_rnd(v[j], s1)));
+                for (int j = 0; j < 16; j++) v[j] = xg_clip16(xg_rshift_rnd(v[j], s1));
+                if (valid) {
+                    if (kw >= 8) {
+                        xg_tc_put8(ahi, alo, xg_tc_mn_off(b * kw + c, i), v);
+                        if (c + 8 < kw) xg_tc_put8(ahi, alo, xg_tc_mn_off(b * kw + c + 8, i), v + 8);
+                    } else {
+                        xg_tc_put4(ahi, alo, xg_tc_mn_off(b * kw, i), v);
+                    }
+                }
             }
-            if (!(ok = run_pass(1, kp, np))) break;
+            if (!(ok = run_pass(1, kp, np, true))) break;
         }
         /* ---- F2 epilogue: quant / dequant, q and r out; -> I1 operand A[(b, j)][kv] = r (the same rows) */
         {
@@ -323,7 +363,7 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                 }
             }
             if (nzb) atomicOr(&snz[b], nzb);
-            if (!(ok = run_pass(2, kp, np))) break;
+            if (!(ok = run_pass(2, kp, np, false))) break;
         }
         /* zeros of q / r beyond the kept 32 x 32 (64-wide or -high blocks), and the maps */
         if (w > 32 || h > 32)
@@ -335,7 +375,7 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                 }
             }
         if (tid < T) nzout[list[tl.first + tid]] = snz[tid];
-        /* ---- I1 epilogue -> I2 operand A[(b, y)][j] = t2 */
+        /* ---- I1 epilogue -> I2 operand A[(b, y)][j] = t2, MN-major (consecutive y, consecutive rows) */
         {
             const int kp = rnd16(jmax), np = rnd16(w);
             zero_a(kp);
@@ -347,10 +387,17 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                 int v[16];
                 xg_tc_row16(tmem, warp, c, v);
 #pragma unroll
-                for (int jj = 0; jj < 16; jj++)
-                    if (valid && c + jj < h) xg_tc_put(ahi, alo, xg_tc_off(b * h + c + jj, j, kp), xg_clip16(xg_rshift_rnd(v[jj], 7)));
+                for (int jj = 0; jj < 16; jj++) v[jj] = xg_clip16(xg_rshift_rnd(v[jj], 7));
+                if (valid) {
+                    if (h >= 8) {
+                        xg_tc_put8(ahi, alo, xg_tc_mn_off(b * h + c, j), v);
+                        if (c + 8 < h) xg_tc_put8(ahi, alo, xg_tc_mn_off(b * h + c + 8, j), v + 8);
+                    } else {
+                        xg_tc_put4(ahi, alo, xg_tc_mn_off(b * h, j), v);
+                    }
+                }
             }
-            if (!(ok = run_pass(3, kp, np))) break;
+            if (!(ok = run_pass(3, kp, np, true))) break;
         }
         /* ---- I2 epilogue: the reconstructed residual */
         {
