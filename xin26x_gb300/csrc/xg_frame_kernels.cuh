@@ -463,18 +463,23 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
             }
 #pragma unroll
             for (int c = 0; c < 5; c++) {
-                uint32_t k = 0xFFFFFFFFu;
+                uint32_t kd[XG_ME_D];
 #pragma unroll
                 for (int d = 0; d < XG_ME_D; d++) {
                     const uint32_t sad = c < 4 ? acc[d][c] : acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
-                    uint32_t kd = (sad << (XG_COST_FRACTION + XG_ME_DB)) + md[d];
+                    kd[d] = (sad << (XG_COST_FRACTION + XG_ME_DB)) + md[d];
                     if (!interior) {
                         const int dy = dyl + d;
                         if (!(dx >= swin[warp][c][0] && dx <= swin[warp][c][1] && dy >= swin[warp][c][2] && dy <= swin[warp][c][3]))
-                            kd = 0xFFFFFFFFu;
+                            kd[d] = 0xFFFFFFFFu;
                     }
-                    k = min(k, kd);
                 }
+                /* the minimum of the keys with three-input minima */
+#if XG_ME_D == 8
+                const uint32_t k = min(__vimin3_u32(kd[0], kd[1], kd[2]), __vimin3_u32(__vimin3_u32(kd[3], kd[4], kd[5]), kd[6], kd[7]));
+#else
+                const uint32_t k = min(__vimin3_u32(kd[0], kd[1], kd[2]), kd[3]);
+#endif
                 const uint32_t cost = k >> XG_ME_DB, gidx = gidx0 + (k & (XG_ME_D - 1)) * (uint32_t)nx;
                 if (live[c] && k < XG_ME_KEY_INVALID && (cost < best[c] || (cost == best[c] && gidx < bidx[c]))) { best[c] = cost; bidx[c] = gidx; }
             }
