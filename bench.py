@@ -191,6 +191,24 @@ def run_reference(args):
     return 0
 
 
+# ---------------------------------------------------------------- replicas
+def max_over_ranks(x, dist=None, device="cpu"):
+    """The largest x over all ranks (the slowest replica's time); x itself without
+    a process group."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, seconds):
+    """Replicas only: every rank processes units_per_rank, the job takes the
+    slowest rank's seconds; the rate counts the units of all ranks."""
+    return units_per_rank * world / seconds
+
+
 # ---------------------------------------------------------------- GPU legs
 def run_gpu(args):
     import torch  # device memory for the resident pictures and the L2 flush buffer
@@ -256,12 +274,8 @@ def run_gpu(args):
     torch.cuda.synchronize()
     launches = lib.xin_gpu_kernel_launches() - launches0
     clk = clocks.stop()
-    total_ms = float(np.sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = npix * args.steps * world / (total_ms * 1e-3) / 1e6
+    total_ms = max_over_ranks(float(np.sum(step_ms)), dist, "cuda")
+    value = whole_job_rate(npix * args.steps, world, total_ms * 1e-3) / 1e6
     stage /= args.steps
 
     # roofline of the integer search kernel
@@ -300,7 +314,8 @@ def run_gpu(args):
     e2e_s = time.perf_counter() - t0
     e2e_fs.wait(copy=False)
     e2e_fs.close()
-    e2e_val = npix * args.steps * world / e2e_s / 1e6
+    e2e_s = max_over_ranks(e2e_s, dist, "cuda")
+    e2e_val = whole_job_rate(npix * args.steps, world, e2e_s) / 1e6
 
     # plain per-call form on a sample of CUs (one synchronous launch per reference call)
     percall = percall_sample(lib, frames)
