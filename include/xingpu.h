@@ -251,6 +251,59 @@ int  xin_gpu_tq_plan_tiles(const xin_gpu_tq_plan *plan, int32_t *tiles);
 int  xin_gpu_tq_plan_status(xin_gpu_tq_plan *plan);
 void xin_gpu_tq_plan_destroy(xin_gpu_tq_plan *plan);
 
+/* ---------------------------------------------------- dependent quantisation
+ * The trellis quantiser Xin266DepQuant (h266_encoder/source/h266_dep_quant.c:1789,
+ * table entry pfXinDepQuant, h266_encoder/include/h266_func_struct.h:664-676,795)
+ * on batches of transform blocks.  Rates come from CABAC context states in the
+ * reference's layout: a context set is the array xin_prob_model[XIN_NUM_OF_CTX]
+ * of the encoder's cabac context (h266_encoder/include/h266_cabac_struct.h:225-235),
+ * 6-byte records.  Block b reads t at offset (row stride `stride`) and writes
+ * q (signed levels) and r (dequantised) at the same places over the whole
+ * w x h block (zeros beyond the low 32 x 32), nz[b] = map of non-zero 4x4
+ * groups (raster order of the low 32 x 32 region).  Bit-exact with the
+ * reference's C for every block size 4..64, QP 0..51 and component. */
+typedef struct xin_gpu_prob { uint16_t state[2]; uint8_t rate; } xin_gpu_prob;    /* xin_prob_model */
+#define XIN_GPU_NUM_CTX 401                                                        /* XIN_NUM_OF_CTX */
+typedef struct xin_gpu_dq_block {
+    uint32_t offset;            /* element offset of the block's top-left coefficient in t, q and r */
+    uint16_t stride;            /* elements between rows (>= w) */
+    uint8_t  log2_w, log2_h;    /* 2..6 */
+    uint8_t  qp;                /* 0..51: the QP the reference passes (10-bit: slice QP + 12, h266_trans_quant.c:104) */
+    uint8_t  comp;              /* 0 luma, 1 Cb, 2 Cr */
+    uint8_t  root_cbf;          /* luma of an inter CU coded as one TU: the cbf rate is the root cbf's */
+    uint8_t  reserved;
+    uint32_t ctx_set;           /* index of the block's context set */
+} xin_gpu_dq_block;
+/* host arrays: t, q, r hold ncoeffs samples, ctx_sets nsets x XIN_GPU_NUM_CTX records */
+int  xin_gpu_dep_quant_batch(const xin_gpu_dq_block *blocks, int32_t nblocks, const XG_COEFF *t, XG_COEFF *q, XG_COEFF *r,
+                             uint64_t *nz, size_t ncoeffs, const xin_gpu_prob *ctx_sets, int32_t nsets);
+/* device arrays (blocks stay a host array); synchronises */
+int  xin_gpu_dep_quant_batch_device(const xin_gpu_dq_block *blocks, int32_t nblocks, const XG_COEFF *t, XG_COEFF *q,
+                                    XG_COEFF *r, uint64_t *nz, size_t ncoeffs, const xin_gpu_prob *ctx_sets,
+                                    int32_t nsets, void *stream);
+/* a plan keeps a validated block list on the device; run only enqueues on
+ * `stream` (device arrays, device context sets) */
+typedef struct xin_gpu_dq_plan xin_gpu_dq_plan;
+int  xin_gpu_dq_plan_create(const xin_gpu_dq_block *blocks, int32_t nblocks, size_t ncoeffs, int32_t nsets,
+                            xin_gpu_dq_plan **plan);
+int  xin_gpu_dq_plan_run(xin_gpu_dq_plan *plan, const XG_COEFF *t, XG_COEFF *q, XG_COEFF *r, uint64_t *nz,
+                         const xin_gpu_prob *ctx_sets, void *stream);
+void xin_gpu_dq_plan_destroy(xin_gpu_dq_plan *plan);
+/* Per-call form with the XinDepQuant signature.  It reads three fields of the
+ * reference's structures: xin_dep_quant.context, xin_fast_md_buf.type and
+ * .fullBuf, xin_full_md_buf.tuNum (h266_encoder/include/h266_dep_quant_struct.h:135,
+ * h266_md_buffer_struct.h:65,71,109); tu is not read (standard scans).  A Cr
+ * block's rates are built from the current contexts (the reference reuses the
+ * tables of its previous call, the Cb block of the same TU, h266_dep_quant.c:296). */
+#define XIN_GPU_DQ_CONTEXT_OFFSET      8
+#define XIN_GPU_FASTBUF_FULLBUF_OFFSET 0
+#define XIN_GPU_FASTBUF_TYPE_OFFSET    880
+#define XIN_GPU_FULLBUF_TUNUM_OFFSET   2184
+#define XIN_GPU_INTRA_MODE             3      /* XIN_INTRA_MODE */
+void XinGpuDepQuant(void *depQuant, void *fastBuf, void *tu, XG_COEFF *tCoeff, XG_COEFF *rCoeff, XG_COEFF *qCoeff,
+                    intptr_t coeffStride, uint32_t qp, int32_t width, int32_t height, uint64_t *nzCGBitMapRs,
+                    uint32_t compId);
+
 /* ------------------------------------------------------- motion search (a7-a8)
  * xin_me_struct is the reference's ME state (h26x_core/include/h26x_me_struct.h:60-131);
  * xingpu_me.h mirrors its layout.  Pass a pointer to the reference's struct.

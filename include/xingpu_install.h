@@ -111,7 +111,7 @@ typedef struct xin_gpu_func_struct {
 #define XIN_GPU_INSTALL_DIST      1u   /* SAD / SATD / Var families, Hadamard 8x8 */
 #define XIN_GPU_INSTALL_INTERP    2u   /* luma / chroma interpolation, bi average, BCW blend */
 #define XIN_GPU_INSTALL_TRANSFORM 4u   /* 1-D / 2-D transforms, skip, residual, reconstruction */
-#define XIN_GPU_INSTALL_QUANT     8u   /* quant / dequant, pre-RDOQ */
+#define XIN_GPU_INSTALL_QUANT     8u   /* quant / dequant, pre-RDOQ, dependent quantisation */
 #define XIN_GPU_INSTALL_ALL       15u
 
 /* funcSet: the reference's xin_func_struct *, meFunc: its xin_me_func *

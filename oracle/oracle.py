@@ -51,6 +51,19 @@ class orc_frame_desc(C.Structure):
                 ("search_range", i32), ("sad_lambda", u32), ("qp", i32), ("uv_qp", i32), ("intra_frame", i32)]
 
 
+class orc_dq_param(C.Structure):
+    _fields_ = [("qShift", i32), ("qAdd", i32), ("qScale", i32), ("maxQIdx", i32), ("thresLast", i32),
+                ("iqShift", i32), ("iqScale", i32), ("distShift", i32), ("distAdd", i32),
+                ("distStepAdd", C.c_int64), ("distOrgFact", C.c_int64)]
+
+
+class xin_dp_param(C.Structure):
+    """the reference's xin_dp_param (h266_encoder/include/h266_seq_struct.h:118-134)"""
+    _fields_ = [("qShift", i32), ("qAdd", i32), ("qScale", i32), ("maxQIdx", i32), ("thresLast", i32),
+                ("thresSSbb", i32), ("iqAdd", i32), ("iqShift", i32), ("iqScale", i32), ("distShift", i32),
+                ("distAdd", i32), ("distStepAdd", C.c_int64), ("distOrgFact", C.c_int64)]
+
+
 class orc_cu_out(C.Structure):
     _fields_ = [("mvx", i32), ("mvy", i32), ("cost", u32), ("int_cost", u32), ("nz", u64 * 3), ("ssd", u64 * 3)]
 
@@ -121,10 +134,17 @@ _SIGS = {
     "cu_hotpath": ("orc_cu_hotpath", None, [C.POINTER(orc_frame_desc), i32, i32, i32, vp * 3, ip * 2, vp * 3, ip * 2,
                                             C.POINTER(orc_cu_out)]),
     "tr_matrix": ("orc_tr_matrix", None, [C.c_int, C.c_int]),
+    "dep_quant": ("orc_dep_quant", "ref_dep_quant", [vp, ip, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int,
+                                                     vp, vp, vp]),
+    "dq_params": ("orc_dq_params", None, [C.c_int, C.c_int, C.POINTER(orc_dq_param)]),
+    "dq_frac_bits": ("orc_dq_frac_bits", None, [C.c_int, vp]),
+    "dq_rice_bits": ("orc_dq_rice_bits", None, [C.c_int, C.c_int]),
+    "dq_last_group": ("orc_dq_last_group", None, [C.c_int]),
 }
 _REF_ONLY = {
     "idct2_wxh_tmp": ("Xin266IDct2WxH", [vp, ip, vp, ip, u32, u32, vp, i32, i32]),
     "full_subpel_me_io": ("ref_full_subpel_me", [vp, ip, vp, ip, u32, u32, i32, i32, u32, i32, i32, i32, i32, vp]),
+    "dq_param_ref": ("ref_dq_param", [C.c_int, C.c_int, C.POINTER(xin_dp_param)]),
     "transform_tu_ref": ("ref_transform_tu", [vp, ip, vp, ip, vp, vp, vp, ip, u32, u32, u32, u32, i32, i32, u32, i32, i32,
                                               i32, vp, vp]),
 }
@@ -149,6 +169,8 @@ class _Lib:
         if which == 0:
             self.mvd_bits.restype = u32
             self.tr_matrix.restype = C.POINTER(C.c_int16)
+            self.dq_rice_bits.restype = i32
+            self.dq_last_group.restype = C.c_int
         else:
             for name, (sym, args) in _REF_ONLY.items():
                 f = getattr(self.lib, sym)

@@ -163,3 +163,62 @@ void ref_transform_tu(PIXEL *in, intptr_t is, PIXEL *pred, intptr_t ps, COEFF *t
     *nz = full.nzCGMapRs[mts][0][plane];
     free(hs);
 }
+
+/* ---- dependent quantisation --------------------------------------------
+ * Xin266DepQuant (h266_encoder/source/h266_dep_quant.c:1789) on tables built
+ * by the reference's own Xin266ContructScanOrder (h266_scan_order.c:83),
+ * Xin266CreateDepQuantRom (h266_dep_quant.c:494) and Xin266CreateDepQuant
+ * (:323).  For a Cr block the Cb rate tables are built first from the same
+ * contexts: the reference reuses the tables of the previous call for Cr
+ * (:296-311), and in the encoder that call is the Cb block of the same TU. */
+#include "h266_dep_quant_struct.h"
+#include "h266_dep_quant.h"
+SINT32 Xin266ContructScanOrder(xin_seq_struct *seqSet);
+void Xin266PreDepQuant(COEFF *, COEFF *, COEFF *, intptr_t, UINT32, UINT32, UINT32, UINT32, SINT32,
+                       xin_scan_pos *, xin_scan_pos *, SINT32 *);
+
+static xin_seq_struct *dq_seq;
+static xin_sec_struct *dq_sec;
+static xin_func_struct dq_fs;
+
+static void dq_setup(void)
+{
+    if (dq_seq) return;
+    dq_seq = (xin_seq_struct *)calloc(1, sizeof(xin_seq_struct));
+    dq_sec = (xin_sec_struct *)calloc(1, sizeof(xin_sec_struct));
+    dq_seq->config.enableDepQuant = 1;
+    dq_seq->funcSet = &dq_fs;
+    dq_fs.pfXinPreDepQuant = Xin266PreDepQuant;
+    Xin266ContructScanOrder(dq_seq);
+    Xin266CreateDepQuantRom(dq_seq);
+    dq_sec->seqSet = dq_seq;
+    Xin266CreateDepQuant(dq_sec);
+}
+
+void ref_dep_quant(COEFF *t, intptr_t stride, int w, int h, int qp, int comp,
+                   xin_prob_model *ctx, int root_cbf, COEFF *q, COEFF *r, UINT64 *nz)
+{
+    static xin_full_md_buf full;
+    static xin_fast_md_buf fast;
+    xin_tu_struct tu;
+    UINT32 lw = calcLog2[w], lh = calcLog2[h], ct = comp != 0;
+    dq_setup();
+    xin_dep_quant *dq = dq_sec->depQuant;
+    memset(&tu, 0, sizeof tu);
+    dq->context = ctx;
+    full.tuNum = 1;
+    fast.fullBuf = &full;
+    fast.type = root_cbf ? 0 : XIN_INTRA_MODE;
+    tu.scanOrderCG[ct] = dq_seq->scanOrderCG[lh][lw];
+    tu.scanOrder[ct] = dq_seq->scanOrder[2][2];
+    if (comp == 2)
+        Xin266InitContext(dq, &fast, dq->tuParam[lw][lh][1], ctx, PLANE_CHROMA_U);
+    Xin266DepQuant(dq, &fast, &tu, t, r, q, stride, (UINT32)qp, w, h, nz, (UINT32)comp);
+}
+
+/* the reference's trellis parameters for lg(w)+lg(h) = lgsum, QP qp (xin_dp_param) */
+void ref_dq_param(int qp, int lgsum, xin_dp_param *out)
+{
+    dq_setup();
+    *out = dq_seq->dpParam[lgsum][qp];
+}

@@ -170,6 +170,28 @@ typedef struct orc_cu_out {
 void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size,
                     ocoef *q[3], intptr_t q_stride[2], opix *rec[3], intptr_t rec_stride[2], orc_cu_out *out);
 
+/* ---- dependent quantisation (oracle_dq.c; pinned (open C)) -------------- */
+/* context-state record, the reference's xin_prob_model
+ * (h266_encoder/include/h266_cabac_struct.h:225-229): 6 bytes */
+typedef struct orc_prob { uint16_t state[2]; uint8_t rate; } orc_prob;
+#define ORC_NUM_CTX 401                    /* XIN_NUM_OF_CTX */
+/* trellis quantiser parameters, the fields of xin_dp_param
+ * (h266_encoder/include/h266_seq_struct.h:118-134) that it uses */
+typedef struct orc_dq_param {
+    int32_t qShift, qAdd, qScale, maxQIdx, thresLast, iqShift, iqScale, distShift, distAdd;
+    int64_t distStepAdd, distOrgFact;
+} orc_dq_param;
+void    orc_dq_frac_bits(int s, uint32_t out[2]);
+int     orc_dq_last_group(int pos);
+int32_t orc_dq_rice_bits(int k, int n);
+void    orc_dq_params(int qp, int lgsum, orc_dq_param *p);
+/* Xin266DepQuant (h266_encoder/source/h266_dep_quant.c:1789): t, q, r share
+ * the stride; q and r are written over min(w,32) x min(h,32).  root_cbf: the
+ * block is the luma of an inter CU with one TU (the last-position rate then
+ * carries the root cbf flag). */
+void orc_dep_quant(const ocoef *t, intptr_t stride, int w, int h, int qp, int comp,
+                   const orc_prob *ctx, int root_cbf, ocoef *q, ocoef *r, uint64_t *nz);
+
 #ifdef __cplusplus
 }
 #endif

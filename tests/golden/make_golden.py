@@ -6,7 +6,7 @@ place, oracle/Makefile target ``ref``) and records seeded inputs with that
 library's outputs.  tests/test_oracle_golden.py replays the inputs through
 the oracle anywhere (no reference tree needed) and requires identical output.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [core|dq]
 """
 import os
 import sys
@@ -105,6 +105,51 @@ def make(bd):
     print("wrote", os.path.join(OUT, f"ref_golden_{bd}bit.npz"))
 
 
+def make_dq(bd):
+    """Dependent quantisation: seeded blocks of every size 4..64 and component,
+    QP 0..51, root cbf on and off, with strided layouts, through the reference's
+    Xin266DepQuant; plus the reference's rate / Rice / group-index tables and
+    trellis parameters that the oracle derives from formulas."""
+    import ctypes as C
+    from xin26x_gb300 import synth as S
+    O.build(ref=True)
+    r = O.reference(bd)
+    rng = np.random.default_rng(4100 + bd)
+    sets = S.contexts(rng, 8)
+    sizes = [(w, h) for w in (4, 8, 16, 32, 64) for h in (4, 8, 16, 32, 64)]
+    meta, tin, qout, rout, nzs = [], [], [], [], []
+    for i in range(8 * len(sizes)):
+        w, h = sizes[i % len(sizes)]
+        stride = w + int(rng.choice([0, 0, 4, 12]))
+        qp, comp, root, cs = int(rng.integers(0, 52)), int(rng.integers(0, 3)), int(rng.integers(0, 2)), int(rng.integers(0, 8))
+        t = np.zeros((h, stride), r.coef)
+        t[:, :w] = S.coefficients(rng, w, h, bd)
+        q = np.zeros((h, stride), r.coef); rr = np.zeros((h, stride), r.coef); nz = np.zeros(1, np.uint64)
+        ctx = np.ascontiguousarray(sets[cs])
+        r.dep_quant(O.ptr(t), stride, w, h, qp, comp, ctx.ctypes.data, root, O.ptr(q), O.ptr(rr), nz.ctypes.data)
+        meta.append([w, h, stride, qp, comp, root, cs])
+        tin.append(t.ravel()); qout.append(q.ravel()); rout.append(rr.ravel()); nzs.append(nz[0])
+    g = {"meta": np.array(meta, np.int32), "t": np.concatenate(tin), "q": np.concatenate(qout),
+         "r": np.concatenate(rout), "nz": np.array(nzs, np.uint64), "sets": sets}
+    g["frac_bits"] = np.ctypeslib.as_array((C.c_uint32 * 512).in_dll(r.lib, "cabacbinFracBits")).copy()
+    g["rice_bits"] = np.ctypeslib.as_array((C.c_int32 * 128).in_dll(r.lib, "goRiceBits")).copy()
+    g["rice_par"] = np.ctypeslib.as_array((C.c_uint32 * 32).in_dll(r.lib, "auiGoRiceParsCoeff")).copy()
+    g["last_group"] = np.ctypeslib.as_array((C.c_uint32 * 64).in_dll(r.lib, "lastSigXYGroupIdx")).copy()
+    par = []
+    for lg in range(4, 13):
+        for qp in range(52):
+            d = O.xin_dp_param()
+            r.dq_param_ref(qp, lg, C.byref(d))
+            par.append([getattr(d, f) for f, _ in O.orc_dq_param._fields_])
+    g["dq_param"] = np.array(par, np.int64)
+    np.savez_compressed(os.path.join(OUT, f"ref_dq_{bd}bit.npz"), **g)
+    print("wrote", os.path.join(OUT, f"ref_dq_{bd}bit.npz"))
+
+
 if __name__ == "__main__":
+    what = sys.argv[1:] or ["all"]
     for bd in (8, 10):
-        make(bd)
+        if "all" in what or "core" in what:
+            make(bd)
+        if "all" in what or "dq" in what:
+            make_dq(bd)

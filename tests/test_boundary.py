@@ -78,7 +78,7 @@ _FUNC_MEMBERS = ["pfXinComputeSad", "pfXinComputeSatd", "pfXinComputeDist", "pfX
                  "pfXinChromaInterp", "pfXinLumaInterpS16", "pfXinChromaInterpS16", "pfXinInterpAvg", "pfXinInterpWeight",
                  "pfXinQuantInvQuant", "pfXinFor2dDct2", "pfXinFor2dSkip", "pfXinInv2dSkip", "pfXinFor1dDct",
                  "pfXinInv2dDct2", "pfXinInv1dDct", "pfXinBlockSubForDct", "pfXinBlockAddForDct", "pfXinComputeHada8x8",
-                 "pfXinPreRdoq", "pfXinFilterIntraNB"]
+                 "pfXinPreRdoq", "pfXinPreDepQuant", "pfXinDepQuant", "pfXinFilterIntraNB"]
 
 
 def _func_probe(struct, headers):
@@ -127,6 +127,57 @@ def test_installer_fills_tables_without_gpu(bd):
     assert fs[offs["pfXinFor1dDct"] // 8 + 1 * 8 + 6] is None                             # no 64-point DCT8
     assert fs[offs["pfXinQuantInvQuant"] // 8 + 5] == addr("XinGpuQuantInvQuant")
     assert fs[offs["pfXinPreRdoq"] // 8] == addr("XinGpuPreRdoq")
+    assert fs[offs["pfXinDepQuant"] // 8] == addr("XinGpuDepQuant")
     assert fs[offs["pfXinFilterIntraNB"] // 8] is None                                    # off the hot path
     assert me.funcSet[0] == addr("XinGpuComputeSad")
     assert lib.xin_gpu_install(None, None, 15) == -2
+
+
+_REF_HDRS = ["xin_typedef.h", "basic_macro.h", "h26x_definition.h", "h266_definition.h", "h266_constant.h",
+             "xin_video_common.h", "h266_picture_struct.h", "h266_intra_pred_context.h", "h266_pred_unit_struct.h",
+             "h266_seq_struct.h", "h266_trans_unit_struct.h", "h26x_me_struct.h", "h266_cabac_struct.h",
+             "h266_md_buffer_struct.h", "h266_coding_unit_struct.h", "h266_alf_struct.h", "h266_section_struct.h",
+             "h266_dep_quant_struct.h"]
+_CTX = ["XIN_CO_QT_ROOT_CBF", "XIN_CO_QT_CBF_Y", "XIN_CO_QT_CBF_U", "XIN_CO_QT_CBF_V", "XIN_CO_SIG_COEFF_GROUP_LUMA",
+        "XIN_CO_SIG_COEFF_GROUP_CHROMA", "XIN_CO_SIG_FLAG_LUMA", "XIN_CO_SIG_FLAG_CHROMA", "XIN_CO_PAR_FLAG_LUMA",
+        "XIN_CO_PAR_FLAG_CHROMA", "XIN_CO_GT2_FLAG_LUMA", "XIN_CO_GT1_FLAG_LUMA", "XIN_CO_LAST_X_LUMA",
+        "XIN_CO_LAST_X_CHROMA", "XIN_CO_LAST_Y_LUMA", "XIN_CO_LAST_Y_CHROMA"]
+_MINE = ["ROOT_CBF", "CBF_Y", "CBF_U", "CBF_V", "SIGGRP_L", "SIGGRP_C", "SIG_L", "SIG_C", "PAR_L", "PAR_C", "GT2_L",
+         "GT1_L", "LASTX_L", "LASTX_C", "LASTY_L", "LASTY_C"]
+
+
+@pytest.mark.parametrize("tenbit", (False, True))
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "h266_encoder")), reason="reference tree absent")
+def test_dep_quant_boundary_matches_reference(tenbit):
+    """The three structure fields XinGpuDepQuant reads, the context layout and
+    the context indices of the library and the oracle equal the reference's."""
+    import re
+    incs = [os.path.join(REF, p) for p in ("common/include", "video_api/video_common/include", "video_api/video_encoder/include",
+                                           "h26x_core/include", "h266_core/include", "h266_encoder/include")]
+    inc = "".join(f'#include "{h}"\n' for h in _REF_HDRS)
+    pre = "#define ENABLE_10BIT_ENCODER\n" if tenbit else ""
+    body = ('printf("ctx %zu\\n", offsetof(xin_dep_quant, context));'
+            'printf("full %zu\\n", offsetof(xin_fast_md_buf, fullBuf));'
+            'printf("type %zu\\n", offsetof(xin_fast_md_buf, type));'
+            'printf("tunum %zu\\n", offsetof(xin_full_md_buf, tuNum));'
+            'printf("intra %d\\n", (int)XIN_INTRA_MODE);'
+            'printf("nctx %d\\n", (int)XIN_NUM_OF_CTX);'
+            'printf("prob %zu\\n", sizeof(xin_prob_model));'
+            + "".join(f'printf("{m} %d\\n", (int){c});' for m, c in zip(_MINE, _CTX)))
+    src = f"{pre}#include <stdio.h>\n#include <stddef.h>\n{inc}int main(void){{{body}return 0;}}\n"
+    ref = _offsets_c(src, incs)
+    hdr = open(os.path.join(ROOT, "include", "xingpu.h")).read()
+    d = {k: int(v) for k, v in re.findall(r"#define (XIN_GPU_\w+)\s+(\d+)", hdr)}
+    assert ref["ctx"] == d["XIN_GPU_DQ_CONTEXT_OFFSET"] and ref["full"] == d["XIN_GPU_FASTBUF_FULLBUF_OFFSET"]
+    assert ref["type"] == d["XIN_GPU_FASTBUF_TYPE_OFFSET"] and ref["tunum"] == d["XIN_GPU_FULLBUF_TUNUM_OFFSET"]
+    assert ref["intra"] == d["XIN_GPU_INTRA_MODE"] and ref["nctx"] == d["XIN_GPU_NUM_CTX"] == _lib.NUM_CTX
+    assert ref["prob"] == C.sizeof(_lib.xin_gpu_prob)
+    for name in ("csrc/xg_dq.cuh",):
+        txt = open(os.path.join(ROOT, "xin26x_gb300", name)).read()
+        mine = {k: int(v) for k, v in re.findall(r"XG_DQC_(\w+) = (\d+)", txt)}
+        for m in _MINE:
+            assert mine[m] == ref[m], m
+    txt = open(os.path.join(ROOT, "oracle", "oracle_dq.c")).read()
+    mine = {k: int(v) for k, v in re.findall(r"DQC_(\w+) = (\d+)", txt)}
+    for m in _MINE:
+        assert mine[m] == ref[m], m

@@ -57,3 +57,38 @@ def test_golden(bd):
         o.full_subpel_me(O.ptr(inp), 16, O.ptr(refp, pad * refp.shape[1] + pad), refp.shape[1], 16, 16, 1, -1, 57,
                          -10, -10, 10, 10, io)
         assert (io.best_mvx, io.best_mvy, io.best_cost) == (ox, oy, oc)
+
+
+@pytest.mark.parametrize("bd", (8, 10))
+def test_golden_dep_quant(bd):
+    """Dependent quantisation: the reference's own outputs and tables (made by
+    make_golden.py dq from h266_dep_quant.c compiled in place) against the oracle."""
+    import ctypes as C
+    g = np.load(os.path.join(GOLD, f"ref_dq_{bd}bit.npz"))
+    o = O.oracle(bd)
+    out = (C.c_uint32 * 2)()
+    for s in range(256):
+        o.dq_frac_bits(s, C.addressof(out))
+        assert (out[0], out[1]) == tuple(g["frac_bits"][2 * s:2 * s + 2]), s
+    assert [o.dq_rice_bits(k, n) for k in range(4) for n in range(32)] == list(g["rice_bits"])
+    assert [o.dq_last_group(p) for p in range(64)] == list(g["last_group"])
+    i = 0
+    for lg in range(4, 13):
+        for qp in range(52):
+            p = O.orc_dq_param()
+            o.dq_params(qp, lg, C.byref(p))
+            assert [getattr(p, f) for f, _ in O.orc_dq_param._fields_] == list(g["dq_param"][i]), (lg, qp)
+            i += 1
+    sets = g["sets"]
+    off = 0
+    for (w, h, stride, qp, comp, root, cs), nz_ref in zip(g["meta"], g["nz"]):
+        n = int(h * stride)
+        t = g["t"][off:off + n].reshape(h, stride).astype(o.coef)
+        q = np.zeros((h, stride), o.coef); r = np.zeros((h, stride), o.coef); nz = np.zeros(1, np.uint64)
+        ctx = np.ascontiguousarray(sets[cs])
+        o.dep_quant(O.ptr(t), int(stride), int(w), int(h), int(qp), int(comp), ctx.ctypes.data, int(root),
+                    O.ptr(q), O.ptr(r), nz.ctypes.data)
+        assert np.array_equal(q.ravel(), g["q"][off:off + n]), (w, h, qp, comp, root)
+        assert np.array_equal(r.ravel(), g["r"][off:off + n]), (w, h, qp, comp, root)
+        assert nz[0] == nz_ref
+        off += n

@@ -275,3 +275,55 @@ def test_full_subpel_me(bd):
             r.full_subpel_me_io(O.ptr(inp), size, ref_at_pu, refp.shape[1], size, size, 3, -2, lam, mnx, mny, mxx, mxy,
                                 O.ptr(rio))
             assert (io.best_mvx, io.best_mvy, io.best_cost) == (int(rio[0]), int(rio[1]), int(np.uint32(rio[2].view(np.uint32)))), (size, trial)
+
+
+@pytest.mark.parametrize("bd", BDS)
+def test_dep_quant_vs_reference(bd):
+    """Xin266DepQuant (h266_dep_quant.c:1789) compiled in place against the
+    oracle restatement: every block size 4..64, QP 0..51, Y / Cb / Cr, root cbf
+    on and off, strided layouts, coefficient magnitudes from near zero to
+    saturated, and all-below-threshold blocks."""
+    from xin26x_gb300 import synth as S
+    o, r = _pair(bd)
+    rng = np.random.default_rng(77 + bd)
+    sizes = [(w, h) for w in (4, 8, 16, 32, 64) for h in (4, 8, 16, 32, 64)]
+    for i in range(60 * len(sizes)):
+        w, h = sizes[i % len(sizes)]
+        stride = w + int(rng.choice([0, 0, 4, 20]))
+        qp, comp, root = int(rng.integers(0, 52)), int(rng.integers(0, 3)), int(rng.integers(0, 2))
+        ctx = S.contexts(rng)[0]
+        t = np.zeros((h, stride), o.coef)
+        t[:, :w] = S.coefficients(rng, w, h, bd, scale=0.3 if i % 23 == 0 else None)
+        if i % 37 == 0:
+            t[:, :w] = np.where(rng.random((h, w)) < 0.5, 32767, -32768)
+        outs = []
+        for lib in (o, r):
+            q = np.full((h, stride), 5, o.coef); rr = np.full((h, stride), 5, o.coef); nz = np.zeros(1, np.uint64)
+            lib.dep_quant(O.ptr(t), stride, w, h, qp, comp, ctx.ctypes.data, root, O.ptr(q), O.ptr(rr), nz.ctypes.data)
+            outs.append((q, rr, nz[0]))
+        assert np.array_equal(outs[0][0], outs[1][0]), (i, w, h, qp, comp, root)
+        assert np.array_equal(outs[0][1], outs[1][1]), (i, w, h, qp, comp, root)
+        assert outs[0][2] == outs[1][2], (i, w, h, qp, comp, root)
+
+
+@pytest.mark.parametrize("bd", BDS)
+def test_dep_quant_tables_vs_reference(bd):
+    """The rate, Rice and group-index tables and the trellis parameters that the
+    oracle (and the library) derive from formulas equal the reference's."""
+    import ctypes as C
+    o, r = _pair(bd)
+    ref_frac = np.ctypeslib.as_array((C.c_uint32 * 512).in_dll(r.lib, "cabacbinFracBits"))
+    out = (C.c_uint32 * 2)()
+    for s in range(256):
+        o.dq_frac_bits(s, C.addressof(out))
+        assert (out[0], out[1]) == (ref_frac[2 * s], ref_frac[2 * s + 1])
+    ref_rice = np.ctypeslib.as_array((C.c_int32 * 128).in_dll(r.lib, "goRiceBits"))
+    assert [o.dq_rice_bits(k, n) for k in range(4) for n in range(32)] == list(ref_rice)
+    ref_grp = np.ctypeslib.as_array((C.c_uint32 * 64).in_dll(r.lib, "lastSigXYGroupIdx"))
+    assert [o.dq_last_group(p) for p in range(64)] == list(ref_grp)
+    for lg in range(4, 13):
+        for qp in range(52):
+            a, b = O.orc_dq_param(), O.xin_dp_param()
+            o.dq_params(qp, lg, C.byref(a))
+            r.dq_param_ref(qp, lg, C.byref(b))
+            assert all(getattr(a, f) == getattr(b, f) for f, _ in a._fields_), (lg, qp)

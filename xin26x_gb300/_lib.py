@@ -39,6 +39,18 @@ class xin_gpu_tq_block(C.Structure):
                 ("qp", i32)]
 
 
+class xin_gpu_dq_block(C.Structure):
+    _fields_ = [("offset", u32), ("stride", C.c_uint16), ("log2_w", C.c_uint8), ("log2_h", C.c_uint8), ("qp", C.c_uint8),
+                ("comp", C.c_uint8), ("root_cbf", C.c_uint8), ("reserved", C.c_uint8), ("ctx_set", u32)]
+
+
+NUM_CTX = 401     # context records per set (xin_gpu_prob, 6 bytes each)
+
+
+class xin_gpu_prob(C.Structure):
+    _fields_ = [("state", C.c_uint16 * 2), ("rate", C.c_uint8)]
+
+
 class xin_gpu_server_cfg(C.Structure):
     _fields_ = [("hbm_budget", C.c_uint64), ("mpix_budget", C.c_double), ("max_inflight", u32), ("max_streams", u32),
                 ("max_queue", u32), ("reserved", u32)]
@@ -141,6 +153,12 @@ SIGNATURES = {
     "xin_gpu_tq_plan_tiles": ([vp, vp], C.c_int),
     "xin_gpu_tq_plan_status": ([vp], C.c_int),
     "xin_gpu_tq_plan_destroy": ([vp], None),
+    "xin_gpu_dep_quant_batch": ([vp, i32, vp, vp, vp, vp, C.c_size_t, vp, i32], C.c_int),
+    "xin_gpu_dep_quant_batch_device": ([vp, i32, vp, vp, vp, vp, C.c_size_t, vp, i32, vp], C.c_int),
+    "xin_gpu_dq_plan_create": ([vp, i32, C.c_size_t, i32, C.POINTER(vp)], C.c_int),
+    "xin_gpu_dq_plan_run": ([vp, vp, vp, vp, vp, vp, vp], C.c_int),
+    "xin_gpu_dq_plan_destroy": ([vp], None),
+    "XinGpuDepQuant": ([vp, vp, vp, vp, vp, vp, C.c_ssize_t, u32, i32, i32, vp, u32], None),
 }
 for _n in ["InterpCopy", "InterpCopyU8S16", "LumaInterpHor", "LumaInterpVet", "LumaInterpHorVet", "LumaInterpHorU8S16",
            "LumaInterpVetU8S16", "LumaInterpHorVetU8S16", "LumaInterpVetS16U8", "LumaInterpVetS16S16",

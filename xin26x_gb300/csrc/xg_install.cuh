@@ -77,7 +77,10 @@ extern "C" int xin_gpu_install(void *funcSet, void *meFunc, uint32_t what)
             if (what & XIN_GPU_INSTALL_QUANT) fs->pfXinQuantInvQuant[lg] = XG_FN(XinGpuQuantInvQuant);
         }
         if (what & XIN_GPU_INSTALL_DIST) fs->pfXinComputeHada8x8 = XG_FN(XinGpuComputeHada8x8);
-        if (what & XIN_GPU_INSTALL_QUANT) fs->pfXinPreRdoq = XG_FN(XinGpuPreRdoq);
+        if (what & XIN_GPU_INSTALL_QUANT) {
+            fs->pfXinPreRdoq = XG_FN(XinGpuPreRdoq);
+            fs->pfXinDepQuant = XG_FN(XinGpuDepQuant);
+        }
     }
     if (mf && (what & XIN_GPU_INSTALL_DIST)) {
         for (int lg = 0; lg < 8; lg++) {

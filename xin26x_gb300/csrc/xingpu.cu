@@ -15,3 +15,4 @@
 #include "xg_install.cuh"
 #include "xg_tq_batch.cuh"
 #include "xg_noalloc.cuh"
+#include "xg_dq.cuh"

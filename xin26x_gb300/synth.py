@@ -108,3 +108,71 @@ def tq_blocks(n: int, seed: int, bitdepth: int = 10, kernel_bench_mix: bool = Tr
     scale = 12 if kernel_bench_mix else 60
     resid = np.clip(np.rint(rng.laplace(0, scale, size=int(area.sum()))), -lim, lim)
     return b, resid.astype(np.int16 if bitdepth == 8 else np.int32)
+
+
+DQ_BLOCK_DTYPE = np.dtype([("offset", "<u4"), ("stride", "<u2"), ("log2_w", "u1"), ("log2_h", "u1"), ("qp", "u1"),
+                           ("comp", "u1"), ("root_cbf", "u1"), ("reserved", "u1"), ("ctx_set", "<u4")])   # xin_gpu_dq_block
+PROB_DTYPE = np.dtype([("s0", "<u2"), ("s1", "<u2"), ("rate", "u1"), ("pad", "u1")])   # xin_gpu_prob (xin_prob_model)
+NUM_CTX = 401
+
+
+def contexts(rng, n_sets: int = 1) -> np.ndarray:
+    """Seeded CABAC context states in the reference layout: n_sets x NUM_CTX records
+    (10-bit and 14-bit probability windows, as the encoder keeps them)."""
+    a = np.zeros((n_sets, NUM_CTX), PROB_DTYPE)
+    a["s0"] = rng.integers(0, 1024, size=a.shape) << 5
+    a["s1"] = rng.integers(0, 16384, size=a.shape) << 1
+    a["rate"] = rng.integers(0, 256, size=a.shape)
+    return a
+
+
+def coefficients(rng, w: int, h: int, bitdepth: int, scale: float = None) -> np.ndarray:
+    """Seeded transform coefficients shaped like a residual spectrum: Laplacian
+    magnitudes decaying away from DC, random zero runs and sparse large values."""
+    coef = np.int16 if bitdepth == 8 else np.int32
+    if scale is None:
+        scale = float(rng.choice([2.0, 8.0, 40.0, 200.0, 1500.0]))
+    y, x = np.mgrid[0:h, 0:w]
+    decay = np.exp(-(x + y) / max(1.0, rng.uniform(1.0, 12.0)))
+    v = rng.laplace(0, scale, size=(h, w)) * (0.15 + decay)
+    v[rng.random((h, w)) < rng.uniform(0.0, 0.6)] = 0
+    big = rng.random((h, w)) < 0.01
+    v[big] = rng.choice([-1, 1], size=big.sum()) * rng.uniform(2000, 30000, size=big.sum())
+    return np.clip(np.rint(v), -32768, 32767).astype(coef)
+
+
+def dq_blocks(n: int, seed: int, bitdepth: int = 10, n_sets: int = 1, qp_range=None, any_mix: bool = False):
+    """Seeded blocks for xin_gpu_dep_quant_batch: (blocks, coefficients, context sets).
+
+    Shapes as tq_blocks (sides 4..64, P(4, 8, 16, 32, 64) = (.12, .34, .30, .16, .08)
+    per axis), blocks packed one after another (stride = width), components
+    luma 2/3 and Cb / Cr 1/6 each, root cbf on half of the luma blocks.  QP: the
+    QP the reference's TU driver passes to the trellis, slice QP U[22, 39]
+    (+12 at 10-bit), or qp_range.  any_mix: coefficient magnitudes spread from
+    near-zero to large (the parity mix); otherwise the spectrum of an
+    11-bit Laplacian residual (scale 12) after a DCT2 of the block's size."""
+    rng = np.random.default_rng(seed)
+    p = np.array([0.12, 0.34, 0.30, 0.16, 0.08])
+    lw = rng.choice(5, size=n, p=p) + 2
+    lh = rng.choice(5, size=n, p=p) + 2
+    b = np.zeros(n, DQ_BLOCK_DTYPE)
+    area = (1 << (lw + lh)).astype(np.int64)
+    off = np.concatenate(([0], np.cumsum(area)[:-1]))
+    lo, hi = qp_range if qp_range else (22 + (12 if bitdepth == 10 else 0), 39 + (12 if bitdepth == 10 else 0))
+    comp = rng.choice(3, size=n, p=[2 / 3, 1 / 6, 1 / 6])
+    b["offset"], b["stride"], b["log2_w"], b["log2_h"] = off, 1 << lw, lw, lh
+    b["qp"] = rng.integers(lo, hi + 1, size=n)
+    b["comp"] = comp
+    b["root_cbf"] = (comp == 0) & (rng.random(n) < 0.5)
+    b["ctx_set"] = rng.integers(0, n_sets, size=n)
+    coef = np.zeros(int(area.sum()), np.int16 if bitdepth == 8 else np.int32)
+    for i in range(n):
+        w, h = 1 << int(lw[i]), 1 << int(lh[i])
+        if any_mix:
+            c = coefficients(rng, w, h, bitdepth)
+        else:
+            # DCT2 of a Laplacian(12) residual keeps its energy: the coefficient
+            # std grows with sqrt(w*h) at the transform's output scaling
+            c = coefficients(rng, w, h, bitdepth, scale=12.0 * np.sqrt(w * h) / 8.0)
+        coef[off[i]:off[i] + w * h] = c.ravel()
+    return b, coef, contexts(rng, n_sets)
