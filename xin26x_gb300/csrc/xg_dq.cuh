@@ -269,23 +269,84 @@ __device__ __forceinline__ long long xg_dq_shfl64(unsigned m, long long v, int s
     return (long long)(((unsigned long long)(unsigned)hi << 32) | (unsigned)lo);
 }
 
-/* One CTA = 4 warps x 8 quads; each warp takes 8 blocks at a time from *counter.
- * full: write q and r over the whole w x h block (zeros beyond 32), else over
- * min(w,32) x min(h,32) only (the reference's extent). */
+/* ---- pass 1: per block (one warp each) gather the low 32x32 in scan order into
+ * tscan, find the last position (Xin266PreDepQuant, h266_dep_quant.c:1683-1770),
+ * zero q and r, and count the block into its length bucket: 0 = nothing above
+ * the threshold (q, r, nz are final), b = 1 + last position / 16 otherwise. */
+__global__ void __launch_bounds__(256)
+k_dq_prep(const xin_gpu_dq_block *__restrict__ jobs, int njobs, const uint32_t *__restrict__ soff,
+          const xg_coef *__restrict__ tin, xg_coef *__restrict__ tscan, xg_coef *__restrict__ qout,
+          xg_coef *__restrict__ rout, unsigned long long *__restrict__ nzout, const uint2 *__restrict__ step_tab, const XgDqParam *__restrict__ par_tab, int32_t *__restrict__ first_out,
+          int *__restrict__ counts, int full)
+{
+    const int lane = threadIdx.x & 31;
+    const int nw = gridDim.x * (blockDim.x >> 5);
+    for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < njobs; i += nw) {
+        const xin_gpu_dq_block jb = jobs[i];
+        const int lgw = jb.log2_w, lgh = jb.log2_h, ew = min(1 << lgw, 32), eh = min(1 << lgh, 32), n = ew * eh;
+        const uint2 *ST = step_tab + c_dq_shape_off[(min(lgw, 5) - 2) * 4 + (min(lgh, 5) - 2)];
+        const XgDqParam *P = par_tab + (lgw + lgh - 4) * 52 + jb.qp;
+        const int thr = P->thresLast / (P->qScale << 2);
+        const xg_coef *T = tin + jb.offset;
+        xg_coef *TS = tscan + soff[i];
+        int best = -1;
+        for (int k = lane; k < n; k += 32) {
+            const uint32_t e = __ldg(&ST[k].x);
+            const xg_coef v = T[((e >> 5) & 31) * jb.stride + (e & 31)];
+            TS[k] = v;
+            if ((v < 0 ? -v : v) > thr) best = k;
+        }
+        best = __reduce_max_sync(0xffffffffu, best);
+        const int zlw = full ? lgw : min(lgw, 5), zh = full ? 1 << lgh : eh;
+        xg_coef *QO = qout + jb.offset, *RO = rout + jb.offset;
+        for (int e = lane; e < (zh << zlw); e += 32) {
+            const int y = e >> zlw, x = e & ((1 << zlw) - 1);
+            QO[y * jb.stride + x] = 0;
+            RO[y * jb.stride + x] = 0;
+        }
+        if (lane == 0) {
+            first_out[i] = best;
+            atomicAdd(&counts[best < 0 ? 0 : (best >> 4) + 1], 1);
+            if (best < 0) nzout[i] = 0;
+        }
+    }
+}
+
+/* ---- pass 2: order the blocks longest first (bucket 65 .. 1), then the empty ones */
+__global__ void k_dq_order(int njobs, const int32_t *__restrict__ first, const int *__restrict__ counts,
+                           int *__restrict__ cursor, int32_t *__restrict__ order)
+{
+    __shared__ int off[66];
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int b = 65; b >= 1; b--) { off[b] = acc; acc += counts[b]; }
+        off[0] = acc;
+    }
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < njobs; i += gridDim.x * blockDim.x) {
+        const int b = first[i] < 0 ? 0 : (first[i] >> 4) + 1;
+        order[off[b] + atomicAdd(&cursor[b], 1)] = i;
+    }
+}
+
+/* ---- pass 3: the trellis.  One CTA = 4 warps x 8 quads; each warp takes the
+ * next 8 blocks of the ordered list (so its quads walk the same number of
+ * sub-blocks). */
 __global__ void __launch_bounds__(XG_DQ_THREADS)
-k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ counter,
-     const xg_coef *__restrict__ tin, xg_coef *__restrict__ qout, xg_coef *__restrict__ rout,
+k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ counter, const int *__restrict__ counts,
+     const int32_t *__restrict__ order, const int32_t *__restrict__ firsts, const uint32_t *__restrict__ soff,
+     const xg_coef *__restrict__ tscan, xg_coef *__restrict__ qout, xg_coef *__restrict__ rout,
      unsigned long long *__restrict__ nzout, const xin_gpu_prob *__restrict__ sets,
      const XgDqRates *__restrict__ rates, const uint2 *__restrict__ step_tab, const uint4 *__restrict__ tpl_tab,
-     const XgDqParam *__restrict__ par_tab, uint32_t *__restrict__ scratch, const int32_t *__restrict__ perm, int full)
+     const XgDqParam *__restrict__ par_tab, uint32_t *__restrict__ scratch)
 {
     extern __shared__ __align__(16) unsigned char xg_dq_raw[];
     XgDqSmem &sm = *reinterpret_cast<XgDqSmem *>(xg_dq_raw);
     const int lane = threadIdx.x & 31, qd = lane >> 2, s = lane & 3;
     const unsigned qmask = 0xFu << (qd * 4);
     XgDqQuad &Q = sm.quad[threadIdx.x >> 2];
-    uint32_t *scr = scratch + (size_t)(blockIdx.x * XG_DQ_QUADS + (threadIdx.x >> 2)) * XG_DQ_SCR_WORDS;
-    uint16_t *scr_q = reinterpret_cast<uint16_t *>(scr + XG_DQ_MAXN);
+    uint32_t *codes = scratch + (size_t)(blockIdx.x * XG_DQ_QUADS + (threadIdx.x >> 2)) * XG_DQ_MAXN;
+    const int ntr = njobs - counts[0];
 
     for (int i = threadIdx.x; i < 128; i += blockDim.x) {
         int k = i >> 5, n = i & 31, p = n >> k;
@@ -300,16 +361,15 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
         int base = 0;
         if (lane == 0) base = atomicAdd(counter, 8);
         base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= njobs) break;
-        const int job = base + qd;
-        const bool has = job < njobs;
+        if (base >= ntr) break;
+        const bool has = base + qd < ntr;
+        const int job = has ? order[base + qd] : 0;
 
         /* ---- block set-up (every lane of the quad holds the same values) ---- */
-        xin_gpu_dq_block jb;
-        if (has) jb = jobs[job];
-        else { jb.offset = 0; jb.stride = 4; jb.log2_w = 2; jb.log2_h = 2; jb.qp = 0; jb.comp = 0; jb.root_cbf = 0; jb.ctx_set = 0; }
+        const xin_gpu_dq_block jb = jobs[job];
+        const int first = has ? firsts[job] : -1;
         const int lgw = jb.log2_w, lgh = jb.log2_h, w = 1 << lgw, h = 1 << lgh;
-        const int ew = min(w, 32), eh = min(h, 32), n = ew * eh, ws = ew >> 2, hs = eh >> 2;
+        const int ew = min(w, 32), eh = min(h, 32), ws = ew >> 2, hs = eh >> 2;
         const int shape = (min(lgw, 5) - 2) * 4 + (min(lgh, 5) - 2);
         const uint2 *ST = step_tab + c_dq_shape_off[shape];
         const uint4 *TT = tpl_tab + c_dq_shape_off[shape];
@@ -318,55 +378,38 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
         const XgDqRates *RT = rates + jb.ctx_set * 2 + (luma ? 0 : 1);
         const xin_gpu_prob *CX = sets + (size_t)jb.ctx_set * XIN_GPU_NUM_CTX;
         const int stride = jb.stride;
-        const xg_coef *T = tin + jb.offset;
+        const xg_coef *TS = tscan + soff[job];
         xg_coef *QO = qout + jb.offset, *RO = rout + jb.offset;
 
-        /* zero the outputs, then the highest scan index with |t| above the
-         * last-position threshold (Xin266PreDepQuant, h266_dep_quant.c:1683-1770) */
-        int first = -1;
-        if (has) {
-            const int zw = full ? w : ew, zh = full ? h : eh;
-            for (int i = s; i < zw * zh; i += 4) {
-                int y = i >> (full ? lgw : min(lgw, 5)), x = i & (zw - 1);
-                QO[y * stride + x] = 0;
-                RO[y * stride + x] = 0;
+        /* last-position rates (Xin266SetLastCoeffOffset, h266_dep_quant.c:208-283): lane 0 x, lane 1 y */
+        if (has && s < 2) {
+            const int xy = s, size = xy ? h : w, lg = xy ? lgh : lgw, nn = min(size, 32);
+            const int shift = luma ? (lg + 1) >> 2 : min((1 << lg) >> 3, 2);
+            const int cbase = luma ? (lg == 2 ? 0 : lg == 3 ? 3 : lg == 4 ? 6 : lg == 5 ? 10 : 15) + (xy ? XG_DQC_LASTY_L : XG_DQC_LASTX_L)
+                                   : (xy ? XG_DQC_LASTY_C : XG_DQC_LASTX_C);
+            uint32_t off = 0;
+            if (xy) {
+                int cc = (luma && jb.root_cbf) ? XG_DQC_ROOT_CBF : jb.comp == 0 ? XG_DQC_CBF_Y : jb.comp == 1 ? XG_DQC_CBF_U : XG_DQC_CBF_V;
+                const uint32_t *cb = xg_dq_bits(CX, cc);
+                off = cb[1] - cb[0];
             }
-            const int thr = P.thresLast / (P.qScale << 2);
-            for (int top = n - 1; top >= 0; top -= 4) {
-                int k = top - s, hit = 0;
-                if (k >= 0) {
-                    uint32_t e = __ldg(&ST[k].x);
-                    int v = T[((e >> 5) & 31) * stride + (e & 31)];
-                    hit = (v < 0 ? -v : v) > thr;
+            const int gmax = nn - 1 < 4 ? nn - 1 : 2 * (31 - __clz(nn - 1)) + (((nn - 1) >> (30 - __clz(nn - 1))) & 1);
+            uint32_t acc = 0, cbits = 0;
+            int gdone = 0;
+            /* groups in increasing order; positions map to non-decreasing groups, so one pass fills the table */
+            for (int p = 0; p < nn; p++) {
+                const int g = p < 4 ? p : 2 * (31 - __clz(p)) + ((p >> (30 - __clz(p))) & 1);
+                while (gdone <= g) {
+                    const uint32_t suf = gdone > 3 ? (uint32_t)(((gdone - 2) >> 1) << 15) : 0;
+                    if (gdone == gmax) cbits = acc + suf + off;
+                    else {
+                        const uint32_t *b = xg_dq_bits(CX, cbase + (gdone >> shift));
+                        cbits = acc + b[0] + suf + off;
+                        acc += b[1];
+                    }
+                    gdone++;
                 }
-                unsigned b = (__ballot_sync(qmask, hit) >> (qd * 4)) & 15u;
-                if (b) { first = top - (__ffs(b) - 1); break; }
-            }
-            /* last-position rates (Xin266SetLastCoeffOffset, h266_dep_quant.c:208-283): lane 0 x, lane 1 y */
-            if (s < 2) {
-                const int xy = s, size = xy ? h : w, lg = xy ? lgh : lgw, nn = min(size, 32);
-                const int shift = luma ? (lg + 1) >> 2 : min((1 << lg) >> 3, 2);
-                const int cbase = luma ? (lg == 2 ? 0 : lg == 3 ? 3 : lg == 4 ? 6 : lg == 5 ? 10 : 15) + (xy ? XG_DQC_LASTY_L : XG_DQC_LASTX_L)
-                                       : (xy ? XG_DQC_LASTY_C : XG_DQC_LASTX_C);
-                uint32_t off = 0;
-                if (xy) {
-                    int cc = (luma && jb.root_cbf) ? XG_DQC_ROOT_CBF : jb.comp == 0 ? XG_DQC_CBF_Y : jb.comp == 1 ? XG_DQC_CBF_U : XG_DQC_CBF_V;
-                    const uint32_t *cb = xg_dq_bits(CX, cc);
-                    off = cb[1] - cb[0];
-                }
-                const int gmax = nn - 1 < 4 ? nn - 1 : 2 * (31 - __clz(nn - 1)) + (((nn - 1) >> (30 - __clz(nn - 1))) & 1);
-                uint32_t acc = 0, cb_[12];
-                for (int g = 0; g <= gmax; g++) {
-                    uint32_t suf = g > 3 ? (uint32_t)(((g - 2) >> 1) << 15) : 0;
-                    if (g == gmax) { cb_[g] = acc + suf + off; break; }
-                    const uint32_t *b = xg_dq_bits(CX, cbase + (g >> shift));
-                    cb_[g] = acc + b[0] + suf + off;
-                    acc += b[1];
-                }
-                for (int p = 0; p < nn; p++) {
-                    int g = p < 4 ? p : 2 * (31 - __clz(p)) + ((p >> (30 - __clz(p))) & 1);
-                    Q.last[xy][p] = (int32_t)cb_[g];
-                }
+                Q.last[xy][p] = (int32_t)cbits;
             }
         }
         __syncwarp(0xffffffffu);
@@ -386,15 +429,41 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
         const uint32_t *sigset = &RT->sig[s > 1 ? s - 1 : 0][0][0];
         const int src1 = s == 1 ? 2 : s == 2 ? 1 : s;      /* round 1 reads candidate A/Z */
         const int src2 = src1 ^ 1;                         /* round 2 reads candidate B */
+        /* coefficients of the current / next sub-block: lane s holds scan positions 4s..4s+3 */
+        xg_coef c0 = 0, c1 = 0, c2 = 0, c3 = 0, n0 = 0, n1 = 0, n2 = 0, n3 = 0;
+        uint4 ea = make_uint4(0, 0, 0, 0), eb = make_uint4(0, 0, 0, 0);
+        auto load_sb = [&](int sb, xg_coef &a0, xg_coef &a1, xg_coef &a2, xg_coef &a3) {
+            const xg_coef *src = TS + sb * 16 + 4 * s;
+#if XG_BITDEPTH == 8
+            const uint2 raw = *reinterpret_cast<const uint2 *>(src);
+            a0 = (xg_coef)(raw.x & 0xFFFF); a1 = (xg_coef)(raw.x >> 16); a2 = (xg_coef)(raw.y & 0xFFFF); a3 = (xg_coef)(raw.y >> 16);
+#else
+            const int4 raw = *reinterpret_cast<const int4 *>(src);
+            a0 = raw.x; a1 = raw.y; a2 = raw.z; a3 = raw.w;
+#endif
+        };
 
         for (int stp = 0; stp < nsteps; stp++) {
             const int k = top - stp;
             if (k < 0 || k > first) continue;                      /* uniform within the quad */
-            const int in = k & 15;
-            const uint2 se = __ldg(&ST[k]);
-            const int px = se.x & 31, py = (se.x >> 5) & 31, ptype = (se.x >> 10) & 3, nin = (se.x >> 12) & 7;
-            int av = T[py * stride + px];
+            const int in = k & 15, sb = k >> 4;
+            if (k == first || in == 15) {
+                if (k == first) load_sb(sb, c0, c1, c2, c3);
+                else { c0 = n0; c1 = n1; c2 = n2; c3 = n3; }
+                if (sb > 0) load_sb(sb - 1, n0, n1, n2, n3);
+                const uint4 *e4 = reinterpret_cast<const uint4 *>(ST + sb * 16 + 4 * s);
+                ea = __ldg(e4); eb = __ldg(e4 + 1);
+            }
+            const int sub = in & 3, srcl = in >> 2;
+            const xg_coef mine = sub == 0 ? c0 : sub == 1 ? c1 : sub == 2 ? c2 : c3;
+            const uint32_t mex = sub == 0 ? ea.x : sub == 1 ? ea.z : sub == 2 ? eb.x : eb.z;
+            const uint32_t mey = sub == 0 ? ea.y : sub == 1 ? ea.w : sub == 2 ? eb.y : eb.w;
+            int av = __shfl_sync(qmask, (int)mine, srcl, 4);
+            uint2 se;
+            se.x = __shfl_sync(qmask, mex, srcl, 4);
+            se.y = __shfl_sync(qmask, mey, srcl, 4);
             av = av < 0 ? -av : av;
+            const int px = se.x & 31, py = (se.x >> 5) & 31, ptype = (se.x >> 10) & 3, nin = (se.x >> 12) & 7;
 
             /* context of this state at position k */
             uint32_t tv = ref >= 0 ? Q.tpl[ref][in] : 0u;
@@ -465,16 +534,16 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
             const long long r1 = xg_dq_shfl64(qmask, caz, src1), r2 = xg_dq_shfl64(qmask, cb, src2);
             const int sels = __shfl_sync(qmask, saz | iB << 4, src1, 4);
             const int sels2 = __shfl_sync(qmask, saz | iB << 4, src2, 4);
-            long long c1, c2;
+            long long cc1, cc2;
             int s1, s2, f1, f2;
-            if (s < 2) { c1 = r1; s1 = sels & 15; f1 = src1; c2 = r2; s2 = sels2 >> 4; f2 = src2; }
-            else       { c1 = r2; s1 = sels2 >> 4; f1 = src2; c2 = r1; s2 = sels & 15; f2 = src1; }
+            if (s < 2) { cc1 = r1; s1 = sels & 15; f1 = src1; cc2 = r2; s2 = sels2 >> 4; f2 = src2; }
+            else       { cc1 = r2; s1 = sels2 >> 4; f1 = src2; cc2 = r1; s2 = sels & 15; f2 = src1; }
 
             /* decision for target state s */
             long long dc = XG_DQ_INF >> 1;
             int dsel = 7, dfrom = -2;
-            if (c1 < dc) { dc = c1; dsel = s1; dfrom = f1; }
-            if (c2 < dc) { dc = c2; dsel = s2; dfrom = f2; }
+            if (cc1 < dc) { dc = cc1; dsel = s1; dfrom = f1; }
+            if (cc2 < dc) { dc = cc2; dsel = s2; dfrom = f2; }
             if (ptype == 2) {
                 long long c = skcost + __ldg(&RT->sbb[sksignb][0]);
                 if (c < dc) { dc = c; dsel = 4; dfrom = 4 + s; }
@@ -489,7 +558,7 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
             uint32_t code = (uint32_t)((dfrom + 2) | dsel << 4) << (8 * s);
             code |= __shfl_xor_sync(qmask, code, 1, 4);
             code |= __shfl_xor_sync(qmask, code, 2, 4);
-            if (s == 0) { scr[k] = code; scr_q[k] = (uint16_t)q; }
+            if (s == 0) codes[k] = code;
 
             if (ptype == 1) { skcost = cost; skrem = rem; skref = ref; sksignb = signb; }
 
@@ -525,8 +594,8 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
                     par16 = (par16 & ~(1u << in)) | (uint32_t)(lv & 1) << in;
                 }
             } else {
-                /* first coefficient (in scan order) of sub-block b: close it and open b - 1 */
-                const int b = k >> 4, slot = b & 15;
+                /* first coefficient (in scan order) of sub-block sb: close it and open sb - 1 */
+                const int slot = sb & 15;
                 int srcref = -1;
                 if (dfrom >= 4) {
                     nsig = 0; rem = (int)(int16_t)(pspk & 0xFFFF); srcref = (int)((pspk >> 16) & 7) - 1;
@@ -557,7 +626,7 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
                 nfl = (nfl & ~(1ull << braster)) | (unsigned long long)(nsig != 0) << braster;
                 nvr = (nvr & ~(3u << (2 * slot))) | (uint32_t)s << (2 * slot);
                 if (upd) *reinterpret_cast<uint4 *>(&Q.ring[slot][s][0]) = make_uint4(l0, l1, l2, l3);
-                /* neighbours of sub-block b - 1 */
+                /* neighbours of sub-block sb - 1 */
                 const uint32_t nx = __ldg(&ST[k - 1].x);
                 const int r1 = (nx >> 15) & 63, x1 = r1 % ws, y1 = r1 / ws;
                 const int right = x1 < ws - 1 ? r1 + 1 : 0, below = y1 < hs - 1 ? r1 + ws : 0;
@@ -576,7 +645,7 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
                             for (int u = 0; u < 5; u++) {
                                 if (u < no) {
                                     const uint32_t nb = nbs[u];
-                                    const int sb = nb & 63, inner = (nb >> 6) & 15, rs = (nb >> 10) & 63, sl = sb & 15;
+                                    const int sbn = nb & 63, inner = (nb >> 6) & 15, rs = (nb >> 10) & 63, sl = sbn & 15;
                                     int v = 0;
                                     if ((nfl >> rs) & 1) {
                                         const int ver = (nvr >> (2 * sl)) & 3;
@@ -595,50 +664,63 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
                 __syncwarp(qmask);
             }
         }
+        __syncwarp(qmask);
 
-        /* ---- best final state, walk back, dequantise (h266_dep_quant.c:1919-1989) ---- */
+        /* ---- best final state, then walk the decisions from position 0 up
+         * (h266_dep_quant.c:1919-1947).  The state a coefficient was quantised
+         * in is the source state of its decision (0 for the last position), so
+         * each level is dequantised as it is found (:1949-1989 walks the same
+         * state machine forward from the last position). */
         const long long f0 = xg_dq_shfl64(qmask, cost, 0), f1v = xg_dq_shfl64(qmask, cost, 1);
         const long long f2v = xg_dq_shfl64(qmask, cost, 2), f3v = xg_dq_shfl64(qmask, cost, 3);
-        if (has && s == 0) {
+        if (has) {
             unsigned long long map = 0;
-            if (first >= 0) {
-                long long best = 0;
-                int st = -1;
-                if (f0 < best) { best = f0; st = 0; }
-                if (f1v < best) { best = f1v; st = 1; }
-                if (f2v < best) { best = f2v; st = 2; }
-                if (f3v < best) { best = f3v; st = 3; }
-                int k = 0;
-                while (st >= 0 && k <= first) {
-                    int lv = 0;
-                    if (!(st >= 4 && (k & 15))) {
-                        const uint32_t code = (scr[k] >> (8 * (st & 3))) & 255u;
-                        const int sel = (int)(code >> 4), qk = scr_q[k];
-                        lv = sel == 4 ? 0 : (qk + ((sel - qk) & 3) + 1) >> 1;
-                        st = (int)(code & 15) - 2;
+            long long best = 0;
+            int st = -1;
+            if (f0 < best) { best = f0; st = 0; }
+            if (f1v < best) { best = f1v; st = 1; }
+            if (f2v < best) { best = f2v; st = 2; }
+            if (f3v < best) { best = f3v; st = 3; }
+            const int iqadd = 1 << (P.iqShift - 1);
+            uint32_t ncode = codes[s];
+            int nval = TS[s];
+            uint32_t nent = __ldg(&ST[s].x);
+            for (int k0 = 0; st >= 0 && k0 <= first; k0 += 4) {
+                const uint32_t mcode = ncode, ment = nent;
+                const int mval = nval;
+                if (k0 + 4 + s <= first) { ncode = codes[k0 + 4 + s]; nval = TS[k0 + 4 + s]; nent = __ldg(&ST[k0 + 4 + s].x); }
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const uint32_t c = __shfl_sync(qmask, mcode, j, 4);
+                    const int v = __shfl_sync(qmask, mval, j, 4);
+                    const int k = k0 + j;
+                    if (st >= 0 && k <= first) {
+                        int lv = 0, ps = 0;
+                        if (!(st >= 4 && (k & 15))) {
+                            const uint32_t byte = (c >> (8 * (st & 3))) & 255u;
+                            const int sel = (int)(byte >> 4), from = (int)(byte & 15) - 2;
+                            const int av = v < 0 ? -v : v;
+                            const long long qi = ((long long)av * P.qScale + P.qAdd) >> P.qShift;
+                            const int q = (int)(qi < 1 ? 1 : qi > P.maxQIdx ? P.maxQIdx : qi);
+                            lv = sel >= 4 ? 0 : (q + ((sel - q) & 3) + 1) >> 1;
+                            ps = from >= 0 && from < 4 ? from : 0;
+                            st = from;
+                        }
+                        if (lv && s == j) {
+                            const int x = ment & 31, y = (ment >> 5) & 31;
+                            const int qv = v < 0 ? -lv : lv;
+                            const int qidx = 2 * qv + (qv > 0 ? -(ps >> 1) : (ps >> 1));
+                            const int rv = (qidx * P.iqScale + iqadd) >> P.iqShift;
+                            QO[y * stride + x] = (xg_coef)qv;
+                            RO[y * stride + x] = (xg_coef)(rv < -32768 ? -32768 : rv > 32767 ? 32767 : rv);
+                            map |= 1ull << ((ment >> 15) & 63);
+                        }
                     }
-                    scr_q[k] = (uint16_t)lv;
-                    k++;
-                }
-                const int iqadd = 1 << (P.iqShift - 1);
-                int state = 0;
-                for (int j = k - 1; j >= 0; j--) {
-                    const int lv = scr_q[j];
-                    const uint32_t e = __ldg(&ST[j].x);
-                    const int x = e & 31, y = (e >> 5) & 31;
-                    int qv = 0;
-                    if (lv) {
-                        qv = T[y * stride + x] < 0 ? -lv : lv;
-                        const int qi = 2 * qv + (qv > 0 ? -(state >> 1) : (state >> 1));
-                        const int v = (qi * P.iqScale + iqadd) >> P.iqShift;
-                        QO[y * stride + x] = (xg_coef)qv;
-                        RO[y * stride + x] = (xg_coef)(v < -32768 ? -32768 : v > 32767 ? 32767 : v);
-                        map |= 1ull << ((e >> 15) & 63);
-                    }
-                    state = (32040 >> ((state << 2) + ((qv & 1) << 1))) & 3;
                 }
             }
-            nzout[perm ? perm[job] : job] = map;
+            map |= __shfl_xor_sync(qmask, map, 1, 4);
+            map |= __shfl_xor_sync(qmask, map, 2, 4);
+            if (s == 0) nzout[job] = map;
         }
         __syncwarp(0xffffffffu);
     }
@@ -661,27 +743,51 @@ static int xg_dq_resident_ctas(void)
     return ctas;
 }
 
-/* device scratch of a run: rates of nsets sets, the job counter and nquads quads' decision areas */
-static size_t xg_dq_scratch_bytes(int nsets, int nquads)
+/* Device work area of a run, in order: job counter, bucket counts and cursors
+ * (256 B); rates of nsets context sets; last positions and order of njobs
+ * blocks; the scan-order copy of the blocks (nscan coefficients); nquads
+ * quads' decision areas. */
+struct XgDqArea {
+    int *counter, *counts, *cursor;
+    XgDqRates *rates;
+    int32_t *first, *order;
+    xg_coef *tscan;
+    uint32_t *codes;
+};
+static size_t xg_dq_area_bytes(int nsets, int njobs, size_t nscan, int nquads, XgDqArea *a, char *base)
 {
-    return 256 + (((size_t)nsets * 2 * sizeof(XgDqRates) + 255) & ~(size_t)255) + (size_t)nquads * XG_DQ_SCR_WORDS * 4;
+    size_t o = 0;
+    auto take = [&](size_t bytes) { size_t at = o; o = (o + bytes + 255) & ~(size_t)255; return base ? base + at : nullptr; };
+    char *hdr = take(1024);
+    char *rt = take((size_t)nsets * 2 * sizeof(XgDqRates));
+    char *fi = take((size_t)njobs * 4);
+    char *od = take((size_t)njobs * 4);
+    char *ts = take(nscan * sizeof(xg_coef));
+    char *cd = take((size_t)nquads * XG_DQ_MAXN * 4);
+    if (a && base) {
+        a->counter = (int *)hdr; a->counts = (int *)hdr + 1; a->cursor = (int *)hdr + 80;
+        a->rates = (XgDqRates *)rt; a->first = (int32_t *)fi; a->order = (int32_t *)od;
+        a->tscan = (xg_coef *)ts; a->codes = (uint32_t *)cd;
+    }
+    return o;
 }
 
-static int xg_dq_enqueue(const xin_gpu_dq_block *d_jobs, const int32_t *d_perm, int njobs, const xg_coef *t, xg_coef *q,
-                         xg_coef *r, unsigned long long *nz, const xin_gpu_prob *d_sets, int nsets, void *d_scratch,
-                         int max_ctas, int full, cudaStream_t st)
+static int xg_dq_enqueue(const xin_gpu_dq_block *d_jobs, const uint32_t *d_soff, int njobs,
+                         const xg_coef *t, xg_coef *q, xg_coef *r, unsigned long long *nz, const xin_gpu_prob *d_sets,
+                         int nsets, const XgDqArea &A, int max_ctas, int full, cudaStream_t st)
 {
-    char *base = (char *)d_scratch;
-    int *counter = (int *)base;
-    XgDqRates *rates = (XgDqRates *)(base + 256);
-    uint32_t *dec = (uint32_t *)(base + 256 + (((size_t)nsets * 2 * sizeof(XgDqRates) + 255) & ~(size_t)255));
     int ctas = (njobs + XG_DQ_QUADS - 1) / XG_DQ_QUADS;
     if (ctas > max_ctas) ctas = max_ctas;
-    if (xg_cuda_check(cudaMemsetAsync(counter, 0, sizeof(int), st), "dq counter")) return XIN_GPU_ERR_CUDA;
-    k_dq_rates<<<nsets, 64, 0, st>>>(d_sets, rates);
-    k_dq<<<ctas, XG_DQ_THREADS, sizeof(XgDqSmem), st>>>(d_jobs, njobs, counter, t, q, r, nz, d_sets, rates, g_dq.d_step,
-                                                        g_dq.d_tpl, g_dq.d_par, dec, d_perm, full);
-    xg_count_launch(2);
+    if (xg_cuda_check(cudaMemsetAsync(A.counter, 0, 1024, st), "dq counters")) return XIN_GPU_ERR_CUDA;
+    k_dq_rates<<<nsets, 64, 0, st>>>(d_sets, A.rates);
+    const int pw = 8, pblocks = std::min((njobs + pw - 1) / pw, 152 * 16);
+    k_dq_prep<<<pblocks, pw * 32, 0, st>>>(d_jobs, njobs, d_soff, t, A.tscan, q, r, nz, g_dq.d_step, g_dq.d_par,
+                                           A.first, A.counts, full);
+    k_dq_order<<<std::min((njobs + 255) / 256, 152 * 4), 256, 0, st>>>(njobs, A.first, A.counts, A.cursor, A.order);
+    k_dq<<<ctas, XG_DQ_THREADS, sizeof(XgDqSmem), st>>>(d_jobs, njobs, A.counter, A.counts, A.order, A.first, d_soff,
+                                                        A.tscan, q, r, nz, d_sets, A.rates, g_dq.d_step, g_dq.d_tpl,
+                                                        g_dq.d_par, A.codes);
+    xg_count_launch(4);
     return xg_cuda_check(cudaGetLastError(), "dep_quant launch");
 }
 
@@ -709,10 +815,11 @@ static int xg_dq_validate(const xin_gpu_dq_block *b, int32_t n, size_t ncoeffs, 
 struct xin_gpu_dq_plan {
     int device;
     int32_t nblocks, nsets, ctas;
-    size_t ncoeffs;
-    xin_gpu_dq_block *d_jobs;       /* largest blocks first */
-    int32_t *d_perm;                /* list position -> caller's block index (for nz) */
-    void *d_scratch;
+    size_t ncoeffs, nscan;
+    xin_gpu_dq_block *d_jobs;
+    uint32_t *d_soff;               /* start of each block's scan-order copy */
+    char *d_area;
+    XgDqArea area;
 };
 
 extern "C" void xin_gpu_dq_plan_destroy(xin_gpu_dq_plan *p);
@@ -729,27 +836,28 @@ extern "C" int xin_gpu_dq_plan_create(const xin_gpu_dq_block *blocks, int32_t nb
     if (!xg_thread() || !xg_dq_tables()) return xin_gpu_last_status();
     int st = xg_dq_validate(blocks, nblocks, ncoeffs, nsets);
     if (st) return st;
-    /* largest blocks first, so that the eight blocks a warp runs together are alike */
-    std::vector<int32_t> order(nblocks);
-    for (int i = 0; i < nblocks; i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        return blocks[a].log2_w + blocks[a].log2_h > blocks[b].log2_w + blocks[b].log2_h;
-    });
-    std::vector<xin_gpu_dq_block> jobs(nblocks);
-    for (int i = 0; i < nblocks; i++) jobs[i] = blocks[order[i]];
+    std::vector<uint32_t> soff(nblocks);
+    size_t nscan = 0;
+    for (int i = 0; i < nblocks; i++) {
+        soff[i] = (uint32_t)nscan;
+        nscan += (size_t)std::min(1 << blocks[i].log2_w, 32) * std::min(1 << blocks[i].log2_h, 32);
+    }
     xin_gpu_dq_plan *p = new xin_gpu_dq_plan();
     cudaGetDevice(&p->device);
-    p->nblocks = nblocks; p->nsets = nsets; p->ncoeffs = ncoeffs;
-    int res = xg_dq_resident_ctas();
-    p->ctas = std::min(res, (nblocks + XG_DQ_QUADS - 1) / XG_DQ_QUADS);
-    if (xg_cuda_check(cudaMalloc(&p->d_perm, (size_t)nblocks * sizeof(int32_t)), "dq plan") ||
-        xg_cuda_check(cudaMemcpy(p->d_perm, order.data(), (size_t)nblocks * sizeof(int32_t), cudaMemcpyHostToDevice), "dq plan") ||
+    p->nblocks = nblocks; p->nsets = nsets; p->ncoeffs = ncoeffs; p->nscan = nscan;
+    p->ctas = std::min(xg_dq_resident_ctas(), (nblocks + XG_DQ_QUADS - 1) / XG_DQ_QUADS);
+    const size_t bytes = xg_dq_area_bytes(nsets, nblocks, nscan, p->ctas * XG_DQ_QUADS, nullptr, nullptr);
+    if (nscan >= (1ull << 32) ||
+        xg_cuda_check(cudaMalloc(&p->d_soff, (size_t)nblocks * 4), "dq plan") ||
+        xg_cuda_check(cudaMemcpy(p->d_soff, soff.data(), (size_t)nblocks * 4, cudaMemcpyHostToDevice), "dq plan") ||
         xg_cuda_check(cudaMalloc(&p->d_jobs, (size_t)nblocks * sizeof(xin_gpu_dq_block)), "dq plan") ||
-        xg_cuda_check(cudaMemcpy(p->d_jobs, jobs.data(), (size_t)nblocks * sizeof(xin_gpu_dq_block), cudaMemcpyHostToDevice), "dq plan") ||
-        xg_cuda_check(cudaMalloc(&p->d_scratch, xg_dq_scratch_bytes(nsets, p->ctas * XG_DQ_QUADS)), "dq plan")) {
+        xg_cuda_check(cudaMemcpy(p->d_jobs, blocks, (size_t)nblocks * sizeof(xin_gpu_dq_block), cudaMemcpyHostToDevice), "dq plan") ||
+        xg_cuda_check(cudaMalloc(&p->d_area, bytes), "dq plan")) {
+        if (nscan >= (1ull << 32)) xg_set_error(XIN_GPU_ERR_ARG, "dq_plan_create: too many coefficients");
         xin_gpu_dq_plan_destroy(p);
-        return XIN_GPU_ERR_CUDA;
+        return xin_gpu_last_status();
     }
+    xg_dq_area_bytes(nsets, nblocks, nscan, p->ctas * XG_DQ_QUADS, &p->area, p->d_area);
     *out = p;
     return XIN_GPU_OK;
 }
@@ -763,16 +871,16 @@ extern "C" int xin_gpu_dq_plan_run(xin_gpu_dq_plan *p, const XG_COEFF *t, XG_COE
         return XIN_GPU_ERR_ARG;
     }
     cudaGetLastError();
-    return xg_dq_enqueue(p->d_jobs, p->d_perm, p->nblocks, (const xg_coef *)t, (xg_coef *)q, (xg_coef *)r, (unsigned long long *)nz,
-                         ctx_sets, p->nsets, p->d_scratch, p->ctas, 1, (cudaStream_t)stream);
+    return xg_dq_enqueue(p->d_jobs, p->d_soff, p->nblocks, (const xg_coef *)t, (xg_coef *)q, (xg_coef *)r,
+                         (unsigned long long *)nz, ctx_sets, p->nsets, p->area, p->ctas, 1, (cudaStream_t)stream);
 }
 
 extern "C" void xin_gpu_dq_plan_destroy(xin_gpu_dq_plan *p)
 {
     if (!p) return;
     cudaFree(p->d_jobs);
-    cudaFree(p->d_perm);
-    cudaFree(p->d_scratch);
+    cudaFree(p->d_soff);
+    cudaFree(p->d_area);
     delete p;
 }
 
@@ -868,9 +976,14 @@ extern "C" void XinGpuDepQuant(void *depQuant, void *fastBuf, void *tu, XG_COEFF
     unsigned long long *dnz = (unsigned long long *)xg_dalloc(th, 8);
     xin_gpu_dq_block *dj = (xin_gpu_dq_block *)xg_stage_in(th, &jb, 1, 1, 1, sizeof jb);
     xin_gpu_prob *dc = (xin_gpu_prob *)xg_stage_in(th, ctx, (intptr_t)cbytes, cbytes, 1, 1);
-    void *scr = xg_dalloc(th, xg_dq_scratch_bytes(1, XG_DQ_QUADS));
-    if (!dt || !dq || !dr || !dnz || !dj || !dc || !scr) return;
-    if (xg_dq_enqueue(dj, nullptr, 1, dt, dq, dr, dnz, dc, 1, scr, 1, 0, th->stream)) return;
+    const uint32_t zero = 0;
+    uint32_t *dso = (uint32_t *)xg_stage_in(th, &zero, 1, 1, 1, 4);
+    const size_t abytes = xg_dq_area_bytes(1, 1, (size_t)ew * eh, XG_DQ_QUADS, nullptr, nullptr);
+    char *area = (char *)xg_dalloc(th, abytes);
+    if (!dt || !dq || !dr || !dnz || !dj || !dc || !dso || !area) return;
+    XgDqArea A;
+    xg_dq_area_bytes(1, 1, (size_t)ew * eh, XG_DQ_QUADS, &A, area);
+    if (xg_dq_enqueue(dj, dso, 1, dt, dq, dr, dnz, dc, 1, A, 1, 0, th->stream)) return;
     if (xg_stage_out(th, qCoeff, coeffStride, dq, ew, eh, sizeof(xg_coef)) ||
         xg_stage_out(th, rCoeff, coeffStride, dr, ew, eh, sizeof(xg_coef)) ||
         xg_cuda_check(cudaMemcpyAsync(th->hbuf, dnz, 8, cudaMemcpyDeviceToHost, th->stream), "d2h") || xg_sync(th))

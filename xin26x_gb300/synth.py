@@ -176,3 +176,50 @@ def dq_blocks(n: int, seed: int, bitdepth: int = 10, n_sets: int = 1, qp_range=N
             c = coefficients(rng, w, h, bitdepth, scale=12.0 * np.sqrt(w * h) / 8.0)
         coef[off[i]:off[i] + w * h] = c.ravel()
     return b, coef, contexts(rng, n_sets)
+
+
+def _diag_scan(w: int, h: int):
+    """up-right diagonal scan of a w x h grid: (x, y) per scan index"""
+    out, x, y = [], 0, 0
+    for _ in range(w * h):
+        out.append((x, y))
+        if x == w - 1 or y == 0:
+            y += x + 1
+            x = 0
+            if y >= h:
+                x += y - (h - 1)
+                y = h - 1
+        else:
+            x += 1
+            y -= 1
+    return out
+
+
+_RASTER_OF_SCAN: dict = {}
+
+
+def dq_steps(blocks, t, bitdepth: int) -> np.ndarray:
+    """Trellis length of each block: 1 + the highest scan index whose |t| exceeds
+    the last-position threshold (thresLast / (qScale << 2) of the trellis
+    parameters), 0 for blocks with none.  This is the number of coefficient
+    steps the trellis walks; it is the work unit of the dependent-quantisation
+    throughput figures."""
+    qm = ((26214, 23302, 20560, 18396, 16384, 14564), (18396, 16384, 14564, 13107, 11651, 10280))
+    out = np.zeros(len(blocks), np.int64)
+    for i, b in enumerate(blocks):
+        lw, lh, qp = int(b["log2_w"]), int(b["log2_h"]), int(b["qp"])
+        ew, eh, st, off = min(1 << lw, 32), min(1 << lh, 32), int(b["stride"]), int(b["offset"])
+        key = (ew, eh, st)
+        if key not in _RASTER_OF_SCAN:
+            cg = _diag_scan(ew // 4, eh // 4)
+            inner = _diag_scan(4, 4)
+            _RASTER_OF_SCAN[key] = np.array([(gy * 4 + iy) * st + gx * 4 + ix for gx, gy in cg for ix, iy in inner])
+        lg = lw + lh
+        adj, per, rem = lg & 1, (qp + 1) // 6, (qp + 1) % 6
+        ts = 15 - bitdepth - (lg >> 1) - adj
+        qshift = 13 + per + ts
+        thr = (8 << (qshift - 1) if qshift else 4) // (qm[adj][rem] << 2)
+        v = np.abs(t[off + _RASTER_OF_SCAN[key]].astype(np.int64))
+        hit = np.nonzero(v > thr)[0]
+        out[i] = hit[-1] + 1 if hit.size else 0
+    return out
