@@ -320,6 +320,7 @@ def run_gpu(args):
     # plain per-call form on a sample of CUs (one synchronous launch per reference call)
     percall = percall_sample(lib, frames)
     kbatch = kernel_batch_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup) if rank == 0 else None
+    dq = dep_quant_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup, cpu=(world == 1)) if rank == 0 else None
     wide = wide_search_bench(torch, flush) if rank == 0 else None
     serving = None
     if rank == 0 and world == 1:
@@ -353,6 +354,7 @@ def run_gpu(args):
                        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}},
                "percall": percall,
                "kernel_batch": kbatch,
+               "dep_quant": dq,
                "wide_search_4k_10bit": wide,
                "serving": serving,
                "gpu_launches": int(launches),
@@ -417,6 +419,82 @@ def kernel_batch_bench(torch, flush, steps, warmup, nblocks=65536, seed=65536):
     out["roofline"] = {"bound": "hbm", "kernel": "k_tq_tc", "achieved": achieved, "peak": hbm or 6800.0, "unit": "GB/s",
                        "frac": achieved / (hbm or 6800.0), "algorithmic_bytes": int(algo),
                        "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "of fallback 6.8 TB/s"}
+    return out
+
+
+def dep_quant_bench(torch, flush, steps, warmup, nblocks=65536, seed=11, cpu=True):
+    """Dependent quantisation (the reference's trellis quantiser, used from
+    preset 4 up in place of plain quantisation) on the kernel-bench shapes:
+    65,536 10-bit blocks of sides 4..64, coefficient spectra of an 11-bit
+    Laplacian residual, QP U[22,39] (+12 internally at 10-bit), luma 2/3 and
+    chroma 1/3, four CABAC context sets.  Plan form timed with CUDA events,
+    L2 flushed between runs.  The work unit is a trellis step: one coefficient
+    position walked by one block (from its last significant position to DC)."""
+    from xin26x_gb300 import _lib, synth
+    g = _lib.load(10)
+    assert g.xin_gpu_init(torch.cuda.current_device()) == 0
+    nsets = 4
+    blocks, t, sets = synth.dq_blocks(nblocks, seed, bitdepth=10, n_sets=nsets)
+    wsteps = synth.dq_steps(blocks, t, 10)
+    nsteps = int(wsteps.sum())
+    d_t = torch.from_numpy(t).cuda()
+    q, r = torch.empty_like(d_t), torch.empty_like(d_t)
+    nz = torch.empty(nblocks, dtype=torch.int64, device="cuda")
+    d_sets = torch.from_numpy(sets.view(np.uint8).reshape(-1)).cuda()
+    stream = torch.cuda.current_stream()
+    plan = C.c_void_p()
+    assert g.xin_gpu_dq_plan_create(blocks.ctypes.data, nblocks, t.size, nsets, C.byref(plan)) == 0, g.xin_gpu_last_error()
+    run = lambda: g.xin_gpu_dq_plan_run(plan, d_t.data_ptr(), q.data_ptr(), r.data_ptr(), nz.data_ptr(), d_sets.data_ptr(),
+                                        stream.cuda_stream)
+    for _ in range(max(3, warmup)):
+        assert run() == 0, g.xin_gpu_last_error()
+    times = []
+    for _ in range(steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        assert run() == 0
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    g.xin_gpu_dq_plan_destroy(plan)
+    ms = float(np.mean(times))
+    algo = t.size * 4 * 3 + nblocks * (16 + 8)             # t in, q / r out, block record, nz
+    peaks = _measured_peaks()
+    hbm = (peaks.get("hbm_gbs") if peaks else None) or 6800.0
+    achieved = algo / (ms * 1e-3) / 1e9
+    out = {"workload": f"{nblocks} blocks, 10-bit, sides 4..64 (kernel-bench shapes), coefficient spectra of an 11-bit "
+                       "Laplacian(12) residual, QP U[22,39] (+12), luma 2/3 / Cb 1/6 / Cr 1/6, root cbf on half of "
+                       f"the luma blocks, {nsets} CABAC context sets",
+           "coefficients": int(t.size), "trellis_steps": nsteps, "blocks_with_trellis": int((wsteps > 0).sum()),
+           "longest_trellis": int(wsteps.max()), "l2": "flushed between runs",
+           "ms": ms, "Mblocks_per_s": nblocks / ms / 1e3, "Gsteps_per_s": nsteps / ms / 1e6,
+           "roofline": {"bound": "latency", "kernel": "k_dq", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                        "frac": achieved / hbm, "algorithmic_bytes": int(algo),
+                        "note": "HBM is not the limit: each block's trellis is a serial chain of coefficient steps "
+                                "(four states on four lanes); the floor is the step latency times the longest "
+                                "trellis of the batch",
+                        "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "of fallback 6.8 TB/s"}}
+    if cpu:
+        from oracle import oracle as O
+        o = O.oracle(10)
+        qq, rr, nzz = np.zeros_like(t), np.zeros_like(t), np.zeros(nblocks, np.uint64)
+        rng = np.random.default_rng(3)
+        idx = rng.permutation(nblocks)
+        t0, n, done_steps = time.perf_counter(), 0, 0
+        while time.perf_counter() - t0 < 10.0 and n < nblocks:
+            b = blocks[idx[n]]
+            off = int(b["offset"])
+            o.dep_quant(O.ptr(t, off), int(b["stride"]), 1 << int(b["log2_w"]), 1 << int(b["log2_h"]), int(b["qp"]),
+                        int(b["comp"]), sets[int(b["ctx_set"])].ctypes.data, int(b["root_cbf"]), O.ptr(qq, off),
+                        O.ptr(rr, off), O.ptr(nzz, int(idx[n])))
+            done_steps += int(wsteps[idx[n]])
+            n += 1
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": done_steps / el / 1e9, "unit": "Gsteps/s", "cores": 1, "kind": "port",
+                               "sample": f"{n} random blocks of the same list, oracle C restatement of Xin266DepQuant, "
+                                         f"1 thread, {el:.1f} s (includes a ctypes call per block)"}
     return out
 
 
