@@ -128,6 +128,19 @@ void XinGpuChromaInterpVetU8S16(XG_INTERP_ARGS(XG_PIXEL, int16_t));
 void XinGpuChromaInterpHorVetU8S16(XG_INTERP_ARGS(XG_PIXEL, int16_t));
 void XinGpuChromaInterpVetS16U8(XG_INTERP_ARGS(int16_t, XG_PIXEL));
 void XinGpuChromaInterpVetS16S16(XG_INTERP_ARGS(int16_t, int16_t));
+/* bilinear DMVR prediction, typedef XinBiliInterp, table entry
+ * pfXinBiliInterp[!!fx][!!fy][lgW] (h266_encoder/include/h266_func_struct.h:150,741;
+ * h266_core/source/h266_bilinear_filter.c:46-260):
+ * frac = fy << 4 | fx (1/16 pel), taps {16 - f, f}, 10-bit intermediate; each
+ * writes h rows of w + 4 int16 samples (DMVR_PADING_SIZE extra columns). */
+void XinGpuBiliInterpCopy(const XG_PIXEL *src, intptr_t srcStride, int16_t *dst, intptr_t dstStride, int32_t frac,
+                          uint32_t width, uint32_t height);
+void XinGpuBiliInterpHor(const XG_PIXEL *src, intptr_t srcStride, int16_t *dst, intptr_t dstStride, int32_t frac,
+                         uint32_t width, uint32_t height);
+void XinGpuBiliInterpVet(const XG_PIXEL *src, intptr_t srcStride, int16_t *dst, intptr_t dstStride, int32_t frac,
+                         uint32_t width, uint32_t height);
+void XinGpuBiliInterpHorVet(const XG_PIXEL *src, intptr_t srcStride, int16_t *dst, intptr_t dstStride, int32_t frac,
+                            uint32_t width, uint32_t height);
 void XinGpuInterpAvgS16U8(const int16_t *src0, intptr_t src0Stride, const int16_t *src1, intptr_t src1Stride,
                           XG_PIXEL *dst, intptr_t dstStride, uint32_t width, uint32_t height);
 void XinGpuInterpWeightS16U8(const int16_t *src0, intptr_t src0Stride, const int16_t *src1, intptr_t src1Stride,

@@ -136,6 +136,7 @@ _SIGS = {
     "tr_matrix": ("orc_tr_matrix", None, [C.c_int, C.c_int]),
     "dep_quant": ("orc_dep_quant", "ref_dep_quant", [vp, ip, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int,
                                                      vp, vp, vp]),
+    "bili_interp": ("orc_bili_interp", "ref_bili_interp", [C.c_int, vp, ip, vp, ip, i32, u32, u32]),
     "dq_params": ("orc_dq_params", None, [C.c_int, C.c_int, C.POINTER(orc_dq_param)]),
     "dq_frac_bits": ("orc_dq_frac_bits", None, [C.c_int, vp]),
     "dq_rice_bits": ("orc_dq_rice_bits", None, [C.c_int, C.c_int]),

@@ -222,3 +222,19 @@ void ref_dq_param(int qp, int lgsum, xin_dp_param *out)
     dq_setup();
     *out = dq_seq->dpParam[lgsum][qp];
 }
+
+/* bilinear DMVR prediction (h266_core/source/h266_bilinear_filter.c:46-260) by variant,
+ * the way pfXinBiliInterp[!!fx][!!fy] selects it (h266_encoder/source/h266_func_init.c:496-530) */
+void Xin266BiliInterpCopy(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32);
+void Xin266BiliInterpHor(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32);
+void Xin266BiliInterpVet(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32);
+void Xin266BiliInterpHorVet(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32);
+void ref_bili_interp(int variant, const PIXEL *src, intptr_t ss, SINT16 *dst, intptr_t ds, SINT32 frac, UINT32 w, UINT32 h)
+{
+    switch (variant) {
+    case 0: Xin266BiliInterpCopy(src, ss, dst, ds, frac, w, h); break;
+    case 1: Xin266BiliInterpHor(src, ss, dst, ds, frac, w, h); break;
+    case 2: Xin266BiliInterpVet(src, ss, dst, ds, frac, w, h); break;
+    default: Xin266BiliInterpHorVet(src, ss, dst, ds, frac, w, h); break;
+    }
+}

@@ -362,6 +362,29 @@ void orc_interp_weight(const int16_t *a, intptr_t as, const int16_t *b, intptr_t
         for (uint32_t x = 0; x < w; x++) dst[x] = clip_pix(((int32_t)a[x] * wa + (int32_t)b[x] * wb + offset) >> shift);
 }
 
+/* Bilinear DMVR prediction (h266_core/source/h266_bilinear_filter.c:46-260), pinned (open C):
+ * two taps {16 - f, f} at 1/16 pel into a 10-bit intermediate; every form
+ * writes h rows of w + 4 (DMVR_PADING_SIZE) samples.  variant 0 copy, 1 H, 2 V,
+ * 3 H over h + 1 rows (16-bit) then V with (+8) >> 4. */
+void orc_bili_interp(int variant, const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h)
+{
+    int fx = frac & 15, fy = frac >> 4, sh = ORC_BITDEPTH - 6, off = 1 << (sh - 1);
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w + 4; x++) {
+            const opix *p = src + (intptr_t)y * ss + x;
+            int v;
+            if (variant == 0) v = (int)p[0] << (10 - ORC_BITDEPTH);
+            else if (variant == 1) v = ((int)p[0] * (16 - fx) + (int)p[1] * fx + off) >> sh;
+            else if (variant == 2) v = ((int)p[0] * (16 - fy) + (int)p[ss] * fy + off) >> sh;
+            else {
+                int a = (int16_t)(((int)p[0] * (16 - fx) + (int)p[1] * fx + off) >> sh);
+                int b = (int16_t)(((int)p[ss] * (16 - fx) + (int)p[ss + 1] * fx + off) >> sh);
+                v = (a * (16 - fy) + b * fy + 8) >> 4;
+            }
+            dst[(intptr_t)y * ds + x] = (int16_t)v;
+        }
+}
+
 /* Table dispatch pfXinLumaInterp[!!fx][!!fy][lgW] (h266_encoder/source/h266_inter_prediction.c:143-169).
  * The 8-argument form is the one h266_sub_pel_refine.c calls through the header
  * h266_encoder/include/h266_inter_prediction.h:43; the filter index is the

@@ -84,6 +84,8 @@ void orc_chroma_vet_s16_pix(const int16_t *src, intptr_t ss, opix *dst, intptr_t
 void orc_chroma_vet_s16_s16(const int16_t *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h, uint32_t fi);
 void orc_interp_avg(const int16_t *a, intptr_t as, const int16_t *b, intptr_t bs, opix *dst, intptr_t ds, uint32_t w, uint32_t h);
 void orc_interp_weight(const int16_t *a, intptr_t as, const int16_t *b, intptr_t bs, opix *dst, intptr_t ds, uint32_t w, uint32_t h, int32_t wa, int32_t wb);
+/* bilinear DMVR prediction (h266_core/source/h266_bilinear_filter.c:46-260); pinned (open C) */
+void orc_bili_interp(int variant, const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h);
 
 /* call-site dispatch (h266_encoder/source/h266_inter_prediction.c) */
 void orc_luma_interpolation(const opix *src, intptr_t ss, opix *dst, intptr_t ds, int32_t frac, uint32_t lgw, uint32_t h, uint32_t fi);

@@ -6,7 +6,7 @@ place, oracle/Makefile target ``ref``) and records seeded inputs with that
 library's outputs.  tests/test_oracle_golden.py replays the inputs through
 the oracle anywhere (no reference tree needed) and requires identical output.
 
-    python tests/golden/make_golden.py [core|dq]
+    python tests/golden/make_golden.py [core|dq|bili]
 """
 import os
 import sys
@@ -146,6 +146,26 @@ def make_dq(bd):
     print("wrote", os.path.join(OUT, f"ref_dq_{bd}bit.npz"))
 
 
+def make_bili(bd):
+    """Bilinear DMVR prediction (h266_bilinear_filter.c) through the reference:
+    four variants, 55 phases spread over all 256, on a 16x8, a 4x4 and a 128x4 block."""
+    O.build(ref=True)
+    r = O.reference(bd)
+    rng = np.random.default_rng(5200 + bd)
+    src = rng.integers(0, r.max_pix + 1, size=(12, 144)).astype(r.pix)
+    g = {"src": src}
+    for (w, h) in ((16, 8), (4, 4), (128, 4)):
+        res = []
+        for variant in range(4):
+            for frac in list(range(0, 256, 5)) + [15, 240, 255]:
+                b = np.zeros((h, w + 4), np.int16)
+                r.bili_interp(variant, O.ptr(src, 2 * src.shape[1] + 2), src.shape[1], O.ptr(b), w + 4, frac, w, h)
+                res.append(b)
+        g[f"out_{w}x{h}"] = np.stack(res)
+    np.savez_compressed(os.path.join(OUT, f"ref_bili_{bd}bit.npz"), **g)
+    print("wrote", os.path.join(OUT, f"ref_bili_{bd}bit.npz"))
+
+
 if __name__ == "__main__":
     what = sys.argv[1:] or ["all"]
     for bd in (8, 10):
@@ -153,3 +173,5 @@ if __name__ == "__main__":
             make(bd)
         if "all" in what or "dq" in what:
             make_dq(bd)
+        if "all" in what or "bili" in what:
+            make_bili(bd)

@@ -75,7 +75,7 @@ def test_me_mirror_matches_reference_layout():
 
 _FUNC_MEMBERS = ["pfXinComputeSad", "pfXinComputeSatd", "pfXinComputeDist", "pfXinComputeAvgSad", "pfXinComputeAvgDist",
                  "pfXinComputeWeightDist", "pfXinComputeSadx8", "pfXinComputeAvgSadx8", "pfXinLumaInterp",
-                 "pfXinChromaInterp", "pfXinLumaInterpS16", "pfXinChromaInterpS16", "pfXinInterpAvg", "pfXinInterpWeight",
+                 "pfXinChromaInterp", "pfXinBiliInterp", "pfXinLumaInterpS16", "pfXinChromaInterpS16", "pfXinInterpAvg", "pfXinInterpWeight",
                  "pfXinQuantInvQuant", "pfXinFor2dDct2", "pfXinFor2dSkip", "pfXinInv2dSkip", "pfXinFor1dDct",
                  "pfXinInv2dDct2", "pfXinInv1dDct", "pfXinBlockSubForDct", "pfXinBlockAddForDct", "pfXinComputeHada8x8",
                  "pfXinPreRdoq", "pfXinPreDepQuant", "pfXinDepQuant", "pfXinFilterIntraNB"]
@@ -128,6 +128,8 @@ def test_installer_fills_tables_without_gpu(bd):
     assert fs[offs["pfXinQuantInvQuant"] // 8 + 5] == addr("XinGpuQuantInvQuant")
     assert fs[offs["pfXinPreRdoq"] // 8] == addr("XinGpuPreRdoq")
     assert fs[offs["pfXinDepQuant"] // 8] == addr("XinGpuDepQuant")
+    assert fs[offs["pfXinBiliInterp"] // 8 + 3 * 8 + 4] == addr("XinGpuBiliInterpHorVet")  # [1][1][4]
+    assert fs[offs["pfXinBiliInterp"] // 8 + 1 * 8 + 2] == addr("XinGpuBiliInterpVet")     # [0][1][2]
     assert fs[offs["pfXinFilterIntraNB"] // 8] is None                                    # off the hot path
     assert me.funcSet[0] == addr("XinGpuComputeSad")
     assert lib.xin_gpu_install(None, None, 15) == -2

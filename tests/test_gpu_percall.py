@@ -131,6 +131,26 @@ def test_interpolation(libs, spec):
                 assert np.array_equal(a, b), (gname, w, h, fi, frac)
 
 
+def test_bilinear_interpolation(libs):
+    """pfXinBiliInterp (DMVR bilinear prediction): the four variants at every
+    tenth 1/16 phase and widths 1..128, h rows of w + 4 outputs, destination
+    columns beyond w + 4 untouched."""
+    g, o, bd = libs
+    rng = np.random.default_rng(77)
+    mx = (1 << bd) - 1
+    for w, h in [(1, 1), (4, 4), (8, 16), (16, 8), (32, 32), (64, 64), (128, 128)]:
+        src = rng.integers(0, mx + 1, size=(h + 4, w + 12)).astype(o.pix)
+        sp = src.shape[1]
+        for variant, name in enumerate(("Copy", "Hor", "Vet", "HorVet")):
+            for frac in list(range(0, 256, 10)) + [255]:
+                a = np.full((h, w + 9), 5, np.int16)
+                b = np.full((h, w + 9), 5, np.int16)
+                getattr(g, "XinGpuBiliInterp" + name)(P(src, sp + 1), sp, P(a), w + 9, frac, w, h)
+                _ok(g, name)
+                o.bili_interp(variant, P(src, sp + 1), sp, P(b), w + 9, frac, w, h)
+                assert np.array_equal(a, b), (name, w, h, frac)
+
+
 def test_interp_avg_weight(libs):
     g, o, bd = libs
     rng = np.random.default_rng(3)

@@ -92,3 +92,20 @@ def test_golden_dep_quant(bd):
         assert np.array_equal(r.ravel(), g["r"][off:off + n]), (w, h, qp, comp, root)
         assert nz[0] == nz_ref
         off += n
+
+
+@pytest.mark.parametrize("bd", (8, 10))
+def test_golden_bilinear(bd):
+    """Bilinear DMVR prediction: the reference's outputs (make_golden.py bili)."""
+    g = np.load(os.path.join(GOLD, f"ref_bili_{bd}bit.npz"))
+    o = O.oracle(bd)
+    src = g["src"]
+    for (w, h) in ((16, 8), (4, 4), (128, 4)):
+        want = g[f"out_{w}x{h}"]
+        i = 0
+        for variant in range(4):
+            for frac in list(range(0, 256, 5)) + [15, 240, 255]:
+                b = np.zeros((h, w + 4), np.int16)
+                o.bili_interp(variant, O.ptr(src, 2 * src.shape[1] + 2), src.shape[1], O.ptr(b), w + 4, frac, w, h)
+                assert np.array_equal(b, want[i]), (w, h, variant, frac)
+                i += 1

@@ -327,3 +327,20 @@ def test_dep_quant_tables_vs_reference(bd):
             o.dq_params(qp, lg, C.byref(a))
             r.dq_param_ref(qp, lg, C.byref(b))
             assert all(getattr(a, f) == getattr(b, f) for f, _ in a._fields_), (lg, qp)
+
+
+@pytest.mark.parametrize("bd", BDS)
+def test_bilinear_interp_every_phase(bd):
+    """Xin266BiliInterpCopy / Hor / Vet / HorVet (h266_bilinear_filter.c:46-260)
+    against the oracle: every 1/16 phase, widths 1..128 (+4 output columns)."""
+    o, r = _pair(bd)
+    rng = np.random.default_rng(900 + bd)
+    for w, h in [(1, 2), (4, 4), (8, 16), (16, 8), (32, 32), (64, 16), (128, 128), (4, 132)]:
+        src = rng.integers(0, o.max_pix + 1, size=(h + 8, w + 12)).astype(o.pix)
+        for variant in range(4):
+            for frac in range(0, 256, 1 if w * h <= 256 else 17):
+                a = np.full((h, w + 8), 7, np.int16)
+                b = np.full((h, w + 8), 7, np.int16)
+                o.bili_interp(variant, O.ptr(src, 2 * src.shape[1] + 2), src.shape[1], O.ptr(a), w + 8, frac, w, h)
+                r.bili_interp(variant, O.ptr(src, 2 * src.shape[1] + 2), src.shape[1], O.ptr(b), w + 8, frac, w, h)
+                assert np.array_equal(a, b), (variant, w, h, frac)

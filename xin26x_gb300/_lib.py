@@ -158,6 +158,10 @@ SIGNATURES = {
     "xin_gpu_dq_plan_create": ([vp, i32, C.c_size_t, i32, C.POINTER(vp)], C.c_int),
     "xin_gpu_dq_plan_run": ([vp, vp, vp, vp, vp, vp, vp], C.c_int),
     "xin_gpu_dq_plan_destroy": ([vp], None),
+    "XinGpuBiliInterpCopy": ([vp, C.c_ssize_t, vp, C.c_ssize_t, i32, u32, u32], None),
+    "XinGpuBiliInterpHor": ([vp, C.c_ssize_t, vp, C.c_ssize_t, i32, u32, u32], None),
+    "XinGpuBiliInterpVet": ([vp, C.c_ssize_t, vp, C.c_ssize_t, i32, u32, u32], None),
+    "XinGpuBiliInterpHorVet": ([vp, C.c_ssize_t, vp, C.c_ssize_t, i32, u32, u32], None),
     "XinGpuDepQuant": ([vp, vp, vp, vp, vp, vp, C.c_ssize_t, u32, i32, i32, vp, u32], None),
 }
 for _n in ["InterpCopy", "InterpCopyU8S16", "LumaInterpHor", "LumaInterpVet", "LumaInterpHorVet", "LumaInterpHorU8S16",

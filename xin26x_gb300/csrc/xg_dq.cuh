@@ -468,15 +468,17 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
             /* context of this state at position k */
             uint32_t tv = ref >= 0 ? Q.tpl[ref][in] : 0u;
             int sum = tv & 127, a1 = (tv >> 7) & 31, cnt = tv >> 12;
+            if (l0 | l1 | l2 | l3) {
 #pragma unroll
-            for (int u = 0; u < 5; u++) {
-                if (u < nin) {
-                    int j = (se.y >> (4 * u)) & 15;
-                    int l = (int)xg_dq_byte(l0, l1, l2, l3, j);
-                    if (l) { sum += l; cnt++; a1 += min(4 + (int)((par16 >> j) & 1), l); }
+                for (int u = 0; u < 5; u++) {
+                    if (u < nin) {
+                        int j = (se.y >> (4 * u)) & 15;
+                        int l = (int)xg_dq_byte(l0, l1, l2, l3, j);
+                        if (l) { sum += l; cnt++; a1 += min(4 + (int)((par16 >> j) & 1), l); }
+                    }
                 }
+                sum = min(sum, 255);
             }
-            sum = min(sum, 255);
             const int d = px + py;
             const int sigoff = luma ? (d < 2 ? 8 : d < 5 ? 4 : 0) : (d < 2 ? 4 : 0);
             const int gtxoff = luma ? (d < 1 ? 16 : d < 3 ? 11 : d < 10 ? 6 : 1) : (d < 1 ? 6 : 1);
@@ -505,9 +507,12 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
                 return (m + P.distAdd) >> P.distShift;
             };
             auto lvof = [&](int i) -> int { return (q + ((i - q) & 3) + 1) >> 1; };
+            /* lane s prices quantisation index class s; lanes 0 / 1 take classes 0 and 2,
+             * lanes 2 / 3 classes 3 and 1 (A and B), even lanes also their own for "start" */
             const int iA = s < 2 ? 0 : 3, iB = s < 2 ? 2 : 1;
             const int lvA = lvof(iA), lvB = lvof(iB);
-            const long long ddA = ddof(iA), ddB = ddof(iB);
+            const long long ddS = ddof(s);
+            const long long ddA = xg_dq_shfl64(qmask, ddS, iA), ddB = xg_dq_shfl64(qmask, ddS, iB);
 
             /* candidates of this state (Xin266CheckRdCosts, h266_dep_quant.c:954-1046) */
             long long ca = cost + ddA, cb = cost + ddB, cz = cost;
@@ -550,7 +555,7 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
             }
             if ((s & 1) == 0) {
                 const int lvs = lvof(s);
-                long long c = ddof(s) + Q.last[0][px] + Q.last[1][py] + __ldg(&RT->gtx[0][lvs < 4 ? lvs : 4 + (lvs & 1)]) +
+                long long c = ddS + Q.last[0][px] + Q.last[1][py] + __ldg(&RT->gtx[0][lvs < 4 ? lvs : 4 + (lvs & 1)]) +
                               (lvs >= 4 ? sm.rice[0][min((lvs - 4) >> 1, 31)] : 0);
                 if (c < dc) { dc = c; dsel = s; dfrom = -1; }
             }
@@ -634,6 +639,7 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
                 const bool need = nsb || (right && below && ((nfl >> (below + 1)) & 1));
                 __syncwarp(qmask);
                 if (upd) {
+#pragma unroll 4
                     for (int j = 0; j < 16; j++) {
                         uint32_t t16 = 0;
                         if (need) {

@@ -61,6 +61,10 @@ extern "C" int xin_gpu_install(void *funcSet, void *meFunc, uint32_t what)
                 fs->pfXinChromaInterpS16[0][1][lg] = XG_FN(XinGpuChromaInterpVetU8S16);
                 fs->pfXinChromaInterpS16[1][1][lg] = XG_FN(XinGpuChromaInterpHorVetU8S16);
                 fs->pfXinInterpAvg[lg] = XG_FN(XinGpuInterpAvgS16U8);
+                fs->pfXinBiliInterp[0][0][lg] = XG_FN(XinGpuBiliInterpCopy);
+                fs->pfXinBiliInterp[1][0][lg] = XG_FN(XinGpuBiliInterpHor);
+                fs->pfXinBiliInterp[0][1][lg] = XG_FN(XinGpuBiliInterpVet);
+                fs->pfXinBiliInterp[1][1][lg] = XG_FN(XinGpuBiliInterpHorVet);
                 fs->pfXinInterpWeight[lg] = XG_FN(XinGpuInterpWeightS16U8);
             }
             if (what & XIN_GPU_INSTALL_TRANSFORM) {

@@ -126,6 +126,30 @@ __global__ void k_interp(const void *srcv, int sp, void *dstv, int w, int h, int
     else ((xg_pix *)dstv)[y * w + x] = (xg_pix)v;
 }
 
+/* bilinear DMVR prediction (h266_core/source/h266_bilinear_filter.c:46-260):
+ * taps {16 - f, f} at 1/16 pel, 10-bit intermediate precision, output rows of
+ * w + 4 samples.  VARIANT 0 copy (<< 10 - bd), 1 horizontal, 2 vertical,
+ * 3 horizontal over h + 1 rows into 16 bits, then vertical with (+8) >> 4. */
+template <int VARIANT>
+__global__ void k_bili(const xg_pix *src, int sp, int16_t *dst, int w, int h, int frac)
+{
+    const int ow = w + 4;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= ow || y >= h) return;
+    const int fx = frac & 15, fy = frac >> 4, sh = XG_BITDEPTH - 6, off = 1 << (sh - 1);
+    const xg_pix *s = src + (intptr_t)y * sp + x;
+    int v;
+    if (VARIANT == 0) v = (int)s[0] << (10 - XG_BITDEPTH);
+    else if (VARIANT == 1) v = ((int)s[0] * (16 - fx) + (int)s[1] * fx + off) >> sh;
+    else if (VARIANT == 2) v = ((int)s[0] * (16 - fy) + (int)s[sp] * fy + off) >> sh;
+    else {
+        const int t0 = (int16_t)(((int)s[0] * (16 - fx) + (int)s[1] * fx + off) >> sh);
+        const int t1 = (int16_t)(((int)s[sp] * (16 - fx) + (int)s[sp + 1] * fx + off) >> sh);
+        v = (t0 * (16 - fy) + t1 * fy + 8) >> 4;
+    }
+    dst[y * ow + x] = (int16_t)v;
+}
+
 /* bi average / BCW blend of intermediates (h266_luma_mc.c:561,595) */
 __global__ void k_interp_avg(const int16_t *a, const int16_t *b, xg_pix *dst, int n, int weighted, int wa, int wb)
 {
@@ -380,6 +404,33 @@ XG_INTERP_DEF(XinGpuChromaInterpVetU8S16, 4, 2, false, true, XG_PIXEL, int16_t)
 XG_INTERP_DEF(XinGpuChromaInterpHorVetU8S16, 4, 3, false, true, XG_PIXEL, int16_t)
 XG_INTERP_DEF(XinGpuChromaInterpVetS16U8, 4, 2, true, false, int16_t, XG_PIXEL)
 XG_INTERP_DEF(XinGpuChromaInterpVetS16S16, 4, 2, true, true, int16_t, int16_t)
+
+/* bilinear DMVR prediction, typedef XinBiliInterp, table entry pfXinBiliInterp
+ * (h266_encoder/include/h266_func_struct.h:150,741): writes h rows of w + 4
+ * samples; reads (w + 4 + hx) x (h + vy) samples from src */
+template <int VARIANT>
+static void xg_bili_call(const XG_PIXEL *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h)
+{
+    XG_BEGIN(t);
+    XG_ARG(src && dst && w >= 1 && h >= 1 && w <= 128 && h <= 128 && frac >= 0 && frac < 256 && ds >= (intptr_t)w + 4,
+           "bilinear interpolation: bad size, phase or pointer");
+    const size_t ww = w + 4 + (VARIANT & 1), hh = h + (VARIANT >> 1);
+    const xg_pix *d = (const xg_pix *)xg_stage_in(t, src, ss, ww, hh, sizeof(xg_pix)); XG_TRY(d);
+    int16_t *dout = (int16_t *)xg_dalloc(t, (size_t)(w + 4) * h * 2); XG_TRY(dout);
+    dim3 blk(32, 8), grd((w + 4 + 31) / 32, (h + 7) / 8);
+    k_bili<VARIANT><<<grd, blk, 0, t->stream>>>(d, (int)ww, dout, (int)w, (int)h, frac);
+    XG_TRY(xg_after_launch(t));
+    XG_TRY(xg_stage_out(t, dst, ds, dout, w + 4, h, 2) == 0);
+    XG_TRY(xg_sync(t) == 0);
+}
+#define XG_BILI_DEF(NAME, VAR)                                                                                   \
+    extern "C" void NAME(const XG_PIXEL *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w,  \
+                         uint32_t h)                                                                             \
+    { xg_bili_call<VAR>(src, ss, dst, ds, frac, w, h); }
+XG_BILI_DEF(XinGpuBiliInterpCopy, 0)
+XG_BILI_DEF(XinGpuBiliInterpHor, 1)
+XG_BILI_DEF(XinGpuBiliInterpVet, 2)
+XG_BILI_DEF(XinGpuBiliInterpHorVet, 3)
 
 static void xg_avg_call(const int16_t *a, intptr_t as, const int16_t *b, intptr_t bs, XG_PIXEL *dst, intptr_t ds, uint32_t w,
                         uint32_t h, int weighted, int wa, int wb)
