@@ -332,7 +332,10 @@ __global__ void k_dq_order(int njobs, const int32_t *__restrict__ first, const i
 /* ---- pass 3: the trellis.  One CTA = 4 warps x 8 quads; each warp takes the
  * next 8 blocks of the ordered list (so its quads walk the same number of
  * sub-blocks). */
-__global__ void __launch_bounds__(XG_DQ_THREADS)
+/* min blocks 1: the compiler keeps more of the step in registers (137 here),
+ * which shortens the serial step; the trellis is bound by that latency, not by
+ * the number of resident warps */
+__global__ void __launch_bounds__(XG_DQ_THREADS, 1)
 k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ counter, const int *__restrict__ counts,
      const int32_t *__restrict__ order, const int32_t *__restrict__ firsts, const uint32_t *__restrict__ soff,
      const xg_coef *__restrict__ tscan, xg_coef *__restrict__ qout, xg_coef *__restrict__ rout,
