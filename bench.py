@@ -39,17 +39,21 @@ W, H = 1920, 1080
 SEARCH = 64
 LEVELS = (64, 32, 16, 8)
 QPS = (27, 32, 37)
-LAMBDA = {27: 45, 32: 64, 37: 91}      # sad lambda per QP (fixed table for the synthetic run)
+LAMBDA = {27: 45, 32: 64, 37: 91}      # sad lambda per QP at 8-bit SAD scale (fixed table for the synthetic run)
+BD, IN_BD = 10, 8                      # the reference's 10-bit build on 8-bit pictures
+LAMBDA_BD = {k: v << (BD - IN_BD) for k, v in LAMBDA.items()}   # x4: the SAD scales with the samples
 NFRAMES = 30
 SEED = 1080
 ME_DRAM_BYTES = 5.260e6        # ncu: DRAM bytes of one k_me_tiles launch at this workload
 
 
 def workload_config():
-    return {"workload": "1080p single stream, 8-bit 4:2:0, low-delay P with the previous picture as reference, "
+    return {"workload": "1080p single stream, 8-bit 4:2:0 pictures coded at 10 bits (the reference's 10-bit build), "
+                        "low-delay P with the previous picture as reference, "
                         "exhaustive +-64 integer search + full sub-pel search, CU levels 64/32/16/8, DCT2 TU=CU, "
                         "QP 27/32/37 cycling, 30 synthetic pictures (seeded texture + 4 moving rectangles)",
-            "width": W, "height": H, "search_range": SEARCH, "levels": list(LEVELS), "frames": NFRAMES,
+            "width": W, "height": H, "input_bitdepth": IN_BD, "internal_bitdepth": BD, "search_range": SEARCH,
+            "levels": list(LEVELS), "frames": NFRAMES, "sad_lambda": LAMBDA_BD,
             "l2": "flushed between steps (512 MB write outside the timed events)"}
 
 
@@ -119,8 +123,8 @@ def cpu_sample(frames, seconds_target=15.0, threads=1):
     from tests import oracle_frame
     from xin26x_gb300.frame import CU_DTYPE  # noqa: F401
 
-    cur, ref = frames[1], frames[0]
-    o = O.oracle(8)
+    cur, ref = [tuple(p.astype(np.uint16) << (BD - IN_BD) for p in f) for f in (frames[1], frames[0])]
+    o = O.oracle(BD)
     ctus = [(x, y) for y in range(0, H - 63, 64) for x in range(0, W - 63, 64)]
     rng = np.random.default_rng(5)
     order = rng.permutation(len(ctus))
@@ -152,8 +156,8 @@ def cpu_sample(frames, seconds_target=15.0, threads=1):
                 k = order[idx[0]]
                 idx[0] += 1
             cx, cy = ctus[k]
-            oracle_frame.run(cur, ref, levels, search_range=SEARCH, qp=32, uv_qp=32, sad_lambda=LAMBDA[32],
-                             cus=cus_of_ctu(cx, cy))
+            oracle_frame.run(cur, ref, levels, search_range=SEARCH, qp=32, uv_qp=32, sad_lambda=LAMBDA_BD[32],
+                             bitdepth=BD, cus=cus_of_ctu(cx, cy))
             with lock:
                 done += 1
 
@@ -182,10 +186,10 @@ def run_reference(args):
     value = float(np.mean(vals))
     line = {"metric": "1080p VVC ME+TQ Mpixel/s", "value": value, "unit": "Mpixel/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": workload_config(),
+            "vs_baseline": None, "dtype": "u16", "data": "synthetic", "config": workload_config(),
             "cpu_baseline": {"value": value, "unit": "Mpixel/s", "cores": cores, "kind": "port",
                              "sample": "each step: as many 64x64 CTUs (all four CU levels, +-64 exhaustive search) as "
-                                       "finish in ~4 s on all host threads, oracle C restatement"},
+                                       "finish in ~4 s on all host threads, oracle C restatement (10-bit build)"},
             "e2e": {"value": value, "unit": "Mpixel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -223,7 +227,7 @@ def run_gpu(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    lib = _lib.load(8)
+    lib = _lib.load(BD)
     assert lib.xin_gpu_init(local) == 0
     frames = make_frames()
     npix = W * H
@@ -234,7 +238,7 @@ def run_gpu(args):
         dev.append(tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in (y, u, v)))
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
 
-    cfg = _lib.xin_gpu_stream_cfg(W, H, 64, SEARCH, sum(LEVELS), 0, 1, 1)
+    cfg = _lib.xin_gpu_stream_cfg(W, H, 64, SEARCH, sum(LEVELS), 0, 1, 1, IN_BD)
     h = C.c_void_p()
     assert lib.xin_gpu_stream_open(C.byref(cfg), C.byref(h)) == 0, lib.xin_gpu_last_error()
 
@@ -245,7 +249,7 @@ def run_gpu(args):
             pic.plane[i] = t.data_ptr()
             pic.stride[i] = t.shape[1]
         qp = QPS[k % 3]
-        pic.qp, pic.uv_qp, pic.sad_lambda = qp, qp, LAMBDA[qp]
+        pic.qp, pic.uv_qp, pic.sad_lambda = qp, qp, LAMBDA_BD[qp]
         assert lib.xin_gpu_frame_submit(h, C.byref(pic)) == 0, lib.xin_gpu_last_error()
 
     res = _lib.xin_gpu_results()
@@ -278,19 +282,23 @@ def run_gpu(args):
     value = whole_job_rate(npix * args.steps, world, total_ms * 1e-3) / 1e6
     stage /= args.steps
 
-    # roofline of the integer search kernel
+    # roofline of the integer search kernel: on 8-bit pictures it runs the packed
+    # 8-bit SAD (vabsdiff4.add), whose peak the 8-bit library's probe measures
+    lib8 = _lib.load(8)
+    assert lib8.xin_gpu_init(local) == 0
     peak = C.c_double()
-    lib.xin_gpu_measure_sad_peak(C.byref(peak))
+    lib8.xin_gpu_measure_sad_peak(C.byref(peak))
     algo = (W // 8) * (H // 8) * (2 * SEARCH + 1) ** 2 * 64      # abs differences per launch (8x8 SADs)
     me_ms = stage[1]
     achieved = algo / (me_ms * 1e-3)
     lib.xin_gpu_stream_close(h)
 
     # e2e through the public API with host buffers
-    e2e_fs = FrameStream(W, H, search_range=SEARCH, levels=LEVELS, out_q=True, out_rec=False, use_graph=True)
+    e2e_fs = FrameStream(W, H, search_range=SEARCH, levels=LEVELS, out_q=True, out_rec=False, use_graph=True,
+                         bitdepth=BD, input_bitdepth=IN_BD)
     cu_bytes = e2e_fs.ncus * 64
-    q_bytes = sum((W * H if p == 0 else W * H // 4) * len(LEVELS) * 2 for p in range(3))
-    e2e_fs.submit(*frames[0], qp=32, uv_qp=32, sad_lambda=LAMBDA[32])
+    q_bytes = sum((W * H if p == 0 else W * H // 4) * len(LEVELS) * 4 for p in range(3))
+    e2e_fs.submit(*frames[0], qp=32, uv_qp=32, sad_lambda=LAMBDA_BD[32])
     e2e_fs.wait()
     # two pictures in flight: picture k + 1 is submitted before picture k is collected, so
     # one picture's copies and host work overlap the other's kernels
@@ -299,7 +307,7 @@ def run_gpu(args):
     def e2e_submit(k):
         qp = QPS[k % 3]
         pending.append(time.perf_counter())
-        e2e_fs.submit(*frames[k % len(frames)], qp=qp, uv_qp=qp, sad_lambda=LAMBDA[qp])
+        e2e_fs.submit(*frames[k % len(frames)], qp=qp, uv_qp=qp, sad_lambda=LAMBDA_BD[qp])
 
     e2e_submit(1)
     for k in range(args.warmup):
@@ -318,10 +326,15 @@ def run_gpu(args):
     e2e_val = whole_job_rate(npix * args.steps, world, e2e_s) / 1e6
 
     # plain per-call form on a sample of CUs (one synchronous launch per reference call)
-    percall = percall_sample(lib, frames)
+    percall = percall_sample(lib, frames, bd=BD)
     kbatch = kernel_batch_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup) if rank == 0 else None
     dq = dep_quant_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup, cpu=(world == 1)) if rank == 0 else None
     wide = wide_search_bench(torch, flush) if rank == 0 else None
+    variants = None
+    if rank == 0:
+        nvar = max(5, min(args.steps, 20))
+        variants = {"eight_bit_build": pipeline_variant_bench(torch, flush, frames, nvar, args.warmup, 8, 0),
+                    "ten_bit_samples": pipeline_variant_bench(torch, flush, frames, nvar, args.warmup, 10, 0)}
     serving = None
     if rank == 0 and world == 1:
         from xin26x_gb300 import serve_bench
@@ -333,20 +346,22 @@ def run_gpu(args):
         if world == 1:
             v, n, el = cpu_sample(frames[:2], seconds_target=12.0, threads=1)
             cpu = {"value": v, "unit": "Mpixel/s", "cores": 1, "kind": "port",
-                   "sample": f"{n} random 64x64 CTUs (all four CU levels, +-64 exhaustive search), oracle C restatement, "
-                             f"1 thread, {el:.1f} s"}
+                   "sample": f"{n} random 64x64 CTUs (all four CU levels, +-64 exhaustive search), oracle C restatement "
+                             f"(10-bit build, pictures << 2), 1 thread, {el:.1f} s"}
         out = {"metric": "1080p VVC ME+TQ Mpixel/s", "value": value, "unit": "Mpixel/s", "n_gpus": world,
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
-               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
                "data": "synthetic (seeded texture + 4 moving rectangles, 1920x1080 4:2:0)",
                "config": workload_config(),
                "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_mc_tq": stage[2], "copies": stage[3]},
-               "roofline": {"bound": "int", "kernel": "k_me_tiles", "achieved": achieved / 1e12, "peak": peak.value / 1e12,
+               "roofline": {"bound": "int", "kernel": "k_me_tiles<8> (8-bit samples, SADs x 4)", "achieved": achieved / 1e12,
+                            "peak": peak.value / 1e12,
                             "unit": "Tabsdiff/s", "frac": achieved / peak.value, "traffic": ME_DRAM_BYTES,
                             "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_me_tiles launch "
                                               "(ncu, 1080p, +-64, cold cache); algorithmic bytes (current + "
                                               "reference luma) 4.15e6",
-                            "peak_source": "xin_gpu_measure_sad_peak: the faster of vabsdiff4+dp4a and vabsdiff4.add register loops on this GPU, this run",
+                            "peak_source": "xin_gpu_measure_sad_peak (8-bit library): the faster of vabsdiff4+dp4a and "
+                                           "vabsdiff4.add register loops on this GPU, this run",
                             "algorithmic": f"(W/8)(H/8)(2R+1)^2*64 = {algo:.4g} abs differences per launch"},
                "e2e": {"value": e2e_val, "unit": "Mpixel/s", "h2d_bytes_per_step": W * H * 3 // 2,
                        "d2h_bytes_per_step": cu_bytes + q_bytes, "pictures_in_flight": 2,
@@ -356,6 +371,7 @@ def run_gpu(args):
                "kernel_batch": kbatch,
                "dep_quant": dq,
                "wide_search_4k_10bit": wide,
+               "pipeline_variants_1080p": variants,
                "serving": serving,
                "gpu_launches": int(launches),
                "clocks": clk,
@@ -498,6 +514,54 @@ def dep_quant_bench(torch, flush, steps, warmup, nblocks=65536, seed=11, cpu=Tru
     return out
 
 
+def pipeline_variant_bench(torch, flush, frames, steps, warmup, bitdepth, input_bitdepth):
+    """The headline pictures through another build, for comparison: the 8-bit
+    library (8-bit arithmetic throughout), or the 10-bit library fed the pictures
+    as 10-bit samples (<< 2; the search then packs two samples a word instead of
+    four).  Device-resident pictures, device time per picture, L2 flushed."""
+    from xin26x_gb300 import _lib
+    lib = _lib.load(bitdepth)
+    assert lib.xin_gpu_init(torch.cuda.current_device()) == 0
+    if bitdepth == 8:
+        dev = [tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f) for f in frames]
+    else:
+        dev = [tuple((torch.from_numpy(np.ascontiguousarray(p)).cuda().to(torch.int32) << 2).to(torch.int16) for p in f)
+               for f in frames]
+    lam = LAMBDA if bitdepth == 8 else LAMBDA_BD
+    cfg = _lib.xin_gpu_stream_cfg(W, H, 64, SEARCH, sum(LEVELS), 0, 1, 1, input_bitdepth)
+    h = C.c_void_p()
+    assert lib.xin_gpu_stream_open(C.byref(cfg), C.byref(h)) == 0, lib.xin_gpu_last_error()
+    res = _lib.xin_gpu_results()
+
+    def submit(k):
+        pic = _lib.xin_gpu_picture()
+        for i, t in enumerate(dev[k % len(dev)]):
+            pic.plane[i] = t.data_ptr()
+            pic.stride[i] = t.shape[1]
+        qp = QPS[k % 3]
+        pic.qp, pic.uv_qp, pic.sad_lambda = qp, qp, lam[qp]
+        assert lib.xin_gpu_frame_submit(h, C.byref(pic)) == 0, lib.xin_gpu_last_error()
+        assert lib.xin_gpu_frame_wait(h, C.byref(res), -1) == 0, lib.xin_gpu_last_error()
+
+    for k in range(1 + max(3, warmup)):
+        submit(k)
+    ms, stage = [], np.zeros(4)
+    for k in range(steps):
+        flush.fill_(k & 255)
+        torch.cuda.synchronize()
+        submit(10 + k)
+        ms.append(res.gpu_ms)
+        st = (C.c_float * 4)()
+        lib.xin_gpu_stream_stage_ms(h, st)
+        stage += np.array(list(st))
+    lib.xin_gpu_stream_close(h)
+    stage /= steps
+    return {"library": f"{bitdepth}-bit", "pictures": "8-bit" if bitdepth == 8 else "10-bit samples (8-bit << 2)",
+            "value": W * H * steps / (float(np.sum(ms)) * 1e-3) / 1e6, "unit": "Mpixel/s",
+            "ms_per_picture": float(np.mean(ms)),
+            "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_mc_tq": stage[2], "copies": stage[3]}}
+
+
 def wide_search_bench(torch, flush, pictures=3):
     """3840x2160 10-bit 4:2:0, CTU 128, exhaustive +-256 integer search (the
     reference's maximum picture size and a wide search), full sub-pel search and
@@ -556,23 +620,26 @@ def _measured_peaks():
         return None
 
 
-def quant_params(qp, lg):
-    """Square-TU DCT2 quant parameters, 8-bit, P picture, no RDOQ (h266_trans_quant.c:107-120)."""
+def quant_params(qp, lg, bd=8):
+    """Square-TU DCT2 quant parameters, P picture, no RDOQ (h266_trans_quant.c:104-120):
+    the 10-bit build adds 12 to the QP."""
+    qp = qp + (12 if bd == 10 else 0)
     qm = (26214, 23302, 20560, 18396, 16384, 14564)[qp % 6]
     iqm = (40, 45, 51, 57, 64, 72)[qp % 6] << (qp // 6)
-    qs = 14 + 7 + qp // 6 - lg
-    iqs = 6 - 7 + lg
+    qs = 14 + (15 - bd) + qp // 6 - lg
+    iqs = 6 - (15 - bd) + lg
     return qm, 85 << (qs - 9), qs, iqm, 1 << (iqs - 1), iqs
 
 
-def percall_sample(lib, frames, seconds=6.0):
+def percall_sample(lib, frames, seconds=6.0, bd=8):
     """Plain per-call GPU form: the same CU hot path as ~20 synchronous per-call
     launches per CU (integer search, sub-pel search, luma and chroma MC, per plane
     residual, DCT2, quant, inverse DCT2, reconstruction) on a sample of CUs;
     Mpixel/s extrapolated per CU area."""
     from xin26x_gb300 import _lib
     from xin26x_gb300.synth import pad_plane
-    cur, ref = frames[1], frames[0]
+    pix_t, coef_t = (np.uint8, np.int16) if bd == 8 else (np.uint16, np.int32)
+    cur, ref = [tuple(p.astype(pix_t) << (bd - 8) for p in f) for f in (frames[1], frames[0])]
     pad = 80
     refp = [pad_plane(ref[0], pad), pad_plane(ref[1], pad // 2), pad_plane(ref[2], pad // 2)]
     rng = np.random.default_rng(3)
@@ -596,12 +663,12 @@ def percall_sample(lib, frames, seconds=6.0):
         me.bestCost = 0xFFFFFFFF
         me.minMv.mvX, me.minMv.mvY = -cx - 72, -cy - 72
         me.maxMv.mvX, me.maxMv.mvY = W + 72 - s - cx, H + 72 - s - cy
-        me.sadLambda = LAMBDA[32]
+        me.sadLambda = LAMBDA[32] << (bd - 8)
         lib.XinGpuMotionEstFull(C.byref(me))
         lib.XinGpuFullSubPelMe(C.byref(me))
         calls += 2
         mvx, mvy = me.bestMv.mvX * 4, me.bestMv.mvY * 4
-        pred = np.zeros((s, s), np.uint8)
+        pred = np.zeros((s, s), pix_t)
         ox, oy = cx * 16 + mvx, cy * 16 + mvy
         frac = ((oy & 15) << 4) | (ox & 15)
         src = P(refp[0], (pad + (oy >> 4)) * refp[0].shape[1] + pad + (ox >> 4))
@@ -609,16 +676,16 @@ def percall_sample(lib, frames, seconds=6.0):
             (1 if frac & 15 else 0) + (2 if frac >> 4 else 0)]
         fn(src, refp[0].shape[1], pred.ctypes.data, s, frac, s, s, 0)
         calls += 1
-        coef = np.zeros((s, s), np.int16)
-        t = np.zeros((s, s), np.int16)
-        q = np.zeros((s, s), np.int16)
-        r = np.zeros((s, s), np.int16)
-        rec = np.zeros((s, s), np.uint8)
+        coef = np.zeros((s, s), coef_t)
+        t = np.zeros((s, s), coef_t)
+        q = np.zeros((s, s), coef_t)
+        r = np.zeros((s, s), coef_t)
+        rec = np.zeros((s, s), pix_t)
         nz = np.zeros(1, np.uint64)
         for p in range(3):
             bs = s if p == 0 else s // 2
             if p:
-                pc = np.zeros((bs, bs), np.uint8)
+                pc = np.zeros((bs, bs), pix_t)
                 cfx, cfy = (cx * 16 + mvx) & 31, (cy * 16 + mvy) & 31
                 csrc = P(refp[p], (pad // 2 + ((cy * 16 + mvy) >> 5)) * refp[p].shape[1] + pad // 2 + ((cx * 16 + mvx) >> 5))
                 lib.XinGpuChromaInterpHorVet(csrc, refp[p].shape[1], pc.ctypes.data, bs, (cfy << 5) | cfx, bs, bs, 0)
@@ -628,12 +695,12 @@ def percall_sample(lib, frames, seconds=6.0):
                 pr, org = pred, inp
             lg = bs.bit_length() - 1
             lib.XinGpuBlockSubForDct(org.ctypes.data, bs, pr.ctypes.data, bs, coef.ctypes.data, bs, bs, bs)
-            lib.XinGpuFDct2WxH(coef.ctypes.data, bs, t.ctypes.data, bs, bs, bs, None, lg - 1, lg + 6)
+            lib.XinGpuFDct2WxH(coef.ctypes.data, bs, t.ctypes.data, bs, bs, bs, None, lg + bd - 9, lg + 6)
             k = min(bs, 32)
-            qm, qa, qs, iqm, iqa, iqs = quant_params(32, lg)
+            qm, qa, qs, iqm, iqa, iqs = quant_params(32, lg, bd)
             lib.XinGpuQuantInvQuant(q.ctypes.data, t.ctypes.data, r.ctypes.data, bs, k, k, 4, 4, qm, qa, qs, iqm, iqa, iqs,
                                     nz.ctypes.data)
-            lib.XinGpuIDct2WxH(r.ctypes.data, bs, coef.ctypes.data, bs, bs, bs, None, 7, 12)
+            lib.XinGpuIDct2WxH(r.ctypes.data, bs, coef.ctypes.data, bs, bs, bs, None, 7, 20 - bd)
             lib.XinGpuBlockAddForDct(coef.ctypes.data, bs, pr.ctypes.data, bs, rec.ctypes.data, bs, bs, bs)
             calls += 5
         _lib.check(lib, "per-call sample")
@@ -641,7 +708,8 @@ def percall_sample(lib, frames, seconds=6.0):
         ncu += 1
     el = time.perf_counter() - t0
     return {"value": pix / el / 1e6, "unit": "Mpixel/s", "cus": ncu, "calls": calls, "seconds": el,
-            "sample": "random CUs of the four levels (10/20/30/40 % of 64/32/16/8), ~20 synchronous C-ABI calls each"}
+            "sample": f"random CUs of the four levels (10/20/30/40 % of 64/32/16/8), ~20 synchronous C-ABI calls each, "
+                      f"{bd}-bit library"}
 
 
 def main():

@@ -366,6 +366,12 @@ typedef struct xin_gpu_stream_cfg {
     int32_t  device_io;          /* 1: picture planes are device pointers and results stay on the
                                     device (xin_gpu_stream_device_results); for callers whose
                                     pictures already live in GPU memory */
+    int32_t  input_bitdepth;     /* 0 (or the library's depth): planes of XG_PIXEL.  8 in the 10-bit
+                                    library: planes of 8-bit samples (uint8_t, cast to the plane
+                                    pointer type), coded at 10 bits as samples << 2 -- the
+                                    reference's 10-bit build on 8-bit input.  The integer search
+                                    then runs on the 8-bit samples with SADs x 4, which equals the
+                                    10-bit SAD of those samples. */
 } xin_gpu_stream_cfg;
 
 typedef struct xin_gpu_picture {

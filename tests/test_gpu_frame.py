@@ -145,3 +145,39 @@ def test_frame_two_in_flight_equals_one_at_a_time():
         assert np.array_equal(a["cu"], b["cu"])
         for p in range(3):
             assert np.array_equal(a["q"][p], b["q"][p]) and np.array_equal(a["rec"][p], b["rec"][p])
+
+
+@pytest.mark.parametrize("w,h,R,ctu", [(192, 128, 16, 64), (416, 240, 64, 64), (256, 136, 24, 128)])
+def test_frame_8bit_input_in_10bit_build(w, h, R, ctu):
+    """8-bit pictures into the 10-bit library (input_bitdepth 8: samples << 2, the
+    integer search on the 8-bit samples with SADs x 4) give exactly the results
+    of the same pictures shifted to 10 bits and fed as 10-bit samples (search on
+    10-bit words), and of the 10-bit oracle on those samples -- every CU, level,
+    coefficient plane and reconstructed plane; with and without graph capture."""
+    seq = synth.sequence(w, h, 3, seed=w + R, objects=2)
+    up = [tuple((p.astype(np.uint16) << 2) for p in f) for f in seq]
+    runs = []
+    for inb, frames, graph in ((8, seq, True), (0, up, True), (8, seq, False)):
+        fs = FrameStream(w, h, ctu=ctu, search_range=R, out_q=True, out_rec=True, bitdepth=10, input_bitdepth=inb,
+                         use_graph=graph)
+        res = []
+        try:
+            fs.submit(*frames[0], qp=32, uv_qp=32, sad_lambda=256)
+            fs.wait()
+            for k in (1, 2):
+                qp = 27 + 5 * k
+                fs.submit(*frames[k], qp=qp, uv_qp=qp + 1, sad_lambda=160 + 120 * k)
+                res.append(fs.wait())
+        finally:
+            fs.close()
+        runs.append(res)
+    for a, b in zip(runs[0], runs[1]):
+        assert np.array_equal(a["cu"], b["cu"])
+        for p in range(3):
+            assert np.array_equal(a["q"][p], b["q"][p]) and np.array_equal(a["rec"][p], b["rec"][p])
+    for a, b in zip(runs[0], runs[2]):
+        assert np.array_equal(a["cu"], b["cu"])
+    if R <= 24:
+        levels = FrameStream(w, h, ctu=ctu, search_range=R, bitdepth=10).levels
+        ref = oracle_frame.run(up[2], up[1], levels, ctu=ctu, search_range=R, qp=37, uv_qp=38, sad_lambda=400, bitdepth=10)
+        _compare(runs[0][1], ref, levels, ("8-bit input", w, h, R))

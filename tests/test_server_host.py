@@ -39,3 +39,24 @@ def test_footprint_arithmetic(bd):
     assert _fp(lib, 1920, 1080, ctu=32)[0] == -2
     assert _fp(lib, 1920, 1080, r=300)[0] == -2
     assert lib.xin_gpu_stream_footprint(None, None, None) == -2
+
+
+def test_footprint_8bit_input_into_10bit_build():
+    """input_bitdepth 8 in the 10-bit library: 8-bit device staging per picture set
+    and 1-byte host staging; the 8-bit library accepts 0 and 8 only."""
+    lib10, lib8 = _lib.load(10), _lib.load(8)
+
+    def fp(lib, inb, dio=0):
+        cfg = _lib.xin_gpu_stream_cfg(1920, 1080, 64, 64, 120, 0, 1, dio, inb)
+        d, hb = C.c_uint64(), C.c_uint64()
+        return lib.xin_gpu_stream_footprint(C.byref(cfg), C.byref(d), C.byref(hb)), d.value, hb.value
+
+    st, d0, h0 = fp(lib10, 0)
+    st8, d8, h8 = fp(lib10, 8)
+    assert st == 0 and st8 == 0
+    lq = 1920 * 1080
+    assert d8 - d0 == 2 * lq * 3 // 2
+    assert h0 - h8 == 2 * lq * 3 // 2
+    assert fp(lib10, 8, dio=1)[1] == fp(lib10, 0, dio=1)[1]
+    assert fp(lib10, 10)[0] == 0 and fp(lib10, 9)[0] == -2 and fp(lib10, 12)[0] == -2
+    assert fp(lib8, 8)[0] == 0 and fp(lib8, 0)[0] == 0 and fp(lib8, 10)[0] == -2

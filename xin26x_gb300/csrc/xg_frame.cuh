@@ -31,7 +31,8 @@ struct xin_gpu_stream {
         xg_coef *dq[3];
         xg_pix *drec[3];
         XgPicParams *dpp;
-        /* pinned host staging */
+        uint8_t *d_in8[3];     /* 8-bit input pictures (10-bit library, input_bitdepth 8): device staging */
+        /* pinned host staging (input samples of in_es bytes) */
         xg_pix *h_in[3];
         XgPicParams *h_pp;
         xin_gpu_cu_result *h_res;
@@ -49,6 +50,9 @@ struct xin_gpu_stream {
     cudaGraphExec_t gexec[2];
     int me_bands, me_band_rows, me_band_rows_alloc, me_row_words, me_nb;
     size_t me_smem;
+    int sbd;               /* sample depth the integer search runs at (8 or 10) */
+    bool widen;            /* 10-bit library fed 8-bit pictures: samples << 2 on the way in */
+    size_t in_es;          /* bytes per input sample */
     int nsub;              /* pictures submitted */
     int ndone;             /* pictures collected by frame_wait (the oldest first) */
     int graph_launches[2]; /* kernels inside each captured graph */
@@ -80,7 +84,7 @@ static int xg_stream_free(xin_gpu_stream *s)
     cudaFree(s->keys);
     for (auto &t : s->set) {
         cudaFree(t.dres); cudaFree(t.dpp);
-        for (int p = 0; p < 3; p++) { cudaFree(t.dq[p]); cudaFree(t.drec[p]); cudaFreeHost(t.h_in[p]); cudaFreeHost(t.h_q[p]); cudaFreeHost(t.h_rec[p]); }
+        for (int p = 0; p < 3; p++) { cudaFree(t.dq[p]); cudaFree(t.drec[p]); cudaFree(t.d_in8[p]); cudaFreeHost(t.h_in[p]); cudaFreeHost(t.h_q[p]); cudaFreeHost(t.h_rec[p]); }
         cudaFreeHost(t.h_pp); cudaFreeHost(t.h_res);
         for (int i = 0; i < 5; i++) if (t.evs[i]) cudaEventDestroy(t.evs[i]);
         if (t.ev0) cudaEventDestroy(t.ev0);
@@ -101,6 +105,17 @@ static int xg_stream_free(xin_gpu_stream *s)
     return XIN_GPU_OK;
 }
 
+/* input_bitdepth: 0 or the library's depth, or 8 in the 10-bit library */
+static bool xg_input_depth_ok(const xin_gpu_stream_cfg &c)
+{
+    return c.input_bitdepth == 0 || c.input_bitdepth == XG_BITDEPTH || (XG_BITDEPTH == 10 && c.input_bitdepth == 8);
+}
+/* bytes per input sample */
+static size_t xg_in_es(const xin_gpu_stream_cfg &c)
+{
+    return (XG_BITDEPTH == 10 && c.input_bitdepth == 8) ? 1 : sizeof(xg_pix);
+}
+
 extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream **out)
 {
     xin_gpu_clear_error();
@@ -110,13 +125,16 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     const xin_gpu_stream_cfg &c = *cfg;
     if (c.width < 16 || c.height < 16 || (c.width & 1) || (c.height & 1) || c.width > 8192 || c.height > 8192 ||
         (c.ctu_size != 64 && c.ctu_size != 128) || c.search_range < 1 || c.search_range > 256 ||
-        !(c.level_mask & (8u | 16u | 32u | 64u))) {
-        xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range or level mask");
+        !(c.level_mask & (8u | 16u | 32u | 64u)) || !xg_input_depth_ok(c)) {
+        xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range, level mask or input bit depth");
         return XIN_GPU_ERR_ARG;
     }
     xin_gpu_stream *s = new (std::nothrow) xin_gpu_stream();
     if (!s) { xg_set_error(XIN_GPU_ERR_NOMEM, "stream_open: host allocation"); return XIN_GPU_ERR_NOMEM; }
     s->cfg = c;
+    s->widen = XG_BITDEPTH == 10 && c.input_bitdepth == 8;
+    s->sbd = s->widen ? 8 : XG_BITDEPTH;
+    s->in_es = s->widen ? 1 : sizeof(xg_pix);
     /* margin: the reference pads ctu + 16; the tile search also reads R + 64 + 8 around full tiles */
     int pad = c.ctu_size + 16 > c.search_range + 72 ? c.ctu_size + 16 : c.search_range + 72;
     pad = (pad + 31) & ~31;
@@ -174,7 +192,8 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
             e = cudaMalloc(&t.dq[p], n * sizeof(xg_coef));
             if (e == cudaSuccess) e = cudaMalloc(&t.drec[p], n * sizeof(xg_pix));
             if (c.device_io) continue;
-            if (e == cudaSuccess) e = cudaMallocHost(&t.h_in[p], (p ? lc : lq) * sizeof(xg_pix));
+            if (e == cudaSuccess && s->widen) e = cudaMalloc(&t.d_in8[p], p ? lc : lq);
+            if (e == cudaSuccess) e = cudaMallocHost(&t.h_in[p], (p ? lc : lq) * s->in_es);
             if (e == cudaSuccess && (c.out_flags & XIN_GPU_OUT_Q)) e = cudaMallocHost(&t.h_q[p], n * sizeof(xg_coef));
             if (e == cudaSuccess && (c.out_flags & XIN_GPU_OUT_REC)) e = cudaMallocHost(&t.h_rec[p], n * sizeof(xg_pix));
         }
@@ -213,19 +232,20 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     if (bands > ndy) bands = ndy;
     {
         /* word positions per band row; pitch congruent to nx (mod 32) */
-        int nx = 2 * R + 1, relw = XG_ME_RELW(nx);
+        int nx = 2 * R + 1, relw = xg_me_relw(s->sbd, nx);
         s->me_row_words = relw + (((nx - relw) % 32) + 32) % 32;
     }
     for (;;) {
         s->me_band_rows = (ndy + bands - 1) / bands;
-        int rows_rounded = (s->me_band_rows + XG_ME_D - 1) / XG_ME_D * XG_ME_D;   /* rounded up to the per-lane chunk */
+        const int dr = xg_me_d(s->sbd);
+        int rows_rounded = (s->me_band_rows + dr - 1) / dr * dr;   /* rounded up to the per-lane chunk */
         s->me_band_rows_alloc = 64 + rows_rounded - 1;
-        size_t fixed = (size_t)s->me_band_rows_alloc * s->me_row_words + (2 * R + 1) + s->me_band_rows_alloc + XG_ME_CUR_WORDS;
+        size_t fixed = (size_t)s->me_band_rows_alloc * s->me_row_words + (2 * R + 1) + s->me_band_rows_alloc + xg_me_cur_words(s->sbd);
         s->me_nb = 0;
         for (int nb = XG_ME_NB_MAX; nb >= 1 && !s->me_nb; nb /= 2)
-            if (sizeof(uint32_t) * (fixed + XG_ME_AGG_WORDS(nb)) <= XG_ME_SMEM_MAX) s->me_nb = nb;
+            if (sizeof(uint32_t) * (fixed + xg_me_agg_words(s->sbd, nb)) <= XG_ME_SMEM_MAX) s->me_nb = nb;
         if (s->me_nb) {
-            s->me_smem = sizeof(uint32_t) * (fixed + XG_ME_AGG_WORDS(s->me_nb));
+            s->me_smem = sizeof(uint32_t) * (fixed + xg_me_agg_words(s->sbd, s->me_nb));
             break;
         }
         if (s->me_band_rows == 1) {
@@ -242,7 +262,11 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     static std::once_flag me_attr_once;
     static cudaError_t me_attr_err = cudaSuccess;
     std::call_once(me_attr_once, [] {
-        me_attr_err = cudaFuncSetAttribute(k_me_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, XG_ME_SMEM_MAX);
+        me_attr_err = cudaFuncSetAttribute(k_me_tiles<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, XG_ME_SMEM_MAX);
+#if XG_BITDEPTH == 10
+        if (me_attr_err == cudaSuccess)
+            me_attr_err = cudaFuncSetAttribute(k_me_tiles<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, XG_ME_SMEM_MAX);
+#endif
     });
     if (xg_cuda_check(me_attr_err, "me smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
     *out = s;
@@ -302,13 +326,23 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
     /* upload and pad the current picture; it becomes the next picture's reference */
     xg_stage_event(t.evs[0], st, capturing);
     cudaMemcpyAsync(t.dpp, t.h_pp, sizeof(XgPicParams), cudaMemcpyHostToDevice, st);
-    if (c.device_io) {
+    if (s->widen) {
+        /* 8-bit samples into the 10-bit slot (<< 2) */
+        if (!c.device_io)
+            for (int p = 0; p < 3; p++) {
+                const XgPlane &pl = s->slot[cur][p];
+                cudaMemcpyAsync(t.d_in8[p], t.h_in[p], (size_t)pl.w * pl.h, cudaMemcpyHostToDevice, st);
+            }
+        k_copy_in8<<<152 * 4, 256, 0, st>>>(s->slot[cur][0], s->slot[cur][1], s->slot[cur][2], t.dpp, t.d_in8[0], t.d_in8[1],
+                                            t.d_in8[2], c.device_io ? 0 : 1);
+        nl++;
+    } else if (c.device_io) {
         k_copy_in<<<152 * 4, 256, 0, st>>>(s->slot[cur][0], s->slot[cur][1], s->slot[cur][2], t.dpp);
         nl++;
     }
     for (int p = 0; p < 3; p++) {
         XgPlane &pl = s->slot[cur][p];
-        if (!c.device_io)
+        if (!c.device_io && !s->widen)
             cudaMemcpy2DAsync(pl.data, (size_t)pl.pitch * sizeof(xg_pix), t.h_in[p], (size_t)pl.w * sizeof(xg_pix),
                               (size_t)pl.w * sizeof(xg_pix), pl.h, cudaMemcpyHostToDevice, st);
         k_pad<<<152 * 4, 256, 0, st>>>(pl);
@@ -332,7 +366,11 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             mp.cus_x[L] = s->lev_cx[L];
         }
         dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, s->me_bands);
-        k_me_tiles<<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, t.dpp);
+#if XG_BITDEPTH == 10
+        if (s->sbd == 10) k_me_tiles<10><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, t.dpp);
+        else
+#endif
+            k_me_tiles<8><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, t.dpp);
         nl++;
         nl += xg_enqueue_qpel(s, cur);
         xg_stage_event(t.evs[2], st, capturing);
@@ -435,8 +473,9 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
             pp.src_stride[p] = pic->stride[p];
             continue;
         }
+        const size_t es = s->in_es;
         for (int y = 0; y < h; y++)
-            memcpy(t.h_in[p] + (size_t)y * w, pic->plane[p] + (size_t)y * pic->stride[p], (size_t)w * sizeof(xg_pix));
+            memcpy((char *)t.h_in[p] + (size_t)y * w * es, (const char *)pic->plane[p] + (size_t)y * pic->stride[p] * es, (size_t)w * es);
     }
     pp.lambda = pic->sad_lambda;
     for (int L = 0; L < 4; L++) {

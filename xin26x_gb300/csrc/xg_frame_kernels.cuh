@@ -149,6 +149,24 @@ __global__ void k_copy_in(XgPlane y, XgPlane u, XgPlane v, const XgPicParams *pp
     }
 }
 
+/* 8-bit pictures into the 10-bit library's padded slot, samples << 2: from the
+ * per-set device staging (staged = 1) or from the caller's device planes in the
+ * picture parameters (device_io streams; 8-bit samples) */
+__global__ void k_copy_in8(XgPlane y, XgPlane u, XgPlane v, const XgPicParams *pp, const uint8_t *s0, const uint8_t *s1,
+                           const uint8_t *s2, int staged)
+{
+    const int ny = y.w * y.h, nc = u.w * u.h;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ny + 2 * nc; i += gridDim.x * blockDim.x) {
+        int pl = 0, k = i;
+        if (i >= ny) { k = i - ny; pl = k < nc ? 1 : 2; k -= (pl - 1) * nc; }
+        XgPlane &d = pl == 0 ? y : pl == 1 ? u : v;
+        const int row = k / d.w, col = k % d.w;
+        const uint8_t *src = staged ? (pl == 0 ? s0 : pl == 1 ? s1 : s2) : reinterpret_cast<const uint8_t *>(pp->src[pl]);
+        const long long stride = staged ? d.w : pp->src_stride[pl];
+        d.data[(intptr_t)row * d.pitch + col] = (xg_pix)((unsigned)src[(intptr_t)row * stride + col] << (XG_BITDEPTH - 8));
+    }
+}
+
 /* packed 8-bit SAD throughput probe: vabsdiff4 + dp4a on register data */
 __global__ void k_sad_peak(const uint32_t *in, uint32_t *out, int iters)
 {
@@ -261,26 +279,34 @@ __device__ __forceinline__ uint32_t xg_absdiff2_biased(uint32_t a, uint32_t an, 
 }
 #define XG_NEG2(x) (0x04000400u - (x))
 
-/* word positions per staged band row: the last word a warp reads starts at
- * 48 + (2R) + 12 (8-bit, 4 pixels a word) or 48 + (2R) + 14 (10-bit, 2 pixels) */
-#define XG_ME_RELW(nx) ((nx) + (XG_BITDEPTH == 8 ? 60 : 62))
-#define XG_ME_CUR_WORDS (XG_BITDEPTH == 8 ? 64 * 16 : 64 * 32)   /* the current 64x64 tile in shared memory */
-/* candidate rows per lane and pass, and the key bits that hold the row: 8-bit 8
- * rows (the register window of current rows is 4 words a row), 10-bit 4 (8
+/* Search geometry by the sample depth the search runs at (sbd): 8 = four
+ * pixels a word, 10 = two.  The 10-bit library also runs the 8-bit form on
+ * pictures that arrive as 8-bit samples (input_bitdepth 8): it packs the
+ * 10-bit samples >> 2 and scales every SAD by 4, which is the 10-bit SAD of
+ * samples that are multiples of 4.
+ * Word positions per staged band row: the last word a warp reads starts at
+ * 48 + (2R) + 12 (sbd 8) or 48 + (2R) + 14 (sbd 10). */
+__host__ __device__ constexpr int xg_me_relw(int sbd, int nx) { return nx + (sbd == 8 ? 60 : 62); }
+/* the current 64x64 tile in shared memory */
+__host__ __device__ constexpr int xg_me_cur_words(int sbd) { return sbd == 8 ? 64 * 16 : 64 * 32; }
+/* candidate rows per lane and pass, and the key bits that hold the row: sbd 8
+ * 8 rows (the register window of current rows is 4 words a row), sbd 10 4 (8
  * words a row plus their negations) */
-#define XG_ME_D (XG_BITDEPTH == 8 ? 8 : 4)
-#define XG_ME_DB (XG_BITDEPTH == 8 ? 3 : 2)
+__host__ __device__ constexpr int xg_me_d(int sbd) { return sbd == 8 ? 8 : 4; }
+__host__ __device__ constexpr int xg_me_db(int sbd) { return sbd == 8 ? 3 : 2; }
 /* keys at or above this are not candidates (padding rows, windows) */
 #define XG_ME_KEY_INVALID 0xC0000000u
-#define XG_ME_SLOTS (32 * XG_ME_D)        /* candidates per warp and pass */
 #define XG_ME_SMEM_MAX (216 * 1024)       /* dynamic shared memory of k_me_tiles, under the 227 KB a CTA may have */
 #define XG_ME_NB_MAX 4                    /* passes buffered between 64x64 updates (at most) */
-/* 16x16 SADs [2][16][SLOTS] (double-buffered per pass) + 32x32 SADs [2][nb][4][SLOTS] */
-#define XG_ME_AGG_WORDS(nb) ((2 * 16 + 2 * (nb) * 4) * XG_ME_SLOTS)
-static_assert(XG_ME_D % 4 == 0 && (1 << XG_ME_DB) == XG_ME_D,
-              "the 32x32 exchange gives each of a quadrant's four warps XG_ME_D / 4 candidate rows");
+/* 16x16 SADs [2][16][slots] (double-buffered per pass) + 32x32 SADs [2][nb][4][slots], slots = 32 x rows */
+__host__ __device__ constexpr int xg_me_agg_words(int sbd, int nb) { return (2 * 16 + 2 * nb * 4) * 32 * xg_me_d(sbd); }
+static_assert(xg_me_d(8) % 4 == 0 && (1 << xg_me_db(8)) == xg_me_d(8) && xg_me_d(10) % 4 == 0 && (1 << xg_me_db(10)) == xg_me_d(10),
+              "the 32x32 exchange gives each of a quadrant's four warps rows / 4 candidate rows");
+template <int SBD>
 __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, const XgPicParams *pp)
 {
+    constexpr int XG_ME_D = xg_me_d(SBD), XG_ME_DB = xg_me_db(SBD), XG_ME_SLOTS = 32 * XG_ME_D;
+    constexpr int SH = XG_BITDEPTH - SBD;  /* sample shift to the search depth; the SADs scale back by 1 << SH */
     extern __shared__ uint32_t sm[];
     __shared__ int swin[16][5][4];        /* per warp: windows of its four 8x8 CUs and its 16x16 CU */
     __shared__ int swin32[4][4], swin64[4];
@@ -294,8 +320,8 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     const int nv = nch * nx;                                 /* (chunk, column) slots, one per lane and pass */
     const int rows = XG_ME_TILE + nch * XG_ME_D - 1;         /* band rows staged */
 
-    const int relw = XG_ME_RELW(nx);                         /* word positions read per band row */
-    uint32_t *refw = sm + XG_ME_CUR_WORDS;                   /* [rows][row_words] */
+    const int relw = xg_me_relw(SBD, nx);                         /* word positions read per band row */
+    uint32_t *refw = sm + xg_me_cur_words(SBD);                   /* [rows][row_words] */
     uint32_t *mvcx = refw + (size_t)p.band_rows_alloc * p.row_words; /* [nx] */
     uint32_t *mvcy = mvcx + nx;                              /* [band_rows rounded to XG_ME_D] */
     const int nb = p.agg_passes;
@@ -309,11 +335,11 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     for (int i = threadIdx.x; i < rows * relw; i += blockDim.x) {
         int r = i / relw, x = i - r * relw;
         const xg_pix *src = p.ref.data + (intptr_t)(Y0 + r) * p.ref.pitch + X0 + x;
-#if XG_BITDEPTH == 8
-        refw[r * p.row_words + x] = (uint32_t)src[0] | ((uint32_t)src[1] << 8) | ((uint32_t)src[2] << 16) | ((uint32_t)src[3] << 24);
-#else
-        refw[r * p.row_words + x] = (uint32_t)src[0] | ((uint32_t)src[1] << 16);
-#endif
+        if constexpr (SBD == 8)
+            refw[r * p.row_words + x] = (uint32_t)(src[0] >> SH) | ((uint32_t)(src[1] >> SH) << 8) |
+                                        ((uint32_t)(src[2] >> SH) << 16) | ((uint32_t)(src[3] >> SH) << 24);
+        else
+            refw[r * p.row_words + x] = (uint32_t)src[0] | ((uint32_t)src[1] << 16);
     }
     const uint32_t lambda = pp->lambda;
     for (int i = threadIdx.x; i < nx; i += blockDim.x) mvcx[i] = xg_mvd_bits(4 * (i - p.R)) * lambda;
@@ -325,17 +351,18 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
 
     /* ---- the current tile in shared memory (read as broadcasts) */
     const int bx = (warp & 3) * 16, by = (warp >> 2) * 16;
-#if XG_BITDEPTH == 8
-    for (int i = threadIdx.x; i < 64 * 16; i += blockDim.x) {
-        const xg_pix *c = p.cur.data + (intptr_t)(ty0 + (i >> 4)) * p.cur.pitch + tx0 + 4 * (i & 15);
-        scur[i] = (uint32_t)c[0] | ((uint32_t)c[1] << 8) | ((uint32_t)c[2] << 16) | ((uint32_t)c[3] << 24);
+    if constexpr (SBD == 8) {
+        for (int i = threadIdx.x; i < 64 * 16; i += blockDim.x) {
+            const xg_pix *c = p.cur.data + (intptr_t)(ty0 + (i >> 4)) * p.cur.pitch + tx0 + 4 * (i & 15);
+            scur[i] = (uint32_t)(c[0] >> SH) | ((uint32_t)(c[1] >> SH) << 8) | ((uint32_t)(c[2] >> SH) << 16) |
+                      ((uint32_t)(c[3] >> SH) << 24);
+        }
+    } else {
+        for (int i = threadIdx.x; i < 64 * 32; i += blockDim.x) {
+            const xg_pix *c = p.cur.data + (intptr_t)(ty0 + (i >> 5)) * p.cur.pitch + tx0 + 2 * (i & 31);
+            scur[i] = (uint32_t)c[0] | ((uint32_t)c[1] << 16);
+        }
     }
-#else
-    for (int i = threadIdx.x; i < 64 * 32; i += blockDim.x) {
-        const xg_pix *c = p.cur.data + (intptr_t)(ty0 + (i >> 5)) * p.cur.pitch + tx0 + 2 * (i & 31);
-        scur[i] = (uint32_t)c[0] | ((uint32_t)c[1] << 16);
-    }
-#endif
 
     /* ---- windows and liveness of this warp's CUs; a band inside every window needs no per-candidate check */
     bool live[5];
@@ -387,7 +414,7 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
 #pragma unroll
                 for (int b = 0; b < 4; b++) acc[d][b] = 0;
             /* reference row t of the block feeds current row t - d of candidate row d */
-#if XG_BITDEPTH == 8
+            if constexpr (SBD == 8) {
             uint32_t cw[XG_ME_D][4];          /* current rows t .. t-XG_ME_D+1 (slot = row % XG_ME_D) */
             const uint32_t *crow = scur + by * 16 + (bx >> 2);
 #pragma unroll
@@ -411,7 +438,14 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                     }
                 }
             }
-#else
+            /* 8-bit samples of 10-bit pictures: the 10-bit SAD is four times the 8-bit one */
+            if constexpr (SH > 0) {
+#pragma unroll
+                for (int d = 0; d < XG_ME_D; d++)
+#pragma unroll
+                    for (int b = 0; b < 4; b++) acc[d][b] <<= SH;
+            }
+            } else {
             uint32_t cw[XG_ME_D][8], cn[XG_ME_D][8];   /* current rows t .. t-XG_ME_D+1 (slot = row % XG_ME_D), negated */
             const uint32_t *crow = scur + by * 32 + (bx >> 1);
 #pragma unroll
@@ -445,7 +479,7 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
             for (int d = 0; d < XG_ME_D; d++)
 #pragma unroll
                 for (int b = 0; b < 4; b++) acc[d][b] = (acc[d][b] & 0xffffu) + (acc[d][b] >> 16) - 64u * 1024u;
-#endif
+            }
             /* Per CU, the best of the lane's XG_ME_D candidates (same column, rows
              * row0 + d: raster order = d order) as one key (cost << XG_ME_DB) | d, then
              * a (cost, raster index) compare with the lane's running best.  Keys of
@@ -475,11 +509,11 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                     }
                 }
                 /* the minimum of the keys with three-input minima */
-#if XG_ME_D == 8
-                const uint32_t k = min(__vimin3_u32(kd[0], kd[1], kd[2]), __vimin3_u32(__vimin3_u32(kd[3], kd[4], kd[5]), kd[6], kd[7]));
-#else
-                const uint32_t k = min(__vimin3_u32(kd[0], kd[1], kd[2]), kd[3]);
-#endif
+                uint32_t k;
+                if constexpr (XG_ME_D == 8)
+                    k = min(__vimin3_u32(kd[0], kd[1], kd[2]), __vimin3_u32(__vimin3_u32(kd[3], kd[4], kd[5]), kd[6], kd[7]));
+                else
+                    k = min(__vimin3_u32(kd[0], kd[1], kd[2]), kd[3]);
                 const uint32_t cost = k >> XG_ME_DB, gidx = gidx0 + (k & (XG_ME_D - 1)) * (uint32_t)nx;
                 if (live[c] && k < XG_ME_KEY_INVALID && (cost < best[c] || (cost == best[c] && gidx < bidx[c]))) { best[c] = cost; bidx[c] = gidx; }
             }

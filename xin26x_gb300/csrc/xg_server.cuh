@@ -28,8 +28,10 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
 {
     if (c->width < 16 || c->height < 16 || (c->width & 1) || (c->height & 1) || c->width > 8192 || c->height > 8192 ||
         (c->ctu_size != 64 && c->ctu_size != 128) || c->search_range < 1 || c->search_range > 256 ||
-        !(c->level_mask & (8u | 16u | 32u | 64u)))
+        !(c->level_mask & (8u | 16u | 32u | 64u)) || !xg_input_depth_ok(*c))
         return XIN_GPU_ERR_ARG;
+    const bool widen = XG_BITDEPTH == 10 && c->input_bitdepth == 8;
+    const uint64_t in_es = widen ? 1 : sizeof(xg_pix);
     int pad = c->ctu_size + 16 > c->search_range + 72 ? c->ctu_size + 16 : c->search_range + 72;
     pad = (pad + 31) & ~31;
     uint64_t pitch = ((c->width + 2 * pad) + 127) & ~127, rows = c->height + 2 * pad;
@@ -47,9 +49,10 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
      * picture sets (results, parameters, pinned staging) */
     uint64_t d = 2 * (ysz + 2 * csz) + 2 * 16 * ysz + 8 * (ncus ? ncus : 1) +
                  2 * (sizeof(xin_gpu_cu_result) * ncus + sizeof(XgPicParams) + (lq + 2 * lc) * nlev * (sizeof(xg_coef) + sizeof(xg_pix)));
+    if (widen && !c->device_io) d += 2 * (lq + 2 * lc);     /* 8-bit device staging per set */
     uint64_t h = sizeof(XgPicParams) + sizeof(xin_gpu_cu_result) * ncus;
     if (!c->device_io) {
-        h += (lq + 2 * lc) * sizeof(xg_pix);
+        h += (lq + 2 * lc) * in_es;
         if (c->out_flags & XIN_GPU_OUT_Q) h += (lq + 2 * lc) * nlev * sizeof(xg_coef);
         if (c->out_flags & XIN_GPU_OUT_REC) h += (lq + 2 * lc) * nlev * sizeof(xg_pix);
     }
@@ -80,7 +83,7 @@ struct XgSrvPic {
     int32_t qp, uv_qp;
     uint32_t lambda;
     double t_submit, t_launch;
-    std::vector<xg_pix> pix;      /* Y, U, V packed (stride = width) */
+    std::vector<uint8_t> pix;     /* Y, U, V packed (stride = width), input samples */
 };
 
 struct XgSrvStream {
@@ -234,9 +237,10 @@ static void xg_srv_loop(xin_gpu_server *v)
             xin_gpu_picture pic;
             memset(&pic, 0, sizeof pic);
             const int w = best->cfg.width, h = best->cfg.height;
-            pic.plane[0] = p->pix.data();
-            pic.plane[1] = p->pix.data() + (size_t)w * h;
-            pic.plane[2] = p->pix.data() + (size_t)w * h + (size_t)(w / 2) * (h / 2);
+            const size_t es = xg_in_es(best->cfg);
+            pic.plane[0] = (const XG_PIXEL *)p->pix.data();
+            pic.plane[1] = (const XG_PIXEL *)(p->pix.data() + (size_t)w * h * es);
+            pic.plane[2] = (const XG_PIXEL *)(p->pix.data() + ((size_t)w * h + (size_t)(w / 2) * (h / 2)) * es);
             pic.stride[0] = w; pic.stride[1] = pic.stride[2] = w / 2;
             pic.qp = p->qp; pic.uv_qp = p->uv_qp; pic.sad_lambda = p->lambda;
             lk.unlock();
@@ -358,6 +362,7 @@ extern "C" int xin_gpu_server_submit(xin_gpu_server *v, int32_t stream_id, const
     }
     XgSrvPic *p = nullptr;
     int w, h;
+    size_t es;
     {
         std::lock_guard<std::mutex> lk(v->mu);
         auto it = v->streams.find(stream_id);
@@ -376,6 +381,7 @@ extern "C" int xin_gpu_server_submit(xin_gpu_server *v, int32_t stream_id, const
             return XIN_GPU_ERR_ARG;
         }
         w = t->cfg.width; h = t->cfg.height;
+        es = xg_in_es(t->cfg);
         if (!t->spare.empty()) { p = t->spare.back(); t->spare.pop_back(); }
     }
     for (int k = 0; k < 3; k++)
@@ -387,12 +393,13 @@ extern "C" int xin_gpu_server_submit(xin_gpu_server *v, int32_t stream_id, const
     if (!p) p = new XgSrvPic();
     /* copy the picture so that the caller's buffers are free on return */
     size_t lq = (size_t)w * h, lc = lq / 4;
-    p->pix.resize(lq + 2 * lc);
-    for (int y = 0; y < h; y++) memcpy(p->pix.data() + (size_t)y * w, pic->plane[0] + (size_t)y * pic->stride[0], w * sizeof(xg_pix));
+    p->pix.resize((lq + 2 * lc) * es);
+    for (int y = 0; y < h; y++)
+        memcpy(p->pix.data() + (size_t)y * w * es, (const char *)pic->plane[0] + (size_t)y * pic->stride[0] * es, w * es);
     for (int k = 1; k < 3; k++)
         for (int y = 0; y < h / 2; y++)
-            memcpy(p->pix.data() + lq + (k - 1) * lc + (size_t)y * (w / 2), pic->plane[k] + (size_t)y * pic->stride[k],
-                   (w / 2) * sizeof(xg_pix));
+            memcpy(p->pix.data() + (lq + (k - 1) * lc + (size_t)y * (w / 2)) * es,
+                   (const char *)pic->plane[k] + (size_t)y * pic->stride[k] * es, (w / 2) * es);
     p->tag = user_tag;
     p->cu_out = cu_out;
     p->qp = pic->qp; p->uv_qp = pic->uv_qp; p->lambda = pic->sad_lambda;

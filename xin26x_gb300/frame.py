@@ -22,9 +22,12 @@ OUT_Q, OUT_REC = 1, 2
 class FrameStream:
     def __init__(self, width: int, height: int, ctu: int = 64, search_range: int = 64,
                  levels=(64, 32, 16, 8), out_q: bool = True, out_rec: bool = False, use_graph: bool = True,
-                 bitdepth: int = 8, device: int = 0):
+                 bitdepth: int = 8, device: int = 0, input_bitdepth: int = 0):
+        """bitdepth: the library (8 or 10, the reference's ENABLE_10BIT_ENCODER);
+        input_bitdepth 8 with bitdepth 10: 8-bit pictures coded at 10 bits."""
         self.lib = _lib.load(bitdepth)
         self.bitdepth = bitdepth
+        self.in_pix = np.uint8 if (bitdepth == 8 or input_bitdepth == 8) else np.uint16
         self.pix = np.uint8 if bitdepth == 8 else np.uint16
         self.coef = np.int16 if bitdepth == 8 else np.int32
         if self.lib.xin_gpu_init(device) != 0:
@@ -33,7 +36,8 @@ class FrameStream:
         for s in levels:
             mask |= int(s)
         self.cfg = _lib.xin_gpu_stream_cfg(width, height, ctu, search_range, mask,
-                                           (OUT_Q if out_q else 0) | (OUT_REC if out_rec else 0), 1 if use_graph else 0)
+                                           (OUT_Q if out_q else 0) | (OUT_REC if out_rec else 0), 1 if use_graph else 0,
+                                           0, input_bitdepth)
         h = C.c_void_p()
         st = self.lib.xin_gpu_stream_open(C.byref(self.cfg), C.byref(h))
         if st != 0:
@@ -49,7 +53,7 @@ class FrameStream:
         self.out_q, self.out_rec = out_q, out_rec
 
     def submit(self, y, u, v, qp: int = 32, uv_qp: int = 32, sad_lambda: int = 64) -> None:
-        planes = [np.ascontiguousarray(p, dtype=self.pix) for p in (y, u, v)]
+        planes = [np.ascontiguousarray(p, dtype=self.in_pix) for p in (y, u, v)]
         pic = _lib.xin_gpu_picture()
         for i, p in enumerate(planes):
             pic.plane[i] = p.ctypes.data

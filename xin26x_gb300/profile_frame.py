@@ -3,7 +3,9 @@ times -- the driver for profiling (ncu) and quick timing of the kernels.
 
     python -m xin26x_gb300.profile_frame [--frames 6] [--width 1920] [--height 1080]
                                          [--search 64] [--bitdepth 8] [--ctu 64]
-                                         [--objects 4] [--octaves 1]
+                                         [--objects 4] [--octaves 1] [--input-bitdepth 0]
+
+--bitdepth 10 --input-bitdepth 8: 8-bit pictures coded by the 10-bit library.
 """
 from __future__ import annotations
 
@@ -27,15 +29,16 @@ def main():
     ap.add_argument("--ctu", type=int, default=64)
     ap.add_argument("--objects", type=int, default=4)
     ap.add_argument("--octaves", type=int, default=1)
+    ap.add_argument("--input-bitdepth", type=int, default=0)
     a = ap.parse_args()
     import torch
     lib = _lib.load(a.bitdepth)
     assert lib.xin_gpu_init(0) == 0
-    seq = synth.sequence(a.width, a.height, min(a.frames, 8), seed=1080, bitdepth=a.bitdepth, objects=a.objects,
-                         octaves=a.octaves)
+    seq = synth.sequence(a.width, a.height, min(a.frames, 8), seed=1080, bitdepth=a.input_bitdepth or a.bitdepth,
+                         objects=a.objects, octaves=a.octaves)
     dev = [tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f) for f in seq]
     mask = sum(int(s) for s in a.levels.split(","))
-    cfg = _lib.xin_gpu_stream_cfg(a.width, a.height, a.ctu, a.search, mask, 0, 1, 1)
+    cfg = _lib.xin_gpu_stream_cfg(a.width, a.height, a.ctu, a.search, mask, 0, 1, 1, a.input_bitdepth)
     h = C.c_void_p()
     if lib.xin_gpu_stream_open(C.byref(cfg), C.byref(h)) != 0:
         raise RuntimeError(lib.xin_gpu_last_error().decode())
@@ -47,7 +50,7 @@ def main():
             pic.plane[i] = t.data_ptr()
             pic.stride[i] = t.shape[1]
         pic.qp = pic.uv_qp = 32
-        pic.sad_lambda = 64
+        pic.sad_lambda = 64 if a.bitdepth == 8 else 256
         assert lib.xin_gpu_frame_submit(h, C.byref(pic)) == 0, lib.xin_gpu_last_error()
         assert lib.xin_gpu_frame_wait(h, C.byref(res), -1) == 0, lib.xin_gpu_last_error()
         if k:
@@ -57,6 +60,7 @@ def main():
     lib.xin_gpu_stream_close(h)
     s = np.array(stages)
     print(json.dumps({"frames": a.frames, "size": [a.width, a.height], "search": a.search, "bitdepth": a.bitdepth,
+                      "input_bitdepth": a.input_bitdepth or a.bitdepth,
                       "ctu": a.ctu, "mpix_s": a.width * a.height / float(np.median(s[:, 4])) / 1e3,
                       "ms": {"prep": float(np.median(s[:, 0])), "integer_search": float(np.median(s[:, 1])),
                              "subpel_mc_tq": float(np.median(s[:, 2])), "copies": float(np.median(s[:, 3])),
