@@ -164,8 +164,14 @@ static void xg_dq_init_tables(void)
             }
             int ptype = (in == 15 && k > 16 && k < n - 1) ? 1 : (in == 0 && k > 0 && k < n - 16) ? 2 : 0;
             int braster = gy[k >> 4] * ws + gx[k >> 4];
+            /* significance / gtx context offsets of the position's diagonal, luma and chroma
+             * (h266_dep_quant.c:466-476): luma sig 0/4/8, gtx 1/6/11/16; chroma sig 0/4, gtx 1/6 */
+            const int dg = px[k] + py[k];
+            const uint32_t ls = dg < 2 ? 2 : dg < 5 ? 1 : 0, lg = dg < 1 ? 3 : dg < 3 ? 2 : dg < 10 ? 1 : 0;
+            const uint32_t cs = dg < 2 ? 1 : 0, cg = dg < 1 ? 1 : 0;
             uint2 e;
-            e.x = (uint32_t)px[k] | (uint32_t)py[k] << 5 | (uint32_t)ptype << 10 | (uint32_t)ni << 12 | (uint32_t)braster << 15;
+            e.x = (uint32_t)px[k] | (uint32_t)py[k] << 5 | (uint32_t)ptype << 10 | (uint32_t)ni << 12 | (uint32_t)braster << 15 |
+                  ls << 21 | lg << 23 | cs << 25 | cg << 26;
             e.y = 0;
             for (int j = 0; j < ni; j++) e.y |= (uint32_t)ins[j] << (4 * j);
             step.push_back(e);
@@ -243,11 +249,14 @@ __global__ void k_dq_rates(const xin_gpu_prob *__restrict__ sets, XgDqRates *__r
 
 /* ------------------------------------------------------------------ trellis */
 
-struct XgDqQuad {
+/* 16-byte aligned: the ring is written with 16-byte stores */
+struct __align__(16) XgDqQuad {
     uint16_t tpl[4][16];            /* outside-neighbour template per sub-block context */
     uint32_t ring[16][4][4];        /* levels of earlier sub-blocks: [slot][state][16 bytes] */
     int32_t  last[2][32];           /* rate of the last position, x and y */
+    XgDqRates rt;                   /* the block's rate tables (its context set and channel) */
 };
+static_assert(sizeof(XgDqQuad) % 16 == 0 && offsetof(XgDqQuad, ring) % 16 == 0, "ring rows must stay 16-byte aligned");
 struct XgDqSmem {
     XgDqQuad quad[XG_DQ_QUADS];
     int32_t  rice[4][32];           /* abs_remainder bits, Rice parameter k, value n */
@@ -415,6 +424,11 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
                 Q.last[xy][p] = (int32_t)cbits;
             }
         }
+        if (has) {
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(RT);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&Q.rt);
+            for (int i = s; i < (int)(sizeof(XgDqRates) / 4); i += 4) dst[i] = __ldg(src + i);
+        }
         __syncwarp(0xffffffffu);
 
         /* ---- trellis state of lane s (state s) ---- */
@@ -429,7 +443,7 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
         const int top = first | 15;
         int nsteps = first >= 0 ? top + 1 : 0;
         nsteps = __reduce_max_sync(0xffffffffu, nsteps);
-        const uint32_t *sigset = &RT->sig[s > 1 ? s - 1 : 0][0][0];
+        const uint32_t *sigset = &Q.rt.sig[s > 1 ? s - 1 : 0][0][0];
         const int src1 = s == 1 ? 2 : s == 2 ? 1 : s;      /* round 1 reads candidate A/Z */
         const int src2 = src1 ^ 1;                         /* round 2 reads candidate B */
         /* coefficients of the current / next sub-block: lane s holds scan positions 4s..4s+3 */
@@ -482,16 +496,15 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
                 }
                 sum = min(sum, 255);
             }
-            const int d = px + py;
-            const int sigoff = luma ? (d < 2 ? 8 : d < 5 ? 4 : 0) : (d < 2 ? 4 : 0);
-            const int gtxoff = luma ? (d < 1 ? 16 : d < 3 ? 11 : d < 10 ? 6 : 1) : (d < 1 ? 6 : 1);
+            const int sigoff = 4 * (int)(luma ? (se.x >> 21) & 3 : (se.x >> 25) & 1);
+            const int gtxoff = 1 + 5 * (int)(luma ? (se.x >> 23) & 3 : (se.x >> 26) & 1);
             uint32_t sig0 = 0, sig1 = 0;
-            const uint32_t *gtx = RT->gtx[0];
+            const uint32_t *gtx = Q.rt.gtx[0];
             int rice, rzero = 0;
             if (rem >= 4) {
                 const uint32_t *sg = sigset + 2 * (sigoff + min((a1 + 1) >> 1, 3));
-                sig0 = __ldg(sg); sig1 = __ldg(sg + 1);
-                gtx = RT->gtx[gtxoff + min(a1 - cnt, 4)];
+                sig0 = sg[0]; sig1 = sg[1];
+                gtx = Q.rt.gtx[gtxoff + min(a1 - cnt, 4)];
                 rice = xg_dq_rpar(min(max(sum - 20, 0), 31));
             } else {
                 rice = xg_dq_rpar(min(sum, 31));
@@ -521,10 +534,10 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
             long long ca = cost + ddA, cb = cost + ddB, cz = cost;
             bool zero_ok = true;
             if (rem >= 4) {
-                ca += __ldg(&gtx[lvA < 4 ? lvA : 4 + (lvA & 1)]) + (lvA >= 4 ? sm.rice[rice][min((lvA - 4) >> 1, 31)] : 0);
-                cb += __ldg(&gtx[lvB < 4 ? lvB : 4 + (lvB & 1)]) + (lvB >= 4 ? sm.rice[rice][min((lvB - 4) >> 1, 31)] : 0);
+                ca += gtx[lvA < 4 ? lvA : 4 + (lvA & 1)] + (lvA >= 4 ? sm.rice[rice][min((lvA - 4) >> 1, 31)] : 0);
+                cb += gtx[lvB < 4 ? lvB : 4 + (lvB & 1)] + (lvB >= 4 ? sm.rice[rice][min((lvB - 4) >> 1, 31)] : 0);
                 if (ptype == 1) {
-                    const uint32_t sb1 = __ldg(&RT->sbb[signb][1]);
+                    const uint32_t sb1 = Q.rt.sbb[signb][1];
                     ca += sb1 + sig1; cb += sb1 + sig1; cz += sb1 + sig0;
                 } else if (ptype == 0 || nsig) {
                     ca += sig1; cb += sig1; cz += sig0;
@@ -553,12 +566,12 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
             if (cc1 < dc) { dc = cc1; dsel = s1; dfrom = f1; }
             if (cc2 < dc) { dc = cc2; dsel = s2; dfrom = f2; }
             if (ptype == 2) {
-                long long c = skcost + __ldg(&RT->sbb[sksignb][0]);
+                long long c = skcost + Q.rt.sbb[sksignb][0];
                 if (c < dc) { dc = c; dsel = 4; dfrom = 4 + s; }
             }
             if ((s & 1) == 0) {
                 const int lvs = lvof(s);
-                long long c = ddS + Q.last[0][px] + Q.last[1][py] + __ldg(&RT->gtx[0][lvs < 4 ? lvs : 4 + (lvs & 1)]) +
+                long long c = ddS + Q.last[0][px] + Q.last[1][py] + Q.rt.gtx[0][lvs < 4 ? lvs : 4 + (lvs & 1)] +
                               (lvs >= 4 ? sm.rice[0][min((lvs - 4) >> 1, 31)] : 0);
                 if (c < dc) { dc = c; dsel = s; dfrom = -1; }
             }
@@ -737,6 +750,8 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
 
 /* ---------------------------------------------------------------- launches */
 
+/* the trellis kernel's shared memory (above the 48 KB default) and the CTAs
+ * that fit on the GPU at once; 0 if the attribute could not be set */
 static int xg_dq_resident_ctas(void)
 {
     static int ctas = 0;
@@ -745,10 +760,15 @@ static int xg_dq_resident_ctas(void)
         int dev = 0, sms = 0, per = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaFuncSetAttribute(k_dq, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(XgDqSmem)) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
         cudaFuncSetAttribute(k_dq, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dq, XG_DQ_THREADS, sizeof(XgDqSmem));
         ctas = sms * (per > 0 ? per : 1);
     });
+    if (!ctas) xg_set_error(XIN_GPU_ERR_CUDA, "dep_quant: kernel set-up failed");
     return ctas;
 }
 
@@ -854,7 +874,9 @@ extern "C" int xin_gpu_dq_plan_create(const xin_gpu_dq_block *blocks, int32_t nb
     xin_gpu_dq_plan *p = new xin_gpu_dq_plan();
     cudaGetDevice(&p->device);
     p->nblocks = nblocks; p->nsets = nsets; p->ncoeffs = ncoeffs; p->nscan = nscan;
-    p->ctas = std::min(xg_dq_resident_ctas(), (nblocks + XG_DQ_QUADS - 1) / XG_DQ_QUADS);
+    const int res = xg_dq_resident_ctas();
+    if (!res) { delete p; return xin_gpu_last_status(); }
+    p->ctas = std::min(res, (nblocks + XG_DQ_QUADS - 1) / XG_DQ_QUADS);
     const size_t bytes = xg_dq_area_bytes(nsets, nblocks, nscan, p->ctas * XG_DQ_QUADS, nullptr, nullptr);
     if (nscan >= (1ull << 32) ||
         xg_cuda_check(cudaMalloc(&p->d_soff, (size_t)nblocks * 4), "dq plan") ||
@@ -965,7 +987,7 @@ extern "C" void XinGpuDepQuant(void *depQuant, void *fastBuf, void *tu, XG_COEFF
         xg_set_error(XIN_GPU_ERR_ARG, "XinGpuDepQuant: bad argument");
         return;
     }
-    if (!xg_dq_tables()) return;
+    if (!xg_dq_tables() || !xg_dq_resident_ctas()) return;
     const xin_gpu_prob *ctx = *(const xin_gpu_prob *const *)((const char *)depQuant + XIN_GPU_DQ_CONTEXT_OFFSET);
     const void *full = *(const void *const *)((const char *)fastBuf + XIN_GPU_FASTBUF_FULLBUF_OFFSET);
     const uint32_t type = *(const uint32_t *)((const char *)fastBuf + XIN_GPU_FASTBUF_TYPE_OFFSET);
