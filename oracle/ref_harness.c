@@ -3,7 +3,7 @@
  *
  * Flat C entry points around the reference's open drivers, which take the
  * encoder's section / sequence / CU structures.  Each harness fills the few
- * fields the driver reads (everything else zero) and calls it unmodified:
+ * fields the function reads (everything else zero) and calls it unmodified:
  *   Xin266FDctWxH       h266_encoder/source/h266_forward_trans.c:45
  *   Xin266IDctWxH       h266_encoder/source/h266_inverse_trans.c:117
  *   Xin266SubFDctWxH    h266_encoder/source/h266_sub_dct.c:47

@@ -10,7 +10,7 @@
  * that ends in them.  One quad of lanes owns one block, lane s owning state s,
  * so a warp runs eight blocks side by side.  Per coefficient every lane prices
  * the three candidates its state offers (level A, level B, zero), the quad
- * swaps them with two rounds of shuffles, and lane t keeps the cheapest path
+ * swaps them with two shuffle exchanges, and lane t keeps the cheapest path
  * into state t (the fixed transition pattern of the reference: 0->{0,2},
  * 1->{2,0}, 2->{1,3}, 3->{3,1}, plus "skip this sub-block" and "start here").
  *
@@ -444,8 +444,8 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
         int nsteps = first >= 0 ? top + 1 : 0;
         nsteps = __reduce_max_sync(0xffffffffu, nsteps);
         const uint32_t *sigset = &Q.rt.sig[s > 1 ? s - 1 : 0][0][0];
-        const int src1 = s == 1 ? 2 : s == 2 ? 1 : s;      /* round 1 reads candidate A/Z */
-        const int src2 = src1 ^ 1;                         /* round 2 reads candidate B */
+        const int src1 = s == 1 ? 2 : s == 2 ? 1 : s;      /* first exchange reads candidate A/Z */
+        const int src2 = src1 ^ 1;                         /* second exchange reads candidate B */
         /* coefficients of the current / next sub-block: lane s holds scan positions 4s..4s+3 */
         xg_coef c0 = 0, c1 = 0, c2 = 0, c3 = 0, n0 = 0, n1 = 0, n2 = 0, n3 = 0;
         uint4 ea = make_uint4(0, 0, 0, 0), eb = make_uint4(0, 0, 0, 0);
@@ -551,7 +551,7 @@ k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ cou
             int saz;
             if (!zero_ok || ca < cz) { caz = ca; saz = iA; } else { caz = cz; saz = 4; }
 
-            /* exchange: round 1 every lane publishes A/Z, round 2 B */
+            /* exchange: first every lane publishes A/Z, then B */
             const long long r1 = xg_dq_shfl64(qmask, caz, src1), r2 = xg_dq_shfl64(qmask, cb, src2);
             const int sels = __shfl_sync(qmask, saz | iB << 4, src1, 4);
             const int sels2 = __shfl_sync(qmask, saz | iB << 4, src2, 4);

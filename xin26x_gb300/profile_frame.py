@@ -1,5 +1,5 @@
 """Run the batched frame form on resident pictures and print per-stage device
-times -- the driver for profiling (ncu) and quick timing of the kernels.
+times -- the program for profiling (ncu) and quick timing of the kernels.
 
     python -m xin26x_gb300.profile_frame [--frames 6] [--width 1920] [--height 1080]
                                          [--search 64] [--bitdepth 8] [--ctu 64]
