@@ -361,6 +361,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         mp.W = c.width; mp.H = c.height; mp.ctu = c.ctu_size; mp.R = c.search_range;
         mp.band_rows = s->me_band_rows; mp.band_rows_alloc = s->me_band_rows_alloc; mp.row_words = s->me_row_words;
         mp.agg_passes = s->me_nb;
+        mp.key_mul = 1u << (XG_COST_FRACTION + xg_me_db(s->sbd) + (XG_BITDEPTH - s->sbd));
         for (int L = 0; L < 4; L++) {
             mp.keys[L] = s->lev_on[L] ? s->keys + s->lev_first[L] : nullptr;
             mp.cus_x[L] = s->lev_cx[L];

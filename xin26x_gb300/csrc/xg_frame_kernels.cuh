@@ -248,6 +248,7 @@ struct XgMeParams {
     int band_rows_alloc;                /* staged band rows: 64 + band_rows rounded up to XG_ME_D, minus 1 */
     int row_words;                      /* words per band row (pitch of the word array) */
     int agg_passes;                     /* passes buffered for the 32x32 / 64x64 sums, 1..XG_ME_NB_MAX */
+    uint32_t key_mul;                   /* 1 << (XG_COST_FRACTION + key bits of the candidate row + sample shift) */
     unsigned long long *keys[4];        /* level 0..3 = 64, 32, 16, 8 (NULL = level off) */
     int cus_x[4];                       /* CUs per row of each level */
 };
@@ -294,6 +295,8 @@ __host__ __device__ constexpr int xg_me_cur_words(int sbd) { return sbd == 8 ? 6
  * words a row plus their negations) */
 __host__ __device__ constexpr int xg_me_d(int sbd) { return sbd == 8 ? 8 : 4; }
 __host__ __device__ constexpr int xg_me_db(int sbd) { return sbd == 8 ? 3 : 2; }
+/* a compile-time flag as a value, for lambdas instantiated per flag */
+template <bool B> struct xg_bool_c { static constexpr bool value = B; };
 /* keys at or above this are not candidates (padding rows, windows) */
 #define XG_ME_KEY_INVALID 0xC0000000u
 #define XG_ME_SMEM_MAX (216 * 1024)       /* dynamic shared memory of k_me_tiles, under the 227 KB a CTA may have */
@@ -342,12 +345,15 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
             refw[r * p.row_words + x] = (uint32_t)src[0] | ((uint32_t)src[1] << 16);
     }
     const uint32_t lambda = pp->lambda;
-    for (int i = threadIdx.x; i < nx; i += blockDim.x) mvcx[i] = xg_mvd_bits(4 * (i - p.R)) * lambda;
-    /* rows past the band (the last chunk's padding) get a sentinel that lifts
+    /* MV-bit costs in key form: column bits * lambda << XG_ME_DB, and row bits *
+     * lambda << XG_ME_DB plus the row's index within its chunk, so that the
+     * key of candidate row d of a chunk is SAD * key_mul + mvcx[col] + mvcy[row].
+     * Rows past the band (the last chunk's padding) get a sentinel that lifts
      * their keys to >= XG_ME_KEY_INVALID without wrapping (lambda <= 2^20 keeps
-     * real keys below 2^30) */
+     * real keys below 2^30). */
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) mvcx[i] = (xg_mvd_bits(4 * (i - p.R)) * lambda) << XG_ME_DB;
     for (int i = threadIdx.x; i < nch * XG_ME_D; i += blockDim.x)
-        mvcy[i] = i < ndy ? xg_mvd_bits(4 * (dyb0 + i)) * lambda : (XG_ME_KEY_INVALID >> XG_ME_DB);
+        mvcy[i] = (i < ndy ? (xg_mvd_bits(4 * (dyb0 + i)) * lambda) << XG_ME_DB : XG_ME_KEY_INVALID) + (uint32_t)(i & (XG_ME_D - 1));
 
     /* ---- the current tile in shared memory (read as broadcasts) */
     const int bx = (warp & 3) * 16, by = (warp >> 2) * 16;
@@ -365,15 +371,18 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     }
 
     /* ---- windows and liveness of this warp's CUs; a band inside every window needs no per-candidate check */
+    /* the running best of each CU as (cost << 32) | raster index; none = a cost
+     * no valid key reaches (keys >= XG_ME_KEY_INVALID have cost >= its value) */
+    constexpr unsigned long long NONE = (unsigned long long)(XG_ME_KEY_INVALID >> XG_ME_DB) << 32;
     bool live[5];
-    uint32_t best[5], bidx[5];
+    unsigned long long best[5];
 #pragma unroll
     for (int c = 0; c < 5; c++) {
         int s = c < 4 ? 8 : 16;
         int cx = tx0 + bx + (c < 4 ? (c & 1) * 8 : 0), cy = ty0 + by + (c < 4 ? (c >> 1) * 8 : 0);
         live[c] = p.keys[c < 4 ? 3 : 2] && cx + s <= p.W && cy + s <= p.H;
         if (lane == 0) xg_cu_window(p, cx, cy, s, swin[warp][c][0], swin[warp][c][1], swin[warp][c][2], swin[warp][c][3]);
-        best[c] = 0xFFFFFFFFu; bidx[c] = 0xFFFFFFFFu;
+        best[c] = NONE;
     }
     if (threadIdx.x < 4) {
         int c32x = tx0 + (threadIdx.x & 1) * 32, c32y = ty0 + (threadIdx.x >> 1) * 32;
@@ -395,19 +404,28 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     const bool live32 = p.keys[1] && c32x + 32 <= p.W && c32y + 32 <= p.H;
     const bool live64 = threadIdx.x < XG_ME_SLOTS && p.keys[0] && tx0 + 64 <= p.W && ty0 + 64 <= p.H;
     const int w32 = (c32 & 1) * 2 + (c32 >> 1) * 8;          /* first warp of the quadrant: w32, +1, +4, +5 */
-    uint32_t best32 = 0xFFFFFFFFu, bidx32 = 0xFFFFFFFFu, best64 = 0xFFFFFFFFu, bidx64 = 0xFFFFFFFFu;
+    unsigned long long best32 = ~0ull, best64 = ~0ull;
     __syncthreads();
     const bool interior = sinterior[warp];
 
+    /* key = SAD * key_mul + MV bits (a multiplier read at run time keeps the key
+     * arithmetic on the multiply-add pipe, beside the SADs on the integer pipe);
+     * key_mul = 1 << (XG_COST_FRACTION + XG_ME_DB + SH) */
+    const uint32_t kmul = p.key_mul;
+    /* v / nx = umulhi(v, nx_rcp) for every v < 2^17 and odd nx in 3..513 (checked exhaustively) */
+    const uint32_t nx_rcp = 0xFFFFFFFFu / (uint32_t)nx + 1u;
     const int npass = (nv + 31) / 32;
+    /* this lane's slot v = pz * 32 + lane as (chunk, column), advanced by 32 slots a pass */
+    int chunk = 0, col = lane;
+    while (col >= nx) { col -= nx; chunk++; }
+    int pb = 0, grp = 0;                                     /* pass within the buffered group, group parity */
     for (int pz = 0; pz < npass; pz++) {
+        const bool vvalid = chunk < nch;
+        /* lanes past the last slot repeat slot nv - 1: same key, no effect */
+        const int ck = vvalid ? chunk : nch - 1, cl = vvalid ? col : nx - 1;
         {
-            const int v = pz * 32 + lane;
-            const bool vvalid = v < nv;
-            const int vv = vvalid ? v : nv - 1;
-            const int chunk = vv / nx, col = vv - chunk * nx;
-            const int row0 = chunk * XG_ME_D;
-            const uint32_t *base = refw + (by + row0) * p.row_words + bx + col;
+            const int row0 = ck * XG_ME_D;
+            const uint32_t *base = refw + (by + row0) * p.row_words + bx + cl;
             uint32_t acc[XG_ME_D][4];
 #pragma unroll
             for (int d = 0; d < XG_ME_D; d++)
@@ -438,13 +456,8 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                     }
                 }
             }
-            /* 8-bit samples of 10-bit pictures: the 10-bit SAD is four times the 8-bit one */
-            if constexpr (SH > 0) {
-#pragma unroll
-                for (int d = 0; d < XG_ME_D; d++)
-#pragma unroll
-                    for (int b = 0; b < 4; b++) acc[d][b] <<= SH;
-            }
+            /* 8-bit samples of 10-bit pictures: the SADs stay at 8 bits here; key_mul
+             * and the 32x32 / 64x64 costs scale them by 1 << SH, the 10-bit SAD */
             } else {
             uint32_t cw[XG_ME_D][8], cn[XG_ME_D][8];   /* current rows t .. t-XG_ME_D+1 (slot = row % XG_ME_D), negated */
             const uint32_t *crow = scur + by * 32 + (bx >> 1);
@@ -485,108 +498,115 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
              * a (cost, raster index) compare with the lane's running best.  Keys of
              * candidates outside the band or the window are >= XG_ME_KEY_INVALID,
              * above any real key (costs stay below 2^27). */
-            const int dx = col - p.R, dyl = dyb0 + row0;
-            const uint32_t gidx0 = (uint32_t)((dyl + p.R) * nx + col);
+            const int dx = cl - p.R, dyl = dyb0 + row0;
+            const uint32_t gidx0 = (uint32_t)((dyl + p.R) * nx + cl);
+            const uint32_t mx = mvcx[cl];
             uint32_t md[XG_ME_D];
-            uint32_t *s16w = s16 + (pz & 1) * 16 * XG_ME_SLOTS + warp * XG_ME_SLOTS + lane;
-            /* lanes past the last candidate repeat candidate nv - 1: same key, no effect */
 #pragma unroll
-            for (int d = 0; d < XG_ME_D; d++) {
-                md[d] = ((mvcx[col] + mvcy[row0 + d]) << XG_ME_DB) | (uint32_t)d;
-                s16w[d * 32] = acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
-            }
+            for (int d = 0; d < XG_ME_D; d++) md[d] = mx + mvcy[row0 + d];
+            auto search = [&](auto check) {
+                /* the 16x16 CU first: its SADs also go to the 32x32 exchange */
+                uint32_t *s16w = s16 + (pz & 1) * 16 * XG_ME_SLOTS + warp * XG_ME_SLOTS + lane;
 #pragma unroll
-            for (int c = 0; c < 5; c++) {
-                uint32_t kd[XG_ME_D];
+                for (int ci = 0; ci < 5; ci++) {
+                    const int c = (ci + 4) % 5;
+                    uint32_t kd[XG_ME_D];
 #pragma unroll
-                for (int d = 0; d < XG_ME_D; d++) {
-                    const uint32_t sad = c < 4 ? acc[d][c] : acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
-                    kd[d] = (sad << (XG_COST_FRACTION + XG_ME_DB)) + md[d];
-                    if (!interior) {
-                        const int dy = dyl + d;
-                        if (!(dx >= swin[warp][c][0] && dx <= swin[warp][c][1] && dy >= swin[warp][c][2] && dy <= swin[warp][c][3]))
-                            kd[d] = 0xFFFFFFFFu;
+                    for (int d = 0; d < XG_ME_D; d++) {
+                        uint32_t sad;
+                        if (c == 4) {
+                            sad = acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
+                            s16w[d * 32] = sad;
+                        } else {
+                            sad = acc[d][c];
+                        }
+                        kd[d] = sad * kmul + md[d];
+                        if constexpr (decltype(check)::value) {
+                            const int dy = dyl + d;
+                            if (!(dx >= swin[warp][c][0] && dx <= swin[warp][c][1] && dy >= swin[warp][c][2] && dy <= swin[warp][c][3]))
+                                kd[d] = 0xFFFFFFFFu;
+                        }
                     }
+                    /* the minimum of the keys with three-input minima */
+                    uint32_t k;
+                    if constexpr (XG_ME_D == 8)
+                        k = min(__vimin3_u32(kd[0], kd[1], kd[2]), __vimin3_u32(__vimin3_u32(kd[3], kd[4], kd[5]), kd[6], kd[7]));
+                    else
+                        k = min(__vimin3_u32(kd[0], kd[1], kd[2]), kd[3]);
+                    const unsigned long long kk =
+                        ((unsigned long long)(k >> XG_ME_DB) << 32) | (gidx0 + (k & (XG_ME_D - 1)) * (uint32_t)nx);
+                    best[c] = kk < best[c] ? kk : best[c];
                 }
-                /* the minimum of the keys with three-input minima */
-                uint32_t k;
-                if constexpr (XG_ME_D == 8)
-                    k = min(__vimin3_u32(kd[0], kd[1], kd[2]), __vimin3_u32(__vimin3_u32(kd[3], kd[4], kd[5]), kd[6], kd[7]));
-                else
-                    k = min(__vimin3_u32(kd[0], kd[1], kd[2]), kd[3]);
-                const uint32_t cost = k >> XG_ME_DB, gidx = gidx0 + (k & (XG_ME_D - 1)) * (uint32_t)nx;
-                if (live[c] && k < XG_ME_KEY_INVALID && (cost < best[c] || (cost == best[c] && gidx < bidx[c]))) { best[c] = cost; bidx[c] = gidx; }
-            }
+            };
+            if (interior) search(xg_bool_c<false>());
+            else search(xg_bool_c<true>());
         }
         /* 32x32: the quadrant's four warps swap their 16x16 SADs (double-buffered by
          * pass parity: a buffer is rewritten two passes later, after the next
          * barrier, when every warp has read it) */
         {
             asm volatile("bar.sync %0, 128;" ::"r"(1 + c32) : "memory");
-            const int v = pz * 32 + lane;
-            const int vv = v < nv ? v : nv - 1;
-            const int chunk = vv / nx, col = vv - chunk * nx;
 #pragma unroll
             for (int e = 0; e < XG_ME_D / 4; e++) {
-                const int d = jq * (XG_ME_D / 4) + e, row = chunk * XG_ME_D + d;
+                const int d = jq * (XG_ME_D / 4) + e, row = ck * XG_ME_D + d;
                 const uint32_t *r16 = s16 + (pz & 1) * 16 * XG_ME_SLOTS + d * 32 + lane;
                 const uint32_t s32 = r16[w32 * XG_ME_SLOTS] + r16[(w32 + 1) * XG_ME_SLOTS] + r16[(w32 + 4) * XG_ME_SLOTS] +
                                      r16[(w32 + 5) * XG_ME_SLOTS];
-                s32r[((((pz / nb) & 1) * nb + pz % nb) * 4 + c32) * XG_ME_SLOTS + d * 32 + lane] = s32;
-                if (live32 && v < nv && row < ndy) {
-                    const int dx = col - p.R, dy = dyb0 + row;
-                    const uint32_t cost = (s32 << XG_COST_FRACTION) + mvcx[col] + mvcy[row];
-                    const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
-                    if (dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3] &&
-                        (cost < best32 || (cost == best32 && gidx < bidx32))) { best32 = cost; bidx32 = gidx; }
+                s32r[((grp * nb + pb) * 4 + c32) * XG_ME_SLOTS + d * 32 + lane] = s32;
+                if (live32 && vvalid && row < ndy) {
+                    const int dx = cl - p.R, dy = dyb0 + row;
+                    const uint32_t cost = (s32 << (XG_COST_FRACTION + SH)) + ((mvcx[cl] + mvcy[row]) >> XG_ME_DB);
+                    const unsigned long long kk = ((unsigned long long)cost << 32) | (uint32_t)((dy + p.R) * nx + cl);
+                    if (dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3] && kk < best32)
+                        best32 = kk;
                 }
             }
         }
         /* 64x64 every nb passes, from the four quadrants' 32x32 SADs (the ring is
          * double-buffered by group: a group's half is rewritten only after the
          * next full barrier, which the reading threads reach after reading) */
-        const int pb = pz % nb;
         if (pb == nb - 1 || pz == npass - 1) {
             __syncthreads();
             if (live64) {
                 const int d = threadIdx.x / 32, pz0 = pz - pb;
-                const uint32_t *r32 = s32r + ((pz / nb) & 1) * nb * 4 * XG_ME_SLOTS + threadIdx.x;
+                const uint32_t *r32 = s32r + grp * nb * 4 * XG_ME_SLOTS + threadIdx.x;
                 for (int j = 0; j <= pb; j++) {
-                    const int v = (pz0 + j) * 32 + lane;
-                    const int vv = v < nv ? v : nv - 1;
-                    const int chunk = vv / nx, col = vv - chunk * nx, row = chunk * XG_ME_D + d;
-                    if (v < nv && row < ndy) {
+                    const uint32_t v = (uint32_t)((pz0 + j) * 32 + lane);
+                    const int chj = (int)__umulhi(v, nx_rcp), colj = (int)v - chj * nx, row = chj * XG_ME_D + d;
+                    if ((int)v < nv && row < ndy) {
                         const uint32_t *q32 = r32 + j * 4 * XG_ME_SLOTS;
                         const uint32_t s64 = q32[0] + q32[XG_ME_SLOTS] + q32[2 * XG_ME_SLOTS] + q32[3 * XG_ME_SLOTS];
-                        const int dx = col - p.R, dy = dyb0 + row;
-                        const uint32_t c64 = (s64 << XG_COST_FRACTION) + mvcx[col] + mvcy[row];
-                        const uint32_t gidx = (uint32_t)((dy + p.R) * nx + col);
-                        if (dx >= swin64[0] && dx <= swin64[1] && dy >= swin64[2] && dy <= swin64[3] &&
-                            (c64 < best64 || (c64 == best64 && gidx < bidx64))) { best64 = c64; bidx64 = gidx; }
+                        const int dx = colj - p.R, dy = dyb0 + row;
+                        const uint32_t c64 = (s64 << (XG_COST_FRACTION + SH)) + ((mvcx[colj] + mvcy[row]) >> XG_ME_DB);
+                        const unsigned long long kk = ((unsigned long long)c64 << 32) | (uint32_t)((dy + p.R) * nx + colj);
+                        if (dx >= swin64[0] && dx <= swin64[1] && dy >= swin64[2] && dy <= swin64[3] && kk < best64) best64 = kk;
                     }
                 }
             }
         }
+        col += 32;
+        while (col >= nx) { col -= nx; chunk++; }
+        if (++pb == nb) { pb = 0; grp ^= 1; }
     }
 
     /* ---- publish: warp minimum of packed keys, then one atomicMin per CU and CTA */
 #pragma unroll
     for (int c = 0; c < 5; c++) {
-        unsigned long long k = ((unsigned long long)best[c] << 32) | bidx[c];
+        unsigned long long k = best[c];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) { unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o); k = v < k ? v : k; }
-        if (lane == 0 && live[c] && k != ~0ull) {
+        if (lane == 0 && live[c] && k < NONE) {
             int s = c < 4 ? 8 : 16, L = c < 4 ? 3 : 2;
             int cx = tx0 + bx + (c < 4 ? (c & 1) * 8 : 0), cy = ty0 + by + (c < 4 ? (c >> 1) * 8 : 0);
             atomicMin(p.keys[L] + (cy / s) * p.cus_x[L] + cx / s, k);
         }
     }
     {
-        unsigned long long k = ((unsigned long long)best32 << 32) | bidx32;
+        unsigned long long k = best32;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) { unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o); k = v < k ? v : k; }
         if (lane == 0 && live32 && k != ~0ull) atomicMin(p.keys[1] + (c32y / 32) * p.cus_x[1] + c32x / 32, k);
-        k = ((unsigned long long)best64 << 32) | bidx64;
+        k = best64;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) { unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o); k = v < k ? v : k; }
         if (lane == 0 && live64 && k != ~0ull) atomicMin(p.keys[0] + (ty0 / 64) * p.cus_x[0] + tx0 / 64, k);
