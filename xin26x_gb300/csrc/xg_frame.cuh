@@ -221,6 +221,12 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         for (int k = 0; k < 16; k++) q.plane[k] = s->qpel_base[i] + (size_t)k * s->plane_elems + (size_t)pad * s->pitch + pad;
         q.plane[0] = s->slot[i][0].data;
         q.pitch = s->pitch; q.w = c.width; q.h = c.height; q.pad = pad;
+        /* the search stages reference rows with 16-byte loads from 8-sample-aligned columns */
+        if (((uintptr_t)s->slot[i][0].data & 15) || (s->pitch & 7)) {
+            xg_set_error(XIN_GPU_ERR_CUDA, "stream_open: luma slot not 16-byte aligned");
+            xg_stream_free(s);
+            return XIN_GPU_ERR_CUDA;
+        }
     }
     /* integer-search band geometry: enough CTAs for the GPU; shared memory within
      * XG_ME_SMEM_MAX, taking more bands (less reuse of staged rows) or fewer

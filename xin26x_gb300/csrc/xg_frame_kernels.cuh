@@ -333,16 +333,57 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     /* current tile, 16-byte aligned: 8-bit [64][16] (pixels 4k .. 4k+3), 10-bit [64][32] (pixels 2k, 2k+1) */
     uint32_t *scur = sm;
 
-    /* ---- stage the reference band: pixels (X0 + x .. X0 + x + 3, Y0 + r) -> refw[r * row_words + x] */
+    /* ---- stage the reference band: pixels (X0 + x .., Y0 + r) -> refw[r * row_words + x].
+     * Group g of band row r is the 8 word positions x = 8g + j - off (j < 8) whose
+     * pixels start at the aligned column A + 8g (A = X0 rounded down to 8, off = X0
+     * - A); a lane reads its pixels A + 8g .. with one 8- or 16-byte load (the slot
+     * layout keeps data and pitch multiples of 32 / 128 elements) plus a short
+     * load of the next pixels when a stored word reaches them (so reads stay
+     * within the right margin), and forms the words with byte permutes.  A warp
+     * covers 8 rows x 4 groups, lane = (row & 7) * 4 + (group & 3): the row pitch
+     * is odd, so the 32 lanes' stores of one j fall in 32 different banks. */
     const int X0 = tx0 - p.R, Y0 = ty0 + dyb0;
-    for (int i = threadIdx.x; i < rows * relw; i += blockDim.x) {
-        int r = i / relw, x = i - r * relw;
-        const xg_pix *src = p.ref.data + (intptr_t)(Y0 + r) * p.ref.pitch + X0 + x;
-        if constexpr (SBD == 8)
-            refw[r * p.row_words + x] = (uint32_t)(src[0] >> SH) | ((uint32_t)(src[1] >> SH) << 8) |
-                                        ((uint32_t)(src[2] >> SH) << 16) | ((uint32_t)(src[3] >> SH) << 24);
-        else
-            refw[r * p.row_words + x] = (uint32_t)src[0] | ((uint32_t)src[1] << 16);
+    {
+        const int A = X0 & ~7, off = X0 - A;
+        const int ngrp = (relw + off + 7) >> 3, ngb = (ngrp + 3) >> 2, nrb = (rows + 7) >> 3;
+        const int need = off + relw + (SBD == 8 ? 2 : 0);    /* last pixel a stored word uses, from A */
+        for (int T = warp; T < nrb * ngb; T += XG_ME_THREADS / 32) {
+            const int rb = T / ngb, r = rb * 8 + (lane >> 2), g = (T - rb * ngb) * 4 + (lane & 3);
+            if (r >= rows || g >= ngrp) continue;
+            const xg_pix *src = p.ref.data + (intptr_t)(Y0 + r) * p.ref.pitch + A + 8 * g;
+            const bool more = 8 * g + 8 <= need;
+            uint32_t wd[8];
+            if constexpr (SBD == 8) {
+                uint32_t b0, b1, b2;                                /* pixel bytes 0-3, 4-7, 8-11 */
+                if constexpr (sizeof(xg_pix) == 1) {
+                    const uint2 c = *reinterpret_cast<const uint2 *>(src);
+                    b0 = c.x; b1 = c.y;
+                    b2 = more ? *reinterpret_cast<const uint32_t *>(src + 8) : 0u;
+                } else {
+                    const uint4 c = *reinterpret_cast<const uint4 *>(src);
+                    const uint2 n = more ? *reinterpret_cast<const uint2 *>(src + 8) : make_uint2(0u, 0u);
+                    /* two 16-bit samples per word -> their >> SH bytes in lanes 0 and 2 */
+                    auto lo = [](uint32_t u) { return (u >> SH) & 0x00ff00ffu; };
+                    b0 = __byte_perm(lo(c.x), lo(c.y), 0x6420);
+                    b1 = __byte_perm(lo(c.z), lo(c.w), 0x6420);
+                    b2 = __byte_perm(lo(n.x), lo(n.y), 0x6420);
+                }
+                wd[0] = b0; wd[1] = __byte_perm(b0, b1, 0x4321); wd[2] = __byte_perm(b0, b1, 0x5432); wd[3] = __byte_perm(b0, b1, 0x6543);
+                wd[4] = b1; wd[5] = __byte_perm(b1, b2, 0x4321); wd[6] = __byte_perm(b1, b2, 0x5432); wd[7] = __byte_perm(b1, b2, 0x6543);
+            } else {
+                const uint4 c = *reinterpret_cast<const uint4 *>(src);
+                const uint32_t n = more ? *reinterpret_cast<const uint32_t *>(src + 8) : 0u;
+                const uint32_t u[5] = { c.x, c.y, c.z, c.w, n };
+#pragma unroll
+                for (int k = 0; k < 4; k++) { wd[2 * k] = u[k]; wd[2 * k + 1] = __byte_perm(u[k], u[k + 1], 0x5432); }
+            }
+            uint32_t *dst = refw + r * p.row_words;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int x = 8 * g + j - off;
+                if ((unsigned)x < (unsigned)relw) dst[x] = wd[j];
+            }
+        }
     }
     const uint32_t lambda = pp->lambda;
     /* MV-bit costs in key form: column bits * lambda << XG_ME_DB, and row bits *
