@@ -228,6 +228,14 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
             return XIN_GPU_ERR_CUDA;
         }
     }
+    /* the quarter-pel plane kernel's compile-time taps are the table's phases 4, 8, 12 */
+    for (int f = 0; f < 3; f++)
+        for (int k = 0; k < 8; k++)
+            if (h_luma_taps[0][4 * (f + 1)][k] != xg_qp_tap(f, k)) {
+                xg_set_error(XIN_GPU_FAIL, "stream_open: quarter-pel taps differ from the luma filter table");
+                xg_stream_free(s);
+                return XIN_GPU_FAIL;
+            }
     /* integer-search band geometry: enough CTAs for the GPU; shared memory within
      * XG_ME_SMEM_MAX, taking more bands (less reuse of staged rows) or fewer
      * buffered passes for the 32x32 / 64x64 sums (more barriers) when it does not fit */

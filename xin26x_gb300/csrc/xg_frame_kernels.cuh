@@ -41,53 +41,91 @@ __global__ void k_pad(XgPlane p)
  * for the padded area shrunk by the filter reach (3 before, 4 after). */
 struct XgQpel { xg_pix *plane[16]; int pitch, w, h, pad; };
 
-/* A CTA covers a 64 x 16 block of positions for all 15 planes: the reference
- * tile with the filter reach is staged in shared memory, the horizontal
- * first-stage values of the three horizontal phases are computed once per row
- * and shared by the three vertical phases, so every output costs one 8-tap sum. */
+/* The three quarter-pel phases (4, 8, 12 of 16) of the luma 8-tap filter, tap k
+ * of phase f = 0, 1, 2 (the 1/4 and 1/2 rows of the reference's luma filter
+ * table, the 3/4 row mirrored): compile-time constants, so that every multiply
+ * of the plane kernel takes an immediate; stream_open checks them against the
+ * table the library builds. */
+__host__ __device__ constexpr int xg_qp_tap(int f, int k)
+{
+    return f == 0 ? (k == 0 ? -1 : k == 1 ? 4 : k == 2 ? -10 : k == 3 ? 58 : k == 4 ? 17 : k == 5 ? -5 : k == 6 ? 1 : 0)
+         : f == 1 ? ((k == 0 || k == 7) ? -1 : (k == 1 || k == 6) ? 4 : (k == 2 || k == 5) ? -11 : 40)
+                  : xg_qp_tap(0, 7 - k);
+}
+
+/* A CTA covers a 64 x 32 block of positions for all 15 planes.  The reference
+ * tile with the filter reach is staged in shared memory.  Pass 1, one position
+ * (row, column) per thread step: its eight horizontal samples give the three
+ * horizontal phases at once -- the first-stage values of every staged row, kept
+ * in shared memory, and for the output rows the pixels of the three fy = 0
+ * planes.  Pass 2, a column and a strip of XG_QP_STRIP output rows per thread:
+ * a sliding window of STRIP + 7 values of each vertical source (the integer
+ * samples, the three first-stage phases) gives the 12 planes with fy != 0, one
+ * 8-tap sum per sample. */
 #define XG_QP_TW 64
-#define XG_QP_TH 16
+#define XG_QP_TH 32
+#define XG_QP_STRIP 8
+static_assert(XG_QP_TW * (XG_QP_TH / XG_QP_STRIP) == 256, "pass 2 gives every thread of the CTA one column strip");
 __global__ void __launch_bounds__(256) k_qpel_planes(XgPlane ref, XgQpel qp)
 {
-    __shared__ xg_pix tile[XG_QP_TH + 7][XG_QP_TW + 8];
-    __shared__ int16_t hs[3][XG_QP_TH + 7][XG_QP_TW];
+    constexpr int TW = XG_QP_TW, TH = XG_QP_TH, HR = TH + 7, ST = XG_QP_STRIP;
+    __shared__ xg_pix tile[HR][TW + 8];
+    __shared__ int16_t hs[3][HR][TW];
     const int lo = -(qp.pad - 4);                            /* first output position (x and y) */
     const int xe = qp.w + qp.pad - 4, ye = qp.h + qp.pad - 4; /* one past the last */
-    const int x0 = lo + (int)blockIdx.x * XG_QP_TW, y0 = lo + (int)blockIdx.y * XG_QP_TH;
+    const int x0 = lo + (int)blockIdx.x * TW, y0 = lo + (int)blockIdx.y * TH;
+    const intptr_t pitch = qp.pitch;
     /* stage rows y0-3 .. y0+TH+3 and columns x0-3 .. x0+TW+4, inside the padded allocation */
-    for (int i = threadIdx.x; i < (XG_QP_TH + 7) * (XG_QP_TW + 7); i += blockDim.x) {
-        int r = i / (XG_QP_TW + 7), c = i % (XG_QP_TW + 7);
+    for (int i = threadIdx.x; i < HR * (TW + 7); i += blockDim.x) {
+        int r = i / (TW + 7), c = i - r * (TW + 7);
         int gy = y0 - 3 + r, gx = x0 - 3 + c;
         bool in = gy >= -ref.pad && gy < ref.h + ref.pad && gx >= -ref.pad && gx < ref.w + ref.pad;
         tile[r][c] = in ? ref.data[(intptr_t)gy * ref.pitch + gx] : (xg_pix)0;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < 3 * (XG_QP_TH + 7) * XG_QP_TW; i += blockDim.x) {
-        int f = i / ((XG_QP_TH + 7) * XG_QP_TW), rem = i % ((XG_QP_TH + 7) * XG_QP_TW);
-        int r = rem / XG_QP_TW, c = rem % XG_QP_TW;
-        hs[f][r][c] = xg_if_to_s16<8>(&tile[r][c + 3], 1, c_luma_taps[0][4 * (f + 1)]);
+    constexpr int sh1 = XG_IF_SHIFT - XG_IF_HEAD;
+    for (int i = threadIdx.x; i < HR * TW; i += blockDim.x) {
+        const int r = i / TW, c = i % TW;
+        int a[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[k] = tile[r][c + k];
+        int sum[3];
+#pragma unroll
+        for (int f = 0; f < 3; f++) {
+            sum[f] = 0;
+#pragma unroll
+            for (int k = 0; k < 8; k++) sum[f] += a[k] * xg_qp_tap(f, k);
+            hs[f][r][c] = (int16_t)((sum[f] - (XG_IF_OFF14 << sh1)) >> sh1);
+        }
+        const int oy = r - 3, gx = x0 + c, gy = y0 + oy;
+        if (oy >= 0 && oy < TH && gx < xe && gy < ye) {
+#pragma unroll
+            for (int f = 0; f < 3; f++)
+                qp.plane[1 + f][(intptr_t)gy * pitch + gx] = (xg_pix)xg_clip_pix((sum[f] + (1 << (XG_IF_SHIFT - 1))) >> XG_IF_SHIFT);
+        }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < 15 * XG_QP_TH * XG_QP_TW; i += blockDim.x) {
-        int q = 1 + i / (XG_QP_TH * XG_QP_TW), rem = i % (XG_QP_TH * XG_QP_TW);
-        int oy = rem / XG_QP_TW, ox = rem % XG_QP_TW;
-        int gx = x0 + ox, gy = y0 + oy;
-        if (gx >= xe || gy >= ye) continue;
-        int fx = (q & 3) * 4, fy = (q >> 2) * 4;
-        int v;
-        if (!fy) {
-            v = xg_if_pix<8>(&tile[oy + 3][ox + 3], 1, c_luma_taps[0][fx]);
-        } else if (!fx) {
-            v = xg_if_pix<8>(&tile[oy + 3][ox + 3], XG_QP_TW + 8, c_luma_taps[0][fy]);
-        } else {
-            const int8_t *tv = c_luma_taps[0][fy];
-            const int f = (fx >> 2) - 1;
-            int sum = 0;
+    const int c = threadIdx.x % TW, oy0 = (threadIdx.x / TW) * ST, gx = x0 + c;
+    if (gx >= xe) return;
+    const int nrow = min(ST, ye - (y0 + oy0));               /* output rows of this strip inside the area */
 #pragma unroll
-            for (int k = 0; k < 8; k++) sum += (int)hs[f][oy + k][ox] * (int)tv[k];
-            v = xg_s16_to_pix(sum);
+    for (int src = 0; src < 4; src++) {                      /* 0: integer samples, 1..3: first-stage phase src - 1 */
+        int w[ST + 7];
+#pragma unroll
+        for (int k = 0; k < ST + 7; k++) w[k] = src == 0 ? (int)tile[oy0 + k][c + 3] : (int)hs[src - 1][oy0 + k][c];
+#pragma unroll
+        for (int j = 0; j < ST; j++) {
+            if (j >= nrow) break;
+            const intptr_t off = (intptr_t)(y0 + oy0 + j) * pitch + gx;
+#pragma unroll
+            for (int f = 0; f < 3; f++) {
+                int v = 0;
+#pragma unroll
+                for (int k = 0; k < 8; k++) v += w[j + k] * xg_qp_tap(f, k);
+                v = src == 0 ? xg_clip_pix((v + (1 << (XG_IF_SHIFT - 1))) >> XG_IF_SHIFT) : xg_s16_to_pix(v);
+                qp.plane[(f + 1) * 4 + src][off] = (xg_pix)v;
+            }
         }
-        qp.plane[q][(intptr_t)gy * qp.pitch + gx] = (xg_pix)v;
     }
 }
 
