@@ -780,6 +780,7 @@ __device__ void xg_tq(XgTqSmem<N> &sm, const XgQuant &qz, int s1, int s2, unsign
                       int tid, int g)
 {
     constexpr int K = XgTqSmem<N>::K;
+    unsigned long long mask = 0;     /* this thread's nonzero 4x4 groups */
     xg_mm<K, N, N, NT>(tid, sm.mat, N, 1, sm.resT, 1, N, [&](int k, int i, int acc) {
         sm.t1T[i * K + k] = (int16_t)xg_clip16(xg_rshift_rnd(acc, s1));
     });
@@ -791,8 +792,11 @@ __device__ void xg_tq(XgTqSmem<N> &sm, const XgQuant &qz, int s1, int s2, unsign
         qv = xg_clip16(t < 0 ? -qv : qv);
         qout[(intptr_t)kv * qpitch + kh] = (xg_coef)qv;
         sm.rr[kv * K + kh] = (int16_t)xg_clip16((int)(((long long)qv * qz.iqmult + qz.iqadd) >> qz.iqshift));
-        if (qv) atomicOr(nz, 1ull << ((kv >> 2) * (K >> 2) + (kh >> 2)));
+        if (qv) mask |= 1ull << ((kv >> 2) * (K >> 2) + (kh >> 2));
     });
+    /* one shared-memory OR per warp instead of one per nonzero coefficient */
+    const unsigned lo = __reduce_or_sync(0xffffffffu, (unsigned)mask), hi = __reduce_or_sync(0xffffffffu, (unsigned)(mask >> 32));
+    if ((tid & 31) == 0 && (lo | hi)) atomicOr(nz, ((unsigned long long)hi << 32) | lo);
     if (N > K)      /* the zeroed-out high frequencies */
         for (int o = tid; o < N * N; o += NT) {
             int y = o / N, x = o % N;
@@ -821,7 +825,12 @@ __device__ void xg_itq(XgTqSmem<N> &sm, const xg_pix *pred, const xg_pix *org, i
         int d = (int)org[(intptr_t)y * opitch + x] - v;
         part += (unsigned long long)(d * d);
     });
-    atomicAdd(ssd, part);
+    /* warp sum in 32 bits: a thread holds at most ceil(N * N / NT) squared
+     * differences, each at most (2^bitdepth - 1)^2, so 32 threads' sum stays below 2^32 */
+    static_assert((unsigned long long)((N * N + NT - 1) / NT) * 32 * ((1ull << XG_BITDEPTH) - 1) * ((1ull << XG_BITDEPTH) - 1) <
+                      (1ull << 32), "warp SSD sum fits 32 bits");
+    const unsigned wsum = __reduce_add_sync(0xffffffffu, (unsigned)part);
+    if ((tid & 31) == 0) atomicAdd(ssd, (unsigned long long)wsum);
     xg_gsync<NT, CPB>(g);
 }
 
