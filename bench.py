@@ -338,7 +338,7 @@ def run_gpu(args):
     serving = None
     if rank == 0 and world == 1:
         from xin26x_gb300 import serve_bench
-        serving = serve_bench.run(seconds=3.0, mpix_budget=1200.0, max_inflight=6)
+        serving = serve_bench.run(seconds=3.0, mpix_budget=1650.0, max_inflight=6)
 
     out = None
     if rank == 0:

@@ -847,8 +847,11 @@ struct XgTailSmem {
 
 /* CPB CUs of size S (luma S x S, chroma S/2 x S/2) per CTA, NT threads per CU
  * (NT = 32: one warp per CU, warp-synchronous) */
+/* CTAs per SM the register allocation must allow: 64 x 64 CUs are held to five by
+ * shared memory anyway, the other sizes keep eight 128-thread CTAs (64 registers) */
+__host__ __device__ constexpr int xg_tail_min_ctas(int s) { return s == 64 ? 5 : 8; }
 template <int S, int NT, int CPB>
-__global__ void __launch_bounds__(NT * CPB) k_cu_tail(XgTailParams p, const XgPicParams *pp, int ncu)
+__global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTailParams p, const XgPicParams *pp, int ncu)
 {
     constexpr int C = S / 2;
     __shared__ XgTailSmem<S, NT> shm[CPB];
@@ -878,57 +881,77 @@ __global__ void __launch_bounds__(NT * CPB) k_cu_tail(XgTailParams p, const XgPi
     const int mxx = (int16_t)(p.W + (p.ctu - S + 8) - cx), mxy = (int16_t)(p.H + (p.ctu - S + 8) - cy);
 
     /* ---- Xin266FullSubPelMe on the quarter-pel planes (h266_sub_pel_refine.c:81-212) */
-    const int offx[8] = { -1, 1, 0, 0, -1, 1, -1, 1 }, offy[8] = { 0, 0, -1, 1, -1, -1, 1, 1 };
+    /* candidate c of a step: (offx(c), offy(c)) * step, the fixed order of the
+     * reference's eight neighbours; offsets + 1 packed two bits per candidate */
+    auto offx = [](int c) { return (int)((0x8858u >> (2 * c)) & 3u) - 1; };   /* -1, 1, 0, 0, -1, 1, -1, 1 */
+    auto offy = [](int c) { return (int)((0xA085u >> (2 * c)) & 3u) - 1; };   /*  0, 0, -1, 1, -1, -1, 1, 1 */
     const xg_pix *org = p.cur[0].data + (intptr_t)cy * p.cur[0].pitch + cx;
+    const intptr_t qpitch = p.qpel.pitch;                /* plane[0] is the reference slot, same pitch */
     int bx = 4 * imx, by = 4 * imy;
     uint32_t bc = (uint32_t)(key >> 32);
     /* the search runs only when the integer start lies in the window (h266_sub_pel_refine.c:117-120) */
     const bool start_in = imx >= mnx && imy >= mny && imx <= mxx && imy <= mxy;
     for (int step = 2; step >= 1 && start_in; step--) {
         const int bx0 = bx, by0 = by;
+        const xg_pix *cb[8];                              /* candidate blocks (top-left sample) */
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const int tx = bx0 + offx(c) * step, ty = by0 + offy(c) * step;
+            cb[c] = p.qpel.plane[(ty & 3) * 4 + (tx & 3)] + (intptr_t)(cy + (ty >> 2)) * qpitch + cx + (tx >> 2);
+        }
         uint32_t acc[8];
 #pragma unroll
         for (int c = 0; c < 8; c++) acc[c] = 0;
+#pragma unroll 1
         for (int i = tid; i < S * S; i += NT) {
-            int x = i % S, y = i / S;
-            int o = org[(intptr_t)y * p.cur[0].pitch + x];
+            const int x = i % S, y = i / S;
+            const unsigned o = org[(intptr_t)y * p.cur[0].pitch + x];
+            const intptr_t off = (intptr_t)y * qpitch + x;
 #pragma unroll
-            for (int c = 0; c < 8; c++) {
-                int tx = bx0 + offx[c] * step, ty = by0 + offy[c] * step;
-                const xg_pix *pl = (tx & 3) | (ty & 3) ? p.qpel.plane[(ty & 3) * 4 + (tx & 3)] : p.ref[0].data;
-                int v = pl[(intptr_t)(cy + y + (ty >> 2)) * p.qpel.pitch + cx + x + (tx >> 2)];
-                acc[c] += (uint32_t)abs(o - v);
-            }
+            for (int c = 0; c < 8; c++) acc[c] = __usad(o, (unsigned)cb[c][off], acc[c]);
         }
-        /* every thread ends with the eight sums (one warp) or reads them back (several) */
+        /* butterfly over the warp that also transposes: lane l ends with the warp's
+         * sum of candidate l >> 2 (9 shuffles for the eight sums) */
+        uint32_t r4[4], r2[2];
 #pragma unroll
-        for (int c = 0; c < 8; c++) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+        for (int j = 0; j < 4; j++) {
+            const bool hi = lane & 16;
+            r4[j] = (hi ? acc[4 + j] : acc[j]) + __shfl_xor_sync(0xffffffffu, hi ? acc[j] : acc[4 + j], 16);
         }
-        if (NT > 32) {
-            if (lane == 0) {
 #pragma unroll
-                for (int c = 0; c < 8; c++) m.part[c][warp] = acc[c];
-            }
+        for (int j = 0; j < 2; j++) {
+            const bool hi = lane & 8;
+            r2[j] = (hi ? r4[2 + j] : r4[j]) + __shfl_xor_sync(0xffffffffu, hi ? r4[j] : r4[2 + j], 8);
+        }
+        uint32_t sad;
+        {
+            const bool hi = lane & 4;
+            sad = (hi ? r2[1] : r2[0]) + __shfl_xor_sync(0xffffffffu, hi ? r2[0] : r2[1], 4);
+        }
+        sad += __shfl_xor_sync(0xffffffffu, sad, 2);
+        sad += __shfl_xor_sync(0xffffffffu, sad, 1);
+        const int c = lane >> 2;
+        if (NT > 32) {                                   /* the group's warps: sums through shared memory */
+            if ((lane & 3) == 0) m.part[c][warp] = sad;
             xg_gsync<NT, CPB>(g);
+            uint32_t t = 0;
 #pragma unroll
-            for (int c = 0; c < 8; c++) {
-                uint32_t t = 0;
-                for (int w = 0; w < NT / 32; w++) t += m.part[c][w];
-                acc[c] = t;
-            }
+            for (int w = 0; w < NT / 32; w++) t += m.part[c][w];
+            sad = t;
             xg_gsync<NT, CPB>(g);
         }
-        /* strict '<' in the fixed candidate order (h266_sub_pel_refine.c:146-160) */
-        int nbx = bx0, nby = by0;
+        /* strict '<' in the fixed candidate order (h266_sub_pel_refine.c:146-160):
+         * the earliest candidate of the smallest cost, taken if below the best so far */
+        const int tx = bx0 + offx(c) * step, ty = by0 + offy(c) * step;
+        uint32_t cost = (sad << XG_COST_FRACTION) + (xg_mvd_bits(tx) + xg_mvd_bits(ty)) * pp->lambda;
+        int cc = c;
 #pragma unroll
-        for (int c = 0; c < 8; c++) {
-            int tx = bx0 + offx[c] * step, ty = by0 + offy[c] * step;
-            uint32_t cost = (acc[c] << XG_COST_FRACTION) + (xg_mvd_bits(tx) + xg_mvd_bits(ty)) * pp->lambda;
-            if (cost < bc) { bc = cost; nbx = tx; nby = ty; }
+        for (int o = 4; o < 32; o <<= 1) {
+            const uint32_t oc = __shfl_xor_sync(0xffffffffu, cost, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, cc, o);
+            if (oc < cost || (oc == cost && oi < cc)) { cost = oc; cc = oi; }
         }
-        bx = nbx; by = nby;
+        if (cost < bc) { bc = cost; bx = bx0 + offx(cc) * step; by = by0 + offy(cc) * step; }
     }
     const int mvx = bx, mvy = by;
 

@@ -13,7 +13,7 @@ run.  Reported: admitted / refused streams, luma Mpixel/s completed, and the
 latency of each picture from submit to results in host memory (p50 / p99 /
 max), measured inside the server.
 
-  python -m xin26x_gb300.serve_bench [--seconds 4] [--mpix-budget 1200] [--max-inflight 6]
+  python -m xin26x_gb300.serve_bench [--seconds 4] [--mpix-budget 1650] [--max-inflight 6]
 """
 from __future__ import annotations
 
@@ -31,7 +31,7 @@ FPS = 30.0
 LAMBDA = {27: 45, 32: 64, 37: 91}
 
 
-def run(seconds=4.0, mpix_budget=1200.0, max_inflight=6, seed=48, search_range=64, frames_per_class=6):
+def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=64, frames_per_class=6):
     from xin26x_gb300 import synth
     from xin26x_gb300.server import Admission, Server
 
@@ -139,7 +139,7 @@ def run(seconds=4.0, mpix_budget=1200.0, max_inflight=6, seed=48, search_range=6
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--seconds", type=float, default=4.0)
-    ap.add_argument("--mpix-budget", type=float, default=1200.0)
+    ap.add_argument("--mpix-budget", type=float, default=1650.0)
     ap.add_argument("--max-inflight", type=int, default=6)
     ap.add_argument("--seed", type=int, default=48)
     a = ap.parse_args()
