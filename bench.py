@@ -44,7 +44,8 @@ BD, IN_BD = 10, 8                      # the reference's 10-bit build on 8-bit p
 LAMBDA_BD = {k: v << (BD - IN_BD) for k, v in LAMBDA.items()}   # x4: the SAD scales with the samples
 NFRAMES = 30
 SEED = 1080
-ME_DRAM_BYTES = 5.260e6        # ncu: DRAM bytes of one k_me_tiles launch at this workload
+ME_DRAM_BYTES = 9.84e6         # ncu: DRAM bytes of one k_me_tiles<8> launch of the 10-bit build at this workload
+ME_ALGO_BYTES = 2 * 1920 * 1080 * 2   # current + reference luma, 16-bit samples
 
 
 def workload_config():
@@ -357,9 +358,9 @@ def run_gpu(args):
                "roofline": {"bound": "int", "kernel": "k_me_tiles<8> (8-bit samples, SADs x 4)", "achieved": achieved / 1e12,
                             "peak": peak.value / 1e12,
                             "unit": "Tabsdiff/s", "frac": achieved / peak.value, "traffic": ME_DRAM_BYTES,
-                            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one k_me_tiles launch "
-                                              "(ncu, 1080p, +-64, cold cache); algorithmic bytes (current + "
-                                              "reference luma) 4.15e6",
+                            "traffic_source": "dram__bytes.sum.per_second x duration of one k_me_tiles<8> launch "
+                                              "(ncu, 1080p, +-64, 10-bit build, cold cache); algorithmic bytes "
+                                              f"(current + reference luma, 16-bit samples) {ME_ALGO_BYTES:.3g}",
                             "peak_source": "xin_gpu_measure_sad_peak (8-bit library): the faster of vabsdiff4+dp4a and "
                                            "vabsdiff4.add register loops on this GPU, this run",
                             "algorithmic": f"(W/8)(H/8)(2R+1)^2*64 = {algo:.4g} abs differences per launch"},
