@@ -29,7 +29,11 @@ def _compare(out, ref, levels, label):
 
 
 @pytest.mark.parametrize("bd", (8, 10))
-@pytest.mark.parametrize("w,h,R,ctu", [(192, 128, 16, 64), (208, 120, 24, 64), (256, 136, 8, 128)])
+# search ranges that are not multiples of 8 put the band's first column off the
+# 8-sample grid the staging loads from; R = 3 wraps the 32 lanes of a pass over
+# several candidate rows; widths that are not multiples of 64 leave partial tiles
+@pytest.mark.parametrize("w,h,R,ctu", [(192, 128, 16, 64), (208, 120, 24, 64), (256, 136, 8, 128),
+                                       (200, 104, 13, 64), (136, 72, 3, 64), (176, 96, 37, 128)])
 def test_frame_pipeline_matches_oracle(bd, w, h, R, ctu):
     seq = synth.sequence(w, h, 3, seed=w + h + R, bitdepth=bd, objects=1)
     fs = FrameStream(w, h, ctu=ctu, search_range=R, out_q=True, out_rec=True, bitdepth=bd)
@@ -147,7 +151,8 @@ def test_frame_two_in_flight_equals_one_at_a_time():
             assert np.array_equal(a["q"][p], b["q"][p]) and np.array_equal(a["rec"][p], b["rec"][p])
 
 
-@pytest.mark.parametrize("w,h,R,ctu", [(192, 128, 16, 64), (416, 240, 64, 64), (256, 136, 24, 128)])
+@pytest.mark.parametrize("w,h,R,ctu", [(192, 128, 16, 64), (416, 240, 64, 64), (256, 136, 24, 128),
+                                       (200, 104, 13, 64)])
 def test_frame_8bit_input_in_10bit_build(w, h, R, ctu):
     """8-bit pictures into the 10-bit library (input_bitdepth 8: samples << 2, the
     integer search on the 8-bit samples with SADs x 4) give exactly the results

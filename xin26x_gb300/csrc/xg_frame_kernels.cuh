@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     extern __shared__ uint32_t sm[];
     __shared__ int swin[16][5][4];        /* per warp: windows of its four 8x8 CUs and its 16x16 CU */
     __shared__ int swin32[4][4], swin64[4];
-    __shared__ int sinterior[16];
+    __shared__ int sinterior[16], sinterior32[4];
     const int tx0 = blockIdx.x * XG_ME_TILE, ty0 = blockIdx.y * XG_ME_TILE;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nx = 2 * p.R + 1;
@@ -466,6 +466,8 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     if (threadIdx.x < 4) {
         int c32x = tx0 + (threadIdx.x & 1) * 32, c32y = ty0 + (threadIdx.x >> 1) * 32;
         xg_cu_window(p, c32x, c32y, 32, swin32[threadIdx.x][0], swin32[threadIdx.x][1], swin32[threadIdx.x][2], swin32[threadIdx.x][3]);
+        const int *w = swin32[threadIdx.x];
+        sinterior32[threadIdx.x] = w[0] <= -p.R && w[1] >= p.R && w[2] <= dyb0 && w[3] >= dyb0 + ndy - 1;
     }
     if (threadIdx.x == 0) xg_cu_window(p, tx0, ty0, 64, swin64[0], swin64[1], swin64[2], swin64[3]);
     __syncwarp();
@@ -483,14 +485,16 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
     const bool live32 = p.keys[1] && c32x + 32 <= p.W && c32y + 32 <= p.H;
     const bool live64 = threadIdx.x < XG_ME_SLOTS && p.keys[0] && tx0 + 64 <= p.W && ty0 + 64 <= p.H;
     const int w32 = (c32 & 1) * 2 + (c32 >> 1) * 8;          /* first warp of the quadrant: w32, +1, +4, +5 */
-    unsigned long long best32 = ~0ull, best64 = ~0ull;
+    unsigned long long best32 = NONE, best64 = ~0ull;
     __syncthreads();
-    const bool interior = sinterior[warp];
+    const bool interior = sinterior[warp], interior32 = sinterior32[c32];
 
     /* key = SAD * key_mul + MV bits (a multiplier read at run time keeps the key
      * arithmetic on the multiply-add pipe, beside the SADs on the integer pipe);
      * key_mul = 1 << (XG_COST_FRACTION + XG_ME_DB + SH) */
     const uint32_t kmul = p.key_mul;
+    /* the same for the 32x32 costs: cost = SAD32 * cmul + MV bits */
+    const uint32_t cmul = kmul >> XG_ME_DB;
     /* v / nx = umulhi(v, nx_rcp) for every v < 2^17 and odd nx in 3..513 (checked exhaustively) */
     const uint32_t nx_rcp = 0xFFFFFFFFu / (uint32_t)nx + 1u;
     const int npass = (nv + 31) / 32;
@@ -502,8 +506,10 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
         const bool vvalid = chunk < nch;
         /* lanes past the last slot repeat slot nv - 1: same key, no effect */
         const int ck = vvalid ? chunk : nch - 1, cl = vvalid ? col : nx - 1;
+        const int row0 = ck * XG_ME_D, dx = cl - p.R, dyl = dyb0 + row0;
+        const uint32_t gidx0 = (uint32_t)((dyl + p.R) * nx + cl);   /* raster index of candidate row 0 of the slot */
+        const uint32_t mx = mvcx[cl];
         {
-            const int row0 = ck * XG_ME_D;
             const uint32_t *base = refw + (by + row0) * p.row_words + bx + cl;
             uint32_t acc[XG_ME_D][4];
 #pragma unroll
@@ -577,9 +583,6 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
              * a (cost, raster index) compare with the lane's running best.  Keys of
              * candidates outside the band or the window are >= XG_ME_KEY_INVALID,
              * above any real key (costs stay below 2^27). */
-            const int dx = cl - p.R, dyl = dyb0 + row0;
-            const uint32_t gidx0 = (uint32_t)((dyl + p.R) * nx + cl);
-            const uint32_t mx = mvcx[cl];
             uint32_t md[XG_ME_D];
 #pragma unroll
             for (int d = 0; d < XG_ME_D; d++) md[d] = mx + mvcy[row0 + d];
@@ -632,13 +635,17 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
                 const uint32_t s32 = r16[w32 * XG_ME_SLOTS] + r16[(w32 + 1) * XG_ME_SLOTS] + r16[(w32 + 4) * XG_ME_SLOTS] +
                                      r16[(w32 + 5) * XG_ME_SLOTS];
                 s32r[((grp * nb + pb) * 4 + c32) * XG_ME_SLOTS + d * 32 + lane] = s32;
-                if (live32 && vvalid && row < ndy) {
-                    const int dx = cl - p.R, dy = dyb0 + row;
-                    const uint32_t cost = (s32 << (XG_COST_FRACTION + SH)) + ((mvcx[cl] + mvcy[row]) >> XG_ME_DB);
-                    const unsigned long long kk = ((unsigned long long)cost << 32) | (uint32_t)((dy + p.R) * nx + cl);
-                    if (dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3] && kk < best32)
-                        best32 = kk;
+                /* rows past the band carry the sentinel (cost >= NONE's, never taken); lanes
+                 * past the last slot repeat slot nv - 1; CUs outside the picture are not
+                 * published */
+                const uint32_t cost = s32 * cmul + ((mx + mvcy[row]) >> XG_ME_DB);
+                const unsigned long long kk = ((unsigned long long)cost << 32) | (gidx0 + (uint32_t)d * (uint32_t)nx);
+                bool in = true;
+                if (!interior32) {
+                    const int dy = dyb0 + row;
+                    in = dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3];
                 }
+                if (in && kk < best32) best32 = kk;
             }
         }
         /* 64x64 every nb passes, from the four quadrants' 32x32 SADs (the ring is
@@ -684,7 +691,7 @@ __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, con
         unsigned long long k = best32;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) { unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o); k = v < k ? v : k; }
-        if (lane == 0 && live32 && k != ~0ull) atomicMin(p.keys[1] + (c32y / 32) * p.cus_x[1] + c32x / 32, k);
+        if (lane == 0 && live32 && k < NONE) atomicMin(p.keys[1] + (c32y / 32) * p.cus_x[1] + c32x / 32, k);
         k = best64;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) { unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o); k = v < k ? v : k; }
