@@ -186,3 +186,58 @@ def test_frame_8bit_input_in_10bit_build(w, h, R, ctu):
         levels = FrameStream(w, h, ctu=ctu, search_range=R, bitdepth=10).levels
         ref = oracle_frame.run(up[2], up[1], levels, ctu=ctu, search_range=R, qp=37, uv_qp=38, sad_lambda=400, bitdepth=10)
         _compare(runs[0][1], ref, levels, ("8-bit input", w, h, R))
+
+
+@pytest.mark.parametrize("bd,inb", [(8, 0), (10, 0), (10, 8)])
+def test_device_io_matches_host(bd, inb):
+    """device_io streams (pictures already in GPU memory, results left there) fill
+    their slots from the caller's device planes -- 8-bit samples << 2 in the
+    10-bit library with input_bitdepth 8 -- and give the CU records of a
+    host-buffer stream on the same pictures (an odd search range, a partial tile)."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    from xin26x_gb300 import _lib
+    from xin26x_gb300.frame import CU_DTYPE
+
+    w, h, R = 200, 104, 13
+    seq = synth.sequence(w, h, 3, seed=11, bitdepth=inb or bd, objects=1)
+    lam = [70, 40, 90]
+    fs = FrameStream(w, h, search_range=R, out_q=False, out_rec=False, bitdepth=bd, input_bitdepth=inb)
+    host = []
+    try:
+        for k in range(3):
+            fs.submit(*seq[k], qp=30 + k, uv_qp=31 + k, sad_lambda=lam[k])
+            out = fs.wait()
+            if k:
+                host.append(out["cu"].copy())
+    finally:
+        fs.close()
+
+    class _Dev:      # a device byte range as a CUDA array for torch
+        def __init__(self, ptr, n):
+            self.__cuda_array_interface__ = {"shape": (n,), "typestr": "|u1", "data": (ptr, False), "version": 3}
+
+    lib = _lib.load(bd)
+    cfg = _lib.xin_gpu_stream_cfg(w, h, 64, R, 120, 0, 1, 1, inb)
+    hs = C.c_void_p()
+    assert lib.xin_gpu_stream_open(C.byref(cfg), C.byref(hs)) == 0, lib.xin_gpu_last_error()
+    try:
+        ncus = lib.xin_gpu_stream_num_cus(hs)
+        dev = [[torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f] for f in seq]
+        for k in range(3):
+            pic = _lib.xin_gpu_picture()
+            for i, t in enumerate(dev[k]):
+                pic.plane[i] = t.data_ptr()
+                pic.stride[i] = t.shape[1]
+            pic.qp, pic.uv_qp, pic.sad_lambda = 30 + k, 31 + k, lam[k]
+            assert lib.xin_gpu_frame_submit(hs, C.byref(pic)) == 0, lib.xin_gpu_last_error()
+            res = _lib.xin_gpu_results()
+            assert lib.xin_gpu_frame_wait(hs, C.byref(res), 60000) == 0, lib.xin_gpu_last_error()
+            if k:
+                cu, q, r = C.c_void_p(), (C.c_void_p * 3)(), (C.c_void_p * 3)()
+                assert lib.xin_gpu_stream_device_results(hs, C.byref(cu), q, r) == 0
+                raw = torch.as_tensor(_Dev(cu.value, ncus * CU_DTYPE.itemsize), device="cuda").cpu().numpy()
+                got = raw.view(CU_DTYPE)
+                assert np.array_equal(got, host[k - 1]), (bd, inb, k)
+    finally:
+        lib.xin_gpu_stream_close(hs)

@@ -340,6 +340,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
     /* upload and pad the current picture; it becomes the next picture's reference */
     xg_stage_event(t.evs[0], st, capturing);
     cudaMemcpyAsync(t.dpp, t.h_pp, sizeof(XgPicParams), cudaMemcpyHostToDevice, st);
+    int mode = XG_FILL_IN_PLACE;
     if (s->widen) {
         /* 8-bit samples into the 10-bit slot (<< 2) */
         if (!c.device_io)
@@ -347,19 +348,22 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
                 const XgPlane &pl = s->slot[cur][p];
                 cudaMemcpyAsync(t.d_in8[p], t.h_in[p], (size_t)pl.w * pl.h, cudaMemcpyHostToDevice, st);
             }
-        k_copy_in8<<<152 * 4, 256, 0, st>>>(s->slot[cur][0], s->slot[cur][1], s->slot[cur][2], t.dpp, t.d_in8[0], t.d_in8[1],
-                                            t.d_in8[2], c.device_io ? 0 : 1);
-        nl++;
+        mode = c.device_io ? XG_FILL_DEV8 : XG_FILL_STAGED8;
     } else if (c.device_io) {
-        k_copy_in<<<152 * 4, 256, 0, st>>>(s->slot[cur][0], s->slot[cur][1], s->slot[cur][2], t.dpp);
-        nl++;
-    }
-    for (int p = 0; p < 3; p++) {
-        XgPlane &pl = s->slot[cur][p];
-        if (!c.device_io && !s->widen)
+        mode = XG_FILL_DEVPIX;
+    } else {
+        for (int p = 0; p < 3; p++) {
+            XgPlane &pl = s->slot[cur][p];
             cudaMemcpy2DAsync(pl.data, (size_t)pl.pitch * sizeof(xg_pix), t.h_in[p], (size_t)pl.w * sizeof(xg_pix),
                               (size_t)pl.w * sizeof(xg_pix), pl.h, cudaMemcpyHostToDevice, st);
-        k_pad<<<152 * 4, 256, 0, st>>>(pl);
+        }
+    }
+    {
+        /* copy-in and edge replication of the three planes: 8 samples a thread */
+        const XgPlane &ly = s->slot[cur][0];
+        dim3 grd(((ly.w + 2 * ly.pad + 7) / 8 + 127) / 128, ly.h + 2 * ly.pad, 3);
+        k_fill_slot<<<grd, 128, 0, st>>>(s->slot[cur][0], s->slot[cur][1], s->slot[cur][2], t.dpp, t.d_in8[0], t.d_in8[1],
+                                         t.d_in8[2], mode);
         nl++;
     }
     xg_stage_event(t.evs[1], st, capturing);

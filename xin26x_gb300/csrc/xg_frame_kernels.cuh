@@ -1,10 +1,11 @@
 /*
  * xg_frame_kernels.cuh -- kernels of the batched frame form.
  *
- *   k_pad            edge replication of a picture into its padded slot
- *                    (the layout of Xin266ConstructRefPicBuf / Xin26xExtendPicture,
+ *   k_fill_slot      a picture into its padded slot: copy-in (and 8-bit samples
+ *                    << 2) with edge replication (the layout of
+ *                    Xin266ConstructRefPicBuf / Xin26xExtendPicture,
  *                    h266_encoder/source/h266_encoder_create.c:1065-1077, with a
- *                    wider margin on the GPU)
+ *                    wider margin on the GPU), all planes in one launch
  *   k_qpel_planes    the 15 fractional quarter-pel luma planes of a reference
  *                    picture, each sample computed exactly like
  *                    Xin266LumaInterpolation computes it for a block
@@ -22,18 +23,6 @@ struct XgPlane {            /* padded plane: data points at picture (0, 0) */
     int pitch;              /* elements */
     int w, h, pad;          /* picture size and margin on each side */
 };
-
-/* ------------------------------------------------------------------ k_pad */
-__global__ void k_pad(XgPlane p)
-{
-    int pw = p.w + 2 * p.pad, ph = p.h + 2 * p.pad;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < pw * ph; i += gridDim.x * blockDim.x) {
-        int x = i % pw - p.pad, y = i / pw - p.pad;
-        if (x >= 0 && x < p.w && y >= 0 && y < p.h) continue;
-        int sx = min(max(x, 0), p.w - 1), sy = min(max(y, 0), p.h - 1);
-        p.data[(intptr_t)y * p.pitch + x] = p.data[(intptr_t)sy * p.pitch + sx];
-    }
-}
 
 /* -------------------------------------------------------------- qpel planes
  * plane index q = (fy / 4) * 4 + fx / 4 for phases fx, fy in {0, 4, 8, 12};
@@ -171,37 +160,59 @@ struct XgPicParams {
     long long src_stride[3];
 };
 
-/* copy a device-resident picture into the padded slot (device_io streams) */
-__global__ void k_copy_in(XgPlane y, XgPlane u, XgPlane v, const XgPicParams *pp)
-{
-    const int ny = y.w * y.h, nc = u.w * u.h;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ny + 2 * nc; i += gridDim.x * blockDim.x) {
-        if (i < ny) {
-            y.data[(intptr_t)(i / y.w) * y.pitch + i % y.w] = pp->src[0][(intptr_t)(i / y.w) * pp->src_stride[0] + i % y.w];
-        } else {
-            int k = i - ny, pl = k < nc ? 1 : 2;
-            k -= (pl - 1) * nc;
-            XgPlane &d = pl == 1 ? u : v;
-            d.data[(intptr_t)(k / d.w) * d.pitch + k % d.w] = pp->src[pl][(intptr_t)(k / d.w) * pp->src_stride[pl] + k % d.w];
-        }
-    }
-}
+/* Sources of k_fill_slot: where a picture's samples come from */
+enum XgFillMode {
+    XG_FILL_IN_PLACE = 0,   /* the slot's interior already holds the picture (host upload): margins only */
+    XG_FILL_STAGED8 = 1,    /* 8-bit samples in the per-set device staging, rows of the plane width, << 2 */
+    XG_FILL_DEV8 = 2,       /* 8-bit samples at the caller's device planes (picture parameters), << 2 */
+    XG_FILL_DEVPIX = 3      /* samples of the library's depth at the caller's device planes */
+};
 
-/* 8-bit pictures into the 10-bit library's padded slot, samples << 2: from the
- * per-set device staging (staged = 1) or from the caller's device planes in the
- * picture parameters (device_io streams; 8-bit samples) */
-__global__ void k_copy_in8(XgPlane y, XgPlane u, XgPlane v, const XgPicParams *pp, const uint8_t *s0, const uint8_t *s1,
-                           const uint8_t *s2, int staged)
+/* Every position of the three padded planes of a slot: the source sample at the
+ * position clamped to the picture (edge replication, the layout of
+ * Xin266ConstructRefPicBuf / Xin26xExtendPicture), in one launch.  Grid
+ * (column groups, padded rows, plane); a thread writes 8 consecutive samples of
+ * one row with one 16-byte (8-byte) store: the margins are multiples of 16
+ * samples and the slot's data and pitch multiples of 32 / 128, so a group starts
+ * on a 16-byte boundary. */
+__global__ void __launch_bounds__(128) k_fill_slot(XgPlane y, XgPlane u, XgPlane v, const XgPicParams *pp, const uint8_t *s0,
+                                                   const uint8_t *s1, const uint8_t *s2, int mode)
 {
-    const int ny = y.w * y.h, nc = u.w * u.h;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ny + 2 * nc; i += gridDim.x * blockDim.x) {
-        int pl = 0, k = i;
-        if (i >= ny) { k = i - ny; pl = k < nc ? 1 : 2; k -= (pl - 1) * nc; }
-        XgPlane &d = pl == 0 ? y : pl == 1 ? u : v;
-        const int row = k / d.w, col = k % d.w;
-        const uint8_t *src = staged ? (pl == 0 ? s0 : pl == 1 ? s1 : s2) : reinterpret_cast<const uint8_t *>(pp->src[pl]);
-        const long long stride = staged ? d.w : pp->src_stride[pl];
-        d.data[(intptr_t)row * d.pitch + col] = (xg_pix)((unsigned)src[(intptr_t)row * stride + col] << (XG_BITDEPTH - 8));
+    const int pl = blockIdx.z;
+    XgPlane d = y;
+    if (pl == 1) d = u;
+    else if (pl == 2) d = v;
+    const int yy = (int)blockIdx.y - d.pad, x0 = -d.pad + 8 * (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (yy >= d.h + d.pad || x0 >= d.w + d.pad) return;
+    const int sy = min(max(yy, 0), d.h - 1);
+    const bool inner_row = yy >= 0 && yy < d.h;
+    if (mode == XG_FILL_IN_PLACE && inner_row && x0 >= 0 && x0 + 8 <= d.w) return;   /* interior already there */
+    xg_pix vals[8];
+    if (mode == XG_FILL_IN_PLACE || mode == XG_FILL_DEVPIX) {
+        const xg_pix *row = mode == XG_FILL_IN_PLACE ? d.data + (intptr_t)sy * d.pitch : pp->src[pl] + (intptr_t)sy * pp->src_stride[pl];
+#pragma unroll
+        for (int j = 0; j < 8; j++) vals[j] = row[min(max(x0 + j, 0), d.w - 1)];
+    } else {
+        const uint8_t *row = mode == XG_FILL_STAGED8 ? (pl == 0 ? s0 : pl == 1 ? s1 : s2) + (intptr_t)sy * d.w
+                                                     : reinterpret_cast<const uint8_t *>(pp->src[pl]) + (intptr_t)sy * pp->src_stride[pl];
+#pragma unroll
+        for (int j = 0; j < 8; j++) vals[j] = (xg_pix)((unsigned)row[min(max(x0 + j, 0), d.w - 1)] << (XG_BITDEPTH - 8));
+    }
+    xg_pix *o = d.data + (intptr_t)yy * d.pitch + x0;
+    if (x0 + 8 <= d.w + d.pad) {
+        if constexpr (sizeof(xg_pix) == 2) {
+            uint4 w;
+            w.x = vals[0] | ((uint32_t)vals[1] << 16); w.y = vals[2] | ((uint32_t)vals[3] << 16);
+            w.z = vals[4] | ((uint32_t)vals[5] << 16); w.w = vals[6] | ((uint32_t)vals[7] << 16);
+            *reinterpret_cast<uint4 *>(o) = w;
+        } else {
+            uint2 w;
+            w.x = vals[0] | ((uint32_t)vals[1] << 8) | ((uint32_t)vals[2] << 16) | ((uint32_t)vals[3] << 24);
+            w.y = vals[4] | ((uint32_t)vals[5] << 8) | ((uint32_t)vals[6] << 16) | ((uint32_t)vals[7] << 24);
+            *reinterpret_cast<uint2 *>(o) = w;
+        }
+    } else {
+        for (int j = 0; j < 8 && x0 + j < d.w + d.pad; j++) o[j] = vals[j];
     }
 }
 
