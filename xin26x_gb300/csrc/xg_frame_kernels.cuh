@@ -733,43 +733,64 @@ __device__ __forceinline__ void xg_gsync(int g)
     else asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(NT) : "memory");
 }
 
-/* C(i, j) = sum_l A(i, l) * B(j, l) over shared-memory operands with
- * A(i, l) = A[i * asi + l * asl] and B(j, l) = B[j * bsj + l * bsl], computed by
- * the NT threads of a group (tid = rank in the group).  Each thread owns a
- * TI x TJ tile of outputs, consecutive threads consecutive j tiles, so B is
- * read along its contiguous dimension and A is broadcast; epi(i, j, acc)
- * consumes every output. */
+/* Output tiles of a thread in a NI x NJ product computed by NT threads: TI x TJ
+ * outputs, consecutive threads consecutive j tiles. */
 __host__ __device__ constexpr int xg_tile_j(int ni, int nj, int nt) { return (ni * nj >= 8 * nt && nj >= 64) ? 4 : ((ni * nj >= 2 * nt && nj >= 32) ? 2 : 1); }
 __host__ __device__ constexpr int xg_tile_i(int ni, int nj, int nt)
 {
     return (ni * nj / (nt * xg_tile_j(ni, nj, nt)) >= 4) ? 4 : ((ni * nj / (nt * xg_tile_j(ni, nj, nt)) >= 2) ? 2 : 1);
 }
 
-template <int NI, int NJ, int NL, int NT, typename TA, typename TB, typename F>
-__device__ __forceinline__ void xg_mm(int tid, const TA *A, int asi, int asl, const TB *B, int bsj, int bsl, F epi)
+/* TN consecutive 32-bit words of shared memory as one vector load */
+template <int TN>
+__device__ __forceinline__ void xg_ldw(const uint32_t *p, uint32_t *v)
 {
-    constexpr int TJ = xg_tile_j(NI, NJ, NT), TI = xg_tile_i(NI, NJ, NT);
-    constexpr int tj = NJ / TJ, tiles = (NI / TI) * tj;
+    if constexpr (TN == 8) { xg_ldw<4>(p, v); xg_ldw<4>(p + 4, v + 4); }
+    else if constexpr (TN == 4) { const uint4 q = *reinterpret_cast<const uint4 *>(p); v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w; }
+    else if constexpr (TN == 2) { const uint2 q = *reinterpret_cast<const uint2 *>(p); v[0] = q.x; v[1] = q.y; }
+    else v[0] = p[0];
+}
+
+/* C(i, j) = sum_l D(i, l) * M(j, l), D int16 and M int8, exact in 32 bits, by the
+ * NT threads of a group (tid = rank in the group); epi(i, j, acc) consumes every
+ * output.  Tiles: TI x TJ outputs a thread, consecutive threads consecutive j
+ * tiles; with IFAST one i row and up to 8 j a thread, consecutive threads
+ * consecutive i (for an epilogue that stores along i).  Operands are interleaved in 32-bit words so that one vector load gives
+ * a thread the words of its TI rows (TJ rows) at an l step, the loads of a warp
+ * are broadcasts or consecutive words, and one dp2a multiplies two int16 samples
+ * by two int8 coefficients:
+ *   D2[(l / 2) * NI + i] = D(i, l), D(i, l + 1)  (int16 pairs)
+ *   M4[(l / 4) * NJ + j] = M(j, l .. l + 3)      (int8 quads).  NL % 4 == 0. */
+__host__ __device__ constexpr int xg_tile_jq(int ni, int nj, int nt)
+{
+    return ni * nj / nt >= 8 ? (nj >= 8 ? 8 : nj) : ni * nj / nt >= 4 ? 4 : ni * nj / nt >= 2 ? 2 : 1;
+}
+template <int NI, int NJ, int NL, int NT, bool IFAST = false, typename F>
+__device__ __forceinline__ void xg_mm_dp2(int tid, const uint32_t *D2, const uint32_t *M4, F epi)
+{
+    constexpr int TJ = IFAST ? xg_tile_jq(NI, NJ, NT) : xg_tile_j(NI, NJ, NT), TI = IFAST ? 1 : xg_tile_i(NI, NJ, NT);
+    constexpr int tj = NJ / TJ, ti = NI / TI, tiles = ti * tj;
+    static_assert(NL % 4 == 0 && NI % TI == 0 && NJ % TJ == 0, "dp2a tiles");
     for (int t = tid; t < tiles; t += NT) {
-        const int i0 = (t / tj) * TI, j0 = (t % tj) * TJ;
+        const int i0 = (IFAST ? t % ti : t / tj) * TI, j0 = (IFAST ? t / ti : t % tj) * TJ;
         int acc[TI][TJ];
 #pragma unroll
         for (int a = 0; a < TI; a++)
 #pragma unroll
             for (int b = 0; b < TJ; b++) acc[a][b] = 0;
-        const TA *pa = A + i0 * asi;
-        const TB *pb = B + j0 * bsj;
-#pragma unroll 8
-        for (int l = 0; l < NL; l++) {
-            int av[TI], bv[TJ];
-#pragma unroll
-            for (int a = 0; a < TI; a++) av[a] = pa[a * asi + l * asl];
-#pragma unroll
-            for (int b = 0; b < TJ; b++) bv[b] = pb[b * bsj + l * bsl];
+#pragma unroll 4
+        for (int l4 = 0; l4 < NL / 4; l4++) {
+            uint32_t dlo[TI], dhi[TI], m[TJ];
+            xg_ldw<TI>(D2 + (2 * l4) * NI + i0, dlo);
+            xg_ldw<TI>(D2 + (2 * l4 + 1) * NI + i0, dhi);
+            xg_ldw<TJ>(M4 + l4 * NJ + j0, m);
 #pragma unroll
             for (int a = 0; a < TI; a++)
 #pragma unroll
-                for (int b = 0; b < TJ; b++) acc[a][b] += av[a] * bv[b];
+                for (int b = 0; b < TJ; b++) {
+                    acc[a][b] = __dp2a_lo((int)dlo[a], (int)m[b], acc[a][b]);
+                    acc[a][b] = __dp2a_hi((int)dhi[a], (int)m[b], acc[a][b]);
+                }
         }
 #pragma unroll
         for (int a = 0; a < TI; a++)
@@ -778,16 +799,43 @@ __device__ __forceinline__ void xg_mm(int tid, const TA *A, int asi, int asl, co
     }
 }
 
-/* Shared-memory work area of one N x N transform block (K = min(N, 32) kept frequencies). */
+/* element index of X(i, l) in the int16 pair layout of a D operand with NI rows */
+template <int NI>
+__device__ __forceinline__ int xg_d2(int i, int l) { return (((l >> 1) * NI + i) << 1) | (l & 1); }
+
+/* Shared-memory work area of one N x N transform block (K = min(N, 32) kept
+ * frequencies), every operand in the layout of the pass that reads it:
+ *   res  residual r(y, x)           D of the forward row pass     (rows y, l = x)
+ *   t1   row pass t1(y, k)          D of the forward column pass  (rows k, l = y)
+ *   rr   dequantised c(kv, kh)      D of the inverse column pass  (rows kh, l = kv)
+ *   t2   column pass t2(kh, y)      D of the inverse row pass     (rows y, l = kh)
+ *   mf   DCT2 rows k < K, M(k, x) = T(k, x)   (rows k, l = x or y)
+ *   mi   the transpose, M(x, k) = T(k, x)      (rows x, l = k) */
 template <int N>
 struct XgTqSmem {
     static constexpr int K = N > 32 ? 32 : N;
-    int16_t mat[K * N];          /* DCT2 rows k < K (row = basis function) */
-    int16_t resT[N * N];         /* residual, transposed: resT[x * N + y] */
-    int16_t t1T[N * K];          /* first forward pass, t1T[i * K + k] (row i, frequency k) */
-    int16_t rr[K * K];           /* dequantised coefficients rr[kv * K + kh] */
-    int16_t t2[K * N];           /* first inverse pass t2[j * N + x] */
+    alignas(16) uint32_t mf[K * N / 4];
+    alignas(16) uint32_t mi[K * N / 4];
+    alignas(16) int16_t res[N * N];
+    alignas(16) int16_t t1[N * K];
+    alignas(16) int16_t rr[K * K];
+    alignas(16) int16_t t2[K * N];
 };
+
+/* the DCT2 matrix T(k, x) (rows k < K of the N-point transform, from the library's
+ * table) into both packed layouts of a work area */
+template <int N, int NT>
+__device__ __forceinline__ void xg_tq_load_mat(XgTqSmem<N> &sm, const int16_t *m, int tid)
+{
+    constexpr int K = XgTqSmem<N>::K;
+    int8_t *mf = reinterpret_cast<int8_t *>(sm.mf), *mi = reinterpret_cast<int8_t *>(sm.mi);
+    for (int i = tid; i < K * N; i += NT) {
+        const int k = i / N, x = i % N;
+        const int8_t v = (int8_t)m[i];               /* |T(k, x)| <= 90 */
+        mf[(((x >> 2) * K + k) << 2) | (x & 3)] = v;
+        mi[(((k >> 2) * N + x) << 2) | (k & 3)] = v;
+    }
+}
 
 /* forward DCT2 (rows, then columns), keeping frequencies below 32 (the rest is
  * zeroed out), quant / dequant over the low min(N, 32) square with 4x4 coding
@@ -799,17 +847,19 @@ __device__ void xg_tq(XgTqSmem<N> &sm, const XgQuant &qz, int s1, int s2, unsign
 {
     constexpr int K = XgTqSmem<N>::K;
     unsigned long long mask = 0;     /* this thread's nonzero 4x4 groups */
-    xg_mm<K, N, N, NT>(tid, sm.mat, N, 1, sm.resT, 1, N, [&](int k, int i, int acc) {
-        sm.t1T[i * K + k] = (int16_t)xg_clip16(xg_rshift_rnd(acc, s1));
+    /* rows: t1(y, k) = sum_x r(y, x) T(k, x) */
+    xg_mm_dp2<N, K, N, NT>(tid, reinterpret_cast<const uint32_t *>(sm.res), sm.mf, [&](int y, int k, int acc) {
+        sm.t1[xg_d2<K>(k, y)] = (int16_t)xg_clip16(xg_rshift_rnd(acc, s1));
     });
     xg_gsync<NT, CPB>(g);
-    xg_mm<K, K, N, NT>(tid, sm.mat, N, 1, sm.t1T, 1, K, [&](int kv, int kh, int acc) {
+    /* columns: c(kv, kh) = sum_y t1(y, kh) T(kv, y), then quant / dequant */
+    xg_mm_dp2<K, K, N, NT, true>(tid, reinterpret_cast<const uint32_t *>(sm.t1), sm.mf, [&](int kh, int kv, int acc) {
         int t = xg_clip16(xg_rshift_rnd(acc, s2));
         int a = abs(t);
         int qv = (int)(((long long)a * qz.qmult + qz.qadd) >> qz.qshift);
         qv = xg_clip16(t < 0 ? -qv : qv);
         qout[(intptr_t)kv * qpitch + kh] = (xg_coef)qv;
-        sm.rr[kv * K + kh] = (int16_t)xg_clip16((int)(((long long)qv * qz.iqmult + qz.iqadd) >> qz.iqshift));
+        sm.rr[xg_d2<K>(kh, kv)] = (int16_t)xg_clip16((int)(((long long)qv * qz.iqmult + qz.iqadd) >> qz.iqshift));
         if (qv) mask |= 1ull << ((kv >> 2) * (K >> 2) + (kh >> 2));
     });
     /* one shared-memory OR per warp instead of one per nonzero coefficient */
@@ -832,12 +882,14 @@ __device__ void xg_itq(XgTqSmem<N> &sm, const xg_pix *pred, const xg_pix *org, i
 {
     constexpr int K = XgTqSmem<N>::K;
     const int s2 = 6 + 15 - 1 - XG_BITDEPTH;
-    xg_mm<K, N, K, NT>(tid, sm.rr, 1, K, sm.mat, 1, N, [&](int j, int x, int acc) {
-        sm.t2[j * N + x] = (int16_t)xg_clip16(xg_rshift_rnd(acc, 7));
+    /* columns: t2(kh, y) = sum_kv c(kv, kh) T(kv, y) */
+    xg_mm_dp2<K, N, K, NT>(tid, reinterpret_cast<const uint32_t *>(sm.rr), sm.mi, [&](int kh, int y, int acc) {
+        sm.t2[xg_d2<N>(y, kh)] = (int16_t)xg_clip16(xg_rshift_rnd(acc, 7));
     });
     xg_gsync<NT, CPB>(g);
     unsigned long long part = 0;
-    xg_mm<N, N, K, NT>(tid, sm.t2, 1, N, sm.mat, 1, N, [&](int y, int x, int acc) {
+    /* rows: r'(y, x) = sum_kh t2(kh, y) T(kh, x) */
+    xg_mm_dp2<N, N, K, NT>(tid, reinterpret_cast<const uint32_t *>(sm.t2), sm.mi, [&](int y, int x, int acc) {
         int v = xg_clip_pix((int)pred[y * N + x] + xg_clip16(xg_rshift_rnd(acc, s2)));
         rec[(intptr_t)y * rpitch + x] = (xg_pix)v;
         int d = (int)org[(intptr_t)y * opitch + x] - v;
@@ -890,8 +942,8 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
     {   /* DCT2 matrices of the luma (S) and chroma (S/2) blocks, rows k < 32 */
         constexpr int lgs = S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : 6;
         const int16_t *ml = xg_mat(0, lgs), *mc = xg_mat(0, lgs - 1);
-        for (int i = tid; i < XgTqSmem<S>::K * S; i += NT) tl.mat[i] = ml[i];
-        for (int i = tid; i < XgTqSmem<C>::K * C; i += NT) tc.mat[i] = mc[i];
+        xg_tq_load_mat<S, NT>(tl, ml, tid);
+        xg_tq_load_mat<C, NT>(tc, mc, tid);
     }
 
     /* window (h266_enc_init.c:1462) */
@@ -990,7 +1042,7 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
     const int lgS = S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : 6;
     for (int i = tid; i < S * S; i += NT) {
         int y = i / S, x = i % S;
-        tl.resT[x * S + y] = (int16_t)((int)org[(intptr_t)y * p.cur[0].pitch + x] - (int)pred[i]);
+        tl.res[xg_d2<S>(y, x)] = (int16_t)((int)org[(intptr_t)y * p.cur[0].pitch + x] - (int)pred[i]);
     }
     xg_gsync<NT, CPB>(g);
     xg_tq<S, NT, CPB>(tl, pp->quant[p.level][0], lgS + XG_BITDEPTH + 6 - 15, lgS + 6, &m.nz[0],
@@ -1022,7 +1074,7 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
             const xg_pix *corg = p.cur[pl].data + (intptr_t)(cy >> 1) * p.cur[pl].pitch + (cx >> 1);
             for (int i = tid; i < C * C; i += NT) {
                 int y = i / C, x = i % C;
-                tc.resT[x * C + y] = (int16_t)((int)corg[(intptr_t)y * p.cur[pl].pitch + x] - (int)pred[i]);
+                tc.res[xg_d2<C>(y, x)] = (int16_t)((int)corg[(intptr_t)y * p.cur[pl].pitch + x] - (int)pred[i]);
             }
             xg_gsync<NT, CPB>(g);
             xg_tq<C, NT, CPB>(tc, pp->quant[p.level][pl], lgC + XG_BITDEPTH + 6 - 15, lgC + 6, &m.nz[pl],
