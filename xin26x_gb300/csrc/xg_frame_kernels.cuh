@@ -972,7 +972,8 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
         uint32_t acc[8];
 #pragma unroll
         for (int c = 0; c < 8; c++) acc[c] = 0;
-#pragma unroll 1
+        /* two pixels' 18 loads in flight a trip (deeper unrolling spills at 32 and 64) */
+#pragma unroll 2
         for (int i = tid; i < S * S; i += NT) {
             const int x = i % S, y = i / S;
             const unsigned o = org[(intptr_t)y * p.cur[0].pitch + x];
