@@ -391,7 +391,9 @@ typedef struct xin_gpu_cu_result {
 
 typedef struct xin_gpu_results {
     xin_gpu_cu_result *cu;       /* [xin_gpu_stream_num_cus()], levels from 64 down to 8 */
-    XG_COEFF *q[3];              /* [levels][plane height][plane width] when XIN_GPU_OUT_Q */
+    XG_COEFF *q[3];              /* [levels][plane height][plane width] when XIN_GPU_OUT_Q; zero where
+                                    the level's CUs do not reach (right and bottom edges of pictures
+                                    that are not multiples of the CU size) */
     XG_PIXEL *rec[3];            /* same layout when XIN_GPU_OUT_REC */
     float    gpu_ms;             /* device time of the picture's launches */
 } xin_gpu_results;

@@ -33,7 +33,8 @@ def _compare(out, ref, levels, label):
 # 8-sample grid the staging loads from; R = 3 wraps the 32 lanes of a pass over
 # several candidate rows; widths that are not multiples of 64 leave partial tiles
 @pytest.mark.parametrize("w,h,R,ctu", [(192, 128, 16, 64), (208, 120, 24, 64), (256, 136, 8, 128),
-                                       (200, 104, 13, 64), (136, 72, 3, 64), (176, 96, 37, 128)])
+                                       (200, 104, 13, 64), (136, 72, 3, 64), (176, 96, 37, 128),
+                                       (202, 100, 11, 64)])
 def test_frame_pipeline_matches_oracle(bd, w, h, R, ctu):
     seq = synth.sequence(w, h, 3, seed=w + h + R, bitdepth=bd, objects=1)
     fs = FrameStream(w, h, ctu=ctu, search_range=R, out_q=True, out_rec=True, bitdepth=bd)
@@ -188,18 +189,20 @@ def test_frame_8bit_input_in_10bit_build(w, h, R, ctu):
         _compare(runs[0][1], ref, levels, ("8-bit input", w, h, R))
 
 
+@pytest.mark.parametrize("w,h", [(200, 104), (202, 100)])
 @pytest.mark.parametrize("bd,inb", [(8, 0), (10, 0), (10, 8)])
-def test_device_io_matches_host(bd, inb):
+def test_device_io_matches_host(bd, inb, w, h):
     """device_io streams (pictures already in GPU memory, results left there) fill
     their slots from the caller's device planes -- 8-bit samples << 2 in the
     10-bit library with input_bitdepth 8 -- and give the CU records of a
-    host-buffer stream on the same pictures (an odd search range, a partial tile)."""
+    host-buffer stream on the same pictures (an odd search range, a partial tile,
+    a width that is not a multiple of 8)."""
     torch = pytest.importorskip("torch")
     import ctypes as C
     from xin26x_gb300 import _lib
     from xin26x_gb300.frame import CU_DTYPE
 
-    w, h, R = 200, 104, 13
+    R = 13
     seq = synth.sequence(w, h, 3, seed=11, bitdepth=inb or bd, objects=1)
     lam = [70, 40, 90]
     fs = FrameStream(w, h, search_range=R, out_q=False, out_rec=False, bitdepth=bd, input_bitdepth=inb)

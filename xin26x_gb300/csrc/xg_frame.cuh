@@ -191,6 +191,10 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
             size_t n = (p ? lc : lq) * s->nlev;
             e = cudaMalloc(&t.dq[p], n * sizeof(xg_coef));
             if (e == cudaSuccess) e = cudaMalloc(&t.drec[p], n * sizeof(xg_pix));
+            /* the kernels write only the area a level's CUs cover: the rest stays zero
+             * (ordered on the stream, before any picture's launches) */
+            if (e == cudaSuccess) e = cudaMemsetAsync(t.dq[p], 0, n * sizeof(xg_coef), s->st);
+            if (e == cudaSuccess) e = cudaMemsetAsync(t.drec[p], 0, n * sizeof(xg_pix), s->st);
             if (c.device_io) continue;
             if (e == cudaSuccess && s->widen) e = cudaMalloc(&t.d_in8[p], p ? lc : lq);
             if (e == cudaSuccess) e = cudaMallocHost(&t.h_in[p], (p ? lc : lq) * s->in_es);
