@@ -349,7 +349,7 @@ template <bool B> struct xg_bool_c { static constexpr bool value = B; };
 /* keys at or above this are not candidates (padding rows, windows) */
 #define XG_ME_KEY_INVALID 0xC0000000u
 #define XG_ME_SMEM_MAX (216 * 1024)       /* dynamic shared memory of k_me_tiles, under the 227 KB a CTA may have */
-#define XG_ME_NB_MAX 4                    /* passes buffered between 64x64 updates (at most) */
+#define XG_ME_NB_MAX 8                    /* passes buffered between 64x64 updates (at most) */
 /* 16x16 SADs [2][16][slots] (double-buffered per pass) + 32x32 SADs [2][nb][4][slots], slots = 32 x rows */
 __host__ __device__ constexpr int xg_me_agg_words(int sbd, int nb) { return (2 * 16 + 2 * nb * 4) * 32 * xg_me_d(sbd); }
 static_assert(xg_me_d(8) % 4 == 0 && (1 << xg_me_db(8)) == xg_me_d(8) && xg_me_d(10) % 4 == 0 && (1 << xg_me_db(10)) == xg_me_d(10),
