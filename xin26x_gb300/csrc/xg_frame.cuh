@@ -40,10 +40,12 @@ struct xin_gpu_stream {
         xg_pix *h_rec[3];
         cudaEvent_t ev0, ev1;  /* submitted; results in host memory */
         cudaEvent_t ev_kern;   /* kernels done (the copy stream waits on it) */
+        cudaEvent_t ev_up;     /* the picture's parameters / staged samples are on the device */
         cudaEvent_t evs[5];    /* stage boundaries, recorded inside the picture's launches */
     } set[2];
     cudaStream_t st;
     cudaStream_t cst;      /* result copies (device to host) */
+    cudaStream_t ust;      /* uploads of the next picture's parameters and staged samples */
     cudaStream_t aux[3];   /* the tails of levels 2..4 run beside the first level's */
     cudaStream_t auxq;     /* quarter-pel planes of the new picture, beside the search (low priority) */
     cudaEvent_t ev_fork, ev_join[3], ev_qfork, ev_qjoin;
@@ -90,8 +92,10 @@ static int xg_stream_free(xin_gpu_stream *s)
         if (t.ev0) cudaEventDestroy(t.ev0);
         if (t.ev1) cudaEventDestroy(t.ev1);
         if (t.ev_kern) cudaEventDestroy(t.ev_kern);
+        if (t.ev_up) cudaEventDestroy(t.ev_up);
     }
     if (s->cst) cudaStreamDestroy(s->cst);
+    if (s->ust) cudaStreamDestroy(s->ust);
     for (int i = 0; i < 3; i++) {
         if (s->ev_join[i]) cudaEventDestroy(s->ev_join[i]);
         if (s->aux[i]) cudaStreamDestroy(s->aux[i]);
@@ -159,10 +163,12 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
 
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->ust, cudaStreamNonBlocking);
     for (auto &t : s->set) {
         if (e == cudaSuccess) e = cudaEventCreate(&t.ev0);
         if (e == cudaSuccess) e = cudaEventCreate(&t.ev1);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.ev_kern, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.ev_up, cudaEventDisableTiming);
         for (int i = 0; i < 5 && e == cudaSuccess; i++) e = cudaEventCreate(&t.evs[i]);
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
@@ -343,15 +349,11 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
     int nl = 0;
     /* upload and pad the current picture; it becomes the next picture's reference */
     xg_stage_event(t.evs[0], st, capturing);
-    cudaMemcpyAsync(t.dpp, t.h_pp, sizeof(XgPicParams), cudaMemcpyHostToDevice, st);
+    /* the parameters and (8-bit input) the staged samples were uploaded on the
+     * upload stream before this picture's launches (xin_gpu_frame_submit) */
     int mode = XG_FILL_IN_PLACE;
     if (s->widen) {
         /* 8-bit samples into the 10-bit slot (<< 2) */
-        if (!c.device_io)
-            for (int p = 0; p < 3; p++) {
-                const XgPlane &pl = s->slot[cur][p];
-                cudaMemcpyAsync(t.d_in8[p], t.h_in[p], (size_t)pl.w * pl.h, cudaMemcpyHostToDevice, st);
-            }
         mode = c.device_io ? XG_FILL_DEV8 : XG_FILL_STAGED8;
     } else if (c.device_io) {
         mode = XG_FILL_DEVPIX;
@@ -510,6 +512,17 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
     *t.h_pp = pp;
     bool with_me = s->nsub > 0;
     cudaEventRecord(t.ev0, s->st);
+    /* uploads on their own stream, so that they overlap the previous picture's
+     * kernels: set cur is not read by the picture in flight (it uses the other
+     * set), and its last user, picture nsub - 2, has completed */
+    cudaMemcpyAsync(t.dpp, t.h_pp, sizeof(XgPicParams), cudaMemcpyHostToDevice, s->ust);
+    if (s->widen && !c.device_io)
+        for (int p = 0; p < 3; p++) {
+            const XgPlane &pl = s->slot[cur][p];
+            cudaMemcpyAsync(t.d_in8[p], t.h_in[p], (size_t)pl.w * pl.h, cudaMemcpyHostToDevice, s->ust);
+        }
+    cudaEventRecord(t.ev_up, s->ust);
+    cudaStreamWaitEvent(s->st, t.ev_up, 0);
     if (with_me && c.use_graph) {
         if (!s->gexec[cur]) {
             cudaGraph_t g;
