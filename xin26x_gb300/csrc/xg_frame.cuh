@@ -79,6 +79,7 @@ static void xg_quant_params(int qp, int lg, int intra_frame, XgQuant *q)
 static int xg_stream_free(xin_gpu_stream *s)
 {
     if (!s) return XIN_GPU_OK;
+    if (s->ust) cudaStreamSynchronize(s->ust);
     if (s->st) cudaStreamSynchronize(s->st);
     if (s->cst) cudaStreamSynchronize(s->cst);
     for (int i = 0; i < 2; i++) if (s->gexec[i]) cudaGraphExecDestroy(s->gexec[i]);
