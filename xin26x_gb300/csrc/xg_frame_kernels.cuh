@@ -132,9 +132,11 @@ __global__ void __launch_bounds__(256) k_qpel_planes(XgPlane ref, XgQpel qp)
  * Per candidate a warp has the SADs of its four 8x8 blocks and of its 16x16
  * block in registers (running minimum per lane).  After each pass the four
  * warps of a 32x32 quadrant swap their 16x16 SADs through shared memory under a
- * 128-thread named barrier, each warp taking one of the XG_ME_D candidate rows
- * for the 32x32 CU; the 32x32 SADs go to a ring from which the first four warps
- * sum the 64x64 SADs every p.agg_passes passes.
+ * 128-thread named barrier, each warp taking XG_ME_D / 4 of the candidate rows
+ * for the 32x32 CU; the 32x32 SADs go to a ring from which the first
+ * XG_ME_SLOTS threads (one candidate slot each) sum the 64x64 SADs every
+ * p.agg_passes passes.  A candidate's 32-bit key is SAD * key_mul plus two
+ * motion-cost table entries, one multiply-add.
  * Every CU keeps (cost, raster index) as one 64-bit key; the
  * unsigned minimum over lanes, warps and CTAs (atomicMin) selects the smallest
  * cost and, among equal costs, the first candidate in raster order -- the
