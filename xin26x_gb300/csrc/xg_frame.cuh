@@ -46,6 +46,8 @@ struct xin_gpu_stream {
     cudaStream_t st;
     cudaStream_t cst;      /* result copies (device to host) */
     cudaStream_t ust;      /* uploads of the next picture's parameters and staged samples */
+    cudaStream_t tst;      /* side branch that records the search's end (stage timing) */
+    cudaEvent_t ev_tfork, ev_tjoin;
     cudaStream_t aux[3];   /* the tails of levels 2..4 run beside the first level's */
     cudaStream_t auxq;     /* quarter-pel planes of the new picture, beside the search (low priority) */
     cudaEvent_t ev_fork, ev_join[3], ev_qfork, ev_qjoin;
@@ -97,6 +99,9 @@ static int xg_stream_free(xin_gpu_stream *s)
     }
     if (s->cst) cudaStreamDestroy(s->cst);
     if (s->ust) cudaStreamDestroy(s->ust);
+    if (s->tst) cudaStreamDestroy(s->tst);
+    if (s->ev_tfork) cudaEventDestroy(s->ev_tfork);
+    if (s->ev_tjoin) cudaEventDestroy(s->ev_tjoin);
     for (int i = 0; i < 3; i++) {
         if (s->ev_join[i]) cudaEventDestroy(s->ev_join[i]);
         if (s->aux[i]) cudaStreamDestroy(s->aux[i]);
@@ -165,6 +170,9 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     cudaError_t e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cst, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->ust, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->tst, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_tfork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_tjoin, cudaEventDisableTiming);
     for (auto &t : s->set) {
         if (e == cudaSuccess) e = cudaEventCreate(&t.ev0);
         if (e == cudaSuccess) e = cudaEventCreate(&t.ev1);
@@ -399,7 +407,13 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             k_me_tiles<8><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, t.dpp);
         nl++;
         nl += xg_enqueue_qpel(s, cur);
-        xg_stage_event(t.evs[2], st, capturing);
+        /* the search's end is recorded on a side branch joined at the picture's
+         * end: a timing node between the search and the tails' fork held the tails
+         * back by about 0.03 ms */
+        cudaEventRecord(s->ev_tfork, st);
+        cudaStreamWaitEvent(s->tst, s->ev_tfork, 0);
+        xg_stage_event(t.evs[2], s->tst, capturing);
+        cudaEventRecord(s->ev_tjoin, s->tst);
         /* the levels' tails are independent: fork them onto the auxiliary streams */
         cudaEventRecord(s->ev_fork, st);
         int li = 0, nfork = 0;
@@ -441,6 +455,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             cudaStreamWaitEvent(st, s->ev_join[i], 0);
         }
         cudaStreamWaitEvent(st, s->ev_qjoin, 0);
+        cudaStreamWaitEvent(st, s->ev_tjoin, 0);
         xg_stage_event(t.evs[3], st, capturing);
     } else {
         nl += xg_enqueue_qpel(s, cur);
