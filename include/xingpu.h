@@ -181,10 +181,12 @@ void XinGpuIDct2WxH(XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, int
  * without waiting.  The intermediate between the two 1-D passes lives in a
  * file-scope device array of 64 x 64 coefficients (held by every GPU that loads
  * the library until exit); larger blocks are rejected with XIN_GPU_ERR_ARG.
- * The first call on a device looks up that array's device address; make that
- * first call before any stream capture.  All calls share the array, so calls
- * that overlap on the GPU race; serialise them.  The current device must be the
- * one given to xin_gpu_init (XIN_GPU_ERR_STATE otherwise). */
+ * xin_gpu_init must have been called (XIN_GPU_ERR_STATE otherwise: this entry
+ * point never initialises the library itself), and the current device must be
+ * the one given to it (XIN_GPU_ERR_STATE otherwise).  The first call on a
+ * device looks up that array's device address; it must come before any stream
+ * capture (XIN_GPU_ERR_STATE if `stream` is capturing then).  All calls share
+ * the array, so calls that overlap on the GPU race; serialise them. */
 int  xin_gpu_fdct2_wxh_noalloc(const XG_COEFF *input, intptr_t inputStride, XG_COEFF *output, intptr_t outputStride,
                                uint32_t width, uint32_t height, int32_t shift1st, int32_t shift2nd, void *stream);
 /* transform skip: replaces Xin26xFSkipWxH (XinFor2dSkip, :217) and Xin266ISkipWxH
@@ -260,8 +262,15 @@ int  xin_gpu_tq_plan_create(const xin_gpu_tq_block *blocks, int32_t nblocks, siz
 int  xin_gpu_tq_plan_run(xin_gpu_tq_plan *plan, const XG_COEFF *resid, XG_COEFF *q, XG_COEFF *r, XG_COEFF *resid_out,
                          uint64_t *nz, void *stream);
 int  xin_gpu_tq_plan_tiles(const xin_gpu_tq_plan *plan, int32_t *tiles);
-/* synchronises; XIN_GPU_ERR_TIMEOUT if a tensor-core wait of a run gave up */
+/* synchronises; XIN_GPU_ERR_TIMEOUT if a tensor-core wait of a run since the
+ * last status call gave up (the outputs of that run are not valid; the flag is
+ * cleared by this call) */
 int  xin_gpu_tq_plan_status(xin_gpu_tq_plan *plan);
+/* Polls of one tensor-core wait before it gives up (default 2^26, about a
+ * second).  A wait that gives up sets the plan's timeout flag, waits (bounded
+ * by the default) for its MMA to finish, releases its tensor memory and ends its
+ * CTA.  0 makes every wait give up at once: a way to exercise that path. */
+int  xin_gpu_tq_plan_set_wait_tries(xin_gpu_tq_plan *plan, int64_t tries);
 void xin_gpu_tq_plan_destroy(xin_gpu_tq_plan *plan);
 
 /* ---------------------------------------------------- dependent quantisation

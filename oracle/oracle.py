@@ -146,6 +146,10 @@ _REF_ONLY = {
     "idct2_wxh_tmp": ("Xin266IDct2WxH", [vp, ip, vp, ip, u32, u32, vp, i32, i32]),
     "full_subpel_me_io": ("ref_full_subpel_me", [vp, ip, vp, ip, u32, u32, i32, i32, u32, i32, i32, i32, i32, vp]),
     "dq_param_ref": ("ref_dq_param", [C.c_int, C.c_int, C.POINTER(xin_dp_param)]),
+    "luma_inter_pred_ref": ("ref_luma_inter_pred", [vp, ip, vp, ip, i32, i32, i32, i32, i32, i32, i32, i32, u32, u32,
+                                                    i32]),
+    "chroma_motion_comp_ref": ("ref_chroma_motion_comp", [vp, vp, vp, vp, ip, vp, vp, ip, vp, i32, i32, u32, i32, i32,
+                                                          i32, i32, i32, i32, u32, u32]),
     "transform_tu_ref": ("ref_transform_tu", [vp, ip, vp, ip, vp, vp, vp, ip, u32, u32, u32, u32, i32, i32, u32, i32, i32,
                                               i32, vp, vp]),
 }

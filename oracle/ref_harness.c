@@ -238,3 +238,59 @@ void ref_bili_interp(int variant, const PIXEL *src, intptr_t ss, SINT16 *dst, in
     default: Xin266BiliInterpHorVet(src, ss, dst, ds, frac, w, h); break;
     }
 }
+
+/* ---- motion-compensation call sites ------------------------------------
+ * Xin266LumaInterPred (h266_encoder/source/h266_inter_prediction.c:302) and
+ * Xin266ChromaMotionComp (:612) called unmodified on a picture set whose
+ * reference lists hold the given planes: the MV is clipped to the CU's
+ * window, split into an integer offset and a phase, and dispatched through
+ * the table (chroma: 1/32 phase of the luma 1/16 position).  ref_*: picture
+ * origins (inside the padding), luma stride rs, chroma stride crs; mv in
+ * 1/16 luma pel; ref_idx1 < 0 selects the uni-prediction branch. */
+void Xin266LumaInterPred(xin_sec_struct *, xin_pu_struct *, PIXEL *, intptr_t, xin_mv32_u *, SINT32, SINT32, BOOL);
+void Xin266ChromaMotionComp(xin_sec_struct *, SINT32, SINT32, PIXEL *, PIXEL *, intptr_t, xin_mv32_u *, SINT8 *, UINT8);
+
+static harness *mc_harness(SINT32 cu_x, SINT32 cu_y, SINT32 min_mvx, SINT32 min_mvy, SINT32 max_mvx, SINT32 max_mvy,
+                           xin_cu_struct *cu)
+{
+    harness *hs = harness_new(0);
+    memset(cu, 0, sizeof *cu);
+    cu->cuPelX = (UINT32)cu_x; cu->cuPelY = (UINT32)cu_y;
+    hs->sec.cu = cu;
+    hs->sec.minMv.mv.mvX = (SINT16)min_mvx; hs->sec.minMv.mv.mvY = (SINT16)min_mvy;
+    hs->sec.maxMv.mv.mvX = (SINT16)max_mvx; hs->sec.maxMv.mv.mvY = (SINT16)max_mvy;
+    return hs;
+}
+
+void ref_luma_inter_pred(PIXEL *ref_origin, intptr_t rs, PIXEL *pred, intptr_t ps, SINT32 mvx16, SINT32 mvy16,
+                         SINT32 cu_x, SINT32 cu_y, SINT32 min_mvx, SINT32 min_mvy, SINT32 max_mvx, SINT32 max_mvy,
+                         UINT32 w, UINT32 h, BOOL alt_hpel)
+{
+    xin_cu_struct cu; xin_pu_struct pu; xin_ref_picture rp; xin_mv32_u mv;
+    harness *hs = mc_harness(cu_x, cu_y, min_mvx, min_mvy, max_mvx, max_mvy, &cu);
+    memset(&pu, 0, sizeof pu); memset(&rp, 0, sizeof rp);
+    pu.width = (UINT8)w; pu.height = (UINT8)h; pu.lgWidth = (UINT8)calcLog2[w]; pu.lgHeight = (UINT8)calcLog2[h];
+    rp.refBuf[PLANE_LUMA] = ref_origin; rp.refStride[PLANE_LUMA] = rs;
+    hs->pic.pictureRead[0][0] = &rp;
+    mv.mv.mv32X = mvx16; mv.mv.mv32Y = mvy16;
+    Xin266LumaInterPred(&hs->sec, &pu, pred, ps, &mv, 0, 0, alt_hpel);
+    free(hs);
+}
+
+void ref_chroma_motion_comp(PIXEL *ref_u0, PIXEL *ref_v0, PIXEL *ref_u1, PIXEL *ref_v1, intptr_t crs,
+                            PIXEL *pred_u, PIXEL *pred_v, intptr_t ps, const SINT32 *mv16, SINT32 ref_idx0,
+                            SINT32 ref_idx1, UINT32 bcw_idx, SINT32 cu_x, SINT32 cu_y, SINT32 min_mvx, SINT32 min_mvy,
+                            SINT32 max_mvx, SINT32 max_mvy, UINT32 w, UINT32 h)
+{
+    xin_cu_struct cu; xin_ref_picture rp0, rp1; xin_mv32_u mv[2]; SINT8 ri[2];
+    harness *hs = mc_harness(cu_x, cu_y, min_mvx, min_mvy, max_mvx, max_mvy, &cu);
+    memset(&rp0, 0, sizeof rp0); memset(&rp1, 0, sizeof rp1);
+    rp0.refBuf[PLANE_CHROMA_U] = ref_u0; rp0.refBuf[PLANE_CHROMA_V] = ref_v0; rp0.refStride[PLANE_CHROMA] = crs;
+    rp1.refBuf[PLANE_CHROMA_U] = ref_u1; rp1.refBuf[PLANE_CHROMA_V] = ref_v1; rp1.refStride[PLANE_CHROMA] = crs;
+    hs->pic.pictureRead[XIN_LIST_0][0] = &rp0;
+    hs->pic.pictureRead[XIN_LIST_1][0] = &rp1;
+    mv[0].mv.mv32X = mv16[0]; mv[0].mv.mv32Y = mv16[1]; mv[1].mv.mv32X = mv16[2]; mv[1].mv.mv32Y = mv16[3];
+    ri[0] = (SINT8)ref_idx0; ri[1] = (SINT8)ref_idx1;
+    Xin266ChromaMotionComp(&hs->sec, (SINT32)w, (SINT32)h, pred_u, pred_v, ps, mv, ri, (UINT8)bcw_idx);
+    free(hs);
+}

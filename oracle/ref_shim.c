@@ -80,6 +80,16 @@ void Xin266InterpCopy(const PIXEL *, intptr_t, PIXEL *, intptr_t, SINT32, UINT32
 void Xin266LumaInterpHor(const PIXEL *, intptr_t, PIXEL *, intptr_t, SINT32, UINT32, UINT32, UINT32);
 void Xin266LumaInterpVet(const PIXEL *, intptr_t, PIXEL *, intptr_t, SINT32, UINT32, UINT32, UINT32);
 void Xin266LumaInterpHorVet(const PIXEL *, intptr_t, PIXEL *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266ChromaInterpHor(const PIXEL *, intptr_t, PIXEL *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266ChromaInterpVet(const PIXEL *, intptr_t, PIXEL *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266ChromaInterpHorVet(const PIXEL *, intptr_t, PIXEL *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266InterpCopyU8S16(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266ChromaInterpHorU8S16(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266ChromaInterpVetU8S16(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266ChromaInterpHorVetU8S16(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266InterpAvgS16U8(const SINT16 *, intptr_t, const SINT16 *, intptr_t, PIXEL *, intptr_t, UINT32, UINT32);
+void Xin266InterpWeightS16U8(const SINT16 *, intptr_t, const SINT16 *, intptr_t, PIXEL *, intptr_t, UINT32, UINT32,
+                             SINT32, SINT32);
 void Xin266IDct2WxH(COEFF *, intptr_t, COEFF *, intptr_t, UINT32, UINT32, COEFF *, SINT32, SINT32);
 void Xin266ISkipWxH(COEFF *, intptr_t, COEFF *, intptr_t, UINT32, UINT32);
 void Xin266QuantInvQuant(COEFF *, COEFF *, COEFF *, intptr_t, UINT32, UINT32, UINT32, UINT32, SINT32, SINT32, SINT32,
@@ -101,6 +111,18 @@ void shim_fill_table(xin_func_struct *fs)
         fs->pfXinLumaInterp[1][0][lg] = Xin266LumaInterpHor;
         fs->pfXinLumaInterp[0][1][lg] = Xin266LumaInterpVet;
         fs->pfXinLumaInterp[1][1][lg] = Xin266LumaInterpHorVet;
+        /* chroma, S16 and bi-average entries as Xin266FuncInit sets them
+         * (h266_encoder/source/h266_func_init.c:532-620) */
+        fs->pfXinChromaInterp[0][0][lg] = Xin266InterpCopy;
+        fs->pfXinChromaInterp[1][0][lg] = Xin266ChromaInterpHor;
+        fs->pfXinChromaInterp[0][1][lg] = Xin266ChromaInterpVet;
+        fs->pfXinChromaInterp[1][1][lg] = Xin266ChromaInterpHorVet;
+        fs->pfXinChromaInterpS16[0][0][lg] = Xin266InterpCopyU8S16;
+        fs->pfXinChromaInterpS16[1][0][lg] = Xin266ChromaInterpHorU8S16;
+        fs->pfXinChromaInterpS16[0][1][lg] = Xin266ChromaInterpVetU8S16;
+        fs->pfXinChromaInterpS16[1][1][lg] = Xin266ChromaInterpHorVetU8S16;
+        fs->pfXinInterpAvg[lg] = Xin266InterpAvgS16U8;
+        fs->pfXinInterpWeight[lg] = Xin266InterpWeightS16U8;
         fs->pfXinBlockSubForDct[lg] = shim_sub;
         fs->pfXinBlockAddForDct[lg] = shim_add;
         fs->pfXinQuantInvQuant[lg] = Xin266QuantInvQuant;
@@ -125,6 +147,10 @@ void Xin266LumaInterpolation(xin_func_struct *fs, const PIXEL *src, intptr_t ss,
     SINT32 fx = frac & XIN_MV_FRAC_MASK, fy = (frac >> XIN_MV_FRAC_BITS) & XIN_MV_FRAC_MASK;
     fs->pfXinLumaInterp[!!fx][!!fy][lgw](src, ss, dst, ds, frac, 1u << lgw, h, 0);
 }
+
+/* affine MV rounding (h266_encoder/source/h266_get_neighbour_mv.c:1380), referenced by the
+ * affine branch of h266_inter_prediction.c; no harness reaches that branch */
+void Xin266RoundAffineMv(SINT32 *mvx, SINT32 *mvy, SINT32 shift) { (void)mvx; (void)mvy; (void)shift; }
 
 /* LMCS chroma residual scaling: never enabled by the harnesses */
 void Xin266FwdScaleSignal(COEFF *r, intptr_t s, UINT32 w, UINT32 h, SINT32 scale) { (void)r; (void)s; (void)w; (void)h; (void)scale; }

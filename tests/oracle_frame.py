@@ -4,6 +4,8 @@ Test infrastructure only."""
 from __future__ import annotations
 
 import ctypes as C
+import os
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -12,9 +14,11 @@ from xin26x_gb300.frame import CU_DTYPE
 from xin26x_gb300.synth import pad_plane
 
 
-def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=64, bitdepth=8, cus=None):
+def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=64, bitdepth=8, cus=None, threads=1):
     """cur, ref: (Y, U, V) planes.  levels: [(size, first, cus_x, cus_y)] as the stream reports.
     cus: optional list of global CU indices to evaluate (others left zero).
+    threads: host threads sharing the CUs (0 = every core); each CU writes only its
+    own record and its own area of the level's planes, so the calls are independent.
     Returns (cu records, q planes [levels,h,w] x3, rec planes x3)."""
     o = O.oracle(bitdepth)
     h, w = cur[0].shape
@@ -36,17 +40,34 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
     q = [np.zeros((nl, h, w), o.coef), np.zeros((nl, h // 2, w // 2), o.coef), np.zeros((nl, h // 2, w // 2), o.coef)]
     rec = [np.zeros((nl, h, w), o.pix), np.zeros((nl, h // 2, w // 2), o.pix), np.zeros((nl, h // 2, w // 2), o.pix)]
     want = None if cus is None else set(int(c) for c in cus)
+    qs = (C.c_ssize_t * 2)(w, w // 2)
+    ptrs = []
+    work = []
     for li, (size, first, cx, cy) in enumerate(levels):
-        qptr = (C.c_void_p * 3)(*[q[p][li].ctypes.data for p in range(3)])
-        rptr = (C.c_void_p * 3)(*[rec[p][li].ctypes.data for p in range(3)])
-        qs = (C.c_ssize_t * 2)(w, w // 2)
+        ptrs.append(((C.c_void_p * 3)(*[q[p][li].ctypes.data for p in range(3)]),
+                     (C.c_void_p * 3)(*[rec[p][li].ctypes.data for p in range(3)])))
         for j in range(cx * cy):
-            if want is not None and first + j not in want:
-                continue
-            out = O.orc_cu_out()
-            o.cu_hotpath(C.byref(f), (j % cx) * size, (j // cx) * size, size, qptr, qs, rptr, qs, C.byref(out))
-            r = recs[first + j]
-            r["mvx"], r["mvy"], r["cost"], r["int_cost"] = out.mvx, out.mvy, out.cost, out.int_cost
-            r["nz"] = list(out.nz)
-            r["ssd"] = list(out.ssd)
+            if want is None or first + j in want:
+                work.append((li, size, first, cx, j))
+
+    def one(item):
+        li, size, first, cx, j = item
+        out = O.orc_cu_out()
+        o.cu_hotpath(C.byref(f), (j % cx) * size, (j // cx) * size, size, ptrs[li][0], qs, ptrs[li][1], qs,
+                     C.byref(out))
+        r = recs[first + j]
+        r["mvx"], r["mvy"], r["cost"], r["int_cost"] = out.mvx, out.mvy, out.cost, out.int_cost
+        r["nz"] = list(out.nz)
+        r["ssd"] = list(out.ssd)
+
+    nthreads = (os.cpu_count() or 1) if threads == 0 else max(1, threads)
+    if nthreads == 1 or len(work) < 2:
+        for item in work:
+            one(item)
+    else:
+        # largest CUs first so that the last ones to finish are short
+        work.sort(key=lambda it: -it[1])
+        one(work[0])        # the oracle builds its transform matrices on first use: once, before the threads
+        with ThreadPoolExecutor(nthreads) as ex:
+            list(ex.map(one, work[1:]))
     return recs, q, rec

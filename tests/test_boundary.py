@@ -11,7 +11,7 @@ import pytest
 from xin26x_gb300 import _lib
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+from __graft_entry__ import REFERENCE_DIR as REF
 
 
 @pytest.mark.parametrize("bd", (8, 10))

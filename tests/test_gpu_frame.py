@@ -244,3 +244,57 @@ def test_device_io_matches_host(bd, inb, w, h):
                 assert np.array_equal(got, host[k - 1]), (bd, inb, k)
     finally:
         lib.xin_gpu_stream_close(hs)
+
+
+def test_frame_1080p_benchmark_configuration():
+    """The benchmark's own workload compared in full: the first three pictures of
+    bench.py's 1920x1080 stream (8-bit 4:2:0 into the 10-bit library,
+    input_bitdepth 8), +-64 exhaustive search, CU levels 64/32/16/8, QPs 32 and 37
+    with their lambdas.  Every CU record and every coefficient and reconstructed
+    plane of every level against the oracle's 10-bit build on all host cores."""
+    import bench
+    frames = bench.make_frames(3)
+    fs = FrameStream(bench.W, bench.H, search_range=bench.SEARCH, levels=bench.LEVELS, out_q=True, out_rec=True,
+                     bitdepth=bench.BD, input_bitdepth=bench.IN_BD)
+    try:
+        assert sum(cx * cy for (_, _, cx, cy) in fs.levels) == fs.ncus
+        fs.submit(*frames[0], qp=32, uv_qp=32, sad_lambda=bench.LAMBDA_BD[32])
+        fs.wait()
+        for k, qp in ((1, 32), (2, 37)):
+            fs.submit(*frames[k], qp=qp, uv_qp=qp, sad_lambda=bench.LAMBDA_BD[qp])
+            out = fs.wait()
+            cur, ref = [tuple(p.astype(np.uint16) << (bench.BD - bench.IN_BD) for p in f)
+                        for f in (frames[k], frames[k - 1])]
+            want = oracle_frame.run(cur, ref, fs.levels, search_range=bench.SEARCH, qp=qp, uv_qp=qp,
+                                    sad_lambda=bench.LAMBDA_BD[qp], bitdepth=bench.BD, threads=0)
+            _compare(out, want, fs.levels, ("1080p", k))
+    finally:
+        fs.close()
+
+
+def test_frame_wait_timeout_then_collect():
+    """xin_gpu_frame_wait with a 0 ms limit right after a 1080p submit returns
+    XIN_GPU_ERR_TIMEOUT (the picture takes about a millisecond); the picture is
+    then collected normally and equals the same picture through a stream that
+    never timed out."""
+    import ctypes as C
+    from xin26x_gb300 import _lib
+    w, h = 1920, 1080
+    seq = synth.sequence(w, h, 2, seed=5, objects=2)
+    outs = []
+    for probe in (True, False):
+        fs = FrameStream(w, h, search_range=64, out_q=True, out_rec=False)
+        try:
+            fs.submit(*seq[0], qp=32, uv_qp=32, sad_lambda=64)
+            fs.wait()
+            fs.submit(*seq[1], qp=32, uv_qp=32, sad_lambda=64)
+            if probe:
+                res = _lib.xin_gpu_results()
+                assert fs.lib.xin_gpu_frame_wait(fs.h, C.byref(res), 0) == -5
+                assert fs.lib.xin_gpu_last_status() == -5
+            outs.append(fs.wait())
+        finally:
+            fs.close()
+    assert np.array_equal(outs[0]["cu"], outs[1]["cu"])
+    for p in range(3):
+        assert np.array_equal(outs[0]["q"][p], outs[1]["q"][p])

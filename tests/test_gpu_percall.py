@@ -329,6 +329,34 @@ def test_motion_search_drivers(libs):
         assert (me.bestMv.mvX, me.bestMv.mvY, me.bestCost, me.bestSad) == (8, 4, 0, 12345)
 
 
+def test_motion_search_default_range(libs):
+    """XinGpuMotionEstFull and XinGpuFullSubPelMe at the encoder's default range of
+    +-64 (h26x_api/source/h26x_encoder_api.c:202) with a window wide enough that
+    the clip does not shorten it, and one window that clips a side to 3."""
+    g, o, bd = libs
+    rng = np.random.default_rng(64)
+    mx = (1 << bd) - 1
+    R = 64
+    for w, h in [(8, 8), (16, 16), (32, 32), (64, 64), (32, 8)]:
+        pad = 96
+        base = rng.integers(0, mx + 1, size=(h + 2 * pad, w + 2 * pad)).astype(np.int32)
+        refp = ((base + np.roll(base, 1, 0) + np.roll(base, 2, 1)) // 3).astype(o.pix)
+        inp = np.ascontiguousarray(refp[pad + 37:pad + 37 + h, pad - 51:pad - 51 + w])
+        for mvp, win in [((0, 0), (-80, -80, 80, 80)), ((-9, 6), (-70, -3, 75, 80))]:
+            lam = int(rng.integers(0, 300))
+            me = _me_state(g, inp, refp, pad, w, h, R, mvp, lam, (0, 0, 0xFFFFFFFF), win)
+            g.XinGpuMotionEstFull(C.byref(me)); _ok(g, "MotionEstFull")
+            io = O.orc_me_io(0, 0, 0xFFFFFFFF, 12345)
+            o.me_full(P(inp), w, P(refp, pad * refp.shape[1] + pad), refp.shape[1], w, h, mvp[0], mvp[1], R, lam,
+                      win[0], win[1], win[2], win[3], io)
+            assert (me.bestMv.mvX, me.bestMv.mvY, me.bestCost, me.bestSad) == \
+                (io.best_mvx, io.best_mvy, io.best_cost, io.best_sad), (w, h, mvp)
+            g.XinGpuFullSubPelMe(C.byref(me)); _ok(g, "FullSubPelMe")
+            o.full_subpel_me(P(inp), w, P(refp, pad * refp.shape[1] + pad), refp.shape[1], w, h, mvp[0], mvp[1], lam,
+                             win[0], win[1], win[2], win[3], io)
+            assert (me.bestMv.mvX, me.bestMv.mvY, me.bestCost) == (io.best_mvx, io.best_mvy, io.best_cost)
+
+
 def test_invalid_arguments_report_errors(libs):
     g, o, bd = libs
     a = np.zeros(64, o.pix)

@@ -143,3 +143,43 @@ def test_tq_tensor_form_with_unaligned_offsets():
                               ro.ctypes.data, nz.ctypes.data, resid.size, -2) == 0, g.xin_gpu_last_error()
     for name, a, b in zip(("q", "r", "resid_out", "nz"), (q, r, ro, nz), want):
         assert np.array_equal(a, b), name
+
+
+def test_tq_tensor_wait_timeout_is_reported_and_recovers():
+    """The tensor-core engine's bounded MMA wait, made to give up at once (0 polls):
+    the plan's status reports XIN_GPU_ERR_TIMEOUT without a hang, the flag is
+    cleared by that report, and the same plan with the default limit then gives
+    the oracle's outputs (the context stayed usable)."""
+    import torch
+    from xin26x_gb300 import _lib
+    g = _lib.load(10)
+    assert g.xin_gpu_init(0) == 0
+    o = O.oracle(10)
+    blocks, resid = make_batch(400, 10, seed=99, kernel_bench_mix=True)
+    want = oracle_batch(o, blocks, resid)
+    plan = C.c_void_p()
+    assert g.xin_gpu_tq_plan_create(blocks.ctypes.data, len(blocks), resid.size, -2, C.byref(plan)) == 0
+    try:
+        d_res = torch.from_numpy(resid).cuda()
+        outs = [torch.zeros_like(d_res) for _ in range(3)]
+        d_nz = torch.zeros(len(blocks), dtype=torch.int64, device="cuda")
+
+        def run():
+            return g.xin_gpu_tq_plan_run(plan, d_res.data_ptr(), outs[0].data_ptr(), outs[1].data_ptr(),
+                                         outs[2].data_ptr(), d_nz.data_ptr(), None)
+
+        assert g.xin_gpu_tq_plan_set_wait_tries(plan, 0) == 0
+        assert run() == 0
+        assert g.xin_gpu_tq_plan_status(plan) == -5
+        assert g.xin_gpu_tq_plan_status(plan) == 0          # reported once
+        assert g.xin_gpu_tq_plan_set_wait_tries(plan, -1) == -2
+        assert g.xin_gpu_tq_plan_set_wait_tries(plan, 1 << 26) == 0
+        for t in outs:
+            t.zero_()
+        assert run() == 0
+        assert g.xin_gpu_tq_plan_status(plan) == 0, g.xin_gpu_last_error()
+        got = [t.cpu().numpy() for t in outs] + [d_nz.cpu().numpy().view(np.uint64)]
+        for name, a, b in zip(("q", "r", "resid_out", "nz"), got, want):
+            assert np.array_equal(a, b), name
+    finally:
+        g.xin_gpu_tq_plan_destroy(plan)

@@ -344,3 +344,76 @@ def test_bilinear_interp_every_phase(bd):
                 o.bili_interp(variant, O.ptr(src, 2 * src.shape[1] + 2), src.shape[1], O.ptr(a), w + 8, frac, w, h)
                 r.bili_interp(variant, O.ptr(src, 2 * src.shape[1] + 2), src.shape[1], O.ptr(b), w + 8, frac, w, h)
                 assert np.array_equal(a, b), (variant, w, h, frac)
+
+
+def _chroma_phase_interp(o, src, ss, dst, ds, frac, w, h, s16):
+    """The table dispatch of pfXinChromaInterp / pfXinChromaInterpS16 by (!!fx, !!fy)."""
+    fx, fy = frac & 31, frac >> 5
+    if s16:
+        f = o.interp_copy_s16 if not fx and not fy else o.chroma_hor_s16 if not fy else \
+            o.chroma_vet_s16 if not fx else o.chroma_hv_s16
+    else:
+        f = o.interp_copy if not fx and not fy else o.chroma_hor if not fy else o.chroma_vet if not fx else o.chroma_hv
+    f(src, ss, dst, ds, frac, w, h, 0)
+
+
+@pytest.mark.parametrize("bd", BDS)
+def test_motion_comp_call_sites(bd):
+    """Xin266LumaInterPred and Xin266ChromaMotionComp (h266_inter_prediction.c:302,612),
+    compiled in place, against the oracle's call-site restatements (orc_luma_inter_pred,
+    orc_chroma_motion_comp) and, for bi-prediction, the oracle's S16 chroma stages with
+    the average or the BCW blend.  MVs reach beyond the window so the clip is exercised."""
+    o, r = _pair(bd)
+    rng = np.random.default_rng(302 + bd)
+    fw, fh, ctu = 192, 128, 64
+    pad = ctu + 16
+    ref = [rng.integers(0, o.max_pix + 1, size=(fh + 2 * pad, fw + 2 * pad)).astype(o.pix) for _ in range(2)]
+    refc = [[rng.integers(0, o.max_pix + 1, size=(fh // 2 + pad, fw // 2 + pad)).astype(o.pix) for _ in range(2)]
+            for _ in range(2)]
+    lo = pad * ref[0].shape[1] + pad
+    co = (pad // 2) * refc[0][0].shape[1] + pad // 2
+    rs, crs = ref[0].shape[1], refc[0][0].shape[1]
+    i32 = O.C.c_int32
+    for w, h in [(8, 8), (16, 16), (32, 32), (64, 64), (128, 128), (16, 8), (8, 32), (4, 8), (32, 16), (64, 128)]:
+        for trial in range(40):
+            cx = int(rng.integers(0, max(1, (fw - w) // 4 + 1))) * 4
+            cy = int(rng.integers(0, max(1, (fh - h) // 4 + 1))) * 4
+            win = [i32() for _ in range(4)]
+            o.mv_window(fw, fh, ctu, cx, cy, w, h, *[O.C.byref(v) for v in win])
+            mnx, mny, mxx, mxy = [v.value for v in win]
+            mv = [int(rng.integers(16 * (mnx - 24), 16 * (mxx + 24) + 1)) if k % 2 == 0 else
+                  int(rng.integers(16 * (mny - 24), 16 * (mxy + 24) + 1)) for k in range(4)]
+            alt = int(trial % 5 == 0)
+            a = np.zeros((h, w), o.pix)
+            b = np.zeros((h, w), o.pix)
+            o.luma_inter_pred(O.ptr(ref[0], lo), rs, O.ptr(a), w, mv[0], mv[1], cx, cy, mnx, mny, mxx, mxy, w, h, alt)
+            r.luma_inter_pred_ref(O.ptr(ref[0], lo), rs, O.ptr(b), w, mv[0], mv[1], cx, cy, mnx, mny, mxx, mxy, w, h, alt)
+            assert np.array_equal(a, b), ("luma", w, h, cx, cy, mv[:2], alt)
+            cw, ch = w // 2, h // 2
+            mvs = np.array(mv, np.int32)
+            bi = trial % 3 != 0
+            bcw = int(rng.integers(0, 5)) if bi else 2
+            r_u, r_v = np.zeros((ch, cw), o.pix), np.zeros((ch, cw), o.pix)
+            r.chroma_motion_comp_ref(O.ptr(refc[0][0], co), O.ptr(refc[0][1], co), O.ptr(refc[1][0], co),
+                                     O.ptr(refc[1][1], co), crs, O.ptr(r_u), O.ptr(r_v), cw, O.ptr(mvs), 0,
+                                     0 if bi else -1, bcw, cx, cy, mnx, mny, mxx, mxy, w, h)
+            for pl, got in ((0, r_u), (1, r_v)):
+                want = np.zeros((ch, cw), o.pix)
+                if not bi:
+                    o.chroma_motion_comp(O.ptr(refc[0][pl], co), crs, O.ptr(want), cw, mv[0], mv[1], cx, cy,
+                                         mnx, mny, mxx, mxy, w, h)
+                else:
+                    s = [np.zeros((ch, 128), np.int16) for _ in range(2)]
+                    for li in range(2):
+                        mx = min(max(mv[2 * li], 16 * mnx), 16 * mxx)
+                        my = min(max(mv[2 * li + 1], 16 * mny), 16 * mxy)
+                        ox, oy = cx * 16 + mx, cy * 16 + my
+                        frac = ((oy & 31) << 5) + (ox & 31)
+                        _chroma_phase_interp(o, O.ptr(refc[li][pl], co + (oy >> 5) * crs + (ox >> 5)), crs,
+                                             O.ptr(s[li]), 128, frac, cw, ch, True)
+                    if bcw == 2:
+                        o.interp_avg(O.ptr(s[0]), 128, O.ptr(s[1]), 128, O.ptr(want), cw, cw, ch)
+                    else:
+                        wb = (-2, 3, 4, 5, 10)[bcw]
+                        o.interp_weight(O.ptr(s[0]), 128, O.ptr(s[1]), 128, O.ptr(want), cw, cw, ch, 8 - wb, wb)
+                assert np.array_equal(got, want), ("chroma", pl, w, h, cx, cy, mv, bi, bcw)

@@ -153,6 +153,7 @@ SIGNATURES = {
     "xin_gpu_tq_plan_run": ([vp, vp, vp, vp, vp, vp, vp], C.c_int),
     "xin_gpu_tq_plan_tiles": ([vp, vp], C.c_int),
     "xin_gpu_tq_plan_status": ([vp], C.c_int),
+    "xin_gpu_tq_plan_set_wait_tries": ([vp, C.c_int64], C.c_int),
     "xin_gpu_tq_plan_destroy": ([vp], None),
     "xin_gpu_dep_quant_batch": ([vp, i32, vp, vp, vp, vp, C.c_size_t, vp, i32], C.c_int),
     "xin_gpu_dep_quant_batch_device": ([vp, i32, vp, vp, vp, vp, C.c_size_t, vp, i32, vp], C.c_int),

@@ -23,14 +23,22 @@
 static __device__ __align__(256) xg_coef g_noalloc_fdct_scratch[XG_NOALLOC_MAX_COEFFS];
 
 /* device address of the scratch array, looked up once per device with that
- * device current (the host-side symbol is not a device address) */
-static xg_coef *xg_noalloc_scratch(int dev)
+ * device current (the host-side symbol is not a device address).  The lookup
+ * is refused while `st` is capturing: make the first call on a device outside
+ * any stream capture. */
+static xg_coef *xg_noalloc_scratch(int dev, cudaStream_t st)
 {
     static std::mutex mu;
     static xg_coef *ptr[64] = {};
     if (dev < 0 || dev >= 64) { xg_set_error(XIN_GPU_ERR_ARG, "noalloc: device index %d out of range", dev); return nullptr; }
     std::lock_guard<std::mutex> lock(mu);
     if (!ptr[dev]) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (xg_cuda_check(cudaStreamIsCapturing(st, &cs), "noalloc: cudaStreamIsCapturing")) return nullptr;
+        if (cs != cudaStreamCaptureStatusNone) {
+            xg_set_error(XIN_GPU_ERR_STATE, "fdct2_wxh_noalloc: the first call on device %d must come before any stream capture", dev);
+            return nullptr;
+        }
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_fdct_scratch);
         if (e != cudaSuccess) { xg_cuda_check(e, "noalloc: cudaGetSymbolAddress"); return nullptr; }
@@ -53,17 +61,22 @@ extern "C" int xin_gpu_fdct2_wxh_noalloc(const XG_COEFF *input, intptr_t inputSt
                      width, height, XG_NOALLOC_MAX_COEFFS);
         return XIN_GPU_ERR_ARG;
     }
-    if (xg_ensure_init() != XIN_GPU_OK) return XIN_GPU_ERR_CUDA;
+    /* no implicit initialisation here: it would make the library's device current
+     * on the caller's thread, whose buffers may live on another device */
+    if (g_init_status != XIN_GPU_OK) {
+        xg_set_error(XIN_GPU_ERR_STATE, "fdct2_wxh_noalloc: call xin_gpu_init first");
+        return XIN_GPU_ERR_STATE;
+    }
     int dev = -1;
     if (xg_cuda_check(cudaGetDevice(&dev), "fdct2_wxh_noalloc: cudaGetDevice")) return XIN_GPU_ERR_CUDA;
     if (dev != g_device) {
         xg_set_error(XIN_GPU_ERR_STATE, "fdct2_wxh_noalloc: current device %d is not the library's device %d", dev, g_device);
         return XIN_GPU_ERR_STATE;
     }
-    xg_coef *scratch = xg_noalloc_scratch(dev);
+    cudaStream_t st = (cudaStream_t)stream;
+    xg_coef *scratch = xg_noalloc_scratch(dev, st);
     if (!scratch) return xin_gpu_last_status();
     (void)cudaGetLastError();
-    cudaStream_t st = (cudaStream_t)stream;
     int n = (int)(width * height);
     k_fdct1d<<<(n + 255) / 256, 256, 0, st>>>(0, lw, input, (int)inputStride, scratch, (int)height, (int)height, shift1st);
     k_fdct1d<<<(n + 255) / 256, 256, 0, st>>>(0, lh, scratch, (int)height, output, (int)outputStride, (int)width, shift2nd);

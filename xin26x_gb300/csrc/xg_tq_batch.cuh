@@ -258,6 +258,7 @@ struct xin_gpu_tq_plan {
     uint32_t *d_tlist;
     int ntiles;
     int *d_err;                 /* set by a tensor-core wait that timed out */
+    long long wait_tries;       /* polls of one tensor-core wait before it gives up */
 };
 
 /* MTS index -> (horizontal, vertical) transform of the host (4 = skip) */
@@ -330,7 +331,8 @@ static int xg_tq_plan_enqueue(xin_gpu_tq_plan *p, const xg_coef *res, xg_coef *q
         });
         if (xg_cuda_check(attr_err, "tq tensor smem attribute")) return XIN_GPU_ERR_CUDA;
         const int grid = std::min(p->ntiles, resident);
-        k_tq_tc<<<grid, XG_TC_THREADS, XG_TC_SMEM, st>>>(p->d_tiles, p->ntiles, p->d_jobs, p->d_tlist, res, q, r, rout, nz, p->d_err);
+        k_tq_tc<<<grid, XG_TC_THREADS, XG_TC_SMEM, st>>>(p->d_tiles, p->ntiles, p->d_jobs, p->d_tlist, res, q, r, rout, nz, p->d_err,
+                                                           p->wait_tries);
         xg_count_launch(1);
         if (xg_cuda_check(cudaGetLastError(), "tq tensor launch")) return XIN_GPU_ERR_CUDA;
     }
@@ -388,7 +390,12 @@ static int xg_tq_plan_status(xin_gpu_tq_plan *p)
     if (!p->d_err) return XIN_GPU_OK;
     int e = 0;
     if (xg_cuda_check(cudaMemcpy(&e, p->d_err, sizeof e, cudaMemcpyDeviceToHost), "tq status")) return XIN_GPU_ERR_CUDA;
-    if (e) { xg_set_error(XIN_GPU_ERR_TIMEOUT, "tq_batch: a tensor-core wait timed out"); return XIN_GPU_ERR_TIMEOUT; }
+    if (e) {
+        /* reported once: later runs start with a clear flag */
+        if (xg_cuda_check(cudaMemset(p->d_err, 0, sizeof(int)), "tq status")) return XIN_GPU_ERR_CUDA;
+        xg_set_error(XIN_GPU_ERR_TIMEOUT, "tq_batch: a tensor-core wait timed out");
+        return XIN_GPU_ERR_TIMEOUT;
+    }
     return XIN_GPU_OK;
 }
 
@@ -412,6 +419,7 @@ extern "C" int xin_gpu_tq_plan_create(const xin_gpu_tq_block *blocks, int32_t nb
     p->nblocks = nblocks;
     p->ncoeffs = ncoeffs;
     p->tile = tile;
+    p->wait_tries = XG_TC_WAIT_TRIES;
     std::vector<XgTcTile> tiles;
     std::vector<uint32_t> tlist;
     if (tile == XIN_GPU_TQ_TENSOR) {
@@ -473,6 +481,14 @@ extern "C" int xin_gpu_tq_plan_status(xin_gpu_tq_plan *p)
     xin_gpu_clear_error();
     if (!p) { xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_status: null plan"); return XIN_GPU_ERR_ARG; }
     return xg_tq_plan_status(p);
+}
+
+extern "C" int xin_gpu_tq_plan_set_wait_tries(xin_gpu_tq_plan *p, int64_t tries)
+{
+    xin_gpu_clear_error();
+    if (!p || tries < 0) { xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_set_wait_tries: bad argument"); return XIN_GPU_ERR_ARG; }
+    p->wait_tries = tries ? (long long)tries : 0;
+    return XIN_GPU_OK;
 }
 
 extern "C" int xin_gpu_tq_batch_device(const xin_gpu_tq_block *blocks, int32_t nblocks, const XG_COEFF *resid, XG_COEFF *q,

@@ -95,11 +95,14 @@ __device__ __forceinline__ void xg_tc_mma(uint32_t tmem, uint32_t ahi, uint32_t 
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
 }
 
-/* bounded wait for the commit of phase `phase`; false after about a second */
-__device__ __forceinline__ bool xg_tc_wait(uint32_t mbar, uint32_t phase)
+/* default bound of a wait for an MMA commit: about a second */
+#define XG_TC_WAIT_TRIES (1LL << 26)
+
+/* bounded wait for the commit of phase `phase`; false after `tries` polls */
+__device__ __forceinline__ bool xg_tc_wait(uint32_t mbar, uint32_t phase, long long tries)
 {
     uint32_t done = 0;
-    for (long it = 0; it < (1L << 26) && !done; it++)
+    for (long long it = 0; it < tries && !done; it++)
         asm volatile("{\n\t.reg .pred q;\n\tmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\n\tselp.u32 %0, 1, 0, q;\n\t}"
                      : "=r"(done) : "r"(mbar), "r"(phase) : "memory");
     return done != 0;
@@ -170,7 +173,8 @@ __device__ __forceinline__ void xg_tc_put4(uint8_t *ahi, uint8_t *alo, int off, 
 
 __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, int ntiles, const XgTqJob *jobs,
                                                         const uint32_t *list, const xg_coef *res, xg_coef *q, xg_coef *r,
-                                                        xg_coef *rout, unsigned long long *nzout, int *err)
+                                                        xg_coef *rout, unsigned long long *nzout, int *err,
+                                                        long long wait_tries)
 {
     extern __shared__ __align__(1024) uint8_t smc[];
     uint8_t *ahi = smc, *alo = smc + XG_TC_A_BYTES, *bm = smc + 2 * XG_TC_A_BYTES;   /* bm: [4][XG_TC_B_BYTES] */
@@ -205,7 +209,7 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (tid == 0) xg_tc_mma(tmem, s_ahi, s_alo, s_b + bi * XG_TC_B_BYTES, kp, np, s_mbar, a_mn);
-        const bool done = xg_tc_wait(s_mbar, phase);
+        const bool done = xg_tc_wait(s_mbar, phase, wait_tries);
         phase ^= 1;
         const bool all = !__syncthreads_or(!done);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -425,7 +429,12 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
-    if (!ok && tid == 0) atomicExch(err, 1);
+    if (!ok && tid == 0) {
+        atomicExch(err, 1);
+        /* the MMA whose wait gave up may still be writing the accumulators: wait for
+         * its commit (again bounded) before the tensor memory is released */
+        xg_tc_wait(s_mbar, phase ^ 1, XG_TC_WAIT_TRIES);
+    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(XG_TC_TMEM_COLS) : "memory");
