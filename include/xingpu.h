@@ -342,6 +342,43 @@ struct xin_me_struct;
 void XinGpuMotionEstFull(struct xin_me_struct *meSet);
 void XinGpuFullSubPelMe(struct xin_me_struct *meSet);
 
+/* ---------------------------------------- search by resolution levels (a7)
+ * The reference's hierarchical search (motionSearchMode 2, the preset-4/6
+ * default; h266_encoder/source/h266_analyze_inter_cu.c:1063-1067) and its
+ * helpers exist only in the closed library; their order is restated here (the
+ * oracle states the same, parity unpinned).
+ *
+ * XinGpuDownscale2x2: stands in for Xin26xDownscale2x2 (typedef XinDownscale2x2,
+ *   h266_encoder/include/h266_func_struct.h:425; table entries
+ *   xin_func_struct.pfXinDownscale2x2 and xin_me_func.pfXinDownscale2x2).
+ *   out(x, y) = (a + b + c + d + 2) >> 2 over the 2x2 input block at (2x, 2y).
+ *   The row flags must be 0, as every open caller passes them
+ *   (h266_enc_init.c:2804-2824, h266_scene_cut.c:64); else XIN_GPU_ERR_ARG.
+ * XinGpuMotionSearchHier: stands in for Xin26xMotionSearchHier1 / 2 (typedef
+ *   XinHierMotionSearch, h266_func_struct.h:435; xin_me_func.pfXinMotionSearchHier1/2,
+ *   h26x_core/include/h26x_hierarchic_motion_search.h:29,42): the SAD of every MV
+ *   of [minMvX, maxMvX] x [minMvY, maxMvY] (units of the level), raster order,
+ *   strict '<'; writes the best to *bestMv (a xin_mv_u); an empty window
+ *   leaves it unchanged.
+ * XinGpuMotionEstHier: stands in for Xin26xMotionEstHier (h26x_motion_est.h:23-36)
+ *   on the ME state (input1/ref1 at 1/2, input2/ref2 at 1/4 resolution):
+ *     window  [c - searchWidth, c + searchWidth] x [c - searchHeight, ...] within
+ *             [minMv, maxMv], c = predMv >> 2; at level L its ends become
+ *             ceil(lo / 2^L) and floor(hi / 2^L)
+ *     start   bestMv / bestCost as given, then meCand[0 .. candNum) (quarter-pel,
+ *             >> 2, clipped to the window) with the full cost, strict '<'
+ *     1/4     exhaustive SAD over the level window, block (w/4) x (h/4)
+ *     1/2     +-1 around twice the 1/4 best, block (w/2) x (h/2)
+ *     full    3 x 3 around twice the 1/2 best, cost (SAD << 8) +
+ *             (bits(mvd x) + bits(mvd y)) * sadLambda, strict '<'
+ *   writes bestMv (quarter-pel), bestCost, bestSad.  width and height are
+ *   multiples of 4. */
+void XinGpuDownscale2x2(XG_PIXEL *input, intptr_t inputStride, int32_t haveRowAbove, int32_t haveRowBelow,
+                        XG_PIXEL *output, intptr_t outputStride, uint32_t outWidth, uint32_t outHeight);
+void XinGpuMotionSearchHier(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *ref, intptr_t refStride, int32_t minMvX,
+                            int32_t maxMvX, int32_t minMvY, int32_t maxMvY, uint32_t width, uint32_t height, void *bestMv);
+void XinGpuMotionEstHier(struct xin_me_struct *meSet);
+
 /* ------------------------------------------------------------- frame form
  * One stream = one sequence.  Pictures are submitted in coding order; each
  * picture after the first uses the previously submitted picture as its
@@ -381,6 +418,11 @@ typedef struct xin_gpu_stream_cfg {
                                     reference's 10-bit build on 8-bit input.  The integer search
                                     then runs on the 8-bit samples with SADs x 4, which equals the
                                     10-bit SAD of those samples. */
+    int32_t  search_mode;        /* 0: exhaustive integer search (as XinGpuMotionEstFull);
+                                    1: by resolution levels (as XinGpuMotionEstHier with predictor
+                                    0 and the zero MV as its candidate, the reference picture
+                                    and the current picture downscaled by 2 and 4 with
+                                    XinGpuDownscale2x2's arithmetic) */
 } xin_gpu_stream_cfg;
 
 typedef struct xin_gpu_picture {

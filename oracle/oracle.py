@@ -48,7 +48,14 @@ class orc_frame_desc(C.Structure):
     _fields_ = [("width", i32), ("height", i32), ("ctu", i32),
                 ("in_", vp * 3), ("in_stride", ip * 2),
                 ("ref", vp * 3), ("ref_stride", ip * 2),
-                ("search_range", i32), ("sad_lambda", u32), ("qp", i32), ("uv_qp", i32), ("intra_frame", i32)]
+                ("search_range", i32), ("sad_lambda", u32), ("qp", i32), ("uv_qp", i32), ("intra_frame", i32),
+                ("search_mode", i32), ("in_lo", vp * 2), ("in_lo_stride", ip * 2),
+                ("ref_lo", vp * 2), ("ref_lo_stride", ip * 2)]
+
+
+class orc_hier_in(C.Structure):
+    _fields_ = [("in_", vp * 3), ("in_stride", ip * 3), ("ref", vp * 3), ("ref_stride", ip * 3),
+                ("cand", vp), ("ncand", u32)]
 
 
 class orc_dq_param(C.Structure):
@@ -131,6 +138,11 @@ _SIGS = {
     "me_full": ("orc_me_full", None, [vp, ip, vp, ip, u32, u32, i32, i32, i32, u32, i32, i32, i32, i32, C.POINTER(orc_me_io)]),
     "full_subpel_me": ("orc_full_subpel_me", None, [vp, ip, vp, ip, u32, u32, i32, i32, u32, i32, i32, i32, i32,
                                                     C.POINTER(orc_me_io)]),
+    "downscale2x2": ("orc_downscale2x2", None, [vp, ip, C.c_int, C.c_int, vp, ip, u32, u32]),
+    "hier_search": ("orc_hier_search", None, [vp, ip, vp, ip, i32, i32, i32, i32, u32, u32, C.POINTER(i32),
+                                              C.POINTER(i32)]),
+    "me_hier": ("orc_me_hier", None, [C.POINTER(orc_hier_in), u32, u32, i32, i32, i32, i32, u32, i32, i32, i32, i32,
+                                      C.POINTER(orc_me_io)]),
     "cu_hotpath": ("orc_cu_hotpath", None, [C.POINTER(orc_frame_desc), i32, i32, i32, vp * 3, ip * 2, vp * 3, ip * 2,
                                             C.POINTER(orc_cu_out)]),
     "tr_matrix": ("orc_tr_matrix", None, [C.c_int, C.c_int]),

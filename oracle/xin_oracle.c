@@ -867,6 +867,95 @@ void orc_me_full(const opix *in, intptr_t is, const opix *ref_at_pu, intptr_t rs
     io->best_cost = best; io->best_sad = bsad; io->best_mvx = bx; io->best_mvy = by;
 }
 
+/* ---- integer search by resolution levels --------------------------------
+ * The reference's hierarchical search (Xin26xMotionEstHier, its level searches
+ * Xin26xMotionSearchHier1/2 and the 2x2 downscale Xin26xDownscale2x2;
+ * h26x_core/include/h26x_motion_est.h:23-36,
+ * h26x_core/include/h26x_hierarchic_motion_search.h:29,42,
+ * h26x_core/include/h26x_downscale_subs.h:23) exists only in the closed
+ * library: its order is not published.  Restated here; parity unpinned. */
+
+/* 2x2 downscale (typedef XinDownscale2x2, h266_encoder/include/h266_func_struct.h:425):
+ * out(x, y) = (a + b + c + d + 2) >> 2 over in(2x..2x+1, 2y..2y+1).  Every open
+ * caller passes FALSE for both row flags (h266_enc_init.c:2804-2824,
+ * h266_scene_cut.c:64); only that form is defined here. */
+void orc_downscale2x2(const opix *in, intptr_t is, int row_above, int row_below, opix *out, intptr_t os,
+                      uint32_t ow, uint32_t oh)
+{
+    (void)row_above; (void)row_below;
+    for (uint32_t y = 0; y < oh; y++)
+        for (uint32_t x = 0; x < ow; x++) {
+            const opix *a = in + (intptr_t)(2 * y) * is + 2 * x;
+            out[(intptr_t)y * os + x] = (opix)((a[0] + a[1] + a[is] + a[is + 1] + 2) >> 2);
+        }
+}
+
+/* one level (typedef XinHierMotionSearch, h266_func_struct.h:435): every MV of
+ * [min_x, max_x] x [min_y, max_y] at the level's resolution, raster order
+ * (y outer), strict '<' on the SAD of the w x h block; an empty window leaves
+ * the output untouched */
+void orc_hier_search(const opix *in, intptr_t is, const opix *ref, intptr_t rs, int32_t min_x, int32_t max_x,
+                     int32_t min_y, int32_t max_y, uint32_t w, uint32_t h, int32_t *best_x, int32_t *best_y)
+{
+    uint32_t best = 0xFFFFFFFFu;
+    for (int32_t y = min_y; y <= max_y; y++)
+        for (int32_t x = min_x; x <= max_x; x++) {
+            uint32_t sad;
+            orc_sad(in, is, ref + (intptr_t)y * rs + x, rs, w, h, &sad);
+            if (sad < best) { best = sad; *best_x = x; *best_y = y; }
+        }
+}
+
+static int32_t ceil_shr(int32_t v, int s) { return -((-v) >> s); }
+
+/* The driver:
+ *  window   [c - range, c + range] intersected with [min, max], c = predictor >> 2
+ *           (full-pel); at level L (1/2, 1/4) its ends become ceil(lo / 2^L) and
+ *           floor(hi / 2^L)
+ *  start    the incoming best, then every candidate (quarter-pel MV >> 2,
+ *           clipped to the window) with the full cost, list order, strict '<'
+ *  1/4      exhaustive SAD over the level window, block (w/4) x (h/4); b2
+ *  1/2      +-1 around 2 * b2 within the level window, block (w/2) x (h/2); b1
+ *  full     the 3 x 3 MVs around 2 * b1 within the window, raster order, full
+ *           cost (SAD << 8) + (bits(mvd x) + bits(mvd y)) * lambda against the
+ *           running best, strict '<'
+ * A level whose window is empty keeps the centre it was given (c >> L). */
+void orc_me_hier(const orc_hier_in *hi, uint32_t w, uint32_t h, int32_t mvpx, int32_t mvpy, int32_t range_x,
+                 int32_t range_y, uint32_t lambda, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
+                 orc_me_io *io)
+{
+    const int32_t cx = mvpx >> 2, cy = mvpy >> 2;
+    const int32_t x0 = cx - range_x > min_mvx ? cx - range_x : min_mvx, x1 = cx + range_x < max_mvx ? cx + range_x : max_mvx;
+    const int32_t y0 = cy - range_y > min_mvy ? cy - range_y : min_mvy, y1 = cy + range_y < max_mvy ? cy + range_y : max_mvy;
+    uint32_t best = io->best_cost, bsad = io->best_sad;
+    int32_t bx = io->best_mvx, by = io->best_mvy;
+    for (uint32_t i = 0; i < hi->ncand; i++) {
+        int32_t x = CLIP3(x0, x1, hi->cand[2 * i] >> 2), y = CLIP3(y0, y1, hi->cand[2 * i + 1] >> 2);
+        uint32_t sad;
+        orc_sad(hi->in[0], hi->in_stride[0], hi->ref[0] + (intptr_t)y * hi->ref_stride[0] + x, hi->ref_stride[0], w, h, &sad);
+        uint32_t c = (sad << 8) + mv_cost(x * 4, y * 4, mvpx, mvpy, lambda);
+        if (c < best) { best = c; bsad = sad; bx = x * 4; by = y * 4; }
+    }
+    int32_t b2x = cx >> 2, b2y = cy >> 2;
+    orc_hier_search(hi->in[2], hi->in_stride[2], hi->ref[2], hi->ref_stride[2], ceil_shr(x0, 2), x1 >> 2,
+                    ceil_shr(y0, 2), y1 >> 2, w >> 2, h >> 2, &b2x, &b2y);
+    const int32_t l1x0 = ceil_shr(x0, 1), l1x1 = x1 >> 1, l1y0 = ceil_shr(y0, 1), l1y1 = y1 >> 1;
+    int32_t b1x = cx >> 1, b1y = cy >> 1;
+    orc_hier_search(hi->in[1], hi->in_stride[1], hi->ref[1], hi->ref_stride[1],
+                    2 * b2x - 1 > l1x0 ? 2 * b2x - 1 : l1x0, 2 * b2x + 1 < l1x1 ? 2 * b2x + 1 : l1x1,
+                    2 * b2y - 1 > l1y0 ? 2 * b2y - 1 : l1y0, 2 * b2y + 1 < l1y1 ? 2 * b2y + 1 : l1y1,
+                    w >> 1, h >> 1, &b1x, &b1y);
+    for (int32_t y = 2 * b1y - 1; y <= 2 * b1y + 1; y++)
+        for (int32_t x = 2 * b1x - 1; x <= 2 * b1x + 1; x++) {
+            if (x < x0 || x > x1 || y < y0 || y > y1) continue;
+            uint32_t sad;
+            orc_sad(hi->in[0], hi->in_stride[0], hi->ref[0] + (intptr_t)y * hi->ref_stride[0] + x, hi->ref_stride[0], w, h, &sad);
+            uint32_t c = (sad << 8) + mv_cost(x * 4, y * 4, mvpx, mvpy, lambda);
+            if (c < best) { best = c; bsad = sad; bx = x * 4; by = y * 4; }
+        }
+    io->best_cost = best; io->best_sad = bsad; io->best_mvx = bx; io->best_mvy = by;
+}
+
 /* Xin266FullSubPelMe (open, h266_sub_pel_refine.c:81-212): 8 half-pel then 8
  * quarter-pel neighbours in the fixed order of :47-55, luma interpolation with the
  * default filter into a W x H block, SAD, strict '<'.  Returns unchanged when the
@@ -913,8 +1002,25 @@ void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t
     const opix *in_y = f->in[0] + (intptr_t)cu_y * f->in_stride[0] + cu_x;
     const opix *ref_y = f->ref[0] + (intptr_t)cu_y * f->ref_stride[0] + cu_x;
     orc_me_io io = { 0, 0, 0xFFFFFFFFu, 0 };
-    orc_me_full(in_y, f->in_stride[0], ref_y, f->ref_stride[0], (uint32_t)size, (uint32_t)size, 0, 0,
-                f->search_range, f->sad_lambda, mnx, mny, mxx, mxy, &io);
+    if (f->search_mode == 1) {
+        /* predictor 0, one candidate: the zero MV (Xin266FillMeCand's meCand[0],
+         * h266_analyze_inter_cu.c:168) */
+        static const int32_t zero[2] = { 0, 0 };
+        orc_hier_in hin;
+        hin.in[0] = in_y; hin.in_stride[0] = f->in_stride[0];
+        hin.ref[0] = ref_y; hin.ref_stride[0] = f->ref_stride[0];
+        for (int l = 1; l <= 2; l++) {
+            hin.in[l] = f->in_lo[l - 1] + (intptr_t)(cu_y >> l) * f->in_lo_stride[l - 1] + (cu_x >> l);
+            hin.in_stride[l] = f->in_lo_stride[l - 1];
+            hin.ref[l] = f->ref_lo[l - 1] + (intptr_t)(cu_y >> l) * f->ref_lo_stride[l - 1] + (cu_x >> l);
+            hin.ref_stride[l] = f->ref_lo_stride[l - 1];
+        }
+        hin.cand = zero; hin.ncand = 1;
+        orc_me_hier(&hin, (uint32_t)size, (uint32_t)size, 0, 0, f->search_range, f->search_range, f->sad_lambda,
+                    mnx, mny, mxx, mxy, &io);
+    } else
+        orc_me_full(in_y, f->in_stride[0], ref_y, f->ref_stride[0], (uint32_t)size, (uint32_t)size, 0, 0,
+                    f->search_range, f->sad_lambda, mnx, mny, mxx, mxy, &io);
     out->int_cost = io.best_cost;
     orc_full_subpel_me(in_y, f->in_stride[0], ref_y, f->ref_stride[0], (uint32_t)size, (uint32_t)size, 0, 0,
                        f->sad_lambda, mnx, mny, mxx, mxy, &io);

@@ -152,6 +152,20 @@ void orc_full_subpel_me(const opix *in, intptr_t is, const opix *ref_at_pu, intp
                         int32_t mvpx, int32_t mvpy, uint32_t lambda,
                         int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy, orc_me_io *io);
 
+/* ---- hierarchical integer search (restated; the reference's is closed) */
+void orc_downscale2x2(const opix *in, intptr_t is, int row_above, int row_below, opix *out, intptr_t os,
+                      uint32_t ow, uint32_t oh);
+void orc_hier_search(const opix *in, intptr_t is, const opix *ref, intptr_t rs, int32_t min_x, int32_t max_x,
+                     int32_t min_y, int32_t max_y, uint32_t w, uint32_t h, int32_t *best_x, int32_t *best_y);
+typedef struct orc_hier_in {
+    const opix *in[3];  intptr_t in_stride[3];    /* current block at full, 1/2 and 1/4 resolution */
+    const opix *ref[3]; intptr_t ref_stride[3];   /* reference at the block's position, same levels */
+    const int32_t *cand; uint32_t ncand;           /* quarter-pel candidate MVs (x, y pairs) */
+} orc_hier_in;
+void orc_me_hier(const orc_hier_in *hi, uint32_t w, uint32_t h, int32_t mvpx, int32_t mvpy, int32_t range_x,
+                 int32_t range_y, uint32_t lambda, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
+                 orc_me_io *io);
+
 /* ---- frame hot path: one CU through ME + MC + TQ + recon (the batched GPU frame stage's checker) */
 typedef struct orc_frame_desc {
     int32_t width, height, ctu;            /* luma size, CTU size (padding = ctu + 16) */
@@ -161,6 +175,9 @@ typedef struct orc_frame_desc {
     uint32_t sad_lambda;
     int32_t qp, uv_qp;
     int32_t intra_frame;                   /* 0 for P/B: qAdd = 85 << (qShift - 9) */
+    int32_t search_mode;                   /* 0 exhaustive, 1 by resolution levels (orc_me_hier) */
+    const opix *in_lo[2];  intptr_t in_lo_stride[2];    /* search_mode 1: luma at 1/2 and 1/4 resolution, */
+    const opix *ref_lo[2]; intptr_t ref_lo_stride[2];   /* pointers at picture (0,0) */
 } orc_frame_desc;
 typedef struct orc_cu_out {
     int32_t mvx, mvy;                      /* quarter-pel */

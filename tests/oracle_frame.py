@@ -14,9 +14,25 @@ from xin26x_gb300.frame import CU_DTYPE
 from xin26x_gb300.synth import pad_plane
 
 
-def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=64, bitdepth=8, cus=None, threads=1):
+def downscaled(plane, o, levels=2):
+    """The plane at 1/2 and 1/4 resolution by the oracle's 2x2 downscale."""
+    out = []
+    src = np.ascontiguousarray(plane)
+    for _ in range(levels):
+        h, w = src.shape[0] // 2, src.shape[1] // 2
+        dst = np.zeros((h, w), src.dtype)
+        o.downscale2x2(src.ctypes.data, src.shape[1], 0, 0, dst.ctypes.data, w, w, h)
+        out.append(dst)
+        src = dst
+    return out
+
+
+def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=64, bitdepth=8, cus=None, threads=1,
+        search_mode=0):
     """cur, ref: (Y, U, V) planes.  levels: [(size, first, cus_x, cus_y)] as the stream reports.
     cus: optional list of global CU indices to evaluate (others left zero).
+    search_mode: 0 exhaustive integer search, 1 by resolution levels (the reference
+    and the current picture downscaled by 2 and 4, the padded reference as a whole).
     threads: host threads sharing the CUs (0 = every core); each CU writes only its
     own record and its own area of the level's planes, so the calls are independent.
     Returns (cu records, q planes [levels,h,w] x3, rec planes x3)."""
@@ -34,6 +50,17 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
     f.in_stride[0], f.in_stride[1] = w, w // 2
     f.ref_stride[0], f.ref_stride[1] = refp[0].shape[1], refp[1].shape[1]
     f.search_range, f.sad_lambda, f.qp, f.uv_qp, f.intra_frame = search_range, sad_lambda, qp, uv_qp, 0
+    f.search_mode = search_mode
+    keep = []
+    if search_mode == 1:
+        ref_lo, in_lo = downscaled(refp[0], o), downscaled(curc[0], o)
+        keep = ref_lo + in_lo
+        for l in range(2):
+            pl = pad >> (l + 1)
+            f.ref_lo[l] = ref_lo[l].ctypes.data + (pl * ref_lo[l].shape[1] + pl) * ref_lo[l].itemsize
+            f.ref_lo_stride[l] = ref_lo[l].shape[1]
+            f.in_lo[l] = in_lo[l].ctypes.data
+            f.in_lo_stride[l] = in_lo[l].shape[1]
     ncu = sum(cx * cy for (_, _, cx, cy) in levels)
     recs = np.zeros(ncu, CU_DTYPE)
     nl = len(levels)

@@ -298,3 +298,31 @@ def test_frame_wait_timeout_then_collect():
     assert np.array_equal(outs[0]["cu"], outs[1]["cu"])
     for p in range(3):
         assert np.array_equal(outs[0]["q"][p], outs[1]["q"][p])
+
+
+@pytest.mark.parametrize("bd,inb", [(8, 0), (10, 0), (10, 8)])
+@pytest.mark.parametrize("w,h,R,ctu", [(192, 128, 16, 64), (208, 120, 64, 64), (200, 104, 37, 128), (384, 256, 256, 128)])
+def test_frame_hier_search_matches_oracle(bd, inb, w, h, R, ctu):
+    """search_mode 1 (search by resolution levels): every CU of every level, the
+    coefficient and reconstructed planes, against the oracle's per-CU hot path
+    with orc_me_hier on the oracle's own 1/2 and 1/4 planes; search ranges up to
+    the reference maximum +-256, 8-bit pictures into the 10-bit library."""
+    seq = synth.sequence(w, h, 3, seed=w + R, bitdepth=8 if inb == 8 else bd, objects=2)
+    fs = FrameStream(w, h, ctu=ctu, search_range=R, out_q=True, out_rec=True, bitdepth=bd, input_bitdepth=inb,
+                     search_mode=1)
+    try:
+        fs.submit(*seq[0], qp=32, uv_qp=32, sad_lambda=64)
+        fs.wait()
+        for k in (1, 2):
+            qp = 27 + 5 * k
+            lam = (40 + 30 * k) << (2 if inb == 8 else 0)
+            fs.submit(*seq[k], qp=qp, uv_qp=qp, sad_lambda=lam)
+            out = fs.wait()
+            cur, ref = seq[k], seq[k - 1]
+            if inb == 8:
+                cur, ref = [tuple(p.astype(np.uint16) << 2 for p in f) for f in (cur, ref)]
+            want = oracle_frame.run(cur, ref, fs.levels, ctu=ctu, search_range=R, qp=qp, uv_qp=qp, sad_lambda=lam,
+                                    bitdepth=bd, threads=0, search_mode=1)
+            _compare(out, want, fs.levels, ("hier", bd, inb, w, h, R, k))
+    finally:
+        fs.close()

@@ -357,6 +357,108 @@ def test_motion_search_default_range(libs):
             assert (me.bestMv.mvX, me.bestMv.mvY, me.bestCost) == (io.best_mvx, io.best_mvy, io.best_cost)
 
 
+def _down(o, plane, levels=2):
+    out, src = [], np.ascontiguousarray(plane)
+    for _ in range(levels):
+        h, w = src.shape[0] // 2, src.shape[1] // 2
+        d = np.zeros((h, w), src.dtype)
+        o.downscale2x2(P(src), src.shape[1], 0, 0, P(d), w, w, h)
+        out.append(d)
+        src = d
+    return out
+
+
+def test_downscale2x2(libs):
+    """XinGpuDownscale2x2 against the oracle's restatement, odd output sizes and
+    strides; the row flags (never set by the reference's callers) are refused."""
+    g, o, bd = libs
+    rng = np.random.default_rng(22)
+    mx = (1 << bd) - 1
+    for ow, oh in [(1, 1), (7, 5), (64, 32), (133, 71), (960, 540)]:
+        src = rng.integers(0, mx + 1, size=(2 * oh + 3, 2 * ow + 5)).astype(o.pix)
+        a = np.full((oh, ow + 2), 7, o.pix)
+        b = a.copy()
+        g.XinGpuDownscale2x2(P(src), src.shape[1], 0, 0, P(a), ow + 2, ow, oh); _ok(g)
+        o.downscale2x2(P(src), src.shape[1], 0, 0, P(b), ow + 2, ow, oh)
+        assert np.array_equal(a, b), (ow, oh)
+    g.XinGpuDownscale2x2(P(src), src.shape[1], 1, 0, P(a), ow + 2, ow, oh)
+    assert g.xin_gpu_last_status() == -2
+
+
+def test_motion_search_hier_level(libs):
+    """XinGpuMotionSearchHier (one level): every MV of the window, SAD, strict '<'
+    in raster order; an empty window leaves the output unchanged."""
+    from xin26x_gb300 import _lib
+    g, o, bd = libs
+    rng = np.random.default_rng(23)
+    mx = (1 << bd) - 1
+    pad = 40
+    for w, h in [(2, 2), (4, 4), (8, 8), (16, 16), (4, 8), (32, 16)]:
+        base = rng.integers(0, mx + 1, size=(h + 2 * pad, w + 2 * pad)).astype(np.int32)
+        refp = ((base + np.roll(base, 1, 1)) // 2).astype(o.pix)
+        inp = np.ascontiguousarray(refp[pad + 3:pad + 3 + h, pad - 6:pad - 6 + w])
+        for win in [(-16, 16, -16, 16), (-3, 9, 0, 0), (5, 30, -30, -2), (4, 3, 0, 0)]:
+            mv = _lib.xin_gpu_mv()
+            mv.mvX, mv.mvY = 77, -77
+            g.XinGpuMotionSearchHier(P(inp), w, P(refp, pad * refp.shape[1] + pad), refp.shape[1], win[0], win[1],
+                                     win[2], win[3], w, h, C.byref(mv)); _ok(g)
+            bx, by = C.c_int32(77), C.c_int32(-77)
+            o.hier_search(P(inp), w, P(refp, pad * refp.shape[1] + pad), refp.shape[1], win[0], win[1], win[2], win[3],
+                          w, h, C.byref(bx), C.byref(by))
+            assert (mv.mvX, mv.mvY) == (bx.value, by.value), (w, h, win)
+
+
+def test_motion_est_hier_driver(libs):
+    """XinGpuMotionEstHier on the reference's ME state against the oracle's
+    restatement (orc_me_hier): levels downscaled from the padded reference and
+    the current picture, candidate lists, predictors, windows that clip, ranges
+    up to the encoder's default +-64."""
+    from xin26x_gb300 import _lib
+    g, o, bd = libs
+    rng = np.random.default_rng(24)
+    mx = (1 << bd) - 1
+    pad = 96
+    H, W = 128, 192
+    base = rng.integers(0, mx + 1, size=(H + 2 * pad, W + 2 * pad)).astype(np.int32)
+    refp = ((base + np.roll(base, 1, 0) + np.roll(base, 1, 1) + np.roll(base, 3, 1)) // 4).astype(o.pix)
+    cur = np.ascontiguousarray(np.roll(refp, (5, -13), (0, 1))[pad:pad + H, pad:pad + W])
+    ref_lo, cur_lo = _down(o, refp), _down(o, cur)
+    for (w, h, px, py) in [(8, 8, 16, 8), (16, 16, 64, 32), (32, 32, 96, 64), (64, 64, 64, 64), (16, 8, 8, 40)]:
+        for R, mvp, win, cands in [(16, (0, 0), (-40, -40, 40, 40), [(0, 0)]),
+                                   (64, (-20, 12), (-80, -70, 75, 60), [(0, 0), (-20, 12), (52, -9)]),
+                                   (24, (8, 8), (-10, -3, 6, 90), [(0, 0), (8, 8), (400, -400)])]:
+            lam = int(rng.integers(0, 300))
+            me = _lib.xin_gpu_me_struct()
+            me.width, me.height = w, h
+            me.input, me.inputStride = P(cur, py * W + px), W
+            me.input1, me.input1Stride = P(cur_lo[0], (py // 2) * cur_lo[0].shape[1] + px // 2), cur_lo[0].shape[1]
+            me.input2, me.input2Stride = P(cur_lo[1], (py // 4) * cur_lo[1].shape[1] + px // 4), cur_lo[1].shape[1]
+            rs = [refp.shape[1], ref_lo[0].shape[1], ref_lo[1].shape[1]]
+            me.ref, me.refStride = P(refp, (pad + py) * rs[0] + pad + px), rs[0]
+            me.ref1, me.ref1Stride = P(ref_lo[0], (pad // 2 + py // 2) * rs[1] + pad // 2 + px // 2), rs[1]
+            me.ref2, me.ref2Stride = P(ref_lo[1], (pad // 4 + py // 4) * rs[2] + pad // 4 + px // 4), rs[2]
+            me.searchWidth = me.searchHeight = R
+            me.predMv.mvX, me.predMv.mvY = mvp
+            me.bestMv.mvX, me.bestMv.mvY = 0, 0
+            me.bestCost, me.bestSad = 0xFFFFFFFF, 0
+            me.minMv.mvX, me.minMv.mvY, me.maxMv.mvX, me.maxMv.mvY = win
+            me.sadLambda = lam
+            me.candNum = len(cands)
+            for i, (cx, cy) in enumerate(cands):
+                me.meCand[i].mvX, me.meCand[i].mvY = cx, cy
+            g.XinGpuMotionEstHier(C.byref(me)); _ok(g, "MotionEstHier")
+            hin = O.orc_hier_in()
+            for l, (ip_, ist, rp_, rst) in enumerate([(me.input, W, me.ref, rs[0]), (me.input1, me.input1Stride, me.ref1, rs[1]),
+                                                      (me.input2, me.input2Stride, me.ref2, rs[2])]):
+                hin.in_[l], hin.in_stride[l], hin.ref[l], hin.ref_stride[l] = ip_, ist, rp_, rst
+            ca = np.array(cands, np.int32).reshape(-1)
+            hin.cand, hin.ncand = ca.ctypes.data, len(cands)
+            io = O.orc_me_io(0, 0, 0xFFFFFFFF, 0)
+            o.me_hier(C.byref(hin), w, h, mvp[0], mvp[1], R, R, lam, win[0], win[1], win[2], win[3], io)
+            assert (me.bestMv.mvX, me.bestMv.mvY, me.bestCost, me.bestSad) == \
+                (io.best_mvx, io.best_mvy, io.best_cost, io.best_sad), (w, h, R, mvp)
+
+
 def test_invalid_arguments_report_errors(libs):
     g, o, bd = libs
     a = np.zeros(64, o.pix)

@@ -20,7 +20,7 @@ i32, u32, u64, ip, vp = C.c_int32, C.c_uint32, C.c_uint64, C.c_ssize_t, C.c_void
 class xin_gpu_stream_cfg(C.Structure):
     _fields_ = [("width", i32), ("height", i32), ("ctu_size", i32), ("search_range", i32),
                 ("level_mask", u32), ("out_flags", u32), ("use_graph", i32), ("device_io", i32),
-                ("input_bitdepth", i32)]
+                ("input_bitdepth", i32), ("search_mode", i32)]
 
 
 class xin_gpu_picture(C.Structure):
@@ -164,6 +164,9 @@ SIGNATURES = {
     "XinGpuBiliInterpHor": ([vp, C.c_ssize_t, vp, C.c_ssize_t, i32, u32, u32], None),
     "XinGpuBiliInterpVet": ([vp, C.c_ssize_t, vp, C.c_ssize_t, i32, u32, u32], None),
     "XinGpuBiliInterpHorVet": ([vp, C.c_ssize_t, vp, C.c_ssize_t, i32, u32, u32], None),
+    "XinGpuDownscale2x2": ([vp, C.c_ssize_t, i32, i32, vp, C.c_ssize_t, u32, u32], None),
+    "XinGpuMotionSearchHier": ([vp, C.c_ssize_t, vp, C.c_ssize_t, i32, i32, i32, i32, u32, u32, vp], None),
+    "XinGpuMotionEstHier": ([vp], None),
     "XinGpuDepQuant": ([vp, vp, vp, vp, vp, vp, C.c_ssize_t, u32, i32, i32, vp, u32], None),
 }
 for _n in ["InterpCopy", "InterpCopyU8S16", "LumaInterpHor", "LumaInterpVet", "LumaInterpHorVet", "LumaInterpHorU8S16",

@@ -4,6 +4,7 @@
  * outputs; the per-picture launches captured once per slot into a CUDA graph.
  */
 #include "xg_frame_kernels.cuh"
+#include "xg_hier.cuh"
 
 #include <chrono>
 #include <new>
@@ -23,6 +24,11 @@ struct xin_gpu_stream {
     XgPlane slot[2][3];
     xg_pix *qpel_base[2];
     XgQpel qpel[2];
+    /* search_mode 1: luma at 1/2 and 1/4 resolution of each slot, downscaled from
+     * the padded slot as a whole (the margins included) */
+    xg_pix *lo_base[2][2];
+    XgPlane lo[2][2];
+    int lo_pitch[2], lo_rows[2];
     unsigned long long *keys;
     /* what a picture in flight owns; picture k uses set k & 1 (its slot), so two
      * pictures can be in flight: one computing while the other's copies run */
@@ -85,7 +91,11 @@ static int xg_stream_free(xin_gpu_stream *s)
     if (s->st) cudaStreamSynchronize(s->st);
     if (s->cst) cudaStreamSynchronize(s->cst);
     for (int i = 0; i < 2; i++) if (s->gexec[i]) cudaGraphExecDestroy(s->gexec[i]);
-    for (int i = 0; i < 2; i++) { for (int p = 0; p < 3; p++) cudaFree(s->slot_base[i][p]); cudaFree(s->qpel_base[i]); }
+    for (int i = 0; i < 2; i++) {
+        for (int p = 0; p < 3; p++) cudaFree(s->slot_base[i][p]);
+        cudaFree(s->qpel_base[i]);
+        for (int l = 0; l < 2; l++) cudaFree(s->lo_base[i][l]);
+    }
     cudaFree(s->keys);
     for (auto &t : s->set) {
         cudaFree(t.dres); cudaFree(t.dpp);
@@ -135,8 +145,8 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     const xin_gpu_stream_cfg &c = *cfg;
     if (c.width < 16 || c.height < 16 || (c.width & 1) || (c.height & 1) || c.width > 8192 || c.height > 8192 ||
         (c.ctu_size != 64 && c.ctu_size != 128) || c.search_range < 1 || c.search_range > 256 ||
-        !(c.level_mask & (8u | 16u | 32u | 64u)) || !xg_input_depth_ok(c)) {
-        xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range, level mask or input bit depth");
+        !(c.level_mask & (8u | 16u | 32u | 64u)) || !xg_input_depth_ok(c) || (c.search_mode != 0 && c.search_mode != 1)) {
+        xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range, level mask, input bit depth or search mode");
         return XIN_GPU_ERR_ARG;
     }
     xin_gpu_stream *s = new (std::nothrow) xin_gpu_stream();
@@ -197,6 +207,11 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     for (int i = 0; i < 2 && e == cudaSuccess; i++) {
         for (int p = 0; p < 3 && e == cudaSuccess; p++) e = cudaMalloc(&s->slot_base[i][p], p ? csz : ysz);
         if (e == cudaSuccess) e = cudaMalloc(&s->qpel_base[i], 16 * ysz);
+        for (int l = 0; l < 2 && e == cudaSuccess && c.search_mode == 1; l++) {
+            s->lo_pitch[l] = (((c.width + 2 * pad) >> (l + 1)) + 127) & ~127;
+            s->lo_rows[l] = (c.height + 2 * pad) >> (l + 1);
+            e = cudaMalloc(&s->lo_base[i][l], (size_t)s->lo_pitch[l] * s->lo_rows[l] * sizeof(xg_pix));
+        }
     }
     if (e == cudaSuccess) e = cudaMalloc(&s->keys, sizeof(unsigned long long) * (s->ncus > 0 ? s->ncus : 1));
     for (auto &t : s->set) {
@@ -235,6 +250,13 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
             pl.w = p ? c.width / 2 : c.width;
             pl.h = p ? c.height / 2 : c.height;
             pl.pad = pd;
+        }
+        for (int l = 0; l < 2 && c.search_mode == 1; l++) {
+            XgPlane &pl = s->lo[i][l];
+            const int pd = pad >> (l + 1);
+            pl.data = s->lo_base[i][l] + (size_t)pd * s->lo_pitch[l] + pd;
+            pl.pitch = s->lo_pitch[l];
+            pl.w = c.width >> (l + 1); pl.h = c.height >> (l + 1); pl.pad = pd;
         }
         XgQpel &q = s->qpel[i];
         for (int k = 0; k < 16; k++) q.plane[k] = s->qpel_base[i] + (size_t)k * s->plane_elems + (size_t)pad * s->pitch + pad;
@@ -381,6 +403,20 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
                                          t.d_in8[2], mode);
         nl++;
     }
+    if (c.search_mode == 1) {
+        /* the new slot at 1/2 and 1/4 resolution: the current picture's levels now,
+         * the reference's for the next picture */
+        const xg_pix *src = s->slot_base[cur][0];
+        long long sp = s->pitch;
+        for (int l = 0; l < 2; l++) {
+            const int ow = (c.width + 2 * s->pad) >> (l + 1), oh = s->lo_rows[l];
+            dim3 grd((ow + 127) / 128, oh);
+            k_downscale2x2<<<grd, 128, 0, st>>>(src, sp, s->lo_base[cur][l], s->lo_pitch[l], ow, oh);
+            src = s->lo_base[cur][l];
+            sp = s->lo_pitch[l];
+            nl++;
+        }
+    }
     xg_stage_event(t.evs[1], st, capturing);
     /* the new picture's quarter-pel planes are read only by the next picture's
      * tails: build them on a low-priority stream beside the search */
@@ -388,6 +424,23 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
     if (with_me) {
         int ref = 1 - cur;
         cudaMemsetAsync(s->keys, 0xff, sizeof(unsigned long long) * s->ncus, st);
+        if (c.search_mode == 1) {
+            XgHierFrameParams hp;
+            memset(&hp, 0, sizeof hp);
+            hp.cur = s->slot[cur][0]; hp.ref = s->slot[ref][0];
+            for (int l = 0; l < 2; l++) { hp.cur_lo[l] = s->lo[cur][l]; hp.ref_lo[l] = s->lo[ref][l]; }
+            hp.W = c.width; hp.H = c.height; hp.ctu = c.ctu_size; hp.R = c.search_range;
+            int nz = 0;
+            for (int L = 0; L < 4; L++) {
+                if (!s->lev_on[L]) continue;
+                hp.level_size[nz] = XG_LEVEL_SIZE[L];
+                hp.keys[nz] = s->keys + s->lev_first[L];
+                hp.cus_x[nz] = s->lev_cx[L];
+                nz++;
+            }
+            dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, nz);
+            k_hier_frame<<<grd, XG_HIER_THREADS, xg_hier_smem(c.search_range), st>>>(hp, t.dpp);
+        } else {
         XgMeParams mp;
         mp.cur = s->slot[cur][0];
         mp.ref = s->slot[ref][0];
@@ -405,6 +458,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         else
 #endif
             k_me_tiles<8><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, t.dpp);
+        }
         nl++;
         nl += xg_enqueue_qpel(s, cur);
         /* the search's end is recorded on a side branch joined at the picture's

@@ -80,7 +80,10 @@ extern "C" int xin_gpu_install(void *funcSet, void *meFunc, uint32_t what)
             }
             if (what & XIN_GPU_INSTALL_QUANT) fs->pfXinQuantInvQuant[lg] = XG_FN(XinGpuQuantInvQuant);
         }
-        if (what & XIN_GPU_INSTALL_DIST) fs->pfXinComputeHada8x8 = XG_FN(XinGpuComputeHada8x8);
+        if (what & XIN_GPU_INSTALL_DIST) {
+            fs->pfXinComputeHada8x8 = XG_FN(XinGpuComputeHada8x8);
+            fs->pfXinDownscale2x2 = XG_FN(XinGpuDownscale2x2);
+        }
         if (what & XIN_GPU_INSTALL_QUANT) {
             fs->pfXinPreRdoq = XG_FN(XinGpuPreRdoq);
             fs->pfXinDepQuant = XG_FN(XinGpuDepQuant);
@@ -96,7 +99,10 @@ extern "C" int xin_gpu_install(void *funcSet, void *meFunc, uint32_t what)
             mf->pfXinComputeAvgSadx8[lg] = (void *)XinGpuComputeAvgSadx8;
             mf->pfXinComputeVar[lg] = (void *)XinGpuComputeVar;
             mf->pfXinComputeAvgVar[lg] = (void *)XinGpuComputeAvgVar;
+            mf->pfXinMotionSearchHier1[lg] = (void *)XinGpuMotionSearchHier;
+            mf->pfXinMotionSearchHier2[lg] = (void *)XinGpuMotionSearchHier;
         }
+        mf->pfXinDownscale2x2 = (void *)XinGpuDownscale2x2;
     }
     return XIN_GPU_OK;
 }

@@ -22,9 +22,10 @@ OUT_Q, OUT_REC = 1, 2
 class FrameStream:
     def __init__(self, width: int, height: int, ctu: int = 64, search_range: int = 64,
                  levels=(64, 32, 16, 8), out_q: bool = True, out_rec: bool = False, use_graph: bool = True,
-                 bitdepth: int = 8, device: int = 0, input_bitdepth: int = 0):
+                 bitdepth: int = 8, device: int = 0, input_bitdepth: int = 0, search_mode: int = 0):
         """bitdepth: the library (8 or 10, the reference's ENABLE_10BIT_ENCODER);
-        input_bitdepth 8 with bitdepth 10: 8-bit pictures coded at 10 bits."""
+        input_bitdepth 8 with bitdepth 10: 8-bit pictures coded at 10 bits;
+        search_mode 0 exhaustive integer search, 1 by resolution levels."""
         self.lib = _lib.load(bitdepth)
         self.bitdepth = bitdepth
         self.in_pix = np.uint8 if (bitdepth == 8 or input_bitdepth == 8) else np.uint16
@@ -37,7 +38,7 @@ class FrameStream:
             mask |= int(s)
         self.cfg = _lib.xin_gpu_stream_cfg(width, height, ctu, search_range, mask,
                                            (OUT_Q if out_q else 0) | (OUT_REC if out_rec else 0), 1 if use_graph else 0,
-                                           0, input_bitdepth)
+                                           0, input_bitdepth, search_mode)
         h = C.c_void_p()
         st = self.lib.xin_gpu_stream_open(C.byref(self.cfg), C.byref(h))
         if st != 0:
