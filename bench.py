@@ -331,11 +331,15 @@ def run_gpu(args):
     kbatch = kernel_batch_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup) if rank == 0 else None
     dq = dep_quant_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup, cpu=(world == 1)) if rank == 0 else None
     wide = wide_search_bench(torch, flush) if rank == 0 else None
+    if wide is not None:
+        wide["by_resolution_levels"] = wide_search_bench(torch, flush, pictures=4, search_mode=1)
     variants = None
     if rank == 0:
         nvar = max(5, min(args.steps, 20))
         variants = {"eight_bit_build": pipeline_variant_bench(torch, flush, frames, nvar, args.warmup, 8, 0),
-                    "ten_bit_samples": pipeline_variant_bench(torch, flush, frames, nvar, args.warmup, 10, 0)}
+                    "ten_bit_samples": pipeline_variant_bench(torch, flush, frames, nvar, args.warmup, 10, 0),
+                    "search_by_resolution_levels": pipeline_variant_bench(torch, flush, frames, nvar, args.warmup,
+                                                                          BD, IN_BD, search_mode=1)}
     serving = None
     if rank == 0 and world == 1:
         from xin26x_gb300 import serve_bench
@@ -515,21 +519,23 @@ def dep_quant_bench(torch, flush, steps, warmup, nblocks=65536, seed=11, cpu=Tru
     return out
 
 
-def pipeline_variant_bench(torch, flush, frames, steps, warmup, bitdepth, input_bitdepth):
-    """The headline pictures through another build, for comparison: the 8-bit
-    library (8-bit arithmetic throughout), or the 10-bit library fed the pictures
-    as 10-bit samples (<< 2; the search then packs two samples a word instead of
-    four).  Device-resident pictures, device time per picture, L2 flushed."""
+def pipeline_variant_bench(torch, flush, frames, steps, warmup, bitdepth, input_bitdepth, search_mode=0):
+    """The headline pictures through another build or search, for comparison: the
+    8-bit library (8-bit arithmetic throughout), the 10-bit library fed the
+    pictures as 10-bit samples (<< 2; the search then packs two samples a word
+    instead of four), or the headline configuration with the search by resolution
+    levels (search_mode 1).  Device-resident pictures, device time per picture,
+    L2 flushed."""
     from xin26x_gb300 import _lib
     lib = _lib.load(bitdepth)
     assert lib.xin_gpu_init(torch.cuda.current_device()) == 0
-    if bitdepth == 8:
+    if bitdepth == 8 or input_bitdepth == 8:
         dev = [tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f) for f in frames]
     else:
         dev = [tuple((torch.from_numpy(np.ascontiguousarray(p)).cuda().to(torch.int32) << 2).to(torch.int16) for p in f)
                for f in frames]
     lam = LAMBDA if bitdepth == 8 else LAMBDA_BD
-    cfg = _lib.xin_gpu_stream_cfg(W, H, 64, SEARCH, sum(LEVELS), 0, 1, 1, input_bitdepth)
+    cfg = _lib.xin_gpu_stream_cfg(W, H, 64, SEARCH, sum(LEVELS), 0, 1, 1, input_bitdepth, search_mode)
     h = C.c_void_p()
     assert lib.xin_gpu_stream_open(C.byref(cfg), C.byref(h)) == 0, lib.xin_gpu_last_error()
     res = _lib.xin_gpu_results()
@@ -557,24 +563,27 @@ def pipeline_variant_bench(torch, flush, frames, steps, warmup, bitdepth, input_
         stage += np.array(list(st))
     lib.xin_gpu_stream_close(h)
     stage /= steps
-    return {"library": f"{bitdepth}-bit", "pictures": "8-bit" if bitdepth == 8 else "10-bit samples (8-bit << 2)",
+    return {"library": f"{bitdepth}-bit",
+            "pictures": "8-bit" if (bitdepth == 8 or input_bitdepth == 8) else "10-bit samples (8-bit << 2)",
+            "search": "by resolution levels (1/4 exhaustive, 1/2 and full +-1)" if search_mode else "exhaustive",
             "value": W * H * steps / (float(np.sum(ms)) * 1e-3) / 1e6, "unit": "Mpixel/s",
             "ms_per_picture": float(np.mean(ms)),
             "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_mc_tq": stage[2], "copies": stage[3]}}
 
 
-def wide_search_bench(torch, flush, pictures=3):
-    """3840x2160 10-bit 4:2:0, CTU 128, exhaustive +-256 integer search (the
-    reference's maximum picture size and a wide search), full sub-pel search and
-    TQ of CU levels 64/32/16/8; device-resident pictures, CUDA-event device time
-    per picture, L2 flushed between pictures."""
+def wide_search_bench(torch, flush, pictures=3, search_mode=0):
+    """3840x2160 10-bit 4:2:0, CTU 128, +-256 integer search (the reference's
+    maximum picture size and a wide search; exhaustive, or by resolution levels
+    with search_mode 1), full sub-pel search and TQ of CU levels 64/32/16/8;
+    device-resident pictures, CUDA-event device time per picture, L2 flushed
+    between pictures."""
     from xin26x_gb300 import _lib, synth
     w, h, r = 3840, 2160, 256
     g = _lib.load(10)
     assert g.xin_gpu_init(torch.cuda.current_device()) == 0
     seq = synth.sequence(w, h, pictures, seed=2160, bitdepth=10, objects=8, octaves=4)
     dev = [tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f) for f in seq]
-    cfg = _lib.xin_gpu_stream_cfg(w, h, 128, r, 120, 0, 1, 1)
+    cfg = _lib.xin_gpu_stream_cfg(w, h, 128, r, 120, 0, 1, 1, 0, search_mode)
     hs = C.c_void_p()
     assert g.xin_gpu_stream_open(C.byref(cfg), C.byref(hs)) == 0, g.xin_gpu_last_error()
     res = _lib.xin_gpu_results()
@@ -597,6 +606,18 @@ def wide_search_bench(torch, flush, pictures=3):
             ms.append(res.gpu_ms)
     g.xin_gpu_stream_close(hs)
     stage /= len(ms)
+    if search_mode == 1:
+        # work of the quarter-resolution level (the bulk): every CU of each level,
+        # (2 * (R >> 2) + 1)^2 candidates of (S/4)^2 samples
+        algo = 4 * (2 * (r >> 2) + 1) ** 2 * (w // 4) * (h // 4)
+        return {"workload": "3840x2160 10-bit 4:2:0, CTU 128, +-256 integer search by resolution levels (1/4 "
+                            "exhaustive +-64, 1/2 and full resolution +-1), full sub-pel search, CU levels 64/32/16/8, "
+                            "DCT2 TU=CU, seeded texture (4 octaves) + 8 moving rectangles",
+                "pictures_timed": len(ms), "ms_per_picture": float(np.mean(ms)), "value": w * h / float(np.mean(ms)) / 1e3,
+                "unit": "Mpixel/s", "dtype": "u16",
+                "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_mc_tq": stage[2]},
+                "search_absdiff_per_s": algo / (stage[1] * 1e-3),
+                "search_algorithmic": f"4 levels x (2*64+1)^2 x (W/4)(H/4) = {algo:.4g} abs differences at 1/4 resolution"}
     peak = C.c_double()
     g.xin_gpu_measure_sad_peak(C.byref(peak))
     algo = (w // 8) * (h // 8) * (2 * r + 1) ** 2 * 64

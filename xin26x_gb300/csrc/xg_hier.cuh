@@ -276,11 +276,14 @@ extern "C" void XinGpuMotionEstHier(struct xin_me_struct *meSetOpaque)
 /* ------------------------------------------------------------ frame form
  * One CTA per (64 x 64 tile, CU level): the tile's CUs of that level.  The
  * quarter-resolution reference window of the whole tile (16 + 2 R4 samples
- * square, R4 = R >> 2) and the tile's quarter-resolution current samples are
- * staged in shared memory; warps take the CUs (several warps share one CU's
- * candidates when the level has fewer than eight CUs a tile).  The 1/2 and
- * full-resolution steps read the planes directly.  Writes the CU's key
- * (cost << 32) | ((mvy + R) * (2R + 1) + mvx + R), the form the tails read. */
+ * square, R4 = R >> 2, rows padded by 4 samples) and the tile's
+ * quarter-resolution current samples are staged in shared memory.  A group of
+ * G warps takes a CU (G = 8 / CUs a tile, at least 1): at 1/4 each lane
+ * evaluates four horizontally adjacent candidates at a time from a sliding
+ * window of reference samples; the 1/2 and full-resolution steps split the
+ * block's samples over the group's lanes and read the planes directly.  Writes
+ * the CU's key (cost << 32) | ((mvy + R) * (2R + 1) + mvx + R), the form the
+ * tails read. */
 struct XgHierFrameParams {
     XgPlane cur, ref;            /* full-resolution luma slots */
     XgPlane cur_lo[2], ref_lo[2];/* 1/2 and 1/4 resolution (pointers at picture (0, 0)) */
@@ -292,104 +295,168 @@ struct XgHierFrameParams {
 
 #define XG_HIER_THREADS 256
 
+/* this lane's shares of the SADs of a (1 << lgw) x h block against the 3 x 3
+ * candidates around ctr (k = (dy + 1) * 3 + dx + 1, raster order) and, with
+ * EXTRA, one more candidate at ext: one load of the current sample and
+ * independent loads of the candidates' samples per position, so the loads of
+ * all candidates are in flight together.  Samples i = t, t + nt, ... */
+template <bool EXTRA>
+__device__ __forceinline__ void xg_sad_3x3(const xg_pix *c, long long cp, const xg_pix *ctr, const xg_pix *ext, long long rp,
+                                           int lgw, int h, int t, int nt, uint32_t s[10])
+{
+#pragma unroll
+    for (int k = 0; k < 10; k++) s[k] = 0;
+    const int n = h << lgw, wm = (1 << lgw) - 1;
+    for (int i = t; i < n; i += nt) {
+        const int y = i >> lgw, x = i & wm;
+        const unsigned cv = c[(long long)y * cp + x];
+        const xg_pix *r = ctr + (long long)y * rp + x;
+#pragma unroll
+        for (int k = 0; k < 9; k++) s[k] = __usad(cv, (unsigned)r[(k / 3 - 1) * rp + (k % 3 - 1)], s[k]);
+        if (EXTRA) s[9] = __usad(cv, (unsigned)ext[(long long)y * rp + x], s[9]);
+    }
+}
+
 __global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(XgHierFrameParams p, const XgPicParams *pp)
 {
     extern __shared__ __align__(16) xg_pix hs[];
     __shared__ unsigned long long wmin[8];
+    __shared__ uint32_t wsum[8][10];
     const int S = p.level_size[blockIdx.z];
+    const int lgS = S == 64 ? 6 : S == 32 ? 5 : S == 16 ? 4 : 3;
     unsigned long long *keys = p.keys[blockIdx.z];
     const int cus_x = p.cus_x[blockIdx.z];
-    const int R = p.R, R4 = R >> 2, WS = 16 + 2 * R4;          /* staged window side */
+    const int R = p.R, R4 = R >> 2, WS = 16 + 2 * R4, WP = WS + 4;   /* window side, row pitch */
     const int tx0 = blockIdx.x * 64, ty0 = blockIdx.y * 64;
-    xg_pix *win = hs, *cur4 = hs + WS * WS;                    /* [WS][WS], [16][16] */
+    xg_pix *win = hs, *cur4 = hs + WS * WP;                  /* [WS][WP], [16][16] */
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t lambda = pp->lambda;
     {
         const xg_pix *src = p.ref_lo[1].data + (long long)(ty0 / 4 - R4) * p.ref_lo[1].pitch + (tx0 / 4 - R4);
-        for (int i = tid; i < WS * WS; i += XG_HIER_THREADS) {
-            const int y = i / WS, x = i - y * WS;
-            win[i] = src[(long long)y * p.ref_lo[1].pitch + x];
+        for (int i = tid; i < WS * WP; i += XG_HIER_THREADS) {
+            const int y = i / WP, x = i - y * WP;
+            /* the four columns past the window feed only candidates beyond it */
+            win[i] = x < WS ? src[(long long)y * p.ref_lo[1].pitch + x] : (xg_pix)0;
         }
         const xg_pix *cs = p.cur_lo[1].data + (long long)(ty0 / 4) * p.cur_lo[1].pitch + tx0 / 4;
         for (int i = tid; i < 256; i += XG_HIER_THREADS) cur4[i] = cs[(long long)(i >> 4) * p.cur_lo[1].pitch + (i & 15)];
     }
     __syncthreads();
-    const int per_row = 64 / S, ncu = per_row * per_row;
+    const int per_row = 64 >> lgS, ncu = per_row * per_row;
     const int G = ncu >= 8 ? 1 : 8 / ncu;                     /* warps per CU */
     const int slots = 8 / G;                                  /* CUs in flight */
     const int b4 = S >> 2;
+    const int grp = warp / G, gw = warp % G, gt = gw * 32 + lane, gn = 32 * G;   /* group, rank, thread in group */
+    /* sums over the group of ten values per thread (every lane gets them) */
+    auto gsum10 = [&](uint32_t v[10]) {
+#pragma unroll
+        for (int k = 0; k < 10; k++) v[k] = xg_warp_sum(v[k]);
+        if (G == 1) return;
+        if (lane < 10) {
+#pragma unroll
+            for (int k = 0; k < 10; k++) if (lane == k) wsum[warp][k] = v[k];
+        }
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(gn) : "memory");
+#pragma unroll
+        for (int k = 0; k < 10; k++) {
+            uint32_t t = 0;
+            for (int j = 0; j < G; j++) t += wsum[grp * G + j][k];
+            v[k] = t;
+        }
+        asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(gn) : "memory");
+    };
     for (int c0 = 0; c0 < ncu; c0 += slots) {
-        const int c = c0 + warp / G, gw = warp % G;           /* this warp's CU and rank within its group */
+        const int c = c0 + grp;
         const int cxi = (c % per_row) * S, cyi = (c / per_row) * S;
         const int cu_x = tx0 + cxi, cu_y = ty0 + cyi;
-        const bool live = c < ncu && cu_x + S <= p.W && cu_y + S <= p.H;
+        const bool live = cu_x + S <= p.W && cu_y + S <= p.H;   /* uniform over the group */
+        if (!live) continue;
         /* window (h266_enc_init.c:1462) within +-R */
         const int mnx = (int16_t)(-cu_x - p.ctu - 8), mny = (int16_t)(-cu_y - p.ctu - 8);
         const int mxx = (int16_t)(p.W + (p.ctu - S + 8) - cu_x), mxy = (int16_t)(p.H + (p.ctu - S + 8) - cu_y);
         const int lox = max(-R, mnx), hix = min(R, mxx), loy = max(-R, mny), hiy = min(R, mxy);
-        /* 1/4: exhaustive over the level window */
+        /* ---- 1/4: exhaustive over the level window, four adjacent candidates a lane */
         const int lx4 = xg_ceil_shr(lox, 2), hx4 = hix >> 2, ly4 = xg_ceil_shr(loy, 2), hy4 = hiy >> 2;
         const int nx4 = hx4 - lx4 + 1, ny4 = hy4 - ly4 + 1;
         unsigned long long k = ~0ull;
-        if (live && nx4 > 0 && ny4 > 0) {
+        if (nx4 > 0 && ny4 > 0) {
+            const int qpr = (nx4 + 3) >> 2, nq = qpr * ny4;      /* quads per row, quads */
             const xg_pix *cb = cur4 + (cyi >> 2) * 16 + (cxi >> 2);
-            const xg_pix *wb = win + ((cyi >> 2) + R4 + ly4) * WS + (cxi >> 2) + R4 + lx4;
-            for (int i = gw * 32 + lane; i < nx4 * ny4; i += 32 * G) {
-                const int y = i / nx4, x = i - y * nx4;
-                const xg_pix *r = wb + y * WS + x;
-                uint32_t s = 0;
-                for (int yy = 0; yy < b4; yy++)
-                    for (int xx = 0; xx < b4; xx++) s += (uint32_t)abs((int)cb[yy * 16 + xx] - (int)r[yy * WS + xx]);
-                const unsigned long long kk = ((unsigned long long)s << 32) | (uint32_t)i;
-                k = kk < k ? kk : k;
+            const xg_pix *wb = win + ((cyi >> 2) + R4 + ly4) * WP + (cxi >> 2) + R4 + lx4;
+            int qy = gt / qpr, qx = gt - qy * qpr;              /* this lane's first quad */
+            const int sy = gn / qpr, sx = gn - sy * qpr;        /* its step */
+            for (int q = gt; q < nq; q += gn) {
+                const xg_pix *r = wb + qy * WP + 4 * qx;
+                uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                for (int yy = 0; yy < b4; yy++) {
+                    const xg_pix *cr = cb + yy * 16, *rr = r + yy * WP;
+                    unsigned w0 = rr[0], w1 = rr[1], w2 = rr[2];
+                    for (int j = 0; j < b4; j++) {
+                        const unsigned w3 = rr[j + 3], cv = cr[j];
+                        s0 = __usad(cv, w0, s0); s1 = __usad(cv, w1, s1); s2 = __usad(cv, w2, s2); s3 = __usad(cv, w3, s3);
+                        w0 = w1; w1 = w2; w2 = w3;
+                    }
+                }
+                const int x0 = 4 * qx, i0 = qy * nx4 + x0;
+                const uint32_t sv[4] = { s0, s1, s2, s3 };
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    if (x0 + u < nx4) {
+                        const unsigned long long kk = ((unsigned long long)sv[u] << 32) | (uint32_t)(i0 + u);
+                        k = kk < k ? kk : k;
+                    }
+                qx += sx; qy += sy;
+                if (qx >= qpr) { qx -= qpr; qy++; }
             }
         }
         k = xg_warp_min64(k);
         if (G > 1) {
             if (lane == 0) wmin[warp] = k;
-            __syncthreads();
-            for (int j = 0; j < G; j++) { const unsigned long long v = wmin[(warp / G) * G + j]; k = v < k ? v : k; }
-            __syncthreads();
+            asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(gn) : "memory");
+            for (int j = 0; j < G; j++) { const unsigned long long v = wmin[grp * G + j]; k = v < k ? v : k; }
+            asm volatile("bar.sync %0, %1;" ::"r"(1 + grp), "r"(gn) : "memory");
         }
-        if (!live || gw != 0) continue;
         int b2x = 0, b2y = 0;
-        if (nx4 > 0 && ny4 > 0) { const int i = (int)(uint32_t)k; b2x = lx4 + i % nx4; b2y = ly4 + i / nx4; }
-        /* 1/2: +-1 around 2 * b2 */
+        if (nx4 > 0 && ny4 > 0) { const int i = (int)(uint32_t)k; b2y = i / nx4; b2x = lx4 + (i - b2y * nx4); b2y += ly4; }
+        /* ---- 1/2: +-1 around 2 * b2 (the nine SADs in one pass; candidates
+         * outside the level window are computed and passed over: the planes'
+         * margins hold them) */
         int b1x = 0, b1y = 0;
         {
             const int l1x = xg_ceil_shr(lox, 1), h1x = hix >> 1, l1y = xg_ceil_shr(loy, 1), h1y = hiy >> 1;
-            const int lx = max(2 * b2x - 1, l1x), hx = min(2 * b2x + 1, h1x), ly = max(2 * b2y - 1, l1y), hy = min(2 * b2y + 1, h1y);
-            const int b2 = S >> 1;
             const long long cpl = p.cur_lo[0].pitch, rpl = p.ref_lo[0].pitch;
             const xg_pix *cb = p.cur_lo[0].data + (long long)(cu_y >> 1) * cpl + (cu_x >> 1);
+            const xg_pix *rc = p.ref_lo[0].data + (long long)((cu_y >> 1) + 2 * b2y) * rpl + (cu_x >> 1) + 2 * b2x;
+            uint32_t sv[10];
+            xg_sad_3x3<false>(cb, cpl, rc, rc, rpl, lgS - 1, S >> 1, gt, gn, sv);
+            gsum10(sv);
             uint32_t bs = 0xFFFFFFFFu;
-            for (int y = ly; y <= hy; y++)
-                for (int x = lx; x <= hx; x++) {
-                    const xg_pix *r = p.ref_lo[0].data + (long long)((cu_y >> 1) + y) * rpl + (cu_x >> 1) + x;
-                    const uint32_t s = xg_warp_sum(xg_sad_part(cb, cpl, r, rpl, b2, b2, lane, 32));
-                    if (s < bs) { bs = s; b1x = x; b1y = y; }
-                }
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                const int x = 2 * b2x + k % 3 - 1, y = 2 * b2y + k / 3 - 1;
+                if (x < l1x || x > h1x || y < l1y || y > h1y) continue;
+                if (sv[k] < bs) { bs = sv[k]; b1x = x; b1y = y; }
+            }
         }
-        /* full resolution: the zero MV (the frame form's predictor and first
-         * candidate), then 3 x 3 around 2 * b1 */
+        /* ---- full resolution: the zero MV (the frame form's predictor and first
+         * candidate), then 3 x 3 around 2 * b1, in one pass */
         const long long cp = p.cur.pitch, rp = p.ref.pitch;
         const xg_pix *cb = p.cur.data + (long long)cu_y * cp + cu_x;
         const xg_pix *rb = p.ref.data + (long long)cu_y * rp + cu_x;
-        uint32_t best = 0xFFFFFFFFu;
+        uint32_t sv[10];
+        xg_sad_3x3<true>(cb, cp, rb + (long long)(2 * b1y) * rp + 2 * b1x, rb, rp, lgS, S, gt, gn, sv);
+        gsum10(sv);
+        uint32_t best = (sv[9] << XG_COST_FRACTION) + 2 * xg_mvd_bits(0) * lambda;
         int bx = 0, by = 0;
-        {
-            const uint32_t s = xg_warp_sum(xg_sad_part(cb, cp, rb, rp, S, S, lane, 32));
-            best = (s << XG_COST_FRACTION) + 2 * xg_mvd_bits(0) * lambda;
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const int x = 2 * b1x + k % 3 - 1, y = 2 * b1y + k / 3 - 1;
+            if (x < lox || x > hix || y < loy || y > hiy) continue;
+            const uint32_t cst = xg_full_cost(sv[k], 4 * x, 4 * y, 0, 0, lambda);
+            if (cst < best) { best = cst; bx = x; by = y; }
         }
-        for (int y = 2 * b1y - 1; y <= 2 * b1y + 1; y++)
-            for (int x = 2 * b1x - 1; x <= 2 * b1x + 1; x++) {
-                if (x < lox || x > hix || y < loy || y > hiy) continue;
-                const uint32_t s = xg_warp_sum(xg_sad_part(cb, cp, rb + (long long)y * rp + x, rp, S, S, lane, 32));
-                const uint32_t cst = xg_full_cost(s, 4 * x, 4 * y, 0, 0, lambda);
-                if (cst < best) { best = cst; bx = x; by = y; }
-            }
-        if (lane == 0)
-            keys[(cu_y / S) * cus_x + cu_x / S] = ((unsigned long long)best << 32) | (uint32_t)((by + R) * (2 * R + 1) + bx + R);
+        if (gt == 0)
+            keys[(cu_y >> lgS) * cus_x + (cu_x >> lgS)] = ((unsigned long long)best << 32) | (uint32_t)((by + R) * (2 * R + 1) + bx + R);
     }
 }
 
@@ -397,5 +464,5 @@ __global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(XgHierFrameParam
 static size_t xg_hier_smem(int R)
 {
     const int ws = 16 + 2 * (R >> 2);
-    return (size_t)(ws * ws + 256) * sizeof(xg_pix);
+    return (size_t)(ws * (ws + 4) + 256) * sizeof(xg_pix);
 }

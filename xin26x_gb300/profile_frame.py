@@ -4,6 +4,7 @@ times -- the program for profiling (ncu) and quick timing of the kernels.
     python -m xin26x_gb300.profile_frame [--frames 6] [--width 1920] [--height 1080]
                                          [--search 64] [--bitdepth 8] [--ctu 64]
                                          [--objects 4] [--octaves 1] [--input-bitdepth 0]
+                                         [--search-mode 0]
 
 --bitdepth 10 --input-bitdepth 8: 8-bit pictures coded by the 10-bit library.
 """
@@ -30,6 +31,7 @@ def main():
     ap.add_argument("--objects", type=int, default=4)
     ap.add_argument("--octaves", type=int, default=1)
     ap.add_argument("--input-bitdepth", type=int, default=0)
+    ap.add_argument("--search-mode", type=int, default=0, help="0 exhaustive, 1 by resolution levels")
     a = ap.parse_args()
     import torch
     lib = _lib.load(a.bitdepth)
@@ -38,7 +40,7 @@ def main():
                          objects=a.objects, octaves=a.octaves)
     dev = [tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f) for f in seq]
     mask = sum(int(s) for s in a.levels.split(","))
-    cfg = _lib.xin_gpu_stream_cfg(a.width, a.height, a.ctu, a.search, mask, 0, 1, 1, a.input_bitdepth)
+    cfg = _lib.xin_gpu_stream_cfg(a.width, a.height, a.ctu, a.search, mask, 0, 1, 1, a.input_bitdepth, a.search_mode)
     h = C.c_void_p()
     if lib.xin_gpu_stream_open(C.byref(cfg), C.byref(h)) != 0:
         raise RuntimeError(lib.xin_gpu_last_error().decode())
@@ -59,7 +61,8 @@ def main():
             stages.append(list(st) + [res.gpu_ms])
     lib.xin_gpu_stream_close(h)
     s = np.array(stages)
-    print(json.dumps({"frames": a.frames, "size": [a.width, a.height], "search": a.search, "bitdepth": a.bitdepth,
+    print(json.dumps({"frames": a.frames, "size": [a.width, a.height], "search": a.search, "search_mode": a.search_mode,
+                      "bitdepth": a.bitdepth,
                       "input_bitdepth": a.input_bitdepth or a.bitdepth,
                       "ctu": a.ctu, "mpix_s": a.width * a.height / float(np.median(s[:, 4])) / 1e3,
                       "ms": {"prep": float(np.median(s[:, 0])), "integer_search": float(np.median(s[:, 1])),
