@@ -379,6 +379,42 @@ void XinGpuMotionSearchHier(XG_PIXEL *input, intptr_t inputStride, XG_PIXEL *ref
                             int32_t maxMvX, int32_t minMvY, int32_t maxMvY, uint32_t width, uint32_t height, void *bestMv);
 void XinGpuMotionEstHier(struct xin_me_struct *meSet);
 
+/* ------------------------------------------------------------------- DMVR
+ * The encoder's emulation of the H.266 decoder-side MV refinement of a
+ * bi-predicted CU (Xin266LumaMotionCompDmvr with Xin266DeriveMvFromDmvr and
+ * Xin266SubPelRefineDmvr, h266_encoder/source/h266_inter_prediction.c:864-1420),
+ * and the table entries it calls.
+ *
+ * XinGpuLumaMotionCompDmvr: the arguments of Xin266LumaMotionCompDmvr unpacked
+ *   from the section state: ref0 / ref1 are the L0 / L1 reference pictures
+ *   (pointers at picture (0, 0) inside their padding, pictureRead[list][refIdx]
+ *   ->refBuf[PLANE_LUMA]), (cuX, cuY) the CU position, [minMv, maxMv] the CU's
+ *   window (secSet->minMv / maxMv, full-pel), mv the L0 and L1 MVs (1/16 pel, x, y
+ *   pairs).  Per 16 x 16 sub-block (raster order): bilinear predictions of both
+ *   lists, the 5 x 5 integer search on row-subsampled SADs (L0 moved by +d, L1
+ *   by -d), the parabolic sub-pel offset; then the refined 8-tap bi-prediction.
+ *   Writes pred (width x height) and mvdL0SubPu (x, y pairs of 1/16-pel L0
+ *   refinements, one per sub-block; xin_mv_s).  width, height: powers of two
+ *   8..128.
+ * XinGpuComputeSadS16: pfXinComputeSadS16 (typedef XinComputeDistS16,
+ *   h266_func_struct.h:540; the closed Xin26xComputeSadS16, restated): the SAD of
+ *   int16 blocks over every (1 << subShift)-th row, times 1 << subShift.
+ * XinGpuCopyAndPad / XinGpuCopyAndPadUv: pfXinCopyAndPad / pfXinCopyAndPadUv
+ *   (typedefs XinCopyAndPad / XinCopyAndPadUv, h266_func_struct.h:604,612;
+ *   h266_encoder/source/h266_copy_and_pad.c:32-112): the region an 8-tap (4-tap)
+ *   filter reads around a w x h block, padded by 2 (1) samples on every side by
+ *   repeating its edge (the closed Xin26xBlockPad2/1, restated). */
+void XinGpuLumaMotionCompDmvr(const XG_PIXEL *ref0, const XG_PIXEL *ref1, intptr_t refStride, int32_t cuX, int32_t cuY,
+                              int32_t minMvX, int32_t minMvY, int32_t maxMvX, int32_t maxMvY, uint32_t width,
+                              uint32_t height, const int32_t mv[4], int32_t useAltHpelIf, XG_PIXEL *pred,
+                              intptr_t predStride, int16_t *mvdL0SubPu);
+void XinGpuComputeSadS16(int16_t *input, intptr_t inputStride, int16_t *pred, intptr_t predStride, uint32_t width,
+                         uint32_t height, uint32_t subShift, uint32_t *sad);
+void XinGpuCopyAndPad(XG_PIXEL *ref, intptr_t refStride, XG_PIXEL *pad, intptr_t padStride, uint32_t width,
+                      uint32_t height);
+void XinGpuCopyAndPadUv(XG_PIXEL *refU, XG_PIXEL *refV, intptr_t refStride, XG_PIXEL *padU, XG_PIXEL *padV,
+                        intptr_t padStride, uint32_t width, uint32_t height);
+
 /* ------------------------------------------------------------- frame form
  * One stream = one sequence.  Pictures are submitted in coding order; each
  * picture after the first uses the previously submitted picture as its

@@ -143,6 +143,12 @@ _SIGS = {
                                               C.POINTER(i32)]),
     "me_hier": ("orc_me_hier", None, [C.POINTER(orc_hier_in), u32, u32, i32, i32, i32, i32, u32, i32, i32, i32, i32,
                                       C.POINTER(orc_me_io)]),
+    "sad_s16": ("orc_sad_s16", None, [vp, ip, vp, ip, u32, u32, u32, vp]),
+    "block_pad": ("orc_block_pad", None, [vp, ip, u32, u32, u32, u32]),
+    "copy_and_pad": ("orc_copy_and_pad", "ref_copy_and_pad", [vp, ip, vp, ip, u32, u32]),
+    "copy_and_pad_uv": ("orc_copy_and_pad_uv", "ref_copy_and_pad_uv", [vp, vp, ip, vp, vp, ip, u32, u32]),
+    "dmvr_luma": ("orc_dmvr_luma", "ref_dmvr_luma", [vp, vp, ip, i32, i32, i32, i32, i32, i32, u32, u32, vp, C.c_int,
+                                                     vp, vp, ip]),
     "cu_hotpath": ("orc_cu_hotpath", None, [C.POINTER(orc_frame_desc), i32, i32, i32, vp * 3, ip * 2, vp * 3, ip * 2,
                                             C.POINTER(orc_cu_out)]),
     "tr_matrix": ("orc_tr_matrix", None, [C.c_int, C.c_int]),

@@ -39,6 +39,7 @@
 #include "h266_sub_dct.h"
 #include "h266_idct_add.h"
 #include "h266_trans_recon.h"
+#include "h266_inter_pred_context.h"
 
 void shim_fill_table(xin_func_struct *fs);
 extern const UINT32 calcLog2[256];
@@ -293,4 +294,47 @@ void ref_chroma_motion_comp(PIXEL *ref_u0, PIXEL *ref_v0, PIXEL *ref_u1, PIXEL *
     ri[0] = (SINT8)ref_idx0; ri[1] = (SINT8)ref_idx1;
     Xin266ChromaMotionComp(&hs->sec, (SINT32)w, (SINT32)h, pred_u, pred_v, ps, mv, ri, (UINT8)bcw_idx);
     free(hs);
+}
+
+/* ---- DMVR ----------------------------------------------------------------
+ * Xin266LumaMotionCompDmvr (h266_encoder/source/h266_inter_prediction.c:1178),
+ * which runs Xin266DeriveMvFromDmvr (:975), called unmodified on a picture set
+ * whose lists hold ref0 / ref1 (picture origins, stride rs); writes the
+ * sub-block refinements (x, y pairs, 1/16 pel) and the refined prediction. */
+void Xin266LumaMotionCompDmvr(xin_sec_struct *, xin_pu_struct *, PIXEL *, intptr_t, xin_mv32_u *, SINT8 *, xin_mv_s *, BOOL);
+void Xin266CopyAndPad(PIXEL *, intptr_t, PIXEL *, intptr_t, UINT32, UINT32);
+void Xin266CopyAndPadUv(PIXEL *, PIXEL *, intptr_t, PIXEL *, PIXEL *, intptr_t, UINT32, UINT32);
+
+void ref_dmvr_luma(PIXEL *ref0, PIXEL *ref1, intptr_t rs, SINT32 cu_x, SINT32 cu_y, SINT32 min_mvx, SINT32 min_mvy,
+                   SINT32 max_mvx, SINT32 max_mvy, UINT32 w, UINT32 h, const SINT32 *mv16, BOOL alt_hpel, SINT16 *mvd,
+                   PIXEL *pred, intptr_t ps)
+{
+    xin_cu_struct cu; xin_pu_struct pu; xin_ref_picture rp0, rp1; xin_mv32_u mv[2]; SINT8 ri[2] = { 0, 0 };
+    xin_mv_s sub[64];
+    harness *hs = mc_harness(cu_x, cu_y, min_mvx, min_mvy, max_mvx, max_mvy, &cu);
+    /* the derivation's two bilinear buffers of BILI_BUF_STRIDE^2 samples */
+    SINT16 *tmp = (SINT16 *)calloc(2 * BILI_BUF_STRIDE * BILI_BUF_STRIDE, sizeof(SINT16));
+    hs->sec.tempBuffer = (UINT8 *)tmp;
+    memset(&pu, 0, sizeof pu); memset(&rp0, 0, sizeof rp0); memset(&rp1, 0, sizeof rp1);
+    pu.width = (UINT8)w; pu.height = (UINT8)h; pu.lgWidth = (UINT8)calcLog2[w]; pu.lgHeight = (UINT8)calcLog2[h];
+    rp0.refBuf[PLANE_LUMA] = ref0; rp0.refStride[PLANE_LUMA] = rs;
+    rp1.refBuf[PLANE_LUMA] = ref1; rp1.refStride[PLANE_LUMA] = rs;
+    hs->pic.pictureRead[XIN_LIST_0][0] = &rp0;
+    hs->pic.pictureRead[XIN_LIST_1][0] = &rp1;
+    mv[0].mv.mv32X = mv16[0]; mv[0].mv.mv32Y = mv16[1]; mv[1].mv.mv32X = mv16[2]; mv[1].mv.mv32Y = mv16[3];
+    Xin266LumaMotionCompDmvr(&hs->sec, &pu, pred, ps, mv, ri, sub, alt_hpel);
+    UINT32 n = ((w + 15) / 16) * ((h + 15) / 16);
+    for (UINT32 i = 0; i < n; i++) { mvd[2 * i] = sub[i].mvX; mvd[2 * i + 1] = sub[i].mvY; }
+    free(tmp);
+    free(hs);
+}
+
+void ref_copy_and_pad(PIXEL *ref, intptr_t rs, PIXEL *pad, intptr_t ps, UINT32 w, UINT32 h)
+{
+    Xin266CopyAndPad(ref, rs, pad, ps, w, h);
+}
+
+void ref_copy_and_pad_uv(PIXEL *ref_u, PIXEL *ref_v, intptr_t rs, PIXEL *pad_u, PIXEL *pad_v, intptr_t ps, UINT32 w, UINT32 h)
+{
+    Xin266CopyAndPadUv(ref_u, ref_v, rs, pad_u, pad_v, ps, w, h);
 }

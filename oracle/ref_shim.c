@@ -87,6 +87,16 @@ void Xin266InterpCopyU8S16(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, 
 void Xin266ChromaInterpHorU8S16(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32, UINT32);
 void Xin266ChromaInterpVetU8S16(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32, UINT32);
 void Xin266ChromaInterpHorVetU8S16(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266LumaInterpHorU8S16(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266LumaInterpVetU8S16(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266LumaInterpHorVetU8S16(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32, UINT32);
+void Xin266BiliInterpCopy(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32);
+void Xin266BiliInterpHor(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32);
+void Xin266BiliInterpVet(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32);
+void Xin266BiliInterpHorVet(const PIXEL *, intptr_t, SINT16 *, intptr_t, SINT32, UINT32, UINT32);
+void Xin266CopyAndPad(PIXEL *, intptr_t, PIXEL *, intptr_t, UINT32, UINT32);
+void Xin26xComputeSadS16(SINT16 *, intptr_t, SINT16 *, intptr_t, UINT32, UINT32, UINT32, UINT32 *);
+void Xin266CopyAndPadUv(PIXEL *, PIXEL *, intptr_t, PIXEL *, PIXEL *, intptr_t, UINT32, UINT32);
 void Xin266InterpAvgS16U8(const SINT16 *, intptr_t, const SINT16 *, intptr_t, PIXEL *, intptr_t, UINT32, UINT32);
 void Xin266InterpWeightS16U8(const SINT16 *, intptr_t, const SINT16 *, intptr_t, PIXEL *, intptr_t, UINT32, UINT32,
                              SINT32, SINT32);
@@ -122,6 +132,16 @@ void shim_fill_table(xin_func_struct *fs)
         fs->pfXinChromaInterpS16[0][1][lg] = Xin266ChromaInterpVetU8S16;
         fs->pfXinChromaInterpS16[1][1][lg] = Xin266ChromaInterpHorVetU8S16;
         fs->pfXinInterpAvg[lg] = Xin266InterpAvgS16U8;
+        /* DMVR entries (h266_func_init.c:118-125,460-530,645-646) */
+        fs->pfXinLumaInterpS16[0][0][lg] = Xin266InterpCopyU8S16;
+        fs->pfXinLumaInterpS16[1][0][lg] = Xin266LumaInterpHorU8S16;
+        fs->pfXinLumaInterpS16[0][1][lg] = Xin266LumaInterpVetU8S16;
+        fs->pfXinLumaInterpS16[1][1][lg] = Xin266LumaInterpHorVetU8S16;
+        fs->pfXinBiliInterp[0][0][lg] = Xin266BiliInterpCopy;
+        fs->pfXinBiliInterp[1][0][lg] = Xin266BiliInterpHor;
+        fs->pfXinBiliInterp[0][1][lg] = Xin266BiliInterpVet;
+        fs->pfXinBiliInterp[1][1][lg] = Xin266BiliInterpHorVet;
+        fs->pfXinComputeSadS16[lg] = Xin26xComputeSadS16;
         fs->pfXinInterpWeight[lg] = Xin266InterpWeightS16U8;
         fs->pfXinBlockSubForDct[lg] = shim_sub;
         fs->pfXinBlockAddForDct[lg] = shim_add;
@@ -138,6 +158,8 @@ void shim_fill_table(xin_func_struct *fs)
         }
     }
     fs->pfXinPreRdoq = Xin266PreRdoq;
+    fs->pfXinCopyAndPad = Xin266CopyAndPad;
+    fs->pfXinCopyAndPadUv = Xin266CopyAndPadUv;
 }
 
 /* 8-argument form declared at h266_encoder/include/h266_inter_prediction.h:43 */
@@ -147,6 +169,14 @@ void Xin266LumaInterpolation(xin_func_struct *fs, const PIXEL *src, intptr_t ss,
     SINT32 fx = frac & XIN_MV_FRAC_MASK, fy = (frac >> XIN_MV_FRAC_BITS) & XIN_MV_FRAC_MASK;
     fs->pfXinLumaInterp[!!fx][!!fy][lgw](src, ss, dst, ds, frac, 1u << lgw, h, 0);
 }
+
+/* closed DMVR helpers (h26x_core/include/h26x_compute_dist.h:942,
+ * h26x_block_utility.h:23,335,343) -> oracle */
+void Xin26xComputeSadS16(SINT16 *a, intptr_t as, SINT16 *b, intptr_t bs, UINT32 w, UINT32 h, UINT32 sub, UINT32 *sad)
+{ orc_sad_s16(a, as, b, bs, w, h, sub, sad); }
+void Xin26xBlockCopy(PIXEL *src, intptr_t ss, PIXEL *dst, intptr_t ds, UINT32 w, UINT32 h) { orc_block_copy(src, ss, dst, ds, w, h); }
+void Xin26xBlockPad1(PIXEL *buf, intptr_t bs, UINT32 w, UINT32 h, UINT32 pw, UINT32 ph) { orc_block_pad(buf, bs, w, h, pw, ph); }
+void Xin26xBlockPad2(PIXEL *buf, intptr_t bs, UINT32 w, UINT32 h, UINT32 pw, UINT32 ph) { orc_block_pad(buf, bs, w, h, pw, ph); }
 
 /* affine MV rounding (h266_encoder/source/h266_get_neighbour_mv.c:1380), referenced by the
  * affine branch of h266_inter_prediction.c; no harness reaches that branch */

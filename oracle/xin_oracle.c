@@ -956,6 +956,183 @@ void orc_me_hier(const orc_hier_in *hi, uint32_t w, uint32_t h, int32_t mvpx, in
     io->best_cost = best; io->best_sad = bsad; io->best_mvx = bx; io->best_mvy = by;
 }
 
+/* ---- DMVR ------------------------------------------------------------
+ * The encoder's emulation of the H.266 decoder-side MV refinement:
+ * Xin266DeriveMvFromDmvr + Xin266SubPelRefineDmvr and Xin266LumaMotionCompDmvr
+ * (open, h266_encoder/source/h266_inter_prediction.c:864-1420) and
+ * Xin266CopyAndPad / Xin266CopyAndPadUv (open, h266_copy_and_pad.c:32-112).
+ * Their closed helpers are restated: Xin26xComputeSadS16
+ * (h26x_core/include/h26x_compute_dist.h:942), Xin26xBlockCopy and
+ * Xin26xBlockPad1/2 (h26x_core/include/h26x_block_utility.h:23,335,343). */
+
+/* SAD over every (1 << sub)-th row, scaled back by 1 << sub (the row-subsampled
+ * distortion of the standard's DMVR).  Restated; unpinned. */
+void orc_sad_s16(const int16_t *a, intptr_t as, const int16_t *b, intptr_t bs, uint32_t w, uint32_t h, uint32_t sub,
+                 uint32_t *sad)
+{
+    uint32_t s = 0;
+    for (uint32_t y = 0; y < h; y += 1u << sub)
+        for (uint32_t x = 0; x < w; x++) {
+            int d = a[(intptr_t)y * as + x] - b[(intptr_t)y * bs + x];
+            s += (uint32_t)(d < 0 ? -d : d);
+        }
+    *sad = s << sub;
+}
+
+void orc_block_copy(const opix *src, intptr_t ss, opix *dst, intptr_t ds, uint32_t w, uint32_t h)
+{
+    for (uint32_t y = 0; y < h; y++) memcpy(dst + (intptr_t)y * ds, src + (intptr_t)y * ss, w * sizeof(opix));
+}
+
+/* extend the w x h block outward by pw columns and ph rows, repeating its edge
+ * samples (the standard's DMVR reference padding).  Restated; unpinned. */
+void orc_block_pad(opix *buf, intptr_t bs, uint32_t w, uint32_t h, uint32_t pw, uint32_t ph)
+{
+    for (uint32_t y = 0; y < h; y++) {
+        opix *row = buf + (intptr_t)y * bs;
+        for (uint32_t i = 1; i <= pw; i++) { row[-(intptr_t)i] = row[0]; row[w - 1 + i] = row[w - 1]; }
+    }
+    for (uint32_t i = 1; i <= ph; i++) {
+        memcpy(buf - (intptr_t)i * bs - pw, buf - pw, (w + 2 * pw) * sizeof(opix));
+        memcpy(buf + (intptr_t)(h - 1 + i) * bs - pw, buf + (intptr_t)(h - 1) * bs - pw, (w + 2 * pw) * sizeof(opix));
+    }
+}
+
+/* h266_copy_and_pad.c:32-57: the (w + 7) x (h + 7) luma region the 8-tap filter
+ * reads, padded by 2 (DMVR_NUM_ITERATION) on every side */
+void orc_copy_and_pad(const opix *ref, intptr_t rs, opix *pad, intptr_t ps, uint32_t w, uint32_t h)
+{
+    orc_block_copy(ref - 3 * rs - 3, rs, pad - 3 * ps - 3, ps, w + 7, h + 7);
+    orc_block_pad(pad - 3 * ps - 3, ps, w + 7, h + 7, 2, 2);
+}
+
+/* h266_copy_and_pad.c:59-112: the (w + 3) x (h + 3) chroma regions of the 4-tap
+ * filter, padded by 1 */
+void orc_copy_and_pad_uv(const opix *ref_u, const opix *ref_v, intptr_t rs, opix *pad_u, opix *pad_v, intptr_t ps,
+                         uint32_t w, uint32_t h)
+{
+    orc_block_copy(ref_u - rs - 1, rs, pad_u - ps - 1, ps, w + 3, h + 3);
+    orc_block_copy(ref_v - rs - 1, rs, pad_v - ps - 1, ps, w + 3, h + 3);
+    orc_block_pad(pad_u - ps - 1, ps, w + 3, h + 3, 1, 1);
+    orc_block_pad(pad_v - ps - 1, ps, w + 3, h + 3, 1, 1);
+}
+
+/* Xin266DivForMaxQ7 (:864-907): |n| / d in eighths as three quotient bits (4, 2, 1), sign of n */
+static int32_t dmvr_div8(int64_t n, int64_t d)
+{
+    const int neg = n < 0;
+    if (neg) n = -n;
+    int32_t q = 0;
+    for (int b = 2; b >= 0; b--) {
+        const int64_t step = d << (b + 1);
+        if (n >= step) { n -= step; q |= 1 << b; }
+    }
+    return neg ? -q : q;
+}
+
+/* Xin266SubPelErrorSrfc + Xin266SubPelRefineDmvr (:909-973): the parabolic
+ * sub-pel offset from the costs around the best integer position */
+static void dmvr_subpel(int non0, int32_t del[2], const uint32_t *c, int cs)
+{
+    if (!non0 || del[0] == 32 || del[0] == -32 || del[1] == 32 || del[1] == -32) return;
+    const int64_t c0 = c[0];
+    const int64_t nb[2][2] = { { c[-1], c[1] }, { c[-cs], c[cs] } };   /* (before, after) per direction */
+    for (int hv = 0; hv < 2; hv++) {
+        const int64_t num = (nb[hv][0] - nb[hv][1]) * 16, den = nb[hv][0] + nb[hv][1] - 2 * c0;
+        if (den == 0) continue;
+        if (nb[hv][0] != c0 && nb[hv][1] != c0) del[hv] += dmvr_div8(num, den);
+        else del[hv] += nb[hv][0] == c0 ? -8 : 8;
+    }
+}
+
+static void dmvr_luma_s16(const opix *src, intptr_t ss, int16_t *dst, intptr_t ds, int32_t frac, uint32_t w, uint32_t h,
+                          uint32_t fi)
+{
+    const int fx = frac & 15, fy = frac >> 4;
+    if (!fx && !fy) orc_interp_copy_s16(src, ss, dst, ds, frac, w, h, fi);
+    else if (fx && !fy) orc_luma_hor_s16(src, ss, dst, ds, frac, w, h, fi);
+    else if (!fx && fy) orc_luma_vet_s16(src, ss, dst, ds, frac, w, h, fi);
+    else orc_luma_hv_s16(src, ss, dst, ds, frac, w, h, fi);
+}
+
+void orc_dmvr_luma(const opix *ref0, const opix *ref1, intptr_t rs, int32_t cu_x, int32_t cu_y, int32_t min_mvx,
+                   int32_t min_mvy, int32_t max_mvx, int32_t max_mvy, uint32_t w, uint32_t h, const int32_t mv16[4],
+                   int alt_hpel, int16_t *mvd, opix *pred, intptr_t ps)
+{
+    enum { BS = 256, CS = 5 };                               /* bilinear buffer stride; cost grid side */
+    const uint32_t sw = w < 16 ? w : 16, sh = h < 16 ? h : 16;
+    const opix *refs[2] = { ref0, ref1 };
+    int16_t *bil = (int16_t *)malloc(sizeof(int16_t) * 2 * BS * BS);
+    int32_t base[2][2];                                      /* clipped MVs, 1/16 */
+    /* bilinear predictions of both lists over (w + 4) x (h + 4), from 2 samples up and left (:1037-1085) */
+    for (int l = 0; l < 2; l++) {
+        base[l][0] = CLIP3(min_mvx * 16, max_mvx * 16, mv16[2 * l]);
+        base[l][1] = CLIP3(min_mvy * 16, max_mvy * 16, mv16[2 * l + 1]);
+        const int32_t ox = cu_x * 16 + base[l][0] - 32, oy = cu_y * 16 + base[l][1] - 32;
+        const int32_t fx = ox & 15, fy = oy & 15;
+        orc_bili_interp((fx ? 1 : 0) | (fy ? 2 : 0), refs[l] + (intptr_t)(oy >> 4) * rs + (ox >> 4), rs, bil + l * BS * BS, BS,
+                        (fy << 4) + fx, w, h + 4);
+    }
+    /* per 16 x 16 sub-block: the 5 x 5 integer search of one iteration and the
+     * sub-pel offset (:1087-1175) */
+    int n = 0;
+    for (uint32_t y0 = 0; y0 < h; y0 += sh)
+        for (uint32_t x0 = 0; x0 < w; x0 += sw, n++) {
+            const int16_t *c0 = bil + (2 + y0) * BS + x0 + 2, *c1 = bil + BS * BS + (2 + y0) * BS + x0 + 2;
+            uint32_t cost[CS * CS];
+            for (int i = 0; i < CS * CS; i++) cost[i] = 0xFFFFFFFFu;
+            int ctr = CS * CS / 2, non0 = 1;
+            int32_t del[2] = { 0, 0 };
+            uint32_t best;
+            orc_sad_s16(c0, BS, c1, BS, sw, sh, 1, &best);
+            best >>= 1;
+            best -= best >> 2;
+            if (best < sh * sw || best == 0) non0 = 0;
+            else {
+                cost[ctr] = best;
+                int bdx = 0, bdy = 0;
+                for (int dy = -2; dy <= 2; dy++)
+                    for (int dx = -2; dx <= 2; dx++) {
+                        uint32_t *c = &cost[ctr + dy * CS + dx];
+                        if (*c == 0xFFFFFFFFu) {
+                            orc_sad_s16(c0 + dy * BS + dx, BS, c1 - dy * BS - dx, BS, sw, sh, 1, c);
+                            *c >>= 1;
+                        }
+                        if (*c < best) { best = *c; bdx = dx; bdy = dy; }
+                    }
+                del[0] = bdx; del[1] = bdy;
+                ctr += bdy * CS + bdx;
+            }
+            del[0] *= 16; del[1] *= 16;
+            dmvr_subpel(non0, del, &cost[ctr], CS);
+            mvd[2 * n] = (int16_t)del[0];
+            mvd[2 * n + 1] = (int16_t)del[1];
+            /* the refined prediction of the sub-block (Xin266LumaMotionCompDmvr, :1260-1420):
+             * L0 moves by +del, L1 by -del; when the integer part moved, the 8-tap
+             * filter reads a copy of the unrefined position's region padded by 2 */
+            int16_t p[2][16 * 16];
+            for (int l = 0; l < 2; l++) {
+                const int32_t sg = l ? -1 : 1;
+                const int32_t rx = mv16[2 * l] + sg * del[0], ry = mv16[2 * l + 1] + sg * del[1];
+                const int32_t dix = (rx >> 4) - (mv16[2 * l] >> 4), diy = (ry >> 4) - (mv16[2 * l + 1] >> 4);
+                if (dix || diy) {
+                    const int32_t ix = (((cu_x + (int32_t)x0) * 16) + base[l][0]) >> 4, iy = (((cu_y + (int32_t)y0) * 16) + base[l][1]) >> 4;
+                    opix padb[32 * 32];
+                    opix *pb = padb + 8 * 32;
+                    orc_copy_and_pad(refs[l] + (intptr_t)iy * rs + ix, rs, pb, 32, sw, sh);
+                    dmvr_luma_s16(pb + diy * 32 + dix, 32, p[l], 16, ((ry & 15) << 4) + (rx & 15), sw, sh, (uint32_t)alt_hpel);
+                } else {
+                    const int32_t cx = CLIP3(min_mvx * 16, max_mvx * 16, rx), cy = CLIP3(min_mvy * 16, max_mvy * 16, ry);
+                    const int32_t ox = (cu_x + (int32_t)x0) * 16 + cx, oy = (cu_y + (int32_t)y0) * 16 + cy;
+                    dmvr_luma_s16(refs[l] + (intptr_t)(oy >> 4) * rs + (ox >> 4), rs, p[l], 16, ((oy & 15) << 4) + (ox & 15), sw,
+                                  sh, (uint32_t)alt_hpel);
+                }
+            }
+            orc_interp_avg(p[0], 16, p[1], 16, pred + (intptr_t)y0 * ps + x0, ps, sw, sh);
+        }
+    free(bil);
+}
+
 /* Xin266FullSubPelMe (open, h266_sub_pel_refine.c:81-212): 8 half-pel then 8
  * quarter-pel neighbours in the fixed order of :47-55, luma interpolation with the
  * default filter into a W x H block, SAD, strict '<'.  Returns unchanged when the

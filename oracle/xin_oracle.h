@@ -166,6 +166,22 @@ void orc_me_hier(const orc_hier_in *hi, uint32_t w, uint32_t h, int32_t mvpx, in
                  int32_t range_y, uint32_t lambda, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
                  orc_me_io *io);
 
+/* ---- DMVR: the encoder's emulation of decoder-side MV refinement --------- */
+void orc_sad_s16(const int16_t *a, intptr_t as, const int16_t *b, intptr_t bs, uint32_t w, uint32_t h, uint32_t sub,
+                 uint32_t *sad);
+void orc_block_copy(const opix *src, intptr_t ss, opix *dst, intptr_t ds, uint32_t w, uint32_t h);
+void orc_block_pad(opix *buf, intptr_t bs, uint32_t w, uint32_t h, uint32_t pw, uint32_t ph);
+void orc_copy_and_pad(const opix *ref, intptr_t rs, opix *pad, intptr_t ps, uint32_t w, uint32_t h);
+void orc_copy_and_pad_uv(const opix *ref_u, const opix *ref_v, intptr_t rs, opix *pad_u, opix *pad_v, intptr_t ps,
+                         uint32_t w, uint32_t h);
+/* one bi-predicted CU: ref0 / ref1 picture origins (stride rs), CU at (cu_x, cu_y),
+ * window [min, max] (full-pel), mv16 = L0 x, y, L1 x, y (1/16 pel); writes the
+ * per-16x16 sub-block L0 refinements mvd[2 * n] (1/16 pel; L1 gets the negation)
+ * and the refined bi-prediction pred (w x h) */
+void orc_dmvr_luma(const opix *ref0, const opix *ref1, intptr_t rs, int32_t cu_x, int32_t cu_y, int32_t min_mvx,
+                   int32_t min_mvy, int32_t max_mvx, int32_t max_mvy, uint32_t w, uint32_t h, const int32_t mv16[4],
+                   int alt_hpel, int16_t *mvd, opix *pred, intptr_t ps);
+
 /* ---- frame hot path: one CU through ME + MC + TQ + recon (the batched GPU frame stage's checker) */
 typedef struct orc_frame_desc {
     int32_t width, height, ctu;            /* luma size, CTU size (padding = ctu + 16) */

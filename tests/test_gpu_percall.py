@@ -459,6 +459,75 @@ def test_motion_est_hier_driver(libs):
                 (io.best_mvx, io.best_mvy, io.best_cost, io.best_sad), (w, h, R, mvp)
 
 
+def test_dmvr_helpers(libs):
+    """pfXinComputeSadS16 (row-subsampled int16 SAD) and pfXinCopyAndPad / Uv
+    against the oracle (itself pinned to h266_copy_and_pad.c compiled in place)."""
+    g, o, bd = libs
+    rng = np.random.default_rng(540)
+    for w, h in [(8, 8), (16, 16), (16, 8), (8, 32), (64, 64), (128, 16)]:
+        a = rng.integers(-9000, 9000, size=(h, w + 5)).astype(np.int16)
+        b = rng.integers(-9000, 9000, size=(h, w + 2)).astype(np.int16)
+        for sub in (0, 1, 2):
+            x, y = np.zeros(1, np.uint32), np.zeros(1, np.uint32)
+            g.XinGpuComputeSadS16(P(a), w + 5, P(b), w + 2, w, h, sub, P(x)); _ok(g)
+            o.sad_s16(P(a), w + 5, P(b), w + 2, w, h, sub, P(y))
+            assert x[0] == y[0], (w, h, sub)
+    src = rng.integers(0, (1 << bd), size=(80, 96)).astype(o.pix)
+    srcv = rng.integers(0, (1 << bd), size=(80, 96)).astype(o.pix)
+    for w, h in [(4, 4), (8, 8), (16, 16), (8, 16), (16, 4)]:
+        bufs = [np.full((32, 32), 5, o.pix) for _ in range(4)]
+        off = 8 * 32 + 8
+        g.XinGpuCopyAndPad(P(src, 20 * 96 + 30), 96, P(bufs[0], off), 32, w, h); _ok(g)
+        o.copy_and_pad(P(src, 20 * 96 + 30), 96, P(bufs[1], off), 32, w, h)
+        assert np.array_equal(bufs[0], bufs[1]), (w, h)
+        g.XinGpuCopyAndPadUv(P(src, 20 * 96 + 30), P(srcv, 20 * 96 + 30), 96, P(bufs[0], off), P(bufs[2], off), 32, w, h)
+        _ok(g)
+        o.copy_and_pad_uv(P(src, 20 * 96 + 30), P(srcv, 20 * 96 + 30), 96, P(bufs[1], off), P(bufs[3], off), 32, w, h)
+        assert np.array_equal(bufs[0], bufs[1]) and np.array_equal(bufs[2], bufs[3]), (w, h)
+
+
+def test_dmvr_luma(libs):
+    """XinGpuLumaMotionCompDmvr against the oracle's restatement of
+    Xin266LumaMotionCompDmvr / Xin266DeriveMvFromDmvr (pinned to the compiled
+    reference): sub-block refinements and the refined bi-prediction, every
+    block size 8..128, shifted reference pairs, flat blocks, clipped windows and
+    the alternative half-pel filter."""
+    g, o, bd = libs
+    rng = np.random.default_rng(975 + bd)
+    pad = 80
+    H, W = 160, 224
+    base = rng.integers(0, 1 << bd, size=(H + 2 * pad, W + 2 * pad)).astype(np.int32)
+    sm = ((base + np.roll(base, 1, 0) + np.roll(base, 1, 1) + np.roll(base, (1, 1), (0, 1))) // 4).astype(o.pix)
+    rs = sm.shape[1]
+    sizes = [(8, 16), (16, 8), (16, 16), (32, 16), (32, 32), (64, 64), (128, 128), (16, 64), (64, 8), (8, 8)]
+    moved = 0
+    for trial in range(160):
+        w, h = sizes[trial % len(sizes)]
+        sx, sy = int(rng.integers(-3, 4)), int(rng.integers(-3, 4))
+        ref1 = np.ascontiguousarray(np.roll(sm, (sy, sx), (0, 1)))
+        if trial % 9 == 4:
+            ref1 = np.full_like(sm, 77)
+        cx = int(rng.integers(0, (W - w) // 8 + 1)) * 8
+        cy = int(rng.integers(0, (H - h) // 8 + 1)) * 8
+        mv = np.array(rng.integers(-120, 121, 4), np.int32)
+        win = (-cx - 72, -cy - 72, W + 72 - w - cx, H + 72 - h - cy) if trial % 5 else (-3, -2, 4, 3)
+        n = (w // min(w, 16)) * (h // min(h, 16))
+        outs = []
+        for which in (0, 1):
+            mvd = np.zeros(2 * n, np.int16)
+            pred = np.zeros((h, w + 3), o.pix)
+            args = (P(sm, pad * rs + pad), P(ref1, pad * rs + pad), rs, cx, cy, *win, w, h, P(mv), int(trial % 4 == 1))
+            if which == 0:
+                g.XinGpuLumaMotionCompDmvr(*args, P(pred), w + 3, P(mvd)); _ok(g, "dmvr")
+            else:
+                o.dmvr_luma(*args, P(mvd), P(pred), w + 3)
+            outs.append((mvd, pred))
+        assert np.array_equal(outs[0][0], outs[1][0]), ("mvd", trial, w, h, outs[0][0], outs[1][0])
+        assert np.array_equal(outs[0][1], outs[1][1]), ("pred", trial, w, h)
+        moved += int(np.any(outs[1][0] != 0))
+    assert moved > 30
+
+
 def test_invalid_arguments_report_errors(libs):
     g, o, bd = libs
     a = np.zeros(64, o.pix)

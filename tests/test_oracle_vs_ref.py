@@ -417,3 +417,70 @@ def test_motion_comp_call_sites(bd):
                         wb = (-2, 3, 4, 5, 10)[bcw]
                         o.interp_weight(O.ptr(s[0]), 128, O.ptr(s[1]), 128, O.ptr(want), cw, cw, ch, 8 - wb, wb)
                 assert np.array_equal(got, want), ("chroma", pl, w, h, cx, cy, mv, bi, bcw)
+
+
+@pytest.mark.parametrize("bd", BDS)
+def test_copy_and_pad(bd):
+    """Xin266CopyAndPad / Xin266CopyAndPadUv (h266_copy_and_pad.c:32-112) compiled in
+    place against the oracle: every written sample of the padded buffers."""
+    o, r = _pair(bd)
+    rng = np.random.default_rng(32 + bd)
+    src = rng.integers(0, o.max_pix + 1, size=(80, 96)).astype(o.pix)
+    srcv = rng.integers(0, o.max_pix + 1, size=(80, 96)).astype(o.pix)
+    for w, h in [(4, 4), (8, 8), (16, 16), (8, 16), (16, 4)]:
+        for uv in (False, True):
+            bufs = [np.full((32, 32), 5, o.pix) for _ in range(4)]
+            off = 8 * 32 + 8
+            if uv:
+                o.copy_and_pad_uv(O.ptr(src, 20 * 96 + 30), O.ptr(srcv, 20 * 96 + 30), 96, O.ptr(bufs[0], off),
+                                  O.ptr(bufs[1], off), 32, w, h)
+                r.copy_and_pad_uv(O.ptr(src, 20 * 96 + 30), O.ptr(srcv, 20 * 96 + 30), 96, O.ptr(bufs[2], off),
+                                  O.ptr(bufs[3], off), 32, w, h)
+                assert np.array_equal(bufs[0], bufs[2]) and np.array_equal(bufs[1], bufs[3]), (w, h)
+            else:
+                o.copy_and_pad(O.ptr(src, 20 * 96 + 30), 96, O.ptr(bufs[0], off), 32, w, h)
+                r.copy_and_pad(O.ptr(src, 20 * 96 + 30), 96, O.ptr(bufs[2], off), 32, w, h)
+                assert np.array_equal(bufs[0], bufs[2]), (w, h)
+
+
+@pytest.mark.parametrize("bd", BDS)
+def test_dmvr_luma(bd):
+    """Xin266LumaMotionCompDmvr with Xin266DeriveMvFromDmvr (h266_inter_prediction.c:975-1420)
+    compiled in place against the oracle's restatement: the per-sub-block
+    refinements and the refined bi-prediction, on pairs of references where one
+    is a shifted copy of the other (so the 5 x 5 search and the sub-pel surface
+    have something to find), flat and noisy blocks, clipped windows."""
+    o, r = _pair(bd)
+    rng = np.random.default_rng(947 + bd)
+    pad = 80
+    H, W = 96, 160
+    base = rng.integers(0, o.max_pix + 1, size=(H + 2 * pad, W + 2 * pad)).astype(np.int32)
+    sm = ((base + np.roll(base, 1, 0) + np.roll(base, 1, 1) + np.roll(base, (1, 1), (0, 1))) // 4).astype(o.pix)
+    rs = sm.shape[1]
+    nonzero = 0
+    for trial in range(120):
+        w, h = [(8, 16), (16, 8), (16, 16), (32, 16), (32, 32), (64, 64), (128, 128), (16, 64)][trial % 8]
+        if w > W or h > H:
+            continue
+        sx, sy = int(rng.integers(-3, 4)), int(rng.integers(-3, 4))
+        ref0 = sm
+        ref1 = np.ascontiguousarray(np.roll(sm, (sy, sx), (0, 1)))
+        if trial % 7 == 3:
+            ref1 = np.ascontiguousarray(np.full_like(sm, 300 % (o.max_pix + 1)))
+        cx = int(rng.integers(0, (W - w) // 8 + 1)) * 8
+        cy = int(rng.integers(0, (H - h) // 8 + 1)) * 8
+        mv = np.array([int(rng.integers(-96, 97)), int(rng.integers(-96, 97)), int(rng.integers(-96, 97)),
+                       int(rng.integers(-96, 97))], np.int32)
+        win = (-cx - 72, -cy - 72, W + 72 - w - cx, H + 72 - h - cy) if trial % 5 else (-3, -2, 4, 3)
+        n = ((w + 15) // 16) * ((h + 15) // 16)
+        outs = []
+        for lib in (o, r):
+            mvd = np.zeros(2 * n, np.int16)
+            pred = np.zeros((h, w + 3), o.pix)
+            lib.dmvr_luma(O.ptr(ref0, pad * rs + pad), O.ptr(ref1, pad * rs + pad), rs, cx, cy, *win, w, h, O.ptr(mv),
+                          trial % 4 == 1, O.ptr(mvd), O.ptr(pred), w + 3)
+            outs.append((mvd, pred))
+        assert np.array_equal(outs[0][0], outs[1][0]), ("mvd", trial, w, h, outs[0][0], outs[1][0])
+        assert np.array_equal(outs[0][1], outs[1][1]), ("pred", trial, w, h)
+        nonzero += int(np.any(outs[0][0] != 0))
+    assert nonzero > 20

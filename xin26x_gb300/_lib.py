@@ -167,6 +167,11 @@ SIGNATURES = {
     "XinGpuDownscale2x2": ([vp, C.c_ssize_t, i32, i32, vp, C.c_ssize_t, u32, u32], None),
     "XinGpuMotionSearchHier": ([vp, C.c_ssize_t, vp, C.c_ssize_t, i32, i32, i32, i32, u32, u32, vp], None),
     "XinGpuMotionEstHier": ([vp], None),
+    "XinGpuLumaMotionCompDmvr": ([vp, vp, C.c_ssize_t, i32, i32, i32, i32, i32, i32, u32, u32, vp, i32, vp, C.c_ssize_t,
+                                  vp], None),
+    "XinGpuComputeSadS16": ([vp, C.c_ssize_t, vp, C.c_ssize_t, u32, u32, u32, vp], None),
+    "XinGpuCopyAndPad": ([vp, C.c_ssize_t, vp, C.c_ssize_t, u32, u32], None),
+    "XinGpuCopyAndPadUv": ([vp, vp, C.c_ssize_t, vp, vp, C.c_ssize_t, u32, u32], None),
     "XinGpuDepQuant": ([vp, vp, vp, vp, vp, vp, C.c_ssize_t, u32, i32, i32, vp, u32], None),
 }
 for _n in ["InterpCopy", "InterpCopyU8S16", "LumaInterpHor", "LumaInterpVet", "LumaInterpHorVet", "LumaInterpHorU8S16",

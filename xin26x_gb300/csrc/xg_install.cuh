@@ -32,6 +32,7 @@ extern "C" int xin_gpu_install(void *funcSet, void *meFunc, uint32_t what)
                 fs->pfXinComputeSadx5[lg] = XG_FN(XinGpuComputeSadx5);
                 fs->pfXinComputeSadx3[lg] = XG_FN(XinGpuComputeSadx3);
                 fs->pfXinComputeAvgSadx8[lg] = XG_FN(XinGpuComputeAvgSadx8);
+                fs->pfXinComputeSadS16[lg] = XG_FN(XinGpuComputeSadS16);
                 if (lg >= 2) {   /* SATD, bi and BCW forms exist from width 4 (h266_func_init.c:182-208,648-655) */
                     fs->pfXinComputeSatd[lg] = XG_FN(XinGpuComputeSatd);
                     fs->pfXinComputeAvgSad[lg] = XG_FN(XinGpuComputeAvgSad);
@@ -83,6 +84,10 @@ extern "C" int xin_gpu_install(void *funcSet, void *meFunc, uint32_t what)
         if (what & XIN_GPU_INSTALL_DIST) {
             fs->pfXinComputeHada8x8 = XG_FN(XinGpuComputeHada8x8);
             fs->pfXinDownscale2x2 = XG_FN(XinGpuDownscale2x2);
+        }
+        if (what & XIN_GPU_INSTALL_INTERP) {
+            fs->pfXinCopyAndPad = XG_FN(XinGpuCopyAndPad);
+            fs->pfXinCopyAndPadUv = XG_FN(XinGpuCopyAndPadUv);
         }
         if (what & XIN_GPU_INSTALL_QUANT) {
             fs->pfXinPreRdoq = XG_FN(XinGpuPreRdoq);
