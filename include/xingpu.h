@@ -342,6 +342,29 @@ struct xin_me_struct;
 void XinGpuMotionEstFull(struct xin_me_struct *meSet);
 void XinGpuFullSubPelMe(struct xin_me_struct *meSet);
 
+/* ------------------------------------------- fast sub-pel by variance (a9)
+ * XinGpuFastSubPelMeVar: Xin266FastSubPelMeVar (h266_encoder/source/h266_sub_pel_refine.c:214-361),
+ *   the same signature, on the ME state: the eight half-pel neighbours of the
+ *   integer start (bestMv, quarter-pel, a multiple of 4) by the variance of the
+ *   difference, then without AMVR (iMvMode 0) the eight quarter-pel neighbours
+ *   of the best, each predicted by the rounded average of two half-grid samples
+ *   (the pairing of the reference's qBufA / qBufB, h266_create_section.c:97-230);
+ *   cost (variance << 8) + (sseLambda * bits << 15 + 2^22) >> 23, strict '<'.
+ *   Writes bestMv and bestPos (as the reference, not bestCost); returns unchanged
+ *   when the start is outside [minMv, maxMv].  It computes its half-pel samples
+ *   itself: the ME state's interpolation buffers are neither read nor written.
+ * XinGpuInterpoHalfPel: pfXinInterpoHalfPel (typedef XinInterpHalfPel,
+ *   h26x_core/include/h26x_me_func_struct.h:143; closed in the reference,
+ *   restated with the luma filter's half-pel phase, the alternative half-pel
+ *   filter when interpAlt): the integer, horizontal, vertical and diagonal
+ *   half-pel planes of the block in the layout the ME state's pointers assume
+ *   (h266_create_section.c:74-86). */
+struct xin_me_struct;
+void XinGpuFastSubPelMeVar(struct xin_me_struct *meSet, int32_t listIdx, int32_t refIdx);
+void XinGpuInterpoHalfPel(XG_PIXEL *ref, intptr_t refStride, uint32_t width, uint32_t height, XG_PIXEL *integPel,
+                          XG_PIXEL *halfPelH, XG_PIXEL *halfPelV, XG_PIXEL *halfPelHv, intptr_t interpStride,
+                          int32_t interpAlt);
+
 /* ---------------------------------------- search by resolution levels (a7)
  * The reference's hierarchical search (motionSearchMode 2, the preset-4/6
  * default; h266_encoder/source/h266_analyze_inter_cu.c:1063-1067) and its

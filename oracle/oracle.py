@@ -143,6 +143,11 @@ _SIGS = {
                                               C.POINTER(i32)]),
     "me_hier": ("orc_me_hier", None, [C.POINTER(orc_hier_in), u32, u32, i32, i32, i32, i32, u32, i32, i32, i32, i32,
                                       C.POINTER(orc_me_io)]),
+    "interpo_half_pel": ("orc_interpo_half_pel", None, [vp, ip, u32, u32, vp, vp, vp, vp, ip, C.c_int]),
+    "qpel_pair": ("orc_qpel_pair", None, [i32, i32, i32, i32, vp]),
+    "half_grid_block": ("orc_half_grid_block", None, [vp, ip, i32, i32, u32, u32, u32, vp, ip]),
+    "fast_subpel_me_var": ("orc_fast_subpel_me_var", "ref_fast_subpel_me_var",
+                           [vp, ip, vp, ip, u32, u32, i32, i32, C.c_uint64, i32, i32, i32, i32, i32, vp]),
     "sad_s16": ("orc_sad_s16", None, [vp, ip, vp, ip, u32, u32, u32, vp]),
     "block_pad": ("orc_block_pad", None, [vp, ip, u32, u32, u32, u32]),
     "copy_and_pad": ("orc_copy_and_pad", "ref_copy_and_pad", [vp, ip, vp, ip, u32, u32]),

@@ -338,3 +338,68 @@ void ref_copy_and_pad_uv(PIXEL *ref_u, PIXEL *ref_v, intptr_t rs, PIXEL *pad_u, 
 {
     Xin266CopyAndPadUv(ref_u, ref_v, rs, pad_u, pad_v, ps, w, h);
 }
+
+/* ---- fast sub-pel search by variance -----------------------------------
+ * Xin266FastSubPelMeVar (h266_encoder/source/h266_sub_pel_refine.c:214) called
+ * unmodified on an ME state whose interpolation buffers are laid out as
+ * Xin266ConstructMe sets them (h266_encoder/source/h266_create_section.c:45-230,
+ * a static function): four XIN_ME_BUF_STRIDE^2 planes, the half-pel pointers
+ * and the quarter-pel pointer pairs.  The pairs are generated from
+ * orc_qpel_pair; tests/test_oracle_vs_ref.py checks that rule against the
+ * assignments in h266_create_section.c read as text.  Variance and the
+ * half-pel planes go to the oracle (closed in the reference). */
+static void shim_var(PIXEL *in, intptr_t is, PIXEL *p, intptr_t ps, UINT32 w, UINT32 h, UINT32 *v)
+{ orc_var(in, is, p, ps, w, h, v); }
+static void shim_avg_var(PIXEL *in, intptr_t is, PIXEL *a, PIXEL *b, intptr_t ps, UINT32 w, UINT32 h, UINT32 *v)
+{ orc_avg_var(in, is, a, b, ps, w, h, v); }
+static void shim_half_pel(PIXEL *ref, intptr_t rs, UINT32 w, UINT32 h, PIXEL *ip, PIXEL *hp, PIXEL *vp, PIXEL *hvp,
+                          intptr_t stride, BOOL alt)
+{ orc_interpo_half_pel(ref, rs, w, h, ip, hp, vp, hvp, stride, alt); }
+
+/* pointer of half-grid point (px, py) in the planes (origins as Xin266ConstructMe) */
+static PIXEL *fsme_grid(PIXEL *integ, PIXEL *hb, PIXEL *vb, PIXEL *hvb, int px, int py)
+{
+    const intptr_t S = XIN_ME_BUF_STRIDE;
+    if (!(px & 1) && !(py & 1)) return integ + S + 1 + (py / 2) * S + px / 2;
+    if (!(py & 1)) return hb + 2 * S + (py / 2) * S + (px + 1) / 2;
+    if (!(px & 1)) return vb + 1 + ((py + 1) / 2) * S + px / 2;
+    return hvb + ((py + 1) / 2) * S + (px + 1) / 2;
+}
+
+
+void ref_fast_subpel_me_var(PIXEL *in, intptr_t is, PIXEL *ref_at_pu, intptr_t rs, UINT32 w, UINT32 h, SINT32 mvpx,
+                            SINT32 mvpy, UINT64 lambda, SINT32 imv, SINT32 min_mvx, SINT32 min_mvy, SINT32 max_mvx,
+                            SINT32 max_mvy, SINT32 *io)
+{
+    static const int off[9][2] = { { -1, 0 }, { 1, 0 }, { 0, -1 }, { 0, 1 }, { -1, -1 }, { 1, -1 }, { -1, 1 }, { 1, 1 }, { 0, 0 } };
+    xin_me_struct *me = (xin_me_struct *)calloc(1, sizeof(xin_me_struct));
+    PIXEL *buf = (PIXEL *)calloc(4 * XIN_ME_BUF_STRIDE * XIN_ME_BUF_STRIDE, sizeof(PIXEL));
+    PIXEL *integ = buf, *hb = buf + XIN_ME_BUF_STRIDE * XIN_ME_BUF_STRIDE;
+    PIXEL *vb = hb + XIN_ME_BUF_STRIDE * XIN_ME_BUF_STRIDE, *hvb = vb + XIN_ME_BUF_STRIDE * XIN_ME_BUF_STRIDE;
+    for (int lg = 0; lg < XIN_ME_SIZE_NUM; lg++) {
+        me->funcSet.pfXinComputeVar[lg] = shim_var;
+        me->funcSet.pfXinComputeAvgVar[lg] = shim_avg_var;
+    }
+    me->funcSet.pfXinInterpoHalfPel = shim_half_pel;
+    me->interpBuf = buf; me->integPel = integ; me->halfPelH = hb; me->halfPelV = vb; me->halfPelHv = hvb;
+    me->interpStride = XIN_ME_BUF_STRIDE;
+    for (int p = 0; p < POS_NUM; p++) me->halfPel[p] = fsme_grid(integ, hb, vb, hvb, off[p][0], off[p][1]);
+    for (int hpos = 0; hpos <= POS_NUM; hpos++)
+        for (int q = 0; q < POS_NUM; q++) {
+            int32_t pr[4];
+            orc_qpel_pair(off[hpos][0], off[hpos][1], off[q][0], off[q][1], pr);
+            me->qBufA[hpos][q] = fsme_grid(integ, hb, vb, hvb, pr[0], pr[1]);
+            me->qBufB[hpos][q] = fsme_grid(integ, hb, vb, hvb, pr[2], pr[3]);
+        }
+    me->input = in; me->inputStride = is; me->ref = ref_at_pu; me->refStride = rs;
+    me->width = w; me->height = h; me->sseLambda = lambda; me->iMvMode = imv;
+    me->predMv.mv.mvX = (SINT16)mvpx; me->predMv.mv.mvY = (SINT16)mvpy;
+    me->bestMv.mv.mvX = (SINT16)io[0]; me->bestMv.mv.mvY = (SINT16)io[1];
+    me->bestPos = 77;
+    me->minMv.mv.mvX = (SINT16)min_mvx; me->minMv.mv.mvY = (SINT16)min_mvy;
+    me->maxMv.mv.mvX = (SINT16)max_mvx; me->maxMv.mv.mvY = (SINT16)max_mvy;
+    Xin266FastSubPelMeVar(me, 0, 0);
+    io[0] = me->bestMv.mv.mvX; io[1] = me->bestMv.mv.mvY; io[2] = (SINT32)me->bestPos;
+    free(buf);
+    free(me);
+}

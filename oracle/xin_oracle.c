@@ -956,6 +956,109 @@ void orc_me_hier(const orc_hier_in *hi, uint32_t w, uint32_t h, int32_t mvpx, in
     io->best_cost = best; io->best_sad = bsad; io->best_mvx = bx; io->best_mvy = by;
 }
 
+/* ---- fast sub-pel search by variance -----------------------------------
+ * Xin266FastSubPelMeVar (open, h266_encoder/source/h266_sub_pel_refine.c:214-361):
+ * the eight half-pel neighbours of an integer start, then (without AMVR) the
+ * eight quarter-pel neighbours of the best, each quarter-pel prediction the
+ * rounded average of two half-grid samples (the pointer pairs qBufA / qBufB set
+ * up by Xin266ConstructMe, h266_encoder/source/h266_create_section.c:45-230);
+ * cost (variance << 8) + (lambda * bits << 15 + 2^22) >> 23.  The half-pel
+ * planes come from the closed pfXinInterpoHalfPel
+ * (h26x_core/include/h26x_me_func_struct.h:143), restated here with the
+ * luma filter's half-pel phase (the alternative half-pel filter under half-pel
+ * AMVR, as the driver's interpAlt argument selects); parity of those samples is
+ * unpinned, the driver and the pairing are pinned. */
+
+/* the w x h block at half-grid point (px, py) in half-sample units relative to
+ * ref: integer, horizontal, vertical or both-direction half-pel samples */
+void orc_half_grid_block(const opix *ref, intptr_t rs, int32_t px, int32_t py, uint32_t w, uint32_t h, uint32_t fi,
+                         opix *out, intptr_t os)
+{
+    const opix *src = ref + (intptr_t)(py >> 1) * rs + (px >> 1);
+    const int32_t frac = ((py & 1) ? 8 << 4 : 0) | ((px & 1) ? 8 : 0);
+    if (!(px & 1) && !(py & 1)) orc_interp_copy(src, rs, out, os, frac, w, h, fi);
+    else if (!(py & 1)) orc_luma_hor(src, rs, out, os, frac, w, h, fi);
+    else if (!(px & 1)) orc_luma_vet(src, rs, out, os, frac, w, h, fi);
+    else orc_luma_hv(src, rs, out, os, frac, w, h, fi);
+}
+
+/* the two half-grid points averaged for the quarter-pel position h + q / 2
+ * (half-sample units): for a diagonal q around the centre or around a
+ * diagonal h, the two points on the other diagonal; otherwise h + q and h */
+void orc_qpel_pair(int32_t hx, int32_t hy, int32_t qx, int32_t qy, int32_t p[4])
+{
+    const int h_same_parity = ((hx ^ hy) & 1) == 0;      /* the centre or a diagonal half position */
+    if (qx && qy && h_same_parity) { p[0] = hx + qx; p[1] = hy; p[2] = hx; p[3] = hy + qy; }
+    else { p[0] = hx + qx; p[1] = hy + qy; p[2] = hx; p[3] = hy; }
+}
+
+/* the four planes in the layout the driver's pointers assume: plane k's
+ * element (x, y), x in [-1, w], y in [-1, h], sits at half-grid point
+ * (2x - dx_k, 2y - dy_k) with (dx, dy) = (0,0) integer, (1,0) H, (0,1) V, (1,1) HV;
+ * origins: integer at integ + stride + 1, H at hb + 2 stride, V at vb + 1, HV at
+ * hvb (h266_create_section.c:74-86) */
+void orc_interpo_half_pel(const opix *ref, intptr_t rs, uint32_t w, uint32_t h, opix *integ, opix *hb, opix *vb, opix *hvb,
+                          intptr_t stride, int alt)
+{
+    opix *org[4] = { integ + stride + 1, hb + 2 * stride, vb + 1, hvb };
+    static const int d[4][2] = { { 0, 0 }, { 1, 0 }, { 0, 1 }, { 1, 1 } };
+    for (int k = 0; k < 4; k++) {
+        /* rows -1 .. h of every plane fit the buffer except above the V and HV
+         * origins (row 0 of their buffers), whose row -1 is not read */
+        const int y0 = (k >= 2) ? 0 : -1, x0 = (k == 1 || k == 3) ? 0 : -1;
+        orc_half_grid_block(ref, rs, 2 * x0 - d[k][0], 2 * y0 - d[k][1], (uint32_t)(w + 1 - x0), (uint32_t)(h + 1 - y0),
+                            alt ? 1u : 0u, org[k] + (intptr_t)y0 * stride + x0, stride);
+    }
+}
+
+static uint64_t fsme_cost(uint32_t var, int32_t mvx, int32_t mvy, int32_t mvpx, int32_t mvpy, int shift, uint64_t lambda)
+{
+    const uint64_t bits = (uint64_t)(orc_mvd_bits((mvx - mvpx) >> shift) + orc_mvd_bits((mvy - mvpy) >> shift)) << 15;
+    return (uint64_t)(uint32_t)(var << 8) + ((lambda * bits + (1ull << 22)) >> 23);
+}
+
+void orc_fast_subpel_me_var(const opix *in, intptr_t is, const opix *ref_at_pu, intptr_t rs, uint32_t w, uint32_t h,
+                            int32_t mvpx, int32_t mvpy, uint64_t lambda, int32_t imv, int32_t min_mvx, int32_t min_mvy,
+                            int32_t max_mvx, int32_t max_mvy, int32_t *io)
+{
+    static const int8_t off[9][2] = { { -1, 0 }, { 1, 0 }, { 0, -1 }, { 0, 1 }, { -1, -1 }, { 1, -1 }, { -1, 1 }, { 1, 1 }, { 0, 0 } };
+    int32_t mvx = io[0], mvy = io[1];
+    const int32_t ix = mvx >> 2, iy = mvy >> 2;
+    if (!(ix >= min_mvx && iy >= min_mvy && ix <= max_mvx && iy <= max_mvy)) return;
+    const int shift = imv == 3 ? 1 : imv << 1;
+    const uint32_t fi = imv == 3 ? 1u : 0u;
+    const opix *r0 = ref_at_pu + (intptr_t)iy * rs + ix;
+    opix *a = (opix *)malloc(sizeof(opix) * w * h), *b = (opix *)malloc(sizeof(opix) * w * h);
+    uint32_t var;
+    orc_var(in, is, r0, rs, w, h, &var);
+    uint64_t best = fsme_cost(var, mvx, mvy, mvpx, mvpy, shift, lambda);
+    int bp = 8;
+    for (int p = 0; p < 8; p++) {
+        orc_half_grid_block(r0, rs, off[p][0], off[p][1], w, h, fi, a, w);
+        orc_var(in, is, a, w, w, h, &var);
+        const uint64_t c = fsme_cost(var, mvx + 2 * off[p][0], mvy + 2 * off[p][1], mvpx, mvpy, shift, lambda);
+        if (c < best) { best = c; bp = p; }
+    }
+    const int hx = off[bp][0], hy = off[bp][1];
+    mvx += 2 * hx; mvy += 2 * hy;
+    if (imv == 0) {
+        int qp = 8;
+        for (int p = 0; p < 8; p++) {
+            int32_t pr[4];
+            orc_qpel_pair(hx, hy, off[p][0], off[p][1], pr);
+            orc_half_grid_block(r0, rs, pr[0], pr[1], w, h, fi, a, w);
+            orc_half_grid_block(r0, rs, pr[2], pr[3], w, h, fi, b, w);
+            orc_avg_var(in, is, a, b, w, w, h, &var);
+            const uint64_t c = fsme_cost(var, mvx + off[p][0], mvy + off[p][1], mvpx, mvpy, shift, lambda);
+            if (c < best) { best = c; qp = p; }
+        }
+        mvx += off[qp][0]; mvy += off[qp][1];
+        bp = qp;
+    }
+    free(a); free(b);
+    io[0] = mvx; io[1] = mvy; io[2] = bp;
+}
+
 /* ---- DMVR ------------------------------------------------------------
  * The encoder's emulation of the H.266 decoder-side MV refinement:
  * Xin266DeriveMvFromDmvr + Xin266SubPelRefineDmvr and Xin266LumaMotionCompDmvr

@@ -166,6 +166,18 @@ void orc_me_hier(const orc_hier_in *hi, uint32_t w, uint32_t h, int32_t mvpx, in
                  int32_t range_y, uint32_t lambda, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
                  orc_me_io *io);
 
+/* ---- fast sub-pel search by variance (a9) ------------------------------- */
+void orc_half_grid_block(const opix *ref, intptr_t rs, int32_t px, int32_t py, uint32_t w, uint32_t h, uint32_t fi,
+                         opix *out, intptr_t os);
+void orc_qpel_pair(int32_t hx, int32_t hy, int32_t qx, int32_t qy, int32_t p[4]);
+void orc_interpo_half_pel(const opix *ref, intptr_t rs, uint32_t w, uint32_t h, opix *integ, opix *hb, opix *vb, opix *hvb,
+                          intptr_t stride, int alt);
+/* io in: mvx, mvy (quarter-pel, integer positions); out: mvx, mvy, best_pos.
+ * lambda: the ME state's sseLambda; imv: its iMvMode (0 or 3 = half-pel AMVR) */
+void orc_fast_subpel_me_var(const opix *in, intptr_t is, const opix *ref_at_pu, intptr_t rs, uint32_t w, uint32_t h,
+                            int32_t mvpx, int32_t mvpy, uint64_t lambda, int32_t imv, int32_t min_mvx, int32_t min_mvy,
+                            int32_t max_mvx, int32_t max_mvy, int32_t *io);
+
 /* ---- DMVR: the encoder's emulation of decoder-side MV refinement --------- */
 void orc_sad_s16(const int16_t *a, intptr_t as, const int16_t *b, intptr_t bs, uint32_t w, uint32_t h, uint32_t sub,
                  uint32_t *sad);

@@ -528,6 +528,50 @@ def test_dmvr_luma(libs):
     assert moved > 30
 
 
+def test_fast_subpel_me_var(libs):
+    """XinGpuFastSubPelMeVar against the oracle's restatement of Xin266FastSubPelMeVar
+    (pinned to the compiled reference on the reference's buffer layout), with and
+    without half-pel AMVR, starts inside and outside the window; and
+    XinGpuInterpoHalfPel's four planes in the ME state's layout."""
+    from xin26x_gb300 import _lib
+    g, o, bd = libs
+    rng = np.random.default_rng(2007 + bd)
+    mx = (1 << bd) - 1
+    pad = 48
+    for w, h in [(8, 8), (16, 16), (32, 32), (64, 64), (128, 128), (16, 8), (8, 32)]:
+        base = rng.integers(0, mx + 1, size=(h + 2 * pad, w + 2 * pad)).astype(np.int32)
+        refp = ((base + np.roll(base, 1, 0) + np.roll(base, 1, 1)) // 3).astype(o.pix)
+        inp = np.ascontiguousarray(refp[pad + 2:pad + 2 + h, pad - 1:pad - 1 + w] // 2 + 3).astype(o.pix)
+        rs = refp.shape[1]
+        for trial in range(10):
+            mv = (int(rng.integers(-6, 7)) * 4, int(rng.integers(-6, 7)) * 4)
+            mvp = (int(rng.integers(-20, 21)), int(rng.integers(-20, 21)))
+            lam = int(rng.integers(0, 1 << 24))
+            imv = 3 if trial % 3 == 2 else 0
+            win = (-8, -8, 8, 8) if trial % 4 else (mv[0] // 4 + 1, -8, 8, 8)
+            me = _lib.xin_gpu_me_struct()
+            me.width, me.height = w, h
+            me.input, me.inputStride = P(inp), w
+            me.ref, me.refStride = P(refp, pad * rs + pad), rs
+            me.predMv.mvX, me.predMv.mvY = mvp
+            me.bestMv.mvX, me.bestMv.mvY = mv
+            me.bestPos = 77
+            me.minMv.mvX, me.minMv.mvY, me.maxMv.mvX, me.maxMv.mvY = win
+            me.sseLambda, me.iMvMode = lam, imv
+            g.XinGpuFastSubPelMeVar(C.byref(me), 0, 0); _ok(g, "FastSubPelMeVar")
+            io = np.array([mv[0], mv[1], 77], np.int32)
+            o.fast_subpel_me_var(P(inp), w, P(refp, pad * rs + pad), rs, w, h, mvp[0], mvp[1], lam, imv, *win, P(io))
+            assert (me.bestMv.mvX, me.bestMv.mvY, me.bestPos) == tuple(int(v) for v in io), (w, h, trial)
+        for alt in (0, 1):
+            S = 200
+            a = [np.full(S * S, 9, o.pix) for _ in range(4)]
+            b = [np.full(S * S, 9, o.pix) for _ in range(4)]
+            g.XinGpuInterpoHalfPel(P(refp, pad * rs + pad), rs, w, h, *[P(x) for x in a], S, alt); _ok(g)
+            o.interpo_half_pel(P(refp, pad * rs + pad), rs, w, h, *[P(x) for x in b], S, alt)
+            for k in range(4):
+                assert np.array_equal(a[k], b[k]), (w, h, alt, k)
+
+
 def test_invalid_arguments_report_errors(libs):
     g, o, bd = libs
     a = np.zeros(64, o.pix)

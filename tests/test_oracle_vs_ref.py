@@ -484,3 +484,74 @@ def test_dmvr_luma(bd):
         assert np.array_equal(outs[0][1], outs[1][1]), ("pred", trial, w, h)
         nonzero += int(np.any(outs[0][0] != 0))
     assert nonzero > 20
+
+
+def test_qpel_pairing_matches_reference_table():
+    """The quarter-pel pairing rule (orc_qpel_pair) against every qBufA / qBufB and
+    halfPel assignment of Xin266ConstructMe (h266_encoder/source/h266_create_section.c),
+    read as text: each pointer expression is turned into the half-grid point it
+    addresses."""
+    import os
+    import re
+    from __graft_entry__ import REFERENCE_DIR
+    path = os.path.join(REFERENCE_DIR, "h266_encoder", "source", "h266_create_section.c")
+    src = open(path).read()
+    org = {"integPel": (0, 0), "halfPelH": (-1, 0), "halfPelV": (0, -1), "halfPelHv": (-1, -1)}
+    pos = {"LFT_POS": (-1, 0), "RGT_POS": (1, 0), "TOP_POS": (0, -1), "BOT_POS": (0, 1), "TOP_LFT_POS": (-1, -1),
+           "TOP_RGT_POS": (1, -1), "BOT_LFT_POS": (-1, 1), "BOT_RGT_POS": (1, 1), "CEN_POS": (0, 0)}
+
+    def point(expr):
+        expr = expr.replace(" ", "")
+        m = re.match(r"(integPel|halfPelHv|halfPelH|halfPelV)(.*)", expr)
+        dx = dy = 0
+        for t in re.findall(r"[+-][^+-]+", m.group(2)):
+            v = t[1:]
+            sg = 1 if t[0] == "+" else -1
+            if v == "XIN_ME_BUF_STRIDE":
+                dy += sg
+            else:
+                dx += sg * int(v)
+        ox, oy = org[m.group(1)]
+        return (ox + 2 * dx, oy + 2 * dy)
+
+    o = O.oracle(8)
+    pairs = {}
+    for m in re.finditer(r"meSet->qBuf([AB])\[(\w+)\]\[(\w+)\]\s*=\s*([^;]+);", src):
+        pairs[(m.group(2), m.group(3), m.group(1))] = point(m.group(4))
+    assert len(pairs) == 144
+    for (h, q, ab), a in pairs.items():
+        if ab != "A":
+            continue
+        p = np.zeros(4, np.int32)
+        o.qpel_pair(*pos[h], *pos[q], O.ptr(p))
+        assert {a, pairs[(h, q, "B")]} == {(int(p[0]), int(p[1])), (int(p[2]), int(p[3]))}, (h, q)
+    halves = {m.group(1): point(m.group(2)) for m in re.finditer(r"meSet->halfPel\[(\w+)\]\s*=\s*([^;]+);", src)}
+    assert len(halves) == 8 and all(halves[k] == pos[k] for k in halves)
+
+
+@pytest.mark.parametrize("bd", BDS)
+def test_fast_subpel_me_var(bd):
+    """Xin266FastSubPelMeVar (h266_sub_pel_refine.c:214-361) compiled in place, on the
+    reference's buffer layout, against the oracle's restatement: with and without
+    half-pel AMVR, starts at the window's edge and outside it, several lambdas."""
+    o, r = _pair(bd)
+    rng = np.random.default_rng(214 + bd)
+    pad = 40
+    for w, h in [(8, 8), (16, 16), (32, 32), (64, 64), (128, 128), (16, 8), (8, 32)]:
+        base = rng.integers(0, o.max_pix + 1, size=(h + 2 * pad, w + 2 * pad)).astype(np.int32)
+        refp = ((base + np.roll(base, 1, 0) + np.roll(base, 1, 1)) // 3).astype(o.pix)
+        inp = np.ascontiguousarray(refp[pad + 2:pad + 2 + h, pad - 1:pad - 1 + w] // 2 + 3).astype(o.pix)
+        rs = refp.shape[1]
+        for trial in range(12):
+            mv = (int(rng.integers(-5, 6)) * 4, int(rng.integers(-5, 6)) * 4)
+            mvp = (int(rng.integers(-20, 21)), int(rng.integers(-20, 21)))
+            lam = int(rng.integers(0, 1 << 24))
+            imv = 3 if trial % 3 == 2 else 0
+            win = (-6, -6, 6, 6) if trial % 4 else (mv[0] // 4, mv[1] // 4 + 1, 9, 9)
+            outs = []
+            for lib in (o, r):
+                io = np.array([mv[0], mv[1], 77], np.int32)
+                lib.fast_subpel_me_var(O.ptr(inp), w, O.ptr(refp, pad * rs + pad), rs, w, h, mvp[0], mvp[1], lam, imv,
+                                       *win, O.ptr(io))
+                outs.append(io)
+            assert np.array_equal(outs[0], outs[1]), (w, h, trial, outs)

@@ -167,6 +167,8 @@ SIGNATURES = {
     "XinGpuDownscale2x2": ([vp, C.c_ssize_t, i32, i32, vp, C.c_ssize_t, u32, u32], None),
     "XinGpuMotionSearchHier": ([vp, C.c_ssize_t, vp, C.c_ssize_t, i32, i32, i32, i32, u32, u32, vp], None),
     "XinGpuMotionEstHier": ([vp], None),
+    "XinGpuFastSubPelMeVar": ([vp, i32, i32], None),
+    "XinGpuInterpoHalfPel": ([vp, C.c_ssize_t, u32, u32, vp, vp, vp, vp, C.c_ssize_t, i32], None),
     "XinGpuLumaMotionCompDmvr": ([vp, vp, C.c_ssize_t, i32, i32, i32, i32, i32, i32, u32, u32, vp, i32, vp, C.c_ssize_t,
                                   vp], None),
     "XinGpuComputeSadS16": ([vp, C.c_ssize_t, vp, C.c_ssize_t, u32, u32, u32, vp], None),

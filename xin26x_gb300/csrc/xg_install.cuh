@@ -108,6 +108,7 @@ extern "C" int xin_gpu_install(void *funcSet, void *meFunc, uint32_t what)
             mf->pfXinMotionSearchHier2[lg] = (void *)XinGpuMotionSearchHier;
         }
         mf->pfXinDownscale2x2 = (void *)XinGpuDownscale2x2;
+        mf->pfXinInterpoHalfPel = (void *)XinGpuInterpoHalfPel;
     }
     return XIN_GPU_OK;
 }

@@ -12,6 +12,7 @@
 #include "xg_me_percall.cuh"
 #include "xg_frame.cuh"
 #include "xg_dmvr.cuh"
+#include "xg_fsme.cuh"
 #include "xg_server.cuh"
 #include "xg_install.cuh"
 #include "xg_tq_batch.cuh"
