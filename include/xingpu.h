@@ -482,6 +482,21 @@ typedef struct xin_gpu_stream_cfg {
                                     0 and the zero MV as its candidate, the reference picture
                                     and the current picture downscaled by 2 and 4 with
                                     XinGpuDownscale2x2's arithmetic) */
+    int32_t  tu_mode;            /* 0: DCT2, TU = CU, quant / dequant (no RDOQ).
+                                    1: the preset-4 TU work: per CU (TU = CU) every transform
+                                    candidate the mode decision may evaluate -- luma DCT2 and,
+                                    for CUs up to 32, the MTS pairs 2..5; chroma DCT2 -- each
+                                    through dependent quantisation (Xin266Transform's DepQuant
+                                    branch, h266_trans_quant.c:61-245, QP + 12 at 10 bits, rates
+                                    from the stream's context set, xin_gpu_stream_set_contexts)
+                                    and the inverse transform and reconstruction
+                                    (Xin266IDctAdd); plus the final luma prediction's cost with
+                                    SATD as the distortion.  The choice among the candidates
+                                    stays with the caller (its rate estimate): the per-CU
+                                    records give each candidate's non-zero map and SSD
+                                    (xin_gpu_results.mts); the coefficient and reconstructed
+                                    planes and xin_gpu_cu_result's nz / ssd hold the DCT2
+                                    candidate.  Slice QPs up to 51 (39 at 10 bits). */
 } xin_gpu_stream_cfg;
 
 typedef struct xin_gpu_picture {
@@ -499,6 +514,16 @@ typedef struct xin_gpu_cu_result {
     uint64_t ssd[3];
 } xin_gpu_cu_result;
 
+/* tu_mode 1: the transform candidates of a CU */
+typedef struct xin_gpu_cu_mts {
+    uint32_t satd_cost;          /* (SATD << 8) + (bits(mvx) + bits(mvy)) * sad_lambda of the final
+                                    luma prediction (h266_analyze_inter_cu.c:1109-1131 with SATD) */
+    uint32_t ncand;              /* luma candidates: 1 (64 x 64) or 5 */
+    uint64_t nz[5];              /* luma non-zero-CG map per candidate: DCT2, then MTS index 2..5
+                                    (DST7/DST7, DCT8/DST7, DST7/DCT8, DCT8/DCT8) */
+    uint64_t ssd[5];             /* luma SSD of each candidate's reconstruction */
+} xin_gpu_cu_mts;
+
 typedef struct xin_gpu_results {
     xin_gpu_cu_result *cu;       /* [xin_gpu_stream_num_cus()], levels from 64 down to 8 */
     XG_COEFF *q[3];              /* [levels][plane height][plane width] when XIN_GPU_OUT_Q; zero where
@@ -506,6 +531,7 @@ typedef struct xin_gpu_results {
                                     that are not multiples of the CU size) */
     XG_PIXEL *rec[3];            /* same layout when XIN_GPU_OUT_REC */
     float    gpu_ms;             /* device time of the picture's launches */
+    xin_gpu_cu_mts *mts;         /* tu_mode 1: [xin_gpu_stream_num_cus()] (NULL: a view is returned) */
 } xin_gpu_results;
 
 int  xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream **out);
@@ -532,6 +558,12 @@ int  xin_gpu_stream_stage_ms(const xin_gpu_stream *s, float ms[4]);
 /* Device pointers of the result arrays of the last collected picture (same
  * layouts as xin_gpu_results), valid until the second submit after it. */
 int  xin_gpu_stream_device_results(const xin_gpu_stream *s, void **cu, void *q[3], void *rec[3]);
+
+/* tu_mode 1: the CABAC context set (XIN_GPU_NUM_CTX records, the reference's
+ * xin_prob_model array) the trellis takes its rates from, for the pictures
+ * submitted after this call; XIN_GPU_ERR_STATE while pictures are in flight.
+ * Until it is called, every context holds probability one half. */
+int  xin_gpu_stream_set_contexts(xin_gpu_stream *s, const xin_gpu_prob *ctx);
 
 /* Device and pinned-host bytes a stream of this configuration allocates
  * (before the CUDA allocator's rounding); no GPU needed. */

@@ -50,7 +50,7 @@ class orc_frame_desc(C.Structure):
                 ("ref", vp * 3), ("ref_stride", ip * 2),
                 ("search_range", i32), ("sad_lambda", u32), ("qp", i32), ("uv_qp", i32), ("intra_frame", i32),
                 ("search_mode", i32), ("in_lo", vp * 2), ("in_lo_stride", ip * 2),
-                ("ref_lo", vp * 2), ("ref_lo_stride", ip * 2)]
+                ("ref_lo", vp * 2), ("ref_lo_stride", ip * 2), ("tu_mode", i32), ("ctx", vp)]
 
 
 class orc_hier_in(C.Structure):
@@ -72,7 +72,8 @@ class xin_dp_param(C.Structure):
 
 
 class orc_cu_out(C.Structure):
-    _fields_ = [("mvx", i32), ("mvy", i32), ("cost", u32), ("int_cost", u32), ("nz", u64 * 3), ("ssd", u64 * 3)]
+    _fields_ = [("mvx", i32), ("mvy", i32), ("cost", u32), ("int_cost", u32), ("nz", u64 * 3), ("ssd", u64 * 3),
+                ("satd_cost", u32), ("ncand", u32), ("nz_mts", u64 * 5), ("ssd_mts", u64 * 5)]
 
 
 # logical name -> (oracle symbol, reference symbol or None, argtypes)

@@ -1274,6 +1274,70 @@ void orc_full_subpel_me(const opix *in, intptr_t is, const opix *ref_at_pu, intp
  *   -> Xin266IDctAdd recon; SSD(recon, input) per plane.
  * The integer search starts from cost UINT32_MAX at MV (0,0).
  * ====================================================================== */
+/* The preset-4 TU of one CU (tu_mode 1), TU = CU: every transform candidate the
+ * reference's mode decision may evaluate, each through the dependent-quantisation
+ * branch of Xin266Transform (h266_encoder/source/h266_trans_quant.c:61-245:
+ * Xin266SubFDctWxH, then pfXinDepQuant with QP + 12 at 10 bits) and
+ * Xin266IDctAdd (h266_idct_add.c:45): luma DCT2 and, for CUs up to 32, the
+ * explicit MTS pairs 2..5 (enableMts at preset 4,
+ * app/common/source/xin_encoder_option.c:196); chroma DCT2.  The rate tables
+ * come from the frame's context set; luma carries the root cbf (an inter CU
+ * coded as one TU).  The choice among the candidates (the host's rate
+ * estimation) is not made: each candidate's non-zero map and SSD are returned,
+ * and the coefficient / reconstructed planes hold the DCT2 candidate.  Also
+ * the cost of the final luma prediction with SATD as the distortion (satdMd
+ * at preset 4, h266_encoder_create.c:1938; the recomputation at
+ * h266_analyze_inter_cu.c:1109-1131 with predictor 0 and one reference). */
+static void orc_cu_tu_p4(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size, int32_t mnx, int32_t mny,
+                         int32_t mxx, int32_t mxy, ocoef *q[3], intptr_t q_stride[2], opix *rec[3], intptr_t rec_stride[2],
+                         opix *pred, ocoef *t, ocoef *qb, ocoef *r, orc_cu_out *out)
+{
+    static const uint32_t mts_list[5] = { 0, 2, 3, 4, 5 };
+    const int32_t cs = size >> 1;
+    opix *rb = (opix *)malloc(sizeof(opix) * (size_t)(size * size));
+    out->ncand = size <= 32 ? 5 : 1;
+    for (int pl = 0; pl < 3; pl++) {
+        const int32_t bs = pl ? cs : size, px = pl ? cu_x >> 1 : cu_x, py = pl ? cu_y >> 1 : cu_y;
+        const intptr_t istr = f->in_stride[pl ? 1 : 0], qstr = q_stride[pl ? 1 : 0], rstr = rec_stride[pl ? 1 : 0];
+        if (pl == 0)
+            orc_luma_inter_pred(f->ref[0], f->ref_stride[0], pred, bs, out->mvx * 4, out->mvy * 4, cu_x, cu_y,
+                                mnx, mny, mxx, mxy, (uint32_t)size, (uint32_t)size, 0);
+        else
+            orc_chroma_motion_comp(f->ref[pl], f->ref_stride[1], pred, bs, out->mvx * 4, out->mvy * 4, cu_x, cu_y,
+                                   mnx, mny, mxx, mxy, (uint32_t)size, (uint32_t)size);
+        const opix *src = f->in[pl] + (intptr_t)py * istr + px;
+        if (pl == 0) {
+            uint32_t satd;
+            orc_satd(src, istr, pred, bs, (uint32_t)bs, (uint32_t)bs, &satd);
+            out->satd_cost = (satd << 8) + (orc_mvd_bits(out->mvx) + orc_mvd_bits(out->mvy)) * f->sad_lambda;
+        }
+        const int32_t qp = (pl ? f->uv_qp : f->qp) + (ORC_BITDEPTH == 10 ? 12 : 0);
+        const uint32_t nc = pl ? 1 : out->ncand;
+        for (uint32_t c = 0; c < nc; c++) {
+            uint64_t nz = 0;
+            orc_sub_fdct_wxh(src, istr, pred, bs, t, bs, pl ? 1u : 0u, mts_list[c], bs, bs, 0, 1);
+            orc_dep_quant(t, bs, bs, bs, qp, pl, f->ctx, pl == 0, qb, r, &nz);
+            orc_idct_add(r, bs, pred, bs, rb, bs, 0, pl ? 1u : 0u, mts_list[c], (uint32_t)bs, (uint32_t)bs, 1);
+            uint64_t ssd = 0;
+            for (int32_t y = 0; y < bs; y++)
+                for (int32_t x = 0; x < bs; x++) {
+                    const int64_t d = (int64_t)src[y * istr + x] - (int64_t)rb[y * bs + x];
+                    ssd += (uint64_t)(d * d);
+                }
+            if (pl == 0) { out->nz_mts[c] = nz; out->ssd_mts[c] = ssd; }
+            if (c == 0) {
+                out->nz[pl] = nz; out->ssd[pl] = ssd;
+                for (int32_t y = 0; y < bs; y++)
+                    for (int32_t x = 0; x < bs; x++) {
+                        q[pl][(intptr_t)(py + y) * qstr + px + x] = qb[y * bs + x];
+                        rec[pl][(intptr_t)(py + y) * rstr + px + x] = rb[y * bs + x];
+                    }
+            }
+        }
+    }
+    free(rb);
+}
+
 void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size,
                     ocoef *q[3], intptr_t q_stride[2], opix *rec[3], intptr_t rec_stride[2], orc_cu_out *out)
 {
@@ -1311,6 +1375,11 @@ void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t
     ocoef *t = (ocoef *)malloc(sizeof(ocoef) * (size_t)(size * size));
     ocoef *qb = (ocoef *)malloc(sizeof(ocoef) * (size_t)(size * size));
     ocoef *r = (ocoef *)malloc(sizeof(ocoef) * (size_t)(size * size));
+    if (f->tu_mode == 1) {
+        orc_cu_tu_p4(f, cu_x, cu_y, size, mnx, mny, mxx, mxy, q, q_stride, rec, rec_stride, pred, t, qb, r, out);
+        free(pred); free(t); free(qb); free(r);
+        return;
+    }
     for (int pl = 0; pl < 3; pl++) {
         int32_t bs = pl ? cs : size, px = pl ? cu_x >> 1 : cu_x, py = pl ? cu_y >> 1 : cu_y;
         intptr_t istr = f->in_stride[pl ? 1 : 0], qstr = q_stride[pl ? 1 : 0], rstr = rec_stride[pl ? 1 : 0];

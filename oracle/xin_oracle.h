@@ -206,6 +206,9 @@ typedef struct orc_frame_desc {
     int32_t search_mode;                   /* 0 exhaustive, 1 by resolution levels (orc_me_hier) */
     const opix *in_lo[2];  intptr_t in_lo_stride[2];    /* search_mode 1: luma at 1/2 and 1/4 resolution, */
     const opix *ref_lo[2]; intptr_t ref_lo_stride[2];   /* pointers at picture (0,0) */
+    int32_t tu_mode;                       /* 0 DCT2 + quant; 1 the preset-4 TU: MTS candidates with
+                                              dependent quantisation (see orc_cu_hotpath) */
+    const struct orc_prob *ctx;            /* tu_mode 1: the CABAC context set (ORC_NUM_CTX records) */
 } orc_frame_desc;
 typedef struct orc_cu_out {
     int32_t mvx, mvy;                      /* quarter-pel */
@@ -213,6 +216,11 @@ typedef struct orc_cu_out {
     uint32_t int_cost;                     /* after integer search */
     uint64_t nz[3];
     uint64_t ssd[3];                       /* recon vs input per plane */
+    /* tu_mode 1 */
+    uint32_t satd_cost;                    /* (SATD << 8) + MV bits * lambda of the final luma prediction */
+    uint32_t ncand;                        /* luma transform candidates: 1 (64x64) or 5 */
+    uint64_t nz_mts[5];                    /* luma per candidate: DCT2, then MTS index 2..5 */
+    uint64_t ssd_mts[5];
 } orc_cu_out;
 void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size,
                     ocoef *q[3], intptr_t q_stride[2], opix *rec[3], intptr_t rec_stride[2], orc_cu_out *out);

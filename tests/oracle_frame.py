@@ -10,7 +10,7 @@ from concurrent.futures import ThreadPoolExecutor
 import numpy as np
 
 from oracle import oracle as O
-from xin26x_gb300.frame import CU_DTYPE
+from xin26x_gb300.frame import CU_DTYPE, MTS_DTYPE
 from xin26x_gb300.synth import pad_plane
 
 
@@ -28,11 +28,13 @@ def downscaled(plane, o, levels=2):
 
 
 def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=64, bitdepth=8, cus=None, threads=1,
-        search_mode=0):
+        search_mode=0, tu_mode=0, contexts=None):
     """cur, ref: (Y, U, V) planes.  levels: [(size, first, cus_x, cus_y)] as the stream reports.
     cus: optional list of global CU indices to evaluate (others left zero).
     search_mode: 0 exhaustive integer search, 1 by resolution levels (the reference
     and the current picture downscaled by 2 and 4, the padded reference as a whole).
+    tu_mode 1: the preset-4 TU (transform candidates with dependent quantisation,
+    rates from contexts); the transform candidates' records are returned too.
     threads: host threads sharing the CUs (0 = every core); each CU writes only its
     own record and its own area of the level's planes, so the calls are independent.
     Returns (cu records, q planes [levels,h,w] x3, rec planes x3)."""
@@ -51,6 +53,11 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
     f.ref_stride[0], f.ref_stride[1] = refp[0].shape[1], refp[1].shape[1]
     f.search_range, f.sad_lambda, f.qp, f.uv_qp, f.intra_frame = search_range, sad_lambda, qp, uv_qp, 0
     f.search_mode = search_mode
+    f.tu_mode = tu_mode
+    ctx = None
+    if tu_mode:
+        ctx = np.ascontiguousarray(contexts)
+        f.ctx = ctx.ctypes.data
     keep = []
     if search_mode == 1:
         ref_lo, in_lo = downscaled(refp[0], o), downscaled(curc[0], o)
@@ -63,6 +70,7 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
             f.in_lo_stride[l] = in_lo[l].shape[1]
     ncu = sum(cx * cy for (_, _, cx, cy) in levels)
     recs = np.zeros(ncu, CU_DTYPE)
+    mts = np.zeros(ncu, MTS_DTYPE)
     nl = len(levels)
     q = [np.zeros((nl, h, w), o.coef), np.zeros((nl, h // 2, w // 2), o.coef), np.zeros((nl, h // 2, w // 2), o.coef)]
     rec = [np.zeros((nl, h, w), o.pix), np.zeros((nl, h // 2, w // 2), o.pix), np.zeros((nl, h // 2, w // 2), o.pix)]
@@ -86,6 +94,11 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
         r["mvx"], r["mvy"], r["cost"], r["int_cost"] = out.mvx, out.mvy, out.cost, out.int_cost
         r["nz"] = list(out.nz)
         r["ssd"] = list(out.ssd)
+        if tu_mode:
+            m = mts[first + j]
+            m["satd_cost"], m["ncand"] = out.satd_cost, out.ncand
+            m["nz"] = list(out.nz_mts)
+            m["ssd"] = list(out.ssd_mts)
 
     nthreads = (os.cpu_count() or 1) if threads == 0 else max(1, threads)
     if nthreads == 1 or len(work) < 2:
@@ -97,4 +110,6 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
         one(work[0])        # the oracle builds its transform matrices on first use: once, before the threads
         with ThreadPoolExecutor(nthreads) as ex:
             list(ex.map(one, work[1:]))
+    if tu_mode:
+        return recs, q, rec, mts
     return recs, q, rec

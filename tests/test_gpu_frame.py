@@ -326,3 +326,54 @@ def test_frame_hier_search_matches_oracle(bd, inb, w, h, R, ctu):
             _compare(out, want, fs.levels, ("hier", bd, inb, w, h, R, k))
     finally:
         fs.close()
+
+
+@pytest.mark.parametrize("bd,inb,search_mode", [(8, 0, 0), (10, 0, 1), (10, 8, 1)])
+@pytest.mark.parametrize("w,h,R", [(192, 128, 16), (200, 104, 24)])
+def test_frame_preset4_tu_matches_oracle(bd, inb, search_mode, w, h, R):
+    """tu_mode 1 (the preset-4 TU work): for every CU of every level, every transform
+    candidate (luma DCT2 and MTS 2..5 up to 32, chroma DCT2) through dependent
+    quantisation, inverse transform and reconstruction -- each candidate's
+    non-zero map and SSD, the DCT2 candidate's coefficient and reconstructed
+    planes, the SATD cost -- against the oracle's restatement of
+    Xin266Transform's DepQuant branch (pinned to the reference's C) on seeded
+    context sets and QPs 12 .. 37."""
+    from xin26x_gb300 import synth as S
+    rng = np.random.default_rng(w + R + bd)
+    ctx = S.contexts(rng, 1)[0]
+    seq = synth.sequence(w, h, 3, seed=w + h, bitdepth=8 if inb == 8 else bd, objects=2)
+    fs = FrameStream(w, h, search_range=R, out_q=True, out_rec=True, bitdepth=bd, input_bitdepth=inb,
+                     search_mode=search_mode, tu_mode=1, contexts=ctx)
+    try:
+        fs.submit(*seq[0], qp=22, uv_qp=22, sad_lambda=64)
+        fs.wait()
+        for k, qp in ((1, 12), (2, 27 if bd == 10 else 37)):
+            lam = 50 << (2 if inb == 8 else 0)
+            fs.submit(*seq[k], qp=qp, uv_qp=qp + 1, sad_lambda=lam)
+            out = fs.wait()
+            cur, ref = seq[k], seq[k - 1]
+            if inb == 8:
+                cur, ref = [tuple(p.astype(np.uint16) << 2 for p in f) for f in (cur, ref)]
+            recs, q, rec, mts = oracle_frame.run(cur, ref, fs.levels, search_range=R, qp=qp, uv_qp=qp + 1, sad_lambda=lam,
+                                                 bitdepth=bd, threads=0, search_mode=search_mode, tu_mode=1,
+                                                 contexts=ctx)
+            _compare(out, (recs, q, rec), fs.levels, ("tu", bd, inb, w, h, R, k))
+            for name in ("satd_cost", "ncand", "nz", "ssd"):
+                bad = np.nonzero(np.any((out["mts"][name] != mts[name]).reshape(len(mts), -1), axis=1))[0]
+                assert bad.size == 0, (name, bad[:5], out["mts"][bad[:3]], mts[bad[:3]])
+    finally:
+        fs.close()
+
+
+def test_frame_preset4_tu_qp_limit():
+    """The trellis's parameters stop at QP 51: at 10 bits (QP + 12) a slice QP above
+    39 is refused before any launch."""
+    fs = FrameStream(64, 64, search_range=8, bitdepth=10, tu_mode=1)
+    try:
+        seq = synth.sequence(64, 64, 2, seed=1, bitdepth=10)
+        fs.submit(*seq[0], qp=39, uv_qp=39, sad_lambda=64)
+        fs.wait()
+        with pytest.raises(RuntimeError, match="QP above 39"):
+            fs.submit(*seq[1], qp=40, uv_qp=40, sad_lambda=64)
+    finally:
+        fs.close()

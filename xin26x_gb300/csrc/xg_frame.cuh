@@ -14,6 +14,8 @@
 
 static const int XG_LEVEL_SIZE[4] = { 64, 32, 16, 8 };
 
+struct XgTuState;   /* the preset-4 TU stage (xg_tu.cuh) */
+
 struct xin_gpu_stream {
     xin_gpu_stream_cfg cfg;
     int pad, pitch, cpad, cpitch, rows, crows;
@@ -34,6 +36,7 @@ struct xin_gpu_stream {
      * pictures can be in flight: one computing while the other's copies run */
     struct Set {
         xin_gpu_cu_result *dres;
+        xin_gpu_cu_mts *dmts, *h_mts;    /* tu_mode 1: per-CU transform candidates */
         xg_coef *dq[3];
         xg_pix *drec[3];
         XgPicParams *dpp;
@@ -66,7 +69,14 @@ struct xin_gpu_stream {
     int nsub;              /* pictures submitted */
     int ndone;             /* pictures collected by frame_wait (the oldest first) */
     int graph_launches[2]; /* kernels inside each captured graph */
+    XgTuState *tu;         /* tu_mode 1 */
 };
+
+static int xg_tu_open(xin_gpu_stream *s);
+static void xg_tu_free(XgTuState *u);
+static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cudaStream_t st);
+static uint64_t xg_tu_bytes(const xin_gpu_stream_cfg *c);
+static int16_t *xg_tu_resid(XgTuState *u, int level, int plane);
 
 static void xg_quant_params(int qp, int lg, int intra_frame, XgQuant *q)
 {
@@ -97,8 +107,9 @@ static int xg_stream_free(xin_gpu_stream *s)
         for (int l = 0; l < 2; l++) cudaFree(s->lo_base[i][l]);
     }
     cudaFree(s->keys);
+    xg_tu_free(s->tu);
     for (auto &t : s->set) {
-        cudaFree(t.dres); cudaFree(t.dpp);
+        cudaFree(t.dres); cudaFree(t.dpp); cudaFree(t.dmts); cudaFreeHost(t.h_mts);
         for (int p = 0; p < 3; p++) { cudaFree(t.dq[p]); cudaFree(t.drec[p]); cudaFree(t.d_in8[p]); cudaFreeHost(t.h_in[p]); cudaFreeHost(t.h_q[p]); cudaFreeHost(t.h_rec[p]); }
         cudaFreeHost(t.h_pp); cudaFreeHost(t.h_res);
         for (int i = 0; i < 5; i++) if (t.evs[i]) cudaEventDestroy(t.evs[i]);
@@ -145,8 +156,9 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     const xin_gpu_stream_cfg &c = *cfg;
     if (c.width < 16 || c.height < 16 || (c.width & 1) || (c.height & 1) || c.width > 8192 || c.height > 8192 ||
         (c.ctu_size != 64 && c.ctu_size != 128) || c.search_range < 1 || c.search_range > 256 ||
-        !(c.level_mask & (8u | 16u | 32u | 64u)) || !xg_input_depth_ok(c) || (c.search_mode != 0 && c.search_mode != 1)) {
-        xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range, level mask, input bit depth or search mode");
+        !(c.level_mask & (8u | 16u | 32u | 64u)) || !xg_input_depth_ok(c) || (c.search_mode != 0 && c.search_mode != 1) ||
+        (c.tu_mode != 0 && c.tu_mode != 1)) {
+        xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range, level mask, input bit depth, search or TU mode");
         return XIN_GPU_ERR_ARG;
     }
     xin_gpu_stream *s = new (std::nothrow) xin_gpu_stream();
@@ -216,6 +228,8 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     if (e == cudaSuccess) e = cudaMalloc(&s->keys, sizeof(unsigned long long) * (s->ncus > 0 ? s->ncus : 1));
     for (auto &t : s->set) {
         if (e == cudaSuccess) e = cudaMalloc(&t.dres, sizeof(xin_gpu_cu_result) * s->ncus);
+        if (e == cudaSuccess && c.tu_mode == 1) e = cudaMalloc(&t.dmts, sizeof(xin_gpu_cu_mts) * s->ncus);
+        if (e == cudaSuccess && c.tu_mode == 1 && !c.device_io) e = cudaMallocHost(&t.h_mts, sizeof(xin_gpu_cu_mts) * s->ncus);
         if (e == cudaSuccess) e = cudaMalloc(&t.dpp, sizeof(XgPicParams));
         for (int p = 0; p < 3 && e == cudaSuccess; p++) {
             size_t n = (p ? lc : lq) * s->nlev;
@@ -324,6 +338,10 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
 #endif
     });
     if (xg_cuda_check(me_attr_err, "me smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
+    if (c.tu_mode == 1) {
+        const int st = xg_tu_open(s);
+        if (st) { xg_stream_free(s); return st; }
+    }
     *out = s;
     return XIN_GPU_OK;
 }
@@ -490,6 +508,9 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
                 tp.rec[p] = t.drec[p] + (p ? lc : lq) * li;
             }
             tp.res = t.dres;
+            for (int p = 0; p < 3; p++) tp.resid[p] = nullptr;
+            if (s->tu)
+                for (int p = 0; p < 3; p++) tp.resid[p] = xg_tu_resid(s->tu, L, p);
             int n = s->lev_cx[L] * s->lev_cy[L];
             if (n > 0) {
                 /* 64 and 32: a 128-thread CTA per CU; 16 and 8: a warp per CU, four CUs per
@@ -508,6 +529,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             cudaEventRecord(s->ev_join[i], s->aux[i]);
             cudaStreamWaitEvent(st, s->ev_join[i], 0);
         }
+        if (s->tu) nl += xg_tu_enqueue(s, cur, t, st);
         cudaStreamWaitEvent(st, s->ev_qjoin, 0);
         cudaStreamWaitEvent(st, s->ev_tjoin, 0);
         xg_stage_event(t.evs[3], st, capturing);
@@ -531,6 +553,7 @@ static void xg_enqueue_results(xin_gpu_stream *s, xin_gpu_stream::Set &t, bool w
     if (with_me && !c.device_io) {
         size_t lq = (size_t)c.width * c.height, lc = lq / 4;
         cudaMemcpyAsync(t.h_res, t.dres, sizeof(xin_gpu_cu_result) * s->ncus, cudaMemcpyDeviceToHost, s->cst);
+        if (t.dmts) cudaMemcpyAsync(t.h_mts, t.dmts, sizeof(xin_gpu_cu_mts) * s->ncus, cudaMemcpyDeviceToHost, s->cst);
         for (int p = 0; p < 3; p++) {
             size_t n = (p ? lc : lq) * s->nlev;
             if (c.out_flags & XIN_GPU_OUT_Q) cudaMemcpyAsync(t.h_q[p], t.dq[p], n * sizeof(xg_coef), cudaMemcpyDeviceToHost, s->cst);
@@ -573,6 +596,16 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
             memcpy((char *)t.h_in[p] + (size_t)y * w * es, (const char *)pic->plane[p] + (size_t)y * pic->stride[p] * es, (size_t)w * es);
     }
     pp.lambda = pic->sad_lambda;
+    if (c.tu_mode == 1) {
+        /* the trellis QP (h266_trans_quant.c:103-104): slice QP, + 12 at 10 bits; its
+         * parameter table stops at 51 */
+        pp.dq_qp[0] = pic->qp + (XG_BITDEPTH == 10 ? 12 : 0);
+        pp.dq_qp[1] = pic->uv_qp + (XG_BITDEPTH == 10 ? 12 : 0);
+        if (pp.dq_qp[0] > 51 || pp.dq_qp[1] > 51) {
+            xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: QP above %d for the dependent-quantisation stage", XG_BITDEPTH == 10 ? 39 : 51);
+            return XIN_GPU_ERR_ARG;
+        }
+    }
     for (int L = 0; L < 4; L++) {
         int lg = XG_LEVEL_SIZE[L] == 64 ? 6 : XG_LEVEL_SIZE[L] == 32 ? 5 : XG_LEVEL_SIZE[L] == 16 ? 4 : 3;
         xg_quant_params(pic->qp, lg, 0, &pp.quant[L][0]);
@@ -646,6 +679,10 @@ extern "C" int xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32
      * pinned buffers, valid until the second frame_submit after this call */
     if (res->cu) memcpy(res->cu, t.h_res, sizeof(xin_gpu_cu_result) * s->ncus);
     else res->cu = t.h_res;
+    if (t.h_mts) {
+        if (res->mts) memcpy(res->mts, t.h_mts, sizeof(xin_gpu_cu_mts) * s->ncus);
+        else res->mts = t.h_mts;
+    }
     for (int p = 0; p < 3; p++) {
         size_t n = (p ? lc : lq) * s->nlev;
         if (c.out_flags & XIN_GPU_OUT_Q) {

@@ -160,6 +160,7 @@ struct XgPicParams {
     XgQuant quant[4][3];                /* [level 64,32,16,8][plane] */
     const xg_pix *src[3];               /* device-resident source planes (device_io streams) */
     long long src_stride[3];
+    int32_t dq_qp[2];                   /* preset-4 TU stage: luma / chroma QP the trellis gets */
 };
 
 /* Sources of k_fill_slot: where a picture's samples come from */
@@ -723,6 +724,8 @@ struct XgTailParams {
     xg_coef *q[3];                    /* this level's coefficient planes (picture layout) */
     xg_pix *rec[3];                   /* this level's reconstructed planes */
     xin_gpu_cu_result *res;           /* all CUs */
+    int16_t *resid[3];                /* set (the preset-4 TU stage follows): write the residual
+                                         planes (picture layout) instead of transforming */
 };
 
 /* synchronisation of the NT threads that work on one CU (group g of a CTA
@@ -1041,16 +1044,25 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
     }
     xg_gsync<NT, CPB>(g);
 
-    /* ---- luma TQ + reconstruction */
+    /* ---- luma TQ + reconstruction (or the residual, for the preset-4 TU stage) */
     const int lgS = S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : 6;
-    for (int i = tid; i < S * S; i += NT) {
-        int y = i / S, x = i % S;
-        tl.res[xg_d2<S>(y, x)] = (int16_t)((int)org[(intptr_t)y * p.cur[0].pitch + x] - (int)pred[i]);
+    const bool resid_only = p.resid[0] != nullptr;       /* uniform over the launch */
+    if (resid_only) {
+        for (int i = tid; i < S * S; i += NT) {
+            int y = i / S, x = i % S;
+            p.resid[0][(intptr_t)(cy + y) * p.W + cx + x] = (int16_t)((int)org[(intptr_t)y * p.cur[0].pitch + x] - (int)pred[i]);
+        }
+        xg_gsync<NT, CPB>(g);
+    } else {
+        for (int i = tid; i < S * S; i += NT) {
+            int y = i / S, x = i % S;
+            tl.res[xg_d2<S>(y, x)] = (int16_t)((int)org[(intptr_t)y * p.cur[0].pitch + x] - (int)pred[i]);
+        }
+        xg_gsync<NT, CPB>(g);
+        xg_tq<S, NT, CPB>(tl, pp->quant[p.level][0], lgS + XG_BITDEPTH + 6 - 15, lgS + 6, &m.nz[0],
+                          p.q[0] + (intptr_t)cy * p.W + cx, p.W, tid, g);
+        xg_itq<S, NT, CPB>(tl, pred, org, p.cur[0].pitch, p.rec[0] + (intptr_t)cy * p.W + cx, p.W, &m.ssd[0], tid, g);
     }
-    xg_gsync<NT, CPB>(g);
-    xg_tq<S, NT, CPB>(tl, pp->quant[p.level][0], lgS + XG_BITDEPTH + 6 - 15, lgS + 6, &m.nz[0],
-                      p.q[0] + (intptr_t)cy * p.W + cx, p.W, tid, g);
-    xg_itq<S, NT, CPB>(tl, pred, org, p.cur[0].pitch, p.rec[0] + (intptr_t)cy * p.W + cx, p.W, &m.ssd[0], tid, g);
 
     /* ---- chroma: uni branch of Xin266ChromaMotionComp (1/32 phase, mask 31), TQ, reconstruction */
     {
@@ -1075,6 +1087,15 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
             }
             xg_gsync<NT, CPB>(g);
             const xg_pix *corg = p.cur[pl].data + (intptr_t)(cy >> 1) * p.cur[pl].pitch + (cx >> 1);
+            if (resid_only) {
+                for (int i = tid; i < C * C; i += NT) {
+                    int y = i / C, x = i % C;
+                    p.resid[pl][(intptr_t)((cy >> 1) + y) * W2 + (cx >> 1) + x] =
+                        (int16_t)((int)corg[(intptr_t)y * p.cur[pl].pitch + x] - (int)pred[i]);
+                }
+                xg_gsync<NT, CPB>(g);
+                continue;
+            }
             for (int i = tid; i < C * C; i += NT) {
                 int y = i / C, x = i % C;
                 tc.res[xg_d2<C>(y, x)] = (int16_t)((int)corg[(intptr_t)y * p.cur[pl].pitch + x] - (int)pred[i]);

@@ -28,7 +28,8 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
 {
     if (c->width < 16 || c->height < 16 || (c->width & 1) || (c->height & 1) || c->width > 8192 || c->height > 8192 ||
         (c->ctu_size != 64 && c->ctu_size != 128) || c->search_range < 1 || c->search_range > 256 ||
-        !(c->level_mask & (8u | 16u | 32u | 64u)) || !xg_input_depth_ok(*c) || (c->search_mode != 0 && c->search_mode != 1))
+        !(c->level_mask & (8u | 16u | 32u | 64u)) || !xg_input_depth_ok(*c) || (c->search_mode != 0 && c->search_mode != 1) ||
+        (c->tu_mode != 0 && c->tu_mode != 1))
         return XIN_GPU_ERR_ARG;
     const bool widen = XG_BITDEPTH == 10 && c->input_bitdepth == 8;
     const uint64_t in_es = widen ? 1 : sizeof(xg_pix);
@@ -50,11 +51,15 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
     uint64_t d = 2 * (ysz + 2 * csz) + 2 * 16 * ysz + 8 * (ncus ? ncus : 1) +
                  2 * (sizeof(xin_gpu_cu_result) * ncus + sizeof(XgPicParams) + (lq + 2 * lc) * nlev * (sizeof(xg_coef) + sizeof(xg_pix)));
     if (widen && !c->device_io) d += 2 * (lq + 2 * lc);     /* 8-bit device staging per set */
+    if (c->tu_mode == 1) {                                  /* the preset-4 TU stage */
+        d += xg_tu_bytes(c) + 2 * sizeof(xin_gpu_cu_mts) * ncus;
+    }
     if (c->search_mode == 1)                                /* 1/2 and 1/4 resolution luma of both slots */
         for (int l = 0; l < 2; l++)
             d += 2 * ((((uint64_t)(c->width + 2 * pad) >> (l + 1)) + 127) & ~127ull) * ((uint64_t)(c->height + 2 * pad) >> (l + 1)) *
                  sizeof(xg_pix);
     uint64_t h = sizeof(XgPicParams) + sizeof(xin_gpu_cu_result) * ncus;
+    if (c->tu_mode == 1 && !c->device_io) h += sizeof(xin_gpu_cu_mts) * ncus;
     if (!c->device_io) {
         h += (lq + 2 * lc) * in_es;
         if (c->out_flags & XIN_GPU_OUT_Q) h += (lq + 2 * lc) * nlev * sizeof(xg_coef);

@@ -18,3 +18,4 @@
 #include "xg_tq_batch.cuh"
 #include "xg_noalloc.cuh"
 #include "xg_dq.cuh"
+#include "xg_tu.cuh"
