@@ -213,7 +213,7 @@ static void dq_build_scan(dq_scan *s, int w, int h)
     s->wsbb = ew >> 2; s->hsbb = eh >> 2; s->nsbb = s->wsbb * s->hsbb; s->n = ew * eh;
     dq_diag(4, 4, cx, cy);
     dq_diag(s->wsbb, s->hsbb, gx, gy);
-    static int sid[32][32];
+    int sid[32][32];                 /* scan index by position (on the stack: callers run on several threads) */
     for (int b = 0; b < s->nsbb; b++) {
         s->sbb_x[b] = gx[b]; s->sbb_y[b] = gy[b]; s->sbb_raster[b] = gy[b] * s->wsbb + gx[b];
         for (int i = 0; i < 16; i++) {

@@ -1316,6 +1316,11 @@ static void orc_cu_tu_p4(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, in
         for (uint32_t c = 0; c < nc; c++) {
             uint64_t nz = 0;
             orc_sub_fdct_wxh(src, istr, pred, bs, t, bs, pl ? 1u : 0u, mts_list[c], bs, bs, 0, 1);
+            /* beyond the low 32 x 32 the dequantised values are zero (Xin266ZeroOutCoeff,
+             * h266_trans_quant.c:155-189) and no level is coded; the trellis writes the
+             * low 32 x 32 */
+            memset(r, 0, sizeof(ocoef) * (size_t)(bs * bs));
+            memset(qb, 0, sizeof(ocoef) * (size_t)(bs * bs));
             orc_dep_quant(t, bs, bs, bs, qp, pl, f->ctx, pl == 0, qb, r, &nz);
             orc_idct_add(r, bs, pred, bs, rb, bs, 0, pl ? 1u : 0u, mts_list[c], (uint32_t)bs, (uint32_t)bs, 1);
             uint64_t ssd = 0;

@@ -18,8 +18,9 @@ def _compare(out, ref, levels, label):
     for name in ("mvx", "mvy", "int_cost", "cost"):
         bad = np.nonzero(cu[name] != recs[name])[0]
         assert bad.size == 0, (label, name, bad[:5], cu[bad[:5]], recs[bad[:5]])
-    assert np.array_equal(cu["nz"], recs["nz"]), label
-    assert np.array_equal(cu["ssd"], recs["ssd"]), label
+    for name in ("nz", "ssd"):
+        bad = np.nonzero(np.any(cu[name] != recs[name], axis=1))[0]
+        assert bad.size == 0, (label, name, bad.size, bad[:5], cu[bad[:3]], recs[bad[:3]])
     for p in range(3):
         for li, (size, first, cx, cy) in enumerate(levels):
             s = size if p == 0 else size // 2

@@ -803,7 +803,7 @@ static size_t xg_dq_area_bytes(int nsets, int njobs, size_t nscan, int nquads, X
 
 static int xg_dq_enqueue(const xin_gpu_dq_block *d_jobs, const uint32_t *d_soff, int njobs,
                          const xg_coef *t, xg_coef *q, xg_coef *r, unsigned long long *nz, const xin_gpu_prob *d_sets,
-                         int nsets, const XgDqArea &A, int max_ctas, int full, cudaStream_t st)
+                         int nsets, const XgDqArea &A, int max_ctas, int full, cudaStream_t st, bool count = true)
 {
     int ctas = (njobs + XG_DQ_QUADS - 1) / XG_DQ_QUADS;
     if (ctas > max_ctas) ctas = max_ctas;
@@ -816,7 +816,7 @@ static int xg_dq_enqueue(const xin_gpu_dq_block *d_jobs, const uint32_t *d_soff,
     k_dq<<<ctas, XG_DQ_THREADS, sizeof(XgDqSmem), st>>>(d_jobs, njobs, A.counter, A.counts, A.order, A.first, d_soff,
                                                         A.tscan, q, r, nz, d_sets, A.rates, g_dq.d_step, g_dq.d_tpl,
                                                         g_dq.d_par, A.codes);
-    xg_count_launch(4);
+    if (count) xg_count_launch(4);
     return xg_cuda_check(cudaGetLastError(), "dep_quant launch");
 }
 

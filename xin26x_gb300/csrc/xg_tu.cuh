@@ -382,7 +382,7 @@ static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cud
     k_tu_setqp<<<(u->nblocks + 255) / 256, 256, 0, st>>>(u->plan->d_jobs, u->nblocks, t.dpp);
     nl++;
     xg_dq_enqueue(u->plan->d_jobs, u->plan->d_soff, u->plan->nblocks, u->T, u->Q, u->R, u->nz, u->ctx, 1, u->plan->area,
-                  u->plan->ctas, 1, st);
+                  u->plan->ctas, 1, st, false);
     nl += 4;
     cudaMemsetAsync(u->satd, 0, sizeof(uint32_t) * (s->ncus > 0 ? s->ncus : 1), st);
     for (int L = 0; L < 4; L++) {
