@@ -330,6 +330,7 @@ def run_gpu(args):
     percall = percall_sample(lib, frames, bd=BD)
     kbatch = kernel_batch_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup) if rank == 0 else None
     dq = dep_quant_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup, cpu=(world == 1)) if rank == 0 else None
+    p4 = preset4_bench(torch, flush, frames, max(5, min(args.steps, 20)), args.warmup) if rank == 0 else None
     wide = wide_search_bench(torch, flush) if rank == 0 else None
     if wide is not None:
         wide["by_resolution_levels"] = wide_search_bench(torch, flush, pictures=4, search_mode=1)
@@ -375,6 +376,7 @@ def run_gpu(args):
                "percall": percall,
                "kernel_batch": kbatch,
                "dep_quant": dq,
+               "preset4_1080p": p4,
                "wide_search_4k_10bit": wide,
                "pipeline_variants_1080p": variants,
                "serving": serving,
@@ -569,6 +571,88 @@ def pipeline_variant_bench(torch, flush, frames, steps, warmup, bitdepth, input_
             "value": W * H * steps / (float(np.sum(ms)) * 1e-3) / 1e6, "unit": "Mpixel/s",
             "ms_per_picture": float(np.mean(ms)),
             "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_mc_tq": stage[2], "copies": stage[3]}}
+
+
+def preset4_bench(torch, flush, frames, steps, warmup, cpu_seconds=8.0):
+    """The preset-4 hot path at 1080p (the named configuration's search and TU
+    work, as far as the frame form carries them): 8-bit pictures coded by the
+    10-bit library, integer search by resolution levels (motionSearchMode 2)
+    over +-64, full sub-pel search, SATD cost of the final prediction, and per
+    CU every transform candidate -- luma DCT2 and the four MTS pairs up to 32,
+    chroma DCT2 -- through dependent quantisation (seeded CABAC context set),
+    inverse transform and reconstruction; QP 27/32/37 cycling.  Device-resident
+    pictures, CUDA-event device time per picture, L2 flushed between pictures;
+    beside it the oracle on a sample of the same CTUs on one host core."""
+    from xin26x_gb300 import _lib, synth
+    lib = _lib.load(BD)
+    assert lib.xin_gpu_init(torch.cuda.current_device()) == 0
+    ctx = np.ascontiguousarray(synth.contexts(np.random.default_rng(4), 1)[0])
+    dev = [tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f) for f in frames]
+    cfg = _lib.xin_gpu_stream_cfg(W, H, 64, SEARCH, sum(LEVELS), 0, 1, 1, IN_BD, 1, 1)
+    h = C.c_void_p()
+    assert lib.xin_gpu_stream_open(C.byref(cfg), C.byref(h)) == 0, lib.xin_gpu_last_error()
+    assert lib.xin_gpu_stream_set_contexts(h, ctx.ctypes.data) == 0
+    res = _lib.xin_gpu_results()
+
+    def submit(k):
+        pic = _lib.xin_gpu_picture()
+        for i, t in enumerate(dev[k % len(dev)]):
+            pic.plane[i] = t.data_ptr()
+            pic.stride[i] = t.shape[1]
+        qp = QPS[k % 3]
+        pic.qp, pic.uv_qp, pic.sad_lambda = qp, qp, LAMBDA_BD[qp]
+        assert lib.xin_gpu_frame_submit(h, C.byref(pic)) == 0, lib.xin_gpu_last_error()
+        assert lib.xin_gpu_frame_wait(h, C.byref(res), -1) == 0, lib.xin_gpu_last_error()
+
+    for k in range(1 + max(3, warmup)):
+        submit(k)
+    launches0 = lib.xin_gpu_kernel_launches()
+    ms, stage = [], np.zeros(4)
+    for k in range(steps):
+        flush.fill_(k & 255)
+        torch.cuda.synchronize()
+        submit(10 + k)
+        ms.append(res.gpu_ms)
+        st = (C.c_float * 4)()
+        lib.xin_gpu_stream_stage_ms(h, st)
+        stage += np.array(list(st))
+    launches = (lib.xin_gpu_kernel_launches() - launches0) / steps
+    lib.xin_gpu_stream_close(h)
+    stage /= steps
+    value = W * H * steps / (float(np.sum(ms)) * 1e-3) / 1e6
+    out = {"workload": "1080p, 8-bit 4:2:0 pictures coded at 10 bits, search by resolution levels (+-64), full sub-pel "
+                       "search, SATD cost, per CU luma DCT2 + MTS 2..5 (CUs up to 32) and chroma DCT2, each through "
+                       "dependent quantisation, inverse transform and reconstruction; CU levels 64/32/16/8, TU = CU, "
+                       "QP 27/32/37 cycling, low-delay P with one reference",
+           "value": value, "unit": "Mpixel/s", "ms_per_picture": float(np.mean(ms)),
+           "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_mc_tu": stage[2], "copies": stage[3]},
+           "gpu_launches_per_picture": launches, "l2": "flushed between pictures (512 MB write outside the timed events)",
+           "not_covered": "random access with bi-prediction and DMVR (built per call, not in the frame form), BT/TT "
+                          "and 4x4 / 128x128 CUs, RDOQ, the host's choice among the candidates"}
+    # the oracle on the same pictures: random 64x64 CTUs, all four levels, one core
+    from tests import oracle_frame
+    cur, ref = [tuple(p.astype(np.uint16) << (BD - IN_BD) for p in f) for f in (frames[1], frames[0])]
+    levels, first = [], 0
+    for sz in LEVELS:
+        levels.append((sz, first, W // sz, H // sz))
+        first += (W // sz) * (H // sz)
+    ctus = [(x, y) for y in range(0, H - 63, 64) for x in range(0, W - 63, 64)]
+    order = np.random.default_rng(6).permutation(len(ctus))
+    done, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < cpu_seconds and done < len(order):
+        cx, cy = ctus[order[done]]
+        cus = [f + ((cy + yy) // sz) * nx + (cx + xx) // sz for (sz, f, nx, ny) in levels
+               for yy in range(0, 64, sz) for xx in range(0, 64, sz)]
+        oracle_frame.run(cur, ref, levels, search_range=SEARCH, qp=32, uv_qp=32, sad_lambda=LAMBDA_BD[32], bitdepth=BD,
+                         cus=cus, search_mode=1, tu_mode=1, contexts=ctx)
+        done += 1
+    el = time.perf_counter() - t0
+    cpu = done * 64 * 64 / el / 1e6
+    out["cpu_oracle"] = {"value": cpu, "unit": "Mpixel/s", "cores": 1, "kind": "port",
+                         "sample": f"{done} random 64x64 CTUs of the same workload (all four levels, QP 32), "
+                                   f"oracle C restatement, 1 thread, {el:.1f} s"}
+    out["gpu_over_cpu_core"] = value / cpu if cpu else None
+    return out
 
 
 def wide_search_bench(torch, flush, pictures=3, search_mode=0):

@@ -54,108 +54,140 @@ struct XgTuLevel {
     int W, S, cus_x, ncu, nc;
 };
 
-template <int G>
-__device__ __forceinline__ void xg_tu_sync(int gid)
+/* A transform matrix of N points (rows k < K = min(N, 32)) into a packed int8
+ * operand of xg_mm_dp2 (|entries| <= 90): FWD, M(k, x) = T(k, x) (rows k, l = x),
+ * the layout of the forward passes; otherwise M(x, k) = T(k, x) (rows x, l = k),
+ * the layout of the inverse passes */
+template <int N, bool FWD>
+__device__ __forceinline__ void xg_tu_load_mat(uint32_t *dst, const int16_t *m, int tid, int nthreads)
 {
-    if (G == 32) __syncwarp();
-    else asm volatile("bar.sync %0, %1;" ::"r"(1 + gid), "r"(G) : "memory");
+    constexpr int K = N > 32 ? 32 : N;
+    int8_t *d = reinterpret_cast<int8_t *>(dst);
+    for (int i = tid; i < K * N; i += nthreads) {
+        const int k = i / N, x = i % N;
+        if (FWD) d[(((x >> 2) * K + k) << 2) | (x & 3)] = (int8_t)m[i];
+        else d[(((k >> 2) * N + x) << 2) | (k & 3)] = (int8_t)m[i];
+    }
 }
 
-/* position and transform pair of job j of plane pl */
-struct XgTuJobPos { int px, py, pw, n, lg, c, hor, ver; };
-__device__ __forceinline__ XgTuJobPos xg_tu_job(const XgTuLevel &L, int pl, int j)
+/* one block's work area: a = the first pass's int16-pair operand, b = the second's */
+template <int N>
+struct XgTuWork {
+    static constexpr int K = N > 32 ? 32 : N;
+    alignas(16) int16_t a[N * N];
+    alignas(16) int16_t b[N * K];
+};
+
+/* position and transform pair of CU cu, candidate c (DCT2, then MTS 2..5), plane pl */
+struct XgTuJobPos { int px, py, pw, hor, ver; };
+__device__ __forceinline__ XgTuJobPos xg_tu_job(const XgTuLevel &L, int pl, int cu, int c, int n)
 {
     XgTuJobPos o;
-    const int nc = pl ? 1 : L.nc, cu = j / nc;
-    o.c = j - cu * nc;
-    o.n = pl ? L.S >> 1 : L.S;
-    o.lg = 31 - __clz(o.n);
-    o.px = (cu % L.cus_x) * o.n;
-    o.py = (cu / L.cus_x) * o.n;
+    o.px = (cu % L.cus_x) * n;
+    o.py = (cu / L.cus_x) * n;
     o.pw = pl ? L.W >> 1 : L.W;
-    const int mts = o.c ? o.c + 1 : 0;     /* candidates: DCT2, then MTS 2..5 */
+    const int mts = c ? c + 1 : 0;
     o.hor = c_mts_tx[mts][0];
     o.ver = c_mts_tx[mts][1];
     return o;
 }
 
-template <int G>
-__global__ void __launch_bounds__(256) k_tu_fwd(XgTuLevel L, int pl)
+/* Forward transforms of N x N blocks: CTA = CPB groups of NT threads, one CU each,
+ * all of candidate blockIdx.y (the CTA loads its two matrices once).  Rows then
+ * columns as dp2a products on the tails' packed operands; the low K x K
+ * frequencies go to the candidate's coefficient plane. */
+template <int N, int NT, int CPB>
+__global__ void __launch_bounds__(NT * CPB) k_tu_fwd(XgTuLevel L, int pl)
 {
-    extern __shared__ uint32_t tsw[];
-    constexpr int NG = 256 / G;
-    const int gid = threadIdx.x / G, t = threadIdx.x % G;
-    const int n = pl ? L.S >> 1 : L.S, k = n > 32 ? 32 : n;
-    int16_t *resT = (int16_t *)tsw + gid * (n * n + n * k), *t1T = resT + n * n;
-    const int njobs = L.ncu * (pl ? 1 : L.nc);
-    for (int j = blockIdx.x * NG + gid; j < njobs; j += gridDim.x * NG) {
-        const XgTuJobPos a = xg_tu_job(L, pl, j);
-        const int16_t *src = L.resid[pl] + (size_t)a.py * a.pw + a.px;
-        for (int o = t; o < n * n; o += G) { const int y = o >> a.lg, x = o & (n - 1); resT[x * n + y] = src[(size_t)y * a.pw + x]; }
-        xg_tu_sync<G>(gid);
-        const int16_t *mh = xg_mat(a.hor, a.lg), *mv = xg_mat(a.ver, a.lg);
-        const int s1 = a.lg + XG_BITDEPTH + 6 - 15, s2 = a.lg + 6;
-        /* rows: t1T[i * k + f] = sum_x mh[f][x] res[i][x], f < k */
-        xg_mm_rt<G>(t, k, n, n, mh, n, 1, resT, 1, n, [&](int f, int i, int acc) {
-            t1T[i * k + f] = (int16_t)xg_clip16(xg_rshift_rnd(acc, s1));
-        });
-        xg_tu_sync<G>(gid);
-        xg_coef *dst = L.T[pl] + (size_t)a.c * L.cstride + (size_t)a.py * a.pw + a.px;
-        /* columns: T[fv][fh] = sum_i mv[fv][i] t1T[i * k + fh] */
-        xg_mm_rt<G>(t, k, k, n, mv, n, 1, t1T, 1, k, [&](int fv, int fh, int acc) {
-            dst[(size_t)fv * a.pw + fh] = (xg_coef)xg_clip16(xg_rshift_rnd(acc, s2));
-        });
-        xg_tu_sync<G>(gid);
-    }
+    constexpr int K = N > 32 ? 32 : N, LG = N == 64 ? 6 : N == 32 ? 5 : N == 16 ? 4 : N == 8 ? 3 : 2;
+    __shared__ alignas(16) uint32_t mh[K * N / 4], mv[K * N / 4];
+    __shared__ XgTuWork<N> work[CPB];
+    const int g = threadIdx.x / NT, tid = threadIdx.x % NT, c = blockIdx.y;
+    const XgTuJobPos a0 = xg_tu_job(L, pl, 0, c, N);
+    xg_tu_load_mat<N, true>(mh, xg_mat(a0.hor, LG), threadIdx.x, NT * CPB);
+    xg_tu_load_mat<N, true>(mv, xg_mat(a0.ver, LG), threadIdx.x, NT * CPB);
+    __syncthreads();
+    const int cu = blockIdx.x * CPB + g;
+    if (cu >= L.ncu) return;               /* no CTA-wide barrier follows */
+    const XgTuJobPos a = xg_tu_job(L, pl, cu, c, N);
+    XgTuWork<N> &w = work[g];
+    const int16_t *src = L.resid[pl] + (size_t)a.py * a.pw + a.px;
+    for (int o = tid; o < N * N; o += NT) { const int y = o >> LG, x = o & (N - 1); w.a[xg_d2<N>(y, x)] = src[(size_t)y * a.pw + x]; }
+    xg_gsync<NT, CPB>(g);
+    const int s1 = LG + XG_BITDEPTH + 6 - 15, s2 = LG + 6;
+    /* rows: t1(y, k) = sum_x r(y, x) Th(k, x) */
+    xg_mm_dp2<N, K, N, NT>(tid, reinterpret_cast<const uint32_t *>(w.a), mh, [&](int y, int k, int acc) {
+        w.b[xg_d2<K>(k, y)] = (int16_t)xg_clip16(xg_rshift_rnd(acc, s1));
+    });
+    xg_gsync<NT, CPB>(g);
+    xg_coef *dst = L.T[pl] + (size_t)c * L.cstride + (size_t)a.py * a.pw + a.px;
+    /* columns: t(kv, kh) = sum_y t1(y, kh) Tv(kv, y), stored along kh */
+    xg_mm_dp2<K, K, N, NT, true>(tid, reinterpret_cast<const uint32_t *>(w.b), mv, [&](int kh, int kv, int acc) {
+        dst[(size_t)kv * a.pw + kh] = (xg_coef)xg_clip16(xg_rshift_rnd(acc, s2));
+    });
 }
 
-template <int G>
-__global__ void __launch_bounds__(256) k_tu_inv(XgTuLevel L, int pl)
+/* Inverse transforms (Xin266IDctWxH, h266_inverse_trans.c:117-229: columns, then
+ * rows; a skipped column line contributes zero, so its coefficients are loaded
+ * as zeros), reconstruction from prediction = input - residual, SSD per block;
+ * the DCT2 candidate's levels and reconstruction go to the picture's planes. */
+template <int N, int NT, int CPB>
+__global__ void __launch_bounds__(NT * CPB) k_tu_inv(XgTuLevel L, int pl)
 {
-    extern __shared__ uint32_t tsw[];
-    constexpr int NG = 256 / G;
-    const int gid = threadIdx.x / G, t = threadIdx.x % G;
-    const int n = pl ? L.S >> 1 : L.S, k = n > 32 ? 32 : n;
-    int16_t *rr = (int16_t *)tsw + gid * (k * k + k * n), *t2 = rr + k * k;
-    __shared__ unsigned long long ssd_g[NG];
-    const int njobs = L.ncu * (pl ? 1 : L.nc);
-    for (int j = blockIdx.x * NG + gid; j < njobs; j += gridDim.x * NG) {
-        const XgTuJobPos a = xg_tu_job(L, pl, j);
-        const size_t off = (size_t)a.py * a.pw + a.px;
-        const xg_coef *rin = L.R[pl] + (size_t)a.c * L.cstride + off;
-        for (int o = t; o < k * k; o += G) { const int y = o / k, x = o - y * k; rr[o] = (int16_t)rin[(size_t)y * a.pw + x]; }
-        if (t == 0) ssd_g[gid] = 0;
-        if (a.c == 0) {   /* the DCT2 candidate's levels to the picture's output plane */
-            const xg_coef *qin = L.Q[pl] + off;
-            for (int o = t; o < n * n; o += G) {
-                const int y = o >> a.lg, x = o & (n - 1);
-                L.qout[pl][off + (size_t)y * a.pw + x] = qin[(size_t)y * a.pw + x];
-            }
-        }
-        xg_tu_sync<G>(gid);
-        /* Xin266IDctWxH (h266_inverse_trans.c:117-229): columns j < jmax, then rows */
-        const int16_t *mh = xg_mat(a.hor, a.lg), *mv = xg_mat(a.ver, a.lg);
-        const int sline = (a.hor != 0 && n == 32) ? 16 : (n > 32 ? n - 32 : 0), jmax = n - sline;
-        const int s2 = 6 + 15 - 1 - XG_BITDEPTH;
-        xg_mm_rt<G>(t, jmax, n, k, rr, 1, k, mv, 1, n, [&](int jc, int y, int acc) {
-            t2[jc * n + y] = (int16_t)xg_clip16(xg_rshift_rnd(acc, 7));
-        });
-        xg_tu_sync<G>(gid);
-        const int16_t *res = L.resid[pl] + off;
-        const xg_pix *org = L.org[pl] + (size_t)a.py * L.opitch[pl] + a.px;
-        xg_pix *rec = L.recout[pl] + off;
-        unsigned long long part = 0;
-        xg_mm_rt<G>(t, n, n, jmax, t2, 1, n, mh, 1, n, [&](int y, int x, int acc) {
-            const int o = (int)org[(size_t)y * L.opitch[pl] + x];
-            const int pred = o - (int)res[(size_t)y * a.pw + x];
-            const int v = xg_clip_pix(pred + xg_clip16(xg_rshift_rnd(acc, s2)));
-            if (a.c == 0) rec[(size_t)y * a.pw + x] = (xg_pix)v;
-            part += (unsigned long long)((o - v) * (o - v));
-        });
-        atomicAdd(&ssd_g[gid], part);
-        xg_tu_sync<G>(gid);
-        if (t == 0) L.ssd[L.blk[pl] + j] = ssd_g[gid];
+    constexpr int K = N > 32 ? 32 : N, LG = N == 64 ? 6 : N == 32 ? 5 : N == 16 ? 4 : N == 8 ? 3 : 2;
+    __shared__ alignas(16) uint32_t mv[K * N / 4], mh[K * N / 4];
+    __shared__ XgTuWork<N> work[CPB];
+    __shared__ unsigned long long ssd_g[CPB];
+    const int g = threadIdx.x / NT, tid = threadIdx.x % NT, c = blockIdx.y;
+    const XgTuJobPos a0 = xg_tu_job(L, pl, 0, c, N);
+    xg_tu_load_mat<N, false>(mv, xg_mat(a0.ver, LG), threadIdx.x, NT * CPB);
+    xg_tu_load_mat<N, false>(mh, xg_mat(a0.hor, LG), threadIdx.x, NT * CPB);
+    if (threadIdx.x < CPB) ssd_g[threadIdx.x] = 0;
+    __syncthreads();
+    const int cu = blockIdx.x * CPB + g;
+    if (cu >= L.ncu) return;
+    const XgTuJobPos a = xg_tu_job(L, pl, cu, c, N);
+    XgTuWork<N> &w = work[g];
+    const size_t off = (size_t)a.py * a.pw + a.px;
+    const int sline = (a.hor != 0 && N == 32) ? 16 : (N > 32 ? N - 32 : 0), jmax = N - sline;
+    const xg_coef *rin = L.R[pl] + (size_t)c * L.cstride + off;
+    for (int o = tid; o < K * K; o += NT) {
+        const int kv = o / K, kh = o - kv * K;
+        w.a[xg_d2<K>(kh, kv)] = kh < jmax ? (int16_t)rin[(size_t)kv * a.pw + kh] : (int16_t)0;
     }
+    if (c == 0) {
+        const xg_coef *qin = L.Q[pl] + off;
+        for (int o = tid; o < N * N; o += NT) {
+            const int y = o >> LG, x = o & (N - 1);
+            L.qout[pl][off + (size_t)y * a.pw + x] = qin[(size_t)y * a.pw + x];
+        }
+    }
+    xg_gsync<NT, CPB>(g);
+    /* columns: t2(kh, y) = sum_kv c(kv, kh) Tv(kv, y) */
+    xg_mm_dp2<K, N, K, NT>(tid, reinterpret_cast<const uint32_t *>(w.a), mv, [&](int kh, int y, int acc) {
+        w.b[xg_d2<N>(y, kh)] = (int16_t)xg_clip16(xg_rshift_rnd(acc, 7));
+    });
+    xg_gsync<NT, CPB>(g);
+    const int s2 = 6 + 15 - 1 - XG_BITDEPTH;
+    const int16_t *res = L.resid[pl] + off;
+    const xg_pix *org = L.org[pl] + (size_t)a.py * L.opitch[pl] + a.px;
+    xg_pix *rec = L.recout[pl] + off;
+    unsigned part = 0;
+    /* rows: r'(y, x) = sum_kh t2(kh, y) Th(kh, x) */
+    xg_mm_dp2<N, N, K, NT>(tid, reinterpret_cast<const uint32_t *>(w.b), mh, [&](int y, int x, int acc) {
+        const int o = (int)org[(size_t)y * L.opitch[pl] + x];
+        const int v = xg_clip_pix(o - (int)res[(size_t)y * a.pw + x] + xg_clip16(xg_rshift_rnd(acc, s2)));
+        if (c == 0) rec[(size_t)y * a.pw + x] = (xg_pix)v;
+        part += (unsigned)((o - v) * (o - v));
+    });
+    /* a thread holds at most ceil(N * N / NT) squared differences below 2^(2 bitdepth):
+     * 32 lanes' sum fits 32 bits */
+    static_assert((unsigned long long)((N * N + NT - 1) / NT) * 32 * ((1ull << XG_BITDEPTH) - 1) * ((1ull << XG_BITDEPTH) - 1) <
+                      (1ull << 32), "warp SSD sum fits 32 bits");
+    const unsigned wsum = __reduce_add_sync(0xffffffffu, part);
+    if ((tid & 31) == 0) atomicAdd(&ssd_g[g], (unsigned long long)wsum);
+    xg_gsync<NT, CPB>(g);
+    if (tid == 0) L.ssd[L.blk[pl] + cu * (pl ? 1 : L.nc) + c] = ssd_g[g];
 }
 
 /* 8x8 Hadamard SATD (HM normalisation, as XinGpuComputeSatd) of the luma
@@ -205,11 +237,6 @@ __global__ void k_tu_setqp(xin_gpu_dq_block *jobs, int n, const XgPicParams *pp)
 /* ------------------------------------------------------------------ host */
 
 static int16_t *xg_tu_resid(XgTuState *u, int level, int plane) { return u->resid + u->res_off[level][plane]; }
-
-static int xg_tu_group(int n) { return n >= 64 ? 256 : n >= 32 ? 128 : n >= 16 ? 64 : 32; }
-
-static size_t xg_tu_smem_fwd(int n, int G) { const int k = n > 32 ? 32 : n; return (size_t)(256 / G) * (n * n + n * k) * 2; }
-static size_t xg_tu_smem_inv(int n, int G) { const int k = n > 32 ? 32 : n; return (size_t)(256 / G) * (k * k + k * n) * 2; }
 
 /* device bytes of the TU stage for cfg (beside the stream's own) */
 static uint64_t xg_tu_bytes(const xin_gpu_stream_cfg *c)
@@ -314,36 +341,28 @@ static int xg_tu_open(xin_gpu_stream *s)
     }
     int st = xin_gpu_dq_plan_create(blocks.data(), nblk, coef, 1, &u->plan);
     if (st) { xg_tu_free(u); return st; }
-    /* the kernels' shared-memory limits, once for the largest layout */
-    static std::once_flag attr_once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(attr_once, [] {
-        const int lim = (int)xg_tu_smem_fwd(64, 256);
-        attr_err = cudaFuncSetAttribute(k_tu_fwd<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        if (attr_err == cudaSuccess) attr_err = cudaFuncSetAttribute(k_tu_inv<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-    });
-    if (xg_cuda_check(attr_err, "TU stage smem attribute")) { xg_tu_free(u); return XIN_GPU_ERR_CUDA; }
     s->tu = u;
     return XIN_GPU_OK;
 }
 
-template <int G>
-static void xg_tu_launch_pair(const XgTuLevel &lv, int pl, int n, bool fwd, cudaStream_t st)
+template <int N, int NT, int CPB>
+static void xg_tu_launch_n(const XgTuLevel &lv, int pl, bool fwd, cudaStream_t st)
 {
-    const int jobs = lv.ncu * (pl ? 1 : lv.nc), ng = 256 / G;
-    const int grid = std::max(1, std::min((jobs + ng - 1) / ng, 152 * 8));
-    if (fwd) k_tu_fwd<G><<<grid, 256, xg_tu_smem_fwd(n, G), st>>>(lv, pl);
-    else k_tu_inv<G><<<grid, 256, xg_tu_smem_inv(n, G), st>>>(lv, pl);
+    const dim3 grid((lv.ncu + CPB - 1) / CPB, pl ? 1 : lv.nc);
+    if (fwd) k_tu_fwd<N, NT, CPB><<<grid, NT * CPB, 0, st>>>(lv, pl);
+    else k_tu_inv<N, NT, CPB><<<grid, NT * CPB, 0, st>>>(lv, pl);
 }
 
+/* block size N of plane pl: a 128-thread CTA per block from 32 up, a warp per
+ * block and four blocks a CTA below (the shapes of the CU tails) */
 static void xg_tu_launch(const XgTuLevel &lv, int pl, bool fwd, cudaStream_t st)
 {
-    const int n = pl ? lv.S >> 1 : lv.S;
-    switch (xg_tu_group(n)) {
-    case 256: xg_tu_launch_pair<256>(lv, pl, n, fwd, st); break;
-    case 128: xg_tu_launch_pair<128>(lv, pl, n, fwd, st); break;
-    case 64: xg_tu_launch_pair<64>(lv, pl, n, fwd, st); break;
-    default: xg_tu_launch_pair<32>(lv, pl, n, fwd, st); break;
+    switch (pl ? lv.S >> 1 : lv.S) {
+    case 64: xg_tu_launch_n<64, 128, 1>(lv, pl, fwd, st); break;
+    case 32: xg_tu_launch_n<32, 128, 1>(lv, pl, fwd, st); break;
+    case 16: xg_tu_launch_n<16, 32, 4>(lv, pl, fwd, st); break;
+    case 8: xg_tu_launch_n<8, 32, 4>(lv, pl, fwd, st); break;
+    default: xg_tu_launch_n<4, 32, 4>(lv, pl, fwd, st); break;
     }
 }
 

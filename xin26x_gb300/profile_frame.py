@@ -32,6 +32,8 @@ def main():
     ap.add_argument("--octaves", type=int, default=1)
     ap.add_argument("--input-bitdepth", type=int, default=0)
     ap.add_argument("--search-mode", type=int, default=0, help="0 exhaustive, 1 by resolution levels")
+    ap.add_argument("--tu-mode", type=int, default=0, help="1: the preset-4 TU work (transform candidates, trellis)")
+    ap.add_argument("--qp", type=int, default=32)
     a = ap.parse_args()
     import torch
     lib = _lib.load(a.bitdepth)
@@ -40,7 +42,8 @@ def main():
                          objects=a.objects, octaves=a.octaves)
     dev = [tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f) for f in seq]
     mask = sum(int(s) for s in a.levels.split(","))
-    cfg = _lib.xin_gpu_stream_cfg(a.width, a.height, a.ctu, a.search, mask, 0, 1, 1, a.input_bitdepth, a.search_mode)
+    cfg = _lib.xin_gpu_stream_cfg(a.width, a.height, a.ctu, a.search, mask, 0, 1, 1, a.input_bitdepth, a.search_mode,
+                                  a.tu_mode)
     h = C.c_void_p()
     if lib.xin_gpu_stream_open(C.byref(cfg), C.byref(h)) != 0:
         raise RuntimeError(lib.xin_gpu_last_error().decode())
@@ -51,7 +54,7 @@ def main():
         for i, t in enumerate(dev[k % len(dev)]):
             pic.plane[i] = t.data_ptr()
             pic.stride[i] = t.shape[1]
-        pic.qp = pic.uv_qp = 32
+        pic.qp = pic.uv_qp = a.qp
         pic.sad_lambda = 64 if a.bitdepth == 8 else 256
         assert lib.xin_gpu_frame_submit(h, C.byref(pic)) == 0, lib.xin_gpu_last_error()
         assert lib.xin_gpu_frame_wait(h, C.byref(res), -1) == 0, lib.xin_gpu_last_error()
@@ -62,6 +65,7 @@ def main():
     lib.xin_gpu_stream_close(h)
     s = np.array(stages)
     print(json.dumps({"frames": a.frames, "size": [a.width, a.height], "search": a.search, "search_mode": a.search_mode,
+                      "tu_mode": a.tu_mode, "qp": a.qp,
                       "bitdepth": a.bitdepth,
                       "input_bitdepth": a.input_bitdepth or a.bitdepth,
                       "ctu": a.ctu, "mpix_s": a.width * a.height / float(np.median(s[:, 4])) / 1e3,
