@@ -290,6 +290,11 @@ k_dq_prep(const xin_gpu_dq_block *__restrict__ jobs, int njobs, const uint32_t *
 {
     const int lane = threadIdx.x & 31;
     const int nw = gridDim.x * (blockDim.x >> 5);
+    /* bucket counts of this CTA's blocks, added to the global ones once at the end
+     * (one global atomic per bucket and CTA instead of one per block) */
+    __shared__ int hist[66];
+    for (int b = threadIdx.x; b < 66; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
     for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < njobs; i += nw) {
         const xin_gpu_dq_block jb = jobs[i];
         const int lgw = jb.log2_w, lgh = jb.log2_h, ew = min(1 << lgw, 32), eh = min(1 << lgh, 32), n = ew * eh;
@@ -315,10 +320,13 @@ k_dq_prep(const xin_gpu_dq_block *__restrict__ jobs, int njobs, const uint32_t *
         }
         if (lane == 0) {
             first_out[i] = best;
-            atomicAdd(&counts[best < 0 ? 0 : (best >> 4) + 1], 1);
+            atomicAdd(&hist[best < 0 ? 0 : (best >> 4) + 1], 1);
             if (best < 0) nzout[i] = 0;
         }
     }
+    __syncthreads();
+    for (int b = threadIdx.x; b < 66; b += blockDim.x)
+        if (hist[b]) atomicAdd(&counts[b], hist[b]);
 }
 
 /* ---- pass 2: order the blocks longest first (bucket 65 .. 1), then the empty ones */
@@ -332,9 +340,18 @@ __global__ void k_dq_order(int njobs, const int32_t *__restrict__ first, const i
         off[0] = acc;
     }
     __syncthreads();
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < njobs; i += gridDim.x * blockDim.x) {
-        const int b = first[i] < 0 ? 0 : (first[i] >> 4) + 1;
-        order[off[b] + atomicAdd(&cursor[b], 1)] = i;
+    /* whole warps walk the list (inactive lanes past the end), so that the lanes
+     * of one bucket take their places with one atomic: the leader reserves them */
+    const int lane = threadIdx.x & 31;
+    for (int i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31); i0 < njobs; i0 += gridDim.x * blockDim.x) {
+        const int i = i0 + lane;
+        const int b = i < njobs ? (first[i] < 0 ? 0 : (first[i] >> 4) + 1) : 66;
+        const unsigned peers = __match_any_sync(0xffffffffu, b);
+        const int leader = __ffs(peers) - 1, rank = __popc(peers & ((1u << lane) - 1));
+        int base = 0;
+        if (lane == leader && b < 66) base = atomicAdd(&cursor[b], __popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (b < 66) order[off[b] + base + rank] = i;
     }
 }
 
