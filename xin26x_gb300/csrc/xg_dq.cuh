@@ -7,31 +7,33 @@
  *
  * Work split.  A block is walked coefficient by coefficient in reverse scan
  * order; at each coefficient four quantiser states each keep the cheapest path
- * that ends in them.  One quad of lanes owns one block, lane s owning state s,
- * so a warp runs eight blocks side by side.  Per coefficient every lane prices
- * the three candidates its state offers (level A, level B, zero), the quad
- * swaps them with two shuffle exchanges, and lane t keeps the cheapest path
- * into state t (the fixed transition pattern of the reference: 0->{0,2},
- * 1->{2,0}, 2->{1,3}, 3->{3,1}, plus "skip this sub-block" and "start here").
+ * that ends in them.  The transitions of the reference (0->{0,2}, 1->{2,0},
+ * 2->{1,3}, 3->{3,1}, plus "skip this sub-block" and "start here") give
+ * targets 0 and 2 their candidates from states 0 and 1 only, and targets 1
+ * and 3 from states 2 and 3 only.  So two lanes own a block: lane h holds
+ * states 2h and 2h + 1, prices their three candidates each (level A, level B,
+ * zero), decides targets h and h + 2 and builds their new states with no
+ * exchange; at the end of the step the lanes swap one state each.  A warp
+ * runs 16 blocks side by side.
  *
  * State layout.  The reference copies a 48-byte template (levels and
  * neighbour sums) and a per-path copy of every earlier sub-block's levels with
- * each transition.  Here a state carries only the 16 levels of its current
- * sub-block (four registers, clipped like the reference's bytes) and their
- * parities; the neighbour sums at a position are recomputed from those levels
- * plus the outside-neighbour template that was built when the sub-block was
- * entered.  Earlier sub-blocks are kept once per (sub-block, state) in a
- * 16-slot ring in shared memory (the farthest right / below neighbour of a
- * 4x4 sub-block in a 32x32 diagonal scan is 15 sub-blocks away); a path's
- * sub-block context is a 64-bit significance map plus a 2-bit state tag per
- * ring slot.  The decisions (one byte per state) and the quantisation index of
- * each position go to a per-quad scratch area in global memory; after the
- * trellis, lane 0 of the quad walks them back and dequantises along the state
- * machine.
+ * each transition.  Here a state carries the 16 levels of its current
+ * sub-block (four words of bytes, clipped like the reference's bytes) and the
+ * same levels capped at 4 or 5 by parity (the values the neighbour sums
+ * take); the neighbour sums at a position are byte dot products of those words
+ * with the position's inside-neighbour mask, plus the outside-neighbour
+ * template built when the sub-block was entered.  Earlier sub-blocks are kept
+ * once per (sub-block, state) in a 16-slot ring (the farthest right / below
+ * neighbour of a 4x4 sub-block in a 32x32 diagonal scan is 15 sub-blocks
+ * away); a path's sub-block context is a 64-bit significance map plus a 2-bit
+ * state tag per ring slot.  The decisions (one byte per state) go to a
+ * per-block scratch column in global memory; after the trellis one lane
+ * walks them back and dequantises along the state machine.
  *
- * The sub-block steps of all quads in a warp are phase aligned (each quad
- * starts at the top of the sub-block holding its last significant position),
- * so the sub-block boundary work never diverges within a warp.
+ * The blocks of a warp come from one length bucket, so every thread is at
+ * the same position of its current sub-block at every step: the sub-block
+ * boundary work never diverges within a warp.
  */
 #ifndef XG_DQ_CUH
 #define XG_DQ_CUH
@@ -40,10 +42,12 @@
 #include <mutex>
 #include <vector>
 
-#define XG_DQ_QUADS    32                       /* blocks per CTA (4 warps x 8 quads) */
-#define XG_DQ_THREADS  (XG_DQ_QUADS * 4)
+#define XG_DQ_THREADS  128                      /* trellis threads per CTA: 64 blocks, two lanes each */
 #define XG_DQ_MAXN     1024                     /* coefficients of the 32x32 region */
-#define XG_DQ_SCR_WORDS (XG_DQ_MAXN + XG_DQ_MAXN / 2)   /* per quad: decisions (u32) + indices (u16) */
+#define XG_DQ_RSETS    16                       /* context sets whose rate tables are staged in shared memory */
+#define XG_DQ_MAX_CTAS (152 * 2)                /* trellis CTAs of a run at most (GB300: 152 SMs): two per SM; a third
+                                                   lengthens the longest trellises more than it adds */
+#define XG_DQ_SLOT_BYTES (XG_DQ_MAXN * 4 + 64 * 16) /* per trellis lane pair: decisions and ring */
 #define XG_DQ_INF      ((long long)((((unsigned long long)1 << 63) - 1) >> 1))
 #define XG_DQ_REG_BINS 28
 
@@ -65,12 +69,32 @@ struct XgDqRates {              /* per (context set, luma / chroma), 1/32768-bit
     uint32_t gtx[21][6];
 };
 
+/* last-position rates per (context set, luma / chroma, x / y, log2 size - 2, position) */
+#define XG_DQ_LAST_WORDS (2 * 2 * 5 * 32)
+
 __constant__ uint32_t c_dq_frac[256][2];        /* bits of a bin at probability state (p0 + p1) >> 8 */
 __constant__ int32_t  c_dq_shape_off[16];       /* start of each region shape in the scan tables */
+__constant__ uint4    c_dq_inm[16];             /* byte masks of the inside neighbours of 4x4 scan position i */
+
+/* the 4x4 up-right diagonal scan (h266_encoder/source/h266_scan_order.c:44-81):
+ * column and row of scan index i, and the scan index of (x, y) */
+__host__ __device__ constexpr int xg_dq_s4x(int i) { return (int)((0x3323213210210100ull >> (4 * i)) & 15); }
+__host__ __device__ constexpr int xg_dq_s4y(int i) { return (int)((0x3231230123012010ull >> (4 * i)) & 15); }
+__host__ __device__ constexpr int xg_dq_s4i(int x, int y)
+{
+    int r = -1;
+    for (int i = 0; i < 16; i++)
+        if (xg_dq_s4x(i) == x && xg_dq_s4y(i) == y) r = i;
+    return r;
+}
+/* the neighbour template of a position: (x+1, y), (x+2, y), (x+1, y+1), (x, y+1), (x, y+2) */
+__host__ __device__ constexpr int xg_dq_ndx(int u) { return u == 0 || u == 2 ? 1 : u == 1 ? 2 : 0; }
+__host__ __device__ constexpr int xg_dq_ndy(int u) { return u < 2 ? 0 : u == 4 ? 2 : 1; }
 
 struct XgDqTables {
-    uint2 *d_step;              /* per shape, per scan index: position, type, inside neighbours */
-    uint4 *d_tpl;               /* per shape, per scan index: outside neighbours */
+    uint2 *d_step;              /* per shape, per scan index: position, type, sub-block, context offsets */
+    uint32_t *d_sbn;            /* per shape, per sub-block: scan indices of its right, below and
+                                   below-right neighbours (bytes 0..2, 255 = none) */
     XgDqParam *d_par;           /* [lg w + lg h - 4][QP 0..51] */
     bool ok;
 };
@@ -137,31 +161,23 @@ static void xg_dq_init_tables(void)
         frac[s][1] = (uint32_t)floor(-log2(p1) * 32768.0 + 0.5);
     }
     std::vector<uint2> step;
-    std::vector<uint4> tpl;
+    std::vector<uint32_t> sbn;
     int32_t off[16];
-    static const int dx[5] = { 1, 2, 1, 0, 0 }, dy[5] = { 0, 0, 1, 1, 2 };
     for (int sh = 0; sh < 16; sh++) {
         int ew = 4 << (sh >> 2), eh = 4 << (sh & 3), n = ew * eh, ws = ew >> 2, hs = eh >> 2;
         off[sh] = (int32_t)step.size();
         std::vector<int> cx, cy, gx, gy;
         xg_dq_diag(4, 4, cx, cy);
         xg_dq_diag(ws, hs, gx, gy);
-        std::vector<int> px(n), py(n), sid(n);
-        for (int b = 0; b < ws * hs; b++)
-            for (int i = 0; i < 16; i++) {
-                int k = b * 16 + i;
-                px[k] = gx[b] * 4 + cx[i]; py[k] = gy[b] * 4 + cy[i];
-                sid[py[k] * ew + px[k]] = k;
-            }
+        for (int i = 0; i < 16; i++)
+            if (cx[i] != xg_dq_s4x(i) || cy[i] != xg_dq_s4y(i)) return;     /* the device's 4x4 scan constants */
+        std::vector<int> px(n), py(n), sbs(ws * hs);
+        for (int b = 0; b < ws * hs; b++) {
+            sbs[gy[b] * ws + gx[b]] = b;
+            for (int i = 0; i < 16; i++) { px[b * 16 + i] = gx[b] * 4 + cx[i]; py[b * 16 + i] = gy[b] * 4 + cy[i]; }
+        }
         for (int k = 0; k < n; k++) {
-            int beg = k & ~15, in = k & 15;
-            int ins[5], outs[5], ni = 0, no = 0;
-            for (int j = 0; j < 5; j++) {
-                int x = px[k] + dx[j], y = py[k] + dy[j];
-                if (x >= ew || y >= eh) continue;
-                int q = sid[y * ew + x];
-                if (q < beg + 16) ins[ni++] = q - beg; else outs[no++] = q;
-            }
+            int in = k & 15;
             int ptype = (in == 15 && k > 16 && k < n - 1) ? 1 : (in == 0 && k > 0 && k < n - 16) ? 2 : 0;
             int braster = gy[k >> 4] * ws + gx[k >> 4];
             /* significance / gtx context offsets of the position's diagonal, luma and chroma
@@ -170,29 +186,38 @@ static void xg_dq_init_tables(void)
             const uint32_t ls = dg < 2 ? 2 : dg < 5 ? 1 : 0, lg = dg < 1 ? 3 : dg < 3 ? 2 : dg < 10 ? 1 : 0;
             const uint32_t cs = dg < 2 ? 1 : 0, cg = dg < 1 ? 1 : 0;
             uint2 e;
-            e.x = (uint32_t)px[k] | (uint32_t)py[k] << 5 | (uint32_t)ptype << 10 | (uint32_t)ni << 12 | (uint32_t)braster << 15 |
+            e.x = (uint32_t)px[k] | (uint32_t)py[k] << 5 | (uint32_t)ptype << 10 | (uint32_t)braster << 15 |
                   ls << 21 | lg << 23 | cs << 25 | cg << 26;
             e.y = 0;
-            for (int j = 0; j < ni; j++) e.y |= (uint32_t)ins[j] << (4 * j);
             step.push_back(e);
-            uint32_t nb[5] = { 0, 0, 0, 0, 0 };
-            for (int j = 0; j < no; j++) {
-                int sb = outs[j] >> 4;
-                nb[j] = (uint32_t)sb | (uint32_t)(outs[j] & 15) << 6 | (uint32_t)(gy[sb] * ws + gx[sb]) << 10;
-            }
-            tpl.push_back(make_uint4((uint32_t)no | nb[0] << 16, nb[1] | nb[2] << 16, nb[3] | nb[4] << 16, 0));
         }
+        for (int b = 0; b < ws * hs; b++) {
+            uint32_t r = gx[b] + 1 < ws ? (uint32_t)sbs[gy[b] * ws + gx[b] + 1] : 255u;
+            uint32_t d = gy[b] + 1 < hs ? (uint32_t)sbs[(gy[b] + 1) * ws + gx[b]] : 255u;
+            uint32_t rd = r != 255u && d != 255u ? (uint32_t)sbs[(gy[b] + 1) * ws + gx[b] + 1] : 255u;
+            sbn.push_back(r | d << 8 | rd << 16);
+        }
+    }
+    uint4 inm[16];
+    for (int i = 0; i < 16; i++) {
+        uint32_t m[4] = { 0, 0, 0, 0 };
+        for (int u = 0; u < 5; u++) {
+            int x = xg_dq_s4x(i) + xg_dq_ndx(u), y = xg_dq_s4y(i) + xg_dq_ndy(u);
+            if (x < 4 && y < 4) { int j = xg_dq_s4i(x, y); m[j >> 2] |= 255u << (8 * (j & 3)); }
+        }
+        inm[i] = make_uint4(m[0], m[1], m[2], m[3]);
     }
     std::vector<XgDqParam> par(9 * 52);
     for (int lg = 4; lg <= 12; lg++)
         for (int qp = 0; qp < 52; qp++) xg_dq_param(qp, lg, &par[(lg - 4) * 52 + qp]);
     if (xg_cuda_check(cudaMemcpyToSymbol(c_dq_frac, frac, sizeof frac), "dq tables") ||
         xg_cuda_check(cudaMemcpyToSymbol(c_dq_shape_off, off, sizeof off), "dq tables") ||
+        xg_cuda_check(cudaMemcpyToSymbol(c_dq_inm, inm, sizeof inm), "dq tables") ||
         xg_cuda_check(cudaMalloc(&g_dq.d_step, step.size() * sizeof(uint2)), "dq tables") ||
-        xg_cuda_check(cudaMalloc(&g_dq.d_tpl, tpl.size() * sizeof(uint4)), "dq tables") ||
+        xg_cuda_check(cudaMalloc(&g_dq.d_sbn, sbn.size() * sizeof(uint32_t)), "dq tables") ||
         xg_cuda_check(cudaMalloc(&g_dq.d_par, par.size() * sizeof(XgDqParam)), "dq tables") ||
         xg_cuda_check(cudaMemcpy(g_dq.d_step, step.data(), step.size() * sizeof(uint2), cudaMemcpyHostToDevice), "dq tables") ||
-        xg_cuda_check(cudaMemcpy(g_dq.d_tpl, tpl.data(), tpl.size() * sizeof(uint4), cudaMemcpyHostToDevice), "dq tables") ||
+        xg_cuda_check(cudaMemcpy(g_dq.d_sbn, sbn.data(), sbn.size() * sizeof(uint32_t), cudaMemcpyHostToDevice), "dq tables") ||
         xg_cuda_check(cudaMemcpy(g_dq.d_par, par.data(), par.size() * sizeof(XgDqParam), cudaMemcpyHostToDevice), "dq tables"))
         return;
     g_dq.ok = true;
@@ -215,10 +240,40 @@ __device__ __forceinline__ const uint32_t *xg_dq_bits(const xin_gpu_prob *ctx, i
 /* Xin266SetSigSbbFracBits / SetSigFlagBits / SetGtxFlagBits (h266_dep_quant.c:116-206)
  * for every context set and both channel types; one CTA per set.  The chroma
  * greater-than-1 / greater-than-2 rates come from the luma contexts, as in the
- * reference (:172-173). */
-__global__ void k_dq_rates(const xin_gpu_prob *__restrict__ sets, XgDqRates *__restrict__ out)
+ * reference (:172-173).  Also the rates of the last position
+ * (Xin266SetLastCoeffOffset, :208-283) per channel type, coordinate and block
+ * side, without the coded-block-flag term of the y table (added per block). */
+__global__ void k_dq_rates(const xin_gpu_prob *__restrict__ sets, XgDqRates *__restrict__ out, uint32_t *__restrict__ lasts)
 {
     const xin_gpu_prob *ctx = sets + (size_t)blockIdx.x * XIN_GPU_NUM_CTX;
+    if (threadIdx.x < 20) {
+        const int ch = threadIdx.x / 10, xy = (threadIdx.x / 5) & 1, lg = 2 + threadIdx.x % 5;
+        const int luma = ch == 0, nn = min(1 << lg, 32);
+        const int shift = luma ? (lg + 1) >> 2 : min((1 << lg) >> 3, 2);
+        const int cbase = luma ? (lg == 2 ? 0 : lg == 3 ? 3 : lg == 4 ? 6 : lg == 5 ? 10 : 15) + (xy ? XG_DQC_LASTY_L : XG_DQC_LASTX_L)
+                               : (xy ? XG_DQC_LASTY_C : XG_DQC_LASTX_C);
+        const int gmax = nn - 1 < 4 ? nn - 1 : 2 * (31 - __clz(nn - 1)) + (((nn - 1) >> (30 - __clz(nn - 1))) & 1);
+        uint32_t *row = lasts + (size_t)blockIdx.x * XG_DQ_LAST_WORDS + ((ch * 2 + xy) * 5 + lg - 2) * 32;
+        uint32_t acc = 0, cbits = 0;
+        int gdone = 0;
+        /* groups in increasing order; positions map to non-decreasing groups, so one pass fills the table */
+        for (int p = 0; p < 32; p++) {
+            if (p < nn) {
+                const int g = p < 4 ? p : 2 * (31 - __clz(p)) + ((p >> (30 - __clz(p))) & 1);
+                while (gdone <= g) {
+                    const uint32_t suf = gdone > 3 ? (uint32_t)(((gdone - 2) >> 1) << 15) : 0;
+                    if (gdone == gmax) cbits = acc + suf;
+                    else {
+                        const uint32_t *b = xg_dq_bits(ctx, cbase + (gdone >> shift));
+                        cbits = acc + b[0] + suf;
+                        acc += b[1];
+                    }
+                    gdone++;
+                }
+            }
+            row[p] = p < nn ? cbits : 0u;
+        }
+    }
     for (int ch = 0; ch < 2; ch++) {
         XgDqRates *rt = out + blockIdx.x * 2 + ch;
         int nsig = ch ? 8 : 12, ngtx = ch ? 11 : 21;
@@ -249,33 +304,79 @@ __global__ void k_dq_rates(const xin_gpu_prob *__restrict__ sets, XgDqRates *__r
 
 /* ------------------------------------------------------------------ trellis */
 
-/* 16-byte aligned: the ring is written with 16-byte stores */
-struct __align__(16) XgDqQuad {
-    uint16_t tpl[4][16];            /* outside-neighbour template per sub-block context */
-    uint32_t ring[16][4][4];        /* levels of earlier sub-blocks: [slot][state][16 bytes] */
-    int32_t  last[2][32];           /* rate of the last position, x and y */
-    XgDqRates rt;                   /* the block's rate tables (its context set and channel) */
-};
-static_assert(sizeof(XgDqQuad) % 16 == 0 && offsetof(XgDqQuad, ring) % 16 == 0, "ring rows must stay 16-byte aligned");
+#define XG_DQ_PAIRS (XG_DQ_THREADS / 2)          /* blocks per CTA: one lane pair per block */
+#define XG_DQ_TPLS  (XG_DQ_PAIRS + 1)            /* template row pitch: the two lanes of a pair read
+                                                   different rows, which then fall in different banks */
 struct XgDqSmem {
-    XgDqQuad quad[XG_DQ_QUADS];
-    int32_t  rice[4][32];           /* abs_remainder bits, Rice parameter k, value n */
+    uint32_t tpl[4 * 16][XG_DQ_TPLS];      /* outside-neighbour template [state * 16 + position][pair] */
+    unsigned long long skc[4][XG_DQ_PAIRS];  /* per state: cost at the top of the current sub-block ("skip") */
+    unsigned long long cfl[4][XG_DQ_PAIRS];  /* per template owner: coded flags of the earlier sub-blocks */
+    uint32_t skp[4][XG_DQ_PAIRS];          /* per state: packed fields at the top of the current sub-block */
+    uint32_t cvr[4][XG_DQ_PAIRS];          /* per template owner: ring version (state) of each slot */
+    int32_t  rice[4][32];                  /* abs_remainder bits, Rice parameter k, value n */
+    XgDqRates rt[XG_DQ_RSETS][2];          /* rate tables of the first context sets */
 };
 
-__device__ __forceinline__ uint32_t xg_dq_byte(uint32_t l0, uint32_t l1, uint32_t l2, uint32_t l3, int j)
+/* a state's small fields in one word: remaining context-coded bins (16 bits,
+ * signed), coded levels in the current sub-block, template owner + 1, coded
+ * flag of the right / below sub-blocks */
+__device__ __forceinline__ uint32_t xg_pk(int rem, int ns, int ref, int sgb)
 {
-    uint32_t w = (j & 8) ? ((j & 4) ? l3 : l2) : ((j & 4) ? l1 : l0);
-    return (w >> ((j & 3) * 8)) & 255u;
+    return (uint32_t)(rem & 0xFFFF) | (uint32_t)ns << 16 | (uint32_t)(ref + 1) << 21 | (uint32_t)sgb << 24;
 }
+__device__ __forceinline__ int xg_pk_rem(uint32_t p) { return (int)(int16_t)(p & 0xFFFFu); }
+__device__ __forceinline__ int xg_pk_ns(uint32_t p) { return (int)((p >> 16) & 31u); }
+__device__ __forceinline__ int xg_pk_ref(uint32_t p) { return (int)((p >> 21) & 7u) - 1; }
+__device__ __forceinline__ int xg_pk_sgb(uint32_t p) { return (int)((p >> 24) & 1u); }
 
 /* Rice parameter from a neighbour sum (H.266 Table 128) */
 __device__ __forceinline__ int xg_dq_rpar(int v) { return v < 7 ? 0 : v < 14 ? 1 : v < 28 ? 2 : 3; }
 
-__device__ __forceinline__ long long xg_dq_shfl64(unsigned m, long long v, int src)
+/* byte i (a constant after unrolling) of 16 bytes */
+__device__ __forceinline__ uint32_t xg_dq_byte16(const uint4 &w, int i)
 {
-    int lo = __shfl_sync(m, (int)(unsigned long long)v, src, 4);
-    int hi = __shfl_sync(m, (int)((unsigned long long)v >> 32), src, 4);
-    return (long long)(((unsigned long long)(unsigned)hi << 32) | (unsigned)lo);
+    const uint32_t x = i < 4 ? w.x : i < 8 ? w.y : i < 12 ? w.z : w.w;
+    return (x >> (8 * (i & 3))) & 255u;
+}
+
+/* a neighbour level's share of a template: sum | min(4 + parity, v) << 11 | (v != 0) << 16 */
+__device__ __forceinline__ uint32_t xg_dq_tplc(uint32_t v)
+{
+    return v | min(4u + (v & 1u), v) << 11 | (uint32_t)(v != 0u) << 16;
+}
+
+/* Outside-neighbour templates of the 16 positions of a sub-block (the sums
+ * Xin266UpdateStateEOS builds from earlier sub-blocks, h266_dep_quant.c:1386-1440):
+ * from the levels of its right (R), below (B) and below-right (D, first byte)
+ * neighbours, 16 bytes each in scan order and zero where the neighbour is
+ * absent or not coded.  Entry: min(sum, 127) | sum of min(4 + parity, v) << 7
+ * | count << 12. */
+__device__ __forceinline__ void xg_dq_build_tpl(const uint4 R, const uint4 B, uint32_t D, uint32_t *dst)
+{
+    uint32_t cr[2][4], cb[4][2];
+#pragma unroll
+    for (int y = 0; y < 4; y++) {
+        cr[0][y] = xg_dq_tplc(xg_dq_byte16(R, xg_dq_s4i(0, y)));
+        cr[1][y] = xg_dq_tplc(xg_dq_byte16(R, xg_dq_s4i(1, y)));
+    }
+#pragma unroll
+    for (int x = 0; x < 4; x++) {
+        cb[x][0] = xg_dq_tplc(xg_dq_byte16(B, xg_dq_s4i(x, 0)));
+        cb[x][1] = xg_dq_tplc(xg_dq_byte16(B, xg_dq_s4i(x, 1)));
+    }
+    const uint32_t cd = xg_dq_tplc(D & 255u);
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        const int x = xg_dq_s4x(j), y = xg_dq_s4y(j);
+        uint32_t acc = 0;
+#pragma unroll
+        for (int u = 0; u < 5; u++) {
+            const int nx = x + xg_dq_ndx(u), ny = y + xg_dq_ndy(u);
+            if (nx < 4 && ny < 4) continue;
+            acc += (nx >= 4 && ny >= 4) ? cd : nx >= 4 ? cr[nx - 4][ny] : cb[nx][ny - 4];
+        }
+        dst[j * XG_DQ_TPLS] = min(acc & 2047u, 127u) | ((acc >> 11) & 31u) << 7 | (acc >> 16) << 12;
+    }
 }
 
 /* ---- pass 1: per block (one warp each) gather the low 32x32 in scan order into
@@ -355,411 +456,431 @@ __global__ void k_dq_order(int njobs, const int32_t *__restrict__ first, const i
     }
 }
 
-/* ---- pass 3: the trellis.  One CTA = 4 warps x 8 quads; each warp takes the
- * next 8 blocks of the ordered list (so its quads walk the same number of
- * sub-blocks). */
-/* min blocks 1: the compiler keeps more of the step in registers (137 here),
- * which shortens the serial step; the trellis is bound by that latency, not by
- * the number of resident warps */
-__global__ void __launch_bounds__(XG_DQ_THREADS, 1)
+/* ---- pass 3: the trellis.  Two lanes per block.  The transitions pair the
+ * states: targets 0 and 2 have their candidates from states 0 and 1 only,
+ * targets 1 and 3 from states 2 and 3 only.  So lane h of a pair holds states
+ * 2h and 2h + 1, prices their candidates, decides targets h and h + 2 and
+ * builds their new states without any exchange; at the end of the step the
+ * lanes swap one state each (lane 0 gives target 2, lane 1 gives target 1), so
+ * that lane h again holds states 2h and 2h + 1.  A warp takes the next 16
+ * blocks of the ordered list: its blocks walk the same number of sub-blocks
+ * and are at the same position of a sub-block at every step. */
+
+/* one state's registers: cost, levels of its current sub-block (bytes) and the
+ * same levels capped at 4 + parity, packed small fields */
+struct XgDqState { long long cost; uint32_t pk, L[4], F[4]; };
+
+/* The new state of target t (Xin266UpdateState / Xin266UpdateStateEOS,
+ * h266_dep_quant.c:1224-1536) from this lane's states before the step:
+ * df is the source state (2h + j from local state j), -1 "start", 4 + t
+ * "skip", -2 none.  A target without a candidate (only the odd ones at the
+ * last position) keeps a cost no later candidate can win with, so its other
+ * fields do not matter.  srcref: the template owner whose sub-block context the
+ * new path continues (for the sub-block boundary). */
+__device__ __forceinline__ XgDqState xg_dq_next(const XgDqState (&S)[2], int h, int t, int df, int lvv, long long dc,
+                                                int in, int regbins, const XgDqSmem &sm, int pi, int &ns, int &srcref)
+{
+    XgDqState n;
+    const bool l1 = df == 2 * h + 1, fresh = df == -1 || df >= 4;
+    const uint32_t pp = l1 ? S[1].pk : S[0].pk;
+    const int dec = lvv < 2 ? lvv : 3;
+    int r = xg_pk_rem(pp) - 1;
+    if (r >= 4) r -= dec;
+    int nsg = xg_pk_ns(pp) + (lvv != 0), rf = xg_pk_ref(pp);
+    if (df == -1) {
+        r = regbins;
+        if (in == 0) { if (r >= 4) r -= dec; } else r -= dec;
+        nsg = 1; rf = -1;
+    } else if (df >= 4) {
+        const uint32_t sp = sm.skp[t][pi];
+        r = xg_pk_rem(sp); nsg = 0; rf = xg_pk_ref(sp);
+    }
+    ns = nsg; srcref = rf;
+    n.cost = dc;
+    n.pk = xg_pk(r, nsg, rf, xg_pk_sgb(pp));
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        n.L[i] = fresh ? 0u : l1 ? S[1].L[i] : S[0].L[i];
+        n.F[i] = fresh ? 0u : l1 ? S[1].F[i] : S[0].F[i];
+    }
+    if (df > -2 && lvv) {
+        /* the level at this position: clipped to a byte (at a sub-block's first
+         * position keeping its parity), and capped at 4 + parity; word in >> 2 by
+         * masks, not by index, so the words stay in registers */
+        const uint32_t b = in ? (uint32_t)min(lvv, 255) : (uint32_t)min(lvv, 254 + (lvv & 1));
+        const uint32_t fb = (uint32_t)min(4 + (lvv & 1), lvv);
+        const int wi = in >> 2, sh = (in & 3) * 8;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const uint32_t sel = 0u - (uint32_t)(i == wi), bm = (255u << sh) & sel;
+            n.L[i] = (n.L[i] & ~bm) | ((b << sh) & sel);
+            n.F[i] = (n.F[i] & ~bm) | ((fb << sh) & sel);
+        }
+    }
+    return n;
+}
+
+__device__ __forceinline__ long long xg_dq_shfl64x(unsigned m, long long v)
+{
+    const int lo = __shfl_xor_sync(m, (int)(unsigned long long)v, 1);
+    const int hi = __shfl_xor_sync(m, (int)((unsigned long long)v >> 32), 1);
+    return (long long)(((unsigned long long)(unsigned)hi << 32) | (unsigned)lo);
+}
+
+template <bool SHR>
+__device__ __forceinline__ void xg_dq_block(XgDqSmem &sm, int job, const xin_gpu_dq_block &jb, int first,
+                                            const uint32_t *__restrict__ soff, const xg_coef *__restrict__ tscan,
+                                            xg_coef *__restrict__ qout, xg_coef *__restrict__ rout,
+                                            unsigned long long *__restrict__ nzout, const xin_gpu_prob *__restrict__ sets,
+                                            int nsets, const XgDqRates *__restrict__ rates,
+                                            const uint32_t *__restrict__ lasts, const uint2 *__restrict__ step_tab,
+                                            const uint32_t *__restrict__ sbn_tab, const XgDqParam *__restrict__ par_tab,
+                                            uint32_t *__restrict__ codes, uint4 *__restrict__ ring, size_t NP)
+{
+    const int lane = threadIdx.x & 31, h = lane & 1, pi = threadIdx.x >> 1;
+    const unsigned pm = 3u << (lane & 30);
+    const int lgw = jb.log2_w, lgh = jb.log2_h, w = 1 << lgw, h2 = 1 << lgh;
+    const int ew = min(w, 32), eh = min(h2, 32);
+    const int shape = (min(lgw, 5) - 2) * 4 + (min(lgh, 5) - 2);
+    const uint2 *ST = step_tab + c_dq_shape_off[shape];
+    const uint32_t *SBN = sbn_tab + (c_dq_shape_off[shape] >> 4);
+    const XgDqParam P = par_tab[(lgw + lgh - 4) * 52 + jb.qp];
+    const int luma = jb.comp == 0, ch = luma ? 0 : 1;
+    /* the rate tables from shared memory when every set is staged there (the loads are
+     * then shared-memory loads, not generic ones, on the step's dependent chain) */
+    const XgDqRates *RT = SHR ? &sm.rt[jb.ctx_set][ch] : rates + jb.ctx_set * 2 + ch;
+    const xin_gpu_prob *CX = sets + (size_t)jb.ctx_set * XIN_GPU_NUM_CTX;
+    const uint32_t *LX = lasts + (size_t)jb.ctx_set * XG_DQ_LAST_WORDS + ((ch * 2 + 0) * 5 + lgw - 2) * 32;
+    const uint32_t *LY = lasts + (size_t)jb.ctx_set * XG_DQ_LAST_WORDS + ((ch * 2 + 1) * 5 + lgh - 2) * 32;
+    uint32_t cbfoff;
+    {
+        const int cc = (luma && jb.root_cbf) ? XG_DQC_ROOT_CBF : jb.comp == 0 ? XG_DQC_CBF_Y : jb.comp == 1 ? XG_DQC_CBF_U : XG_DQC_CBF_V;
+        const uint32_t *cb = xg_dq_bits(CX, cc);
+        cbfoff = cb[1] - cb[0];
+    }
+    const xg_coef *TS = tscan + soff[job];
+    uint32_t *CD = codes + (size_t)blockIdx.x * XG_DQ_PAIRS + pi;          /* decisions of position k at CD[k * NP] */
+    uint4 *RG = ring + (size_t)blockIdx.x * XG_DQ_PAIRS + pi;             /* ring row (slot, state) at RG[(slot * 4 + state) * NP] */
+    uint32_t *TP = &sm.tpl[0][pi];                                         /* template (state, position) at TP[(state * 16 + position) * TPLS] */
+    const int regbins = ew * eh * XG_DQ_REG_BINS / 16;
+    /* this lane's quantisation index classes: candidate A and B of states 2h, 2h + 1
+     * (lane 0 also prices "start" of targets 0 and 2 with classes 0 and 2) */
+    const int cA = h ? 3 : 0, cB = h ? 1 : 2;
+    const int tf = h, ts = h + 2;                 /* the targets this lane decides */
+
+    XgDqState S[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        S[j].cost = XG_DQ_INF;
+#pragma unroll
+        for (int i = 0; i < 4; i++) { S[j].L[i] = 0; S[j].F[i] = 0; }
+        S[j].pk = xg_pk(4, 0, -1, 0);
+        const int s = 2 * h + j;
+        sm.skc[s][pi] = (unsigned long long)XG_DQ_INF; sm.skp[s][pi] = xg_pk(4, 0, -1, 0);
+        sm.cfl[s][pi] = 0; sm.cvr[s][pi] = 0;
+    }
+    __syncwarp(pm);
+
+    const int top = first | 15;
+    /* loads ahead of the steps that use them: coefficient and position entry one
+     * and two steps ahead, the last-position rates of the next position */
+    auto clampk = [first](int x) { return max(min(x, first), 0); };
+    auto lastxy = [&](uint32_t e) {
+        return (long long)(int32_t)__ldg(&LX[e & 31]) + (long long)(int32_t)(__ldg(&LY[(e >> 5) & 31]) + cbfoff);
+    };
+    xg_coef cv = TS[first];
+    uint2 ce = __ldg(&ST[clampk(top)]), ce1 = __ldg(&ST[clampk(top - 1)]);
+    long long clxy = lastxy(ce.x);
+    for (int k = top; k >= 0; k--) {
+        const int in = k & 15, sb = k >> 4;
+        const xg_coef nv = TS[clampk(k - 1)];
+        const uint2 ne2 = __ldg(&ST[clampk(k - 2)]);
+        const long long nlxy = lastxy(ce1.x);
+        if (k <= first) {
+            const uint32_t ex = ce.x;
+            const int av = cv < 0 ? -(int)cv : (int)cv;
+            const int ptype = (ex >> 10) & 3;
+            const int sigoff = 4 * (int)(luma ? (ex >> 21) & 3 : (ex >> 25) & 1);
+            const int gtxoff = 1 + 5 * (int)(luma ? (ex >> 23) & 3 : (ex >> 26) & 1);
+
+            /* pre-quantisation (Xin266PreQuantCoeff, h266_dep_quant.c:920-952): for this lane's
+             * classes the level and its distortion change */
+            const long long org = (long long)av * P.qScale;
+            const long long qi = (org + P.qAdd) >> P.qShift;
+            const int q = (int)(qi < 1 ? 1 : qi > P.maxQIdx ? P.maxQIdx : qi);
+            const long long bse = (long long)((unsigned long long)q * (unsigned long long)P.distStepAdd -
+                                              (unsigned long long)org * (unsigned long long)P.distOrgFact);
+            long long dd[2];
+            int lv[2], gi[2], ri[2];
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                const int kk = ((c ? cB : cA) - q) & 3;
+                const long long m = (long long)((unsigned long long)(bse + kk * P.distStepAdd) * (unsigned long long)(long long)(q + kk));
+                dd[c] = (m + P.distAdd) >> P.distShift;
+                lv[c] = (q + kk + 1) >> 1;
+                gi[c] = lv[c] < 4 ? lv[c] : 4 + (lv[c] & 1);            /* column of the gtx rate table */
+                ri[c] = min(max((lv[c] - 4) >> 1, 0), 31);                /* Rice index of the remainder */
+            }
+
+            /* ---- candidates of this lane's states (Xin266CheckRdCosts, h266_dep_quant.c:954-1046) ---- */
+            const uint4 m = c_dq_inm[in];
+            long long caz[2], cb[2];
+            int saz[2], laz[2];
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const uint32_t spk = S[j].pk;
+                const int sref = xg_pk_ref(spk), srem = xg_pk_rem(spk);
+                const uint32_t tv = sref >= 0 ? TP[(sref * 16 + in) * XG_DQ_TPLS] : 0u;
+                uint32_t sum = tv & 127u, a1 = (tv >> 7) & 31u;
+                const uint32_t f0 = S[j].F[0] & m.x, f1 = S[j].F[1] & m.y, f2 = S[j].F[2] & m.z, f3 = S[j].F[3] & m.w;
+                sum = __dp4a(S[j].L[0] & m.x, 0x01010101u, sum);
+                sum = __dp4a(S[j].L[1] & m.y, 0x01010101u, sum);
+                sum = __dp4a(S[j].L[2] & m.z, 0x01010101u, sum);
+                sum = __dp4a(S[j].L[3] & m.w, 0x01010101u, sum);
+                a1 = __dp4a(f0, 0x01010101u, a1);
+                a1 = __dp4a(f1, 0x01010101u, a1);
+                a1 = __dp4a(f2, 0x01010101u, a1);
+                a1 = __dp4a(f3, 0x01010101u, a1);
+                /* capped levels are at most 5, so + 7 sets bit 3 of a byte exactly where it is non-zero */
+                const uint32_t nzb = ((f0 + 0x07070707u) & 0x08080808u) | ((f1 + 0x07070707u) & 0x08080808u) >> 1 |
+                                     ((f2 + 0x07070707u) & 0x08080808u) >> 2 | ((f3 + 0x07070707u) & 0x08080808u) >> 3;
+                const uint32_t cnt = (tv >> 12) + (uint32_t)__popc(nzb);
+
+                const bool rc = srem >= 4;                           /* context-coded bins left */
+                const int rice = xg_dq_rpar(rc ? min(max((int)sum - 20, 0), 31) : min((int)sum, 31));
+                const int rzero = (h ? 2 : 1) << rice;               /* read only without context-coded bins */
+                const uint2 sg = *reinterpret_cast<const uint2 *>(&RT->sig[h ? 1 + j : 0][sigoff + min((int)(a1 + 1) >> 1, 3)][0]);
+                const uint32_t *gx = RT->gtx[gtxoff + min((int)(a1 - cnt), 4)];
+                const int lvA = lv[0], lvB = lv[1];
+                const int xA = rc ? ri[0] : (lvA <= rzero ? lvA - 1 : min(lvA, 31));
+                const int xB = rc ? ri[1] : (lvB <= rzero ? lvB - 1 : min(lvB, 31));
+                const uint32_t rA = (uint32_t)sm.rice[rice][xA], rB = (uint32_t)sm.rice[rice][xB];
+                uint32_t addAB = 0, addZ = 0;
+                bool zok = true;
+                if (ptype == 1) {
+                    const uint32_t sb1 = RT->sbb[xg_pk_sgb(spk)][1];
+                    addAB = sb1 + sg.y; addZ = sb1 + sg.x;
+                } else if (ptype == 0 || xg_pk_ns(spk)) {
+                    addAB = sg.y; addZ = sg.x;
+                } else zok = !rc;
+                const uint32_t tA = rc ? gx[gi[0]] + (lvA >= 4 ? rA : 0u) + addAB : (1u << 15) + rA;
+                const uint32_t tB = rc ? gx[gi[1]] + (lvB >= 4 ? rB : 0u) + addAB : (1u << 15) + rB;
+                const uint32_t tZ = rc ? addZ : (uint32_t)sm.rice[rice][rzero];
+                const long long ca = S[j].cost + dd[0] + (long long)tA;
+                cb[j] = S[j].cost + dd[1] + (long long)tB;
+                const long long cz = S[j].cost + (long long)tZ;
+                if (!zok || ca < cz) { caz[j] = ca; saz[j] = cA; laz[j] = lvA; }
+                else                 { caz[j] = cz; saz[j] = 4;  laz[j] = 0; }
+            }
+
+            /* ---- decisions of targets tf = h (A / zero of state 2h, then B of 2h + 1) and
+             * ts = h + 2 (B of state 2h, then A / zero of 2h + 1), then "skip the
+             * sub-block" and, for targets 0 and 2, "start here" ---- */
+            long long dc[2];
+            int dfrom[2], dlv[2];
+            uint32_t code = 0;
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int t = u ? ts : tf;
+                long long c1 = u ? cb[0] : caz[0], c2 = u ? caz[1] : cb[1];
+                const int e1 = u ? cB : saz[0], e2 = u ? saz[1] : cB;
+                const int f1 = u ? 2 * h : 2 * h, f2 = 2 * h + 1;
+                const int g1 = u ? lv[1] : laz[0], g2 = u ? laz[1] : lv[1];
+                long long d = XG_DQ_INF >> 1;
+                int dsel = 7, df = -2, dl = -1;
+                if (c1 < d) { d = c1; dsel = e1; df = f1; dl = g1; }
+                if (c2 < d) { d = c2; dsel = e2; df = f2; dl = g2; }
+                if (ptype == 2) {
+                    const long long c = (long long)sm.skc[t][pi] + (long long)RT->sbb[xg_pk_sgb(sm.skp[t][pi])][0];
+                    if (c < d) { d = c; dsel = 4; df = 4 + t; dl = 0; }
+                }
+                {
+                    /* start here (the last position): targets 0 and 2 (lane 0), classes 0 and 2;
+                     * priced on both lanes so that the warp does not branch */
+                    const int c = u;
+                    const long long cs = dd[c] + clxy + (long long)RT->gtx[0][gi[c]] + (lv[c] >= 4 ? sm.rice[0][ri[c]] : 0);
+                    const bool take = (h == 0) & (cs < d);
+                    d = take ? cs : d; dsel = take ? t : dsel; df = take ? -1 : df; dl = take ? lv[c] : dl;
+                }
+                dc[u] = d; dfrom[u] = df; dlv[u] = dl;
+                code |= (uint32_t)((df + 2) | dsel << 4) << (8 * t);
+            }
+            code |= __shfl_xor_sync(pm, code, 1);
+            if (h == 0) CD[(size_t)k * NP] = code;
+
+            if (ptype == 1) {
+#pragma unroll
+                for (int j = 0; j < 2; j++) { sm.skc[2 * h + j][pi] = (unsigned long long)S[j].cost; sm.skp[2 * h + j][pi] = S[j].pk; }
+                __syncwarp(pm);
+            }
+
+            /* ---- new states of tf and ts, then the swap ---- */
+            XgDqState N[2];
+            int nns[2], srcref[2];
+            if (k > 0) {
+#pragma unroll
+                for (int u = 0; u < 2; u++)
+                    N[u] = xg_dq_next(S, h, u ? ts : tf, dfrom[u], dlv[u], dc[u], in, regbins, sm, pi, nns[u], srcref[u]);
+                if (in == 0) {
+                    /* first coefficient (in scan order) of sub-block sb: close it and open sb - 1.
+                     * The sub-block context of a new path is its predecessor's (that of the owner
+                     * of its template) plus this sub-block; its levels go to the ring. */
+                    const int slot = sb & 15;
+                    unsigned long long nfl[2];
+                    uint32_t nvr[2];
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        const int t = u ? ts : tf, cr = srcref[u];
+                        const unsigned long long fl = cr >= 0 ? sm.cfl[cr][pi] : 0ull;
+                        const uint32_t fv = cr >= 0 ? sm.cvr[cr][pi] : 0u;
+                        nfl[u] = (fl & ~(1ull << sb)) | (unsigned long long)(nns[u] != 0) << sb;
+                        nvr[u] = (fv & ~(3u << (2 * slot))) | (uint32_t)t << (2 * slot);
+                        if (dfrom[u] > -2) RG[(size_t)(slot * 4 + t) * NP] = make_uint4(N[u].L[0], N[u].L[1], N[u].L[2], N[u].L[3]);
+                    }
+                    __syncwarp(pm);                  /* both lanes' ring rows written, old contexts read */
+                    const uint32_t nb = __ldg(&SBN[sb - 1]);
+                    const int nR = nb & 255, nB = (nb >> 8) & 255, nD = (nb >> 16) & 255;
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        const int t = u ? ts : tf;
+                        if (dfrom[u] > -2) {
+                            const unsigned long long fl = nfl[u];
+                            const bool sR = nR != 255 && ((fl >> nR) & 1), sB = nB != 255 && ((fl >> nB) & 1);
+                            const bool sD = nD != 255 && ((fl >> nD) & 1);
+                            const int nsb = sR || sB;
+                            uint32_t *dst = TP + (size_t)t * 16 * XG_DQ_TPLS;
+                            if (nsb || sD) {
+                                const uint4 z = make_uint4(0, 0, 0, 0);
+                                const uint4 vR = sR ? RG[(size_t)((nR & 15) * 4 + ((nvr[u] >> (2 * (nR & 15))) & 3)) * NP] : z;
+                                const uint4 vB = sB ? RG[(size_t)((nB & 15) * 4 + ((nvr[u] >> (2 * (nB & 15))) & 3)) * NP] : z;
+                                const uint4 vD = sD ? RG[(size_t)((nD & 15) * 4 + ((nvr[u] >> (2 * (nD & 15))) & 3)) * NP] : z;
+                                xg_dq_build_tpl(vR, vB, vD.x, dst);
+                            } else {
+#pragma unroll
+                                for (int j = 0; j < 16; j++) dst[j * XG_DQ_TPLS] = 0;
+                            }
+                            N[u].pk = xg_pk(xg_pk_rem(N[u].pk), 0, t, nsb);
+                            sm.cfl[t][pi] = fl; sm.cvr[t][pi] = nvr[u];
+#pragma unroll
+                            for (int i = 0; i < 4; i++) { N[u].L[i] = 0; N[u].F[i] = 0; }
+                        }
+                    }
+                    __syncwarp(pm);                  /* templates and contexts visible to both lanes */
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < 2; u++) { N[u] = S[u]; N[u].cost = dc[u]; }
+            }
+            /* lane 0 keeps target 0 and gives target 2; lane 1 keeps target 3 and gives target 1 */
+            {
+                const XgDqState &give = h ? N[0] : N[1];
+                XgDqState got;
+                got.cost = xg_dq_shfl64x(pm, give.cost);
+                got.pk = __shfl_xor_sync(pm, give.pk, 1);
+#pragma unroll
+                for (int i = 0; i < 4; i++) { got.L[i] = __shfl_xor_sync(pm, give.L[i], 1); got.F[i] = __shfl_xor_sync(pm, give.F[i], 1); }
+                if (h) { S[0] = got; S[1] = N[1]; }
+                else   { S[0] = N[0]; S[1] = got; }
+            }
+        }
+        cv = nv; ce = ce1; ce1 = ne2; clxy = nlxy;
+    }
+
+    /* ---- best final state, then walk the decisions from position 0 up
+     * (h266_dep_quant.c:1919-1947), on lane 0.  The state a coefficient was
+     * quantised in is the source state of its decision (0 for the last
+     * position), so each level is dequantised as it is found (:1949-1989 walks
+     * the same state machine forward from the last position). */
+    const long long o0 = xg_dq_shfl64x(pm, S[0].cost), o1 = xg_dq_shfl64x(pm, S[1].cost);
+    if (h) return;
+    const long long fc[4] = { S[0].cost, S[1].cost, o0, o1 };
+    long long best = 0;
+    int st = -1;
+#pragma unroll
+    for (int s = 0; s < 4; s++)
+        if (fc[s] < best) { best = fc[s]; st = s; }
+    unsigned long long map = 0;
+    const int iqadd = 1 << (P.iqShift - 1);
+    xg_coef *QO = qout + jb.offset, *RO = rout + jb.offset;
+    const int stride = jb.stride;
+    uint32_t ncode = CD[0];
+    xg_coef nval = TS[0];
+    uint32_t nent = __ldg(&ST[0].x);
+    for (int k = 0; st >= 0 && k <= first; k++) {
+        const uint32_t c = ncode, ent = nent;
+        const int v = nval;
+        const int kn = min(k + 1, first);
+        ncode = CD[(size_t)kn * NP]; nval = TS[kn]; nent = __ldg(&ST[kn].x);
+        int lv = 0, ps = 0;
+        if (!(st >= 4 && (k & 15))) {
+            const uint32_t byte = (c >> (8 * (st & 3))) & 255u;
+            const int sel = (int)(byte >> 4), from = (int)(byte & 15) - 2;
+            const int av = v < 0 ? -v : v;
+            const long long qi = ((long long)av * P.qScale + P.qAdd) >> P.qShift;
+            const int q = (int)(qi < 1 ? 1 : qi > P.maxQIdx ? P.maxQIdx : qi);
+            lv = sel >= 4 ? 0 : (q + ((sel - q) & 3) + 1) >> 1;
+            ps = from >= 0 && from < 4 ? from : 0;
+            st = from;
+        }
+        if (lv) {
+            const int x = ent & 31, y = (ent >> 5) & 31;
+            const int qv = v < 0 ? -lv : lv;
+            const int qidx = 2 * qv + (qv > 0 ? -(ps >> 1) : (ps >> 1));
+            const int rv = (qidx * P.iqScale + iqadd) >> P.iqShift;
+            QO[y * stride + x] = (xg_coef)qv;
+            RO[y * stride + x] = (xg_coef)(rv < -32768 ? -32768 : rv > 32767 ? 32767 : rv);
+            map |= 1ull << ((ent >> 15) & 63);
+        }
+    }
+    nzout[job] = map;
+}
+
+/* min blocks 3: three CTAs of 128 threads per SM */
+__global__ void __launch_bounds__(XG_DQ_THREADS, 3)
 k_dq(const xin_gpu_dq_block *__restrict__ jobs, int njobs, int *__restrict__ counter, const int *__restrict__ counts,
      const int32_t *__restrict__ order, const int32_t *__restrict__ firsts, const uint32_t *__restrict__ soff,
      const xg_coef *__restrict__ tscan, xg_coef *__restrict__ qout, xg_coef *__restrict__ rout,
-     unsigned long long *__restrict__ nzout, const xin_gpu_prob *__restrict__ sets,
-     const XgDqRates *__restrict__ rates, const uint2 *__restrict__ step_tab, const uint4 *__restrict__ tpl_tab,
-     const XgDqParam *__restrict__ par_tab, uint32_t *__restrict__ scratch)
+     unsigned long long *__restrict__ nzout, const xin_gpu_prob *__restrict__ sets, int nsets,
+     const XgDqRates *__restrict__ rates, const uint32_t *__restrict__ lasts, const uint2 *__restrict__ step_tab,
+     const uint32_t *__restrict__ sbn_tab, const XgDqParam *__restrict__ par_tab, uint32_t *__restrict__ codes,
+     uint4 *__restrict__ ring)
 {
     extern __shared__ __align__(16) unsigned char xg_dq_raw[];
     XgDqSmem &sm = *reinterpret_cast<XgDqSmem *>(xg_dq_raw);
-    const int lane = threadIdx.x & 31, qd = lane >> 2, s = lane & 3;
-    const unsigned qmask = 0xFu << (qd * 4);
-    XgDqQuad &Q = sm.quad[threadIdx.x >> 2];
-    uint32_t *codes = scratch + (size_t)(blockIdx.x * XG_DQ_QUADS + (threadIdx.x >> 2)) * XG_DQ_MAXN;
+    const int lane = threadIdx.x & 31;
+    const size_t NP = (size_t)gridDim.x * XG_DQ_PAIRS;
     const int ntr = njobs - counts[0];
 
     for (int i = threadIdx.x; i < 128; i += blockDim.x) {
         int k = i >> 5, n = i & 31, p = n >> k;
         int bits;
         if (p < 6) bits = p + 1 + k;
-        else { unsigned m = (unsigned)(n - (6 << k)); bits = 6 + 2 * (31 - __clz((int)((m >> (k + 1)) + 1))) + 1 + (k + 1); }
+        else { unsigned mm = (unsigned)(n - (6 << k)); bits = 6 + 2 * (31 - __clz((int)((mm >> (k + 1)) + 1))) + 1 + (k + 1); }
         sm.rice[k][n] = bits << 15;
+    }
+    {
+        const int nw = min(nsets, XG_DQ_RSETS) * 2 * (int)(sizeof(XgDqRates) / 4);
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(rates);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(&sm.rt[0][0]);
+        for (int i = threadIdx.x; i < nw; i += blockDim.x) dst[i] = src[i];
     }
     __syncthreads();
 
     for (;;) {
         int base = 0;
-        if (lane == 0) base = atomicAdd(counter, 8);
+        if (lane == 0) base = atomicAdd(counter, 16);
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= ntr) break;
-        const bool has = base + qd < ntr;
-        const int job = has ? order[base + qd] : 0;
-
-        /* ---- block set-up (every lane of the quad holds the same values) ---- */
-        const xin_gpu_dq_block jb = jobs[job];
-        const int first = has ? firsts[job] : -1;
-        const int lgw = jb.log2_w, lgh = jb.log2_h, w = 1 << lgw, h = 1 << lgh;
-        const int ew = min(w, 32), eh = min(h, 32), ws = ew >> 2, hs = eh >> 2;
-        const int shape = (min(lgw, 5) - 2) * 4 + (min(lgh, 5) - 2);
-        const uint2 *ST = step_tab + c_dq_shape_off[shape];
-        const uint4 *TT = tpl_tab + c_dq_shape_off[shape];
-        const XgDqParam P = par_tab[(lgw + lgh - 4) * 52 + jb.qp];
-        const int luma = jb.comp == 0;
-        const XgDqRates *RT = rates + jb.ctx_set * 2 + (luma ? 0 : 1);
-        const xin_gpu_prob *CX = sets + (size_t)jb.ctx_set * XIN_GPU_NUM_CTX;
-        const int stride = jb.stride;
-        const xg_coef *TS = tscan + soff[job];
-        xg_coef *QO = qout + jb.offset, *RO = rout + jb.offset;
-
-        /* last-position rates (Xin266SetLastCoeffOffset, h266_dep_quant.c:208-283): lane 0 x, lane 1 y */
-        if (has && s < 2) {
-            const int xy = s, size = xy ? h : w, lg = xy ? lgh : lgw, nn = min(size, 32);
-            const int shift = luma ? (lg + 1) >> 2 : min((1 << lg) >> 3, 2);
-            const int cbase = luma ? (lg == 2 ? 0 : lg == 3 ? 3 : lg == 4 ? 6 : lg == 5 ? 10 : 15) + (xy ? XG_DQC_LASTY_L : XG_DQC_LASTX_L)
-                                   : (xy ? XG_DQC_LASTY_C : XG_DQC_LASTX_C);
-            uint32_t off = 0;
-            if (xy) {
-                int cc = (luma && jb.root_cbf) ? XG_DQC_ROOT_CBF : jb.comp == 0 ? XG_DQC_CBF_Y : jb.comp == 1 ? XG_DQC_CBF_U : XG_DQC_CBF_V;
-                const uint32_t *cb = xg_dq_bits(CX, cc);
-                off = cb[1] - cb[0];
-            }
-            const int gmax = nn - 1 < 4 ? nn - 1 : 2 * (31 - __clz(nn - 1)) + (((nn - 1) >> (30 - __clz(nn - 1))) & 1);
-            uint32_t acc = 0, cbits = 0;
-            int gdone = 0;
-            /* groups in increasing order; positions map to non-decreasing groups, so one pass fills the table */
-            for (int p = 0; p < nn; p++) {
-                const int g = p < 4 ? p : 2 * (31 - __clz(p)) + ((p >> (30 - __clz(p))) & 1);
-                while (gdone <= g) {
-                    const uint32_t suf = gdone > 3 ? (uint32_t)(((gdone - 2) >> 1) << 15) : 0;
-                    if (gdone == gmax) cbits = acc + suf + off;
-                    else {
-                        const uint32_t *b = xg_dq_bits(CX, cbase + (gdone >> shift));
-                        cbits = acc + b[0] + suf + off;
-                        acc += b[1];
-                    }
-                    gdone++;
-                }
-                Q.last[xy][p] = (int32_t)cbits;
-            }
-        }
-        if (has) {
-            const uint32_t *src = reinterpret_cast<const uint32_t *>(RT);
-            uint32_t *dst = reinterpret_cast<uint32_t *>(&Q.rt);
-            for (int i = s; i < (int)(sizeof(XgDqRates) / 4); i += 4) dst[i] = __ldg(src + i);
-        }
-        __syncwarp(0xffffffffu);
-
-        /* ---- trellis state of lane s (state s) ---- */
-        long long cost = XG_DQ_INF;
-        uint32_t l0 = 0, l1 = 0, l2 = 0, l3 = 0, par16 = 0;
-        int rem = 4, nsig = 0, ref = -1, signb = 0;
-        unsigned long long cflags = 0;
-        uint32_t cvers = 0;
-        long long skcost = XG_DQ_INF;
-        int skrem = 4, skref = -1, sksignb = 0;
-        const int regbins = ew * eh * XG_DQ_REG_BINS / 16;
-        const int top = first | 15;
-        int nsteps = first >= 0 ? top + 1 : 0;
-        nsteps = __reduce_max_sync(0xffffffffu, nsteps);
-        const uint32_t *sigset = &Q.rt.sig[s > 1 ? s - 1 : 0][0][0];
-        const int src1 = s == 1 ? 2 : s == 2 ? 1 : s;      /* first exchange reads candidate A/Z */
-        const int src2 = src1 ^ 1;                         /* second exchange reads candidate B */
-        /* coefficients of the current / next sub-block: lane s holds scan positions 4s..4s+3 */
-        xg_coef c0 = 0, c1 = 0, c2 = 0, c3 = 0, n0 = 0, n1 = 0, n2 = 0, n3 = 0;
-        uint4 ea = make_uint4(0, 0, 0, 0), eb = make_uint4(0, 0, 0, 0);
-        auto load_sb = [&](int sb, xg_coef &a0, xg_coef &a1, xg_coef &a2, xg_coef &a3) {
-            const xg_coef *src = TS + sb * 16 + 4 * s;
-#if XG_BITDEPTH == 8
-            const uint2 raw = *reinterpret_cast<const uint2 *>(src);
-            a0 = (xg_coef)(raw.x & 0xFFFF); a1 = (xg_coef)(raw.x >> 16); a2 = (xg_coef)(raw.y & 0xFFFF); a3 = (xg_coef)(raw.y >> 16);
-#else
-            const int4 raw = *reinterpret_cast<const int4 *>(src);
-            a0 = raw.x; a1 = raw.y; a2 = raw.z; a3 = raw.w;
-#endif
-        };
-
-        for (int stp = 0; stp < nsteps; stp++) {
-            const int k = top - stp;
-            if (k < 0 || k > first) continue;                      /* uniform within the quad */
-            const int in = k & 15, sb = k >> 4;
-            if (k == first || in == 15) {
-                if (k == first) load_sb(sb, c0, c1, c2, c3);
-                else { c0 = n0; c1 = n1; c2 = n2; c3 = n3; }
-                if (sb > 0) load_sb(sb - 1, n0, n1, n2, n3);
-                const uint4 *e4 = reinterpret_cast<const uint4 *>(ST + sb * 16 + 4 * s);
-                ea = __ldg(e4); eb = __ldg(e4 + 1);
-            }
-            const int sub = in & 3, srcl = in >> 2;
-            const xg_coef mine = sub == 0 ? c0 : sub == 1 ? c1 : sub == 2 ? c2 : c3;
-            const uint32_t mex = sub == 0 ? ea.x : sub == 1 ? ea.z : sub == 2 ? eb.x : eb.z;
-            const uint32_t mey = sub == 0 ? ea.y : sub == 1 ? ea.w : sub == 2 ? eb.y : eb.w;
-            int av = __shfl_sync(qmask, (int)mine, srcl, 4);
-            uint2 se;
-            se.x = __shfl_sync(qmask, mex, srcl, 4);
-            se.y = __shfl_sync(qmask, mey, srcl, 4);
-            av = av < 0 ? -av : av;
-            const int px = se.x & 31, py = (se.x >> 5) & 31, ptype = (se.x >> 10) & 3, nin = (se.x >> 12) & 7;
-
-            /* context of this state at position k */
-            uint32_t tv = ref >= 0 ? Q.tpl[ref][in] : 0u;
-            int sum = tv & 127, a1 = (tv >> 7) & 31, cnt = tv >> 12;
-            if (l0 | l1 | l2 | l3) {
-#pragma unroll
-                for (int u = 0; u < 5; u++) {
-                    if (u < nin) {
-                        int j = (se.y >> (4 * u)) & 15;
-                        int l = (int)xg_dq_byte(l0, l1, l2, l3, j);
-                        if (l) { sum += l; cnt++; a1 += min(4 + (int)((par16 >> j) & 1), l); }
-                    }
-                }
-                sum = min(sum, 255);
-            }
-            const int sigoff = 4 * (int)(luma ? (se.x >> 21) & 3 : (se.x >> 25) & 1);
-            const int gtxoff = 1 + 5 * (int)(luma ? (se.x >> 23) & 3 : (se.x >> 26) & 1);
-            uint32_t sig0 = 0, sig1 = 0;
-            const uint32_t *gtx = Q.rt.gtx[0];
-            int rice, rzero = 0;
-            if (rem >= 4) {
-                const uint32_t *sg = sigset + 2 * (sigoff + min((a1 + 1) >> 1, 3));
-                sig0 = sg[0]; sig1 = sg[1];
-                gtx = Q.rt.gtx[gtxoff + min(a1 - cnt, 4)];
-                rice = xg_dq_rpar(min(max(sum - 20, 0), 31));
-            } else {
-                rice = xg_dq_rpar(min(sum, 31));
-                rzero = (s < 2 ? 1 : 2) << rice;
-            }
-
-            /* pre-quantisation (Xin266PreQuantCoeff, h266_dep_quant.c:920-952) */
-            const long long org = (long long)av * P.qScale;
-            long long qi = (org + P.qAdd) >> P.qShift;
-            const int q = (int)(qi < 1 ? 1 : qi > P.maxQIdx ? P.maxQIdx : qi);
-            const long long bse = (long long)((unsigned long long)q * (unsigned long long)P.distStepAdd -
-                                              (unsigned long long)org * (unsigned long long)P.distOrgFact);
-            auto ddof = [&](int i) -> long long {
-                int kk = (i - q) & 3;
-                long long m = (long long)((unsigned long long)(bse + kk * P.distStepAdd) * (unsigned long long)(long long)(q + kk));
-                return (m + P.distAdd) >> P.distShift;
-            };
-            auto lvof = [&](int i) -> int { return (q + ((i - q) & 3) + 1) >> 1; };
-            /* lane s prices quantisation index class s; lanes 0 / 1 take classes 0 and 2,
-             * lanes 2 / 3 classes 3 and 1 (A and B), even lanes also their own for "start" */
-            const int iA = s < 2 ? 0 : 3, iB = s < 2 ? 2 : 1;
-            const int lvA = lvof(iA), lvB = lvof(iB);
-            const long long ddS = ddof(s);
-            const long long ddA = xg_dq_shfl64(qmask, ddS, iA), ddB = xg_dq_shfl64(qmask, ddS, iB);
-
-            /* candidates of this state (Xin266CheckRdCosts, h266_dep_quant.c:954-1046) */
-            long long ca = cost + ddA, cb = cost + ddB, cz = cost;
-            bool zero_ok = true;
-            if (rem >= 4) {
-                ca += gtx[lvA < 4 ? lvA : 4 + (lvA & 1)] + (lvA >= 4 ? sm.rice[rice][min((lvA - 4) >> 1, 31)] : 0);
-                cb += gtx[lvB < 4 ? lvB : 4 + (lvB & 1)] + (lvB >= 4 ? sm.rice[rice][min((lvB - 4) >> 1, 31)] : 0);
-                if (ptype == 1) {
-                    const uint32_t sb1 = Q.rt.sbb[signb][1];
-                    ca += sb1 + sig1; cb += sb1 + sig1; cz += sb1 + sig0;
-                } else if (ptype == 0 || nsig) {
-                    ca += sig1; cb += sig1; cz += sig0;
-                } else zero_ok = false;
-            } else {
-                ca += (1 << 15) + sm.rice[rice][lvA <= rzero ? lvA - 1 : min(lvA, 31)];
-                cb += (1 << 15) + sm.rice[rice][lvB <= rzero ? lvB - 1 : min(lvB, 31)];
-                cz += sm.rice[rice][rzero];
-            }
-            long long caz;
-            int saz;
-            if (!zero_ok || ca < cz) { caz = ca; saz = iA; } else { caz = cz; saz = 4; }
-
-            /* exchange: first every lane publishes A/Z, then B */
-            const long long r1 = xg_dq_shfl64(qmask, caz, src1), r2 = xg_dq_shfl64(qmask, cb, src2);
-            const int sels = __shfl_sync(qmask, saz | iB << 4, src1, 4);
-            const int sels2 = __shfl_sync(qmask, saz | iB << 4, src2, 4);
-            long long cc1, cc2;
-            int s1, s2, f1, f2;
-            if (s < 2) { cc1 = r1; s1 = sels & 15; f1 = src1; cc2 = r2; s2 = sels2 >> 4; f2 = src2; }
-            else       { cc1 = r2; s1 = sels2 >> 4; f1 = src2; cc2 = r1; s2 = sels & 15; f2 = src1; }
-
-            /* decision for target state s */
-            long long dc = XG_DQ_INF >> 1;
-            int dsel = 7, dfrom = -2;
-            if (cc1 < dc) { dc = cc1; dsel = s1; dfrom = f1; }
-            if (cc2 < dc) { dc = cc2; dsel = s2; dfrom = f2; }
-            if (ptype == 2) {
-                long long c = skcost + Q.rt.sbb[sksignb][0];
-                if (c < dc) { dc = c; dsel = 4; dfrom = 4 + s; }
-            }
-            if ((s & 1) == 0) {
-                const int lvs = lvof(s);
-                long long c = ddS + Q.last[0][px] + Q.last[1][py] + Q.rt.gtx[0][lvs < 4 ? lvs : 4 + (lvs & 1)] +
-                              (lvs >= 4 ? sm.rice[0][min((lvs - 4) >> 1, 31)] : 0);
-                if (c < dc) { dc = c; dsel = s; dfrom = -1; }
-            }
-            const int dlv = dsel == 4 ? 0 : dsel == 7 ? -1 : lvof(dsel);
-            uint32_t code = (uint32_t)((dfrom + 2) | dsel << 4) << (8 * s);
-            code |= __shfl_xor_sync(qmask, code, 1, 4);
-            code |= __shfl_xor_sync(qmask, code, 2, 4);
-            if (s == 0) codes[k] = code;
-
-            if (ptype == 1) { skcost = cost; skrem = rem; skref = ref; sksignb = signb; }
-
-            /* state update (Xin266UpdateState / Xin266UpdateStateEOS, h266_dep_quant.c:1224-1536) */
-            const int psrc = dfrom >= 4 ? dfrom - 4 : dfrom >= 0 ? dfrom : s;
-            const uint32_t pk = (uint32_t)(rem & 0xFFFF) | (uint32_t)nsig << 16 | (uint32_t)(ref + 1) << 22 | (uint32_t)signb << 25;
-            const uint32_t spk = (uint32_t)(skrem & 0xFFFF) | (uint32_t)(skref + 1) << 16;
-            const uint32_t p0 = __shfl_sync(qmask, l0, psrc, 4), p1 = __shfl_sync(qmask, l1, psrc, 4);
-            const uint32_t p2 = __shfl_sync(qmask, l2, psrc, 4), p3 = __shfl_sync(qmask, l3, psrc, 4);
-            const uint32_t ppar = __shfl_sync(qmask, par16, psrc, 4);
-            const uint32_t ppk = __shfl_sync(qmask, pk, psrc, 4), pspk = __shfl_sync(qmask, spk, psrc, 4);
-            cost = dc;
-            if (k == 0) continue;
-            const int p_rem = (int)(int16_t)(ppk & 0xFFFF), p_nsig = (ppk >> 16) & 31, p_ref = (int)((ppk >> 22) & 7) - 1;
-            const int p_signb = (ppk >> 25) & 1;
-            const int lv = dlv;
-            if (in != 0) {
-                if (dfrom >= 0) {
-                    nsig = p_nsig + (lv != 0); ref = p_ref; signb = p_signb;
-                    rem = p_rem - 1;
-                    if (rem >= 4) rem -= lv < 2 ? lv : 3;
-                    l0 = p0; l1 = p1; l2 = p2; l3 = p3; par16 = ppar;
-                } else if (dfrom == -1) {
-                    nsig = 1; ref = -1;
-                    rem = regbins - (lv < 2 ? lv : 3);
-                    l0 = l1 = l2 = l3 = 0; par16 = 0;
-                }
-                if (dfrom > -2 && lv) {
-                    const uint32_t b = (uint32_t)min(lv, 255), sh = (in & 3) * 8, m = ~(255u << sh);
-                    const int wi = in >> 2;
-                    if (wi == 0) l0 = (l0 & m) | b << sh; else if (wi == 1) l1 = (l1 & m) | b << sh;
-                    else if (wi == 2) l2 = (l2 & m) | b << sh; else l3 = (l3 & m) | b << sh;
-                    par16 = (par16 & ~(1u << in)) | (uint32_t)(lv & 1) << in;
-                }
-            } else {
-                /* first coefficient (in scan order) of sub-block sb: close it and open sb - 1 */
-                const int slot = sb & 15;
-                int srcref = -1;
-                if (dfrom >= 4) {
-                    nsig = 0; rem = (int)(int16_t)(pspk & 0xFFFF); srcref = (int)((pspk >> 16) & 7) - 1;
-                    l0 = l1 = l2 = l3 = 0; par16 = 0;
-                } else if (dfrom >= 0) {
-                    nsig = p_nsig + (lv != 0);
-                    rem = p_rem - 1;
-                    if (rem >= 4) rem -= lv < 2 ? lv : 3;
-                    l0 = p0; l1 = p1; l2 = p2; l3 = p3; par16 = ppar; srcref = p_ref;
-                } else if (dfrom == -1) {
-                    nsig = 1; rem = regbins;
-                    if (rem >= 4) rem -= lv < 2 ? lv : 3;
-                    l0 = l1 = l2 = l3 = 0; par16 = 0;
-                }
-                const bool upd = dfrom > -2;
-                if (upd) {
-                    const uint32_t cap = 254u + (uint32_t)(lv & 1);
-                    l0 = (l0 & ~255u) | min((uint32_t)lv, cap);
-                }
-                /* sub-block context of the new path: the predecessor's plus this sub-block */
-                const int cr = srcref >= 0 ? srcref : s;
-                const uint32_t fl = __shfl_sync(qmask, (uint32_t)cflags, cr, 4);
-                const uint32_t fh = __shfl_sync(qmask, (uint32_t)(cflags >> 32), cr, 4);
-                const uint32_t fv = __shfl_sync(qmask, cvers, cr, 4);
-                const int braster = (se.x >> 15) & 63;
-                unsigned long long nfl = srcref >= 0 ? ((unsigned long long)fh << 32 | fl) : 0ull;
-                uint32_t nvr = srcref >= 0 ? fv : 0u;
-                nfl = (nfl & ~(1ull << braster)) | (unsigned long long)(nsig != 0) << braster;
-                nvr = (nvr & ~(3u << (2 * slot))) | (uint32_t)s << (2 * slot);
-                if (upd) *reinterpret_cast<uint4 *>(&Q.ring[slot][s][0]) = make_uint4(l0, l1, l2, l3);
-                /* neighbours of sub-block sb - 1 */
-                const uint32_t nx = __ldg(&ST[k - 1].x);
-                const int r1 = (nx >> 15) & 63, x1 = r1 % ws, y1 = r1 / ws;
-                const int right = x1 < ws - 1 ? r1 + 1 : 0, below = y1 < hs - 1 ? r1 + ws : 0;
-                const int nsb = (right && ((nfl >> right) & 1)) || (below && ((nfl >> below) & 1));
-                const bool need = nsb || (right && below && ((nfl >> (below + 1)) & 1));
-                __syncwarp(qmask);
-                if (upd) {
-#pragma unroll 4
-                    for (int j = 0; j < 16; j++) {
-                        uint32_t t16 = 0;
-                        if (need) {
-                            const uint4 te = __ldg(&TT[k - 16 + j]);
-                            const int no = te.x & 7;
-                            int sa = 0, s1v = 0, cn = 0;
-                            const uint32_t nbs[5] = { te.x >> 16, te.y & 0xFFFF, te.y >> 16, te.z & 0xFFFF, te.z >> 16 };
-#pragma unroll
-                            for (int u = 0; u < 5; u++) {
-                                if (u < no) {
-                                    const uint32_t nb = nbs[u];
-                                    const int sbn = nb & 63, inner = (nb >> 6) & 15, rs = (nb >> 10) & 63, sl = sbn & 15;
-                                    int v = 0;
-                                    if ((nfl >> rs) & 1) {
-                                        const int ver = (nvr >> (2 * sl)) & 3;
-                                        v = reinterpret_cast<const uint8_t *>(&Q.ring[sl][ver][0])[inner];
-                                    }
-                                    sa += v; s1v += min(4 + (v & 1), v); cn += v != 0;
-                                }
-                            }
-                            t16 = (uint32_t)min(sa, 127) | (uint32_t)s1v << 7 | (uint32_t)cn << 12;
-                        }
-                        Q.tpl[s][j] = (uint16_t)t16;
-                    }
-                    nsig = 0; l0 = l1 = l2 = l3 = 0; par16 = 0; ref = s; signb = nsb;
-                    cflags = nfl; cvers = nvr;
-                }
-                __syncwarp(qmask);
-            }
-        }
-        __syncwarp(qmask);
-
-        /* ---- best final state, then walk the decisions from position 0 up
-         * (h266_dep_quant.c:1919-1947).  The state a coefficient was quantised
-         * in is the source state of its decision (0 for the last position), so
-         * each level is dequantised as it is found (:1949-1989 walks the same
-         * state machine forward from the last position). */
-        const long long f0 = xg_dq_shfl64(qmask, cost, 0), f1v = xg_dq_shfl64(qmask, cost, 1);
-        const long long f2v = xg_dq_shfl64(qmask, cost, 2), f3v = xg_dq_shfl64(qmask, cost, 3);
-        if (has) {
-            unsigned long long map = 0;
-            long long best = 0;
-            int st = -1;
-            if (f0 < best) { best = f0; st = 0; }
-            if (f1v < best) { best = f1v; st = 1; }
-            if (f2v < best) { best = f2v; st = 2; }
-            if (f3v < best) { best = f3v; st = 3; }
-            const int iqadd = 1 << (P.iqShift - 1);
-            uint32_t ncode = codes[s];
-            int nval = TS[s];
-            uint32_t nent = __ldg(&ST[s].x);
-            for (int k0 = 0; st >= 0 && k0 <= first; k0 += 4) {
-                const uint32_t mcode = ncode, ment = nent;
-                const int mval = nval;
-                if (k0 + 4 + s <= first) { ncode = codes[k0 + 4 + s]; nval = TS[k0 + 4 + s]; nent = __ldg(&ST[k0 + 4 + s].x); }
-#pragma unroll
-                for (int j = 0; j < 4; j++) {
-                    const uint32_t c = __shfl_sync(qmask, mcode, j, 4);
-                    const int v = __shfl_sync(qmask, mval, j, 4);
-                    const int k = k0 + j;
-                    if (st >= 0 && k <= first) {
-                        int lv = 0, ps = 0;
-                        if (!(st >= 4 && (k & 15))) {
-                            const uint32_t byte = (c >> (8 * (st & 3))) & 255u;
-                            const int sel = (int)(byte >> 4), from = (int)(byte & 15) - 2;
-                            const int av = v < 0 ? -v : v;
-                            const long long qi = ((long long)av * P.qScale + P.qAdd) >> P.qShift;
-                            const int q = (int)(qi < 1 ? 1 : qi > P.maxQIdx ? P.maxQIdx : qi);
-                            lv = sel >= 4 ? 0 : (q + ((sel - q) & 3) + 1) >> 1;
-                            ps = from >= 0 && from < 4 ? from : 0;
-                            st = from;
-                        }
-                        if (lv && s == j) {
-                            const int x = ment & 31, y = (ment >> 5) & 31;
-                            const int qv = v < 0 ? -lv : lv;
-                            const int qidx = 2 * qv + (qv > 0 ? -(ps >> 1) : (ps >> 1));
-                            const int rv = (qidx * P.iqScale + iqadd) >> P.iqShift;
-                            QO[y * stride + x] = (xg_coef)qv;
-                            RO[y * stride + x] = (xg_coef)(rv < -32768 ? -32768 : rv > 32767 ? 32767 : rv);
-                            map |= 1ull << ((ment >> 15) & 63);
-                        }
-                    }
-                }
-            }
-            map |= __shfl_xor_sync(qmask, map, 1, 4);
-            map |= __shfl_xor_sync(qmask, map, 2, 4);
-            if (s == 0) nzout[job] = map;
+        const int idx = base + (lane >> 1);
+        if (idx < ntr) {
+            const int job = order[idx];
+            const xin_gpu_dq_block jb = jobs[job];
+            if (nsets <= XG_DQ_RSETS)
+                xg_dq_block<true>(sm, job, jb, firsts[job], soff, tscan, qout, rout, nzout, sets, nsets, rates, lasts,
+                                  step_tab, sbn_tab, par_tab, codes, ring, NP);
+            else
+                xg_dq_block<false>(sm, job, jb, firsts[job], soff, tscan, qout, rout, nzout, sets, nsets, rates, lasts,
+                                   step_tab, sbn_tab, par_tab, codes, ring, NP);
         }
         __syncwarp(0xffffffffu);
     }
@@ -790,30 +911,36 @@ static int xg_dq_resident_ctas(void)
 }
 
 /* Device work area of a run, in order: job counter, bucket counts and cursors
- * (256 B); rates of nsets context sets; last positions and order of njobs
- * blocks; the scan-order copy of the blocks (nscan coefficients); nquads
- * quads' decision areas. */
+ * (1 KB); rates and last-position rates of nsets context sets; last positions
+ * and order of njobs blocks; the scan-order copy of the blocks (nscan
+ * coefficients); per trellis thread (nslots) its decision column and its ring
+ * of earlier sub-blocks' levels. */
 struct XgDqArea {
     int *counter, *counts, *cursor;
     XgDqRates *rates;
+    uint32_t *lasts;
     int32_t *first, *order;
     xg_coef *tscan;
     uint32_t *codes;
+    uint4 *ring;
 };
-static size_t xg_dq_area_bytes(int nsets, int njobs, size_t nscan, int nquads, XgDqArea *a, char *base)
+static size_t xg_dq_area_bytes(int nsets, int njobs, size_t nscan, int nslots, XgDqArea *a, char *base)
 {
     size_t o = 0;
     auto take = [&](size_t bytes) { size_t at = o; o = (o + bytes + 255) & ~(size_t)255; return base ? base + at : nullptr; };
     char *hdr = take(1024);
     char *rt = take((size_t)nsets * 2 * sizeof(XgDqRates));
+    char *la = take((size_t)nsets * XG_DQ_LAST_WORDS * 4);
     char *fi = take((size_t)njobs * 4);
     char *od = take((size_t)njobs * 4);
     char *ts = take(nscan * sizeof(xg_coef));
-    char *cd = take((size_t)nquads * XG_DQ_MAXN * 4);
+    char *cd = take((size_t)nslots * XG_DQ_MAXN * 4);
+    char *rg = take((size_t)nslots * 64 * sizeof(uint4));
+    static_assert(XG_DQ_SLOT_BYTES == XG_DQ_MAXN * 4 + 64 * sizeof(uint4), "trellis slot bytes");
     if (a && base) {
         a->counter = (int *)hdr; a->counts = (int *)hdr + 1; a->cursor = (int *)hdr + 80;
-        a->rates = (XgDqRates *)rt; a->first = (int32_t *)fi; a->order = (int32_t *)od;
-        a->tscan = (xg_coef *)ts; a->codes = (uint32_t *)cd;
+        a->rates = (XgDqRates *)rt; a->lasts = (uint32_t *)la; a->first = (int32_t *)fi; a->order = (int32_t *)od;
+        a->tscan = (xg_coef *)ts; a->codes = (uint32_t *)cd; a->ring = (uint4 *)rg;
     }
     return o;
 }
@@ -822,17 +949,17 @@ static int xg_dq_enqueue(const xin_gpu_dq_block *d_jobs, const uint32_t *d_soff,
                          const xg_coef *t, xg_coef *q, xg_coef *r, unsigned long long *nz, const xin_gpu_prob *d_sets,
                          int nsets, const XgDqArea &A, int max_ctas, int full, cudaStream_t st, bool count = true)
 {
-    int ctas = (njobs + XG_DQ_QUADS - 1) / XG_DQ_QUADS;
+    int ctas = (njobs + XG_DQ_PAIRS - 1) / XG_DQ_PAIRS;
     if (ctas > max_ctas) ctas = max_ctas;
     if (xg_cuda_check(cudaMemsetAsync(A.counter, 0, 1024, st), "dq counters")) return XIN_GPU_ERR_CUDA;
-    k_dq_rates<<<nsets, 64, 0, st>>>(d_sets, A.rates);
+    k_dq_rates<<<nsets, 64, 0, st>>>(d_sets, A.rates, A.lasts);
     const int pw = 8, pblocks = std::min((njobs + pw - 1) / pw, 152 * 16);
     k_dq_prep<<<pblocks, pw * 32, 0, st>>>(d_jobs, njobs, d_soff, t, A.tscan, q, r, nz, g_dq.d_step, g_dq.d_par,
                                            A.first, A.counts, full);
     k_dq_order<<<std::min((njobs + 255) / 256, 152 * 4), 256, 0, st>>>(njobs, A.first, A.counts, A.cursor, A.order);
     k_dq<<<ctas, XG_DQ_THREADS, sizeof(XgDqSmem), st>>>(d_jobs, njobs, A.counter, A.counts, A.order, A.first, d_soff,
-                                                        A.tscan, q, r, nz, d_sets, A.rates, g_dq.d_step, g_dq.d_tpl,
-                                                        g_dq.d_par, A.codes);
+                                                        A.tscan, q, r, nz, d_sets, nsets, A.rates, A.lasts, g_dq.d_step,
+                                                        g_dq.d_sbn, g_dq.d_par, A.codes, A.ring);
     if (count) xg_count_launch(4);
     return xg_cuda_check(cudaGetLastError(), "dep_quant launch");
 }
@@ -893,8 +1020,8 @@ extern "C" int xin_gpu_dq_plan_create(const xin_gpu_dq_block *blocks, int32_t nb
     p->nblocks = nblocks; p->nsets = nsets; p->ncoeffs = ncoeffs; p->nscan = nscan;
     const int res = xg_dq_resident_ctas();
     if (!res) { delete p; return xin_gpu_last_status(); }
-    p->ctas = std::min(res, (nblocks + XG_DQ_QUADS - 1) / XG_DQ_QUADS);
-    const size_t bytes = xg_dq_area_bytes(nsets, nblocks, nscan, p->ctas * XG_DQ_QUADS, nullptr, nullptr);
+    p->ctas = std::min(std::min(res, XG_DQ_MAX_CTAS), (nblocks + XG_DQ_PAIRS - 1) / XG_DQ_PAIRS);
+    const size_t bytes = xg_dq_area_bytes(nsets, nblocks, nscan, p->ctas * XG_DQ_PAIRS, nullptr, nullptr);
     if (nscan >= (1ull << 32) ||
         xg_cuda_check(cudaMalloc(&p->d_soff, (size_t)nblocks * 4), "dq plan") ||
         xg_cuda_check(cudaMemcpy(p->d_soff, soff.data(), (size_t)nblocks * 4, cudaMemcpyHostToDevice), "dq plan") ||
@@ -905,7 +1032,7 @@ extern "C" int xin_gpu_dq_plan_create(const xin_gpu_dq_block *blocks, int32_t nb
         xin_gpu_dq_plan_destroy(p);
         return xin_gpu_last_status();
     }
-    xg_dq_area_bytes(nsets, nblocks, nscan, p->ctas * XG_DQ_QUADS, &p->area, p->d_area);
+    xg_dq_area_bytes(nsets, nblocks, nscan, p->ctas * XG_DQ_PAIRS, &p->area, p->d_area);
     *out = p;
     return XIN_GPU_OK;
 }
@@ -1026,11 +1153,11 @@ extern "C" void XinGpuDepQuant(void *depQuant, void *fastBuf, void *tu, XG_COEFF
     xin_gpu_prob *dc = (xin_gpu_prob *)xg_stage_in(th, ctx, (intptr_t)cbytes, cbytes, 1, 1);
     const uint32_t zero = 0;
     uint32_t *dso = (uint32_t *)xg_stage_in(th, &zero, 1, 1, 1, 4);
-    const size_t abytes = xg_dq_area_bytes(1, 1, (size_t)ew * eh, XG_DQ_QUADS, nullptr, nullptr);
+    const size_t abytes = xg_dq_area_bytes(1, 1, (size_t)ew * eh, XG_DQ_PAIRS, nullptr, nullptr);
     char *area = (char *)xg_dalloc(th, abytes);
     if (!dt || !dq || !dr || !dnz || !dj || !dc || !dso || !area) return;
     XgDqArea A;
-    xg_dq_area_bytes(1, 1, (size_t)ew * eh, XG_DQ_QUADS, &A, area);
+    xg_dq_area_bytes(1, 1, (size_t)ew * eh, XG_DQ_PAIRS, &A, area);
     if (xg_dq_enqueue(dj, dso, 1, dt, dq, dr, dnz, dc, 1, A, 1, 0, th->stream)) return;
     if (xg_stage_out(th, qCoeff, coeffStride, dq, ew, eh, sizeof(xg_coef)) ||
         xg_stage_out(th, rCoeff, coeffStride, dr, ew, eh, sizeof(xg_coef)) ||

@@ -252,8 +252,10 @@ static uint64_t xg_tu_bytes(const xin_gpu_stream_cfg *c)
         blocks += n * (nc + 2);
         cus += n;
     }
+    const uint64_t slots = std::min<uint64_t>((uint64_t)XG_DQ_MAX_CTAS, (blocks + XG_DQ_PAIRS - 1) / XG_DQ_PAIRS) * XG_DQ_PAIRS;
     return 3 * coef * sizeof(xg_coef) + res * 2 + blocks * (16 + 16 + sizeof(xin_gpu_dq_block)) + cus * 4 +
-           XIN_GPU_NUM_CTX * sizeof(xin_gpu_prob) + coef * 2 /* the trellis plan's scan-order copies */;
+           XIN_GPU_NUM_CTX * sizeof(xin_gpu_prob) + coef * 2 /* the trellis plan's scan-order copies */ +
+           slots * XG_DQ_SLOT_BYTES /* its decision columns and rings */;
 }
 
 static void xg_tu_free(XgTuState *u)
