@@ -301,6 +301,42 @@ def test_frame_wait_timeout_then_collect():
         assert np.array_equal(outs[0]["q"][p], outs[1]["q"][p])
 
 
+@pytest.mark.parametrize("bd", (8, 10))
+def test_frame_hier_wait_bound_is_reported_and_recovers(bd):
+    """The search by resolution levels waits for its TMA window loads with a
+    bounded poll.  With the bound set to 0 polls the wait gives up at once:
+    frame_wait reports XIN_GPU_ERR_TIMEOUT for that picture, and after the
+    default bound is restored the next picture equals the same picture through
+    a stream that never gave up (the reference planes were built either way)."""
+    w, h = 192, 128
+    seq = synth.sequence(w, h, 3, seed=77, bitdepth=bd, objects=2)
+    outs = []
+    for probe in (True, False):
+        fs = FrameStream(w, h, search_range=16, out_q=True, out_rec=True, bitdepth=bd, search_mode=1)
+        try:
+            fs.submit(*seq[0], qp=32, uv_qp=32, sad_lambda=64)
+            fs.wait()
+            if probe:
+                assert fs.lib.xin_gpu_stream_set_wait_tries(fs.h, 0) == 0
+            fs.submit(*seq[1], qp=32, uv_qp=32, sad_lambda=64)
+            if probe:
+                with pytest.raises(RuntimeError, match=r"\(-5\).*bound"):
+                    fs.wait()
+                assert fs.lib.xin_gpu_stream_set_wait_tries(fs.h, -1) == 0
+                assert fs.lib.xin_gpu_stream_set_wait_tries(fs.h, -2) == -2
+            else:
+                fs.wait()
+            fs.submit(*seq[2], qp=32, uv_qp=32, sad_lambda=64)
+            outs.append(fs.wait())
+        finally:
+            fs.close()
+    for k in ("cu",):
+        assert np.array_equal(outs[0][k], outs[1][k])
+    for p in range(3):
+        assert np.array_equal(outs[0]["q"][p], outs[1]["q"][p])
+        assert np.array_equal(outs[0]["rec"][p], outs[1]["rec"][p])
+
+
 @pytest.mark.parametrize("bd,inb", [(8, 0), (10, 0), (10, 8)])
 @pytest.mark.parametrize("w,h,R,ctu", [(192, 128, 16, 64), (208, 120, 64, 64), (200, 104, 37, 128), (384, 256, 256, 128)])
 def test_frame_hier_search_matches_oracle(bd, inb, w, h, R, ctu):

@@ -135,6 +135,7 @@ SIGNATURES = {
     "xin_gpu_frame_submit": ([vp, C.POINTER(xin_gpu_picture)], C.c_int),
     "xin_gpu_frame_wait": ([vp, C.POINTER(xin_gpu_results), i32], C.c_int),
     "xin_gpu_stream_stage_ms": ([vp, C.POINTER(C.c_float)], C.c_int),
+    "xin_gpu_stream_set_wait_tries": ([vp, C.c_int64], C.c_int),
     "xin_gpu_stream_device_results": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)], C.c_int),
     "xin_gpu_measure_sad_peak": ([C.POINTER(C.c_double)], C.c_int),
     "xin_gpu_install": ([vp, vp, u32], C.c_int),

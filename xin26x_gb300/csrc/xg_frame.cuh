@@ -31,6 +31,10 @@ struct xin_gpu_stream {
     xg_pix *lo_base[2][2];
     XgPlane lo[2][2];
     int lo_pitch[2], lo_rows[2];
+    CUtensorMap tm_win[2], tm_cur[2];  /* TMA maps of each slot's 1/4 plane: reference window, current tile */
+    int hier_win_rem, hier_win_pitch, hier_cur_rem, hier_cur_pitch;
+    size_t hier_smem;
+    long long wait_tries;  /* bound of the kernels' waits (polls) */
     unsigned long long *keys;
     /* what a picture in flight owns; picture k uses set k & 1 (its slot), so two
      * pictures can be in flight: one computing while the other's copies run */
@@ -44,6 +48,7 @@ struct xin_gpu_stream {
         /* pinned host staging (input samples of in_es bytes) */
         xg_pix *h_in[3];
         XgPicParams *h_pp;
+        int32_t *h_stat;       /* the picture's device status (XgPicParams.status), read back with the results */
         xin_gpu_cu_result *h_res;
         xg_coef *h_q[3];
         xg_pix *h_rec[3];
@@ -111,7 +116,7 @@ static int xg_stream_free(xin_gpu_stream *s)
     for (auto &t : s->set) {
         cudaFree(t.dres); cudaFree(t.dpp); cudaFree(t.dmts); cudaFreeHost(t.h_mts);
         for (int p = 0; p < 3; p++) { cudaFree(t.dq[p]); cudaFree(t.drec[p]); cudaFree(t.d_in8[p]); cudaFreeHost(t.h_in[p]); cudaFreeHost(t.h_q[p]); cudaFreeHost(t.h_rec[p]); }
-        cudaFreeHost(t.h_pp); cudaFreeHost(t.h_res);
+        cudaFreeHost(t.h_pp); cudaFreeHost(t.h_res); cudaFreeHost(t.h_stat);
         for (int i = 0; i < 5; i++) if (t.evs[i]) cudaEventDestroy(t.evs[i]);
         if (t.ev0) cudaEventDestroy(t.ev0);
         if (t.ev1) cudaEventDestroy(t.ev1);
@@ -246,6 +251,8 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
             if (e == cudaSuccess && (c.out_flags & XIN_GPU_OUT_REC)) e = cudaMallocHost(&t.h_rec[p], n * sizeof(xg_pix));
         }
         if (e == cudaSuccess) e = cudaMallocHost(&t.h_pp, sizeof(XgPicParams));
+        if (e == cudaSuccess) e = cudaMallocHost(&t.h_stat, sizeof(int32_t));
+        if (e == cudaSuccess) *t.h_stat = 0;
         if (e == cudaSuccess) e = cudaMallocHost(&t.h_res, sizeof(xin_gpu_cu_result) * s->ncus);
     }
     if (e != cudaSuccess) {
@@ -338,6 +345,32 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
 #endif
     });
     if (xg_cuda_check(me_attr_err, "me smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
+    s->wait_tries = XG_TMA_WAIT_TRIES;
+    if (c.search_mode == 1) {
+        /* TMA maps of the 1/4 planes: the window box of each tile starts
+         * 16pb + pad/4 - R/4 - rem samples into the plane and the current box
+         * 16bx + pad/4 - cur_rem, both multiples of 16 bytes (rem is that
+         * offset's remainder, 16bx is a multiple of 16 samples) */
+        const int A = 16 / (int)sizeof(xg_pix), pad4 = pad >> 2, R4 = c.search_range >> 2, WS = 16 + 2 * R4;
+        xg_hier_boxes(pad, c.search_range, &s->hier_win_rem, &s->hier_win_pitch, &s->hier_cur_rem, &s->hier_cur_pitch,
+                      &s->hier_smem);
+        const long long ow4 = (c.width + 2 * pad) >> 2;
+        if ((pad4 - R4 - s->hier_win_rem) % A || (pad4 - s->hier_cur_rem) % A || pad4 - R4 - s->hier_win_rem < 0 ||
+            s->hier_smem > 48 * 1024) {
+            xg_set_error(XIN_GPU_ERR_ARG, "stream_open: search by levels: window boxes off the 16-byte grid or too large");
+            xg_stream_free(s);
+            return XIN_GPU_ERR_ARG;
+        }
+        for (int i = 0; i < 2; i++)
+            if (!xg_tma_map_2d(&s->tm_win[i], s->lo_base[i][1], (int)sizeof(xg_pix), ow4, s->lo_rows[1], s->lo_pitch[1],
+                               s->hier_win_pitch, WS) ||
+                !xg_tma_map_2d(&s->tm_cur[i], s->lo_base[i][1], (int)sizeof(xg_pix), ow4, s->lo_rows[1], s->lo_pitch[1],
+                               s->hier_cur_pitch, 16)) {
+                const int st = xin_gpu_last_status();
+                xg_stream_free(s);
+                return st;
+            }
+    }
     if (c.tu_mode == 1) {
         const int st = xg_tu_open(s);
         if (st) { xg_stream_free(s); return st; }
@@ -445,6 +478,11 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         if (c.search_mode == 1) {
             XgHierFrameParams hp;
             memset(&hp, 0, sizeof hp);
+            hp.tm_win = s->tm_win[ref]; hp.tm_cur = s->tm_cur[cur];
+            hp.pad4 = s->pad >> 2;
+            hp.win_rem = s->hier_win_rem; hp.win_pitch = s->hier_win_pitch;
+            hp.cur_rem = s->hier_cur_rem; hp.cur_pitch = s->hier_cur_pitch;
+            hp.wait_tries = s->wait_tries;
             hp.cur = s->slot[cur][0]; hp.ref = s->slot[ref][0];
             for (int l = 0; l < 2; l++) { hp.cur_lo[l] = s->lo[cur][l]; hp.ref_lo[l] = s->lo[ref][l]; }
             hp.W = c.width; hp.H = c.height; hp.ctu = c.ctu_size; hp.R = c.search_range;
@@ -457,7 +495,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
                 nz++;
             }
             dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, nz);
-            k_hier_frame<<<grd, XG_HIER_THREADS, xg_hier_smem(c.search_range), st>>>(hp, t.dpp);
+            k_hier_frame<<<grd, XG_HIER_THREADS, s->hier_smem, st>>>(hp, t.dpp, &t.dpp->status);
         } else {
         XgMeParams mp;
         mp.cur = s->slot[cur][0];
@@ -560,6 +598,8 @@ static void xg_enqueue_results(xin_gpu_stream *s, xin_gpu_stream::Set &t, bool w
             if (c.out_flags & XIN_GPU_OUT_REC) cudaMemcpyAsync(t.h_rec[p], t.drec[p], n * sizeof(xg_pix), cudaMemcpyDeviceToHost, s->cst);
         }
     }
+    /* the picture's device status (a wait bound reached) */
+    cudaMemcpyAsync(t.h_stat, &t.dpp->status, sizeof(int32_t), cudaMemcpyDeviceToHost, s->cst);
     cudaEventRecord(t.evs[4], s->cst);
     cudaEventRecord(t.ev1, s->cst);
 }
@@ -664,6 +704,10 @@ extern "C" int xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32
         std::this_thread::yield();
     }
     s->ndone++;
+    if (*t.h_stat) {
+        xg_set_error(XIN_GPU_ERR_TIMEOUT, "frame_wait: picture %d: a device wait reached its bound (status %d)", k, *t.h_stat);
+        return XIN_GPU_ERR_TIMEOUT;
+    }
     if (k == 0) {                           /* the first picture only becomes the reference */
         if (res) res->gpu_ms = 0;
         return XIN_GPU_OK;
@@ -694,6 +738,18 @@ extern "C" int xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32
             else res->rec[p] = t.h_rec[p];
         }
     }
+    return XIN_GPU_OK;
+}
+
+extern "C" int xin_gpu_stream_set_wait_tries(xin_gpu_stream *s, int64_t tries)
+{
+    xin_gpu_clear_error();
+    if (!s || tries < -1) { xg_set_error(XIN_GPU_ERR_ARG, "stream_set_wait_tries: null stream or tries below -1"); return XIN_GPU_ERR_ARG; }
+    if (s->nsub != s->ndone) { xg_set_error(XIN_GPU_ERR_STATE, "stream_set_wait_tries: pictures in flight"); return XIN_GPU_ERR_STATE; }
+    s->wait_tries = tries < 0 ? XG_TMA_WAIT_TRIES : tries;
+    /* the bound is a parameter of the captured graphs: capture them again */
+    for (int i = 0; i < 2; i++)
+        if (s->gexec[i]) { cudaGraphExecDestroy(s->gexec[i]); s->gexec[i] = nullptr; }
     return XIN_GPU_OK;
 }
 

@@ -156,12 +156,15 @@ __global__ void __launch_bounds__(256) k_qpel_planes(XgPlane ref, XgQpel qp)
 struct XgQuant { int qmult, qadd, qshift, iqmult, iqadd, iqshift; };
 struct XgPicParams {
     uint32_t lambda;
-    uint32_t reserved;
+    int32_t status;                     /* written by the kernels: XG_STATUS_* bits (0 = fine) */
     XgQuant quant[4][3];                /* [level 64,32,16,8][plane] */
     const xg_pix *src[3];               /* device-resident source planes (device_io streams) */
     long long src_stride[3];
     int32_t dq_qp[2];                   /* preset-4 TU stage: luma / chroma QP the trellis gets */
 };
+
+/* device status bits of a picture */
+#define XG_STATUS_TMA_WAIT 1                    /* a TMA load did not complete within its wait bound */
 
 /* Sources of k_fill_slot: where a picture's samples come from */
 enum XgFillMode {

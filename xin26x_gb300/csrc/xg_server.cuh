@@ -58,7 +58,7 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
         for (int l = 0; l < 2; l++)
             d += 2 * ((((uint64_t)(c->width + 2 * pad) >> (l + 1)) + 127) & ~127ull) * ((uint64_t)(c->height + 2 * pad) >> (l + 1)) *
                  sizeof(xg_pix);
-    uint64_t h = sizeof(XgPicParams) + sizeof(xin_gpu_cu_result) * ncus;
+    uint64_t h = sizeof(XgPicParams) + sizeof(int32_t) + sizeof(xin_gpu_cu_result) * ncus;
     if (c->tu_mode == 1 && !c->device_io) h += sizeof(xin_gpu_cu_mts) * ncus;
     if (!c->device_io) {
         h += (lq + 2 * lc) * in_es;
