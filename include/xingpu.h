@@ -551,12 +551,13 @@ int  xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic);
  * until the second frame_submit after this call.  Every submitted picture is
  * collected once, the first one included. */
 int  xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32_t timeout_ms);
-/* Bound of the waits inside a stream's kernels (the search by resolution
- * levels waits for its TMA window loads), in polls of the barrier; -1 restores
- * the default (about a second).  A picture whose wait reaches the bound is
- * reported by xin_gpu_frame_wait as XIN_GPU_ERR_TIMEOUT (its CUs get the zero
- * vector); the stream stays usable.  XIN_GPU_ERR_STATE while pictures are in
- * flight.  No counterpart in the reference (a GPU wait bound). */
+/* Bound of the waits inside a stream's kernels (the quarter-pel planes wait
+ * for their TMA tile loads), in polls of the barrier; -1 restores the default
+ * (about a second).  A picture whose wait reaches the bound is reported by
+ * xin_gpu_frame_wait as XIN_GPU_ERR_TIMEOUT (the kernel stages with plain
+ * loads once the copies have landed); the stream stays usable.
+ * XIN_GPU_ERR_STATE while pictures are in flight.  No counterpart in the
+ * reference (a GPU wait bound). */
 int  xin_gpu_stream_set_wait_tries(xin_gpu_stream *s, int64_t tries);
 /* Device time of the stages of the last collected picture:
  * ms[0] upload + padding + quarter-pel planes, ms[1] integer search,

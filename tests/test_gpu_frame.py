@@ -301,18 +301,19 @@ def test_frame_wait_timeout_then_collect():
         assert np.array_equal(outs[0]["q"][p], outs[1]["q"][p])
 
 
-@pytest.mark.parametrize("bd", (8, 10))
-def test_frame_hier_wait_bound_is_reported_and_recovers(bd):
-    """The search by resolution levels waits for its TMA window loads with a
-    bounded poll.  With the bound set to 0 polls the wait gives up at once:
-    frame_wait reports XIN_GPU_ERR_TIMEOUT for that picture, and after the
-    default bound is restored the next picture equals the same picture through
-    a stream that never gave up (the reference planes were built either way)."""
+@pytest.mark.parametrize("bd,mode", [(8, 0), (10, 1)])
+def test_frame_tma_wait_bound_is_reported_and_recovers(bd, mode):
+    """The TMA loads of the quarter-pel planes' tiles are waited for with a
+    bounded poll.  With the bound set to 0 polls every wait gives up at once:
+    frame_wait reports XIN_GPU_ERR_TIMEOUT for that picture (the kernel then
+    stages its tiles with plain loads once the copies have landed), and after
+    the default bound is restored the next picture equals the same picture
+    through a stream that never gave up."""
     w, h = 192, 128
     seq = synth.sequence(w, h, 3, seed=77, bitdepth=bd, objects=2)
     outs = []
     for probe in (True, False):
-        fs = FrameStream(w, h, search_range=16, out_q=True, out_rec=True, bitdepth=bd, search_mode=1)
+        fs = FrameStream(w, h, search_range=16, out_q=True, out_rec=True, bitdepth=bd, search_mode=mode)
         try:
             fs.submit(*seq[0], qp=32, uv_qp=32, sad_lambda=64)
             fs.wait()

@@ -31,9 +31,7 @@ struct xin_gpu_stream {
     xg_pix *lo_base[2][2];
     XgPlane lo[2][2];
     int lo_pitch[2], lo_rows[2];
-    CUtensorMap tm_win[2], tm_cur[2];  /* TMA maps of each slot's 1/4 plane: reference window, current tile */
-    int hier_win_rem, hier_win_pitch, hier_cur_rem, hier_cur_pitch;
-    size_t hier_smem;
+    CUtensorMap tm_qp[2];              /* TMA map of each slot's padded luma plane: quarter-pel tiles */
     long long wait_tries;  /* bound of the kernels' waits (polls) */
     unsigned long long *keys;
     /* what a picture in flight owns; picture k uses set k & 1 (its slot), so two
@@ -346,31 +344,15 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     });
     if (xg_cuda_check(me_attr_err, "me smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
     s->wait_tries = XG_TMA_WAIT_TRIES;
-    if (c.search_mode == 1) {
-        /* TMA maps of the 1/4 planes: the window box of each tile starts
-         * 16pb + pad/4 - R/4 - rem samples into the plane and the current box
-         * 16bx + pad/4 - cur_rem, both multiples of 16 bytes (rem is that
-         * offset's remainder, 16bx is a multiple of 16 samples) */
-        const int A = 16 / (int)sizeof(xg_pix), pad4 = pad >> 2, R4 = c.search_range >> 2, WS = 16 + 2 * R4;
-        xg_hier_boxes(pad, c.search_range, &s->hier_win_rem, &s->hier_win_pitch, &s->hier_cur_rem, &s->hier_cur_pitch,
-                      &s->hier_smem);
-        const long long ow4 = (c.width + 2 * pad) >> 2;
-        if ((pad4 - R4 - s->hier_win_rem) % A || (pad4 - s->hier_cur_rem) % A || pad4 - R4 - s->hier_win_rem < 0 ||
-            s->hier_smem > 48 * 1024) {
-            xg_set_error(XIN_GPU_ERR_ARG, "stream_open: search by levels: window boxes off the 16-byte grid or too large");
+    /* TMA maps of the padded luma slots for the quarter-pel tiles: the box of
+     * tile (bx, by) starts at padded column XG_QP_TW bx (16-byte aligned) */
+    for (int i = 0; i < 2; i++)
+        if (!xg_tma_map_2d(&s->tm_qp[i], s->slot_base[i][0], (int)sizeof(xg_pix), c.width + 2 * pad, c.height + 2 * pad,
+                           s->pitch, XG_QP_BW, XG_QP_TH + 7)) {
+            const int st = xin_gpu_last_status();
             xg_stream_free(s);
-            return XIN_GPU_ERR_ARG;
+            return st;
         }
-        for (int i = 0; i < 2; i++)
-            if (!xg_tma_map_2d(&s->tm_win[i], s->lo_base[i][1], (int)sizeof(xg_pix), ow4, s->lo_rows[1], s->lo_pitch[1],
-                               s->hier_win_pitch, WS) ||
-                !xg_tma_map_2d(&s->tm_cur[i], s->lo_base[i][1], (int)sizeof(xg_pix), ow4, s->lo_rows[1], s->lo_pitch[1],
-                               s->hier_cur_pitch, 16)) {
-                const int st = xin_gpu_last_status();
-                xg_stream_free(s);
-                return st;
-            }
-    }
     if (c.tu_mode == 1) {
         const int st = xg_tu_open(s);
         if (st) { xg_stream_free(s); return st; }
@@ -411,12 +393,12 @@ static void xg_stage_event(cudaEvent_t e, cudaStream_t st, bool capturing)
 static cudaEvent_t xg_stream_last_event(const xin_gpu_stream *s) { return s->set[(s->nsub - 1) & 1].ev1; }
 
 /* quarter-pel planes of slot cur on the low-priority stream, after ev_qfork */
-static int xg_enqueue_qpel(xin_gpu_stream *s, int cur)
+static int xg_enqueue_qpel(xin_gpu_stream *s, int cur, int *status)
 {
     const xin_gpu_stream_cfg &c = s->cfg;
     cudaStreamWaitEvent(s->auxq, s->ev_qfork, 0);
     dim3 grd((c.width + 2 * s->pad - 8 + XG_QP_TW - 1) / XG_QP_TW, (c.height + 2 * s->pad - 8 + XG_QP_TH - 1) / XG_QP_TH);
-    k_qpel_planes<<<grd, 256, 0, s->auxq>>>(s->slot[cur][0], s->qpel[cur]);
+    k_qpel_planes<<<grd, 256, 0, s->auxq>>>(s->tm_qp[cur], s->slot[cur][0], s->qpel[cur], status, s->wait_tries);
     cudaEventRecord(s->ev_qjoin, s->auxq);
     return 1;
 }
@@ -478,11 +460,6 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         if (c.search_mode == 1) {
             XgHierFrameParams hp;
             memset(&hp, 0, sizeof hp);
-            hp.tm_win = s->tm_win[ref]; hp.tm_cur = s->tm_cur[cur];
-            hp.pad4 = s->pad >> 2;
-            hp.win_rem = s->hier_win_rem; hp.win_pitch = s->hier_win_pitch;
-            hp.cur_rem = s->hier_cur_rem; hp.cur_pitch = s->hier_cur_pitch;
-            hp.wait_tries = s->wait_tries;
             hp.cur = s->slot[cur][0]; hp.ref = s->slot[ref][0];
             for (int l = 0; l < 2; l++) { hp.cur_lo[l] = s->lo[cur][l]; hp.ref_lo[l] = s->lo[ref][l]; }
             hp.W = c.width; hp.H = c.height; hp.ctu = c.ctu_size; hp.R = c.search_range;
@@ -495,7 +472,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
                 nz++;
             }
             dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, nz);
-            k_hier_frame<<<grd, XG_HIER_THREADS, s->hier_smem, st>>>(hp, t.dpp, &t.dpp->status);
+            k_hier_frame<<<grd, XG_HIER_THREADS, xg_hier_smem(c.search_range), st>>>(hp, t.dpp);
         } else {
         XgMeParams mp;
         mp.cur = s->slot[cur][0];
@@ -516,7 +493,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             k_me_tiles<8><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, t.dpp);
         }
         nl++;
-        nl += xg_enqueue_qpel(s, cur);
+        nl += xg_enqueue_qpel(s, cur, &t.dpp->status);
         /* the search's end is recorded on a side branch joined at the picture's
          * end: a timing node between the search and the tails' fork held the tails
          * back by about 0.03 ms */
@@ -572,7 +549,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         cudaStreamWaitEvent(st, s->ev_tjoin, 0);
         xg_stage_event(t.evs[3], st, capturing);
     } else {
-        nl += xg_enqueue_qpel(s, cur);
+        nl += xg_enqueue_qpel(s, cur, &t.dpp->status);
         cudaStreamWaitEvent(st, s->ev_qjoin, 0);
         xg_stage_event(t.evs[2], st, capturing);
         xg_stage_event(t.evs[3], st, capturing);

@@ -16,6 +16,7 @@
  *                    dequant, inverse DCT2, reconstruction, SSD
  */
 #include "xg_device.cuh"
+#include "xg_tma.cuh"
 
 /* ------------------------------------------------------------------ layout */
 struct XgPlane {            /* padded plane: data points at picture (0, 0) */
@@ -51,33 +52,58 @@ __host__ __device__ constexpr int xg_qp_tap(int f, int k)
  * a sliding window of STRIP + 7 values of each vertical source (the integer
  * samples, the three first-stage phases) gives the 12 planes with fy != 0, one
  * 8-tap sum per sample. */
+/* device status bits of a picture */
+#define XG_STATUS_TMA_WAIT 1                    /* a TMA load did not complete within its wait bound */
+
 #define XG_QP_TW 64
 #define XG_QP_TH 32
 #define XG_QP_STRIP 8
+/* staged tile row: the TW + 7 samples a tile needs start one sample into a
+ * 16-byte-aligned TMA box (padded-plane column 1 + TW bx) */
+#define XG_QP_BW ((XG_QP_TW + 8 + 16 / (int)sizeof(xg_pix) - 1) / (16 / (int)sizeof(xg_pix)) * (16 / (int)sizeof(xg_pix)))
 static_assert(XG_QP_TW * (XG_QP_TH / XG_QP_STRIP) == 256, "pass 2 gives every thread of the CTA one column strip");
-__global__ void __launch_bounds__(256) k_qpel_planes(XgPlane ref, XgQpel qp)
+__global__ void __launch_bounds__(256) k_qpel_planes(const __grid_constant__ CUtensorMap tm, XgPlane ref, XgQpel qp,
+                                                      int *status, long long wait_tries)
 {
     constexpr int TW = XG_QP_TW, TH = XG_QP_TH, HR = TH + 7, ST = XG_QP_STRIP;
-    __shared__ xg_pix tile[HR][TW + 8];
+    __shared__ __align__(128) xg_pix tbox[HR][XG_QP_BW];
     __shared__ int16_t hs[3][HR][TW];
+    __shared__ unsigned long long tbar;
+    __shared__ int tok;
     const int lo = -(qp.pad - 4);                            /* first output position (x and y) */
     const int xe = qp.w + qp.pad - 4, ye = qp.h + qp.pad - 4; /* one past the last */
     const int x0 = lo + (int)blockIdx.x * TW, y0 = lo + (int)blockIdx.y * TH;
     const intptr_t pitch = qp.pitch;
-    /* stage rows y0-3 .. y0+TH+3 and columns x0-3 .. x0+TW+4, inside the padded allocation */
-    for (int i = threadIdx.x; i < HR * (TW + 7); i += blockDim.x) {
-        int r = i / (TW + 7), c = i - r * (TW + 7);
-        int gy = y0 - 3 + r, gx = x0 - 3 + c;
-        bool in = gy >= -ref.pad && gy < ref.h + ref.pad && gx >= -ref.pad && gx < ref.w + ref.pad;
-        tile[r][c] = in ? ref.data[(intptr_t)gy * ref.pitch + gx] : (xg_pix)0;
+    /* rows y0-3 .. y0+TH+3 and columns x0-3 .. x0+TW+4 of the padded plane by TMA
+     * (zeros outside it): the box starts one column earlier, at padded column TW bx */
+    if (threadIdx.x == 0) {
+        xg_mbar_init(&tbar, 1);
+        xg_mbar_expect_tx(&tbar, (uint32_t)sizeof tbox);
+        xg_tma_load_2d(&tbox[0][0], &tm, (int)blockIdx.x * TW, (int)blockIdx.y * TH + 1, &tbar);
+        tok = xg_mbar_wait(&tbar, 0, wait_tries) ? 1 : 0;
+        if (!tok) {
+            /* report; once the copy has landed, stage the tile with plain loads */
+            atomicOr(status, XG_STATUS_TMA_WAIT);
+            tok = xg_mbar_wait(&tbar, 0, XG_TMA_WAIT_TRIES) ? 2 : 0;
+        }
     }
     __syncthreads();
+    if (!tok) return;
+    if (tok == 2) {
+        for (int i = threadIdx.x; i < HR * (TW + 7); i += blockDim.x) {
+            const int r = i / (TW + 7), c = i - r * (TW + 7), gy = y0 - 3 + r, gx = x0 - 3 + c;
+            const bool in = gy >= -ref.pad && gy < ref.h + ref.pad && gx >= -ref.pad && gx < ref.w + ref.pad;
+            tbox[r][c + 1] = in ? ref.data[(intptr_t)gy * ref.pitch + gx] : (xg_pix)0;
+        }
+        __syncthreads();
+    }
+    auto tile = [&](int r, int c) -> int { return tbox[r][c + 1]; };
     constexpr int sh1 = XG_IF_SHIFT - XG_IF_HEAD;
     for (int i = threadIdx.x; i < HR * TW; i += blockDim.x) {
         const int r = i / TW, c = i % TW;
         int a[8];
 #pragma unroll
-        for (int k = 0; k < 8; k++) a[k] = tile[r][c + k];
+        for (int k = 0; k < 8; k++) a[k] = tile(r, c + k);
         int sum[3];
 #pragma unroll
         for (int f = 0; f < 3; f++) {
@@ -101,7 +127,7 @@ __global__ void __launch_bounds__(256) k_qpel_planes(XgPlane ref, XgQpel qp)
     for (int src = 0; src < 4; src++) {                      /* 0: integer samples, 1..3: first-stage phase src - 1 */
         int w[ST + 7];
 #pragma unroll
-        for (int k = 0; k < ST + 7; k++) w[k] = src == 0 ? (int)tile[oy0 + k][c + 3] : (int)hs[src - 1][oy0 + k][c];
+        for (int k = 0; k < ST + 7; k++) w[k] = src == 0 ? tile(oy0 + k, c + 3) : (int)hs[src - 1][oy0 + k][c];
 #pragma unroll
         for (int j = 0; j < ST; j++) {
             if (j >= nrow) break;
@@ -162,9 +188,6 @@ struct XgPicParams {
     long long src_stride[3];
     int32_t dq_qp[2];                   /* preset-4 TU stage: luma / chroma QP the trellis gets */
 };
-
-/* device status bits of a picture */
-#define XG_STATUS_TMA_WAIT 1                    /* a TMA load did not complete within its wait bound */
 
 /* Sources of k_fill_slot: where a picture's samples come from */
 enum XgFillMode {

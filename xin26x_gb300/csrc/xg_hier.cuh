@@ -24,8 +24,6 @@
  * stream is opened with search_mode 1.
  */
 
-#include "xg_tma.cuh"
-
 /* (a + b + c + d + 2) >> 2 over the 2x2 block at (2x, 2y) */
 __global__ void k_downscale2x2(const xg_pix *in, long long ip, xg_pix *out, long long op, int ow, int oh)
 {
@@ -278,8 +276,8 @@ extern "C" void XinGpuMotionEstHier(struct xin_me_struct *meSetOpaque)
 /* ------------------------------------------------------------ frame form
  * One CTA per (64 x 64 tile, CU level): the tile's CUs of that level.  The
  * quarter-resolution reference window of the whole tile (16 + 2 R4 samples
- * square, R4 = R >> 2, and 4 more columns) and the tile's quarter-resolution
- * current samples are loaded into shared memory by TMA.  A group of
+ * square, R4 = R >> 2, rows padded by 4 samples) and the tile's
+ * quarter-resolution current samples are staged in shared memory.  A group of
  * G warps takes a CU (G = 8 / CUs a tile, at least 1): at 1/4 each lane
  * evaluates four horizontally adjacent candidates at a time from a sliding
  * window of reference samples; the 1/2 and full-resolution steps split the
@@ -287,33 +285,13 @@ extern "C" void XinGpuMotionEstHier(struct xin_me_struct *meSetOpaque)
  * the CU's key (cost << 32) | ((mvy + R) * (2R + 1) + mvx + R), the form the
  * tails read. */
 struct XgHierFrameParams {
-    CUtensorMap tm_win;          /* the reference's 1/4 plane, box win_pitch x (16 + 2 R4) */
-    CUtensorMap tm_cur;          /* the current picture's 1/4 plane, box cur_pitch x 16 */
     XgPlane cur, ref;            /* full-resolution luma slots */
     XgPlane cur_lo[2], ref_lo[2];/* 1/2 and 1/4 resolution (pointers at picture (0, 0)) */
     int W, H, ctu, R;
     int level_size[4];           /* CU size of blockIdx.z */
     unsigned long long *keys[4];
     int cus_x[4];
-    /* the 1/4 planes' margin, and per box the samples before the first one used
-     * (the box starts 16-byte aligned) and its row pitch in shared memory */
-    int pad4, win_rem, win_pitch, cur_rem, cur_pitch;
-    long long wait_tries;        /* bound of the wait for the TMA loads (polls) */
 };
-
-/* the TMA box geometry of the 1/4-resolution window and current tile for a
- * stream: rem = samples before the used ones, pitch = box width (a multiple
- * of 16 bytes); shared memory of k_hier_frame */
-static void xg_hier_boxes(int pad, int R, int *win_rem, int *win_pitch, int *cur_rem, int *cur_pitch, size_t *smem)
-{
-    const int A = 16 / (int)sizeof(xg_pix), pad4 = pad >> 2, R4 = R >> 2, WS = 16 + 2 * R4;
-    *win_rem = ((pad4 - R4) % A + A) % A;
-    *win_pitch = (*win_rem + WS + 4 + A - 1) / A * A;
-    *cur_rem = pad4 % A;
-    *cur_pitch = (*cur_rem + 16 + A - 1) / A * A;
-    const size_t wb = ((size_t)*win_pitch * WS * sizeof(xg_pix) + 127) & ~(size_t)127;
-    *smem = 128 + wb + (size_t)*cur_pitch * 16 * sizeof(xg_pix);
-}
 
 #define XG_HIER_THREADS 256
 
@@ -339,52 +317,31 @@ __device__ __forceinline__ void xg_sad_3x3(const xg_pix *c, long long cp, const 
     }
 }
 
-__global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(const __grid_constant__ XgHierFrameParams p,
-                                                               const XgPicParams *pp, int *status)
+__global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(XgHierFrameParams p, const XgPicParams *pp)
 {
-    extern __shared__ __align__(128) unsigned char hraw[];
+    extern __shared__ __align__(16) xg_pix hs[];
     __shared__ unsigned long long wmin[8];
     __shared__ uint32_t wsum[8][10];
-    __shared__ unsigned long long tbar;
-    __shared__ int tok;
     const int S = p.level_size[blockIdx.z];
     const int lgS = S == 64 ? 6 : S == 32 ? 5 : S == 16 ? 4 : 3;
     unsigned long long *keys = p.keys[blockIdx.z];
     const int cus_x = p.cus_x[blockIdx.z];
-    const int R = p.R, R4 = R >> 2, WS = 16 + 2 * R4, WP = p.win_pitch, CP = p.cur_pitch;   /* window side, row pitches */
+    const int R = p.R, R4 = R >> 2, WS = 16 + 2 * R4, WP = WS + 4;   /* window side, row pitch */
     const int tx0 = blockIdx.x * 64, ty0 = blockIdx.y * 64;
+    xg_pix *win = hs, *cur4 = hs + WS * WP;                  /* [WS][WP], [16][16] */
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t lambda = pp->lambda;
-    /* the tile's 1/4-resolution reference window (WS rows, the four columns past
-     * it feed only candidates beyond it) and current samples, by TMA from
-     * 16-byte-aligned columns: the used samples start rem samples into each row */
-    xg_pix *wbuf = reinterpret_cast<xg_pix *>(((uintptr_t)hraw + 127) & ~(uintptr_t)127);
-    xg_pix *cbuf = wbuf + (((size_t)WP * WS * sizeof(xg_pix) + 127) & ~(size_t)127) / sizeof(xg_pix);
-    const xg_pix *win = wbuf + p.win_rem, *cur4 = cbuf + p.cur_rem;
-    if (tid == 0) {
-        xg_mbar_init(&tbar, 1);
-        xg_mbar_expect_tx(&tbar, (uint32_t)((WP * WS + CP * 16) * sizeof(xg_pix)));
-        xg_tma_load_2d(wbuf, &p.tm_win, tx0 / 4 - R4 + p.pad4 - p.win_rem, ty0 / 4 - R4 + p.pad4, &tbar);
-        xg_tma_load_2d(cbuf, &p.tm_cur, tx0 / 4 + p.pad4 - p.cur_rem, ty0 / 4 + p.pad4, &tbar);
-        const bool ok = xg_mbar_wait(&tbar, 0, p.wait_tries);
-        if (!ok) {
-            /* report, and let the copies in flight land before the CTA leaves */
-            atomicOr(status, XG_STATUS_TMA_WAIT);
-            xg_mbar_wait(&tbar, 0, XG_TMA_WAIT_TRIES);
+    {
+        const xg_pix *src = p.ref_lo[1].data + (long long)(ty0 / 4 - R4) * p.ref_lo[1].pitch + (tx0 / 4 - R4);
+        for (int i = tid; i < WS * WP; i += XG_HIER_THREADS) {
+            const int y = i / WP, x = i - y * WP;
+            /* the four columns past the window feed only candidates beyond it */
+            win[i] = x < WS ? src[(long long)y * p.ref_lo[1].pitch + x] : (xg_pix)0;
         }
-        tok = ok;
+        const xg_pix *cs = p.cur_lo[1].data + (long long)(ty0 / 4) * p.cur_lo[1].pitch + tx0 / 4;
+        for (int i = tid; i < 256; i += XG_HIER_THREADS) cur4[i] = cs[(long long)(i >> 4) * p.cur_lo[1].pitch + (i & 15)];
     }
     __syncthreads();
-    if (!tok) {
-        /* no search: the tile's CUs get the zero vector at the highest cost */
-        const int per_row = 64 >> lgS;
-        for (int c = tid; c < per_row * per_row; c += XG_HIER_THREADS) {
-            const int cu_x = tx0 + (c % per_row) * S, cu_y = ty0 + (c / per_row) * S;
-            if (cu_x + S <= p.W && cu_y + S <= p.H)
-                keys[(cu_y >> lgS) * cus_x + (cu_x >> lgS)] = ~0ull << 32 | (uint32_t)(R * (2 * R + 1) + R);
-        }
-        return;
-    }
     const int per_row = 64 >> lgS, ncu = per_row * per_row;
     const int G = ncu >= 8 ? 1 : 8 / ncu;                     /* warps per CU */
     const int slots = 8 / G;                                  /* CUs in flight */
@@ -424,7 +381,7 @@ __global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(const __grid_con
         unsigned long long k = ~0ull;
         if (nx4 > 0 && ny4 > 0) {
             const int qpr = (nx4 + 3) >> 2, nq = qpr * ny4;      /* quads per row, quads */
-            const xg_pix *cb = cur4 + (cyi >> 2) * CP + (cxi >> 2);
+            const xg_pix *cb = cur4 + (cyi >> 2) * 16 + (cxi >> 2);
             const xg_pix *wb = win + ((cyi >> 2) + R4 + ly4) * WP + (cxi >> 2) + R4 + lx4;
             int qy = gt / qpr, qx = gt - qy * qpr;              /* this lane's first quad */
             const int sy = gn / qpr, sx = gn - sy * qpr;        /* its step */
@@ -432,7 +389,7 @@ __global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(const __grid_con
                 const xg_pix *r = wb + qy * WP + 4 * qx;
                 uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
                 for (int yy = 0; yy < b4; yy++) {
-                    const xg_pix *cr = cb + yy * CP, *rr = r + yy * WP;
+                    const xg_pix *cr = cb + yy * 16, *rr = r + yy * WP;
                     unsigned w0 = rr[0], w1 = rr[1], w2 = rr[2];
                     for (int j = 0; j < b4; j++) {
                         const unsigned w3 = rr[j + 3], cv = cr[j];
@@ -504,3 +461,8 @@ __global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(const __grid_con
 }
 
 /* shared memory of k_hier_frame for search range R */
+static size_t xg_hier_smem(int R)
+{
+    const int ws = 16 + 2 * (R >> 2);
+    return (size_t)(ws * (ws + 4) + 256) * sizeof(xg_pix);
+}
