@@ -629,6 +629,38 @@ def preset4_bench(torch, flush, frames, steps, warmup, cpu_seconds=8.0):
            "gpu_launches_per_picture": launches, "l2": "flushed between pictures (512 MB write outside the timed events)",
            "not_covered": "random access with bi-prediction and DMVR (built per call, not in the frame form), BT/TT "
                           "and 4x4 / 128x128 CUs, RDOQ, the host's choice among the candidates"}
+    # end to end through the public API with host buffers, two pictures in flight: the
+    # TU stage of picture k (its own picture set, stream and TU state) runs beside the
+    # search and tails of picture k + 1.  The working set of a picture (its TU state,
+    # about 0.5 GB) is above L2.
+    from xin26x_gb300.frame import FrameStream
+    fs = FrameStream(W, H, search_range=SEARCH, levels=LEVELS, out_q=True, out_rec=False, use_graph=True, bitdepth=BD,
+                     input_bitdepth=IN_BD, search_mode=1, tu_mode=1, contexts=ctx)
+    n_e2e = max(steps, 10)
+    h2d = W * H * 3 // 2
+    d2h = fs.ncus * (64 + 64) + sum((W * H if p == 0 else W * H // 4) * len(LEVELS) * 4 for p in range(3))
+
+    def e2e_submit(k):
+        qp = QPS[k % 3]
+        fs.submit(*frames[k % len(frames)], qp=qp, uv_qp=qp, sad_lambda=LAMBDA_BD[qp])
+
+    e2e_submit(0)
+    fs.wait(copy=False)
+    e2e_submit(1)
+    for k in range(max(3, warmup)):
+        e2e_submit(k + 2)
+        fs.wait(copy=False)
+    t0 = time.perf_counter()
+    for k in range(n_e2e):
+        e2e_submit(k + 2 + max(3, warmup))
+        fs.wait(copy=False)
+    el = time.perf_counter() - t0
+    fs.wait(copy=False)
+    fs.close()
+    out["e2e_two_in_flight"] = {"value": W * H * n_e2e / el / 1e6, "unit": "Mpixel/s", "pictures": n_e2e,
+                                "ms_per_picture": el * 1e3 / n_e2e, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                                "note": "host 8-bit planes in, CU records, per-CU transform-candidate records and "
+                                        "coefficient planes out; wall clock over the pictures"}
     # the oracle on the same pictures: random 64x64 CTUs, all four levels, one core
     from tests import oracle_frame
     cur, ref = [tuple(p.astype(np.uint16) << (BD - IN_BD) for p in f) for f in (frames[1], frames[0])]

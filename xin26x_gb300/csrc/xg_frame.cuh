@@ -54,6 +54,9 @@ struct xin_gpu_stream {
         cudaEvent_t ev_kern;   /* kernels done (the copy stream waits on it) */
         cudaEvent_t ev_up;     /* the picture's parameters / staged samples are on the device */
         cudaEvent_t evs[5];    /* stage boundaries, recorded inside the picture's launches */
+        cudaStream_t pst;      /* the picture's launches (a stream per set, so that the TU stage of
+                                  one picture runs beside the next picture's search and tails) */
+        cudaEvent_t ev_main;   /* the picture's reference planes, search and tails are done */
     } set[2];
     cudaStream_t st;
     cudaStream_t cst;      /* result copies (device to host) */
@@ -72,10 +75,10 @@ struct xin_gpu_stream {
     int nsub;              /* pictures submitted */
     int ndone;             /* pictures collected by frame_wait (the oldest first) */
     int graph_launches[2]; /* kernels inside each captured graph */
-    XgTuState *tu;         /* tu_mode 1 */
+    XgTuState *tu[2];      /* tu_mode 1: per picture set */
 };
 
-static int xg_tu_open(xin_gpu_stream *s);
+static int xg_tu_open(xin_gpu_stream *s, int set);
 static void xg_tu_free(XgTuState *u);
 static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cudaStream_t st);
 static uint64_t xg_tu_bytes(const xin_gpu_stream_cfg *c);
@@ -102,6 +105,7 @@ static int xg_stream_free(xin_gpu_stream *s)
     if (!s) return XIN_GPU_OK;
     if (s->ust) cudaStreamSynchronize(s->ust);
     if (s->st) cudaStreamSynchronize(s->st);
+    for (auto &t : s->set) if (t.pst) cudaStreamSynchronize(t.pst);
     if (s->cst) cudaStreamSynchronize(s->cst);
     for (int i = 0; i < 2; i++) if (s->gexec[i]) cudaGraphExecDestroy(s->gexec[i]);
     for (int i = 0; i < 2; i++) {
@@ -110,7 +114,8 @@ static int xg_stream_free(xin_gpu_stream *s)
         for (int l = 0; l < 2; l++) cudaFree(s->lo_base[i][l]);
     }
     cudaFree(s->keys);
-    xg_tu_free(s->tu);
+    xg_tu_free(s->tu[0]);
+    xg_tu_free(s->tu[1]);
     for (auto &t : s->set) {
         cudaFree(t.dres); cudaFree(t.dpp); cudaFree(t.dmts); cudaFreeHost(t.h_mts);
         for (int p = 0; p < 3; p++) { cudaFree(t.dq[p]); cudaFree(t.drec[p]); cudaFree(t.d_in8[p]); cudaFreeHost(t.h_in[p]); cudaFreeHost(t.h_q[p]); cudaFreeHost(t.h_rec[p]); }
@@ -120,6 +125,8 @@ static int xg_stream_free(xin_gpu_stream *s)
         if (t.ev1) cudaEventDestroy(t.ev1);
         if (t.ev_kern) cudaEventDestroy(t.ev_kern);
         if (t.ev_up) cudaEventDestroy(t.ev_up);
+        if (t.ev_main) cudaEventDestroy(t.ev_main);
+        if (t.pst) cudaStreamDestroy(t.pst);
     }
     if (s->cst) cudaStreamDestroy(s->cst);
     if (s->ust) cudaStreamDestroy(s->ust);
@@ -204,6 +211,8 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.ev_kern, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.ev_up, cudaEventDisableTiming);
         for (int i = 0; i < 5 && e == cudaSuccess; i++) e = cudaEventCreate(&t.evs[i]);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&t.pst, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.ev_main, cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_qfork, cudaEventDisableTiming);
@@ -240,8 +249,8 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
             if (e == cudaSuccess) e = cudaMalloc(&t.drec[p], n * sizeof(xg_pix));
             /* the kernels write only the area a level's CUs cover: the rest stays zero
              * (ordered on the stream, before any picture's launches) */
-            if (e == cudaSuccess) e = cudaMemsetAsync(t.dq[p], 0, n * sizeof(xg_coef), s->st);
-            if (e == cudaSuccess) e = cudaMemsetAsync(t.drec[p], 0, n * sizeof(xg_pix), s->st);
+            if (e == cudaSuccess) e = cudaMemsetAsync(t.dq[p], 0, n * sizeof(xg_coef), t.pst);
+            if (e == cudaSuccess) e = cudaMemsetAsync(t.drec[p], 0, n * sizeof(xg_pix), t.pst);
             if (c.device_io) continue;
             if (e == cudaSuccess && s->widen) e = cudaMalloc(&t.d_in8[p], p ? lc : lq);
             if (e == cudaSuccess) e = cudaMallocHost(&t.h_in[p], (p ? lc : lq) * s->in_es);
@@ -353,10 +362,11 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
             xg_stream_free(s);
             return st;
         }
-    if (c.tu_mode == 1) {
-        const int st = xg_tu_open(s);
-        if (st) { xg_stream_free(s); return st; }
-    }
+    if (c.tu_mode == 1)
+        for (int i = 0; i < 2; i++) {
+            const int st = xg_tu_open(s, i);
+            if (st) { xg_stream_free(s); return st; }
+        }
     *out = s;
     return XIN_GPU_OK;
 }
@@ -408,9 +418,14 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
 {
     const xin_gpu_stream_cfg &c = s->cfg;
     xin_gpu_stream::Set &t = s->set[cur];
-    cudaStream_t st = s->st;
+    cudaStream_t st = t.pst;
     size_t lq = (size_t)c.width * c.height, lc = lq / 4;
     int nl = 0;
+    /* the previous picture (the other set, on its own stream) must have finished
+     * with the planes this picture overwrites: its reference slot, quarter-pel and
+     * downscaled planes, the search keys; its TU stage may still run */
+    if (capturing) cudaStreamWaitEvent(st, s->set[1 - cur].ev_main, cudaEventWaitExternal);
+    else cudaStreamWaitEvent(st, s->set[1 - cur].ev_main, 0);
     /* upload and pad the current picture; it becomes the next picture's reference */
     xg_stage_event(t.evs[0], st, capturing);
     /* the parameters and (8-bit input) the staged samples were uploaded on the
@@ -524,8 +539,8 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             }
             tp.res = t.dres;
             for (int p = 0; p < 3; p++) tp.resid[p] = nullptr;
-            if (s->tu)
-                for (int p = 0; p < 3; p++) tp.resid[p] = xg_tu_resid(s->tu, L, p);
+            if (s->tu[cur])
+                for (int p = 0; p < 3; p++) tp.resid[p] = xg_tu_resid(s->tu[cur], L, p);
             int n = s->lev_cx[L] * s->lev_cy[L];
             if (n > 0) {
                 /* 64 and 32: a 128-thread CTA per CU; 16 and 8: a warp per CU, four CUs per
@@ -544,13 +559,15 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             cudaEventRecord(s->ev_join[i], s->aux[i]);
             cudaStreamWaitEvent(st, s->ev_join[i], 0);
         }
-        if (s->tu) nl += xg_tu_enqueue(s, cur, t, st);
         cudaStreamWaitEvent(st, s->ev_qjoin, 0);
         cudaStreamWaitEvent(st, s->ev_tjoin, 0);
+        xg_stage_event(t.ev_main, st, capturing);
+        if (s->tu[cur]) nl += xg_tu_enqueue(s, cur, t, st);
         xg_stage_event(t.evs[3], st, capturing);
     } else {
         nl += xg_enqueue_qpel(s, cur, &t.dpp->status);
         cudaStreamWaitEvent(st, s->ev_qjoin, 0);
+        xg_stage_event(t.ev_main, st, capturing);
         xg_stage_event(t.evs[2], st, capturing);
         xg_stage_event(t.evs[3], st, capturing);
     }
@@ -563,7 +580,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
 static void xg_enqueue_results(xin_gpu_stream *s, xin_gpu_stream::Set &t, bool with_me)
 {
     const xin_gpu_stream_cfg &c = s->cfg;
-    cudaEventRecord(t.ev_kern, s->st);
+    cudaEventRecord(t.ev_kern, t.pst);
     cudaStreamWaitEvent(s->cst, t.ev_kern, 0);
     if (with_me && !c.device_io) {
         size_t lq = (size_t)c.width * c.height, lc = lq / 4;
@@ -631,7 +648,7 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
     }
     *t.h_pp = pp;
     bool with_me = s->nsub > 0;
-    cudaEventRecord(t.ev0, s->st);
+    cudaEventRecord(t.ev0, t.pst);
     /* uploads on their own stream, so that they overlap the previous picture's
      * kernels: set cur is not read by the picture in flight (it uses the other
      * set), and its last user, picture nsub - 2, has completed */
@@ -642,18 +659,18 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
             cudaMemcpyAsync(t.d_in8[p], t.h_in[p], (size_t)pl.w * pl.h, cudaMemcpyHostToDevice, s->ust);
         }
     cudaEventRecord(t.ev_up, s->ust);
-    cudaStreamWaitEvent(s->st, t.ev_up, 0);
+    cudaStreamWaitEvent(t.pst, t.ev_up, 0);
     if (with_me && c.use_graph) {
         if (!s->gexec[cur]) {
             cudaGraph_t g;
-            if (xg_cuda_check(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal), "begin capture")) return XIN_GPU_ERR_CUDA;
+            if (xg_cuda_check(cudaStreamBeginCapture(t.pst, cudaStreamCaptureModeThreadLocal), "begin capture")) return XIN_GPU_ERR_CUDA;
             s->graph_launches[cur] = xg_enqueue_picture(s, cur, true, true);
-            if (xg_cuda_check(cudaStreamEndCapture(s->st, &g), "end capture")) return XIN_GPU_ERR_CUDA;
+            if (xg_cuda_check(cudaStreamEndCapture(t.pst, &g), "end capture")) return XIN_GPU_ERR_CUDA;
             cudaError_t e = cudaGraphInstantiate(&s->gexec[cur], g, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(g);
             if (xg_cuda_check(e, "graph instantiate")) return XIN_GPU_ERR_CUDA;
         }
-        if (xg_cuda_check(cudaGraphLaunch(s->gexec[cur], s->st), "graph launch")) return XIN_GPU_ERR_CUDA;
+        if (xg_cuda_check(cudaGraphLaunch(s->gexec[cur], t.pst), "graph launch")) return XIN_GPU_ERR_CUDA;
         xg_count_launch((uint64_t)s->graph_launches[cur]);
     } else {
         xg_count_launch((uint64_t)xg_enqueue_picture(s, cur, with_me, false));

@@ -52,7 +52,7 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
                  2 * (sizeof(xin_gpu_cu_result) * ncus + sizeof(XgPicParams) + (lq + 2 * lc) * nlev * (sizeof(xg_coef) + sizeof(xg_pix)));
     if (widen && !c->device_io) d += 2 * (lq + 2 * lc);     /* 8-bit device staging per set */
     if (c->tu_mode == 1) {                                  /* the preset-4 TU stage */
-        d += xg_tu_bytes(c) + 2 * sizeof(xin_gpu_cu_mts) * ncus;
+        d += 2 * xg_tu_bytes(c) + 2 * sizeof(xin_gpu_cu_mts) * ncus;   /* a TU state per picture set */
     }
     if (c->search_mode == 1)                                /* 1/2 and 1/4 resolution luma of both slots */
         for (int l = 0; l < 2; l++)

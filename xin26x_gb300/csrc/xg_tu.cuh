@@ -274,7 +274,9 @@ static void xg_tu_default_contexts(std::vector<xin_gpu_prob> &v)
     for (auto &p : v) { p.state[0] = (uint16_t)(512 << 5); p.state[1] = (uint16_t)(8192 << 1); p.rate = 0x55; }
 }
 
-static int xg_tu_open(xin_gpu_stream *s)
+/* the TU state of picture set `set` (each set has its own, so that the TU
+ * stages of two pictures in flight can overlap) */
+static int xg_tu_open(xin_gpu_stream *s, int set)
 {
     const xin_gpu_stream_cfg &c = s->cfg;
     XgTuState *u = new (std::nothrow) XgTuState();
@@ -343,7 +345,7 @@ static int xg_tu_open(xin_gpu_stream *s)
     }
     int st = xin_gpu_dq_plan_create(blocks.data(), nblk, coef, 1, &u->plan);
     if (st) { xg_tu_free(u); return st; }
-    s->tu = u;
+    s->tu[set] = u;
     return XIN_GPU_OK;
 }
 
@@ -371,7 +373,7 @@ static void xg_tu_launch(const XgTuLevel &lv, int pl, bool fwd, cudaStream_t st)
 /* the TU stage of the picture in slot cur (picture set t), on st; returns launches */
 static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cudaStream_t st)
 {
-    XgTuState *u = s->tu;
+    XgTuState *u = s->tu[cur];
     const xin_gpu_stream_cfg &c = s->cfg;
     const size_t lq = (size_t)c.width * c.height, lc = lq / 4;
     int nl = 0;
@@ -424,8 +426,11 @@ extern "C" int xin_gpu_stream_set_contexts(xin_gpu_stream *s, const xin_gpu_prob
 {
     xin_gpu_clear_error();
     if (!s || !ctx) { xg_set_error(XIN_GPU_ERR_ARG, "stream_set_contexts: null argument"); return XIN_GPU_ERR_ARG; }
-    if (!s->tu) { xg_set_error(XIN_GPU_ERR_STATE, "stream_set_contexts: the stream has no preset-4 TU stage (tu_mode 0)"); return XIN_GPU_ERR_STATE; }
+    if (!s->tu[0]) { xg_set_error(XIN_GPU_ERR_STATE, "stream_set_contexts: the stream has no preset-4 TU stage (tu_mode 0)"); return XIN_GPU_ERR_STATE; }
     if (s->nsub != s->ndone) { xg_set_error(XIN_GPU_ERR_STATE, "stream_set_contexts: pictures in flight"); return XIN_GPU_ERR_STATE; }
-    return xg_cuda_check(cudaMemcpy(s->tu->ctx, ctx, XIN_GPU_NUM_CTX * sizeof(xin_gpu_prob), cudaMemcpyHostToDevice),
-                         "stream_set_contexts");
+    for (int i = 0; i < 2; i++)
+        if (xg_cuda_check(cudaMemcpy(s->tu[i]->ctx, ctx, XIN_GPU_NUM_CTX * sizeof(xin_gpu_prob), cudaMemcpyHostToDevice),
+                          "stream_set_contexts"))
+            return XIN_GPU_ERR_CUDA;
+    return XIN_GPU_OK;
 }
