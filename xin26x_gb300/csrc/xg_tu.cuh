@@ -379,6 +379,24 @@ static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cud
     int nl = 0;
     XgTuLevel lv[4];
     int li = 0;
+    /* the levels' transforms are independent: level i after the first runs on
+     * auxiliary stream i - 1 (fork here, join before the trellis and again at
+     * the end) */
+    cudaStream_t ls[4];
+    int nls = 0;
+    cudaEventRecord(s->ev_fork, st);
+    for (int L = 0; L < 4; L++) {
+        if (!s->lev_on[L]) continue;
+        ls[L] = nls == 0 ? st : s->aux[nls - 1];
+        if (nls > 0) cudaStreamWaitEvent(ls[L], s->ev_fork, 0);
+        nls++;
+    }
+    auto join = [&]() {
+        for (int i = 0; i + 1 < nls; i++) {
+            cudaEventRecord(s->ev_join[i], s->aux[i]);
+            cudaStreamWaitEvent(st, s->ev_join[i], 0);
+        }
+    };
     for (int L = 0; L < 4; L++) {
         if (!s->lev_on[L]) continue;
         XgTuLevel &v = lv[L];
@@ -400,25 +418,30 @@ static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cud
         v.W = c.width; v.S = XG_LEVEL_SIZE[L]; v.cus_x = s->lev_cx[L]; v.ncu = s->lev_cx[L] * s->lev_cy[L]; v.nc = u->nc[L];
         li++;
         if (v.ncu == 0) continue;
-        for (int p = 0; p < 3; p++) { xg_tu_launch(v, p, true, st); nl++; }
+        for (int p = 0; p < 3; p++) { xg_tu_launch(v, p, true, ls[L]); nl++; }
     }
+    join();
     k_tu_setqp<<<(u->nblocks + 255) / 256, 256, 0, st>>>(u->plan->d_jobs, u->nblocks, t.dpp);
     nl++;
     xg_dq_enqueue(u->plan->d_jobs, u->plan->d_soff, u->plan->nblocks, u->T, u->Q, u->R, u->nz, u->ctx, 1, u->plan->area,
                   u->plan->ctas, 1, st, false);
     nl += 4;
     cudaMemsetAsync(u->satd, 0, sizeof(uint32_t) * (s->ncus > 0 ? s->ncus : 1), st);
+    cudaEventRecord(s->ev_fork, st);
+    for (int L = 0; L < 4; L++)
+        if (s->lev_on[L] && ls[L] != st) cudaStreamWaitEvent(ls[L], s->ev_fork, 0);
     for (int L = 0; L < 4; L++) {
         if (!s->lev_on[L]) continue;
         XgTuLevel &v = lv[L];
         if (v.ncu == 0) continue;
-        for (int p = 0; p < 3; p++) { xg_tu_launch(v, p, false, st); nl++; }
+        for (int p = 0; p < 3; p++) { xg_tu_launch(v, p, false, ls[L]); nl++; }
         const int tiles = v.ncu * (v.S >> 3) * (v.S >> 3);
-        k_tu_satd<<<(tiles + 255) / 256, 256, 0, st>>>(v, u->satd + s->lev_first[L]);
-        k_tu_collect<<<(v.ncu + 127) / 128, 128, 0, st>>>(v, u->satd + s->lev_first[L], t.dres + s->lev_first[L],
-                                                          t.dmts + s->lev_first[L], t.dpp);
+        k_tu_satd<<<(tiles + 255) / 256, 256, 0, ls[L]>>>(v, u->satd + s->lev_first[L]);
+        k_tu_collect<<<(v.ncu + 127) / 128, 128, 0, ls[L]>>>(v, u->satd + s->lev_first[L], t.dres + s->lev_first[L],
+                                                             t.dmts + s->lev_first[L], t.dpp);
         nl += 2;
     }
+    join();
     return nl;
 }
 
