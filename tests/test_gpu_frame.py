@@ -403,6 +403,40 @@ def test_frame_preset4_tu_matches_oracle(bd, inb, search_mode, w, h, R):
         fs.close()
 
 
+def test_frame_preset4_1080p_two_in_flight():
+    """The bench's preset-4 workload compared in full: bench.py's 1920x1080 pictures
+    (8-bit into the 10-bit library), search by resolution levels, every transform
+    candidate through the trellis with the bench's seeded context set, QPs 32 and
+    37.  Pictures 1 and 2 are in flight together (the TU stage of picture 1 runs
+    beside picture 2's search and tails, each on its own picture set): every CU
+    record, transform-candidate record and plane of both against the oracle on
+    all host cores."""
+    import bench
+    from xin26x_gb300 import synth as S
+    frames = bench.make_frames(3)
+    ctx = np.ascontiguousarray(S.contexts(np.random.default_rng(4), 1)[0])
+    fs = FrameStream(bench.W, bench.H, search_range=bench.SEARCH, levels=bench.LEVELS, out_q=True, out_rec=True,
+                     bitdepth=bench.BD, input_bitdepth=bench.IN_BD, search_mode=1, tu_mode=1, contexts=ctx)
+    try:
+        fs.submit(*frames[0], qp=32, uv_qp=32, sad_lambda=bench.LAMBDA_BD[32])
+        fs.wait()
+        qps = {1: 32, 2: 37}
+        for k in (1, 2):
+            fs.submit(*frames[k], qp=qps[k], uv_qp=qps[k], sad_lambda=bench.LAMBDA_BD[qps[k]])
+        outs = {k: fs.wait() for k in (1, 2)}
+        for k in (1, 2):
+            cur, ref = [tuple(p.astype(np.uint16) << (bench.BD - bench.IN_BD) for p in f) for f in (frames[k], frames[k - 1])]
+            recs, q, rec, mts = oracle_frame.run(cur, ref, fs.levels, search_range=bench.SEARCH, qp=qps[k], uv_qp=qps[k],
+                                                 sad_lambda=bench.LAMBDA_BD[qps[k]], bitdepth=bench.BD, threads=0,
+                                                 search_mode=1, tu_mode=1, contexts=ctx)
+            _compare(outs[k], (recs, q, rec), fs.levels, ("1080p preset 4", k))
+            for name in ("satd_cost", "ncand", "nz", "ssd"):
+                bad = np.nonzero(np.any((outs[k]["mts"][name] != mts[name]).reshape(len(mts), -1), axis=1))[0]
+                assert bad.size == 0, (name, k, bad[:5])
+    finally:
+        fs.close()
+
+
 def test_frame_preset4_tu_qp_limit():
     """The trellis's parameters stop at QP 51: at 10 bits (QP + 12) a slice QP above
     39 is refused before any launch."""
