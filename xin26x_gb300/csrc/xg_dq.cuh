@@ -630,7 +630,8 @@ __device__ __forceinline__ void xg_dq_block(XgDqSmem &sm, int job, const xin_gpu
             for (int j = 0; j < 2; j++) {
                 const uint32_t spk = S[j].pk;
                 const int sref = xg_pk_ref(spk), srem = xg_pk_rem(spk);
-                const uint32_t tv = sref >= 0 ? TP[(sref * 16 + in) * XG_DQ_TPLS] : 0u;
+                const uint32_t tv0 = TP[(max(sref, 0) * 16 + in) * XG_DQ_TPLS];  /* loaded either way: no branch */
+                const uint32_t tv = sref >= 0 ? tv0 : 0u;
                 uint32_t sum = tv & 127u, a1 = (tv >> 7) & 31u;
                 const uint32_t f0 = S[j].F[0] & m.x, f1 = S[j].F[1] & m.y, f2 = S[j].F[2] & m.z, f3 = S[j].F[3] & m.w;
                 sum = __dp4a(S[j].L[0] & m.x, 0x01010101u, sum);
@@ -655,14 +656,16 @@ __device__ __forceinline__ void xg_dq_block(XgDqSmem &sm, int job, const xin_gpu
                 const int xA = rc ? ri[0] : (lvA <= rzero ? lvA - 1 : min(lvA, 31));
                 const int xB = rc ? ri[1] : (lvB <= rzero ? lvB - 1 : min(lvB, 31));
                 const uint32_t rA = (uint32_t)sm.rice[rice][xA], rB = (uint32_t)sm.rice[rice][xB];
-                uint32_t addAB = 0, addZ = 0;
-                bool zok = true;
-                if (ptype == 1) {
-                    const uint32_t sb1 = RT->sbb[xg_pk_sgb(spk)][1];
-                    addAB = sb1 + sg.y; addZ = sb1 + sg.x;
-                } else if (ptype == 0 || xg_pk_ns(spk)) {
-                    addAB = sg.y; addZ = sg.x;
-                } else zok = !rc;
+                /* significance and coded-sub-block rates, by selects (the two states'
+                 * chains then interleave): at a sub-block's first position in scan
+                 * order the sub-block flag, elsewhere the significance flag, except
+                 * at a sub-block's last position with nothing coded yet, where the
+                 * level cannot be zero */
+                const uint32_t sb1 = RT->sbb[xg_pk_sgb(spk)][1];
+                const bool p1 = ptype == 1, sig_on = p1 || ptype == 0 || xg_pk_ns(spk) != 0;
+                const uint32_t addAB = (p1 ? sb1 : 0u) + (sig_on ? sg.y : 0u);
+                const uint32_t addZ = (p1 ? sb1 : 0u) + (sig_on ? sg.x : 0u);
+                const bool zok = !rc || sig_on;
                 const uint32_t tA = rc ? gx[gi[0]] + (lvA >= 4 ? rA : 0u) + addAB : (1u << 15) + rA;
                 const uint32_t tB = rc ? gx[gi[1]] + (lvB >= 4 ? rB : 0u) + addAB : (1u << 15) + rB;
                 const uint32_t tZ = rc ? addZ : (uint32_t)sm.rice[rice][rzero];
@@ -690,9 +693,11 @@ __device__ __forceinline__ void xg_dq_block(XgDqSmem &sm, int job, const xin_gpu
                 int dsel = 7, df = -2, dl = -1;
                 if (c1 < d) { d = c1; dsel = e1; df = f1; dl = g1; }
                 if (c2 < d) { d = c2; dsel = e2; df = f2; dl = g2; }
-                if (ptype == 2) {
+                {
+                    /* skip the sub-block (only at a sub-block's first position in scan order) */
                     const long long c = (long long)sm.skc[t][pi] + (long long)RT->sbb[xg_pk_sgb(sm.skp[t][pi])][0];
-                    if (c < d) { d = c; dsel = 4; df = 4 + t; dl = 0; }
+                    const bool take = (ptype == 2) & (c < d);
+                    d = take ? c : d; dsel = take ? 4 : dsel; df = take ? 4 + t : df; dl = take ? 0 : dl;
                 }
                 {
                     /* start here (the last position): targets 0 and 2 (lane 0), classes 0 and 2;
