@@ -487,13 +487,15 @@ __device__ __forceinline__ XgDqState xg_dq_next(const XgDqState (&S)[2], int h, 
     int r = xg_pk_rem(pp) - 1;
     if (r >= 4) r -= dec;
     int nsg = xg_pk_ns(pp) + (lvv != 0), rf = xg_pk_ref(pp);
-    if (df == -1) {
-        r = regbins;
-        if (in == 0) { if (r >= 4) r -= dec; } else r -= dec;
-        nsg = 1; rf = -1;
-    } else if (df >= 4) {
+    {
+        /* "start here" and "skip", by selects */
+        int r0 = regbins;
+        if (in != 0 || r0 >= 4) r0 -= dec;
         const uint32_t sp = sm.skp[t][pi];
-        r = xg_pk_rem(sp); nsg = 0; rf = xg_pk_ref(sp);
+        const bool st = df == -1, sk = df >= 4;
+        r = st ? r0 : sk ? xg_pk_rem(sp) : r;
+        nsg = st ? 1 : sk ? 0 : nsg;
+        rf = st ? -1 : sk ? xg_pk_ref(sp) : rf;
     }
     ns = nsg; srcref = rf;
     n.cost = dc;
@@ -503,12 +505,14 @@ __device__ __forceinline__ XgDqState xg_dq_next(const XgDqState (&S)[2], int h, 
         n.L[i] = fresh ? 0u : l1 ? S[1].L[i] : S[0].L[i];
         n.F[i] = fresh ? 0u : l1 ? S[1].F[i] : S[0].F[i];
     }
-    if (df > -2 && lvv) {
+    {
         /* the level at this position: clipped to a byte (at a sub-block's first
          * position keeping its parity), and capped at 4 + parity; word in >> 2 by
-         * masks, not by index, so the words stay in registers */
-        const uint32_t b = in ? (uint32_t)min(lvv, 255) : (uint32_t)min(lvv, 254 + (lvv & 1));
-        const uint32_t fb = (uint32_t)min(4 + (lvv & 1), lvv);
+         * masks, not by index, so the words stay in registers.  Without a level
+         * (zero, or no candidate) a zero goes to a byte that is zero already. */
+        const int lvi = df > -2 ? max(lvv, 0) : 0;
+        const uint32_t b = in ? (uint32_t)min(lvi, 255) : (uint32_t)min(lvi, 254 + (lvi & 1));
+        const uint32_t fb = (uint32_t)min(4 + (lvi & 1), lvi);
         const int wi = in >> 2, sh = (in & 3) * 8;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
