@@ -782,14 +782,22 @@ __device__ __forceinline__ void xg_dq_block(XgDqSmem &sm, int job, const xin_gpu
             }
             /* lane 0 keeps target 0 and gives target 2; lane 1 keeps target 3 and gives target 1 */
             {
-                const XgDqState &give = h ? N[0] : N[1];
                 XgDqState got;
-                got.cost = xg_dq_shfl64x(pm, give.cost);
-                got.pk = __shfl_xor_sync(pm, give.pk, 1);
+                got.cost = xg_dq_shfl64x(pm, h ? N[0].cost : N[1].cost);
+                got.pk = __shfl_xor_sync(pm, h ? N[0].pk : N[1].pk, 1);
 #pragma unroll
-                for (int i = 0; i < 4; i++) { got.L[i] = __shfl_xor_sync(pm, give.L[i], 1); got.F[i] = __shfl_xor_sync(pm, give.F[i], 1); }
-                if (h) { S[0] = got; S[1] = N[1]; }
-                else   { S[0] = N[0]; S[1] = got; }
+                for (int i = 0; i < 4; i++) {
+                    got.L[i] = __shfl_xor_sync(pm, h ? N[0].L[i] : N[1].L[i], 1);
+                    got.F[i] = __shfl_xor_sync(pm, h ? N[0].F[i] : N[1].F[i], 1);
+                }
+                /* by selects: the two lanes of a pair take different sides */
+                S[0].cost = h ? got.cost : N[0].cost; S[1].cost = h ? N[1].cost : got.cost;
+                S[0].pk = h ? got.pk : N[0].pk;       S[1].pk = h ? N[1].pk : got.pk;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    S[0].L[i] = h ? got.L[i] : N[0].L[i]; S[1].L[i] = h ? N[1].L[i] : got.L[i];
+                    S[0].F[i] = h ? got.F[i] : N[0].F[i]; S[1].F[i] = h ? N[1].F[i] : got.F[i];
+                }
             }
         }
         cv = nv; ce = ce1; ce1 = ne2; clxy = nlxy;
