@@ -90,6 +90,17 @@ __host__ __device__ constexpr int xg_dq_s4i(int x, int y)
 /* the neighbour template of a position: (x+1, y), (x+2, y), (x+1, y+1), (x, y+1), (x, y+2) */
 __host__ __device__ constexpr int xg_dq_ndx(int u) { return u == 0 || u == 2 ? 1 : u == 1 ? 2 : 0; }
 __host__ __device__ constexpr int xg_dq_ndy(int u) { return u < 2 ? 0 : u == 4 ? 2 : 1; }
+/* scan index of raster position y * 4 + x in a 4x4 sub-block (the inverse of the above) */
+__host__ __device__ constexpr int xg_dq_s4r(int p) { return (int)((0xFDA6EB73C8419520ull >> (4 * p)) & 15); }
+/* scan index of position (x, y) of a square n x n region (n = 4 .. 32): the
+ * sub-block's index in the diagonal order of the (n/4)^2 grid, then the 4x4 scan */
+__host__ __device__ __forceinline__ int xg_dq_scan_sq(int x, int y, int n)
+{
+    const int g = n >> 2, gx = x >> 2, gy = y >> 2, d = gx + gy;
+    const int before = d < g ? d * (d + 1) / 2 : g * g - (2 * g - 1 - d) * (2 * g - d) / 2;
+    const int lo = d - (g - 1) > 0 ? d - (g - 1) : 0;
+    return (before + gx - lo) * 16 + xg_dq_s4r((y & 3) * 4 + (x & 3));
+}
 
 struct XgDqTables {
     uint2 *d_step;              /* per shape, per scan index: position, type, sub-block, context offsets */
@@ -170,12 +181,16 @@ static void xg_dq_init_tables(void)
         xg_dq_diag(4, 4, cx, cy);
         xg_dq_diag(ws, hs, gx, gy);
         for (int i = 0; i < 16; i++)
-            if (cx[i] != xg_dq_s4x(i) || cy[i] != xg_dq_s4y(i)) return;     /* the device's 4x4 scan constants */
+            if (cx[i] != xg_dq_s4x(i) || cy[i] != xg_dq_s4y(i) || xg_dq_s4r(cy[i] * 4 + cx[i]) != i)
+                return;                                                      /* the device's 4x4 scan constants */
         std::vector<int> px(n), py(n), sbs(ws * hs);
         for (int b = 0; b < ws * hs; b++) {
             sbs[gy[b] * ws + gx[b]] = b;
             for (int i = 0; i < 16; i++) { px[b * 16 + i] = gx[b] * 4 + cx[i]; py[b * 16 + i] = gy[b] * 4 + cy[i]; }
         }
+        if (ew == eh)                                                        /* the square regions' scan formula */
+            for (int k = 0; k < n; k++)
+                if (xg_dq_scan_sq(px[k], py[k], ew) != k) return;
         for (int k = 0; k < n; k++) {
             int in = k & 15;
             int ptype = (in == 15 && k > 16 && k < n - 1) ? 1 : (in == 0 && k > 0 && k < n - 16) ? 2 : 0;
@@ -424,6 +439,23 @@ k_dq_prep(const xin_gpu_dq_block *__restrict__ jobs, int njobs, const uint32_t *
             atomicAdd(&hist[best < 0 ? 0 : (best >> 4) + 1], 1);
             if (best < 0) nzout[i] = 0;
         }
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < 66; b += blockDim.x)
+        if (hist[b]) atomicAdd(&counts[b], hist[b]);
+}
+
+/* ---- pass 1 for blocks whose producer already wrote the scan-order copy, the
+ * last positions and zeroed q / r (the preset-4 TU stage's forward transforms):
+ * count the length buckets (per CTA, then one global atomic per bucket) */
+__global__ void __launch_bounds__(256) k_dq_count(int njobs, const int32_t *__restrict__ first, int *__restrict__ counts)
+{
+    __shared__ int hist[66];
+    for (int b = threadIdx.x; b < 66; b += blockDim.x) hist[b] = 0;
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < njobs; i += gridDim.x * blockDim.x) {
+        const int f = first[i];
+        atomicAdd(&hist[f < 0 ? 0 : (f >> 4) + 1], 1);
     }
     __syncthreads();
     for (int b = threadIdx.x; b < 66; b += blockDim.x)
@@ -978,6 +1010,24 @@ static int xg_dq_enqueue(const xin_gpu_dq_block *d_jobs, const uint32_t *d_soff,
                                                         A.tscan, q, r, nz, d_sets, nsets, A.rates, A.lasts, g_dq.d_step,
                                                         g_dq.d_sbn, g_dq.d_par, A.codes, A.ring);
     if (count) xg_count_launch(4);
+    return xg_cuda_check(cudaGetLastError(), "dep_quant launch");
+}
+
+/* the trellis for blocks already gathered (scan-order copy in A.tscan at d_soff,
+ * last positions in A.first, q and r zeroed, nz of blocks without a trellis
+ * written); the counters are cleared by the caller before the producer runs */
+static int xg_dq_enqueue_gathered(const xin_gpu_dq_block *d_jobs, const uint32_t *d_soff, int njobs, xg_coef *q, xg_coef *r,
+                                  unsigned long long *nz, const xin_gpu_prob *d_sets, int nsets, const XgDqArea &A,
+                                  int max_ctas, cudaStream_t st)
+{
+    int ctas = (njobs + XG_DQ_PAIRS - 1) / XG_DQ_PAIRS;
+    if (ctas > max_ctas) ctas = max_ctas;
+    k_dq_rates<<<nsets, 64, 0, st>>>(d_sets, A.rates, A.lasts);
+    k_dq_count<<<std::min((njobs + 255) / 256, 152 * 4), 256, 0, st>>>(njobs, A.first, A.counts);
+    k_dq_order<<<std::min((njobs + 255) / 256, 152 * 4), 256, 0, st>>>(njobs, A.first, A.counts, A.cursor, A.order);
+    k_dq<<<ctas, XG_DQ_THREADS, sizeof(XgDqSmem), st>>>(d_jobs, njobs, A.counter, A.counts, A.order, A.first, d_soff,
+                                                        A.tscan, q, r, nz, d_sets, nsets, A.rates, A.lasts, g_dq.d_step,
+                                                        g_dq.d_sbn, g_dq.d_par, A.codes, A.ring);
     return xg_cuda_check(cudaGetLastError(), "dep_quant launch");
 }
 

@@ -11,7 +11,9 @@
  * chroma DCT2.  Per picture, after the CU tails have written the prediction
  * residual planes:
  *
- *   k_tu_fwd     forward transforms of every (CU, plane, candidate) block
+ *   k_tu_fwd     forward transforms of every (CU, plane, candidate) block, written
+ *                in the trellis's scan order, with the trellis's set-up (last
+ *                position above the threshold, q and r cleared)
  *   (DQ)         the dependent-quantisation trellis over all blocks (xg_dq.cuh),
  *                QPs from the picture, rates from the stream's context set
  *   k_tu_inv     inverse transforms, reconstruction (prediction = input -
@@ -29,7 +31,7 @@ struct XgTuState {
     int nc[4];                         /* luma candidates per level (1 at 64, else 5) */
     int16_t *resid;                    /* residual planes: per level Y, U, V (picture layout) */
     size_t res_off[4][3];
-    xg_coef *T, *Q, *R;                /* candidate coefficient planes */
+    xg_coef *Q, *R;                    /* candidate coefficient planes: levels, dequantised */
     size_t ncoef;
     size_t cand_off[4][3][5];
     unsigned long long *nz, *ssd;      /* per trellis block */
@@ -45,9 +47,17 @@ struct XgTuLevel {
     const int16_t *resid[3];
     const xg_pix *org[3];
     int opitch[3];
-    xg_coef *T[3], *Q[3], *R[3];       /* candidate 0's plane of each plane; candidate c at + c * cstride */
+    xg_coef *Q[3], *R[3];              /* candidate 0's plane of each plane; candidate c at + c * cstride */
     size_t cstride;                    /* elements between a luma candidate's planes */
     unsigned long long *nz, *ssd;      /* trellis blocks of plane 0 of this level */
+    /* the trellis plan's set-up, written by the forward transforms: blocks are
+     * numbered from blk0 (this level's first) */
+    xg_coef *tscan;                    /* scan-order copies */
+    const uint32_t *soff;              /* start of each block's copy */
+    int32_t *first;                    /* last position above the threshold (-1: none) */
+    const XgDqParam *par;              /* trellis parameters [lg w + lg h - 4][QP] */
+    const XgPicParams *pp;             /* the picture's trellis QPs */
+    int blk0;
     int blk[3];                        /* first block of each plane, relative to the level's first */
     xg_coef *qout[3];                  /* the picture's output planes of this level */
     xg_pix *recout[3];
@@ -120,11 +130,42 @@ __global__ void __launch_bounds__(NT * CPB) k_tu_fwd(XgTuLevel L, int pl)
         w.b[xg_d2<K>(k, y)] = (int16_t)xg_clip16(xg_rshift_rnd(acc, s1));
     });
     xg_gsync<NT, CPB>(g);
-    xg_coef *dst = L.T[pl] + (size_t)c * L.cstride + (size_t)a.py * a.pw + a.px;
-    /* columns: t(kv, kh) = sum_y t1(y, kh) Tv(kv, y), stored along kh */
+    /* the trellis's set-up (Xin266PreDepQuant, h266_dep_quant.c:1683-1770, as
+     * k_dq_prep): the coefficients in scan order, the last one above the
+     * threshold, q and r of the block cleared */
+    const int b = L.blk[pl] + cu * (pl ? 1 : L.nc) + c;          /* block, from the level's first */
+    const XgDqParam *P = L.par + (2 * LG - 4) * 52 + L.pp->dq_qp[pl ? 1 : 0];
+    const int thr = P->thresLast / (P->qScale << 2);
+    xg_coef *TS = L.tscan + L.soff[L.blk0 + b];
+    int best = -1;
+    /* columns: t(kv, kh) = sum_y t1(y, kh) Tv(kv, y), to scan position (kh, kv) */
     xg_mm_dp2<K, K, N, NT, true>(tid, reinterpret_cast<const uint32_t *>(w.b), mv, [&](int kh, int kv, int acc) {
-        dst[(size_t)kv * a.pw + kh] = (xg_coef)xg_clip16(xg_rshift_rnd(acc, s2));
+        const int v = xg_clip16(xg_rshift_rnd(acc, s2)), k = xg_dq_scan_sq(kh, kv, K);
+        TS[k] = (xg_coef)v;
+        if ((v < 0 ? -v : v) > thr) best = max(best, k);
     });
+    {
+        xg_coef *QO = L.Q[pl] + (size_t)c * L.cstride + (size_t)a.py * a.pw + a.px;
+        xg_coef *RO = L.R[pl] + (size_t)c * L.cstride + (size_t)a.py * a.pw + a.px;
+        for (int o = tid; o < N * N; o += NT) {
+            const int y = o >> LG, x = o & (N - 1);
+            QO[(size_t)y * a.pw + x] = 0;
+            RO[(size_t)y * a.pw + x] = 0;
+        }
+    }
+    best = __reduce_max_sync(0xffffffffu, best);
+    if (NT > 32) {
+        __shared__ int gbest[CPB];
+        if (tid == 0) gbest[g] = -1;
+        xg_gsync<NT, CPB>(g);
+        if ((tid & 31) == 0) atomicMax(&gbest[g], best);
+        xg_gsync<NT, CPB>(g);
+        best = gbest[g];
+    }
+    if (tid == 0) {
+        L.first[L.blk0 + b] = best;
+        if (best < 0) L.nz[b] = 0;
+    }
 }
 
 /* Inverse transforms (Xin266IDctWxH, h266_inverse_trans.c:117-229: columns, then
@@ -253,7 +294,7 @@ static uint64_t xg_tu_bytes(const xin_gpu_stream_cfg *c)
         cus += n;
     }
     const uint64_t slots = std::min<uint64_t>((uint64_t)XG_DQ_MAX_CTAS, (blocks + XG_DQ_PAIRS - 1) / XG_DQ_PAIRS) * XG_DQ_PAIRS;
-    return 3 * coef * sizeof(xg_coef) + res * 2 + blocks * (16 + 16 + sizeof(xin_gpu_dq_block)) + cus * 4 +
+    return 2 * coef * sizeof(xg_coef) + res * 2 + blocks * (16 + 16 + sizeof(xin_gpu_dq_block)) + cus * 4 +
            XIN_GPU_NUM_CTX * sizeof(xin_gpu_prob) + coef * 2 /* the trellis plan's scan-order copies */ +
            slots * XG_DQ_SLOT_BYTES /* its decision columns and rings */;
 }
@@ -261,7 +302,7 @@ static uint64_t xg_tu_bytes(const xin_gpu_stream_cfg *c)
 static void xg_tu_free(XgTuState *u)
 {
     if (!u) return;
-    cudaFree(u->resid); cudaFree(u->T); cudaFree(u->Q); cudaFree(u->R);
+    cudaFree(u->resid); cudaFree(u->Q); cudaFree(u->R);
     cudaFree(u->nz); cudaFree(u->ssd); cudaFree(u->satd); cudaFree(u->ctx);
     if (u->plan) xin_gpu_dq_plan_destroy(u->plan);
     delete u;
@@ -323,14 +364,12 @@ static int xg_tu_open(xin_gpu_stream *s, int set)
         return XIN_GPU_ERR_ARG;
     }
     cudaError_t e = cudaMalloc(&u->resid, res * 2);
-    if (e == cudaSuccess) e = cudaMalloc(&u->T, coef * sizeof(xg_coef));
     if (e == cudaSuccess) e = cudaMalloc(&u->Q, coef * sizeof(xg_coef));
     if (e == cudaSuccess) e = cudaMalloc(&u->R, coef * sizeof(xg_coef));
     if (e == cudaSuccess) e = cudaMalloc(&u->nz, (size_t)nblk * 8);
     if (e == cudaSuccess) e = cudaMalloc(&u->ssd, (size_t)nblk * 8);
     if (e == cudaSuccess) e = cudaMalloc(&u->satd, (size_t)(ncu ? ncu : 1) * 4);
     if (e == cudaSuccess) e = cudaMalloc(&u->ctx, XIN_GPU_NUM_CTX * sizeof(xin_gpu_prob));
-    if (e == cudaSuccess) e = cudaMemset(u->T, 0, coef * sizeof(xg_coef));
     if (e == cudaSuccess) {
         std::vector<xin_gpu_prob> ctx;
         xg_tu_default_contexts(ctx);
@@ -384,6 +423,8 @@ static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cud
      * the end) */
     cudaStream_t ls[4];
     int nls = 0;
+    /* the trellis's bucket counters, before the forward transforms write its set-up */
+    cudaMemsetAsync(u->plan->area.counter, 0, 1024, st);
     cudaEventRecord(s->ev_fork, st);
     for (int L = 0; L < 4; L++) {
         if (!s->lev_on[L]) continue;
@@ -405,7 +446,6 @@ static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cud
             v.resid[p] = u->resid + u->res_off[L][p];
             v.org[p] = s->slot[cur][p].data;
             v.opitch[p] = s->slot[cur][p].pitch;
-            v.T[p] = u->T + u->cand_off[L][p][0];
             v.Q[p] = u->Q + u->cand_off[L][p][0];
             v.R[p] = u->R + u->cand_off[L][p][0];
             v.blk[p] = u->blk[L][p] - u->blk[L][0];
@@ -413,6 +453,8 @@ static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cud
             v.recout[p] = t.drec[p] + (p ? lc : lq) * li;
         }
         v.cstride = lq;
+        v.tscan = u->plan->area.tscan; v.soff = u->plan->d_soff; v.first = u->plan->area.first;
+        v.par = g_dq.d_par; v.pp = t.dpp; v.blk0 = u->blk[L][0];
         v.nz = u->nz + u->blk[L][0];
         v.ssd = u->ssd + u->blk[L][0];
         v.W = c.width; v.S = XG_LEVEL_SIZE[L]; v.cus_x = s->lev_cx[L]; v.ncu = s->lev_cx[L] * s->lev_cy[L]; v.nc = u->nc[L];
@@ -423,8 +465,8 @@ static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cud
     join();
     k_tu_setqp<<<(u->nblocks + 255) / 256, 256, 0, st>>>(u->plan->d_jobs, u->nblocks, t.dpp);
     nl++;
-    xg_dq_enqueue(u->plan->d_jobs, u->plan->d_soff, u->plan->nblocks, u->T, u->Q, u->R, u->nz, u->ctx, 1, u->plan->area,
-                  u->plan->ctas, 1, st, false);
+    xg_dq_enqueue_gathered(u->plan->d_jobs, u->plan->d_soff, u->plan->nblocks, u->Q, u->R, u->nz, u->ctx, 1, u->plan->area,
+                           u->plan->ctas, st);
     nl += 4;
     cudaMemsetAsync(u->satd, 0, sizeof(uint32_t) * (s->ncus > 0 ? s->ncus : 1), st);
     cudaEventRecord(s->ev_fork, st);
