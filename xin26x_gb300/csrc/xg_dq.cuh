@@ -324,9 +324,7 @@ __global__ void k_dq_rates(const xin_gpu_prob *__restrict__ sets, XgDqRates *__r
                                                    different rows, which then fall in different banks */
 struct XgDqSmem {
     uint32_t tpl[4 * 16][XG_DQ_TPLS];      /* outside-neighbour template [state * 16 + position][pair] */
-    unsigned long long skc[4][XG_DQ_PAIRS];  /* per state: cost at the top of the current sub-block ("skip") */
     unsigned long long cfl[4][XG_DQ_PAIRS];  /* per template owner: coded flags of the earlier sub-blocks */
-    uint32_t skp[4][XG_DQ_PAIRS];          /* per state: packed fields at the top of the current sub-block */
     uint32_t cvr[4][XG_DQ_PAIRS];          /* per template owner: ring version (state) of each slot */
     int32_t  rice[4][32];                  /* abs_remainder bits, Rice parameter k, value n */
     XgDqRates rt[XG_DQ_RSETS][2];          /* rate tables of the first context sets */
@@ -508,9 +506,10 @@ struct XgDqState { long long cost; uint32_t pk, L[4], F[4]; };
  * "skip", -2 none.  A target without a candidate (only the odd ones at the
  * last position) keeps a cost no later candidate can win with, so its other
  * fields do not matter.  srcref: the template owner whose sub-block context the
- * new path continues (for the sub-block boundary). */
-__device__ __forceinline__ XgDqState xg_dq_next(const XgDqState (&S)[2], int h, int t, int df, int lvv, long long dc,
-                                                int in, int regbins, const XgDqSmem &sm, int pi, int &ns, int &srcref)
+ * new path continues (for the sub-block boundary).  sp: the packed fields of
+ * the target's "skip" record. */
+__device__ __forceinline__ XgDqState xg_dq_next(const XgDqState (&S)[2], int h, int df, int lvv, long long dc,
+                                                int in, int regbins, uint32_t sp, int &ns, int &srcref)
 {
     XgDqState n;
     const bool l1 = df == 2 * h + 1, fresh = df == -1 || df >= 4;
@@ -523,7 +522,6 @@ __device__ __forceinline__ XgDqState xg_dq_next(const XgDqState (&S)[2], int h, 
         /* "start here" and "skip", by selects */
         int r0 = regbins;
         if (in != 0 || r0 >= 4) r0 -= dec;
-        const uint32_t sp = sm.skp[t][pi];
         const bool st = df == -1, sk = df >= 4;
         r = st ? r0 : sk ? xg_pk_rem(sp) : r;
         nsg = st ? 1 : sk ? 0 : nsg;
@@ -612,10 +610,13 @@ __device__ __forceinline__ void xg_dq_block(XgDqSmem &sm, int job, const xin_gpu
         for (int i = 0; i < 4; i++) { S[j].L[i] = 0; S[j].F[i] = 0; }
         S[j].pk = xg_pk(4, 0, -1, 0);
         const int s = 2 * h + j;
-        sm.skc[s][pi] = (unsigned long long)XG_DQ_INF; sm.skp[s][pi] = xg_pk(4, 0, -1, 0);
         sm.cfl[s][pi] = 0; sm.cvr[s][pi] = 0;
     }
     __syncwarp(pm);
+    /* the "skip" records (state at the top of the current sub-block) of this lane's
+     * targets tf and ts: cost and packed fields */
+    long long skc[2] = { XG_DQ_INF, XG_DQ_INF };
+    uint32_t skp[2] = { xg_pk(4, 0, -1, 0), xg_pk(4, 0, -1, 0) };
 
     const int top = first | 15;
     /* loads ahead of the steps that use them: coefficient and position entry one
@@ -731,7 +732,7 @@ __device__ __forceinline__ void xg_dq_block(XgDqSmem &sm, int job, const xin_gpu
                 if (c2 < d) { d = c2; dsel = e2; df = f2; dl = g2; }
                 {
                     /* skip the sub-block (only at a sub-block's first position in scan order) */
-                    const long long c = (long long)sm.skc[t][pi] + (long long)RT->sbb[xg_pk_sgb(sm.skp[t][pi])][0];
+                    const long long c = skc[u] + (long long)RT->sbb[xg_pk_sgb(skp[u])][0];
                     const bool take = (ptype == 2) & (c < d);
                     d = take ? c : d; dsel = take ? 4 : dsel; df = take ? 4 + t : df; dl = take ? 0 : dl;
                 }
@@ -750,9 +751,13 @@ __device__ __forceinline__ void xg_dq_block(XgDqSmem &sm, int job, const xin_gpu
             if (h == 0) CD[(size_t)k * NP] = code;
 
             if (ptype == 1) {
-#pragma unroll
-                for (int j = 0; j < 2; j++) { sm.skc[2 * h + j][pi] = (unsigned long long)S[j].cost; sm.skp[2 * h + j][pi] = S[j].pk; }
-                __syncwarp(pm);
+                /* the records of targets h and h + 2 are states h and h + 2 before the
+                 * step: lane 0 holds state 0 and gets state 2 (lane 1's first), lane 1
+                 * holds state 3 and gets state 1 (lane 0's second) */
+                const long long oc = xg_dq_shfl64x(pm, h ? S[0].cost : S[1].cost);
+                const uint32_t op = __shfl_xor_sync(pm, h ? S[0].pk : S[1].pk, 1);
+                skc[0] = h ? oc : S[0].cost; skp[0] = h ? op : S[0].pk;
+                skc[1] = h ? S[1].cost : oc; skp[1] = h ? S[1].pk : op;
             }
 
             /* ---- new states of tf and ts, then the swap ---- */
@@ -761,7 +766,7 @@ __device__ __forceinline__ void xg_dq_block(XgDqSmem &sm, int job, const xin_gpu
             if (k > 0) {
 #pragma unroll
                 for (int u = 0; u < 2; u++)
-                    N[u] = xg_dq_next(S, h, u ? ts : tf, dfrom[u], dlv[u], dc[u], in, regbins, sm, pi, nns[u], srcref[u]);
+                    N[u] = xg_dq_next(S, h, dfrom[u], dlv[u], dc[u], in, regbins, skp[u], nns[u], srcref[u]);
                 if (in == 0) {
                     /* first coefficient (in scan order) of sub-block sb: close it and open sb - 1.
                      * The sub-block context of a new path is its predecessor's (that of the owner
