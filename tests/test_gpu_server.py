@@ -16,9 +16,9 @@ def _frames(w, h, n, seed):
     return synth.sequence(w, h, n, seed=seed, objects=2)
 
 
-def _alone(w, h, frames):
+def _alone(w, h, frames, **kw):
     from xin26x_gb300.frame import FrameStream
-    fs = FrameStream(w, h, search_range=R, out_q=False, out_rec=False)
+    fs = FrameStream(w, h, search_range=R, out_q=False, out_rec=False, **kw)
     out = []
     for k, f in enumerate(frames):
         fs.submit(*f, qp=27 + 5 * (k % 3), uv_qp=27 + 5 * (k % 3), sad_lambda=64)
@@ -29,13 +29,15 @@ def _alone(w, h, frames):
     return out
 
 
-def _serve(streams, max_inflight=4, leave_after=None):
+def _serve(streams, max_inflight=4, leave_after=None, kws=None):
     """streams: list of (w, h, frames).  Pictures are submitted round-robin;
-    leave_after = (stream number, pictures) makes that stream leave early."""
+    leave_after = (stream number, pictures) makes that stream leave early;
+    kws: per stream extra stream options."""
     from xin26x_gb300.server import Server
     got = {}
+    kws = kws or [{}] * len(streams)
     with Server(max_inflight=max_inflight, max_queue=2) as srv:
-        sids = [srv.join(w, h, fps=30, search_range=R) for (w, h, _) in streams]
+        sids = [srv.join(w, h, fps=30, search_range=R, **kw) for (w, h, _), kw in zip(streams, kws)]
         nxt = [0] * len(streams)
         limit = [len(f) for (_, _, f) in streams]
         if leave_after:
@@ -84,6 +86,23 @@ def test_server_results_equal_alone_and_mixed():
         w = _alone(*o)
         for k in range(1, len(o[2])):
             assert np.array_equal(mixed[(i, k)], w[k - 1]), (i, k)
+
+
+def test_server_preset4_streams_alone_and_mixed():
+    """Streams in the preset-4 form (search by resolution levels, every transform
+    candidate through the trellis) served beside plain streams: each one's CU
+    records (whose non-zero maps and SSDs come from the trellis stage) equal the
+    same stream run alone, with several pictures of different streams in flight."""
+    p4 = {"search_mode": 1, "tu_mode": 1}
+    a = (192, 128, _frames(192, 128, 5, seed=31))
+    b = (256, 128, _frames(256, 128, 4, seed=32))
+    c = (416, 240, _frames(416, 240, 4, seed=33))
+    want_a, want_b = _alone(*a, **p4), _alone(*b, **p4)
+    want_c = _alone(*c)
+    mixed = _serve([a, b, c], max_inflight=3, kws=[p4, p4, {}])
+    for i, (x, want) in enumerate(((a, want_a), (b, want_b), (c, want_c))):
+        for k in range(1, len(x[2])):
+            assert np.array_equal(mixed[(i, k)], want[k - 1]), (i, k)
 
 
 def test_server_leave_while_others_run():

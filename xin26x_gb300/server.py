@@ -43,11 +43,15 @@ class Server:
         self._mu = threading.Lock()
 
     @staticmethod
-    def stream_cfg(width, height, ctu=64, search_range=64, levels=(64, 32, 16, 8)):
+    def stream_cfg(width, height, ctu=64, search_range=64, levels=(64, 32, 16, 8), input_bitdepth=0, search_mode=0,
+                   tu_mode=0):
+        """search_mode 1: search by resolution levels; tu_mode 1: the preset-4 TU
+        stage (every transform candidate through the trellis, the stream's
+        default context set)."""
         mask = 0
         for s in levels:
             mask |= int(s)
-        return _lib.xin_gpu_stream_cfg(width, height, ctu, search_range, mask, 0, 1, 0)
+        return _lib.xin_gpu_stream_cfg(width, height, ctu, search_range, mask, 0, 1, 0, input_bitdepth, search_mode, tu_mode)
 
     def footprint(self, width, height, **kw):
         d, hbytes = C.c_uint64(), C.c_uint64()
