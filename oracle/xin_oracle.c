@@ -1394,21 +1394,33 @@ void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t
         else
             orc_chroma_motion_comp(f->ref[pl], f->ref_stride[1], pred, bs, io.best_mvx * 4, io.best_mvy * 4, cu_x, cu_y,
                                    mnx, mny, mxx, mxy, (uint32_t)size, (uint32_t)size);
-        const opix *src = f->in[pl] + (intptr_t)py * istr + px;
-        ocoef *qo = q[pl] + (intptr_t)py * qstr + px;
-        opix *ro = rec[pl] + (intptr_t)py * rstr + px;
-        orc_transform_tu(src, istr, pred, bs, t, qb, r, bs, (uint32_t)bs, (uint32_t)bs,
-                         pl ? 1u : 0u, 0, pl ? f->uv_qp : f->qp, 0, f->intra_frame, 0, 0, &out->nz[pl]);
-        for (int32_t y = 0; y < bs; y++)
-            for (int32_t x = 0; x < bs; x++) qo[y * qstr + x] = qb[y * bs + x];
-        orc_idct_add(r, bs, pred, bs, ro, rstr, 0, pl ? 1u : 0u, 0, (uint32_t)bs, (uint32_t)bs, 0);
-        uint64_t ssd = 0;
-        for (int32_t y = 0; y < bs; y++)
-            for (int32_t x = 0; x < bs; x++) {
-                int64_t d = (int64_t)src[y * istr + x] - (int64_t)ro[y * rstr + x];
-                ssd += (uint64_t)(d * d);
+        /* the CU's TUs: the CU itself up to the largest transform (64 luma, 32 chroma);
+         * a 128 x 128 CU is four TUs per plane in raster order (the reference's implicit
+         * split): its non-zero maps are OR-ed, its SSDs added */
+        const int32_t tb = bs < (pl ? 32 : 64) ? bs : (pl ? 32 : 64);
+        out->nz[pl] = 0;
+        out->ssd[pl] = 0;
+        for (int32_t oy = 0; oy < bs; oy += tb)
+            for (int32_t ox = 0; ox < bs; ox += tb) {
+                const opix *src = f->in[pl] + (intptr_t)(py + oy) * istr + px + ox;
+                const opix *pr = pred + oy * bs + ox;
+                ocoef *qo = q[pl] + (intptr_t)(py + oy) * qstr + px + ox;
+                opix *ro = rec[pl] + (intptr_t)(py + oy) * rstr + px + ox;
+                uint64_t nz = 0;
+                orc_transform_tu(src, istr, pr, bs, t, qb, r, tb, (uint32_t)tb, (uint32_t)tb,
+                                 pl ? 1u : 0u, 0, pl ? f->uv_qp : f->qp, 0, f->intra_frame, 0, 0, &nz);
+                out->nz[pl] |= nz;
+                for (int32_t y = 0; y < tb; y++)
+                    for (int32_t x = 0; x < tb; x++) qo[y * qstr + x] = qb[y * tb + x];
+                orc_idct_add(r, tb, pr, bs, ro, rstr, 0, pl ? 1u : 0u, 0, (uint32_t)tb, (uint32_t)tb, 0);
+                uint64_t ssd = 0;
+                for (int32_t y = 0; y < tb; y++)
+                    for (int32_t x = 0; x < tb; x++) {
+                        int64_t d = (int64_t)src[y * istr + x] - (int64_t)ro[y * rstr + x];
+                        ssd += (uint64_t)(d * d);
+                    }
+                out->ssd[pl] += ssd;
             }
-        out->ssd[pl] = ssd;
     }
     free(pred); free(t); free(qb); free(r);
 }

@@ -403,6 +403,42 @@ def test_frame_preset4_tu_matches_oracle(bd, inb, search_mode, w, h, R):
         fs.close()
 
 
+@pytest.mark.parametrize("bd,inb", [(8, 0), (10, 8)])
+@pytest.mark.parametrize("w,h,R", [(384, 256, 64), (392, 264, 37)])
+def test_frame_level_128_matches_oracle(bd, inb, w, h, R):
+    """The 128 x 128 CU level (CTU 128, search by resolution levels) beside levels
+    64 .. 8: every CU record, coefficient and reconstructed plane against the
+    oracle, whose 128 x 128 CUs are coded as four 64 x 64 luma and four 32 x 32
+    chroma TUs per plane; pictures whose sizes are not multiples of 128."""
+    seq = synth.sequence(w, h, 3, seed=w + h + R, bitdepth=8 if inb == 8 else bd, objects=2)
+    fs = FrameStream(w, h, ctu=128, search_range=R, levels=(128, 64, 32, 16, 8), out_q=True, out_rec=True, bitdepth=bd,
+                     input_bitdepth=inb, search_mode=1)
+    try:
+        assert [lv[0] for lv in fs.levels] == [64, 32, 16, 8, 128]
+        fs.submit(*seq[0], qp=32, uv_qp=32, sad_lambda=64)
+        fs.wait()
+        for k, qp in ((1, 22), (2, 37)):
+            lam = 50 << (2 if inb == 8 else 0)
+            fs.submit(*seq[k], qp=qp, uv_qp=qp, sad_lambda=lam)
+            out = fs.wait()
+            cur, ref = seq[k], seq[k - 1]
+            if inb == 8:
+                cur, ref = [tuple(p.astype(np.uint16) << 2 for p in f) for f in (cur, ref)]
+            want = oracle_frame.run(cur, ref, fs.levels, ctu=128, search_range=R, qp=qp, uv_qp=qp, sad_lambda=lam,
+                                    bitdepth=bd, threads=0, search_mode=1)
+            _compare(out, want, fs.levels, ("128", bd, inb, w, h, R, k))
+    finally:
+        fs.close()
+
+
+def test_frame_level_128_needs_ctu_128_and_search_by_levels():
+    """The 128 x 128 level is refused with CTU 64, with the exhaustive search and
+    with the preset-4 TU stage."""
+    for kw in ({"ctu": 64, "search_mode": 1}, {"ctu": 128, "search_mode": 0}, {"ctu": 128, "search_mode": 1, "tu_mode": 1}):
+        with pytest.raises(RuntimeError, match="128 x 128 level"):
+            FrameStream(256, 256, search_range=16, levels=(128, 64), **kw)
+
+
 def test_frame_preset4_1080p_two_in_flight():
     """The bench's preset-4 workload compared in full: bench.py's 1920x1080 pictures
     (8-bit into the 10-bit library), search by resolution levels, every transform

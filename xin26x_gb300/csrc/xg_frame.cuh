@@ -12,14 +12,17 @@
 #include <mutex>
 #include <thread>
 
-static const int XG_LEVEL_SIZE[4] = { 64, 32, 16, 8 };
+/* CU levels: 64 .. 8 (every configuration), then 128 (CTU 128 with the search by
+ * resolution levels): results are level-major in this order */
+#define XG_NLEV 5
+static const int XG_LEVEL_SIZE[XG_NLEV] = { 64, 32, 16, 8, 128 };
 
 struct XgTuState;   /* the preset-4 TU stage (xg_tu.cuh) */
 
 struct xin_gpu_stream {
     xin_gpu_stream_cfg cfg;
     int pad, pitch, cpad, cpitch, rows, crows;
-    int lev_on[4], lev_first[4], lev_cx[4], lev_cy[4];
+    int lev_on[XG_NLEV], lev_first[XG_NLEV], lev_cx[XG_NLEV], lev_cy[XG_NLEV];
     int nlev, ncus;
     size_t plane_elems, cplane_elems;
     xg_pix *slot_base[2][3];
@@ -63,9 +66,9 @@ struct xin_gpu_stream {
     cudaStream_t ust;      /* uploads of the next picture's parameters and staged samples */
     cudaStream_t tst;      /* side branch that records the search's end (stage timing) */
     cudaEvent_t ev_tfork, ev_tjoin;
-    cudaStream_t aux[3];   /* the tails of levels 2..4 run beside the first level's */
+    cudaStream_t aux[XG_NLEV - 1];   /* the tails of levels 2..5 run beside the first level's */
     cudaStream_t auxq;     /* quarter-pel planes of the new picture, beside the search (low priority) */
-    cudaEvent_t ev_fork, ev_join[3], ev_qfork, ev_qjoin;
+    cudaEvent_t ev_fork, ev_join[XG_NLEV - 1], ev_qfork, ev_qjoin;
     cudaGraphExec_t gexec[2];
     int me_bands, me_band_rows, me_band_rows_alloc, me_row_words, me_nb;
     size_t me_smem;
@@ -133,7 +136,7 @@ static int xg_stream_free(xin_gpu_stream *s)
     if (s->tst) cudaStreamDestroy(s->tst);
     if (s->ev_tfork) cudaEventDestroy(s->ev_tfork);
     if (s->ev_tjoin) cudaEventDestroy(s->ev_tjoin);
-    for (int i = 0; i < 3; i++) {
+    for (int i = 0; i < XG_NLEV - 1; i++) {
         if (s->ev_join[i]) cudaEventDestroy(s->ev_join[i]);
         if (s->aux[i]) cudaStreamDestroy(s->aux[i]);
     }
@@ -166,9 +169,11 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     const xin_gpu_stream_cfg &c = *cfg;
     if (c.width < 16 || c.height < 16 || (c.width & 1) || (c.height & 1) || c.width > 8192 || c.height > 8192 ||
         (c.ctu_size != 64 && c.ctu_size != 128) || c.search_range < 1 || c.search_range > 256 ||
-        !(c.level_mask & (8u | 16u | 32u | 64u)) || !xg_input_depth_ok(c) || (c.search_mode != 0 && c.search_mode != 1) ||
-        (c.tu_mode != 0 && c.tu_mode != 1)) {
-        xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range, level mask, input bit depth, search or TU mode");
+        !(c.level_mask & (8u | 16u | 32u | 64u | 128u)) || (c.level_mask & ~(8u | 16u | 32u | 64u | 128u)) ||
+        !xg_input_depth_ok(c) || (c.search_mode != 0 && c.search_mode != 1) || (c.tu_mode != 0 && c.tu_mode != 1) ||
+        ((c.level_mask & 128u) && (c.ctu_size != 128 || c.search_mode != 1 || c.tu_mode != 0))) {
+        xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range, level mask, input bit depth, search or "
+                                      "TU mode (the 128 x 128 level needs CTU 128, the search by levels and TU mode 0)");
         return XIN_GPU_ERR_ARG;
     }
     xin_gpu_stream *s = new (std::nothrow) xin_gpu_stream();
@@ -189,7 +194,7 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     s->plane_elems = (size_t)s->pitch * s->rows;
     s->cplane_elems = (size_t)s->cpitch * s->crows;
     int first = 0;
-    for (int L = 0; L < 4; L++) {
+    for (int L = 0; L < XG_NLEV; L++) {
         int sz = XG_LEVEL_SIZE[L];
         s->lev_on[L] = (c.level_mask & (uint32_t)sz) != 0;
         s->lev_cx[L] = c.width / sz;
@@ -222,7 +227,7 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         cudaDeviceGetStreamPriorityRange(&lo, &hi);    /* lo: the least urgent */
         e = cudaStreamCreateWithPriority(&s->auxq, cudaStreamNonBlocking, lo);
     }
-    for (int i = 0; i < 3 && e == cudaSuccess; i++) {
+    for (int i = 0; i < XG_NLEV - 1 && e == cudaSuccess; i++) {
         e = cudaStreamCreateWithFlags(&s->aux[i], cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_join[i], cudaEventDisableTiming);
     }
@@ -352,6 +357,19 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
 #endif
     });
     if (xg_cuda_check(me_attr_err, "me smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
+    if (s->lev_on[4]) {
+        /* the 128 x 128 level's kernels take more than the default 48 KB of shared memory */
+        static std::once_flag l128_once;
+        static cudaError_t l128_err = cudaSuccess;
+        std::call_once(l128_once, [] {
+            l128_err = cudaFuncSetAttribute(k_hier_frame<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)xg_hier_smem(256, 128));
+            if (l128_err == cudaSuccess)
+                l128_err = cudaFuncSetAttribute(k_cu_tail<128, 128, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)xg_tail_smem<128, 128, 1>());
+        });
+        if (xg_cuda_check(l128_err, "128 x 128 level smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
+    }
     s->wait_tries = XG_TMA_WAIT_TRIES;
     /* TMA maps of the padded luma slots for the quarter-pel tiles: the box of
      * tile (bx, by) starts at padded column XG_QP_TW bx (16-byte aligned) */
@@ -379,7 +397,7 @@ extern "C" int xin_gpu_stream_level_info(const xin_gpu_stream *s, int level, int
 {
     if (!s) return XIN_GPU_ERR_ARG;
     int k = 0;
-    for (int L = 0; L < 4; L++) {
+    for (int L = 0; L < XG_NLEV; L++) {
         if (!s->lev_on[L]) continue;
         if (k++ != level) continue;
         if (size) *size = XG_LEVEL_SIZE[L];
@@ -486,8 +504,17 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
                 hp.cus_x[nz] = s->lev_cx[L];
                 nz++;
             }
-            dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, nz);
-            k_hier_frame<<<grd, XG_HIER_THREADS, xg_hier_smem(c.search_range), st>>>(hp, t.dpp);
+            if (nz > 0) {
+                dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, nz);
+                k_hier_frame<64><<<grd, XG_HIER_THREADS, xg_hier_smem(c.search_range, 64), st>>>(hp, t.dpp);
+            }
+            if (s->lev_on[4]) {
+                /* the 128 x 128 level: 128 x 128 tiles */
+                hp.level_size[0] = 128; hp.keys[0] = s->keys + s->lev_first[4]; hp.cus_x[0] = s->lev_cx[4];
+                dim3 grd((c.width + 127) / 128, (c.height + 127) / 128, 1);
+                k_hier_frame<128><<<grd, XG_HIER_THREADS, xg_hier_smem(c.search_range, 128), st>>>(hp, t.dpp);
+                nl++;
+            }
         } else {
         XgMeParams mp;
         mp.cur = s->slot[cur][0];
@@ -519,7 +546,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         /* the levels' tails are independent: fork them onto the auxiliary streams */
         cudaEventRecord(s->ev_fork, st);
         int li = 0, nfork = 0;
-        for (int L = 0; L < 4; L++) {
+        for (int L = 0; L < XG_NLEV; L++) {
             if (!s->lev_on[L]) continue;
             cudaStream_t ls = st;
             if (li > 0) {
@@ -546,10 +573,11 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
                 /* 64 and 32: a 128-thread CTA per CU; 16 and 8: a warp per CU, four CUs per
                  * CTA (the fastest of the shapes measured on GB300 at 1080p) */
                 switch (XG_LEVEL_SIZE[L]) {
-                case 64: k_cu_tail<64, 128, 1><<<n, 128, 0, ls>>>(tp, t.dpp, n); break;
-                case 32: k_cu_tail<32, 128, 1><<<n, 128, 0, ls>>>(tp, t.dpp, n); break;
-                case 16: k_cu_tail<16, 32, 4><<<(n + 3) / 4, 128, 0, ls>>>(tp, t.dpp, n); break;
-                default: k_cu_tail<8, 32, 4><<<(n + 3) / 4, 128, 0, ls>>>(tp, t.dpp, n); break;
+                case 128: k_cu_tail<128, 128, 1><<<n, 128, xg_tail_smem<128, 128, 1>(), ls>>>(tp, t.dpp, n); break;
+                case 64: k_cu_tail<64, 128, 1><<<n, 128, xg_tail_smem<64, 128, 1>(), ls>>>(tp, t.dpp, n); break;
+                case 32: k_cu_tail<32, 128, 1><<<n, 128, xg_tail_smem<32, 128, 1>(), ls>>>(tp, t.dpp, n); break;
+                case 16: k_cu_tail<16, 32, 4><<<(n + 3) / 4, 128, xg_tail_smem<16, 32, 4>(), ls>>>(tp, t.dpp, n); break;
+                default: k_cu_tail<8, 32, 4><<<(n + 3) / 4, 128, xg_tail_smem<8, 32, 4>(), ls>>>(tp, t.dpp, n); break;
                 }
                 nl++;
             }
@@ -640,8 +668,9 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
             return XIN_GPU_ERR_ARG;
         }
     }
-    for (int L = 0; L < 4; L++) {
-        int lg = XG_LEVEL_SIZE[L] == 64 ? 6 : XG_LEVEL_SIZE[L] == 32 ? 5 : XG_LEVEL_SIZE[L] == 16 ? 4 : 3;
+    for (int L = 0; L < XG_NLEV; L++) {
+        /* the TU's size: the CU's, at most 64 (a 128 x 128 CU has 64 x 64 TUs) */
+        int lg = XG_LEVEL_SIZE[L] >= 64 ? 6 : XG_LEVEL_SIZE[L] == 32 ? 5 : XG_LEVEL_SIZE[L] == 16 ? 4 : 3;
         xg_quant_params(pic->qp, lg, 0, &pp.quant[L][0]);
         xg_quant_params(pic->uv_qp, lg - 1, 0, &pp.quant[L][1]);
         pp.quant[L][2] = pp.quant[L][1];

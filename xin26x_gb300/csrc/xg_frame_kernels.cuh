@@ -183,7 +183,7 @@ struct XgQuant { int qmult, qadd, qshift, iqmult, iqadd, iqshift; };
 struct XgPicParams {
     uint32_t lambda;
     int32_t status;                     /* written by the kernels: XG_STATUS_* bits (0 = fine) */
-    XgQuant quant[4][3];                /* [level 64,32,16,8][plane] */
+    XgQuant quant[5][3];                /* [level 64, 32, 16, 8, 128][plane] */
     const xg_pix *src[3];               /* device-resident source planes (device_io streams) */
     long long src_stride[3];
     int32_t dq_qp[2];                   /* preset-4 TU stage: luma / chroma QP the trellis gets */
@@ -908,7 +908,7 @@ __device__ void xg_tq(XgTqSmem<N> &sm, const XgQuant &qz, int s1, int s2, unsign
  * first, lines >= 32 skipped (Xin266IDct2WxH), then rows; adds the prediction,
  * clips, writes the reconstruction and accumulates the SSD */
 template <int N, int NT, int CPB>
-__device__ void xg_itq(XgTqSmem<N> &sm, const xg_pix *pred, const xg_pix *org, int opitch, xg_pix *rec, int rpitch,
+__device__ void xg_itq(XgTqSmem<N> &sm, const xg_pix *pred, int ppitch, const xg_pix *org, int opitch, xg_pix *rec, int rpitch,
                        unsigned long long *ssd, int tid, int g)
 {
     constexpr int K = XgTqSmem<N>::K;
@@ -921,7 +921,7 @@ __device__ void xg_itq(XgTqSmem<N> &sm, const xg_pix *pred, const xg_pix *org, i
     unsigned long long part = 0;
     /* rows: r'(y, x) = sum_kh t2(kh, y) T(kh, x) */
     xg_mm_dp2<N, N, K, NT>(tid, reinterpret_cast<const uint32_t *>(sm.t2), sm.mi, [&](int y, int x, int acc) {
-        int v = xg_clip_pix((int)pred[y * N + x] + xg_clip16(xg_rshift_rnd(acc, s2)));
+        int v = xg_clip_pix((int)pred[y * ppitch + x] + xg_clip16(xg_rshift_rnd(acc, s2)));
         rec[(intptr_t)y * rpitch + x] = (xg_pix)v;
         int d = (int)org[(intptr_t)y * opitch + x] - v;
         part += (unsigned long long)(d * d);
@@ -935,11 +935,16 @@ __device__ void xg_itq(XgTqSmem<N> &sm, const xg_pix *pred, const xg_pix *org, i
     xg_gsync<NT, CPB>(g);
 }
 
+/* transform sizes of a CU of size S: TU = CU up to 64; a 128 x 128 CU is coded as
+ * four 64 x 64 luma and four 32 x 32 chroma TUs per plane (the largest transform) */
+__host__ __device__ constexpr int xg_tu_luma(int s) { return s > 64 ? 64 : s; }
+__host__ __device__ constexpr int xg_tu_chroma(int s) { return s > 64 ? 32 : s / 2; }
+
 /* the shared state of one CU */
 template <int S, int NT>
 struct XgTailSmem {
-    XgTqSmem<S> tl;
-    XgTqSmem<S / 2> tc;
+    XgTqSmem<xg_tu_luma(S)> tl;
+    XgTqSmem<xg_tu_chroma(S)> tc;
     xg_pix pred[S * S];
     uint32_t part[8][NT / 32];
     int bmv[3];
@@ -950,18 +955,22 @@ struct XgTailSmem {
  * (NT = 32: one warp per CU, warp-synchronous) */
 /* CTAs per SM the register allocation must allow: 64 x 64 CUs are held to five by
  * shared memory anyway, the other sizes keep eight 128-thread CTAs (64 registers) */
-__host__ __device__ constexpr int xg_tail_min_ctas(int s) { return s == 64 ? 5 : 8; }
+__host__ __device__ constexpr int xg_tail_min_ctas(int s) { return s == 128 ? 2 : s == 64 ? 5 : 8; }
+/* shared memory (dynamic) of a launch */
+template <int S, int NT, int CPB>
+__host__ __device__ constexpr size_t xg_tail_smem() { return sizeof(XgTailSmem<S, NT>) * CPB; }
 template <int S, int NT, int CPB>
 __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTailParams p, const XgPicParams *pp, int ncu)
 {
-    constexpr int C = S / 2;
-    __shared__ XgTailSmem<S, NT> shm[CPB];
+    constexpr int C = S / 2, TL = xg_tu_luma(S), TC = xg_tu_chroma(S);
+    extern __shared__ __align__(16) unsigned char xg_tail_raw[];
+    XgTailSmem<S, NT> *shm = reinterpret_cast<XgTailSmem<S, NT> *>(xg_tail_raw);
     const int g = threadIdx.x / NT, tid = threadIdx.x % NT;
     const int cu = blockIdx.x * CPB + g;
     if (cu >= ncu) return;          /* whole groups only: no barrier is shared with a missing group */
     XgTailSmem<S, NT> &m = shm[g];
-    XgTqSmem<S> &tl = m.tl;
-    XgTqSmem<C> &tc = m.tc;
+    XgTqSmem<TL> &tl = m.tl;
+    XgTqSmem<TC> &tc = m.tc;
     xg_pix *pred = m.pred;
     const int cx = (cu % p.cus_x) * S, cy = (cu / p.cus_x) * S;
     const int lane = tid & 31, warp = tid >> 5;
@@ -970,11 +979,11 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
     const int gidx = (int)(uint32_t)key;
     const int imx = gidx % nx - p.R, imy = gidx / nx - p.R;
     if (tid < 3) { m.nz[tid] = 0; m.ssd[tid] = 0; }
-    {   /* DCT2 matrices of the luma (S) and chroma (S/2) blocks, rows k < 32 */
-        constexpr int lgs = S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : 6;
-        const int16_t *ml = xg_mat(0, lgs), *mc = xg_mat(0, lgs - 1);
-        xg_tq_load_mat<S, NT>(tl, ml, tid);
-        xg_tq_load_mat<C, NT>(tc, mc, tid);
+    {   /* DCT2 matrices of the luma and chroma TUs, rows k < 32 */
+        constexpr int lgl = TL == 8 ? 3 : TL == 16 ? 4 : TL == 32 ? 5 : 6, lgc = TC == 4 ? 2 : TC == 8 ? 3 : TC == 16 ? 4 : 5;
+        const int16_t *ml = xg_mat(0, lgl), *mc = xg_mat(0, lgc);
+        xg_tq_load_mat<TL, NT>(tl, ml, tid);
+        xg_tq_load_mat<TC, NT>(tc, mc, tid);
     }
 
     /* window (h266_enc_init.c:1462) */
@@ -1070,8 +1079,10 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
     }
     xg_gsync<NT, CPB>(g);
 
-    /* ---- luma TQ + reconstruction (or the residual, for the preset-4 TU stage) */
-    const int lgS = S == 8 ? 3 : S == 16 ? 4 : S == 32 ? 5 : 6;
+    /* ---- luma TQ + reconstruction (or the residual, for the preset-4 TU stage); a
+     * 128 x 128 CU TU by TU (64 x 64, in raster order: the non-zero maps of the
+     * record are the union of its TUs', the SSDs their sum) */
+    const int lgS = TL == 8 ? 3 : TL == 16 ? 4 : TL == 32 ? 5 : 6;
     const bool resid_only = p.resid[0] != nullptr;       /* uniform over the launch */
     if (resid_only) {
         for (int i = tid; i < S * S; i += NT) {
@@ -1080,19 +1091,24 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
         }
         xg_gsync<NT, CPB>(g);
     } else {
-        for (int i = tid; i < S * S; i += NT) {
-            int y = i / S, x = i % S;
-            tl.res[xg_d2<S>(y, x)] = (int16_t)((int)org[(intptr_t)y * p.cur[0].pitch + x] - (int)pred[i]);
+        for (int tu = 0; tu < (S / TL) * (S / TL); tu++) {
+            const int ox = (tu % (S / TL)) * TL, oy = (tu / (S / TL)) * TL;
+            for (int i = tid; i < TL * TL; i += NT) {
+                int y = i / TL, x = i % TL;
+                tl.res[xg_d2<TL>(y, x)] = (int16_t)((int)org[(intptr_t)(oy + y) * p.cur[0].pitch + ox + x] -
+                                                    (int)pred[(oy + y) * S + ox + x]);
+            }
+            xg_gsync<NT, CPB>(g);
+            xg_tq<TL, NT, CPB>(tl, pp->quant[p.level][0], lgS + XG_BITDEPTH + 6 - 15, lgS + 6, &m.nz[0],
+                               p.q[0] + (intptr_t)(cy + oy) * p.W + cx + ox, p.W, tid, g);
+            xg_itq<TL, NT, CPB>(tl, pred + oy * S + ox, S, org + (intptr_t)oy * p.cur[0].pitch + ox, p.cur[0].pitch,
+                                p.rec[0] + (intptr_t)(cy + oy) * p.W + cx + ox, p.W, &m.ssd[0], tid, g);
         }
-        xg_gsync<NT, CPB>(g);
-        xg_tq<S, NT, CPB>(tl, pp->quant[p.level][0], lgS + XG_BITDEPTH + 6 - 15, lgS + 6, &m.nz[0],
-                          p.q[0] + (intptr_t)cy * p.W + cx, p.W, tid, g);
-        xg_itq<S, NT, CPB>(tl, pred, org, p.cur[0].pitch, p.rec[0] + (intptr_t)cy * p.W + cx, p.W, &m.ssd[0], tid, g);
     }
 
     /* ---- chroma: uni branch of Xin266ChromaMotionComp (1/32 phase, mask 31), TQ, reconstruction */
     {
-        const int lgC = lgS - 1;
+        const int lgC = TC == 4 ? 2 : TC == 8 ? 3 : TC == 16 ? 4 : 5;
         int m16x = min(max(mvx * 4, mnx * 16), mxx * 16), m16y = min(max(mvy * 4, mny * 16), mxy * 16);
         int ox = cx * 16 + m16x, oy = cy * 16 + m16y;
         int fx = ox & 31, fy = oy & 31;
@@ -1122,15 +1138,19 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
                 xg_gsync<NT, CPB>(g);
                 continue;
             }
-            for (int i = tid; i < C * C; i += NT) {
-                int y = i / C, x = i % C;
-                tc.res[xg_d2<C>(y, x)] = (int16_t)((int)corg[(intptr_t)y * p.cur[pl].pitch + x] - (int)pred[i]);
+            for (int tu = 0; tu < (C / TC) * (C / TC); tu++) {
+                const int ox = (tu % (C / TC)) * TC, oy = (tu / (C / TC)) * TC;
+                for (int i = tid; i < TC * TC; i += NT) {
+                    int y = i / TC, x = i % TC;
+                    tc.res[xg_d2<TC>(y, x)] = (int16_t)((int)corg[(intptr_t)(oy + y) * p.cur[pl].pitch + ox + x] -
+                                                        (int)pred[(oy + y) * C + ox + x]);
+                }
+                xg_gsync<NT, CPB>(g);
+                xg_tq<TC, NT, CPB>(tc, pp->quant[p.level][pl], lgC + XG_BITDEPTH + 6 - 15, lgC + 6, &m.nz[pl],
+                                   p.q[pl] + (intptr_t)((cy >> 1) + oy) * W2 + (cx >> 1) + ox, W2, tid, g);
+                xg_itq<TC, NT, CPB>(tc, pred + oy * C + ox, C, corg + (intptr_t)oy * p.cur[pl].pitch + ox, p.cur[pl].pitch,
+                                    p.rec[pl] + (intptr_t)((cy >> 1) + oy) * W2 + (cx >> 1) + ox, W2, &m.ssd[pl], tid, g);
             }
-            xg_gsync<NT, CPB>(g);
-            xg_tq<C, NT, CPB>(tc, pp->quant[p.level][pl], lgC + XG_BITDEPTH + 6 - 15, lgC + 6, &m.nz[pl],
-                              p.q[pl] + (intptr_t)(cy >> 1) * W2 + (cx >> 1), W2, tid, g);
-            xg_itq<C, NT, CPB>(tc, pred, corg, p.cur[pl].pitch, p.rec[pl] + (intptr_t)(cy >> 1) * W2 + (cx >> 1), W2,
-                               &m.ssd[pl], tid, g);
         }
     }
     if (tid == 0) {

@@ -317,20 +317,26 @@ __device__ __forceinline__ void xg_sad_3x3(const xg_pix *c, long long cp, const 
     }
 }
 
+/* TILE: 64 for CU levels 64 .. 8, 128 for the 128 x 128 level (CTU 128) */
+template <int TILE>
 __global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(XgHierFrameParams p, const XgPicParams *pp)
 {
+    constexpr int T4 = TILE / 4;                              /* the tile at 1/4 resolution */
     extern __shared__ __align__(16) xg_pix hs[];
     __shared__ unsigned long long wmin[8];
     __shared__ uint32_t wsum[8][10];
     const int S = p.level_size[blockIdx.z];
-    const int lgS = S == 64 ? 6 : S == 32 ? 5 : S == 16 ? 4 : 3;
+    const int lgS = S == 128 ? 7 : S == 64 ? 6 : S == 32 ? 5 : S == 16 ? 4 : 3;
     unsigned long long *keys = p.keys[blockIdx.z];
     const int cus_x = p.cus_x[blockIdx.z];
-    const int R = p.R, R4 = R >> 2, WS = 16 + 2 * R4, WP = WS + 4;   /* window side, row pitch */
-    const int tx0 = blockIdx.x * 64, ty0 = blockIdx.y * 64;
-    xg_pix *win = hs, *cur4 = hs + WS * WP;                  /* [WS][WP], [16][16] */
+    const int R = p.R, R4 = R >> 2, WS = T4 + 2 * R4, WP = WS + 4;   /* window side, row pitch */
+    const int tx0 = blockIdx.x * TILE, ty0 = blockIdx.y * TILE;
+    xg_pix *win = hs, *cur4 = hs + WS * WP;                  /* [WS][WP], [T4][T4] */
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t lambda = pp->lambda;
+    /* a 128 tile holds one CU: without it (a partial tile) nothing is staged, so the
+     * window never reaches past the planes' margins (R/4 + 18 samples at 1/4) */
+    if (TILE == 128 && (tx0 + 128 > p.W || ty0 + 128 > p.H)) return;
     {
         const xg_pix *src = p.ref_lo[1].data + (long long)(ty0 / 4 - R4) * p.ref_lo[1].pitch + (tx0 / 4 - R4);
         for (int i = tid; i < WS * WP; i += XG_HIER_THREADS) {
@@ -339,10 +345,10 @@ __global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(XgHierFrameParam
             win[i] = x < WS ? src[(long long)y * p.ref_lo[1].pitch + x] : (xg_pix)0;
         }
         const xg_pix *cs = p.cur_lo[1].data + (long long)(ty0 / 4) * p.cur_lo[1].pitch + tx0 / 4;
-        for (int i = tid; i < 256; i += XG_HIER_THREADS) cur4[i] = cs[(long long)(i >> 4) * p.cur_lo[1].pitch + (i & 15)];
+        for (int i = tid; i < T4 * T4; i += XG_HIER_THREADS) cur4[i] = cs[(long long)(i / T4) * p.cur_lo[1].pitch + (i % T4)];
     }
     __syncthreads();
-    const int per_row = 64 >> lgS, ncu = per_row * per_row;
+    const int per_row = TILE >> lgS, ncu = per_row * per_row;
     const int G = ncu >= 8 ? 1 : 8 / ncu;                     /* warps per CU */
     const int slots = 8 / G;                                  /* CUs in flight */
     const int b4 = S >> 2;
@@ -381,7 +387,7 @@ __global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(XgHierFrameParam
         unsigned long long k = ~0ull;
         if (nx4 > 0 && ny4 > 0) {
             const int qpr = (nx4 + 3) >> 2, nq = qpr * ny4;      /* quads per row, quads */
-            const xg_pix *cb = cur4 + (cyi >> 2) * 16 + (cxi >> 2);
+            const xg_pix *cb = cur4 + (cyi >> 2) * T4 + (cxi >> 2);
             const xg_pix *wb = win + ((cyi >> 2) + R4 + ly4) * WP + (cxi >> 2) + R4 + lx4;
             int qy = gt / qpr, qx = gt - qy * qpr;              /* this lane's first quad */
             const int sy = gn / qpr, sx = gn - sy * qpr;        /* its step */
@@ -389,7 +395,7 @@ __global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(XgHierFrameParam
                 const xg_pix *r = wb + qy * WP + 4 * qx;
                 uint32_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
                 for (int yy = 0; yy < b4; yy++) {
-                    const xg_pix *cr = cb + yy * 16, *rr = r + yy * WP;
+                    const xg_pix *cr = cb + yy * T4, *rr = r + yy * WP;
                     unsigned w0 = rr[0], w1 = rr[1], w2 = rr[2];
                     for (int j = 0; j < b4; j++) {
                         const unsigned w3 = rr[j + 3], cv = cr[j];
@@ -460,9 +466,9 @@ __global__ void __launch_bounds__(XG_HIER_THREADS) k_hier_frame(XgHierFrameParam
     }
 }
 
-/* shared memory of k_hier_frame for search range R */
-static size_t xg_hier_smem(int R)
+/* shared memory of k_hier_frame<TILE> for search range R */
+static size_t xg_hier_smem(int R, int tile = 64)
 {
-    const int ws = 16 + 2 * (R >> 2);
-    return (size_t)(ws * (ws + 4) + 256) * sizeof(xg_pix);
+    const int t4 = tile / 4, ws = t4 + 2 * (R >> 2);
+    return (size_t)(ws * (ws + 4) + t4 * t4) * sizeof(xg_pix);
 }

@@ -28,7 +28,9 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
 {
     if (c->width < 16 || c->height < 16 || (c->width & 1) || (c->height & 1) || c->width > 8192 || c->height > 8192 ||
         (c->ctu_size != 64 && c->ctu_size != 128) || c->search_range < 1 || c->search_range > 256 ||
-        !(c->level_mask & (8u | 16u | 32u | 64u)) || !xg_input_depth_ok(*c) || (c->search_mode != 0 && c->search_mode != 1) ||
+        !(c->level_mask & (8u | 16u | 32u | 64u | 128u)) || (c->level_mask & ~(8u | 16u | 32u | 64u | 128u)) ||
+        ((c->level_mask & 128u) && (c->ctu_size != 128 || c->search_mode != 1 || c->tu_mode != 0)) ||
+        !xg_input_depth_ok(*c) || (c->search_mode != 0 && c->search_mode != 1) ||
         (c->tu_mode != 0 && c->tu_mode != 1))
         return XIN_GPU_ERR_ARG;
     const bool widen = XG_BITDEPTH == 10 && c->input_bitdepth == 8;
@@ -41,7 +43,7 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
     uint64_t lq = (uint64_t)c->width * c->height, lc = lq / 4;
     int nlev = 0;
     uint64_t ncus = 0;
-    for (int L = 0; L < 4; L++)
+    for (int L = 0; L < XG_NLEV; L++)
         if (c->level_mask & (uint32_t)XG_LEVEL_SIZE[L]) {
             nlev++;
             ncus += (uint64_t)(c->width / XG_LEVEL_SIZE[L]) * (c->height / XG_LEVEL_SIZE[L]);
