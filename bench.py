@@ -699,7 +699,9 @@ def wide_search_bench(torch, flush, pictures=3, search_mode=0):
     assert g.xin_gpu_init(torch.cuda.current_device()) == 0
     seq = synth.sequence(w, h, pictures, seed=2160, bitdepth=10, objects=8, octaves=4)
     dev = [tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f) for f in seq]
-    cfg = _lib.xin_gpu_stream_cfg(w, h, 128, r, 120, 0, 1, 1, 0, search_mode)
+    # the search by levels also takes the 128 x 128 CU level (CTU 128)
+    mask = 120 | (128 if search_mode == 1 else 0)
+    cfg = _lib.xin_gpu_stream_cfg(w, h, 128, r, mask, 0, 1, 1, 0, search_mode)
     hs = C.c_void_p()
     assert g.xin_gpu_stream_open(C.byref(cfg), C.byref(hs)) == 0, g.xin_gpu_last_error()
     res = _lib.xin_gpu_results()
@@ -725,15 +727,17 @@ def wide_search_bench(torch, flush, pictures=3, search_mode=0):
     if search_mode == 1:
         # work of the quarter-resolution level (the bulk): every CU of each level,
         # (2 * (R >> 2) + 1)^2 candidates of (S/4)^2 samples
-        algo = 4 * (2 * (r >> 2) + 1) ** 2 * (w // 4) * (h // 4)
+        algo = sum((w // sz) * (h // sz) * (sz // 4) ** 2 for sz in (128, 64, 32, 16, 8)) * (2 * (r >> 2) + 1) ** 2
         return {"workload": "3840x2160 10-bit 4:2:0, CTU 128, +-256 integer search by resolution levels (1/4 "
-                            "exhaustive +-64, 1/2 and full resolution +-1), full sub-pel search, CU levels 64/32/16/8, "
-                            "DCT2 TU=CU, seeded texture (4 octaves) + 8 moving rectangles",
+                            "exhaustive +-64, 1/2 and full resolution +-1), full sub-pel search, CU levels "
+                            "128/64/32/16/8 (128 x 128 CUs as four 64 x 64 TUs), DCT2, seeded texture (4 octaves) + 8 "
+                            "moving rectangles",
                 "pictures_timed": len(ms), "ms_per_picture": float(np.mean(ms)), "value": w * h / float(np.mean(ms)) / 1e3,
                 "unit": "Mpixel/s", "dtype": "u16",
                 "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_mc_tq": stage[2]},
                 "search_absdiff_per_s": algo / (stage[1] * 1e-3),
-                "search_algorithmic": f"4 levels x (2*64+1)^2 x (W/4)(H/4) = {algo:.4g} abs differences at 1/4 resolution"}
+                "search_algorithmic": f"every CU of the five levels x (2*64+1)^2 candidates x (S/4)^2 samples = "
+                                      f"{algo:.4g} abs differences at 1/4 resolution"}
     peak = C.c_double()
     g.xin_gpu_measure_sad_peak(C.byref(peak))
     algo = (w // 8) * (h // 8) * (2 * r + 1) ** 2 * 64
