@@ -241,7 +241,8 @@ typedef struct xin_gpu_tq_block {
 #define XIN_GPU_TQ_MTS_ENABLED 16u
 /* tile: the CUDA-core kernel's thread-group size (-1 autotune, 0 fixed, 32..256),
  * or XIN_GPU_TQ_TENSOR: transform passes on the tensor cores (tcgen05, exact
- * f16 halves, f32 accumulation), transform-skip blocks on the CUDA cores */
+ * f16 halves, f32 accumulation), transform-skip blocks on the CUDA cores; the
+ * tensor form needs the four coefficient arrays 16-byte aligned */
 #define XIN_GPU_TQ_TENSOR      (-2)
 /* host arrays of ncoeffs samples; samples that no block covers are returned as zeros */
 int  xin_gpu_tq_batch(const xin_gpu_tq_block *blocks, int32_t nblocks, const XG_COEFF *resid, XG_COEFF *q, XG_COEFF *r,
@@ -253,7 +254,9 @@ int  xin_gpu_tq_batch_device(const xin_gpu_tq_block *blocks, int32_t nblocks, co
                              int32_t *tiles_used);
 /* A plan keeps a validated block list, sorted by size class, on the device so
  * that one list can run on new residuals without host work: run only enqueues
- * launches on `stream` (device arrays).  With tile -1 the first run of a class
+ * launches on `stream` (device arrays).  Runs of one plan must not overlap in
+ * time (the tensor form's tile queue and timeout flag belong to the plan):
+ * enqueue them on one stream, or create a plan per stream.  With tile -1 the first run of a class
  * not tuned yet times the candidates and synchronises; later runs are
  * asynchronous.  tiles: 49 entries, 0 for classes not resolved yet. */
 typedef struct xin_gpu_tq_plan xin_gpu_tq_plan;

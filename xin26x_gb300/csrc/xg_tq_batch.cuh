@@ -257,7 +257,7 @@ struct xin_gpu_tq_plan {
     XgTcTile *d_tiles;
     uint32_t *d_tlist;
     int ntiles;
-    int *d_err;                 /* set by a tensor-core wait that timed out */
+    int *d_err;                 /* [0] set by a tensor-core wait that timed out; [1] the tile queue's counter */
     long long wait_tries;       /* polls of one tensor-core wait before it gives up */
 };
 
@@ -310,8 +310,8 @@ static void xg_tq_tiles(const xin_gpu_tq_block *blocks, int32_t n, std::vector<X
 static int xg_tq_plan_enqueue(xin_gpu_tq_plan *p, const xg_coef *res, xg_coef *q, xg_coef *r, xg_coef *rout,
                               unsigned long long *nz, cudaStream_t st)
 {
-    if (p->ntiles && (((uintptr_t)res | (uintptr_t)rout) & 15)) {
-        xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_run: the tensor-core form needs 16-byte aligned residual arrays");
+    if (p->ntiles && (((uintptr_t)res | (uintptr_t)q | (uintptr_t)r | (uintptr_t)rout) & 15)) {
+        xg_set_error(XIN_GPU_ERR_ARG, "tq_plan_run: the tensor-core form needs 16-byte aligned arrays");
         return XIN_GPU_ERR_ARG;
     }
     if (p->ntiles) {
@@ -331,8 +331,9 @@ static int xg_tq_plan_enqueue(xin_gpu_tq_plan *p, const xg_coef *res, xg_coef *q
         });
         if (xg_cuda_check(attr_err, "tq tensor smem attribute")) return XIN_GPU_ERR_CUDA;
         const int grid = std::min(p->ntiles, resident);
+        if (xg_cuda_check(cudaMemsetAsync(p->d_err + 1, 0, sizeof(int), st), "tq tile queue")) return XIN_GPU_ERR_CUDA;
         k_tq_tc<<<grid, XG_TC_THREADS, XG_TC_SMEM, st>>>(p->d_tiles, p->ntiles, p->d_jobs, p->d_tlist, res, q, r, rout, nz, p->d_err,
-                                                           p->wait_tries);
+                                                           p->d_err + 1, p->wait_tries);
         xg_count_launch(1);
         if (xg_cuda_check(cudaGetLastError(), "tq tensor launch")) return XIN_GPU_ERR_CUDA;
     }
@@ -445,8 +446,8 @@ extern "C" int xin_gpu_tq_plan_create(const xin_gpu_tq_block *blocks, int32_t nb
     if (p->ntiles &&
         (xg_cuda_check(cudaMalloc(&p->d_tiles, tiles.size() * sizeof(XgTcTile)), "tq plan") ||
          xg_cuda_check(cudaMalloc(&p->d_tlist, tlist.size() * 4), "tq plan") ||
-         xg_cuda_check(cudaMalloc(&p->d_err, sizeof(int)), "tq plan") ||
-         xg_cuda_check(cudaMemset(p->d_err, 0, sizeof(int)), "tq plan") ||
+         xg_cuda_check(cudaMalloc(&p->d_err, 2 * sizeof(int)), "tq plan") ||
+         xg_cuda_check(cudaMemset(p->d_err, 0, 2 * sizeof(int)), "tq plan") ||
          xg_cuda_check(cudaMemcpy(p->d_tiles, tiles.data(), tiles.size() * sizeof(XgTcTile), cudaMemcpyHostToDevice), "tq plan") ||
          xg_cuda_check(cudaMemcpy(p->d_tlist, tlist.data(), tlist.size() * 4, cudaMemcpyHostToDevice), "tq plan"))) {
         xin_gpu_tq_plan_destroy(p);

@@ -18,8 +18,12 @@
  *   I1  rows (b, j)  K = kv N = y  : t2 = clip16(rnd(sum, 7))              (Xin26xIDct*, columns)
  *   I2  rows (b, y)  K = j  N = x  : out = clip16(rnd(sum, 20 - bd)) (A MN-major) (rows, skip-line rule)
  * The epilogue of a pass (tcgen05.ld, one row per thread) writes the next
- * pass's A operand in shared memory.  Transform-skip blocks stay on the CUDA
- * cores (xg_tq_batch.cuh).
+ * pass's A operand in shared memory.  A pass has one CTA barrier (before its
+ * MMA); every thread then waits for the commit itself, so the epilogue needs no
+ * second one.  Work that does not depend on the pass (the next tile's job
+ * records, the zero tails of 64-wide blocks, the non-zero maps) runs while its
+ * MMA is in flight.  Transform-skip blocks stay on the CUDA cores
+ * (xg_tq_batch.cuh).
  */
 
 #include <cuda_fp16.h>
@@ -29,7 +33,8 @@
 #define XG_TC_A_BYTES (128 * XG_TC_KMAX * 2)
 #define XG_TC_B_BYTES (32 * XG_TC_KMAX * 2)    /* one pass's B: at most 32 x 64 or 64 x 32 */
 /* dynamic shared memory: A hi, A lo, the four passes' B (kept while the tile
- * group does not change), then small state; 50 KB lets four CTAs share an SM,
+ * group does not change), then small state (the mbarrier, the TMEM address, job
+ * records and non-zero maps of two tiles); 50 KB lets four CTAs share an SM,
  * and no more (4 x 128 TMEM columns = the SM's 512) */
 #define XG_TC_SMEM (50 * 1024)
 #define XG_TC_TMEM_COLS 128               /* hi accumulator at column 0, lo at 64 */
@@ -68,11 +73,28 @@ __device__ __forceinline__ uint64_t xg_tc_desc_mn(uint32_t saddr)
     return d;
 }
 
-/* store x (an int16 value) split into exact f16 halves */
-__device__ __forceinline__ void xg_tc_put(uint8_t *ahi, uint8_t *alo, int off, int x)
+/* Conversions without the conversion unit.  In: two int16 values (the halves
+ * of w) as exact f16 pairs hi = x >> 8 in [-128, 127] and lo = x & 255: the
+ * bytes are or-ed under the exponent of 1024 (where the f16 step is 1), and
+ * 1024 (+ 128 for the sign-flipped high byte) is taken off by one half2
+ * subtraction, exact for integers below 2048.  Out: an accumulator (an integer
+ * below 2^22 in magnitude) plus 1.5 * 2^23 has the integer in its low mantissa
+ * bits. */
+__device__ __forceinline__ void xg_tc_split2(uint32_t w, uint32_t &hi, uint32_t &lo)
 {
-    *(__half *)(ahi + off) = __int2half_rn(x >> 8);
-    *(__half *)(alo + off) = __int2half_rn(x & 255);
+    const uint32_t l = (w & 0x00FF00FFu) | 0x64006400u;                  /* 1024 + lo */
+    const uint32_t h = ((w >> 8) & 0x00FF00FFu) ^ 0x64806480u;            /* 1152 + hi */
+    const __half2 lh = __hsub2(*(const __half2 *)&l, __halves2half2(__ushort_as_half(0x6400), __ushort_as_half(0x6400)));
+    const __half2 hh = __hsub2(*(const __half2 *)&h, __halves2half2(__ushort_as_half(0x6480), __ushort_as_half(0x6480)));
+    lo = *(const uint32_t *)&lh;
+    hi = *(const uint32_t *)&hh;
+}
+
+/* 256 * hi + lo from the raw f32 accumulators of the two halves */
+__device__ __forceinline__ int xg_tc_comb(uint32_t h, uint32_t l)
+{
+    const uint32_t bh = __float_as_uint(__uint_as_float(h) + 12582912.0f), bl = __float_as_uint(__uint_as_float(l) + 12582912.0f);
+    return (int)(bh * 256u + bl - 257u * 0x4B400000u);
 }
 
 /* D[hi|lo] (128 x np) = A[hi|lo] (128 x kp) . B (np x kp)^T, issued by one thread;
@@ -119,7 +141,7 @@ __device__ __forceinline__ void xg_tc_row8(uint32_t tmem, int warp, int c0, int 
                  : "=r"(l[0]), "=r"(l[1]), "=r"(l[2]), "=r"(l[3]), "=r"(l[4]), "=r"(l[5]), "=r"(l[6]), "=r"(l[7]) : "r"(a + 64));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 8; j++) out[j] = (int)__uint_as_float(h[j]) * 256 + (int)__uint_as_float(l[j]);
+    for (int j = 0; j < 8; j++) out[j] = xg_tc_comb(h[j], l[j]);
 }
 
 /* columns [c0, c0 + 16) of this thread's TMEM lane, hi and lo combined: both
@@ -138,7 +160,7 @@ __device__ __forceinline__ void xg_tc_row16(uint32_t tmem, int warp, int c0, int
                  : "r"(a + 64));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 16; j++) out[j] = (int)__uint_as_float(h[j]) * 256 + (int)__uint_as_float(l[j]);
+    for (int j = 0; j < 16; j++) out[j] = xg_tc_comb(h[j], l[j]);
 }
 
 /* eight int16 values as the f16 halves of one 16-byte core-matrix row each */
@@ -146,12 +168,7 @@ __device__ __forceinline__ void xg_tc_put8(uint8_t *ahi, uint8_t *alo, int off, 
 {
     uint32_t hw[4], lw[4];
 #pragma unroll
-    for (int p = 0; p < 4; p++) {
-        const __half2 hh = __halves2half2(__int2half_rn(x[2 * p] >> 8), __int2half_rn(x[2 * p + 1] >> 8));
-        const __half2 ll = __halves2half2(__int2half_rn(x[2 * p] & 255), __int2half_rn(x[2 * p + 1] & 255));
-        hw[p] = *(const uint32_t *)&hh;
-        lw[p] = *(const uint32_t *)&ll;
-    }
+    for (int p = 0; p < 4; p++) xg_tc_split2(__byte_perm(x[2 * p], x[2 * p + 1], 0x5410), hw[p], lw[p]);
     *(uint4 *)(ahi + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
     *(uint4 *)(alo + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
 }
@@ -161,12 +178,7 @@ __device__ __forceinline__ void xg_tc_put4(uint8_t *ahi, uint8_t *alo, int off, 
 {
     uint32_t hw[2], lw[2];
 #pragma unroll
-    for (int p = 0; p < 2; p++) {
-        const __half2 hh = __halves2half2(__int2half_rn(x[2 * p] >> 8), __int2half_rn(x[2 * p + 1] >> 8));
-        const __half2 ll = __halves2half2(__int2half_rn(x[2 * p] & 255), __int2half_rn(x[2 * p + 1] & 255));
-        hw[p] = *(const uint32_t *)&hh;
-        lw[p] = *(const uint32_t *)&ll;
-    }
+    for (int p = 0; p < 2; p++) xg_tc_split2(__byte_perm(x[2 * p], x[2 * p + 1], 0x5410), hw[p], lw[p]);
     *(uint2 *)(ahi + off) = make_uint2(hw[0], hw[1]);
     *(uint2 *)(alo + off) = make_uint2(lw[0], lw[1]);
 }
@@ -174,18 +186,29 @@ __device__ __forceinline__ void xg_tc_put4(uint8_t *ahi, uint8_t *alo, int off, 
 __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, int ntiles, const XgTqJob *jobs,
                                                         const uint32_t *list, const xg_coef *res, xg_coef *q, xg_coef *r,
                                                         xg_coef *rout, unsigned long long *nzout, int *err,
-                                                        long long wait_tries)
+                                                        int *next_tile, long long wait_tries)
 {
     extern __shared__ __align__(1024) uint8_t smc[];
     uint8_t *ahi = smc, *alo = smc + XG_TC_A_BYTES, *bm = smc + 2 * XG_TC_A_BYTES;   /* bm: [4][XG_TC_B_BYTES] */
     uint64_t *mbar = (uint64_t *)(bm + 4 * XG_TC_B_BYTES);
     uint32_t *tslot = (uint32_t *)(mbar + 1);
-    unsigned long long *snz = (unsigned long long *)(mbar + 2);         /* [32] per-block non-zero maps */
-    XgTqJob *sjob = (XgTqJob *)(snz + 32);                              /* [32] */
+    unsigned long long *snz = (unsigned long long *)(mbar + 2);         /* [2][32] per-block non-zero maps, by tile parity */
+    XgTqJob *sjob = (XgTqJob *)(snz + 64);                              /* [2][32] job records, by tile parity */
+    int *snext = (int *)(sjob + 64);                                    /* [2] the tile after this one, by parity */
     const int tid = threadIdx.x, warp = tid >> 5;
     const uint32_t s_ahi = (uint32_t)__cvta_generic_to_shared(ahi), s_alo = (uint32_t)__cvta_generic_to_shared(alo);
     const uint32_t s_b = (uint32_t)__cvta_generic_to_shared(bm), s_mbar = (uint32_t)__cvta_generic_to_shared(mbar);
-    static_assert(2 * XG_TC_A_BYTES + 4 * XG_TC_B_BYTES + 16 + 32 * 8 + 32 * sizeof(XgTqJob) <= XG_TC_SMEM, "shared layout");
+    static_assert(2 * XG_TC_A_BYTES + 4 * XG_TC_B_BYTES + 16 + 64 * 8 + 64 * sizeof(XgTqJob) + 8 <= XG_TC_SMEM, "shared layout");
+    /* tiles from a queue: CTA i starts with tile i, then takes tile gridDim.x + (the
+     * counter's next value).  The tiles come largest first, so taking the next one
+     * whenever a CTA is free balances them (a static split gave the CTAs with the
+     * 64 x 64 tiles several times the average work) */
+    const int t0 = blockIdx.x;
+    /* the A operands once: padding lanes that a pass does not write then hold finite
+     * values (zeros, or an earlier pass's), which meet zero B entries or land in
+     * accumulator rows no epilogue reads */
+    for (int e = tid; e < 2 * XG_TC_A_BYTES / 16; e += XG_TC_THREADS) ((uint4 *)smc)[e] = make_uint4(0, 0, 0, 0);
+    if (t0 < ntiles && tid < tiles[t0].count) { sjob[tid] = jobs[list[tiles[t0].first + tid]]; snz[tid] = 0; }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                      ::"r"((uint32_t)__cvta_generic_to_shared(tslot)), "r"(XG_TC_TMEM_COLS) : "memory");
@@ -200,20 +223,29 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
     uint32_t phase = 0;
-    bool ok = true;
+    bool tout = false;                    /* this warp's last wait gave up (the same in every lane) */
 
-    /* one pass: operands written -> MMA with B number bi -> wait; false (for the whole CTA) on a timeout */
-    auto run_pass = [&](int bi, int kp, int np, bool a_mn) -> bool {
+    /* the one barrier of a pass: every thread's operand writes visible to the MMA
+     * issuer and the previous accumulator reads finished; false (for the whole CTA)
+     * when a warp's wait gave up */
+    auto sync_pass = [&]() -> bool {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
+        const int bad = __syncthreads_or(tout);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        return !bad;
+    };
+    auto issue = [&](int bi, int kp, int np, bool a_mn) {
         if (tid == 0) xg_tc_mma(tmem, s_ahi, s_alo, s_b + bi * XG_TC_B_BYTES, kp, np, s_mbar, a_mn);
+    };
+    /* each thread's own bounded wait for the commit: after it the thread may read the
+     * accumulator and overwrite the operands; a warp with a lane that gave up skips
+     * its epilogue and the next barrier ends the CTA's loop */
+    auto wait_pass = [&]() {
         const bool done = xg_tc_wait(s_mbar, phase, wait_tries);
         phase ^= 1;
-        const bool all = !__syncthreads_or(!done);
+        tout = !__all_sync(0xffffffffu, done);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        return all;
     };
     /* B number bi (np x kp) from an int16 matrix: B[n][k] = m[n * ms_n + k * ms_k] for n < nv, k < kv, else 0 */
     auto load_b = [&](int bi, const int16_t *m, int ms_n, int ms_k, int nv, int kv, int np, int kp) {
@@ -233,40 +265,34 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
             }
         }
     };
-    auto zero_a = [&](int kp) {
-        for (int e = tid; e < 128 * kp / 8; e += XG_TC_THREADS) {
-            ((uint4 *)ahi)[e] = make_uint4(0, 0, 0, 0);
-            ((uint4 *)alo)[e] = make_uint4(0, 0, 0, 0);
-        }
-    };
 
-    /* a contiguous range of tiles per CTA: consecutive tiles mostly share their group's matrices */
-    const int per = (ntiles + gridDim.x - 1) / gridDim.x, t_end = min(ntiles, (int)(blockIdx.x + 1) * per);
     int cached = -1;                      /* group (sizes and transform pair) whose B are loaded */
-    for (int ti = blockIdx.x * per; ti < t_end && ok; ti++) {
+    for (int ti = t0, cur = 0; ti < ntiles; cur ^= 1) {
         const XgTcTile tl = tiles[ti];
         const int T = tl.count, lw = tl.lw, lh = tl.lh, w = 1 << lw, h = 1 << lh;
         const int kw = w > 32 ? 32 : w, kh = h > 32 ? 32 : h;
         const int sline = (tl.hor != 0 && w == 32) ? 16 : (w > 32 ? w - 32 : 0), jmax = w - sline;
         const int16_t *mh = xg_mat(tl.hor, lw), *mv = xg_mat(tl.ver, lh);
+        const XgTqJob *tj = sjob + cur * 32;
+        unsigned long long *tnz = snz + cur * 32;
         const int p16 = 16;
         auto rnd16 = [&](int v) { return (v + p16 - 1) & ~(p16 - 1); };
-        if (tid < T) { sjob[tid] = jobs[list[tl.first + tid]]; snz[tid] = 0; }
         const int group = ((lw * 7 + lh) * 3 + tl.hor) * 3 + tl.ver;
-        if (group != cached) {            /* the previous tile's MMAs are all done */
-            load_b(0, mh, w, 1, kw, w, rnd16(kw), rnd16(w));         /* F1: B[k][j] = mh[k][j] */
-            load_b(1, mv, h, 1, kh, h, rnd16(kh), rnd16(h));         /* F2: B[kv][i] = mv[kv][i] */
-            load_b(2, mv, 1, h, h, kh, rnd16(h), rnd16(kh));         /* I1: B[y][kv] = mv[kv][y] */
-            load_b(3, mh, 1, w, w, jmax, rnd16(w), rnd16(jmax));     /* I2: B[x][j] = mh[j][x] */
-            cached = group;
-        }
-        __syncthreads();
 
-        /* ---- F1: A[(b, i)][j] = residual; B[k][j] = mh[k][j] */
-        {
-            const int kp = rnd16(w), np = rnd16(kw);
-            zero_a(kp);
-            __syncthreads();
+        /* the next tile, read by all after the barrier below (this slot's readers, two
+         * tiles back, have passed the previous tile's barriers) */
+        if (tid == 0) snext[cur] = (int)gridDim.x + atomicAdd(next_tile, 1);
+        /* ---- F1: A[(b, i)][j] = residual; B[k][j] = mh[k][j] (every thread has seen the
+         * previous tile's last MMA complete: operands and B are free) */
+        const int kp1 = rnd16(w), np1 = rnd16(kw);
+        if (!tout) {
+            if (group != cached) {
+                load_b(0, mh, w, 1, kw, w, rnd16(kw), rnd16(w));         /* F1: B[k][j] = mh[k][j] */
+                load_b(1, mv, h, 1, kh, h, rnd16(kh), rnd16(h));         /* F2: B[kv][i] = mv[kv][i] */
+                load_b(2, mv, 1, h, h, kh, rnd16(h), rnd16(kh));         /* I1: B[y][kv] = mv[kv][y] */
+                load_b(3, mh, 1, w, w, jmax, rnd16(w), rnd16(jmax));     /* I2: B[x][j] = mh[j][x] */
+                cached = group;
+            }
             /* eight consecutive samples per load (16-byte aligned: the plan keeps block
              * offsets at multiples of 8), four chunks in flight per thread */
             const int nchunk = (T * h * w) >> 3, lbs = lw + lh;
@@ -277,7 +303,7 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                     const int c = c0 + u * XG_TC_THREADS;
                     if (c < nchunk) {
                         const int e = c << 3, b = e >> lbs, o = e & ((1 << lbs) - 1);
-                        const uint4 *src = (const uint4 *)(res + sjob[b].off + o);
+                        const uint4 *src = (const uint4 *)(res + tj[b].off + o);
                         *(uint4 *)v[u] = src[0];
                         if (sizeof(xg_coef) == 4) *(uint4 *)(v[u] + 4) = src[1];
                     }
@@ -291,22 +317,28 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
 #pragma unroll
                     for (int x = 0; x < 8; x++) x8[x] = (int16_t)v[u][x];
                     if (w >= 8) {         /* one core-matrix row: columns j .. j + 7 of row i */
-                        xg_tc_put8(ahi, alo, xg_tc_off(b * h + (o >> lw), o & (w - 1), kp), x8);
-                    } else {
-#pragma unroll
-                        for (int x = 0; x < 8; x++)
-                            xg_tc_put(ahi, alo, xg_tc_off(b * h + ((o + x) >> lw), (o + x) & (w - 1), kp), x8[x]);
+                        xg_tc_put8(ahi, alo, xg_tc_off(b * h + (o >> lw), o & (w - 1), kp1), x8);
+                    } else {              /* w = 4: two rows of four (o is a multiple of 8) */
+                        xg_tc_put4(ahi, alo, xg_tc_off(b * h + (o >> 2), 0, kp1), x8);
+                        xg_tc_put4(ahi, alo, xg_tc_off(b * h + (o >> 2) + 1, 0, kp1), x8 + 4);
                     }
                 }
             }
-            if (!(ok = run_pass(0, kp, np, false))) break;
         }
+        if (!sync_pass()) break;
+        issue(0, kp1, np1, false);
+        /* the next tile's job records, while the MMA runs: this buffer's last readers
+         * (the previous tile) finished before the barrier above */
+        const int nxt = snext[cur];
+        if (nxt < ntiles) {
+            const XgTcTile tn = tiles[nxt];
+            if (tid < tn.count) { sjob[(cur ^ 1) * 32 + tid] = jobs[list[tn.first + tid]]; snz[(cur ^ 1) * 32 + tid] = 0; }
+        }
+        wait_pass();
         /* ---- F1 epilogue -> F2 operand A[(b, k)][i] = t1, MN-major: a thread's values for
-         * consecutive k are consecutive rows (the MMA is done: A and B are free) */
-        {
-            const int kp = rnd16(h), np = rnd16(kh);
-            zero_a(kp);
-            __syncthreads();
+         * consecutive k are consecutive rows */
+        const int kp2 = rnd16(h), np2 = rnd16(kh);
+        if (!tout) {
             const int m = tid, b = m >> lh, i = m & (h - 1);
             const bool valid = m < T * h;
             const int s1 = lw + XG_BITDEPTH + 6 - 15;
@@ -324,17 +356,17 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                     }
                 }
             }
-            if (!(ok = run_pass(1, kp, np, true))) break;
         }
+        if (!sync_pass()) break;
+        issue(1, kp2, np2, true);
+        wait_pass();
         /* ---- F2 epilogue: quant / dequant, q and r out; -> I1 operand A[(b, j)][kv] = r (the same rows) */
-        {
-            const int kp = rnd16(kh), np = rnd16(h);
-            zero_a(kp);
-            __syncthreads();
+        const int kp3 = rnd16(kh), np3 = rnd16(h);
+        if (!tout) {
             const int lkw = lw > 5 ? 5 : lw;
             const int m = tid, b = m >> lkw, k = m & (kw - 1);     /* row (b, k): coefficients C[kv][k] */
             const bool valid = m < T * kw;
-            const XgTqJob jb = sjob[valid ? b : 0];
+            const XgTqJob jb = tj[valid ? b : 0];
             const int s2 = lh + 6;
             /* quant parameters (Xin266ConstructQuantParam + Xin266Transform), as in k_tq_batch */
             const int adj = ((lw + lh) & 1), lgs = (lw + lh) >> 1;
@@ -353,7 +385,8 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                     rr[j] = 0;                /* beyond kh: the I1 operand's zero padding */
                     if (!valid || kv >= kh) continue;
                     const int tv = xg_clip16(xg_rshift_rnd(v[j], s2)), a = abs(tv);
-                    int qv = (int)(((long long)a * qmult + qadd) >> qshift);
+                    /* a * qmult + qadd < 2^15 * 26214 + 2^28 < 2^31: exact in 32 bits */
+                    int qv = (int)(((uint32_t)a * (uint32_t)qmult + (uint32_t)qadd) >> qshift);
                     qv = xg_clip16(tv < 0 ? -qv : qv);
                     const int rv = xg_clip16((int)(((long long)qv * iqmult + iqadd) >> iqshift));
                     q[jb.off + kv * w + k] = (xg_coef)qv;
@@ -362,28 +395,36 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                     rr[j] = rv;
                 }
                 if (valid && k < jmax) {      /* row m of the I1 operand, columns c .. c + 15 */
-                    xg_tc_put8(ahi, alo, xg_tc_off(m, c, kp), rr);
-                    xg_tc_put8(ahi, alo, xg_tc_off(m, c + 8, kp), rr + 8);
+                    xg_tc_put8(ahi, alo, xg_tc_off(m, c, kp3), rr);
+                    xg_tc_put8(ahi, alo, xg_tc_off(m, c + 8, kp3), rr + 8);
                 }
             }
-            if (nzb) atomicOr(&snz[b], nzb);
-            if (!(ok = run_pass(2, kp, np, false))) break;
+            if (nzb) atomicOr(&tnz[b], nzb);
         }
-        /* zeros of q / r beyond the kept 32 x 32 (64-wide or -high blocks), and the maps */
-        if (w > 32 || h > 32)
+        if (!sync_pass()) break;
+        issue(2, kp3, np3, false);
+        /* while the MMA runs: zeros of q / r beyond the kept 32 x 32 (64-wide or -high
+         * blocks; a 16-byte chunk lies wholly inside or outside it) and the maps, whose
+         * bits were all set before the barrier above */
+        if (w > 32 || h > 32) {
+            constexpr int E = 16 / (int)sizeof(xg_coef);
+            const int nch = (w * h) / E;
             for (int bb = 0; bb < T; bb++) {
-                const uint32_t off = sjob[bb].off;
-                for (int o = tid; o < w * h; o += XG_TC_THREADS) {
-                    const int y = o >> lw, x = o & (w - 1);
-                    if (y >= kh || x >= kw) { q[off + o] = 0; r[off + o] = 0; }
+                const uint32_t off = tj[bb].off;
+                for (int c = tid; c < nch; c += XG_TC_THREADS) {
+                    const int o = c * E, y = o >> lw, x = o & (w - 1);
+                    if (y >= kh || x >= kw) {
+                        *(uint4 *)(q + off + o) = make_uint4(0, 0, 0, 0);
+                        *(uint4 *)(r + off + o) = make_uint4(0, 0, 0, 0);
+                    }
                 }
             }
-        if (tid < T) nzout[list[tl.first + tid]] = snz[tid];
+        }
+        if (tid < T) nzout[list[tl.first + tid]] = tnz[tid];
+        wait_pass();
         /* ---- I1 epilogue -> I2 operand A[(b, y)][j] = t2, MN-major (consecutive y, consecutive rows) */
-        {
-            const int kp = rnd16(jmax), np = rnd16(w);
-            zero_a(kp);
-            __syncthreads();
+        const int kp4 = rnd16(jmax), np4 = rnd16(w);
+        if (!tout) {
             const int lkw = lw > 5 ? 5 : lw;
             const int m = tid, b = m >> lkw, j = m & (kw - 1);
             const bool valid = m < T * kw && j < jmax;
@@ -401,14 +442,16 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                     }
                 }
             }
-            if (!(ok = run_pass(3, kp, np, true))) break;
         }
+        if (!sync_pass()) break;
+        issue(3, kp4, np4, true);
+        wait_pass();
         /* ---- I2 epilogue: the reconstructed residual */
-        {
+        if (!tout) {
             const int m = tid, b = m >> lh, y = m & (h - 1);
             const bool valid = m < T * h;
             const int s2 = 6 + 15 - 1 - XG_BITDEPTH;
-            const int off = valid ? sjob[b].off + y * w : 0;
+            const int off = valid ? tj[b].off + y * w : 0;
             for (int c = 0; c < rnd16(w); c += 16) {
                 int v[16];
                 xg_tc_row16(tmem, warp, c, v);
@@ -425,17 +468,16 @@ __global__ void __launch_bounds__(XG_TC_THREADS) k_tq_tc(const XgTcTile *tiles, 
                 }
             }
         }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        ti = nxt;
     }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    const bool ok = !__syncthreads_or(tout);
     if (!ok && tid == 0) {
         atomicExch(err, 1);
         /* the MMA whose wait gave up may still be writing the accumulators: wait for
          * its commit (again bounded) before the tensor memory is released */
         xg_tc_wait(s_mbar, phase ^ 1, XG_TC_WAIT_TRIES);
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(XG_TC_TMEM_COLS) : "memory");
 }
