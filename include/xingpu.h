@@ -500,6 +500,19 @@ typedef struct xin_gpu_stream_cfg {
                                     (xin_gpu_results.mts); the coefficient and reconstructed
                                     planes and xin_gpu_cu_result's nz / ssd hold the DCT2
                                     candidate.  Slice QPs up to 51 (39 at 10 bits). */
+    int32_t  refs;               /* 0 or 1: one reference, the previous picture (list 0).
+                                    2: two references, list 0 = the previous picture and list 1 =
+                                    the one before it (the second picture uses the previous one
+                                    for both).  Per CU: the integer and sub-pel search in each
+                                    list, the bi search of Xin266InterBiSearch
+                                    (h266_analyze_inter_cu.c:507; default BCW weight, predictor 0,
+                                    a +-4 integer step in place of the closed BBDGS step), the
+                                    choice of the lowest of the list-0, list-1 and bi costs (strict,
+                                    in that order), and the prediction, transform and
+                                    reconstruction of that choice (the bi prediction:
+                                    Xin266LumaMotionComp / Xin266ChromaMotionComp's average of the
+                                    14-bit predictions).  xin_gpu_cu_result keeps list 0's search;
+                                    xin_gpu_results.bi the rest.  tu_mode 0 and CU levels up to 64. */
 } xin_gpu_stream_cfg;
 
 typedef struct xin_gpu_picture {
@@ -527,6 +540,16 @@ typedef struct xin_gpu_cu_mts {
     uint64_t ssd[5];             /* luma SSD of each candidate's reconstruction */
 } xin_gpu_cu_mts;
 
+/* refs 2: list 1's search, the bi pair and the choice of a CU */
+typedef struct xin_gpu_cu_bi {
+    int32_t  mvx1, mvy1;         /* list 1, quarter-pel */
+    uint32_t cost1;              /* list 1 after sub-pel */
+    uint32_t int_cost1;          /* list 1 after the integer search */
+    int32_t  bmv[4];             /* the bi pair: list 0 (x, y), list 1 (x, y), quarter-pel */
+    uint32_t bi_cost;            /* (averaged-prediction SAD << 8) + both MVs' bits * sad_lambda */
+    uint32_t inter_dir;          /* the prediction coded: 1 list 0, 2 list 1, 3 bi */
+} xin_gpu_cu_bi;
+
 typedef struct xin_gpu_results {
     xin_gpu_cu_result *cu;       /* [xin_gpu_stream_num_cus()], levels from 64 down to 8 */
     XG_COEFF *q[3];              /* [levels][plane height][plane width] when XIN_GPU_OUT_Q; zero where
@@ -535,6 +558,7 @@ typedef struct xin_gpu_results {
     XG_PIXEL *rec[3];            /* same layout when XIN_GPU_OUT_REC */
     float    gpu_ms;             /* device time of the picture's launches */
     xin_gpu_cu_mts *mts;         /* tu_mode 1: [xin_gpu_stream_num_cus()] (NULL: a view is returned) */
+    xin_gpu_cu_bi  *bi;          /* refs 2: [xin_gpu_stream_num_cus()] (NULL: a view is returned) */
 } xin_gpu_results;
 
 int  xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream **out);

@@ -50,7 +50,8 @@ class orc_frame_desc(C.Structure):
                 ("ref", vp * 3), ("ref_stride", ip * 2),
                 ("search_range", i32), ("sad_lambda", u32), ("qp", i32), ("uv_qp", i32), ("intra_frame", i32),
                 ("search_mode", i32), ("in_lo", vp * 2), ("in_lo_stride", ip * 2),
-                ("ref_lo", vp * 2), ("ref_lo_stride", ip * 2), ("tu_mode", i32), ("ctx", vp)]
+                ("ref_lo", vp * 2), ("ref_lo_stride", ip * 2), ("tu_mode", i32), ("ctx", vp),
+                ("refs", i32), ("ref1", vp * 3), ("ref1_lo", vp * 2)]
 
 
 class orc_hier_in(C.Structure):
@@ -73,7 +74,9 @@ class xin_dp_param(C.Structure):
 
 class orc_cu_out(C.Structure):
     _fields_ = [("mvx", i32), ("mvy", i32), ("cost", u32), ("int_cost", u32), ("nz", u64 * 3), ("ssd", u64 * 3),
-                ("satd_cost", u32), ("ncand", u32), ("nz_mts", u64 * 5), ("ssd_mts", u64 * 5)]
+                ("satd_cost", u32), ("ncand", u32), ("nz_mts", u64 * 5), ("ssd_mts", u64 * 5),
+                ("mvx1", i32), ("mvy1", i32), ("cost1", u32), ("int_cost1", u32), ("bmv", i32 * 4), ("bi_cost", u32),
+                ("inter_dir", u32)]
 
 
 # logical name -> (oracle symbol, reference symbol or None, argtypes)
@@ -129,6 +132,10 @@ _SIGS = {
     "luma_interpolation": ("orc_luma_interpolation", None, [vp, ip, vp, ip, i32, u32, u32, u32]),
     "luma_inter_pred": ("orc_luma_inter_pred", None, [vp, ip, vp, ip, i32, i32, i32, i32, i32, i32, i32, i32, u32, u32, u32]),
     "chroma_motion_comp": ("orc_chroma_motion_comp", None, [vp, ip, vp, ip, i32, i32, i32, i32, i32, i32, i32, i32, u32, u32]),
+    "luma_motion_comp_bi": ("orc_luma_motion_comp_bi", None, [vp, vp, ip, vp, ip, vp, i32, i32, i32, i32, i32, i32, u32, u32]),
+    "chroma_motion_comp_bi": ("orc_chroma_motion_comp_bi", None, [vp, vp, ip, vp, ip, vp, i32, i32, i32, i32, i32, i32,
+                                                                  u32, u32]),
+    "bi_me_input": ("orc_bi_me_input", None, [vp, ip, vp, ip, vp, ip, u32, u32]),
     "quant_params": ("orc_quant_params", None, [i32, u32, u32, u32, C.c_int, C.c_int, C.POINTER(orc_qparams)]),
     "transform_tu": ("orc_transform_tu", None, [vp, ip, vp, ip, vp, vp, vp, ip, u32, u32, u32, u32, i32, C.c_int, C.c_int,
                                                 C.c_int, C.c_int, vp]),
@@ -174,6 +181,8 @@ _REF_ONLY = {
                                                     i32]),
     "chroma_motion_comp_ref": ("ref_chroma_motion_comp", [vp, vp, vp, vp, ip, vp, vp, ip, vp, i32, i32, u32, i32, i32,
                                                           i32, i32, i32, i32, u32, u32]),
+    "luma_motion_comp_ref": ("ref_luma_motion_comp", [vp, vp, ip, vp, ip, vp, i32, i32, i32, i32, i32, i32, u32, u32]),
+    "weight_bi_me_input_ref": ("Xin266ConstructWeightBiMeInput", [vp, ip, vp, ip, vp, ip, u32, u32, i32]),
     "transform_tu_ref": ("ref_transform_tu", [vp, ip, vp, ip, vp, vp, vp, ip, u32, u32, u32, u32, i32, i32, u32, i32, i32,
                                               i32, vp, vp]),
 }

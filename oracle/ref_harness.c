@@ -296,6 +296,26 @@ void ref_chroma_motion_comp(PIXEL *ref_u0, PIXEL *ref_v0, PIXEL *ref_u1, PIXEL *
     free(hs);
 }
 
+/* Xin266LumaMotionComp (h266_encoder/source/h266_inter_prediction.c:433), called
+ * unmodified with both lists set (its bi-prediction branch, default BCW weight) */
+void Xin266LumaMotionComp(xin_sec_struct *, SINT32, SINT32, PIXEL *, intptr_t, xin_mv32_u *, SINT8 *, UINT8, UINT32);
+
+void ref_luma_motion_comp(PIXEL *ref0, PIXEL *ref1, intptr_t rs, PIXEL *pred, intptr_t ps, const SINT32 *mv16,
+                          SINT32 cu_x, SINT32 cu_y, SINT32 min_mvx, SINT32 min_mvy, SINT32 max_mvx, SINT32 max_mvy,
+                          UINT32 w, UINT32 h)
+{
+    xin_cu_struct cu; xin_ref_picture rp0, rp1; xin_mv32_u mv[2]; SINT8 ri[2] = { 0, 0 };
+    harness *hs = mc_harness(cu_x, cu_y, min_mvx, min_mvy, max_mvx, max_mvy, &cu);
+    memset(&rp0, 0, sizeof rp0); memset(&rp1, 0, sizeof rp1);
+    rp0.refBuf[PLANE_LUMA] = ref0; rp0.refStride[0] = rs;
+    rp1.refBuf[PLANE_LUMA] = ref1; rp1.refStride[0] = rs;
+    hs->pic.pictureRead[XIN_LIST_0][0] = &rp0;
+    hs->pic.pictureRead[XIN_LIST_1][0] = &rp1;
+    mv[0].mv.mv32X = mv16[0]; mv[0].mv.mv32Y = mv16[1]; mv[1].mv.mv32X = mv16[2]; mv[1].mv.mv32Y = mv16[3];
+    Xin266LumaMotionComp(&hs->sec, (SINT32)w, (SINT32)h, pred, ps, mv, ri, XIN_BCW_DEFAULT, 0);
+    free(hs);
+}
+
 /* ---- DMVR ----------------------------------------------------------------
  * Xin266LumaMotionCompDmvr (h266_encoder/source/h266_inter_prediction.c:1178),
  * which runs Xin266DeriveMvFromDmvr (:975), called unmodified on a picture set

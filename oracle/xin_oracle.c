@@ -438,6 +438,62 @@ void orc_chroma_motion_comp(const opix *ref_origin, intptr_t rs, opix *pred, int
     else orc_chroma_hv(src, rs, pred, ps, frac, cw, ch, 0);
 }
 
+/* Bi-prediction branch of Xin266LumaMotionComp (h266_inter_prediction.c:473-552):
+ * each list's 1/16-pel MV clamped to the window, its 14-bit intermediate
+ * prediction (pfXinLumaInterpS16 by phase), then Xin266InterpAvgS16U8. */
+void orc_luma_motion_comp_bi(const opix *ref0, const opix *ref1, intptr_t rs, opix *pred, intptr_t ps, const int32_t *mv16,
+                             int32_t cu_x, int32_t cu_y, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
+                             uint32_t w, uint32_t h)
+{
+    int16_t *b[2];
+    for (int l = 0; l < 2; l++) {
+        b[l] = (int16_t *)malloc(sizeof(int16_t) * w * h);
+        int32_t mvx = CLIP3(min_mvx * 16, max_mvx * 16, mv16[2 * l]), mvy = CLIP3(min_mvy * 16, max_mvy * 16, mv16[2 * l + 1]);
+        int32_t ox = cu_x * 16 + mvx, oy = cu_y * 16 + mvy, fx = ox & 15, fy = oy & 15, frac = (fy << 4) + fx;
+        const opix *src = (l ? ref1 : ref0) + (intptr_t)(oy >> 4) * rs + (ox >> 4);
+        if (!fx && !fy) orc_interp_copy_s16(src, rs, b[l], w, frac, w, h, 0);
+        else if (fx && !fy) orc_luma_hor_s16(src, rs, b[l], w, frac, w, h, 0);
+        else if (!fx && fy) orc_luma_vet_s16(src, rs, b[l], w, frac, w, h, 0);
+        else orc_luma_hv_s16(src, rs, b[l], w, frac, w, h, 0);
+    }
+    orc_interp_avg(b[0], w, b[1], w, pred, ps, w, h);
+    free(b[0]); free(b[1]);
+}
+
+/* Bi-prediction branch of Xin266ChromaMotionComp (h266_inter_prediction.c:658-755):
+ * the 1/32 chroma phase (mask 31) of each list, the 14-bit intermediate
+ * (pfXinChromaInterpS16), then Xin266InterpAvgS16U8 over the (w/2) x (h/2) block. */
+void orc_chroma_motion_comp_bi(const opix *ref0, const opix *ref1, intptr_t rs, opix *pred, intptr_t ps, const int32_t *mv16,
+                               int32_t cu_x, int32_t cu_y, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
+                               uint32_t w, uint32_t h)
+{
+    uint32_t cw = w >> 1, ch = h >> 1;
+    int16_t *b[2];
+    for (int l = 0; l < 2; l++) {
+        b[l] = (int16_t *)malloc(sizeof(int16_t) * cw * ch);
+        int32_t mvx = CLIP3(min_mvx * 16, max_mvx * 16, mv16[2 * l]), mvy = CLIP3(min_mvy * 16, max_mvy * 16, mv16[2 * l + 1]);
+        int32_t ox = cu_x * 16 + mvx, oy = cu_y * 16 + mvy, fx = ox & 31, fy = oy & 31, frac = (fy << 5) + fx;
+        const opix *src = (l ? ref1 : ref0) + (intptr_t)(oy >> 5) * rs + (ox >> 5);
+        if (!fx && !fy) orc_interp_copy_s16(src, rs, b[l], cw, frac, cw, ch, 0);
+        else if (fx && !fy) orc_chroma_hor_s16(src, rs, b[l], cw, frac, cw, ch, 0);
+        else if (!fx && fy) orc_chroma_vet_s16(src, rs, b[l], cw, frac, cw, ch, 0);
+        else orc_chroma_hv_s16(src, rs, b[l], cw, frac, cw, ch, 0);
+    }
+    orc_interp_avg(b[0], cw, b[1], cw, pred, ps, cw, ch);
+    free(b[0]); free(b[1]);
+}
+
+/* Target of the bi refinement, clip(2 in - pred).  The default-weight
+ * constructor (Xin26xConstructBiMeInput) is closed; the open weighted form
+ * Xin266ConstructWeightBiMeInput (h266_construct_weight_input.c:24-58) at the
+ * default weight 4 of 8 computes (8192 in - 4096 pred + 2048) >> 12, which is
+ * 2 in - pred exactly, clipped to the sample range. */
+void orc_bi_me_input(const opix *in, intptr_t is, const opix *pred, intptr_t ps, opix *out, intptr_t os, uint32_t w, uint32_t h)
+{
+    for (uint32_t y = 0; y < h; y++)
+        for (uint32_t x = 0; x < w; x++) out[y * os + x] = clip_pix(2 * (int32_t)in[y * is + x] - (int32_t)pred[y * ps + x]);
+}
+
 /* ======================================================================
  * Transforms.
  * Matrices: H.266 clause 8.7.4.5 transMatrix (DCT-II up to 64 points) and the
@@ -1343,14 +1399,15 @@ static void orc_cu_tu_p4(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, in
     free(rb);
 }
 
-void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size,
-                    ocoef *q[3], intptr_t q_stride[2], opix *rec[3], intptr_t rec_stride[2], orc_cu_out *out)
+/* integer search and Xin266FullSubPelMe of one list (ref: the list's padded luma
+ * at picture (0,0); ref_lo its downscaled planes for search_mode 1) */
+static void orc_uni_search(const orc_frame_desc *f, const opix *ref, const opix *const *ref_lo, int32_t cu_x, int32_t cu_y,
+                           int32_t size, int32_t mnx, int32_t mny, int32_t mxx, int32_t mxy, orc_me_io *io, uint32_t *int_cost)
 {
-    int32_t mnx, mny, mxx, mxy;
-    orc_mv_window(f->width, f->height, f->ctu, cu_x, cu_y, size, size, &mnx, &mny, &mxx, &mxy);
     const opix *in_y = f->in[0] + (intptr_t)cu_y * f->in_stride[0] + cu_x;
-    const opix *ref_y = f->ref[0] + (intptr_t)cu_y * f->ref_stride[0] + cu_x;
-    orc_me_io io = { 0, 0, 0xFFFFFFFFu, 0 };
+    const opix *ref_y = ref + (intptr_t)cu_y * f->ref_stride[0] + cu_x;
+    orc_me_io z = { 0, 0, 0xFFFFFFFFu, 0 };
+    *io = z;
     if (f->search_mode == 1) {
         /* predictor 0, one candidate: the zero MV (Xin266FillMeCand's meCand[0],
          * h266_analyze_inter_cu.c:168) */
@@ -1361,19 +1418,122 @@ void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t
         for (int l = 1; l <= 2; l++) {
             hin.in[l] = f->in_lo[l - 1] + (intptr_t)(cu_y >> l) * f->in_lo_stride[l - 1] + (cu_x >> l);
             hin.in_stride[l] = f->in_lo_stride[l - 1];
-            hin.ref[l] = f->ref_lo[l - 1] + (intptr_t)(cu_y >> l) * f->ref_lo_stride[l - 1] + (cu_x >> l);
+            hin.ref[l] = ref_lo[l - 1] + (intptr_t)(cu_y >> l) * f->ref_lo_stride[l - 1] + (cu_x >> l);
             hin.ref_stride[l] = f->ref_lo_stride[l - 1];
         }
         hin.cand = zero; hin.ncand = 1;
         orc_me_hier(&hin, (uint32_t)size, (uint32_t)size, 0, 0, f->search_range, f->search_range, f->sad_lambda,
-                    mnx, mny, mxx, mxy, &io);
+                    mnx, mny, mxx, mxy, io);
     } else
         orc_me_full(in_y, f->in_stride[0], ref_y, f->ref_stride[0], (uint32_t)size, (uint32_t)size, 0, 0,
-                    f->search_range, f->sad_lambda, mnx, mny, mxx, mxy, &io);
-    out->int_cost = io.best_cost;
+                    f->search_range, f->sad_lambda, mnx, mny, mxx, mxy, io);
+    *int_cost = io->best_cost;
     orc_full_subpel_me(in_y, f->in_stride[0], ref_y, f->ref_stride[0], (uint32_t)size, (uint32_t)size, 0, 0,
-                       f->sad_lambda, mnx, mny, mxx, mxy, &io);
+                       f->sad_lambda, mnx, mny, mxx, mxy, io);
+}
+
+/* Integer step of the bi refinement.  The reference runs the closed
+ * Xin26xMotionEstBbdgs with searchWidth = searchHeight = 4 around the list's
+ * uni MV (h266_analyze_inter_cu.c:607-608,665-677); restated here as every
+ * integer MV in [c - 4, c + 4]^2 within the window, raster order, strict '<'
+ * from UINT32_MAX, cost (SAD << 8) + bits(mv) * lambda with predictor 0.
+ * Unpinned (the closed search's order is not visible). */
+static void orc_me_square(const opix *in, intptr_t is, const opix *ref_at_pu, intptr_t rs, uint32_t w, uint32_t h,
+                          int32_t cx, int32_t cy, int32_t range, uint32_t lambda,
+                          int32_t mnx, int32_t mny, int32_t mxx, int32_t mxy, orc_me_io *io)
+{
+    uint32_t best = 0xFFFFFFFFu, bsad = 0;
+    int32_t bx = 0, by = 0;
+    for (int32_t y = cy - range; y <= cy + range; y++)
+        for (int32_t x = cx - range; x <= cx + range; x++) {
+            if (x < mnx || x > mxx || y < mny || y > mxy) continue;
+            uint32_t sad;
+            orc_sad(in, is, ref_at_pu + (intptr_t)y * rs + x, rs, w, h, &sad);
+            uint32_t c = (sad << 8) + mv_cost(x * 4, y * 4, 0, 0, lambda);
+            if (c < best) { best = c; bsad = sad; bx = x * 4; by = y * 4; }
+        }
+    io->best_cost = best; io->best_sad = bsad; io->best_mvx = bx; io->best_mvy = by;
+}
+
+/* Xin266InterBiSearch (h266_analyze_inter_cu.c:507-870) for one reference per
+ * list, the default BCW weight, mvdL1Zero off (two iterations) and predictor 0:
+ * the list with the larger uni cost is refined first (:580-591), each time
+ * against clip(2 in - the other list's prediction) (:617-641) from the integer
+ * part of its uni MV (:665-671), integer step then Xin266FullSubPelMe
+ * (:676-701); the pair's cost is the SAD against the average of the two
+ * predictions (pfXinComputeAvgDist, :718-729) plus both MVs' bits (:780-782),
+ * kept when it improves (:784-794).  The prediction buffers keep each
+ * iteration's last MV, and the final cost is taken on them (:815-852).  Ref-index,
+ * predictor-index, BCW and direction bits are left out (one reference per
+ * list, predictor 0).  Returns the bi pair and cost. */
+static void orc_cu_bi(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size, int32_t mnx, int32_t mny,
+                      int32_t mxx, int32_t mxy, const int32_t uni[2][2], const uint32_t ucost[2], int32_t bmv[2][2],
+                      uint32_t *bi_cost)
+{
+    const opix *in_y = f->in[0] + (intptr_t)cu_y * f->in_stride[0] + cu_x;
+    const intptr_t is = f->in_stride[0], rs = f->ref_stride[0];
+    const opix *refo[2] = { f->ref[0], f->ref1[0] };
+    const uint32_t n = (uint32_t)(size * size), lambda = f->sad_lambda;
+    opix *bp[2], *tgt = (opix *)malloc(sizeof(opix) * n);
+    for (int l = 0; l < 2; l++) {
+        bp[l] = (opix *)malloc(sizeof(opix) * n);
+        orc_luma_inter_pred(refo[l], rs, bp[l], size, uni[l][0] * 4, uni[l][1] * 4, cu_x, cu_y, mnx, mny, mxx, mxy,
+                            (uint32_t)size, (uint32_t)size, 0);
+        bmv[l][0] = uni[l][0]; bmv[l][1] = uni[l][1];
+    }
+    int li = ucost[0] <= ucost[1] ? 1 : 0;
+    uint32_t best = 0xFFFFFFFFu, sad;
+    for (int it = 0; it < 2; it++, li = 1 - li) {
+        orc_bi_me_input(in_y, is, bp[1 - li], size, tgt, size, (uint32_t)size, (uint32_t)size);
+        const opix *ref_y = refo[li] + (intptr_t)cu_y * rs + cu_x;
+        orc_me_io io;
+        orc_me_square(tgt, size, ref_y, rs, (uint32_t)size, (uint32_t)size, uni[li][0] >> 2, uni[li][1] >> 2, 4, lambda,
+                      mnx, mny, mxx, mxy, &io);
+        orc_full_subpel_me(tgt, size, ref_y, rs, (uint32_t)size, (uint32_t)size, 0, 0, lambda, mnx, mny, mxx, mxy, &io);
+        orc_luma_inter_pred(refo[li], rs, bp[li], size, io.best_mvx * 4, io.best_mvy * 4, cu_x, cu_y, mnx, mny, mxx, mxy,
+                            (uint32_t)size, (uint32_t)size, 0);
+        orc_avg_sad(in_y, is, bp[0], bp[1], size, (uint32_t)size, (uint32_t)size, &sad);
+        const uint32_t c = (sad << 8) + (orc_mvd_bits(io.best_mvx) + orc_mvd_bits(io.best_mvy) +
+                                         orc_mvd_bits(bmv[1 - li][0]) + orc_mvd_bits(bmv[1 - li][1])) * lambda;
+        if (c < best) { best = c; bmv[li][0] = io.best_mvx; bmv[li][1] = io.best_mvy; }
+    }
+    orc_avg_sad(in_y, is, bp[0], bp[1], size, (uint32_t)size, (uint32_t)size, &sad);
+    *bi_cost = (sad << 8) + (orc_mvd_bits(bmv[0][0]) + orc_mvd_bits(bmv[0][1]) + orc_mvd_bits(bmv[1][0]) +
+                             orc_mvd_bits(bmv[1][1])) * lambda;
+    free(bp[0]); free(bp[1]); free(tgt);
+}
+
+void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size,
+                    ocoef *q[3], intptr_t q_stride[2], opix *rec[3], intptr_t rec_stride[2], orc_cu_out *out)
+{
+    int32_t mnx, mny, mxx, mxy;
+    orc_mv_window(f->width, f->height, f->ctu, cu_x, cu_y, size, size, &mnx, &mny, &mxx, &mxy);
+    orc_me_io io;
+    orc_uni_search(f, f->ref[0], f->ref_lo, cu_x, cu_y, size, mnx, mny, mxx, mxy, &io, &out->int_cost);
     out->mvx = io.best_mvx; out->mvy = io.best_mvy; out->cost = io.best_cost;
+    /* the prediction that is coded: list 0 (refs 1), or the choice among list 0,
+     * list 1 and the pair (lowest cost, strict '<' in that order) */
+    int32_t dir = 1, mv16[4] = { io.best_mvx * 4, io.best_mvy * 4, 0, 0 };
+    if (f->refs == 2) {
+        orc_me_io io1;
+        orc_uni_search(f, f->ref1[0], f->ref1_lo, cu_x, cu_y, size, mnx, mny, mxx, mxy, &io1, &out->int_cost1);
+        out->mvx1 = io1.best_mvx; out->mvy1 = io1.best_mvy; out->cost1 = io1.best_cost;
+        const int32_t uni[2][2] = { { io.best_mvx, io.best_mvy }, { io1.best_mvx, io1.best_mvy } };
+        const uint32_t ucost[2] = { io.best_cost, io1.best_cost };
+        int32_t bmv[2][2];
+        orc_cu_bi(f, cu_x, cu_y, size, mnx, mny, mxx, mxy, uni, ucost, bmv, &out->bi_cost);
+        for (int l = 0; l < 2; l++) { out->bmv[2 * l] = bmv[l][0]; out->bmv[2 * l + 1] = bmv[l][1]; }
+        uint32_t best = ucost[0];
+        if (ucost[1] < best) { best = ucost[1]; dir = 2; }
+        if (out->bi_cost < best) dir = 3;
+        if (dir == 2) { mv16[0] = io1.best_mvx * 4; mv16[1] = io1.best_mvy * 4; }
+        if (dir == 3)
+            for (int k = 0; k < 4; k++) mv16[k] = out->bmv[k] * 4;
+        out->inter_dir = (uint32_t)dir;
+    }
+    const opix *lref[3] = { f->ref[0], f->ref[1], f->ref[2] };
+    if (dir == 2)
+        for (int p = 0; p < 3; p++) lref[p] = f->ref1[p];
 
     int32_t cs = size >> 1;
     opix *pred = (opix *)malloc(sizeof(opix) * (size_t)(size * size));
@@ -1388,11 +1548,17 @@ void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t
     for (int pl = 0; pl < 3; pl++) {
         int32_t bs = pl ? cs : size, px = pl ? cu_x >> 1 : cu_x, py = pl ? cu_y >> 1 : cu_y;
         intptr_t istr = f->in_stride[pl ? 1 : 0], qstr = q_stride[pl ? 1 : 0], rstr = rec_stride[pl ? 1 : 0];
-        if (pl == 0)
-            orc_luma_inter_pred(f->ref[0], f->ref_stride[0], pred, bs, io.best_mvx * 4, io.best_mvy * 4, cu_x, cu_y,
+        if (dir == 3 && pl == 0)
+            orc_luma_motion_comp_bi(f->ref[0], f->ref1[0], f->ref_stride[0], pred, bs, mv16, cu_x, cu_y, mnx, mny, mxx, mxy,
+                                    (uint32_t)size, (uint32_t)size);
+        else if (dir == 3)
+            orc_chroma_motion_comp_bi(f->ref[pl], f->ref1[pl], f->ref_stride[1], pred, bs, mv16, cu_x, cu_y, mnx, mny, mxx,
+                                      mxy, (uint32_t)size, (uint32_t)size);
+        else if (pl == 0)
+            orc_luma_inter_pred(lref[0], f->ref_stride[0], pred, bs, mv16[0], mv16[1], cu_x, cu_y,
                                 mnx, mny, mxx, mxy, (uint32_t)size, (uint32_t)size, 0);
         else
-            orc_chroma_motion_comp(f->ref[pl], f->ref_stride[1], pred, bs, io.best_mvx * 4, io.best_mvy * 4, cu_x, cu_y,
+            orc_chroma_motion_comp(lref[pl], f->ref_stride[1], pred, bs, mv16[0], mv16[1], cu_x, cu_y,
                                    mnx, mny, mxx, mxy, (uint32_t)size, (uint32_t)size);
         /* the CU's TUs: the CU itself up to the largest transform (64 luma, 32 chroma);
          * a 128 x 128 CU is four TUs per plane in raster order (the reference's implicit

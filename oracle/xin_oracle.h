@@ -96,6 +96,15 @@ void orc_luma_inter_pred(const opix *ref_origin, intptr_t rs, opix *pred, intptr
 void orc_chroma_motion_comp(const opix *ref_origin, intptr_t rs, opix *pred, intptr_t ps, int32_t mvx16, int32_t mvy16,
                             int32_t cu_x, int32_t cu_y, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
                             uint32_t w, uint32_t h);
+/* bi-prediction branches of Xin266LumaMotionComp / Xin266ChromaMotionComp: mv16 = L0 (x, y), L1 (x, y) in 1/16 pel */
+void orc_luma_motion_comp_bi(const opix *ref0, const opix *ref1, intptr_t rs, opix *pred, intptr_t ps, const int32_t *mv16,
+                             int32_t cu_x, int32_t cu_y, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
+                             uint32_t w, uint32_t h);
+void orc_chroma_motion_comp_bi(const opix *ref0, const opix *ref1, intptr_t rs, opix *pred, intptr_t ps, const int32_t *mv16,
+                               int32_t cu_x, int32_t cu_y, int32_t min_mvx, int32_t min_mvy, int32_t max_mvx, int32_t max_mvy,
+                               uint32_t w, uint32_t h);
+/* target of the bi refinement: clip(2 in - pred) */
+void orc_bi_me_input(const opix *in, intptr_t is, const opix *pred, intptr_t ps, opix *out, intptr_t os, uint32_t w, uint32_t h);
 
 /* ---- transforms (1-D closed, 2-D wrappers open) */
 const int16_t *orc_tr_matrix(int type, int n);   /* [n][n] row = basis function k */
@@ -209,6 +218,9 @@ typedef struct orc_frame_desc {
     int32_t tu_mode;                       /* 0 DCT2 + quant; 1 the preset-4 TU: MTS candidates with
                                               dependent quantisation (see orc_cu_hotpath) */
     const struct orc_prob *ctx;            /* tu_mode 1: the CABAC context set (ORC_NUM_CTX records) */
+    int32_t refs;                          /* 2: a second reference (list 1) and the bi search */
+    const opix *ref1[3];                   /* list 1's padded planes (strides as ref) */
+    const opix *ref1_lo[2];                /* search_mode 1: list 1's luma at 1/2 and 1/4 resolution */
 } orc_frame_desc;
 typedef struct orc_cu_out {
     int32_t mvx, mvy;                      /* quarter-pel */
@@ -221,6 +233,12 @@ typedef struct orc_cu_out {
     uint32_t ncand;                        /* luma transform candidates: 1 (64x64) or 5 */
     uint64_t nz_mts[5];                    /* luma per candidate: DCT2, then MTS index 2..5 */
     uint64_t ssd_mts[5];
+    /* refs 2: list 1's uni search, the bi pair and the choice */
+    int32_t mvx1, mvy1;
+    uint32_t cost1, int_cost1;
+    int32_t bmv[4];                        /* L0 (x, y), L1 (x, y), quarter-pel */
+    uint32_t bi_cost;
+    uint32_t inter_dir;                    /* 1 list 0, 2 list 1, 3 bi */
 } orc_cu_out;
 void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size,
                     ocoef *q[3], intptr_t q_stride[2], opix *rec[3], intptr_t rec_stride[2], orc_cu_out *out);

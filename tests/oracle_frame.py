@@ -10,7 +10,7 @@ from concurrent.futures import ThreadPoolExecutor
 import numpy as np
 
 from oracle import oracle as O
-from xin26x_gb300.frame import CU_DTYPE, MTS_DTYPE
+from xin26x_gb300.frame import BI_DTYPE, CU_DTYPE, MTS_DTYPE
 from xin26x_gb300.synth import pad_plane
 
 
@@ -28,7 +28,7 @@ def downscaled(plane, o, levels=2):
 
 
 def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=64, bitdepth=8, cus=None, threads=1,
-        search_mode=0, tu_mode=0, contexts=None):
+        search_mode=0, tu_mode=0, contexts=None, ref1=None):
     """cur, ref: (Y, U, V) planes.  levels: [(size, first, cus_x, cus_y)] as the stream reports.
     cus: optional list of global CU indices to evaluate (others left zero).
     search_mode: 0 exhaustive integer search, 1 by resolution levels (the reference
@@ -37,6 +37,8 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
     rates from contexts); the transform candidates' records are returned too.
     threads: host threads sharing the CUs (0 = every core); each CU writes only its
     own record and its own area of the level's planes, so the calls are independent.
+    ref1: list 1's planes (two references and the bi search); its records
+    (BI_DTYPE) are returned after the planes.
     Returns (cu records, q planes [levels,h,w] x3, rec planes x3)."""
     o = O.oracle(bitdepth)
     h, w = cur[0].shape
@@ -54,6 +56,13 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
     f.search_range, f.sad_lambda, f.qp, f.uv_qp, f.intra_frame = search_range, sad_lambda, qp, uv_qp, 0
     f.search_mode = search_mode
     f.tu_mode = tu_mode
+    ref1p = None
+    if ref1 is not None:
+        ref1p = [pad_plane(ref1[0], pad), pad_plane(ref1[1], pad // 2), pad_plane(ref1[2], pad // 2)]
+        f.refs = 2
+        for i in range(3):
+            pp = pad if i == 0 else pad // 2
+            f.ref1[i] = ref1p[i].ctypes.data + (pp * ref1p[i].shape[1] + pp) * ref1p[i].itemsize
     ctx = None
     if tu_mode:
         ctx = np.ascontiguousarray(contexts)
@@ -68,9 +77,16 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
             f.ref_lo_stride[l] = ref_lo[l].shape[1]
             f.in_lo[l] = in_lo[l].ctypes.data
             f.in_lo_stride[l] = in_lo[l].shape[1]
+        if ref1p is not None:
+            ref1_lo = downscaled(ref1p[0], o)
+            keep += ref1_lo
+            for l in range(2):
+                pl = pad >> (l + 1)
+                f.ref1_lo[l] = ref1_lo[l].ctypes.data + (pl * ref1_lo[l].shape[1] + pl) * ref1_lo[l].itemsize
     ncu = sum(cx * cy for (_, _, cx, cy) in levels)
     recs = np.zeros(ncu, CU_DTYPE)
     mts = np.zeros(ncu, MTS_DTYPE)
+    bis = np.zeros(ncu, BI_DTYPE)
     nl = len(levels)
     q = [np.zeros((nl, h, w), o.coef), np.zeros((nl, h // 2, w // 2), o.coef), np.zeros((nl, h // 2, w // 2), o.coef)]
     rec = [np.zeros((nl, h, w), o.pix), np.zeros((nl, h // 2, w // 2), o.pix), np.zeros((nl, h // 2, w // 2), o.pix)]
@@ -94,6 +110,11 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
         r["mvx"], r["mvy"], r["cost"], r["int_cost"] = out.mvx, out.mvy, out.cost, out.int_cost
         r["nz"] = list(out.nz)
         r["ssd"] = list(out.ssd)
+        if ref1 is not None:
+            b = bis[first + j]
+            b["mvx1"], b["mvy1"], b["cost1"], b["int_cost1"] = out.mvx1, out.mvy1, out.cost1, out.int_cost1
+            b["bmv"] = list(out.bmv)
+            b["bi_cost"], b["inter_dir"] = out.bi_cost, out.inter_dir
         if tu_mode:
             m = mts[first + j]
             m["satd_cost"], m["ncand"] = out.satd_cost, out.ncand
@@ -112,4 +133,6 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
             list(ex.map(one, work[1:]))
     if tu_mode:
         return recs, q, rec, mts
+    if ref1 is not None:
+        return recs, q, rec, bis
     return recs, q, rec

@@ -366,6 +366,56 @@ def test_frame_hier_search_matches_oracle(bd, inb, w, h, R, ctu):
         fs.close()
 
 
+@pytest.mark.parametrize("bd,inb,search_mode", [(8, 0, 0), (10, 0, 1), (10, 8, 0), (8, 0, 1)])
+@pytest.mark.parametrize("w,h,R", [(192, 128, 16), (200, 104, 24)])
+def test_frame_bi_matches_oracle(bd, inb, search_mode, w, h, R):
+    """refs 2 (two references and the bi search): picture 1 (lists 0 and 1 both
+    picture 0), pictures 2 and 3 (list 0 the previous picture, list 1 the one
+    before) and picture 8 (a graph captured for picture 2 run again): every CU's
+    list-0 and list-1 searches, bi pair, bi cost and choice, and the coded
+    prediction's coefficient and reconstructed planes, against the oracle's
+    restatement of Xin266InterBiSearch and of the bi motion compensation (pinned
+    to the reference's C)."""
+    from xin26x_gb300.frame import BI_DTYPE
+    seq = synth.sequence(w, h, 9, seed=w + h + R, bitdepth=8 if inb == 8 else bd, objects=3)
+    fs = FrameStream(w, h, search_range=R, out_q=True, out_rec=True, bitdepth=bd, input_bitdepth=inb,
+                     search_mode=search_mode, refs=2)
+    dirs = np.zeros(4, np.int64)
+    try:
+        fs.submit(*seq[0], qp=32, uv_qp=32, sad_lambda=64)
+        fs.wait()
+        for k in range(1, 9):
+            qp = 27 + (k % 3) * 5
+            lam = (40 + 10 * k) << (2 if inb == 8 else 0)
+            fs.submit(*seq[k], qp=qp, uv_qp=qp, sad_lambda=lam)
+            out = fs.wait()
+            if k not in (1, 2, 3, 8):
+                continue
+            cur, r0, r1 = seq[k], seq[k - 1], seq[max(k - 2, 0)]
+            if inb == 8:
+                cur, r0, r1 = [tuple(p.astype(np.uint16) << 2 for p in f) for f in (cur, r0, r1)]
+            want = oracle_frame.run(cur, r0, fs.levels, search_range=R, qp=qp, uv_qp=qp, sad_lambda=lam, bitdepth=bd,
+                                    threads=0, search_mode=search_mode, ref1=r1)
+            label = ("bi", bd, inb, search_mode, w, h, R, k)
+            _compare(out, want[:3], fs.levels, label)
+            got, exp = out["bi"], want[3]
+            for name in BI_DTYPE.names:
+                bad = np.nonzero(np.any((got[name] != exp[name]).reshape(len(got), -1), axis=1))[0]
+                assert bad.size == 0, (label, name, bad[:5], got[bad[:5]], exp[bad[:5]])
+            dirs += np.bincount(got["inter_dir"].astype(np.int64), minlength=4)[:4]
+    finally:
+        fs.close()
+    assert dirs[0] == 0 and dirs[3] > 0 and dirs[1] + dirs[2] > 0, dirs   # both kinds of choice occur
+
+
+def test_frame_bi_needs_tu_mode_0_and_levels_up_to_64():
+    """refs 2 is refused with the preset-4 TU stage, with the 128 x 128 level and
+    above two references."""
+    for kw in ({"tu_mode": 1, "refs": 2}, {"ctu": 128, "search_mode": 1, "levels": (128, 64), "refs": 2}, {"refs": 3}):
+        with pytest.raises(RuntimeError, match="two references need TU mode 0"):
+            FrameStream(256, 256, search_range=16, **kw)
+
+
 @pytest.mark.parametrize("bd,inb,search_mode", [(8, 0, 0), (10, 0, 1), (10, 8, 1)])
 @pytest.mark.parametrize("w,h,R", [(192, 128, 16), (200, 104, 24)])
 def test_frame_preset4_tu_matches_oracle(bd, inb, search_mode, w, h, R):

@@ -420,6 +420,58 @@ def test_motion_comp_call_sites(bd):
 
 
 @pytest.mark.parametrize("bd", BDS)
+def test_bi_motion_comp_and_target(bd):
+    """The bi-prediction branches of Xin266LumaMotionComp and Xin266ChromaMotionComp
+    (h266_inter_prediction.c:473,658; default BCW weight) and the bi search's target
+    (Xin266ConstructWeightBiMeInput, h266_construct_weight_input.c:24, at the default
+    weight 4) compiled in place, against the oracle's orc_luma_motion_comp_bi,
+    orc_chroma_motion_comp_bi and orc_bi_me_input.  MVs reach beyond the window."""
+    o, r = _pair(bd)
+    rng = np.random.default_rng(473 + bd)
+    fw, fh, ctu = 192, 128, 64
+    pad = ctu + 16
+    ref = [rng.integers(0, o.max_pix + 1, size=(fh + 2 * pad, fw + 2 * pad)).astype(o.pix) for _ in range(2)]
+    refc = [rng.integers(0, o.max_pix + 1, size=(fh // 2 + pad, fw // 2 + pad)).astype(o.pix) for _ in range(4)]
+    lo = pad * ref[0].shape[1] + pad
+    co = (pad // 2) * refc[0].shape[1] + pad // 2
+    rs, crs = ref[0].shape[1], refc[0].shape[1]
+    i32 = O.C.c_int32
+    for w, h in [(8, 8), (16, 16), (32, 32), (64, 64), (128, 128)]:
+        for trial in range(24):
+            cx = int(rng.integers(0, max(1, (fw - w) // 8 + 1))) * 8
+            cy = int(rng.integers(0, max(1, (fh - h) // 8 + 1))) * 8
+            win = [i32() for _ in range(4)]
+            o.mv_window(fw, fh, ctu, cx, cy, w, h, *[O.C.byref(v) for v in win])
+            mnx, mny, mxx, mxy = [v.value for v in win]
+            # quarter-pel MVs in 1/16 units (the frame form's), some beyond the window
+            mv = np.array([4 * int(rng.integers(4 * (mnx - 6), 4 * (mxx + 6) + 1)) if k % 2 == 0 else
+                           4 * int(rng.integers(4 * (mny - 6), 4 * (mxy + 6) + 1)) for k in range(4)], np.int32)
+            a, b = np.zeros((h, w), o.pix), np.zeros((h, w), o.pix)
+            o.luma_motion_comp_bi(O.ptr(ref[0], lo), O.ptr(ref[1], lo), rs, O.ptr(a), w, O.ptr(mv), cx, cy,
+                                  mnx, mny, mxx, mxy, w, h)
+            r.luma_motion_comp_ref(O.ptr(ref[0], lo), O.ptr(ref[1], lo), rs, O.ptr(b), w, O.ptr(mv), cx, cy,
+                                   mnx, mny, mxx, mxy, w, h)
+            assert np.array_equal(a, b), ("luma", w, h, cx, cy, list(mv))
+            cw, ch = w // 2, h // 2
+            r_u, r_v = np.zeros((ch, cw), o.pix), np.zeros((ch, cw), o.pix)
+            r.chroma_motion_comp_ref(O.ptr(refc[0], co), O.ptr(refc[1], co), O.ptr(refc[2], co), O.ptr(refc[3], co),
+                                     crs, O.ptr(r_u), O.ptr(r_v), cw, O.ptr(mv), 0, 0, 2, cx, cy, mnx, mny, mxx, mxy, w, h)
+            for pl, got in ((0, r_u), (1, r_v)):
+                want = np.zeros((ch, cw), o.pix)
+                o.chroma_motion_comp_bi(O.ptr(refc[pl], co), O.ptr(refc[2 + pl], co), crs, O.ptr(want), cw, O.ptr(mv),
+                                        cx, cy, mnx, mny, mxx, mxy, w, h)
+                assert np.array_equal(got, want), ("chroma", pl, w, h, cx, cy, list(mv))
+        cur = rng.integers(0, o.max_pix + 1, size=(h, w)).astype(o.pix)
+        pred = rng.integers(0, o.max_pix + 1, size=(h, w)).astype(o.pix)
+        pred[0, :] = 0
+        pred[1, :] = o.max_pix
+        t1, t2 = np.zeros((h, w), o.pix), np.zeros((h, w), o.pix)
+        o.bi_me_input(O.ptr(cur), w, O.ptr(pred), w, O.ptr(t1), w, w, h)
+        r.weight_bi_me_input_ref(O.ptr(cur), w, O.ptr(pred), w, O.ptr(t2), w, w, h, 4)
+        assert np.array_equal(t1, t2), ("target", w, h)
+
+
+@pytest.mark.parametrize("bd", BDS)
 def test_copy_and_pad(bd):
     """Xin266CopyAndPad / Xin266CopyAndPadUv (h266_copy_and_pad.c:32-112) compiled in
     place against the oracle: every written sample of the padded buffers."""

@@ -60,3 +60,27 @@ def test_footprint_8bit_input_into_10bit_build():
     assert fp(lib10, 8, dio=1)[1] == fp(lib10, 0, dio=1)[1]
     assert fp(lib10, 10)[0] == 0 and fp(lib10, 9)[0] == -2 and fp(lib10, 12)[0] == -2
     assert fp(lib8, 8)[0] == 0 and fp(lib8, 0)[0] == 0 and fp(lib8, 10)[0] == -2
+
+
+@pytest.mark.parametrize("bd", (8, 10))
+def test_footprint_two_references(bd):
+    """refs 2: a third picture slot with its quarter-pel planes, list 1's search keys
+    and a bi record per CU in each picture set (pinned host copies too); refused
+    with the preset-4 TU stage, the 128 x 128 level or more than two references."""
+    lib = _lib.load(bd)
+    es = 1 if bd == 8 else 2
+
+    def fp(refs, tu=0, mask=120, ctu=64, sm=0):
+        cfg = _lib.xin_gpu_stream_cfg(1920, 1080, ctu, 64, mask, 0, 1, 0, 0, sm, tu, refs)
+        d, hb = C.c_uint64(), C.c_uint64()
+        return lib.xin_gpu_stream_footprint(C.byref(cfg), C.byref(d), C.byref(hb)), d.value, hb.value
+
+    st1, d1, h1 = fp(1)
+    st2, d2, h2 = fp(2)
+    assert st1 == 0 and st2 == 0 and fp(0)[1:] == (d1, h1)
+    ysz, csz = 2304 * 1400 * es, 1152 * 700 * es
+    ncus = 30 * 16 + 60 * 33 + 120 * 67 + 240 * 135
+    assert d2 - d1 == (ysz + 2 * csz) + 16 * ysz + 8 * ncus + 2 * 40 * ncus    # xin_gpu_cu_bi: 40 bytes
+    assert h2 - h1 == 2 * 40 * ncus
+    assert fp(2, tu=1)[0] == -2 and fp(3)[0] == -2 and fp(-1)[0] == -2
+    assert fp(2, mask=248, ctu=128, sm=1)[0] == -2 and fp(1, mask=248, ctu=128, sm=1)[0] == 0

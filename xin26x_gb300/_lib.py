@@ -20,7 +20,7 @@ i32, u32, u64, ip, vp = C.c_int32, C.c_uint32, C.c_uint64, C.c_ssize_t, C.c_void
 class xin_gpu_stream_cfg(C.Structure):
     _fields_ = [("width", i32), ("height", i32), ("ctu_size", i32), ("search_range", i32),
                 ("level_mask", u32), ("out_flags", u32), ("use_graph", i32), ("device_io", i32),
-                ("input_bitdepth", i32), ("search_mode", i32), ("tu_mode", i32)]
+                ("input_bitdepth", i32), ("search_mode", i32), ("tu_mode", i32), ("refs", i32)]
 
 
 class xin_gpu_picture(C.Structure):
@@ -32,7 +32,7 @@ class xin_gpu_cu_result(C.Structure):
 
 
 class xin_gpu_results(C.Structure):
-    _fields_ = [("cu", vp), ("q", vp * 3), ("rec", vp * 3), ("gpu_ms", C.c_float), ("mts", vp)]
+    _fields_ = [("cu", vp), ("q", vp * 3), ("rec", vp * 3), ("gpu_ms", C.c_float), ("mts", vp), ("bi", vp)]
 
 
 class xin_gpu_tq_block(C.Structure):

@@ -25,23 +25,28 @@ struct xin_gpu_stream {
     int lev_on[XG_NLEV], lev_first[XG_NLEV], lev_cx[XG_NLEV], lev_cy[XG_NLEV];
     int nlev, ncus;
     size_t plane_elems, cplane_elems;
-    xg_pix *slot_base[2][3];
-    XgPlane slot[2][3];
-    xg_pix *qpel_base[2];
-    XgQpel qpel[2];
+    /* picture slots: picture k fills slot k % nslots; list 0 is the slot before it,
+     * list 1 (refs 2) the one before that */
+    int nslots;
+    xg_pix *slot_base[3][3];
+    XgPlane slot[3][3];
+    xg_pix *qpel_base[3];
+    XgQpel qpel[3];
     /* search_mode 1: luma at 1/2 and 1/4 resolution of each slot, downscaled from
      * the padded slot as a whole (the margins included) */
-    xg_pix *lo_base[2][2];
-    XgPlane lo[2][2];
+    xg_pix *lo_base[3][2];
+    XgPlane lo[3][2];
     int lo_pitch[2], lo_rows[2];
-    CUtensorMap tm_qp[2];              /* TMA map of each slot's padded luma plane: quarter-pel tiles */
+    CUtensorMap tm_qp[3];              /* TMA map of each slot's padded luma plane: quarter-pel tiles */
     long long wait_tries;  /* bound of the kernels' waits (polls) */
     unsigned long long *keys;
+    unsigned long long *keys1;         /* refs 2: list 1's integer search */
     /* what a picture in flight owns; picture k uses set k & 1 (its slot), so two
      * pictures can be in flight: one computing while the other's copies run */
     struct Set {
         xin_gpu_cu_result *dres;
         xin_gpu_cu_mts *dmts, *h_mts;    /* tu_mode 1: per-CU transform candidates */
+        xin_gpu_cu_bi *dbi, *h_bi;       /* refs 2: per-CU list-1 search, bi pair and choice */
         xg_coef *dq[3];
         xg_pix *drec[3];
         XgPicParams *dpp;
@@ -69,7 +74,7 @@ struct xin_gpu_stream {
     cudaStream_t aux[XG_NLEV - 1];   /* the tails of levels 2..5 run beside the first level's */
     cudaStream_t auxq;     /* quarter-pel planes of the new picture, beside the search (low priority) */
     cudaEvent_t ev_fork, ev_join[XG_NLEV - 1], ev_qfork, ev_qjoin;
-    cudaGraphExec_t gexec[2];
+    cudaGraphExec_t gexec[2][3];   /* by picture set and slot */
     int me_bands, me_band_rows, me_band_rows_alloc, me_row_words, me_nb;
     size_t me_smem;
     int sbd;               /* sample depth the integer search runs at (8 or 10) */
@@ -77,13 +82,13 @@ struct xin_gpu_stream {
     size_t in_es;          /* bytes per input sample */
     int nsub;              /* pictures submitted */
     int ndone;             /* pictures collected by frame_wait (the oldest first) */
-    int graph_launches[2]; /* kernels inside each captured graph */
+    int graph_launches[2][3]; /* kernels inside each captured graph */
     XgTuState *tu[2];      /* tu_mode 1: per picture set */
 };
 
 static int xg_tu_open(xin_gpu_stream *s, int set);
 static void xg_tu_free(XgTuState *u);
-static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cudaStream_t st);
+static int xg_tu_enqueue(xin_gpu_stream *s, int set, int cur, xin_gpu_stream::Set &t, cudaStream_t st);
 static uint64_t xg_tu_bytes(const xin_gpu_stream_cfg *c);
 static int16_t *xg_tu_resid(XgTuState *u, int level, int plane);
 
@@ -110,17 +115,20 @@ static int xg_stream_free(xin_gpu_stream *s)
     if (s->st) cudaStreamSynchronize(s->st);
     for (auto &t : s->set) if (t.pst) cudaStreamSynchronize(t.pst);
     if (s->cst) cudaStreamSynchronize(s->cst);
-    for (int i = 0; i < 2; i++) if (s->gexec[i]) cudaGraphExecDestroy(s->gexec[i]);
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < 2; i++)
+        for (int j = 0; j < 3; j++)
+            if (s->gexec[i][j]) cudaGraphExecDestroy(s->gexec[i][j]);
+    for (int i = 0; i < 3; i++) {
         for (int p = 0; p < 3; p++) cudaFree(s->slot_base[i][p]);
         cudaFree(s->qpel_base[i]);
         for (int l = 0; l < 2; l++) cudaFree(s->lo_base[i][l]);
     }
     cudaFree(s->keys);
+    cudaFree(s->keys1);
     xg_tu_free(s->tu[0]);
     xg_tu_free(s->tu[1]);
     for (auto &t : s->set) {
-        cudaFree(t.dres); cudaFree(t.dpp); cudaFree(t.dmts); cudaFreeHost(t.h_mts);
+        cudaFree(t.dres); cudaFree(t.dpp); cudaFree(t.dmts); cudaFreeHost(t.h_mts); cudaFree(t.dbi); cudaFreeHost(t.h_bi);
         for (int p = 0; p < 3; p++) { cudaFree(t.dq[p]); cudaFree(t.drec[p]); cudaFree(t.d_in8[p]); cudaFreeHost(t.h_in[p]); cudaFreeHost(t.h_q[p]); cudaFreeHost(t.h_rec[p]); }
         cudaFreeHost(t.h_pp); cudaFreeHost(t.h_res); cudaFreeHost(t.h_stat);
         for (int i = 0; i < 5; i++) if (t.evs[i]) cudaEventDestroy(t.evs[i]);
@@ -171,9 +179,11 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         (c.ctu_size != 64 && c.ctu_size != 128) || c.search_range < 1 || c.search_range > 256 ||
         !(c.level_mask & (8u | 16u | 32u | 64u | 128u)) || (c.level_mask & ~(8u | 16u | 32u | 64u | 128u)) ||
         !xg_input_depth_ok(c) || (c.search_mode != 0 && c.search_mode != 1) || (c.tu_mode != 0 && c.tu_mode != 1) ||
-        ((c.level_mask & 128u) && (c.ctu_size != 128 || c.search_mode != 1 || c.tu_mode != 0))) {
+        ((c.level_mask & 128u) && (c.ctu_size != 128 || c.search_mode != 1 || c.tu_mode != 0)) || c.refs < 0 || c.refs > 2 ||
+        (c.refs == 2 && (c.tu_mode != 0 || (c.level_mask & 128u)))) {
         xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range, level mask, input bit depth, search or "
-                                      "TU mode (the 128 x 128 level needs CTU 128, the search by levels and TU mode 0)");
+                                      "TU mode, or references (the 128 x 128 level needs CTU 128, the search by levels and TU "
+                                      "mode 0; two references need TU mode 0 and CU levels up to 64)");
         return XIN_GPU_ERR_ARG;
     }
     xin_gpu_stream *s = new (std::nothrow) xin_gpu_stream();
@@ -182,6 +192,7 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     s->widen = XG_BITDEPTH == 10 && c.input_bitdepth == 8;
     s->sbd = s->widen ? 8 : XG_BITDEPTH;
     s->in_es = s->widen ? 1 : sizeof(xg_pix);
+    s->nslots = c.refs == 2 ? 3 : 2;
     /* margin: the reference pads ctu + 16; the tile search also reads R + 64 + 8 around full tiles */
     int pad = c.ctu_size + 16 > c.search_range + 72 ? c.ctu_size + 16 : c.search_range + 72;
     pad = (pad + 31) & ~31;
@@ -233,7 +244,7 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     }
     size_t ysz = s->plane_elems * sizeof(xg_pix), csz = s->cplane_elems * sizeof(xg_pix);
     size_t lq = (size_t)c.width * c.height, lc = lq / 4;
-    for (int i = 0; i < 2 && e == cudaSuccess; i++) {
+    for (int i = 0; i < s->nslots && e == cudaSuccess; i++) {
         for (int p = 0; p < 3 && e == cudaSuccess; p++) e = cudaMalloc(&s->slot_base[i][p], p ? csz : ysz);
         if (e == cudaSuccess) e = cudaMalloc(&s->qpel_base[i], 16 * ysz);
         for (int l = 0; l < 2 && e == cudaSuccess && c.search_mode == 1; l++) {
@@ -243,8 +254,11 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         }
     }
     if (e == cudaSuccess) e = cudaMalloc(&s->keys, sizeof(unsigned long long) * (s->ncus > 0 ? s->ncus : 1));
+    if (e == cudaSuccess && c.refs == 2) e = cudaMalloc(&s->keys1, sizeof(unsigned long long) * (s->ncus > 0 ? s->ncus : 1));
     for (auto &t : s->set) {
         if (e == cudaSuccess) e = cudaMalloc(&t.dres, sizeof(xin_gpu_cu_result) * s->ncus);
+        if (e == cudaSuccess && c.refs == 2) e = cudaMalloc(&t.dbi, sizeof(xin_gpu_cu_bi) * s->ncus);
+        if (e == cudaSuccess && c.refs == 2 && !c.device_io) e = cudaMallocHost(&t.h_bi, sizeof(xin_gpu_cu_bi) * s->ncus);
         if (e == cudaSuccess && c.tu_mode == 1) e = cudaMalloc(&t.dmts, sizeof(xin_gpu_cu_mts) * s->ncus);
         if (e == cudaSuccess && c.tu_mode == 1 && !c.device_io) e = cudaMallocHost(&t.h_mts, sizeof(xin_gpu_cu_mts) * s->ncus);
         if (e == cudaSuccess) e = cudaMalloc(&t.dpp, sizeof(XgPicParams));
@@ -274,7 +288,7 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         xg_stream_free(s);
         return st;
     }
-    for (int i = 0; i < 2; i++) {
+    for (int i = 0; i < s->nslots; i++) {
         for (int p = 0; p < 3; p++) {
             XgPlane &pl = s->slot[i][p];
             int pd = p ? s->cpad : s->pad, pt = p ? s->cpitch : s->pitch;
@@ -365,15 +379,25 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
             l128_err = cudaFuncSetAttribute(k_hier_frame<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)xg_hier_smem(256, 128));
             if (l128_err == cudaSuccess)
-                l128_err = cudaFuncSetAttribute(k_cu_tail<128, 128, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                l128_err = cudaFuncSetAttribute(k_cu_tail<128, 128, 1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)xg_tail_smem<128, 128, 1>());
         });
         if (xg_cuda_check(l128_err, "128 x 128 level smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
     }
+    if (c.refs == 2) {
+        /* the bi search's 64 x 64 tails take more than the default 48 KB of shared memory */
+        static std::once_flag bi_once;
+        static cudaError_t bi_err = cudaSuccess;
+        std::call_once(bi_once, [] {
+            bi_err = cudaFuncSetAttribute(k_cu_tail<64, 128, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)xg_tail_smem<64, 128, 1, true>());
+        });
+        if (xg_cuda_check(bi_err, "bi tail smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
+    }
     s->wait_tries = XG_TMA_WAIT_TRIES;
     /* TMA maps of the padded luma slots for the quarter-pel tiles: the box of
      * tile (bx, by) starts at padded column XG_QP_TW bx (16-byte aligned) */
-    for (int i = 0; i < 2; i++)
+    for (int i = 0; i < s->nslots; i++)
         if (!xg_tma_map_2d(&s->tm_qp[i], s->slot_base[i][0], (int)sizeof(xg_pix), c.width + 2 * pad, c.height + 2 * pad,
                            s->pitch, XG_QP_BW, XG_QP_TH + 7)) {
             const int st = xin_gpu_last_status();
@@ -431,19 +455,20 @@ static int xg_enqueue_qpel(xin_gpu_stream *s, int cur, int *status)
     return 1;
 }
 
-/* the launches of one picture in slot `cur` against the reference in 1 - cur */
-static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool capturing)
+/* the launches of one picture of picture set `set` into slot `cur`, against the
+ * references in slots l0 (list 0) and l1 (list 1, refs 2) */
+static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l1, bool with_me, bool capturing)
 {
     const xin_gpu_stream_cfg &c = s->cfg;
-    xin_gpu_stream::Set &t = s->set[cur];
+    xin_gpu_stream::Set &t = s->set[set];
     cudaStream_t st = t.pst;
     size_t lq = (size_t)c.width * c.height, lc = lq / 4;
     int nl = 0;
     /* the previous picture (the other set, on its own stream) must have finished
      * with the planes this picture overwrites: its reference slot, quarter-pel and
      * downscaled planes, the search keys; its TU stage may still run */
-    if (capturing) cudaStreamWaitEvent(st, s->set[1 - cur].ev_main, cudaEventWaitExternal);
-    else cudaStreamWaitEvent(st, s->set[1 - cur].ev_main, 0);
+    if (capturing) cudaStreamWaitEvent(st, s->set[1 - set].ev_main, cudaEventWaitExternal);
+    else cudaStreamWaitEvent(st, s->set[1 - set].ev_main, 0);
     /* upload and pad the current picture; it becomes the next picture's reference */
     xg_stage_event(t.evs[0], st, capturing);
     /* the parameters and (8-bit input) the staged samples were uploaded on the
@@ -488,8 +513,11 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
      * tails: build them on a low-priority stream beside the search */
     cudaEventRecord(s->ev_qfork, st);
     if (with_me) {
-        int ref = 1 - cur;
-        cudaMemsetAsync(s->keys, 0xff, sizeof(unsigned long long) * s->ncus, st);
+        /* the integer search of each list: list 0 into keys, list 1 (refs 2) into keys1 */
+        for (int li = 0; li < (c.refs == 2 ? 2 : 1); li++) {
+        const int ref = li ? l1 : l0;
+        unsigned long long *keys = li ? s->keys1 : s->keys;
+        cudaMemsetAsync(keys, 0xff, sizeof(unsigned long long) * s->ncus, st);
         if (c.search_mode == 1) {
             XgHierFrameParams hp;
             memset(&hp, 0, sizeof hp);
@@ -500,7 +528,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             for (int L = 0; L < 4; L++) {
                 if (!s->lev_on[L]) continue;
                 hp.level_size[nz] = XG_LEVEL_SIZE[L];
-                hp.keys[nz] = s->keys + s->lev_first[L];
+                hp.keys[nz] = keys + s->lev_first[L];
                 hp.cus_x[nz] = s->lev_cx[L];
                 nz++;
             }
@@ -510,7 +538,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             }
             if (s->lev_on[4]) {
                 /* the 128 x 128 level: 128 x 128 tiles */
-                hp.level_size[0] = 128; hp.keys[0] = s->keys + s->lev_first[4]; hp.cus_x[0] = s->lev_cx[4];
+                hp.level_size[0] = 128; hp.keys[0] = keys + s->lev_first[4]; hp.cus_x[0] = s->lev_cx[4];
                 dim3 grd((c.width + 127) / 128, (c.height + 127) / 128, 1);
                 k_hier_frame<128><<<grd, XG_HIER_THREADS, xg_hier_smem(c.search_range, 128), st>>>(hp, t.dpp);
                 nl++;
@@ -524,7 +552,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         mp.agg_passes = s->me_nb;
         mp.key_mul = 1u << (XG_COST_FRACTION + xg_me_db(s->sbd) + (XG_BITDEPTH - s->sbd));
         for (int L = 0; L < 4; L++) {
-            mp.keys[L] = s->lev_on[L] ? s->keys + s->lev_first[L] : nullptr;
+            mp.keys[L] = s->lev_on[L] ? keys + s->lev_first[L] : nullptr;
             mp.cus_x[L] = s->lev_cx[L];
         }
         dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, s->me_bands);
@@ -535,6 +563,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             k_me_tiles<8><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, t.dpp);
         }
         nl++;
+        }
         nl += xg_enqueue_qpel(s, cur, &t.dpp->status);
         /* the search's end is recorded on a side branch joined at the picture's
          * end: a timing node between the search and the tails' fork held the tails
@@ -555,8 +584,11 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
                 nfork = li;
             }
             XgTailParams tp;
-            for (int p = 0; p < 3; p++) { tp.cur[p] = s->slot[cur][p]; tp.ref[p] = s->slot[ref][p]; }
-            tp.qpel = s->qpel[ref];
+            for (int p = 0; p < 3; p++) { tp.cur[p] = s->slot[cur][p]; tp.ref[p] = s->slot[l0][p]; tp.ref1[p] = s->slot[l1][p]; }
+            tp.qpel = s->qpel[l0];
+            tp.qpel1 = s->qpel[l1];
+            tp.keys1 = c.refs == 2 ? s->keys1 + s->lev_first[L] : nullptr;
+            tp.bi = t.dbi;
             tp.W = c.width; tp.H = c.height; tp.ctu = c.ctu_size; tp.R = c.search_range;
             tp.keys = s->keys + s->lev_first[L];
             tp.cus_x = s->lev_cx[L]; tp.first_cu = s->lev_first[L]; tp.size = XG_LEVEL_SIZE[L]; tp.level = L;
@@ -566,18 +598,30 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
             }
             tp.res = t.dres;
             for (int p = 0; p < 3; p++) tp.resid[p] = nullptr;
-            if (s->tu[cur])
-                for (int p = 0; p < 3; p++) tp.resid[p] = xg_tu_resid(s->tu[cur], L, p);
+            if (s->tu[set])
+                for (int p = 0; p < 3; p++) tp.resid[p] = xg_tu_resid(s->tu[set], L, p);
             int n = s->lev_cx[L] * s->lev_cy[L];
-            if (n > 0) {
+            if (n > 0 && c.refs == 2) {
+                switch (XG_LEVEL_SIZE[L]) {
+                case 64: k_cu_tail<64, 128, 1, true><<<n, 128, xg_tail_smem<64, 128, 1, true>(), ls>>>(tp, t.dpp, n); break;
+                case 32: k_cu_tail<32, 128, 1, true><<<n, 128, xg_tail_smem<32, 128, 1, true>(), ls>>>(tp, t.dpp, n); break;
+                case 16:
+                    k_cu_tail<16, 32, 4, true><<<(n + 3) / 4, 128, xg_tail_smem<16, 32, 4, true>(), ls>>>(tp, t.dpp, n);
+                    break;
+                default:
+                    k_cu_tail<8, 32, 4, true><<<(n + 3) / 4, 128, xg_tail_smem<8, 32, 4, true>(), ls>>>(tp, t.dpp, n);
+                    break;
+                }
+                nl++;
+            } else if (n > 0) {
                 /* 64 and 32: a 128-thread CTA per CU; 16 and 8: a warp per CU, four CUs per
                  * CTA (the fastest of the shapes measured on GB300 at 1080p) */
                 switch (XG_LEVEL_SIZE[L]) {
-                case 128: k_cu_tail<128, 128, 1><<<n, 128, xg_tail_smem<128, 128, 1>(), ls>>>(tp, t.dpp, n); break;
-                case 64: k_cu_tail<64, 128, 1><<<n, 128, xg_tail_smem<64, 128, 1>(), ls>>>(tp, t.dpp, n); break;
-                case 32: k_cu_tail<32, 128, 1><<<n, 128, xg_tail_smem<32, 128, 1>(), ls>>>(tp, t.dpp, n); break;
-                case 16: k_cu_tail<16, 32, 4><<<(n + 3) / 4, 128, xg_tail_smem<16, 32, 4>(), ls>>>(tp, t.dpp, n); break;
-                default: k_cu_tail<8, 32, 4><<<(n + 3) / 4, 128, xg_tail_smem<8, 32, 4>(), ls>>>(tp, t.dpp, n); break;
+                case 128: k_cu_tail<128, 128, 1, false><<<n, 128, xg_tail_smem<128, 128, 1>(), ls>>>(tp, t.dpp, n); break;
+                case 64: k_cu_tail<64, 128, 1, false><<<n, 128, xg_tail_smem<64, 128, 1>(), ls>>>(tp, t.dpp, n); break;
+                case 32: k_cu_tail<32, 128, 1, false><<<n, 128, xg_tail_smem<32, 128, 1>(), ls>>>(tp, t.dpp, n); break;
+                case 16: k_cu_tail<16, 32, 4, false><<<(n + 3) / 4, 128, xg_tail_smem<16, 32, 4>(), ls>>>(tp, t.dpp, n); break;
+                default: k_cu_tail<8, 32, 4, false><<<(n + 3) / 4, 128, xg_tail_smem<8, 32, 4>(), ls>>>(tp, t.dpp, n); break;
                 }
                 nl++;
             }
@@ -590,7 +634,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int cur, bool with_me, bool cap
         cudaStreamWaitEvent(st, s->ev_qjoin, 0);
         cudaStreamWaitEvent(st, s->ev_tjoin, 0);
         xg_stage_event(t.ev_main, st, capturing);
-        if (s->tu[cur]) nl += xg_tu_enqueue(s, cur, t, st);
+        if (s->tu[set]) nl += xg_tu_enqueue(s, set, cur, t, st);
         xg_stage_event(t.evs[3], st, capturing);
     } else {
         nl += xg_enqueue_qpel(s, cur, &t.dpp->status);
@@ -614,6 +658,7 @@ static void xg_enqueue_results(xin_gpu_stream *s, xin_gpu_stream::Set &t, bool w
         size_t lq = (size_t)c.width * c.height, lc = lq / 4;
         cudaMemcpyAsync(t.h_res, t.dres, sizeof(xin_gpu_cu_result) * s->ncus, cudaMemcpyDeviceToHost, s->cst);
         if (t.dmts) cudaMemcpyAsync(t.h_mts, t.dmts, sizeof(xin_gpu_cu_mts) * s->ncus, cudaMemcpyDeviceToHost, s->cst);
+        if (t.dbi) cudaMemcpyAsync(t.h_bi, t.dbi, sizeof(xin_gpu_cu_bi) * s->ncus, cudaMemcpyDeviceToHost, s->cst);
         for (int p = 0; p < 3; p++) {
             size_t n = (p ? lc : lq) * s->nlev;
             if (c.out_flags & XIN_GPU_OUT_Q) cudaMemcpyAsync(t.h_q[p], t.dq[p], n * sizeof(xg_coef), cudaMemcpyDeviceToHost, s->cst);
@@ -639,9 +684,13 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
     if (pic->qp < 0 || pic->qp > 63 || pic->uv_qp < 0 || pic->uv_qp > 63) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: QP out of range"); return XIN_GPU_ERR_ARG; }
     /* the search packs (cost << 2 | row) into 32 bits: costs must stay below 2^29 */
     if (pic->sad_lambda > (1u << 20)) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: sad_lambda above 2^20"); return XIN_GPU_ERR_ARG; }
-    const int cur = s->nsub & 1;
-    xin_gpu_stream::Set &t = s->set[cur];
-    /* set cur was last used by picture nsub - 2, already collected by frame_wait
+    /* picture set (in-flight resources) and slots: the picture's own, list 0 = the
+     * previous picture's, list 1 = the one before (the previous one again for the
+     * second picture) */
+    const int set = s->nsub & 1, ns = s->nslots;
+    const int cur = s->nsub % ns, l0 = (s->nsub + ns - 1) % ns, l1 = s->nsub >= 2 ? (s->nsub + ns - 2) % ns : l0;
+    xin_gpu_stream::Set &t = s->set[set];
+    /* set `set` was last used by picture nsub - 2, already collected by frame_wait
      * (at most two in flight), so its staging is free */
     XgPicParams pp;
     memset(&pp, 0, sizeof pp);
@@ -689,20 +738,24 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
         }
     cudaEventRecord(t.ev_up, s->ust);
     cudaStreamWaitEvent(t.pst, t.ev_up, 0);
-    if (with_me && c.use_graph) {
-        if (!s->gexec[cur]) {
+    /* a graph per (set, slot): its slots fix both references once the stream has
+     * two pictures behind it (before that, with two references, the launches run
+     * directly) */
+    if (with_me && c.use_graph && (c.refs != 2 || s->nsub >= 2)) {
+        cudaGraphExec_t &gx = s->gexec[set][cur];
+        if (!gx) {
             cudaGraph_t g;
             if (xg_cuda_check(cudaStreamBeginCapture(t.pst, cudaStreamCaptureModeThreadLocal), "begin capture")) return XIN_GPU_ERR_CUDA;
-            s->graph_launches[cur] = xg_enqueue_picture(s, cur, true, true);
+            s->graph_launches[set][cur] = xg_enqueue_picture(s, set, cur, l0, l1, true, true);
             if (xg_cuda_check(cudaStreamEndCapture(t.pst, &g), "end capture")) return XIN_GPU_ERR_CUDA;
-            cudaError_t e = cudaGraphInstantiate(&s->gexec[cur], g, cudaGraphInstantiateFlagUseNodePriority);
+            cudaError_t e = cudaGraphInstantiate(&gx, g, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(g);
             if (xg_cuda_check(e, "graph instantiate")) return XIN_GPU_ERR_CUDA;
         }
-        if (xg_cuda_check(cudaGraphLaunch(s->gexec[cur], t.pst), "graph launch")) return XIN_GPU_ERR_CUDA;
-        xg_count_launch((uint64_t)s->graph_launches[cur]);
+        if (xg_cuda_check(cudaGraphLaunch(gx, t.pst), "graph launch")) return XIN_GPU_ERR_CUDA;
+        xg_count_launch((uint64_t)s->graph_launches[set][cur]);
     } else {
-        xg_count_launch((uint64_t)xg_enqueue_picture(s, cur, with_me, false));
+        xg_count_launch((uint64_t)xg_enqueue_picture(s, set, cur, l0, l1, with_me, false));
     }
     xg_enqueue_results(s, t, with_me);
     if (xg_cuda_check(cudaGetLastError(), "frame_submit")) return XIN_GPU_ERR_CUDA;
@@ -750,6 +803,10 @@ extern "C" int xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32
         if (res->mts) memcpy(res->mts, t.h_mts, sizeof(xin_gpu_cu_mts) * s->ncus);
         else res->mts = t.h_mts;
     }
+    if (t.h_bi) {
+        if (res->bi) memcpy(res->bi, t.h_bi, sizeof(xin_gpu_cu_bi) * s->ncus);
+        else res->bi = t.h_bi;
+    }
     for (int p = 0; p < 3; p++) {
         size_t n = (p ? lc : lq) * s->nlev;
         if (c.out_flags & XIN_GPU_OUT_Q) {
@@ -772,7 +829,8 @@ extern "C" int xin_gpu_stream_set_wait_tries(xin_gpu_stream *s, int64_t tries)
     s->wait_tries = tries < 0 ? XG_TMA_WAIT_TRIES : tries;
     /* the bound is a parameter of the captured graphs: capture them again */
     for (int i = 0; i < 2; i++)
-        if (s->gexec[i]) { cudaGraphExecDestroy(s->gexec[i]); s->gexec[i] = nullptr; }
+        for (int j = 0; j < 3; j++)
+            if (s->gexec[i][j]) { cudaGraphExecDestroy(s->gexec[i][j]); s->gexec[i][j] = nullptr; }
     return XIN_GPU_OK;
 }
 

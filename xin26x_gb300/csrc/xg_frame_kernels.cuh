@@ -752,6 +752,12 @@ struct XgTailParams {
     xin_gpu_cu_result *res;           /* all CUs */
     int16_t *resid[3];                /* set (the preset-4 TU stage follows): write the residual
                                          planes (picture layout) instead of transforming */
+    /* refs 2: list 1 (its planes, quarter-pel planes and integer search) and the
+     * bi records (all CUs) */
+    XgPlane ref1[3];
+    XgQpel qpel1;
+    const unsigned long long *keys1;
+    xin_gpu_cu_bi *bi;
 };
 
 /* synchronisation of the NT threads that work on one CU (group g of a CTA
@@ -946,68 +952,69 @@ struct XgTailSmem {
     XgTqSmem<xg_tu_luma(S)> tl;
     XgTqSmem<xg_tu_chroma(S)> tc;
     xg_pix pred[S * S];
-    uint32_t part[8][NT / 32];
-    int bmv[3];
+    uint32_t part[9][NT / 32];
     unsigned long long nz[3], ssd[3];
+};
+/* refs 2: each list's luma prediction and the bi search's target */
+template <int S>
+struct XgTailBiSmem {
+    alignas(16) xg_pix bp[2][S * S];
+    alignas(16) xg_pix tgt[S * S];
 };
 
 /* CPB CUs of size S (luma S x S, chroma S/2 x S/2) per CTA, NT threads per CU
  * (NT = 32: one warp per CU, warp-synchronous) */
 /* CTAs per SM the register allocation must allow: 64 x 64 CUs are held to five by
- * shared memory anyway, the other sizes keep eight 128-thread CTAs (64 registers) */
-__host__ __device__ constexpr int xg_tail_min_ctas(int s) { return s == 128 ? 2 : s == 64 ? 5 : 8; }
-/* shared memory (dynamic) of a launch */
-template <int S, int NT, int CPB>
-__host__ __device__ constexpr size_t xg_tail_smem() { return sizeof(XgTailSmem<S, NT>) * CPB; }
-template <int S, int NT, int CPB>
-__global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTailParams p, const XgPicParams *pp, int ncu)
+ * shared memory anyway, the other sizes keep eight 128-thread CTAs (64 registers);
+ * the bi search's kernels hold twice the shared state */
+__host__ __device__ constexpr int xg_tail_min_ctas(int s, bool bi = false)
 {
-    constexpr int C = S / 2, TL = xg_tu_luma(S), TC = xg_tu_chroma(S);
-    extern __shared__ __align__(16) unsigned char xg_tail_raw[];
-    XgTailSmem<S, NT> *shm = reinterpret_cast<XgTailSmem<S, NT> *>(xg_tail_raw);
-    const int g = threadIdx.x / NT, tid = threadIdx.x % NT;
-    const int cu = blockIdx.x * CPB + g;
-    if (cu >= ncu) return;          /* whole groups only: no barrier is shared with a missing group */
-    XgTailSmem<S, NT> &m = shm[g];
-    XgTqSmem<TL> &tl = m.tl;
-    XgTqSmem<TC> &tc = m.tc;
-    xg_pix *pred = m.pred;
-    const int cx = (cu % p.cus_x) * S, cy = (cu / p.cus_x) * S;
-    const int lane = tid & 31, warp = tid >> 5;
-    const unsigned long long key = p.keys[cu];
-    const int nx = 2 * p.R + 1;
-    const int gidx = (int)(uint32_t)key;
-    const int imx = gidx % nx - p.R, imy = gidx / nx - p.R;
-    if (tid < 3) { m.nz[tid] = 0; m.ssd[tid] = 0; }
-    {   /* DCT2 matrices of the luma and chroma TUs, rows k < 32 */
-        constexpr int lgl = TL == 8 ? 3 : TL == 16 ? 4 : TL == 32 ? 5 : 6, lgc = TC == 4 ? 2 : TC == 8 ? 3 : TC == 16 ? 4 : 5;
-        const int16_t *ml = xg_mat(0, lgl), *mc = xg_mat(0, lgc);
-        xg_tq_load_mat<TL, NT>(tl, ml, tid);
-        xg_tq_load_mat<TC, NT>(tc, mc, tid);
-    }
+    return bi ? (s == 64 ? 2 : 4) : s == 128 ? 2 : s == 64 ? 5 : 8;
+}
+/* shared memory (dynamic) of a launch */
+template <int S, int NT, int CPB, bool BI = false>
+__host__ __device__ constexpr size_t xg_tail_smem()
+{
+    return (sizeof(XgTailSmem<S, NT>) + (BI ? sizeof(XgTailBiSmem<S>) : 0)) * CPB;
+}
 
-    /* window (h266_enc_init.c:1462) */
-    const int mnx = (int16_t)(-cx - p.ctu - 8), mny = (int16_t)(-cy - p.ctu - 8);
-    const int mxx = (int16_t)(p.W + (p.ctu - S + 8) - cx), mxy = (int16_t)(p.H + (p.ctu - S + 8) - cy);
+/* the sum of every thread's v over the NT threads of group g (all threads get it) */
+template <int NT, int CPB>
+__device__ __forceinline__ uint32_t xg_group_sum(uint32_t v, uint32_t *part, int g, int tid)
+{
+    v = __reduce_add_sync(0xffffffffu, v);
+    if (NT == 32) return v;
+    if ((tid & 31) == 0) part[tid >> 5] = v;
+    xg_gsync<NT, CPB>(g);
+    uint32_t t = 0;
+#pragma unroll
+    for (int w = 0; w < NT / 32; w++) t += part[w];
+    xg_gsync<NT, CPB>(g);
+    return t;
+}
 
-    /* ---- Xin266FullSubPelMe on the quarter-pel planes (h266_sub_pel_refine.c:81-212) */
+/* Xin266FullSubPelMe on the quarter-pel planes (h266_sub_pel_refine.c:81-212) by
+ * the NT threads of group g: org (pitch op) against the planes of qp from
+ * (bx, by) (quarter-pel) with cost bc: two steps of eight neighbours in the
+ * reference's fixed order, strict '<'.  The caller checks that the integer
+ * start lies in the window (:117-120). */
+template <int S, int NT, int CPB>
+__device__ void xg_subpel(const xg_pix *org, intptr_t op, const XgQpel &qp, int cx, int cy, uint32_t lambda,
+                          uint32_t (*part)[NT / 32], int g, int tid, int &bx, int &by, uint32_t &bc)
+{
     /* candidate c of a step: (offx(c), offy(c)) * step, the fixed order of the
      * reference's eight neighbours; offsets + 1 packed two bits per candidate */
     auto offx = [](int c) { return (int)((0x8858u >> (2 * c)) & 3u) - 1; };   /* -1, 1, 0, 0, -1, 1, -1, 1 */
     auto offy = [](int c) { return (int)((0xA085u >> (2 * c)) & 3u) - 1; };   /*  0, 0, -1, 1, -1, -1, 1, 1 */
-    const xg_pix *org = p.cur[0].data + (intptr_t)cy * p.cur[0].pitch + cx;
-    const intptr_t qpitch = p.qpel.pitch;                /* plane[0] is the reference slot, same pitch */
-    int bx = 4 * imx, by = 4 * imy;
-    uint32_t bc = (uint32_t)(key >> 32);
-    /* the search runs only when the integer start lies in the window (h266_sub_pel_refine.c:117-120) */
-    const bool start_in = imx >= mnx && imy >= mny && imx <= mxx && imy <= mxy;
-    for (int step = 2; step >= 1 && start_in; step--) {
+    const int lane = tid & 31, warp = tid >> 5;
+    const intptr_t qpitch = qp.pitch;
+    for (int step = 2; step >= 1; step--) {
         const int bx0 = bx, by0 = by;
         const xg_pix *cb[8];                              /* candidate blocks (top-left sample) */
 #pragma unroll
         for (int c = 0; c < 8; c++) {
             const int tx = bx0 + offx(c) * step, ty = by0 + offy(c) * step;
-            cb[c] = p.qpel.plane[(ty & 3) * 4 + (tx & 3)] + (intptr_t)(cy + (ty >> 2)) * qpitch + cx + (tx >> 2);
+            cb[c] = qp.plane[(ty & 3) * 4 + (tx & 3)] + (intptr_t)(cy + (ty >> 2)) * qpitch + cx + (tx >> 2);
         }
         uint32_t acc[8];
 #pragma unroll
@@ -1016,7 +1023,7 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
 #pragma unroll 2
         for (int i = tid; i < S * S; i += NT) {
             const int x = i % S, y = i / S;
-            const unsigned o = org[(intptr_t)y * p.cur[0].pitch + x];
+            const unsigned o = org[(intptr_t)y * op + x];
             const intptr_t off = (intptr_t)y * qpitch + x;
 #pragma unroll
             for (int c = 0; c < 8; c++) acc[c] = __usad(o, (unsigned)cb[c][off], acc[c]);
@@ -1043,18 +1050,18 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
         sad += __shfl_xor_sync(0xffffffffu, sad, 1);
         const int c = lane >> 2;
         if (NT > 32) {                                   /* the group's warps: sums through shared memory */
-            if ((lane & 3) == 0) m.part[c][warp] = sad;
+            if ((lane & 3) == 0) part[c][warp] = sad;
             xg_gsync<NT, CPB>(g);
             uint32_t t = 0;
 #pragma unroll
-            for (int w = 0; w < NT / 32; w++) t += m.part[c][w];
+            for (int w = 0; w < NT / 32; w++) t += part[c][w];
             sad = t;
             xg_gsync<NT, CPB>(g);
         }
         /* strict '<' in the fixed candidate order (h266_sub_pel_refine.c:146-160):
          * the earliest candidate of the smallest cost, taken if below the best so far */
         const int tx = bx0 + offx(c) * step, ty = by0 + offy(c) * step;
-        uint32_t cost = (sad << XG_COST_FRACTION) + (xg_mvd_bits(tx) + xg_mvd_bits(ty)) * pp->lambda;
+        uint32_t cost = (sad << XG_COST_FRACTION) + (xg_mvd_bits(tx) + xg_mvd_bits(ty)) * lambda;
         int cc = c;
 #pragma unroll
         for (int o = 4; o < 32; o <<= 1) {
@@ -1064,18 +1071,234 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
         }
         if (cost < bc) { bc = cost; bx = bx0 + offx(cc) * step; by = by0 + offy(cc) * step; }
     }
-    const int mvx = bx, mvy = by;
+}
 
-    /* ---- luma MC (Xin266LumaInterPred: clamp to the window in 1/16 pel) */
-    {
-        int m16x = min(max(mvx * 4, mnx * 16), mxx * 16), m16y = min(max(mvy * 4, mny * 16), mxy * 16);
-        int ox = cx * 16 + m16x, oy = cy * 16 + m16y;
-        int q = ((oy & 15) >> 2) * 4 + ((ox & 15) >> 2);
-        const xg_pix *pl = q ? p.qpel.plane[q] : p.ref[0].data;
+/* luma uni prediction of Xin266LumaInterPred (h266_inter_prediction.c:302-351):
+ * the quarter-pel MV clamped to the window in 1/16 pel, read from the
+ * quarter-pel plane of its phase (plane 0 is the reference itself) */
+template <int S, int NT>
+__device__ __forceinline__ void xg_luma_uni(const XgQpel &qp, int cx, int cy, int mvx, int mvy, int mnx, int mny, int mxx,
+                                            int mxy, xg_pix *dst, int tid)
+{
+    const int m16x = min(max(mvx * 4, mnx * 16), mxx * 16), m16y = min(max(mvy * 4, mny * 16), mxy * 16);
+    const int ox = cx * 16 + m16x, oy = cy * 16 + m16y;
+    const xg_pix *pl = qp.plane[((oy & 15) >> 2) * 4 + ((ox & 15) >> 2)];
+    for (int i = tid; i < S * S; i += NT) {
+        const int x = i % S, y = i / S;
+        dst[i] = pl[(intptr_t)((oy >> 4) + y) * qp.pitch + (ox >> 4) + x];
+    }
+}
+
+/* the 14-bit intermediate of sample (x, y) of a block at 1/16-pel luma position
+ * (ox, oy) in plane rp: pfXinLumaInterpS16 by phase (copy, H, V, HV; default
+ * filter), and the same for chroma at 1/32 pel (pfXinChromaInterpS16) */
+__device__ __forceinline__ int xg_luma_s16(const XgPlane &rp, int ox, int oy, int x, int y)
+{
+    const int fx = ox & 15, fy = oy & 15;
+    const xg_pix *sp = rp.data + (intptr_t)((oy >> 4) + y) * rp.pitch + (ox >> 4) + x;
+    if (!fx && !fy) return ((int)sp[0] << XG_IF_HEAD) - XG_IF_OFF14;
+    const int8_t *th = c_luma_taps[0][fx], *tv = c_luma_taps[0][fy];
+    if (!fy) return xg_if_to_s16<8>(sp, 1, th);
+    if (!fx) return xg_if_to_s16<8>(sp, rp.pitch, tv);
+    return xg_if_hv<8, true>(sp, rp.pitch, th, tv);
+}
+__device__ __forceinline__ int xg_chroma_s16(const XgPlane &rp, int ox, int oy, int x, int y)
+{
+    const int fx = ox & 31, fy = oy & 31;
+    const xg_pix *sp = rp.data + (intptr_t)((oy >> 5) + y) * rp.pitch + (ox >> 5) + x;
+    if (!fx && !fy) return ((int)sp[0] << XG_IF_HEAD) - XG_IF_OFF14;
+    const int8_t *th = c_chroma_taps[fx], *tv = c_chroma_taps[fy];
+    if (!fy) return xg_if_to_s16<4>(sp, 1, th);
+    if (!fx) return xg_if_to_s16<4>(sp, rp.pitch, tv);
+    return xg_if_hv<4, true>(sp, rp.pitch, th, tv);
+}
+/* Xin266InterpAvgS16U8 (h266_luma_mc.c:561): clip((a + b + 2^head + 2 * 8192) >> (head + 1)) */
+__device__ __forceinline__ xg_pix xg_bi_avg(int a, int b)
+{
+    return (xg_pix)xg_clip_pix((a + b + (1 << XG_IF_HEAD) + 2 * XG_IF_OFF14) >> (XG_IF_HEAD + 1));
+}
+
+/* The bi search's integer step: the reference runs the closed Xin26xMotionEstBbdgs
+ * with searchWidth = searchHeight = 4 around the list's uni MV
+ * (h266_analyze_inter_cu.c:607-608,665-677); here every integer MV of the +-4
+ * square around (ccx, ccy) inside the window, raster order, strict '<' from
+ * UINT32_MAX, cost (SAD << 8) + bits(mv) * lambda with predictor 0, on the target
+ * t (pitch S) against the list's luma plane rp.  A candidate row is one pass:
+ * nine SADs a thread, summed over the group.  Leaves (bx, by, bc) = (0, 0,
+ * UINT32_MAX) when no candidate lies in the window. */
+template <int S, int NT, int CPB>
+__device__ void xg_bi_square(const xg_pix *t, const XgPlane &rp, int cx, int cy, int ccx, int ccy, int mnx, int mny, int mxx,
+                             int mxy, uint32_t lambda, uint32_t (*part)[NT / 32], int g, int tid, int &bx, int &by, uint32_t &bc)
+{
+    const int lane = tid & 31, warp = tid >> 5;
+    bx = 0; by = 0; bc = 0xFFFFFFFFu;
+    for (int dy = -4; dy <= 4; dy++) {
+        const int my = ccy + dy;
+        if (my < mny || my > mxy) continue;               /* uniform over the group */
+        uint32_t acc[9];
+#pragma unroll
+        for (int k = 0; k < 9; k++) acc[k] = 0;
+        /* the nine candidates of the row: columns ccx - 4 .. ccx + 4 (within the
+         * reference's padding also where they leave the window) */
+        const xg_pix *row = rp.data + (intptr_t)(cy + my) * rp.pitch + cx + ccx - 4;
         for (int i = tid; i < S * S; i += NT) {
-            int x = i % S, y = i / S;
-            pred[i] = pl[(intptr_t)((oy >> 4) + y) * p.qpel.pitch + (ox >> 4) + x];
+            const int x = i % S, y = i / S;
+            const unsigned o = t[y * S + x];
+            const xg_pix *r = row + (intptr_t)y * rp.pitch + x;
+#pragma unroll
+            for (int k = 0; k < 9; k++) acc[k] = __usad(o, (unsigned)r[k], acc[k]);
         }
+#pragma unroll
+        for (int k = 0; k < 9; k++) acc[k] = __reduce_add_sync(0xffffffffu, acc[k]);
+        if (NT > 32) {
+            if (lane == 0)
+#pragma unroll
+                for (int k = 0; k < 9; k++) part[k][warp] = acc[k];
+            xg_gsync<NT, CPB>(g);
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                uint32_t s = 0;
+#pragma unroll
+                for (int w = 0; w < NT / 32; w++) s += part[k][w];
+                acc[k] = s;
+            }
+            xg_gsync<NT, CPB>(g);
+        }
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            const int mx = ccx + k - 4;
+            if (mx < mnx || mx > mxx) continue;
+            const uint32_t c = (acc[k] << XG_COST_FRACTION) + (xg_mvd_bits(4 * mx) + xg_mvd_bits(4 * my)) * lambda;
+            if (c < bc) { bc = c; bx = 4 * mx; by = 4 * my; }
+        }
+    }
+}
+
+/* SAD of org against the average of the two luma predictions (pfXinComputeAvgDist:
+ * |o - ((a + b + 1) >> 1)|), summed over the group */
+template <int S, int NT, int CPB>
+__device__ __forceinline__ uint32_t xg_avg_sad(const xg_pix *org, intptr_t op, const xg_pix *a, const xg_pix *b,
+                                               uint32_t (*part)[NT / 32], int g, int tid)
+{
+    uint32_t s = 0;
+    for (int i = tid; i < S * S; i += NT) {
+        const int x = i % S, y = i / S;
+        s = __usad((unsigned)org[(intptr_t)y * op + x], ((unsigned)a[i] + (unsigned)b[i] + 1u) >> 1, s);
+    }
+    return xg_group_sum<NT, CPB>(s, part[0], g, tid);
+}
+
+template <int S, int NT, int CPB, bool BI>
+__global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, BI)) k_cu_tail(XgTailParams p, const XgPicParams *pp, int ncu)
+{
+    constexpr int C = S / 2, TL = xg_tu_luma(S), TC = xg_tu_chroma(S);
+    extern __shared__ __align__(16) unsigned char xg_tail_raw[];
+    XgTailSmem<S, NT> *shm = reinterpret_cast<XgTailSmem<S, NT> *>(xg_tail_raw);
+    const int g = threadIdx.x / NT, tid = threadIdx.x % NT;
+    const int cu = blockIdx.x * CPB + g;
+    if (cu >= ncu) return;          /* whole groups only: no barrier is shared with a missing group */
+    XgTailSmem<S, NT> &m = shm[g];
+    XgTqSmem<TL> &tl = m.tl;
+    XgTqSmem<TC> &tc = m.tc;
+    xg_pix *pred = m.pred;
+    const int cx = (cu % p.cus_x) * S, cy = (cu / p.cus_x) * S;
+    const unsigned long long key = p.keys[cu];
+    const int nx = 2 * p.R + 1;
+    const uint32_t lambda = pp->lambda;
+    if (tid < 3) { m.nz[tid] = 0; m.ssd[tid] = 0; }
+    {   /* DCT2 matrices of the luma and chroma TUs, rows k < 32 */
+        constexpr int lgl = TL == 8 ? 3 : TL == 16 ? 4 : TL == 32 ? 5 : 6, lgc = TC == 4 ? 2 : TC == 8 ? 3 : TC == 16 ? 4 : 5;
+        const int16_t *ml = xg_mat(0, lgl), *mc = xg_mat(0, lgc);
+        xg_tq_load_mat<TL, NT>(tl, ml, tid);
+        xg_tq_load_mat<TC, NT>(tc, mc, tid);
+    }
+
+    /* window (h266_enc_init.c:1462) */
+    const int mnx = (int16_t)(-cx - p.ctu - 8), mny = (int16_t)(-cy - p.ctu - 8);
+    const int mxx = (int16_t)(p.W + (p.ctu - S + 8) - cx), mxy = (int16_t)(p.H + (p.ctu - S + 8) - cy);
+    auto in_window = [&](int qx, int qy) { return (qx >> 2) >= mnx && (qy >> 2) >= mny && (qx >> 2) <= mxx && (qy >> 2) <= mxy; };
+
+    /* ---- list 0: Xin266FullSubPelMe from the integer search's best, when its
+     * integer MV lies in the window (h266_sub_pel_refine.c:117-120) */
+    const xg_pix *org = p.cur[0].data + (intptr_t)cy * p.cur[0].pitch + cx;
+    const intptr_t opitch = p.cur[0].pitch;
+    int mvx, mvy;
+    uint32_t bc = (uint32_t)(key >> 32);
+    {
+        const int gidx = (int)(uint32_t)key;
+        mvx = 4 * (gidx % nx - p.R); mvy = 4 * (gidx / nx - p.R);
+        if (in_window(mvx, mvy)) xg_subpel<S, NT, CPB>(org, opitch, p.qpel, cx, cy, lambda, m.part, g, tid, mvx, mvy, bc);
+    }
+
+    /* the prediction coded: list 0, or (refs 2) the lowest of list 0, list 1 and the pair */
+    int dir = 1;
+    int mv1x = 0, mv1y = 0, bmv[2][2] = { { mvx, mvy }, { 0, 0 } };
+    uint32_t bc1 = 0, bi_cost = 0;
+    if constexpr (BI) {
+        XgTailBiSmem<S> &bs = reinterpret_cast<XgTailBiSmem<S> *>(xg_tail_raw + sizeof(XgTailSmem<S, NT>) * CPB)[g];
+        const unsigned long long key1 = p.keys1[cu];
+        bc1 = (uint32_t)(key1 >> 32);
+        {
+            const int gidx = (int)(uint32_t)key1;
+            mv1x = 4 * (gidx % nx - p.R); mv1y = 4 * (gidx / nx - p.R);
+            if (in_window(mv1x, mv1y))
+                xg_subpel<S, NT, CPB>(org, opitch, p.qpel1, cx, cy, lambda, m.part, g, tid, mv1x, mv1y, bc1);
+        }
+        /* Xin266InterBiSearch (h266_analyze_inter_cu.c:507-870; one reference per list,
+         * default BCW weight, two iterations, predictor 0): the list with the larger uni
+         * cost is refined first against clip(2 org - the other list's prediction), from
+         * the integer part of its uni MV: integer step, then Xin266FullSubPelMe; the pair
+         * is costed by the SAD against the average of the two predictions and kept when
+         * it improves; the final cost is taken on the last predictions (:815-852) */
+        const int uni[2][2] = { { mvx, mvy }, { mv1x, mv1y } };
+        bmv[1][0] = mv1x; bmv[1][1] = mv1y;
+        xg_luma_uni<S, NT>(p.qpel, cx, cy, mvx, mvy, mnx, mny, mxx, mxy, bs.bp[0], tid);
+        xg_luma_uni<S, NT>(p.qpel1, cx, cy, mv1x, mv1y, mnx, mny, mxx, mxy, bs.bp[1], tid);
+        xg_gsync<NT, CPB>(g);
+        int li = bc <= bc1 ? 1 : 0;
+        uint32_t best = 0xFFFFFFFFu;
+        for (int it = 0; it < 2; it++, li ^= 1) {
+            const xg_pix *other = bs.bp[1 - li];
+            for (int i = tid; i < S * S; i += NT) {
+                const int x = i % S, y = i / S;
+                bs.tgt[i] = (xg_pix)xg_clip_pix(2 * (int)org[(intptr_t)y * opitch + x] - (int)other[i]);
+            }
+            xg_gsync<NT, CPB>(g);
+            int ix, iy;
+            uint32_t ic;
+            xg_bi_square<S, NT, CPB>(bs.tgt, li ? p.ref1[0] : p.ref[0], cx, cy, uni[li][0] >> 2, uni[li][1] >> 2, mnx, mny, mxx,
+                                     mxy, lambda, m.part, g, tid, ix, iy, ic);
+            if (in_window(ix, iy))
+                xg_subpel<S, NT, CPB>(bs.tgt, S, li ? p.qpel1 : p.qpel, cx, cy, lambda, m.part, g, tid, ix, iy, ic);
+            xg_luma_uni<S, NT>(li ? p.qpel1 : p.qpel, cx, cy, ix, iy, mnx, mny, mxx, mxy, bs.bp[li], tid);
+            xg_gsync<NT, CPB>(g);
+            const uint32_t sad = xg_avg_sad<S, NT, CPB>(org, opitch, bs.bp[0], bs.bp[1], m.part, g, tid);
+            const uint32_t c = (sad << XG_COST_FRACTION) + (xg_mvd_bits(ix) + xg_mvd_bits(iy) + xg_mvd_bits(bmv[1 - li][0]) +
+                                                            xg_mvd_bits(bmv[1 - li][1])) * lambda;
+            if (c < best) { best = c; bmv[li][0] = ix; bmv[li][1] = iy; }
+        }
+        const uint32_t sad = xg_avg_sad<S, NT, CPB>(org, opitch, bs.bp[0], bs.bp[1], m.part, g, tid);
+        bi_cost = (sad << XG_COST_FRACTION) +
+                  (xg_mvd_bits(bmv[0][0]) + xg_mvd_bits(bmv[0][1]) + xg_mvd_bits(bmv[1][0]) + xg_mvd_bits(bmv[1][1])) * lambda;
+        uint32_t ubest = bc;
+        if (bc1 < ubest) { ubest = bc1; dir = 2; }
+        if (bi_cost < ubest) dir = 3;
+    }
+    /* the coded MV of each list (1/16 pel, clamped to the window as the motion
+     * compensation does) */
+    const int c0x = dir == 3 ? bmv[0][0] : dir == 2 ? mv1x : mvx, c0y = dir == 3 ? bmv[0][1] : dir == 2 ? mv1y : mvy;
+    const int c1x = bmv[1][0], c1y = bmv[1][1];
+
+    /* ---- luma MC: Xin266LumaInterPred (uni) or the bi branch of Xin266LumaMotionComp */
+    if (BI && dir == 3) {
+        const int o0x = cx * 16 + min(max(c0x * 4, mnx * 16), mxx * 16), o0y = cy * 16 + min(max(c0y * 4, mny * 16), mxy * 16);
+        const int o1x = cx * 16 + min(max(c1x * 4, mnx * 16), mxx * 16), o1y = cy * 16 + min(max(c1y * 4, mny * 16), mxy * 16);
+        for (int i = tid; i < S * S; i += NT) {
+            const int x = i % S, y = i / S;
+            pred[i] = xg_bi_avg(xg_luma_s16(p.ref[0], o0x, o0y, x, y), xg_luma_s16(p.ref1[0], o1x, o1y, x, y));
+        }
+    } else {
+        xg_luma_uni<S, NT>(BI && dir == 2 ? p.qpel1 : p.qpel, cx, cy, c0x, c0y, mnx, mny, mxx, mxy, pred, tid);
     }
     xg_gsync<NT, CPB>(g);
 
@@ -1087,7 +1310,7 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
     if (resid_only) {
         for (int i = tid; i < S * S; i += NT) {
             int y = i / S, x = i % S;
-            p.resid[0][(intptr_t)(cy + y) * p.W + cx + x] = (int16_t)((int)org[(intptr_t)y * p.cur[0].pitch + x] - (int)pred[i]);
+            p.resid[0][(intptr_t)(cy + y) * p.W + cx + x] = (int16_t)((int)org[(intptr_t)y * opitch + x] - (int)pred[i]);
         }
         xg_gsync<NT, CPB>(g);
     } else {
@@ -1095,37 +1318,45 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
             const int ox = (tu % (S / TL)) * TL, oy = (tu / (S / TL)) * TL;
             for (int i = tid; i < TL * TL; i += NT) {
                 int y = i / TL, x = i % TL;
-                tl.res[xg_d2<TL>(y, x)] = (int16_t)((int)org[(intptr_t)(oy + y) * p.cur[0].pitch + ox + x] -
+                tl.res[xg_d2<TL>(y, x)] = (int16_t)((int)org[(intptr_t)(oy + y) * opitch + ox + x] -
                                                     (int)pred[(oy + y) * S + ox + x]);
             }
             xg_gsync<NT, CPB>(g);
             xg_tq<TL, NT, CPB>(tl, pp->quant[p.level][0], lgS + XG_BITDEPTH + 6 - 15, lgS + 6, &m.nz[0],
                                p.q[0] + (intptr_t)(cy + oy) * p.W + cx + ox, p.W, tid, g);
-            xg_itq<TL, NT, CPB>(tl, pred + oy * S + ox, S, org + (intptr_t)oy * p.cur[0].pitch + ox, p.cur[0].pitch,
+            xg_itq<TL, NT, CPB>(tl, pred + oy * S + ox, S, org + (intptr_t)oy * opitch + ox, opitch,
                                 p.rec[0] + (intptr_t)(cy + oy) * p.W + cx + ox, p.W, &m.ssd[0], tid, g);
         }
     }
 
-    /* ---- chroma: uni branch of Xin266ChromaMotionComp (1/32 phase, mask 31), TQ, reconstruction */
+    /* ---- chroma: Xin266ChromaMotionComp (uni branch: 1/32 phase, mask 31; or the bi
+     * branch), TQ, reconstruction */
     {
         const int lgC = TC == 4 ? 2 : TC == 8 ? 3 : TC == 16 ? 4 : 5;
-        int m16x = min(max(mvx * 4, mnx * 16), mxx * 16), m16y = min(max(mvy * 4, mny * 16), mxy * 16);
-        int ox = cx * 16 + m16x, oy = cy * 16 + m16y;
-        int fx = ox & 31, fy = oy & 31;
+        const int ox = cx * 16 + min(max(c0x * 4, mnx * 16), mxx * 16), oy = cy * 16 + min(max(c0y * 4, mny * 16), mxy * 16);
+        const int o1x = cx * 16 + min(max(c1x * 4, mnx * 16), mxx * 16), o1y = cy * 16 + min(max(c1y * 4, mny * 16), mxy * 16);
+        const int fx = ox & 31, fy = oy & 31;
         const int8_t *th = c_chroma_taps[fx], *tv = c_chroma_taps[fy];
         const int W2 = p.W >> 1;
         for (int pl = 1; pl <= 2; pl++) {
-            const XgPlane &rp = p.ref[pl];
-            const xg_pix *src = rp.data + (intptr_t)(oy >> 5) * rp.pitch + (ox >> 5);
-            for (int i = tid; i < C * C; i += NT) {
-                int x = i % C, y = i / C;
-                const xg_pix *sp = src + (intptr_t)y * rp.pitch + x;
-                int v;
-                if (!fx && !fy) v = sp[0];
-                else if (fx && !fy) v = xg_if_pix<4>(sp, 1, th);
-                else if (!fx && fy) v = xg_if_pix<4>(sp, rp.pitch, tv);
-                else v = xg_if_hv<4, false>(sp, rp.pitch, th, tv);
-                pred[i] = (xg_pix)v;
+            if (BI && dir == 3) {
+                for (int i = tid; i < C * C; i += NT) {
+                    const int x = i % C, y = i / C;
+                    pred[i] = xg_bi_avg(xg_chroma_s16(p.ref[pl], ox, oy, x, y), xg_chroma_s16(p.ref1[pl], o1x, o1y, x, y));
+                }
+            } else {
+                const XgPlane &rp = BI && dir == 2 ? p.ref1[pl] : p.ref[pl];
+                const xg_pix *src = rp.data + (intptr_t)(oy >> 5) * rp.pitch + (ox >> 5);
+                for (int i = tid; i < C * C; i += NT) {
+                    int x = i % C, y = i / C;
+                    const xg_pix *sp = src + (intptr_t)y * rp.pitch + x;
+                    int v;
+                    if (!fx && !fy) v = sp[0];
+                    else if (fx && !fy) v = xg_if_pix<4>(sp, 1, th);
+                    else if (!fx && fy) v = xg_if_pix<4>(sp, rp.pitch, tv);
+                    else v = xg_if_hv<4, false>(sp, rp.pitch, th, tv);
+                    pred[i] = (xg_pix)v;
+                }
             }
             xg_gsync<NT, CPB>(g);
             const xg_pix *corg = p.cur[pl].data + (intptr_t)(cy >> 1) * p.cur[pl].pitch + (cx >> 1);
@@ -1157,5 +1388,12 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S)) k_cu_tail(XgTai
         xin_gpu_cu_result *o = p.res + p.first_cu + cu;
         o->mvx = mvx; o->mvy = mvy; o->cost = bc; o->int_cost = (uint32_t)(key >> 32);
         for (int i = 0; i < 3; i++) { o->nz[i] = m.nz[i]; o->ssd[i] = m.ssd[i]; }
+        if constexpr (BI) {
+            xin_gpu_cu_bi *b = p.bi + p.first_cu + cu;
+            b->mvx1 = mv1x; b->mvy1 = mv1y; b->cost1 = bc1; b->int_cost1 = (uint32_t)(p.keys1[cu] >> 32);
+            for (int l = 0; l < 2; l++) { b->bmv[2 * l] = bmv[l][0]; b->bmv[2 * l + 1] = bmv[l][1]; }
+            b->bi_cost = bi_cost;
+            b->inter_dir = (uint32_t)dir;
+        }
     }
 }

@@ -31,7 +31,8 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
         !(c->level_mask & (8u | 16u | 32u | 64u | 128u)) || (c->level_mask & ~(8u | 16u | 32u | 64u | 128u)) ||
         ((c->level_mask & 128u) && (c->ctu_size != 128 || c->search_mode != 1 || c->tu_mode != 0)) ||
         !xg_input_depth_ok(*c) || (c->search_mode != 0 && c->search_mode != 1) ||
-        (c->tu_mode != 0 && c->tu_mode != 1))
+        (c->tu_mode != 0 && c->tu_mode != 1) || c->refs < 0 || c->refs > 2 ||
+        (c->refs == 2 && (c->tu_mode != 0 || (c->level_mask & 128u))))
         return XIN_GPU_ERR_ARG;
     const bool widen = XG_BITDEPTH == 10 && c->input_bitdepth == 8;
     const uint64_t in_es = widen ? 1 : sizeof(xg_pix);
@@ -48,20 +49,23 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
             nlev++;
             ncus += (uint64_t)(c->width / XG_LEVEL_SIZE[L]) * (c->height / XG_LEVEL_SIZE[L]);
         }
-    /* two picture slots with their quarter-pel planes, the search keys, and two
-     * picture sets (results, parameters, pinned staging) */
-    uint64_t d = 2 * (ysz + 2 * csz) + 2 * 16 * ysz + 8 * (ncus ? ncus : 1) +
+    /* two picture slots (three with two references) with their quarter-pel planes,
+     * the search keys, and two picture sets (results, parameters, pinned staging) */
+    const uint64_t nslots = c->refs == 2 ? 3 : 2;
+    uint64_t d = nslots * (ysz + 2 * csz) + nslots * 16 * ysz + 8 * (ncus ? ncus : 1) +
                  2 * (sizeof(xin_gpu_cu_result) * ncus + sizeof(XgPicParams) + (lq + 2 * lc) * nlev * (sizeof(xg_coef) + sizeof(xg_pix)));
+    if (c->refs == 2) d += 8 * (ncus ? ncus : 1) + 2 * sizeof(xin_gpu_cu_bi) * ncus;   /* list 1's keys, bi records */
     if (widen && !c->device_io) d += 2 * (lq + 2 * lc);     /* 8-bit device staging per set */
     if (c->tu_mode == 1) {                                  /* the preset-4 TU stage */
         d += 2 * xg_tu_bytes(c) + 2 * sizeof(xin_gpu_cu_mts) * ncus;   /* a TU state per picture set */
     }
-    if (c->search_mode == 1)                                /* 1/2 and 1/4 resolution luma of both slots */
+    if (c->search_mode == 1)                                /* 1/2 and 1/4 resolution luma of every slot */
         for (int l = 0; l < 2; l++)
-            d += 2 * ((((uint64_t)(c->width + 2 * pad) >> (l + 1)) + 127) & ~127ull) * ((uint64_t)(c->height + 2 * pad) >> (l + 1)) *
+            d += nslots * ((((uint64_t)(c->width + 2 * pad) >> (l + 1)) + 127) & ~127ull) * ((uint64_t)(c->height + 2 * pad) >> (l + 1)) *
                  sizeof(xg_pix);
     uint64_t h = sizeof(XgPicParams) + sizeof(int32_t) + sizeof(xin_gpu_cu_result) * ncus;
     if (c->tu_mode == 1 && !c->device_io) h += sizeof(xin_gpu_cu_mts) * ncus;
+    if (c->refs == 2 && !c->device_io) h += sizeof(xin_gpu_cu_bi) * ncus;
     if (!c->device_io) {
         h += (lq + 2 * lc) * in_es;
         if (c->out_flags & XIN_GPU_OUT_Q) h += (lq + 2 * lc) * nlev * sizeof(xg_coef);

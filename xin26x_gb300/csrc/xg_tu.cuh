@@ -410,9 +410,9 @@ static void xg_tu_launch(const XgTuLevel &lv, int pl, bool fwd, cudaStream_t st)
 }
 
 /* the TU stage of the picture in slot cur (picture set t), on st; returns launches */
-static int xg_tu_enqueue(xin_gpu_stream *s, int cur, xin_gpu_stream::Set &t, cudaStream_t st)
+static int xg_tu_enqueue(xin_gpu_stream *s, int set, int cur, xin_gpu_stream::Set &t, cudaStream_t st)
 {
-    XgTuState *u = s->tu[cur];
+    XgTuState *u = s->tu[set];
     const xin_gpu_stream_cfg &c = s->cfg;
     const size_t lq = (size_t)c.width * c.height, lc = lq / 4;
     int nl = 0;

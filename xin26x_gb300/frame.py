@@ -19,18 +19,22 @@ CU_DTYPE = np.dtype([("mvx", "<i4"), ("mvy", "<i4"), ("cost", "<u4"), ("int_cost
 OUT_Q, OUT_REC = 1, 2
 # xin_gpu_cu_mts: the transform candidates of a CU (tu_mode 1)
 MTS_DTYPE = np.dtype([("satd_cost", "<u4"), ("ncand", "<u4"), ("nz", "<u8", (5,)), ("ssd", "<u8", (5,))])
+# xin_gpu_cu_bi: list 1's search, the bi pair and the choice of a CU (refs 2)
+BI_DTYPE = np.dtype([("mvx1", "<i4"), ("mvy1", "<i4"), ("cost1", "<u4"), ("int_cost1", "<u4"), ("bmv", "<i4", (4,)),
+                     ("bi_cost", "<u4"), ("inter_dir", "<u4")])
 
 
 class FrameStream:
     def __init__(self, width: int, height: int, ctu: int = 64, search_range: int = 64,
                  levels=(64, 32, 16, 8), out_q: bool = True, out_rec: bool = False, use_graph: bool = True,
                  bitdepth: int = 8, device: int = 0, input_bitdepth: int = 0, search_mode: int = 0,
-                 tu_mode: int = 0, contexts=None):
+                 tu_mode: int = 0, contexts=None, refs: int = 1):
         """bitdepth: the library (8 or 10, the reference's ENABLE_10BIT_ENCODER);
         input_bitdepth 8 with bitdepth 10: 8-bit pictures coded at 10 bits;
         search_mode 0 exhaustive integer search, 1 by resolution levels;
         tu_mode 1 the preset-4 TU work (transform candidates with dependent
-        quantisation), contexts its CABAC context set (synth.PROB_DTYPE records)."""
+        quantisation), contexts its CABAC context set (synth.PROB_DTYPE records);
+        refs 2: two references (the previous two pictures) with the bi search."""
         self.lib = _lib.load(bitdepth)
         self.bitdepth = bitdepth
         self.in_pix = np.uint8 if (bitdepth == 8 or input_bitdepth == 8) else np.uint16
@@ -43,7 +47,7 @@ class FrameStream:
             mask |= int(s)
         self.cfg = _lib.xin_gpu_stream_cfg(width, height, ctu, search_range, mask,
                                            (OUT_Q if out_q else 0) | (OUT_REC if out_rec else 0), 1 if use_graph else 0,
-                                           0, input_bitdepth, search_mode, tu_mode)
+                                           0, input_bitdepth, search_mode, tu_mode, refs)
         h = C.c_void_p()
         st = self.lib.xin_gpu_stream_open(C.byref(self.cfg), C.byref(h))
         if st != 0:
@@ -58,6 +62,7 @@ class FrameStream:
             self.levels.append((a.value, b.value, c.value, d.value))
         self.out_q, self.out_rec = out_q, out_rec
         self.tu_mode = tu_mode
+        self.refs = refs
         if tu_mode and contexts is not None:
             ctx = np.ascontiguousarray(contexts)
             if self.lib.xin_gpu_stream_set_contexts(h, ctx.ctypes.data) != 0:
@@ -87,6 +92,9 @@ class FrameStream:
             if self.tu_mode:
                 bufs["mts"] = np.zeros(self.ncus, MTS_DTYPE)
                 res.mts = bufs["mts"].ctypes.data
+            if self.refs == 2:
+                bufs["bi"] = np.zeros(self.ncus, BI_DTYPE)
+                res.bi = bufs["bi"].ctypes.data
             nl = len(self.levels)
             for p in range(3):
                 hh, ww = (self.height, self.width) if p == 0 else (self.height // 2, self.width // 2)
@@ -104,6 +112,8 @@ class FrameStream:
         out = {"cu": bufs["cu"], "gpu_ms": res.gpu_ms}
         if self.tu_mode:
             out["mts"] = bufs["mts"]
+        if self.refs == 2:
+            out["bi"] = bufs["bi"]
         if self.out_q:
             out["q"] = [bufs[("q", p)] for p in range(3)]
         if self.out_rec:
