@@ -512,7 +512,12 @@ typedef struct xin_gpu_stream_cfg {
                                     reconstruction of that choice (the bi prediction:
                                     Xin266LumaMotionComp / Xin266ChromaMotionComp's average of the
                                     14-bit predictions).  xin_gpu_cu_result keeps list 0's search;
-                                    xin_gpu_results.bi the rest.  tu_mode 0 and CU levels up to 64. */
+                                    xin_gpu_results.bi the rest.  With tu_mode 1 (satdMd) the
+                                    decision's distortion is SATD: each list's uni cost is its final
+                                    prediction's SATD cost and the pair's the averaged prediction's
+                                    SATD (pfXinComputeAvgSatd); the TU stage takes the coded
+                                    prediction, and its satd_cost the coded MVs' bits.  CU levels up
+                                    to 64. */
 } xin_gpu_stream_cfg;
 
 typedef struct xin_gpu_picture {

@@ -1345,8 +1345,8 @@ void orc_full_subpel_me(const opix *in, intptr_t is, const opix *ref_at_pu, intp
  * at preset 4, h266_encoder_create.c:1938; the recomputation at
  * h266_analyze_inter_cu.c:1109-1131 with predictor 0 and one reference). */
 static void orc_cu_tu_p4(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size, int32_t mnx, int32_t mny,
-                         int32_t mxx, int32_t mxy, ocoef *q[3], intptr_t q_stride[2], opix *rec[3], intptr_t rec_stride[2],
-                         opix *pred, ocoef *t, ocoef *qb, ocoef *r, orc_cu_out *out)
+                         int32_t mxx, int32_t mxy, int32_t dir, const int32_t *mv16, ocoef *q[3], intptr_t q_stride[2],
+                         opix *rec[3], intptr_t rec_stride[2], opix *pred, ocoef *t, ocoef *qb, ocoef *r, orc_cu_out *out)
 {
     static const uint32_t mts_list[5] = { 0, 2, 3, 4, 5 };
     const int32_t cs = size >> 1;
@@ -1355,17 +1355,26 @@ static void orc_cu_tu_p4(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, in
     for (int pl = 0; pl < 3; pl++) {
         const int32_t bs = pl ? cs : size, px = pl ? cu_x >> 1 : cu_x, py = pl ? cu_y >> 1 : cu_y;
         const intptr_t istr = f->in_stride[pl ? 1 : 0], qstr = q_stride[pl ? 1 : 0], rstr = rec_stride[pl ? 1 : 0];
-        if (pl == 0)
-            orc_luma_inter_pred(f->ref[0], f->ref_stride[0], pred, bs, out->mvx * 4, out->mvy * 4, cu_x, cu_y,
+        const opix *const *lref = dir == 2 ? f->ref1 : f->ref;
+        if (dir == 3 && pl == 0)
+            orc_luma_motion_comp_bi(f->ref[0], f->ref1[0], f->ref_stride[0], pred, bs, mv16, cu_x, cu_y, mnx, mny, mxx, mxy,
+                                    (uint32_t)size, (uint32_t)size);
+        else if (dir == 3)
+            orc_chroma_motion_comp_bi(f->ref[pl], f->ref1[pl], f->ref_stride[1], pred, bs, mv16, cu_x, cu_y, mnx, mny, mxx,
+                                      mxy, (uint32_t)size, (uint32_t)size);
+        else if (pl == 0)
+            orc_luma_inter_pred(lref[0], f->ref_stride[0], pred, bs, mv16[0], mv16[1], cu_x, cu_y,
                                 mnx, mny, mxx, mxy, (uint32_t)size, (uint32_t)size, 0);
         else
-            orc_chroma_motion_comp(f->ref[pl], f->ref_stride[1], pred, bs, out->mvx * 4, out->mvy * 4, cu_x, cu_y,
+            orc_chroma_motion_comp(lref[pl], f->ref_stride[1], pred, bs, mv16[0], mv16[1], cu_x, cu_y,
                                    mnx, mny, mxx, mxy, (uint32_t)size, (uint32_t)size);
         const opix *src = f->in[pl] + (intptr_t)py * istr + px;
         if (pl == 0) {
-            uint32_t satd;
+            /* the coded prediction's MV bits: one MV, or both of the pair */
+            uint32_t satd, bits = orc_mvd_bits(mv16[0] >> 2) + orc_mvd_bits(mv16[1] >> 2);
+            if (dir == 3) bits += orc_mvd_bits(mv16[2] >> 2) + orc_mvd_bits(mv16[3] >> 2);
             orc_satd(src, istr, pred, bs, (uint32_t)bs, (uint32_t)bs, &satd);
-            out->satd_cost = (satd << 8) + (orc_mvd_bits(out->mvx) + orc_mvd_bits(out->mvy)) * f->sad_lambda;
+            out->satd_cost = (satd << 8) + bits * f->sad_lambda;
         }
         const int32_t qp = (pl ? f->uv_qp : f->qp) + (ORC_BITDEPTH == 10 ? 12 : 0);
         const uint32_t nc = pl ? 1 : out->ncand;
@@ -1467,7 +1476,7 @@ static void orc_me_square(const opix *in, intptr_t is, const opix *ref_at_pu, in
  * predictor-index, BCW and direction bits are left out (one reference per
  * list, predictor 0).  Returns the bi pair and cost. */
 static void orc_cu_bi(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t size, int32_t mnx, int32_t mny,
-                      int32_t mxx, int32_t mxy, const int32_t uni[2][2], const uint32_t ucost[2], int32_t bmv[2][2],
+                      int32_t mxx, int32_t mxy, const int32_t uni[2][2], uint32_t ucost[2], int32_t bmv[2][2],
                       uint32_t *bi_cost)
 {
     const opix *in_y = f->in[0] + (intptr_t)cu_y * f->in_stride[0] + cu_x;
@@ -1481,6 +1490,17 @@ static void orc_cu_bi(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32
                             (uint32_t)size, (uint32_t)size, 0);
         bmv[l][0] = uni[l][0]; bmv[l][1] = uni[l][1];
     }
+    /* tu_mode 1 (preset 4, satdMd): the distortion of the mode decision is SATD --
+     * pfXinComputeAvgDist is pfXinComputeAvgSatd (h266_encoder_create.c:3336-3345),
+     * and each list's uni cost is its final prediction's SATD cost (the
+     * recomputation at h266_analyze_inter_cu.c:1103-1131) */
+    const int satd = f->tu_mode == 1;
+    if (satd)
+        for (int l = 0; l < 2; l++) {
+            uint32_t d;
+            orc_satd(in_y, is, bp[l], size, (uint32_t)size, (uint32_t)size, &d);
+            ucost[l] = (d << 8) + (orc_mvd_bits(uni[l][0]) + orc_mvd_bits(uni[l][1])) * lambda;
+        }
     int li = ucost[0] <= ucost[1] ? 1 : 0;
     uint32_t best = 0xFFFFFFFFu, sad;
     for (int it = 0; it < 2; it++, li = 1 - li) {
@@ -1492,12 +1512,14 @@ static void orc_cu_bi(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32
         orc_full_subpel_me(tgt, size, ref_y, rs, (uint32_t)size, (uint32_t)size, 0, 0, lambda, mnx, mny, mxx, mxy, &io);
         orc_luma_inter_pred(refo[li], rs, bp[li], size, io.best_mvx * 4, io.best_mvy * 4, cu_x, cu_y, mnx, mny, mxx, mxy,
                             (uint32_t)size, (uint32_t)size, 0);
-        orc_avg_sad(in_y, is, bp[0], bp[1], size, (uint32_t)size, (uint32_t)size, &sad);
+        if (satd) orc_avg_satd(in_y, is, bp[0], bp[1], size, (uint32_t)size, (uint32_t)size, &sad);
+        else orc_avg_sad(in_y, is, bp[0], bp[1], size, (uint32_t)size, (uint32_t)size, &sad);
         const uint32_t c = (sad << 8) + (orc_mvd_bits(io.best_mvx) + orc_mvd_bits(io.best_mvy) +
                                          orc_mvd_bits(bmv[1 - li][0]) + orc_mvd_bits(bmv[1 - li][1])) * lambda;
         if (c < best) { best = c; bmv[li][0] = io.best_mvx; bmv[li][1] = io.best_mvy; }
     }
-    orc_avg_sad(in_y, is, bp[0], bp[1], size, (uint32_t)size, (uint32_t)size, &sad);
+    if (satd) orc_avg_satd(in_y, is, bp[0], bp[1], size, (uint32_t)size, (uint32_t)size, &sad);
+    else orc_avg_sad(in_y, is, bp[0], bp[1], size, (uint32_t)size, (uint32_t)size, &sad);
     *bi_cost = (sad << 8) + (orc_mvd_bits(bmv[0][0]) + orc_mvd_bits(bmv[0][1]) + orc_mvd_bits(bmv[1][0]) +
                              orc_mvd_bits(bmv[1][1])) * lambda;
     free(bp[0]); free(bp[1]); free(tgt);
@@ -1519,7 +1541,7 @@ void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t
         orc_uni_search(f, f->ref1[0], f->ref1_lo, cu_x, cu_y, size, mnx, mny, mxx, mxy, &io1, &out->int_cost1);
         out->mvx1 = io1.best_mvx; out->mvy1 = io1.best_mvy; out->cost1 = io1.best_cost;
         const int32_t uni[2][2] = { { io.best_mvx, io.best_mvy }, { io1.best_mvx, io1.best_mvy } };
-        const uint32_t ucost[2] = { io.best_cost, io1.best_cost };
+        uint32_t ucost[2] = { io.best_cost, io1.best_cost };
         int32_t bmv[2][2];
         orc_cu_bi(f, cu_x, cu_y, size, mnx, mny, mxx, mxy, uni, ucost, bmv, &out->bi_cost);
         for (int l = 0; l < 2; l++) { out->bmv[2 * l] = bmv[l][0]; out->bmv[2 * l + 1] = bmv[l][1]; }
@@ -1541,7 +1563,7 @@ void orc_cu_hotpath(const orc_frame_desc *f, int32_t cu_x, int32_t cu_y, int32_t
     ocoef *qb = (ocoef *)malloc(sizeof(ocoef) * (size_t)(size * size));
     ocoef *r = (ocoef *)malloc(sizeof(ocoef) * (size_t)(size * size));
     if (f->tu_mode == 1) {
-        orc_cu_tu_p4(f, cu_x, cu_y, size, mnx, mny, mxx, mxy, q, q_stride, rec, rec_stride, pred, t, qb, r, out);
+        orc_cu_tu_p4(f, cu_x, cu_y, size, mnx, mny, mxx, mxy, dir, mv16, q, q_stride, rec, rec_stride, pred, t, qb, r, out);
         free(pred); free(t); free(qb); free(r);
         return;
     }

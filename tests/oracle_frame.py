@@ -38,7 +38,7 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
     threads: host threads sharing the CUs (0 = every core); each CU writes only its
     own record and its own area of the level's planes, so the calls are independent.
     ref1: list 1's planes (two references and the bi search); its records
-    (BI_DTYPE) are returned after the planes.
+    (BI_DTYPE) are returned last.
     Returns (cu records, q planes [levels,h,w] x3, rec planes x3)."""
     o = O.oracle(bitdepth)
     h, w = cur[0].shape
@@ -132,7 +132,7 @@ def run(cur, ref, levels, ctu=64, search_range=16, qp=32, uv_qp=32, sad_lambda=6
         with ThreadPoolExecutor(nthreads) as ex:
             list(ex.map(one, work[1:]))
     if tu_mode:
-        return recs, q, rec, mts
+        return (recs, q, rec, mts, bis) if ref1 is not None else (recs, q, rec, mts)
     if ref1 is not None:
         return recs, q, rec, bis
     return recs, q, rec

@@ -408,11 +408,10 @@ def test_frame_bi_matches_oracle(bd, inb, search_mode, w, h, R):
     assert dirs[0] == 0 and dirs[3] > 0 and dirs[1] + dirs[2] > 0, dirs   # both kinds of choice occur
 
 
-def test_frame_bi_needs_tu_mode_0_and_levels_up_to_64():
-    """refs 2 is refused with the preset-4 TU stage, with the 128 x 128 level and
-    above two references."""
-    for kw in ({"tu_mode": 1, "refs": 2}, {"ctu": 128, "search_mode": 1, "levels": (128, 64), "refs": 2}, {"refs": 3}):
-        with pytest.raises(RuntimeError, match="two references need TU mode 0"):
+def test_frame_bi_needs_levels_up_to_64():
+    """refs 2 is refused with the 128 x 128 level, and more than two references."""
+    for kw in ({"ctu": 128, "search_mode": 1, "levels": (128, 64), "refs": 2}, {"refs": 3}):
+        with pytest.raises(RuntimeError, match="two references need CU levels up to 64"):
             FrameStream(256, 256, search_range=16, **kw)
 
 
@@ -451,6 +450,49 @@ def test_frame_preset4_tu_matches_oracle(bd, inb, search_mode, w, h, R):
                 assert bad.size == 0, (name, bad[:5], out["mts"][bad[:3]], mts[bad[:3]])
     finally:
         fs.close()
+
+
+@pytest.mark.parametrize("bd,inb,search_mode", [(8, 0, 0), (10, 8, 1)])
+def test_frame_preset4_bi_matches_oracle(bd, inb, search_mode):
+    """tu_mode 1 with two references: the bi search with SATD as the decision's
+    distortion (the uni lists' final-prediction SATD costs and the averaged
+    prediction's SATD), the coded prediction (list 0, list 1 or the pair) through
+    every transform candidate and dependent quantisation, and the SATD cost with
+    the coded MVs' bits, against the oracle for pictures 1 .. 3."""
+    from xin26x_gb300 import synth as S
+    from xin26x_gb300.frame import BI_DTYPE
+    w, h, R = 192, 128, 16
+    rng = np.random.default_rng(77 + bd)
+    ctx = S.contexts(rng, 1)[0]
+    seq = synth.sequence(w, h, 4, seed=w + bd, bitdepth=8 if inb == 8 else bd, objects=3)
+    fs = FrameStream(w, h, search_range=R, out_q=True, out_rec=True, bitdepth=bd, input_bitdepth=inb,
+                     search_mode=search_mode, tu_mode=1, contexts=ctx, refs=2)
+    dirs = np.zeros(4, np.int64)
+    try:
+        fs.submit(*seq[0], qp=22, uv_qp=22, sad_lambda=64)
+        fs.wait()
+        for k in (1, 2, 3):
+            qp, lam = 22 + 5 * k, (40 + 10 * k) << (2 if inb == 8 else 0)
+            fs.submit(*seq[k], qp=qp, uv_qp=qp, sad_lambda=lam)
+            out = fs.wait()
+            cur, r0, r1 = seq[k], seq[k - 1], seq[max(k - 2, 0)]
+            if inb == 8:
+                cur, r0, r1 = [tuple(p.astype(np.uint16) << 2 for p in f) for f in (cur, r0, r1)]
+            recs, q, rec, mts, bis = oracle_frame.run(cur, r0, fs.levels, search_range=R, qp=qp, uv_qp=qp, sad_lambda=lam,
+                                                      bitdepth=bd, threads=0, search_mode=search_mode, tu_mode=1,
+                                                      contexts=ctx, ref1=r1)
+            label = ("p4bi", bd, inb, search_mode, k)
+            _compare(out, (recs, q, rec), fs.levels, label)
+            for name in ("satd_cost", "ncand", "nz", "ssd"):
+                bad = np.nonzero(np.any((out["mts"][name] != mts[name]).reshape(len(mts), -1), axis=1))[0]
+                assert bad.size == 0, (label, name, bad[:5], out["mts"][bad[:3]], mts[bad[:3]])
+            for name in BI_DTYPE.names:
+                bad = np.nonzero(np.any((out["bi"][name] != bis[name]).reshape(len(bis), -1), axis=1))[0]
+                assert bad.size == 0, (label, name, bad[:5], out["bi"][bad[:5]], bis[bad[:5]])
+            dirs += np.bincount(out["bi"]["inter_dir"].astype(np.int64), minlength=4)[:4]
+    finally:
+        fs.close()
+    assert dirs[3] > 0 and dirs[1] + dirs[2] > 0, dirs
 
 
 @pytest.mark.parametrize("bd,inb", [(8, 0), (10, 8)])

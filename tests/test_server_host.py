@@ -66,7 +66,7 @@ def test_footprint_8bit_input_into_10bit_build():
 def test_footprint_two_references(bd):
     """refs 2: a third picture slot with its quarter-pel planes, list 1's search keys
     and a bi record per CU in each picture set (pinned host copies too); refused
-    with the preset-4 TU stage, the 128 x 128 level or more than two references."""
+    with the 128 x 128 level or more than two references."""
     lib = _lib.load(bd)
     es = 1 if bd == 8 else 2
 
@@ -82,5 +82,5 @@ def test_footprint_two_references(bd):
     ncus = 30 * 16 + 60 * 33 + 120 * 67 + 240 * 135
     assert d2 - d1 == (ysz + 2 * csz) + 16 * ysz + 8 * ncus + 2 * 40 * ncus    # xin_gpu_cu_bi: 40 bytes
     assert h2 - h1 == 2 * 40 * ncus
-    assert fp(2, tu=1)[0] == -2 and fp(3)[0] == -2 and fp(-1)[0] == -2
+    assert fp(3)[0] == -2 and fp(-1)[0] == -2 and fp(2, tu=1)[0] == 0
     assert fp(2, mask=248, ctu=128, sm=1)[0] == -2 and fp(1, mask=248, ctu=128, sm=1)[0] == 0

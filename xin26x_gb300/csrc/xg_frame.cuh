@@ -180,10 +180,10 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         !(c.level_mask & (8u | 16u | 32u | 64u | 128u)) || (c.level_mask & ~(8u | 16u | 32u | 64u | 128u)) ||
         !xg_input_depth_ok(c) || (c.search_mode != 0 && c.search_mode != 1) || (c.tu_mode != 0 && c.tu_mode != 1) ||
         ((c.level_mask & 128u) && (c.ctu_size != 128 || c.search_mode != 1 || c.tu_mode != 0)) || c.refs < 0 || c.refs > 2 ||
-        (c.refs == 2 && (c.tu_mode != 0 || (c.level_mask & 128u)))) {
+        (c.refs == 2 && (c.level_mask & 128u))) {
         xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range, level mask, input bit depth, search or "
                                       "TU mode, or references (the 128 x 128 level needs CTU 128, the search by levels and TU "
-                                      "mode 0; two references need TU mode 0 and CU levels up to 64)");
+                                      "mode 0; two references need CU levels up to 64)");
         return XIN_GPU_ERR_ARG;
     }
     xin_gpu_stream *s = new (std::nothrow) xin_gpu_stream();

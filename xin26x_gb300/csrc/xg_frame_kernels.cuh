@@ -1188,6 +1188,30 @@ __device__ __forceinline__ uint32_t xg_avg_sad(const xg_pix *org, intptr_t op, c
     return xg_group_sum<NT, CPB>(s, part[0], g, tid);
 }
 
+/* SATD of org against a (or against the average of a and b, pfXinComputeAvgSatd):
+ * sum over the 8 x 8 blocks of (Hadamard sum + 2) >> 2, summed over the group */
+template <int S, int NT, int CPB>
+__device__ uint32_t xg_satd_blocks(const xg_pix *org, intptr_t op, const xg_pix *a, const xg_pix *b, uint32_t (*part)[NT / 32],
+                                   int g, int tid)
+{
+    constexpr int NB = (S / 8) * (S / 8);
+    uint32_t s = 0;
+    for (int k = tid; k < NB; k += NT) {
+        const int bx = (k % (S / 8)) * 8, by = (k / (S / 8)) * 8;
+        int d[64];
+#pragma unroll
+        for (int y = 0; y < 8; y++)
+#pragma unroll
+            for (int x = 0; x < 8; x++) {
+                const int i = (by + y) * S + bx + x;
+                const int pv = b ? ((int)a[i] + (int)b[i] + 1) >> 1 : (int)a[i];
+                d[y * 8 + x] = (int)org[(intptr_t)(by + y) * op + bx + x] - pv;
+            }
+        s += (xg_had8(d) + 2) >> 2;
+    }
+    return xg_group_sum<NT, CPB>(s, part[0], g, tid);
+}
+
 template <int S, int NT, int CPB, bool BI>
 __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, BI)) k_cu_tail(XgTailParams p, const XgPicParams *pp, int ncu)
 {
@@ -1255,7 +1279,23 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, BI)) k_cu_tail(X
         xg_luma_uni<S, NT>(p.qpel, cx, cy, mvx, mvy, mnx, mny, mxx, mxy, bs.bp[0], tid);
         xg_luma_uni<S, NT>(p.qpel1, cx, cy, mv1x, mv1y, mnx, mny, mxx, mxy, bs.bp[1], tid);
         xg_gsync<NT, CPB>(g);
-        int li = bc <= bc1 ? 1 : 0;
+        /* the preset-4 TU stage (satdMd): SATD is the decision's distortion --
+         * pfXinComputeAvgDist is the averaged SATD (h266_encoder_create.c:3336-3345)
+         * and each list's uni cost its final prediction's SATD cost
+         * (h266_analyze_inter_cu.c:1103-1131) */
+        const bool satd = p.resid[0] != nullptr;
+        uint32_t uc0 = bc, uc1 = bc1;
+        if (satd) {
+            uc0 = (xg_satd_blocks<S, NT, CPB>(org, opitch, bs.bp[0], nullptr, m.part, g, tid) << XG_COST_FRACTION) +
+                  (xg_mvd_bits(mvx) + xg_mvd_bits(mvy)) * lambda;
+            uc1 = (xg_satd_blocks<S, NT, CPB>(org, opitch, bs.bp[1], nullptr, m.part, g, tid) << XG_COST_FRACTION) +
+                  (xg_mvd_bits(mv1x) + xg_mvd_bits(mv1y)) * lambda;
+        }
+        auto dist2 = [&]() {
+            return satd ? xg_satd_blocks<S, NT, CPB>(org, opitch, bs.bp[0], bs.bp[1], m.part, g, tid)
+                        : xg_avg_sad<S, NT, CPB>(org, opitch, bs.bp[0], bs.bp[1], m.part, g, tid);
+        };
+        int li = uc0 <= uc1 ? 1 : 0;
         uint32_t best = 0xFFFFFFFFu;
         for (int it = 0; it < 2; it++, li ^= 1) {
             const xg_pix *other = bs.bp[1 - li];
@@ -1272,16 +1312,16 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, BI)) k_cu_tail(X
                 xg_subpel<S, NT, CPB>(bs.tgt, S, li ? p.qpel1 : p.qpel, cx, cy, lambda, m.part, g, tid, ix, iy, ic);
             xg_luma_uni<S, NT>(li ? p.qpel1 : p.qpel, cx, cy, ix, iy, mnx, mny, mxx, mxy, bs.bp[li], tid);
             xg_gsync<NT, CPB>(g);
-            const uint32_t sad = xg_avg_sad<S, NT, CPB>(org, opitch, bs.bp[0], bs.bp[1], m.part, g, tid);
+            const uint32_t sad = dist2();
             const uint32_t c = (sad << XG_COST_FRACTION) + (xg_mvd_bits(ix) + xg_mvd_bits(iy) + xg_mvd_bits(bmv[1 - li][0]) +
                                                             xg_mvd_bits(bmv[1 - li][1])) * lambda;
             if (c < best) { best = c; bmv[li][0] = ix; bmv[li][1] = iy; }
         }
-        const uint32_t sad = xg_avg_sad<S, NT, CPB>(org, opitch, bs.bp[0], bs.bp[1], m.part, g, tid);
+        const uint32_t sad = dist2();
         bi_cost = (sad << XG_COST_FRACTION) +
                   (xg_mvd_bits(bmv[0][0]) + xg_mvd_bits(bmv[0][1]) + xg_mvd_bits(bmv[1][0]) + xg_mvd_bits(bmv[1][1])) * lambda;
-        uint32_t ubest = bc;
-        if (bc1 < ubest) { ubest = bc1; dir = 2; }
+        uint32_t ubest = uc0;
+        if (uc1 < ubest) { ubest = uc1; dir = 2; }
         if (bi_cost < ubest) dir = 3;
     }
     /* the coded MV of each list (1/16 pel, clamped to the window as the motion

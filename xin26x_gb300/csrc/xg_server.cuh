@@ -32,7 +32,7 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
         ((c->level_mask & 128u) && (c->ctu_size != 128 || c->search_mode != 1 || c->tu_mode != 0)) ||
         !xg_input_depth_ok(*c) || (c->search_mode != 0 && c->search_mode != 1) ||
         (c->tu_mode != 0 && c->tu_mode != 1) || c->refs < 0 || c->refs > 2 ||
-        (c->refs == 2 && (c->tu_mode != 0 || (c->level_mask & 128u))))
+        (c->refs == 2 && (c->level_mask & 128u)))
         return XIN_GPU_ERR_ARG;
     const bool widen = XG_BITDEPTH == 10 && c->input_bitdepth == 8;
     const uint64_t in_es = widen ? 1 : sizeof(xg_pix);

@@ -62,6 +62,7 @@ struct XgTuLevel {
     xg_coef *qout[3];                  /* the picture's output planes of this level */
     xg_pix *recout[3];
     int W, S, cus_x, ncu, nc;
+    const xin_gpu_cu_bi *bi;           /* refs 2: this level's bi records (the coded prediction) */
 };
 
 /* A transform matrix of N points (rows k < K = min(N, 32)) into a packed int8
@@ -260,7 +261,14 @@ __global__ void k_tu_collect(XgTuLevel L, const uint32_t *satd, xin_gpu_cu_resul
         o.nz[pl] = L.nz[b];
         o.ssd[pl] = L.ssd[b];
     }
-    m.satd_cost = (satd[cu] << XG_COST_FRACTION) + (xg_mvd_bits(o.mvx) + xg_mvd_bits(o.mvy)) * pp->lambda;
+    /* the coded prediction's MV bits: list 0's MV, list 1's, or both of the pair */
+    unsigned bits = xg_mvd_bits(o.mvx) + xg_mvd_bits(o.mvy);
+    if (L.bi) {
+        const xin_gpu_cu_bi &b = L.bi[cu];
+        if (b.inter_dir == 2) bits = xg_mvd_bits(b.mvx1) + xg_mvd_bits(b.mvy1);
+        if (b.inter_dir == 3) bits = xg_mvd_bits(b.bmv[0]) + xg_mvd_bits(b.bmv[1]) + xg_mvd_bits(b.bmv[2]) + xg_mvd_bits(b.bmv[3]);
+    }
+    m.satd_cost = (satd[cu] << XG_COST_FRACTION) + bits * pp->lambda;
     m.ncand = (uint32_t)L.nc;
     for (int c = 0; c < 5; c++) {
         m.nz[c] = c < L.nc ? L.nz[cu * L.nc + c] : 0ull;
@@ -458,6 +466,7 @@ static int xg_tu_enqueue(xin_gpu_stream *s, int set, int cur, xin_gpu_stream::Se
         v.nz = u->nz + u->blk[L][0];
         v.ssd = u->ssd + u->blk[L][0];
         v.W = c.width; v.S = XG_LEVEL_SIZE[L]; v.cus_x = s->lev_cx[L]; v.ncu = s->lev_cx[L] * s->lev_cy[L]; v.nc = u->nc[L];
+        v.bi = t.dbi ? t.dbi + s->lev_first[L] : nullptr;
         li++;
         if (v.ncu == 0) continue;
         for (int p = 0; p < 3; p++) { xg_tu_launch(v, p, true, ls[L]); nl++; }
