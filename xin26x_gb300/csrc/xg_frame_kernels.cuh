@@ -1132,6 +1132,33 @@ __device__ void xg_bi_square(const xg_pix *t, const XgPlane &rp, int cx, int cy,
 {
     const int lane = tid & 31, warp = tid >> 5;
     bx = 0; by = 0; bc = 0xFFFFFFFFu;
+    if constexpr (NT == 32 && S == 8) {
+        /* 8 x 8 CUs: a lane takes whole candidates (c = lane, lane + 32, lane + 64),
+         * then one warp minimum of (cost, raster index) -- the first of the lowest
+         * cost, as the strict '<' in raster order keeps */
+        unsigned long long best = ~0ull;
+        for (int c = lane; c < 81; c += 32) {
+            const int mx = ccx + c % 9 - 4, my = ccy + c / 9 - 4;
+            if (mx < mnx || mx > mxx || my < mny || my > mxy) continue;
+            const xg_pix *r = rp.data + (intptr_t)(cy + my) * rp.pitch + cx + mx;
+            uint32_t sad = 0;
+#pragma unroll 4
+            for (int i = 0; i < S * S; i++) sad = __usad((unsigned)t[i], (unsigned)r[(intptr_t)(i / S) * rp.pitch + i % S], sad);
+            const uint32_t cost = (sad << XG_COST_FRACTION) + (xg_mvd_bits(4 * mx) + xg_mvd_bits(4 * my)) * lambda;
+            const unsigned long long k = ((unsigned long long)cost << 32) | (unsigned)c;
+            best = k < best ? k : best;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ok = __shfl_xor_sync(0xffffffffu, best, o);
+            best = ok < best ? ok : best;
+        }
+        if (best != ~0ull) {
+            const int c = (int)(uint32_t)best;
+            bc = (uint32_t)(best >> 32); bx = 4 * (ccx + c % 9 - 4); by = 4 * (ccy + c / 9 - 4);
+        }
+        return;
+    }
     for (int dy = -4; dy <= 4; dy++) {
         const int my = ccy + dy;
         if (my < mny || my > mxy) continue;               /* uniform over the group */
@@ -1189,27 +1216,40 @@ __device__ __forceinline__ uint32_t xg_avg_sad(const xg_pix *org, intptr_t op, c
 }
 
 /* SATD of org against a (or against the average of a and b, pfXinComputeAvgSatd):
- * sum over the 8 x 8 blocks of (Hadamard sum + 2) >> 2, summed over the group */
+ * sum over the 8 x 8 blocks of (Hadamard sum + 2) >> 2, summed over the group.
+ * A warp takes a block at a time: lane l holds elements 2l and 2l + 1 (row-major),
+ * and the 8 x 8 Hadamard is the 64-point Walsh-Hadamard transform of the block,
+ * one butterfly stage per element-index bit (bit 0 inside the lane, bits 1..5
+ * across lanes by shuffles); the sum of absolute values does not depend on the
+ * order of the stages. */
 template <int S, int NT, int CPB>
 __device__ uint32_t xg_satd_blocks(const xg_pix *org, intptr_t op, const xg_pix *a, const xg_pix *b, uint32_t (*part)[NT / 32],
                                    int g, int tid)
 {
-    constexpr int NB = (S / 8) * (S / 8);
+    constexpr int NB = (S / 8) * (S / 8), NW = NT / 32;
+    const int lane = tid & 31, warp = tid >> 5, y = lane >> 2, x = (lane & 3) * 2;
     uint32_t s = 0;
-    for (int k = tid; k < NB; k += NT) {
+    for (int k = warp; k < NB; k += NW) {
         const int bx = (k % (S / 8)) * 8, by = (k / (S / 8)) * 8;
-        int d[64];
+        const int i = (by + y) * S + bx + x;
+        const xg_pix *o = org + (intptr_t)(by + y) * op + bx + x;
+        int v0 = (int)o[0] - (b ? ((int)a[i] + (int)b[i] + 1) >> 1 : (int)a[i]);
+        int v1 = (int)o[1] - (b ? ((int)a[i + 1] + (int)b[i + 1] + 1) >> 1 : (int)a[i + 1]);
+        const int s0 = v0 + v1;
+        v1 = v0 - v1;
+        v0 = s0;
 #pragma unroll
-        for (int y = 0; y < 8; y++)
-#pragma unroll
-            for (int x = 0; x < 8; x++) {
-                const int i = (by + y) * S + bx + x;
-                const int pv = b ? ((int)a[i] + (int)b[i] + 1) >> 1 : (int)a[i];
-                d[y * 8 + x] = (int)org[(intptr_t)(by + y) * op + bx + x] - pv;
-            }
-        s += (xg_had8(d) + 2) >> 2;
+        for (int bit = 0; bit < 5; bit++) {
+            const int p0 = __shfl_xor_sync(0xffffffffu, v0, 1 << bit), p1 = __shfl_xor_sync(0xffffffffu, v1, 1 << bit);
+            const bool hi = (lane >> bit) & 1;
+            v0 = hi ? p0 - v0 : v0 + p0;
+            v1 = hi ? p1 - v1 : v1 + p1;
+        }
+        const uint32_t sum = __reduce_add_sync(0xffffffffu, (uint32_t)(abs(v0) + abs(v1)));
+        s += (sum + 2) >> 2;
     }
-    return xg_group_sum<NT, CPB>(s, part[0], g, tid);
+    /* every lane of a warp holds the warp's total: one lane adds it */
+    return xg_group_sum<NT, CPB>(lane == 0 ? s : 0u, part[0], g, tid);
 }
 
 template <int S, int NT, int CPB, bool BI>
@@ -1256,7 +1296,7 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, BI)) k_cu_tail(X
 
     /* the prediction coded: list 0, or (refs 2) the lowest of list 0, list 1 and the pair */
     int dir = 1;
-    int mv1x = 0, mv1y = 0, bmv[2][2] = { { mvx, mvy }, { 0, 0 } };
+    int mv1x = 0, mv1y = 0, b0x = mvx, b0y = mvy, b1x = 0, b1y = 0;   /* list 1's MV; the bi pair */
     uint32_t bc1 = 0, bi_cost = 0;
     if constexpr (BI) {
         XgTailBiSmem<S> &bs = reinterpret_cast<XgTailBiSmem<S> *>(xg_tail_raw + sizeof(XgTailSmem<S, NT>) * CPB)[g];
@@ -1274,8 +1314,7 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, BI)) k_cu_tail(X
          * the integer part of its uni MV: integer step, then Xin266FullSubPelMe; the pair
          * is costed by the SAD against the average of the two predictions and kept when
          * it improves; the final cost is taken on the last predictions (:815-852) */
-        const int uni[2][2] = { { mvx, mvy }, { mv1x, mv1y } };
-        bmv[1][0] = mv1x; bmv[1][1] = mv1y;
+        b1x = mv1x; b1y = mv1y;
         xg_luma_uni<S, NT>(p.qpel, cx, cy, mvx, mvy, mnx, mny, mxx, mxy, bs.bp[0], tid);
         xg_luma_uni<S, NT>(p.qpel1, cx, cy, mv1x, mv1y, mnx, mny, mxx, mxy, bs.bp[1], tid);
         xg_gsync<NT, CPB>(g);
@@ -1306,28 +1345,30 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, BI)) k_cu_tail(X
             xg_gsync<NT, CPB>(g);
             int ix, iy;
             uint32_t ic;
-            xg_bi_square<S, NT, CPB>(bs.tgt, li ? p.ref1[0] : p.ref[0], cx, cy, uni[li][0] >> 2, uni[li][1] >> 2, mnx, mny, mxx,
-                                     mxy, lambda, m.part, g, tid, ix, iy, ic);
+            xg_bi_square<S, NT, CPB>(bs.tgt, li ? p.ref1[0] : p.ref[0], cx, cy, (li ? mv1x : mvx) >> 2, (li ? mv1y : mvy) >> 2,
+                                     mnx, mny, mxx, mxy, lambda, m.part, g, tid, ix, iy, ic);
             if (in_window(ix, iy))
                 xg_subpel<S, NT, CPB>(bs.tgt, S, li ? p.qpel1 : p.qpel, cx, cy, lambda, m.part, g, tid, ix, iy, ic);
             xg_luma_uni<S, NT>(li ? p.qpel1 : p.qpel, cx, cy, ix, iy, mnx, mny, mxx, mxy, bs.bp[li], tid);
             xg_gsync<NT, CPB>(g);
             const uint32_t sad = dist2();
-            const uint32_t c = (sad << XG_COST_FRACTION) + (xg_mvd_bits(ix) + xg_mvd_bits(iy) + xg_mvd_bits(bmv[1 - li][0]) +
-                                                            xg_mvd_bits(bmv[1 - li][1])) * lambda;
-            if (c < best) { best = c; bmv[li][0] = ix; bmv[li][1] = iy; }
+            const uint32_t c = (sad << XG_COST_FRACTION) + (xg_mvd_bits(ix) + xg_mvd_bits(iy) + xg_mvd_bits(li ? b0x : b1x) +
+                                                            xg_mvd_bits(li ? b0y : b1y)) * lambda;
+            if (c < best) {
+                best = c;
+                if (li) { b1x = ix; b1y = iy; } else { b0x = ix; b0y = iy; }
+            }
         }
         const uint32_t sad = dist2();
-        bi_cost = (sad << XG_COST_FRACTION) +
-                  (xg_mvd_bits(bmv[0][0]) + xg_mvd_bits(bmv[0][1]) + xg_mvd_bits(bmv[1][0]) + xg_mvd_bits(bmv[1][1])) * lambda;
+        bi_cost = (sad << XG_COST_FRACTION) + (xg_mvd_bits(b0x) + xg_mvd_bits(b0y) + xg_mvd_bits(b1x) + xg_mvd_bits(b1y)) * lambda;
         uint32_t ubest = uc0;
         if (uc1 < ubest) { ubest = uc1; dir = 2; }
         if (bi_cost < ubest) dir = 3;
     }
     /* the coded MV of each list (1/16 pel, clamped to the window as the motion
      * compensation does) */
-    const int c0x = dir == 3 ? bmv[0][0] : dir == 2 ? mv1x : mvx, c0y = dir == 3 ? bmv[0][1] : dir == 2 ? mv1y : mvy;
-    const int c1x = bmv[1][0], c1y = bmv[1][1];
+    const int c0x = dir == 3 ? b0x : dir == 2 ? mv1x : mvx, c0y = dir == 3 ? b0y : dir == 2 ? mv1y : mvy;
+    const int c1x = b1x, c1y = b1y;
 
     /* ---- luma MC: Xin266LumaInterPred (uni) or the bi branch of Xin266LumaMotionComp */
     if (BI && dir == 3) {
@@ -1431,7 +1472,7 @@ __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, BI)) k_cu_tail(X
         if constexpr (BI) {
             xin_gpu_cu_bi *b = p.bi + p.first_cu + cu;
             b->mvx1 = mv1x; b->mvy1 = mv1y; b->cost1 = bc1; b->int_cost1 = (uint32_t)(p.keys1[cu] >> 32);
-            for (int l = 0; l < 2; l++) { b->bmv[2 * l] = bmv[l][0]; b->bmv[2 * l + 1] = bmv[l][1]; }
+            b->bmv[0] = b0x; b->bmv[1] = b0y; b->bmv[2] = b1x; b->bmv[3] = b1y;
             b->bi_cost = bi_cost;
             b->inter_dir = (uint32_t)dir;
         }
