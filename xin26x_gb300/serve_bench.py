@@ -6,14 +6,16 @@ live streams at 30 pictures/s each (1,548.3 luma Mpixel/s offered), each with
 Streams ask to join in a seeded order at seeded times over the first 0.5 s;
 the server admits a stream only if its device footprint fits and the luma
 Mpixel/s already promised plus its own stays within --mpix-budget.  Each
-admitted stream then submits a picture every 1/30 s plus a seeded 0..4 ms
-jitter; a picture that finds its stream's queue full is dropped (counted).  A
+admitted stream's pictures then arrive as a Poisson process at 30 pictures/s
+(exponential gaps of mean 1/30 s, seeded) plus a seeded 0..2 ms jitter
+(--arrivals periodic: a picture every 1/30 s plus 0..4 ms); a picture that
+finds its stream's queue full is dropped (counted).  A
 quarter of the admitted streams leave at seeded times in the last 40 % of the
 run.  Reported: admitted / refused streams, luma Mpixel/s completed, and the
 latency of each picture from submit to results in host memory (p50 / p99 /
 max), measured inside the server.
 
-  python -m xin26x_gb300.serve_bench [--seconds 4] [--mpix-budget 1650] [--max-inflight 6]
+  python -m xin26x_gb300.serve_bench [--seconds 4] [--mpix-budget 1650] [--max-inflight 6] [--arrivals poisson]
 """
 from __future__ import annotations
 
@@ -31,7 +33,7 @@ FPS = 30.0
 LAMBDA = {27: 45, 32: 64, 37: 91}
 
 
-def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=64, frames_per_class=6):
+def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=64, frames_per_class=6, arrivals="poisson"):
     from xin26x_gb300 import synth
     from xin26x_gb300.server import Admission, Server
 
@@ -112,8 +114,11 @@ def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=6
             else:
                 raise RuntimeError(f"submit failed: {st}")
             a_of[si] += 1
-            nxt = a_of[si] / FPS + float(rng.uniform(0, 0.004))
-            heapq.heappush(events, (float(join_t[list(order).index(si)]) + nxt, 1, si))
+            if arrivals == "poisson":
+                heapq.heappush(events, (t + float(rng.exponential(1.0 / FPS)) + float(rng.uniform(0, 0.002)), 1, si))
+            else:
+                nxt = a_of[si] / FPS + float(rng.uniform(0, 0.004))
+                heapq.heappush(events, (float(join_t[list(order).index(si)]) + nxt, 1, si))
         else:                              # leave (drains the stream's queue)
             srv.leave(sid_of[si], 60000)
     wall_submit = time.perf_counter() - t0
@@ -125,6 +130,8 @@ def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=6
     by_class = {f"{w}x{h}": sum(1 for si in admitted if streams[si][0] == (w, h)) for (w, h) in CLASSES}
     return {"workload": f"{len(streams)} streams (16 x 640x360, 16 x 1280x720, 16 x 1920x1080) at 30 fps, "
                         f"+-{search_range} exhaustive search, CU levels 64/32/16/8, {seconds:.1f} s",
+            "arrivals": "Poisson at 30 pictures/s per stream + 0..2 ms jitter" if arrivals == "poisson"
+                        else "every 1/30 s + 0..4 ms jitter",
             "offered_mpix_s": offered, "mpix_budget": mpix_budget, "max_inflight": max_inflight,
             "admitted": len(admitted), "refused": len(refused), "admitted_by_class": by_class,
             "pictures": len(lat), "arrived": int(sum(a_of.values())), "dropped": dropped, "failed": len(failed), "first_failures": failed[:4],
@@ -142,8 +149,9 @@ def main():
     ap.add_argument("--mpix-budget", type=float, default=1650.0)
     ap.add_argument("--max-inflight", type=int, default=6)
     ap.add_argument("--seed", type=int, default=48)
+    ap.add_argument("--arrivals", choices=("poisson", "periodic"), default="poisson")
     a = ap.parse_args()
-    print(json.dumps(run(a.seconds, a.mpix_budget, a.max_inflight, a.seed)), flush=True)
+    print(json.dumps(run(a.seconds, a.mpix_budget, a.max_inflight, a.seed, arrivals=a.arrivals)), flush=True)
 
 
 if __name__ == "__main__":
