@@ -55,7 +55,10 @@ def workload_config():
                         "QP 27/32/37 cycling, 30 synthetic pictures (seeded texture + 4 moving rectangles)",
             "width": W, "height": H, "input_bitdepth": IN_BD, "internal_bitdepth": BD, "search_range": SEARCH,
             "levels": list(LEVELS), "frames": NFRAMES, "sad_lambda": LAMBDA_BD,
-            "l2": "flushed between steps (512 MB write outside the timed events)"}
+            "l2": "flushed between steps (512 MB write outside the timed events)",
+            "preset4_random_access": "measured beside the headline as preset4_ra_1080p: GOP 16 coding order, two "
+                                     "references per picture with the bi search, search by resolution levels, MTS "
+                                     "candidates through dependent quantisation, SATD"}
 
 
 def make_frames(n=NFRAMES):
@@ -331,7 +334,7 @@ def run_gpu(args):
     kbatch = kernel_batch_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup) if rank == 0 else None
     dq = dep_quant_bench(torch, flush, max(5, min(args.steps, 20)), args.warmup, cpu=(world == 1)) if rank == 0 else None
     p4 = preset4_bench(torch, flush, frames, max(5, min(args.steps, 20)), args.warmup) if rank == 0 else None
-    p4bi = preset4_bi_bench(torch, flush, frames, max(5, min(args.steps, 20)), args.warmup) if rank == 0 else None
+    p4ra = preset4_ra_bench(torch, flush, frames, 16) if rank == 0 else None
     wide = wide_search_bench(torch, flush) if rank == 0 else None
     if wide is not None:
         wide["by_resolution_levels"] = wide_search_bench(torch, flush, pictures=4, search_mode=1)
@@ -378,7 +381,7 @@ def run_gpu(args):
                "kernel_batch": kbatch,
                "dep_quant": dq,
                "preset4_1080p": p4,
-               "preset4_bi_1080p": p4bi,
+               "preset4_ra_1080p": p4ra,
                "wide_search_4k_10bit": wide,
                "pipeline_variants_1080p": variants,
                "serving": serving,
@@ -523,90 +526,111 @@ def dep_quant_bench(torch, flush, steps, warmup, nblocks=65536, seed=11, cpu=Tru
     return out
 
 
-def preset4_bi_bench(torch, flush, frames, steps, warmup):
-    """The preset-4 form with two references at 1080p: the preset-4 workload
-    (search by resolution levels, full sub-pel search, every transform candidate
-    through dependent quantisation, SATD) with list 0 = the previous picture and
-    list 1 = the one before, the bi search of Xin266InterBiSearch per CU (SATD as
-    the decision's distortion) and the coded prediction -- list 0, list 1 or the
-    bi pair -- through the TU stage.  Device-resident pictures, CUDA-event device
-    time per picture, L2 flushed between pictures; then end to end through the
-    public API with host buffers, two pictures in flight."""
+def preset4_ra_bench(torch, flush, frames, steps):
+    """The preset-4 form in random-access order at 1080p: GOP 16 coding order
+    (synth.ra_gop: each key picture from the previous key picture, each B picture
+    from the nearest coded pictures before and after it), two references per
+    picture named through xin_gpu_frame_submit_refs (dpb 32: the graph pattern
+    repeats every two GOPs), the search by resolution levels and full sub-pel
+    search per list, the bi search of Xin266InterBiSearch per CU with SATD as
+    the decision's distortion, and the coded prediction (list 0, list 1 or bi)
+    through every transform candidate and dependent quantisation.  Device-
+    resident pictures, CUDA-event device time per picture after two GOPs of
+    warm-up, L2 flushed between pictures; then end to end through the public API
+    with host buffers, two pictures in flight.  Picture POC p is frame p % 30."""
     from xin26x_gb300 import _lib, synth
     lib = _lib.load(BD)
     assert lib.xin_gpu_init(torch.cuda.current_device()) == 0
     ctx = np.ascontiguousarray(synth.contexts(np.random.default_rng(4), 1)[0])
     dev = [tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f) for f in frames]
-    cfg = _lib.xin_gpu_stream_cfg(W, H, 64, SEARCH, sum(LEVELS), 0, 1, 1, IN_BD, 1, 1, 2)
+    nwarm = 32
+    order = synth.ra_gop(16, (nwarm + steps + 15) // 16 + 1)
+
+    def run_order(submit, n):
+        """submit POC 0 then n pictures of the order: submit(k, poc, ref0, ref1)
+        with picture numbers for the references"""
+        num = {0: 0}
+        submit(0, 0, -1, -1)
+        for k, (poc, r0, r1) in enumerate(order[:n], start=1):
+            submit(k, poc, num[r0], num[r1])
+            num[poc] = k
+
+    cfg = _lib.xin_gpu_stream_cfg(W, H, 64, SEARCH, sum(LEVELS), 0, 1, 1, IN_BD, 1, 1, 2, 32)
     h = C.c_void_p()
     assert lib.xin_gpu_stream_open(C.byref(cfg), C.byref(h)) == 0, lib.xin_gpu_last_error()
     assert lib.xin_gpu_stream_set_contexts(h, ctx.ctypes.data) == 0
     res = _lib.xin_gpu_results()
+    ms, stage = [], np.zeros(4)
+    launches = [0, 0]
 
-    def submit(k):
+    def submit(k, poc, r0, r1):
         pic = _lib.xin_gpu_picture()
-        for i, t in enumerate(dev[k % len(dev)]):
+        for i, t in enumerate(dev[poc % len(dev)]):
             pic.plane[i] = t.data_ptr()
             pic.stride[i] = t.shape[1]
         qp = QPS[k % 3]
         pic.qp, pic.uv_qp, pic.sad_lambda = qp, qp, LAMBDA_BD[qp]
-        assert lib.xin_gpu_frame_submit(h, C.byref(pic)) == 0, lib.xin_gpu_last_error()
+        timed = k > nwarm
+        if timed:
+            flush.fill_(k & 255)
+            torch.cuda.synchronize()
+            if k == nwarm + 1:
+                launches[0] = lib.xin_gpu_kernel_launches()
+        assert lib.xin_gpu_frame_submit_refs(h, C.byref(pic), r0, r1) == 0, lib.xin_gpu_last_error()
         assert lib.xin_gpu_frame_wait(h, C.byref(res), -1) == 0, lib.xin_gpu_last_error()
+        if timed:
+            ms.append(res.gpu_ms)
+            st = (C.c_float * 4)()
+            lib.xin_gpu_stream_stage_ms(h, st)
+            stage[:] += np.array(list(st))
+            launches[1] = lib.xin_gpu_kernel_launches()
 
-    for k in range(1 + max(6, warmup)):      # every (picture set, slot) graph captured
-        submit(k)
-    launches0 = lib.xin_gpu_kernel_launches()
-    ms, stage = [], np.zeros(4)
-    for k in range(steps):
-        flush.fill_(k & 255)
-        torch.cuda.synchronize()
-        submit(10 + k)
-        ms.append(res.gpu_ms)
-        st = (C.c_float * 4)()
-        lib.xin_gpu_stream_stage_ms(h, st)
-        stage += np.array(list(st))
-    launches = (lib.xin_gpu_kernel_launches() - launches0) / steps
+    run_order(submit, nwarm + steps)
     lib.xin_gpu_stream_close(h)
     stage /= steps
-    out = {"workload": "1080p, 8-bit 4:2:0 pictures coded at 10 bits, two references (the previous two pictures): "
-                       "per list the search by resolution levels (+-64) and full sub-pel search, the bi search "
-                       "(target 2 org - other list's prediction, +-4 integer step, sub-pel; averaged-prediction SATD), "
-                       "the choice of list 0 / list 1 / bi by SATD cost, the bi average of 14-bit predictions, then per "
-                       "CU luma DCT2 + MTS 2..5 (CUs up to 32) and chroma DCT2 through dependent quantisation, inverse "
-                       "transform and reconstruction; CU levels 64/32/16/8, TU = CU, QP 27/32/37 cycling",
+    out = {"workload": "1080p, 8-bit 4:2:0 pictures coded at 10 bits, random-access GOP 16 coding order (key pictures "
+                       "from the previous key picture, B pictures from the nearest coded pictures before and after), "
+                       "two references per picture: per list the search by resolution levels (+-64) and full sub-pel "
+                       "search, the bi search (target 2 org - other list's prediction, +-4 integer step, sub-pel; "
+                       "averaged-prediction SATD), the choice of list 0 / list 1 / bi by SATD cost, the bi average of "
+                       "14-bit predictions, then per CU luma DCT2 + MTS 2..5 (CUs up to 32) and chroma DCT2 through "
+                       "dependent quantisation, inverse transform and reconstruction; CU levels 64/32/16/8, TU = CU, "
+                       "QP 27/32/37 cycling",
            "value": W * H * steps / (float(np.sum(ms)) * 1e-3) / 1e6, "unit": "Mpixel/s", "ms_per_picture": float(np.mean(ms)),
+           "pictures_timed": steps, "warmup_pictures": nwarm + 1,
            "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_bi_mc_tu": stage[2], "copies": stage[3]},
-           "gpu_launches_per_picture": launches, "l2": "flushed between pictures (512 MB write outside the timed events)",
-           "not_covered": "DMVR and BCW weights in the frame form (built per call), more than one reference per list, "
-                          "BT/TT CUs, RDOQ, the host's choice among the transform candidates"}
+           "gpu_launches_per_picture": (launches[1] - launches[0]) / steps,
+           "l2": "flushed between pictures (512 MB write outside the timed events)",
+           "not_covered": "the intra key picture (POC 0 is the first reference only), DMVR and BCW weights in the frame "
+                          "form (built per call), more than one reference per list, BT/TT CUs, RDOQ, the host's choice "
+                          "among the transform candidates"}
     from xin26x_gb300.frame import FrameStream
     fs = FrameStream(W, H, search_range=SEARCH, levels=LEVELS, out_q=True, out_rec=False, use_graph=True, bitdepth=BD,
-                     input_bitdepth=IN_BD, search_mode=1, tu_mode=1, contexts=ctx, refs=2)
-    n_e2e = max(steps, 10)
+                     input_bitdepth=IN_BD, search_mode=1, tu_mode=1, contexts=ctx, refs=2, dpb=32)
+    n_e2e = max(steps, 16)
     h2d = W * H * 3 // 2
     d2h = fs.ncus * (64 + 64 + 40) + sum((W * H if p == 0 else W * H // 4) * len(LEVELS) * 4 for p in range(3))
+    t0 = [0.0]
+    inflight = [0]
 
-    def e2e_submit(k):
+    def e2e_submit(k, poc, r0, r1):
+        if k == nwarm + 1:
+            t0[0] = time.perf_counter()
         qp = QPS[k % 3]
-        fs.submit(*frames[k % len(frames)], qp=qp, uv_qp=qp, sad_lambda=LAMBDA_BD[qp])
+        fs.submit(*frames[poc % len(frames)], qp=qp, uv_qp=qp, sad_lambda=LAMBDA_BD[qp], ref0=r0, ref1=r1)
+        inflight[0] += 1
+        if inflight[0] == 2:          # two in flight: collect the older one
+            fs.wait(copy=False)
+            inflight[0] -= 1
 
-    e2e_submit(0)
+    run_order(e2e_submit, nwarm + n_e2e)
     fs.wait(copy=False)
-    e2e_submit(1)
-    for k in range(max(6, warmup)):
-        e2e_submit(k + 2)
-        fs.wait(copy=False)
-    t0 = time.perf_counter()
-    for k in range(n_e2e):
-        e2e_submit(k + 2 + max(6, warmup))
-        fs.wait(copy=False)
-    el = time.perf_counter() - t0
-    fs.wait(copy=False)
+    el = time.perf_counter() - t0[0]
     fs.close()
     out["e2e_two_in_flight"] = {"value": W * H * n_e2e / el / 1e6, "unit": "Mpixel/s", "pictures": n_e2e,
                                 "ms_per_picture": el * 1e3 / n_e2e, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                                 "note": "host 8-bit planes in, CU, bi and transform-candidate records and coefficient "
-                                        "planes out; wall clock over the pictures"}
+                                        "planes out; wall clock over the pictures (the last collected inside)"}
     return out
 
 

@@ -518,6 +518,13 @@ typedef struct xin_gpu_stream_cfg {
                                     SATD (pfXinComputeAvgSatd); the TU stage takes the coded
                                     prediction, and its satd_cost the coded MVs' bits.  CU levels up
                                     to 64. */
+    int32_t  dpb;                /* pictures kept as references: 0 = refs + 1 (the previous one or
+                                    two), up to 32.  Picture k occupies slot k % dpb, so a picture
+                                    may reference any of the dpb - 1 pictures submitted before it
+                                    (xin_gpu_frame_submit_refs): the random-access GOP structures
+                                    (in GOP 16 coding order a B picture reaches up to 20 submissions
+                                    back: dpb 21 or more; 32 repeats the graph pattern every two
+                                    GOPs). */
 } xin_gpu_stream_cfg;
 
 typedef struct xin_gpu_picture {
@@ -577,6 +584,13 @@ int  xin_gpu_stream_num_levels(const xin_gpu_stream *s);
  * be in flight (the next one's upload and kernels overlap the previous one's
  * result copies); a third submit before a frame_wait is XIN_GPU_ERR_STATE. */
 int  xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic);
+/* The same with the references named: ref0 (list 0) and ref1 (list 1, refs 2)
+ * are picture numbers (0 = the stream's first submitted picture) of earlier
+ * pictures at most dpb - 1 submissions back; -1 takes the default (the previous
+ * picture for list 0, the one before it for list 1).  For a random-access GOP
+ * the encoder submits in coding order and names each B picture's past and
+ * future references.  XIN_GPU_ERR_ARG when a reference is out of reach. */
+int  xin_gpu_frame_submit_refs(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_t ref0, int32_t ref1);
 /* Wait for the oldest picture in flight (bounded by timeout_ms; < 0 waits
  * without limit) and copy its results into the caller's buffers.  Members of res
  * left NULL receive views of the stream's pinned result buffers instead, valid

@@ -408,6 +408,55 @@ def test_frame_bi_matches_oracle(bd, inb, search_mode, w, h, R):
     assert dirs[0] == 0 and dirs[3] > 0 and dirs[1] + dirs[2] > 0, dirs   # both kinds of choice occur
 
 
+@pytest.mark.parametrize("bd,inb,search_mode,tu_mode", [(8, 0, 0, 0), (10, 8, 1, 1)])
+def test_frame_random_access_gop_matches_oracle(bd, inb, search_mode, tu_mode):
+    """Two GOPs of 8 in random-access coding order (synth.ra_gop) with the
+    references named per picture (xin_gpu_frame_submit_refs; dpb 12, the least
+    that two GOPs of 8 need -- picture 12, POC 9, reaches back to picture 1, POC 8): key pictures from the previous key
+    picture, B pictures from their past and future references.  Selected
+    pictures of both GOPs against the oracle with those references; references
+    out of reach are refused."""
+    from xin26x_gb300 import synth as S
+    from xin26x_gb300.frame import BI_DTYPE
+    w, h, R = 192, 128, 16
+    ctx = S.contexts(np.random.default_rng(5), 1)[0] if tu_mode else None
+    seq = synth.sequence(w, h, 17, seed=w + 17 + bd, bitdepth=8 if inb == 8 else bd, objects=3)
+    order = S.ra_gop(8, 2)
+    fs = FrameStream(w, h, search_range=R, out_q=True, out_rec=True, bitdepth=bd, input_bitdepth=inb,
+                     search_mode=search_mode, tu_mode=tu_mode, contexts=ctx, refs=2, dpb=12)
+    num = {0: 0}                     # POC -> picture number (submit order)
+    try:
+        fs.submit(*seq[0], qp=27, uv_qp=27, sad_lambda=64)
+        fs.wait()
+        for n, (poc, r0, r1) in enumerate(order, start=1):
+            qp, lam = (27, 32, 37)[n % 3], (40 + 5 * n) << (2 if inb == 8 else 0)
+            fs.submit(*seq[poc], qp=qp, uv_qp=qp, sad_lambda=lam, ref0=num[r0], ref1=num[r1])
+            num[poc] = n
+            out = fs.wait()
+            if poc not in (8, 2, 5, 16, 12, 15):
+                continue
+            cur, p0, p1 = seq[poc], seq[r0], seq[r1]
+            if inb == 8:
+                cur, p0, p1 = [tuple(p.astype(np.uint16) << 2 for p in f) for f in (cur, p0, p1)]
+            want = oracle_frame.run(cur, p0, fs.levels, search_range=R, qp=qp, uv_qp=qp, sad_lambda=lam, bitdepth=bd,
+                                    threads=0, search_mode=search_mode, tu_mode=tu_mode, contexts=ctx, ref1=p1)
+            label = ("ra", bd, inb, search_mode, tu_mode, poc)
+            _compare(out, want[:3], fs.levels, label)
+            if tu_mode:
+                for name in ("satd_cost", "ncand", "nz", "ssd"):
+                    bad = np.nonzero(np.any((out["mts"][name] != want[3][name]).reshape(len(out["mts"]), -1), axis=1))[0]
+                    assert bad.size == 0, (label, name, bad[:5])
+            for name in BI_DTYPE.names:
+                bad = np.nonzero(np.any((out["bi"][name] != want[-1][name]).reshape(len(out["bi"]), -1), axis=1))[0]
+                assert bad.size == 0, (label, name, bad[:5], out["bi"][bad[:5]], want[-1][bad[:5]])
+        # 17 pictures submitted: picture 17 may reach back to picture 6 (dpb 12), not further
+        for r0, r1 in ((5, 16), (16, 17), (16, 5)):
+            with pytest.raises(RuntimeError, match="out of reach"):
+                fs.submit(*seq[1], qp=32, uv_qp=32, sad_lambda=64, ref0=r0, ref1=r1)
+    finally:
+        fs.close()
+
+
 def test_frame_bi_needs_levels_up_to_64():
     """refs 2 is refused with the 128 x 128 level, and more than two references."""
     for kw in ({"ctu": 128, "search_mode": 1, "levels": (128, 64), "refs": 2}, {"refs": 3}):

@@ -20,7 +20,7 @@ i32, u32, u64, ip, vp = C.c_int32, C.c_uint32, C.c_uint64, C.c_ssize_t, C.c_void
 class xin_gpu_stream_cfg(C.Structure):
     _fields_ = [("width", i32), ("height", i32), ("ctu_size", i32), ("search_range", i32),
                 ("level_mask", u32), ("out_flags", u32), ("use_graph", i32), ("device_io", i32),
-                ("input_bitdepth", i32), ("search_mode", i32), ("tu_mode", i32), ("refs", i32)]
+                ("input_bitdepth", i32), ("search_mode", i32), ("tu_mode", i32), ("refs", i32), ("dpb", i32)]
 
 
 class xin_gpu_picture(C.Structure):
@@ -133,6 +133,7 @@ SIGNATURES = {
     "xin_gpu_stream_num_levels": ([vp], C.c_int),
     "xin_gpu_stream_level_info": ([vp, C.c_int, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], C.c_int),
     "xin_gpu_frame_submit": ([vp, C.POINTER(xin_gpu_picture)], C.c_int),
+    "xin_gpu_frame_submit_refs": ([vp, C.POINTER(xin_gpu_picture), i32, i32], C.c_int),
     "xin_gpu_frame_wait": ([vp, C.POINTER(xin_gpu_results), i32], C.c_int),
     "xin_gpu_stream_stage_ms": ([vp, C.POINTER(C.c_float)], C.c_int),
     "xin_gpu_stream_set_wait_tries": ([vp, C.c_int64], C.c_int),

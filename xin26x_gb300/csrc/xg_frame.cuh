@@ -9,6 +9,7 @@
 #include <chrono>
 #include <new>
 #include <string.h>
+#include <map>
 #include <mutex>
 #include <thread>
 
@@ -19,25 +20,31 @@ static const int XG_LEVEL_SIZE[XG_NLEV] = { 64, 32, 16, 8, 128 };
 
 struct XgTuState;   /* the preset-4 TU stage (xg_tu.cuh) */
 
+#define XG_MAX_DPB 32      /* picture slots a stream may keep */
+/* captured graphs a stream keeps: one per (picture set, slot, list-0 slot, list-1
+ * slot) met; beyond this the launches of a new combination run directly */
+#define XG_MAX_GRAPHS 72
+
 struct xin_gpu_stream {
     xin_gpu_stream_cfg cfg;
     int pad, pitch, cpad, cpitch, rows, crows;
     int lev_on[XG_NLEV], lev_first[XG_NLEV], lev_cx[XG_NLEV], lev_cy[XG_NLEV];
     int nlev, ncus;
     size_t plane_elems, cplane_elems;
-    /* picture slots: picture k fills slot k % nslots; list 0 is the slot before it,
-     * list 1 (refs 2) the one before that */
+    /* picture slots: picture k fills slot k % nslots; its references are the
+     * slots of earlier pictures at most nslots - 1 back (by default list 0 the
+     * previous picture, list 1 the one before) */
     int nslots;
-    xg_pix *slot_base[3][3];
-    XgPlane slot[3][3];
-    xg_pix *qpel_base[3];
-    XgQpel qpel[3];
+    xg_pix *slot_base[XG_MAX_DPB][3];
+    XgPlane slot[XG_MAX_DPB][3];
+    xg_pix *qpel_base[XG_MAX_DPB];
+    XgQpel qpel[XG_MAX_DPB];
     /* search_mode 1: luma at 1/2 and 1/4 resolution of each slot, downscaled from
      * the padded slot as a whole (the margins included) */
-    xg_pix *lo_base[3][2];
-    XgPlane lo[3][2];
+    xg_pix *lo_base[XG_MAX_DPB][2];
+    XgPlane lo[XG_MAX_DPB][2];
     int lo_pitch[2], lo_rows[2];
-    CUtensorMap tm_qp[3];              /* TMA map of each slot's padded luma plane: quarter-pel tiles */
+    CUtensorMap tm_qp[XG_MAX_DPB];     /* TMA map of each slot's padded luma plane: quarter-pel tiles */
     long long wait_tries;  /* bound of the kernels' waits (polls) */
     unsigned long long *keys;
     unsigned long long *keys1;         /* refs 2: list 1's integer search */
@@ -74,7 +81,8 @@ struct xin_gpu_stream {
     cudaStream_t aux[XG_NLEV - 1];   /* the tails of levels 2..5 run beside the first level's */
     cudaStream_t auxq;     /* quarter-pel planes of the new picture, beside the search (low priority) */
     cudaEvent_t ev_fork, ev_join[XG_NLEV - 1], ev_qfork, ev_qjoin;
-    cudaGraphExec_t gexec[2][3];   /* by picture set and slot */
+    /* captured graphs by (picture set, slot, list-0 slot, list-1 slot) */
+    std::map<uint32_t, std::pair<cudaGraphExec_t, int>> graphs;   /* exec, kernels inside */
     int me_bands, me_band_rows, me_band_rows_alloc, me_row_words, me_nb;
     size_t me_smem;
     int sbd;               /* sample depth the integer search runs at (8 or 10) */
@@ -82,7 +90,6 @@ struct xin_gpu_stream {
     size_t in_es;          /* bytes per input sample */
     int nsub;              /* pictures submitted */
     int ndone;             /* pictures collected by frame_wait (the oldest first) */
-    int graph_launches[2][3]; /* kernels inside each captured graph */
     XgTuState *tu[2];      /* tu_mode 1: per picture set */
 };
 
@@ -115,10 +122,9 @@ static int xg_stream_free(xin_gpu_stream *s)
     if (s->st) cudaStreamSynchronize(s->st);
     for (auto &t : s->set) if (t.pst) cudaStreamSynchronize(t.pst);
     if (s->cst) cudaStreamSynchronize(s->cst);
-    for (int i = 0; i < 2; i++)
-        for (int j = 0; j < 3; j++)
-            if (s->gexec[i][j]) cudaGraphExecDestroy(s->gexec[i][j]);
-    for (int i = 0; i < 3; i++) {
+    for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.first);
+    s->graphs.clear();
+    for (int i = 0; i < XG_MAX_DPB; i++) {
         for (int p = 0; p < 3; p++) cudaFree(s->slot_base[i][p]);
         cudaFree(s->qpel_base[i]);
         for (int l = 0; l < 2; l++) cudaFree(s->lo_base[i][l]);
@@ -180,10 +186,10 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         !(c.level_mask & (8u | 16u | 32u | 64u | 128u)) || (c.level_mask & ~(8u | 16u | 32u | 64u | 128u)) ||
         !xg_input_depth_ok(c) || (c.search_mode != 0 && c.search_mode != 1) || (c.tu_mode != 0 && c.tu_mode != 1) ||
         ((c.level_mask & 128u) && (c.ctu_size != 128 || c.search_mode != 1 || c.tu_mode != 0)) || c.refs < 0 || c.refs > 2 ||
-        (c.refs == 2 && (c.level_mask & 128u))) {
+        (c.refs == 2 && (c.level_mask & 128u)) || c.dpb < 0 || c.dpb > XG_MAX_DPB || (c.dpb && c.dpb < (c.refs == 2 ? 3 : 2))) {
         xg_set_error(XIN_GPU_ERR_ARG, "stream_open: unsupported size, CTU, search range, level mask, input bit depth, search or "
                                       "TU mode, or references (the 128 x 128 level needs CTU 128, the search by levels and TU "
-                                      "mode 0; two references need CU levels up to 64)");
+                                      "mode 0; two references need CU levels up to 64; dpb 0 or refs + 1 .. 32)");
         return XIN_GPU_ERR_ARG;
     }
     xin_gpu_stream *s = new (std::nothrow) xin_gpu_stream();
@@ -192,7 +198,7 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     s->widen = XG_BITDEPTH == 10 && c.input_bitdepth == 8;
     s->sbd = s->widen ? 8 : XG_BITDEPTH;
     s->in_es = s->widen ? 1 : sizeof(xg_pix);
-    s->nslots = c.refs == 2 ? 3 : 2;
+    s->nslots = c.dpb ? c.dpb : (c.refs == 2 ? 3 : 2);
     /* margin: the reference pads ctu + 16; the tile search also reads R + 64 + 8 around full tiles */
     int pad = c.ctu_size + 16 > c.search_range + 72 ? c.ctu_size + 16 : c.search_range + 72;
     pad = (pad + 31) & ~31;
@@ -671,7 +677,10 @@ static void xg_enqueue_results(xin_gpu_stream *s, xin_gpu_stream::Set &t, bool w
     cudaEventRecord(t.ev1, s->cst);
 }
 
-extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic)
+extern "C" int xin_gpu_frame_submit_refs(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_t ref0, int32_t ref1);
+extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic) { return xin_gpu_frame_submit_refs(s, pic, -1, -1); }
+
+extern "C" int xin_gpu_frame_submit_refs(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_t ref0, int32_t ref1)
 {
     xin_gpu_clear_error();
     (void)cudaGetLastError();   /* errors of earlier, unrelated calls are not this picture's */
@@ -684,11 +693,17 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
     if (pic->qp < 0 || pic->qp > 63 || pic->uv_qp < 0 || pic->uv_qp > 63) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: QP out of range"); return XIN_GPU_ERR_ARG; }
     /* the search packs (cost << 2 | row) into 32 bits: costs must stay below 2^29 */
     if (pic->sad_lambda > (1u << 20)) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: sad_lambda above 2^20"); return XIN_GPU_ERR_ARG; }
-    /* picture set (in-flight resources) and slots: the picture's own, list 0 = the
-     * previous picture's, list 1 = the one before (the previous one again for the
-     * second picture) */
-    const int set = s->nsub & 1, ns = s->nslots;
-    const int cur = s->nsub % ns, l0 = (s->nsub + ns - 1) % ns, l1 = s->nsub >= 2 ? (s->nsub + ns - 2) % ns : l0;
+    /* picture set (in-flight resources) and slots: the picture's own, and its
+     * references' -- named, or list 0 = the previous picture and list 1 = the one
+     * before (the previous one again for the second picture) */
+    const int set = s->nsub & 1, ns = s->nslots, k = s->nsub;
+    if (ref0 < 0) ref0 = k - 1;
+    if (ref1 < 0) ref1 = k >= 2 ? k - 2 : k - 1;
+    if (k > 0 && (ref0 >= k || ref1 >= k || k - ref0 > ns - 1 || (c.refs == 2 && k - ref1 > ns - 1))) {
+        xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: reference pictures %d, %d out of reach of picture %d (dpb %d)", ref0, ref1, k, ns);
+        return XIN_GPU_ERR_ARG;
+    }
+    const int cur = k % ns, l0 = k > 0 ? ref0 % ns : 0, l1 = c.refs == 2 && k > 0 ? ref1 % ns : l0;
     xin_gpu_stream::Set &t = s->set[set];
     /* set `set` was last used by picture nsub - 2, already collected by frame_wait
      * (at most two in flight), so its staging is free */
@@ -738,22 +753,24 @@ extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pi
         }
     cudaEventRecord(t.ev_up, s->ust);
     cudaStreamWaitEvent(t.pst, t.ev_up, 0);
-    /* a graph per (set, slot): its slots fix both references once the stream has
-     * two pictures behind it (before that, with two references, the launches run
-     * directly) */
-    if (with_me && c.use_graph && (c.refs != 2 || s->nsub >= 2)) {
-        cudaGraphExec_t &gx = s->gexec[set][cur];
-        if (!gx) {
+    /* a graph per (set, slot, list-0 slot, list-1 slot): the launches bake in the
+     * slots' planes */
+    const uint32_t gkey = ((uint32_t)set << 15) | ((uint32_t)cur << 10) | ((uint32_t)l0 << 5) | (uint32_t)l1;
+    auto git = s->graphs.find(gkey);
+    if (with_me && c.use_graph && (git != s->graphs.end() || (int)s->graphs.size() < XG_MAX_GRAPHS)) {
+        if (git == s->graphs.end()) {
             cudaGraph_t g;
+            cudaGraphExec_t gx = nullptr;
             if (xg_cuda_check(cudaStreamBeginCapture(t.pst, cudaStreamCaptureModeThreadLocal), "begin capture")) return XIN_GPU_ERR_CUDA;
-            s->graph_launches[set][cur] = xg_enqueue_picture(s, set, cur, l0, l1, true, true);
+            const int n = xg_enqueue_picture(s, set, cur, l0, l1, true, true);
             if (xg_cuda_check(cudaStreamEndCapture(t.pst, &g), "end capture")) return XIN_GPU_ERR_CUDA;
             cudaError_t e = cudaGraphInstantiate(&gx, g, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(g);
             if (xg_cuda_check(e, "graph instantiate")) return XIN_GPU_ERR_CUDA;
+            git = s->graphs.emplace(gkey, std::make_pair(gx, n)).first;
         }
-        if (xg_cuda_check(cudaGraphLaunch(gx, t.pst), "graph launch")) return XIN_GPU_ERR_CUDA;
-        xg_count_launch((uint64_t)s->graph_launches[set][cur]);
+        if (xg_cuda_check(cudaGraphLaunch(git->second.first, t.pst), "graph launch")) return XIN_GPU_ERR_CUDA;
+        xg_count_launch((uint64_t)git->second.second);
     } else {
         xg_count_launch((uint64_t)xg_enqueue_picture(s, set, cur, l0, l1, with_me, false));
     }
@@ -828,9 +845,8 @@ extern "C" int xin_gpu_stream_set_wait_tries(xin_gpu_stream *s, int64_t tries)
     if (s->nsub != s->ndone) { xg_set_error(XIN_GPU_ERR_STATE, "stream_set_wait_tries: pictures in flight"); return XIN_GPU_ERR_STATE; }
     s->wait_tries = tries < 0 ? XG_TMA_WAIT_TRIES : tries;
     /* the bound is a parameter of the captured graphs: capture them again */
-    for (int i = 0; i < 2; i++)
-        for (int j = 0; j < 3; j++)
-            if (s->gexec[i][j]) { cudaGraphExecDestroy(s->gexec[i][j]); s->gexec[i][j] = nullptr; }
+    for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.first);
+    s->graphs.clear();
     return XIN_GPU_OK;
 }
 

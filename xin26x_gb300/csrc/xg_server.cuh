@@ -32,7 +32,7 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
         ((c->level_mask & 128u) && (c->ctu_size != 128 || c->search_mode != 1 || c->tu_mode != 0)) ||
         !xg_input_depth_ok(*c) || (c->search_mode != 0 && c->search_mode != 1) ||
         (c->tu_mode != 0 && c->tu_mode != 1) || c->refs < 0 || c->refs > 2 ||
-        (c->refs == 2 && (c->level_mask & 128u)))
+        (c->refs == 2 && (c->level_mask & 128u)) || c->dpb < 0 || c->dpb > XG_MAX_DPB || (c->dpb && c->dpb < (c->refs == 2 ? 3 : 2)))
         return XIN_GPU_ERR_ARG;
     const bool widen = XG_BITDEPTH == 10 && c->input_bitdepth == 8;
     const uint64_t in_es = widen ? 1 : sizeof(xg_pix);
@@ -49,9 +49,9 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
             nlev++;
             ncus += (uint64_t)(c->width / XG_LEVEL_SIZE[L]) * (c->height / XG_LEVEL_SIZE[L]);
         }
-    /* two picture slots (three with two references) with their quarter-pel planes,
+    /* the picture slots (two; three with two references; dpb when set) with their quarter-pel planes,
      * the search keys, and two picture sets (results, parameters, pinned staging) */
-    const uint64_t nslots = c->refs == 2 ? 3 : 2;
+    const uint64_t nslots = c->dpb ? c->dpb : (c->refs == 2 ? 3 : 2);
     uint64_t d = nslots * (ysz + 2 * csz) + nslots * 16 * ysz + 8 * (ncus ? ncus : 1) +
                  2 * (sizeof(xin_gpu_cu_result) * ncus + sizeof(XgPicParams) + (lq + 2 * lc) * nlev * (sizeof(xg_coef) + sizeof(xg_pix)));
     if (c->refs == 2) d += 8 * (ncus ? ncus : 1) + 2 * sizeof(xin_gpu_cu_bi) * ncus;   /* list 1's keys, bi records */

@@ -28,13 +28,14 @@ class FrameStream:
     def __init__(self, width: int, height: int, ctu: int = 64, search_range: int = 64,
                  levels=(64, 32, 16, 8), out_q: bool = True, out_rec: bool = False, use_graph: bool = True,
                  bitdepth: int = 8, device: int = 0, input_bitdepth: int = 0, search_mode: int = 0,
-                 tu_mode: int = 0, contexts=None, refs: int = 1):
+                 tu_mode: int = 0, contexts=None, refs: int = 1, dpb: int = 0):
         """bitdepth: the library (8 or 10, the reference's ENABLE_10BIT_ENCODER);
         input_bitdepth 8 with bitdepth 10: 8-bit pictures coded at 10 bits;
         search_mode 0 exhaustive integer search, 1 by resolution levels;
         tu_mode 1 the preset-4 TU work (transform candidates with dependent
         quantisation), contexts its CABAC context set (synth.PROB_DTYPE records);
-        refs 2: two references (the previous two pictures) with the bi search."""
+        refs 2: two references (by default the previous two pictures) with the bi
+        search; dpb: pictures kept as references (0 = refs + 1, up to 32)."""
         self.lib = _lib.load(bitdepth)
         self.bitdepth = bitdepth
         self.in_pix = np.uint8 if (bitdepth == 8 or input_bitdepth == 8) else np.uint16
@@ -47,7 +48,7 @@ class FrameStream:
             mask |= int(s)
         self.cfg = _lib.xin_gpu_stream_cfg(width, height, ctu, search_range, mask,
                                            (OUT_Q if out_q else 0) | (OUT_REC if out_rec else 0), 1 if use_graph else 0,
-                                           0, input_bitdepth, search_mode, tu_mode, refs)
+                                           0, input_bitdepth, search_mode, tu_mode, refs, dpb)
         h = C.c_void_p()
         st = self.lib.xin_gpu_stream_open(C.byref(self.cfg), C.byref(h))
         if st != 0:
@@ -68,14 +69,16 @@ class FrameStream:
             if self.lib.xin_gpu_stream_set_contexts(h, ctx.ctypes.data) != 0:
                 raise RuntimeError("xin_gpu_stream_set_contexts: " + self.lib.xin_gpu_last_error().decode())
 
-    def submit(self, y, u, v, qp: int = 32, uv_qp: int = 32, sad_lambda: int = 64) -> None:
+    def submit(self, y, u, v, qp: int = 32, uv_qp: int = 32, sad_lambda: int = 64, ref0: int = -1, ref1: int = -1) -> None:
+        """ref0 / ref1: picture numbers of the references (-1: the previous picture,
+        the one before)."""
         planes = [np.ascontiguousarray(p, dtype=self.in_pix) for p in (y, u, v)]
         pic = _lib.xin_gpu_picture()
         for i, p in enumerate(planes):
             pic.plane[i] = p.ctypes.data
             pic.stride[i] = p.shape[1]
         pic.qp, pic.uv_qp, pic.sad_lambda = qp, uv_qp, sad_lambda
-        st = self.lib.xin_gpu_frame_submit(self.h, C.byref(pic))
+        st = self.lib.xin_gpu_frame_submit_refs(self.h, C.byref(pic), ref0, ref1)
         if st != 0:
             raise RuntimeError(f"xin_gpu_frame_submit ({st}): " + self.lib.xin_gpu_last_error().decode())
 

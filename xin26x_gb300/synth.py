@@ -223,3 +223,27 @@ def dq_steps(blocks, t, bitdepth: int) -> np.ndarray:
         hit = np.nonzero(v > thr)[0]
         out[i] = hit[-1] + 1 if hit.size else 0
     return out
+
+def ra_gop(gop: int, ngops: int):
+    """Random-access coding order of ngops GOPs of size gop (a power of two)
+    after picture 0: a list of (poc, ref0_poc, ref1_poc).  Each GOP codes its
+    key picture (both references the previous key picture), then the pictures
+    between, halving: a B picture's list 0 is the nearest coded picture before
+    it and list 1 the nearest after it (the hierarchy of the reference's
+    random-access GOP)."""
+    out = []
+    for gi in range(ngops):
+        base = gi * gop
+        key = base + gop
+        out.append((key, base, base))
+
+        def split(lo, hi):
+            if hi - lo < 2:
+                return
+            mid = (lo + hi) // 2
+            out.append((mid, lo, hi))
+            split(lo, mid)
+            split(mid, hi)
+
+        split(base, key)
+    return out
