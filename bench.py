@@ -262,6 +262,20 @@ def run_gpu(args):
     for k in range(1, args.warmup + 1):
         submit_dev(k)
         lib.xin_gpu_frame_wait(h, C.byref(res), -1)
+    # the search's geometry (band count per tile) chosen by the library's autotuner
+    # on the last warm-up picture; two more warm-up pictures capture the graphs again
+    tune_bands, tune_ms = C.c_int32(), (C.c_float * 2)()
+    assert lib.xin_gpu_stream_tune_search(h, C.byref(tune_bands), tune_ms) == 0, lib.xin_gpu_last_error()
+    tn, tb, tm = C.c_int32(), (C.c_int32 * 6)(), (C.c_float * 6)()
+    lib.xin_gpu_stream_tune_table(h, C.byref(tn), tb, tm)
+    search_tuning = {"bands": tune_bands.value, "search_ms_default_geometry": tune_ms[0],
+                     "timed": {str(tb[i]): round(float(tm[i]), 4) for i in range(tn.value)},
+                     "search_ms_chosen": tune_ms[1], "candidates": "default band count and x1/2, x2, x3, x4, x6 of it",
+                     "note": "xin_gpu_stream_tune_search: CUDA-event time of the search of the last warm-up picture "
+                             "per geometry (one warm-up, three timed launches each); results do not depend on it"}
+    for k in range(args.warmup + 1, args.warmup + 3):
+        submit_dev(k)
+        lib.xin_gpu_frame_wait(h, C.byref(res), -1)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -314,13 +328,17 @@ def run_gpu(args):
         e2e_fs.submit(*frames[k % len(frames)], qp=qp, uv_qp=qp, sad_lambda=LAMBDA_BD[qp])
 
     e2e_submit(1)
+    e2e_fs.wait(copy=False)
+    pending.pop(0)
+    assert e2e_fs.lib.xin_gpu_stream_tune_search(e2e_fs.h, None, None) == 0, e2e_fs.lib.xin_gpu_last_error()
+    e2e_submit(2)
     for k in range(args.warmup):
-        e2e_submit(k + 2)
+        e2e_submit(k + 3)
         e2e_fs.wait(copy=False)
         pending.pop(0)
     t0 = time.perf_counter()
     for k in range(args.steps):
-        e2e_submit(args.warmup + k + 2)
+        e2e_submit(args.warmup + k + 3)
         e2e_fs.wait(copy=False)
         lat.append((time.perf_counter() - pending.pop(0)) * 1e3)
     e2e_s = time.perf_counter() - t0
@@ -364,6 +382,7 @@ def run_gpu(args):
                "data": "synthetic (seeded texture + 4 moving rectangles, 1920x1080 4:2:0)",
                "config": workload_config(),
                "stage_ms": {"prep": stage[0], "integer_search": stage[1], "subpel_mc_tq": stage[2], "copies": stage[3]},
+               "search_tuning": search_tuning,
                "roofline": {"bound": "int", "kernel": "k_me_tiles<8> (8-bit samples, SADs x 4)", "achieved": achieved / 1e12,
                             "peak": peak.value / 1e12,
                             "unit": "Tabsdiff/s", "frac": achieved / peak.value, "traffic": ME_DRAM_BYTES,

@@ -579,6 +579,18 @@ int  xin_gpu_stream_num_cus(const xin_gpu_stream *s);             /* CUs per pic
 int  xin_gpu_stream_level_info(const xin_gpu_stream *s, int level, int32_t *size, int32_t *first_cu,
                                int32_t *cus_x, int32_t *cus_y);      /* level 0 = largest size */
 int  xin_gpu_stream_num_levels(const xin_gpu_stream *s);
+/* Autotune the exhaustive search's geometry (search_mode 0): the number of
+ * candidate-row bands per 64 x 64 tile, which sets the CTAs of a launch, the
+ * reference rows each CTA stages in shared memory and the buffered passes of
+ * the 32 x 32 / 64 x 64 sums.  Times the search of the last picture against
+ * its reference for the stream's default and up to five other band counts,
+ * keeps the fastest for later pictures and re-captures the graphs.  The search
+ * results do not depend on the geometry.  Call between pictures, after at
+ * least two submitted and none in flight; bands = the chosen count, ms[0] /
+ * ms[1] = the default's and the chosen geometry's search time (ms). */
+int  xin_gpu_stream_tune_search(xin_gpu_stream *s, int32_t *bands, float ms[2]);
+/* the geometries the last tune_search timed (n <= 6): band counts and search times (ms) */
+int  xin_gpu_stream_tune_table(const xin_gpu_stream *s, int32_t *n, int32_t bands[6], float ms[6]);
 /* Upload a picture and queue its hot path (asynchronous).  The first picture of
  * a stream only becomes the reference (no CU results).  Up to two pictures may
  * be in flight (the next one's upload and kernels overlap the previous one's

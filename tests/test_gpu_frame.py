@@ -457,6 +457,36 @@ def test_frame_random_access_gop_matches_oracle(bd, inb, search_mode, tu_mode):
         fs.close()
 
 
+@pytest.mark.parametrize("bd,inb,R", [(8, 0, 64), (10, 8, 24)])
+def test_frame_search_tuning_keeps_results(bd, inb, R):
+    """xin_gpu_stream_tune_search: the geometry it picks (timed on the last
+    picture) changes no result -- pictures after the tuning equal those of an
+    untuned stream on the same input, every record and plane."""
+    import ctypes as C
+    w, h = 416, 240
+    seq = synth.sequence(w, h, 5, seed=99 + bd, bitdepth=8 if inb == 8 else bd, objects=2)
+    outs = []
+    for tune in (False, True):
+        fs = FrameStream(w, h, search_range=R, out_q=True, out_rec=True, bitdepth=bd, input_bitdepth=inb)
+        try:
+            got = []
+            for k in range(5):
+                fs.submit(*seq[k], qp=32, uv_qp=32, sad_lambda=64 << (2 if inb == 8 else 0))
+                got.append(fs.wait())
+                if tune and k == 1:
+                    bands, ms = C.c_int32(), (C.c_float * 2)()
+                    assert fs.lib.xin_gpu_stream_tune_search(fs.h, C.byref(bands), ms) == 0, fs.lib.xin_gpu_last_error()
+                    assert bands.value >= 1 and ms[0] > 0 and 0 < ms[1] <= ms[0]
+            outs.append(got)
+        finally:
+            fs.close()
+    for k in range(2, 5):
+        a, b = outs[0][k], outs[1][k]
+        assert np.array_equal(a["cu"], b["cu"]), k
+        for p in range(3):
+            assert np.array_equal(a["q"][p], b["q"][p]) and np.array_equal(a["rec"][p], b["rec"][p]), (k, p)
+
+
 def test_frame_bi_needs_levels_up_to_64():
     """refs 2 is refused with the 128 x 128 level, and more than two references."""
     for kw in ({"ctu": 128, "search_mode": 1, "levels": (128, 64), "refs": 2}, {"refs": 3}):

@@ -91,6 +91,9 @@ struct xin_gpu_stream {
     int nsub;              /* pictures submitted */
     int ndone;             /* pictures collected by frame_wait (the oldest first) */
     XgTuState *tu[2];      /* tu_mode 1: per picture set */
+    int tune_n;            /* the last xin_gpu_stream_tune_search: geometries timed */
+    int32_t tune_bands[6];
+    float tune_ms[6];
 };
 
 static int xg_tu_open(xin_gpu_stream *s, int set);
@@ -161,6 +164,42 @@ static int xg_stream_free(xin_gpu_stream *s)
     if (s->st) cudaStreamDestroy(s->st);
     delete s;
     return XIN_GPU_OK;
+}
+
+/* integer-search band geometry from a starting number of candidate-row bands
+ * per 64 x 64 tile (more bands: more CTAs, less reuse of each staged row):
+ * shared memory within XG_ME_SMEM_MAX, taking more bands or fewer buffered
+ * passes for the 32x32 / 64x64 sums (more barriers) when it does not fit;
+ * false when no geometry fits */
+static bool xg_me_geometry(xin_gpu_stream *s, int bands)
+{
+    const xin_gpu_stream_cfg &c = s->cfg;
+    const int R = c.search_range, ndy = 2 * R + 1;
+    if (bands < 1) bands = 1;
+    if (bands > ndy) bands = ndy;
+    {
+        /* word positions per band row; pitch congruent to nx (mod 32) */
+        int nx = 2 * R + 1, relw = xg_me_relw(s->sbd, nx);
+        s->me_row_words = relw + (((nx - relw) % 32) + 32) % 32;
+    }
+    for (;;) {
+        s->me_band_rows = (ndy + bands - 1) / bands;
+        const int dr = xg_me_d(s->sbd);
+        int rows_rounded = (s->me_band_rows + dr - 1) / dr * dr;   /* rounded up to the per-lane chunk */
+        s->me_band_rows_alloc = 64 + rows_rounded - 1;
+        size_t fixed = (size_t)s->me_band_rows_alloc * s->me_row_words + (2 * R + 1) + s->me_band_rows_alloc + xg_me_cur_words(s->sbd);
+        s->me_nb = 0;
+        for (int nb = XG_ME_NB_MAX; nb >= 1 && !s->me_nb; nb /= 2)
+            if (sizeof(uint32_t) * (fixed + xg_me_agg_words(s->sbd, nb)) <= XG_ME_SMEM_MAX) s->me_nb = nb;
+        if (s->me_nb) {
+            s->me_smem = sizeof(uint32_t) * (fixed + xg_me_agg_words(s->sbd, s->me_nb));
+            break;
+        }
+        if (s->me_band_rows == 1) return false;
+        bands++;
+    }
+    s->me_bands = (ndy + s->me_band_rows - 1) / s->me_band_rows;
+    return true;
 }
 
 /* input_bitdepth: 0 or the library's depth, or 8 in the 10-bit library */
@@ -333,37 +372,12 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     /* integer-search band geometry: enough CTAs for the GPU; shared memory within
      * XG_ME_SMEM_MAX, taking more bands (less reuse of staged rows) or fewer
      * buffered passes for the 32x32 / 64x64 sums (more barriers) when it does not fit */
-    int R = c.search_range, ndy = 2 * R + 1;
     int tiles = ((c.width + 63) / 64) * ((c.height + 63) / 64);
-    int bands = (4 * 152 + tiles - 1) / tiles;
-    if (bands < 1) bands = 1;
-    if (bands > ndy) bands = ndy;
-    {
-        /* word positions per band row; pitch congruent to nx (mod 32) */
-        int nx = 2 * R + 1, relw = xg_me_relw(s->sbd, nx);
-        s->me_row_words = relw + (((nx - relw) % 32) + 32) % 32;
+    if (!xg_me_geometry(s, (4 * 152 + tiles - 1) / tiles)) {
+        xg_set_error(XIN_GPU_ERR_ARG, "stream_open: search range %d needs more shared memory than a CTA has", c.search_range);
+        xg_stream_free(s);
+        return XIN_GPU_ERR_ARG;
     }
-    for (;;) {
-        s->me_band_rows = (ndy + bands - 1) / bands;
-        const int dr = xg_me_d(s->sbd);
-        int rows_rounded = (s->me_band_rows + dr - 1) / dr * dr;   /* rounded up to the per-lane chunk */
-        s->me_band_rows_alloc = 64 + rows_rounded - 1;
-        size_t fixed = (size_t)s->me_band_rows_alloc * s->me_row_words + (2 * R + 1) + s->me_band_rows_alloc + xg_me_cur_words(s->sbd);
-        s->me_nb = 0;
-        for (int nb = XG_ME_NB_MAX; nb >= 1 && !s->me_nb; nb /= 2)
-            if (sizeof(uint32_t) * (fixed + xg_me_agg_words(s->sbd, nb)) <= XG_ME_SMEM_MAX) s->me_nb = nb;
-        if (s->me_nb) {
-            s->me_smem = sizeof(uint32_t) * (fixed + xg_me_agg_words(s->sbd, s->me_nb));
-            break;
-        }
-        if (s->me_band_rows == 1) {
-            xg_set_error(XIN_GPU_ERR_ARG, "stream_open: search range %d needs more shared memory than a CTA has", R);
-            xg_stream_free(s);
-            return XIN_GPU_ERR_ARG;
-        }
-        bands++;
-    }
-    s->me_bands = (ndy + s->me_band_rows - 1) / s->me_band_rows;
     /* the limit is per kernel, not per launch: set it once to the most any
      * stream uses, so that streams of other sizes opened later (on any thread)
      * cannot lower it under a stream already running */
@@ -461,6 +475,31 @@ static int xg_enqueue_qpel(xin_gpu_stream *s, int cur, int *status)
     return 1;
 }
 
+/* the exhaustive integer search of slot cur against slot ref into keys (the
+ * stream's current band geometry) */
+static void xg_enqueue_me_tiles(xin_gpu_stream *s, int cur, int ref, unsigned long long *keys, const XgPicParams *dpp,
+                                cudaStream_t st)
+{
+    const xin_gpu_stream_cfg &c = s->cfg;
+    XgMeParams mp;
+    mp.cur = s->slot[cur][0];
+    mp.ref = s->slot[ref][0];
+    mp.W = c.width; mp.H = c.height; mp.ctu = c.ctu_size; mp.R = c.search_range;
+    mp.band_rows = s->me_band_rows; mp.band_rows_alloc = s->me_band_rows_alloc; mp.row_words = s->me_row_words;
+    mp.agg_passes = s->me_nb;
+    mp.key_mul = 1u << (XG_COST_FRACTION + xg_me_db(s->sbd) + (XG_BITDEPTH - s->sbd));
+    for (int L = 0; L < 4; L++) {
+        mp.keys[L] = s->lev_on[L] ? keys + s->lev_first[L] : nullptr;
+        mp.cus_x[L] = s->lev_cx[L];
+    }
+    dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, s->me_bands);
+#if XG_BITDEPTH == 10
+    if (s->sbd == 10) k_me_tiles<10><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, dpp);
+    else
+#endif
+        k_me_tiles<8><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, dpp);
+}
+
 /* the launches of one picture of picture set `set` into slot `cur`, against the
  * references in slots l0 (list 0) and l1 (list 1, refs 2) */
 static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l1, bool with_me, bool capturing)
@@ -550,23 +589,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l
                 nl++;
             }
         } else {
-        XgMeParams mp;
-        mp.cur = s->slot[cur][0];
-        mp.ref = s->slot[ref][0];
-        mp.W = c.width; mp.H = c.height; mp.ctu = c.ctu_size; mp.R = c.search_range;
-        mp.band_rows = s->me_band_rows; mp.band_rows_alloc = s->me_band_rows_alloc; mp.row_words = s->me_row_words;
-        mp.agg_passes = s->me_nb;
-        mp.key_mul = 1u << (XG_COST_FRACTION + xg_me_db(s->sbd) + (XG_BITDEPTH - s->sbd));
-        for (int L = 0; L < 4; L++) {
-            mp.keys[L] = s->lev_on[L] ? keys + s->lev_first[L] : nullptr;
-            mp.cus_x[L] = s->lev_cx[L];
-        }
-        dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, s->me_bands);
-#if XG_BITDEPTH == 10
-        if (s->sbd == 10) k_me_tiles<10><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, t.dpp);
-        else
-#endif
-            k_me_tiles<8><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, t.dpp);
+            xg_enqueue_me_tiles(s, cur, ref, keys, t.dpp, st);
         }
         nl++;
         }
@@ -847,6 +870,68 @@ extern "C" int xin_gpu_stream_set_wait_tries(xin_gpu_stream *s, int64_t tries)
     /* the bound is a parameter of the captured graphs: capture them again */
     for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.first);
     s->graphs.clear();
+    return XIN_GPU_OK;
+}
+
+extern "C" int xin_gpu_stream_tune_search(xin_gpu_stream *s, int32_t *bands, float ms[2])
+{
+    xin_gpu_clear_error();
+    if (!s) { xg_set_error(XIN_GPU_ERR_ARG, "stream_tune_search: null stream"); return XIN_GPU_ERR_ARG; }
+    const xin_gpu_stream_cfg &c = s->cfg;
+    if (c.search_mode != 0 || s->nsub < 2 || s->nsub != s->ndone) {
+        xg_set_error(XIN_GPU_ERR_STATE, "stream_tune_search: needs the exhaustive search, two pictures submitted and none in flight");
+        return XIN_GPU_ERR_STATE;
+    }
+    /* the last picture against its list-0 reference (the previous picture) */
+    const int ns = s->nslots, k = s->nsub - 1, cur = k % ns, ref = (k + ns - 1) % ns;
+    const XgPicParams *dpp = s->set[k & 1].dpp;
+    cudaStream_t st = s->st;
+    const int b0 = s->me_bands;
+    const int cand[6] = { b0, b0 / 2, 2 * b0, 3 * b0, 4 * b0, 6 * b0 };
+    cudaEvent_t e0, e1;
+    if (xg_cuda_check(cudaEventCreate(&e0), "tune event") || xg_cuda_check(cudaEventCreate(&e1), "tune event")) return XIN_GPU_ERR_CUDA;
+    float best_ms = 0, first_ms = 0;
+    int best_b = b0, tried[6], ntried = 0;
+    for (int i = 0; i < 6; i++) {
+        if (cand[i] < 1 || !xg_me_geometry(s, cand[i])) continue;
+        bool seen = false;                       /* a geometry once */
+        for (int j = 0; j < ntried; j++) seen |= tried[j] == s->me_bands;
+        if (seen) continue;
+        tried[ntried++] = s->me_bands;
+        float t = 0;
+        for (int rep = 0; rep < 4; rep++) {      /* one warm-up, three timed */
+            if (rep == 1) cudaEventRecord(e0, st);
+            xg_enqueue_me_tiles(s, cur, ref, s->keys, dpp, st);
+        }
+        cudaEventRecord(e1, st);
+        if (xg_cuda_check(cudaEventSynchronize(e1), "tune search")) { cudaEventDestroy(e0); cudaEventDestroy(e1); return XIN_GPU_ERR_CUDA; }
+        cudaEventElapsedTime(&t, e0, e1);
+        t /= 3;
+        s->tune_bands[ntried - 1] = s->me_bands;
+        s->tune_ms[ntried - 1] = t;
+        s->tune_n = ntried;
+        if (i == 0) first_ms = t;
+        if (i == 0 || t < best_ms) { best_ms = t; best_b = s->me_bands; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    xg_me_geometry(s, best_b);
+    /* the geometry is baked into the captured graphs: capture them again */
+    for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.first);
+    s->graphs.clear();
+    if (bands) *bands = s->me_bands;
+    if (ms) { ms[0] = first_ms; ms[1] = best_ms; }
+    return xg_cuda_check(cudaGetLastError(), "tune search");
+}
+
+extern "C" int xin_gpu_stream_tune_table(const xin_gpu_stream *s, int32_t *n, int32_t bands[6], float ms[6])
+{
+    if (!s || !n) return XIN_GPU_ERR_ARG;
+    *n = s->tune_n;
+    for (int i = 0; i < s->tune_n; i++) {
+        if (bands) bands[i] = s->tune_bands[i];
+        if (ms) ms[i] = s->tune_ms[i];
+    }
     return XIN_GPU_OK;
 }
 
