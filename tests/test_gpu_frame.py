@@ -644,6 +644,51 @@ def test_frame_preset4_1080p_two_in_flight():
         fs.close()
 
 
+def test_frame_preset4_random_access_1080p():
+    """The bench's random-access preset-4 workload (preset4_ra_1080p) compared in
+    full at 1920x1080: the first pictures of the GOP 16 coding order -- POC 16
+    (both lists POC 0) and POC 8 (list 0 POC 0, list 1 POC 16) -- through the
+    stream the bench opens (8-bit into the 10-bit library, search by resolution
+    levels, two references named per picture, dpb 32, the bi search with SATD,
+    every transform candidate through the trellis), both pictures in flight
+    together; every CU, bi and transform-candidate record and every plane
+    against the oracle on all host cores."""
+    import bench
+    from xin26x_gb300 import synth as S
+    from xin26x_gb300.frame import BI_DTYPE
+    frames = bench.make_frames(17)
+    ctx = np.ascontiguousarray(S.contexts(np.random.default_rng(4), 1)[0])
+    fs = FrameStream(bench.W, bench.H, search_range=bench.SEARCH, levels=bench.LEVELS, out_q=True, out_rec=True,
+                     bitdepth=bench.BD, input_bitdepth=bench.IN_BD, search_mode=1, tu_mode=1, contexts=ctx, refs=2, dpb=32)
+    order = S.ra_gop(16, 1)[:2]                 # (16, 0, 0), (8, 0, 16)
+    num = {0: 0}
+    try:
+        fs.submit(*frames[0], qp=32, uv_qp=32, sad_lambda=bench.LAMBDA_BD[32])
+        fs.wait()
+        qps = {16: 32, 8: 37}
+        for k, (poc, r0, r1) in enumerate(order, start=1):
+            fs.submit(*frames[poc], qp=qps[poc], uv_qp=qps[poc], sad_lambda=bench.LAMBDA_BD[qps[poc]], ref0=num[r0],
+                      ref1=num[r1])
+            num[poc] = k
+        outs = {poc: fs.wait() for poc, _, _ in order}
+        for poc, r0, r1 in order:
+            cur, p0, p1 = [tuple(p.astype(np.uint16) << (bench.BD - bench.IN_BD) for p in f)
+                           for f in (frames[poc], frames[r0], frames[r1])]
+            recs, q, rec, mts, bis = oracle_frame.run(cur, p0, fs.levels, search_range=bench.SEARCH, qp=qps[poc],
+                                                      uv_qp=qps[poc], sad_lambda=bench.LAMBDA_BD[qps[poc]],
+                                                      bitdepth=bench.BD, threads=0, search_mode=1, tu_mode=1,
+                                                      contexts=ctx, ref1=p1)
+            _compare(outs[poc], (recs, q, rec), fs.levels, ("1080p random access", poc))
+            for name in ("satd_cost", "ncand", "nz", "ssd"):
+                bad = np.nonzero(np.any((outs[poc]["mts"][name] != mts[name]).reshape(len(mts), -1), axis=1))[0]
+                assert bad.size == 0, (name, poc, bad[:5])
+            for name in BI_DTYPE.names:
+                bad = np.nonzero(np.any((outs[poc]["bi"][name] != bis[name]).reshape(len(bis), -1), axis=1))[0]
+                assert bad.size == 0, (name, poc, bad[:5], outs[poc]["bi"][bad[:3]], bis[bad[:3]])
+    finally:
+        fs.close()
+
+
 def test_frame_preset4_tu_qp_limit():
     """The trellis's parameters stop at QP 51: at 10 bits (QP + 12) a slice QP above
     39 is refused before any launch."""
