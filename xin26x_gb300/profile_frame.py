@@ -4,7 +4,7 @@ times -- the program for profiling (ncu) and quick timing of the kernels.
     python -m xin26x_gb300.profile_frame [--frames 6] [--width 1920] [--height 1080]
                                          [--search 64] [--bitdepth 8] [--ctu 64]
                                          [--objects 4] [--octaves 1] [--input-bitdepth 0]
-                                         [--search-mode 0]
+                                         [--search-mode 0] [--tu-mode 0] [--refs 1]
 
 --bitdepth 10 --input-bitdepth 8: 8-bit pictures coded by the 10-bit library.
 """
@@ -33,6 +33,7 @@ def main():
     ap.add_argument("--input-bitdepth", type=int, default=0)
     ap.add_argument("--search-mode", type=int, default=0, help="0 exhaustive, 1 by resolution levels")
     ap.add_argument("--tu-mode", type=int, default=0, help="1: the preset-4 TU work (transform candidates, trellis)")
+    ap.add_argument("--refs", type=int, default=1, help="2: two references (the previous two pictures), bi search")
     ap.add_argument("--qp", type=int, default=32)
     a = ap.parse_args()
     import torch
@@ -43,7 +44,7 @@ def main():
     dev = [tuple(torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in f) for f in seq]
     mask = sum(int(s) for s in a.levels.split(","))
     cfg = _lib.xin_gpu_stream_cfg(a.width, a.height, a.ctu, a.search, mask, 0, 1, 1, a.input_bitdepth, a.search_mode,
-                                  a.tu_mode)
+                                  a.tu_mode, a.refs)
     h = C.c_void_p()
     if lib.xin_gpu_stream_open(C.byref(cfg), C.byref(h)) != 0:
         raise RuntimeError(lib.xin_gpu_last_error().decode())
@@ -65,7 +66,7 @@ def main():
     lib.xin_gpu_stream_close(h)
     s = np.array(stages)
     print(json.dumps({"frames": a.frames, "size": [a.width, a.height], "search": a.search, "search_mode": a.search_mode,
-                      "tu_mode": a.tu_mode, "qp": a.qp,
+                      "tu_mode": a.tu_mode, "refs": a.refs, "qp": a.qp,
                       "bitdepth": a.bitdepth,
                       "input_bitdepth": a.input_bitdepth or a.bitdepth,
                       "ctu": a.ctu, "mpix_s": a.width * a.height / float(np.median(s[:, 4])) / 1e3,
