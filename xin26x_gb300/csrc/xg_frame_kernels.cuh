@@ -965,11 +965,13 @@ struct XgTailBiSmem {
 /* CPB CUs of size S (luma S x S, chroma S/2 x S/2) per CTA, NT threads per CU
  * (NT = 32: one warp per CU, warp-synchronous) */
 /* CTAs per SM the register allocation must allow: 64 x 64 CUs are held to five by
- * shared memory anyway, the other sizes keep eight 128-thread CTAs (64 registers);
- * the bi search's kernels hold twice the shared state */
+ * shared memory anyway, the other sizes keep eight 128-thread CTAs (64 registers).
+ * The bi search's kernels: 64 x 64 two, 32 x 32 four, and the warp-per-CU sizes
+ * eight (64 registers with a few spilled: 3.42-3.46 ms against 3.51-3.54 ms per
+ * 1080p preset-4 picture at four, 3.46-3.50 at six) */
 __host__ __device__ constexpr int xg_tail_min_ctas(int s, bool bi = false)
 {
-    return bi ? (s == 64 ? 2 : 4) : s == 128 ? 2 : s == 64 ? 5 : 8;
+    return bi ? (s == 64 ? 2 : s == 32 ? 4 : 8) : s == 128 ? 2 : s == 64 ? 5 : 8;
 }
 /* shared memory (dynamic) of a launch */
 template <int S, int NT, int CPB, bool BI = false>
