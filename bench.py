@@ -363,10 +363,11 @@ def run_gpu(args):
                     "ten_bit_samples": pipeline_variant_bench(torch, flush, frames, nvar, args.warmup, 10, 0),
                     "search_by_resolution_levels": pipeline_variant_bench(torch, flush, frames, nvar, args.warmup,
                                                                           BD, IN_BD, search_mode=1)}
-    serving = None
+    serving = serving_planes = None
     if rank == 0 and world == 1:
         from xin26x_gb300 import serve_bench
         serving = serve_bench.run(seconds=3.0, mpix_budget=1650.0, max_inflight=6)
+        serving_planes = serve_bench.run(seconds=3.0, mpix_budget=1650.0, max_inflight=8, planes=True)
 
     out = None
     if rank == 0:
@@ -404,6 +405,7 @@ def run_gpu(args):
                "wide_search_4k_10bit": wide,
                "pipeline_variants_1080p": variants,
                "serving": serving,
+               "serving_with_planes": serving_planes,
                "gpu_launches": int(launches),
                "clocks": clk,
                "cpu_baseline": cpu}

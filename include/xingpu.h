@@ -646,7 +646,10 @@ int  xin_gpu_stream_footprint(const xin_gpu_stream_cfg *cfg, uint64_t *device_by
  * One scheduler thread runs up to max_inflight pictures of different streams
  * at once and starts the oldest waiting picture whenever one finishes; the
  * pictures of one stream run in order.  A stream's results are the same as
- * when it runs alone.  leave drains the stream's queue, then frees it. */
+ * when it runs alone.  leave drains the stream's queue, then frees it.  A
+ * served stream keeps XIN_GPU_OUT_Q of its cfg.out_flags (its coefficient
+ * planes, through xin_gpu_server_submit_planes); the other output flags are
+ * cleared. */
 typedef struct xin_gpu_server xin_gpu_server;
 typedef struct xin_gpu_server_cfg {
     uint64_t hbm_budget;         /* device bytes for streams; 0 = 90 % of the free memory at open */
@@ -677,6 +680,15 @@ int  xin_gpu_server_open(const xin_gpu_server_cfg *cfg, xin_gpu_server **srv);  
 int  xin_gpu_server_join(xin_gpu_server *srv, const xin_gpu_stream_cfg *cfg, double fps, int32_t *stream_id);
 int  xin_gpu_server_submit(xin_gpu_server *srv, int32_t stream_id, const xin_gpu_picture *pic,
                            xin_gpu_cu_result *cu_out, uint64_t user_tag);
+/* The same, with the picture's coefficient planes returned too: q_out[3] are
+ * caller buffers laid out as xin_gpu_results.q ([levels][plane height][plane
+ * width]), filled straight from the device when the picture completes (the
+ * latency a poll reports includes that copy).  Pinned host memory
+ * (cudaHostAlloc) keeps the copies asynchronous.  The stream must have been
+ * joined with XIN_GPU_OUT_Q in its out_flags; a buffer must stay untouched
+ * until its picture is polled. */
+int  xin_gpu_server_submit_planes(xin_gpu_server *srv, int32_t stream_id, const xin_gpu_picture *pic,
+                                  xin_gpu_cu_result *cu_out, XG_COEFF *const q_out[3], uint64_t user_tag);
 /* up to max completed pictures; waits up to timeout_ms (< 0: until one completes) */
 int  xin_gpu_server_poll(xin_gpu_server *srv, xin_gpu_server_done *out, int32_t max, int32_t timeout_ms, int32_t *n);
 int  xin_gpu_server_leave(xin_gpu_server *srv, int32_t stream_id, int32_t timeout_ms);

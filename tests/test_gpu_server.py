@@ -170,3 +170,49 @@ def test_server_argument_and_queue_errors():
             for d, _ in srv.poll(timeout_ms=1000):
                 assert d.status == 0
                 seen += 1
+
+
+def test_server_planes_equal_alone():
+    """xin_gpu_server_submit_planes: a served stream joined with XIN_GPU_OUT_Q
+    returns each picture's coefficient planes straight into caller buffers
+    (pinned host memory), equal to the same stream run alone; a stream beside
+    it without planes is unaffected; planes are refused for a stream joined
+    without XIN_GPU_OUT_Q."""
+    import torch
+    from xin26x_gb300.frame import FrameStream
+    from xin26x_gb300.server import Server
+    w, h = 256, 128
+    a = _frames(w, h, 4, seed=41)
+    b = _frames(192, 128, 4, seed=42)
+    fs = FrameStream(w, h, search_range=R, out_q=True, out_rec=False)
+    want = []
+    for k, f in enumerate(a):
+        fs.submit(*f, qp=27 + 5 * (k % 3), uv_qp=27 + 5 * (k % 3), sad_lambda=64)
+        r = fs.wait()
+        want.append((r["cu"].copy(), [q.copy() for q in r["q"]]) if k else None)
+    nlev, coef = len(fs.levels), fs.coef
+    fs.close()
+    want_b = _alone(192, 128, b)
+    with Server(max_inflight=3, max_queue=2) as srv:
+        sa = srv.join(w, h, fps=30, search_range=R, out_q=True)
+        sb = srv.join(192, 128, fps=30, search_range=R)
+        tdt = torch.int16 if coef == np.int16 else torch.int32
+        bufs = {k: [torch.empty((nlev, hh, ww), dtype=tdt, pin_memory=True).numpy()
+                    for hh, ww in ((h, w), (h // 2, w // 2), (h // 2, w // 2))] for k in range(4)}
+        got, got_b = {}, {}
+        for k in range(4):
+            assert srv.submit(sa, *a[k], qp=27 + 5 * (k % 3), sad_lambda=64, tag=k, q_out=bufs[k]) == 0
+            assert srv.submit(sb, *b[k], qp=27 + 5 * (k % 3), sad_lambda=64, tag=100 + k) == 0
+            while len(got) + len(got_b) < 2 * (k + 1):
+                for d, cu in srv.poll(timeout_ms=1000):
+                    assert d.status == 0
+                    (got if d.user_tag < 100 else got_b)[d.user_tag % 100] = cu
+        with pytest.raises(RuntimeError):
+            st = srv.submit(sb, *b[0], qp=32, sad_lambda=64, tag=999, q_out=bufs[0])
+            if st:
+                raise RuntimeError(st)
+    for k in range(1, 4):
+        assert np.array_equal(got[k], want[k][0]), k
+        for p in range(3):
+            assert np.array_equal(bufs[k][p], want[k][1][p]), (k, p)
+        assert np.array_equal(got_b[k], want_b[k - 1]), k

@@ -149,6 +149,7 @@ SIGNATURES = {
     "xin_gpu_server_open": ([vp, C.POINTER(vp)], C.c_int),
     "xin_gpu_server_join": ([vp, vp, C.c_double, C.POINTER(i32)], C.c_int),
     "xin_gpu_server_submit": ([vp, i32, vp, vp, C.c_uint64], C.c_int),
+    "xin_gpu_server_submit_planes": ([vp, i32, vp, vp, vp, C.c_uint64], C.c_int),
     "xin_gpu_server_poll": ([vp, vp, i32, i32, C.POINTER(i32)], C.c_int),
     "xin_gpu_server_leave": ([vp, i32, i32], C.c_int),
     "xin_gpu_server_get_stats": ([vp, vp], C.c_int),

@@ -64,6 +64,7 @@ struct xin_gpu_stream {
         int32_t *h_stat;       /* the picture's device status (XgPicParams.status), read back with the results */
         xin_gpu_cu_result *h_res;
         xg_coef *h_q[3];
+        xg_coef *q_dst[3];     /* this picture's coefficient planes go here instead of h_q (caller buffers) */
         xg_pix *h_rec[3];
         cudaEvent_t ev0, ev1;  /* submitted; results in host memory */
         cudaEvent_t ev_kern;   /* kernels done (the copy stream waits on it) */
@@ -690,7 +691,8 @@ static void xg_enqueue_results(xin_gpu_stream *s, xin_gpu_stream::Set &t, bool w
         if (t.dbi) cudaMemcpyAsync(t.h_bi, t.dbi, sizeof(xin_gpu_cu_bi) * s->ncus, cudaMemcpyDeviceToHost, s->cst);
         for (int p = 0; p < 3; p++) {
             size_t n = (p ? lc : lq) * s->nlev;
-            if (c.out_flags & XIN_GPU_OUT_Q) cudaMemcpyAsync(t.h_q[p], t.dq[p], n * sizeof(xg_coef), cudaMemcpyDeviceToHost, s->cst);
+            if (c.out_flags & XIN_GPU_OUT_Q)
+                cudaMemcpyAsync(t.q_dst[p] ? t.q_dst[p] : t.h_q[p], t.dq[p], n * sizeof(xg_coef), cudaMemcpyDeviceToHost, s->cst);
             if (c.out_flags & XIN_GPU_OUT_REC) cudaMemcpyAsync(t.h_rec[p], t.drec[p], n * sizeof(xg_pix), cudaMemcpyDeviceToHost, s->cst);
         }
     }
@@ -700,10 +702,17 @@ static void xg_enqueue_results(xin_gpu_stream *s, xin_gpu_stream::Set &t, bool w
     cudaEventRecord(t.ev1, s->cst);
 }
 
-extern "C" int xin_gpu_frame_submit_refs(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_t ref0, int32_t ref1);
-extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic) { return xin_gpu_frame_submit_refs(s, pic, -1, -1); }
-
+static int xg_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_t ref0, int32_t ref1, xg_coef *const *q_dst);
+extern "C" int xin_gpu_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic) { return xg_frame_submit(s, pic, -1, -1, nullptr); }
 extern "C" int xin_gpu_frame_submit_refs(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_t ref0, int32_t ref1)
+{
+    return xg_frame_submit(s, pic, ref0, ref1, nullptr);
+}
+
+/* q_dst (optional): caller buffers that receive this picture's coefficient planes
+ * (XIN_GPU_OUT_Q) straight from the device -- pinned host memory keeps the copy
+ * asynchronous -- instead of the picture set's pinned staging */
+static int xg_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_t ref0, int32_t ref1, xg_coef *const *q_dst)
 {
     xin_gpu_clear_error();
     (void)cudaGetLastError();   /* errors of earlier, unrelated calls are not this picture's */
@@ -797,6 +806,7 @@ extern "C" int xin_gpu_frame_submit_refs(xin_gpu_stream *s, const xin_gpu_pictur
     } else {
         xg_count_launch((uint64_t)xg_enqueue_picture(s, set, cur, l0, l1, with_me, false));
     }
+    for (int p = 0; p < 3; p++) t.q_dst[p] = q_dst ? q_dst[p] : nullptr;
     xg_enqueue_results(s, t, with_me);
     if (xg_cuda_check(cudaGetLastError(), "frame_submit")) return XIN_GPU_ERR_CUDA;
     s->nsub++;
@@ -850,8 +860,12 @@ extern "C" int xin_gpu_frame_wait(xin_gpu_stream *s, xin_gpu_results *res, int32
     for (int p = 0; p < 3; p++) {
         size_t n = (p ? lc : lq) * s->nlev;
         if (c.out_flags & XIN_GPU_OUT_Q) {
-            if (res->q[p]) memcpy(res->q[p], t.h_q[p], n * sizeof(xg_coef));
-            else res->q[p] = t.h_q[p];
+            xg_coef *src = t.q_dst[p] ? t.q_dst[p] : t.h_q[p];    /* where the picture's planes were copied */
+            if (res->q[p]) {
+                if (res->q[p] != src) memcpy(res->q[p], src, n * sizeof(xg_coef));
+            } else {
+                res->q[p] = src;
+            }
         }
         if (c.out_flags & XIN_GPU_OUT_REC) {
             if (res->rec[p]) memcpy(res->rec[p], t.h_rec[p], n * sizeof(xg_pix));

@@ -95,6 +95,7 @@ struct XgSrvPic {
     uint32_t index;
     uint64_t tag;
     xin_gpu_cu_result *cu_out;
+    xg_coef *q_out[3];            /* caller buffers of the coefficient planes (XIN_GPU_OUT_Q streams), or none */
     int32_t qp, uv_qp;
     uint32_t lambda;
     double t_submit, t_launch;
@@ -187,6 +188,7 @@ static void xg_srv_loop(xin_gpu_server *v)
                     xin_gpu_results r;
                     memset(&r, 0, sizeof r);
                     r.cu = p->cu_out;
+                    for (int k = 0; k < 3; k++) r.q[k] = p->q_out[k];   /* already in place: no copy */
                     d.status = xin_gpu_frame_wait(t->s, &r, 0);
                     d.has_results = p->index > 0 && d.status == XIN_GPU_OK;
                     d.gpu_ms = r.gpu_ms;
@@ -259,7 +261,7 @@ static void xg_srv_loop(xin_gpu_server *v)
             pic.stride[0] = w; pic.stride[1] = pic.stride[2] = w / 2;
             pic.qp = p->qp; pic.uv_qp = p->uv_qp; pic.sad_lambda = p->lambda;
             lk.unlock();
-            int st = xin_gpu_frame_submit(best->s, &pic);
+            int st = xg_frame_submit(best->s, &pic, -1, -1, p->q_out[0] ? p->q_out : nullptr);
             lk.lock();
             v->launched++;
             if (st) {
@@ -342,7 +344,7 @@ extern "C" int xin_gpu_server_join(xin_gpu_server *v, const xin_gpu_stream_cfg *
         v->mpix_used += mpix;
     }
     xin_gpu_stream_cfg c = *cfg;
-    c.out_flags = 0;             /* served streams return CU records only */
+    c.out_flags &= XIN_GPU_OUT_Q;   /* served streams return CU records and, when asked, coefficient planes */
     xin_gpu_stream *s = nullptr;
     int st = xin_gpu_stream_open(&c, &s);
     std::lock_guard<std::mutex> lk(v->mu);
@@ -366,8 +368,26 @@ extern "C" int xin_gpu_server_join(xin_gpu_server *v, const xin_gpu_stream_cfg *
     return XIN_GPU_OK;
 }
 
+static int xg_server_submit(xin_gpu_server *v, int32_t stream_id, const xin_gpu_picture *pic, xin_gpu_cu_result *cu_out,
+                            XG_COEFF *const *q_out, uint64_t user_tag);
 extern "C" int xin_gpu_server_submit(xin_gpu_server *v, int32_t stream_id, const xin_gpu_picture *pic,
                                      xin_gpu_cu_result *cu_out, uint64_t user_tag)
+{
+    return xg_server_submit(v, stream_id, pic, cu_out, nullptr, user_tag);
+}
+extern "C" int xin_gpu_server_submit_planes(xin_gpu_server *v, int32_t stream_id, const xin_gpu_picture *pic,
+                                            xin_gpu_cu_result *cu_out, XG_COEFF *const q_out[3], uint64_t user_tag)
+{
+    if (!q_out || !q_out[0] || !q_out[1] || !q_out[2]) {
+        xin_gpu_clear_error();
+        xg_set_error(XIN_GPU_ERR_ARG, "server_submit_planes: three plane buffers needed");
+        return XIN_GPU_ERR_ARG;
+    }
+    return xg_server_submit(v, stream_id, pic, cu_out, q_out, user_tag);
+}
+
+static int xg_server_submit(xin_gpu_server *v, int32_t stream_id, const xin_gpu_picture *pic, xin_gpu_cu_result *cu_out,
+                            XG_COEFF *const *q_out, uint64_t user_tag)
 {
     xin_gpu_clear_error();
     if (!v || !pic) { xg_set_error(XIN_GPU_ERR_ARG, "server_submit: null argument"); return XIN_GPU_ERR_ARG; }
@@ -395,6 +415,10 @@ extern "C" int xin_gpu_server_submit(xin_gpu_server *v, int32_t stream_id, const
             xg_set_error(XIN_GPU_ERR_ARG, "server_submit: cu_out needed (xin_gpu_stream_num_cus records)");
             return XIN_GPU_ERR_ARG;
         }
+        if (q_out && !(t->cfg.out_flags & XIN_GPU_OUT_Q)) {
+            xg_set_error(XIN_GPU_ERR_ARG, "server_submit_planes: stream %d was joined without XIN_GPU_OUT_Q", stream_id);
+            return XIN_GPU_ERR_ARG;
+        }
         w = t->cfg.width; h = t->cfg.height;
         es = xg_in_es(t->cfg);
         if (!t->spare.empty()) { p = t->spare.back(); t->spare.pop_back(); }
@@ -417,6 +441,7 @@ extern "C" int xin_gpu_server_submit(xin_gpu_server *v, int32_t stream_id, const
                    (const char *)pic->plane[k] + (size_t)y * pic->stride[k] * es, (w / 2) * es);
     p->tag = user_tag;
     p->cu_out = cu_out;
+    for (int k = 0; k < 3; k++) p->q_out[k] = q_out ? (xg_coef *)q_out[k] : nullptr;
     p->qp = pic->qp; p->uv_qp = pic->uv_qp; p->lambda = pic->sad_lambda;
     std::lock_guard<std::mutex> lk(v->mu);
     auto it = v->streams.find(stream_id);

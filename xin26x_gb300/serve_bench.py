@@ -33,7 +33,8 @@ FPS = 30.0
 LAMBDA = {27: 45, 32: 64, 37: 91}
 
 
-def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=64, frames_per_class=6, arrivals="poisson"):
+def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=64, frames_per_class=6, arrivals="poisson",
+        planes=False):
     from xin26x_gb300 import synth
     from xin26x_gb300.server import Admission, Server
 
@@ -74,7 +75,15 @@ def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=6
     events = []
     for n, si in enumerate(order):
         heapq.heappush(events, (float(join_t[n]), 0, int(si)))
-    sid_of, leave_at = {}, {}
+    sid_of, leave_at, qbufs = {}, {}, {}
+    if planes:
+        # every stream's plane buffers, allocated before the clock starts: four sets of
+        # pinned host memory a stream (a picture running, two queued, one being polled)
+        import torch
+        tdt = torch.int16 if srv.pix == np.uint8 else torch.int32
+        for si, ((w, h), _) in enumerate(streams):
+            qbufs[si] = [[torch.empty((4, hh, ww), dtype=tdt, pin_memory=True).numpy()
+                          for hh, ww in ((h, w), (h // 2, w // 2), (h // 2, w // 2))] for _ in range(4)]
     k_of, a_of = {}, {}             # pictures accepted / arrived per stream
     th = threading.Thread(target=poller, daemon=True)
     th.start()
@@ -89,7 +98,7 @@ def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=6
         (w, h), j = streams[si]
         if kind == 0:                      # join
             try:
-                sid_of[si] = srv.join(w, h, fps=FPS, search_range=search_range)
+                sid_of[si] = srv.join(w, h, fps=FPS, search_range=search_range, out_q=planes)
             except Admission:
                 refused.append(si)
                 continue
@@ -106,7 +115,8 @@ def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=6
             k = k_of[si]
             f = content[(w, h)][(k + j) % frames_per_class]
             qp = (27, 32, 37)[k % 3]
-            st = srv.submit(sid_of[si], *f, qp=qp, sad_lambda=LAMBDA[qp], tag=w * h)
+            st = srv.submit(sid_of[si], *f, qp=qp, sad_lambda=LAMBDA[qp], tag=w * h,
+                            q_out=qbufs[si][k % 4] if planes else None)
             if st == 0:
                 k_of[si] = k + 1
             elif st == -6:            # queue full (or the stream failed: reported by poll)
@@ -132,6 +142,8 @@ def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=6
                         f"+-{search_range} exhaustive search, CU levels 64/32/16/8, {seconds:.1f} s",
             "arrivals": "Poisson at 30 pictures/s per stream + 0..2 ms jitter" if arrivals == "poisson"
                         else "every 1/30 s + 0..4 ms jitter",
+            "results": "CU records and every picture's coefficient planes (all levels) copied into pinned caller buffers"
+                       if planes else "CU records",
             "offered_mpix_s": offered, "mpix_budget": mpix_budget, "max_inflight": max_inflight,
             "admitted": len(admitted), "refused": len(refused), "admitted_by_class": by_class,
             "pictures": len(lat), "arrived": int(sum(a_of.values())), "dropped": dropped, "failed": len(failed), "first_failures": failed[:4],
@@ -150,8 +162,9 @@ def main():
     ap.add_argument("--max-inflight", type=int, default=6)
     ap.add_argument("--seed", type=int, default=48)
     ap.add_argument("--arrivals", choices=("poisson", "periodic"), default="poisson")
+    ap.add_argument("--planes", action="store_true", help="every picture's coefficient planes returned too")
     a = ap.parse_args()
-    print(json.dumps(run(a.seconds, a.mpix_budget, a.max_inflight, a.seed, arrivals=a.arrivals)), flush=True)
+    print(json.dumps(run(a.seconds, a.mpix_budget, a.max_inflight, a.seed, arrivals=a.arrivals, planes=a.planes)), flush=True)
 
 
 if __name__ == "__main__":

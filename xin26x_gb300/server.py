@@ -44,14 +44,15 @@ class Server:
 
     @staticmethod
     def stream_cfg(width, height, ctu=64, search_range=64, levels=(64, 32, 16, 8), input_bitdepth=0, search_mode=0,
-                   tu_mode=0):
+                   tu_mode=0, out_q=False):
         """search_mode 1: search by resolution levels; tu_mode 1: the preset-4 TU
         stage (every transform candidate through the trellis, the stream's
-        default context set)."""
+        default context set); out_q: coefficient planes returned (submit(q_out=))."""
         mask = 0
         for s in levels:
             mask |= int(s)
-        return _lib.xin_gpu_stream_cfg(width, height, ctu, search_range, mask, 0, 1, 0, input_bitdepth, search_mode, tu_mode)
+        return _lib.xin_gpu_stream_cfg(width, height, ctu, search_range, mask, 1 if out_q else 0, 1, 0, input_bitdepth,
+                                       search_mode, tu_mode)
 
     def footprint(self, width, height, **kw):
         d, hbytes = C.c_uint64(), C.c_uint64()
@@ -76,9 +77,12 @@ class Server:
             self._next[sid.value] = 0
         return sid.value
 
-    def submit(self, sid, y, u, v, qp=32, uv_qp=None, sad_lambda=64, tag=0) -> int:
+    def submit(self, sid, y, u, v, qp=32, uv_qp=None, sad_lambda=64, tag=0, q_out=None) -> int:
         """Queue a picture; returns the status (0, or -6 when the stream's queue is full).
-        One thread submits to a given stream."""
+        One thread submits to a given stream.  q_out: three arrays [levels, h, w]
+        (pinned host memory keeps the copies asynchronous) that receive the
+        picture's coefficient planes (a stream joined with out_q); they must stay
+        alive and untouched until the picture is polled."""
         pic = _lib.xin_gpu_picture()
         planes = [np.ascontiguousarray(p, dtype=self.pix) for p in (y, u, v)]
         for i, p in enumerate(planes):
@@ -91,7 +95,12 @@ class Server:
             idx = self._next[sid]
             cu = np.zeros(self._ncus[sid], CU_DTYPE) if idx > 0 else None
             self._pending[(sid, idx)] = cu
-        st = self.lib.xin_gpu_server_submit(self.h, sid, C.byref(pic), cu.ctypes.data if cu is not None else None, tag)
+        if q_out is None:
+            st = self.lib.xin_gpu_server_submit(self.h, sid, C.byref(pic), cu.ctypes.data if cu is not None else None, tag)
+        else:
+            qp3 = (C.c_void_p * 3)(*[q.ctypes.data for q in q_out])
+            st = self.lib.xin_gpu_server_submit_planes(self.h, sid, C.byref(pic), cu.ctypes.data if cu is not None else None,
+                                                       qp3, tag)
         with self._mu:
             if st == 0:
                 self._next[sid] = idx + 1
