@@ -645,7 +645,14 @@ int  xin_gpu_stream_footprint(const xin_gpu_stream_cfg *cfg, uint64_t *device_by
  * picture is reported by poll; it may be NULL for a stream's first picture).
  * One scheduler thread runs up to max_inflight pictures of different streams
  * at once and starts the oldest waiting picture whenever one finishes; the
- * pictures of one stream run in order.  A stream's results are the same as
+ * pictures of one stream run in order.  Streams of the plain form (exhaustive
+ * search, one reference, tu_mode 0) with the same picture size, CTU size,
+ * search range, levels and input depth share launches: the oldest waiting
+ * picture takes up to batch_max - 1 waiting pictures of such streams into one
+ * batch, one launch per stage over all of them (each picture still counts
+ * toward max_inflight), as long as the batch's integer search stays within two
+ * waves of the GPU's SMs: a batch completes its pictures together, so pictures
+ * whose search fills the GPU on its own run alone.  A stream's results are the same as
  * when it runs alone.  leave drains the stream's queue, then frees it.  A
  * served stream keeps XIN_GPU_OUT_Q of its cfg.out_flags (its coefficient
  * planes, through xin_gpu_server_submit_planes); the other output flags are
@@ -657,6 +664,10 @@ typedef struct xin_gpu_server_cfg {
     uint32_t max_inflight;       /* pictures on the GPU at once; 0 = 8 */
     uint32_t max_streams;        /* 0 = 256 */
     uint32_t max_queue;          /* pictures a stream may have waiting; 0 = 4 */
+    uint32_t batch_max;          /* pictures of different streams one launch per stage may carry
+                                    (cross-stream batches); 0 = 8, 1 = one picture a launch */
+    uint32_t batch_window_us;    /* how long the oldest waiting picture may be held for others to
+                                    join its batch; 0 = launch at once with what is waiting */
     uint32_t reserved;
 } xin_gpu_server_cfg;
 typedef struct xin_gpu_server_done {
@@ -675,6 +686,8 @@ typedef struct xin_gpu_server_stats {
     uint64_t hbm_budget, hbm_used;
     double   mpix_used;
     uint64_t launched, completed;
+    uint64_t batches;            /* launches that carried pictures of two or more streams */
+    uint64_t batched_pictures;   /* pictures those launches carried */
 } xin_gpu_server_stats;
 int  xin_gpu_server_open(const xin_gpu_server_cfg *cfg, xin_gpu_server **srv);     /* cfg may be NULL */
 int  xin_gpu_server_join(xin_gpu_server *srv, const xin_gpu_stream_cfg *cfg, double fps, int32_t *stream_id);

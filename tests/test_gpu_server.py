@@ -216,3 +216,57 @@ def test_server_planes_equal_alone():
         for p in range(3):
             assert np.array_equal(bufs[k][p], want[k][1][p]), (k, p)
         assert np.array_equal(got_b[k], want_b[k - 1]), k
+
+
+def test_server_cross_stream_batches_equal_alone():
+    """Cross-stream batches (xg_batch.cuh): three plain streams of one shape, two
+    of them returning coefficient planes, share one launch per stage (the
+    window holds the oldest picture until the three have arrived); a stream of
+    another shape runs beside them.  Every stream's CU records and planes equal
+    the same stream run alone, and the server counts the batches.  128 x 64
+    pictures at +-16: a picture's integer search is 2 tiles x 33 bands = 66
+    CTAs, so four fit the two waves of SMs a batch may fill."""
+    import torch
+    from xin26x_gb300.frame import FrameStream
+    from xin26x_gb300.server import Server
+    w, h, n = 128, 64, 5
+    seqs = [_frames(w, h, n, seed=51 + i) for i in range(3)]
+    other = _frames(256, 128, n, seed=54)
+    qp = [27 + 5 * (k % 3) for k in range(n)]
+    want = []
+    for fr in seqs:
+        fs = FrameStream(w, h, search_range=R, out_q=True, out_rec=False)
+        ww = []
+        for k, f in enumerate(fr):
+            fs.submit(*f, qp=qp[k], uv_qp=qp[k], sad_lambda=64)
+            r = fs.wait()
+            ww.append((r["cu"].copy(), [q.copy() for q in r["q"]]) if k else None)
+        nlev, coef = len(fs.levels), fs.coef
+        fs.close()
+        want.append(ww)
+    want_o = _alone(256, 128, other)
+    tdt = torch.int16 if coef == np.int16 else torch.int32
+    bufs = {(i, k): [torch.empty((nlev, hh, ww_), dtype=tdt, pin_memory=True).numpy()
+                     for hh, ww_ in ((h, w), (h // 2, w // 2), (h // 2, w // 2))] for i in range(2) for k in range(n)}
+    got = {}
+    with Server(max_inflight=8, max_queue=2, batch_max=3, batch_window_us=200000) as srv:
+        sids = [srv.join(w, h, fps=30, search_range=R, out_q=i < 2) for i in range(3)]
+        so = srv.join(256, 128, fps=30, search_range=R)
+        for k in range(n):
+            for i in range(3):
+                assert srv.submit(sids[i], *seqs[i][k], qp=qp[k], sad_lambda=64, tag=100 * i + k,
+                                  q_out=bufs[(i, k)] if i < 2 else None) == 0
+            assert srv.submit(so, *other[k], qp=qp[k], sad_lambda=64, tag=300 + k) == 0
+            while len(got) < 4 * (k + 1):
+                for d, cu in srv.poll(timeout_ms=2000):
+                    assert d.status == 0
+                    got[d.user_tag] = cu
+        st = srv.stats()
+    assert st["batches"] == n - 1 and st["batched_pictures"] == 3 * (n - 1), st
+    for k in range(1, n):
+        for i in range(3):
+            assert np.array_equal(got[100 * i + k], want[i][k][0]), (i, k)
+            if i < 2:
+                for p in range(3):
+                    assert np.array_equal(bufs[(i, k)][p], want[i][k][1][p]), (i, k, p)
+        assert np.array_equal(got[300 + k], want_o[k - 1]), k

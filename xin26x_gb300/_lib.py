@@ -54,7 +54,7 @@ class xin_gpu_prob(C.Structure):
 
 class xin_gpu_server_cfg(C.Structure):
     _fields_ = [("hbm_budget", C.c_uint64), ("mpix_budget", C.c_double), ("max_inflight", u32), ("max_streams", u32),
-                ("max_queue", u32), ("reserved", u32)]
+                ("max_queue", u32), ("batch_max", u32), ("batch_window_us", u32), ("reserved", u32)]
 
 
 class xin_gpu_server_done(C.Structure):
@@ -66,7 +66,7 @@ class xin_gpu_server_done(C.Structure):
 class xin_gpu_server_stats(C.Structure):
     _fields_ = [("streams", i32), ("running", i32), ("queued", i32), ("reserved", i32), ("hbm_budget", C.c_uint64),
                 ("hbm_used", C.c_uint64), ("mpix_used", C.c_double), ("launched", C.c_uint64),
-                ("completed", C.c_uint64)]
+                ("completed", C.c_uint64), ("batches", C.c_uint64), ("batched_pictures", C.c_uint64)]
 
 
 class xin_gpu_mv(C.Structure):

@@ -478,8 +478,7 @@ static int xg_enqueue_qpel(xin_gpu_stream *s, int cur, int *status)
 
 /* the exhaustive integer search of slot cur against slot ref into keys (the
  * stream's current band geometry) */
-static void xg_enqueue_me_tiles(xin_gpu_stream *s, int cur, int ref, unsigned long long *keys, const XgPicParams *dpp,
-                                cudaStream_t st)
+static XgMeParams xg_me_params(const xin_gpu_stream *s, int cur, int ref, unsigned long long *keys)
 {
     const xin_gpu_stream_cfg &c = s->cfg;
     XgMeParams mp;
@@ -493,12 +492,47 @@ static void xg_enqueue_me_tiles(xin_gpu_stream *s, int cur, int ref, unsigned lo
         mp.keys[L] = s->lev_on[L] ? keys + s->lev_first[L] : nullptr;
         mp.cus_x[L] = s->lev_cx[L];
     }
+    return mp;
+}
+
+static void xg_enqueue_me_tiles(xin_gpu_stream *s, int cur, int ref, unsigned long long *keys, const XgPicParams *dpp,
+                                cudaStream_t st)
+{
+    const xin_gpu_stream_cfg &c = s->cfg;
+    const XgMeParams mp = xg_me_params(s, cur, ref, keys);
     dim3 grd((c.width + 63) / 64, (c.height + 63) / 64, s->me_bands);
 #if XG_BITDEPTH == 10
     if (s->sbd == 10) k_me_tiles<10><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, dpp);
     else
 #endif
         k_me_tiles<8><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, dpp);
+}
+
+/* the tails' parameters of level L (the li-th level on) of a picture of set
+ * `set` in slot cur against slots l0 and l1 */
+static XgTailParams xg_tail_params(xin_gpu_stream *s, int set, int cur, int l0, int l1, int L, int li)
+{
+    const xin_gpu_stream_cfg &c = s->cfg;
+    const xin_gpu_stream::Set &t = s->set[set];
+    const size_t lq = (size_t)c.width * c.height, lc = lq / 4;
+    XgTailParams tp;
+    for (int p = 0; p < 3; p++) { tp.cur[p] = s->slot[cur][p]; tp.ref[p] = s->slot[l0][p]; tp.ref1[p] = s->slot[l1][p]; }
+    tp.qpel = s->qpel[l0];
+    tp.qpel1 = s->qpel[l1];
+    tp.keys1 = c.refs == 2 ? s->keys1 + s->lev_first[L] : nullptr;
+    tp.bi = t.dbi;
+    tp.W = c.width; tp.H = c.height; tp.ctu = c.ctu_size; tp.R = c.search_range;
+    tp.keys = s->keys + s->lev_first[L];
+    tp.cus_x = s->lev_cx[L]; tp.first_cu = s->lev_first[L]; tp.size = XG_LEVEL_SIZE[L]; tp.level = L;
+    for (int p = 0; p < 3; p++) {
+        tp.q[p] = t.dq[p] + (p ? lc : lq) * li;
+        tp.rec[p] = t.drec[p] + (p ? lc : lq) * li;
+    }
+    tp.res = t.dres;
+    for (int p = 0; p < 3; p++) tp.resid[p] = nullptr;
+    if (s->tu[set])
+        for (int p = 0; p < 3; p++) tp.resid[p] = xg_tu_resid(s->tu[set], L, p);
+    return tp;
 }
 
 /* the launches of one picture of picture set `set` into slot `cur`, against the
@@ -508,7 +542,6 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l
     const xin_gpu_stream_cfg &c = s->cfg;
     xin_gpu_stream::Set &t = s->set[set];
     cudaStream_t st = t.pst;
-    size_t lq = (size_t)c.width * c.height, lc = lq / 4;
     int nl = 0;
     /* the previous picture (the other set, on its own stream) must have finished
      * with the planes this picture overwrites: its reference slot, quarter-pel and
@@ -613,23 +646,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l
                 cudaStreamWaitEvent(ls, s->ev_fork, 0);
                 nfork = li;
             }
-            XgTailParams tp;
-            for (int p = 0; p < 3; p++) { tp.cur[p] = s->slot[cur][p]; tp.ref[p] = s->slot[l0][p]; tp.ref1[p] = s->slot[l1][p]; }
-            tp.qpel = s->qpel[l0];
-            tp.qpel1 = s->qpel[l1];
-            tp.keys1 = c.refs == 2 ? s->keys1 + s->lev_first[L] : nullptr;
-            tp.bi = t.dbi;
-            tp.W = c.width; tp.H = c.height; tp.ctu = c.ctu_size; tp.R = c.search_range;
-            tp.keys = s->keys + s->lev_first[L];
-            tp.cus_x = s->lev_cx[L]; tp.first_cu = s->lev_first[L]; tp.size = XG_LEVEL_SIZE[L]; tp.level = L;
-            for (int p = 0; p < 3; p++) {
-                tp.q[p] = t.dq[p] + (p ? lc : lq) * li;
-                tp.rec[p] = t.drec[p] + (p ? lc : lq) * li;
-            }
-            tp.res = t.dres;
-            for (int p = 0; p < 3; p++) tp.resid[p] = nullptr;
-            if (s->tu[set])
-                for (int p = 0; p < 3; p++) tp.resid[p] = xg_tu_resid(s->tu[set], L, p);
+            const XgTailParams tp = xg_tail_params(s, set, cur, l0, l1, L, li);
             int n = s->lev_cx[L] * s->lev_cy[L];
             if (n > 0 && c.refs == 2) {
                 switch (XG_LEVEL_SIZE[L]) {
@@ -679,27 +696,32 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l
 /* the result copies of picture set t on the copy stream, after the picture's
  * kernels, so that they overlap the next picture's kernels; then the picture's
  * completion event */
-static void xg_enqueue_results(xin_gpu_stream *s, xin_gpu_stream::Set &t, bool with_me)
+static void xg_enqueue_result_copies(xin_gpu_stream *s, xin_gpu_stream::Set &t, bool with_me, cudaStream_t cst)
 {
     const xin_gpu_stream_cfg &c = s->cfg;
-    cudaEventRecord(t.ev_kern, t.pst);
-    cudaStreamWaitEvent(s->cst, t.ev_kern, 0);
     if (with_me && !c.device_io) {
         size_t lq = (size_t)c.width * c.height, lc = lq / 4;
-        cudaMemcpyAsync(t.h_res, t.dres, sizeof(xin_gpu_cu_result) * s->ncus, cudaMemcpyDeviceToHost, s->cst);
-        if (t.dmts) cudaMemcpyAsync(t.h_mts, t.dmts, sizeof(xin_gpu_cu_mts) * s->ncus, cudaMemcpyDeviceToHost, s->cst);
-        if (t.dbi) cudaMemcpyAsync(t.h_bi, t.dbi, sizeof(xin_gpu_cu_bi) * s->ncus, cudaMemcpyDeviceToHost, s->cst);
+        cudaMemcpyAsync(t.h_res, t.dres, sizeof(xin_gpu_cu_result) * s->ncus, cudaMemcpyDeviceToHost, cst);
+        if (t.dmts) cudaMemcpyAsync(t.h_mts, t.dmts, sizeof(xin_gpu_cu_mts) * s->ncus, cudaMemcpyDeviceToHost, cst);
+        if (t.dbi) cudaMemcpyAsync(t.h_bi, t.dbi, sizeof(xin_gpu_cu_bi) * s->ncus, cudaMemcpyDeviceToHost, cst);
         for (int p = 0; p < 3; p++) {
             size_t n = (p ? lc : lq) * s->nlev;
             if (c.out_flags & XIN_GPU_OUT_Q)
-                cudaMemcpyAsync(t.q_dst[p] ? t.q_dst[p] : t.h_q[p], t.dq[p], n * sizeof(xg_coef), cudaMemcpyDeviceToHost, s->cst);
-            if (c.out_flags & XIN_GPU_OUT_REC) cudaMemcpyAsync(t.h_rec[p], t.drec[p], n * sizeof(xg_pix), cudaMemcpyDeviceToHost, s->cst);
+                cudaMemcpyAsync(t.q_dst[p] ? t.q_dst[p] : t.h_q[p], t.dq[p], n * sizeof(xg_coef), cudaMemcpyDeviceToHost, cst);
+            if (c.out_flags & XIN_GPU_OUT_REC) cudaMemcpyAsync(t.h_rec[p], t.drec[p], n * sizeof(xg_pix), cudaMemcpyDeviceToHost, cst);
         }
     }
     /* the picture's device status (a wait bound reached) */
-    cudaMemcpyAsync(t.h_stat, &t.dpp->status, sizeof(int32_t), cudaMemcpyDeviceToHost, s->cst);
-    cudaEventRecord(t.evs[4], s->cst);
-    cudaEventRecord(t.ev1, s->cst);
+    cudaMemcpyAsync(t.h_stat, &t.dpp->status, sizeof(int32_t), cudaMemcpyDeviceToHost, cst);
+    cudaEventRecord(t.evs[4], cst);
+    cudaEventRecord(t.ev1, cst);
+}
+
+static void xg_enqueue_results(xin_gpu_stream *s, xin_gpu_stream::Set &t, bool with_me)
+{
+    cudaEventRecord(t.ev_kern, t.pst);
+    cudaStreamWaitEvent(s->cst, t.ev_kern, 0);
+    xg_enqueue_result_copies(s, t, with_me, s->cst);
 }
 
 static int xg_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_t ref0, int32_t ref1, xg_coef *const *q_dst);
@@ -709,14 +731,12 @@ extern "C" int xin_gpu_frame_submit_refs(xin_gpu_stream *s, const xin_gpu_pictur
     return xg_frame_submit(s, pic, ref0, ref1, nullptr);
 }
 
-/* q_dst (optional): caller buffers that receive this picture's coefficient planes
- * (XIN_GPU_OUT_Q) straight from the device -- pinned host memory keeps the copy
- * asynchronous -- instead of the picture set's pinned staging */
-static int xg_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_t ref0, int32_t ref1, xg_coef *const *q_dst)
+/* picture nsub of stream s: the checks, the host staging of its samples and its
+ * parameter block (in the picture set's pinned staging); its picture set and
+ * slots */
+struct XgSubmitPlan { int set, cur, l0, l1; };
+static int xg_frame_prepare(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_t ref0, int32_t ref1, XgSubmitPlan &plan)
 {
-    xin_gpu_clear_error();
-    (void)cudaGetLastError();   /* errors of earlier, unrelated calls are not this picture's */
-    if (!s || !pic) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: null argument"); return XIN_GPU_ERR_ARG; }
     if (s->nsub - s->ndone >= 2) {
         xg_set_error(XIN_GPU_ERR_STATE, "frame_submit: two pictures in flight; collect one with frame_wait first");
         return XIN_GPU_ERR_STATE;
@@ -772,6 +792,23 @@ static int xg_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_
         pp.quant[L][2] = pp.quant[L][1];
     }
     *t.h_pp = pp;
+    plan.set = set; plan.cur = cur; plan.l0 = l0; plan.l1 = l1;
+    return XIN_GPU_OK;
+}
+
+/* q_dst (optional): caller buffers that receive this picture's coefficient planes
+ * (XIN_GPU_OUT_Q) straight from the device -- pinned host memory keeps the copy
+ * asynchronous -- instead of the picture set's pinned staging */
+static int xg_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_t ref0, int32_t ref1, xg_coef *const *q_dst)
+{
+    xin_gpu_clear_error();
+    (void)cudaGetLastError();   /* errors of earlier, unrelated calls are not this picture's */
+    if (!s || !pic) { xg_set_error(XIN_GPU_ERR_ARG, "frame_submit: null argument"); return XIN_GPU_ERR_ARG; }
+    XgSubmitPlan plan;
+    if (int e = xg_frame_prepare(s, pic, ref0, ref1, plan)) return e;
+    const int set = plan.set, cur = plan.cur, l0 = plan.l0, l1 = plan.l1;
+    xin_gpu_stream::Set &t = s->set[set];
+    const xin_gpu_stream_cfg &c = s->cfg;
     bool with_me = s->nsub > 0;
     cudaEventRecord(t.ev0, t.pst);
     /* uploads on their own stream, so that they overlap the previous picture's

@@ -62,8 +62,8 @@ __host__ __device__ constexpr int xg_qp_tap(int f, int k)
  * 16-byte-aligned TMA box (padded-plane column 1 + TW bx) */
 #define XG_QP_BW ((XG_QP_TW + 8 + 16 / (int)sizeof(xg_pix) - 1) / (16 / (int)sizeof(xg_pix)) * (16 / (int)sizeof(xg_pix)))
 static_assert(XG_QP_TW * (XG_QP_TH / XG_QP_STRIP) == 256, "pass 2 gives every thread of the CTA one column strip");
-__global__ void __launch_bounds__(256) k_qpel_planes(const __grid_constant__ CUtensorMap tm, XgPlane ref, XgQpel qp,
-                                                      int *status, long long wait_tries)
+__device__ __forceinline__ void xg_qpel_planes_body(const CUtensorMap *tm, const XgPlane &ref, const XgQpel &qp,
+                                                    int *status, long long wait_tries)
 {
     constexpr int TW = XG_QP_TW, TH = XG_QP_TH, HR = TH + 7, ST = XG_QP_STRIP;
     __shared__ __align__(128) xg_pix tbox[HR][XG_QP_BW];
@@ -77,14 +77,18 @@ __global__ void __launch_bounds__(256) k_qpel_planes(const __grid_constant__ CUt
     /* rows y0-3 .. y0+TH+3 and columns x0-3 .. x0+TW+4 of the padded plane by TMA
      * (zeros outside it): the box starts one column earlier, at padded column TW bx */
     if (threadIdx.x == 0) {
-        xg_mbar_init(&tbar, 1);
-        xg_mbar_expect_tx(&tbar, (uint32_t)sizeof tbox);
-        xg_tma_load_2d(&tbox[0][0], &tm, (int)blockIdx.x * TW, (int)blockIdx.y * TH + 1, &tbar);
-        tok = xg_mbar_wait(&tbar, 0, wait_tries) ? 1 : 0;
-        if (!tok) {
-            /* report; once the copy has landed, stage the tile with plain loads */
-            atomicOr(status, XG_STATUS_TMA_WAIT);
-            tok = xg_mbar_wait(&tbar, 0, XG_TMA_WAIT_TRIES) ? 2 : 0;
+        if (!tm) {
+            tok = 2;        /* no map (one not on a 64-byte boundary): plain loads */
+        } else {
+            xg_mbar_init(&tbar, 1);
+            xg_mbar_expect_tx(&tbar, (uint32_t)sizeof tbox);
+            xg_tma_load_2d(&tbox[0][0], tm, (int)blockIdx.x * TW, (int)blockIdx.y * TH + 1, &tbar);
+            tok = xg_mbar_wait(&tbar, 0, wait_tries) ? 1 : 0;
+            if (!tok) {
+                /* report; once the copy has landed, stage the tile with plain loads */
+                atomicOr(status, XG_STATUS_TMA_WAIT);
+                tok = xg_mbar_wait(&tbar, 0, XG_TMA_WAIT_TRIES) ? 2 : 0;
+            }
         }
     }
     __syncthreads();
@@ -143,6 +147,32 @@ __global__ void __launch_bounds__(256) k_qpel_planes(const __grid_constant__ CUt
         }
     }
 }
+
+__global__ void __launch_bounds__(256) k_qpel_planes(const __grid_constant__ CUtensorMap tm, const __grid_constant__ XgPlane ref,
+                                                      const __grid_constant__ XgQpel qp, int *status, long long wait_tries)
+{
+    xg_qpel_planes_body(&tm, ref, qp, status, wait_tries);
+}
+
+/* Pictures of several streams of one shape in one launch (cross-stream
+ * batches): grid z is the picture. */
+#define XG_BATCH_MAX 8
+struct XgQpelBatch {
+    CUtensorMap tm[XG_BATCH_MAX];
+    XgPlane ref[XG_BATCH_MAX];
+    XgQpel qp[XG_BATCH_MAX];
+    int *status[XG_BATCH_MAX];
+    long long wait_tries;
+};
+static_assert(alignof(XgQpelBatch) % 64 == 0 && offsetof(XgQpelBatch, tm) == 0 && sizeof(CUtensorMap) % 64 == 0,
+              "each picture's TMA map on a 64-byte boundary of the parameter");
+__global__ void __launch_bounds__(256) k_qpel_planes_batch(const __grid_constant__ XgQpelBatch b)
+{
+    const int i = blockIdx.z;
+    const CUtensorMap *tm = &b.tm[i];
+    xg_qpel_planes_body(((uintptr_t)tm & 63) ? nullptr : tm, b.ref[i], b.qp[i], b.status[i], b.wait_tries);
+}
+
 
 /* -------------------------------------------------------------- k_me_tiles
  * Grid: (tiles_x, tiles_y, bands).  A CTA takes one 64x64 tile and one band of
@@ -204,10 +234,9 @@ enum XgFillMode {
  * one row with one 16-byte (8-byte) store: the margins are multiples of 16
  * samples and the slot's data and pitch multiples of 32 / 128, so a group starts
  * on a 16-byte boundary. */
-__global__ void __launch_bounds__(128) k_fill_slot(XgPlane y, XgPlane u, XgPlane v, const XgPicParams *pp, const uint8_t *s0,
-                                                   const uint8_t *s1, const uint8_t *s2, int mode)
+__device__ __forceinline__ void xg_fill_slot_body(const XgPlane &y, const XgPlane &u, const XgPlane &v, const XgPicParams *pp,
+                                                  const uint8_t *s0, const uint8_t *s1, const uint8_t *s2, int mode, int pl)
 {
-    const int pl = blockIdx.z;
     XgPlane d = y;
     if (pl == 1) d = u;
     else if (pl == 2) d = v;
@@ -244,6 +273,27 @@ __global__ void __launch_bounds__(128) k_fill_slot(XgPlane y, XgPlane u, XgPlane
         for (int j = 0; j < 8 && x0 + j < d.w + d.pad; j++) o[j] = vals[j];
     }
 }
+
+__global__ void __launch_bounds__(128) k_fill_slot(const __grid_constant__ XgPlane y, const __grid_constant__ XgPlane u,
+                                                   const __grid_constant__ XgPlane v, const XgPicParams *pp, const uint8_t *s0,
+                                                   const uint8_t *s1, const uint8_t *s2, int mode)
+{
+    xg_fill_slot_body(y, u, v, pp, s0, s1, s2, mode, blockIdx.z);
+}
+
+/* cross-stream batch: grid z = 3 x picture + plane; one fill mode for all */
+struct XgFillBatch {
+    XgPlane pl[XG_BATCH_MAX][3];
+    const XgPicParams *pp[XG_BATCH_MAX];
+    const uint8_t *s8[XG_BATCH_MAX][3];
+    int mode;
+};
+__global__ void __launch_bounds__(128) k_fill_slot_batch(const __grid_constant__ XgFillBatch b)
+{
+    const int i = blockIdx.z / 3, pl = blockIdx.z % 3;
+    xg_fill_slot_body(b.pl[i][0], b.pl[i][1], b.pl[i][2], b.pp[i], b.s8[i][0], b.s8[i][1], b.s8[i][2], b.mode, pl);
+}
+
 
 /* packed 8-bit SAD throughput probe: vabsdiff4 + dp4a on register data */
 __global__ void k_sad_peak(const uint32_t *in, uint32_t *out, int iters)
@@ -386,357 +436,24 @@ static_assert(xg_me_d(8) % 4 == 0 && (1 << xg_me_db(8)) == xg_me_d(8) && xg_me_d
 template <int SBD>
 __global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles(XgMeParams p, const XgPicParams *pp)
 {
-    constexpr int XG_ME_D = xg_me_d(SBD), XG_ME_DB = xg_me_db(SBD), XG_ME_SLOTS = 32 * XG_ME_D;
-    constexpr int SH = XG_BITDEPTH - SBD;  /* sample shift to the search depth; the SADs scale back by 1 << SH */
-    extern __shared__ uint32_t sm[];
-    __shared__ int swin[16][5][4];        /* per warp: windows of its four 8x8 CUs and its 16x16 CU */
-    __shared__ int swin32[4][4], swin64[4];
-    __shared__ int sinterior[16], sinterior32[4];
-    const int tx0 = blockIdx.x * XG_ME_TILE, ty0 = blockIdx.y * XG_ME_TILE;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nx = 2 * p.R + 1;
-    const int dyb0 = -p.R + (int)blockIdx.z * p.band_rows;
-    const int ndy = min(p.band_rows, p.R - dyb0 + 1);
-    const int nch = (ndy + XG_ME_D - 1) / XG_ME_D;          /* chunks of XG_ME_D candidate rows */
-    const int nv = nch * nx;                                 /* (chunk, column) slots, one per lane and pass */
-    const int rows = XG_ME_TILE + nch * XG_ME_D - 1;         /* band rows staged */
+    const int band = blockIdx.z;
+#include "xg_me_tiles_body.inc"
+}
 
-    const int relw = xg_me_relw(SBD, nx);                         /* word positions read per band row */
-    uint32_t *refw = sm + xg_me_cur_words(SBD);                   /* [rows][row_words] */
-    uint32_t *mvcx = refw + (size_t)p.band_rows_alloc * p.row_words; /* [nx] */
-    uint32_t *mvcy = mvcx + nx;                              /* [band_rows rounded to XG_ME_D] */
-    const int nb = p.agg_passes;
-    uint32_t *s16 = mvcy + p.band_rows_alloc;                /* [2][16][XG_ME_SLOTS] */
-    uint32_t *s32r = s16 + 2 * 16 * XG_ME_SLOTS;             /* [2][nb][4][XG_ME_SLOTS] */
-    /* current tile, 16-byte aligned: 8-bit [64][16] (pixels 4k .. 4k+3), 10-bit [64][32] (pixels 2k, 2k+1) */
-    uint32_t *scur = sm;
-
-    /* ---- stage the reference band: pixels (X0 + x .., Y0 + r) -> refw[r * row_words + x].
-     * Group g of band row r is the 8 word positions x = 8g + j - off (j < 8) whose
-     * pixels start at the aligned column A + 8g (A = X0 rounded down to 8, off = X0
-     * - A); a lane reads its pixels A + 8g .. with one 8- or 16-byte load (the slot
-     * layout keeps data and pitch multiples of 32 / 128 elements) plus a short
-     * load of the next pixels when a stored word reaches them (so reads stay
-     * within the right margin), and forms the words with byte permutes.  A warp
-     * covers 8 rows x 4 groups, lane = (row & 7) * 4 + (group & 3): the row pitch
-     * is odd, so the 32 lanes' stores of one j fall in 32 different banks. */
-    const int X0 = tx0 - p.R, Y0 = ty0 + dyb0;
-    {
-        const int A = X0 & ~7, off = X0 - A;
-        const int ngrp = (relw + off + 7) >> 3, ngb = (ngrp + 3) >> 2, nrb = (rows + 7) >> 3;
-        const int need = off + relw + (SBD == 8 ? 2 : 0);    /* last pixel a stored word uses, from A */
-        for (int T = warp; T < nrb * ngb; T += XG_ME_THREADS / 32) {
-            const int rb = T / ngb, r = rb * 8 + (lane >> 2), g = (T - rb * ngb) * 4 + (lane & 3);
-            if (r >= rows || g >= ngrp) continue;
-            const xg_pix *src = p.ref.data + (intptr_t)(Y0 + r) * p.ref.pitch + A + 8 * g;
-            const bool more = 8 * g + 8 <= need;
-            uint32_t wd[8];
-            if constexpr (SBD == 8) {
-                uint32_t b0, b1, b2;                                /* pixel bytes 0-3, 4-7, 8-11 */
-                if constexpr (sizeof(xg_pix) == 1) {
-                    const uint2 c = *reinterpret_cast<const uint2 *>(src);
-                    b0 = c.x; b1 = c.y;
-                    b2 = more ? *reinterpret_cast<const uint32_t *>(src + 8) : 0u;
-                } else {
-                    const uint4 c = *reinterpret_cast<const uint4 *>(src);
-                    const uint2 n = more ? *reinterpret_cast<const uint2 *>(src + 8) : make_uint2(0u, 0u);
-                    /* two 16-bit samples per word -> their >> SH bytes in lanes 0 and 2 */
-                    auto lo = [](uint32_t u) { return (u >> SH) & 0x00ff00ffu; };
-                    b0 = __byte_perm(lo(c.x), lo(c.y), 0x6420);
-                    b1 = __byte_perm(lo(c.z), lo(c.w), 0x6420);
-                    b2 = __byte_perm(lo(n.x), lo(n.y), 0x6420);
-                }
-                wd[0] = b0; wd[1] = __byte_perm(b0, b1, 0x4321); wd[2] = __byte_perm(b0, b1, 0x5432); wd[3] = __byte_perm(b0, b1, 0x6543);
-                wd[4] = b1; wd[5] = __byte_perm(b1, b2, 0x4321); wd[6] = __byte_perm(b1, b2, 0x5432); wd[7] = __byte_perm(b1, b2, 0x6543);
-            } else {
-                const uint4 c = *reinterpret_cast<const uint4 *>(src);
-                const uint32_t n = more ? *reinterpret_cast<const uint32_t *>(src + 8) : 0u;
-                const uint32_t u[5] = { c.x, c.y, c.z, c.w, n };
-#pragma unroll
-                for (int k = 0; k < 4; k++) { wd[2 * k] = u[k]; wd[2 * k + 1] = __byte_perm(u[k], u[k + 1], 0x5432); }
-            }
-            uint32_t *dst = refw + r * p.row_words;
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const int x = 8 * g + j - off;
-                if ((unsigned)x < (unsigned)relw) dst[x] = wd[j];
-            }
-        }
-    }
-    const uint32_t lambda = pp->lambda;
-    /* MV-bit costs in key form: column bits * lambda << XG_ME_DB, and row bits *
-     * lambda << XG_ME_DB plus the row's index within its chunk, so that the
-     * key of candidate row d of a chunk is SAD * key_mul + mvcx[col] + mvcy[row].
-     * Rows past the band (the last chunk's padding) get a sentinel that lifts
-     * their keys to >= XG_ME_KEY_INVALID without wrapping (lambda <= 2^20 keeps
-     * real keys below 2^30). */
-    for (int i = threadIdx.x; i < nx; i += blockDim.x) mvcx[i] = (xg_mvd_bits(4 * (i - p.R)) * lambda) << XG_ME_DB;
-    for (int i = threadIdx.x; i < nch * XG_ME_D; i += blockDim.x)
-        mvcy[i] = (i < ndy ? (xg_mvd_bits(4 * (dyb0 + i)) * lambda) << XG_ME_DB : XG_ME_KEY_INVALID) + (uint32_t)(i & (XG_ME_D - 1));
-
-    /* ---- the current tile in shared memory (read as broadcasts) */
-    const int bx = (warp & 3) * 16, by = (warp >> 2) * 16;
-    if constexpr (SBD == 8) {
-        for (int i = threadIdx.x; i < 64 * 16; i += blockDim.x) {
-            const xg_pix *c = p.cur.data + (intptr_t)(ty0 + (i >> 4)) * p.cur.pitch + tx0 + 4 * (i & 15);
-            scur[i] = (uint32_t)(c[0] >> SH) | ((uint32_t)(c[1] >> SH) << 8) | ((uint32_t)(c[2] >> SH) << 16) |
-                      ((uint32_t)(c[3] >> SH) << 24);
-        }
-    } else {
-        for (int i = threadIdx.x; i < 64 * 32; i += blockDim.x) {
-            const xg_pix *c = p.cur.data + (intptr_t)(ty0 + (i >> 5)) * p.cur.pitch + tx0 + 2 * (i & 31);
-            scur[i] = (uint32_t)c[0] | ((uint32_t)c[1] << 16);
-        }
-    }
-
-    /* ---- windows and liveness of this warp's CUs; a band inside every window needs no per-candidate check */
-    /* the running best of each CU as (cost << 32) | raster index; none = a cost
-     * no valid key reaches (keys >= XG_ME_KEY_INVALID have cost >= its value) */
-    constexpr unsigned long long NONE = (unsigned long long)(XG_ME_KEY_INVALID >> XG_ME_DB) << 32;
-    bool live[5];
-    unsigned long long best[5];
-#pragma unroll
-    for (int c = 0; c < 5; c++) {
-        int s = c < 4 ? 8 : 16;
-        int cx = tx0 + bx + (c < 4 ? (c & 1) * 8 : 0), cy = ty0 + by + (c < 4 ? (c >> 1) * 8 : 0);
-        live[c] = p.keys[c < 4 ? 3 : 2] && cx + s <= p.W && cy + s <= p.H;
-        if (lane == 0) xg_cu_window(p, cx, cy, s, swin[warp][c][0], swin[warp][c][1], swin[warp][c][2], swin[warp][c][3]);
-        best[c] = NONE;
-    }
-    if (threadIdx.x < 4) {
-        int c32x = tx0 + (threadIdx.x & 1) * 32, c32y = ty0 + (threadIdx.x >> 1) * 32;
-        xg_cu_window(p, c32x, c32y, 32, swin32[threadIdx.x][0], swin32[threadIdx.x][1], swin32[threadIdx.x][2], swin32[threadIdx.x][3]);
-        const int *w = swin32[threadIdx.x];
-        sinterior32[threadIdx.x] = w[0] <= -p.R && w[1] >= p.R && w[2] <= dyb0 && w[3] >= dyb0 + ndy - 1;
-    }
-    if (threadIdx.x == 0) xg_cu_window(p, tx0, ty0, 64, swin64[0], swin64[1], swin64[2], swin64[3]);
-    __syncwarp();
-    if (lane == 0) {
-        bool in = true;
-        for (int c = 0; c < 5; c++)
-            in = in && swin[warp][c][0] <= -p.R && swin[warp][c][1] >= p.R && swin[warp][c][2] <= dyb0 && swin[warp][c][3] >= dyb0 + ndy - 1;
-        sinterior[warp] = in;
-    }
-    /* 32x32: this warp's quadrant c32 and its rank jq among the quadrant's four
-     * warps (it evaluates candidate rows jq * XG_ME_D / 4 .. of each pass);
-     * 64x64: threads t < XG_ME_SLOTS, candidate slot t */
-    const int c32 = ((warp >> 1) & 1) + ((warp >> 3) << 1), jq = (warp & 1) + ((warp >> 1) & 2);
-    const int c32x = tx0 + (c32 & 1) * 32, c32y = ty0 + (c32 >> 1) * 32;
-    const bool live32 = p.keys[1] && c32x + 32 <= p.W && c32y + 32 <= p.H;
-    const bool live64 = threadIdx.x < XG_ME_SLOTS && p.keys[0] && tx0 + 64 <= p.W && ty0 + 64 <= p.H;
-    const int w32 = (c32 & 1) * 2 + (c32 >> 1) * 8;          /* first warp of the quadrant: w32, +1, +4, +5 */
-    unsigned long long best32 = NONE, best64 = ~0ull;
-    __syncthreads();
-    const bool interior = sinterior[warp], interior32 = sinterior32[c32];
-
-    /* key = SAD * key_mul + MV bits (a multiplier read at run time keeps the key
-     * arithmetic on the multiply-add pipe, beside the SADs on the integer pipe);
-     * key_mul = 1 << (XG_COST_FRACTION + XG_ME_DB + SH) */
-    const uint32_t kmul = p.key_mul;
-    /* the same for the 32x32 costs: cost = SAD32 * cmul + MV bits */
-    const uint32_t cmul = kmul >> XG_ME_DB;
-    /* v / nx = umulhi(v, nx_rcp) for every v < 2^17 and odd nx in 3..513 (checked exhaustively) */
-    const uint32_t nx_rcp = 0xFFFFFFFFu / (uint32_t)nx + 1u;
-    const int npass = (nv + 31) / 32;
-    /* this lane's slot v = pz * 32 + lane as (chunk, column), advanced by 32 slots a pass */
-    int chunk = 0, col = lane;
-    while (col >= nx) { col -= nx; chunk++; }
-    int pb = 0, grp = 0;                                     /* pass within the buffered group, group parity */
-    for (int pz = 0; pz < npass; pz++) {
-        const bool vvalid = chunk < nch;
-        /* lanes past the last slot repeat slot nv - 1: same key, no effect */
-        const int ck = vvalid ? chunk : nch - 1, cl = vvalid ? col : nx - 1;
-        const int row0 = ck * XG_ME_D, dx = cl - p.R, dyl = dyb0 + row0;
-        const uint32_t gidx0 = (uint32_t)((dyl + p.R) * nx + cl);   /* raster index of candidate row 0 of the slot */
-        const uint32_t mx = mvcx[cl];
-        {
-            const uint32_t *base = refw + (by + row0) * p.row_words + bx + cl;
-            uint32_t acc[XG_ME_D][4];
-#pragma unroll
-            for (int d = 0; d < XG_ME_D; d++)
-#pragma unroll
-                for (int b = 0; b < 4; b++) acc[d][b] = 0;
-            /* reference row t of the block feeds current row t - d of candidate row d */
-            if constexpr (SBD == 8) {
-            uint32_t cw[XG_ME_D][4];          /* current rows t .. t-XG_ME_D+1 (slot = row % XG_ME_D) */
-            const uint32_t *crow = scur + by * 16 + (bx >> 2);
-#pragma unroll
-            for (int t = 0; t < 16 + XG_ME_D - 1; t++) {
-                if (t < 16) {
-                    const uint4 c4 = *(const uint4 *)(crow + t * 16);
-                    cw[t % XG_ME_D][0] = c4.x; cw[t % XG_ME_D][1] = c4.y; cw[t % XG_ME_D][2] = c4.z; cw[t % XG_ME_D][3] = c4.w;
-                }
-                const uint32_t *q = base + t * p.row_words;
-                const uint32_t w0 = q[0], w1 = q[4], w2 = q[8], w3 = q[12];
-#pragma unroll
-                for (int d = 0; d < XG_ME_D; d++) {
-                    const int r = t - d;
-                    if (r >= 0 && r < 16) {
-                        const int b = r < 8 ? 0 : 2;
-                        const uint32_t *c = cw[r % XG_ME_D];
-                        acc[d][b] = xg_sad4(c[0], w0, acc[d][b]);
-                        acc[d][b] = xg_sad4(c[1], w1, acc[d][b]);
-                        acc[d][b + 1] = xg_sad4(c[2], w2, acc[d][b + 1]);
-                        acc[d][b + 1] = xg_sad4(c[3], w3, acc[d][b + 1]);
-                    }
-                }
-            }
-            /* 8-bit samples of 10-bit pictures: the SADs stay at 8 bits here; key_mul
-             * and the 32x32 / 64x64 costs scale them by 1 << SH, the 10-bit SAD */
-            } else {
-            uint32_t cw[XG_ME_D][8], cn[XG_ME_D][8];   /* current rows t .. t-XG_ME_D+1 (slot = row % XG_ME_D), negated */
-            const uint32_t *crow = scur + by * 32 + (bx >> 1);
-#pragma unroll
-            for (int t = 0; t < 16 + XG_ME_D - 1; t++) {
-                if (t < 16) {
-                    const uint4 lo = *(const uint4 *)(crow + t * 32), hi = *(const uint4 *)(crow + t * 32 + 4);
-                    uint32_t *w = cw[t % XG_ME_D], *wn = cn[t % XG_ME_D];
-                    w[0] = lo.x; w[1] = lo.y; w[2] = lo.z; w[3] = lo.w; w[4] = hi.x; w[5] = hi.y; w[6] = hi.z; w[7] = hi.w;
-#pragma unroll
-                    for (int k = 0; k < 8; k++) wn[k] = XG_NEG2(w[k]);
-                }
-                const uint32_t *q = base + t * p.row_words;
-                uint32_t rw[8], rn[8];
-#pragma unroll
-                for (int k = 0; k < 8; k++) { rw[k] = q[2 * k]; rn[k] = XG_NEG2(rw[k]); }
-#pragma unroll
-                for (int d = 0; d < XG_ME_D; d++) {
-                    const int r = t - d;
-                    if (r >= 0 && r < 16) {
-                        const int b = r < 8 ? 0 : 2;
-                        const uint32_t *c = cw[r % XG_ME_D], *cng = cn[r % XG_ME_D];
-#pragma unroll
-                        for (int k = 0; k < 8; k += 2)
-                            acc[d][b + (k >> 2)] += xg_absdiff2_biased(c[k], cng[k], rw[k], rn[k]) +
-                                                    xg_absdiff2_biased(c[k + 1], cng[k + 1], rw[k + 1], rn[k + 1]);
-                    }
-                }
-            }
-            /* lanes -> SAD: both lanes summed, less the bias of 64 pixels x 1024 */
-#pragma unroll
-            for (int d = 0; d < XG_ME_D; d++)
-#pragma unroll
-                for (int b = 0; b < 4; b++) acc[d][b] = (acc[d][b] & 0xffffu) + (acc[d][b] >> 16) - 64u * 1024u;
-            }
-            /* Per CU, the best of the lane's XG_ME_D candidates (same column, rows
-             * row0 + d: raster order = d order) as one key (cost << XG_ME_DB) | d, then
-             * a (cost, raster index) compare with the lane's running best.  Keys of
-             * candidates outside the band or the window are >= XG_ME_KEY_INVALID,
-             * above any real key (costs stay below 2^27). */
-            uint32_t md[XG_ME_D];
-#pragma unroll
-            for (int d = 0; d < XG_ME_D; d++) md[d] = mx + mvcy[row0 + d];
-            auto search = [&](auto check) {
-                /* the 16x16 CU first: its SADs also go to the 32x32 exchange */
-                uint32_t *s16w = s16 + (pz & 1) * 16 * XG_ME_SLOTS + warp * XG_ME_SLOTS + lane;
-#pragma unroll
-                for (int ci = 0; ci < 5; ci++) {
-                    const int c = (ci + 4) % 5;
-                    uint32_t kd[XG_ME_D];
-#pragma unroll
-                    for (int d = 0; d < XG_ME_D; d++) {
-                        uint32_t sad;
-                        if (c == 4) {
-                            sad = acc[d][0] + acc[d][1] + acc[d][2] + acc[d][3];
-                            s16w[d * 32] = sad;
-                        } else {
-                            sad = acc[d][c];
-                        }
-                        kd[d] = sad * kmul + md[d];
-                        if constexpr (decltype(check)::value) {
-                            const int dy = dyl + d;
-                            if (!(dx >= swin[warp][c][0] && dx <= swin[warp][c][1] && dy >= swin[warp][c][2] && dy <= swin[warp][c][3]))
-                                kd[d] = 0xFFFFFFFFu;
-                        }
-                    }
-                    /* the minimum of the keys with three-input minima */
-                    uint32_t k;
-                    if constexpr (XG_ME_D == 8)
-                        k = min(__vimin3_u32(kd[0], kd[1], kd[2]), __vimin3_u32(__vimin3_u32(kd[3], kd[4], kd[5]), kd[6], kd[7]));
-                    else
-                        k = min(__vimin3_u32(kd[0], kd[1], kd[2]), kd[3]);
-                    const unsigned long long kk =
-                        ((unsigned long long)(k >> XG_ME_DB) << 32) | (gidx0 + (k & (XG_ME_D - 1)) * (uint32_t)nx);
-                    best[c] = kk < best[c] ? kk : best[c];
-                }
-            };
-            if (interior) search(xg_bool_c<false>());
-            else search(xg_bool_c<true>());
-        }
-        /* 32x32: the quadrant's four warps swap their 16x16 SADs (double-buffered by
-         * pass parity: a buffer is rewritten two passes later, after the next
-         * barrier, when every warp has read it) */
-        {
-            asm volatile("bar.sync %0, 128;" ::"r"(1 + c32) : "memory");
-#pragma unroll
-            for (int e = 0; e < XG_ME_D / 4; e++) {
-                const int d = jq * (XG_ME_D / 4) + e, row = ck * XG_ME_D + d;
-                const uint32_t *r16 = s16 + (pz & 1) * 16 * XG_ME_SLOTS + d * 32 + lane;
-                const uint32_t s32 = r16[w32 * XG_ME_SLOTS] + r16[(w32 + 1) * XG_ME_SLOTS] + r16[(w32 + 4) * XG_ME_SLOTS] +
-                                     r16[(w32 + 5) * XG_ME_SLOTS];
-                s32r[((grp * nb + pb) * 4 + c32) * XG_ME_SLOTS + d * 32 + lane] = s32;
-                /* rows past the band carry the sentinel (cost >= NONE's, never taken); lanes
-                 * past the last slot repeat slot nv - 1; CUs outside the picture are not
-                 * published */
-                const uint32_t cost = s32 * cmul + ((mx + mvcy[row]) >> XG_ME_DB);
-                const unsigned long long kk = ((unsigned long long)cost << 32) | (gidx0 + (uint32_t)d * (uint32_t)nx);
-                bool in = true;
-                if (!interior32) {
-                    const int dy = dyb0 + row;
-                    in = dx >= swin32[c32][0] && dx <= swin32[c32][1] && dy >= swin32[c32][2] && dy <= swin32[c32][3];
-                }
-                if (in && kk < best32) best32 = kk;
-            }
-        }
-        /* 64x64 every nb passes, from the four quadrants' 32x32 SADs (the ring is
-         * double-buffered by group: a group's half is rewritten only after the
-         * next full barrier, which the reading threads reach after reading) */
-        if (pb == nb - 1 || pz == npass - 1) {
-            __syncthreads();
-            if (live64) {
-                const int d = threadIdx.x / 32, pz0 = pz - pb;
-                const uint32_t *r32 = s32r + grp * nb * 4 * XG_ME_SLOTS + threadIdx.x;
-                for (int j = 0; j <= pb; j++) {
-                    const uint32_t v = (uint32_t)((pz0 + j) * 32 + lane);
-                    const int chj = (int)__umulhi(v, nx_rcp), colj = (int)v - chj * nx, row = chj * XG_ME_D + d;
-                    if ((int)v < nv && row < ndy) {
-                        const uint32_t *q32 = r32 + j * 4 * XG_ME_SLOTS;
-                        const uint32_t s64 = q32[0] + q32[XG_ME_SLOTS] + q32[2 * XG_ME_SLOTS] + q32[3 * XG_ME_SLOTS];
-                        const int dx = colj - p.R, dy = dyb0 + row;
-                        const uint32_t c64 = (s64 << (XG_COST_FRACTION + SH)) + ((mvcx[colj] + mvcy[row]) >> XG_ME_DB);
-                        const unsigned long long kk = ((unsigned long long)c64 << 32) | (uint32_t)((dy + p.R) * nx + colj);
-                        if (dx >= swin64[0] && dx <= swin64[1] && dy >= swin64[2] && dy <= swin64[3] && kk < best64) best64 = kk;
-                    }
-                }
-            }
-        }
-        col += 32;
-        while (col >= nx) { col -= nx; chunk++; }
-        if (++pb == nb) { pb = 0; grp ^= 1; }
-    }
-
-    /* ---- publish: warp minimum of packed keys, then one atomicMin per CU and CTA */
-#pragma unroll
-    for (int c = 0; c < 5; c++) {
-        unsigned long long k = best[c];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) { unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o); k = v < k ? v : k; }
-        if (lane == 0 && live[c] && k < NONE) {
-            int s = c < 4 ? 8 : 16, L = c < 4 ? 3 : 2;
-            int cx = tx0 + bx + (c < 4 ? (c & 1) * 8 : 0), cy = ty0 + by + (c < 4 ? (c >> 1) * 8 : 0);
-            atomicMin(p.keys[L] + (cy / s) * p.cus_x[L] + cx / s, k);
-        }
-    }
-    {
-        unsigned long long k = best32;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) { unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o); k = v < k ? v : k; }
-        if (lane == 0 && live32 && k < NONE) atomicMin(p.keys[1] + (c32y / 32) * p.cus_x[1] + c32x / 32, k);
-        k = best64;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) { unsigned long long v = __shfl_xor_sync(0xffffffffu, k, o); k = v < k ? v : k; }
-        if (lane == 0 && live64 && k != ~0ull) atomicMin(p.keys[0] + (ty0 / 64) * p.cus_x[0] + tx0 / 64, k);
-    }
+/* cross-stream batch: grid z = bands x picture + band (one band geometry for
+ * all); the body is included again, as for k_cu_tail_batch */
+struct XgMeBatch {
+    XgMeParams p[XG_BATCH_MAX];
+    const XgPicParams *pp[XG_BATCH_MAX];
+    int bands;
+};
+template <int SBD>
+__global__ void __launch_bounds__(XG_ME_THREADS, 1) k_me_tiles_batch(const __grid_constant__ XgMeBatch b)
+{
+    const int item = blockIdx.z / b.bands, band = blockIdx.z - item * b.bands;
+    const XgMeParams &p = b.p[item];
+    const XgPicParams *pp = b.pp[item];
+#include "xg_me_tiles_body.inc"
 }
 
 /* -------------------------------------------------------------- k_cu_tail */
@@ -1257,226 +974,25 @@ __device__ uint32_t xg_satd_blocks(const xg_pix *org, intptr_t op, const xg_pix 
 template <int S, int NT, int CPB, bool BI>
 __global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, BI)) k_cu_tail(XgTailParams p, const XgPicParams *pp, int ncu)
 {
-    constexpr int C = S / 2, TL = xg_tu_luma(S), TC = xg_tu_chroma(S);
-    extern __shared__ __align__(16) unsigned char xg_tail_raw[];
-    XgTailSmem<S, NT> *shm = reinterpret_cast<XgTailSmem<S, NT> *>(xg_tail_raw);
-    const int g = threadIdx.x / NT, tid = threadIdx.x % NT;
-    const int cu = blockIdx.x * CPB + g;
-    if (cu >= ncu) return;          /* whole groups only: no barrier is shared with a missing group */
-    XgTailSmem<S, NT> &m = shm[g];
-    XgTqSmem<TL> &tl = m.tl;
-    XgTqSmem<TC> &tc = m.tc;
-    xg_pix *pred = m.pred;
-    const int cx = (cu % p.cus_x) * S, cy = (cu / p.cus_x) * S;
-    const unsigned long long key = p.keys[cu];
-    const int nx = 2 * p.R + 1;
-    const uint32_t lambda = pp->lambda;
-    if (tid < 3) { m.nz[tid] = 0; m.ssd[tid] = 0; }
-    {   /* DCT2 matrices of the luma and chroma TUs, rows k < 32 */
-        constexpr int lgl = TL == 8 ? 3 : TL == 16 ? 4 : TL == 32 ? 5 : 6, lgc = TC == 4 ? 2 : TC == 8 ? 3 : TC == 16 ? 4 : 5;
-        const int16_t *ml = xg_mat(0, lgl), *mc = xg_mat(0, lgc);
-        xg_tq_load_mat<TL, NT>(tl, ml, tid);
-        xg_tq_load_mat<TC, NT>(tc, mc, tid);
-    }
+#include "xg_cu_tail_body.inc"
+}
 
-    /* window (h266_enc_init.c:1462) */
-    const int mnx = (int16_t)(-cx - p.ctu - 8), mny = (int16_t)(-cy - p.ctu - 8);
-    const int mxx = (int16_t)(p.W + (p.ctu - S + 8) - cx), mxy = (int16_t)(p.H + (p.ctu - S + 8) - cy);
-    auto in_window = [&](int qx, int qy) { return (qx >> 2) >= mnx && (qy >> 2) >= mny && (qx >> 2) <= mxx && (qy >> 2) <= mxy; };
-
-    /* ---- list 0: Xin266FullSubPelMe from the integer search's best, when its
-     * integer MV lies in the window (h266_sub_pel_refine.c:117-120) */
-    const xg_pix *org = p.cur[0].data + (intptr_t)cy * p.cur[0].pitch + cx;
-    const intptr_t opitch = p.cur[0].pitch;
-    int mvx, mvy;
-    uint32_t bc = (uint32_t)(key >> 32);
-    {
-        const int gidx = (int)(uint32_t)key;
-        mvx = 4 * (gidx % nx - p.R); mvy = 4 * (gidx / nx - p.R);
-        if (in_window(mvx, mvy)) xg_subpel<S, NT, CPB>(org, opitch, p.qpel, cx, cy, lambda, m.part, g, tid, mvx, mvy, bc);
-    }
-
-    /* the prediction coded: list 0, or (refs 2) the lowest of list 0, list 1 and the pair */
-    int dir = 1;
-    int mv1x = 0, mv1y = 0, b0x = mvx, b0y = mvy, b1x = 0, b1y = 0;   /* list 1's MV; the bi pair */
-    uint32_t bc1 = 0, bi_cost = 0;
-    if constexpr (BI) {
-        XgTailBiSmem<S> &bs = reinterpret_cast<XgTailBiSmem<S> *>(xg_tail_raw + sizeof(XgTailSmem<S, NT>) * CPB)[g];
-        const unsigned long long key1 = p.keys1[cu];
-        bc1 = (uint32_t)(key1 >> 32);
-        {
-            const int gidx = (int)(uint32_t)key1;
-            mv1x = 4 * (gidx % nx - p.R); mv1y = 4 * (gidx / nx - p.R);
-            if (in_window(mv1x, mv1y))
-                xg_subpel<S, NT, CPB>(org, opitch, p.qpel1, cx, cy, lambda, m.part, g, tid, mv1x, mv1y, bc1);
-        }
-        /* Xin266InterBiSearch (h266_analyze_inter_cu.c:507-870; one reference per list,
-         * default BCW weight, two iterations, predictor 0): the list with the larger uni
-         * cost is refined first against clip(2 org - the other list's prediction), from
-         * the integer part of its uni MV: integer step, then Xin266FullSubPelMe; the pair
-         * is costed by the SAD against the average of the two predictions and kept when
-         * it improves; the final cost is taken on the last predictions (:815-852) */
-        b1x = mv1x; b1y = mv1y;
-        xg_luma_uni<S, NT>(p.qpel, cx, cy, mvx, mvy, mnx, mny, mxx, mxy, bs.bp[0], tid);
-        xg_luma_uni<S, NT>(p.qpel1, cx, cy, mv1x, mv1y, mnx, mny, mxx, mxy, bs.bp[1], tid);
-        xg_gsync<NT, CPB>(g);
-        /* the preset-4 TU stage (satdMd): SATD is the decision's distortion --
-         * pfXinComputeAvgDist is the averaged SATD (h266_encoder_create.c:3336-3345)
-         * and each list's uni cost its final prediction's SATD cost
-         * (h266_analyze_inter_cu.c:1103-1131) */
-        const bool satd = p.resid[0] != nullptr;
-        uint32_t uc0 = bc, uc1 = bc1;
-        if (satd) {
-            uc0 = (xg_satd_blocks<S, NT, CPB>(org, opitch, bs.bp[0], nullptr, m.part, g, tid) << XG_COST_FRACTION) +
-                  (xg_mvd_bits(mvx) + xg_mvd_bits(mvy)) * lambda;
-            uc1 = (xg_satd_blocks<S, NT, CPB>(org, opitch, bs.bp[1], nullptr, m.part, g, tid) << XG_COST_FRACTION) +
-                  (xg_mvd_bits(mv1x) + xg_mvd_bits(mv1y)) * lambda;
-        }
-        auto dist2 = [&]() {
-            return satd ? xg_satd_blocks<S, NT, CPB>(org, opitch, bs.bp[0], bs.bp[1], m.part, g, tid)
-                        : xg_avg_sad<S, NT, CPB>(org, opitch, bs.bp[0], bs.bp[1], m.part, g, tid);
-        };
-        int li = uc0 <= uc1 ? 1 : 0;
-        uint32_t best = 0xFFFFFFFFu;
-        for (int it = 0; it < 2; it++, li ^= 1) {
-            const xg_pix *other = bs.bp[1 - li];
-            for (int i = tid; i < S * S; i += NT) {
-                const int x = i % S, y = i / S;
-                bs.tgt[i] = (xg_pix)xg_clip_pix(2 * (int)org[(intptr_t)y * opitch + x] - (int)other[i]);
-            }
-            xg_gsync<NT, CPB>(g);
-            int ix, iy;
-            uint32_t ic;
-            xg_bi_square<S, NT, CPB>(bs.tgt, li ? p.ref1[0] : p.ref[0], cx, cy, (li ? mv1x : mvx) >> 2, (li ? mv1y : mvy) >> 2,
-                                     mnx, mny, mxx, mxy, lambda, m.part, g, tid, ix, iy, ic);
-            if (in_window(ix, iy))
-                xg_subpel<S, NT, CPB>(bs.tgt, S, li ? p.qpel1 : p.qpel, cx, cy, lambda, m.part, g, tid, ix, iy, ic);
-            xg_luma_uni<S, NT>(li ? p.qpel1 : p.qpel, cx, cy, ix, iy, mnx, mny, mxx, mxy, bs.bp[li], tid);
-            xg_gsync<NT, CPB>(g);
-            const uint32_t sad = dist2();
-            const uint32_t c = (sad << XG_COST_FRACTION) + (xg_mvd_bits(ix) + xg_mvd_bits(iy) + xg_mvd_bits(li ? b0x : b1x) +
-                                                            xg_mvd_bits(li ? b0y : b1y)) * lambda;
-            if (c < best) {
-                best = c;
-                if (li) { b1x = ix; b1y = iy; } else { b0x = ix; b0y = iy; }
-            }
-        }
-        const uint32_t sad = dist2();
-        bi_cost = (sad << XG_COST_FRACTION) + (xg_mvd_bits(b0x) + xg_mvd_bits(b0y) + xg_mvd_bits(b1x) + xg_mvd_bits(b1y)) * lambda;
-        uint32_t ubest = uc0;
-        if (uc1 < ubest) { ubest = uc1; dir = 2; }
-        if (bi_cost < ubest) dir = 3;
-    }
-    /* the coded MV of each list (1/16 pel, clamped to the window as the motion
-     * compensation does) */
-    const int c0x = dir == 3 ? b0x : dir == 2 ? mv1x : mvx, c0y = dir == 3 ? b0y : dir == 2 ? mv1y : mvy;
-    const int c1x = b1x, c1y = b1y;
-
-    /* ---- luma MC: Xin266LumaInterPred (uni) or the bi branch of Xin266LumaMotionComp */
-    if (BI && dir == 3) {
-        const int o0x = cx * 16 + min(max(c0x * 4, mnx * 16), mxx * 16), o0y = cy * 16 + min(max(c0y * 4, mny * 16), mxy * 16);
-        const int o1x = cx * 16 + min(max(c1x * 4, mnx * 16), mxx * 16), o1y = cy * 16 + min(max(c1y * 4, mny * 16), mxy * 16);
-        for (int i = tid; i < S * S; i += NT) {
-            const int x = i % S, y = i / S;
-            pred[i] = xg_bi_avg(xg_luma_s16(p.ref[0], o0x, o0y, x, y), xg_luma_s16(p.ref1[0], o1x, o1y, x, y));
-        }
-    } else {
-        xg_luma_uni<S, NT>(BI && dir == 2 ? p.qpel1 : p.qpel, cx, cy, c0x, c0y, mnx, mny, mxx, mxy, pred, tid);
-    }
-    xg_gsync<NT, CPB>(g);
-
-    /* ---- luma TQ + reconstruction (or the residual, for the preset-4 TU stage); a
-     * 128 x 128 CU TU by TU (64 x 64, in raster order: the non-zero maps of the
-     * record are the union of its TUs', the SSDs their sum) */
-    const int lgS = TL == 8 ? 3 : TL == 16 ? 4 : TL == 32 ? 5 : 6;
-    const bool resid_only = p.resid[0] != nullptr;       /* uniform over the launch */
-    if (resid_only) {
-        for (int i = tid; i < S * S; i += NT) {
-            int y = i / S, x = i % S;
-            p.resid[0][(intptr_t)(cy + y) * p.W + cx + x] = (int16_t)((int)org[(intptr_t)y * opitch + x] - (int)pred[i]);
-        }
-        xg_gsync<NT, CPB>(g);
-    } else {
-        for (int tu = 0; tu < (S / TL) * (S / TL); tu++) {
-            const int ox = (tu % (S / TL)) * TL, oy = (tu / (S / TL)) * TL;
-            for (int i = tid; i < TL * TL; i += NT) {
-                int y = i / TL, x = i % TL;
-                tl.res[xg_d2<TL>(y, x)] = (int16_t)((int)org[(intptr_t)(oy + y) * opitch + ox + x] -
-                                                    (int)pred[(oy + y) * S + ox + x]);
-            }
-            xg_gsync<NT, CPB>(g);
-            xg_tq<TL, NT, CPB>(tl, pp->quant[p.level][0], lgS + XG_BITDEPTH + 6 - 15, lgS + 6, &m.nz[0],
-                               p.q[0] + (intptr_t)(cy + oy) * p.W + cx + ox, p.W, tid, g);
-            xg_itq<TL, NT, CPB>(tl, pred + oy * S + ox, S, org + (intptr_t)oy * opitch + ox, opitch,
-                                p.rec[0] + (intptr_t)(cy + oy) * p.W + cx + ox, p.W, &m.ssd[0], tid, g);
-        }
-    }
-
-    /* ---- chroma: Xin266ChromaMotionComp (uni branch: 1/32 phase, mask 31; or the bi
-     * branch), TQ, reconstruction */
-    {
-        const int lgC = TC == 4 ? 2 : TC == 8 ? 3 : TC == 16 ? 4 : 5;
-        const int ox = cx * 16 + min(max(c0x * 4, mnx * 16), mxx * 16), oy = cy * 16 + min(max(c0y * 4, mny * 16), mxy * 16);
-        const int o1x = cx * 16 + min(max(c1x * 4, mnx * 16), mxx * 16), o1y = cy * 16 + min(max(c1y * 4, mny * 16), mxy * 16);
-        const int fx = ox & 31, fy = oy & 31;
-        const int8_t *th = c_chroma_taps[fx], *tv = c_chroma_taps[fy];
-        const int W2 = p.W >> 1;
-        for (int pl = 1; pl <= 2; pl++) {
-            if (BI && dir == 3) {
-                for (int i = tid; i < C * C; i += NT) {
-                    const int x = i % C, y = i / C;
-                    pred[i] = xg_bi_avg(xg_chroma_s16(p.ref[pl], ox, oy, x, y), xg_chroma_s16(p.ref1[pl], o1x, o1y, x, y));
-                }
-            } else {
-                const XgPlane &rp = BI && dir == 2 ? p.ref1[pl] : p.ref[pl];
-                const xg_pix *src = rp.data + (intptr_t)(oy >> 5) * rp.pitch + (ox >> 5);
-                for (int i = tid; i < C * C; i += NT) {
-                    int x = i % C, y = i / C;
-                    const xg_pix *sp = src + (intptr_t)y * rp.pitch + x;
-                    int v;
-                    if (!fx && !fy) v = sp[0];
-                    else if (fx && !fy) v = xg_if_pix<4>(sp, 1, th);
-                    else if (!fx && fy) v = xg_if_pix<4>(sp, rp.pitch, tv);
-                    else v = xg_if_hv<4, false>(sp, rp.pitch, th, tv);
-                    pred[i] = (xg_pix)v;
-                }
-            }
-            xg_gsync<NT, CPB>(g);
-            const xg_pix *corg = p.cur[pl].data + (intptr_t)(cy >> 1) * p.cur[pl].pitch + (cx >> 1);
-            if (resid_only) {
-                for (int i = tid; i < C * C; i += NT) {
-                    int y = i / C, x = i % C;
-                    p.resid[pl][(intptr_t)((cy >> 1) + y) * W2 + (cx >> 1) + x] =
-                        (int16_t)((int)corg[(intptr_t)y * p.cur[pl].pitch + x] - (int)pred[i]);
-                }
-                xg_gsync<NT, CPB>(g);
-                continue;
-            }
-            for (int tu = 0; tu < (C / TC) * (C / TC); tu++) {
-                const int ox = (tu % (C / TC)) * TC, oy = (tu / (C / TC)) * TC;
-                for (int i = tid; i < TC * TC; i += NT) {
-                    int y = i / TC, x = i % TC;
-                    tc.res[xg_d2<TC>(y, x)] = (int16_t)((int)corg[(intptr_t)(oy + y) * p.cur[pl].pitch + ox + x] -
-                                                        (int)pred[(oy + y) * C + ox + x]);
-                }
-                xg_gsync<NT, CPB>(g);
-                xg_tq<TC, NT, CPB>(tc, pp->quant[p.level][pl], lgC + XG_BITDEPTH + 6 - 15, lgC + 6, &m.nz[pl],
-                                   p.q[pl] + (intptr_t)((cy >> 1) + oy) * W2 + (cx >> 1) + ox, W2, tid, g);
-                xg_itq<TC, NT, CPB>(tc, pred + oy * C + ox, C, corg + (intptr_t)oy * p.cur[pl].pitch + ox, p.cur[pl].pitch,
-                                    p.rec[pl] + (intptr_t)((cy >> 1) + oy) * W2 + (cx >> 1) + ox, W2, &m.ssd[pl], tid, g);
-            }
-        }
-    }
-    if (tid == 0) {
-        xin_gpu_cu_result *o = p.res + p.first_cu + cu;
-        o->mvx = mvx; o->mvy = mvy; o->cost = bc; o->int_cost = (uint32_t)(key >> 32);
-        for (int i = 0; i < 3; i++) { o->nz[i] = m.nz[i]; o->ssd[i] = m.ssd[i]; }
-        if constexpr (BI) {
-            xin_gpu_cu_bi *b = p.bi + p.first_cu + cu;
-            b->mvx1 = mv1x; b->mvy1 = mv1y; b->cost1 = bc1; b->int_cost1 = (uint32_t)(p.keys1[cu] >> 32);
-            b->bmv[0] = b0x; b->bmv[1] = b0y; b->bmv[2] = b1x; b->bmv[3] = b1y;
-            b->bi_cost = bi_cost;
-            b->inter_dir = (uint32_t)dir;
-        }
-    }
+/* cross-stream batch (one list): grid y is the picture, every picture has ncu CUs
+ * at this level.  The body is the single-picture kernel's, included again rather
+ * than shared through a device function, so that the single-picture kernels keep
+ * their register allocation. */
+struct XgTailBatch {
+    XgTailParams p[XG_BATCH_MAX];
+    const XgPicParams *pp[XG_BATCH_MAX];
+};
+/* kernel parameters may take 32,764 bytes */
+static_assert(sizeof(XgTailBatch) + sizeof(int) <= 32764 && sizeof(XgMeBatch) <= 32764 && sizeof(XgQpelBatch) <= 32764 &&
+              sizeof(XgFillBatch) <= 32764, "batch parameters within the kernel parameter limit");
+template <int S, int NT, int CPB>
+__global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, false)) k_cu_tail_batch(const __grid_constant__ XgTailBatch b, int ncu)
+{
+    constexpr bool BI = false;
+    const XgTailParams &p = b.p[blockIdx.y];
+    const XgPicParams *pp = b.pp[blockIdx.y];
+#include "xg_cu_tail_body.inc"
 }

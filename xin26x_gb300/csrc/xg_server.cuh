@@ -9,12 +9,16 @@
  * per-stream ordering (a picture uses the previous picture of its stream as the
  * reference, so one stream runs one picture at a time), and continuous batching
  * across streams: one scheduler thread keeps up to max_inflight pictures of
- * different streams running at once, each on its stream's own CUDA stream and
- * CUDA graph, and starts the oldest waiting picture as soon as a slot frees.
+ * different streams running at once and starts the oldest waiting picture as
+ * soon as a slot frees.  A picture runs on its stream's own CUDA streams and
+ * graph, or -- streams of the plain form and one shape, several pictures
+ * waiting -- in a cross-stream batch (xg_batch.cuh) with the other waiting
+ * pictures of that shape, one launch per stage for all of them.
  *
  * Each stream's device state is private to it, so a stream's results do not
  * depend on which other streams share the GPU.
  */
+#include <algorithm>
 #include <condition_variable>
 #include <deque>
 #include <map>
@@ -113,6 +117,7 @@ struct XgSrvStream {
     bool leaving, failed;
     uint32_t next_index;
     uint32_t max_queue;
+    int lane;                     /* batch lane of the running picture, or -1 (its own streams) */
     std::vector<XgSrvPic *> spare;
 };
 
@@ -129,7 +134,9 @@ struct xin_gpu_server {
     double mpix_used;
     int32_t next_id;
     int running;
-    uint64_t completed, launched;
+    uint64_t completed, launched, batches, batched_pictures;
+    int sms;                          /* SMs of the device (batch sizes) */
+    std::vector<XgBatchLane> lanes;   /* cross-stream batches in flight: one lane each */
 };
 
 static void xg_srv_release(XgSrvStream *t, XgSrvPic *p)
@@ -144,10 +151,27 @@ static void xg_srv_finish(xin_gpu_server *v, XgSrvStream *t, xin_gpu_server_done
     XgSrvPic *p = t->running;
     t->running = nullptr;
     v->running--;
+    if (t->lane >= 0) {
+        v->lanes[t->lane].busy--;
+        t->lane = -1;
+    }
     v->completed++;
     xg_srv_release(t, p);
     v->done.push_back(d);
     v->cv_done.notify_all();
+}
+
+/* the library picture of a queued server picture (its packed planes) */
+static void xg_srv_picture(const XgSrvStream *t, const XgSrvPic *p, xin_gpu_picture *pic)
+{
+    memset(pic, 0, sizeof *pic);
+    const int w = t->cfg.width, h = t->cfg.height;
+    const size_t es = xg_in_es(t->cfg);
+    pic->plane[0] = (const XG_PIXEL *)p->pix.data();
+    pic->plane[1] = (const XG_PIXEL *)(p->pix.data() + (size_t)w * h * es);
+    pic->plane[2] = (const XG_PIXEL *)(p->pix.data() + ((size_t)w * h + (size_t)(w / 2) * (h / 2)) * es);
+    pic->stride[0] = w; pic->stride[1] = pic->stride[2] = w / 2;
+    pic->qp = p->qp; pic->uv_qp = p->uv_qp; pic->sad_lambda = p->lambda;
 }
 
 /* scheduler thread: collect finished pictures, close drained streams, start
@@ -227,7 +251,9 @@ static void xg_srv_loop(xin_gpu_server *v)
             v->cv_left.notify_all();
             progress = true;
         }
-        /* launches, oldest submission first */
+        /* launches, oldest submission first; the oldest picture of a plain stream
+         * takes the oldest waiting pictures of compatible streams into its batch */
+        bool held = false;
         while (v->running < (int)v->cfg.max_inflight) {
             XgSrvStream *best = nullptr;
             for (auto &kv : v->streams) {
@@ -236,6 +262,76 @@ static void xg_srv_loop(xin_gpu_server *v)
                 if (!best || t->queue.front()->t_submit < best->queue.front()->t_submit) best = t;
             }
             if (!best) break;
+            XgSrvStream *mem[XG_BATCH_MAX];
+            int nb = 1, lane = -1;
+            mem[0] = best;
+            if (v->cfg.batch_max > 1 && !best->failed && xg_batchable(best->s)) {
+                for (size_t i = 0; i < v->lanes.size() && lane < 0; i++)
+                    if (!v->lanes[i].busy) lane = (int)i;
+                const int cap = std::min(std::min((int)v->cfg.batch_max, (int)v->cfg.max_inflight - v->running),
+                                         xg_batch_fill_limit(best->s, v->sms));
+                while (lane >= 0 && nb < cap) {
+                    XgSrvStream *nx = nullptr;
+                    for (auto &kv : v->streams) {
+                        XgSrvStream *t = kv.second;
+                        if (t->running || t->queue.empty() || t->failed) continue;
+                        bool in = false;
+                        for (int j = 0; j < nb; j++) in |= mem[j] == t;
+                        if (in || !xg_batchable(t->s) || !xg_batch_compatible(best->s, t->s)) continue;
+                        if (!nx || t->queue.front()->t_submit < nx->queue.front()->t_submit) nx = t;
+                    }
+                    if (!nx) break;
+                    mem[nb++] = nx;
+                }
+                /* hold an incomplete batch open while its oldest picture is younger
+                 * than the window */
+                if (lane >= 0 && nb < cap && v->cfg.batch_window_us > 0 &&
+                    xg_now_ms() - best->queue.front()->t_submit < v->cfg.batch_window_us * 1e-3) {
+                    held = true;
+                    break;
+                }
+            }
+            if (nb > 1) {
+                XgSrvPic *ps[XG_BATCH_MAX];
+                xin_gpu_picture pics[XG_BATCH_MAX];
+                const xin_gpu_picture *pp[XG_BATCH_MAX];
+                xg_coef *const *qd[XG_BATCH_MAX];
+                xin_gpu_stream *ss[XG_BATCH_MAX];
+                const double now = xg_now_ms();
+                for (int j = 0; j < nb; j++) {
+                    XgSrvStream *t = mem[j];
+                    XgSrvPic *q = t->queue.front();
+                    t->queue.pop_front();
+                    t->running = q;
+                    t->lane = lane;
+                    v->running++;
+                    q->t_launch = now;
+                    xg_srv_picture(t, q, &pics[j]);
+                    ps[j] = q;
+                    pp[j] = &pics[j];
+                    qd[j] = q->q_out[0] ? q->q_out : nullptr;
+                    ss[j] = t->s;
+                }
+                v->lanes[lane].busy = nb;
+                progress = true;
+                lk.unlock();
+                int st = xg_batch_submit(ss, pp, qd, nb, v->lanes[lane]);
+                lk.lock();
+                v->launched += nb;
+                if (st) {
+                    for (int j = 0; j < nb; j++) {
+                        xin_gpu_server_done d;
+                        memset(&d, 0, sizeof d);
+                        d.stream_id = mem[j]->id; d.frame_index = ps[j]->index; d.user_tag = ps[j]->tag; d.status = st;
+                        mem[j]->failed = true;
+                        xg_srv_finish(v, mem[j], d);
+                    }
+                } else {
+                    v->batches++;
+                    v->batched_pictures += nb;
+                }
+                continue;
+            }
             XgSrvPic *p = best->queue.front();
             best->queue.pop_front();
             progress = true;
@@ -252,14 +348,7 @@ static void xg_srv_loop(xin_gpu_server *v)
             v->running++;
             p->t_launch = xg_now_ms();
             xin_gpu_picture pic;
-            memset(&pic, 0, sizeof pic);
-            const int w = best->cfg.width, h = best->cfg.height;
-            const size_t es = xg_in_es(best->cfg);
-            pic.plane[0] = (const XG_PIXEL *)p->pix.data();
-            pic.plane[1] = (const XG_PIXEL *)(p->pix.data() + (size_t)w * h * es);
-            pic.plane[2] = (const XG_PIXEL *)(p->pix.data() + ((size_t)w * h + (size_t)(w / 2) * (h / 2)) * es);
-            pic.stride[0] = w; pic.stride[1] = pic.stride[2] = w / 2;
-            pic.qp = p->qp; pic.uv_qp = p->uv_qp; pic.sad_lambda = p->lambda;
+            xg_srv_picture(best, p, &pic);
             lk.unlock();
             int st = xg_frame_submit(best->s, &pic, -1, -1, p->q_out[0] ? p->q_out : nullptr);
             lk.lock();
@@ -278,7 +367,7 @@ static void xg_srv_loop(xin_gpu_server *v)
             if (!queued && v->streams.empty()) break;
         }
         if (!progress) {
-            if (v->running) {
+            if (v->running || held) {
                 /* pictures on the GPU: poll their events at a short interval */
                 lk.unlock();
                 std::this_thread::sleep_for(std::chrono::microseconds(20));
@@ -303,7 +392,20 @@ extern "C" int xin_gpu_server_open(const xin_gpu_server_cfg *cfg, xin_gpu_server
     if (!v->cfg.max_inflight) v->cfg.max_inflight = 8;
     if (!v->cfg.max_streams) v->cfg.max_streams = 256;
     if (!v->cfg.max_queue) v->cfg.max_queue = 4;
+    if (!v->cfg.batch_max || v->cfg.batch_max > XG_BATCH_MAX) v->cfg.batch_max = XG_BATCH_MAX;
     cudaGetDevice(&v->device);
+    v->sms = 0;
+    cudaDeviceGetAttribute(&v->sms, cudaDevAttrMultiProcessorCount, v->device);
+    if (v->cfg.batch_max > 1) {
+        /* a batch carries two pictures or more: at most max_inflight / 2 run at once */
+        v->lanes.resize(v->cfg.max_inflight / 2 > 0 ? v->cfg.max_inflight / 2 : 1);
+        for (size_t i = 0; i < v->lanes.size(); i++)
+            if (int e = xg_lane_open(v->lanes[i])) {
+                for (size_t j = 0; j < i; j++) xg_lane_close(v->lanes[j]);
+                delete v;
+                return e;
+            }
+    }
     v->hbm_budget = v->cfg.hbm_budget;
     if (!v->hbm_budget) {
         size_t fr = 0, tot = 0;
@@ -363,6 +465,7 @@ extern "C" int xin_gpu_server_join(xin_gpu_server *v, const xin_gpu_stream_cfg *
     t->leaving = t->failed = false;
     t->next_index = 0;
     t->max_queue = v->cfg.max_queue;
+    t->lane = -1;
     v->streams[t->id] = t;
     *stream_id = t->id;
     return XIN_GPU_OK;
@@ -504,6 +607,8 @@ extern "C" int xin_gpu_server_get_stats(xin_gpu_server *v, xin_gpu_server_stats 
     s->mpix_used = v->mpix_used;
     s->launched = v->launched;
     s->completed = v->completed;
+    s->batches = v->batches;
+    s->batched_pictures = v->batched_pictures;
     s->queued = 0;
     for (auto &kv : v->streams) s->queued += (int32_t)kv.second->queue.size();
     return XIN_GPU_OK;
@@ -526,6 +631,7 @@ extern "C" int xin_gpu_server_close(xin_gpu_server *v)
         for (XgSrvPic *p : t->spare) delete p;
         delete t;
     }
+    for (XgBatchLane &ln : v->lanes) xg_lane_close(ln);
     delete v;
     return XIN_GPU_OK;
 }

@@ -11,6 +11,7 @@
 #include "xg_percall.cuh"
 #include "xg_me_percall.cuh"
 #include "xg_frame.cuh"
+#include "xg_batch.cuh"
 #include "xg_dmvr.cuh"
 #include "xg_fsme.cuh"
 #include "xg_server.cuh"

@@ -34,7 +34,7 @@ LAMBDA = {27: 45, 32: 64, 37: 91}
 
 
 def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=64, frames_per_class=6, arrivals="poisson",
-        planes=False):
+        planes=False, batch_max=0):
     from xin26x_gb300 import synth
     from xin26x_gb300.server import Admission, Server
 
@@ -46,7 +46,7 @@ def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=6
     join_t = np.sort(rng.uniform(0, 0.5, size=len(streams)))
     offered = sum(w * h * FPS for (w, h), _ in streams) / 1e6
 
-    srv = Server(mpix_budget=mpix_budget, max_inflight=max_inflight, max_queue=2)
+    srv = Server(mpix_budget=mpix_budget, max_inflight=max_inflight, max_queue=2, batch_max=batch_max)
     admitted, refused = [], []
     lat, qms, gpu, done_px = [], [], [], 0
     dropped = 0
@@ -135,6 +135,7 @@ def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=6
     stop.set()
     th.join()
     wall = time.perf_counter() - t0
+    sst = srv.stats()
     srv.close()
     lat_a = np.array(lat) if lat else np.zeros(1)
     by_class = {f"{w}x{h}": sum(1 for si in admitted if streams[si][0] == (w, h)) for (w, h) in CLASSES}
@@ -152,6 +153,9 @@ def run(seconds=4.0, mpix_budget=1650.0, max_inflight=6, seed=48, search_range=6
                            "max": float(lat_a.max())},
             "queue_ms_p99": float(np.percentile(qms, 99)) if qms else None,
             "gpu_ms_mean": float(np.mean(gpu)) if gpu else None,
+            "cross_stream_batches": {"batch_max": batch_max or 8, "batches": int(sst["batches"]),
+                                     "pictures_in_batches": int(sst["batched_pictures"]),
+                                     "share_of_pictures": sst["batched_pictures"] / max(1, sst["launched"])},
             "wall_s": wall}
 
 
@@ -163,8 +167,10 @@ def main():
     ap.add_argument("--seed", type=int, default=48)
     ap.add_argument("--arrivals", choices=("poisson", "periodic"), default="poisson")
     ap.add_argument("--planes", action="store_true", help="every picture's coefficient planes returned too")
+    ap.add_argument("--batch-max", type=int, default=0, help="pictures a cross-stream batch may carry (1 = none)")
     a = ap.parse_args()
-    print(json.dumps(run(a.seconds, a.mpix_budget, a.max_inflight, a.seed, arrivals=a.arrivals, planes=a.planes)), flush=True)
+    print(json.dumps(run(a.seconds, a.mpix_budget, a.max_inflight, a.seed, arrivals=a.arrivals, planes=a.planes,
+                         batch_max=a.batch_max)), flush=True)
 
 
 if __name__ == "__main__":

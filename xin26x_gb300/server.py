@@ -27,12 +27,17 @@ class Admission(RuntimeError):
 
 class Server:
     def __init__(self, hbm_budget: int = 0, mpix_budget: float = 0.0, max_inflight: int = 8, max_streams: int = 256,
-                 max_queue: int = 4, bitdepth: int = 8, device: int = 0):
+                 max_queue: int = 4, bitdepth: int = 8, device: int = 0, batch_max: int = 0, batch_window_us: int = 0):
+        """batch_max: pictures of different plain streams of one shape a launch
+        may carry (0 = the library's default, 1 = no cross-stream batches);
+        batch_window_us: how long the oldest waiting picture may be held for
+        others to join its batch."""
         self.lib = _lib.load(bitdepth)
         self.pix = np.uint8 if bitdepth == 8 else np.uint16
         if self.lib.xin_gpu_init(device) != 0:
             raise RuntimeError("xin_gpu_init: " + self.lib.xin_gpu_last_error().decode())
-        cfg = _lib.xin_gpu_server_cfg(hbm_budget, mpix_budget, max_inflight, max_streams, max_queue, 0)
+        cfg = _lib.xin_gpu_server_cfg(hbm_budget, mpix_budget, max_inflight, max_streams, max_queue, batch_max,
+                                      batch_window_us, 0)
         h = C.c_void_p()
         if self.lib.xin_gpu_server_open(C.byref(cfg), C.byref(h)) != 0:
             raise RuntimeError("xin_gpu_server_open: " + self.lib.xin_gpu_last_error().decode())
