@@ -428,17 +428,19 @@ def kernel_batch_bench(torch, flush, steps, warmup, nblocks=65536, seed=65536):
     assert g.xin_gpu_init(torch.cuda.current_device()) == 0
     blocks, resid = synth.tq_blocks(nblocks, seed, bitdepth=10, kernel_bench_mix=True)
     d_res = torch.from_numpy(resid).cuda()
-    q, r, ro = torch.empty_like(d_res), torch.empty_like(d_res), torch.empty_like(d_res)
-    nz = torch.empty(nblocks, dtype=torch.int64, device="cuda")
     stream = torch.cuda.current_stream()
     out = {"workload": f"{nblocks} blocks, 10-bit, sides 4..64, 11-bit Laplacian residuals (scale 12), DCT2 70 % / "
                        "DST7-DCT8 pairs 30 % on sides <= 32, QP U[22,42]; forward transform + quant + dequant + "
                        "inverse transform per block",
            "coefficients": int(resid.size), "l2": "flushed between runs"}
     algo = resid.size * 4 * 4 + nblocks * (8 + 12 + 4)      # resid in, q/r/resid_out out, nz, job + list entry
-    for name, tile in (("tensor_cores", -2), ("autotuned", -1), ("fixed", 0)):
+
+    def time_plan(blocks, resid, d_res, tile):
+        """mean CUDA-event ms of one plan run (L2 flushed before each) and the plan's tiles"""
+        q, r, ro = torch.empty_like(d_res), torch.empty_like(d_res), torch.empty_like(d_res)
+        nz = torch.empty(len(blocks), dtype=torch.int64, device="cuda")
         plan = C.c_void_p()
-        assert g.xin_gpu_tq_plan_create(blocks.ctypes.data, nblocks, resid.size, tile, C.byref(plan)) == 0, \
+        assert g.xin_gpu_tq_plan_create(blocks.ctypes.data, len(blocks), resid.size, tile, C.byref(plan)) == 0, \
             g.xin_gpu_last_error()
         run = lambda: g.xin_gpu_tq_plan_run(plan, d_res.data_ptr(), q.data_ptr(), r.data_ptr(), ro.data_ptr(),
                                             nz.data_ptr(), stream.cuda_stream)
@@ -457,9 +459,28 @@ def kernel_batch_bench(torch, flush, steps, warmup, nblocks=65536, seed=65536):
         tiles = (C.c_int32 * 49)()
         g.xin_gpu_tq_plan_tiles(plan, tiles)
         g.xin_gpu_tq_plan_destroy(plan)
-        ms = float(np.mean(times))
+        return float(np.mean(times)), tiles
+
+    for name, tile in (("tensor_cores", -2), ("autotuned", -1), ("fixed", 0)):
+        ms, tiles = time_plan(blocks, resid, d_res, tile)
         out[name] = {"ms": ms, "Mblocks_per_s": nblocks / ms / 1e3, "Gcoeff_per_s": resid.size / ms / 1e6,
                      "tiles": {f"{1 << (c // 7)}x{1 << (c % 7)}": int(tiles[c]) for c in range(49) if tiles[c]}}
+    # the largest transforms alone (the frame form's 32 x 32 and 64 x 64 TUs): DCT2
+    # blocks of one side, 4.2 M coefficients each, on either engine
+    rng = np.random.default_rng(seed + 1)
+    large = {}
+    for lg, nb in ((5, 4096), (6, 1024)):
+        bl = np.zeros(nb, synth.TQ_BLOCK_DTYPE)
+        bl["offset"] = np.arange(nb, dtype=np.int64) << (2 * lg)
+        bl["log2w"], bl["log2h"], bl["qp"] = lg, lg, rng.integers(22, 43, size=nb)
+        rs = np.clip(np.rint(rng.laplace(0, 12, size=nb << (2 * lg))), -1023, 1023).astype(np.int32)
+        d_rs = torch.from_numpy(rs).cuda()
+        t_ms, _ = time_plan(bl, rs, d_rs, -2)
+        c_ms, _ = time_plan(bl, rs, d_rs, -1)
+        large[f"{1 << lg}x{1 << lg}"] = {"blocks": nb, "tensor_cores_ms": t_ms, "cuda_cores_autotuned_ms": c_ms,
+                                         "tensor_speedup": c_ms / t_ms}
+        del d_rs
+    out["dct2_one_side"] = large
     peaks = _measured_peaks()
     hbm = peaks.get("hbm_gbs") if peaks else None
     achieved = algo / (out["tensor_cores"]["ms"] * 1e-3) / 1e9
