@@ -183,3 +183,35 @@ def test_dep_quant_boundary_matches_reference(tenbit):
     mine = {k: int(v) for k, v in re.findall(r"DQC_(\w+) = (\d+)", txt)}
     for m in _MINE:
         assert mine[m] == ref[m], m
+
+
+# the library's own public structs: the ctypes and numpy mirrors the Python side
+# passes across the C ABI have the header's layout (sizes and member offsets)
+_MIRRORS = ["xin_gpu_stream_cfg", "xin_gpu_picture", "xin_gpu_cu_result", "xin_gpu_results", "xin_gpu_tq_block",
+            "xin_gpu_dq_block", "xin_gpu_server_cfg", "xin_gpu_server_done", "xin_gpu_server_stats"]
+
+
+@pytest.mark.parametrize("bd", (8, 10))
+def test_public_struct_mirrors_match_the_header(bd):
+    import numpy as np
+    from xin26x_gb300 import frame
+    checks = []                                  # (C struct, {member: offset}, size)
+    for name in _MIRRORS:
+        cls = getattr(_lib, name)
+        checks.append((name, {f: getattr(cls, f).offset for f, *_ in cls._fields_ if not f.startswith("reserved")},
+                       C.sizeof(cls)))
+    for name, dt in (("xin_gpu_cu_result", frame.CU_DTYPE), ("xin_gpu_cu_mts", frame.MTS_DTYPE),
+                     ("xin_gpu_cu_bi", frame.BI_DTYPE)):
+        checks.append((name, {f: dt.fields[f][1] for f in dt.names if not f.startswith("reserved")}, dt.itemsize))
+    inc = '#define ENABLE_10BIT_ENCODER\n' if bd == 10 else ''
+    body = ""
+    for i, (name, offs, _) in enumerate(checks):
+        body += "".join(f'printf("{i}.{f} %zu\\n", offsetof({name}, {f}));\n' for f in offs)
+        body += f'printf("{i}.sizeof %zu\\n", sizeof({name}));\n'
+    src = (f"#include <stdio.h>\n#include <stddef.h>\n#include <stdint.h>\n{inc}#include \"xingpu.h\"\n"
+           f"int main(void){{\n{body}return 0;}}\n")
+    got = _offsets_c(src, [os.path.join(ROOT, "include")])
+    for i, (name, offs, size) in enumerate(checks):
+        assert got[f"{i}.sizeof"] == size, (name, got[f"{i}.sizeof"], size)
+        for f, o in offs.items():
+            assert got[f"{i}.{f}"] == o, (name, f, got[f"{i}.{f}"], o)
