@@ -887,12 +887,30 @@ __device__ void xg_bi_square(const xg_pix *t, const XgPlane &rp, int cx, int cy,
         /* the nine candidates of the row: columns ccx - 4 .. ccx + 4 (within the
          * reference's padding also where they leave the window) */
         const xg_pix *row = rp.data + (intptr_t)(cy + my) * rp.pitch + cx + ccx - 4;
-        for (int i = tid; i < S * S; i += NT) {
-            const int x = i % S, y = i / S;
-            const unsigned o = t[y * S + x];
-            const xg_pix *r = row + (intptr_t)y * rp.pitch + x;
+        if constexpr (S >= 32) {
+            /* a thread takes runs of eight target samples: sixteen reference samples,
+             * loaded once, give all nine candidates' differences */
+            for (int c = tid; c < S * S / 8; c += NT) {
+                const int y = c / (S / 8), x0 = (c % (S / 8)) * 8;
+                const xg_pix *r = row + (intptr_t)y * rp.pitch + x0;
+                unsigned rv[16], tv[8];
 #pragma unroll
-            for (int k = 0; k < 9; k++) acc[k] = __usad(o, (unsigned)r[k], acc[k]);
+                for (int j = 0; j < 16; j++) rv[j] = r[j];
+#pragma unroll
+                for (int j = 0; j < 8; j++) tv[j] = t[y * S + x0 + j];
+#pragma unroll
+                for (int k = 0; k < 9; k++)
+#pragma unroll
+                    for (int j = 0; j < 8; j++) acc[k] = __usad(tv[j], rv[j + k], acc[k]);
+            }
+        } else {
+            for (int i = tid; i < S * S; i += NT) {
+                const int x = i % S, y = i / S;
+                const unsigned o = t[y * S + x];
+                const xg_pix *r = row + (intptr_t)y * rp.pitch + x;
+#pragma unroll
+                for (int k = 0; k < 9; k++) acc[k] = __usad(o, (unsigned)r[k], acc[k]);
+            }
         }
 #pragma unroll
         for (int k = 0; k < 9; k++) acc[k] = __reduce_add_sync(0xffffffffu, acc[k]);
