@@ -677,6 +677,7 @@ template <int S>
 struct XgTailBiSmem {
     alignas(16) xg_pix bp[2][S * S];
     alignas(16) xg_pix tgt[S * S];
+    alignas(16) int16_t hv[2][(S + 7) * S];    /* the coded bi prediction: each list's horizontal-pass rows */
 };
 
 /* CPB CUs of size S (luma S x S, chroma S/2 x S/2) per CTA, NT threads per CU
