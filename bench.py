@@ -273,6 +273,15 @@ def run_gpu(args):
                      "search_ms_chosen": tune_ms[1], "candidates": "default band count and x1/2, x2, x3, x4, x6 of it",
                      "note": "xin_gpu_stream_tune_search: CUDA-event time of the search of the last warm-up picture "
                              "per geometry (one warm-up, three timed launches each); results do not depend on it"}
+    # the CUs per CTA of the 16 x 16 and 8 x 8 tails, also autotuned on the last picture
+    tcpb, tms = (C.c_int32 * 2)(), (C.c_float * 6)()
+    assert lib.xin_gpu_stream_tune_tails(h, tcpb, tms) == 0, lib.xin_gpu_last_error()
+    search_tuning["tails_cus_per_cta"] = {"16x16": tcpb[0], "8x8": tcpb[1],
+                                          "timed_ms": {f"{s}x{s}": {str(c): round(float(tms[3 * j + o]), 4)
+                                                                    for o, c in enumerate((2, 4, 8))}
+                                                       for j, s in enumerate((16, 8))},
+                                          "note": "xin_gpu_stream_tune_tails: CUDA-event time of the last warm-up "
+                                                  "picture's tails per choice; results do not depend on it"}
     for k in range(args.warmup + 1, args.warmup + 3):
         submit_dev(k)
         lib.xin_gpu_frame_wait(h, C.byref(res), -1)
@@ -331,6 +340,7 @@ def run_gpu(args):
     e2e_fs.wait(copy=False)
     pending.pop(0)
     assert e2e_fs.lib.xin_gpu_stream_tune_search(e2e_fs.h, None, None) == 0, e2e_fs.lib.xin_gpu_last_error()
+    assert e2e_fs.lib.xin_gpu_stream_tune_tails(e2e_fs.h, None, None) == 0, e2e_fs.lib.xin_gpu_last_error()
     e2e_submit(2)
     for k in range(args.warmup):
         e2e_submit(k + 3)

@@ -589,6 +589,14 @@ int  xin_gpu_stream_num_levels(const xin_gpu_stream *s);
  * least two submitted and none in flight; bands = the chosen count, ms[0] /
  * ms[1] = the default's and the chosen geometry's search time (ms). */
 int  xin_gpu_stream_tune_search(xin_gpu_stream *s, int32_t *bands, float ms[2]);
+/* Autotune the CUs per CTA of the plain tails of the 16 x 16 and 8 x 8 levels (a
+ * warp per CU; 2, 4 or 8 CUs a CTA): times those levels' tails of the last
+ * picture for each, keeps the fastest for later pictures and re-captures the
+ * graphs.  Results do not depend on it.  Streams with one reference; call
+ * between pictures, after at least two submitted and none in flight.  cpb = the
+ * choice for 16 x 16 and 8 x 8; ms[3 level + option] = each option's time (ms,
+ * 0 for a level that is off). */
+int  xin_gpu_stream_tune_tails(xin_gpu_stream *s, int32_t cpb[2], float ms[6]);
 /* the geometries the last tune_search timed (n <= 6): band counts and search times (ms) */
 int  xin_gpu_stream_tune_table(const xin_gpu_stream *s, int32_t *n, int32_t bands[6], float ms[6]);
 /* Upload a picture and queue its hot path (asynchronous).  The first picture of

@@ -487,6 +487,45 @@ def test_frame_search_tuning_keeps_results(bd, inb, R):
             assert np.array_equal(a["q"][p], b["q"][p]) and np.array_equal(a["rec"][p], b["rec"][p]), (k, p)
 
 
+def test_frame_tail_tuning_keeps_results():
+    """xin_gpu_stream_tune_tails: the CUs per CTA it picks for the 16 x 16 and
+    8 x 8 tails (timed on the last picture) change no result -- pictures after
+    the tuning equal those of an untuned stream, every record and plane; a
+    stream with two references is refused."""
+    import ctypes as C
+    w, h = 416, 240
+    seq = synth.sequence(w, h, 5, seed=77, bitdepth=8, objects=2)
+    outs, picked = [], None
+    for tune in (False, True):
+        fs = FrameStream(w, h, search_range=16, out_q=True, out_rec=True)
+        try:
+            got = []
+            for k in range(5):
+                fs.submit(*seq[k], qp=32, uv_qp=32, sad_lambda=64)
+                got.append(fs.wait())
+                if tune and k == 1:
+                    cpb, ms = (C.c_int32 * 2)(), (C.c_float * 6)()
+                    assert fs.lib.xin_gpu_stream_tune_tails(fs.h, cpb, ms) == 0, fs.lib.xin_gpu_last_error()
+                    picked = list(cpb)
+                    assert all(c in (2, 4, 8) for c in picked) and all(ms[i] > 0 for i in range(6))
+            outs.append(got)
+        finally:
+            fs.close()
+    for k in range(2, 5):
+        a, b = outs[0][k], outs[1][k]
+        assert np.array_equal(a["cu"], b["cu"]), (k, picked)
+        for p in range(3):
+            assert np.array_equal(a["q"][p], b["q"][p]) and np.array_equal(a["rec"][p], b["rec"][p]), (k, p, picked)
+    fs = FrameStream(w, h, search_range=16, out_q=False, out_rec=False, refs=2)
+    try:
+        for k in range(2):
+            fs.submit(*seq[k], qp=32, uv_qp=32, sad_lambda=64)
+            fs.wait()
+        assert fs.lib.xin_gpu_stream_tune_tails(fs.h, None, None) == -6
+    finally:
+        fs.close()
+
+
 def test_frame_bi_needs_levels_up_to_64():
     """refs 2 is refused with the 128 x 128 level, and more than two references."""
     for kw in ({"ctu": 128, "search_mode": 1, "levels": (128, 64), "refs": 2}, {"refs": 3}):

@@ -136,6 +136,7 @@ SIGNATURES = {
     "xin_gpu_frame_submit_refs": ([vp, C.POINTER(xin_gpu_picture), i32, i32], C.c_int),
     "xin_gpu_stream_tune_search": ([vp, vp, vp], C.c_int),
     "xin_gpu_stream_tune_table": ([vp, vp, vp, vp], C.c_int),
+    "xin_gpu_stream_tune_tails": ([vp, vp, vp], C.c_int),
     "xin_gpu_frame_wait": ([vp, C.POINTER(xin_gpu_results), i32], C.c_int),
     "xin_gpu_stream_stage_ms": ([vp, C.POINTER(C.c_float)], C.c_int),
     "xin_gpu_stream_set_wait_tries": ([vp, C.c_int64], C.c_int),

@@ -92,6 +92,7 @@ struct xin_gpu_stream {
     int nsub;              /* pictures submitted */
     int ndone;             /* pictures collected by frame_wait (the oldest first) */
     XgTuState *tu[2];      /* tu_mode 1: per picture set */
+    int tail_cpb[2];       /* CUs per CTA of the plain 16 x 16 and 8 x 8 tails (2, 4 or 8; warp per CU) */
     int tune_n;            /* the last xin_gpu_stream_tune_search: geometries timed */
     int32_t tune_bands[6];
     float tune_ms[6];
@@ -415,6 +416,7 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         });
         if (xg_cuda_check(bi_err, "bi tail smem attribute")) { xg_stream_free(s); return XIN_GPU_ERR_CUDA; }
     }
+    s->tail_cpb[0] = s->tail_cpb[1] = 4;
     s->wait_tries = XG_TMA_WAIT_TRIES;
     /* TMA maps of the padded luma slots for the quarter-pel tiles: the box of
      * tile (bx, by) starts at padded column XG_QP_TW bx (16-byte aligned) */
@@ -506,6 +508,18 @@ static void xg_enqueue_me_tiles(xin_gpu_stream *s, int cur, int ref, unsigned lo
     else
 #endif
         k_me_tiles<8><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, dpp);
+}
+
+/* the plain tails of a 16 x 16 or 8 x 8 level: a warp per CU, cpb CUs per CTA */
+template <int S>
+static void xg_launch_small_tail(int cpb, const XgTailParams &tp, const XgPicParams *dpp, int n, cudaStream_t ls)
+{
+    static_assert(xg_tail_smem<S, 32, 8>() <= 48 * 1024, "eight CUs a CTA within the default shared memory");
+    switch (cpb) {
+    case 2: k_cu_tail<S, 32, 2, false><<<(n + 1) / 2, 64, xg_tail_smem<S, 32, 2>(), ls>>>(tp, dpp, n); break;
+    case 8: k_cu_tail<S, 32, 8, false><<<(n + 7) / 8, 256, xg_tail_smem<S, 32, 8>(), ls>>>(tp, dpp, n); break;
+    default: k_cu_tail<S, 32, 4, false><<<(n + 3) / 4, 128, xg_tail_smem<S, 32, 4>(), ls>>>(tp, dpp, n); break;
+    }
 }
 
 /* the tails' parameters of level L (the li-th level on) of a picture of set
@@ -667,8 +681,8 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l
                 case 128: k_cu_tail<128, 128, 1, false><<<n, 128, xg_tail_smem<128, 128, 1>(), ls>>>(tp, t.dpp, n); break;
                 case 64: k_cu_tail<64, 128, 1, false><<<n, 128, xg_tail_smem<64, 128, 1>(), ls>>>(tp, t.dpp, n); break;
                 case 32: k_cu_tail<32, 128, 1, false><<<n, 128, xg_tail_smem<32, 128, 1>(), ls>>>(tp, t.dpp, n); break;
-                case 16: k_cu_tail<16, 32, 4, false><<<(n + 3) / 4, 128, xg_tail_smem<16, 32, 4>(), ls>>>(tp, t.dpp, n); break;
-                default: k_cu_tail<8, 32, 4, false><<<(n + 3) / 4, 128, xg_tail_smem<8, 32, 4>(), ls>>>(tp, t.dpp, n); break;
+                case 16: xg_launch_small_tail<16>(s->tail_cpb[0], tp, t.dpp, n, ls); break;
+                default: xg_launch_small_tail<8>(s->tail_cpb[1], tp, t.dpp, n, ls); break;
                 }
                 nl++;
             }
@@ -973,6 +987,57 @@ extern "C" int xin_gpu_stream_tune_search(xin_gpu_stream *s, int32_t *bands, flo
     if (bands) *bands = s->me_bands;
     if (ms) { ms[0] = first_ms; ms[1] = best_ms; }
     return xg_cuda_check(cudaGetLastError(), "tune search");
+}
+
+extern "C" int xin_gpu_stream_tune_tails(xin_gpu_stream *s, int32_t cpb[2], float ms[6])
+{
+    xin_gpu_clear_error();
+    if (!s) { xg_set_error(XIN_GPU_ERR_ARG, "stream_tune_tails: null stream"); return XIN_GPU_ERR_ARG; }
+    const xin_gpu_stream_cfg &c = s->cfg;
+    if (c.refs == 2 || s->nsub < 2 || s->nsub != s->ndone) {
+        xg_set_error(XIN_GPU_ERR_STATE, "stream_tune_tails: needs one reference, two pictures submitted and none in flight");
+        return XIN_GPU_ERR_STATE;
+    }
+    /* the last picture's tails again (against its list-0 reference, the previous
+     * picture): they rewrite that picture's device results with the same values */
+    const int ns = s->nslots, k = s->nsub - 1, set = k & 1, cur = k % ns, ref = (k + ns - 1) % ns;
+    const XgPicParams *dpp = s->set[set].dpp;
+    cudaStream_t st = s->st;
+    const int opt[3] = { 2, 4, 8 };
+    cudaEvent_t e0, e1;
+    if (xg_cuda_check(cudaEventCreate(&e0), "tune event") || xg_cuda_check(cudaEventCreate(&e1), "tune event")) return XIN_GPU_ERR_CUDA;
+    for (int j = 0; j < 2; j++) {                     /* the 16 x 16 and the 8 x 8 level */
+        const int L = j ? 3 : 2;
+        for (int o = 0; o < 3; o++)
+            if (ms) ms[3 * j + o] = 0;
+        if (!s->lev_on[L]) continue;
+        int li = 0;
+        for (int l = 0; l < L; l++) li += s->lev_on[l] ? 1 : 0;
+        const XgTailParams tp = xg_tail_params(s, set, cur, ref, ref, L, li);
+        const int n = s->lev_cx[L] * s->lev_cy[L];
+        float best = 0;
+        for (int o = 0; o < 3; o++) {
+            for (int rep = 0; rep < 4; rep++) {          /* one warm-up, three timed */
+                if (rep == 1) cudaEventRecord(e0, st);
+                if (j) xg_launch_small_tail<8>(opt[o], tp, dpp, n, st);
+                else xg_launch_small_tail<16>(opt[o], tp, dpp, n, st);
+            }
+            cudaEventRecord(e1, st);
+            if (xg_cuda_check(cudaEventSynchronize(e1), "tune tails")) { cudaEventDestroy(e0); cudaEventDestroy(e1); return XIN_GPU_ERR_CUDA; }
+            float t = 0;
+            cudaEventElapsedTime(&t, e0, e1);
+            t /= 3;
+            if (ms) ms[3 * j + o] = t;
+            if (o == 0 || t < best) { best = t; s->tail_cpb[j] = opt[o]; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    /* the launch shapes are baked into the captured graphs: capture them again */
+    for (auto &g : s->graphs) cudaGraphExecDestroy(g.second.first);
+    s->graphs.clear();
+    if (cpb) { cpb[0] = s->tail_cpb[0]; cpb[1] = s->tail_cpb[1]; }
+    return xg_cuda_check(cudaGetLastError(), "tune tails");
 }
 
 extern "C" int xin_gpu_stream_tune_table(const xin_gpu_stream *s, int32_t *n, int32_t bands[6], float ms[6])

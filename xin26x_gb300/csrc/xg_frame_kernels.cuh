@@ -687,9 +687,10 @@ struct XgTailBiSmem {
  * The bi search's kernels: 64 x 64 two, 32 x 32 four, and the warp-per-CU sizes
  * eight (64 registers with a few spilled: 3.42-3.46 ms against 3.51-3.54 ms per
  * 1080p preset-4 picture at four, 3.46-3.50 at six) */
-__host__ __device__ constexpr int xg_tail_min_ctas(int s, bool bi = false)
+__host__ __device__ constexpr int xg_tail_min_ctas(int s, bool bi = false, int threads = 128)
 {
-    return bi ? (s == 64 ? 2 : s == 32 ? 4 : 8) : s == 128 ? 2 : s == 64 ? 5 : 8;
+    /* plain tails up to 32: 1024 threads an SM, so 64 registers a thread at any CTA size */
+    return bi ? (s == 64 ? 2 : s == 32 ? 4 : 8) : s == 128 ? 2 : s == 64 ? 5 : 1024 / threads;
 }
 /* shared memory (dynamic) of a launch */
 template <int S, int NT, int CPB, bool BI = false>
@@ -991,7 +992,7 @@ __device__ uint32_t xg_satd_blocks(const xg_pix *org, intptr_t op, const xg_pix 
 }
 
 template <int S, int NT, int CPB, bool BI>
-__global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, BI)) k_cu_tail(XgTailParams p, const XgPicParams *pp, int ncu)
+__global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, BI, NT * CPB)) k_cu_tail(XgTailParams p, const XgPicParams *pp, int ncu)
 {
 #include "xg_cu_tail_body.inc"
 }
@@ -1008,7 +1009,7 @@ struct XgTailBatch {
 static_assert(sizeof(XgTailBatch) + sizeof(int) <= 32764 && sizeof(XgMeBatch) <= 32764 && sizeof(XgQpelBatch) <= 32764 &&
               sizeof(XgFillBatch) <= 32764, "batch parameters within the kernel parameter limit");
 template <int S, int NT, int CPB>
-__global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, false)) k_cu_tail_batch(const __grid_constant__ XgTailBatch b, int ncu)
+__global__ void __launch_bounds__(NT * CPB, xg_tail_min_ctas(S, false, NT * CPB)) k_cu_tail_batch(const __grid_constant__ XgTailBatch b, int ncu)
 {
     constexpr bool BI = false;
     const XgTailParams &p = b.p[blockIdx.y];
