@@ -147,6 +147,7 @@ def test_server_argument_and_queue_errors():
         sid = srv.join(1920, 1080, search_range=64)
         assert srv.submit(sid + 100, *fr[0]) == -2                 # no such stream
         assert srv.submit(sid, *fr[0], qp=64) == -2                # QP out of range
+        assert srv.submit(sid, *fr[0], sad_lambda=(1 << 20) + 1) == -2   # lambda the search cannot pack
         assert srv.submit(sid, *fr[0]) == 0
         pic = _lib.xin_gpu_picture()
         planes = [np.ascontiguousarray(p) for p in fr[1]]

@@ -498,6 +498,9 @@ static int xg_server_submit(xin_gpu_server *v, int32_t stream_id, const xin_gpu_
         xg_set_error(XIN_GPU_ERR_ARG, "server_submit: QP out of range");
         return XIN_GPU_ERR_ARG;
     }
+    /* refused here rather than at launch, where the picture may share a batch with
+     * other streams' pictures */
+    if (pic->sad_lambda > (1u << 20)) { xg_set_error(XIN_GPU_ERR_ARG, "server_submit: sad_lambda above 2^20"); return XIN_GPU_ERR_ARG; }
     XgSrvPic *p = nullptr;
     int w, h;
     size_t es;
