@@ -321,8 +321,9 @@ def run_gpu(args):
     lib.xin_gpu_stream_close(h)
 
     # e2e through the public API with host buffers
+    # three picture slots: picture k + 1 (its own slot) starts beside picture k's tails
     e2e_fs = FrameStream(W, H, search_range=SEARCH, levels=LEVELS, out_q=True, out_rec=False, use_graph=True,
-                         bitdepth=BD, input_bitdepth=IN_BD)
+                         bitdepth=BD, input_bitdepth=IN_BD, dpb=3)
     cu_bytes = e2e_fs.ncus * 64
     q_bytes = sum((W * H if p == 0 else W * H // 4) * len(LEVELS) * 4 for p in range(3))
     e2e_fs.submit(*frames[0], qp=32, uv_qp=32, sad_lambda=LAMBDA_BD[32])
@@ -800,7 +801,7 @@ def preset4_bench(torch, flush, frames, steps, warmup, cpu_seconds=8.0):
     # about 0.5 GB) is above L2.
     from xin26x_gb300.frame import FrameStream
     fs = FrameStream(W, H, search_range=SEARCH, levels=LEVELS, out_q=True, out_rec=False, use_graph=True, bitdepth=BD,
-                     input_bitdepth=IN_BD, search_mode=1, tu_mode=1, contexts=ctx)
+                     input_bitdepth=IN_BD, search_mode=1, tu_mode=1, contexts=ctx, dpb=3)
     n_e2e = max(steps, 10)
     h2d = W * H * 3 // 2
     d2h = fs.ncus * (64 + 64) + sum((W * H if p == 0 else W * H // 4) * len(LEVELS) * 4 for p in range(3))

@@ -120,20 +120,24 @@ def test_frame_wide_search_sampled(bd, R):
         assert np.array_equal(out["cu"]["nz"][i], recs["nz"][i]) and np.array_equal(out["cu"]["ssd"][i], recs["ssd"][i])
 
 
-def test_frame_two_in_flight_equals_one_at_a_time():
+@pytest.mark.parametrize("dpb,refs,tu_mode", [(0, 1, 0), (3, 1, 0), (3, 1, 1), (4, 2, 0)])
+def test_frame_two_in_flight_equals_one_at_a_time(dpb, refs, tu_mode):
     """Two pictures in flight (submit k + 1 before collecting k) give the same results
-    as submit / wait one picture at a time; a third submit and an empty wait are refused."""
+    as submit / wait one picture at a time; a third submit and an empty wait are refused.
+    With a slot more than the references need (dpb 3 for one reference, 4 for two),
+    picture k + 1 starts once picture k's planes are written, beside k's tails."""
     w, h = 256, 192
     seq = synth.sequence(w, h, 6, seed=5, objects=2)
+    kw = {"dpb": dpb, "refs": refs, "tu_mode": tu_mode}
     ref = []
-    fs = FrameStream(w, h, search_range=24, out_q=True, out_rec=True)
+    fs = FrameStream(w, h, search_range=24, out_q=True, out_rec=True, **kw)
     for k in range(6):
         fs.submit(*seq[k], qp=27 + k, uv_qp=28 + k, sad_lambda=50 + k)
         r = fs.wait()
         if k:
             ref.append(r)
     fs.close()
-    fs = FrameStream(w, h, search_range=24, out_q=True, out_rec=True)
+    fs = FrameStream(w, h, search_range=24, out_q=True, out_rec=True, **kw)
     got = []
     fs.submit(*seq[0], qp=27, uv_qp=28, sad_lambda=50)
     fs.submit(*seq[1], qp=28, uv_qp=29, sad_lambda=51)

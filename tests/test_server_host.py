@@ -25,9 +25,9 @@ def test_footprint_arithmetic(bd):
     ysz, csz = 2304 * 1400 * es, 1152 * 700 * es
     ncus = 30 * 16 + 60 * 33 + 120 * 67 + 240 * 135
     lq = 1920 * 1080
-    # two slots + quarter-pel planes + keys, and two picture sets (CU records, coefficient
-    # and reconstruction planes of four levels, a parameter block each)
-    want = 2 * (ysz + 2 * csz) + 32 * ysz + 8 * ncus + 2 * (64 * ncus + lq * 3 // 2 * 4 * (cs + es))
+    # two slots + quarter-pel planes, and two picture sets (search keys, CU records,
+    # coefficient and reconstruction planes of four levels, a parameter block each)
+    want = 2 * (ysz + 2 * csz) + 32 * ysz + 2 * (8 * ncus + 64 * ncus + lq * 3 // 2 * 4 * (cs + es))
     assert want < d < want + 8192
     assert h >= 2 * (64 * ncus + lq * 3 // 2 * es)
     # a wider search needs a wider margin; dropping levels drops their outputs
@@ -80,7 +80,7 @@ def test_footprint_two_references(bd):
     assert st1 == 0 and st2 == 0 and fp(0)[1:] == (d1, h1)
     ysz, csz = 2304 * 1400 * es, 1152 * 700 * es
     ncus = 30 * 16 + 60 * 33 + 120 * 67 + 240 * 135
-    assert d2 - d1 == (ysz + 2 * csz) + 16 * ysz + 8 * ncus + 2 * 40 * ncus    # xin_gpu_cu_bi: 40 bytes
+    assert d2 - d1 == (ysz + 2 * csz) + 16 * ysz + 2 * 8 * ncus + 2 * 40 * ncus    # keys per set; xin_gpu_cu_bi: 40 bytes
     assert h2 - h1 == 2 * 40 * ncus
     assert fp(3)[0] == -2 and fp(-1)[0] == -2 and fp(2, tu=1)[0] == 0
     assert fp(2, mask=248, ctu=128, sm=1)[0] == -2 and fp(1, mask=248, ctu=128, sm=1)[0] == 0

@@ -115,6 +115,10 @@ static int xg_batch_submit(xin_gpu_stream *const *ss, const xin_gpu_picture *con
     XgSubmitPlan plan[XG_BATCH_MAX];
     for (int i = 0; i < n; i++)
         if (int e = xg_frame_prepare(ss[i], pics[i], -1, -1, plan[i])) return e;
+    for (int i = 0; i < n; i++) {
+        int *rd = ss[i]->set[plan[i].set].rd;
+        rd[0] = plan[i].cur; rd[1] = plan[i].l0; rd[2] = plan[i].l1;
+    }
     xin_gpu_stream *s0 = ss[0];
     const xin_gpu_stream_cfg &c = s0->cfg;
     cudaStream_t st = ln.st;
@@ -169,6 +173,7 @@ static int xg_batch_submit(xin_gpu_stream *const *ss, const xin_gpu_picture *con
         dim3 grd((c.width + 2 * s0->pad - 8 + XG_QP_TW - 1) / XG_QP_TW, (c.height + 2 * s0->pad - 8 + XG_QP_TH - 1) / XG_QP_TH, n);
         k_qpel_planes_batch<<<grd, 256, 0, ln.auxq>>>(qb);
     }
+    for (int i = 0; i < n; i++) cudaEventRecord(ss[i]->set[plan[i].set].ev_ref, ln.auxq);
     cudaEventRecord(ln.ev_qjoin, ln.auxq);
     /* the integer search against each stream's previous picture */
     {
@@ -177,6 +182,7 @@ static int xg_batch_submit(xin_gpu_stream *const *ss, const xin_gpu_picture *con
         mb.bands = s0->me_bands;
         for (int i = 0; i < n; i++) {
             xin_gpu_stream *s = ss[i];
+            xg_use_set_keys(s, plan[i].set);
             cudaMemsetAsync(s->keys, 0xff, sizeof(unsigned long long) * s->ncus, st);
             mb.p[i] = xg_me_params(s, plan[i].cur, plan[i].l0, s->keys);
             mb.pp[i] = s->set[plan[i].set].dpp;
@@ -203,6 +209,7 @@ static int xg_batch_submit(xin_gpu_stream *const *ss, const xin_gpu_picture *con
         XgTailBatch tb;
         memset(&tb, 0, sizeof tb);
         for (int i = 0; i < n; i++) {
+            xg_use_set_keys(ss[i], plan[i].set);
             tb.p[i] = xg_tail_params(ss[i], plan[i].set, plan[i].cur, plan[i].l0, plan[i].l1, L, li);
             tb.pp[i] = ss[i]->set[plan[i].set].dpp;
         }

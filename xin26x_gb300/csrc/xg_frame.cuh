@@ -46,6 +46,10 @@ struct xin_gpu_stream {
     int lo_pitch[2], lo_rows[2];
     CUtensorMap tm_qp[XG_MAX_DPB];     /* TMA map of each slot's padded luma plane: quarter-pel tiles */
     long long wait_tries;  /* bound of the kernels' waits (polls) */
+    /* the integer search's results, one buffer per picture set (so that a picture's
+     * search may run beside the previous picture's tails); keys / keys1 point at
+     * the buffers of the set being enqueued */
+    unsigned long long *keys_base, *keys1_base;
     unsigned long long *keys;
     unsigned long long *keys1;         /* refs 2: list 1's integer search */
     /* what a picture in flight owns; picture k uses set k & 1 (its slot), so two
@@ -73,6 +77,9 @@ struct xin_gpu_stream {
         cudaStream_t pst;      /* the picture's launches (a stream per set, so that the TU stage of
                                   one picture runs beside the next picture's search and tails) */
         cudaEvent_t ev_main;   /* the picture's reference planes, search and tails are done */
+        cudaEvent_t ev_ref;    /* its slot, downscaled and quarter-pel planes are done (what the next
+                                  picture reads of it) */
+        int rd[3];             /* the slots the picture reads: its own, list 0's and list 1's */
     } set[2];
     cudaStream_t st;
     cudaStream_t cst;      /* result copies (device to host) */
@@ -92,6 +99,7 @@ struct xin_gpu_stream {
     int nsub;              /* pictures submitted */
     int ndone;             /* pictures collected by frame_wait (the oldest first) */
     XgTuState *tu[2];      /* tu_mode 1: per picture set */
+    int prio_hi;           /* the most urgent stream priority (the tails' launches) */
     int tail_cpb[2];       /* CUs per CTA of the plain 16 x 16 and 8 x 8 tails (2, 4 or 8; warp per CU) */
     int tune_n;            /* the last xin_gpu_stream_tune_search: geometries timed */
     int32_t tune_bands[6];
@@ -134,8 +142,8 @@ static int xg_stream_free(xin_gpu_stream *s)
         cudaFree(s->qpel_base[i]);
         for (int l = 0; l < 2; l++) cudaFree(s->lo_base[i][l]);
     }
-    cudaFree(s->keys);
-    cudaFree(s->keys1);
+    cudaFree(s->keys_base);
+    cudaFree(s->keys1_base);
     xg_tu_free(s->tu[0]);
     xg_tu_free(s->tu[1]);
     for (auto &t : s->set) {
@@ -148,6 +156,7 @@ static int xg_stream_free(xin_gpu_stream *s)
         if (t.ev_kern) cudaEventDestroy(t.ev_kern);
         if (t.ev_up) cudaEventDestroy(t.ev_up);
         if (t.ev_main) cudaEventDestroy(t.ev_main);
+        if (t.ev_ref) cudaEventDestroy(t.ev_ref);
         if (t.pst) cudaStreamDestroy(t.pst);
     }
     if (s->cst) cudaStreamDestroy(s->cst);
@@ -276,6 +285,7 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
         for (int i = 0; i < 5 && e == cudaSuccess; i++) e = cudaEventCreate(&t.evs[i]);
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&t.pst, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.ev_main, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.ev_ref, cudaEventDisableTiming);
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_qfork, cudaEventDisableTiming);
@@ -283,6 +293,7 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
     if (e == cudaSuccess) {
         int lo = 0, hi = 0;
         cudaDeviceGetStreamPriorityRange(&lo, &hi);    /* lo: the least urgent */
+        s->prio_hi = hi;
         e = cudaStreamCreateWithPriority(&s->auxq, cudaStreamNonBlocking, lo);
     }
     for (int i = 0; i < XG_NLEV - 1 && e == cudaSuccess; i++) {
@@ -300,8 +311,10 @@ extern "C" int xin_gpu_stream_open(const xin_gpu_stream_cfg *cfg, xin_gpu_stream
             e = cudaMalloc(&s->lo_base[i][l], (size_t)s->lo_pitch[l] * s->lo_rows[l] * sizeof(xg_pix));
         }
     }
-    if (e == cudaSuccess) e = cudaMalloc(&s->keys, sizeof(unsigned long long) * (s->ncus > 0 ? s->ncus : 1));
-    if (e == cudaSuccess && c.refs == 2) e = cudaMalloc(&s->keys1, sizeof(unsigned long long) * (s->ncus > 0 ? s->ncus : 1));
+    if (e == cudaSuccess) e = cudaMalloc(&s->keys_base, 2 * sizeof(unsigned long long) * (s->ncus > 0 ? s->ncus : 1));
+    if (e == cudaSuccess && c.refs == 2) e = cudaMalloc(&s->keys1_base, 2 * sizeof(unsigned long long) * (s->ncus > 0 ? s->ncus : 1));
+    s->keys = s->keys_base;
+    s->keys1 = s->keys1_base;
     for (auto &t : s->set) {
         if (e == cudaSuccess) e = cudaMalloc(&t.dres, sizeof(xin_gpu_cu_result) * s->ncus);
         if (e == cudaSuccess && c.refs == 2) e = cudaMalloc(&t.dbi, sizeof(xin_gpu_cu_bi) * s->ncus);
@@ -467,13 +480,18 @@ static void xg_stage_event(cudaEvent_t e, cudaStream_t st, bool capturing)
 /* completion event of the last submitted picture */
 static cudaEvent_t xg_stream_last_event(const xin_gpu_stream *s) { return s->set[(s->nsub - 1) & 1].ev1; }
 
-/* quarter-pel planes of slot cur on the low-priority stream, after ev_qfork */
-static int xg_enqueue_qpel(xin_gpu_stream *s, int cur, int *status)
+
+
+/* quarter-pel planes of slot cur on the low-priority stream, after ev_qfork; then
+ * `ready` (the picture's planes are all written, ev_ref) */
+static void xg_stage_event(cudaEvent_t e, cudaStream_t st, bool capturing);
+static int xg_enqueue_qpel(xin_gpu_stream *s, int cur, int *status, cudaEvent_t ready, bool capturing)
 {
     const xin_gpu_stream_cfg &c = s->cfg;
     cudaStreamWaitEvent(s->auxq, s->ev_qfork, 0);
     dim3 grd((c.width + 2 * s->pad - 8 + XG_QP_TW - 1) / XG_QP_TW, (c.height + 2 * s->pad - 8 + XG_QP_TH - 1) / XG_QP_TH);
     k_qpel_planes<<<grd, 256, 0, s->auxq>>>(s->tm_qp[cur], s->slot[cur][0], s->qpel[cur], status, s->wait_tries);
+    xg_stage_event(ready, s->auxq, capturing);
     cudaEventRecord(s->ev_qjoin, s->auxq);
     return 1;
 }
@@ -510,15 +528,31 @@ static void xg_enqueue_me_tiles(xin_gpu_stream *s, int cur, int ref, unsigned lo
         k_me_tiles<8><<<grd, XG_ME_THREADS, s->me_smem, st>>>(mp, dpp);
 }
 
+/* a kernel launch at the given stream priority (a node priority inside captured
+ * graphs, which are instantiated with node priorities): the tails run at the
+ * highest, so that the next picture's search, started beside them, does not
+ * hold them back */
+template <typename... KArgs, typename... Args>
+static void xg_launch_prio(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, int prio, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid; cfg.blockDim = block; cfg.dynamicSmemBytes = smem; cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributePriority;
+    at[0].val.priority = prio;
+    cfg.attrs = at; cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 /* the plain tails of a 16 x 16 or 8 x 8 level: a warp per CU, cpb CUs per CTA */
 template <int S>
-static void xg_launch_small_tail(int cpb, const XgTailParams &tp, const XgPicParams *dpp, int n, cudaStream_t ls)
+static void xg_launch_small_tail(int cpb, const XgTailParams &tp, const XgPicParams *dpp, int n, cudaStream_t ls, int prio)
 {
     static_assert(xg_tail_smem<S, 32, 8>() <= 48 * 1024, "eight CUs a CTA within the default shared memory");
     switch (cpb) {
-    case 2: k_cu_tail<S, 32, 2, false><<<(n + 1) / 2, 64, xg_tail_smem<S, 32, 2>(), ls>>>(tp, dpp, n); break;
-    case 8: k_cu_tail<S, 32, 8, false><<<(n + 7) / 8, 256, xg_tail_smem<S, 32, 8>(), ls>>>(tp, dpp, n); break;
-    default: k_cu_tail<S, 32, 4, false><<<(n + 3) / 4, 128, xg_tail_smem<S, 32, 4>(), ls>>>(tp, dpp, n); break;
+    case 2: xg_launch_prio(k_cu_tail<S, 32, 2, false>, dim3((n + 1) / 2), dim3(64), xg_tail_smem<S, 32, 2>(), ls, prio, tp, dpp, n); break;
+    case 8: xg_launch_prio(k_cu_tail<S, 32, 8, false>, dim3((n + 7) / 8), dim3(256), xg_tail_smem<S, 32, 8>(), ls, prio, tp, dpp, n); break;
+    default: xg_launch_prio(k_cu_tail<S, 32, 4, false>, dim3((n + 3) / 4), dim3(128), xg_tail_smem<S, 32, 4>(), ls, prio, tp, dpp, n); break;
     }
 }
 
@@ -549,19 +583,32 @@ static XgTailParams xg_tail_params(xin_gpu_stream *s, int set, int cur, int l0, 
     return tp;
 }
 
+/* point keys / keys1 at picture set `set`'s search buffers */
+static void xg_use_set_keys(xin_gpu_stream *s, int set)
+{
+    const size_t n = s->ncus > 0 ? s->ncus : 1;
+    s->keys = s->keys_base + set * n;
+    if (s->keys1_base) s->keys1 = s->keys1_base + set * n;
+}
+
 /* the launches of one picture of picture set `set` into slot `cur`, against the
  * references in slots l0 (list 0) and l1 (list 1, refs 2) */
-static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l1, bool with_me, bool capturing)
+static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l1, bool with_me, bool capturing,
+                              bool early = false)
 {
     const xin_gpu_stream_cfg &c = s->cfg;
     xin_gpu_stream::Set &t = s->set[set];
     cudaStream_t st = t.pst;
     int nl = 0;
-    /* the previous picture (the other set, on its own stream) must have finished
-     * with the planes this picture overwrites: its reference slot, quarter-pel and
-     * downscaled planes, the search keys; its TU stage may still run */
-    if (capturing) cudaStreamWaitEvent(st, s->set[1 - set].ev_main, cudaEventWaitExternal);
-    else cudaStreamWaitEvent(st, s->set[1 - set].ev_main, 0);
+    xg_use_set_keys(s, set);
+    /* the previous picture (the other set, on its own stream) must have written
+     * the planes this picture reads of it (its slot, downscaled and quarter-pel
+     * planes: ev_ref) and, unless this picture's slot is none of those it reads
+     * (`early`), finished its search and tails (ev_main); its TU stage may still
+     * run.  The search keys are per set. */
+    const cudaEvent_t prev = early ? s->set[1 - set].ev_ref : s->set[1 - set].ev_main;
+    if (capturing) cudaStreamWaitEvent(st, prev, cudaEventWaitExternal);
+    else cudaStreamWaitEvent(st, prev, 0);
     /* upload and pad the current picture; it becomes the next picture's reference */
     xg_stage_event(t.evs[0], st, capturing);
     /* the parameters and (8-bit input) the staged samples were uploaded on the
@@ -641,7 +688,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l
         }
         nl++;
         }
-        nl += xg_enqueue_qpel(s, cur, &t.dpp->status);
+        nl += xg_enqueue_qpel(s, cur, &t.dpp->status, t.ev_ref, capturing);
         /* the search's end is recorded on a side branch joined at the picture's
          * end: a timing node between the search and the tails' fork held the tails
          * back by about 0.03 ms */
@@ -664,13 +711,13 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l
             int n = s->lev_cx[L] * s->lev_cy[L];
             if (n > 0 && c.refs == 2) {
                 switch (XG_LEVEL_SIZE[L]) {
-                case 64: k_cu_tail<64, 128, 1, true><<<n, 128, xg_tail_smem<64, 128, 1, true>(), ls>>>(tp, t.dpp, n); break;
-                case 32: k_cu_tail<32, 128, 1, true><<<n, 128, xg_tail_smem<32, 128, 1, true>(), ls>>>(tp, t.dpp, n); break;
+                case 64: xg_launch_prio(k_cu_tail<64, 128, 1, true>, dim3(n), dim3(128), xg_tail_smem<64, 128, 1, true>(), ls, s->prio_hi, tp, (const XgPicParams *)t.dpp, n); break;
+                case 32: xg_launch_prio(k_cu_tail<32, 128, 1, true>, dim3(n), dim3(128), xg_tail_smem<32, 128, 1, true>(), ls, s->prio_hi, tp, (const XgPicParams *)t.dpp, n); break;
                 case 16:
-                    k_cu_tail<16, 32, 4, true><<<(n + 3) / 4, 128, xg_tail_smem<16, 32, 4, true>(), ls>>>(tp, t.dpp, n);
+                    xg_launch_prio(k_cu_tail<16, 32, 4, true>, dim3((n + 3) / 4), dim3(128), xg_tail_smem<16, 32, 4, true>(), ls, s->prio_hi, tp, (const XgPicParams *)t.dpp, n);
                     break;
                 default:
-                    k_cu_tail<8, 32, 4, true><<<(n + 3) / 4, 128, xg_tail_smem<8, 32, 4, true>(), ls>>>(tp, t.dpp, n);
+                    xg_launch_prio(k_cu_tail<8, 32, 4, true>, dim3((n + 3) / 4), dim3(128), xg_tail_smem<8, 32, 4, true>(), ls, s->prio_hi, tp, (const XgPicParams *)t.dpp, n);
                     break;
                 }
                 nl++;
@@ -678,11 +725,11 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l
                 /* 64 and 32: a 128-thread CTA per CU; 16 and 8: a warp per CU, four CUs per
                  * CTA (the fastest of the shapes measured on GB300 at 1080p) */
                 switch (XG_LEVEL_SIZE[L]) {
-                case 128: k_cu_tail<128, 128, 1, false><<<n, 128, xg_tail_smem<128, 128, 1>(), ls>>>(tp, t.dpp, n); break;
-                case 64: k_cu_tail<64, 128, 1, false><<<n, 128, xg_tail_smem<64, 128, 1>(), ls>>>(tp, t.dpp, n); break;
-                case 32: k_cu_tail<32, 128, 1, false><<<n, 128, xg_tail_smem<32, 128, 1>(), ls>>>(tp, t.dpp, n); break;
-                case 16: xg_launch_small_tail<16>(s->tail_cpb[0], tp, t.dpp, n, ls); break;
-                default: xg_launch_small_tail<8>(s->tail_cpb[1], tp, t.dpp, n, ls); break;
+                case 128: xg_launch_prio(k_cu_tail<128, 128, 1, false>, dim3(n), dim3(128), xg_tail_smem<128, 128, 1>(), ls, s->prio_hi, tp, (const XgPicParams *)t.dpp, n); break;
+                case 64: xg_launch_prio(k_cu_tail<64, 128, 1, false>, dim3(n), dim3(128), xg_tail_smem<64, 128, 1>(), ls, s->prio_hi, tp, (const XgPicParams *)t.dpp, n); break;
+                case 32: xg_launch_prio(k_cu_tail<32, 128, 1, false>, dim3(n), dim3(128), xg_tail_smem<32, 128, 1>(), ls, s->prio_hi, tp, (const XgPicParams *)t.dpp, n); break;
+                case 16: xg_launch_small_tail<16>(s->tail_cpb[0], tp, t.dpp, n, ls, s->prio_hi); break;
+                default: xg_launch_small_tail<8>(s->tail_cpb[1], tp, t.dpp, n, ls, s->prio_hi); break;
                 }
                 nl++;
             }
@@ -698,7 +745,7 @@ static int xg_enqueue_picture(xin_gpu_stream *s, int set, int cur, int l0, int l
         if (s->tu[set]) nl += xg_tu_enqueue(s, set, cur, t, st);
         xg_stage_event(t.evs[3], st, capturing);
     } else {
-        nl += xg_enqueue_qpel(s, cur, &t.dpp->status);
+        nl += xg_enqueue_qpel(s, cur, &t.dpp->status, t.ev_ref, capturing);
         cudaStreamWaitEvent(st, s->ev_qjoin, 0);
         xg_stage_event(t.ev_main, st, capturing);
         xg_stage_event(t.evs[2], st, capturing);
@@ -838,14 +885,19 @@ static int xg_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_
     cudaStreamWaitEvent(t.pst, t.ev_up, 0);
     /* a graph per (set, slot, list-0 slot, list-1 slot): the launches bake in the
      * slots' planes */
-    const uint32_t gkey = ((uint32_t)set << 15) | ((uint32_t)cur << 10) | ((uint32_t)l0 << 5) | (uint32_t)l1;
+    /* the previous picture's tails may still run while this one starts when this
+     * picture's slot is none of the slots it reads */
+    const xin_gpu_stream::Set &pv = s->set[1 - set];
+    const bool early = s->nsub >= 1 && s->nslots >= 3 && cur != pv.rd[0] && cur != pv.rd[1] && cur != pv.rd[2];
+    t.rd[0] = cur; t.rd[1] = l0; t.rd[2] = l1;
+    const uint32_t gkey = ((uint32_t)early << 20) | ((uint32_t)set << 15) | ((uint32_t)cur << 10) | ((uint32_t)l0 << 5) | (uint32_t)l1;
     auto git = s->graphs.find(gkey);
     if (with_me && c.use_graph && (git != s->graphs.end() || (int)s->graphs.size() < XG_MAX_GRAPHS)) {
         if (git == s->graphs.end()) {
             cudaGraph_t g;
             cudaGraphExec_t gx = nullptr;
             if (xg_cuda_check(cudaStreamBeginCapture(t.pst, cudaStreamCaptureModeThreadLocal), "begin capture")) return XIN_GPU_ERR_CUDA;
-            const int n = xg_enqueue_picture(s, set, cur, l0, l1, true, true);
+            const int n = xg_enqueue_picture(s, set, cur, l0, l1, true, true, early);
             if (xg_cuda_check(cudaStreamEndCapture(t.pst, &g), "end capture")) return XIN_GPU_ERR_CUDA;
             cudaError_t e = cudaGraphInstantiate(&gx, g, cudaGraphInstantiateFlagUseNodePriority);
             cudaGraphDestroy(g);
@@ -855,7 +907,7 @@ static int xg_frame_submit(xin_gpu_stream *s, const xin_gpu_picture *pic, int32_
         if (xg_cuda_check(cudaGraphLaunch(git->second.first, t.pst), "graph launch")) return XIN_GPU_ERR_CUDA;
         xg_count_launch((uint64_t)git->second.second);
     } else {
-        xg_count_launch((uint64_t)xg_enqueue_picture(s, set, cur, l0, l1, with_me, false));
+        xg_count_launch((uint64_t)xg_enqueue_picture(s, set, cur, l0, l1, with_me, false, early));
     }
     for (int p = 0; p < 3; p++) t.q_dst[p] = q_dst ? q_dst[p] : nullptr;
     xg_enqueue_results(s, t, with_me);
@@ -951,6 +1003,7 @@ extern "C" int xin_gpu_stream_tune_search(xin_gpu_stream *s, int32_t *bands, flo
     const int ns = s->nslots, k = s->nsub - 1, cur = k % ns, ref = (k + ns - 1) % ns;
     const XgPicParams *dpp = s->set[k & 1].dpp;
     cudaStream_t st = s->st;
+    xg_use_set_keys(s, k & 1);
     const int b0 = s->me_bands;
     const int cand[6] = { b0, b0 / 2, 2 * b0, 3 * b0, 4 * b0, 6 * b0 };
     cudaEvent_t e0, e1;
@@ -1003,6 +1056,7 @@ extern "C" int xin_gpu_stream_tune_tails(xin_gpu_stream *s, int32_t cpb[2], floa
     const int ns = s->nslots, k = s->nsub - 1, set = k & 1, cur = k % ns, ref = (k + ns - 1) % ns;
     const XgPicParams *dpp = s->set[set].dpp;
     cudaStream_t st = s->st;
+    xg_use_set_keys(s, set);
     const int opt[3] = { 2, 4, 8 };
     cudaEvent_t e0, e1;
     if (xg_cuda_check(cudaEventCreate(&e0), "tune event") || xg_cuda_check(cudaEventCreate(&e1), "tune event")) return XIN_GPU_ERR_CUDA;
@@ -1019,8 +1073,8 @@ extern "C" int xin_gpu_stream_tune_tails(xin_gpu_stream *s, int32_t cpb[2], floa
         for (int o = 0; o < 3; o++) {
             for (int rep = 0; rep < 4; rep++) {          /* one warm-up, three timed */
                 if (rep == 1) cudaEventRecord(e0, st);
-                if (j) xg_launch_small_tail<8>(opt[o], tp, dpp, n, st);
-                else xg_launch_small_tail<16>(opt[o], tp, dpp, n, st);
+                if (j) xg_launch_small_tail<8>(opt[o], tp, dpp, n, st, s->prio_hi);
+                else xg_launch_small_tail<16>(opt[o], tp, dpp, n, st, s->prio_hi);
             }
             cudaEventRecord(e1, st);
             if (xg_cuda_check(cudaEventSynchronize(e1), "tune tails")) { cudaEventDestroy(e0); cudaEventDestroy(e1); return XIN_GPU_ERR_CUDA; }

@@ -56,9 +56,9 @@ static int xg_stream_bytes(const xin_gpu_stream_cfg *c, uint64_t *dev, uint64_t 
     /* the picture slots (two; three with two references; dpb when set) with their quarter-pel planes,
      * the search keys, and two picture sets (results, parameters, pinned staging) */
     const uint64_t nslots = c->dpb ? c->dpb : (c->refs == 2 ? 3 : 2);
-    uint64_t d = nslots * (ysz + 2 * csz) + nslots * 16 * ysz + 8 * (ncus ? ncus : 1) +
+    uint64_t d = nslots * (ysz + 2 * csz) + nslots * 16 * ysz + 2 * 8 * (ncus ? ncus : 1) +
                  2 * (sizeof(xin_gpu_cu_result) * ncus + sizeof(XgPicParams) + (lq + 2 * lc) * nlev * (sizeof(xg_coef) + sizeof(xg_pix)));
-    if (c->refs == 2) d += 8 * (ncus ? ncus : 1) + 2 * sizeof(xin_gpu_cu_bi) * ncus;   /* list 1's keys, bi records */
+    if (c->refs == 2) d += 2 * 8 * (ncus ? ncus : 1) + 2 * sizeof(xin_gpu_cu_bi) * ncus;   /* list 1's keys, bi records */
     if (widen && !c->device_io) d += 2 * (lq + 2 * lc);     /* 8-bit device staging per set */
     if (c->tu_mode == 1) {                                  /* the preset-4 TU stage */
         d += 2 * xg_tu_bytes(c) + 2 * sizeof(xin_gpu_cu_mts) * ncus;   /* a TU state per picture set */
