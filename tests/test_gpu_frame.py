@@ -120,15 +120,16 @@ def test_frame_wide_search_sampled(bd, R):
         assert np.array_equal(out["cu"]["nz"][i], recs["nz"][i]) and np.array_equal(out["cu"]["ssd"][i], recs["ssd"][i])
 
 
-@pytest.mark.parametrize("dpb,refs,tu_mode", [(0, 1, 0), (3, 1, 0), (3, 1, 1), (4, 2, 0)])
-def test_frame_two_in_flight_equals_one_at_a_time(dpb, refs, tu_mode):
+@pytest.mark.parametrize("dpb,refs,tu_mode,graph", [(0, 1, 0, True), (3, 1, 0, True), (3, 1, 0, False), (3, 1, 1, True),
+                                                    (4, 2, 0, True)])
+def test_frame_two_in_flight_equals_one_at_a_time(dpb, refs, tu_mode, graph):
     """Two pictures in flight (submit k + 1 before collecting k) give the same results
     as submit / wait one picture at a time; a third submit and an empty wait are refused.
     With a slot more than the references need (dpb 3 for one reference, 4 for two),
     picture k + 1 starts once picture k's planes are written, beside k's tails."""
     w, h = 256, 192
     seq = synth.sequence(w, h, 6, seed=5, objects=2)
-    kw = {"dpb": dpb, "refs": refs, "tu_mode": tu_mode}
+    kw = {"dpb": dpb, "refs": refs, "tu_mode": tu_mode, "use_graph": graph}
     ref = []
     fs = FrameStream(w, h, search_range=24, out_q=True, out_rec=True, **kw)
     for k in range(6):
