@@ -658,8 +658,9 @@ def test_frame_preset4_1080p_two_in_flight():
     """The bench's preset-4 workload compared in full: bench.py's 1920x1080 pictures
     (8-bit into the 10-bit library), search by resolution levels, every transform
     candidate through the trellis with the bench's seeded context set, QPs 32 and
-    37.  Pictures 1 and 2 are in flight together (the TU stage of picture 1 runs
-    beside picture 2's search and tails, each on its own picture set): every CU
+    37.  Pictures 1 and 2 are in flight together on a stream of three slots, as in
+    the bench: picture 2 starts once picture 1's planes are written, beside its
+    tails and TU stage, each on its own picture set and search keys.  Every CU
     record, transform-candidate record and plane of both against the oracle on
     all host cores."""
     import bench
@@ -667,7 +668,7 @@ def test_frame_preset4_1080p_two_in_flight():
     frames = bench.make_frames(3)
     ctx = np.ascontiguousarray(S.contexts(np.random.default_rng(4), 1)[0])
     fs = FrameStream(bench.W, bench.H, search_range=bench.SEARCH, levels=bench.LEVELS, out_q=True, out_rec=True,
-                     bitdepth=bench.BD, input_bitdepth=bench.IN_BD, search_mode=1, tu_mode=1, contexts=ctx)
+                     bitdepth=bench.BD, input_bitdepth=bench.IN_BD, search_mode=1, tu_mode=1, contexts=ctx, dpb=3)
     try:
         fs.submit(*frames[0], qp=32, uv_qp=32, sad_lambda=bench.LAMBDA_BD[32])
         fs.wait()
