@@ -378,7 +378,8 @@ def run_gpu(args):
     if rank == 0 and world == 1:
         from xin26x_gb300 import serve_bench
         serving = serve_bench.run(seconds=3.0, mpix_budget=1650.0, max_inflight=6)
-        serving_planes = serve_bench.run(seconds=3.0, mpix_budget=1650.0, max_inflight=8, planes=True)
+        # the plane copies hold a picture's in-flight slot longer: more slots
+        serving_planes = serve_bench.run(seconds=3.0, mpix_budget=1650.0, max_inflight=16, planes=True)
 
     out = None
     if rank == 0:
