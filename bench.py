@@ -376,10 +376,10 @@ def run_gpu(args):
                                                                           BD, IN_BD, search_mode=1)}
     serving = serving_planes = None
     if rank == 0 and world == 1:
-        from xin26x_gb300 import serve_bench
-        serving = serve_bench.run(seconds=3.0, mpix_budget=1650.0, max_inflight=6)
+        # each serving run in a process of its own, as a server would be
+        serving = serve_process(max_inflight=6)
         # the plane copies hold a picture's in-flight slot longer: more slots
-        serving_planes = serve_bench.run(seconds=3.0, mpix_budget=1650.0, max_inflight=16, planes=True)
+        serving_planes = serve_process(max_inflight=16, planes=True)
 
     out = None
     if rank == 0:
@@ -426,6 +426,21 @@ def run_gpu(args):
         dist.barrier()
         dist.destroy_process_group()
     return 0
+
+
+def serve_process(max_inflight, planes=False, seconds=3.0, mpix_budget=1650.0):
+    """serve_bench.py's 48-stream run in a fresh process (its last output line)."""
+    cmd = [sys.executable, "-m", "xin26x_gb300.serve_bench", "--seconds", str(seconds), "--mpix-budget",
+           str(mpix_budget), "--max-inflight", str(max_inflight)] + (["--planes"] if planes else [])
+    clocks = ClockSampler()
+    clocks.start()
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    clk = clocks.stop()
+    if r.returncode != 0:
+        raise RuntimeError(f"serve_bench failed ({r.returncode}): {r.stderr[-2000:]}")
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    out["clocks"] = clk
+    return out
 
 
 def kernel_batch_bench(torch, flush, steps, warmup, nblocks=65536, seed=65536):
