@@ -406,7 +406,7 @@ def run_gpu(args):
                                            "vabsdiff4.add register loops on this GPU, this run",
                             "algorithmic": f"(W/8)(H/8)(2R+1)^2*64 = {algo:.4g} abs differences per launch"},
                "e2e": {"value": e2e_val, "unit": "Mpixel/s", "h2d_bytes_per_step": W * H * 3 // 2,
-                       "d2h_bytes_per_step": cu_bytes + q_bytes, "pictures_in_flight": 2,
+                       "d2h_bytes_per_step": cu_bytes + q_bytes, "pictures_in_flight": 2, "picture_slots": 3,
                        "l2": "not flushed: every picture arrives from pinned host memory inside the timed region",
                        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}},
                "percall": percall,
