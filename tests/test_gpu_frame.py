@@ -253,27 +253,41 @@ def test_device_io_matches_host(bd, inb, w, h):
 
 
 def test_frame_1080p_benchmark_configuration():
-    """The benchmark's own workload compared in full: the first three pictures of
-    bench.py's 1920x1080 stream (8-bit 4:2:0 into the 10-bit library,
-    input_bitdepth 8), +-64 exhaustive search, CU levels 64/32/16/8, QPs 32 and 37
-    with their lambdas.  Every CU record and every coefficient and reconstructed
-    plane of every level against the oracle's 10-bit build on all host cores."""
+    """The benchmark's own workload compared in full, as its end-to-end leg runs it:
+    the first four pictures of bench.py's 1920x1080 stream (8-bit 4:2:0 into the
+    10-bit library, input_bitdepth 8), +-64 exhaustive search, CU levels
+    64/32/16/8, QPs 32, 37 and 27 with their lambdas; three picture slots, both
+    autotuners run after picture 1, pictures 2 and 3 in flight together (picture
+    3 starting beside picture 2's tails).  Every CU record and every coefficient
+    and reconstructed plane of every level against the oracle's 10-bit build on
+    all host cores."""
+    import ctypes as C
     import bench
-    frames = bench.make_frames(3)
+    frames = bench.make_frames(4)
     fs = FrameStream(bench.W, bench.H, search_range=bench.SEARCH, levels=bench.LEVELS, out_q=True, out_rec=True,
-                     bitdepth=bench.BD, input_bitdepth=bench.IN_BD)
+                     bitdepth=bench.BD, input_bitdepth=bench.IN_BD, dpb=3)
+    qps = {1: 32, 2: 37, 3: 27}
+
+    def check(k, out):
+        cur, ref = [tuple(p.astype(np.uint16) << (bench.BD - bench.IN_BD) for p in f) for f in (frames[k], frames[k - 1])]
+        want = oracle_frame.run(cur, ref, fs.levels, search_range=bench.SEARCH, qp=qps[k], uv_qp=qps[k],
+                                sad_lambda=bench.LAMBDA_BD[qps[k]], bitdepth=bench.BD, threads=0)
+        _compare(out, want, fs.levels, ("1080p", k))
+
     try:
         assert sum(cx * cy for (_, _, cx, cy) in fs.levels) == fs.ncus
         fs.submit(*frames[0], qp=32, uv_qp=32, sad_lambda=bench.LAMBDA_BD[32])
         fs.wait()
-        for k, qp in ((1, 32), (2, 37)):
-            fs.submit(*frames[k], qp=qp, uv_qp=qp, sad_lambda=bench.LAMBDA_BD[qp])
-            out = fs.wait()
-            cur, ref = [tuple(p.astype(np.uint16) << (bench.BD - bench.IN_BD) for p in f)
-                        for f in (frames[k], frames[k - 1])]
-            want = oracle_frame.run(cur, ref, fs.levels, search_range=bench.SEARCH, qp=qp, uv_qp=qp,
-                                    sad_lambda=bench.LAMBDA_BD[qp], bitdepth=bench.BD, threads=0)
-            _compare(out, want, fs.levels, ("1080p", k))
+        fs.submit(*frames[1], qp=32, uv_qp=32, sad_lambda=bench.LAMBDA_BD[32])
+        check(1, fs.wait())
+        assert fs.lib.xin_gpu_stream_tune_search(fs.h, None, None) == 0, fs.lib.xin_gpu_last_error()
+        cpb = (C.c_int32 * 2)()
+        assert fs.lib.xin_gpu_stream_tune_tails(fs.h, cpb, None) == 0, fs.lib.xin_gpu_last_error()
+        for k in (2, 3):
+            fs.submit(*frames[k], qp=qps[k], uv_qp=qps[k], sad_lambda=bench.LAMBDA_BD[qps[k]])
+        outs = {k: fs.wait() for k in (2, 3)}
+        for k in (2, 3):
+            check(k, outs[k])
     finally:
         fs.close()
 
